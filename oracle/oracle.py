@@ -1,0 +1,196 @@
+"""ctypes wrapper of the CPU FP64 oracle (oracle/trixi_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY.  The oracle restates Trixi.jl's DGSEM TreeMesh
+Euler path on the CPU; only the test suite, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` may load it, and only as the checker or the
+timed CPU reference -- never as part of the product path.
+
+All arrays use Trixi's column-major layouts, exposed here as C-ordered numpy
+arrays with the axes reversed: ``u[element, (k), j, i, v]``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+
+# enums mirrored from trixi_oracle.cpp
+VI_WEAK, VI_FLUXDIFF, VI_SHOCKCAPTURING_HG = 0, 1, 2
+FLUX_CENTRAL, FLUX_RANOCHA, FLUX_SHIMA_ETAL, FLUX_LAX_FRIEDRICHS, FLUX_LAX_FRIEDRICHS_NAIVE = range(5)
+SRC_NONE, SRC_CONVERGENCE_TEST = 0, 1
+(IC_CONSTANT, IC_CONVERGENCE_TEST, IC_ISENTROPIC_VORTEX, IC_WEAK_BLAST_WAVE,
+ IC_KELVIN_HELMHOLTZ, IC_TAYLOR_GREEN, IC_GAUSSIAN_BLAST) = range(7)
+
+_lib = None
+
+
+def build() -> str:
+    """Compile the oracle with its own recipe (oracle/build.sh)."""
+    subprocess.run(["sh", os.path.join(_HERE, "build.sh")], check=True)
+    return _LIB_PATH
+
+
+def _load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        build()
+    lib = ctypes.CDLL(_LIB_PATH)
+    d, i, i64, vp = ctypes.c_double, ctypes.c_int, ctypes.c_int64, ctypes.c_void_p
+    P = ctypes.POINTER
+    lib.orc_create.restype = vp
+    lib.orc_create.argtypes = [i, i, i, P(d), P(d), d, i, i, i, i, d, d, i, i]
+    lib.orc_destroy.argtypes = [vp]
+    lib.orc_set_threads.argtypes = [i]
+    lib.orc_max_threads.restype = i
+    for name in ("orc_nelements", "orc_ninterfaces", "orc_ndofs"):
+        getattr(lib, name).restype = i64
+        getattr(lib, name).argtypes = [vp]
+    lib.orc_nnodes.restype = i
+    lib.orc_nnodes.argtypes = [vp]
+    lib.orc_get_basis.argtypes = [vp] + [P(d)] * 7
+    lib.orc_get_mesh.argtypes = [vp, P(i64), P(i64), P(d), P(d)]
+    lib.orc_initial_condition.argtypes = [vp, i, P(d), d, P(d)]
+    lib.orc_rhs.argtypes = [vp, P(d), P(d), d]
+    lib.orc_alpha.argtypes = [vp, P(d), P(d)]
+    lib.orc_max_dt.restype = d
+    lib.orc_max_dt.argtypes = [vp, P(d)]
+    lib.orc_rk_stage.argtypes = [vp, P(d), P(d), P(d), i, d, d]
+    lib.orc_solve.restype = i
+    lib.orc_solve.argtypes = [vp, P(d), d, d, d, i64, P(d), P(i64)]
+    lib.orc_error_norms.argtypes = [vp, P(d), d, i, P(d), P(d), P(d)]
+    lib.orc_integrals.argtypes = [vp, P(d), P(d)]
+    _lib = lib
+    return lib
+
+
+def _p(a, ctype=ctypes.c_double):
+    return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+class Oracle:
+    """One semidiscretization of the oracle (mesh + basis + solver options)."""
+
+    def __init__(self, ndims, polydeg, level, xmin, xmax, gamma=1.4,
+                 volume_integral=VI_WEAK, volume_flux=FLUX_CENTRAL,
+                 surface_flux=FLUX_LAX_FRIEDRICHS, fv_flux=None,
+                 alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
+                 source=SRC_NONE):
+        lib = _load()
+        self.lib = lib
+        self.ndims, self.polydeg, self.n = ndims, polydeg, polydeg + 1
+        self.nvar = ndims + 2
+        xmin = np.ascontiguousarray(xmin, dtype=np.float64)
+        xmax = np.ascontiguousarray(xmax, dtype=np.float64)
+        if fv_flux is None:
+            fv_flux = surface_flux
+        h = lib.orc_create(ndims, polydeg, level, _p(xmin), _p(xmax), gamma,
+                           volume_integral, volume_flux, surface_flux, fv_flux,
+                           alpha_max, alpha_min, int(alpha_smooth), source)
+        if not h:
+            raise ValueError("oracle: unsupported configuration")
+        self.h = h
+        self.nelements = lib.orc_nelements(h)
+        self.ninterfaces = lib.orc_ninterfaces(h)
+        self.ndofs = lib.orc_ndofs(h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.orc_destroy(self.h)
+            self.h = None
+
+    @property
+    def shape(self):
+        return (self.nelements,) + (self.n,) * self.ndims + (self.nvar,)
+
+    def basis(self):
+        n = self.n
+        vecs = [np.zeros(n) for _ in range(3)]
+        mats = [np.zeros((n, n)) for _ in range(4)]  # column-major buffers
+        self.lib.orc_get_basis(self.h, *[_p(v) for v in vecs], *[_p(m) for m in mats])
+        names = ["nodes", "weights", "inverse_weights"]
+        out = dict(zip(names, vecs))
+        # buffers were written column-major: reinterpret as (n, n) Fortran arrays
+        for name, m in zip(["derivative_matrix", "derivative_hat", "derivative_split",
+                            "inverse_vandermonde_legendre"], mats):
+            out[name] = m.reshape(-1).reshape((n, n), order="F").copy()
+        return out
+
+    def mesh(self):
+        I, E = self.ninterfaces, self.nelements
+        nb = np.zeros((I, 2), dtype=np.int64)
+        orient = np.zeros(I, dtype=np.int64)
+        invj = np.zeros(E)
+        coords = np.zeros((E,) + (self.n,) * self.ndims + (self.ndims,))
+        self.lib.orc_get_mesh(self.h, _p(nb, ctypes.c_int64), _p(orient, ctypes.c_int64),
+                              _p(invj), _p(coords))
+        return dict(neighbor_ids=nb, orientations=orient, inverse_jacobian=invj,
+                    node_coordinates=coords)
+
+    def initial_condition(self, ic, params=None, t=0.0):
+        u = np.zeros(self.shape)
+        par = None if params is None else np.ascontiguousarray(params, dtype=np.float64)
+        self.lib.orc_initial_condition(self.h, ic, None if par is None else _p(par), t, _p(u))
+        return u
+
+    def rhs(self, u, t=0.0):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        du = np.zeros_like(u)
+        self.lib.orc_rhs(self.h, _p(du), _p(u), t)
+        return du
+
+    def alpha(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        a = np.zeros(self.nelements)
+        self.lib.orc_alpha(self.h, _p(u), _p(a))
+        return a
+
+    def max_dt(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        return self.lib.orc_max_dt(self.h, _p(u))
+
+    def rk_stage(self, u, u_tmp, stage, t, dt):
+        """In place: du = rhs(u, t + c_s dt); u_tmp = du - a_s u_tmp; u += b_s dt u_tmp."""
+        du = np.zeros_like(u)
+        self.lib.orc_rk_stage(self.h, _p(u), _p(u_tmp), _p(du), stage, t, dt)
+        return du
+
+    def solve(self, u, t0, t_end, cfl, max_steps=10**9):
+        u = np.ascontiguousarray(u, dtype=np.float64).copy()
+        t_out = ctypes.c_double(0)
+        nsteps = ctypes.c_int64(0)
+        rc = self.lib.orc_solve(self.h, _p(u), t0, t_end, cfl, max_steps,
+                                ctypes.byref(t_out), ctypes.byref(nsteps))
+        if rc != 0:
+            raise FloatingPointError("oracle: time step size is NaN")
+        return u, t_out.value, nsteps.value
+
+    def error_norms(self, u, t, ic, params=None):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        l2 = np.zeros(self.nvar)
+        linf = np.zeros(self.nvar)
+        par = None if params is None else np.ascontiguousarray(params, dtype=np.float64)
+        self.lib.orc_error_norms(self.h, _p(u), t, ic, None if par is None else _p(par),
+                                 _p(l2), _p(linf))
+        return l2, linf
+
+    def integrals(self, u):
+        """Domain totals of each conserved variable, then entropy, then kinetic energy."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        out = np.zeros(self.nvar + 2)
+        self.lib.orc_integrals(self.h, _p(u), _p(out))
+        return out
+
+
+def set_threads(n: int) -> None:
+    _load().orc_set_threads(int(n))
+
+
+def max_threads() -> int:
+    return _load().orc_max_threads()

@@ -1,0 +1,1226 @@
+// TEST INFRASTRUCTURE ONLY -- the oracle.
+//
+// A CPU, FP64 restatement of Trixi.jl's DGSEM semidiscretization of the
+// compressible Euler equations on a uniformly refined, periodic TreeMesh
+// (2D and 3D), together with Trixi's own 2N low-storage Runge-Kutta driver,
+// the CFL step-size rule and the error norms of its AnalysisCallback.
+//
+// Only the test suite, the smoke check and the CPU-baseline leg of the
+// benchmark load this library.  It is never part of the product path.
+//
+// Each function names the reference file:line it restates (paths relative to
+// the Trixi.jl source tree).  Parity of this restatement is pinned against the
+// L2/Linf goldens that Trixi's own regression tests hold for the TreeMesh
+// Euler elixirs (test/test_tree_2d_euler.jl, test/test_tree_3d_euler.jl).
+//
+// Layout conventions follow Trixi exactly:
+//   u[v, i, j, (k), element]    (column-major; variables fastest)
+//   node_coordinates[d, i, j, (k), element]
+//   neighbor_ids[2, interface]  (1-based element ids), orientations[interface]
+// Matrices are stored row-major here: M[a*n + b] = M[a, b] (0-based a, b).
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+
+enum VolumeIntegral { VI_WEAK = 0, VI_FLUXDIFF = 1, VI_SHOCKCAPTURING_HG = 2 };
+enum Flux {
+  FLUX_CENTRAL = 0,
+  FLUX_RANOCHA = 1,
+  FLUX_SHIMA_ETAL = 2,
+  FLUX_LAX_FRIEDRICHS = 3,        // FluxLaxFriedrichs(max_abs_speed)
+  FLUX_LAX_FRIEDRICHS_NAIVE = 4,  // FluxLaxFriedrichs(max_abs_speed_naive)
+};
+enum Source { SRC_NONE = 0, SRC_CONVERGENCE_TEST = 1 };
+enum InitialCondition {
+  IC_CONSTANT = 0,
+  IC_CONVERGENCE_TEST = 1,
+  IC_ISENTROPIC_VORTEX = 2,
+  IC_WEAK_BLAST_WAVE = 3,
+  IC_KELVIN_HELMHOLTZ = 4,
+  IC_TAYLOR_GREEN = 5,
+  IC_GAUSSIAN_BLAST = 6,
+};
+
+// ---------------------------------------------------------------------------
+// LGL basis: src/solvers/dgsem/basis_lobatto_legendre.jl
+// ---------------------------------------------------------------------------
+
+// calc_q_and_l, basis_lobatto_legendre.jl:643-665 (Kopriva alg. 24)
+static void calc_q_and_l(int N, double x, double& q, double& qder, double& L) {
+  double L_Nm2 = 1.0, L_Nm1 = x, Lder_Nm2 = 0.0, Lder_Nm1 = 1.0;
+  L = x;
+  for (int i = 2; i <= N; ++i) {
+    L = ((2 * i - 1) * x * L_Nm1 - (i - 1) * L_Nm2) / i;
+    double Lder = Lder_Nm2 + (2 * i - 1) * L_Nm1;
+    L_Nm2 = L_Nm1;
+    L_Nm1 = L;
+    Lder_Nm2 = Lder_Nm1;
+    Lder_Nm1 = Lder;
+  }
+  q = (2.0 * N + 1) / (N + 1) * (x * L - L_Nm2);
+  qder = (2.0 * N + 1) * L;
+}
+
+// gauss_lobatto_nodes_weights, basis_lobatto_legendre.jl:570-640 (Kopriva alg. 25)
+static void lgl_nodes_weights(int n_nodes, std::vector<double>& nodes,
+                              std::vector<double>& weights) {
+  nodes.assign(n_nodes, 0.0);
+  weights.assign(n_nodes, 0.0);
+  if (n_nodes == 1) {
+    nodes[0] = 0;
+    weights[0] = 2;
+    return;
+  }
+  const int N = n_nodes - 1;
+  const double tol = 2 * 2.220446049250313e-16;
+  nodes[0] = -1;
+  nodes[N] = 1;
+  weights[0] = 2.0 / (N * (N + 1));
+  weights[N] = weights[0];
+  if (N > 1) {
+    const double cont1 = M_PI / N;
+    const double cont2 = 3.0 / (8 * N * M_PI);
+    for (int i = 1; i <= (N + 1) / 2 - 1; ++i) {
+      nodes[i] = -std::cos(cont1 * (i + 0.25) - cont2 / (i + 0.25));
+      for (int k = 0; k <= 20; ++k) {
+        double q, qder, L;
+        calc_q_and_l(N, nodes[i], q, qder, L);
+        double dx = -q / qder;
+        nodes[i] += dx;
+        if (std::fabs(dx) < tol * std::fabs(nodes[i])) break;
+      }
+      double q, qder, L;
+      calc_q_and_l(N, nodes[i], q, qder, L);
+      weights[i] = weights[0] / (L * L);
+      nodes[N - i] = -nodes[i];
+      weights[N - i] = weights[i];
+    }
+  }
+  if (n_nodes % 2 == 1) {
+    double q, qder, L;
+    calc_q_and_l(N, 0.0, q, qder, L);
+    nodes[N / 2] = 0;
+    weights[N / 2] = weights[0] / (L * L);
+  }
+}
+
+// barycentric_weights, basis_lobatto_legendre.jl:518-531
+static std::vector<double> barycentric_weights(const std::vector<double>& x) {
+  const int n = (int)x.size();
+  std::vector<double> w(n, 1.0);
+  for (int j = 1; j < n; ++j)
+    for (int k = 0; k < j; ++k) {
+      w[k] *= x[k] - x[j];
+      w[j] *= x[j] - x[k];
+    }
+  for (int j = 0; j < n; ++j) w[j] = 1.0 / w[j];
+  return w;
+}
+
+// polynomial_interpolation_matrix!, basis_lobatto_legendre.jl:471-498 (Kopriva alg. 32)
+static std::vector<double> interpolation_matrix(const std::vector<double>& xin,
+                                                const std::vector<double>& xout) {
+  const int nin = (int)xin.size(), nout = (int)xout.size();
+  std::vector<double> wb = barycentric_weights(xin);
+  std::vector<double> V(nout * nin, 0.0);
+  const double rt = 1.4901161193847656e-08;  // sqrt(eps), Julia isapprox default
+  for (int k = 0; k < nout; ++k) {
+    bool match = false;
+    for (int j = 0; j < nin; ++j) {
+      double a = xout[k], b = xin[j];
+      if (a == b || std::fabs(a - b) <= rt * std::max(std::fabs(a), std::fabs(b))) {
+        match = true;
+        V[k * nin + j] = 1;
+      }
+    }
+    if (!match) {
+      double s = 0;
+      for (int j = 0; j < nin; ++j) {
+        double t = wb[j] / (xout[k] - xin[j]);
+        V[k * nin + j] = t;
+        s += t;
+      }
+      for (int j = 0; j < nin; ++j) V[k * nin + j] /= s;
+    }
+  }
+  return V;
+}
+
+// legendre_polynomial_and_derivative, basis_lobatto_legendre.jl:677-706 (normalised)
+static double legendre_normalised(int N, double x) {
+  double poly;
+  if (N == 0) {
+    poly = 1;
+  } else if (N == 1) {
+    poly = x;
+  } else {
+    double p2 = 1, p1 = x;
+    poly = 0;
+    for (int i = 2; i <= N; ++i) {
+      poly = ((2 * i - 1) * x * p1 - (i - 1) * p2) / i;
+      p2 = p1;
+      p1 = poly;
+    }
+  }
+  return poly * std::sqrt(N + 0.5);
+}
+
+// Gauss-Jordan inverse with partial pivoting (Trixi calls LAPACK `inv`,
+// basis_lobatto_legendre.jl:721).
+static std::vector<double> invert(std::vector<double> A, int n) {
+  std::vector<double> B(n * n, 0.0);
+  for (int i = 0; i < n; ++i) B[i * n + i] = 1;
+  for (int c = 0; c < n; ++c) {
+    int p = c;
+    for (int r = c + 1; r < n; ++r)
+      if (std::fabs(A[r * n + c]) > std::fabs(A[p * n + c])) p = r;
+    if (p != c)
+      for (int k = 0; k < n; ++k) {
+        std::swap(A[c * n + k], A[p * n + k]);
+        std::swap(B[c * n + k], B[p * n + k]);
+      }
+    double piv = A[c * n + c];
+    for (int k = 0; k < n; ++k) {
+      A[c * n + k] /= piv;
+      B[c * n + k] /= piv;
+    }
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      double f = A[r * n + c];
+      if (f == 0) continue;
+      for (int k = 0; k < n; ++k) {
+        A[r * n + k] -= f * A[c * n + k];
+        B[r * n + k] -= f * B[c * n + k];
+      }
+    }
+  }
+  return B;
+}
+
+struct Basis {
+  int n = 0;
+  std::vector<double> nodes, weights, inv_weights;
+  std::vector<double> D, Dhat, Dsplit, Vinv;  // n x n, row-major
+  // analyzer (AnalysisCallback default analysis_polydeg = 2*polydeg,
+  // basis_lobatto_legendre.jl:274-290)
+  int na = 0;
+  std::vector<double> anodes, aweights, avand;  // avand: na x n
+};
+
+// LobattoLegendreBasis(RealT, polydeg), basis_lobatto_legendre.jl:54-85
+static Basis make_basis(int polydeg) {
+  Basis b;
+  b.n = polydeg + 1;
+  const int n = b.n;
+  lgl_nodes_weights(n, b.nodes, b.weights);
+  b.inv_weights.resize(n);
+  for (int i = 0; i < n; ++i) b.inv_weights[i] = 1.0 / b.weights[i];
+  // vandermonde_legendre + inv, basis_lobatto_legendre.jl:709-724
+  std::vector<double> V(n * n);
+  for (int i = 0; i < n; ++i)
+    for (int m = 0; m < n; ++m) V[i * n + m] = legendre_normalised(m, b.nodes[i]);
+  b.Vinv = invert(V, n);
+  // polynomial_derivative_matrix, basis_lobatto_legendre.jl:427-440 (Kopriva alg. 37)
+  std::vector<double> wb = barycentric_weights(b.nodes);
+  b.D.assign(n * n, 0.0);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j)
+      if (j != i) {
+        b.D[i * n + j] = (wb[j] / wb[i]) * 1.0 / (b.nodes[i] - b.nodes[j]);
+        b.D[i * n + i] -= b.D[i * n + j];
+      }
+  // calc_Dsplit, basis_lobatto_legendre.jl:414-424
+  b.Dsplit.resize(n * n);
+  for (int k = 0; k < n * n; ++k) b.Dsplit[k] = 2 * b.D[k];
+  b.Dsplit[0] += 1.0 / b.weights[0];
+  b.Dsplit[n * n - 1] -= 1.0 / b.weights[n - 1];
+  // calc_Dhat, basis_lobatto_legendre.jl:399-409
+  b.Dhat.resize(n * n);
+  for (int j = 0; j < n; ++j)
+    for (int m = 0; m < n; ++m) b.Dhat[j * n + m] = b.D[m * n + j];
+  for (int m = 0; m < n; ++m)
+    for (int j = 0; j < n; ++j) b.Dhat[j * n + m] *= -b.weights[m] / b.weights[j];
+  // analyzer
+  b.na = 2 * polydeg + 1;
+  lgl_nodes_weights(b.na, b.anodes, b.aweights);
+  b.avand = interpolation_matrix(b.nodes, b.anodes);
+  return b;
+}
+
+// ---------------------------------------------------------------------------
+// Euler physics: src/equations/compressible_euler_{2,3}d.jl,
+// src/equations/numerical_fluxes.jl, src/auxiliary/math.jl
+// ---------------------------------------------------------------------------
+
+struct Eq {
+  int D = 2;
+  int NV = 4;
+  double gamma = 1.4;
+  double inv_gamma_minus_one = 2.5;
+};
+
+// cons2prim, compressible_euler_2d.jl:2038-2046 / 3d analogue
+static inline void cons2prim(const Eq& eq, const double* u, double* prim) {
+  const double rho = u[0];
+  double ke = 0;
+  for (int d = 0; d < eq.D; ++d) {
+    prim[1 + d] = u[1 + d] / rho;
+    ke += u[1 + d] * prim[1 + d];
+  }
+  prim[0] = rho;
+  prim[eq.NV - 1] = (eq.gamma - 1) * (u[eq.NV - 1] - 0.5 * ke);
+}
+
+// flux(u, orientation), compressible_euler_2d.jl:415-432, 3d.jl:420-447
+static inline void flux_phys(const Eq& eq, const double* u, int o, double* f) {
+  double prim[5];
+  cons2prim(eq, u, prim);
+  const double p = prim[eq.NV - 1];
+  const double rvo = u[1 + o];
+  f[0] = rvo;
+  for (int d = 0; d < eq.D; ++d) f[1 + d] = rvo * prim[1 + d];
+  f[1 + o] += p;
+  f[eq.NV - 1] = (u[eq.NV - 1] + p) * prim[1 + o];
+}
+
+// ln_mean / inv_ln_mean, math.jl:198-210, 238-250
+static inline double ln_mean(double x, double y) {
+  const double f2 = (x * (x - 2 * y) + y * y) / (x * (x + 2 * y) + y * y);
+  if (f2 < 1.0e-4)
+    return (x + y) / (2 + f2 * (2.0 / 3 + f2 * (2.0 / 5 + f2 * (2.0 / 7))));
+  return (y - x) / std::log(y / x);
+}
+static inline double inv_ln_mean(double x, double y) {
+  const double f2 = (x * (x - 2 * y) + y * y) / (x * (x + 2 * y) + y * y);
+  if (f2 < 1.0e-4)
+    return (2 + f2 * (2.0 / 3 + f2 * (2.0 / 5 + f2 * (2.0 / 7)))) / (x + y);
+  return std::log(y / x) / (y - x);
+}
+
+// flux_ranocha, compressible_euler_2d.jl:686-722, 3d.jl:746-792
+static inline void flux_ranocha(const Eq& eq, const double* ul, const double* ur, int o,
+                                double* f) {
+  double pl[5], pr[5];
+  cons2prim(eq, ul, pl);
+  cons2prim(eq, ur, pr);
+  const int P = eq.NV - 1;
+  const double rho_mean = ln_mean(pl[0], pr[0]);
+  const double inv_rho_p_mean = pl[P] * pr[P] * inv_ln_mean(pl[0] * pr[P], pr[0] * pl[P]);
+  double vavg[3] = {0, 0, 0}, vsq = 0;
+  for (int d = 0; d < eq.D; ++d) {
+    vavg[d] = 0.5 * (pl[1 + d] + pr[1 + d]);
+    vsq += pl[1 + d] * pr[1 + d];
+  }
+  vsq *= 0.5;
+  const double p_avg = 0.5 * (pl[P] + pr[P]);
+  const double f1 = rho_mean * vavg[o];
+  f[0] = f1;
+  for (int d = 0; d < eq.D; ++d) f[1 + d] = f1 * vavg[d];
+  f[1 + o] += p_avg;
+  f[P] = f1 * (vsq + inv_rho_p_mean * eq.inv_gamma_minus_one) +
+         0.5 * (pl[P] * pr[1 + o] + pr[P] * pl[1 + o]);
+}
+
+// flux_shima_etal, compressible_euler_2d.jl:466-495, 3d analogue
+static inline void flux_shima(const Eq& eq, const double* ul, const double* ur, int o,
+                              double* f) {
+  double pl[5], pr[5];
+  cons2prim(eq, ul, pl);
+  cons2prim(eq, ur, pr);
+  const int P = eq.NV - 1;
+  const double rho_avg = 0.5 * (pl[0] + pr[0]);
+  double vavg[3] = {0, 0, 0}, kin = 0;
+  for (int d = 0; d < eq.D; ++d) {
+    vavg[d] = 0.5 * (pl[1 + d] + pr[1 + d]);
+    kin += pl[1 + d] * pr[1 + d];
+  }
+  kin *= 0.5;
+  const double p_avg = 0.5 * (pl[P] + pr[P]);
+  const double pv_avg = 0.5 * (pl[P] * pr[1 + o] + pr[P] * pl[1 + o]);
+  const double f1 = rho_avg * vavg[o];
+  f[0] = f1;
+  for (int d = 0; d < eq.D; ++d) f[1 + d] = f1 * vavg[d];
+  f[1 + o] += p_avg;
+  f[P] = p_avg * vavg[o] * eq.inv_gamma_minus_one + f1 * kin + pv_avg;
+}
+
+// flux_central, numerical_fluxes.jl:17-25
+static inline void flux_central(const Eq& eq, const double* ul, const double* ur, int o,
+                                double* f) {
+  double fl[5], fr[5];
+  flux_phys(eq, ul, o, fl);
+  flux_phys(eq, ur, o, fr);
+  for (int v = 0; v < eq.NV; ++v) f[v] = 0.5 * (fl[v] + fr[v]);
+}
+
+// max_abs_speed / max_abs_speed_naive, compressible_euler_2d.jl:1423-1482
+static inline double max_abs_speed(const Eq& eq, const double* ul, const double* ur, int o,
+                                   bool naive) {
+  double pl[5], pr[5];
+  cons2prim(eq, ul, pl);
+  cons2prim(eq, ur, pr);
+  const int P = eq.NV - 1;
+  const double vl = pl[1 + o], vr = pr[1 + o];
+  const double cl = std::sqrt(eq.gamma * pl[P] / pl[0]);
+  const double cr = std::sqrt(eq.gamma * pr[P] / pr[0]);
+  if (naive) return std::max(std::fabs(vl), std::fabs(vr)) + std::max(cl, cr);
+  return std::max(std::fabs(vl) + cl, std::fabs(vr) + cr);
+}
+
+// FluxLaxFriedrichs = flux_central + DissipationLocalLaxFriedrichs,
+// numerical_fluxes.jl:32-45, 166-178, 222-253
+static inline void flux_llf(const Eq& eq, const double* ul, const double* ur, int o,
+                            bool naive, double* f) {
+  flux_central(eq, ul, ur, o, f);
+  const double lam = max_abs_speed(eq, ul, ur, o, naive);
+  for (int v = 0; v < eq.NV; ++v) f[v] = f[v] + (-0.5 * lam * (ur[v] - ul[v]));
+}
+
+static inline void two_point_flux(const Eq& eq, int kind, const double* ul, const double* ur,
+                                  int o, double* f) {
+  switch (kind) {
+    case FLUX_CENTRAL: flux_central(eq, ul, ur, o, f); break;
+    case FLUX_RANOCHA: flux_ranocha(eq, ul, ur, o, f); break;
+    case FLUX_SHIMA_ETAL: flux_shima(eq, ul, ur, o, f); break;
+    case FLUX_LAX_FRIEDRICHS: flux_llf(eq, ul, ur, o, false, f); break;
+    case FLUX_LAX_FRIEDRICHS_NAIVE: flux_llf(eq, ul, ur, o, true, f); break;
+    default: for (int v = 0; v < eq.NV; ++v) f[v] = NAN;
+  }
+}
+
+// max_abs_speeds, compressible_euler_2d.jl:2025-2030
+static inline void max_abs_speeds(const Eq& eq, const double* u, double* lam) {
+  double prim[5];
+  cons2prim(eq, u, prim);
+  const double c = std::sqrt(eq.gamma * prim[eq.NV - 1] / prim[0]);
+  for (int d = 0; d < eq.D; ++d) lam[d] = std::fabs(prim[1 + d]) + c;
+}
+
+// density_pressure, compressible_euler_2d.jl:2205-2210, 3d analogue
+static inline double density_pressure(const Eq& eq, const double* u) {
+  double m2 = 0;
+  for (int d = 0; d < eq.D; ++d) m2 += u[1 + d] * u[1 + d];
+  return (eq.gamma - 1) * (u[0] * u[eq.NV - 1] - 0.5 * m2);
+}
+
+// source_terms_convergence_test, compressible_euler_2d.jl:116-145, 3d.jl:127-150
+static inline void source_convergence(const Eq& eq, const double* x, double t, double* s) {
+  const double c = 2, A = 0.1, omega = 2 * M_PI * 0.5;
+  const double g = eq.gamma;
+  // Julia evaluates x1 + x2 (+ x3) - t left to right
+  double arg = x[0] + x[1];
+  if (eq.D == 3) arg += x[2];
+  arg = omega * (arg - t);
+  const double si = std::sin(arg), co = std::cos(arg);
+  const double rho = c + A * si;
+  const double rho_x = omega * A * co;
+  if (eq.D == 2) {
+    const double tmp = (2 * rho - 1) * (g - 1);
+    s[0] = rho_x;
+    s[1] = rho_x * (1 + tmp);
+    s[2] = s[1];
+    s[3] = 2 * rho_x * (rho + tmp);
+  } else {
+    const double tmp = (2 * rho - 1.5) * (g - 1);
+    s[0] = 2 * rho_x;
+    s[1] = rho_x * (2 + tmp);
+    s[2] = s[1];
+    s[3] = s[1];
+    s[4] = rho_x * (4 * rho + 3 * tmp);
+  }
+}
+
+// sin(pi a) with the argument reduced to [-1, 1] first, so that integer
+// arguments give an exact zero (Julia's sinpi has the same property).
+static inline double sinpi(double a) {
+  double r = std::fmod(a, 2.0);
+  if (r > 1) r -= 2;
+  if (r < -1) r += 2;
+  if (r == 0 || r == 1 || r == -1) return 0.0;
+  return std::sin(M_PI * r);
+}
+
+static inline void prim2cons(const Eq& eq, const double* prim, double* u) {
+  u[0] = prim[0];
+  double ke = 0;
+  for (int d = 0; d < eq.D; ++d) {
+    u[1 + d] = prim[0] * prim[1 + d];
+    ke += u[1 + d] * prim[1 + d];
+  }
+  u[eq.NV - 1] = prim[eq.NV - 1] * eq.inv_gamma_minus_one + 0.5 * ke;
+}
+
+// Initial conditions.  params[] carries the free constants of the configurable
+// ones (see each case).
+static void initial_condition(const Eq& eq, int ic, const double* par, const double* x,
+                              double t, double* u) {
+  double prim[5];
+  const int P = eq.NV - 1;
+  switch (ic) {
+    case IC_CONSTANT: {
+      // initial_condition_constant, compressible_euler_2d.jl:71-78 / 3d.jl:71-79
+      if (eq.D == 2) {
+        u[0] = 1; u[1] = 0.1; u[2] = -0.2; u[3] = 10;
+      } else {
+        u[0] = 1; u[1] = 0.1; u[2] = -0.2; u[3] = 0.7; u[4] = 10;
+      }
+      return;
+    }
+    case IC_CONVERGENCE_TEST: {
+      // initial_condition_convergence_test, compressible_euler_2d.jl:87-104, 3d.jl:93-110
+      const double c = 2, A = 0.1, omega = 2 * M_PI * 0.5;
+      double arg = x[0] + x[1];
+      if (eq.D == 3) arg += x[2];
+      const double ini = c + A * std::sin(omega * (arg - t));
+      for (int v = 0; v < P; ++v) u[v] = ini;
+      u[P] = ini * ini;
+      return;
+    }
+    case IC_ISENTROPIC_VORTEX: {
+      // examples/tree_2d_dgsem/elixir_euler_vortex.jl:18-52; par = {p_inf, amplitude}
+      const double p0 = par ? par[0] : 25.0;
+      const double amp = par ? par[1] : 5.0;
+      double rho = 1, v1 = 1, v2 = 1, p = p0;
+      const double rt = p / rho;
+      double c0 = x[0], c1 = x[1];
+      double cent0 = -c1, cent1 = c0;
+      const double r2 = cent0 * cent0 + cent1 * cent1;
+      const double du = amp / (2 * M_PI) * std::exp(0.5 * (1 - r2));
+      const double dtemp = -(eq.gamma - 1) / (2 * eq.gamma * rt) * du * du;
+      rho = rho * std::pow(1 + dtemp, 1 / (eq.gamma - 1));
+      v1 = v1 + du * cent0;
+      v2 = v2 + du * cent1;
+      p = p * std::pow(1 + dtemp, eq.gamma / (eq.gamma - 1));
+      prim[0] = rho; prim[1] = v1; prim[2] = v2; prim[3] = p;
+      prim2cons(eq, prim, u);
+      return;
+    }
+    case IC_WEAK_BLAST_WAVE: {
+      // initial_condition_weak_blast_wave, compressible_euler_2d.jl:245-264, 3d.jl:241-263
+      if (eq.D == 2) {
+        const double r = std::sqrt(x[0] * x[0] + x[1] * x[1]);
+        const double phi = std::atan2(x[1], x[0]);
+        const double s = std::sin(phi), c = std::cos(phi);
+        const bool out = r > 0.5;
+        prim[0] = out ? 1.0 : 1.1691;
+        prim[1] = out ? 0.0 : 0.1882 * c;
+        prim[2] = out ? 0.0 : 0.1882 * s;
+        prim[3] = out ? 1.0 : 1.245;
+      } else {
+        const double r = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+        const double phi = std::atan2(x[1], x[0]);
+        const double theta = r == 0 ? 0.0 : std::acos(x[2] / r);
+        const bool out = r > 0.5;
+        prim[0] = out ? 1.0 : 1.1691;
+        prim[1] = out ? 0.0 : 0.1882 * std::cos(phi) * std::sin(theta);
+        prim[2] = out ? 0.0 : 0.1882 * std::sin(phi) * std::sin(theta);
+        prim[3] = out ? 0.0 : 0.1882 * std::cos(theta);
+        prim[4] = out ? 1.0 : 1.245;
+      }
+      prim2cons(eq, prim, u);
+      return;
+    }
+    case IC_KELVIN_HELMHOLTZ: {
+      // examples/tree_2d_dgsem/elixir_euler_kelvin_helmholtz_instability.jl:18-31
+      const double slope = 15;
+      const double B = std::tanh(slope * x[1] + 7.5) - std::tanh(slope * x[1] - 7.5);
+      prim[0] = 0.5 + 0.75 * B;
+      prim[1] = 0.5 * (B - 1);
+      prim[2] = 0.1 * sinpi(2 * x[0]);
+      prim[3] = 1;
+      prim2cons(eq, prim, u);
+      return;
+    }
+    case IC_TAYLOR_GREEN: {
+      // examples/tree_3d_dgsem/elixir_euler_taylor_green_vortex.jl:14-30; par = {Ms}
+      const double A = 1.0, Ms = par ? par[0] : 0.1, rho = 1.0;
+      prim[0] = rho;
+      prim[1] = A * std::sin(x[0]) * std::cos(x[1]) * std::cos(x[2]);
+      prim[2] = -A * std::cos(x[0]) * std::sin(x[1]) * std::cos(x[2]);
+      prim[3] = 0.0;
+      double p = (A / Ms) * (A / Ms) * rho / eq.gamma;
+      p = p + 1.0 / 16.0 * A * A * rho *
+                  (std::cos(2 * x[0]) * std::cos(2 * x[2]) + 2 * std::cos(2 * x[1]) +
+                   2 * std::cos(2 * x[0]) + std::cos(2 * x[1]) * std::cos(2 * x[2]));
+      prim[4] = p;
+      prim2cons(eq, prim, u);
+      return;
+    }
+    case IC_GAUSSIAN_BLAST: {
+      // Gaussian energy deposit (no reference elixir): rho = 1, p = p_bg +
+      // (gamma-1) * E * exp(-r^2/w^2) / (pi w^2); par = {p_bg, E, w}
+      const double pbg = par ? par[0] : 1e-5, E = par ? par[1] : 1.0, w = par ? par[2] : 0.25;
+      double r2 = 0;
+      for (int d = 0; d < eq.D; ++d) r2 += x[d] * x[d];
+      double norm = eq.D == 2 ? M_PI * w * w : std::pow(M_PI * w * w, 1.5);
+      prim[0] = 1;
+      for (int d = 0; d < eq.D; ++d) prim[1 + d] = 0;
+      prim[P] = pbg + (eq.gamma - 1) * E * std::exp(-r2 / (w * w)) / norm;
+      prim2cons(eq, prim, u);
+      return;
+    }
+    default:
+      for (int v = 0; v < eq.NV; ++v) u[v] = NAN;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Mesh: uniformly refined periodic TreeMesh
+//   src/meshes/tree_mesh.jl:128-185, abstract_tree.jl:122-130, 206-248, 668-674,
+//   src/solvers/dgsem_tree/containers_2d.jl:85-127, 228-284 (3d: 87, 229)
+// ---------------------------------------------------------------------------
+
+struct Mesh {
+  int D = 2, level = 0, M = 1;  // M cells per direction
+  int64_t nelem = 0, nif = 0;
+  std::vector<int> cart;        // [3, E] Cartesian cell index
+  std::vector<double> center;   // [D, E]
+  std::vector<double> inverse_jacobian;  // [E]
+  std::vector<double> node_coords;       // [D, n^D, E]
+  std::vector<int64_t> if_left, if_right;  // 0-based
+  std::vector<int> if_orient;               // 0-based orientation
+  std::vector<int64_t> nbr;  // [E, 2D]: neighbour across face (0:-x,1:+x,2:-y,...)
+  double length0 = 0;
+  double xmin[3] = {0, 0, 0};
+};
+
+static void refine_dfs(Mesh& m, int level, int maxlevel, const double* c, double len,
+                       const int* ci) {
+  if (level >= maxlevel) {
+    for (int d = 0; d < m.D; ++d) m.center.push_back(c[d]);
+    for (int d = 0; d < 3; ++d) m.cart.push_back(ci[d]);
+    return;
+  }
+  const int nchild = 1 << m.D;
+  for (int child = 0; child < nchild; ++child) {
+    double cc[3];
+    int cci[3] = {0, 0, 0};
+    const double child_len = len / 2;
+    for (int d = 0; d < m.D; ++d) {
+      const int bit = (child >> d) & 1;  // _child_signs: x fastest
+      const double sign = bit ? 1.0 : -1.0;
+      cc[d] = c[d] + sign * child_len / 2;
+      cci[d] = 2 * ci[d] + bit;
+    }
+    refine_dfs(m, level + 1, maxlevel, cc, child_len, cci);
+  }
+}
+
+static Mesh make_mesh(int D, int level, const double* xmin, const double* xmax,
+                      const Basis& b) {
+  Mesh m;
+  m.D = D;
+  m.level = level;
+  m.M = 1 << level;
+  double c0[3];
+  for (int d = 0; d < D; ++d) {
+    c0[d] = (xmin[d] + xmax[d]) / 2;
+    m.xmin[d] = xmin[d];
+  }
+  m.length0 = xmax[0] - xmin[0];
+  int ci0[3] = {0, 0, 0};
+  refine_dfs(m, 0, level, c0, m.length0, ci0);
+  m.nelem = (int64_t)m.center.size() / D;
+  const int n = b.n;
+  int nn = 1;
+  for (int d = 0; d < D; ++d) nn *= n;
+  // reference_length = integrate(one, nodes, basis): sum of weights
+  double reference_length = 0;
+  for (int i = 0; i < n; ++i) reference_length += 1.0 * b.weights[i];
+  const double reference_offset = (b.nodes[0] + b.nodes[n - 1]) / 2;
+  const double dx = m.length0 / (double)(1 << level);
+  const double jac = dx / reference_length;
+  m.inverse_jacobian.assign(m.nelem, 1.0 / jac);
+  m.node_coords.resize((size_t)D * nn * m.nelem);
+  for (int64_t e = 0; e < m.nelem; ++e)
+    for (int node = 0; node < nn; ++node) {
+      int idx[3] = {node % n, (node / n) % n, node / (n * n)};
+      for (int d = 0; d < D; ++d)
+        m.node_coords[((size_t)e * nn + node) * D + d] =
+            m.center[e * D + d] + jac * (b.nodes[idx[d]] - reference_offset);
+    }
+  // cartesian -> element map
+  std::vector<int64_t> c2e((size_t)1 << (D * level));
+  auto lin = [&](int i, int j, int k) -> size_t {
+    return (size_t)i + (size_t)m.M * ((size_t)j + (size_t)m.M * (size_t)k);
+  };
+  for (int64_t e = 0; e < m.nelem; ++e)
+    c2e[lin(m.cart[3 * e], m.cart[3 * e + 1], m.cart[3 * e + 2])] = e;
+  m.nbr.assign((size_t)m.nelem * 2 * D, -1);
+  for (int64_t e = 0; e < m.nelem; ++e) {
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      int c[3] = {m.cart[3 * e], m.cart[3 * e + 1], m.cart[3 * e + 2]};
+      const int d = dir / 2;
+      c[d] = (c[d] + (dir % 2 ? 1 : m.M - 1)) % m.M;
+      m.nbr[e * 2 * D + dir] = c2e[lin(c[0], c[1], c[2])];
+    }
+    // init_interfaces!: per element in order, positive directions only
+    for (int d = 0; d < D; ++d) {
+      m.if_left.push_back(e);
+      m.if_right.push_back(m.nbr[e * 2 * D + 2 * d + 1]);
+      m.if_orient.push_back(d);
+    }
+  }
+  m.nif = (int64_t)m.if_left.size();
+  return m;
+}
+
+// ---------------------------------------------------------------------------
+// Solver
+// ---------------------------------------------------------------------------
+
+struct Solver {
+  Eq eq;
+  Basis b;
+  Mesh m;
+  int nn = 0;  // nodes per element
+  int vi = VI_WEAK, vflux = FLUX_CENTRAL, sflux = FLUX_LAX_FRIEDRICHS,
+      fvflux = FLUX_LAX_FRIEDRICHS;
+  double alpha_max = 0.5, alpha_min = 0.001;
+  bool alpha_smooth = true;
+  int source = SRC_NONE;
+  std::vector<double> alpha, alpha_tmp, sfv;  // sfv: [NV, n^(D-1), 2D, E]
+  int64_t ndofs() const { return (int64_t)nn * m.nelem; }
+};
+
+static inline size_t uidx(const Solver& s, int64_t e, int node, int v) {
+  return ((size_t)e * s.nn + node) * s.eq.NV + v;
+}
+
+// HG indicator: indicators.jl:114-148 + indicators_2d.jl:30-101, indicators_3d.jl:39-123
+static void calc_alpha(Solver& s, const double* u) {
+  const int n = s.b.n, D = s.eq.D, nn = s.nn;
+  const double threshold = 0.5 * std::pow(10.0, -1.8 * std::pow((double)n, 0.25));
+  const double o_0001 = 0.0001;
+  const double parameter_s = std::log((1 - o_0001) / o_0001);
+  s.alpha.assign(s.m.nelem, 0.0);
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < s.m.nelem; ++e) {
+    double ind[512], t1[512], t2[512];
+    for (int node = 0; node < nn; ++node) ind[node] = density_pressure(s.eq, &u[uidx(s, e, node, 0)]);
+    const double* V = s.b.Vinv.data();
+    // multiply_scalar_dimensionwise!, interpolation.jl:207-234, 348-385
+    double* in = ind;
+    double* out = t1;
+    for (int d = 0; d < D; ++d) {
+      int stride = 1;
+      for (int q = 0; q < d; ++q) stride *= n;
+      for (int node = 0; node < nn; ++node) {
+        const int i = (node / stride) % n;
+        const int base = node - i * stride;
+        double r = 0;
+        for (int ii = 0; ii < n; ++ii) r += V[i * n + ii] * in[base + ii * stride];
+        out[node] = r;
+      }
+      in = out;
+      out = (out == t1) ? t2 : t1;
+    }
+    const double* modal = in;
+    double e_clip2 = 0, e_clip1 = 0, e_tot = 0;
+    for (int node = 0; node < nn; ++node) {
+      int idx[3] = {node % n, (node / n) % n, node / (n * n)};
+      int mx = 0;
+      for (int d = 0; d < D; ++d) mx = std::max(mx, idx[d]);
+      const double m2 = modal[node] * modal[node];
+      if (mx <= n - 3) e_clip2 += m2;
+      if (mx <= n - 2) e_clip1 += m2;
+      e_tot += m2;
+    }
+    double f1 = e_tot != 0 ? (e_tot - e_clip1) / e_tot : 0.0;
+    double f2 = e_clip1 != 0 ? (e_clip1 - e_clip2) / e_clip1 : 0.0;
+    const double energy = std::max(f1, f2);
+    double a = 1 / (1 + std::exp(-parameter_s / threshold * (energy - threshold)));
+    if (a < s.alpha_min) a = 0;
+    if (a > 1 - s.alpha_min) a = 1;
+    s.alpha[e] = std::min(s.alpha_max, a);
+  }
+  if (s.alpha_smooth) {
+    // apply_smoothing!, indicators_2d.jl:104-136
+    s.alpha_tmp = s.alpha;
+    for (int64_t f = 0; f < s.m.nif; ++f) {
+      const int64_t l = s.m.if_left[f], r = s.m.if_right[f];
+      s.alpha[l] = std::max({s.alpha_tmp[l], 0.5 * s.alpha_tmp[r], s.alpha[l]});
+      s.alpha[r] = std::max({s.alpha_tmp[r], 0.5 * s.alpha_tmp[l], s.alpha[r]});
+    }
+  }
+}
+
+// weak_form_kernel!, dg_2d.jl:195-221, dg_3d.jl:133-164
+static void weak_form(const Solver& s, double* du, const double* u, int64_t e) {
+  const int n = s.b.n, D = s.eq.D, NV = s.eq.NV;
+  for (int node = 0; node < s.nn; ++node) {
+    const double* un = &u[uidx(s, e, node, 0)];
+    int idx[3] = {node % n, (node / n) % n, node / (n * n)};
+    for (int d = 0; d < D; ++d) {
+      double f[5];
+      flux_phys(s.eq, un, d, f);
+      int stride = 1;
+      for (int q = 0; q < d; ++q) stride *= n;
+      const int base = node - idx[d] * stride;
+      for (int ii = 0; ii < n; ++ii) {
+        const double fac = s.b.Dhat[ii * n + idx[d]];
+        double* dt = &du[uidx(s, e, base + ii * stride, 0)];
+        for (int v = 0; v < NV; ++v) dt[v] = dt[v] + fac * f[v];
+      }
+    }
+  }
+}
+
+// flux_differencing_kernel!, dg_2d.jl:223-259, dg_3d.jl:166-214
+static void flux_differencing(const Solver& s, double* du, const double* u, int64_t e,
+                              double alpha) {
+  const int n = s.b.n, D = s.eq.D, NV = s.eq.NV;
+  for (int node = 0; node < s.nn; ++node) {
+    const double* un = &u[uidx(s, e, node, 0)];
+    int idx[3] = {node % n, (node / n) % n, node / (n * n)};
+    for (int d = 0; d < D; ++d) {
+      int stride = 1;
+      for (int q = 0; q < d; ++q) stride *= n;
+      const int i = idx[d];
+      const int base = node - i * stride;
+      for (int ii = i + 1; ii < n; ++ii) {
+        const int pn = base + ii * stride;
+        double f[5];
+        two_point_flux(s.eq, s.vflux, un, &u[uidx(s, e, pn, 0)], d, f);
+        const double f_i = alpha * s.b.Dsplit[i * n + ii];
+        const double f_ii = alpha * s.b.Dsplit[ii * n + i];
+        double* di = &du[uidx(s, e, node, 0)];
+        double* dii = &du[uidx(s, e, pn, 0)];
+        for (int v = 0; v < NV; ++v) {
+          di[v] = di[v] + f_i * f[v];
+          dii[v] = dii[v] + f_ii * f[v];
+        }
+      }
+    }
+  }
+}
+
+// fv_kernel! + calcflux_fv!, dg_2d.jl:407-464, dg_3d.jl:268-390
+static void fv_volume(const Solver& s, double* du, const double* u, int64_t e, double alpha) {
+  const int n = s.b.n, D = s.eq.D, NV = s.eq.NV;
+  // fstar[d][v][node-position along d in 0..n][other node]: stored per node as
+  // flux between (i-1, i) at slot i, zero at slots 0 and n.
+  std::vector<double> fstar((size_t)D * (n + 1) * s.nn / n * NV, 0.0);
+  const int nl = s.nn / n;  // lines per direction
+  auto fidx = [&](int d, int slot, int line, int v) -> size_t {
+    return (((size_t)d * (n + 1) + slot) * nl + line) * NV + v;
+  };
+  for (int d = 0; d < D; ++d) {
+    int stride = 1;
+    for (int q = 0; q < d; ++q) stride *= n;
+    for (int node = 0; node < s.nn; ++node) {
+      const int i = (node / stride) % n;
+      if (i == 0) continue;
+      const int base = node - i * stride;
+      const int line = (base % stride) + (base / (stride * n)) * stride;
+      double f[5];
+      two_point_flux(s.eq, s.fvflux, &u[uidx(s, e, base + (i - 1) * stride, 0)],
+                     &u[uidx(s, e, node, 0)], d, f);
+      for (int v = 0; v < NV; ++v) fstar[fidx(d, i, line, v)] = f[v];
+    }
+  }
+  for (int node = 0; node < s.nn; ++node) {
+    double acc[5] = {0, 0, 0, 0, 0};
+    for (int d = 0; d < D; ++d) {
+      int stride = 1;
+      for (int q = 0; q < d; ++q) stride *= n;
+      const int i = (node / stride) % n;
+      const int base = node - i * stride;
+      const int line = (base % stride) + (base / (stride * n)) * stride;
+      for (int v = 0; v < NV; ++v)
+        acc[v] += s.b.inv_weights[i] * (fstar[fidx(d, i + 1, line, v)] - fstar[fidx(d, i, line, v)]);
+    }
+    double* dn = &du[uidx(s, e, node, 0)];
+    for (int v = 0; v < NV; ++v) dn[v] += alpha * acc[v];
+  }
+}
+
+// rhs_hyperbolic!, dg_2d.jl:113-186 (periodic, conforming: no boundaries/mortars)
+static void rhs(Solver& s, double* du, const double* u, double t) {
+  const int n = s.b.n, D = s.eq.D, NV = s.eq.NV, nn = s.nn;
+  const int64_t E = s.m.nelem;
+  const int nf = nn / n;  // nodes per face
+  // set_zero!
+  std::memset(du, 0, sizeof(double) * (size_t)E * nn * NV);
+  // calc_volume_integral!, calc_volume_integral.jl:180-191, 231-272
+  if (s.vi == VI_SHOCKCAPTURING_HG) calc_alpha(s, u);
+  const double atol = std::max(100 * 2.220446049250313e-16, std::pow(2.220446049250313e-16, 0.75));
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < E; ++e) {
+    if (s.vi == VI_WEAK) {
+      weak_form(s, du, u, e);
+    } else if (s.vi == VI_FLUXDIFF) {
+      flux_differencing(s, du, u, e, 1.0);
+    } else {
+      const double a = s.alpha[e];
+      if (std::fabs(a) <= atol) {
+        flux_differencing(s, du, u, e, 1.0);
+      } else {
+        flux_differencing(s, du, u, e, 1 - a);
+        fv_volume(s, du, u, e, a);
+      }
+    }
+  }
+  // prolong2interfaces! + calc_interface_flux!, dg_2d.jl:515-541, 600-632
+  s.sfv.resize((size_t)NV * nf * 2 * D * E);
+  auto sidx = [&](int64_t e, int dir, int fn, int v) -> size_t {
+    return (((size_t)e * 2 * D + dir) * nf + fn) * NV + v;
+  };
+#pragma omp parallel for schedule(static)
+  for (int64_t f = 0; f < s.m.nif; ++f) {
+    const int64_t l = s.m.if_left[f], r = s.m.if_right[f];
+    const int o = s.m.if_orient[f];
+    int stride = 1;
+    for (int q = 0; q < o; ++q) stride *= n;
+    for (int fn = 0; fn < nf; ++fn) {
+      // face node fn enumerates the remaining indices in order
+      const int lo = fn % stride, hi = fn / stride;
+      const int base = lo + hi * stride * n;
+      const double* ul = &u[uidx(s, l, base + (n - 1) * stride, 0)];
+      const double* ur = &u[uidx(s, r, base, 0)];
+      double F[5];
+      two_point_flux(s.eq, s.sflux, ul, ur, o, F);
+      for (int v = 0; v < NV; ++v) {
+        s.sfv[sidx(l, 2 * o + 1, fn, v)] = F[v];
+        s.sfv[sidx(r, 2 * o, fn, v)] = F[v];
+      }
+    }
+  }
+  // calc_surface_integral!, dg_2d.jl:1245-1287; apply_jacobian!, dg_2d.jl:1345-1363;
+  // calc_sources!, dg_2d.jl:1366-1386
+  const double factor = s.b.inv_weights[0];
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < E; ++e) {
+    for (int o = 0; o < D; ++o) {
+      int stride = 1;
+      for (int q = 0; q < o; ++q) stride *= n;
+      for (int fn = 0; fn < nf; ++fn) {
+        const int lo = fn % stride, hi = fn / stride;
+        const int base = lo + hi * stride * n;
+        double* dm = &du[uidx(s, e, base, 0)];
+        double* dp = &du[uidx(s, e, base + (n - 1) * stride, 0)];
+        for (int v = 0; v < NV; ++v) {
+          dm[v] = dm[v] - s.sfv[sidx(e, 2 * o, fn, v)] * factor;
+          dp[v] = dp[v] + s.sfv[sidx(e, 2 * o + 1, fn, v)] * factor;
+        }
+      }
+    }
+    const double fac = -s.m.inverse_jacobian[e];
+    for (int node = 0; node < nn; ++node)
+      for (int v = 0; v < NV; ++v) du[uidx(s, e, node, v)] *= fac;
+    if (s.source == SRC_CONVERGENCE_TEST) {
+      for (int node = 0; node < nn; ++node) {
+        double src[5];
+        source_convergence(s.eq, &s.m.node_coords[((size_t)e * nn + node) * D], t, src);
+        for (int v = 0; v < NV; ++v) du[uidx(s, e, node, v)] += src[v];
+      }
+    }
+  }
+}
+
+// max_dt, stepsize_dg2d.jl:8-30, stepsize_dg3d.jl:8-33
+static double max_dt(const Solver& s, const double* u) {
+  const int D = s.eq.D;
+  double mss = 4.9406564584124654e-324;  // nextfloat(0.0)
+  for (int64_t e = 0; e < s.m.nelem; ++e) {
+    double ml[3] = {0, 0, 0};
+    for (int node = 0; node < s.nn; ++node) {
+      double lam[3];
+      max_abs_speeds(s.eq, &u[uidx(s, e, node, 0)], lam);
+      for (int d = 0; d < D; ++d) ml[d] = std::max(ml[d], lam[d]);
+    }
+    double sum = ml[0] + ml[1];
+    if (D == 3) sum += ml[2];
+    mss = std::max(mss, s.m.inverse_jacobian[e] * sum);
+  }
+  return 2 / (s.b.n * mss);
+}
+
+// CarpenterKennedy2N54, methods_2N.jl:24-48
+static const double CK_A[5] = {0.0, 567301805773.0 / 1357537059087.0,
+                                2404267990393.0 / 2016746695238.0,
+                                3550918686646.0 / 2091501179385.0,
+                                1275806237668.0 / 842570457699.0};
+static const double CK_B[5] = {1432997174477.0 / 9575080441755.0,
+                               5161836677717.0 / 13612068292357.0,
+                               1720146321549.0 / 2090206949498.0,
+                               3134564353537.0 / 4481467310338.0,
+                               2277821191437.0 / 14882151754819.0};
+static const double CK_C[5] = {0.0, 1432997174477.0 / 9575080441755.0,
+                               2526269341429.0 / 6820363962896.0,
+                               2006345519317.0 / 3224310063776.0,
+                               2802321613138.0 / 2924317926251.0};
+
+// One 2N stage update, methods_2N.jl:153-157
+static void rk_update(int64_t ndof, double* u, double* u_tmp, const double* du, double a,
+                      double b_dt) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < ndof; ++i) {
+    u_tmp[i] = du[i] - u_tmp[i] * a;
+    u[i] += u_tmp[i] * b_dt;
+  }
+}
+
+// Julia isapprox(a, b) with default rtol = sqrt(eps)
+static bool isapprox(double a, double b) {
+  return a == b || std::fabs(a - b) <= 1.4901161193847656e-08 * std::max(std::fabs(a), std::fabs(b));
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+extern "C" {
+
+void* orc_create(int ndims, int polydeg, int level, const double* xmin, const double* xmax,
+                 double gamma, int volume_integral, int volume_flux, int surface_flux,
+                 int fv_flux, double alpha_max, double alpha_min, int alpha_smooth,
+                 int source) {
+  if (ndims < 2 || ndims > 3 || polydeg < 1 || polydeg > 7 || level < 0 || level > 10)
+    return nullptr;
+  Solver* s = new Solver();
+  s->eq.D = ndims;
+  s->eq.NV = ndims + 2;
+  s->eq.gamma = gamma;
+  s->eq.inv_gamma_minus_one = 1.0 / (gamma - 1);
+  s->b = make_basis(polydeg);
+  s->m = make_mesh(ndims, level, xmin, xmax, s->b);
+  s->nn = 1;
+  for (int d = 0; d < ndims; ++d) s->nn *= s->b.n;
+  s->vi = volume_integral;
+  s->vflux = volume_flux;
+  s->sflux = surface_flux;
+  s->fvflux = fv_flux;
+  s->alpha_max = alpha_max;
+  s->alpha_min = alpha_min;
+  s->alpha_smooth = alpha_smooth != 0;
+  s->source = source;
+  return s;
+}
+
+void orc_destroy(void* h) { delete (Solver*)h; }
+
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+int64_t orc_nelements(void* h) { return ((Solver*)h)->m.nelem; }
+int64_t orc_ninterfaces(void* h) { return ((Solver*)h)->m.nif; }
+int orc_nnodes(void* h) { return ((Solver*)h)->b.n; }
+int64_t orc_ndofs(void* h) { return ((Solver*)h)->ndofs(); }
+
+// Basis matrices are written column-major (Julia order) so that they compare
+// directly with what a Julia host passes.
+void orc_get_basis(void* h, double* nodes, double* weights, double* inv_weights, double* D,
+                   double* Dhat, double* Dsplit, double* Vinv) {
+  const Basis& b = ((Solver*)h)->b;
+  const int n = b.n;
+  for (int i = 0; i < n; ++i) {
+    nodes[i] = b.nodes[i];
+    weights[i] = b.weights[i];
+    inv_weights[i] = b.inv_weights[i];
+  }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      D[i + j * n] = b.D[i * n + j];
+      Dhat[i + j * n] = b.Dhat[i * n + j];
+      Dsplit[i + j * n] = b.Dsplit[i * n + j];
+      Vinv[i + j * n] = b.Vinv[i * n + j];
+    }
+}
+
+// neighbor_ids[2, I] (1-based), orientations[I] (1-based), inverse_jacobian[E],
+// node_coordinates[D, n^D, E]
+void orc_get_mesh(void* h, int64_t* neighbor_ids, int64_t* orientations,
+                  double* inverse_jacobian, double* node_coordinates) {
+  const Solver& s = *(Solver*)h;
+  for (int64_t f = 0; f < s.m.nif; ++f) {
+    neighbor_ids[2 * f] = s.m.if_left[f] + 1;
+    neighbor_ids[2 * f + 1] = s.m.if_right[f] + 1;
+    orientations[f] = s.m.if_orient[f] + 1;
+  }
+  for (int64_t e = 0; e < s.m.nelem; ++e) inverse_jacobian[e] = s.m.inverse_jacobian[e];
+  std::memcpy(node_coordinates, s.m.node_coords.data(), sizeof(double) * s.m.node_coords.size());
+}
+
+void orc_initial_condition(void* h, int ic, const double* params, double t, double* u) {
+  const Solver& s = *(Solver*)h;
+  const int D = s.eq.D;
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < s.m.nelem; ++e)
+    for (int node = 0; node < s.nn; ++node)
+      initial_condition(s.eq, ic, params, &s.m.node_coords[((size_t)e * s.nn + node) * D], t,
+                        &u[uidx(s, e, node, 0)]);
+}
+
+void orc_rhs(void* h, double* du, const double* u, double t) { rhs(*(Solver*)h, du, u, t); }
+
+void orc_alpha(void* h, const double* u, double* alpha) {
+  Solver& s = *(Solver*)h;
+  calc_alpha(s, u);
+  std::memcpy(alpha, s.alpha.data(), sizeof(double) * s.m.nelem);
+}
+
+double orc_max_dt(void* h, const double* u) { return max_dt(*(Solver*)h, u); }
+
+// One 2N stage: du = rhs(u, t_stage); u_tmp = du - a u_tmp; u += b dt u_tmp
+void orc_rk_stage(void* h, double* u, double* u_tmp, double* du, int stage, double t,
+                  double dt) {
+  Solver& s = *(Solver*)h;
+  rhs(s, du, u, t + dt * CK_C[stage]);
+  rk_update(s.ndofs() * s.eq.NV, u, u_tmp, du, CK_A[stage], CK_B[stage] * dt);
+}
+
+// Trixi's SimpleIntegrator2N driven by a StepsizeCallback(cfl), methods_2N.jl:113-168,
+// time_integration.jl:46-55, stepsize.jl:93-126.  Returns 0 on success, -1 on NaN dt.
+int orc_solve(void* h, double* u, double t0, double t_end, double cfl, int64_t max_steps,
+              double* t_out, int64_t* nsteps_out) {
+  Solver& s = *(Solver*)h;
+  const int64_t ndof = s.ndofs() * s.eq.NV;
+  std::vector<double> du(ndof), u_tmp(ndof);
+  double t = t0;
+  double dt = cfl * max_dt(s, u);
+  int64_t iter = 0;
+  bool finalstep = false;
+  while (!finalstep && iter < max_steps) {
+    if (std::isnan(dt)) {
+      *t_out = t;
+      *nsteps_out = iter;
+      return -1;
+    }
+    if (t + dt > t_end || isapprox(t + dt, t_end)) {
+      dt = t_end - t;
+      finalstep = true;
+    }
+    std::fill(u_tmp.begin(), u_tmp.end(), 0.0);
+    for (int stage = 0; stage < 5; ++stage) {
+      rhs(s, du.data(), u, t + dt * CK_C[stage]);
+      rk_update(ndof, u, u_tmp.data(), du.data(), CK_A[stage], CK_B[stage] * dt);
+    }
+    iter += 1;
+    t += dt;
+    dt = cfl * max_dt(s, u);
+  }
+  *t_out = t;
+  *nsteps_out = iter;
+  return 0;
+}
+
+// calc_error_norms, analysis_dg2d.jl:95-139 (cons2cons errors against the
+// initial condition evaluated at time t)
+void orc_error_norms(void* h, const double* u, double t, int ic, const double* params,
+                     double* l2, double* linf) {
+  const Solver& s = *(Solver*)h;
+  const int n = s.b.n, na = s.b.na, D = s.eq.D, NV = s.eq.NV;
+  int nna = 1;
+  for (int d = 0; d < D; ++d) nna *= na;
+  double L2[5] = {0, 0, 0, 0, 0}, LI[5] = {0, 0, 0, 0, 0};
+  std::vector<double> ua((size_t)nna * NV), xa((size_t)nna * D), tmp1, tmp2;
+  for (int64_t e = 0; e < s.m.nelem; ++e) {
+    // multiply_dimensionwise! applied to u and to the node coordinates
+    auto interp = [&](const double* in, int nv, double* out) {
+      // in: [nv, n^D] -> out [nv, na^D], x then y then z
+      std::vector<double> cur(in, in + (size_t)nv * s.nn), nxt;
+      int dims_in[3] = {n, n, n};
+      for (int d = 0; d < D; ++d) {
+        int shape_out[3] = {dims_in[0], dims_in[1], dims_in[2]};
+        shape_out[d] = na;
+        int tot = 1;
+        for (int q = 0; q < D; ++q) tot *= shape_out[q];
+        nxt.assign((size_t)tot * nv, 0.0);
+        for (int o = 0; o < tot; ++o) {
+          int ii[3] = {o % shape_out[0], (o / shape_out[0]) % shape_out[1],
+                       o / (shape_out[0] * shape_out[1])};
+          for (int v = 0; v < nv; ++v) {
+            double r = 0;
+            for (int k = 0; k < n; ++k) {
+              int src[3] = {ii[0], ii[1], ii[2]};
+              src[d] = k;
+              const int si = src[0] + dims_in[0] * (src[1] + dims_in[1] * src[2]);
+              r += s.b.avand[ii[d] * n + k] * cur[(size_t)si * nv + v];
+            }
+            nxt[(size_t)o * nv + v] = r;
+          }
+        }
+        dims_in[d] = na;
+        cur.swap(nxt);
+      }
+      std::memcpy(out, cur.data(), sizeof(double) * cur.size());
+    };
+    interp(&u[uidx(s, e, 0, 0)], NV, ua.data());
+    interp(&s.m.node_coords[(size_t)e * s.nn * D], D, xa.data());
+    double vj = 1.0 / s.m.inverse_jacobian[e];
+    vj = D == 2 ? vj * vj : vj * vj * vj;
+    double loc[5] = {0, 0, 0, 0, 0};
+    for (int node = 0; node < nna; ++node) {
+      int idx[3] = {node % na, (node / na) % na, node / (na * na)};
+      double w = s.b.aweights[idx[0]] * s.b.aweights[idx[1]];
+      if (D == 3) w *= s.b.aweights[idx[2]];
+      double ue[5];
+      initial_condition(s.eq, ic, params, &xa[(size_t)node * D], t, ue);
+      for (int v = 0; v < NV; ++v) {
+        const double diff = ue[v] - ua[(size_t)node * NV + v];
+        loc[v] += diff * diff * (w * vj);
+        LI[v] = std::max(LI[v], std::fabs(diff));
+      }
+    }
+    for (int v = 0; v < NV; ++v) L2[v] += loc[v];
+  }
+  double vol = s.m.length0;
+  vol = D == 2 ? vol * vol : vol * vol * vol;
+  for (int v = 0; v < NV; ++v) {
+    l2[v] = std::sqrt(L2[v] / vol);
+    linf[v] = LI[v];
+  }
+}
+
+// integrate_via_indices(u -> u[v]), analysis_dg2d.jl:313-336, without
+// normalisation: the domain totals of the conserved variables, plus the total
+// mathematical entropy (compressible_euler_2d.jl:2236-2255) and kinetic energy.
+void orc_integrals(void* h, const double* u, double* out) {
+  const Solver& s = *(Solver*)h;
+  const int n = s.b.n, D = s.eq.D, NV = s.eq.NV;
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int64_t e = 0; e < s.m.nelem; ++e) {
+    double vj = 1.0 / s.m.inverse_jacobian[e];
+    vj = D == 2 ? vj * vj : vj * vj * vj;
+    for (int node = 0; node < s.nn; ++node) {
+      int idx[3] = {node % n, (node / n) % n, node / (n * n)};
+      double w = s.b.weights[idx[0]] * s.b.weights[idx[1]];
+      if (D == 3) w *= s.b.weights[idx[2]];
+      const double* un = &u[uidx(s, e, node, 0)];
+      for (int v = 0; v < NV; ++v) acc[v] += vj * w * un[v];
+      double m2 = 0;
+      for (int d = 0; d < D; ++d) m2 += un[1 + d] * un[1 + d];
+      const double p = (s.eq.gamma - 1) * (un[NV - 1] - 0.5 * m2 / un[0]);
+      const double sth = std::log(p) - s.eq.gamma * std::log(un[0]);
+      acc[5] += vj * w * (-sth * un[0] * s.eq.inv_gamma_minus_one);
+      acc[6] += vj * w * (m2 / (2 * un[0]));
+    }
+  }
+  for (int v = 0; v < NV; ++v) out[v] = acc[v];
+  out[NV] = acc[5];
+  out[NV + 1] = acc[6];
+}
+
+}  // extern "C"

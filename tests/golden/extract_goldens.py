@@ -1,0 +1,131 @@
+"""Extract the L2/Linf goldens of Trixi.jl's TreeMesh Euler regression tests.
+
+Run once in a checkout that has the Trixi.jl sources (read as text, nothing is
+executed):
+
+    python tests/golden/extract_goldens.py /path/to/Trixi.jl
+
+It writes ``tests/golden/trixi_goldens.json``: for each selected ``@testitem``
+the golden ``l2``/``linf`` vectors and the overridden keyword arguments, next
+to the elixir settings (transcribed from the elixir files named in each entry)
+that the oracle needs to reproduce the run.
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import sys
+
+# Elixir settings transcribed from examples/tree_{2,3}d_dgsem/*.jl.
+# vi: weak | fluxdiff | hg ; fluxes: central | ranocha | shima_etal | llf | llf_naive
+CASES = {
+    "TreeMesh2D Euler: elixir_euler_source_terms.jl": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_source_terms.jl",
+        ndims=2, polydeg=3, level=4, xmin=[0.0, 0.0], xmax=[2.0, 2.0],
+        ic="convergence_test", source="convergence_test", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=1.0, tspan=[0.0, 2.0]),
+    "TreeMesh2D Euler: elixir_euler_ec.jl": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_ec.jl",
+        ndims=2, polydeg=3, level=5, xmin=[-2.0, -2.0], xmax=[2.0, 2.0],
+        ic="weak_blast_wave", source="none", vi="fluxdiff",
+        volume_flux="ranocha", surface_flux="ranocha", cfl=1.0, tspan=[0.0, 0.4]),
+    "TreeMesh2D Euler: elixir_euler_shockcapturing.jl": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_shockcapturing.jl",
+        ndims=2, polydeg=3, level=5, xmin=[-2.0, -2.0], xmax=[2.0, 2.0],
+        ic="weak_blast_wave", source="none", vi="hg", volume_flux="shima_etal",
+        surface_flux="llf_naive", alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
+        cfl=1.0, tspan=[0.0, 1.0]),
+    "TreeMesh2D Euler: elixir_euler_kelvin_helmholtz_instability.jl": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_kelvin_helmholtz_instability.jl",
+        ndims=2, polydeg=3, level=5, xmin=[-1.0, -1.0], xmax=[1.0, 1.0],
+        ic="kelvin_helmholtz", source="none", vi="hg", volume_flux="ranocha",
+        surface_flux="llf_naive", alpha_max=0.002, alpha_min=0.0001, alpha_smooth=True,
+        cfl=1.3, tspan=[0.0, 3.0]),
+    "TreeMesh2D Euler: elixir_euler_vortex.jl": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_vortex.jl",
+        ndims=2, polydeg=3, level=4, xmin=[-10.0, -10.0], xmax=[10.0, 10.0],
+        ic="isentropic_vortex", ic_params=[25.0, 5.0], source="none", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=1.1, tspan=[0.0, 20.0]),
+    "TreeMesh2D Euler: elixir_euler_vortex.jl one step with initial_condition_constant": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_vortex.jl",
+        ndims=2, polydeg=3, level=4, xmin=[-10.0, -10.0], xmax=[10.0, 10.0],
+        ic="constant", source="none", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=1.1, tspan=[0.0, 20.0]),
+    "TreeMesh3D Euler: elixir_euler_source_terms.jl": dict(
+        file="test/test_tree_3d_euler.jl",
+        elixir="examples/tree_3d_dgsem/elixir_euler_source_terms.jl",
+        ndims=3, polydeg=3, level=2, xmin=[0.0] * 3, xmax=[2.0] * 3,
+        ic="convergence_test", source="convergence_test", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=0.6, tspan=[0.0, 5.0]),
+    "TreeMesh3D Euler: elixir_euler_source_terms.jl with split_form": dict(
+        file="test/test_tree_3d_euler.jl",
+        elixir="examples/tree_3d_dgsem/elixir_euler_source_terms.jl",
+        ndims=3, polydeg=3, level=2, xmin=[0.0] * 3, xmax=[2.0] * 3,
+        ic="convergence_test", source="convergence_test", vi="fluxdiff",
+        volume_flux="central", surface_flux="llf_naive", cfl=0.6, tspan=[0.0, 5.0]),
+    "TreeMesh3D Euler: elixir_euler_taylor_green_vortex.jl": dict(
+        file="test/test_tree_3d_euler.jl",
+        elixir="examples/tree_3d_dgsem/elixir_euler_taylor_green_vortex.jl",
+        ndims=3, polydeg=3, level=3, xmin=[-3.141592653589793] * 3,
+        xmax=[3.141592653589793] * 3, ic="taylor_green", ic_params=[0.1], source="none",
+        vi="fluxdiff", volume_flux="ranocha", surface_flux="llf_naive", cfl=1.4,
+        tspan=[0.0, 10.0]),
+    "TreeMesh3D Euler: elixir_euler_ec.jl": dict(
+        file="test/test_tree_3d_euler.jl",
+        elixir="examples/tree_3d_dgsem/elixir_euler_ec.jl",
+        ndims=3, polydeg=3, level=3, xmin=[-2.0] * 3, xmax=[2.0] * 3,
+        ic="weak_blast_wave", source="none", vi="fluxdiff", volume_flux="ranocha",
+        surface_flux="ranocha", cfl=1.3, tspan=[0.0, 0.4]),
+}
+
+_NUM = r"[-+]?\d+(?:\.\d*)?(?:[eE][-+]?\d+)?"
+
+
+def _testitem_body(text: str, name: str) -> tuple[str, int]:
+    key = '@testitem "' + name + '"'
+    start = text.find(key)
+    if start < 0:
+        raise KeyError(name)
+    end = text.find("@testitem", start + len(key))
+    line = text.count("\n", 0, start) + 1
+    return text[start:end if end > 0 else len(text)], line
+
+
+def _vector(body: str, key: str) -> list[float]:
+    m = re.search(key + r"\s*=\s*\[([^\]]*)\]", body)
+    if not m:
+        raise KeyError(key)
+    return [float(x) for x in re.findall(_NUM, m.group(1))]
+
+
+def main(root: str) -> None:
+    out = {}
+    for name, case in CASES.items():
+        text = open(os.path.join(root, case["file"]), encoding="utf-8").read()
+        body, line = _testitem_body(text, name)
+        entry = dict(case)
+        entry["source_line"] = f"{case['file']}:{line}"
+        entry["l2"] = _vector(body, "l2")
+        entry["linf"] = _vector(body, "linf")
+        m = re.search(r"tspan\s*=\s*\((" + _NUM + r"),\s*(" + _NUM + r")\)", body)
+        if m:
+            entry["tspan"] = [float(m.group(1)), float(m.group(2))]
+        m = re.search(r"maxiters\s*=\s*(\d+)", body)
+        if m:
+            entry["maxiters"] = int(m.group(1))
+        out[name] = entry
+    dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "trixi_goldens.json")
+    with open(dst, "w", encoding="utf-8") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+    print(f"wrote {len(out)} goldens to {dst}")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
