@@ -1,0 +1,350 @@
+#!/usr/bin/env python
+"""DOF-updates/s per RK stage of the DGSEM hot path on GB300.
+
+Workload: 3D compressible Euler manufactured solution on a periodic [0,2]^3
+TreeMesh with 32^3 elements (refinement level 5), polydeg 3 (2,097,152 DOFs
+per field), VolumeIntegralFluxDifferencing(flux_ranocha), flux_lax_friedrichs
+surface flux, source_terms_convergence_test, CarpenterKennedy2N54 with
+StepsizeCallback(cfl = 0.6, the elixir's value), t_end = 1.
+
+A "step" is one CK2N54 time step (5 fused RK stages, CUDA graph).  The
+headline `value` is the mixed path (FP32 bulk arithmetic, FP64 solution and
+stage accumulation); the FP64 path is measured the same way and reported
+beside it, together with both paths' L2 density errors at t_end against the
+exact solution.  `e2e` drives the same steps through the C ABI with the state
+uploaded from and downloaded to pinned host memory every step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+`--impl reference` times the oracle (the CPU restatement of Trixi's FP64
+rhs! + 2N54 step) on all host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "trixi.jl_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+LEVEL, POLYDEG, CFL, T_END = 5, 3, 0.6, 1.0
+WORKLOAD = "3D Euler MMS, periodic [0,2]^3 TreeMesh 32^3 elements, polydeg 3, " \
+           "FluxDifferencing(flux_ranocha), flux_lax_friedrichs, CK2N54 CFL 0.6"
+METRIC = "DOF-updates/s per RK stage"
+L2_BYTES = 126 * 2 ** 20
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "stage_kernel_3d_mms_32cubed_mixed.json")
+
+
+def make_semi(precision: str, epb: int = 0):
+    import trixi_gb300 as T
+    eq = T.CompressibleEulerEquations3D(1.4)
+    solver = T.DGSEM(polydeg=POLYDEG, surface_flux=T.flux_lax_friedrichs,
+                     volume_integral=T.VolumeIntegralFluxDifferencing(T.flux_ranocha))
+    mesh = T.TreeMesh((0.0,) * 3, (2.0,) * 3, initial_refinement_level=LEVEL)
+    return T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_convergence_test, solver,
+                                          source_terms=T.source_terms_convergence_test,
+                                          precision=precision, elements_per_block=epb)
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(gpu_index)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        self.lines = []
+        if self.proc:
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def gpu_arm(args, rank: int, world: int):
+    import torch
+
+    import trixi_gb300 as T
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    results = {}
+    semis = {}
+    for prec in ("mixed", "fp64"):
+        semi = make_semi(prec, args.epb)
+        semis[prec] = semi
+        ctx = semi.device_context
+        stream = torch.cuda.ExternalStream(ctx.stream())
+        u0 = semi.compute_coefficients(0.0)
+        ctx.upload(u0)
+        steps = args.steps if prec == "mixed" else max(3, min(args.steps, args.fp64_steps))
+        t, _n = ctx.step(args.warmup, CFL, math.inf, 0.0)
+        ctx.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        sampler = ClockSampler(dev) if (prec == "mixed" and rank == 0) else None
+        # K back-to-back step graphs; the state and stage buffers (2 x 84 MB FP64
+        # + u_tmp) are larger than L2, so every step streams them from HBM.
+        with torch.cuda.stream(stream):
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+        t, n = ctx.step(steps, CFL, math.inf, t)
+        with torch.cuda.stream(stream):
+            ev1.record(stream)
+        ev1.synchronize()
+        assert n == steps
+        times = [ev0.elapsed_time(ev1)]
+        ctx.synchronize()
+        clocks = sampler.stop() if sampler else None
+        if world > 1:
+            torch.distributed.barrier()
+        tot = sum(times)
+        if world > 1:
+            tt = torch.tensor([tot], dtype=torch.float64, device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            tot = float(tt.item())
+        ms_step = tot / steps
+        results[prec] = dict(ms_per_step=ms_step, steps=steps,
+                             value=world * semi.ndofs * 5 / (ms_step * 1e-3), clocks=clocks)
+        if ctx.status() != 0:
+            raise RuntimeError(f"{prec}: device status word flagged a non-physical state")
+
+    # ---- roofline of the stage kernel (mixed): events around single stages ----
+    semi = semis["mixed"]
+    ctx = semi.device_context
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    ctx.upload(semi.compute_coefficients(0.0))
+    dt = 0.6 * ctx.max_dt()
+    for s in range(5):
+        ctx.rk_stage(s, 0.0, dt)
+    st = []
+    for rep in range(max(10, args.steps)):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        ctx.rk_stage(rep % 5, 0.0, dt)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        st.append(e0.elapsed_time(e1))
+    stage_ms = statistics.mean(st)
+    alg_bytes = semi.ndofs * (2 * 8 + 2 * 4) * semi.equations.nvariables  # u r/w FP64, u_tmp r/w FP32
+    achieved = alg_bytes / (stage_ms * 1e-3) / 1e9
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    traffic = None
+    try:
+        with open(PROFILE_TRAFFIC) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+    except (OSError, ValueError):
+        pass
+
+    # ---- e2e through the C ABI with pinned host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        u_host = torch.from_numpy(semi.compute_coefficients(0.0).reshape(-1)).pin_memory()
+        out_host = torch.empty_like(u_host).pin_memory()
+        ctx.upload(u_host.data_ptr())
+        t = 0.0
+        et = []
+        for k in range(args.warmup + args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            ctx.upload(u_host.data_ptr())
+            t, _n = ctx.step(1, CFL, math.inf, t)
+            ctx.download(out_host.data_ptr())
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            e1.synchronize()
+            if k >= args.warmup:
+                et.append(e0.elapsed_time(e1))
+        ms = statistics.mean(et)
+        nbytes = semi.nvalues * 8
+        e2e = {"value": world * semi.ndofs * 5 / (ms * 1e-3), "unit": "DOF-updates/s",
+               "ms_per_step": ms, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
+
+    # ---- accuracy at t_end (untimed): L2 density error of both paths ----
+    acc = None
+    if not args.no_accuracy:
+        acc = {}
+        for prec, semi_p in semis.items():
+            c = semi_p.device_context
+            c.upload(semi_p.compute_coefficients(0.0))
+            tt, n = c.step(10 ** 7, CFL, T_END, 0.0)
+            l2, linf = T.calc_error_norms(c.download(), tt, semi_p)
+            acc[prec] = {"l2_rho": float(l2[0]), "linf_rho": float(linf[0]), "t": tt, "steps": n}
+    return results, dict(stage_ms=stage_ms, achieved=achieved, peak=peak, alg_bytes=alg_bytes,
+                         traffic=traffic, peak_src="measured" if "hbm_gbs" in peaks else "fallback"), \
+        e2e, acc, semis["mixed"]
+
+
+def cpu_oracle_rate(threads: int, nsteps: int, max_seconds: float):
+    """Oracle (CPU FP64 restatement of Trixi's rhs! + 2N54) DOF-updates/s per RK stage."""
+    from oracle import oracle as O
+    O.set_threads(threads)
+    orc = O.Oracle(3, POLYDEG, LEVEL, [0.0] * 3, [2.0] * 3, volume_integral=O.VI_FLUXDIFF,
+                   volume_flux=O.FLUX_RANOCHA, surface_flux=O.FLUX_LAX_FRIEDRICHS,
+                   source=O.SRC_CONVERGENCE_TEST)
+    u = orc.initial_condition(O.IC_CONVERGENCE_TEST, None, 0.0)
+    u_tmp = np.zeros_like(u)
+    dt = CFL * orc.max_dt(u)
+    done, t0 = 0, time.perf_counter()
+    while done < nsteps:
+        for s in range(5):
+            orc.rk_stage(u, u_tmp, s, 0.0, dt)
+        done += 1
+        if time.perf_counter() - t0 > max_seconds:
+            break
+    el = time.perf_counter() - t0
+    return orc.ndofs * 5 * done / el, done, el, orc.ndofs
+
+
+def reference_arm(args, rank: int, world: int):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    # warm-up: one stage
+    cpu_oracle_rate(threads, 1, 0.0) if args.warmup > 0 else None
+    budget = float(os.environ.get("TG_REFERENCE_SECONDS", "120"))
+    rate, done, el, ndofs = cpu_oracle_rate(threads, args.steps, budget)
+    line = {"metric": METRIC, "value": rate, "unit": "DOF-updates/s", "n_gpus": args.gpus,
+            "steps": done, "warmup": args.warmup, "ms_per_step": el / done * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (analytic manufactured solution)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "ndofs_per_field": ndofs, "precision": "fp64"},
+            "cpu_baseline": {"value": rate, "unit": "DOF-updates/s", "cores": threads,
+                             "kind": "port",
+                             "sample": f"{done} CK2N54 steps of the full 32^3 mesh "
+                                       f"(C++ restatement of Trixi's CPU rhs!, not Trixi)"},
+            "e2e": {"value": rate, "unit": "DOF-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--epb", type=int, default=0, help="elements per block (0: library default)")
+    ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group(
+            "nccl" if args.impl == "gb300" else "gloo")
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    results, roof, e2e, acc, semi = gpu_arm(args, rank, world)
+    if rank != 0:
+        return
+    mixed, fp64 = results["mixed"], results["fp64"]
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, done, el, _ = cpu_oracle_rate(threads, 2, 20.0)
+        cpu = {"value": rate, "unit": "DOF-updates/s", "cores": threads, "kind": "port",
+               "sample": f"{done} CK2N54 steps of the full 32^3 mesh, FP64, {threads} threads "
+                         f"(C++ restatement of Trixi's CPU rhs!, not Trixi)"}
+    line = {
+        "metric": METRIC, "value": mixed["value"], "unit": "DOF-updates/s", "n_gpus": world,
+        "steps": mixed["steps"], "warmup": args.warmup, "ms_per_step": mixed["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (analytic manufactured solution)",
+        "config": {"workload": WORKLOAD, "ndofs_per_field": semi.ndofs, "precision": "mixed",
+                   "elements_per_block": semi.device_context.elements_per_block(),
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2_policy": "inputs larger than L2: per step 2 x 84 MB FP64 state + 42 MB "
+                                "FP32 u_tmp vs 126 MB L2; stage-kernel roofline timed after a "
+                                "256 MB L2 flush"},
+        "fp64": {"value": fp64["value"], "ms_per_step": fp64["ms_per_step"],
+                 "steps": fp64["steps"], "dtype": "f64"},
+        "mixed_over_fp64": mixed["value"] / fp64["value"],
+        "accuracy": acc,
+        "roofline": {"bound": "hbm", "achieved": roof["achieved"], "peak": roof["peak"],
+                     "unit": "GB/s", "frac": roof["achieved"] / roof["peak"],
+                     "traffic": roof["traffic"], "kernel": "dg_element_kernel<3,4,float,FD>",
+                     "stage_ms": roof["stage_ms"], "algorithmic_bytes": roof["alg_bytes"],
+                     "peak_source": roof["peak_src"]},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": mixed["clocks"],
+        "gpu_launches": 7 * mixed["steps"],
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,212 @@
+/*
+ * trixi_gb300.h -- C ABI of the GB300 (sm_103a) DGSEM hot path.
+ *
+ * Drop-in device backend for Trixi.jl's TreeMesh DGSEM semidiscretization of
+ * the compressible Euler equations (2D/3D, periodic, conforming meshes).  The
+ * entry points replace, one for one, the pieces of the reference that a Julia
+ * `ccall` shim hands to the device (paths relative to the Trixi.jl sources):
+ *
+ *   rhs_hyperbolic!(du_ode, u_ode, semi, t)
+ *       src/semidiscretization/semidiscretization_hyperbolic.jl:578-597
+ *       -> dispatch rhs_hyperbolic!(backend, du, u, t, mesh::TreeMesh, ...)
+ *          src/solvers/dgsem_tree/dg_2d.jl:113-186 (3D shares it, dg_2d.jl:117)
+ *   the 2N low-storage Runge-Kutta stage and step
+ *       src/time_integration/methods_2N.jl:131-168, time_integration.jl:46-55
+ *   max_dt / StepsizeCallback
+ *       src/callbacks_step/stepsize_dg2d.jl:8-30, stepsize_dg3d.jl:8-33,
+ *       src/callbacks_step/stepsize.jl:93-126
+ *   integrate_via_indices (conserved totals, entropy, kinetic energy)
+ *       src/callbacks_step/analysis_dg2d.jl:313-336
+ *   IndicatorHennemannGassner blending factors
+ *       src/solvers/dgsem/indicators.jl:114-148,
+ *       src/solvers/dgsem_tree/indicators_2d.jl:30-136, indicators_3d.jl:39-176
+ *
+ * Conventions
+ *   - Every function returns an int status (TG_OK = 0, negative on error).  No
+ *     exception, abort or device trap crosses the ABI; tg_last_error() gives
+ *     the message of the last failure.
+ *   - State arrays use Trixi's own layout u[v, i, j, (k), element]
+ *     (column-major, variables fastest), FP64, ndofs * nvariables values.
+ *   - The library owns the device memory of a context.  Host pointers are
+ *     borrowed for the duration of a call; device pointers handed out stay
+ *     valid until tg_ctx_destroy (the state pointer until the next tg_step or
+ *     tg_rk_stage, see tg_state_device_ptr).
+ *   - Calls are ordered on the context's CUDA stream.  One context per host
+ *     thread; distinct contexts are independent.
+ */
+#ifndef TRIXI_GB300_H
+#define TRIXI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TG_API_VERSION 1
+
+typedef enum tg_status_code {
+  TG_OK = 0,
+  TG_ERR_INVALID_ARGUMENT = -1,
+  TG_ERR_UNSUPPORTED = -2,   /* mesh/solver option outside the GPU path */
+  TG_ERR_CUDA = -3,          /* a CUDA runtime call failed */
+  TG_ERR_NUMERICAL = -4,     /* NaN time step or non-physical state detected */
+  TG_ERR_STATE = -5          /* call order violated (e.g. no state uploaded) */
+} tg_status_code;
+
+/* VolumeIntegralWeakForm / VolumeIntegralFluxDifferencing /
+ * VolumeIntegralShockCapturingHG, src/solvers/dg.jl:105, 135-141, 208-221 */
+typedef enum tg_volume_integral {
+  TG_VOLUME_WEAK_FORM = 0,
+  TG_VOLUME_FLUX_DIFFERENCING = 1,
+  TG_VOLUME_SHOCK_CAPTURING_HG = 2
+} tg_volume_integral;
+
+/* two-point fluxes: flux_central (numerical_fluxes.jl:17-25), flux_ranocha
+ * (compressible_euler_2d.jl:686-722), flux_shima_etal (:466-495),
+ * FluxLaxFriedrichs(max_abs_speed) = flux_lax_friedrichs and
+ * FluxLaxFriedrichs(max_abs_speed_naive) (numerical_fluxes.jl:222-253) */
+typedef enum tg_flux {
+  TG_FLUX_CENTRAL = 0,
+  TG_FLUX_RANOCHA = 1,
+  TG_FLUX_SHIMA_ETAL = 2,
+  TG_FLUX_LAX_FRIEDRICHS = 3,
+  TG_FLUX_LAX_FRIEDRICHS_NAIVE = 4
+} tg_flux;
+
+/* source_terms_convergence_test, compressible_euler_2d.jl:116-145, 3d.jl:127-150 */
+typedef enum tg_source {
+  TG_SOURCE_NONE = 0,
+  TG_SOURCE_CONVERGENCE_TEST = 1
+} tg_source;
+
+/* TG_PRECISION_FP64: every operation in FP64 (the reference's Float64 run).
+ * TG_PRECISION_MIXED: fluxes, volume/surface integrals and the 2N register
+ * u_tmp in FP32; the solution u and its stage accumulation, the time, the
+ * step size and all integrals stay FP64. */
+typedef enum tg_precision {
+  TG_PRECISION_FP64 = 0,
+  TG_PRECISION_MIXED = 1
+} tg_precision;
+
+typedef struct tg_config {
+  int32_t ndims;            /* 2 or 3 */
+  int32_t polydeg;          /* 1..7 (LobattoLegendreBasis) */
+  int64_t nelements;        /* nelements(dg, cache) */
+  int64_t ninterfaces;      /* ninterfaces(dg, cache) */
+  double gamma;             /* CompressibleEulerEquations{2,3}D(gamma) */
+  int32_t volume_integral;  /* tg_volume_integral */
+  int32_t volume_flux;      /* tg_flux: volume_flux / volume_flux_dg */
+  int32_t surface_flux;     /* tg_flux */
+  int32_t volume_flux_fv;   /* tg_flux: HG low-order flux (LLF variants) */
+  double alpha_max;         /* IndicatorHennemannGassner(alpha_max, alpha_min, */
+  double alpha_min;         /*   alpha_smooth, variable = density_pressure)     */
+  int32_t alpha_smooth;
+  int32_t source_terms;     /* tg_source */
+  int32_t precision;        /* tg_precision */
+  int32_t device;           /* CUDA device ordinal */
+  /* dg.basis (LobattoLegendreBasis): vectors of length n = polydeg + 1 and
+   * n x n matrices in Julia's column-major order */
+  const double* nodes;
+  const double* weights;
+  const double* inverse_weights;
+  const double* derivative_hat;
+  const double* derivative_split;
+  const double* inverse_vandermonde_legendre;
+  /* cache.interfaces / cache.elements (containers_{2,3}d.jl) */
+  const int64_t* neighbor_ids;     /* [2, ninterfaces], 1-based element ids */
+  const int64_t* orientations;     /* [ninterfaces], 1..ndims */
+  const double* inverse_jacobian;  /* [nelements] */
+  const double* node_coordinates;  /* [ndims, n^ndims, nelements]; may be NULL
+                                      when source_terms == TG_SOURCE_NONE */
+  int32_t elements_per_block;      /* 0 = library default */
+} tg_config;
+
+typedef struct tg_ctx tg_ctx;
+
+int tg_api_version(void);
+
+/* Builds a device context for one semidiscretization.  Replaces the device
+ * side of create_cache (src/solvers/dgsem_tree/dg_2d.jl:14-37): copies the
+ * basis and connectivity to HBM and allocates state/stage buffers. */
+int tg_ctx_create(const tg_config* cfg, tg_ctx** out);
+int tg_ctx_destroy(tg_ctx* ctx);
+
+/* Message of the last failed call on ctx (ctx == NULL: last failed
+ * tg_ctx_create of this thread).  Always NUL-terminates when len > 0. */
+int tg_last_error(const tg_ctx* ctx, char* buf, size_t len);
+
+/* ndofs(mesh, dg, cache) (dg.jl:969-971) and ndofs * nvariables. */
+int tg_ndofs(const tg_ctx* ctx, int64_t* ndofs, int64_t* nvalues);
+
+/* Host <-> device copies of the solution (compute_coefficients! output,
+ * dg.jl:1280-1325, in Trixi's layout).  Download synchronises. */
+int tg_upload_state(tg_ctx* ctx, const double* u_host);
+int tg_download_state(tg_ctx* ctx, double* u_host);
+
+/* Device pointer of the current solution buffer.  The solution ping-pongs
+ * between two buffers during tg_rk_stage/tg_step: query again after them. */
+int tg_state_device_ptr(tg_ctx* ctx, double** u_dev);
+
+/* rhs_hyperbolic!(du, u, t): du and u are DEVICE pointers in Trixi's layout
+ * (for instance the context state, or buffers of the caller's own).  du must
+ * not alias u.  Asynchronous on the context stream. */
+int tg_rhs(tg_ctx* ctx, double* du_dev, const double* u_dev, double t);
+
+/* Same with HOST buffers: uploads u, evaluates, downloads du (synchronous). */
+int tg_rhs_host(tg_ctx* ctx, double* du_host, const double* u_host, double t);
+
+/* max_dt(u, t, mesh, constant_speed = False, equations, dg, cache) without
+ * the CFL factor; u_dev == NULL uses the context state.  Synchronous. */
+int tg_max_dt(tg_ctx* ctx, const double* u_dev, double* dt);
+
+/* One fused stage of CarpenterKennedy2N54 on the context state at time t
+ * with step dt (methods_2N.jl:146-158): du = rhs(u, t + c_s dt);
+ * u_tmp = du - a_s u_tmp; u = u + b_s dt u_tmp.  stage = 0..4; stage 0
+ * zeroes u_tmp first.  du never leaves the chip.  Asynchronous. */
+int tg_rk_stage(tg_ctx* ctx, int32_t stage, double t, double dt);
+
+/* Time stepping with Trixi's SimpleIntegrator2N + StepsizeCallback(cfl)
+ * semantics: dt = cfl * max_dt(u) after every step (and before the first
+ * one), clamped to reach t_end exactly (limit_dt!).  Steps are CUDA-graph
+ * launches with t, dt and the CFL reduction kept on the device; the host
+ * only polls for the end.  *t_inout is the start time on entry (used on the
+ * first call after an upload or tg_set_time) and the reached time on exit.
+ * Stops after max_steps steps or at t_end.  Returns TG_ERR_NUMERICAL if dt
+ * became NaN. */
+int tg_step(tg_ctx* ctx, int64_t max_steps, double cfl, double t_end, double* t_inout,
+            int64_t* steps_taken);
+
+/* Resets the device clock to t (next tg_step recomputes dt). */
+int tg_set_time(tg_ctx* ctx, double t);
+
+/* FP64 domain integrals of the context state (integrate_via_indices without
+ * normalisation): out[0..nvar-1] = totals of the conserved variables,
+ * out[nvar] = total mathematical entropy, out[nvar+1] = kinetic energy. */
+int tg_integrals(tg_ctx* ctx, double* out);
+
+/* Blending factors of IndicatorHennemannGassner (after smoothing) for u_dev
+ * (NULL: the context state), written to alpha_host[nelements].  Synchronous.
+ * Only for TG_VOLUME_SHOCK_CAPTURING_HG contexts. */
+int tg_alpha(tg_ctx* ctx, const double* u_dev, double* alpha_host);
+
+/* Sticky device status word (bit 0: NaN in the state, bit 1: non-positive
+ * density or pressure seen by the CFL reduction).  Reading clears it. */
+int tg_status(tg_ctx* ctx, int32_t* flags);
+
+int tg_synchronize(tg_ctx* ctx);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or timing events with the library's launches. */
+int tg_stream(tg_ctx* ctx, void** stream);
+
+/* Elements per CUDA block in use (set by tg_config.elements_per_block or the
+ * library default for the (ndims, polydeg, precision) combination). */
+int tg_elements_per_block(const tg_ctx* ctx, int32_t* epb);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TRIXI_GB300_H */

@@ -1,0 +1,218 @@
+"""GPU (sm_103a) parity of the fused DGSEM kernels against the oracle.
+
+FP64 path: rhs!, the HG blending factors, the CFL step and whole time
+integrations must match the oracle's restatement of Trixi to 1e-12 relative
+(normwise per variable); conservation and free-stream preservation hold to
+round-off.  Mixed path: FP32 bulk arithmetic, FP64 accumulation; its error
+against the exact solution must stay within 1.1x of the FP64 path's error.
+Every call goes through the C ABI (libtrixi_gb300.so).
+"""
+import numpy as np
+import pytest
+
+from _cases import load_goldens
+from _gpu_cases import build, perturbed_state, rel_err
+import trixi_gb300 as T
+
+pytestmark = pytest.mark.gpu
+
+RHS_CASES = [
+    dict(ndims=2, polydeg=3, level=3, xmin=[0, 0], xmax=[2, 2], vi="weak", surface_flux="llf",
+         ic="convergence_test", source="convergence_test"),
+    dict(ndims=2, polydeg=3, level=3, xmin=[-1, -1], xmax=[1, 1], vi="fluxdiff",
+         volume_flux="ranocha", surface_flux="llf_naive", ic="kelvin_helmholtz"),
+    dict(ndims=2, polydeg=2, level=3, xmin=[-10, -10], xmax=[10, 10], vi="weak",
+         surface_flux="llf_naive", ic="isentropic_vortex", ic_params=[1.0, 5.0]),
+    dict(ndims=2, polydeg=4, level=2, xmin=[-2, -2], xmax=[2, 2], vi="fluxdiff",
+         volume_flux="shima_etal", surface_flux="ranocha", ic="weak_blast_wave"),
+    dict(ndims=2, polydeg=3, level=4, xmin=[-1, -1], xmax=[1, 1], vi="hg", volume_flux="ranocha",
+         surface_flux="llf", ic="kelvin_helmholtz", alpha_max=0.002, alpha_min=0.0001),
+    dict(ndims=2, polydeg=3, level=4, xmin=[-2, -2], xmax=[2, 2], vi="hg",
+         volume_flux="shima_etal", surface_flux="llf_naive", ic="weak_blast_wave"),
+    dict(ndims=3, polydeg=3, level=2, xmin=[0] * 3, xmax=[2] * 3, vi="fluxdiff",
+         volume_flux="ranocha", surface_flux="llf", ic="convergence_test", source="convergence_test"),
+    dict(ndims=3, polydeg=3, level=2, xmin=[0] * 3, xmax=[2] * 3, vi="weak", surface_flux="llf_naive",
+         ic="convergence_test", source="convergence_test"),
+    dict(ndims=3, polydeg=2, level=2, xmin=[-3.14159] * 3, xmax=[3.14159] * 3, vi="fluxdiff",
+         volume_flux="ranocha", surface_flux="llf_naive", ic="taylor_green"),
+    dict(ndims=3, polydeg=4, level=1, xmin=[-2] * 3, xmax=[2] * 3, vi="fluxdiff",
+         volume_flux="central", surface_flux="ranocha", ic="weak_blast_wave"),
+    dict(ndims=3, polydeg=3, level=2, xmin=[-2] * 3, xmax=[2] * 3, vi="hg", volume_flux="ranocha",
+         surface_flux="llf_naive", ic="weak_blast_wave"),
+]
+
+
+def _id(c):
+    return f"{c['ndims']}d-p{c['polydeg']}-{c['vi']}-{c.get('volume_flux', '')}-{c['surface_flux']}-{c['ic']}"
+
+
+@pytest.mark.parametrize("c", RHS_CASES, ids=[_id(c) for c in RHS_CASES])
+def test_rhs_fp64_matches_oracle(c):
+    semi, orc = build(c)
+    u = perturbed_state(semi, seed=3)
+    du_gpu = semi.device_context.rhs_host(u, 0.37)
+    du_orc = orc.rhs(u, 0.37)
+    assert rel_err(du_gpu, du_orc) < 1e-12
+
+
+@pytest.mark.parametrize("c", [c for c in RHS_CASES if c["vi"] == "hg"], ids=lambda c: _id(c))
+def test_hg_alpha_fp64_matches_oracle(c):
+    semi, orc = build(c)
+    u = perturbed_state(semi, seed=5, amp=0.05)
+    ctx = semi.device_context
+    ctx.upload(u)
+    a_gpu = ctx.alpha()
+    a_orc = orc.alpha(u)
+    assert np.max(np.abs(a_gpu - a_orc)) < 1e-12
+    assert np.any(a_orc > 0)  # the case exercises the blending
+
+
+@pytest.mark.parametrize("c", RHS_CASES[:7], ids=lambda c: _id(c))
+def test_rhs_mixed_close_to_oracle(c):
+    semi, orc = build(c, precision="mixed")
+    u = perturbed_state(semi, seed=3)
+    du_gpu = semi.device_context.rhs_host(u, 0.37)
+    du_orc = orc.rhs(u, 0.37)
+    assert rel_err(du_gpu, du_orc) < 2e-4
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("c", [RHS_CASES[1], RHS_CASES[4], RHS_CASES[8]], ids=lambda c: _id(c))
+def test_conservation_to_roundoff(c, precision):
+    # sum over the domain of w J du vanishes for periodic meshes without sources
+    semi, _ = build(c, precision=precision)
+    u = perturbed_state(semi, seed=7)
+    du = semi.device_context.rhs_host(u, 0.0)
+    b = semi.solver.basis
+    D = semi.equations.ndims
+    W = np.einsum("j,i->ji", b.weights, b.weights) if D == 2 else \
+        np.einsum("k,j,i->kji", b.weights, b.weights, b.weights)
+    J = (1.0 / semi.inverse_jacobian) ** D
+    tot = np.einsum("e...v,...,e->v", du, W, J)
+    scale = np.einsum("e...v,...,e->v", np.abs(du), W, J)
+    tol = 1e-13 if precision == "fp64" else 1e-6
+    assert np.all(np.abs(tot) <= tol * scale)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("ndims,vi", [(2, "weak"), (2, "fluxdiff"), (3, "fluxdiff"), (2, "hg")])
+def test_free_stream_preservation(ndims, vi, precision):
+    c = dict(ndims=ndims, polydeg=3, level=2, xmin=[-1] * ndims, xmax=[1] * ndims, vi=vi,
+             volume_flux="ranocha", surface_flux="llf", ic="constant")
+    semi, _ = build(c, precision=precision)
+    u = semi.compute_coefficients(0.0)
+    du = semi.device_context.rhs_host(u, 0.0)
+    assert np.max(np.abs(du)) < (1e-12 if precision == "fp64" else 1e-4)
+
+
+def test_rhs_is_deterministic():
+    semi, _ = build(RHS_CASES[6])
+    u = perturbed_state(semi)
+    a = semi.device_context.rhs_host(u, 0.1)
+    b = semi.device_context.rhs_host(u, 0.1)
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("c", [RHS_CASES[0], RHS_CASES[4], RHS_CASES[6]], ids=lambda c: _id(c))
+def test_max_dt_and_integrals_match_oracle(c):
+    semi, orc = build(c)
+    u = perturbed_state(semi, seed=11)
+    ctx = semi.device_context
+    ctx.upload(u)
+    assert ctx.max_dt() == pytest.approx(orc.max_dt(u), rel=1e-14)
+    np.testing.assert_allclose(ctx.integrals(), orc.integrals(u), rtol=1e-12)
+
+
+@pytest.mark.parametrize("c", [RHS_CASES[0], RHS_CASES[4], RHS_CASES[6], RHS_CASES[10]],
+                         ids=lambda c: _id(c))
+def test_time_steps_fp64_match_oracle(c):
+    semi, orc = build(c)
+    u0 = perturbed_state(semi, seed=13, amp=1e-3)
+    ctx = semi.device_context
+    ctx.upload(u0)
+    t, n = ctx.step(6, 0.9, 10.0, 0.0)
+    u_gpu = ctx.download()
+    u_orc, t_orc, n_orc = orc.solve(u0, 0.0, 10.0, 0.9, max_steps=6)
+    assert n == n_orc == 6
+    assert t == pytest.approx(t_orc, rel=1e-13)
+    assert rel_err(u_gpu, u_orc) < 1e-12
+
+
+def test_rk_stage_matches_oracle():
+    c = RHS_CASES[6]
+    semi, orc = build(c)
+    u = perturbed_state(semi, seed=17)
+    ctx = semi.device_context
+    ctx.upload(u)
+    u_o = u.copy()
+    ut_o = np.zeros_like(u)
+    for s in range(5):
+        ctx.rk_stage(s, 0.2, 1e-3)
+        orc.rk_stage(u_o, ut_o, s, 0.2, 1e-3)
+    assert rel_err(ctx.download(), u_o) < 1e-13
+
+
+GOLDENS = load_goldens()
+GOLDEN_NAMES = sorted(k for k in GOLDENS if "maxiters" not in GOLDENS[k])
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_gpu_fp64_reproduces_trixi_goldens(name):
+    c = dict(GOLDENS[name])
+    semi, _ = build(c)
+    ode = T.semidiscretize(semi, c["tspan"])
+    ana = T.AnalysisCallback(semi)
+    sol = T.solve(ode, T.CarpenterKennedy2N54(williamson_condition=False), dt=1.0,
+                  callback=T.CallbackSet(T.StepsizeCallback(cfl=c["cfl"]), ana))
+    assert sol.t[-1] == pytest.approx(c["tspan"][1], rel=1e-14)
+    np.testing.assert_allclose(ana.l2, c["l2"], rtol=1e-8)
+    np.testing.assert_allclose(ana.linf, c["linf"], rtol=1e-7)
+
+
+def test_gpu_free_stream_golden_one_step():
+    name = "TreeMesh2D Euler: elixir_euler_vortex.jl one step with initial_condition_constant"
+    c = dict(GOLDENS[name])
+    semi, _ = build(c)
+    ode = T.semidiscretize(semi, c["tspan"])
+    ana = T.AnalysisCallback(semi)
+    T.solve(ode, T.CarpenterKennedy2N54(), dt=1.0, maxiters=1,
+            callback=T.CallbackSet(T.StepsizeCallback(cfl=c["cfl"]), ana))
+    assert np.all(ana.l2 < 1e-14) and np.all(ana.linf < 1e-13)
+
+
+@pytest.mark.parametrize("name", ["TreeMesh3D Euler: elixir_euler_source_terms.jl",
+                                  "TreeMesh2D Euler: elixir_euler_source_terms.jl"])
+def test_mixed_precision_error_within_1p1x_of_fp64(name):
+    c = dict(GOLDENS[name])
+    errs = {}
+    for prec in ("fp64", "mixed"):
+        semi, _ = build(c, precision=prec)
+        ana = T.AnalysisCallback(semi)
+        T.solve(T.semidiscretize(semi, c["tspan"]), T.CarpenterKennedy2N54(), dt=1.0,
+                callback=T.CallbackSet(T.StepsizeCallback(cfl=c["cfl"]), ana))
+        errs[prec] = ana.l2
+    assert errs["mixed"][0] <= 1.1 * errs["fp64"][0]
+
+
+def test_status_flags_nonphysical_state():
+    # failure detection: a negative density planted in the host input is
+    # reported through the status word after one step, without faulting
+    semi, _ = build(RHS_CASES[0])
+    u = semi.compute_coefficients(0.0)
+    u[3, 1, 1, 0] = -1.0
+    ctx = semi.device_context
+    ctx.upload(u)
+    ctx.step(1, 0.5, 10.0, 0.0)
+    assert ctx.status() != 0
+    assert ctx.status() == 0  # reading clears it
+
+
+def test_rhs_with_device_pointers():
+    torch = pytest.importorskip("torch")
+    semi, orc = build(RHS_CASES[6])
+    u = perturbed_state(semi, seed=19)
+    ud = torch.from_numpy(u).cuda()
+    dud = torch.empty_like(ud)
+    semi.rhs(dud, ud, 0.4)
+    semi.device_context.synchronize()
+    assert rel_err(dud.cpu().numpy(), orc.rhs(u, 0.4)) < 1e-12

@@ -1,0 +1,833 @@
+// C ABI of the GB300 DGSEM hot path (declared in include/trixi_gb300.h).
+//
+// A context owns, in HBM: two FP64 solution buffers (the stage kernel reads
+// one and writes the other, since neighbour traces must come from the
+// pre-stage state), the 2N register u_tmp (FP64, or FP32 in mixed mode),
+// the face-neighbour table, the inverse Jacobians, the node coordinates
+// along each axis (source terms), the indicator arrays, a device clock
+// (t, dt, CFL reduction) and a status word.  A time step is one CUDA graph:
+// clock_begin -> 5 fused stage kernels -> clock_end, with no host round trip.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/trixi_gb300.h"
+#include "tg_dg.cuh"
+
+namespace tg {
+
+// Declared per instantiation unit (tg_inst_*.cu).
+#define TG_DECL(D, R, V)                                                                 \
+  int launch_element_##D##d_##R##_##V(int N, int epb, const DgParams& P, const StageArgs& A, \
+                                      cudaStream_t s);
+TG_DECL(2, f64, weak) TG_DECL(2, f64, fd) TG_DECL(2, f64, hg)
+TG_DECL(2, f32, weak) TG_DECL(2, f32, fd) TG_DECL(2, f32, hg)
+TG_DECL(3, f64, weak) TG_DECL(3, f64, fd) TG_DECL(3, f64, hg)
+TG_DECL(3, f32, weak) TG_DECL(3, f32, fd) TG_DECL(3, f32, hg)
+#undef TG_DECL
+int launch_indicator_2d_f64_hg(int N, const DgParams& P, const double* u, void* a, cudaStream_t s);
+int launch_indicator_2d_f32_hg(int N, const DgParams& P, const double* u, void* a, cudaStream_t s);
+int launch_indicator_3d_f64_hg(int N, const DgParams& P, const double* u, void* a, cudaStream_t s);
+int launch_indicator_3d_f32_hg(int N, const DgParams& P, const double* u, void* a, cudaStream_t s);
+
+int launch_element(int D, int N, bool fp64, int vi, int epb, const DgParams& P,
+                   const StageArgs& A, cudaStream_t s) {
+  typedef int (*Fn)(int, int, const DgParams&, const StageArgs&, cudaStream_t);
+  static const Fn table[2][2][3] = {
+      {{launch_element_2d_f32_weak, launch_element_2d_f32_fd, launch_element_2d_f32_hg},
+       {launch_element_2d_f64_weak, launch_element_2d_f64_fd, launch_element_2d_f64_hg}},
+      {{launch_element_3d_f32_weak, launch_element_3d_f32_fd, launch_element_3d_f32_hg},
+       {launch_element_3d_f64_weak, launch_element_3d_f64_fd, launch_element_3d_f64_hg}}};
+  if (D < 2 || D > 3 || vi < 0 || vi > 2) return -2;
+  return table[D - 2][fp64 ? 1 : 0][vi](N, epb, P, A, s);
+}
+
+int launch_indicator(int D, int N, bool fp64, const DgParams& P, const double* u,
+                     void* alpha_raw, cudaStream_t s) {
+  if (D == 2)
+    return fp64 ? launch_indicator_2d_f64_hg(N, P, u, alpha_raw, s)
+                : launch_indicator_2d_f32_hg(N, P, u, alpha_raw, s);
+  return fp64 ? launch_indicator_3d_f64_hg(N, P, u, alpha_raw, s)
+              : launch_indicator_3d_f32_hg(N, P, u, alpha_raw, s);
+}
+
+int default_epb(int D, int N) {
+  if (D == 2) {
+    switch (N) {
+      case 2: return 64;
+      case 3: return 28;
+      case 4: return 16;
+      case 5: return 10;
+      case 6: return 7;
+    }
+  } else {
+    switch (N) {
+      case 2: return 32;
+      case 3: return 9;
+      case 4: return 4;
+      case 5: return 2;
+    }
+  }
+  return 0;
+}
+
+bool supported_epb(int D, int N, int epb) {
+  if (epb == default_epb(D, N)) return true;
+  if (D == 2 && N == 4) return epb == 8 || epb == 32;
+  if (D == 3 && N == 4) return epb == 2 || epb == 8;
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// Small kernels: CFL reduction, clock, integrals, smoothing
+// ---------------------------------------------------------------------------
+
+// max_dt's reduction (stepsize_dg2d.jl:8-30): max_e invJ_e * sum_d max_nodes lambda_d.
+template <int D>
+__global__ void max_speed_kernel(const double* __restrict__ u, const double* __restrict__ inv_jac,
+                                 int64_t E, int NN, double gamma,
+                                 unsigned long long* __restrict__ speed_bits,
+                                 int32_t* __restrict__ status) {
+  constexpr int NV = D + 2;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  double ml[D];
+  for (int d = 0; d < D; ++d) ml[d] = 0;
+  bool bad = false;
+  for (int q = 0; q < NN; ++q) {
+    const double* p = u + ((size_t)e * NN + q) * NV;
+    double uu[NV], w[NV];
+    for (int v = 0; v < NV; ++v) uu[v] = p[v];
+    Euler<D, double>::cons2prim(uu, w, gamma);
+    const double c = sqrt(gamma * w[NV - 1] / w[0]);
+    bad |= !(w[0] > 0) || !(w[NV - 1] > 0);
+    for (int d = 0; d < D; ++d) ml[d] = fmax(ml[d], fabs(w[1 + d]) + c);
+  }
+  double sum = ml[0];
+  for (int d = 1; d < D; ++d) sum += ml[d];
+  const double sp = inv_jac[e] * sum;
+  if (sp == sp)
+    atomicMax(speed_bits, (unsigned long long)__double_as_longlong(sp));
+  else
+    bad = true;
+  if (bad) atomicOr(status, 2);
+}
+
+__global__ void speed_reset_kernel(unsigned long long* speed_bits) {
+  // nextfloat(0.0): max_dt starts its reduction there (stepsize_dg2d.jl:12)
+  *speed_bits = 1ull;
+}
+
+// initialize! of StepsizeCallback: dt = cfl * max_dt(u)
+__global__ void clock_init_kernel(Clock* c, double t, double t_end, double cfl, int n) {
+  c->t = t;
+  c->t_end = t_end;
+  c->cfl = cfl;
+  const double speed = __longlong_as_double((long long)c->speed_bits);
+  c->dt = cfl * (2.0 / (n * speed));
+  c->skip = 0;
+  c->finalstep = 0;
+  c->finished = 0;
+  c->nan_dt = 0;
+  c->steps = 0;
+}
+
+__global__ void clock_set_kernel(Clock* c, double t, double dt) {
+  c->t = t;
+  c->dt = dt;
+  c->t_end = INFINITY;
+  c->skip = 0;
+  c->finalstep = 0;
+  c->finished = 0;
+}
+
+__global__ void clock_config_kernel(Clock* c, double t_end, double cfl) {
+  c->t_end = t_end;
+  c->cfl = cfl;
+  c->finished = 0;
+  c->finalstep = 0;
+}
+
+// step! prologue: NaN check and limit_dt! (methods_2N.jl:131-140,
+// time_integration.jl:46-55), then reset of the CFL reduction.
+__global__ void clock_begin_kernel(Clock* c) {
+  c->speed_bits = 1ull;
+  if (c->finished) {
+    c->skip = 1;
+    return;
+  }
+  if (isnan(c->dt)) {
+    c->nan_dt = 1;
+    c->finished = 1;
+    c->skip = 1;
+    return;
+  }
+  c->skip = 0;
+  const double tn = c->t + c->dt;
+  const double te = c->t_end;
+  const bool approx = tn == te || fabs(tn - te) <= 1.4901161193847656e-08 * fmax(fabs(tn), fabs(te));
+  if (tn > te || approx) {
+    c->dt = te - c->t;
+    c->finalstep = 1;
+  }
+}
+
+// step! epilogue: t += dt, then StepsizeCallback: dt = cfl * max_dt(u_new).
+__global__ void clock_end_kernel(Clock* c, int n) {
+  if (c->skip) return;
+  c->t += c->dt;
+  c->steps += 1;
+  const double speed = __longlong_as_double((long long)c->speed_bits);
+  c->dt = c->cfl * (2.0 / (n * speed));
+  if (c->finalstep) c->finished = 1;
+}
+
+// Per-element FP64 integrals (integrate_via_indices, analysis_dg2d.jl:313-336):
+// conserved totals, mathematical entropy (compressible_euler_2d.jl:2236-2255)
+// and kinetic energy (:2297-2300).
+template <int D>
+__global__ void element_integrals_kernel(const double* __restrict__ u,
+                                         const double* __restrict__ inv_jac,
+                                         const double* __restrict__ weights, int64_t E, int N,
+                                         double gamma, double* __restrict__ partial) {
+  constexpr int NV = D + 2;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  int NN = N * N;
+  if (D == 3) NN *= N;
+  double vj = 1.0 / inv_jac[e];
+  vj = D == 2 ? vj * vj : vj * vj * vj;
+  double acc[NV + 2];
+  for (int k = 0; k < NV + 2; ++k) acc[k] = 0;
+  for (int q = 0; q < NN; ++q) {
+    const int i = q % N, j = (q / N) % N, k = q / (N * N);
+    double w = weights[i] * weights[j];
+    if (D == 3) w *= weights[k];
+    const double* p = u + ((size_t)e * NN + q) * NV;
+    double m2 = 0;
+    for (int d = 0; d < D; ++d) m2 += p[1 + d] * p[1 + d];
+    for (int v = 0; v < NV; ++v) acc[v] += vj * w * p[v];
+    const double pr = (gamma - 1) * (p[NV - 1] - 0.5 * m2 / p[0]);
+    const double s = log(pr) - gamma * log(p[0]);
+    acc[NV] += vj * w * (-s * p[0] / (gamma - 1));
+    acc[NV + 1] += vj * w * (m2 / (2 * p[0]));
+  }
+  for (int k = 0; k < NV + 2; ++k) partial[(size_t)e * (NV + 2) + k] = acc[k];
+}
+
+// Deterministic sum of partial[E][K] over elements (one block).
+__global__ void sum_rows_kernel(const double* __restrict__ partial, int64_t E, int K,
+                                double* __restrict__ out) {
+  extern __shared__ double sh[];
+  for (int k = 0; k < K; ++k) {
+    double s = 0;
+    for (int64_t e = threadIdx.x; e < E; e += blockDim.x) s += partial[(size_t)e * K + k];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[k] = sh[0];
+    __syncthreads();
+  }
+}
+
+// apply_smoothing! as a gather (indicators_2d.jl:104-136): alpha_e =
+// max(raw_e, 0.5 * raw_n for every face neighbour n).
+template <typename R>
+__global__ void smooth_alpha_kernel(const R* __restrict__ raw, const int32_t* __restrict__ nbr,
+                                    int64_t E, int nfaces, int smooth, double* __restrict__ out) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  R a = raw[e];
+  if (smooth)
+    for (int f = 0; f < nfaces; ++f) a = fmax(a, R(0.5) * raw[nbr[e * nfaces + f]]);
+  out[e] = (double)a;
+}
+
+}  // namespace tg
+
+using namespace tg;
+
+// CarpenterKennedy2N54 (methods_2N.jl:24-48)
+static const double CK_A[5] = {0.0, 567301805773.0 / 1357537059087.0,
+                                2404267990393.0 / 2016746695238.0,
+                                3550918686646.0 / 2091501179385.0,
+                                1275806237668.0 / 842570457699.0};
+static const double CK_B[5] = {1432997174477.0 / 9575080441755.0,
+                               5161836677717.0 / 13612068292357.0,
+                               1720146321549.0 / 2090206949498.0,
+                               3134564353537.0 / 4481467310338.0,
+                               2277821191437.0 / 14882151754819.0};
+static const double CK_C[5] = {0.0, 1432997174477.0 / 9575080441755.0,
+                               2526269341429.0 / 6820363962896.0,
+                               2006345519317.0 / 3224310063776.0,
+                               2802321613138.0 / 2924317926251.0};
+
+struct tg_ctx {
+  int D = 0, N = 0, NN = 0, NV = 0, vi = 0, epb = 0, device = 0;
+  bool fp64 = true;
+  int64_t E = 0, ndofs = 0, nvalues = 0;
+  DgParams P{};
+  cudaStream_t stream = nullptr;
+  double* d_u[2] = {nullptr, nullptr};
+  int cur = 0;
+  void* d_utmp = nullptr;
+  double* d_du = nullptr;
+  double* d_uscratch = nullptr;
+  void* d_alpha_raw = nullptr;
+  double* d_alpha = nullptr;
+  int32_t* d_nbr = nullptr;
+  double* d_invj = nullptr;
+  double* d_xline = nullptr;
+  double* d_weights = nullptr;
+  double* d_partial = nullptr;
+  double* d_sums = nullptr;
+  Clock* d_clock = nullptr;
+  int32_t* d_status = nullptr;
+  unsigned long long* d_speed = nullptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  bool clock_valid = false;
+  double clock_t = 0;
+  bool uploaded = false;
+  std::vector<double> weights;
+  std::string err;
+};
+
+static thread_local std::string g_create_err;
+
+static int fail(tg_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c)
+    c->err = buf;
+  else
+    g_create_err = buf;
+  return code;
+}
+
+#define CUDA_TRY(ctx, call)                                                                    \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess)                                                                     \
+      return fail((ctx), TG_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));         \
+  } while (0)
+
+static size_t rsize(const tg_ctx* c) { return c->fp64 ? sizeof(double) : sizeof(float); }
+
+static void free_ctx(tg_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  for (int p = 0; p < 2; ++p)
+    if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
+  void* ptrs[] = {c->d_u[0], c->d_u[1], c->d_utmp, c->d_du, c->d_uscratch, c->d_alpha_raw,
+                  c->d_alpha, c->d_nbr, c->d_invj, c->d_xline, c->d_weights, c->d_partial,
+                  c->d_sums, c->d_clock, c->d_status, c->d_speed};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+// Element-chunk stage/rhs launch with the context's parameters.
+static int launch(tg_ctx* c, const StageArgs& A) {
+  const int rc = launch_element(c->D, c->N, c->fp64, c->vi, c->epb, c->P, A, c->stream);
+  if (rc != 0) {
+    cudaError_t e = cudaGetLastError();
+    return fail(c, TG_ERR_CUDA, "element kernel launch failed (%d): %s", rc,
+                cudaGetErrorString(e));
+  }
+  return TG_OK;
+}
+
+static int indicator(tg_ctx* c, const double* u) {
+  if (c->vi != VI_HG) return TG_OK;
+  const int rc = launch_indicator(c->D, c->N, c->fp64, c->P, u, c->d_alpha_raw, c->stream);
+  if (rc != 0) return fail(c, TG_ERR_CUDA, "indicator kernel launch failed (%d)", rc);
+  return TG_OK;
+}
+
+static StageArgs base_args(tg_ctx* c) {
+  StageArgs A{};
+  A.alpha_raw = c->d_alpha_raw;
+  A.status = c->d_status;
+  A.clock = c->d_clock;
+  return A;
+}
+
+// Enqueue one fused 2N stage reading d_u[cur] and writing d_u[cur ^ 1].
+static int enqueue_stage(tg_ctx* c, int stage, bool reduce_speed) {
+  int rc = indicator(c, c->d_u[c->cur]);
+  if (rc) return rc;
+  StageArgs A = base_args(c);
+  A.mode = MODE_STAGE;
+  A.u_in = c->d_u[c->cur];
+  A.u_out = c->d_u[c->cur ^ 1];
+  A.u_tmp = c->d_utmp;
+  A.a = CK_A[stage];
+  A.b = CK_B[stage];
+  A.c = CK_C[stage];
+  A.zero_tmp = stage == 0;
+  A.speed_bits = reduce_speed ? &c->d_clock->speed_bits : nullptr;
+  rc = launch(c, A);
+  if (rc) return rc;
+  c->cur ^= 1;
+  return TG_OK;
+}
+
+static int reduce_speed(tg_ctx* c, const double* u, unsigned long long* dst) {
+  speed_reset_kernel<<<1, 1, 0, c->stream>>>(dst);
+  const int64_t nb = (c->E + 127) / 128;
+  if (c->D == 2)
+    max_speed_kernel<2><<<(unsigned)nb, 128, 0, c->stream>>>(u, c->d_invj, c->E, c->NN, c->P.gamma,
+                                                            dst, c->d_status);
+  else
+    max_speed_kernel<3><<<(unsigned)nb, 128, 0, c->stream>>>(u, c->d_invj, c->E, c->NN, c->P.gamma,
+                                                            dst, c->d_status);
+  CUDA_TRY(c, cudaGetLastError());
+  return TG_OK;
+}
+
+extern "C" {
+
+int tg_api_version(void) { return TG_API_VERSION; }
+
+int tg_last_error(const tg_ctx* ctx, char* buf, size_t len) {
+  if (!buf || len == 0) return TG_ERR_INVALID_ARGUMENT;
+  const std::string& s = ctx ? ctx->err : g_create_err;
+  const size_t n = std::min(len - 1, s.size());
+  std::memcpy(buf, s.data(), n);
+  buf[n] = 0;
+  return TG_OK;
+}
+
+int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
+  if (!cfg || !out) return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  const int D = cfg->ndims;
+  if (D != 2 && D != 3) return fail(nullptr, TG_ERR_UNSUPPORTED, "ndims must be 2 or 3");
+  const int N = cfg->polydeg + 1;
+  if (default_epb(D, N) == 0)
+    return fail(nullptr, TG_ERR_UNSUPPORTED, "polydeg %d is not compiled for %dD", cfg->polydeg, D);
+  if (cfg->nelements <= 0) return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "nelements must be > 0");
+  if (cfg->ninterfaces != (int64_t)D * cfg->nelements)
+    return fail(nullptr, TG_ERR_UNSUPPORTED,
+                "ninterfaces != ndims * nelements: only periodic conforming TreeMesh "
+                "(no boundaries, no mortars) is supported");
+  if (cfg->volume_integral < 0 || cfg->volume_integral > 2)
+    return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "unknown volume integral %d", cfg->volume_integral);
+  const int fl[3] = {cfg->volume_flux, cfg->surface_flux, cfg->volume_flux_fv};
+  for (int k = 0; k < 3; ++k)
+    if (fl[k] < 0 || fl[k] > 4) return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "unknown flux %d", fl[k]);
+  if (cfg->source_terms != TG_SOURCE_NONE && cfg->source_terms != TG_SOURCE_CONVERGENCE_TEST)
+    return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "unknown source terms %d", cfg->source_terms);
+  if (cfg->precision != TG_PRECISION_FP64 && cfg->precision != TG_PRECISION_MIXED)
+    return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "unknown precision %d", cfg->precision);
+  if (!cfg->nodes || !cfg->weights || !cfg->inverse_weights || !cfg->derivative_hat ||
+      !cfg->derivative_split || !cfg->inverse_vandermonde_legendre || !cfg->neighbor_ids ||
+      !cfg->orientations || !cfg->inverse_jacobian)
+    return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "missing basis or mesh array");
+  if (cfg->source_terms != TG_SOURCE_NONE && !cfg->node_coordinates)
+    return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "source terms need node_coordinates");
+  int epb = cfg->elements_per_block > 0 ? cfg->elements_per_block : default_epb(D, N);
+  if (!supported_epb(D, N, epb))
+    return fail(nullptr, TG_ERR_UNSUPPORTED, "elements_per_block %d not compiled for %dD N=%d", epb,
+                D, N);
+
+  tg_ctx* c = new tg_ctx();
+  c->D = D;
+  c->N = N;
+  c->NN = D == 2 ? N * N : N * N * N;
+  c->NV = D + 2;
+  c->E = cfg->nelements;
+  c->ndofs = c->E * c->NN;
+  c->nvalues = c->ndofs * c->NV;
+  c->vi = cfg->volume_integral;
+  c->fp64 = cfg->precision == TG_PRECISION_FP64;
+  c->epb = epb;
+  c->device = cfg->device;
+
+  // ---- face-neighbour table from the interface container ----
+  const int nf = 2 * D;
+  std::vector<int32_t> nbr((size_t)c->E * nf, -1);
+  for (int64_t f = 0; f < cfg->ninterfaces; ++f) {
+    const int64_t l = cfg->neighbor_ids[2 * f] - 1, r = cfg->neighbor_ids[2 * f + 1] - 1;
+    const int64_t o = cfg->orientations[f] - 1;
+    if (l < 0 || l >= c->E || r < 0 || r >= c->E || o < 0 || o >= D) {
+      delete c;
+      return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "interface %lld out of range", (long long)f);
+    }
+    int32_t& a = nbr[l * nf + 2 * o + 1];
+    int32_t& b = nbr[r * nf + 2 * o];
+    if (a != -1 || b != -1) {
+      delete c;
+      return fail(nullptr, TG_ERR_UNSUPPORTED, "element face used by two interfaces");
+    }
+    a = (int32_t)r;
+    b = (int32_t)l;
+  }
+  for (size_t k = 0; k < nbr.size(); ++k)
+    if (nbr[k] < 0) {
+      delete c;
+      return fail(nullptr, TG_ERR_UNSUPPORTED,
+                  "element face without interface: only periodic conforming meshes");
+    }
+
+  // ---- node coordinates along each axis (tensor-product TreeMesh elements) ----
+  std::vector<double> xline;
+  if (cfg->node_coordinates) {
+    xline.resize((size_t)c->E * D * N);
+    const double* X = cfg->node_coordinates;
+    for (int64_t e = 0; e < c->E; ++e)
+      for (int q = 0; q < c->NN; ++q) {
+        const int idx[3] = {q % N, (q / N) % N, q / (N * N)};
+        for (int d = 0; d < D; ++d) {
+          const double x = X[((size_t)e * c->NN + q) * D + d];
+          double& slot = xline[((size_t)e * D + d) * N + idx[d]];
+          bool first = true;
+          for (int dd = 0; dd < D; ++dd)
+            if (dd != d && idx[dd] != 0) first = false;
+          if (first)
+            slot = x;
+          else if (slot != x) {
+            delete c;
+            return fail(nullptr, TG_ERR_UNSUPPORTED, "node coordinates are not a tensor product");
+          }
+        }
+      }
+  }
+
+  // ---- parameters ----
+  DgParams& P = c->P;
+  P.nelements = c->E;
+  P.gamma = cfg->gamma;
+  P.inv_gamma_minus_one = 1.0 / (cfg->gamma - 1.0);
+  for (int i = 0; i < N; ++i) {
+    P.nodes[i] = cfg->nodes[i];
+    P.inv_weights[i] = cfg->inverse_weights[i];
+    c->weights.push_back(cfg->weights[i]);
+  }
+  for (int a = 0; a < N; ++a)
+    for (int b = 0; b < N; ++b) {
+      // Julia column-major (a, b) -> a + b * N
+      P.Dhat[a * N + b] = cfg->derivative_hat[a + b * N];
+      P.Dsplit[a * N + b] = cfg->derivative_split[a + b * N];
+      P.Vinv[a * N + b] = cfg->inverse_vandermonde_legendre[a + b * N];
+    }
+  P.volume_flux = cfg->volume_flux;
+  P.surface_flux = cfg->surface_flux;
+  P.fv_flux = cfg->volume_flux_fv;
+  P.source = cfg->source_terms;
+  P.alpha_max = cfg->alpha_max;
+  P.alpha_min = cfg->alpha_min;
+  P.alpha_smooth = cfg->alpha_smooth;
+  // indicators.jl:128-131 and calc_volume_integral.jl:242-245
+  P.hg_threshold = 0.5 * std::pow(10.0, -1.8 * std::pow((double)N, 0.25));
+  P.hg_parameter_s = std::log((1 - 0.0001) / 0.0001);
+  P.alpha_atol = c->fp64 ? std::max(100 * 2.220446049250313e-16, std::pow(2.220446049250313e-16, 0.75))
+                         : (double)std::max(100 * 1.1920929e-07f, std::pow(1.1920929e-07f, 0.75f));
+
+  // ---- device allocations ----
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(nullptr, TG_ERR_CUDA, "cudaSetDevice(%d): %s", cfg->device, cudaGetErrorString(e));
+  }
+#define ALLOC(ptr, bytes)                                                                 \
+  do {                                                                                    \
+    e = cudaMalloc((void**)&(ptr), (bytes));                                              \
+    if (e != cudaSuccess) {                                                               \
+      free_ctx(c);                                                                        \
+      return fail(nullptr, TG_ERR_CUDA, "cudaMalloc(%zu): %s", (size_t)(bytes),          \
+                  cudaGetErrorString(e));                                                 \
+    }                                                                                     \
+  } while (0)
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    free_ctx(c);
+    return fail(nullptr, TG_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+  }
+  const size_t vb = sizeof(double) * (size_t)c->nvalues;
+  ALLOC(c->d_u[0], vb);
+  ALLOC(c->d_u[1], vb);
+  ALLOC(c->d_utmp, rsize(c) * (size_t)c->nvalues);
+  ALLOC(c->d_nbr, sizeof(int32_t) * nbr.size());
+  ALLOC(c->d_invj, sizeof(double) * c->E);
+  ALLOC(c->d_weights, sizeof(double) * N);
+  ALLOC(c->d_clock, sizeof(Clock));
+  ALLOC(c->d_status, sizeof(int32_t));
+  ALLOC(c->d_speed, sizeof(unsigned long long));
+  ALLOC(c->d_sums, sizeof(double) * 16);
+  if (!xline.empty()) ALLOC(c->d_xline, sizeof(double) * xline.size());
+  if (c->vi == VI_HG) {
+    ALLOC(c->d_alpha_raw, rsize(c) * c->E);
+    ALLOC(c->d_alpha, sizeof(double) * c->E);
+  }
+#undef ALLOC
+  cudaMemcpy(c->d_nbr, nbr.data(), sizeof(int32_t) * nbr.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(c->d_invj, cfg->inverse_jacobian, sizeof(double) * c->E, cudaMemcpyHostToDevice);
+  cudaMemcpy(c->d_weights, c->weights.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
+  if (!xline.empty())
+    cudaMemcpy(c->d_xline, xline.data(), sizeof(double) * xline.size(), cudaMemcpyHostToDevice);
+  cudaMemset(c->d_status, 0, sizeof(int32_t));
+  cudaMemset(c->d_clock, 0, sizeof(Clock));
+  cudaMemset(c->d_utmp, 0, rsize(c) * (size_t)c->nvalues);
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    free_ctx(c);
+    return fail(nullptr, TG_ERR_CUDA, "context setup: %s", cudaGetErrorString(e));
+  }
+  P.nbr = c->d_nbr;
+  P.inv_jac = c->d_invj;
+  P.xline = c->d_xline;
+  *out = c;
+  return TG_OK;
+}
+
+int tg_ctx_destroy(tg_ctx* ctx) {
+  if (!ctx) return TG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  free_ctx(ctx);
+  return TG_OK;
+}
+
+int tg_ndofs(const tg_ctx* ctx, int64_t* ndofs, int64_t* nvalues) {
+  if (!ctx) return TG_ERR_INVALID_ARGUMENT;
+  if (ndofs) *ndofs = ctx->ndofs;
+  if (nvalues) *nvalues = ctx->nvalues;
+  return TG_OK;
+}
+
+int tg_elements_per_block(const tg_ctx* ctx, int32_t* epb) {
+  if (!ctx || !epb) return TG_ERR_INVALID_ARGUMENT;
+  *epb = ctx->epb;
+  return TG_OK;
+}
+
+int tg_upload_state(tg_ctx* c, const double* u_host) {
+  if (!c || !u_host) return TG_ERR_INVALID_ARGUMENT;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_u[c->cur], u_host, sizeof(double) * c->nvalues,
+                              cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  c->uploaded = true;
+  c->clock_valid = false;
+  return TG_OK;
+}
+
+int tg_download_state(tg_ctx* c, double* u_host) {
+  if (!c || !u_host) return TG_ERR_INVALID_ARGUMENT;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  CUDA_TRY(c, cudaMemcpyAsync(u_host, c->d_u[c->cur], sizeof(double) * c->nvalues,
+                              cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return TG_OK;
+}
+
+int tg_state_device_ptr(tg_ctx* c, double** u_dev) {
+  if (!c || !u_dev) return TG_ERR_INVALID_ARGUMENT;
+  *u_dev = c->d_u[c->cur];
+  return TG_OK;
+}
+
+int tg_rhs(tg_ctx* c, double* du_dev, const double* u_dev, double t) {
+  if (!c || !du_dev || !u_dev) return TG_ERR_INVALID_ARGUMENT;
+  if ((const double*)du_dev == u_dev) return fail(c, TG_ERR_INVALID_ARGUMENT, "du aliases u");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  int rc = indicator(c, u_dev);
+  if (rc) return rc;
+  StageArgs A = base_args(c);
+  A.mode = MODE_RHS;
+  A.u_in = u_dev;
+  A.du_out = du_dev;
+  A.t_rhs = t;
+  return launch(c, A);
+}
+
+int tg_rhs_host(tg_ctx* c, double* du_host, const double* u_host, double t) {
+  if (!c || !du_host || !u_host) return TG_ERR_INVALID_ARGUMENT;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  const size_t vb = sizeof(double) * c->nvalues;
+  if (!c->d_uscratch) CUDA_TRY(c, cudaMalloc((void**)&c->d_uscratch, vb));
+  if (!c->d_du) CUDA_TRY(c, cudaMalloc((void**)&c->d_du, vb));
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_uscratch, u_host, vb, cudaMemcpyHostToDevice, c->stream));
+  int rc = tg_rhs(c, c->d_du, c->d_uscratch, t);
+  if (rc) return rc;
+  CUDA_TRY(c, cudaMemcpyAsync(du_host, c->d_du, vb, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return TG_OK;
+}
+
+int tg_max_dt(tg_ctx* c, const double* u_dev, double* dt) {
+  if (!c || !dt) return TG_ERR_INVALID_ARGUMENT;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  int rc = reduce_speed(c, u_dev ? u_dev : c->d_u[c->cur], c->d_speed);
+  if (rc) return rc;
+  unsigned long long bits = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&bits, c->d_speed, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  double speed;
+  std::memcpy(&speed, &bits, sizeof(speed));
+  *dt = 2.0 / (c->N * speed);
+  return TG_OK;
+}
+
+int tg_rk_stage(tg_ctx* c, int32_t stage, double t, double dt) {
+  if (!c || stage < 0 || stage > 4) return TG_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return fail(c, TG_ERR_STATE, "no state uploaded");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  // the stage clock is written in stream order, without a host round trip
+  clock_set_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, t, dt);
+  CUDA_TRY(c, cudaGetLastError());
+  c->clock_valid = false;
+  return enqueue_stage(c, stage, false);
+}
+
+int tg_stream(tg_ctx* c, void** stream) {
+  if (!c || !stream) return TG_ERR_INVALID_ARGUMENT;
+  *stream = (void*)c->stream;
+  return TG_OK;
+}
+
+int tg_set_time(tg_ctx* c, double t) {
+  if (!c) return TG_ERR_INVALID_ARGUMENT;
+  c->clock_valid = false;
+  c->clock_t = t;
+  return TG_OK;
+}
+
+static int capture_step_graph(tg_ctx* c, int parity) {
+  const int saved = c->cur;
+  c->cur = parity;
+  cudaGraph_t g = nullptr;
+  CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+  clock_begin_kernel<<<1, 1, 0, c->stream>>>(c->d_clock);
+  int rc = TG_OK;
+  for (int s = 0; s < 5 && rc == TG_OK; ++s) rc = enqueue_stage(c, s, s == 4);
+  if (rc == TG_OK) clock_end_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, c->N);
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  c->cur = saved;
+  if (rc != TG_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(c, TG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&c->graph[parity], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(c, TG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  return TG_OK;
+}
+
+int tg_step(tg_ctx* c, int64_t max_steps, double cfl, double t_end, double* t_inout,
+            int64_t* steps_taken) {
+  if (!c || !t_inout || max_steps < 0 || !(cfl > 0)) return TG_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return fail(c, TG_ERR_STATE, "no state uploaded");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  for (int p = 0; p < 2; ++p)
+    if (!c->graph[p]) {
+      int rc = capture_step_graph(c, p);
+      if (rc) return rc;
+    }
+  if (!c->clock_valid) {
+    // initialize!(StepsizeCallback): dt = cfl * max_dt(u0)
+    int rc = reduce_speed(c, c->d_u[c->cur], &c->d_clock->speed_bits);
+    if (rc) return rc;
+    clock_init_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, *t_inout, t_end, cfl, c->N);
+    CUDA_TRY(c, cudaGetLastError());
+    c->clock_valid = true;
+  } else {
+    clock_config_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, t_end, cfl);
+    CUDA_TRY(c, cudaGetLastError());
+  }
+  Clock h{};
+  CUDA_TRY(c, cudaMemcpyAsync(&h, c->d_clock, sizeof(Clock), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  const int64_t steps0 = h.steps;
+  int64_t launched = 0;
+  const int64_t poll = 64;
+  while (launched < max_steps) {
+    const int64_t chunk = std::min(poll, max_steps - launched);
+    for (int64_t k = 0; k < chunk; ++k) {
+      CUDA_TRY(c, cudaGraphLaunch(c->graph[c->cur], c->stream));
+      c->cur ^= 1;
+    }
+    launched += chunk;
+    if (std::isfinite(t_end) || launched >= max_steps) {
+      CUDA_TRY(c, cudaMemcpyAsync(&h, c->d_clock, sizeof(Clock), cudaMemcpyDeviceToHost, c->stream));
+      CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+      if (h.finished) break;
+    }
+  }
+  *t_inout = h.t;
+  if (steps_taken) *steps_taken = h.steps - steps0;
+  if (h.nan_dt) return fail(c, TG_ERR_NUMERICAL, "time step size `dt` is NaN");
+  return TG_OK;
+}
+
+int tg_integrals(tg_ctx* c, double* out) {
+  if (!c || !out) return TG_ERR_INVALID_ARGUMENT;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  const int K = c->NV + 2;
+  if (!c->d_partial) CUDA_TRY(c, cudaMalloc((void**)&c->d_partial, sizeof(double) * K * c->E));
+  const int64_t nb = (c->E + 127) / 128;
+  if (c->D == 2)
+    element_integrals_kernel<2><<<(unsigned)nb, 128, 0, c->stream>>>(
+        c->d_u[c->cur], c->d_invj, c->d_weights, c->E, c->N, c->P.gamma, c->d_partial);
+  else
+    element_integrals_kernel<3><<<(unsigned)nb, 128, 0, c->stream>>>(
+        c->d_u[c->cur], c->d_invj, c->d_weights, c->E, c->N, c->P.gamma, c->d_partial);
+  sum_rows_kernel<<<1, 256, 256 * sizeof(double), c->stream>>>(c->d_partial, c->E, K, c->d_sums);
+  CUDA_TRY(c, cudaGetLastError());
+  CUDA_TRY(c, cudaMemcpyAsync(out, c->d_sums, sizeof(double) * K, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return TG_OK;
+}
+
+int tg_alpha(tg_ctx* c, const double* u_dev, double* alpha_host) {
+  if (!c || !alpha_host) return TG_ERR_INVALID_ARGUMENT;
+  if (c->vi != VI_HG) return fail(c, TG_ERR_STATE, "context has no shock-capturing indicator");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  int rc = indicator(c, u_dev ? u_dev : c->d_u[c->cur]);
+  if (rc) return rc;
+  const int64_t nb = (c->E + 127) / 128;
+  if (c->fp64)
+    smooth_alpha_kernel<double><<<(unsigned)nb, 128, 0, c->stream>>>(
+        (const double*)c->d_alpha_raw, c->d_nbr, c->E, 2 * c->D, c->P.alpha_smooth, c->d_alpha);
+  else
+    smooth_alpha_kernel<float><<<(unsigned)nb, 128, 0, c->stream>>>(
+        (const float*)c->d_alpha_raw, c->d_nbr, c->E, 2 * c->D, c->P.alpha_smooth, c->d_alpha);
+  CUDA_TRY(c, cudaGetLastError());
+  CUDA_TRY(c, cudaMemcpyAsync(alpha_host, c->d_alpha, sizeof(double) * c->E, cudaMemcpyDeviceToHost,
+                              c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return TG_OK;
+}
+
+int tg_status(tg_ctx* c, int32_t* flags) {
+  if (!c || !flags) return TG_ERR_INVALID_ARGUMENT;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  CUDA_TRY(c, cudaMemcpyAsync(flags, c->d_status, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemsetAsync(c->d_status, 0, sizeof(int32_t), c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return TG_OK;
+}
+
+int tg_synchronize(tg_ctx* c) {
+  if (!c) return TG_ERR_INVALID_ARGUMENT;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return TG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,242 @@
+// Compressible Euler physics for the GB300 DGSEM kernels, templated on the
+// compute type R (double for the FP64 path, float for the mixed path) and on
+// the dimension D.  State vectors live in registers: u[NV] conservative,
+// w[NV] primitive (rho, v_1..v_D, p), NV = D + 2.
+//
+// Formulas follow src/equations/compressible_euler_{2,3}d.jl,
+// src/equations/numerical_fluxes.jl and src/auxiliary/math.jl of Trixi.jl.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tg {
+
+enum VolumeIntegralKind { VI_WEAK = 0, VI_FD = 1, VI_HG = 2 };
+enum FluxKind {
+  FLUX_CENTRAL = 0,
+  FLUX_RANOCHA = 1,
+  FLUX_SHIMA_ETAL = 2,
+  FLUX_LLF = 3,
+  FLUX_LLF_NAIVE = 4
+};
+enum SourceKind { SRC_NONE = 0, SRC_CONVERGENCE_TEST = 1 };
+
+template <typename R>
+struct Real;
+
+template <>
+struct Real<double> {
+  static __device__ __forceinline__ double log(double x) { return ::log(x); }
+  static __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+  static __device__ __forceinline__ double sin(double x) { return ::sin(x); }
+  static __device__ __forceinline__ double cos(double x) { return ::cos(x); }
+  static __device__ __forceinline__ double exp(double x) { return ::exp(x); }
+};
+
+template <>
+struct Real<float> {
+  // logf / sinf / cosf / expf are CUDA's accurate single-precision functions;
+  // division and sqrt follow the translation unit's -prec-div/-prec-sqrt.
+  static __device__ __forceinline__ float log(float x) { return ::logf(x); }
+  static __device__ __forceinline__ float sqrt(float x) { return ::sqrtf(x); }
+  static __device__ __forceinline__ float sin(float x) { return ::sinf(x); }
+  static __device__ __forceinline__ float cos(float x) { return ::cosf(x); }
+  static __device__ __forceinline__ float exp(float x) { return ::expf(x); }
+};
+
+// ---------------------------------------------------------------------------
+// Logarithmic mean (math.jl:198-250).
+//
+// FP64: Trixi's algorithm as is -- the series in f^2 = ((y-x)/(y+x))^2 below
+// f^2 < 1e-4, else (y - x) / log(y / x).
+//
+// FP32: the same series, one term longer (2/9 f^8), used below f^2 < 0.05.
+// Its truncation error is f^10 / 11 < 3e-8 there, under FP32 rounding, and
+// above the switch y/x > 1.58 so log(y/x) > 0.45 keeps the direct formula
+// well conditioned; f is formed as (y-x)/(y+x) instead of Trixi's
+// cancellation-prone quotient of quadratics.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double ln_mean(double x, double y) {
+  const double f2 = (x * (x - 2 * y) + y * y) / (x * (x + 2 * y) + y * y);
+  if (f2 < 1.0e-4)
+    return (x + y) / (2.0 + f2 * (2.0 / 3.0 + f2 * (2.0 / 5.0 + f2 * (2.0 / 7.0))));
+  return (y - x) / ::log(y / x);
+}
+__device__ __forceinline__ double inv_ln_mean(double x, double y) {
+  const double f2 = (x * (x - 2 * y) + y * y) / (x * (x + 2 * y) + y * y);
+  if (f2 < 1.0e-4)
+    return (2.0 + f2 * (2.0 / 3.0 + f2 * (2.0 / 5.0 + f2 * (2.0 / 7.0)))) / (x + y);
+  return ::log(y / x) / (y - x);
+}
+__device__ __forceinline__ float ln_mean(float x, float y) {
+  const float f = (y - x) / (y + x);
+  const float f2 = f * f;
+  if (f2 < 0.05f)
+    return (x + y) /
+           (2.0f + f2 * (2.0f / 3.0f + f2 * (2.0f / 5.0f + f2 * (2.0f / 7.0f + f2 * (2.0f / 9.0f)))));
+  return (y - x) / ::logf(y / x);
+}
+__device__ __forceinline__ float inv_ln_mean(float x, float y) {
+  const float f = (y - x) / (y + x);
+  const float f2 = f * f;
+  if (f2 < 0.05f)
+    return (2.0f + f2 * (2.0f / 3.0f + f2 * (2.0f / 5.0f + f2 * (2.0f / 7.0f + f2 * (2.0f / 9.0f))))) /
+           (x + y);
+  return ::logf(y / x) / (y - x);
+}
+
+template <int D, typename R>
+struct Euler {
+  static constexpr int NV = D + 2;
+  static constexpr int P = D + 1;
+
+  // cons2prim, compressible_euler_2d.jl:2038-2046
+  static __device__ __forceinline__ void cons2prim(const R* u, R* w, R gamma) {
+    const R rho = u[0];
+    const R inv_rho = R(1) / rho;
+    R ke = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      w[1 + d] = u[1 + d] * inv_rho;
+      ke += u[1 + d] * w[1 + d];
+    }
+    w[0] = rho;
+    w[P] = (gamma - R(1)) * (u[P] - R(0.5) * ke);
+  }
+
+  // Component o (0-based direction) of a D-vector stored at a[0..D-1], with a
+  // runtime o but compile-time indexing only (keeps arrays in registers).
+  static __device__ __forceinline__ R pick(const R* a, int o) {
+    R r = a[0];
+#pragma unroll
+    for (int d = 1; d < D; ++d) r = (o == d) ? a[d] : r;
+    return r;
+  }
+
+  // flux(u, orientation), compressible_euler_2d.jl:415-432, 3d.jl:420-447
+  static __device__ __forceinline__ void flux(const R* u, const R* w, int o, R* f) {
+    const R rvo = pick(u + 1, o);
+    const R vo = pick(w + 1, o);
+    f[0] = rvo;
+#pragma unroll
+    for (int d = 0; d < D; ++d) f[1 + d] = (d == o) ? rvo * w[1 + d] + w[P] : rvo * w[1 + d];
+    f[P] = (u[P] + w[P]) * vo;
+  }
+
+  // flux_ranocha, compressible_euler_2d.jl:686-722, 3d.jl:746-792
+  static __device__ __forceinline__ void flux_ranocha(const R* wl, const R* wr, int o,
+                                                       R inv_gm1, R* f) {
+    const R rho_mean = ln_mean(wl[0], wr[0]);
+    const R inv_rho_p_mean = wl[P] * wr[P] * inv_ln_mean(wl[0] * wr[P], wr[0] * wl[P]);
+    R vavg[D];
+    R vsq = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      vavg[d] = R(0.5) * (wl[1 + d] + wr[1 + d]);
+      vsq += wl[1 + d] * wr[1 + d];
+    }
+    vsq *= R(0.5);
+    const R p_avg = R(0.5) * (wl[P] + wr[P]);
+    const R f1 = rho_mean * pick(vavg, o);
+    f[0] = f1;
+#pragma unroll
+    for (int d = 0; d < D; ++d) f[1 + d] = (d == o) ? f1 * vavg[d] + p_avg : f1 * vavg[d];
+    f[P] = f1 * (vsq + inv_rho_p_mean * inv_gm1) +
+           R(0.5) * (wl[P] * pick(wr + 1, o) + wr[P] * pick(wl + 1, o));
+  }
+
+  // flux_shima_etal, compressible_euler_2d.jl:466-495
+  static __device__ __forceinline__ void flux_shima(const R* wl, const R* wr, int o, R inv_gm1,
+                                                     R* f) {
+    const R rho_avg = R(0.5) * (wl[0] + wr[0]);
+    R vavg[D];
+    R kin = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      vavg[d] = R(0.5) * (wl[1 + d] + wr[1 + d]);
+      kin += wl[1 + d] * wr[1 + d];
+    }
+    kin *= R(0.5);
+    const R p_avg = R(0.5) * (wl[P] + wr[P]);
+    const R vo = pick(vavg, o);
+    const R pv_avg = R(0.5) * (wl[P] * pick(wr + 1, o) + wr[P] * pick(wl + 1, o));
+    const R f1 = rho_avg * vo;
+    f[0] = f1;
+#pragma unroll
+    for (int d = 0; d < D; ++d) f[1 + d] = (d == o) ? f1 * vavg[d] + p_avg : f1 * vavg[d];
+    f[P] = p_avg * vo * inv_gm1 + f1 * kin + pv_avg;
+  }
+
+  // flux_central, numerical_fluxes.jl:17-25
+  static __device__ __forceinline__ void flux_central(const R* ul, const R* wl, const R* ur,
+                                                       const R* wr, int o, R* f) {
+    R fl[NV], fr[NV];
+    flux(ul, wl, o, fl);
+    flux(ur, wr, o, fr);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) f[v] = R(0.5) * (fl[v] + fr[v]);
+  }
+
+  // FluxLaxFriedrichs(max_abs_speed[_naive]), numerical_fluxes.jl:166-178, 222-253,
+  // max_abs_speed(_naive), compressible_euler_2d.jl:1423-1482
+  static __device__ __forceinline__ void flux_llf(const R* ul, const R* wl, const R* ur,
+                                                   const R* wr, int o, bool naive, R gamma,
+                                                   R* f) {
+    flux_central(ul, wl, ur, wr, o, f);
+    const R cl = Real<R>::sqrt(gamma * wl[P] / wl[0]);
+    const R cr = Real<R>::sqrt(gamma * wr[P] / wr[0]);
+    const R al = fabs(pick(wl + 1, o)), ar = fabs(pick(wr + 1, o));
+    const R lam = naive ? fmax(al, ar) + fmax(cl, cr) : fmax(al + cl, ar + cr);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) f[v] = f[v] + (R(-0.5) * lam * (ur[v] - ul[v]));
+  }
+
+  static __device__ __forceinline__ void two_point(int kind, const R* ul, const R* wl,
+                                                    const R* ur, const R* wr, int o, R gamma,
+                                                    R inv_gm1, R* f) {
+    switch (kind) {
+      case FLUX_RANOCHA: flux_ranocha(wl, wr, o, inv_gm1, f); break;
+      case FLUX_SHIMA_ETAL: flux_shima(wl, wr, o, inv_gm1, f); break;
+      case FLUX_LLF: flux_llf(ul, wl, ur, wr, o, false, gamma, f); break;
+      case FLUX_LLF_NAIVE: flux_llf(ul, wl, ur, wr, o, true, gamma, f); break;
+      default: flux_central(ul, wl, ur, wr, o, f); break;
+    }
+  }
+
+  // source_terms_convergence_test, compressible_euler_2d.jl:116-145, 3d.jl:127-150
+  static __device__ __forceinline__ void source_convergence(const R* x, R t, R gamma, R* s) {
+    const R c = 2, A = R(0.1);
+    const R omega = R(3.141592653589793);  // 2 * pi * (1/2)
+    R arg = x[0] + x[1];
+    if (D == 3) arg += x[D == 3 ? 2 : 0];
+    arg = omega * (arg - t);
+    const R si = Real<R>::sin(arg), co = Real<R>::cos(arg);
+    const R rho = c + A * si;
+    const R rho_x = omega * A * co;
+    if (D == 2) {
+      const R tmp = (2 * rho - 1) * (gamma - 1);
+      s[0] = rho_x;
+      s[1] = rho_x * (1 + tmp);
+      s[2] = s[1];
+      s[P] = 2 * rho_x * (rho + tmp);
+    } else {
+      const R tmp = (2 * rho - R(1.5)) * (gamma - 1);
+      s[0] = 2 * rho_x;
+      s[1] = rho_x * (2 + tmp);
+      s[2] = s[1];
+      s[D] = s[1];
+      s[P] = rho_x * (4 * rho + 3 * tmp);
+    }
+  }
+
+  // density_pressure, compressible_euler_2d.jl:2205-2210
+  static __device__ __forceinline__ R density_pressure(const R* u, R gamma) {
+    R m2 = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) m2 += u[1 + d] * u[1 + d];
+    return (gamma - R(1)) * (u[0] * u[P] - R(0.5) * m2);
+  }
+};
+
+}  // namespace tg

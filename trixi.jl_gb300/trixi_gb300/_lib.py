@@ -1,0 +1,125 @@
+"""ctypes binding of libtrixi_gb300.so (include/trixi_gb300.h).
+
+The library is built in-tree (trixi.jl_gb300/_build).  There is no fallback:
+if the shared library cannot be loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+PKG_ROOT = os.path.dirname(_HERE)
+LIB_PATH = os.path.join(PKG_ROOT, "_build", "libtrixi_gb300.so")
+
+TG_OK = 0
+STATUS_NAMES = {-1: "invalid argument", -2: "unsupported", -3: "CUDA error",
+                -4: "numerical failure", -5: "invalid call order"}
+
+# enums (trixi_gb300.h)
+TG_VOLUME_WEAK_FORM, TG_VOLUME_FLUX_DIFFERENCING, TG_VOLUME_SHOCK_CAPTURING_HG = 0, 1, 2
+(TG_FLUX_CENTRAL, TG_FLUX_RANOCHA, TG_FLUX_SHIMA_ETAL, TG_FLUX_LAX_FRIEDRICHS,
+ TG_FLUX_LAX_FRIEDRICHS_NAIVE) = range(5)
+TG_SOURCE_NONE, TG_SOURCE_CONVERGENCE_TEST = 0, 1
+TG_PRECISION_FP64, TG_PRECISION_MIXED = 0, 1
+
+# Every symbol declared in include/trixi_gb300.h.
+EXPORTS = ("tg_api_version", "tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ndofs",
+           "tg_upload_state", "tg_download_state", "tg_state_device_ptr", "tg_rhs",
+           "tg_rhs_host", "tg_max_dt", "tg_rk_stage", "tg_step", "tg_set_time",
+           "tg_integrals", "tg_alpha", "tg_status", "tg_synchronize",
+           "tg_elements_per_block", "tg_stream")
+
+
+class TrixiGB300Error(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{STATUS_NAMES.get(code, code)}] {msg}")
+        self.code = code
+
+
+class tg_config(ctypes.Structure):
+    _fields_ = [
+        ("ndims", ctypes.c_int32),
+        ("polydeg", ctypes.c_int32),
+        ("nelements", ctypes.c_int64),
+        ("ninterfaces", ctypes.c_int64),
+        ("gamma", ctypes.c_double),
+        ("volume_integral", ctypes.c_int32),
+        ("volume_flux", ctypes.c_int32),
+        ("surface_flux", ctypes.c_int32),
+        ("volume_flux_fv", ctypes.c_int32),
+        ("alpha_max", ctypes.c_double),
+        ("alpha_min", ctypes.c_double),
+        ("alpha_smooth", ctypes.c_int32),
+        ("source_terms", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("device", ctypes.c_int32),
+        ("nodes", ctypes.POINTER(ctypes.c_double)),
+        ("weights", ctypes.POINTER(ctypes.c_double)),
+        ("inverse_weights", ctypes.POINTER(ctypes.c_double)),
+        ("derivative_hat", ctypes.POINTER(ctypes.c_double)),
+        ("derivative_split", ctypes.POINTER(ctypes.c_double)),
+        ("inverse_vandermonde_legendre", ctypes.POINTER(ctypes.c_double)),
+        ("neighbor_ids", ctypes.POINTER(ctypes.c_int64)),
+        ("orientations", ctypes.POINTER(ctypes.c_int64)),
+        ("inverse_jacobian", ctypes.POINTER(ctypes.c_double)),
+        ("node_coordinates", ctypes.POINTER(ctypes.c_double)),
+        ("elements_per_block", ctypes.c_int32),
+    ]
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load the shared library (raises OSError if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise OSError(f"libtrixi_gb300.so not found at {path}: run trixi.jl_gb300/build.py "
+                      "(there is no CPU fallback)")
+    lib = ctypes.CDLL(path)
+    P = ctypes.POINTER
+    d, i32, i64, vp = ctypes.c_double, ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p
+    pd = P(d)
+    sigs = {
+        "tg_api_version": ([], ctypes.c_int),
+        "tg_ctx_create": ([P(tg_config), P(vp)], ctypes.c_int),
+        "tg_ctx_destroy": ([vp], ctypes.c_int),
+        "tg_last_error": ([vp, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
+        "tg_ndofs": ([vp, P(i64), P(i64)], ctypes.c_int),
+        "tg_upload_state": ([vp, vp], ctypes.c_int),
+        "tg_download_state": ([vp, vp], ctypes.c_int),
+        "tg_state_device_ptr": ([vp, P(vp)], ctypes.c_int),
+        "tg_rhs": ([vp, vp, vp, d], ctypes.c_int),
+        "tg_rhs_host": ([vp, vp, vp, d], ctypes.c_int),
+        "tg_max_dt": ([vp, vp, pd], ctypes.c_int),
+        "tg_rk_stage": ([vp, i32, d, d], ctypes.c_int),
+        "tg_step": ([vp, i64, d, d, pd, P(i64)], ctypes.c_int),
+        "tg_set_time": ([vp, d], ctypes.c_int),
+        "tg_integrals": ([vp, pd], ctypes.c_int),
+        "tg_alpha": ([vp, vp, pd], ctypes.c_int),
+        "tg_status": ([vp, P(i32)], ctypes.c_int),
+        "tg_synchronize": ([vp], ctypes.c_int),
+        "tg_elements_per_block": ([vp, P(i32)], ctypes.c_int),
+        "tg_stream": ([vp, P(vp)], ctypes.c_int),
+    }
+    for name, (args, res) in sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def last_error(ctx=None) -> str:
+    buf = ctypes.create_string_buffer(1024)
+    load().tg_last_error(ctx, buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(rc: int, ctx=None) -> None:
+    if rc != TG_OK:
+        raise TrixiGB300Error(rc, last_error(ctx))

@@ -1,0 +1,263 @@
+"""SemidiscretizationHyperbolic on the GB300 path.
+
+Host-side mirror of src/semidiscretization/semidiscretization_hyperbolic.jl
+and src/semidiscretization/semidiscretization.jl: the semidiscretization
+builds the TreeMesh containers (elements, interfaces) on the host, hands them
+with the basis to the C ABI (tg_ctx_create) and exposes rhs! / compute
+coefficients / time stepping through the device context.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .equations import CompressibleEulerEquations2D
+from .mesh import TreeMesh
+from .solvers import DGSEM, VolumeIntegralShockCapturingHG
+
+
+class BoundaryConditionPeriodic:
+    def __repr__(self):
+        return "boundary_condition_periodic"
+
+
+boundary_condition_periodic = BoundaryConditionPeriodic()
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ptr_of(x):
+    """Address of a device or host buffer: torch tensor, numpy array or int."""
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    raise TypeError(f"cannot take the address of {type(x)}")
+
+
+class DeviceContext:
+    """One tg_ctx: device-resident state, stage buffers and step graphs."""
+
+    def __init__(self, semi, precision="fp64", device=0, elements_per_block=0):
+        lib = _lib.load()
+        self.lib = lib
+        self.semi = semi
+        dg, eq = semi.solver, semi.equations
+        vi = dg.volume_integral
+        b = dg.basis
+        # keep every array alive while the config points at it
+        self._keep = []
+
+        def arr(a, dtype=np.float64):
+            a = np.ascontiguousarray(a, dtype=dtype)
+            self._keep.append(a)
+            return a
+
+        nb, orient = semi.neighbor_ids, semi.orientations
+        cfg = _lib.tg_config()
+        cfg.ndims = eq.ndims
+        cfg.polydeg = b.polydeg
+        cfg.nelements = semi.nelements
+        cfg.ninterfaces = nb.shape[0]
+        cfg.gamma = eq.gamma
+        cfg.volume_integral = vi.code
+        if isinstance(vi, VolumeIntegralShockCapturingHG):
+            ind = vi.indicator
+            cfg.volume_flux = vi.volume_flux_dg.code
+            cfg.volume_flux_fv = vi.volume_flux_fv.code
+            cfg.alpha_max, cfg.alpha_min = ind.alpha_max, ind.alpha_min
+            cfg.alpha_smooth = int(ind.alpha_smooth)
+        else:
+            cfg.volume_flux = getattr(vi, "volume_flux", None).code if hasattr(vi, "volume_flux") else 0
+            cfg.volume_flux_fv = dg.surface_flux.code
+        cfg.surface_flux = dg.surface_flux.code
+        cfg.source_terms = semi.source_terms.code if semi.source_terms is not None else 0
+        cfg.precision = {"fp64": _lib.TG_PRECISION_FP64, "mixed": _lib.TG_PRECISION_MIXED}[precision]
+        cfg.device = device
+        # Julia column-major matrices: pass the transpose's C buffer
+        cfg.nodes = _dptr(arr(b.nodes))
+        cfg.weights = _dptr(arr(b.weights))
+        cfg.inverse_weights = _dptr(arr(b.inverse_weights))
+        cfg.derivative_hat = _dptr(arr(np.asfortranarray(b.derivative_hat).ravel(order="F")))
+        cfg.derivative_split = _dptr(arr(np.asfortranarray(b.derivative_split).ravel(order="F")))
+        cfg.inverse_vandermonde_legendre = _dptr(
+            arr(np.asfortranarray(b.inverse_vandermonde_legendre).ravel(order="F")))
+        cfg.neighbor_ids = arr(nb, np.int64).ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        cfg.orientations = arr(orient, np.int64).ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        cfg.inverse_jacobian = _dptr(arr(semi.inverse_jacobian))
+        cfg.node_coordinates = _dptr(arr(semi.node_coordinates))
+        cfg.elements_per_block = int(elements_per_block)
+        h = ctypes.c_void_p()
+        _lib.check(lib.tg_ctx_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+        self.precision = precision
+        self.t = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.tg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        _lib.check(rc, self.h)
+
+    # -- state --------------------------------------------------------------
+    def upload(self, u):
+        if isinstance(u, np.ndarray):
+            u = np.ascontiguousarray(u, dtype=np.float64)
+            assert u.size == self.semi.nvalues
+        self._check(self.lib.tg_upload_state(self.h, _ptr_of(u)))
+
+    def download(self, out=None):
+        if out is None:
+            out = np.empty(self.semi.u_shape)
+        self._check(self.lib.tg_download_state(self.h, _ptr_of(out)))
+        return out
+
+    def state_ptr(self) -> int:
+        p = ctypes.c_void_p()
+        self._check(self.lib.tg_state_device_ptr(self.h, ctypes.byref(p)))
+        return p.value
+
+    # -- evaluations --------------------------------------------------------
+    def rhs(self, du, u, t):
+        """rhs! with device buffers (torch CUDA tensors or raw device addresses)."""
+        self._check(self.lib.tg_rhs(self.h, _ptr_of(du), _ptr_of(u), float(t)))
+
+    def rhs_host(self, u, t=0.0):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        du = np.empty_like(u)
+        self._check(self.lib.tg_rhs_host(self.h, _ptr_of(du), _ptr_of(u), float(t)))
+        return du
+
+    def max_dt(self, u=None) -> float:
+        dt = ctypes.c_double()
+        self._check(self.lib.tg_max_dt(self.h, None if u is None else _ptr_of(u), ctypes.byref(dt)))
+        return dt.value
+
+    def rk_stage(self, stage, t, dt):
+        self._check(self.lib.tg_rk_stage(self.h, int(stage), float(t), float(dt)))
+
+    def step(self, max_steps, cfl, t_end, t):
+        tt = ctypes.c_double(t)
+        n = ctypes.c_int64(0)
+        self._check(self.lib.tg_step(self.h, int(max_steps), float(cfl), float(t_end),
+                                     ctypes.byref(tt), ctypes.byref(n)))
+        return tt.value, n.value
+
+    def integrals(self):
+        out = np.zeros(self.semi.equations.nvariables + 2)
+        self._check(self.lib.tg_integrals(self.h, _dptr(out)))
+        return out
+
+    def alpha(self, u=None):
+        a = np.zeros(self.semi.nelements)
+        self._check(self.lib.tg_alpha(self.h, None if u is None else _ptr_of(u), _dptr(a)))
+        return a
+
+    def status(self) -> int:
+        f = ctypes.c_int32()
+        self._check(self.lib.tg_status(self.h, ctypes.byref(f)))
+        return f.value
+
+    def synchronize(self):
+        self._check(self.lib.tg_synchronize(self.h))
+
+    def stream(self) -> int:
+        """cudaStream_t of the context (for torch.cuda.ExternalStream)."""
+        p = ctypes.c_void_p()
+        self._check(self.lib.tg_stream(self.h, ctypes.byref(p)))
+        return p.value
+
+    def elements_per_block(self) -> int:
+        v = ctypes.c_int32()
+        self._check(self.lib.tg_elements_per_block(self.h, ctypes.byref(v)))
+        return v.value
+
+
+class SemidiscretizationHyperbolic:
+    """SemidiscretizationHyperbolic(mesh, equations, initial_condition, solver;
+    source_terms, boundary_conditions), semidiscretization_hyperbolic.jl:50-76."""
+
+    def __init__(self, mesh: TreeMesh, equations: CompressibleEulerEquations2D, initial_condition,
+                 solver: DGSEM, source_terms=None, boundary_conditions=boundary_condition_periodic,
+                 precision="fp64", device=0, elements_per_block=0):
+        if mesh.ndims != equations.ndims:
+            raise ValueError("mesh and equations have different dimensions")
+        if not isinstance(boundary_conditions, BoundaryConditionPeriodic):
+            raise NotImplementedError("only periodic boundary conditions are on the GPU path")
+        if precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.mesh, self.equations, self.solver = mesh, equations, solver
+        self.initial_condition = initial_condition
+        self.source_terms = source_terms
+        self.precision = precision
+        self.device, self.elements_per_block = device, elements_per_block
+        D, n = equations.ndims, solver.nnodes()
+        self.nelements = mesh.nelements
+        self.nnodes_per_element = n ** D
+        self.ndofs = self.nelements * self.nnodes_per_element
+        self.nvalues = self.ndofs * equations.nvariables
+        self.u_shape = (self.nelements,) + (n,) * D + (equations.nvariables,)
+        # init_elements!, containers_2d.jl:85-127
+        b = solver.basis
+        reference_length = 0.0
+        for w in b.weights:
+            reference_length += 1.0 * w
+        reference_offset = (b.nodes[0] + b.nodes[-1]) / 2
+        dx = mesh.element_length()
+        jac = dx / reference_length
+        self.inverse_jacobian = np.full(self.nelements, 1.0 / jac)
+        centers = mesh.cell_centers()
+        X = np.empty((self.nelements,) + (n,) * D + (D,))
+        rel = jac * (b.nodes - reference_offset)
+        for d in range(D):
+            # axis of node index along d in the (e, k, j, i) array order
+            ax = D - d
+            shape = [1] * (D + 1)
+            shape[ax] = n
+            X[..., d] = centers[:, d].reshape((-1,) + (1,) * D) + rel.reshape(shape)
+        self.node_coordinates = X
+        self.neighbor_ids, self.orientations = mesh.interfaces()
+        self._ctx = None
+
+    @property
+    def device_context(self) -> DeviceContext:
+        if self._ctx is None:
+            self._ctx = DeviceContext(self, self.precision, self.device, self.elements_per_block)
+        return self._ctx
+
+    def compute_coefficients(self, t=0.0):
+        """compute_coefficients(t, semi): the initial condition at the nodes (dg.jl:1280-1325)."""
+        return np.ascontiguousarray(self.initial_condition(self.node_coordinates, t, self.equations))
+
+    def rhs(self, du, u, t):
+        """rhs!(du, u, semi, t) with device buffers."""
+        self.device_context.rhs(du, u, t)
+
+    def __repr__(self):
+        return (f"SemidiscretizationHyperbolic({self.mesh!r}, {self.equations!r}, {self.solver!r}, "
+                f"precision={self.precision})")
+
+
+class ODEProblem:
+    def __init__(self, f, u0, tspan, p):
+        self.f, self.u0, self.tspan, self.p = f, u0, tuple(float(x) for x in tspan), p
+
+
+def semidiscretize(semi: SemidiscretizationHyperbolic, tspan) -> ODEProblem:
+    """semidiscretize(semi, tspan), semidiscretization.jl:102-153."""
+    u0 = semi.compute_coefficients(tspan[0])
+    return ODEProblem(semi.rhs, u0, tspan, semi)
