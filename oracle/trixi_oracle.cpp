@@ -971,7 +971,8 @@ static void rk_update(int64_t ndof, double* u, double* u_tmp, const double* du, 
 
 // Julia isapprox(a, b) with default rtol = sqrt(eps)
 static bool isapprox(double a, double b) {
-  return a == b || std::fabs(a - b) <= 1.4901161193847656e-08 * std::max(std::fabs(a), std::fabs(b));
+  return a == b || (std::isfinite(a) && std::isfinite(b) &&
+                    std::fabs(a - b) <= 1.4901161193847656e-08 * std::max(std::fabs(a), std::fabs(b)));
 }
 
 }  // namespace orc

@@ -88,8 +88,10 @@ def test_conservation_to_roundoff(c, precision):
     W = np.einsum("j,i->ji", b.weights, b.weights) if D == 2 else \
         np.einsum("k,j,i->kji", b.weights, b.weights, b.weights)
     J = (1.0 / semi.inverse_jacobian) ** D
-    tot = np.einsum("e...v,...,e->v", du, W, J)
-    scale = np.einsum("e...v,...,e->v", np.abs(du), W, J)
+    nv = du.shape[-1]
+    wj = (J[:, None] * W.reshape(1, -1)).reshape(-1, 1)
+    tot = np.sum(du.reshape(-1, nv) * wj, axis=0)
+    scale = np.sum(np.abs(du.reshape(-1, nv)) * wj, axis=0)
     tol = 1e-13 if precision == "fp64" else 1e-6
     assert np.all(np.abs(tot) <= tol * scale)
 

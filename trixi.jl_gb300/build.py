@@ -23,8 +23,8 @@ LIB = os.path.join(BUILD, "libtrixi_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE,
           "-Xptxas", "-warn-spills"]
-# FP32 units: approximate division/sqrt and flush-to-zero for the FP32 flux
-# arithmetic (FP64 operations in the same units are unaffected).
+# Mixed-precision units: approximate FP32 division/sqrt and flush-to-zero for
+# the FP32 flux arithmetic.
 FP32_FLAGS = ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
 
 
@@ -49,7 +49,7 @@ def _compile(src: str, force: bool) -> str:
     if not force and os.path.exists(obj) and os.path.getmtime(obj) >= newest:
         return obj
     flags = list(COMMON)
-    if "_f32_" in os.path.basename(src):
+    if "_mixed_" in os.path.basename(src):
         flags += FP32_FLAGS
     cmd = [_nvcc()] + ARCH + flags + ["-c", src, "-o", obj]
     res = subprocess.run(cmd, capture_output=True, text=True)

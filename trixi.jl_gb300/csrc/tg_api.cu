@@ -18,7 +18,7 @@
 #include <vector>
 
 #include "../../include/trixi_gb300.h"
-#include "tg_dg.cuh"
+#include "tg_mixed.cuh"
 
 namespace tg {
 
@@ -27,34 +27,43 @@ namespace tg {
   int launch_element_##D##d_##R##_##V(int N, int epb, const DgParams& P, const StageArgs& A, \
                                       cudaStream_t s);
 TG_DECL(2, f64, weak) TG_DECL(2, f64, fd) TG_DECL(2, f64, hg)
-TG_DECL(2, f32, weak) TG_DECL(2, f32, fd) TG_DECL(2, f32, hg)
 TG_DECL(3, f64, weak) TG_DECL(3, f64, fd) TG_DECL(3, f64, hg)
-TG_DECL(3, f32, weak) TG_DECL(3, f32, fd) TG_DECL(3, f32, hg)
 #undef TG_DECL
+#define TG_DECLM(D, V)                                                              \
+  int launch_mixed_##D##d_##V(int N, int epb, const MixedParams& P, const MixedArgs& A, \
+                              cudaStream_t s);
+TG_DECLM(2, weak) TG_DECLM(2, fd) TG_DECLM(2, hg)
+TG_DECLM(3, weak) TG_DECLM(3, fd) TG_DECLM(3, hg)
+#undef TG_DECLM
 int launch_indicator_2d_f64_hg(int N, const DgParams& P, const double* u, void* a, cudaStream_t s);
-int launch_indicator_2d_f32_hg(int N, const DgParams& P, const double* u, void* a, cudaStream_t s);
 int launch_indicator_3d_f64_hg(int N, const DgParams& P, const double* u, void* a, cudaStream_t s);
-int launch_indicator_3d_f32_hg(int N, const DgParams& P, const double* u, void* a, cudaStream_t s);
+int launch_indicator_mixed_2(int N, const MixedParams& P, const float2* u, float* a, cudaStream_t s);
+int launch_indicator_mixed_3(int N, const MixedParams& P, const float2* u, float* a, cudaStream_t s);
 
 int launch_element(int D, int N, bool fp64, int vi, int epb, const DgParams& P,
                    const StageArgs& A, cudaStream_t s) {
   typedef int (*Fn)(int, int, const DgParams&, const StageArgs&, cudaStream_t);
-  static const Fn table[2][2][3] = {
-      {{launch_element_2d_f32_weak, launch_element_2d_f32_fd, launch_element_2d_f32_hg},
-       {launch_element_2d_f64_weak, launch_element_2d_f64_fd, launch_element_2d_f64_hg}},
-      {{launch_element_3d_f32_weak, launch_element_3d_f32_fd, launch_element_3d_f32_hg},
-       {launch_element_3d_f64_weak, launch_element_3d_f64_fd, launch_element_3d_f64_hg}}};
+  static const Fn table[2][3] = {
+      {launch_element_2d_f64_weak, launch_element_2d_f64_fd, launch_element_2d_f64_hg},
+      {launch_element_3d_f64_weak, launch_element_3d_f64_fd, launch_element_3d_f64_hg}};
+  if (D < 2 || D > 3 || vi < 0 || vi > 2 || !fp64) return -2;
+  return table[D - 2][vi](N, epb, P, A, s);
+}
+
+static int launch_mixed(int D, int N, int vi, int epb, const MixedParams& P, const MixedArgs& A,
+                        cudaStream_t s) {
+  typedef int (*Fn)(int, int, const MixedParams&, const MixedArgs&, cudaStream_t);
+  static const Fn table[2][3] = {{launch_mixed_2d_weak, launch_mixed_2d_fd, launch_mixed_2d_hg},
+                                 {launch_mixed_3d_weak, launch_mixed_3d_fd, launch_mixed_3d_hg}};
   if (D < 2 || D > 3 || vi < 0 || vi > 2) return -2;
-  return table[D - 2][fp64 ? 1 : 0][vi](N, epb, P, A, s);
+  return table[D - 2][vi](N, epb, P, A, s);
 }
 
 int launch_indicator(int D, int N, bool fp64, const DgParams& P, const double* u,
                      void* alpha_raw, cudaStream_t s) {
-  if (D == 2)
-    return fp64 ? launch_indicator_2d_f64_hg(N, P, u, alpha_raw, s)
-                : launch_indicator_2d_f32_hg(N, P, u, alpha_raw, s);
-  return fp64 ? launch_indicator_3d_f64_hg(N, P, u, alpha_raw, s)
-              : launch_indicator_3d_f32_hg(N, P, u, alpha_raw, s);
+  if (!fp64) return -2;
+  return D == 2 ? launch_indicator_2d_f64_hg(N, P, u, alpha_raw, s)
+                : launch_indicator_3d_f64_hg(N, P, u, alpha_raw, s);
 }
 
 int default_epb(int D, int N) {
@@ -88,9 +97,27 @@ bool supported_epb(int D, int N, int epb) {
 // Small kernels: CFL reduction, clock, integrals, smoothing
 // ---------------------------------------------------------------------------
 
+__device__ __forceinline__ double state_f64(double x) { return x; }
+__device__ __forceinline__ double state_f64(float2 x) { return (double)x.x + (double)x.y; }
+
+// FP64 <-> float-float conversion of the state (mixed path boundary)
+__global__ void to_ff_kernel(const double* __restrict__ in, float2* __restrict__ out, int64_t n) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const double x = in[k];
+    const float hi = __double2float_rn(x);
+    out[k] = make_float2(hi, __double2float_rn(x - (double)hi));
+  }
+}
+__global__ void from_ff_kernel(const float2* __restrict__ in, double* __restrict__ out, int64_t n) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = state_f64(in[k]);
+}
+
 // max_dt's reduction (stepsize_dg2d.jl:8-30): max_e invJ_e * sum_d max_nodes lambda_d.
-template <int D>
-__global__ void max_speed_kernel(const double* __restrict__ u, const double* __restrict__ inv_jac,
+template <int D, typename TS>
+__global__ void max_speed_kernel(const TS* __restrict__ u, const double* __restrict__ inv_jac,
                                  int64_t E, int NN, double gamma,
                                  unsigned long long* __restrict__ speed_bits,
                                  int32_t* __restrict__ status) {
@@ -101,9 +128,9 @@ __global__ void max_speed_kernel(const double* __restrict__ u, const double* __r
   for (int d = 0; d < D; ++d) ml[d] = 0;
   bool bad = false;
   for (int q = 0; q < NN; ++q) {
-    const double* p = u + ((size_t)e * NN + q) * NV;
+    const TS* p = u + ((size_t)e * NN + q) * NV;
     double uu[NV], w[NV];
-    for (int v = 0; v < NV; ++v) uu[v] = p[v];
+    for (int v = 0; v < NV; ++v) uu[v] = state_f64(p[v]);
     Euler<D, double>::cons2prim(uu, w, gamma);
     const double c = sqrt(gamma * w[NV - 1] / w[0]);
     bad |= !(w[0] > 0) || !(w[NV - 1] > 0);
@@ -171,7 +198,9 @@ __global__ void clock_begin_kernel(Clock* c) {
   c->skip = 0;
   const double tn = c->t + c->dt;
   const double te = c->t_end;
-  const bool approx = tn == te || fabs(tn - te) <= 1.4901161193847656e-08 * fmax(fabs(tn), fabs(te));
+  // Julia isapprox: exact equality, or finite operands within rtol = sqrt(eps)
+  const bool approx = tn == te || (isfinite(tn) && isfinite(te) &&
+                                   fabs(tn - te) <= 1.4901161193847656e-08 * fmax(fabs(tn), fabs(te)));
   if (tn > te || approx) {
     c->dt = te - c->t;
     c->finalstep = 1;
@@ -191,8 +220,8 @@ __global__ void clock_end_kernel(Clock* c, int n) {
 // Per-element FP64 integrals (integrate_via_indices, analysis_dg2d.jl:313-336):
 // conserved totals, mathematical entropy (compressible_euler_2d.jl:2236-2255)
 // and kinetic energy (:2297-2300).
-template <int D>
-__global__ void element_integrals_kernel(const double* __restrict__ u,
+template <int D, typename TS>
+__global__ void element_integrals_kernel(const TS* __restrict__ u,
                                          const double* __restrict__ inv_jac,
                                          const double* __restrict__ weights, int64_t E, int N,
                                          double gamma, double* __restrict__ partial) {
@@ -209,7 +238,8 @@ __global__ void element_integrals_kernel(const double* __restrict__ u,
     const int i = q % N, j = (q / N) % N, k = q / (N * N);
     double w = weights[i] * weights[j];
     if (D == 3) w *= weights[k];
-    const double* p = u + ((size_t)e * NN + q) * NV;
+    double p[NV];
+    for (int v = 0; v < NV; ++v) p[v] = state_f64(u[((size_t)e * NN + q) * NV + v]);
     double m2 = 0;
     for (int d = 0; d < D; ++d) m2 += p[1 + d] * p[1 + d];
     for (int v = 0; v < NV; ++v) acc[v] += vj * w * p[v];
@@ -276,17 +306,23 @@ struct tg_ctx {
   bool fp64 = true;
   int64_t E = 0, ndofs = 0, nvalues = 0;
   DgParams P{};
+  MixedParams MP{};
   cudaStream_t stream = nullptr;
-  double* d_u[2] = {nullptr, nullptr};
+  // state: FP64 values (fp64) or float-float pairs (mixed), 8 bytes per value
+  void* d_u[2] = {nullptr, nullptr};
   int cur = 0;
-  void* d_utmp = nullptr;
-  double* d_du = nullptr;
-  double* d_uscratch = nullptr;
+  void* d_utmp = nullptr;            // double (fp64) or float (mixed)
+  double* d_du = nullptr;            // tg_rhs_host scratch
+  double* d_uscratch = nullptr;      // tg_rhs_host scratch
+  double* d_stage64 = nullptr;       // mixed: FP64 staging of the state
+  float2* d_uff = nullptr;           // mixed: float-float copy of a tg_rhs input
   void* d_alpha_raw = nullptr;
   double* d_alpha = nullptr;
   int32_t* d_nbr = nullptr;
   double* d_invj = nullptr;
   double* d_xline = nullptr;
+  float* d_invj_f = nullptr;
+  float* d_xline_f = nullptr;
   double* d_weights = nullptr;
   double* d_partial = nullptr;
   double* d_sums = nullptr;
@@ -295,7 +331,6 @@ struct tg_ctx {
   unsigned long long* d_speed = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   bool clock_valid = false;
-  double clock_t = 0;
   bool uploaded = false;
   std::vector<double> weights;
   std::string err;
@@ -330,70 +365,137 @@ static void free_ctx(tg_ctx* c) {
   cudaSetDevice(c->device);
   for (int p = 0; p < 2; ++p)
     if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
-  void* ptrs[] = {c->d_u[0], c->d_u[1], c->d_utmp, c->d_du, c->d_uscratch, c->d_alpha_raw,
-                  c->d_alpha, c->d_nbr, c->d_invj, c->d_xline, c->d_weights, c->d_partial,
-                  c->d_sums, c->d_clock, c->d_status, c->d_speed};
+  void* ptrs[] = {c->d_u[0], c->d_u[1], c->d_utmp, c->d_du, c->d_uscratch, c->d_stage64,
+                  c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_nbr, c->d_invj, c->d_xline,
+                  c->d_invj_f, c->d_xline_f, c->d_weights, c->d_partial, c->d_sums, c->d_clock,
+                  c->d_status, c->d_speed};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
 
-// Element-chunk stage/rhs launch with the context's parameters.
-static int launch(tg_ctx* c, const StageArgs& A) {
-  const int rc = launch_element(c->D, c->N, c->fp64, c->vi, c->epb, c->P, A, c->stream);
-  if (rc != 0) {
-    cudaError_t e = cudaGetLastError();
-    return fail(c, TG_ERR_CUDA, "element kernel launch failed (%d): %s", rc,
-                cudaGetErrorString(e));
-  }
+static unsigned conv_blocks(int64_t n) {
+  return (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16);
+}
+
+static int ensure(tg_ctx* c, void** p, size_t bytes) {
+  if (!*p) CUDA_TRY(c, cudaMalloc(p, bytes));
   return TG_OK;
 }
 
-static int indicator(tg_ctx* c, const double* u) {
+// FP64 state (Trixi layout) -> context representation in `dst`
+static int import_state(tg_ctx* c, const double* src, void* dst) {
+  if (c->fp64) {
+    if (src != dst)
+      CUDA_TRY(c, cudaMemcpyAsync(dst, src, sizeof(double) * c->nvalues, cudaMemcpyDeviceToDevice,
+                                  c->stream));
+    return TG_OK;
+  }
+  to_ff_kernel<<<conv_blocks(c->nvalues), 256, 0, c->stream>>>(src, (float2*)dst, c->nvalues);
+  CUDA_TRY(c, cudaGetLastError());
+  return TG_OK;
+}
+
+// Context state -> FP64 values (for mixed: into d_stage64); returns the FP64 pointer.
+static const double* export_state(tg_ctx* c, int* rc) {
+  *rc = TG_OK;
+  if (c->fp64) return (const double*)c->d_u[c->cur];
+  if ((*rc = ensure(c, (void**)&c->d_stage64, sizeof(double) * c->nvalues))) return nullptr;
+  from_ff_kernel<<<conv_blocks(c->nvalues), 256, 0, c->stream>>>((const float2*)c->d_u[c->cur],
+                                                                  c->d_stage64, c->nvalues);
+  if (cudaGetLastError() != cudaSuccess) {
+    *rc = fail(c, TG_ERR_CUDA, "state conversion launch failed");
+    return nullptr;
+  }
+  return c->d_stage64;
+}
+
+// HG indicator (unsmoothed) of a state in the context representation.
+static int indicator(tg_ctx* c, const void* u) {
   if (c->vi != VI_HG) return TG_OK;
-  const int rc = launch_indicator(c->D, c->N, c->fp64, c->P, u, c->d_alpha_raw, c->stream);
+  int rc;
+  if (c->fp64)
+    rc = launch_indicator(c->D, c->N, true, c->P, (const double*)u, c->d_alpha_raw, c->stream);
+  else if (c->D == 2)
+    rc = launch_indicator_mixed_2(c->N, c->MP, (const float2*)u, (float*)c->d_alpha_raw, c->stream);
+  else
+    rc = launch_indicator_mixed_3(c->N, c->MP, (const float2*)u, (float*)c->d_alpha_raw, c->stream);
   if (rc != 0) return fail(c, TG_ERR_CUDA, "indicator kernel launch failed (%d)", rc);
   return TG_OK;
 }
 
-static StageArgs base_args(tg_ctx* c) {
-  StageArgs A{};
-  A.alpha_raw = c->d_alpha_raw;
-  A.status = c->d_status;
-  A.clock = c->d_clock;
-  return A;
+// One element-kernel launch.  u_in is in the context representation.
+static int launch_kernel(tg_ctx* c, int mode, const void* u_in, void* u_out, double* du_out,
+                         double t_rhs, int stage, bool reduce) {
+  int rc;
+  if (c->fp64) {
+    StageArgs A{};
+    A.alpha_raw = c->d_alpha_raw;
+    A.status = c->d_status;
+    A.clock = c->d_clock;
+    A.mode = mode;
+    A.u_in = (const double*)u_in;
+    A.u_out = (double*)u_out;
+    A.du_out = du_out;
+    A.u_tmp = c->d_utmp;
+    A.t_rhs = t_rhs;
+    if (mode == MODE_STAGE) {
+      A.a = CK_A[stage];
+      A.b = CK_B[stage];
+      A.c = CK_C[stage];
+      A.zero_tmp = stage == 0;
+    }
+    A.speed_bits = reduce ? &c->d_clock->speed_bits : nullptr;
+    rc = launch_element(c->D, c->N, true, c->vi, c->epb, c->P, A, c->stream);
+  } else {
+    MixedArgs A{};
+    A.alpha_raw = (const float*)c->d_alpha_raw;
+    A.status = c->d_status;
+    A.clock = c->d_clock;
+    A.mode = mode;
+    A.u_in = (const float2*)u_in;
+    A.u_out = (float2*)u_out;
+    A.du_out = du_out;
+    A.u_tmp = (float*)c->d_utmp;
+    A.t_rhs = t_rhs;
+    if (mode == MODE_STAGE) {
+      A.a = CK_A[stage];
+      A.b = CK_B[stage];
+      A.c = CK_C[stage];
+      A.zero_tmp = stage == 0;
+    }
+    A.speed_bits = reduce ? &c->d_clock->speed_bits : nullptr;
+    rc = launch_mixed(c->D, c->N, c->vi, c->epb, c->MP, A, c->stream);
+  }
+  if (rc != 0) {
+    cudaError_t e = cudaGetLastError();
+    return fail(c, TG_ERR_CUDA, "element kernel launch failed (%d): %s", rc, cudaGetErrorString(e));
+  }
+  return TG_OK;
 }
 
 // Enqueue one fused 2N stage reading d_u[cur] and writing d_u[cur ^ 1].
 static int enqueue_stage(tg_ctx* c, int stage, bool reduce_speed) {
   int rc = indicator(c, c->d_u[c->cur]);
   if (rc) return rc;
-  StageArgs A = base_args(c);
-  A.mode = MODE_STAGE;
-  A.u_in = c->d_u[c->cur];
-  A.u_out = c->d_u[c->cur ^ 1];
-  A.u_tmp = c->d_utmp;
-  A.a = CK_A[stage];
-  A.b = CK_B[stage];
-  A.c = CK_C[stage];
-  A.zero_tmp = stage == 0;
-  A.speed_bits = reduce_speed ? &c->d_clock->speed_bits : nullptr;
-  rc = launch(c, A);
+  rc = launch_kernel(c, MODE_STAGE, c->d_u[c->cur], c->d_u[c->cur ^ 1], nullptr, 0.0, stage,
+                     reduce_speed);
   if (rc) return rc;
   c->cur ^= 1;
   return TG_OK;
 }
 
+// CFL reduction of an FP64 state (Trixi layout).
 static int reduce_speed(tg_ctx* c, const double* u, unsigned long long* dst) {
   speed_reset_kernel<<<1, 1, 0, c->stream>>>(dst);
   const int64_t nb = (c->E + 127) / 128;
   if (c->D == 2)
-    max_speed_kernel<2><<<(unsigned)nb, 128, 0, c->stream>>>(u, c->d_invj, c->E, c->NN, c->P.gamma,
-                                                            dst, c->d_status);
+    max_speed_kernel<2, double><<<(unsigned)nb, 128, 0, c->stream>>>(u, c->d_invj, c->E, c->NN,
+                                                                     c->P.gamma, dst, c->d_status);
   else
-    max_speed_kernel<3><<<(unsigned)nb, 128, 0, c->stream>>>(u, c->d_invj, c->E, c->NN, c->P.gamma,
-                                                            dst, c->d_status);
+    max_speed_kernel<3, double><<<(unsigned)nb, 128, 0, c->stream>>>(u, c->d_invj, c->E, c->NN,
+                                                                     c->P.gamma, dst, c->d_status);
   CUDA_TRY(c, cudaGetLastError());
   return TG_OK;
 }
@@ -573,7 +675,21 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     ALLOC(c->d_alpha_raw, rsize(c) * c->E);
     ALLOC(c->d_alpha, sizeof(double) * c->E);
   }
+  std::vector<float> invj_f, xline_f;
+  if (!c->fp64) {
+    invj_f.resize(c->E);
+    for (int64_t k = 0; k < c->E; ++k) invj_f[k] = (float)cfg->inverse_jacobian[k];
+    xline_f.assign(xline.begin(), xline.end());
+    ALLOC(c->d_invj_f, sizeof(float) * c->E);
+    if (!xline_f.empty()) ALLOC(c->d_xline_f, sizeof(float) * xline_f.size());
+  }
 #undef ALLOC
+  if (!c->fp64) {
+    cudaMemcpy(c->d_invj_f, invj_f.data(), sizeof(float) * c->E, cudaMemcpyHostToDevice);
+    if (!xline_f.empty())
+      cudaMemcpy(c->d_xline_f, xline_f.data(), sizeof(float) * xline_f.size(),
+                 cudaMemcpyHostToDevice);
+  }
   cudaMemcpy(c->d_nbr, nbr.data(), sizeof(int32_t) * nbr.size(), cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_invj, cfg->inverse_jacobian, sizeof(double) * c->E, cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_weights, c->weights.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
@@ -590,6 +706,30 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   P.nbr = c->d_nbr;
   P.inv_jac = c->d_invj;
   P.xline = c->d_xline;
+  // single-precision copy of the parameters for the mixed path
+  MixedParams& M = c->MP;
+  M.nelements = P.nelements;
+  M.gamma = (float)P.gamma;
+  M.inv_gamma_minus_one = (float)P.inv_gamma_minus_one;
+  for (int k = 0; k < MAXN; ++k) M.inv_weights[k] = (float)P.inv_weights[k];
+  for (int k = 0; k < MAXN * MAXN; ++k) {
+    M.Dhat[k] = (float)P.Dhat[k];
+    M.Dsplit[k] = (float)P.Dsplit[k];
+    M.Vinv[k] = (float)P.Vinv[k];
+  }
+  M.volume_flux = P.volume_flux;
+  M.surface_flux = P.surface_flux;
+  M.fv_flux = P.fv_flux;
+  M.source = P.source;
+  M.alpha_max = (float)P.alpha_max;
+  M.alpha_min = (float)P.alpha_min;
+  M.alpha_atol = (float)P.alpha_atol;
+  M.hg_threshold = (float)P.hg_threshold;
+  M.hg_parameter_s = (float)P.hg_parameter_s;
+  M.alpha_smooth = P.alpha_smooth;
+  M.nbr = c->d_nbr;
+  M.inv_jac = c->d_invj_f;
+  M.xline = c->d_xline_f;
   *out = c;
   return TG_OK;
 }
@@ -618,8 +758,16 @@ int tg_elements_per_block(const tg_ctx* ctx, int32_t* epb) {
 int tg_upload_state(tg_ctx* c, const double* u_host) {
   if (!c || !u_host) return TG_ERR_INVALID_ARGUMENT;
   CUDA_TRY(c, cudaSetDevice(c->device));
-  CUDA_TRY(c, cudaMemcpyAsync(c->d_u[c->cur], u_host, sizeof(double) * c->nvalues,
-                              cudaMemcpyHostToDevice, c->stream));
+  const size_t vb = sizeof(double) * c->nvalues;
+  if (c->fp64) {
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_u[c->cur], u_host, vb, cudaMemcpyHostToDevice, c->stream));
+  } else {
+    int rc = ensure(c, (void**)&c->d_stage64, vb);
+    if (rc) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_stage64, u_host, vb, cudaMemcpyHostToDevice, c->stream));
+    rc = import_state(c, c->d_stage64, c->d_u[c->cur]);
+    if (rc) return rc;
+  }
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   c->uploaded = true;
   c->clock_valid = false;
@@ -629,15 +777,18 @@ int tg_upload_state(tg_ctx* c, const double* u_host) {
 int tg_download_state(tg_ctx* c, double* u_host) {
   if (!c || !u_host) return TG_ERR_INVALID_ARGUMENT;
   CUDA_TRY(c, cudaSetDevice(c->device));
-  CUDA_TRY(c, cudaMemcpyAsync(u_host, c->d_u[c->cur], sizeof(double) * c->nvalues,
-                              cudaMemcpyDeviceToHost, c->stream));
+  int rc;
+  const double* src = export_state(c, &rc);
+  if (rc) return rc;
+  CUDA_TRY(c, cudaMemcpyAsync(u_host, src, sizeof(double) * c->nvalues, cudaMemcpyDeviceToHost,
+                              c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return TG_OK;
 }
 
 int tg_state_device_ptr(tg_ctx* c, double** u_dev) {
   if (!c || !u_dev) return TG_ERR_INVALID_ARGUMENT;
-  *u_dev = c->d_u[c->cur];
+  *u_dev = (double*)c->d_u[c->cur];
   return TG_OK;
 }
 
@@ -645,24 +796,29 @@ int tg_rhs(tg_ctx* c, double* du_dev, const double* u_dev, double t) {
   if (!c || !du_dev || !u_dev) return TG_ERR_INVALID_ARGUMENT;
   if ((const double*)du_dev == u_dev) return fail(c, TG_ERR_INVALID_ARGUMENT, "du aliases u");
   CUDA_TRY(c, cudaSetDevice(c->device));
-  int rc = indicator(c, u_dev);
+  const void* u_in = u_dev;
+  if (!c->fp64) {
+    int rc = ensure(c, (void**)&c->d_uff, sizeof(float2) * c->nvalues);
+    if (rc) return rc;
+    rc = import_state(c, u_dev, c->d_uff);
+    if (rc) return rc;
+    u_in = c->d_uff;
+  }
+  int rc = indicator(c, u_in);
   if (rc) return rc;
-  StageArgs A = base_args(c);
-  A.mode = MODE_RHS;
-  A.u_in = u_dev;
-  A.du_out = du_dev;
-  A.t_rhs = t;
-  return launch(c, A);
+  return launch_kernel(c, MODE_RHS, u_in, nullptr, du_dev, t, 0, false);
 }
 
 int tg_rhs_host(tg_ctx* c, double* du_host, const double* u_host, double t) {
   if (!c || !du_host || !u_host) return TG_ERR_INVALID_ARGUMENT;
   CUDA_TRY(c, cudaSetDevice(c->device));
   const size_t vb = sizeof(double) * c->nvalues;
-  if (!c->d_uscratch) CUDA_TRY(c, cudaMalloc((void**)&c->d_uscratch, vb));
-  if (!c->d_du) CUDA_TRY(c, cudaMalloc((void**)&c->d_du, vb));
+  int rc = ensure(c, (void**)&c->d_uscratch, vb);
+  if (rc) return rc;
+  rc = ensure(c, (void**)&c->d_du, vb);
+  if (rc) return rc;
   CUDA_TRY(c, cudaMemcpyAsync(c->d_uscratch, u_host, vb, cudaMemcpyHostToDevice, c->stream));
-  int rc = tg_rhs(c, c->d_du, c->d_uscratch, t);
+  rc = tg_rhs(c, c->d_du, c->d_uscratch, t);
   if (rc) return rc;
   CUDA_TRY(c, cudaMemcpyAsync(du_host, c->d_du, vb, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -672,7 +828,10 @@ int tg_rhs_host(tg_ctx* c, double* du_host, const double* u_host, double t) {
 int tg_max_dt(tg_ctx* c, const double* u_dev, double* dt) {
   if (!c || !dt) return TG_ERR_INVALID_ARGUMENT;
   CUDA_TRY(c, cudaSetDevice(c->device));
-  int rc = reduce_speed(c, u_dev ? u_dev : c->d_u[c->cur], c->d_speed);
+  int rc = TG_OK;
+  const double* u = u_dev ? u_dev : export_state(c, &rc);
+  if (rc) return rc;
+  rc = reduce_speed(c, u, c->d_speed);
   if (rc) return rc;
   unsigned long long bits = 0;
   CUDA_TRY(c, cudaMemcpyAsync(&bits, c->d_speed, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
@@ -703,7 +862,7 @@ int tg_stream(tg_ctx* c, void** stream) {
 int tg_set_time(tg_ctx* c, double t) {
   if (!c) return TG_ERR_INVALID_ARGUMENT;
   c->clock_valid = false;
-  c->clock_t = t;
+  (void)t;
   return TG_OK;
 }
 
@@ -741,7 +900,10 @@ int tg_step(tg_ctx* c, int64_t max_steps, double cfl, double t_end, double* t_in
     }
   if (!c->clock_valid) {
     // initialize!(StepsizeCallback): dt = cfl * max_dt(u0)
-    int rc = reduce_speed(c, c->d_u[c->cur], &c->d_clock->speed_bits);
+    int rc = TG_OK;
+    const double* u64 = export_state(c, &rc);
+    if (rc) return rc;
+    rc = reduce_speed(c, u64, &c->d_clock->speed_bits);
     if (rc) return rc;
     clock_init_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, *t_inout, t_end, cfl, c->N);
     CUDA_TRY(c, cudaGetLastError());
@@ -781,12 +943,23 @@ int tg_integrals(tg_ctx* c, double* out) {
   const int K = c->NV + 2;
   if (!c->d_partial) CUDA_TRY(c, cudaMalloc((void**)&c->d_partial, sizeof(double) * K * c->E));
   const int64_t nb = (c->E + 127) / 128;
-  if (c->D == 2)
-    element_integrals_kernel<2><<<(unsigned)nb, 128, 0, c->stream>>>(
-        c->d_u[c->cur], c->d_invj, c->d_weights, c->E, c->N, c->P.gamma, c->d_partial);
-  else
-    element_integrals_kernel<3><<<(unsigned)nb, 128, 0, c->stream>>>(
-        c->d_u[c->cur], c->d_invj, c->d_weights, c->E, c->N, c->P.gamma, c->d_partial);
+  if (c->fp64) {
+    const double* u = (const double*)c->d_u[c->cur];
+    if (c->D == 2)
+      element_integrals_kernel<2, double><<<(unsigned)nb, 128, 0, c->stream>>>(
+          u, c->d_invj, c->d_weights, c->E, c->N, c->P.gamma, c->d_partial);
+    else
+      element_integrals_kernel<3, double><<<(unsigned)nb, 128, 0, c->stream>>>(
+          u, c->d_invj, c->d_weights, c->E, c->N, c->P.gamma, c->d_partial);
+  } else {
+    const float2* u = (const float2*)c->d_u[c->cur];
+    if (c->D == 2)
+      element_integrals_kernel<2, float2><<<(unsigned)nb, 128, 0, c->stream>>>(
+          u, c->d_invj, c->d_weights, c->E, c->N, c->P.gamma, c->d_partial);
+    else
+      element_integrals_kernel<3, float2><<<(unsigned)nb, 128, 0, c->stream>>>(
+          u, c->d_invj, c->d_weights, c->E, c->N, c->P.gamma, c->d_partial);
+  }
   sum_rows_kernel<<<1, 256, 256 * sizeof(double), c->stream>>>(c->d_partial, c->E, K, c->d_sums);
   CUDA_TRY(c, cudaGetLastError());
   CUDA_TRY(c, cudaMemcpyAsync(out, c->d_sums, sizeof(double) * K, cudaMemcpyDeviceToHost, c->stream));
@@ -798,7 +971,18 @@ int tg_alpha(tg_ctx* c, const double* u_dev, double* alpha_host) {
   if (!c || !alpha_host) return TG_ERR_INVALID_ARGUMENT;
   if (c->vi != VI_HG) return fail(c, TG_ERR_STATE, "context has no shock-capturing indicator");
   CUDA_TRY(c, cudaSetDevice(c->device));
-  int rc = indicator(c, u_dev ? u_dev : c->d_u[c->cur]);
+  const void* u_in = c->d_u[c->cur];
+  if (u_dev) {
+    u_in = u_dev;
+    if (!c->fp64) {
+      int rc = ensure(c, (void**)&c->d_uff, sizeof(float2) * c->nvalues);
+      if (rc) return rc;
+      rc = import_state(c, u_dev, c->d_uff);
+      if (rc) return rc;
+      u_in = c->d_uff;
+    }
+  }
+  int rc = indicator(c, u_in);
   if (rc) return rc;
   const int64_t nb = (c->E + 127) / 128;
   if (c->fp64)

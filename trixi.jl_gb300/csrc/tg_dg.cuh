@@ -482,9 +482,13 @@ __global__ void __launch_bounds__(EPB * Pow<N, D>::value)
 // Hennemann-Gassner indicator (unsmoothed), one thread per node:
 // indicators.jl:114-148, indicators_2d.jl:30-101, indicators_3d.jl:39-123.
 // ---------------------------------------------------------------------------
-template <int D, int N, typename R, int EPB>
+__device__ __forceinline__ double state_value(double x) { return x; }
+__device__ __forceinline__ float state_value(float2 x) { return x.x; }
+
+// PT: DgParams (FP64 path) or MixedParams; TS: double or float2 (float-float) state.
+template <int D, int N, typename R, int EPB, typename PT, typename TS>
 __global__ void __launch_bounds__(EPB * Pow<N, D>::value)
-    hg_indicator_kernel(const DgParams P, const double* __restrict__ u, R* __restrict__ alpha_raw) {
+    hg_indicator_kernel(const PT P, const TS* __restrict__ u, R* __restrict__ alpha_raw) {
   constexpr int NV = D + 2, NN = Pow<N, D>::value, NT = EPB * NN;
   __shared__ R s_a[EPB * NN], s_b[EPB * NN], s_v[N * N];
   const int tid = threadIdx.x;
@@ -496,9 +500,9 @@ __global__ void __launch_bounds__(EPB * Pow<N, D>::value)
   for (int k = tid; k < N * N; k += NT) s_v[k] = (R)P.Vinv[k];
   if (active) {
     R uu[NV];
-    const double* p = u + ((size_t)e * NN + node) * NV;
+    const TS* p = u + ((size_t)e * NN + node) * NV;
 #pragma unroll
-    for (int v = 0; v < NV; ++v) uu[v] = (R)p[v];
+    for (int v = 0; v < NV; ++v) uu[v] = (R)state_value(p[v]);
     s_a[tid] = Euler<D, R>::density_pressure(uu, (R)P.gamma);
   }
   __syncthreads();

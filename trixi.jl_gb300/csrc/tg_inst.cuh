@@ -1,5 +1,5 @@
-// Explicit instantiation of the element kernels for one (dimension, compute
-// type, volume integral) triple.  Each tg_inst_*.cu unit defines TG_D,
+// Explicit instantiation of the FP64 element kernels for one (dimension,
+// volume integral) pair.  Each tg_inst_*.cu unit defines TG_D,
 // TG_REAL and TG_VI and includes this file, so the instantiations compile in
 // parallel.
 #include "tg_dg.cuh"
@@ -65,7 +65,7 @@ template <int D, int N, typename R, int EPB>
 static int launch_ind(const DgParams& P, const double* u, void* alpha, cudaStream_t s) {
   const int64_t nblocks = (P.nelements + EPB - 1) / EPB;
   if (nblocks <= 0) return 0;
-  hg_indicator_kernel<D, N, R, EPB>
+  hg_indicator_kernel<D, N, R, EPB, DgParams, double>
       <<<(unsigned)nblocks, EPB * Pow<N, D>::value, 0, s>>>(P, u, reinterpret_cast<R*>(alpha));
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -1,0 +1,88 @@
+// Explicit instantiation of the mixed-precision element kernels (tg_mixed.cuh)
+// for one (dimension, volume integral) pair; each tg_inst_*_mixed_*.cu unit
+// defines TG_D, TG_VI and TG_SUFFIX and includes this file.
+#include "tg_mixed.cuh"
+
+namespace tg {
+
+template <int D, int N, int VI, int EPB>
+static int launch_mixed_one(const MixedParams& P, const MixedArgs& A, cudaStream_t s) {
+  using K = MixedKernel<D, N, VI, EPB>;
+  auto kern = mixed_element_kernel<D, N, VI, EPB>;
+  static bool configured = false;
+  const size_t smem = K::smem_bytes();
+  if (!configured) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return -1;
+    configured = true;
+  }
+  const int64_t nblocks = (P.nelements + EPB - 1) / EPB;
+  if (nblocks <= 0) return 0;
+  kern<<<(unsigned)nblocks, K::NT, smem, s>>>(P, A);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+#define TG_CAT2(a, b) a##b
+#define TG_CAT(a, b) TG_CAT2(a, b)
+
+int TG_CAT(launch_mixed_, TG_SUFFIX)(int N, int epb, const MixedParams& P, const MixedArgs& A,
+                                     cudaStream_t s) {
+#if TG_D == 2
+  switch (N) {
+    case 2: return launch_mixed_one<2, 2, TG_VI, 64>(P, A, s);
+    case 3: return launch_mixed_one<2, 3, TG_VI, 28>(P, A, s);
+    case 4:
+      if (epb == 8) return launch_mixed_one<2, 4, TG_VI, 8>(P, A, s);
+      if (epb == 32) return launch_mixed_one<2, 4, TG_VI, 32>(P, A, s);
+      return launch_mixed_one<2, 4, TG_VI, 16>(P, A, s);
+    case 5: return launch_mixed_one<2, 5, TG_VI, 10>(P, A, s);
+    case 6: return launch_mixed_one<2, 6, TG_VI, 7>(P, A, s);
+  }
+#else
+  switch (N) {
+    case 2: return launch_mixed_one<3, 2, TG_VI, 32>(P, A, s);
+    case 3: return launch_mixed_one<3, 3, TG_VI, 9>(P, A, s);
+    case 4:
+      if (epb == 2) return launch_mixed_one<3, 4, TG_VI, 2>(P, A, s);
+      if (epb == 8) return launch_mixed_one<3, 4, TG_VI, 8>(P, A, s);
+      return launch_mixed_one<3, 4, TG_VI, 4>(P, A, s);
+    case 5: return launch_mixed_one<3, 5, TG_VI, 2>(P, A, s);
+  }
+#endif
+  return -2;
+}
+
+#if TG_VI == 2
+template <int D, int N, int EPB>
+static int launch_ind_mixed(const MixedParams& P, const float2* u, float* alpha, cudaStream_t s) {
+  const int64_t nblocks = (P.nelements + EPB - 1) / EPB;
+  if (nblocks <= 0) return 0;
+  hg_indicator_kernel<D, N, float, EPB, MixedParams, float2>
+      <<<(unsigned)nblocks, EPB * Pow<N, D>::value, 0, s>>>(P, u, alpha);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int TG_CAT(launch_indicator_mixed_, TG_D)(int N, const MixedParams& P, const float2* u,
+                                          float* alpha, cudaStream_t s) {
+#if TG_D == 2
+  switch (N) {
+    case 2: return launch_ind_mixed<2, 2, 64>(P, u, alpha, s);
+    case 3: return launch_ind_mixed<2, 3, 28>(P, u, alpha, s);
+    case 4: return launch_ind_mixed<2, 4, 16>(P, u, alpha, s);
+    case 5: return launch_ind_mixed<2, 5, 10>(P, u, alpha, s);
+    case 6: return launch_ind_mixed<2, 6, 7>(P, u, alpha, s);
+  }
+#else
+  switch (N) {
+    case 2: return launch_ind_mixed<3, 2, 32>(P, u, alpha, s);
+    case 3: return launch_ind_mixed<3, 3, 9>(P, u, alpha, s);
+    case 4: return launch_ind_mixed<3, 4, 4>(P, u, alpha, s);
+    case 5: return launch_ind_mixed<3, 5, 2>(P, u, alpha, s);
+  }
+#endif
+  return -2;
+}
+#endif
+
+}  // namespace tg

@@ -27,22 +27,22 @@ struct Real;
 
 template <>
 struct Real<double> {
-  static __device__ __forceinline__ double log(double x) { return ::log(x); }
-  static __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
-  static __device__ __forceinline__ double sin(double x) { return ::sin(x); }
-  static __device__ __forceinline__ double cos(double x) { return ::cos(x); }
-  static __device__ __forceinline__ double exp(double x) { return ::exp(x); }
+  static __host__ __device__ __forceinline__ double log(double x) { return ::log(x); }
+  static __host__ __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+  static __host__ __device__ __forceinline__ double sin(double x) { return ::sin(x); }
+  static __host__ __device__ __forceinline__ double cos(double x) { return ::cos(x); }
+  static __host__ __device__ __forceinline__ double exp(double x) { return ::exp(x); }
 };
 
 template <>
 struct Real<float> {
   // logf / sinf / cosf / expf are CUDA's accurate single-precision functions;
   // division and sqrt follow the translation unit's -prec-div/-prec-sqrt.
-  static __device__ __forceinline__ float log(float x) { return ::logf(x); }
-  static __device__ __forceinline__ float sqrt(float x) { return ::sqrtf(x); }
-  static __device__ __forceinline__ float sin(float x) { return ::sinf(x); }
-  static __device__ __forceinline__ float cos(float x) { return ::cosf(x); }
-  static __device__ __forceinline__ float exp(float x) { return ::expf(x); }
+  static __host__ __device__ __forceinline__ float log(float x) { return ::logf(x); }
+  static __host__ __device__ __forceinline__ float sqrt(float x) { return ::sqrtf(x); }
+  static __host__ __device__ __forceinline__ float sin(float x) { return ::sinf(x); }
+  static __host__ __device__ __forceinline__ float cos(float x) { return ::cosf(x); }
+  static __host__ __device__ __forceinline__ float exp(float x) { return ::expf(x); }
 };
 
 // ---------------------------------------------------------------------------
@@ -57,19 +57,19 @@ struct Real<float> {
 // well conditioned; f is formed as (y-x)/(y+x) instead of Trixi's
 // cancellation-prone quotient of quadratics.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double ln_mean(double x, double y) {
+__host__ __device__ __forceinline__ double ln_mean(double x, double y) {
   const double f2 = (x * (x - 2 * y) + y * y) / (x * (x + 2 * y) + y * y);
   if (f2 < 1.0e-4)
     return (x + y) / (2.0 + f2 * (2.0 / 3.0 + f2 * (2.0 / 5.0 + f2 * (2.0 / 7.0))));
   return (y - x) / ::log(y / x);
 }
-__device__ __forceinline__ double inv_ln_mean(double x, double y) {
+__host__ __device__ __forceinline__ double inv_ln_mean(double x, double y) {
   const double f2 = (x * (x - 2 * y) + y * y) / (x * (x + 2 * y) + y * y);
   if (f2 < 1.0e-4)
     return (2.0 + f2 * (2.0 / 3.0 + f2 * (2.0 / 5.0 + f2 * (2.0 / 7.0)))) / (x + y);
   return ::log(y / x) / (y - x);
 }
-__device__ __forceinline__ float ln_mean(float x, float y) {
+__host__ __device__ __forceinline__ float ln_mean(float x, float y) {
   const float f = (y - x) / (y + x);
   const float f2 = f * f;
   if (f2 < 0.05f)
@@ -77,7 +77,7 @@ __device__ __forceinline__ float ln_mean(float x, float y) {
            (2.0f + f2 * (2.0f / 3.0f + f2 * (2.0f / 5.0f + f2 * (2.0f / 7.0f + f2 * (2.0f / 9.0f)))));
   return (y - x) / ::logf(y / x);
 }
-__device__ __forceinline__ float inv_ln_mean(float x, float y) {
+__host__ __device__ __forceinline__ float inv_ln_mean(float x, float y) {
   const float f = (y - x) / (y + x);
   const float f2 = f * f;
   if (f2 < 0.05f)
@@ -92,7 +92,7 @@ struct Euler {
   static constexpr int P = D + 1;
 
   // cons2prim, compressible_euler_2d.jl:2038-2046
-  static __device__ __forceinline__ void cons2prim(const R* u, R* w, R gamma) {
+  static __host__ __device__ __forceinline__ void cons2prim(const R* u, R* w, R gamma) {
     const R rho = u[0];
     const R inv_rho = R(1) / rho;
     R ke = 0;
@@ -107,7 +107,7 @@ struct Euler {
 
   // Component o (0-based direction) of a D-vector stored at a[0..D-1], with a
   // runtime o but compile-time indexing only (keeps arrays in registers).
-  static __device__ __forceinline__ R pick(const R* a, int o) {
+  static __host__ __device__ __forceinline__ R pick(const R* a, int o) {
     R r = a[0];
 #pragma unroll
     for (int d = 1; d < D; ++d) r = (o == d) ? a[d] : r;
@@ -115,7 +115,7 @@ struct Euler {
   }
 
   // flux(u, orientation), compressible_euler_2d.jl:415-432, 3d.jl:420-447
-  static __device__ __forceinline__ void flux(const R* u, const R* w, int o, R* f) {
+  static __host__ __device__ __forceinline__ void flux(const R* u, const R* w, int o, R* f) {
     const R rvo = pick(u + 1, o);
     const R vo = pick(w + 1, o);
     f[0] = rvo;
@@ -125,7 +125,7 @@ struct Euler {
   }
 
   // flux_ranocha, compressible_euler_2d.jl:686-722, 3d.jl:746-792
-  static __device__ __forceinline__ void flux_ranocha(const R* wl, const R* wr, int o,
+  static __host__ __device__ __forceinline__ void flux_ranocha(const R* wl, const R* wr, int o,
                                                        R inv_gm1, R* f) {
     const R rho_mean = ln_mean(wl[0], wr[0]);
     const R inv_rho_p_mean = wl[P] * wr[P] * inv_ln_mean(wl[0] * wr[P], wr[0] * wl[P]);
@@ -147,7 +147,7 @@ struct Euler {
   }
 
   // flux_shima_etal, compressible_euler_2d.jl:466-495
-  static __device__ __forceinline__ void flux_shima(const R* wl, const R* wr, int o, R inv_gm1,
+  static __host__ __device__ __forceinline__ void flux_shima(const R* wl, const R* wr, int o, R inv_gm1,
                                                      R* f) {
     const R rho_avg = R(0.5) * (wl[0] + wr[0]);
     R vavg[D];
@@ -169,7 +169,7 @@ struct Euler {
   }
 
   // flux_central, numerical_fluxes.jl:17-25
-  static __device__ __forceinline__ void flux_central(const R* ul, const R* wl, const R* ur,
+  static __host__ __device__ __forceinline__ void flux_central(const R* ul, const R* wl, const R* ur,
                                                        const R* wr, int o, R* f) {
     R fl[NV], fr[NV];
     flux(ul, wl, o, fl);
@@ -180,7 +180,7 @@ struct Euler {
 
   // FluxLaxFriedrichs(max_abs_speed[_naive]), numerical_fluxes.jl:166-178, 222-253,
   // max_abs_speed(_naive), compressible_euler_2d.jl:1423-1482
-  static __device__ __forceinline__ void flux_llf(const R* ul, const R* wl, const R* ur,
+  static __host__ __device__ __forceinline__ void flux_llf(const R* ul, const R* wl, const R* ur,
                                                    const R* wr, int o, bool naive, R gamma,
                                                    R* f) {
     flux_central(ul, wl, ur, wr, o, f);
@@ -192,7 +192,7 @@ struct Euler {
     for (int v = 0; v < NV; ++v) f[v] = f[v] + (R(-0.5) * lam * (ur[v] - ul[v]));
   }
 
-  static __device__ __forceinline__ void two_point(int kind, const R* ul, const R* wl,
+  static __host__ __device__ __forceinline__ void two_point(int kind, const R* ul, const R* wl,
                                                     const R* ur, const R* wr, int o, R gamma,
                                                     R inv_gm1, R* f) {
     switch (kind) {
@@ -205,7 +205,7 @@ struct Euler {
   }
 
   // source_terms_convergence_test, compressible_euler_2d.jl:116-145, 3d.jl:127-150
-  static __device__ __forceinline__ void source_convergence(const R* x, R t, R gamma, R* s) {
+  static __host__ __device__ __forceinline__ void source_convergence(const R* x, R t, R gamma, R* s) {
     const R c = 2, A = R(0.1);
     const R omega = R(3.141592653589793);  // 2 * pi * (1/2)
     R arg = x[0] + x[1];
@@ -231,7 +231,7 @@ struct Euler {
   }
 
   // density_pressure, compressible_euler_2d.jl:2205-2210
-  static __device__ __forceinline__ R density_pressure(const R* u, R gamma) {
+  static __host__ __device__ __forceinline__ R density_pressure(const R* u, R gamma) {
     R m2 = 0;
 #pragma unroll
     for (int d = 0; d < D; ++d) m2 += u[1 + d] * u[1 + d];
