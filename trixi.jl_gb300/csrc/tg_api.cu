@@ -86,6 +86,34 @@ int default_epb(int D, int N) {
   return 0;
 }
 
+// Elements per block of the mixed-precision kernel (threads = EPB x lines per element).
+int default_epb_mixed(int D, int N) {
+  if (D == 2) {
+    switch (N) {
+      case 2: return 32;
+      case 3: return 32;
+      case 4: return 16;
+      case 5: return 16;
+      case 6: return 16;
+    }
+  } else {
+    switch (N) {
+      case 2: return 16;
+      case 3: return 8;
+      case 4: return 4;
+      case 5: return 2;
+    }
+  }
+  return 0;
+}
+
+bool supported_epb_mixed(int D, int N, int epb) {
+  if (epb == default_epb_mixed(D, N)) return true;
+  if (D == 2 && N == 4) return epb == 8 || epb == 32;
+  if (D == 3 && N == 4) return epb == 2 || epb == 8;
+  return false;
+}
+
 bool supported_epb(int D, int N, int epb) {
   if (epb == default_epb(D, N)) return true;
   if (D == 2 && N == 4) return epb == 8 || epb == 32;
@@ -165,6 +193,22 @@ __global__ void clock_init_kernel(Clock* c, double t, double t_end, double cfl, 
   c->steps = 0;
 }
 
+// CarpenterKennedy2N54 stage times c_s (methods_2N.jl:39-44)
+__device__ const double CK_C_DEV[5] = {0.0, 1432997174477.0 / 9575080441755.0,
+                                       2526269341429.0 / 6820363962896.0,
+                                       2006345519317.0 / 3224310063776.0,
+                                       2802321613138.0 / 2924317926251.0};
+
+// sin/cos(pi t_s) of the five stage times, for the mixed kernels' source phase
+__device__ void stage_phases(Clock* c) {
+  for (int s = 0; s < 5; ++s) {
+    double sn, cs;
+    sincospi(c->t + CK_C_DEV[s] * c->dt, &sn, &cs);
+    c->sin_t[s] = (float)sn;
+    c->cos_t[s] = (float)cs;
+  }
+}
+
 __global__ void clock_set_kernel(Clock* c, double t, double dt) {
   c->t = t;
   c->dt = dt;
@@ -172,6 +216,7 @@ __global__ void clock_set_kernel(Clock* c, double t, double dt) {
   c->skip = 0;
   c->finalstep = 0;
   c->finished = 0;
+  stage_phases(c);
 }
 
 __global__ void clock_config_kernel(Clock* c, double t_end, double cfl) {
@@ -205,6 +250,7 @@ __global__ void clock_begin_kernel(Clock* c) {
     c->dt = te - c->t;
     c->finalstep = 1;
   }
+  stage_phases(c);
 }
 
 // step! epilogue: t += dt, then StepsizeCallback: dt = cfl * max_dt(u_new).
@@ -323,6 +369,9 @@ struct tg_ctx {
   double* d_xline = nullptr;
   float* d_invj_f = nullptr;
   float* d_xline_f = nullptr;
+  double* d_x0 = nullptr;
+  float* d_xoff = nullptr;
+  float2* d_sc0 = nullptr;
   double* d_weights = nullptr;
   double* d_partial = nullptr;
   double* d_sums = nullptr;
@@ -367,7 +416,7 @@ static void free_ctx(tg_ctx* c) {
     if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
   void* ptrs[] = {c->d_u[0], c->d_u[1], c->d_utmp, c->d_du, c->d_uscratch, c->d_stage64,
                   c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_nbr, c->d_invj, c->d_xline,
-                  c->d_invj_f, c->d_xline_f, c->d_weights, c->d_partial, c->d_sums, c->d_clock,
+                  c->d_invj_f, c->d_xline_f, c->d_x0, c->d_xoff, c->d_sc0, c->d_weights, c->d_partial, c->d_sums, c->d_clock,
                   c->d_status, c->d_speed};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -464,6 +513,10 @@ static int launch_kernel(tg_ctx* c, int mode, const void* u_in, void* u_out, dou
       A.b = CK_B[stage];
       A.c = CK_C[stage];
       A.zero_tmp = stage == 0;
+      A.stage = stage;
+    } else {
+      A.sin_t = (float)std::sin(M_PI * t_rhs);
+      A.cos_t = (float)std::cos(M_PI * t_rhs);
     }
     A.speed_bits = reduce ? &c->d_clock->speed_bits : nullptr;
     rc = launch_mixed(c->D, c->N, c->vi, c->epb, c->MP, A, c->stream);
@@ -541,8 +594,10 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "missing basis or mesh array");
   if (cfg->source_terms != TG_SOURCE_NONE && !cfg->node_coordinates)
     return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "source terms need node_coordinates");
-  int epb = cfg->elements_per_block > 0 ? cfg->elements_per_block : default_epb(D, N);
-  if (!supported_epb(D, N, epb))
+  const bool mixed = cfg->precision == TG_PRECISION_MIXED;
+  int epb = cfg->elements_per_block > 0 ? cfg->elements_per_block
+                                        : (mixed ? default_epb_mixed(D, N) : default_epb(D, N));
+  if (mixed ? !supported_epb_mixed(D, N, epb) : !supported_epb(D, N, epb))
     return fail(nullptr, TG_ERR_UNSUPPORTED, "elements_per_block %d not compiled for %dD N=%d", epb,
                 D, N);
 
@@ -675,20 +730,46 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     ALLOC(c->d_alpha_raw, rsize(c) * c->E);
     ALLOC(c->d_alpha, sizeof(double) * c->E);
   }
-  std::vector<float> invj_f, xline_f;
+  std::vector<float> invj_f, xline_f, xoff;
+  std::vector<double> x0;
   if (!c->fp64) {
     invj_f.resize(c->E);
     for (int64_t k = 0; k < c->E; ++k) invj_f[k] = (float)cfg->inverse_jacobian[k];
     xline_f.assign(xline.begin(), xline.end());
     ALLOC(c->d_invj_f, sizeof(float) * c->E);
-    if (!xline_f.empty()) ALLOC(c->d_xline_f, sizeof(float) * xline_f.size());
+    if (!xline_f.empty()) {
+      // first node coordinate (FP64) and offsets along each axis (FP32) for
+      // the mixed path's source-term phase
+      x0.resize((size_t)c->E * D);
+      xoff.resize(xline.size());
+      for (int64_t e2 = 0; e2 < c->E; ++e2)
+        for (int d = 0; d < D; ++d) {
+          const double* xl = &xline[((size_t)e2 * D + d) * N];
+          x0[(size_t)e2 * D + d] = xl[0];
+          for (int i = 0; i < N; ++i) xoff[((size_t)e2 * D + d) * N + i] = (float)(xl[i] - xl[0]);
+        }
+      ALLOC(c->d_xline_f, sizeof(float) * xline_f.size());
+      ALLOC(c->d_x0, sizeof(double) * x0.size());
+      ALLOC(c->d_xoff, sizeof(float) * xoff.size());
+      ALLOC(c->d_sc0, sizeof(float2) * c->E);
+    }
   }
 #undef ALLOC
   if (!c->fp64) {
     cudaMemcpy(c->d_invj_f, invj_f.data(), sizeof(float) * c->E, cudaMemcpyHostToDevice);
-    if (!xline_f.empty())
+    if (!xline_f.empty()) {
       cudaMemcpy(c->d_xline_f, xline_f.data(), sizeof(float) * xline_f.size(),
                  cudaMemcpyHostToDevice);
+      cudaMemcpy(c->d_x0, x0.data(), sizeof(double) * x0.size(), cudaMemcpyHostToDevice);
+      cudaMemcpy(c->d_xoff, xoff.data(), sizeof(float) * xoff.size(), cudaMemcpyHostToDevice);
+      std::vector<float2> sc0((size_t)c->E);
+      for (int64_t e2 = 0; e2 < c->E; ++e2) {
+        double ph = 0;
+        for (int d = 0; d < D; ++d) ph += x0[(size_t)e2 * D + d];
+        sc0[e2] = make_float2((float)std::sin(M_PI * ph), (float)std::cos(M_PI * ph));
+      }
+      cudaMemcpy(c->d_sc0, sc0.data(), sizeof(float2) * c->E, cudaMemcpyHostToDevice);
+    }
   }
   cudaMemcpy(c->d_nbr, nbr.data(), sizeof(int32_t) * nbr.size(), cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_invj, cfg->inverse_jacobian, sizeof(double) * c->E, cudaMemcpyHostToDevice);
@@ -730,6 +811,9 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   M.nbr = c->d_nbr;
   M.inv_jac = c->d_invj_f;
   M.xline = c->d_xline_f;
+  M.x0 = c->d_x0;
+  M.xoff = c->d_xoff;
+  M.sc0 = c->d_sc0;
   *out = c;
   return TG_OK;
 }

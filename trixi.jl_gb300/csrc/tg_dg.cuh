@@ -63,6 +63,7 @@ struct Clock {
   unsigned long long speed_bits;  // max scaled wave speed of the state (as bits)
   int32_t skip, finalstep, finished, nan_dt;
   int64_t steps;
+  float sin_t[5], cos_t[5];       // sin/cos(pi (t + c_s dt)) of the 2N stages
 };
 
 enum StageMode { MODE_RHS = 0, MODE_STAGE = 1 };

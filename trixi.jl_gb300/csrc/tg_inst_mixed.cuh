@@ -5,10 +5,10 @@
 
 namespace tg {
 
-template <int D, int N, int VI, int EPB>
+template <int D, int N, int VI, int VF, int SF, int EPB>
 static int launch_mixed_one(const MixedParams& P, const MixedArgs& A, cudaStream_t s) {
   using K = MixedKernel<D, N, VI, EPB>;
-  auto kern = mixed_element_kernel<D, N, VI, EPB>;
+  auto kern = mixed_element_kernel<D, N, VI, VF, SF, EPB>;
   static bool configured = false;
   const size_t smem = K::smem_bytes();
   if (!configured) {
@@ -23,31 +23,45 @@ static int launch_mixed_one(const MixedParams& P, const MixedArgs& A, cudaStream
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+// Flux-specialised instances for polydeg 3 (flux_ranocha volume flux with the
+// two Lax-Friedrichs surface fluxes); every other choice dispatches at run time.
+template <int D, int VI, int EPB>
+static int launch_mixed_n4(const MixedParams& P, const MixedArgs& A, cudaStream_t s) {
+  const bool ranocha = VI == VI_WEAK || P.volume_flux == FLUX_RANOCHA;
+  if (ranocha && P.surface_flux == FLUX_LLF)
+    return launch_mixed_one<D, 4, VI, VI == VI_WEAK ? -1 : FLUX_RANOCHA, FLUX_LLF, EPB>(P, A, s);
+  if (ranocha && P.surface_flux == FLUX_LLF_NAIVE)
+    return launch_mixed_one<D, 4, VI, VI == VI_WEAK ? -1 : FLUX_RANOCHA, FLUX_LLF_NAIVE, EPB>(P, A,
+                                                                                              s);
+  return launch_mixed_one<D, 4, VI, -1, -1, EPB>(P, A, s);
+}
+
 #define TG_CAT2(a, b) a##b
 #define TG_CAT(a, b) TG_CAT2(a, b)
 
+// Elements per block (threads = EPB x lines per element); the first is the default.
 int TG_CAT(launch_mixed_, TG_SUFFIX)(int N, int epb, const MixedParams& P, const MixedArgs& A,
                                      cudaStream_t s) {
 #if TG_D == 2
   switch (N) {
-    case 2: return launch_mixed_one<2, 2, TG_VI, 64>(P, A, s);
-    case 3: return launch_mixed_one<2, 3, TG_VI, 28>(P, A, s);
+    case 2: return launch_mixed_one<2, 2, TG_VI, -1, -1, 32>(P, A, s);
+    case 3: return launch_mixed_one<2, 3, TG_VI, -1, -1, 32>(P, A, s);
     case 4:
-      if (epb == 8) return launch_mixed_one<2, 4, TG_VI, 8>(P, A, s);
-      if (epb == 32) return launch_mixed_one<2, 4, TG_VI, 32>(P, A, s);
-      return launch_mixed_one<2, 4, TG_VI, 16>(P, A, s);
-    case 5: return launch_mixed_one<2, 5, TG_VI, 10>(P, A, s);
-    case 6: return launch_mixed_one<2, 6, TG_VI, 7>(P, A, s);
+      if (epb == 8) return launch_mixed_n4<2, TG_VI, 8>(P, A, s);
+      if (epb == 32) return launch_mixed_n4<2, TG_VI, 32>(P, A, s);
+      return launch_mixed_n4<2, TG_VI, 16>(P, A, s);
+    case 5: return launch_mixed_one<2, 5, TG_VI, -1, -1, 16>(P, A, s);
+    case 6: return launch_mixed_one<2, 6, TG_VI, -1, -1, 16>(P, A, s);
   }
 #else
   switch (N) {
-    case 2: return launch_mixed_one<3, 2, TG_VI, 32>(P, A, s);
-    case 3: return launch_mixed_one<3, 3, TG_VI, 9>(P, A, s);
+    case 2: return launch_mixed_one<3, 2, TG_VI, -1, -1, 16>(P, A, s);
+    case 3: return launch_mixed_one<3, 3, TG_VI, -1, -1, 8>(P, A, s);
     case 4:
-      if (epb == 2) return launch_mixed_one<3, 4, TG_VI, 2>(P, A, s);
-      if (epb == 8) return launch_mixed_one<3, 4, TG_VI, 8>(P, A, s);
-      return launch_mixed_one<3, 4, TG_VI, 4>(P, A, s);
-    case 5: return launch_mixed_one<3, 5, TG_VI, 2>(P, A, s);
+      if (epb == 2) return launch_mixed_n4<3, TG_VI, 2>(P, A, s);
+      if (epb == 8) return launch_mixed_n4<3, TG_VI, 8>(P, A, s);
+      return launch_mixed_n4<3, TG_VI, 4>(P, A, s);
+    case 5: return launch_mixed_one<3, 5, TG_VI, -1, -1, 2>(P, A, s);
   }
 #endif
   return -2;

@@ -32,6 +32,8 @@ namespace tg {
 
 struct MixedParams {
   int64_t nelements;
+  const double* x0;         // [E][D] coordinates of node (0,0,0) (source terms)
+  const float* xoff;        // [E][D][N] node coordinates minus x0 along each axis
   float gamma, inv_gamma_minus_one;
   float inv_weights[MAXN];
   float Dhat[MAXN * MAXN];
@@ -42,7 +44,8 @@ struct MixedParams {
   int32_t alpha_smooth;
   const int32_t* nbr;       // [E][2D]
   const float* inv_jac;     // [E]
-  const float* xline;       // [E][D][N] or null
+  const float* xline;       // [E][D][N] or null (unused by the stage kernel)
+  const float2* sc0;        // [E] (sin, cos)(pi * sum_d x0_d) for the source phase
 };
 
 struct MixedArgs {
@@ -59,6 +62,8 @@ struct MixedArgs {
   double a, b, c;           // 2N coefficients of the stage
   int32_t mode;
   int32_t zero_tmp;
+  int32_t stage;            // MODE_STAGE: index into the clock's per-stage phase
+  float sin_t, cos_t;       // MODE_RHS: sin/cos(pi t)
 };
 
 // ---------------------------------------------------------------------------
@@ -77,6 +82,7 @@ struct Node {
   float du[D + 2];      // conservative deviation from cons(w_e)
   float dw[D + 2];      // primitive deviation (drho, dv_1..dv_D, dp)
   float w[D + 2];       // full primitives
+  float dq;             // deviation of rho/p from the reference q
 };
 
 template <int D>
@@ -138,6 +144,15 @@ struct Dev {
     n.w[0] = rho;
     n.dw[P] = dp;
     n.w[P] = R.p + dp;
+    n.dq = (R.rq + drho - R.q * dp) / n.w[P];
+  }
+
+  // Full primitives from deviations (nodes stored as dw + dq only).
+  static __host__ __device__ __forceinline__ void complete(const RefState<D>& R, Node<D>& n) {
+    n.w[0] = R.rho + n.dw[0];
+#pragma unroll
+    for (int d = 0; d < D; ++d) n.w[1 + d] = R.v[d] + n.dw[1 + d];
+    n.w[P] = R.p + n.dw[P];
   }
 
   static __host__ __device__ __forceinline__ float pick(const float* a, int o) {
@@ -204,10 +219,8 @@ struct Dev {
   static __host__ __device__ __forceinline__ void dranocha(const RefState<D>& R, const Node<D>& a,
                                                    const Node<D>& b, int o, float igm1, float* f) {
     const float drho_ln = dev_ln_mean(R.rho, a.dw[0], b.dw[0], a.w[0], b.w[0]);
-    // q = rho / p relative to R.q, with the exact residual R.rq = rho_ref - q_ref p_ref
-    const float dqa = (R.rq + a.dw[0] - R.q * a.dw[P]) / a.w[P];
-    const float dqb = (R.rq + b.dw[0] - R.q * b.dw[P]) / b.w[P];
-    const float dq_ln = dev_ln_mean(R.q, dqa, dqb, R.q + dqa, R.q + dqb);
+    // q = rho / p relative to R.q (node deviations a.dq, b.dq from make_node)
+    const float dq_ln = dev_ln_mean(R.q, a.dq, b.dq, R.q + a.dq, R.q + b.dq);
     const float q_ln = R.q + dq_ln;
     float dvavg[D], vavg[D];
     float dvsq = 0;
@@ -264,6 +277,19 @@ struct Dev {
     f[P] = igm1 * (dpavg * pick(vavg, o) + R.p * pick(dvavg, o)) + d1 * kin + F1r * dkin + dpv;
   }
 
+  // KIND >= 0 selects the flux at compile time; KIND < 0 dispatches on `kind`.
+  template <int KIND>
+  static __host__ __device__ __forceinline__ void flux2(int kind, const RefState<D>& R,
+                                                         const Node<D>& a, const Node<D>& b, int o,
+                                                         float gamma, float igm1, float* f) {
+    if constexpr (KIND == FLUX_RANOCHA) dranocha(R, a, b, o, igm1, f);
+    else if constexpr (KIND == FLUX_SHIMA_ETAL) dshima(R, a, b, o, igm1, f);
+    else if constexpr (KIND == FLUX_LLF) dllf(R, a, b, o, false, gamma, igm1, f);
+    else if constexpr (KIND == FLUX_LLF_NAIVE) dllf(R, a, b, o, true, gamma, igm1, f);
+    else if constexpr (KIND == FLUX_CENTRAL) dcentral(R, a, b, o, gamma, igm1, f);
+    else two_point(kind, R, a, b, o, gamma, igm1, f);
+  }
+
   static __host__ __device__ __forceinline__ void two_point(int kind, const RefState<D>& R,
                                                     const Node<D>& a, const Node<D>& b, int o,
                                                     float gamma, float igm1, float* f) {
@@ -288,346 +314,374 @@ __device__ __forceinline__ float2 ff_add(float2 u, float x) {
   return make_float2(h, l);
 }
 
+// cp.async (sm_80+ asynchronous global->shared copies) helpers
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// Thread layout: one thread per (direction, line) of each element, lines
+// ordered direction-major so that a warp works on one direction.  A line
+// thread evaluates the N(N-1)/2 two-point fluxes of its line (or the N
+// physical fluxes of the weak form, and the subcell fluxes of the HG blend)
+// and its two face fluxes, accumulating the line's N nodal contributions in
+// registers; the D partial sums per node meet once in shared memory.  All
+// global reads of a block (state chunk, u_tmp chunk and the neighbour traces
+// of faces between blocks) are issued up front as cp.async copies.
 template <int D, int N, int VI, int EPB>
 struct MixedKernel {
   static constexpr int NV = D + 2;
   static constexpr int NN = Pow<N, D>::value;
-  static constexpr int NF = NN / N;
-  static constexpr int NT = EPB * NN;
-  static constexpr int SP = EPB * NN + 1;
-  static constexpr int NP = N * (N - 1) / 2;
+  static constexpr int NF = NN / N;          // lines per direction = nodes per face
+  static constexpr int L = D * NF;           // lines per element
+  static constexpr int NT = EPB * L;         // threads per block
+  static constexpr int SP = EPB * NN + 1;    // SoA stride of node fields
+  static constexpr int NFLD = 2 * NV + 1;    // dw[NV], dq, du[NV]
   static constexpr int CHUNK = EPB * NN * NV;
-  static constexpr int VOL_WEAK = D * NV * SP;
-  static constexpr int VOL_FD = EPB * D * NF * NP * NV;
-  static constexpr int VOL_FV = EPB * D * NF * (N - 1) * NV;
-  static constexpr int VOL = VI == VI_WEAK ? VOL_WEAK : (VI == VI_FD ? VOL_FD : VOL_FD + VOL_FV);
-  static constexpr int REFW = (sizeof(RefState<D>) + 3) / 4;  // floats per reference
+  static constexpr int FACE = EPB * 2 * D * NF * NV;  // neighbour traces (float2)
+  static constexpr int REFW = (sizeof(RefState<D>) + 3) / 4;
+  static constexpr int MINB = NT <= 128 ? 4 : (NT <= 256 ? 3 : 1);  // resident blocks per SM
 
   static constexpr size_t smem_bytes() {
-    return sizeof(float2) * CHUNK + sizeof(float) * CHUNK  // state, u_tmp
-           + sizeof(float) * (3 * NV * SP                  // du, dw, w (SoA)
-                              + EPB * 2 * D * NF * NV      // face fluxes
-                              + VOL                        // volume fluxes
-                              + N * N + N                  // matrix, inverse weights
-                              + EPB * REFW                 // references
-                              + EPB * (D + 1) + 4 + 8);    // alpha, scalars, speed maxima
+    return sizeof(float2) * (CHUNK + FACE) + sizeof(float) * CHUNK  // state, traces, u_tmp
+           + sizeof(float) * (NFLD * SP + D * NV * SP               // node fields, partial du
+                              + EPB * REFW + EPB * 4 + 4            // references, per element
+                              + EPB * D                             // speed maxima
+                              + N * N + N + 4);                     // matrix, inverse weights
   }
 };
 
-template <int D, int N, int VI, int EPB>
-__global__ void __launch_bounds__(EPB * Pow<N, D>::value)
+template <int D>
+struct SourceMMS {
+  // source_terms_convergence_test, compressible_euler_2d.jl:116-145, 3d.jl:127-150,
+  // given sin/cos of the phase omega (x+y(+z)-t)
+  static __device__ __forceinline__ void eval(float si, float co, float gamma, float* s) {
+    const float A = 0.1f, omega = 3.14159265358979f;
+    const float rho = 2.0f + A * si;
+    const float rho_x = omega * A * co;
+    if (D == 2) {
+      const float tmp = (2.0f * rho - 1.0f) * (gamma - 1.0f);
+      s[0] = rho_x;
+      s[1] = rho_x * (1.0f + tmp);
+      s[2] = s[1];
+      s[D + 1] = 2.0f * rho_x * (rho + tmp);
+    } else {
+      const float tmp = (2.0f * rho - 1.5f) * (gamma - 1.0f);
+      s[0] = 2.0f * rho_x;
+      s[1] = rho_x * (2.0f + tmp);
+      s[2] = s[1];
+      s[D] = s[1];
+      s[D + 1] = rho_x * (4.0f * rho + 3.0f * tmp);
+    }
+  }
+};
+
+template <int D, int N, int VI, int VF, int SF, int EPB>
+__device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<D>& R,
+                                           const float2* s_u, const float2* s_fu,
+                                           const float* s_nd, float* s_part, const float* s_mat,
+                                           const float* s_iw, float alpha, int slot, int line,
+                                           int dd, int64_t e, int64_t e0, int nel) {
+  using K = MixedKernel<D, N, VI, EPB>;
+  using Dv = Dev<D>;
+  constexpr int NV = K::NV, NN = K::NN, SP = K::SP, NF = K::NF;
+  const float gamma = P.gamma, igm1 = P.inv_gamma_minus_one;
+  const int S = axis_stride<N>(dd);
+  const int lb = line_base<N>(line, dd);
+  const int base = slot * NN + lb;
+  constexpr bool NEED_DU = VI == VI_HG || VF < 0 || VF == FLUX_LLF || VF == FLUX_LLF_NAIVE;
+  Node<D> nd[N];
+#pragma unroll
+  for (int a = 0; a < N; ++a) {
+    const int idx = base + a * S;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) nd[a].dw[v] = s_nd[v * SP + idx];
+    nd[a].dq = s_nd[NV * SP + idx];
+    if (NEED_DU) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) nd[a].du[v] = s_nd[(NV + 1 + v) * SP + idx];
+    }
+    Dv::complete(R, nd[a]);
+  }
+  float acc[N][NV];
+#pragma unroll
+  for (int a = 0; a < N; ++a)
+#pragma unroll
+    for (int v = 0; v < NV; ++v) acc[a][v] = 0.0f;
+
+  if (VI == VI_WEAK) {
+    // weak_form_kernel!: du[ii] += Dhat[ii, a] f(u_a)
+#pragma unroll
+    for (int a = 0; a < N; ++a) {
+      float f[NV];
+      Dv::dflux(R, nd[a], dd, gamma, igm1, f);
+#pragma unroll
+      for (int ii = 0; ii < N; ++ii) {
+        const float c = s_mat[ii * N + a];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc[ii][v] = fmaf(c, f[v], acc[ii][v]);
+      }
+    }
+  } else {
+    // flux_differencing_kernel!: each pair once, both nodes updated
+#pragma unroll
+    for (int a = 0; a < N; ++a)
+#pragma unroll
+      for (int b = a + 1; b < N; ++b) {
+        float F[NV];
+        Dv::template flux2<VF>(P.volume_flux, R, nd[a], nd[b], dd, gamma, igm1, F);
+        const float cab = s_mat[a * N + b], cba = s_mat[b * N + a];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          acc[a][v] = fmaf(cab, F[v], acc[a][v]);
+          acc[b][v] = fmaf(cba, F[v], acc[b][v]);
+        }
+      }
+    if (VI == VI_HG && fabsf(alpha) > P.alpha_atol) {
+      // (1 - alpha) FD + alpha FV (fv_kernel!, zero-padded subcell fluxes)
+#pragma unroll
+      for (int a = 0; a < N; ++a)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc[a][v] *= (1.0f - alpha);
+#pragma unroll
+      for (int a = 0; a + 1 < N; ++a) {
+        float F[NV];
+        Dv::two_point(P.fv_flux, R, nd[a], nd[a + 1], dd, gamma, igm1, F);
+        const float ca = alpha * s_iw[a], cb = alpha * s_iw[a + 1];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          acc[a][v] = fmaf(ca, F[v], acc[a][v]);
+          acc[a + 1][v] = fmaf(-cb, F[v], acc[a + 1][v]);
+        }
+      }
+    }
+  }
+
+  // faces -dd (node 0) and +dd (node N-1): interface fluxes with the
+  // neighbour's trace expressed relative to this element's reference
+  const float factor = s_iw[0];
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const int dir = 2 * dd + side;
+    const int64_t nb = P.nbr[e * 2 * D + dir];
+    const int64_t nbs = nb - e0;
+    const float2* src;
+    if (nbs >= 0 && nbs < nel)
+      src = s_u + ((int)nbs * NN + lb + (side ? 0 : (N - 1) * S)) * NV;
+    else
+      src = s_fu + ((slot * 2 * D + dir) * NF + line) * NV;
+    float hi[NV], lo[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const float2 x = src[v];
+      hi[v] = x.x;
+      lo[v] = x.y;
+    }
+    Node<D> nn_;
+    Dv::make_node(hi, lo, R, gamma, nn_);
+    Node<D>& own = side ? nd[N - 1] : nd[0];
+    if (!NEED_DU) {
+      const int idx = base + (side ? (N - 1) * S : 0);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) own.du[v] = s_nd[(NV + 1 + v) * SP + idx];
+    }
+    float F[NV];
+    if (side) {
+      Dv::template flux2<SF>(P.surface_flux, R, own, nn_, dd, gamma, igm1, F);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc[N - 1][v] = fmaf(F[v], factor, acc[N - 1][v]);
+    } else {
+      Dv::template flux2<SF>(P.surface_flux, R, nn_, own, dd, gamma, igm1, F);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc[0][v] = fmaf(-F[v], factor, acc[0][v]);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < N; ++a)
+#pragma unroll
+    for (int v = 0; v < NV; ++v) s_part[(dd * NV + v) * SP + base + a * S] = acc[a][v];
+}
+
+template <int D, int N, int VI, int VF, int SF, int EPB>
+__global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D, N, VI, EPB>::MINB)
     mixed_element_kernel(const MixedParams P, const MixedArgs A) {
   using K = MixedKernel<D, N, VI, EPB>;
   using Dv = Dev<D>;
-  constexpr int NV = K::NV, NN = K::NN, NF = K::NF, NT = K::NT, SP = K::SP, NP = K::NP;
-  constexpr int CHUNK = K::CHUNK;
+  constexpr int NV = K::NV, NN = K::NN, NF = K::NF, NT = K::NT, SP = K::SP;
+  constexpr int CHUNK = K::CHUNK, NFLD = K::NFLD, FACE = K::FACE;
   constexpr int PP = D + 1;
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* s_u = reinterpret_cast<float2*>(smem_raw);
-  float* s_tmp = reinterpret_cast<float*>(s_u + CHUNK);
-  float* s_du = s_tmp + CHUNK;
-  float* s_dw = s_du + NV * SP;
-  float* s_w = s_dw + NV * SP;
-  float* s_face = s_w + NV * SP;
-  float* s_vol = s_face + EPB * 2 * D * NF * NV;
-  float* s_fv = s_vol + K::VOL_FD;
-  float* s_mat = s_vol + K::VOL;
-  float* s_iw = s_mat + N * N;
-  RefState<D>* s_ref = reinterpret_cast<RefState<D>*>(s_iw + N);
-  float* s_alpha = reinterpret_cast<float*>(s_ref + EPB);
-  float* s_scal = s_alpha + EPB;  // [0] stage time, [1] b dt, [2] a
+  float2* s_fu = s_u + CHUNK;                               // neighbour traces
+  float* s_tmp = reinterpret_cast<float*>(s_fu + FACE);
+  float* s_nd = s_tmp + CHUNK;
+  float* s_part = s_nd + NFLD * SP;
+  RefState<D>* s_ref = reinterpret_cast<RefState<D>*>(s_part + D * NV * SP);
+  float* s_elem = reinterpret_cast<float*>(s_ref + EPB);  // [EPB][4]: alpha, sin, cos
+  float* s_scal = s_elem + EPB * 4;                         // b dt, a, sin(pi t), cos(pi t)
   unsigned int* s_smax = reinterpret_cast<unsigned int*>(s_scal + 4);
+  float* s_mat = reinterpret_cast<float*>(s_smax + EPB * D);
+  float* s_iw = s_mat + N * N;
 
   const int tid = threadIdx.x;
-  const int slot = tid / NN;
-  const int node = tid - slot * NN;
   const int64_t e0 = (int64_t)blockIdx.x * EPB;
   const int nel = (int)min((int64_t)EPB, P.nelements - e0);
-  const bool active = slot < nel;
-  const int64_t e = e0 + slot;
   const size_t gofs = (size_t)e0 * NN * NV;
   const int nval = nel * NN * NV;
-  const float gamma = P.gamma, igm1 = P.inv_gamma_minus_one;
+  const float gamma = P.gamma;
 
   if (A.mode == MODE_STAGE && A.clock->skip) {
     for (int k = tid; k < nval; k += NT) A.u_out[gofs + k] = A.u_in[gofs + k];
     return;
   }
 
-  // ---- stage chunk, matrices, references --------------------------------------
-  for (int k = tid; k < nval; k += NT) s_u[k] = __ldg(A.u_in + gofs + k);
-  if (A.mode == MODE_STAGE) {
-    for (int k = tid; k < nval; k += NT) s_tmp[k] = A.zero_tmp ? 0.0f : A.u_tmp[gofs + k];
+  // ---- asynchronous staging of every global input of the block -----------------
+  for (int k = tid; k < nval; k += NT) cp_async8(s_u + k, A.u_in + gofs + k);
+  const bool load_tmp = A.mode == MODE_STAGE && !A.zero_tmp;
+  if (load_tmp)
+    for (int k = tid; k < nval; k += NT) cp_async4(s_tmp + k, A.u_tmp + gofs + k);
+  for (int k = tid; k < nel * 2 * D * NF; k += NT) {
+    // face traces of neighbours in other blocks
+    const int sl = k / (2 * D * NF);
+    const int rem = k - sl * (2 * D * NF);
+    const int dir = rem / NF;
+    const int fn = rem - dir * NF;
+    const int64_t nb = P.nbr[(e0 + sl) * 2 * D + dir];
+    if (nb >= e0 && nb < e0 + nel) continue;
+    const int dd = dir >> 1;
+    const int nnode = line_base<N>(fn, dd) + ((dir & 1) ? 0 : (N - 1) * axis_stride<N>(dd));
+    const float2* g = A.u_in + ((size_t)nb * NN + nnode) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) cp_async8(s_fu + k * NV + v, g + v);
   }
+  if (!load_tmp && A.mode == MODE_STAGE)
+    for (int k = tid; k < nval; k += NT) s_tmp[k] = 0.0f;
   for (int k = tid; k < N * N; k += NT) s_mat[k] = VI == VI_WEAK ? P.Dhat[k] : P.Dsplit[k];
   if (tid < N) s_iw[tid] = P.inv_weights[tid];
   if (tid < EPB * D) s_smax[tid] = 0u;
   if (tid == 0) {
-    // the only FP64 arithmetic of the kernel: a few scalars per block
     if (A.mode == MODE_RHS) {
-      s_scal[0] = (float)A.t_rhs;
-      s_scal[1] = 0.0f;
+      s_scal[0] = 0.0f;
+      s_scal[2] = A.sin_t;
+      s_scal[3] = A.cos_t;
     } else {
-      const double dt = A.clock->dt;
-      s_scal[0] = (float)(A.clock->t + A.c * dt);
-      s_scal[1] = (float)(A.b * dt);
+      s_scal[0] = (float)(A.b * A.clock->dt);
+      s_scal[2] = A.clock->sin_t[A.stage];
+      s_scal[3] = A.clock->cos_t[A.stage];
     }
-    s_scal[2] = (float)A.a;
+    s_scal[1] = (float)A.a;
   }
-  __syncthreads();
-  if (active && node == 0) {
-    float hi[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) hi[v] = s_u[slot * NN * NV + v].x;
-    Dv::make_ref(hi, gamma, igm1, s_ref[slot]);
+  if (tid < nel) {
+    const int64_t e = e0 + tid;
     if (VI == VI_HG) {
       float a = A.alpha_raw[e];
       if (P.alpha_smooth) {
 #pragma unroll
-        for (int dir = 0; dir < 2 * D; ++dir)
-          a = fmaxf(a, 0.5f * A.alpha_raw[P.nbr[e * 2 * D + dir]]);
+        for (int dir = 0; dir < 2 * D; ++dir) a = fmaxf(a, 0.5f * A.alpha_raw[P.nbr[e * 2 * D + dir]]);
       }
-      s_alpha[slot] = a;
+      s_elem[tid * 4 + 0] = a;
       if (A.alpha_out) A.alpha_out[e] = a;
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+
+  // ---- per element: reference state and source phase ------------------------------
+  if (tid < nel) {
+    float hi[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) hi[v] = s_u[tid * NN * NV + v].x;
+    Dv::make_ref(hi, gamma, P.inv_gamma_minus_one, s_ref[tid]);
+    if (P.source == SRC_CONVERGENCE_TEST) {
+      // sin/cos of pi (x0_e - t) by the angle-difference formula
+      const float2 sc = P.sc0[e0 + tid];
+      const float st = s_scal[2], ct = s_scal[3];
+      s_elem[tid * 4 + 1] = sc.x * ct - sc.y * st;
+      s_elem[tid * 4 + 2] = sc.y * ct + sc.x * st;
     }
   }
   __syncthreads();
 
-  if (active) {
+  // ---- node deviations -----------------------------------------------------------
+  for (int n = tid; n < nel * NN; n += NT) {
+    const int sl = n / NN;
     float hi[NV], lo[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      const float2 x = s_u[(slot * NN + node) * NV + v];
+      const float2 x = s_u[n * NV + v];
       hi[v] = x.x;
       lo[v] = x.y;
     }
     Node<D> nd;
-    Dv::make_node(hi, lo, s_ref[slot], gamma, nd);
+    Dv::make_node(hi, lo, s_ref[sl], gamma, nd);
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      s_du[v * SP + tid] = nd.du[v];
-      s_dw[v * SP + tid] = nd.dw[v];
-      s_w[v * SP + tid] = nd.w[v];
+      s_nd[v * SP + n] = nd.dw[v];
+      s_nd[(NV + 1 + v) * SP + n] = nd.du[v];
     }
+    s_nd[NV * SP + n] = nd.dq;
   }
   __syncthreads();
 
-  auto load_node = [&](int idx, Node<D>& n) {
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      n.du[v] = s_du[v * SP + idx];
-      n.dw[v] = s_dw[v * SP + idx];
-      n.w[v] = s_w[v * SP + idx];
-    }
-  };
-
-  // ---- interface fluxes (deviation form, own element's reference) -----------
-  for (int it = tid; it < nel * 2 * D * NF; it += NT) {
-    const int sl = it / (2 * D * NF);
-    const int rem = it - sl * (2 * D * NF);
-    const int dir = rem / NF;
-    const int fn = rem - dir * NF;
-    const int d = dir >> 1;
-    const int side = dir & 1;
-    const int S = axis_stride<N>(d);
-    const int base = line_base<N>(fn, d);
-    const int own = base + (side ? (N - 1) * S : 0);
-    const int nnode = base + (side ? 0 : (N - 1) * S);
-    const int64_t nb = P.nbr[(e0 + sl) * 2 * D + dir];
-    const RefState<D>& R = s_ref[sl];
-    Node<D> no, nn_;
-    load_node(sl * NN + own, no);
-    {
-      float hi[NV], lo[NV];
-      const int64_t nbs = nb - e0;
-      if (nbs >= 0 && nbs < nel) {
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          const float2 x = s_u[((int)nbs * NN + nnode) * NV + v];
-          hi[v] = x.x;
-          lo[v] = x.y;
-        }
-      } else {
-        const float2* p = A.u_in + ((size_t)nb * NN + nnode) * NV;
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          const float2 x = __ldg(p + v);
-          hi[v] = x.x;
-          lo[v] = x.y;
-        }
-      }
-      Dv::make_node(hi, lo, R, gamma, nn_);
-    }
-    float F[NV];
-    if (side)
-      Dv::two_point(P.surface_flux, R, no, nn_, d, gamma, igm1, F);
-    else
-      Dv::two_point(P.surface_flux, R, nn_, no, d, gamma, igm1, F);
-#pragma unroll
-    for (int v = 0; v < NV; ++v) s_face[((sl * 2 * D + dir) * NF + fn) * NV + v] = F[v];
-  }
-
-  // ---- volume fluxes -----------------------------------------------------------
-  if (active) {
-    const RefState<D>& R = s_ref[slot];
-    if (VI == VI_WEAK) {
-      Node<D> nd;
-      load_node(tid, nd);
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        float f[NV];
-        Dv::dflux(R, nd, d, gamma, igm1, f);
-#pragma unroll
-        for (int v = 0; v < NV; ++v) s_vol[(d * NV + v) * SP + tid] = f[v];
-      }
-    } else {
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        const int S = axis_stride<N>(d);
-        const int i = axis_index<N>(node, d);
-        const int line = line_index<N>(node, d);
-        const int lb = line_base<N>(line, d);
-        for (int p = i; p < NP; p += N) {
-          int a = 0, q = p;
-          while (q >= N - 1 - a) {
-            q -= N - 1 - a;
-            ++a;
-          }
-          const int b = a + 1 + q;
-          Node<D> na, nb2;
-          load_node(slot * NN + lb + a * S, na);
-          load_node(slot * NN + lb + b * S, nb2);
-          float F[NV];
-          Dv::two_point(P.volume_flux, R, na, nb2, d, gamma, igm1, F);
-#pragma unroll
-          for (int v = 0; v < NV; ++v)
-            s_vol[(((slot * D + d) * NF + line) * NP + p) * NV + v] = F[v];
-        }
-        if (VI == VI_HG && i < N - 1 && fabsf(s_alpha[slot]) > P.alpha_atol) {
-          Node<D> na, nb2;
-          load_node(tid, na);
-          load_node(tid + S, nb2);
-          float F[NV];
-          Dv::two_point(P.fv_flux, R, na, nb2, d, gamma, igm1, F);
-#pragma unroll
-          for (int v = 0; v < NV; ++v)
-            s_fv[(((slot * D + d) * NF + line) * (N - 1) + i) * NV + v] = F[v];
-        }
-      }
-    }
+  // ---- lines: volume + surface contributions -----------------------------------
+  {
+    const int dd = tid / (EPB * NF);
+    const int r = tid - dd * (EPB * NF);
+    const int sl = r / NF;
+    const int line = r - sl * NF;
+    if (sl < nel)
+      mixed_line<D, N, VI, VF, SF, EPB>(P, s_ref[sl], s_u, s_fu, s_nd, s_part, s_mat, s_iw,
+                                        VI == VI_HG ? s_elem[sl * 4] : 0.0f, sl, line, dd,
+                                        e0 + sl, e0, nel);
   }
   __syncthreads();
 
-  // ---- gather --------------------------------------------------------------------
-  float du[NV];
-#pragma unroll
-  for (int v = 0; v < NV; ++v) du[v] = 0;
-  if (active) {
-    if (VI == VI_WEAK) {
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        const int S = axis_stride<N>(d);
-        const int i = axis_index<N>(node, d);
-        const int lb = line_base<N>(line_index<N>(node, d), d);
-#pragma unroll
-        for (int l = 0; l < N; ++l) {
-          const float c = s_mat[i * N + l];
-          const int src = slot * NN + lb + l * S;
-#pragma unroll
-          for (int v = 0; v < NV; ++v) du[v] = fmaf(c, s_vol[(d * NV + v) * SP + src], du[v]);
-        }
-      }
-    } else {
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        const int i = axis_index<N>(node, d);
-        const int line = line_index<N>(node, d);
-#pragma unroll
-        for (int l = 0; l < N; ++l) {
-          if (l == i) continue;
-          const int p = l > i ? pair_index<N>(i, l) : pair_index<N>(l, i);
-          const float c = s_mat[i * N + l];
-          const float* F = s_vol + (((slot * D + d) * NF + line) * NP + p) * NV;
-#pragma unroll
-          for (int v = 0; v < NV; ++v) du[v] = fmaf(c, F[v], du[v]);
-        }
-      }
-      if (VI == VI_HG) {
-        const float alpha = s_alpha[slot];
-        if (fabsf(alpha) > P.alpha_atol) {
-          float fv[NV];
-#pragma unroll
-          for (int v = 0; v < NV; ++v) fv[v] = 0;
-#pragma unroll
-          for (int d = 0; d < D; ++d) {
-            const int i = axis_index<N>(node, d);
-            const int line = line_index<N>(node, d);
-            const float iw = s_iw[i];
-            const float* Fb = s_fv + ((slot * D + d) * NF + line) * (N - 1) * NV;
-#pragma unroll
-            for (int v = 0; v < NV; ++v) {
-              const float fr = i < N - 1 ? Fb[i * NV + v] : 0.0f;
-              const float fl = i > 0 ? Fb[(i - 1) * NV + v] : 0.0f;
-              fv[v] += iw * (fr - fl);
-            }
-          }
-#pragma unroll
-          for (int v = 0; v < NV; ++v) du[v] = (1.0f - alpha) * du[v] + alpha * fv[v];
-        }
-      }
-    }
-    const float factor = s_iw[0];
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-      const int i = axis_index<N>(node, d);
-      const int fn = line_index<N>(node, d);
-      if (i == 0) {
-        const float* F = s_face + ((slot * 2 * D + 2 * d) * NF + fn) * NV;
-#pragma unroll
-        for (int v = 0; v < NV; ++v) du[v] = du[v] - F[v] * factor;
-      }
-      if (i == N - 1) {
-        const float* F = s_face + ((slot * 2 * D + 2 * d + 1) * NF + fn) * NV;
-#pragma unroll
-        for (int v = 0; v < NV; ++v) du[v] = du[v] + F[v] * factor;
-      }
-    }
-    const float jfac = -P.inv_jac[e];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) du[v] *= jfac;
-    if (P.source == SRC_CONVERGENCE_TEST) {
-      float x[D], s[NV];
-      const float* xl = P.xline + (size_t)e * D * N;
-#pragma unroll
-      for (int d = 0; d < D; ++d) x[d] = xl[d * N + axis_index<N>(node, d)];
-      Euler<D, float>::source_convergence(x, s_scal[0], gamma, s);
-#pragma unroll
-      for (int v = 0; v < NV; ++v) du[v] += s[v];
-    }
-  }
-  if (A.mode == MODE_RHS) {
-    __syncthreads();
-    // du in FP64 through the (now free) float state buffer as two halves
-    double* s_d = reinterpret_cast<double*>(s_u);
-    if (active) {
-#pragma unroll
-      for (int v = 0; v < NV; ++v) s_d[tid * NV + v] = (double)du[v];
-    }
-    __syncthreads();
-    for (int k = tid; k < nval; k += NT) A.du_out[gofs + k] = s_d[k];
-    return;
-  }
-
-  // ---- 2N stage update in float-float ------------------------------------------
-  const float bdt = s_scal[1];
-  const float a_s = s_scal[2];
+  // ---- nodes: sum of directions, Jacobian, sources, 2N update ---------------------
+  const float bdt = s_scal[0];
+  const float a_s = s_scal[1];
   bool bad = false;
-  if (active) {
+  for (int n = tid; n < nel * NN; n += NT) {
+    const int sl = n / NN;
+    const int node = n - sl * NN;
+    const int64_t e = e0 + sl;
+    const float jfac = -P.inv_jac[e];
+    float du[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      float s = 0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) s += s_part[(d * NV + v) * SP + n];
+      du[v] = s * jfac;
+    }
+    if (P.source == SRC_CONVERGENCE_TEST) {
+      float ph = 0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) ph += P.xoff[(e * D + d) * N + axis_index<N>(node, d)];
+      float sd, cd;
+      sincospif(ph, &sd, &cd);
+      const float s0 = s_elem[sl * 4 + 1], c0 = s_elem[sl * 4 + 2];
+      float src[NV];
+      SourceMMS<D>::eval(s0 * cd + c0 * sd, c0 * cd - s0 * sd, gamma, src);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) du[v] += src[v];
+    }
+    if (A.mode == MODE_RHS) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) s_tmp[n * NV + v] = du[v];
+      continue;
+    }
     float hi[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      const int k = tid * NV + v;
+      const int k = n * NV + v;
       const float ut = du[v] - s_tmp[k] * a_s;
       s_tmp[k] = ut;
       const float2 un = ff_add(s_u[k], ut * bdt);
@@ -643,21 +697,25 @@ __global__ void __launch_bounds__(EPB * Pow<N, D>::value)
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         const float lam = fabsf(w[1 + d]) + cs;
-        if (lam == lam) atomicMax(&s_smax[slot * D + d], __float_as_uint(lam));
+        if (lam == lam) atomicMax(&s_smax[sl * D + d], __float_as_uint(lam));
       }
     }
   }
   if (bad) atomicOr(A.status, 1);
   __syncthreads();
+  if (A.mode == MODE_RHS) {
+    for (int k = tid; k < nval; k += NT) A.du_out[gofs + k] = (double)s_tmp[k];
+    return;
+  }
   for (int k = tid; k < nval; k += NT) {
     A.u_out[gofs + k] = s_u[k];
     A.u_tmp[gofs + k] = s_tmp[k];
   }
-  if (A.speed_bits && active && node == 0) {
+  if (A.speed_bits && tid < nel) {
     float sum = 0;
 #pragma unroll
-    for (int d = 0; d < D; ++d) sum += __uint_as_float(s_smax[slot * D + d]);
-    const float sp = P.inv_jac[e] * sum;
+    for (int d = 0; d < D; ++d) sum += __uint_as_float(s_smax[tid * D + d]);
+    const float sp = P.inv_jac[e0 + tid] * sum;
     if (sp == sp) atomicMax(A.speed_bits, (unsigned long long)__double_as_longlong((double)sp));
   }
 }
