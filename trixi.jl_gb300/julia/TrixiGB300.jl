@@ -1,0 +1,160 @@
+# TrixiGB300.jl -- Julia side of the drop-in: a device backend for Trixi.jl's
+# TreeMesh DGSEM Euler path that forwards to libtrixi_gb300.so through ccall.
+#
+# The seam is rhs_hyperbolic!(backend, du, u, t, mesh, equations, ...)
+# (src/solvers/dgsem_tree/dg_2d.jl:113), selected by trixi_backend(u)
+# (src/auxiliary/containers.jl:278); the KernelAbstractions backend plugs in
+# at the same place (src/solvers/dgsem_p4est/dg_2d_gpu.jl:8).
+#
+# Not exercised in this repository's tests (no Julia toolchain here); the C ABI
+# it calls is tested from Python through the same entry points.
+module TrixiGB300
+
+using Trixi
+
+const lib = joinpath(@__DIR__, "..", "_build", "libtrixi_gb300.so")
+
+# tg_config, include/trixi_gb300.h (field order and types must match)
+struct TgConfig
+    ndims::Int32
+    polydeg::Int32
+    nelements::Int64
+    ninterfaces::Int64
+    gamma::Float64
+    volume_integral::Int32
+    volume_flux::Int32
+    surface_flux::Int32
+    volume_flux_fv::Int32
+    alpha_max::Float64
+    alpha_min::Float64
+    alpha_smooth::Int32
+    source_terms::Int32
+    precision::Int32
+    device::Int32
+    nodes::Ptr{Float64}
+    weights::Ptr{Float64}
+    inverse_weights::Ptr{Float64}
+    derivative_hat::Ptr{Float64}
+    derivative_split::Ptr{Float64}
+    inverse_vandermonde_legendre::Ptr{Float64}
+    neighbor_ids::Ptr{Int64}
+    orientations::Ptr{Int64}
+    inverse_jacobian::Ptr{Float64}
+    node_coordinates::Ptr{Float64}
+    elements_per_block::Int32
+end
+
+const TG_VOLUME_WEAK_FORM, TG_VOLUME_FLUX_DIFFERENCING, TG_VOLUME_SHOCK_CAPTURING_HG = 0, 1, 2
+const TG_FLUX_CENTRAL, TG_FLUX_RANOCHA, TG_FLUX_SHIMA_ETAL = 0, 1, 2
+const TG_FLUX_LAX_FRIEDRICHS, TG_FLUX_LAX_FRIEDRICHS_NAIVE = 3, 4
+
+flux_code(::typeof(Trixi.flux_central)) = TG_FLUX_CENTRAL
+flux_code(::typeof(Trixi.flux_ranocha)) = TG_FLUX_RANOCHA
+flux_code(::typeof(Trixi.flux_shima_etal)) = TG_FLUX_SHIMA_ETAL
+function flux_code(f::Trixi.FluxLaxFriedrichs)
+    f.dissipation.max_abs_speed === Trixi.max_abs_speed_naive ?
+    TG_FLUX_LAX_FRIEDRICHS_NAIVE : TG_FLUX_LAX_FRIEDRICHS
+end
+
+source_code(::Nothing) = 0
+source_code(::typeof(Trixi.source_terms_convergence_test)) = 1
+
+struct GB300Backend end
+
+mutable struct GB300Context
+    ptr::Ptr{Cvoid}
+end
+
+function last_error(ctx::Ptr{Cvoid})
+    buf = Vector{UInt8}(undef, 1024)
+    ccall((:tg_last_error, lib), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t), ctx, buf, length(buf))
+    return unsafe_string(pointer(buf))
+end
+
+check(rc, ctx = C_NULL) = rc == 0 || error("libtrixi_gb300: " * last_error(ctx))
+
+function volume_codes(vi::VolumeIntegralWeakForm, surface_flux)
+    return (TG_VOLUME_WEAK_FORM, TG_FLUX_CENTRAL, flux_code(surface_flux), 0.5, 0.001, true)
+end
+function volume_codes(vi::VolumeIntegralFluxDifferencing, surface_flux)
+    return (TG_VOLUME_FLUX_DIFFERENCING, flux_code(vi.volume_flux), flux_code(surface_flux),
+            0.5, 0.001, true)
+end
+function volume_codes(vi::Trixi.VolumeIntegralShockCapturingHGType, surface_flux)
+    ind = vi.indicator
+    return (TG_VOLUME_SHOCK_CAPTURING_HG, flux_code(vi.volume_integral_blend_high_order.volume_flux),
+            flux_code(vi.volume_integral_blend_low_order.volume_flux_fv),
+            ind.alpha_max, ind.alpha_min, ind.alpha_smooth)
+end
+
+"""
+    create_context(semi; precision = 0, device = 0)
+
+Builds a device context from a `SemidiscretizationHyperbolic` on a periodic
+`TreeMesh` with `DGSEM` (precision 0 = FP64, 1 = mixed FP32/float-float).
+"""
+function create_context(semi; precision = 0, device = 0)
+    (; mesh, equations, solver, cache, source_terms) = semi
+    b = solver.basis
+    vi, vf, sf_fv, amax, amin, asmooth = volume_codes(solver.volume_integral,
+                                                      solver.surface_integral.surface_flux)
+    sf = flux_code(solver.surface_integral.surface_flux)
+    GC.@preserve b cache begin
+        cfg = TgConfig(ndims(mesh), Trixi.polydeg(solver), nelements(solver, cache),
+                       ninterfaces(solver, cache), equations.gamma, vi, vf, sf,
+                       vi == TG_VOLUME_SHOCK_CAPTURING_HG ? sf_fv : sf, amax, amin, asmooth,
+                       source_code(source_terms), precision, device,
+                       pointer(b.nodes), pointer(b.weights), pointer(b.inverse_weights),
+                       pointer(b.derivative_hat), pointer(b.derivative_split),
+                       pointer(b.inverse_vandermonde_legendre),
+                       pointer(cache.interfaces.neighbor_ids),
+                       pointer(cache.interfaces.orientations),
+                       pointer(cache.elements.inverse_jacobian),
+                       pointer(cache.elements.node_coordinates), 0)
+        out = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ccall((:tg_ctx_create, lib), Cint, (Ref{TgConfig}, Ref{Ptr{Cvoid}}), cfg, out))
+    end
+    ctx = GB300Context(out[])
+    finalizer(c -> ccall((:tg_ctx_destroy, lib), Cint, (Ptr{Cvoid},), c.ptr), ctx)
+    return ctx
+end
+
+"""
+    rhs!(ctx, du, u, t)
+
+`rhs_hyperbolic!` for device vectors `du`, `u` (Trixi layout, Float64).
+"""
+function rhs!(ctx::GB300Context, du, u, t)
+    check(ccall((:tg_rhs, lib), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Cdouble),
+                ctx.ptr, pointer(du), pointer(u), t), ctx.ptr)
+    return nothing
+end
+
+upload!(ctx::GB300Context, u::Vector{Float64}) =
+    check(ccall((:tg_upload_state, lib), Cint, (Ptr{Cvoid}, Ptr{Float64}), ctx.ptr, u), ctx.ptr)
+download!(u::Vector{Float64}, ctx::GB300Context) =
+    check(ccall((:tg_download_state, lib), Cint, (Ptr{Cvoid}, Ptr{Float64}), ctx.ptr, u), ctx.ptr)
+
+"""
+    step_to!(ctx, t0, t_end, cfl; max_steps)
+
+CarpenterKennedy2N54 with StepsizeCallback(cfl) semantics on the device (CUDA
+graphs); returns the reached time and the number of steps.
+"""
+function step_to!(ctx::GB300Context, t0, t_end, cfl; max_steps = typemax(Int64))
+    t = Ref{Cdouble}(t0)
+    n = Ref{Int64}(0)
+    check(ccall((:tg_step, lib), Cint,
+                (Ptr{Cvoid}, Int64, Cdouble, Cdouble, Ref{Cdouble}, Ref{Int64}),
+                ctx.ptr, max_steps, cfl, t_end, t, n), ctx.ptr)
+    return t[], n[]
+end
+
+function max_dt(ctx::GB300Context)
+    dt = Ref{Cdouble}(0)
+    check(ccall((:tg_max_dt, lib), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ref{Cdouble}),
+                ctx.ptr, C_NULL, dt), ctx.ptr)
+    return dt[]
+end
+
+end # module
