@@ -134,7 +134,8 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out);
 int tg_ctx_destroy(tg_ctx* ctx);
 
 /* Message of the last failed call on ctx (ctx == NULL: last failed
- * tg_ctx_create of this thread).  Always NUL-terminates when len > 0. */
+ * tg_ctx_create or tg_integrals_noalloc of this thread).  Always
+ * NUL-terminates when len > 0. */
 int tg_last_error(const tg_ctx* ctx, char* buf, size_t len);
 
 /* ndofs(mesh, dg, cache) (dg.jl:969-971) and ndofs * nvariables. */
@@ -200,6 +201,25 @@ int tg_synchronize(tg_ctx* ctx);
 /* The context's CUDA stream (a cudaStream_t), for callers that order their
  * own work or timing events with the library's launches. */
 int tg_stream(tg_ctx* ctx, void** stream);
+
+/* Allocation-free variant of tg_integrals, for callers that cannot allocate
+ * device memory (a fixed-size memory pool, a runtime that owns all device
+ * memory, work recorded while allocation is forbidden) and so cannot create a
+ * context.  It has no counterpart in the reference.  Computes the same FP64
+ * integrals (conserved totals, entropy, kinetic energy; ndims + 4 values) of
+ * an FP64 state u_dev in Trixi's layout, with the element inverse Jacobians
+ * inverse_jacobian_dev[nelements] and the LGL weights weights[polydeg + 1]
+ * (host array), into out_dev on `stream` (a cudaStream_t; NULL = legacy
+ * default stream), asynchronously.  It calls no cudaMalloc/cudaFree: its
+ * scratch is a 4 MiB static device array, which limits nelements to
+ * 4,194,304 (larger meshes are rejected with TG_ERR_INVALID_ARGUMENT and a
+ * message for tg_last_error(NULL, ...)).  The first call on a device resolves
+ * the array's device address; make that first call before any stream
+ * capture.  All calls share the array, so calls that overlap on the GPU (for
+ * example on two streams at once) race. */
+int tg_integrals_noalloc(int32_t ndims, int32_t polydeg, int64_t nelements, double gamma,
+                         const double* weights, const double* u_dev,
+                         const double* inverse_jacobian_dev, double* out_dev, void* stream);
 
 /* Elements per CUDA block in use (set by tg_config.elements_per_block or the
  * library default for the (ndims, polydeg, precision) combination). */

@@ -387,6 +387,10 @@ struct tg_ctx {
 
 static thread_local std::string g_create_err;
 
+namespace tg {
+void set_thread_error(const char* msg) { g_create_err = msg; }
+}  // namespace tg
+
 static int fail(tg_ctx* c, int code, const char* fmt, ...) {
   char buf[512];
   va_list ap;

@@ -28,7 +28,7 @@ EXPORTS = ("tg_api_version", "tg_ctx_create", "tg_ctx_destroy", "tg_last_error",
            "tg_upload_state", "tg_download_state", "tg_state_device_ptr", "tg_rhs",
            "tg_rhs_host", "tg_max_dt", "tg_rk_stage", "tg_step", "tg_set_time",
            "tg_integrals", "tg_alpha", "tg_status", "tg_synchronize",
-           "tg_elements_per_block", "tg_stream")
+           "tg_elements_per_block", "tg_stream", "tg_integrals_noalloc")
 
 
 class TrixiGB300Error(RuntimeError):
@@ -105,6 +105,7 @@ def load(path: str | None = None):
         "tg_synchronize": ([vp], ctypes.c_int),
         "tg_elements_per_block": ([vp, P(i32)], ctypes.c_int),
         "tg_stream": ([vp, P(vp)], ctypes.c_int),
+        "tg_integrals_noalloc": ([i32, i32, i64, d, pd, vp, vp, vp, vp], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)
