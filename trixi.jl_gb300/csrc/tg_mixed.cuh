@@ -83,6 +83,7 @@ struct Node {
   float dw[D + 2];      // primitive deviation (drho, dv_1..dv_D, dp)
   float w[D + 2];       // full primitives
   float dq;             // deviation of rho/p from the reference q
+  float vo, dvo;        // velocity along the current direction and its deviation
 };
 
 template <int D>
@@ -162,6 +163,13 @@ struct Dev {
     return r;
   }
 
+  // Velocity components along direction o, selected once per node and line
+  // (the fluxes below use n.vo / n.dvo and the reference's vro = v_ref[o]).
+  static __host__ __device__ __forceinline__ void orient(Node<D>& n, int o) {
+    n.vo = pick(n.w + 1, o);
+    n.dvo = pick(n.dw + 1, o);
+  }
+
   // ln_mean(x_ref + dx, x_ref + dy) - x_ref (series below f^2 < 0.05, see
   // tg_physics.cuh for the FP32 threshold)
   static __host__ __device__ __forceinline__ float dev_ln_mean(float xr, float dx, float dy, float x,
@@ -178,8 +186,8 @@ struct Dev {
 
   // physical flux deviation f(w) - f(w_ref), orientation o
   static __host__ __device__ __forceinline__ void dflux(const RefState<D>& R, const Node<D>& a, int o,
-                                                float gamma, float igm1, float* f) {
-    const float vro = pick(R.v, o), vo = pick(a.w + 1, o), dvo = pick(a.dw + 1, o);
+                                                float vro, float gamma, float igm1, float* f) {
+    const float vo = a.vo, dvo = a.dvo;
     const float d1 = a.dw[0] * vro + a.w[0] * dvo;
     const float F1r = R.rho * vro;
     f[0] = d1;
@@ -194,22 +202,22 @@ struct Dev {
   }
 
   static __host__ __device__ __forceinline__ void dcentral(const RefState<D>& R, const Node<D>& a,
-                                                   const Node<D>& b, int o, float gamma,
+                                                   const Node<D>& b, int o, float vro, float gamma,
                                                    float igm1, float* f) {
     float fa[NV], fb[NV];
-    dflux(R, a, o, gamma, igm1, fa);
-    dflux(R, b, o, gamma, igm1, fb);
+    dflux(R, a, o, vro, gamma, igm1, fa);
+    dflux(R, b, o, vro, gamma, igm1, fb);
 #pragma unroll
     for (int v = 0; v < NV; ++v) f[v] = 0.5f * (fa[v] + fb[v]);
   }
 
   static __host__ __device__ __forceinline__ void dllf(const RefState<D>& R, const Node<D>& a,
-                                               const Node<D>& b, int o, bool naive, float gamma,
-                                               float igm1, float* f) {
-    dcentral(R, a, b, o, gamma, igm1, f);
+                                               const Node<D>& b, int o, float vro, bool naive,
+                                               float gamma, float igm1, float* f) {
+    dcentral(R, a, b, o, vro, gamma, igm1, f);
     const float ca = sqrtf(gamma * a.w[P] / a.w[0]);
     const float cb = sqrtf(gamma * b.w[P] / b.w[0]);
-    const float va = fabsf(pick(a.w + 1, o)), vb = fabsf(pick(b.w + 1, o));
+    const float va = fabsf(a.vo), vb = fabsf(b.vo);
     const float lam = naive ? fmaxf(va, vb) + fmaxf(ca, cb) : fmaxf(va + ca, vb + cb);
 #pragma unroll
     for (int v = 0; v < NV; ++v) f[v] = f[v] + (-0.5f * lam * (b.du[v] - a.du[v]));
@@ -217,7 +225,8 @@ struct Dev {
 
   // flux_ranocha(a, b) - f(w_ref)
   static __host__ __device__ __forceinline__ void dranocha(const RefState<D>& R, const Node<D>& a,
-                                                   const Node<D>& b, int o, float igm1, float* f) {
+                                                   const Node<D>& b, int o, float vro, float igm1,
+                                                   float* f) {
     const float drho_ln = dev_ln_mean(R.rho, a.dw[0], b.dw[0], a.w[0], b.w[0]);
     // q = rho / p relative to R.q (node deviations a.dq, b.dq from make_node)
     const float dq_ln = dev_ln_mean(R.q, a.dq, b.dq, R.q + a.dq, R.q + b.dq);
@@ -232,9 +241,9 @@ struct Dev {
     }
     dvsq *= 0.5f;
     const float dpavg = 0.5f * (a.dw[P] + b.dw[P]);
-    const float vro = pick(R.v, o);
     const float F1r = R.rho * vro;
-    const float d1 = R.rho * pick(dvavg, o) + drho_ln * pick(vavg, o);
+    const float dvavgo = 0.5f * (a.dvo + b.dvo);
+    const float d1 = R.rho * dvavgo + drho_ln * (vro + dvavgo);
     f[0] = d1;
 #pragma unroll
     for (int d = 0; d < D; ++d) f[1 + d] = d1 * vavg[d] + F1r * dvavg[d] + ((d == o) ? dpavg : 0.0f);
@@ -243,7 +252,7 @@ struct Dev {
     for (int d = 0; d < D; ++d) vsq += a.w[1 + d] * b.w[1 + d];
     const float H = 0.5f * vsq + igm1 / q_ln;
     const float dH = dvsq + igm1 * (R.rq - R.p * dq_ln) / (R.rho * q_ln);
-    const float dvao = pick(a.dw + 1, o), dvbo = pick(b.dw + 1, o);
+    const float dvao = a.dvo, dvbo = b.dvo;
     const float dpv = 0.5f * (R.p * (dvao + dvbo) + vro * (a.dw[P] + b.dw[P]) +
                               a.dw[P] * dvbo + b.dw[P] * dvao);
     f[P] = d1 * H + F1r * dH + dpv;
@@ -251,7 +260,8 @@ struct Dev {
 
   // flux_shima_etal(a, b) - f(w_ref)
   static __host__ __device__ __forceinline__ void dshima(const RefState<D>& R, const Node<D>& a,
-                                                 const Node<D>& b, int o, float igm1, float* f) {
+                                                 const Node<D>& b, int o, float vro, float igm1,
+                                                 float* f) {
     const float drho = 0.5f * (a.dw[0] + b.dw[0]);
     float dvavg[D], vavg[D];
     float dkin = 0, kin = 0;
@@ -265,40 +275,41 @@ struct Dev {
     dkin *= 0.5f;
     kin *= 0.5f;
     const float dpavg = 0.5f * (a.dw[P] + b.dw[P]);
-    const float vro = pick(R.v, o);
     const float F1r = R.rho * vro;
-    const float d1 = R.rho * pick(dvavg, o) + drho * pick(vavg, o);
+    const float dvavgo = 0.5f * (a.dvo + b.dvo);
+    const float vavgo = vro + dvavgo;
+    const float d1 = R.rho * dvavgo + drho * vavgo;
     f[0] = d1;
 #pragma unroll
     for (int d = 0; d < D; ++d) f[1 + d] = d1 * vavg[d] + F1r * dvavg[d] + ((d == o) ? dpavg : 0.0f);
-    const float dvao = pick(a.dw + 1, o), dvbo = pick(b.dw + 1, o);
+    const float dvao = a.dvo, dvbo = b.dvo;
     const float dpv = 0.5f * (R.p * (dvao + dvbo) + vro * (a.dw[P] + b.dw[P]) +
                               a.dw[P] * dvbo + b.dw[P] * dvao);
-    f[P] = igm1 * (dpavg * pick(vavg, o) + R.p * pick(dvavg, o)) + d1 * kin + F1r * dkin + dpv;
+    f[P] = igm1 * (dpavg * vavgo + R.p * dvavgo) + d1 * kin + F1r * dkin + dpv;
   }
 
   // KIND >= 0 selects the flux at compile time; KIND < 0 dispatches on `kind`.
   template <int KIND>
   static __host__ __device__ __forceinline__ void flux2(int kind, const RefState<D>& R,
                                                          const Node<D>& a, const Node<D>& b, int o,
-                                                         float gamma, float igm1, float* f) {
-    if constexpr (KIND == FLUX_RANOCHA) dranocha(R, a, b, o, igm1, f);
-    else if constexpr (KIND == FLUX_SHIMA_ETAL) dshima(R, a, b, o, igm1, f);
-    else if constexpr (KIND == FLUX_LLF) dllf(R, a, b, o, false, gamma, igm1, f);
-    else if constexpr (KIND == FLUX_LLF_NAIVE) dllf(R, a, b, o, true, gamma, igm1, f);
-    else if constexpr (KIND == FLUX_CENTRAL) dcentral(R, a, b, o, gamma, igm1, f);
-    else two_point(kind, R, a, b, o, gamma, igm1, f);
+                                                         float vro, float gamma, float igm1, float* f) {
+    if constexpr (KIND == FLUX_RANOCHA) dranocha(R, a, b, o, vro, igm1, f);
+    else if constexpr (KIND == FLUX_SHIMA_ETAL) dshima(R, a, b, o, vro, igm1, f);
+    else if constexpr (KIND == FLUX_LLF) dllf(R, a, b, o, vro, false, gamma, igm1, f);
+    else if constexpr (KIND == FLUX_LLF_NAIVE) dllf(R, a, b, o, vro, true, gamma, igm1, f);
+    else if constexpr (KIND == FLUX_CENTRAL) dcentral(R, a, b, o, vro, gamma, igm1, f);
+    else two_point(kind, R, a, b, o, vro, gamma, igm1, f);
   }
 
   static __host__ __device__ __forceinline__ void two_point(int kind, const RefState<D>& R,
                                                     const Node<D>& a, const Node<D>& b, int o,
-                                                    float gamma, float igm1, float* f) {
+                                                    float vro, float gamma, float igm1, float* f) {
     switch (kind) {
-      case FLUX_RANOCHA: dranocha(R, a, b, o, igm1, f); break;
-      case FLUX_SHIMA_ETAL: dshima(R, a, b, o, igm1, f); break;
-      case FLUX_LLF: dllf(R, a, b, o, false, gamma, igm1, f); break;
-      case FLUX_LLF_NAIVE: dllf(R, a, b, o, true, gamma, igm1, f); break;
-      default: dcentral(R, a, b, o, gamma, igm1, f); break;
+      case FLUX_RANOCHA: dranocha(R, a, b, o, vro, igm1, f); break;
+      case FLUX_SHIMA_ETAL: dshima(R, a, b, o, vro, igm1, f); break;
+      case FLUX_LLF: dllf(R, a, b, o, vro, false, gamma, igm1, f); break;
+      case FLUX_LLF_NAIVE: dllf(R, a, b, o, vro, true, gamma, igm1, f); break;
+      default: dcentral(R, a, b, o, vro, gamma, igm1, f); break;
     }
   }
 };
@@ -335,6 +346,23 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // registers; the D partial sums per node meet once in shared memory.  All
 // global reads of a block (state chunk, u_tmp chunk and the neighbour traces
 // of faces between blocks) are issued up front as cp.async copies.
+// Position of node n of block slot `slot` inside one SoA field of the node
+// arrays.  For 3D polydeg 3 (the production case) the slot stride is 80
+// (= 16 mod 32) with 4 words of padding after every 16 nodes: then the 32
+// lanes of a warp (2 elements x 16 lines of one direction) hit 32 distinct
+// banks for y- and z-lines, and an x-line's 4 nodes stay contiguous and
+// 16-byte aligned so it reads each field with one 128-bit load.
+template <int D, int N, int EPB>
+struct NodeLayout {
+  static constexpr int NN = Pow<N, D>::value;
+  static constexpr bool PADDED = (D == 3 && N == 4);
+  static constexpr int SS = PADDED ? 80 : NN;
+  static constexpr int FS = PADDED ? EPB * 80 : EPB * NN + 1;  // field stride
+  static __host__ __device__ __forceinline__ int pos(int slot, int n) {
+    return PADDED ? slot * SS + n + 4 * (n >> 4) : slot * SS + n;
+  }
+};
+
 template <int D, int N, int VI, int EPB>
 struct MixedKernel {
   static constexpr int NV = D + 2;
@@ -342,15 +370,17 @@ struct MixedKernel {
   static constexpr int NF = NN / N;          // lines per direction = nodes per face
   static constexpr int L = D * NF;           // lines per element
   static constexpr int NT = EPB * L;         // threads per block
-  static constexpr int SP = EPB * NN + 1;    // SoA stride of node fields
+  static constexpr int SP = NodeLayout<D, N, EPB>::FS;  // field stride of node arrays
   static constexpr int NFLD = 2 * NV + 1;    // dw[NV], dq, du[NV]
   static constexpr int CHUNK = EPB * NN * NV;
   static constexpr int FACE = EPB * 2 * D * NF * NV;  // neighbour traces (float2)
   static constexpr int REFW = (sizeof(RefState<D>) + 3) / 4;
   static constexpr int MINB = NT <= 128 ? 4 : (NT <= 256 ? 3 : 1);  // resident blocks per SM
 
+  static constexpr int ALIGN4 = (4 - (CHUNK % 4)) % 4;  // keeps node fields 16-byte aligned
+
   static constexpr size_t smem_bytes() {
-    return sizeof(float2) * (CHUNK + FACE) + sizeof(float) * CHUNK  // state, traces, u_tmp
+    return sizeof(float2) * (CHUNK + FACE) + sizeof(float) * (CHUNK + ALIGN4)  // state, traces, u_tmp
            + sizeof(float) * (NFLD * SP + D * NV * SP               // node fields, partial du
                               + EPB * REFW + EPB * 4 + 4            // references, per element
                               + EPB * D                             // speed maxima
@@ -390,25 +420,52 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
                                            const float* s_iw, float alpha, int slot, int line,
                                            int dd, int64_t e, int64_t e0, int nel) {
   using K = MixedKernel<D, N, VI, EPB>;
+  using Lay = NodeLayout<D, N, EPB>;
   using Dv = Dev<D>;
   constexpr int NV = K::NV, NN = K::NN, SP = K::SP, NF = K::NF;
   const float gamma = P.gamma, igm1 = P.inv_gamma_minus_one;
   const int S = axis_stride<N>(dd);
   const int lb = line_base<N>(line, dd);
-  const int base = slot * NN + lb;
+  const float vro = Dv::pick(R.v, dd);
   constexpr bool NEED_DU = VI == VI_HG || VF < 0 || VF == FLUX_LLF || VF == FLUX_LLF_NAIVE;
+  // node a of the line sits at field position pos(slot, lb + a S)
+  const bool vec4 = Lay::PADDED && dd == 0;  // x-line: 4 contiguous, aligned nodes
   Node<D> nd[N];
+  {
+    constexpr int NLOAD = NEED_DU ? 2 * NV + 1 : NV + 1;
 #pragma unroll
-  for (int a = 0; a < N; ++a) {
-    const int idx = base + a * S;
+    for (int f = 0; f < NLOAD; ++f) {
+      float x[N];
+      if constexpr (N == 4) {
+        if (vec4) {
+          const float4 q = *reinterpret_cast<const float4*>(s_nd + f * SP + Lay::pos(slot, lb));
+          x[0] = q.x;
+          x[1] = q.y;
+          x[2] = q.z;
+          x[3] = q.w;
+        } else {
 #pragma unroll
-    for (int v = 0; v < NV; ++v) nd[a].dw[v] = s_nd[v * SP + idx];
-    nd[a].dq = s_nd[NV * SP + idx];
-    if (NEED_DU) {
+          for (int a = 0; a < N; ++a) x[a] = s_nd[f * SP + Lay::pos(slot, lb + a * S)];
+        }
+      } else {
 #pragma unroll
-      for (int v = 0; v < NV; ++v) nd[a].du[v] = s_nd[(NV + 1 + v) * SP + idx];
+        for (int a = 0; a < N; ++a) x[a] = s_nd[f * SP + Lay::pos(slot, lb + a * S)];
+      }
+#pragma unroll
+      for (int a = 0; a < N; ++a) {
+        if (f < NV)
+          nd[a].dw[f] = x[a];
+        else if (f == NV)
+          nd[a].dq = x[a];
+        else
+          nd[a].du[f - NV - 1] = x[a];
+      }
     }
-    Dv::complete(R, nd[a]);
+#pragma unroll
+    for (int a = 0; a < N; ++a) {
+      Dv::complete(R, nd[a]);
+      Dv::orient(nd[a], dd);
+    }
   }
   float acc[N][NV];
 #pragma unroll
@@ -421,7 +478,7 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
 #pragma unroll
     for (int a = 0; a < N; ++a) {
       float f[NV];
-      Dv::dflux(R, nd[a], dd, gamma, igm1, f);
+      Dv::dflux(R, nd[a], dd, vro, gamma, igm1, f);
 #pragma unroll
       for (int ii = 0; ii < N; ++ii) {
         const float c = s_mat[ii * N + a];
@@ -436,7 +493,7 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
 #pragma unroll
       for (int b = a + 1; b < N; ++b) {
         float F[NV];
-        Dv::template flux2<VF>(P.volume_flux, R, nd[a], nd[b], dd, gamma, igm1, F);
+        Dv::template flux2<VF>(P.volume_flux, R, nd[a], nd[b], dd, vro, gamma, igm1, F);
         const float cab = s_mat[a * N + b], cba = s_mat[b * N + a];
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
@@ -453,7 +510,7 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
 #pragma unroll
       for (int a = 0; a + 1 < N; ++a) {
         float F[NV];
-        Dv::two_point(P.fv_flux, R, nd[a], nd[a + 1], dd, gamma, igm1, F);
+        Dv::two_point(P.fv_flux, R, nd[a], nd[a + 1], dd, vro, gamma, igm1, F);
         const float ca = alpha * s_iw[a], cb = alpha * s_iw[a + 1];
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
@@ -486,33 +543,44 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
     }
     Node<D> nn_;
     Dv::make_node(hi, lo, R, gamma, nn_);
+    Dv::orient(nn_, dd);
     Node<D>& own = side ? nd[N - 1] : nd[0];
     if (!NEED_DU) {
-      const int idx = base + (side ? (N - 1) * S : 0);
+      const int idx = Lay::pos(slot, lb + (side ? (N - 1) * S : 0));
 #pragma unroll
       for (int v = 0; v < NV; ++v) own.du[v] = s_nd[(NV + 1 + v) * SP + idx];
     }
     float F[NV];
     if (side) {
-      Dv::template flux2<SF>(P.surface_flux, R, own, nn_, dd, gamma, igm1, F);
+      Dv::template flux2<SF>(P.surface_flux, R, own, nn_, dd, vro, gamma, igm1, F);
 #pragma unroll
       for (int v = 0; v < NV; ++v) acc[N - 1][v] = fmaf(F[v], factor, acc[N - 1][v]);
     } else {
-      Dv::template flux2<SF>(P.surface_flux, R, nn_, own, dd, gamma, igm1, F);
+      Dv::template flux2<SF>(P.surface_flux, R, nn_, own, dd, vro, gamma, igm1, F);
 #pragma unroll
       for (int v = 0; v < NV; ++v) acc[0][v] = fmaf(-F[v], factor, acc[0][v]);
     }
   }
 #pragma unroll
-  for (int a = 0; a < N; ++a)
+  for (int v = 0; v < NV; ++v) {
+    float* dst = s_part + (dd * NV + v) * SP;
+    if constexpr (N == 4) {
+      if (vec4) {
+        *reinterpret_cast<float4*>(dst + Lay::pos(slot, lb)) =
+            make_float4(acc[0][v], acc[1][v], acc[2][v], acc[3][v]);
+        continue;
+      }
+    }
 #pragma unroll
-    for (int v = 0; v < NV; ++v) s_part[(dd * NV + v) * SP + base + a * S] = acc[a][v];
+    for (int a = 0; a < N; ++a) dst[Lay::pos(slot, lb + a * S)] = acc[a][v];
+  }
 }
 
 template <int D, int N, int VI, int VF, int SF, int EPB>
 __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D, N, VI, EPB>::MINB)
     mixed_element_kernel(const MixedParams P, const MixedArgs A) {
   using K = MixedKernel<D, N, VI, EPB>;
+  using Lay = NodeLayout<D, N, EPB>;
   using Dv = Dev<D>;
   constexpr int NV = K::NV, NN = K::NN, NF = K::NF, NT = K::NT, SP = K::SP;
   constexpr int CHUNK = K::CHUNK, NFLD = K::NFLD, FACE = K::FACE;
@@ -522,7 +590,7 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
   float2* s_u = reinterpret_cast<float2*>(smem_raw);
   float2* s_fu = s_u + CHUNK;                               // neighbour traces
   float* s_tmp = reinterpret_cast<float*>(s_fu + FACE);
-  float* s_nd = s_tmp + CHUNK;
+  float* s_nd = s_tmp + CHUNK + K::ALIGN4;
   float* s_part = s_nd + NFLD * SP;
   RefState<D>* s_ref = reinterpret_cast<RefState<D>*>(s_part + D * NV * SP);
   float* s_elem = reinterpret_cast<float*>(s_ref + EPB);  // [EPB][4]: alpha, sin, cos
@@ -622,12 +690,13 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
     }
     Node<D> nd;
     Dv::make_node(hi, lo, s_ref[sl], gamma, nd);
+    const int ps = Lay::pos(sl, n - sl * NN);
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      s_nd[v * SP + n] = nd.dw[v];
-      s_nd[(NV + 1 + v) * SP + n] = nd.du[v];
+      s_nd[v * SP + ps] = nd.dw[v];
+      s_nd[(NV + 1 + v) * SP + ps] = nd.du[v];
     }
-    s_nd[NV * SP + n] = nd.dq;
+    s_nd[NV * SP + ps] = nd.dq;
   }
   __syncthreads();
 
@@ -653,12 +722,13 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
     const int node = n - sl * NN;
     const int64_t e = e0 + sl;
     const float jfac = -P.inv_jac[e];
+    const int ps = Lay::pos(sl, node);
     float du[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       float s = 0;
 #pragma unroll
-      for (int d = 0; d < D; ++d) s += s_part[(d * NV + v) * SP + n];
+      for (int d = 0; d < D; ++d) s += s_part[(d * NV + v) * SP + ps];
       du[v] = s * jfac;
     }
     if (P.source == SRC_CONVERGENCE_TEST) {
