@@ -335,7 +335,8 @@ def main():
         "accuracy": acc,
         "roofline": {"bound": "hbm", "achieved": roof["achieved"], "peak": roof["peak"],
                      "unit": "GB/s", "frac": roof["achieved"] / roof["peak"],
-                     "traffic": roof["traffic"], "kernel": "dg_element_kernel<3,4,float,FD>",
+                     "traffic": roof["traffic"],
+                     "kernel": "mixed_element_kernel<3,4,FD,flux_ranocha,flux_lax_friedrichs>",
                      "stage_ms": roof["stage_ms"], "algorithmic_bytes": roof["alg_bytes"],
                      "peak_source": roof["peak_src"]},
         "cpu_baseline": cpu,
