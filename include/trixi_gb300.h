@@ -221,6 +221,41 @@ int tg_integrals_noalloc(int32_t ndims, int32_t polydeg, int64_t nelements, doub
                          const double* weights, const double* u_dev,
                          const double* inverse_jacobian_dev, double* out_dev, void* stream);
 
+/* ---- Learned shock indicator ----------------------------------------------
+ * A small MLP (2D polydeg 3: 16 -> 64 -> 64 -> 1; 3D: 64 -> 128 -> 128 -> 1,
+ * ReLU, BF16 weights, FP32 accumulation) predicting log10 of the
+ * Hennemann-Gassner smoothness indicator E of an element from its normalised
+ * modal coefficients of density*pressure (indicators_2d.jl:30-101).  Deployed
+ * in place of IndicatorHennemannGassner for TG_VOLUME_SHOCK_CAPTURING_HG
+ * contexts; the HG indicator stays as fallback (elements whose prediction is
+ * within `band` decades of the switching threshold, or whose nodal
+ * density*pressure is not positive) and as the judge of its error.  No
+ * counterpart in the reference, which has no learned indicator. */
+typedef struct tg_mlp tg_mlp;
+int tg_mlp_create(int32_t ndims, int32_t polydeg, int32_t hidden, uint64_t seed, tg_mlp** out);
+int tg_mlp_destroy(tg_mlp* m);
+int tg_mlp_nparams(const tg_mlp* m, int64_t* n);
+/* FP32 master parameters, layout W1[H][NM], b1[H], W2[H][H], b2[H], w3[H], b3. */
+int tg_mlp_get_params(tg_mlp* m, float* host);
+int tg_mlp_set_params(tg_mlp* m, const float* host);
+/* Appends the (features, log10 E) pairs of every stride-th element of the
+ * context's current state to the network's training set. */
+int tg_mlp_harvest(tg_mlp* m, tg_ctx* c, int32_t stride, int32_t phase, int64_t* total);
+int tg_mlp_dataset(tg_mlp* m, float* x_host, float* y_host);
+/* Adam on the mean squared error of log10 E, minibatches drawn with
+ * replacement; rows i with i % holdout == 0 are held out (holdout > 1). */
+int tg_mlp_train(tg_mlp* m, int64_t steps, int32_t batch, float lr, int32_t holdout,
+                 uint64_t seed, float* mean_loss);
+/* Gradient of the MSE over explicit rows (for checks against a CPU oracle). */
+int tg_mlp_gradient(tg_mlp* m, const float* x_host, const float* y_host, int32_t n,
+                    float* grad_host, float* loss_host);
+int tg_mlp_predict(tg_mlp* m, const float* x_host, int64_t n, float* pred_host);
+/* Use m as the context's shock indicator (m == NULL: back to HG). */
+int tg_ctx_set_learned_indicator(tg_ctx* ctx, tg_mlp* m, float band);
+/* Diagnostics of the last indicator evaluation and running fallback counts
+ * {elements evaluated, band fallbacks, positivity fallbacks}. */
+int tg_mlp_last(tg_mlp* m, float* pred, float* hg, int32_t* flag, uint64_t* counts);
+
 /* Elements per CUDA block in use (set by tg_config.elements_per_block or the
  * library default for the (ndims, polydeg, precision) combination). */
 int tg_elements_per_block(const tg_ctx* ctx, int32_t* epb);

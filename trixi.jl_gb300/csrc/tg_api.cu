@@ -381,6 +381,8 @@ struct tg_ctx {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   bool clock_valid = false;
   bool uploaded = false;
+  tg_mlp* learned = nullptr;      // learned shock indicator (HG contexts), or null
+  const void* view_state = nullptr;  // state the learned indicator reads next
   std::vector<double> weights;
   std::string err;
 };
@@ -389,6 +391,7 @@ static thread_local std::string g_create_err;
 
 namespace tg {
 void set_thread_error(const char* msg) { g_create_err = msg; }
+int mlp_alpha(tg_mlp* m, tg_ctx* c, void* alpha_raw, bool fp64, float alpha_min, float alpha_max);
 }  // namespace tg
 
 static int fail(tg_ctx* c, int code, const char* fmt, ...) {
@@ -468,6 +471,13 @@ static const double* export_state(tg_ctx* c, int* rc) {
 static int indicator(tg_ctx* c, const void* u) {
   if (c->vi != VI_HG) return TG_OK;
   int rc;
+  if (c->learned) {
+    c->view_state = u;
+    rc = mlp_alpha(c->learned, c, c->d_alpha_raw, c->fp64, (float)c->P.alpha_min,
+                   (float)c->P.alpha_max);
+    c->view_state = nullptr;
+    return rc;
+  }
   if (c->fp64)
     rc = launch_indicator(c->D, c->N, true, c->P, (const double*)u, c->d_alpha_raw, c->stream);
   else if (c->D == 2)
@@ -556,6 +566,37 @@ static int reduce_speed(tg_ctx* c, const double* u, unsigned long long* dst) {
   CUDA_TRY(c, cudaGetLastError());
   return TG_OK;
 }
+
+namespace tg {
+// State, shape and basis of a context for the learned indicator (tg_learned.cu).
+int ctx_state_view(tg_ctx* c, const void** state, int* is_ff, int* D, int* N, int64_t* E,
+                   double* gamma, const double** vinv_rowmajor, void** stream) {
+  if (!c) return TG_ERR_INVALID_ARGUMENT;
+  *state = c->view_state ? c->view_state : c->d_u[c->cur];
+  *is_ff = c->fp64 ? 0 : 1;
+  *D = c->D;
+  *N = c->N;
+  *E = c->E;
+  *gamma = c->P.gamma;
+  *vinv_rowmajor = c->P.Vinv;
+  *stream = (void*)c->stream;
+  return TG_OK;
+}
+
+int ctx_set_alpha_source(tg_ctx* c, tg_mlp* m) {
+  if (m && c->vi != VI_HG)
+    return fail(c, TG_ERR_STATE, "the learned indicator replaces the HG indicator: "
+                                 "VolumeIntegralShockCapturingHG contexts only");
+  c->learned = m;
+  // step graphs embed the indicator launches: capture them again
+  for (int p = 0; p < 2; ++p)
+    if (c->graph[p]) {
+      cudaGraphExecDestroy(c->graph[p]);
+      c->graph[p] = nullptr;
+    }
+  return TG_OK;
+}
+}  // namespace tg
 
 extern "C" {
 

@@ -1,0 +1,762 @@
+// Learned shock indicator: a small MLP that predicts the Hennemann-Gassner
+// smoothness indicator of an element from its modal coefficients.
+//
+// Features.  The n^d modal coefficients m of density*pressure (the same
+// dimension-wise inverse-Vandermonde transform as the HG indicator,
+// indicators_2d.jl:50-56 / indicators_3d.jl:54-60), normalised to unit
+// energy, m / |m|.
+// Target.   log10 of the HG energy indicator E = max(energy fractions of the
+// highest and second-highest modes) (indicators_2d.jl:58-90); the HG logistic
+// map alpha = 1 / (1 + exp(-s/T (E - T))), the clipping at alpha_min and the
+// cap alpha_max (indicators_2d.jl:92-100) are then applied to the prediction
+// exactly as to E itself.
+// Fallback/judge.  Elements whose predicted log10 E lies within `band`
+// decades of log10 T (where alpha switches on) or whose nodal rho*p is not
+// positive take the HG alpha, which is computed from the same modes.
+//
+// Network: NM -> H -> H -> 1 with ReLU (2D polydeg 3: 16 -> 64 -> 64 -> 1,
+// 3D: 64 -> 128 -> 128 -> 1), weights stored in BF16 for the forward pass
+// with FP32 master copies, FP32 accumulation, trained with Adam on the MSE of
+// log10 E by the fused forward+backward kernel below.  Layers this small
+// (K = 16..128) run on the CUDA cores.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/trixi_gb300.h"
+#include "tg_dg.cuh"
+
+namespace tg {
+void set_thread_error(const char* msg);
+// Provided by tg_api.cu: state access and basis of a context.
+int ctx_state_view(tg_ctx* c, const void** state, int* is_ff, int* D, int* N, int64_t* E,
+                   double* gamma, const double** vinv_rowmajor, void** stream);
+int ctx_set_alpha_source(tg_ctx* c, struct tg_mlp* m);
+}  // namespace tg
+
+struct tg_mlp {
+  int D = 2, N = 4, NM = 16, H = 64;
+  int64_t nparams = 0;
+  float* d_w = nullptr;              // FP32 master parameters
+  __nv_bfloat16* d_wb = nullptr;     // BF16 copy used by the kernels
+  float* d_g = nullptr;              // gradients
+  float* d_m = nullptr;              // Adam first moments
+  float* d_v = nullptr;              // Adam second moments
+  float* d_x = nullptr;              // dataset features [cap][NM]
+  float* d_y = nullptr;              // dataset targets [cap]
+  int64_t cap = 0, count = 0;
+  float* d_loss = nullptr;           // [2]: loss sum, sample count
+  int64_t adam_t = 0;
+  float band = 0.5f;                 // confidence band in decades of E
+  double log10_threshold = 0.0;      // log10 T of the HG indicator
+  // deployment scratch
+  float* d_feat = nullptr;           // [E][NM] features of the current state
+  float* d_pred = nullptr;           // [E] predicted log10 E
+  float* d_hg = nullptr;             // [E] HG alpha (unsmoothed)
+  int32_t* d_flag = nullptr;         // [E] fallback reason (0 none, 1 band, 2 positivity)
+  int64_t ecap = 0;
+  unsigned long long* d_stats = nullptr;  // [3]: elements, band fallbacks, positivity fallbacks
+  std::string err;
+};
+
+namespace tg {
+
+// Offsets of the parameter blocks: W1[H][NM], b1[H], W2[H][H], b2[H], w3[H], b3.
+struct MlpLayout {
+  int NM, H;
+  __host__ __device__ int w1() const { return 0; }
+  __host__ __device__ int b1() const { return H * NM; }
+  __host__ __device__ int w2() const { return H * NM + H; }
+  __host__ __device__ int b2() const { return H * NM + H + H * H; }
+  __host__ __device__ int w3() const { return H * NM + 2 * H + H * H; }
+  __host__ __device__ int b3() const { return H * NM + 3 * H + H * H; }
+  __host__ __device__ int count() const { return H * NM + 3 * H + H * H + 1; }
+};
+
+__device__ __forceinline__ float wld(const __nv_bfloat16* w, int k) { return __bfloat162float(w[k]); }
+
+// ---------------------------------------------------------------------------
+// Features of every element: normalised modes, log10 E target, HG alpha, and
+// the positivity flag.  One thread per element (dimension-wise transforms in
+// registers; n <= 5).
+// ---------------------------------------------------------------------------
+struct FeatParams {
+  int64_t E;
+  double gamma;
+  float Vinv[MAXN * MAXN];
+  float alpha_min, alpha_max, hg_threshold, hg_parameter_s;
+};
+
+template <int D, int N, typename TS>
+__global__ void features_kernel(const FeatParams P, const TS* __restrict__ u,
+                                float* __restrict__ feat, float* __restrict__ target,
+                                float* __restrict__ alpha_hg, int32_t* __restrict__ pos_flag) {
+  constexpr int NV = D + 2, NN = Pow<N, D>::value;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.E) return;
+  float a[NN], b[NN];
+  bool positive = true;
+  for (int q = 0; q < NN; ++q) {
+    float uu[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) uu[v] = (float)state_value(u[((size_t)e * NN + q) * NV + v]);
+    a[q] = Euler<D, float>::density_pressure(uu, (float)P.gamma);
+    positive &= a[q] > 0.0f;
+  }
+  // multiply_scalar_dimensionwise!: x, then y, then z
+  float* in = a;
+  float* out = b;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const int S = d == 0 ? 1 : (d == 1 ? N : N * N);
+#pragma unroll
+    for (int q = 0; q < NN; ++q) {
+      const int i = (q / S) % N;
+      const int base = q - i * S;
+      float r = 0;
+#pragma unroll
+      for (int k = 0; k < N; ++k) r += P.Vinv[i * N + k] * in[base + k * S];
+      out[q] = r;
+    }
+    float* t = in;
+    in = out;
+    out = t;
+  }
+  float clip2 = 0, clip1 = 0, tot = 0;
+#pragma unroll
+  for (int q = 0; q < NN; ++q) {
+    int mx = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) mx = max(mx, (q / (d == 0 ? 1 : (d == 1 ? N : N * N))) % N);
+    const float m2 = in[q] * in[q];
+    if (mx <= N - 3) clip2 += m2;
+    if (mx <= N - 2) clip1 += m2;
+    tot += m2;
+  }
+  const float f1 = tot != 0.0f ? (tot - clip1) / tot : 0.0f;
+  const float f2 = clip1 != 0.0f ? (clip1 - clip2) / clip1 : 0.0f;
+  const float energy = fmaxf(f1, f2);
+  float al = 1.0f / (1.0f + expf(-P.hg_parameter_s / P.hg_threshold * (energy - P.hg_threshold)));
+  if (al < P.alpha_min) al = 0.0f;
+  if (al > 1.0f - P.alpha_min) al = 1.0f;
+  alpha_hg[e] = fminf(P.alpha_max, al);
+  const float inv = tot > 0.0f ? rsqrtf(tot) : 0.0f;
+#pragma unroll
+  for (int q = 0; q < NN; ++q) feat[(size_t)e * NN + q] = in[q] * inv;
+  if (target) target[e] = log10f(fmaxf(energy, 1e-12f));
+  pos_flag[e] = positive ? 0 : 2;
+}
+
+// ---------------------------------------------------------------------------
+// Inference: one thread per element; hidden layer 1 in shared memory, weights
+// read as warp-uniform (broadcast) loads.
+// ---------------------------------------------------------------------------
+template <int NM, int H, int BT>
+__global__ void __launch_bounds__(BT) mlp_infer_kernel(const __nv_bfloat16* __restrict__ w,
+                                                       const float* __restrict__ x, int64_t M,
+                                                       float* __restrict__ pred) {
+  __shared__ float s_h1[H * BT];
+  const MlpLayout L{NM, H};
+  const int tid = threadIdx.x;
+  const int64_t s = (int64_t)blockIdx.x * BT + tid;
+  const bool act = s < M;
+  float xv[NM];
+#pragma unroll
+  for (int k = 0; k < NM; ++k) xv[k] = act ? x[s * NM + k] : 0.0f;
+  for (int i = 0; i < H; ++i) {
+    float z = wld(w, L.b1() + i);
+#pragma unroll
+    for (int k = 0; k < NM; ++k) z = fmaf(wld(w, L.w1() + i * NM + k), xv[k], z);
+    s_h1[i * BT + tid] = fmaxf(z, 0.0f);
+  }
+  float out = wld(w, L.b3());
+  for (int i = 0; i < H; ++i) {
+    float z = wld(w, L.b2() + i);
+    for (int j = 0; j < H; ++j) z = fmaf(wld(w, L.w2() + i * H + j), s_h1[j * BT + tid], z);
+    out = fmaf(wld(w, L.w3() + i), fmaxf(z, 0.0f), out);
+  }
+  if (act) pred[s] = out;
+}
+
+// Predicted log10 E -> blending factor, with the HG fallback near the switch
+// and for non-positive rho*p; writes alpha_raw (R) for the stage kernels.
+template <typename R>
+__global__ void learned_alpha_kernel(const float* __restrict__ pred, const float* __restrict__ hg,
+                                     int32_t* __restrict__ flag, int64_t E, float log10_thr,
+                                     float band, float thr, float s_par, float alpha_min,
+                                     float alpha_max, R* __restrict__ alpha_raw,
+                                     unsigned long long* __restrict__ stats) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  int f = flag[e];
+  const float p = pred[e];
+  if (f == 0 && !(fabsf(p - log10_thr) >= band)) f = 1;  // also catches NaN
+  // logistic of the HG indicator (fallback) or of the predicted one, then the
+  // clipping of indicators_2d.jl:92-100 with the context's constants
+  float a = f != 0 ? hg[e] : 1.0f / (1.0f + expf(-s_par / thr * (exp10f(p) - thr)));
+  if (a < alpha_min) a = 0.0f;
+  if (a > 1.0f - alpha_min) a = 1.0f;
+  a = fminf(alpha_max, a);
+  flag[e] = f;
+  alpha_raw[e] = (R)a;
+  if (f == 1) atomicAdd(&stats[1], 1ull);
+  if (f == 2) atomicAdd(&stats[2], 1ull);
+  if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&stats[0], (unsigned long long)E);
+}
+
+// ---------------------------------------------------------------------------
+// Training: fused forward + backward over a tile of TS samples (one thread
+// per sample), weight gradients as tile-level contractions, accumulated into
+// the global gradient with atomics.  Loss: mean squared error.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t hash32(uint64_t x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ull;
+  x ^= x >> 33;
+  return (uint32_t)x;
+}
+
+template <int NM, int H, int TS>
+__global__ void __launch_bounds__(TS) mlp_train_kernel(const __nv_bfloat16* __restrict__ w,
+                                                       const float* __restrict__ X,
+                                                       const float* __restrict__ Y, int64_t M,
+                                                       const int64_t* __restrict__ idx_explicit,
+                                                       uint64_t seed, int batch, int holdout,
+                                                       float* __restrict__ grad,
+                                                       float* __restrict__ loss) {
+  extern __shared__ float sm[];
+  float* sX = sm;             // [NM][TS]
+  float* sH1 = sX + NM * TS;  // [H][TS]: h1, later dz1
+  float* sH2 = sH1 + H * TS;  // [H][TS]: h2, later dz2
+  float* sD = sH2 + H * TS;   // [TS]: dout
+  const MlpLayout L{NM, H};
+  const int tid = threadIdx.x;
+  const int k0 = blockIdx.x * TS + tid;
+  const bool act = k0 < batch;
+  int64_t s = 0;
+  if (act) {
+    if (idx_explicit) {
+      s = idx_explicit[k0];
+    } else {
+      // sample with replacement among the training rows (every holdout-th row is held out)
+      s = (int64_t)(hash32(seed * 0x9e3779b97f4a7c15ull + (uint64_t)k0) % (uint32_t)M);
+      if (holdout > 1 && s % holdout == 0) s = (s + 1) % M;
+    }
+  }
+  for (int k = 0; k < NM; ++k) sX[k * TS + tid] = act ? X[s * NM + k] : 0.0f;
+  for (int i = 0; i < H; ++i) {
+    float z = wld(w, L.b1() + i);
+    for (int k = 0; k < NM; ++k) z = fmaf(wld(w, L.w1() + i * NM + k), sX[k * TS + tid], z);
+    sH1[i * TS + tid] = fmaxf(z, 0.0f);
+  }
+  float out = wld(w, L.b3());
+  for (int i = 0; i < H; ++i) {
+    float z = wld(w, L.b2() + i);
+    for (int j = 0; j < H; ++j) z = fmaf(wld(w, L.w2() + i * H + j), sH1[j * TS + tid], z);
+    const float h = fmaxf(z, 0.0f);
+    sH2[i * TS + tid] = h;
+    out = fmaf(wld(w, L.w3() + i), h, out);
+  }
+  const float r = act ? out - Y[s] : 0.0f;
+  if (act) atomicAdd(&loss[0], r * r);
+  sD[tid] = act ? 2.0f * r / (float)batch : 0.0f;
+  __syncthreads();
+  // output layer gradients
+  for (int i = tid; i < H; i += TS) {
+    float g = 0;
+    for (int t = 0; t < TS; ++t) g = fmaf(sD[t], sH2[i * TS + t], g);
+    atomicAdd(&grad[L.w3() + i], g);
+  }
+  if (tid == 0) {
+    float g = 0;
+    for (int t = 0; t < TS; ++t) g += sD[t];
+    atomicAdd(&grad[L.b3()], g);
+  }
+  __syncthreads();
+  // dz2 = dout * w3 * [h2 > 0]   (in place of h2)
+  for (int i = 0; i < H; ++i) {
+    const float h = sH2[i * TS + tid];
+    sH2[i * TS + tid] = h > 0.0f ? sD[tid] * wld(w, L.w3() + i) : 0.0f;
+  }
+  __syncthreads();
+  // dW2[i][j] = sum_t dz2[i][t] h1[j][t], db2[i] = sum_t dz2[i][t]
+  for (int i = tid; i < H; i += TS) {
+    float gb = 0;
+    for (int t = 0; t < TS; ++t) gb += sH2[i * TS + t];
+    atomicAdd(&grad[L.b2() + i], gb);
+    for (int j = 0; j < H; ++j) {
+      float g = 0;
+      for (int t = 0; t < TS; ++t) g = fmaf(sH2[i * TS + t], sH1[j * TS + t], g);
+      atomicAdd(&grad[L.w2() + i * H + j], g);
+    }
+  }
+  __syncthreads();
+  // dh1[j] = sum_i dz2[i] W2[i][j]; dz1 = dh1 [h1 > 0]  (own sample, in place of h1)
+  {
+    float dh[H];
+    for (int j = 0; j < H; ++j) dh[j] = 0.0f;
+    for (int i = 0; i < H; ++i) {
+      const float dz = sH2[i * TS + tid];
+      if (dz != 0.0f)
+        for (int j = 0; j < H; ++j) dh[j] = fmaf(dz, wld(w, L.w2() + i * H + j), dh[j]);
+    }
+    __syncthreads();
+    for (int j = 0; j < H; ++j) sH1[j * TS + tid] = sH1[j * TS + tid] > 0.0f ? dh[j] : 0.0f;
+  }
+  __syncthreads();
+  // dW1[i][k] = sum_t dz1[i][t] x[k][t], db1[i] = sum_t dz1[i][t]
+  for (int i = tid; i < H; i += TS) {
+    float gb = 0;
+    for (int t = 0; t < TS; ++t) gb += sH1[i * TS + t];
+    atomicAdd(&grad[L.b1() + i], gb);
+    for (int k = 0; k < NM; ++k) {
+      float g = 0;
+      for (int t = 0; t < TS; ++t) g = fmaf(sH1[i * TS + t], sX[k * TS + t], g);
+      atomicAdd(&grad[L.w1() + i * NM + k], g);
+    }
+  }
+  if (tid == 0 && blockIdx.x == 0) atomicAdd(&loss[1], (float)batch);
+}
+
+__global__ void adam_kernel(float* __restrict__ w, __nv_bfloat16* __restrict__ wb,
+                            float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                            int64_t n, float lr, float b1, float b2, float eps, float c1, float c2) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const float gk = g[k];
+  const float mk = b1 * m[k] + (1.0f - b1) * gk;
+  const float vk = b2 * v[k] + (1.0f - b2) * gk * gk;
+  m[k] = mk;
+  v[k] = vk;
+  const float wk = w[k] - lr * (mk / c1) / (sqrtf(vk / c2) + eps);
+  w[k] = wk;
+  wb[k] = __float2bfloat16(wk);
+  g[k] = 0.0f;
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ w, __nv_bfloat16* __restrict__ wb,
+                               int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) wb[k] = __float2bfloat16(w[k]);
+}
+
+}  // namespace tg
+
+using namespace tg;
+
+static int mfail(tg_mlp* m, int code, const char* msg) {
+  if (m) m->err = msg;
+  set_thread_error(msg);
+  return code;
+}
+
+#define MCUDA(m, call)                                                        \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) return mfail((m), TG_ERR_CUDA, cudaGetErrorString(e_)); \
+  } while (0)
+
+static int launch_features(tg_mlp* m, tg_ctx* c, float* feat, float* target, float* alpha_hg,
+                           int32_t* flag, cudaStream_t* s_out, int64_t* E_out) {
+  const void* state;
+  int ff, D, N;
+  int64_t E;
+  double gamma;
+  const double* vinv;
+  void* stream;
+  int rc = ctx_state_view(c, &state, &ff, &D, &N, &E, &gamma, &vinv, &stream);
+  if (rc) return rc;
+  if (D != m->D || N != m->N) return mfail(m, TG_ERR_INVALID_ARGUMENT, "network/context shape mismatch");
+  FeatParams P{};
+  P.E = E;
+  P.gamma = gamma;
+  for (int k = 0; k < N * N; ++k) P.Vinv[k] = (float)vinv[k];
+  // HG constants of this polydeg (indicators.jl:128-131)
+  P.hg_threshold = (float)(0.5 * std::pow(10.0, -1.8 * std::pow((double)N, 0.25)));
+  P.hg_parameter_s = (float)std::log((1 - 0.0001) / 0.0001);
+  P.alpha_min = 0.0f;
+  P.alpha_max = 1.0f;
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned nb = (unsigned)((E + 127) / 128);
+#define FEAT(DD, NN)                                                                           \
+  if (D == DD && N == NN) {                                                                    \
+    if (ff)                                                                                    \
+      features_kernel<DD, NN, float2><<<nb, 128, 0, s>>>(P, (const float2*)state, feat, target, \
+                                                         alpha_hg, flag);                      \
+    else                                                                                       \
+      features_kernel<DD, NN, double><<<nb, 128, 0, s>>>(P, (const double*)state, feat, target, \
+                                                         alpha_hg, flag);                      \
+  } else
+  FEAT(2, 3) FEAT(2, 4) FEAT(2, 5) FEAT(3, 3) FEAT(3, 4) {
+    return mfail(m, TG_ERR_UNSUPPORTED, "learned indicator: polydeg 2..4 only");
+  }
+#undef FEAT
+  MCUDA(m, cudaGetLastError());
+  *s_out = s;
+  *E_out = E;
+  return TG_OK;
+}
+
+static int launch_infer(tg_mlp* m, const float* x, int64_t M, float* pred, cudaStream_t s) {
+  const unsigned nb = (unsigned)((M + 127) / 128);
+  if (m->NM == 16 && m->H == 64)
+    mlp_infer_kernel<16, 64, 128><<<nb, 128, 0, s>>>(m->d_wb, x, M, pred);
+  else if (m->NM == 9 && m->H == 64)
+    mlp_infer_kernel<9, 64, 128><<<nb, 128, 0, s>>>(m->d_wb, x, M, pred);
+  else if (m->NM == 25 && m->H == 64)
+    mlp_infer_kernel<25, 64, 128><<<nb, 128, 0, s>>>(m->d_wb, x, M, pred);
+  else if (m->NM == 27 && m->H == 128)
+    mlp_infer_kernel<27, 128, 64><<<nb * 2, 64, 0, s>>>(m->d_wb, x, M, pred);
+  else if (m->NM == 64 && m->H == 128)
+    mlp_infer_kernel<64, 128, 64><<<nb * 2, 64, 0, s>>>(m->d_wb, x, M, pred);
+  else
+    return mfail(m, TG_ERR_UNSUPPORTED, "network shape not compiled");
+  MCUDA(m, cudaGetLastError());
+  return TG_OK;
+}
+
+namespace tg {
+// Called by the context before every stage when the learned indicator is on:
+// writes the blending factors (unsmoothed) into alpha_raw (R = float or double).
+int mlp_alpha(tg_mlp* m, tg_ctx* c, void* alpha_raw, bool fp64, float alpha_min,
+              float alpha_max) {
+  cudaStream_t s;
+  int64_t E;
+  if (m->ecap == 0) return mfail(m, TG_ERR_STATE, "learned indicator not prepared for this context");
+  int rc = launch_features(m, c, m->d_feat, nullptr, m->d_hg, m->d_flag, &s, &E);
+  if (rc) return rc;
+  if (E > m->ecap) return mfail(m, TG_ERR_STATE, "context larger than prepared");
+  rc = launch_infer(m, m->d_feat, E, m->d_pred, s);
+  if (rc) return rc;
+  const float thr = (float)(0.5 * std::pow(10.0, -1.8 * std::pow((double)m->N, 0.25)));
+  const float spar = (float)std::log((1 - 0.0001) / 0.0001);
+  const unsigned nb = (unsigned)((E + 255) / 256);
+  // d_hg holds the unclipped HG logistic; the alpha kernel clips both paths
+  if (fp64)
+    learned_alpha_kernel<double><<<nb, 256, 0, s>>>(m->d_pred, m->d_hg, m->d_flag, E,
+                                                    (float)m->log10_threshold, m->band, thr, spar,
+                                                    alpha_min, alpha_max, (double*)alpha_raw,
+                                                    m->d_stats);
+  else
+    learned_alpha_kernel<float><<<nb, 256, 0, s>>>(m->d_pred, m->d_hg, m->d_flag, E,
+                                                   (float)m->log10_threshold, m->band, thr, spar,
+                                                   alpha_min, alpha_max, (float*)alpha_raw,
+                                                   m->d_stats);
+  MCUDA(m, cudaGetLastError());
+  return TG_OK;
+}
+}  // namespace tg
+
+extern "C" {
+
+int tg_mlp_create(int32_t ndims, int32_t polydeg, int32_t hidden, uint64_t seed, tg_mlp** out) {
+  if (!out) return mfail(nullptr, TG_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  const int N = polydeg + 1;
+  if ((ndims != 2 && ndims != 3) || N < 3 || N > 5)
+    return mfail(nullptr, TG_ERR_UNSUPPORTED, "learned indicator: 2D/3D, polydeg 2..4");
+  const int NM = ndims == 2 ? N * N : N * N * N;
+  const int H = hidden > 0 ? hidden : (ndims == 2 ? 64 : 128);
+  const bool ok = (NM == 16 && H == 64) || (NM == 9 && H == 64) || (NM == 25 && H == 64) ||
+                  (NM == 27 && H == 128) || (NM == 64 && H == 128);
+  if (!ok) return mfail(nullptr, TG_ERR_UNSUPPORTED, "network shape not compiled");
+  tg_mlp* m = new tg_mlp();
+  m->D = ndims;
+  m->N = N;
+  m->NM = NM;
+  m->H = H;
+  const MlpLayout L{NM, H};
+  m->nparams = L.count();
+  m->log10_threshold = std::log10(0.5 * std::pow(10.0, -1.8 * std::pow((double)N, 0.25)));
+  // He-uniform initialisation from a fixed-seed LCG
+  std::vector<float> w(m->nparams, 0.0f);
+  uint64_t st = seed * 6364136223846793005ull + 1442695040888963407ull;
+  auto uni = [&]() {
+    st = st * 6364136223846793005ull + 1442695040888963407ull;
+    return ((st >> 40) & 0xffffff) / 16777216.0f * 2.0f - 1.0f;
+  };
+  for (int i = 0; i < H * NM; ++i) w[L.w1() + i] = uni() * std::sqrt(6.0f / NM);
+  for (int i = 0; i < H * H; ++i) w[L.w2() + i] = uni() * std::sqrt(6.0f / H);
+  for (int i = 0; i < H; ++i) w[L.w3() + i] = uni() * std::sqrt(3.0f / H);
+  w[L.b3()] = -4.0f;  // a typical smooth-flow log10 E
+  const size_t pb = sizeof(float) * m->nparams;
+  cudaError_t e = cudaSuccess;
+  e = e ? e : cudaMalloc(&m->d_w, pb);
+  e = e ? e : cudaMalloc(&m->d_wb, sizeof(__nv_bfloat16) * m->nparams);
+  e = e ? e : cudaMalloc(&m->d_g, pb);
+  e = e ? e : cudaMalloc(&m->d_m, pb);
+  e = e ? e : cudaMalloc(&m->d_v, pb);
+  e = e ? e : cudaMalloc(&m->d_loss, 2 * sizeof(float));
+  e = e ? e : cudaMalloc(&m->d_stats, 3 * sizeof(unsigned long long));
+  if (e != cudaSuccess) {
+    delete m;
+    return mfail(nullptr, TG_ERR_CUDA, cudaGetErrorString(e));
+  }
+  cudaMemcpy(m->d_w, w.data(), pb, cudaMemcpyHostToDevice);
+  cudaMemset(m->d_g, 0, pb);
+  cudaMemset(m->d_m, 0, pb);
+  cudaMemset(m->d_v, 0, pb);
+  cudaMemset(m->d_stats, 0, 3 * sizeof(unsigned long long));
+  to_bf16_kernel<<<(unsigned)((m->nparams + 255) / 256), 256>>>(m->d_w, m->d_wb, m->nparams);
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return mfail(nullptr, TG_ERR_CUDA, cudaGetErrorString(e));
+  *out = m;
+  return TG_OK;
+}
+
+int tg_mlp_destroy(tg_mlp* m) {
+  if (!m) return TG_ERR_INVALID_ARGUMENT;
+  void* ptrs[] = {m->d_w, m->d_wb, m->d_g, m->d_m, m->d_v, m->d_x, m->d_y, m->d_loss,
+                  m->d_feat, m->d_pred, m->d_hg, m->d_flag, m->d_stats};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  delete m;
+  return TG_OK;
+}
+
+int tg_mlp_nparams(const tg_mlp* m, int64_t* n) {
+  if (!m || !n) return TG_ERR_INVALID_ARGUMENT;
+  *n = m->nparams;
+  return TG_OK;
+}
+
+int tg_mlp_get_params(tg_mlp* m, float* host) {
+  if (!m || !host) return TG_ERR_INVALID_ARGUMENT;
+  MCUDA(m, cudaMemcpy(host, m->d_w, sizeof(float) * m->nparams, cudaMemcpyDeviceToHost));
+  return TG_OK;
+}
+
+int tg_mlp_set_params(tg_mlp* m, const float* host) {
+  if (!m || !host) return TG_ERR_INVALID_ARGUMENT;
+  MCUDA(m, cudaMemcpy(m->d_w, host, sizeof(float) * m->nparams, cudaMemcpyHostToDevice));
+  to_bf16_kernel<<<(unsigned)((m->nparams + 255) / 256), 256>>>(m->d_w, m->d_wb, m->nparams);
+  MCUDA(m, cudaDeviceSynchronize());
+  return TG_OK;
+}
+
+// Appends the features/targets of every `stride`-th element of the context
+// state (offset `phase`) to the training set (grown on demand).
+int tg_mlp_harvest(tg_mlp* m, tg_ctx* c, int32_t stride, int32_t phase, int64_t* total) {
+  if (!m || !c || stride < 1) return TG_ERR_INVALID_ARGUMENT;
+  cudaStream_t s;
+  int64_t E;
+  // scratch for the full element set
+  {
+    const void* st;
+    int ff, D, N;
+    double g;
+    const double* vi;
+    void* strm;
+    int rc = ctx_state_view(c, &st, &ff, &D, &N, &E, &g, &vi, &strm);
+    if (rc) return rc;
+  }
+  float *feat = nullptr, *tgt = nullptr, *hg = nullptr;
+  int32_t* flag = nullptr;
+  MCUDA(m, cudaMalloc(&feat, sizeof(float) * E * m->NM));
+  MCUDA(m, cudaMalloc(&tgt, sizeof(float) * E));
+  MCUDA(m, cudaMalloc(&hg, sizeof(float) * E));
+  MCUDA(m, cudaMalloc(&flag, sizeof(int32_t) * E));
+  int rc = launch_features(m, c, feat, tgt, hg, flag, &s, &E);
+  if (rc == TG_OK) {
+    const int64_t take = (E - phase + stride - 1) / stride;
+    if (m->count + take > m->cap) {
+      const int64_t ncap = std::max<int64_t>(2 * m->cap, m->count + take);
+      float *nx = nullptr, *ny = nullptr;
+      cudaMalloc(&nx, sizeof(float) * ncap * m->NM);
+      cudaMalloc(&ny, sizeof(float) * ncap);
+      if (m->count) {
+        cudaMemcpyAsync(nx, m->d_x, sizeof(float) * m->count * m->NM, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(ny, m->d_y, sizeof(float) * m->count, cudaMemcpyDeviceToDevice, s);
+      }
+      cudaStreamSynchronize(s);
+      cudaFree(m->d_x);
+      cudaFree(m->d_y);
+      m->d_x = nx;
+      m->d_y = ny;
+      m->cap = ncap;
+    }
+    // strided gather of rows (pitched 2D copies)
+    cudaMemcpy2DAsync(m->d_x + m->count * m->NM, sizeof(float) * m->NM, feat + phase * m->NM,
+                      sizeof(float) * m->NM * stride, sizeof(float) * m->NM, take,
+                      cudaMemcpyDeviceToDevice, s);
+    cudaMemcpy2DAsync(m->d_y + m->count, sizeof(float), tgt + phase, sizeof(float) * stride,
+                      sizeof(float), take, cudaMemcpyDeviceToDevice, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = mfail(m, TG_ERR_CUDA, cudaGetErrorString(e));
+    else m->count += take;
+  }
+  cudaFree(feat);
+  cudaFree(tgt);
+  cudaFree(hg);
+  cudaFree(flag);
+  if (total) *total = m->count;
+  return rc;
+}
+
+// Adam training on the harvested set: `steps` minibatches of `batch` samples
+// drawn with replacement (rows i with i % holdout == 0 are held out when
+// holdout > 1).  *mean_loss receives the mean squared error over all steps.
+int tg_mlp_train(tg_mlp* m, int64_t steps, int32_t batch, float lr, int32_t holdout,
+                 uint64_t seed, float* mean_loss) {
+  if (!m || steps < 0 || batch < 1) return TG_ERR_INVALID_ARGUMENT;
+  if (m->count < 2) return mfail(m, TG_ERR_STATE, "no training data harvested");
+  constexpr int TS = 64;
+  const int nb = (batch + TS - 1) / TS;
+  MCUDA(m, cudaMemset(m->d_loss, 0, 2 * sizeof(float)));
+  const size_t smem = sizeof(float) * (m->NM * TS + 2 * m->H * TS + TS);
+  for (int64_t it = 0; it < steps; ++it) {
+    const uint64_t sd = seed * 1000003ull + (uint64_t)(m->adam_t + 1);
+    if (m->NM == 16 && m->H == 64) {
+      cudaFuncSetAttribute(mlp_train_kernel<16, 64, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      mlp_train_kernel<16, 64, TS><<<nb, TS, smem>>>(m->d_wb, m->d_x, m->d_y, m->count, nullptr, sd,
+                                                     batch, holdout, m->d_g, m->d_loss);
+    } else if (m->NM == 9 && m->H == 64) {
+      mlp_train_kernel<9, 64, TS><<<nb, TS, smem>>>(m->d_wb, m->d_x, m->d_y, m->count, nullptr, sd,
+                                                    batch, holdout, m->d_g, m->d_loss);
+    } else if (m->NM == 25 && m->H == 64) {
+      cudaFuncSetAttribute(mlp_train_kernel<25, 64, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      mlp_train_kernel<25, 64, TS><<<nb, TS, smem>>>(m->d_wb, m->d_x, m->d_y, m->count, nullptr, sd,
+                                                     batch, holdout, m->d_g, m->d_loss);
+    } else if (m->NM == 27 && m->H == 128) {
+      cudaFuncSetAttribute(mlp_train_kernel<27, 128, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      mlp_train_kernel<27, 128, TS><<<nb, TS, smem>>>(m->d_wb, m->d_x, m->d_y, m->count, nullptr, sd,
+                                                      batch, holdout, m->d_g, m->d_loss);
+    } else {
+      cudaFuncSetAttribute(mlp_train_kernel<64, 128, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      mlp_train_kernel<64, 128, TS><<<nb, TS, smem>>>(m->d_wb, m->d_x, m->d_y, m->count, nullptr, sd,
+                                                      batch, holdout, m->d_g, m->d_loss);
+    }
+    m->adam_t += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.0f - std::pow(b1, (float)m->adam_t), c2 = 1.0f - std::pow(b2, (float)m->adam_t);
+    adam_kernel<<<(unsigned)((m->nparams + 255) / 256), 256>>>(m->d_w, m->d_wb, m->d_g, m->d_m,
+                                                              m->d_v, m->nparams, lr, b1, b2, 1e-8f,
+                                                              c1, c2);
+  }
+  float l[2] = {0, 0};
+  MCUDA(m, cudaMemcpy(l, m->d_loss, sizeof(l), cudaMemcpyDeviceToHost));
+  if (mean_loss) *mean_loss = l[1] > 0 ? l[0] / l[1] : 0.0f;
+  return TG_OK;
+}
+
+// Gradient of the mean squared error over explicit rows (x_host [n][NM],
+// y_host [n]) at the current weights, written to grad_host [nparams] (FP32),
+// without changing the weights: the check against the CPU oracle.
+int tg_mlp_gradient(tg_mlp* m, const float* x_host, const float* y_host, int32_t n,
+                    float* grad_host, float* loss_host) {
+  if (!m || !x_host || !y_host || !grad_host || n < 1) return TG_ERR_INVALID_ARGUMENT;
+  float *x = nullptr, *y = nullptr;
+  int64_t* idx = nullptr;
+  MCUDA(m, cudaMalloc(&x, sizeof(float) * n * m->NM));
+  MCUDA(m, cudaMalloc(&y, sizeof(float) * n));
+  MCUDA(m, cudaMalloc(&idx, sizeof(int64_t) * n));
+  std::vector<int64_t> id(n);
+  for (int i = 0; i < n; ++i) id[i] = i;
+  cudaMemcpy(x, x_host, sizeof(float) * n * m->NM, cudaMemcpyHostToDevice);
+  cudaMemcpy(y, y_host, sizeof(float) * n, cudaMemcpyHostToDevice);
+  cudaMemcpy(idx, id.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice);
+  cudaMemset(m->d_g, 0, sizeof(float) * m->nparams);
+  cudaMemset(m->d_loss, 0, 2 * sizeof(float));
+  constexpr int TS = 64;
+  const int nb = (n + TS - 1) / TS;
+  const size_t smem = sizeof(float) * (m->NM * TS + 2 * m->H * TS + TS);
+#define TRAIN(NMv, Hv)                                                                          \
+  if (m->NM == NMv && m->H == Hv) {                                                             \
+    cudaFuncSetAttribute(mlp_train_kernel<NMv, Hv, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                         (int)smem);                                                            \
+    mlp_train_kernel<NMv, Hv, TS><<<nb, TS, smem>>>(m->d_wb, x, y, n, idx, 0, n, 0, m->d_g,     \
+                                                    m->d_loss);                                  \
+  } else
+  TRAIN(16, 64) TRAIN(9, 64) TRAIN(25, 64) TRAIN(27, 128) TRAIN(64, 128) {}
+#undef TRAIN
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(grad_host, m->d_g, sizeof(float) * m->nparams, cudaMemcpyDeviceToHost);
+  float l[2];
+  if (e == cudaSuccess) e = cudaMemcpy(l, m->d_loss, sizeof(l), cudaMemcpyDeviceToHost);
+  if (loss_host && e == cudaSuccess) *loss_host = l[0] / n;
+  cudaMemset(m->d_g, 0, sizeof(float) * m->nparams);
+  cudaFree(x);
+  cudaFree(y);
+  cudaFree(idx);
+  if (e != cudaSuccess) return mfail(m, TG_ERR_CUDA, cudaGetErrorString(e));
+  return TG_OK;
+}
+
+// Network predictions (log10 E) for explicit rows x_host [n][NM].
+int tg_mlp_predict(tg_mlp* m, const float* x_host, int64_t n, float* pred_host) {
+  if (!m || !x_host || !pred_host || n < 1) return TG_ERR_INVALID_ARGUMENT;
+  float *x = nullptr, *p = nullptr;
+  MCUDA(m, cudaMalloc(&x, sizeof(float) * n * m->NM));
+  MCUDA(m, cudaMalloc(&p, sizeof(float) * n));
+  cudaMemcpy(x, x_host, sizeof(float) * n * m->NM, cudaMemcpyHostToDevice);
+  int rc = launch_infer(m, x, n, p, 0);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (rc == TG_OK && e == cudaSuccess) e = cudaMemcpy(pred_host, p, sizeof(float) * n, cudaMemcpyDeviceToHost);
+  cudaFree(x);
+  cudaFree(p);
+  if (rc) return rc;
+  if (e != cudaSuccess) return mfail(m, TG_ERR_CUDA, cudaGetErrorString(e));
+  return TG_OK;
+}
+
+// Harvested rows (features, targets) copied to the host (count from tg_mlp_harvest).
+int tg_mlp_dataset(tg_mlp* m, float* x_host, float* y_host) {
+  if (!m || !x_host || !y_host) return TG_ERR_INVALID_ARGUMENT;
+  MCUDA(m, cudaMemcpy(x_host, m->d_x, sizeof(float) * m->count * m->NM, cudaMemcpyDeviceToHost));
+  MCUDA(m, cudaMemcpy(y_host, m->d_y, sizeof(float) * m->count, cudaMemcpyDeviceToHost));
+  return TG_OK;
+}
+
+// Use the network as the context's shock indicator (band: half-width of the
+// fallback zone in decades of E around the HG threshold).  m == NULL restores
+// the Hennemann-Gassner indicator.
+int tg_ctx_set_learned_indicator(tg_ctx* c, tg_mlp* m, float band) {
+  if (!c) return TG_ERR_INVALID_ARGUMENT;
+  if (m) {
+    const void* st;
+    int ff, D, N;
+    int64_t E;
+    double g;
+    const double* vi;
+    void* strm;
+    int rc = ctx_state_view(c, &st, &ff, &D, &N, &E, &g, &vi, &strm);
+    if (rc) return rc;
+    if (D != m->D || N != m->N) return mfail(m, TG_ERR_INVALID_ARGUMENT, "network/context shape mismatch");
+    if (E > m->ecap) {
+      cudaFree(m->d_feat);
+      cudaFree(m->d_pred);
+      cudaFree(m->d_hg);
+      cudaFree(m->d_flag);
+      MCUDA(m, cudaMalloc(&m->d_feat, sizeof(float) * E * m->NM));
+      MCUDA(m, cudaMalloc(&m->d_pred, sizeof(float) * E));
+      MCUDA(m, cudaMalloc(&m->d_hg, sizeof(float) * E));
+      MCUDA(m, cudaMalloc(&m->d_flag, sizeof(int32_t) * E));
+      m->ecap = E;
+    }
+    m->band = band;
+  }
+  return ctx_set_alpha_source(c, m);
+}
+
+// Learned-indicator diagnostics of the last stage: per element the network's
+// blending factor inputs (pred: predicted log10 E), the HG factor (hg, with
+// alpha_min = 0 and alpha_max = 1) and the fallback flag, plus the running
+// counts {elements evaluated, band fallbacks, positivity fallbacks}.
+int tg_mlp_last(tg_mlp* m, float* pred, float* hg, int32_t* flag, uint64_t* counts) {
+  if (!m) return TG_ERR_INVALID_ARGUMENT;
+  cudaDeviceSynchronize();
+  if (pred) MCUDA(m, cudaMemcpy(pred, m->d_pred, sizeof(float) * m->ecap, cudaMemcpyDeviceToHost));
+  if (hg) MCUDA(m, cudaMemcpy(hg, m->d_hg, sizeof(float) * m->ecap, cudaMemcpyDeviceToHost));
+  if (flag) MCUDA(m, cudaMemcpy(flag, m->d_flag, sizeof(int32_t) * m->ecap, cudaMemcpyDeviceToHost));
+  if (counts) MCUDA(m, cudaMemcpy(counts, m->d_stats, 3 * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+  return TG_OK;
+}
+
+}  // extern "C"

@@ -28,7 +28,10 @@ EXPORTS = ("tg_api_version", "tg_ctx_create", "tg_ctx_destroy", "tg_last_error",
            "tg_upload_state", "tg_download_state", "tg_state_device_ptr", "tg_rhs",
            "tg_rhs_host", "tg_max_dt", "tg_rk_stage", "tg_step", "tg_set_time",
            "tg_integrals", "tg_alpha", "tg_status", "tg_synchronize",
-           "tg_elements_per_block", "tg_stream", "tg_integrals_noalloc")
+           "tg_elements_per_block", "tg_stream", "tg_integrals_noalloc",
+           "tg_mlp_create", "tg_mlp_destroy", "tg_mlp_nparams", "tg_mlp_get_params",
+           "tg_mlp_set_params", "tg_mlp_harvest", "tg_mlp_dataset", "tg_mlp_train",
+           "tg_mlp_gradient", "tg_mlp_predict", "tg_ctx_set_learned_indicator", "tg_mlp_last")
 
 
 class TrixiGB300Error(RuntimeError):
@@ -106,6 +109,19 @@ def load(path: str | None = None):
         "tg_elements_per_block": ([vp, P(i32)], ctypes.c_int),
         "tg_stream": ([vp, P(vp)], ctypes.c_int),
         "tg_integrals_noalloc": ([i32, i32, i64, d, pd, vp, vp, vp, vp], ctypes.c_int),
+        "tg_mlp_create": ([i32, i32, i32, ctypes.c_uint64, P(vp)], ctypes.c_int),
+        "tg_mlp_destroy": ([vp], ctypes.c_int),
+        "tg_mlp_nparams": ([vp, P(i64)], ctypes.c_int),
+        "tg_mlp_get_params": ([vp, vp], ctypes.c_int),
+        "tg_mlp_set_params": ([vp, vp], ctypes.c_int),
+        "tg_mlp_harvest": ([vp, vp, i32, i32, P(i64)], ctypes.c_int),
+        "tg_mlp_dataset": ([vp, vp, vp], ctypes.c_int),
+        "tg_mlp_train": ([vp, i64, i32, ctypes.c_float, i32, ctypes.c_uint64,
+                          P(ctypes.c_float)], ctypes.c_int),
+        "tg_mlp_gradient": ([vp, vp, vp, i32, vp, P(ctypes.c_float)], ctypes.c_int),
+        "tg_mlp_predict": ([vp, vp, i64, vp], ctypes.c_int),
+        "tg_ctx_set_learned_indicator": ([vp, vp, ctypes.c_float], ctypes.c_int),
+        "tg_mlp_last": ([vp, vp, vp, vp, vp], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)
