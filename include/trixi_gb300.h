@@ -223,14 +223,15 @@ int tg_integrals_noalloc(int32_t ndims, int32_t polydeg, int64_t nelements, doub
 
 /* ---- Learned shock indicator ----------------------------------------------
  * A small MLP (2D polydeg 3: 16 -> 64 -> 64 -> 1; 3D: 64 -> 128 -> 128 -> 1,
- * ReLU, BF16 weights, FP32 accumulation) predicting log10 of the
- * Hennemann-Gassner smoothness indicator E of an element from its normalised
- * modal coefficients of density*pressure (indicators_2d.jl:30-101).  Deployed
- * in place of IndicatorHennemannGassner for TG_VOLUME_SHOCK_CAPTURING_HG
- * contexts; the HG indicator stays as fallback (elements whose prediction is
- * within `band` decades of the switching threshold, or whose nodal
- * density*pressure is not positive) and as the judge of its error.  No
- * counterpart in the reference, which has no learned indicator. */
+ * ReLU, BF16 weights, FP32 accumulation) predicting sqrt of the
+ * Hennemann-Gassner smoothness indicator E of an element from its modal
+ * coefficients of density*pressure normalised to unit energy
+ * (indicators_2d.jl:30-101).  Deployed in place of IndicatorHennemannGassner
+ * for TG_VOLUME_SHOCK_CAPTURING_HG contexts; the HG indicator stays as
+ * fallback (elements whose prediction is within `band` of sqrt of the
+ * switching threshold, or whose nodal density*pressure is not positive) and
+ * as the judge of its error.  No counterpart in the reference, which has no
+ * learned indicator. */
 typedef struct tg_mlp tg_mlp;
 int tg_mlp_create(int32_t ndims, int32_t polydeg, int32_t hidden, uint64_t seed, tg_mlp** out);
 int tg_mlp_destroy(tg_mlp* m);
@@ -238,11 +239,11 @@ int tg_mlp_nparams(const tg_mlp* m, int64_t* n);
 /* FP32 master parameters, layout W1[H][NM], b1[H], W2[H][H], b2[H], w3[H], b3. */
 int tg_mlp_get_params(tg_mlp* m, float* host);
 int tg_mlp_set_params(tg_mlp* m, const float* host);
-/* Appends the (features, log10 E) pairs of every stride-th element of the
+/* Appends the (features, sqrt E) pairs of every stride-th element of the
  * context's current state to the network's training set. */
 int tg_mlp_harvest(tg_mlp* m, tg_ctx* c, int32_t stride, int32_t phase, int64_t* total);
 int tg_mlp_dataset(tg_mlp* m, float* x_host, float* y_host);
-/* Adam on the mean squared error of log10 E, minibatches drawn with
+/* Adam on the mean squared error of sqrt E, minibatches drawn with
  * replacement; rows i with i % holdout == 0 are held out (holdout > 1). */
 int tg_mlp_train(tg_mlp* m, int64_t steps, int32_t batch, float lr, int32_t holdout,
                  uint64_t seed, float* mean_loss);

@@ -5,20 +5,22 @@
 // dimension-wise inverse-Vandermonde transform as the HG indicator,
 // indicators_2d.jl:50-56 / indicators_3d.jl:54-60), normalised to unit
 // energy, m / |m|.
-// Target.   log10 of the HG energy indicator E = max(energy fractions of the
-// highest and second-highest modes) (indicators_2d.jl:58-90); the HG logistic
-// map alpha = 1 / (1 + exp(-s/T (E - T))), the clipping at alpha_min and the
-// cap alpha_max (indicators_2d.jl:92-100) are then applied to the prediction
-// exactly as to E itself.
-// Fallback/judge.  Elements whose predicted log10 E lies within `band`
-// decades of log10 T (where alpha switches on) or whose nodal rho*p is not
-// positive take the HG alpha, which is computed from the same modes.
+// Target.   sqrt(E) of the HG energy indicator E = max(energy fractions of the
+// highest and second-highest modes) (indicators_2d.jl:58-90): the relative
+// norm of the high modes, homogeneous of degree one in the normalised
+// features and so well suited to a ReLU network.  The HG logistic map
+// alpha = 1 / (1 + exp(-s/T (E - T))), the clipping at alpha_min and the cap
+// alpha_max (indicators_2d.jl:92-100) are applied to E = prediction^2 exactly
+// as to E itself.
+// Fallback/judge.  Elements whose predicted sqrt(E) lies within `band` of
+// sqrt(T) (where alpha switches on) or whose nodal rho*p is not positive
+// take the HG alpha, which is computed from the same modes.
 //
 // Network: NM -> H -> H -> 1 with ReLU (2D polydeg 3: 16 -> 64 -> 64 -> 1,
 // 3D: 64 -> 128 -> 128 -> 1), weights stored in BF16 for the forward pass
 // with FP32 master copies, FP32 accumulation, trained with Adam on the MSE of
-// log10 E by the fused forward+backward kernel below.  Layers this small
-// (K = 16..128) run on the CUDA cores.
+// sqrt E by the fused forward+backward kernel below.  Layers this small
+// (K = 16..128) run on the CUDA cores.  Loss: mean squared error of sqrt(E).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -52,11 +54,11 @@ struct tg_mlp {
   int64_t cap = 0, count = 0;
   float* d_loss = nullptr;           // [2]: loss sum, sample count
   int64_t adam_t = 0;
-  float band = 0.5f;                 // confidence band in decades of E
-  double log10_threshold = 0.0;      // log10 T of the HG indicator
+  float band = 0.01f;                // half-width of the fallback zone around sqrt(T)
+  double sqrt_threshold = 0.0;       // sqrt(T) of the HG indicator
   // deployment scratch
   float* d_feat = nullptr;           // [E][NM] features of the current state
-  float* d_pred = nullptr;           // [E] predicted log10 E
+  float* d_pred = nullptr;           // [E] predicted sqrt(E)
   float* d_hg = nullptr;             // [E] HG alpha (unsmoothed)
   int32_t* d_flag = nullptr;         // [E] fallback reason (0 none, 1 band, 2 positivity)
   int64_t ecap = 0;
@@ -81,7 +83,7 @@ struct MlpLayout {
 __device__ __forceinline__ float wld(const __nv_bfloat16* w, int k) { return __bfloat162float(w[k]); }
 
 // ---------------------------------------------------------------------------
-// Features of every element: normalised modes, log10 E target, HG alpha, and
+// Features of every element: normalised modes, sqrt E target, HG alpha, and
 // the positivity flag.  One thread per element (dimension-wise transforms in
 // registers; n <= 5).
 // ---------------------------------------------------------------------------
@@ -148,7 +150,7 @@ __global__ void features_kernel(const FeatParams P, const TS* __restrict__ u,
   const float inv = tot > 0.0f ? rsqrtf(tot) : 0.0f;
 #pragma unroll
   for (int q = 0; q < NN; ++q) feat[(size_t)e * NN + q] = in[q] * inv;
-  if (target) target[e] = log10f(fmaxf(energy, 1e-12f));
+  if (target) target[e] = sqrtf(fmaxf(energy, 0.0f));
   pos_flag[e] = positive ? 0 : 2;
 }
 
@@ -183,11 +185,11 @@ __global__ void __launch_bounds__(BT) mlp_infer_kernel(const __nv_bfloat16* __re
   if (act) pred[s] = out;
 }
 
-// Predicted log10 E -> blending factor, with the HG fallback near the switch
+// Predicted sqrt(E) -> blending factor, with the HG fallback near the switch
 // and for non-positive rho*p; writes alpha_raw (R) for the stage kernels.
 template <typename R>
 __global__ void learned_alpha_kernel(const float* __restrict__ pred, const float* __restrict__ hg,
-                                     int32_t* __restrict__ flag, int64_t E, float log10_thr,
+                                     int32_t* __restrict__ flag, int64_t E, float sqrt_thr,
                                      float band, float thr, float s_par, float alpha_min,
                                      float alpha_max, R* __restrict__ alpha_raw,
                                      unsigned long long* __restrict__ stats) {
@@ -195,10 +197,11 @@ __global__ void learned_alpha_kernel(const float* __restrict__ pred, const float
   if (e >= E) return;
   int f = flag[e];
   const float p = pred[e];
-  if (f == 0 && !(fabsf(p - log10_thr) >= band)) f = 1;  // also catches NaN
+  if (f == 0 && !(fabsf(p - sqrt_thr) >= band)) f = 1;  // also catches NaN
   // logistic of the HG indicator (fallback) or of the predicted one, then the
   // clipping of indicators_2d.jl:92-100 with the context's constants
-  float a = f != 0 ? hg[e] : 1.0f / (1.0f + expf(-s_par / thr * (exp10f(p) - thr)));
+  const float ep = fmaxf(p, 0.0f);
+  float a = f != 0 ? hg[e] : 1.0f / (1.0f + expf(-s_par / thr * (ep * ep - thr)));
   if (a < alpha_min) a = 0.0f;
   if (a > 1.0f - alpha_min) a = 1.0f;
   a = fminf(alpha_max, a);
@@ -441,12 +444,12 @@ int mlp_alpha(tg_mlp* m, tg_ctx* c, void* alpha_raw, bool fp64, float alpha_min,
   // d_hg holds the unclipped HG logistic; the alpha kernel clips both paths
   if (fp64)
     learned_alpha_kernel<double><<<nb, 256, 0, s>>>(m->d_pred, m->d_hg, m->d_flag, E,
-                                                    (float)m->log10_threshold, m->band, thr, spar,
+                                                    (float)m->sqrt_threshold, m->band, thr, spar,
                                                     alpha_min, alpha_max, (double*)alpha_raw,
                                                     m->d_stats);
   else
     learned_alpha_kernel<float><<<nb, 256, 0, s>>>(m->d_pred, m->d_hg, m->d_flag, E,
-                                                   (float)m->log10_threshold, m->band, thr, spar,
+                                                   (float)m->sqrt_threshold, m->band, thr, spar,
                                                    alpha_min, alpha_max, (float*)alpha_raw,
                                                    m->d_stats);
   MCUDA(m, cudaGetLastError());
@@ -474,7 +477,7 @@ int tg_mlp_create(int32_t ndims, int32_t polydeg, int32_t hidden, uint64_t seed,
   m->H = H;
   const MlpLayout L{NM, H};
   m->nparams = L.count();
-  m->log10_threshold = std::log10(0.5 * std::pow(10.0, -1.8 * std::pow((double)N, 0.25)));
+  m->sqrt_threshold = std::sqrt(0.5 * std::pow(10.0, -1.8 * std::pow((double)N, 0.25)));
   // He-uniform initialisation from a fixed-seed LCG
   std::vector<float> w(m->nparams, 0.0f);
   uint64_t st = seed * 6364136223846793005ull + 1442695040888963407ull;
@@ -485,7 +488,7 @@ int tg_mlp_create(int32_t ndims, int32_t polydeg, int32_t hidden, uint64_t seed,
   for (int i = 0; i < H * NM; ++i) w[L.w1() + i] = uni() * std::sqrt(6.0f / NM);
   for (int i = 0; i < H * H; ++i) w[L.w2() + i] = uni() * std::sqrt(6.0f / H);
   for (int i = 0; i < H; ++i) w[L.w3() + i] = uni() * std::sqrt(3.0f / H);
-  w[L.b3()] = -4.0f;  // a typical smooth-flow log10 E
+  w[L.b3()] = 0.0f;
   const size_t pb = sizeof(float) * m->nparams;
   cudaError_t e = cudaSuccess;
   e = e ? e : cudaMalloc(&m->d_w, pb);
@@ -689,7 +692,7 @@ int tg_mlp_gradient(tg_mlp* m, const float* x_host, const float* y_host, int32_t
   return TG_OK;
 }
 
-// Network predictions (log10 E) for explicit rows x_host [n][NM].
+// Network predictions (sqrt E) for explicit rows x_host [n][NM].
 int tg_mlp_predict(tg_mlp* m, const float* x_host, int64_t n, float* pred_host) {
   if (!m || !x_host || !pred_host || n < 1) return TG_ERR_INVALID_ARGUMENT;
   float *x = nullptr, *p = nullptr;
@@ -715,8 +718,8 @@ int tg_mlp_dataset(tg_mlp* m, float* x_host, float* y_host) {
 }
 
 // Use the network as the context's shock indicator (band: half-width of the
-// fallback zone in decades of E around the HG threshold).  m == NULL restores
-// the Hennemann-Gassner indicator.
+// fallback zone in sqrt(E) around sqrt of the HG threshold).  m == NULL
+// restores the Hennemann-Gassner indicator.
 int tg_ctx_set_learned_indicator(tg_ctx* c, tg_mlp* m, float band) {
   if (!c) return TG_ERR_INVALID_ARGUMENT;
   if (m) {
@@ -746,7 +749,7 @@ int tg_ctx_set_learned_indicator(tg_ctx* c, tg_mlp* m, float band) {
 }
 
 // Learned-indicator diagnostics of the last stage: per element the network's
-// blending factor inputs (pred: predicted log10 E), the HG factor (hg, with
+// blending factor inputs (pred: predicted sqrt E), the HG factor (hg, with
 // alpha_min = 0 and alpha_max = 1) and the fallback flag, plus the running
 // counts {elements evaluated, band fallbacks, positivity fallbacks}.
 int tg_mlp_last(tg_mlp* m, float* pred, float* hg, int32_t* flag, uint64_t* counts) {

@@ -17,8 +17,8 @@ def _fp(a):
 
 class ShockIndicatorMLP:
     """MLP n^d -> H -> H -> 1 (ReLU, BF16 weights, FP32 accumulation) predicting
-    log10 of the HG energy indicator from normalised modal coefficients of
-    density*pressure.  2D polydeg 3: 16 -> 64 -> 64 -> 1; 3D: 64 -> 128 -> 128 -> 1."""
+    sqrt of the HG energy indicator from modal coefficients of density*pressure
+    normalised to unit energy.  2D polydeg 3: 16 -> 64 -> 64 -> 1; 3D: 64 -> 128 -> 128 -> 1."""
 
     def __init__(self, ndims: int, polydeg: int, hidden: int = 0, seed: int = 1):
         self.lib = _lib.load()
@@ -60,7 +60,7 @@ class ShockIndicatorMLP:
         self._check(self.lib.tg_mlp_set_params(self.h, _fp(w)))
 
     def harvest(self, semi, stride: int = 1, phase: int = 0) -> int:
-        """Append (features, log10 E) of every stride-th element of the semi's
+        """Append (features, sqrt E) of every stride-th element of the semi's
         current device state to the training set; returns the set's size."""
         tot = ctypes.c_int64()
         self._check(self.lib.tg_mlp_harvest(self.h, semi.device_context.h, stride, phase,
@@ -96,9 +96,10 @@ class ShockIndicatorMLP:
         self._check(self.lib.tg_mlp_predict(self.h, _fp(x), len(x), _fp(p)))
         return p
 
-    def deploy(self, semi, band: float = 0.5):
-        """Use the network as semi's shock indicator (HG fallback within `band`
-        decades of the switching threshold and for non-positive rho*p)."""
+    def deploy(self, semi, band: float = 0.01):
+        """Use the network as semi's shock indicator (HG fallback where the
+        predicted sqrt(E) is within `band` of sqrt(threshold), and for
+        non-positive rho*p)."""
         self._check(self.lib.tg_ctx_set_learned_indicator(semi.device_context.h, self.h, band))
 
     @staticmethod
@@ -106,7 +107,7 @@ class ShockIndicatorMLP:
         _lib.check(_lib.load().tg_ctx_set_learned_indicator(semi.device_context.h, None, 0.0))
 
     def last(self, nelements: int):
-        """Per element: predicted log10 E, HG logistic, fallback flag; and the
+        """Per element: predicted sqrt(E), HG logistic, fallback flag; and the
         running counts (evaluated, band fallbacks, positivity fallbacks)."""
         pred = np.zeros(nelements, dtype=np.float32)
         hg = np.zeros(nelements, dtype=np.float32)
