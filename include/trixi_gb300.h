@@ -187,6 +187,12 @@ int tg_set_time(tg_ctx* ctx, double t);
  * out[nvar] = total mathematical entropy, out[nvar+1] = kinetic energy. */
 int tg_integrals(tg_ctx* ctx, double* out);
 
+/* analyze(entropy_timederivative, du, u, t, ...) (analysis_dg2d.jl:460-472):
+ * the volume-normalised integral of cons2entropy(u) . du with du = rhs(u, t)
+ * of the context state, evaluated by the context's own rhs! (FP64 or mixed)
+ * and integrated in FP64.  Synchronous. */
+int tg_entropy_timederivative(tg_ctx* ctx, double t, double* out);
+
 /* Blending factors of IndicatorHennemannGassner (after smoothing) for u_dev
  * (NULL: the context state), written to alpha_host[nelements].  Synchronous.
  * Only for TG_VOLUME_SHOCK_CAPTURING_HG contexts. */

@@ -66,6 +66,8 @@ def _load():
     lib.orc_solve.argtypes = [vp, P(d), d, d, d, i64, P(d), P(i64)]
     lib.orc_error_norms.argtypes = [vp, P(d), d, i, P(d), P(d), P(d)]
     lib.orc_integrals.argtypes = [vp, P(d), P(d)]
+    lib.orc_entropy_timederivative.restype = d
+    lib.orc_entropy_timederivative.argtypes = [vp, P(d), d]
     _lib = lib
     return lib
 
@@ -186,6 +188,15 @@ class Oracle:
         out = np.zeros(self.nvar + 2)
         self.lib.orc_integrals(self.h, _p(u), _p(out))
         return out
+
+
+def _entropy_timederivative(self, u, t=0.0):
+    """Normalised integral of cons2entropy(u) . rhs(u, t) (analysis_dg2d.jl:460-472)."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    return self.lib.orc_entropy_timederivative(self.h, _p(u), t)
+
+
+Oracle.entropy_timederivative = _entropy_timederivative
 
 
 def set_threads(n: int) -> None:

@@ -1224,4 +1224,42 @@ void orc_integrals(void* h, const double* u, double* out) {
   out[NV + 1] = acc[6];
 }
 
+// analyze(entropy_timederivative, ...), analysis_dg2d.jl:460-472: the
+// normalised integral of cons2entropy(u) . du with du = rhs(u, t);
+// cons2entropy, compressible_euler_2d.jl:2049-2066.
+double orc_entropy_timederivative(void* h, const double* u, double t) {
+  Solver& s = *(Solver*)h;
+  const int n = s.b.n, D = s.eq.D, NV = s.eq.NV;
+  std::vector<double> du((size_t)s.ndofs() * NV);
+  rhs(s, du.data(), u, t);
+  const double g = s.eq.gamma;
+  double acc = 0;
+  for (int64_t e = 0; e < s.m.nelem; ++e) {
+    double vj = 1.0 / s.m.inverse_jacobian[e];
+    vj = D == 2 ? vj * vj : vj * vj * vj;
+    for (int node = 0; node < s.nn; ++node) {
+      int idx[3] = {node % n, (node / n) % n, node / (n * n)};
+      double w = s.b.weights[idx[0]] * s.b.weights[idx[1]];
+      if (D == 3) w *= s.b.weights[idx[2]];
+      const double* un = &u[uidx(s, e, node, 0)];
+      const double* dn = &du[uidx(s, e, node, 0)];
+      double v[3], v2 = 0;
+      for (int d = 0; d < D; ++d) {
+        v[d] = un[1 + d] / un[0];
+        v2 += v[d] * v[d];
+      }
+      const double p = (g - 1) * (un[NV - 1] - 0.5 * un[0] * v2);
+      const double sth = std::log(p) - g * std::log(un[0]);
+      const double rho_p = un[0] / p;
+      double dot = ((g - sth) * s.eq.inv_gamma_minus_one - 0.5 * rho_p * v2) * dn[0];
+      for (int d = 0; d < D; ++d) dot += rho_p * v[d] * dn[1 + d];
+      dot += -rho_p * dn[NV - 1];
+      acc += vj * w * dot;
+    }
+  }
+  double vol = s.m.length0;
+  vol = D == 2 ? vol * vol : vol * vol * vol;
+  return acc / vol;
+}
+
 }  // extern "C"

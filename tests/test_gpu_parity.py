@@ -218,3 +218,35 @@ def test_rhs_with_device_pointers():
     semi.rhs(dud, ud, 0.4)
     semi.device_context.synchronize()
     assert rel_err(dud.cpu().numpy(), orc.rhs(u, 0.4)) < 1e-12
+
+
+@pytest.mark.parametrize("c", [RHS_CASES[0], RHS_CASES[4], RHS_CASES[6]], ids=lambda c: _id(c))
+def test_entropy_timederivative_matches_oracle(c):
+    semi, orc = build(c)
+    u = perturbed_state(semi, seed=29)
+    ctx = semi.device_context
+    ctx.upload(u)
+    ref = orc.entropy_timederivative(u, 0.3)
+    got = ctx.entropy_timederivative(0.3)
+    scale = abs(orc.integrals(u)[-2])  # total entropy, for the absolute tolerance
+    assert abs(got - ref) <= 1e-12 * scale + 1e-10 * abs(ref)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 1e-3)])
+@pytest.mark.parametrize("ndims", [2, 3])
+def test_entropy_conservative_scheme_produces_no_entropy(ndims, precision, tol):
+    # flux_ranocha as volume and surface flux is entropy conservative on a
+    # periodic mesh (elixir_euler_ec.jl): d/dt of the total entropy vanishes up
+    # to rounding, while the LLF surface flux dissipates at the jumps.
+    c = dict(ndims=ndims, polydeg=3, level=3 if ndims == 2 else 2, xmin=[-2.0] * ndims,
+             xmax=[2.0] * ndims, vi="fluxdiff", volume_flux="ranocha", surface_flux="ranocha",
+             ic="weak_blast_wave")
+    semi, _ = build(c, precision=precision)
+    semi_llf, _ = build(dict(c, surface_flux="llf"), precision=precision)
+    u = perturbed_state(semi, seed=31, amp=0.02)  # opens jumps at the interfaces
+    semi.device_context.upload(u)
+    semi_llf.device_context.upload(u)
+    ds = semi.device_context.entropy_timederivative(0.0)
+    ds_llf = semi_llf.device_context.entropy_timederivative(0.0)
+    assert ds_llf < 0
+    assert abs(ds) <= tol * abs(ds_llf), (ds, ds_llf)

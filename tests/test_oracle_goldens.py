@@ -32,3 +32,20 @@ def test_oracle_reproduces_trixi_golden(oracle_mod, name):
     assert t == pytest.approx(c["tspan"][1], rel=1e-14)
     np.testing.assert_allclose(l2, c["l2"], rtol=1e-9, atol=0)
     np.testing.assert_allclose(linf, c["linf"], rtol=1e-8, atol=0)
+
+
+def test_oracle_entropy_timederivative_ec_vs_llf():
+    # analysis_dg2d.jl:460-472 on a perturbed weak blast wave: zero up to rounding for
+    # the entropy-conservative flux_ranocha surface flux, negative for LLF
+    from oracle import oracle as O
+    kw = dict(volume_integral=O.VI_FLUXDIFF, volume_flux=O.FLUX_RANOCHA)
+    ec = O.Oracle(2, 3, 3, [-2.0, -2.0], [2.0, 2.0], surface_flux=O.FLUX_RANOCHA, **kw)
+    llf = O.Oracle(2, 3, 3, [-2.0, -2.0], [2.0, 2.0], surface_flux=O.FLUX_LAX_FRIEDRICHS, **kw)
+    u = ec.initial_condition(O.IC_WEAK_BLAST_WAVE)
+    # nodal interpolation is continuous across interfaces; a perturbation
+    # opens jumps for the surface flux to act on
+    u *= 1.0 + 0.02 * np.random.default_rng(11).uniform(-1, 1, size=u.shape)
+    ds_ec = ec.entropy_timederivative(u)
+    ds_llf = llf.entropy_timederivative(u)
+    assert ds_llf < 0
+    assert abs(ds_ec) < 1e-10 * abs(ds_llf)

@@ -297,6 +297,45 @@ __global__ void element_integrals_kernel(const TS* __restrict__ u,
   for (int k = 0; k < NV + 2; ++k) partial[(size_t)e * (NV + 2) + k] = acc[k];
 }
 
+// Per-element FP64 entropy production sum_nodes w J cons2entropy(u) . du
+// (analysis_dg2d.jl:460-472; cons2entropy, compressible_euler_2d.jl:2049-2066).
+template <int D>
+__global__ void element_entropy_kernel(const double* __restrict__ u, const double* __restrict__ du,
+                                       const double* __restrict__ inv_jac,
+                                       const double* __restrict__ weights, int64_t E, int N,
+                                       double gamma, double* __restrict__ partial) {
+  constexpr int NV = D + 2;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  int NN = N * N;
+  if (D == 3) NN *= N;
+  double vj = 1.0 / inv_jac[e];
+  vj = D == 2 ? vj * vj : vj * vj * vj;
+  double acc = 0, vol = 0;
+  for (int q = 0; q < NN; ++q) {
+    const int i = q % N, j = (q / N) % N, k = q / (N * N);
+    double w = weights[i] * weights[j];
+    if (D == 3) w *= weights[k];
+    const double* p = u + ((size_t)e * NN + q) * NV;
+    const double* dp = du + ((size_t)e * NN + q) * NV;
+    double v[D], v2 = 0;
+    for (int d = 0; d < D; ++d) {
+      v[d] = p[1 + d] / p[0];
+      v2 += v[d] * v[d];
+    }
+    const double pr = (gamma - 1) * (p[NV - 1] - 0.5 * p[0] * v2);
+    const double s = log(pr) - gamma * log(p[0]);
+    const double rho_p = p[0] / pr;
+    double dot = ((gamma - s) / (gamma - 1) - 0.5 * rho_p * v2) * dp[0];
+    for (int d = 0; d < D; ++d) dot += rho_p * v[d] * dp[1 + d];
+    dot += -rho_p * dp[NV - 1];
+    acc += vj * w * dot;
+    vol += vj * w;
+  }
+  partial[2 * e] = acc;
+  partial[2 * e + 1] = vol;
+}
+
 // Deterministic sum of partial[E][K] over elements (one block).
 __global__ void sum_rows_kernel(const double* __restrict__ partial, int64_t E, int K,
                                 double* __restrict__ out) {
@@ -1093,6 +1132,34 @@ int tg_integrals(tg_ctx* c, double* out) {
   CUDA_TRY(c, cudaGetLastError());
   CUDA_TRY(c, cudaMemcpyAsync(out, c->d_sums, sizeof(double) * K, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return TG_OK;
+}
+
+int tg_entropy_timederivative(tg_ctx* c, double t, double* out) {
+  if (!c || !out) return TG_ERR_INVALID_ARGUMENT;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  const size_t vb = sizeof(double) * c->nvalues;
+  int rc = ensure(c, (void**)&c->d_du, vb);
+  if (rc) return rc;
+  const double* u64 = export_state(c, &rc);
+  if (rc) return rc;
+  rc = tg_rhs(c, c->d_du, u64, t);
+  if (rc) return rc;
+  const int K = c->NV + 2;  // the integrals' partial buffer has room for 2 per element
+  if (!c->d_partial) CUDA_TRY(c, cudaMalloc((void**)&c->d_partial, sizeof(double) * K * c->E));
+  const int64_t nb = (c->E + 127) / 128;
+  if (c->D == 2)
+    element_entropy_kernel<2><<<(unsigned)nb, 128, 0, c->stream>>>(u64, c->d_du, c->d_invj, c->d_weights,
+                                                                   c->E, c->N, c->P.gamma, c->d_partial);
+  else
+    element_entropy_kernel<3><<<(unsigned)nb, 128, 0, c->stream>>>(u64, c->d_du, c->d_invj, c->d_weights,
+                                                                   c->E, c->N, c->P.gamma, c->d_partial);
+  sum_rows_kernel<<<1, 256, 256 * sizeof(double), c->stream>>>(c->d_partial, c->E, 2, c->d_sums);
+  CUDA_TRY(c, cudaGetLastError());
+  double h[2];
+  CUDA_TRY(c, cudaMemcpyAsync(h, c->d_sums, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  *out = h[0] / h[1];
   return TG_OK;
 }
 

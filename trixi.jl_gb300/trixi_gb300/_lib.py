@@ -31,7 +31,8 @@ EXPORTS = ("tg_api_version", "tg_ctx_create", "tg_ctx_destroy", "tg_last_error",
            "tg_elements_per_block", "tg_stream", "tg_integrals_noalloc",
            "tg_mlp_create", "tg_mlp_destroy", "tg_mlp_nparams", "tg_mlp_get_params",
            "tg_mlp_set_params", "tg_mlp_harvest", "tg_mlp_dataset", "tg_mlp_train",
-           "tg_mlp_gradient", "tg_mlp_predict", "tg_ctx_set_learned_indicator", "tg_mlp_last")
+           "tg_mlp_gradient", "tg_mlp_predict", "tg_ctx_set_learned_indicator", "tg_mlp_last",
+           "tg_entropy_timederivative")
 
 
 class TrixiGB300Error(RuntimeError):
@@ -122,6 +123,7 @@ def load(path: str | None = None):
         "tg_mlp_predict": ([vp, vp, i64, vp], ctypes.c_int),
         "tg_ctx_set_learned_indicator": ([vp, vp, ctypes.c_float], ctypes.c_int),
         "tg_mlp_last": ([vp, vp, vp, vp, vp], ctypes.c_int),
+        "tg_entropy_timederivative": ([vp, d, pd], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

@@ -162,6 +162,12 @@ class DeviceContext:
         self._check(self.lib.tg_integrals(self.h, _dptr(out)))
         return out
 
+    def entropy_timederivative(self, t=0.0) -> float:
+        """Normalised integral of cons2entropy(u) . rhs(u, t) of the device state."""
+        out = ctypes.c_double()
+        self._check(self.lib.tg_entropy_timederivative(self.h, float(t), ctypes.byref(out)))
+        return out.value
+
     def alpha(self, u=None):
         a = np.zeros(self.semi.nelements)
         self._check(self.lib.tg_alpha(self.h, None if u is None else _ptr_of(u), _dptr(a)))
