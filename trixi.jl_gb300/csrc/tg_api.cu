@@ -206,6 +206,8 @@ __device__ void stage_phases(Clock* c) {
     sincospi(c->t + CK_C_DEV[s] * c->dt, &sn, &cs);
     c->sin_t[s] = (float)sn;
     c->cos_t[s] = (float)cs;
+    c->sin_tl[s] = (float)(sn - (double)c->sin_t[s]);
+    c->cos_tl[s] = (float)(cs - (double)c->cos_t[s]);
   }
 }
 
@@ -408,9 +410,8 @@ struct tg_ctx {
   double* d_xline = nullptr;
   float* d_invj_f = nullptr;
   float* d_xline_f = nullptr;
-  double* d_x0 = nullptr;
-  float* d_xoff = nullptr;
-  float2* d_sc0 = nullptr;
+  float4* d_sc0 = nullptr;            // mixed source phase of each element's first node
+  float4* d_scn = nullptr;            // and of the node offsets (one table)
   double* d_weights = nullptr;
   double* d_partial = nullptr;
   double* d_sums = nullptr;
@@ -462,7 +463,7 @@ static void free_ctx(tg_ctx* c) {
     if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
   void* ptrs[] = {c->d_u[0], c->d_u[1], c->d_utmp, c->d_du, c->d_uscratch, c->d_stage64,
                   c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_nbr, c->d_invj, c->d_xline,
-                  c->d_invj_f, c->d_xline_f, c->d_x0, c->d_xoff, c->d_sc0, c->d_weights, c->d_partial, c->d_sums, c->d_clock,
+                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_weights, c->d_partial, c->d_sums, c->d_clock,
                   c->d_status, c->d_speed};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -568,8 +569,11 @@ static int launch_kernel(tg_ctx* c, int mode, const void* u_in, void* u_out, dou
       A.zero_tmp = stage == 0;
       A.stage = stage;
     } else {
-      A.sin_t = (float)std::sin(M_PI * t_rhs);
-      A.cos_t = (float)std::cos(M_PI * t_rhs);
+      const double sn = std::sin(M_PI * t_rhs), cs = std::cos(M_PI * t_rhs);
+      A.sin_t = (float)sn;
+      A.cos_t = (float)cs;
+      A.sin_tl = (float)(sn - (double)A.sin_t);
+      A.cos_tl = (float)(cs - (double)A.cos_t);
     }
     A.speed_bits = reduce ? &c->d_clock->speed_bits : nullptr;
     rc = launch_mixed(c->D, c->N, c->vi, c->epb, c->MP, A, c->stream);
@@ -814,28 +818,52 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     ALLOC(c->d_alpha_raw, rsize(c) * c->E);
     ALLOC(c->d_alpha, sizeof(double) * c->E);
   }
-  std::vector<float> invj_f, xline_f, xoff;
-  std::vector<double> x0;
+  std::vector<float> invj_f, xline_f;
+  std::vector<float4> sc0, scn;
   if (!c->fp64) {
     invj_f.resize(c->E);
     for (int64_t k = 0; k < c->E; ++k) invj_f[k] = (float)cfg->inverse_jacobian[k];
     xline_f.assign(xline.begin(), xline.end());
     ALLOC(c->d_invj_f, sizeof(float) * c->E);
     if (!xline_f.empty()) {
-      // first node coordinate (FP64) and offsets along each axis (FP32) for
-      // the mixed path's source-term phase
-      x0.resize((size_t)c->E * D);
-      xoff.resize(xline.size());
-      for (int64_t e2 = 0; e2 < c->E; ++e2)
-        for (int d = 0; d < D; ++d) {
-          const double* xl = &xline[((size_t)e2 * D + d) * N];
-          x0[(size_t)e2 * D + d] = xl[0];
-          for (int i = 0; i < N; ++i) xoff[((size_t)e2 * D + d) * N + i] = (float)(xl[i] - xl[0]);
-        }
       ALLOC(c->d_xline_f, sizeof(float) * xline_f.size());
-      ALLOC(c->d_x0, sizeof(double) * x0.size());
-      ALLOC(c->d_xoff, sizeof(float) * xoff.size());
-      ALLOC(c->d_sc0, sizeof(float2) * c->E);
+      if (c->P.source == SRC_CONVERGENCE_TEST) {
+        // source phase pi (sum_d x_d - t) of the mixed path, split into the
+        // first node of each element (FP64 -> float-float sin/cos) and the
+        // node offsets from it, which are the same for every element of a
+        // conforming mesh (checked)
+        auto ffsc = [](double ph) {
+          const double sn = std::sin(M_PI * ph), cs = std::cos(M_PI * ph);
+          const float sh = (float)sn, ch = (float)cs;
+          return make_float4(sh, ch, (float)(sn - (double)sh), (float)(cs - (double)ch));
+        };
+        sc0.resize(c->E);
+        for (int64_t e2 = 0; e2 < c->E; ++e2) {
+          double ph = 0;
+          for (int d = 0; d < D; ++d) {
+            const double* xl = &xline[((size_t)e2 * D + d) * N];
+            const double* x1 = &xline[(size_t)d * N];
+            ph += xl[0];
+            for (int i = 0; i < N; ++i)
+              if (std::fabs((xl[i] - xl[0]) - (x1[i] - x1[0])) > 1e-12 * std::fabs(x1[N - 1] - x1[0])) {
+                free_ctx(c);
+                return fail(nullptr, TG_ERR_UNSUPPORTED,
+                            "mixed precision source terms need elements of one size");
+              }
+          }
+          sc0[e2] = ffsc(ph);
+        }
+        int NN = 1;
+        for (int d = 0; d < D; ++d) NN *= N;
+        scn.resize(NN);
+        for (int q = 0; q < NN; ++q) {
+          double ph = 0;
+          for (int d = 0, r = q; d < D; ++d, r /= N) ph += xline[(size_t)d * N + r % N] - xline[(size_t)d * N];
+          scn[q] = ffsc(ph);
+        }
+        ALLOC(c->d_sc0, sizeof(float4) * sc0.size());
+        ALLOC(c->d_scn, sizeof(float4) * scn.size());
+      }
     }
   }
 #undef ALLOC
@@ -844,15 +872,10 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     if (!xline_f.empty()) {
       cudaMemcpy(c->d_xline_f, xline_f.data(), sizeof(float) * xline_f.size(),
                  cudaMemcpyHostToDevice);
-      cudaMemcpy(c->d_x0, x0.data(), sizeof(double) * x0.size(), cudaMemcpyHostToDevice);
-      cudaMemcpy(c->d_xoff, xoff.data(), sizeof(float) * xoff.size(), cudaMemcpyHostToDevice);
-      std::vector<float2> sc0((size_t)c->E);
-      for (int64_t e2 = 0; e2 < c->E; ++e2) {
-        double ph = 0;
-        for (int d = 0; d < D; ++d) ph += x0[(size_t)e2 * D + d];
-        sc0[e2] = make_float2((float)std::sin(M_PI * ph), (float)std::cos(M_PI * ph));
+      if (!sc0.empty()) {
+        cudaMemcpy(c->d_sc0, sc0.data(), sizeof(float4) * sc0.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(c->d_scn, scn.data(), sizeof(float4) * scn.size(), cudaMemcpyHostToDevice);
       }
-      cudaMemcpy(c->d_sc0, sc0.data(), sizeof(float2) * c->E, cudaMemcpyHostToDevice);
     }
   }
   cudaMemcpy(c->d_nbr, nbr.data(), sizeof(int32_t) * nbr.size(), cudaMemcpyHostToDevice);
@@ -876,6 +899,11 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   M.nelements = P.nelements;
   M.gamma = (float)P.gamma;
   M.inv_gamma_minus_one = (float)P.inv_gamma_minus_one;
+  M.eos.gamma = (float)P.gamma;
+  M.eos.gm1 = (float)(P.gamma - 1.0);
+  M.eos.gm1_lo = (float)((P.gamma - 1.0) - (double)M.eos.gm1);
+  M.eos.igm1 = (float)P.inv_gamma_minus_one;
+  M.eos.gigm1 = (float)(P.gamma * P.inv_gamma_minus_one);
   for (int k = 0; k < MAXN; ++k) M.inv_weights[k] = (float)P.inv_weights[k];
   for (int k = 0; k < MAXN * MAXN; ++k) {
     M.Dhat[k] = (float)P.Dhat[k];
@@ -895,9 +923,8 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   M.nbr = c->d_nbr;
   M.inv_jac = c->d_invj_f;
   M.xline = c->d_xline_f;
-  M.x0 = c->d_x0;
-  M.xoff = c->d_xoff;
   M.sc0 = c->d_sc0;
+  M.scn = c->d_scn;
   *out = c;
   return TG_OK;
 }

@@ -64,6 +64,7 @@ struct Clock {
   int32_t skip, finalstep, finished, nan_dt;
   int64_t steps;
   float sin_t[5], cos_t[5];       // sin/cos(pi (t + c_s dt)) of the 2N stages
+  float sin_tl[5], cos_tl[5];     // their low parts (float-float)
 };
 
 enum StageMode { MODE_RHS = 0, MODE_STAGE = 1 };

@@ -10,8 +10,8 @@
 //
 // 2. Deviation form.  Within element e all fluxes are evaluated as deviations
 //    F(a, b) - f(w_e) from the physical flux of a reference state w_e (the
-//    primitives of node 0's `hi` part), using algebra that involves only node
-//    deviations from w_e.  Those deviations are formed exactly from the
+//    primitives of the mean `hi` of two opposite corner nodes), using algebra
+//    that involves only node deviations from w_e.  Those are formed from the
 //    float-float state ((hi_i - hi_ref) + lo_i), so FP32 rounding is relative
 //    to |u_i - u_ref| instead of |u_i|.  The reference flux drops out exactly:
 //    the split-form and weak-form derivative matrices have zero interior row
@@ -30,11 +30,23 @@
 
 namespace tg {
 
+// FP32 equation-of-state constants, each rounded once from the FP64 gamma.
+// gamma - 1 multiplies every pressure and pressure deviation; rounded to a
+// float it is off by up to 3e-8 in the same direction everywhere, which acts
+// like a slightly different gas and shifts the whole solution coherently over
+// a long run, so it is carried as a float-float pair (hi + lo).  For gamma =
+// 1.4 the other two are exact (2.5 and 3.5).
+struct EosF {
+  float gamma, gm1, gm1_lo, igm1, gigm1;  // gamma, gamma-1 (hi, lo), 1/(gamma-1), gamma/(gamma-1)
+  __host__ __device__ __forceinline__ float pressure(float x) const {
+    return fmaf(gm1_lo, x, gm1 * x);  // (gamma - 1) x with one rounding
+  }
+};
+
 struct MixedParams {
   int64_t nelements;
-  const double* x0;         // [E][D] coordinates of node (0,0,0) (source terms)
-  const float* xoff;        // [E][D][N] node coordinates minus x0 along each axis
   float gamma, inv_gamma_minus_one;
+  EosF eos;                 // the same constants, consistent for the flux algebra
   float inv_weights[MAXN];
   float Dhat[MAXN * MAXN];
   float Dsplit[MAXN * MAXN];
@@ -45,7 +57,12 @@ struct MixedParams {
   const int32_t* nbr;       // [E][2D]
   const float* inv_jac;     // [E]
   const float* xline;       // [E][D][N] or null (unused by the stage kernel)
-  const float2* sc0;        // [E] (sin, cos)(pi * sum_d x0_d) for the source phase
+  // source phase pi (sum_d x_d - t) as float-float sin/cos parts
+  // (sin_hi, cos_hi, sin_lo, cos_lo): of the first node of each element, and
+  // of each node's offset from the first node (one table: all elements of a
+  // conforming mesh have one size)
+  const float4* sc0;        // [E]
+  const float4* scn;        // [NN]
 };
 
 struct MixedArgs {
@@ -63,7 +80,8 @@ struct MixedArgs {
   int32_t mode;
   int32_t zero_tmp;
   int32_t stage;            // MODE_STAGE: index into the clock's per-stage phase
-  float sin_t, cos_t;       // MODE_RHS: sin/cos(pi t)
+  float sin_t, cos_t;       // MODE_RHS: sin/cos(pi t), float-float
+  float sin_tl, cos_tl;
 };
 
 // ---------------------------------------------------------------------------
@@ -73,7 +91,7 @@ template <int D>
 struct RefState {
   float rho, v[D], p;   // reference primitives w_e
   float q, rq;          // q = rho/p and its residual rho - q p (exact by FMA)
-  float hi[D + 2];      // conservative reference (hi of node 0)
+  float hi[D + 2];      // conservative reference (mean hi of opposite corners)
   float r[D + 2];       // hi - cons(w_e): momentum residual exact, energy to FP32
 };
 
@@ -90,8 +108,9 @@ template <int D>
 struct Dev {
   static constexpr int NV = D + 2, P = D + 1;
 
-  static __host__ __device__ __forceinline__ void make_ref(const float* hi, float gamma, float igm1,
+  static __host__ __device__ __forceinline__ void make_ref(const float* hi, const EosF& eos,
                                                    RefState<D>& R) {
+    const float igm1 = eos.igm1;
     R.rho = hi[0];
     const float irho = 1.0f / R.rho;
     float ke = 0;
@@ -100,7 +119,7 @@ struct Dev {
       R.v[d] = hi[1 + d] * irho;
       ke += hi[1 + d] * R.v[d];
     }
-    R.p = (gamma - 1.0f) * (hi[P] - 0.5f * ke);
+    R.p = eos.pressure(hi[P] - 0.5f * ke);
     R.q = R.rho / R.p;
     R.rq = fmaf(-R.q, R.p, R.rho);
     float v2 = 0;
@@ -122,7 +141,7 @@ struct Dev {
 
   // Node state (hi, lo) -> deviations relative to R and full primitives.
   static __host__ __device__ __forceinline__ void make_node(const float* hi, const float* lo,
-                                                    const RefState<D>& R, float gamma, Node<D>& n) {
+                                                    const RefState<D>& R, const EosF& eos, Node<D>& n) {
 #pragma unroll
     for (int v = 0; v < NV; ++v) n.du[v] = ((hi[v] - R.hi[v]) + lo[v]) + R.r[v];
     const float drho = n.du[0];
@@ -140,7 +159,7 @@ struct Dev {
     }
     // rho|v|^2 - rho_ref|v_ref|^2 = drho |v_ref|^2 + rho (2 v_ref.dv + |dv|^2)
     const float dkin = drho * vbar2 + rho * kin;
-    const float dp = (gamma - 1.0f) * (n.du[P] - 0.5f * dkin);
+    const float dp = eos.pressure(n.du[P] - 0.5f * dkin);
     n.dw[0] = drho;
     n.w[0] = rho;
     n.dw[P] = dp;
@@ -186,7 +205,7 @@ struct Dev {
 
   // physical flux deviation f(w) - f(w_ref), orientation o
   static __host__ __device__ __forceinline__ void dflux(const RefState<D>& R, const Node<D>& a, int o,
-                                                float vro, float gamma, float igm1, float* f) {
+                                                float vro, const EosF& eos, float* f) {
     const float vo = a.vo, dvo = a.dvo;
     const float d1 = a.dw[0] * vro + a.w[0] * dvo;
     const float F1r = R.rho * vro;
@@ -198,25 +217,25 @@ struct Dev {
       dk += a.dw[1 + d] * (R.v[d] + 0.5f * a.dw[1 + d]);
       k += a.w[1 + d] * a.w[1 + d];
     }
-    f[P] = d1 * (0.5f * k) + F1r * dk + gamma * igm1 * (a.dw[P] * vo + R.p * dvo);
+    f[P] = d1 * (0.5f * k) + F1r * dk + eos.gigm1 * (a.dw[P] * vo + R.p * dvo);
   }
 
   static __host__ __device__ __forceinline__ void dcentral(const RefState<D>& R, const Node<D>& a,
-                                                   const Node<D>& b, int o, float vro, float gamma,
-                                                   float igm1, float* f) {
+                                                   const Node<D>& b, int o, float vro,
+                                                   const EosF& eos, float* f) {
     float fa[NV], fb[NV];
-    dflux(R, a, o, vro, gamma, igm1, fa);
-    dflux(R, b, o, vro, gamma, igm1, fb);
+    dflux(R, a, o, vro, eos, fa);
+    dflux(R, b, o, vro, eos, fb);
 #pragma unroll
     for (int v = 0; v < NV; ++v) f[v] = 0.5f * (fa[v] + fb[v]);
   }
 
   static __host__ __device__ __forceinline__ void dllf(const RefState<D>& R, const Node<D>& a,
                                                const Node<D>& b, int o, float vro, bool naive,
-                                               float gamma, float igm1, float* f) {
-    dcentral(R, a, b, o, vro, gamma, igm1, f);
-    const float ca = sqrtf(gamma * a.w[P] / a.w[0]);
-    const float cb = sqrtf(gamma * b.w[P] / b.w[0]);
+                                               const EosF& eos, float* f) {
+    dcentral(R, a, b, o, vro, eos, f);
+    const float ca = sqrtf(eos.gamma * a.w[P] / a.w[0]);
+    const float cb = sqrtf(eos.gamma * b.w[P] / b.w[0]);
     const float va = fabsf(a.vo), vb = fabsf(b.vo);
     const float lam = naive ? fmaxf(va, vb) + fmaxf(ca, cb) : fmaxf(va + ca, vb + cb);
 #pragma unroll
@@ -225,8 +244,9 @@ struct Dev {
 
   // flux_ranocha(a, b) - f(w_ref)
   static __host__ __device__ __forceinline__ void dranocha(const RefState<D>& R, const Node<D>& a,
-                                                   const Node<D>& b, int o, float vro, float igm1,
+                                                   const Node<D>& b, int o, float vro, const EosF& eos,
                                                    float* f) {
+    const float igm1 = eos.igm1;
     const float drho_ln = dev_ln_mean(R.rho, a.dw[0], b.dw[0], a.w[0], b.w[0]);
     // q = rho / p relative to R.q (node deviations a.dq, b.dq from make_node)
     const float dq_ln = dev_ln_mean(R.q, a.dq, b.dq, R.q + a.dq, R.q + b.dq);
@@ -260,8 +280,9 @@ struct Dev {
 
   // flux_shima_etal(a, b) - f(w_ref)
   static __host__ __device__ __forceinline__ void dshima(const RefState<D>& R, const Node<D>& a,
-                                                 const Node<D>& b, int o, float vro, float igm1,
+                                                 const Node<D>& b, int o, float vro, const EosF& eos,
                                                  float* f) {
+    const float igm1 = eos.igm1;
     const float drho = 0.5f * (a.dw[0] + b.dw[0]);
     float dvavg[D], vavg[D];
     float dkin = 0, kin = 0;
@@ -292,24 +313,24 @@ struct Dev {
   template <int KIND>
   static __host__ __device__ __forceinline__ void flux2(int kind, const RefState<D>& R,
                                                          const Node<D>& a, const Node<D>& b, int o,
-                                                         float vro, float gamma, float igm1, float* f) {
-    if constexpr (KIND == FLUX_RANOCHA) dranocha(R, a, b, o, vro, igm1, f);
-    else if constexpr (KIND == FLUX_SHIMA_ETAL) dshima(R, a, b, o, vro, igm1, f);
-    else if constexpr (KIND == FLUX_LLF) dllf(R, a, b, o, vro, false, gamma, igm1, f);
-    else if constexpr (KIND == FLUX_LLF_NAIVE) dllf(R, a, b, o, vro, true, gamma, igm1, f);
-    else if constexpr (KIND == FLUX_CENTRAL) dcentral(R, a, b, o, vro, gamma, igm1, f);
-    else two_point(kind, R, a, b, o, vro, gamma, igm1, f);
+                                                         float vro, const EosF& eos, float* f) {
+    if constexpr (KIND == FLUX_RANOCHA) dranocha(R, a, b, o, vro, eos, f);
+    else if constexpr (KIND == FLUX_SHIMA_ETAL) dshima(R, a, b, o, vro, eos, f);
+    else if constexpr (KIND == FLUX_LLF) dllf(R, a, b, o, vro, false, eos, f);
+    else if constexpr (KIND == FLUX_LLF_NAIVE) dllf(R, a, b, o, vro, true, eos, f);
+    else if constexpr (KIND == FLUX_CENTRAL) dcentral(R, a, b, o, vro, eos, f);
+    else two_point(kind, R, a, b, o, vro, eos, f);
   }
 
   static __host__ __device__ __forceinline__ void two_point(int kind, const RefState<D>& R,
                                                     const Node<D>& a, const Node<D>& b, int o,
-                                                    float vro, float gamma, float igm1, float* f) {
+                                                    float vro, const EosF& eos, float* f) {
     switch (kind) {
-      case FLUX_RANOCHA: dranocha(R, a, b, o, vro, igm1, f); break;
-      case FLUX_SHIMA_ETAL: dshima(R, a, b, o, vro, igm1, f); break;
-      case FLUX_LLF: dllf(R, a, b, o, vro, false, gamma, igm1, f); break;
-      case FLUX_LLF_NAIVE: dllf(R, a, b, o, vro, true, gamma, igm1, f); break;
-      default: dcentral(R, a, b, o, vro, gamma, igm1, f); break;
+      case FLUX_RANOCHA: dranocha(R, a, b, o, vro, eos, f); break;
+      case FLUX_SHIMA_ETAL: dshima(R, a, b, o, vro, eos, f); break;
+      case FLUX_LLF: dllf(R, a, b, o, vro, false, eos, f); break;
+      case FLUX_LLF_NAIVE: dllf(R, a, b, o, vro, true, eos, f); break;
+      default: dcentral(R, a, b, o, vro, eos, f); break;
     }
   }
 };
@@ -323,6 +344,22 @@ __device__ __forceinline__ float2 ff_add(float2 u, float x) {
   const float h = __fadd_rn(s, t);
   const float l = __fsub_rn(t, __fsub_rn(h, s));
   return make_float2(h, l);
+}
+
+// (ah + al)(bh + bl) + (ch + cl)(dh + dl) as a normalised float-float pair:
+// exact products and TwoSum of the leading terms, cross terms added to the
+// low part (relative error a few units of 2^-46).  The _rn intrinsics keep
+// the compiler from contracting the error-free transformations into FMAs.
+__device__ __forceinline__ float2 ff_dot2(float ah, float al, float bh, float bl, float ch, float cl,
+                                          float dh, float dl) {
+  const float p = __fmul_rn(ah, bh), q = __fmul_rn(ch, dh);
+  const float ep = fmaf(ah, bh, -p), eq = fmaf(ch, dh, -q);
+  const float s = __fadd_rn(p, q);
+  const float bp = __fsub_rn(s, p);
+  const float es = __fadd_rn(__fsub_rn(p, __fsub_rn(s, bp)), __fsub_rn(q, bp));
+  const float lo = es + ep + eq + fmaf(ah, bl, fmaf(al, bh, fmaf(ch, dl, cl * dh)));
+  const float hi = __fadd_rn(s, lo);
+  return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
 }
 
 // cp.async (sm_80+ asynchronous global->shared copies) helpers
@@ -382,7 +419,7 @@ struct MixedKernel {
   static constexpr size_t smem_bytes() {
     return sizeof(float2) * (CHUNK + FACE) + sizeof(float) * (CHUNK + ALIGN4)  // state, traces, u_tmp
            + sizeof(float) * (NFLD * SP + D * NV * SP               // node fields, partial du
-                              + EPB * REFW + EPB * 4 + 4            // references, per element
+                              + EPB * REFW + EPB * 8 + 8            // references, per element
                               + EPB * D                             // speed maxima
                               + N * N + N + 4);                     // matrix, inverse weights
   }
@@ -392,18 +429,22 @@ template <int D>
 struct SourceMMS {
   // source_terms_convergence_test, compressible_euler_2d.jl:116-145, 3d.jl:127-150,
   // given sin/cos of the phase omega (x+y(+z)-t)
-  static __device__ __forceinline__ void eval(float si, float co, float gamma, float* s) {
-    const float A = 0.1f, omega = 3.14159265358979f;
-    const float rho = 2.0f + A * si;
-    const float rho_x = omega * A * co;
+  static __device__ __forceinline__ void eval(float si, float co, const EosF& eos, float* s) {
+    // A omega = 0.1 pi as a float-float pair: one rounded constant would bias
+    // the source by the same relative amount at every node and stage
+    constexpr double AW = 0.1 * 3.14159265358979323846;
+    constexpr float aw_hi = (float)AW;
+    constexpr float aw_lo = (float)(AW - (double)aw_hi);
+    const float rho = 2.0f + 0.1f * si;
+    const float rho_x = fmaf(co, aw_lo, co * aw_hi);
     if (D == 2) {
-      const float tmp = (2.0f * rho - 1.0f) * (gamma - 1.0f);
+      const float tmp = eos.pressure(2.0f * rho - 1.0f);
       s[0] = rho_x;
       s[1] = rho_x * (1.0f + tmp);
       s[2] = s[1];
       s[D + 1] = 2.0f * rho_x * (rho + tmp);
     } else {
-      const float tmp = (2.0f * rho - 1.5f) * (gamma - 1.0f);
+      const float tmp = eos.pressure(2.0f * rho - 1.5f);
       s[0] = 2.0f * rho_x;
       s[1] = rho_x * (2.0f + tmp);
       s[2] = s[1];
@@ -423,7 +464,7 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
   using Lay = NodeLayout<D, N, EPB>;
   using Dv = Dev<D>;
   constexpr int NV = K::NV, NN = K::NN, SP = K::SP, NF = K::NF;
-  const float gamma = P.gamma, igm1 = P.inv_gamma_minus_one;
+  const EosF& eos = P.eos;
   const int S = axis_stride<N>(dd);
   const int lb = line_base<N>(line, dd);
   const float vro = Dv::pick(R.v, dd);
@@ -478,7 +519,7 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
 #pragma unroll
     for (int a = 0; a < N; ++a) {
       float f[NV];
-      Dv::dflux(R, nd[a], dd, vro, gamma, igm1, f);
+      Dv::dflux(R, nd[a], dd, vro, eos, f);
 #pragma unroll
       for (int ii = 0; ii < N; ++ii) {
         const float c = s_mat[ii * N + a];
@@ -493,7 +534,7 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
 #pragma unroll
       for (int b = a + 1; b < N; ++b) {
         float F[NV];
-        Dv::template flux2<VF>(P.volume_flux, R, nd[a], nd[b], dd, vro, gamma, igm1, F);
+        Dv::template flux2<VF>(P.volume_flux, R, nd[a], nd[b], dd, vro, eos, F);
         const float cab = s_mat[a * N + b], cba = s_mat[b * N + a];
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
@@ -510,7 +551,7 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
 #pragma unroll
       for (int a = 0; a + 1 < N; ++a) {
         float F[NV];
-        Dv::two_point(P.fv_flux, R, nd[a], nd[a + 1], dd, vro, gamma, igm1, F);
+        Dv::two_point(P.fv_flux, R, nd[a], nd[a + 1], dd, vro, eos, F);
         const float ca = alpha * s_iw[a], cb = alpha * s_iw[a + 1];
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
@@ -542,7 +583,7 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
       lo[v] = x.y;
     }
     Node<D> nn_;
-    Dv::make_node(hi, lo, R, gamma, nn_);
+    Dv::make_node(hi, lo, R, eos, nn_);
     Dv::orient(nn_, dd);
     Node<D>& own = side ? nd[N - 1] : nd[0];
     if (!NEED_DU) {
@@ -552,11 +593,11 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
     }
     float F[NV];
     if (side) {
-      Dv::template flux2<SF>(P.surface_flux, R, own, nn_, dd, vro, gamma, igm1, F);
+      Dv::template flux2<SF>(P.surface_flux, R, own, nn_, dd, vro, eos, F);
 #pragma unroll
       for (int v = 0; v < NV; ++v) acc[N - 1][v] = fmaf(F[v], factor, acc[N - 1][v]);
     } else {
-      Dv::template flux2<SF>(P.surface_flux, R, nn_, own, dd, vro, gamma, igm1, F);
+      Dv::template flux2<SF>(P.surface_flux, R, nn_, own, dd, vro, eos, F);
 #pragma unroll
       for (int v = 0; v < NV; ++v) acc[0][v] = fmaf(-F[v], factor, acc[0][v]);
     }
@@ -593,9 +634,11 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
   float* s_nd = s_tmp + CHUNK + K::ALIGN4;
   float* s_part = s_nd + NFLD * SP;
   RefState<D>* s_ref = reinterpret_cast<RefState<D>*>(s_part + D * NV * SP);
-  float* s_elem = reinterpret_cast<float*>(s_ref + EPB);  // [EPB][4]: alpha, sin, cos
-  float* s_scal = s_elem + EPB * 4;                         // b dt, a, sin(pi t), cos(pi t)
-  unsigned int* s_smax = reinterpret_cast<unsigned int*>(s_scal + 4);
+  // [EPB][8]: alpha, then sin/cos (hi, hi, lo, lo) of pi (x_first - t)
+  float* s_elem = reinterpret_cast<float*>(s_ref + EPB);
+  // b dt, a, sin/cos(pi t) (hi, hi, lo, lo), b dt lo, a lo
+  float* s_scal = s_elem + EPB * 8;
+  unsigned int* s_smax = reinterpret_cast<unsigned int*>(s_scal + 8);
   float* s_mat = reinterpret_cast<float*>(s_smax + EPB * D);
   float* s_iw = s_mat + N * N;
 
@@ -636,16 +679,25 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
   if (tid < N) s_iw[tid] = P.inv_weights[tid];
   if (tid < EPB * D) s_smax[tid] = 0u;
   if (tid == 0) {
+    // b dt and a as float-float pairs: rounded once they would perturb the
+    // 2N weights by the same amount every step (a drift of the time axis)
+    const double bdt = A.mode == MODE_RHS ? 0.0 : A.b * A.clock->dt;
+    const float bh = (float)bdt, ah = (float)A.a;
+    s_scal[0] = bh;
+    s_scal[6] = (float)(bdt - (double)bh);
+    s_scal[1] = ah;
+    s_scal[7] = (float)(A.a - (double)ah);
     if (A.mode == MODE_RHS) {
-      s_scal[0] = 0.0f;
       s_scal[2] = A.sin_t;
       s_scal[3] = A.cos_t;
+      s_scal[4] = A.sin_tl;
+      s_scal[5] = A.cos_tl;
     } else {
-      s_scal[0] = (float)(A.b * A.clock->dt);
       s_scal[2] = A.clock->sin_t[A.stage];
       s_scal[3] = A.clock->cos_t[A.stage];
+      s_scal[4] = A.clock->sin_tl[A.stage];
+      s_scal[5] = A.clock->cos_tl[A.stage];
     }
-    s_scal[1] = (float)A.a;
   }
   if (tid < nel) {
     const int64_t e = e0 + tid;
@@ -655,7 +707,7 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
 #pragma unroll
         for (int dir = 0; dir < 2 * D; ++dir) a = fmaxf(a, 0.5f * A.alpha_raw[P.nbr[e * 2 * D + dir]]);
       }
-      s_elem[tid * 4 + 0] = a;
+      s_elem[tid * 8 + 0] = a;
       if (A.alpha_out) A.alpha_out[e] = a;
     }
   }
@@ -664,16 +716,26 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
 
   // ---- per element: reference state and source phase ------------------------------
   if (tid < nel) {
+    // reference = mean of two opposite corner nodes: the element centre for a
+    // linear state, which makes the deviations (and their FP32 rounding) about
+    // three times smaller in rms than those from a corner
     float hi[NV];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) hi[v] = s_u[tid * NN * NV + v].x;
-    Dv::make_ref(hi, gamma, P.inv_gamma_minus_one, s_ref[tid]);
+    for (int v = 0; v < NV; ++v)
+      hi[v] = 0.5f * (s_u[tid * NN * NV + v].x + s_u[(tid * NN + NN - 1) * NV + v].x);
+    Dv::make_ref(hi, P.eos, s_ref[tid]);
     if (P.source == SRC_CONVERGENCE_TEST) {
-      // sin/cos of pi (x0_e - t) by the angle-difference formula
-      const float2 sc = P.sc0[e0 + tid];
-      const float st = s_scal[2], ct = s_scal[3];
-      s_elem[tid * 4 + 1] = sc.x * ct - sc.y * st;
-      s_elem[tid * 4 + 2] = sc.y * ct + sc.x * st;
+      // sin/cos of pi (x_first - t) in float-float by the angle-difference
+      // formula: sin(a - b) = sa cb - ca sb, cos(a - b) = ca cb + sa sb
+      const float4 a = P.sc0[e0 + tid];
+      const float st = s_scal[2], ct = s_scal[3], stl = s_scal[4], ctl = s_scal[5];
+      const float2 sn = ff_dot2(a.x, a.z, ct, ctl, -a.y, -a.w, st, stl);
+      const float2 cs = ff_dot2(a.y, a.w, ct, ctl, a.x, a.z, st, stl);
+      float* el = s_elem + tid * 8;
+      el[1] = sn.x;
+      el[2] = cs.x;
+      el[3] = sn.y;
+      el[4] = cs.y;
     }
   }
   __syncthreads();
@@ -689,7 +751,7 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
       lo[v] = x.y;
     }
     Node<D> nd;
-    Dv::make_node(hi, lo, s_ref[sl], gamma, nd);
+    Dv::make_node(hi, lo, s_ref[sl], P.eos, nd);
     const int ps = Lay::pos(sl, n - sl * NN);
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
@@ -708,14 +770,14 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
     const int line = r - sl * NF;
     if (sl < nel)
       mixed_line<D, N, VI, VF, SF, EPB>(P, s_ref[sl], s_u, s_fu, s_nd, s_part, s_mat, s_iw,
-                                        VI == VI_HG ? s_elem[sl * 4] : 0.0f, sl, line, dd,
+                                        VI == VI_HG ? s_elem[sl * 8] : 0.0f, sl, line, dd,
                                         e0 + sl, e0, nel);
   }
   __syncthreads();
 
   // ---- nodes: sum of directions, Jacobian, sources, 2N update ---------------------
-  const float bdt = s_scal[0];
-  const float a_s = s_scal[1];
+  const float bdt = s_scal[0], bdt_lo = s_scal[6];
+  const float a_s = s_scal[1], a_lo = s_scal[7];
   bool bad = false;
   for (int n = tid; n < nel * NN; n += NT) {
     const int sl = n / NN;
@@ -732,14 +794,15 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
       du[v] = s * jfac;
     }
     if (P.source == SRC_CONVERGENCE_TEST) {
-      float ph = 0;
-#pragma unroll
-      for (int d = 0; d < D; ++d) ph += P.xoff[(e * D + d) * N + axis_index<N>(node, d)];
-      float sd, cd;
-      sincospif(ph, &sd, &cd);
-      const float s0 = s_elem[sl * 4 + 1], c0 = s_elem[sl * 4 + 2];
+      // phase of this node: element part + node offset, each float-float, so
+      // that the only rounding is the final one (which varies with t instead
+      // of repeating the same pattern every stage)
+      const float4 o = P.scn[node];
+      const float* el = s_elem + sl * 8;
+      const float2 sn = ff_dot2(el[1], el[3], o.y, o.w, el[2], el[4], o.x, o.z);
+      const float2 cs = ff_dot2(el[2], el[4], o.y, o.w, -el[1], -el[3], o.x, o.z);
       float src[NV];
-      SourceMMS<D>::eval(s0 * cd + c0 * sd, c0 * cd - s0 * sd, gamma, src);
+      SourceMMS<D>::eval(sn.x, cs.x, P.eos, src);
 #pragma unroll
       for (int v = 0; v < NV; ++v) du[v] += src[v];
     }
@@ -752,9 +815,9 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       const int k = n * NV + v;
-      const float ut = du[v] - s_tmp[k] * a_s;
+      const float ut = fmaf(-a_lo, s_tmp[k], fmaf(-a_s, s_tmp[k], du[v]));
       s_tmp[k] = ut;
-      const float2 un = ff_add(s_u[k], ut * bdt);
+      const float2 un = ff_add(s_u[k], fmaf(ut, bdt_lo, ut * bdt));
       s_u[k] = un;
       hi[v] = un.x;
       bad |= !(un.x == un.x);
