@@ -263,6 +263,43 @@ int tg_ctx_set_learned_indicator(tg_ctx* ctx, tg_mlp* m, float band);
  * {elements evaluated, band fallbacks, positivity fallbacks}. */
 int tg_mlp_last(tg_mlp* m, float* pred, float* hg, int32_t* flag, uint64_t* counts);
 
+/* ---- Batched ensembles ------------------------------------------------------
+ * Many independent 2D meshes of uneven sizes and polynomial degrees, advanced
+ * together.  No single counterpart in the reference, where each elixir is its
+ * own semidiscretize + solve (semidiscretization.jl:129-151,
+ * methods_2N.jl:95-168); every instance follows exactly that.  All instances
+ * are 2D, polydeg 2..4, TG_PRECISION_MIXED, with the same volume integral
+ * (weak form or flux differencing), fluxes and device.  Each 2N stage of all
+ * instances is one persistent kernel launch over (instance, element block)
+ * work items, and each step of all instances (per-instance clocks included)
+ * is one CUDA graph. */
+typedef struct tg_ensemble tg_ensemble;
+
+/* threads_per_block: 0 (default, 120), 120 or 240 (multiples of 120 fill a
+ * block with whole elements for every polydeg 2..4). */
+int tg_ensemble_create(const tg_config* cfgs, int32_t n, int32_t threads_per_block,
+                       tg_ensemble** out);
+int tg_ensemble_destroy(tg_ensemble* ens);
+int tg_ensemble_size(const tg_ensemble* ens);
+/* Instance i's context, owned by the ensemble: upload, download, integrals,
+ * rhs and the other per-context calls work on it as usual. */
+int tg_ensemble_context(tg_ensemble* ens, int32_t i, tg_ctx** ctx);
+/* tg_step for every instance at once: instance i advances from t[i] (used on
+ * the first step after an upload) with its own StepsizeCallback dt until
+ * t_end or max_steps steps; t[i] and steps[i] (may be NULL) receive each
+ * instance's reached time and step count. */
+int tg_ensemble_step(tg_ensemble* ens, int64_t max_steps, double cfl, double t_end, double* t,
+                     int64_t* steps);
+/* Autotuner: times one stage of all instances for every block size the
+ * ensemble kernel is built for (iters launches each, on the current states,
+ * without changing the solution) and keeps the fastest. */
+int tg_ensemble_autotune(tg_ensemble* ens, int32_t iters, int32_t* threads_per_block,
+                         double* ms_per_stage);
+int tg_ensemble_threads_per_block(const tg_ensemble* ens);
+/* Message of the last failed call on `ens` (ens == NULL: of a failed
+ * tg_ensemble_create on this thread). */
+int tg_ensemble_last_error(const tg_ensemble* ens, char* buf, size_t len);
+
 /* Elements per CUDA block in use (set by tg_config.elements_per_block or the
  * library default for the (ndims, polydeg, precision) combination). */
 int tg_elements_per_block(const tg_ctx* ctx, int32_t* epb);

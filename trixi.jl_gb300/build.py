@@ -40,7 +40,8 @@ def _sources():
 
 
 def _headers():
-    return glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+    return (glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) +
+            glob.glob(os.path.join(INCLUDE, "*.h")))
 
 
 def _compile(src: str, force: bool) -> str:
@@ -49,7 +50,8 @@ def _compile(src: str, force: bool) -> str:
     if not force and os.path.exists(obj) and os.path.getmtime(obj) >= newest:
         return obj
     flags = list(COMMON)
-    if "_mixed_" in os.path.basename(src):
+    name = os.path.basename(src)
+    if "_mixed_" in name or name.startswith("tg_ensemble"):
         flags += FP32_FLAGS
     cmd = [_nvcc()] + ARCH + flags + ["-c", src, "-o", obj]
     res = subprocess.run(cmd, capture_output=True, text=True)

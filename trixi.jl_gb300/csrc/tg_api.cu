@@ -18,6 +18,8 @@
 #include <vector>
 
 #include "../../include/trixi_gb300.h"
+#include "tg_clock.cuh"
+#include "tg_internal.h"
 #include "tg_mixed.cuh"
 
 namespace tg {
@@ -193,24 +195,6 @@ __global__ void clock_init_kernel(Clock* c, double t, double t_end, double cfl, 
   c->steps = 0;
 }
 
-// CarpenterKennedy2N54 stage times c_s (methods_2N.jl:39-44)
-__device__ const double CK_C_DEV[5] = {0.0, 1432997174477.0 / 9575080441755.0,
-                                       2526269341429.0 / 6820363962896.0,
-                                       2006345519317.0 / 3224310063776.0,
-                                       2802321613138.0 / 2924317926251.0};
-
-// sin/cos(pi t_s) of the five stage times, for the mixed kernels' source phase
-__device__ void stage_phases(Clock* c) {
-  for (int s = 0; s < 5; ++s) {
-    double sn, cs;
-    sincospi(c->t + CK_C_DEV[s] * c->dt, &sn, &cs);
-    c->sin_t[s] = (float)sn;
-    c->cos_t[s] = (float)cs;
-    c->sin_tl[s] = (float)(sn - (double)c->sin_t[s]);
-    c->cos_tl[s] = (float)(cs - (double)c->cos_t[s]);
-  }
-}
-
 __global__ void clock_set_kernel(Clock* c, double t, double dt) {
   c->t = t;
   c->dt = dt;
@@ -228,42 +212,9 @@ __global__ void clock_config_kernel(Clock* c, double t_end, double cfl) {
   c->finalstep = 0;
 }
 
-// step! prologue: NaN check and limit_dt! (methods_2N.jl:131-140,
-// time_integration.jl:46-55), then reset of the CFL reduction.
-__global__ void clock_begin_kernel(Clock* c) {
-  c->speed_bits = 1ull;
-  if (c->finished) {
-    c->skip = 1;
-    return;
-  }
-  if (isnan(c->dt)) {
-    c->nan_dt = 1;
-    c->finished = 1;
-    c->skip = 1;
-    return;
-  }
-  c->skip = 0;
-  const double tn = c->t + c->dt;
-  const double te = c->t_end;
-  // Julia isapprox: exact equality, or finite operands within rtol = sqrt(eps)
-  const bool approx = tn == te || (isfinite(tn) && isfinite(te) &&
-                                   fabs(tn - te) <= 1.4901161193847656e-08 * fmax(fabs(tn), fabs(te)));
-  if (tn > te || approx) {
-    c->dt = te - c->t;
-    c->finalstep = 1;
-  }
-  stage_phases(c);
-}
+__global__ void clock_begin_kernel(Clock* c) { clock_begin(c); }
 
-// step! epilogue: t += dt, then StepsizeCallback: dt = cfl * max_dt(u_new).
-__global__ void clock_end_kernel(Clock* c, int n) {
-  if (c->skip) return;
-  c->t += c->dt;
-  c->steps += 1;
-  const double speed = __longlong_as_double((long long)c->speed_bits);
-  c->dt = c->cfl * (2.0 / (n * speed));
-  if (c->finalstep) c->finished = 1;
-}
+__global__ void clock_end_kernel(Clock* c, int n) { clock_end(c, n); }
 
 // Per-element FP64 integrals (integrate_via_indices, analysis_dg2d.jl:313-336):
 // conserved totals, mathematical entropy (compressible_euler_2d.jl:2236-2255)
@@ -372,21 +323,6 @@ __global__ void smooth_alpha_kernel(const R* __restrict__ raw, const int32_t* __
 }  // namespace tg
 
 using namespace tg;
-
-// CarpenterKennedy2N54 (methods_2N.jl:24-48)
-static const double CK_A[5] = {0.0, 567301805773.0 / 1357537059087.0,
-                                2404267990393.0 / 2016746695238.0,
-                                3550918686646.0 / 2091501179385.0,
-                                1275806237668.0 / 842570457699.0};
-static const double CK_B[5] = {1432997174477.0 / 9575080441755.0,
-                               5161836677717.0 / 13612068292357.0,
-                               1720146321549.0 / 2090206949498.0,
-                               3134564353537.0 / 4481467310338.0,
-                               2277821191437.0 / 14882151754819.0};
-static const double CK_C[5] = {0.0, 1432997174477.0 / 9575080441755.0,
-                               2526269341429.0 / 6820363962896.0,
-                               2006345519317.0 / 3224310063776.0,
-                               2802321613138.0 / 2924317926251.0};
 
 struct tg_ctx {
   int D = 0, N = 0, NN = 0, NV = 0, vi = 0, epb = 0, device = 0;
@@ -1061,6 +997,51 @@ int tg_set_time(tg_ctx* c, double t) {
   return TG_OK;
 }
 
+extern "C++" {
+namespace tg {
+int ctx_clock_prepare(tg_ctx* c, double t0, double t_end, double cfl) {
+  if (!c->clock_valid) {
+    // initialize!(StepsizeCallback): dt = cfl * max_dt(u0)
+    int rc = TG_OK;
+    const double* u64 = export_state(c, &rc);
+    if (rc) return rc;
+    rc = reduce_speed(c, u64, &c->d_clock->speed_bits);
+    if (rc) return rc;
+    clock_init_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, t0, t_end, cfl, c->N);
+    CUDA_TRY(c, cudaGetLastError());
+    c->clock_valid = true;
+  } else {
+    clock_config_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, t_end, cfl);
+    CUDA_TRY(c, cudaGetLastError());
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return TG_OK;
+}
+
+int ctx_view(tg_ctx* c, CtxView* v) {
+  if (!c || !v) return TG_ERR_INVALID_ARGUMENT;
+  v->mp = &c->MP;
+  v->u[0] = c->d_u[0];
+  v->u[1] = c->d_u[1];
+  v->cur = c->cur;
+  v->utmp = c->d_utmp;
+  v->clock = c->d_clock;
+  v->status = c->d_status;
+  v->D = c->D;
+  v->N = c->N;
+  v->vi = c->vi;
+  v->fp64 = c->fp64 ? 1 : 0;
+  v->epb = c->epb;
+  v->E = c->E;
+  v->stream = c->stream;
+  v->uploaded = c->uploaded;
+  return TG_OK;
+}
+
+void ctx_set_cur(tg_ctx* c, int cur) { c->cur = cur & 1; }
+}  // namespace tg
+}  // extern "C++"
+
 static int capture_step_graph(tg_ctx* c, int parity) {
   const int saved = c->cur;
   c->cur = parity;
@@ -1093,20 +1074,8 @@ int tg_step(tg_ctx* c, int64_t max_steps, double cfl, double t_end, double* t_in
       int rc = capture_step_graph(c, p);
       if (rc) return rc;
     }
-  if (!c->clock_valid) {
-    // initialize!(StepsizeCallback): dt = cfl * max_dt(u0)
-    int rc = TG_OK;
-    const double* u64 = export_state(c, &rc);
-    if (rc) return rc;
-    rc = reduce_speed(c, u64, &c->d_clock->speed_bits);
-    if (rc) return rc;
-    clock_init_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, *t_inout, t_end, cfl, c->N);
-    CUDA_TRY(c, cudaGetLastError());
-    c->clock_valid = true;
-  } else {
-    clock_config_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, t_end, cfl);
-    CUDA_TRY(c, cudaGetLastError());
-  }
+  int rc = tg::ctx_clock_prepare(c, *t_inout, t_end, cfl);
+  if (rc) return rc;
   Clock h{};
   CUDA_TRY(c, cudaMemcpyAsync(&h, c->d_clock, sizeof(Clock), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));

@@ -1,0 +1,535 @@
+// Batched ensemble: many independent 2D meshes of uneven sizes and polynomial
+// degrees (TreeMesh + DGSEM, mixed precision) advanced together.
+//
+// Each instance is an ordinary mixed-precision context (its own state, 2N
+// register, parameters and clock), so setup, upload, download and analysis
+// work per instance as usual.  Time stepping is shared: one 2N stage of every
+// instance is ONE persistent kernel launch whose blocks walk a list of work
+// items (instance, element block); a block runs the same per-block body as
+// the single-mesh stage kernel (mixed_element_block in tg_mixed.cuh), picked
+// by the instance's polynomial degree.  The kernel is built for block sizes
+// that are multiples of 120 threads, so that every degree 2..4 (2N = 6, 8,
+// 10 element lines per element) fills a block exactly: EPB = NT / (2N)
+// elements per block.  Each instance keeps its own t and dt (its own
+// StepsizeCallback), and a whole step of all instances -- clock prologue, five
+// stage launches, clock epilogue -- is one CUDA graph (two: one per parity of
+// the ping-pong state buffers).  tg_ensemble_autotune times the supported
+// block sizes on the uploaded states and keeps the faster.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/trixi_gb300.h"
+#include "tg_clock.cuh"
+#include "tg_internal.h"
+#include "tg_mixed.cuh"
+
+namespace tg {
+namespace {
+
+struct EnsItem {
+  int32_t inst;  // instance index
+  int32_t n;     // nodes per direction of that instance (3, 4 or 5)
+  int32_t blk;   // element block within the instance
+  int32_t pad;
+};
+
+template <int VI, int NT>
+struct EnsShape {
+  static_assert(NT % 120 == 0, "block size must be a multiple of 120");
+  static constexpr size_t smem() {
+    const size_t a = MixedKernel<2, 3, VI, NT / 6>::smem_bytes();
+    const size_t b = MixedKernel<2, 4, VI, NT / 8>::smem_bytes();
+    const size_t c = MixedKernel<2, 5, VI, NT / 10>::smem_bytes();
+    return a > b ? (a > c ? a : c) : (b > c ? b : c);
+  }
+};
+
+// One 2N stage of every instance (at most 128 registers per thread, so that
+// 480 threads are resident per SM).  params[i] and args[i] are instance i's
+// parameters and stage arguments; a block stages them in shared memory before
+// running a work item (they are read many times by every thread).
+template <int VI, int VF, int SF, int NT>
+__global__ void __launch_bounds__(NT, 480 / NT) ensemble_stage_kernel(const MixedParams* __restrict__ params,
+                                                            const MixedArgs* __restrict__ args,
+                                                            const EnsItem* __restrict__ items,
+                                                            int nitems) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(16) MixedParams sP;
+  __shared__ __align__(16) MixedArgs sA;
+  static_assert(sizeof(MixedParams) % 4 == 0 && sizeof(MixedArgs) % 4 == 0, "word copies");
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const EnsItem w = items[it];
+    {
+      const int* src = reinterpret_cast<const int*>(params + w.inst);
+      int* dst = reinterpret_cast<int*>(&sP);
+      for (int k = threadIdx.x; k < (int)(sizeof(MixedParams) / 4); k += NT) dst[k] = src[k];
+      const int* srca = reinterpret_cast<const int*>(args + w.inst);
+      int* dsta = reinterpret_cast<int*>(&sA);
+      for (int k = threadIdx.x; k < (int)(sizeof(MixedArgs) / 4); k += NT) dsta[k] = srca[k];
+    }
+    __syncthreads();
+    switch (w.n) {
+      case 3: mixed_element_block<2, 3, VI, VF, SF, NT / 6>(sP, sA, w.blk, smem_raw); break;
+      case 4: mixed_element_block<2, 4, VI, VF, SF, NT / 8>(sP, sA, w.blk, smem_raw); break;
+      case 5: mixed_element_block<2, 5, VI, VF, SF, NT / 10>(sP, sA, w.blk, smem_raw); break;
+      default: break;
+    }
+    __syncthreads();  // shared memory is reused by the next item
+  }
+}
+
+__global__ void ens_clock_begin_kernel(Clock* const* clocks, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) clock_begin(clocks[i]);
+}
+
+__global__ void ens_clock_end_kernel(Clock* const* clocks, const int32_t* nnodes, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) clock_end(clocks[i], nnodes[i]);
+}
+
+// Copy every instance's clock into one array (one read-back per poll).
+__global__ void ens_clock_gather_kernel(Clock* const* clocks, int n, Clock* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = *clocks[i];
+}
+
+// Kernel variants: (volume integral, volume flux, surface flux) x block size.
+// KIND -1 dispatches the flux at run time.
+struct Variant {
+  int vi, vf, sf, nt;
+  void (*kern)(const MixedParams*, const MixedArgs*, const EnsItem*, int);
+  size_t smem;
+};
+
+template <int VI, int VF, int SF, int NT>
+Variant make_variant() {
+  return Variant{VI, VF, SF, NT, ensemble_stage_kernel<VI, VF, SF, NT>, EnsShape<VI, NT>::smem()};
+}
+
+const std::vector<Variant>& variants() {
+  static const std::vector<Variant> v = {
+      make_variant<VI_WEAK, -1, FLUX_LLF, 120>(),  make_variant<VI_WEAK, -1, FLUX_LLF, 240>(),
+      make_variant<VI_WEAK, -1, -1, 120>(),        make_variant<VI_WEAK, -1, -1, 240>(),
+      make_variant<VI_FD, -1, -1, 120>(),    make_variant<VI_FD, -1, -1, 240>(),
+  };
+  return v;
+}
+
+}  // namespace
+}  // namespace tg
+
+using namespace tg;
+
+struct tg_ensemble {
+  int n = 0, device = 0, vi = 0, vf = -1, sf = -1;
+  const Variant* var = nullptr;  // chosen kernel (block size var->nt)
+  int grid = 0;                  // persistent grid: resident blocks on all SMs
+  int cur = 0;                   // state buffer holding every instance's state
+  std::vector<tg_ctx*> ctx;
+  std::vector<CtxView> view;
+  cudaStream_t stream = nullptr;
+  MixedParams* d_params = nullptr;  // [n]
+  MixedArgs* d_args = nullptr;      // [2 parities][5 stages][n]
+  EnsItem* d_items = nullptr;
+  int nitems = 0;
+  Clock** d_clocks = nullptr;       // [n] device clocks of the contexts
+  int32_t* d_nnodes = nullptr;      // [n]
+  Clock* d_gather = nullptr;        // [n]
+  std::vector<Clock> h_clock;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  std::string err;
+};
+
+namespace {
+
+int efail(tg_ensemble* s, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (s)
+    s->err = buf;
+  else
+    tg::set_thread_error(buf);
+  return code;
+}
+
+#define ENS_TRY(s, call)                                                                       \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess)                                                                     \
+      return efail((s), TG_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));          \
+  } while (0)
+
+void drop_graphs(tg_ensemble* s) {
+  for (int p = 0; p < 2; ++p)
+    if (s->graph[p]) {
+      cudaGraphExecDestroy(s->graph[p]);
+      s->graph[p] = nullptr;
+    }
+}
+
+// Work items, stage arguments and grid size for the chosen kernel variant.
+int build_schedule(tg_ensemble* s) {
+  const Variant& v = *s->var;
+  std::vector<EnsItem> items;
+  for (int i = 0; i < s->n; ++i) {
+    const int epb = v.nt / (2 * s->view[i].N);
+    const int64_t nb = (s->view[i].E + epb - 1) / epb;
+    for (int64_t b = 0; b < nb; ++b) items.push_back(EnsItem{i, s->view[i].N, (int32_t)b, 0});
+  }
+  s->nitems = (int)items.size();
+  if (s->d_items) cudaFree(s->d_items);
+  s->d_items = nullptr;
+  ENS_TRY(s, cudaMalloc((void**)&s->d_items, sizeof(EnsItem) * items.size()));
+  ENS_TRY(s, cudaMemcpy(s->d_items, items.data(), sizeof(EnsItem) * items.size(),
+                        cudaMemcpyHostToDevice));
+  ENS_TRY(s, cudaFuncSetAttribute(v.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem));
+  int per_sm = 0, sms = 0;
+  ENS_TRY(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.kern, v.nt, v.smem));
+  ENS_TRY(s, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
+  if (per_sm < 1) return efail(s, TG_ERR_UNSUPPORTED, "ensemble kernel does not fit on an SM");
+  s->grid = std::max(1, std::min(per_sm * sms, s->nitems));
+  drop_graphs(s);
+  return TG_OK;
+}
+
+// MixedArgs of every (parity, stage, instance): stage s of parity p reads
+// buffer p ^ (s & 1) and writes the other one.
+int build_args(tg_ensemble* s) {
+  std::vector<MixedArgs> a((size_t)10 * s->n);
+  for (int p = 0; p < 2; ++p)
+    for (int st = 0; st < 5; ++st)
+      for (int i = 0; i < s->n; ++i) {
+        const CtxView& v = s->view[i];
+        MixedArgs& A = a[((size_t)p * 5 + st) * s->n + i];
+        A = MixedArgs{};
+        const int in = p ^ (st & 1);
+        A.u_in = (const float2*)v.u[in];
+        A.u_out = (float2*)v.u[in ^ 1];
+        A.u_tmp = (float*)v.utmp;
+        A.clock = v.clock;
+        A.speed_bits = st == 4 ? &v.clock->speed_bits : nullptr;
+        A.status = v.status;
+        A.a = CK_A[st];
+        A.b = CK_B[st];
+        A.c = CK_C[st];
+        A.mode = MODE_STAGE;
+        A.zero_tmp = st == 0;
+        A.stage = st;
+      }
+  ENS_TRY(s, cudaMemcpy(s->d_args, a.data(), sizeof(MixedArgs) * a.size(), cudaMemcpyHostToDevice));
+  return TG_OK;
+}
+
+int launch_stage(tg_ensemble* s, const MixedArgs* args) {
+  const Variant& v = *s->var;
+  v.kern<<<s->grid, v.nt, v.smem, s->stream>>>(s->d_params, args, s->d_items, s->nitems);
+  ENS_TRY(s, cudaGetLastError());
+  return TG_OK;
+}
+
+int capture(tg_ensemble* s, int p) {
+  cudaGraph_t g = nullptr;
+  ENS_TRY(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeRelaxed));
+  const unsigned cb = (unsigned)((s->n + 63) / 64);
+  ens_clock_begin_kernel<<<cb, 64, 0, s->stream>>>(s->d_clocks, s->n);
+  int rc = TG_OK;
+  for (int st = 0; st < 5 && rc == TG_OK; ++st)
+    rc = launch_stage(s, s->d_args + ((size_t)p * 5 + st) * s->n);
+  if (rc == TG_OK) ens_clock_end_kernel<<<cb, 64, 0, s->stream>>>(s->d_clocks, s->d_nnodes, s->n);
+  cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+  if (rc != TG_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return efail(s, TG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&s->graph[p], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return efail(s, TG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  return TG_OK;
+}
+
+void free_ensemble(tg_ensemble* s) {
+  if (!s) return;
+  cudaSetDevice(s->device);
+  drop_graphs(s);
+  void* ptrs[] = {s->d_params, s->d_args, s->d_items, s->d_clocks, s->d_nnodes, s->d_gather};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  for (tg_ctx* c : s->ctx)
+    if (c) tg_ctx_destroy(c);
+  delete s;
+}
+
+const Variant* find_variant(int vi, int vf, int sf, int nt) {
+  for (const Variant& v : variants())
+    if (v.vi == vi && v.vf == vf && v.sf == sf && v.nt == nt) return &v;
+  return nullptr;
+}
+
+// Every instance's state into buffer s->cur (contexts stepped on their own,
+// or freshly uploaded, may hold it in the other buffer).
+int align_buffers(tg_ensemble* s) {
+  for (int i = 0; i < s->n; ++i) {
+    CtxView& v = s->view[i];
+    tg::ctx_view(s->ctx[i], &v);
+    if (v.cur != s->cur) {
+      ENS_TRY(s, cudaMemcpyAsync(v.u[s->cur], v.u[v.cur], sizeof(float2) * (size_t)v.E *
+                                     (size_t)(v.N * v.N) * 4, cudaMemcpyDeviceToDevice, s->stream));
+      tg::ctx_set_cur(s->ctx[i], s->cur);
+      v.cur = s->cur;
+    }
+  }
+  ENS_TRY(s, cudaStreamSynchronize(s->stream));
+  return TG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tg_ensemble_create(const tg_config* cfgs, int32_t n, int32_t threads_per_block,
+                       tg_ensemble** out) {
+  if (!cfgs || n <= 0 || !out) return efail(nullptr, TG_ERR_INVALID_ARGUMENT, "invalid argument");
+  *out = nullptr;
+  const int nt = threads_per_block == 0 ? 120 : threads_per_block;
+  const tg_config& c0 = cfgs[0];
+  for (int i = 0; i < n; ++i) {
+    const tg_config& c = cfgs[i];
+    if (c.ndims != 2 || c.polydeg < 2 || c.polydeg > 4 || c.precision != TG_PRECISION_MIXED)
+      return efail(nullptr, TG_ERR_UNSUPPORTED,
+                   "ensemble instance %d: needs ndims 2, polydeg 2..4 and mixed precision", i);
+    if (c.volume_integral != c0.volume_integral || c.volume_flux != c0.volume_flux ||
+        c.surface_flux != c0.surface_flux || c.device != c0.device)
+      return efail(nullptr, TG_ERR_UNSUPPORTED,
+                   "ensemble instance %d: all instances need the same solver and device", i);
+  }
+  const int vi = c0.volume_integral;
+  if (vi != TG_VOLUME_WEAK_FORM && vi != TG_VOLUME_FLUX_DIFFERENCING)
+    return efail(nullptr, TG_ERR_UNSUPPORTED, "ensemble: weak form or flux differencing only");
+  int vf = -1, sf = -1;
+  if (vi == TG_VOLUME_WEAK_FORM && c0.surface_flux == TG_FLUX_LAX_FRIEDRICHS) sf = FLUX_LLF;
+  const Variant* var = find_variant(vi == TG_VOLUME_WEAK_FORM ? VI_WEAK : VI_FD, vf, sf, nt);
+  if (!var) return efail(nullptr, TG_ERR_INVALID_ARGUMENT, "threads_per_block must be 0, 120 or 240");
+
+  tg_ensemble* s = new tg_ensemble();
+  s->n = n;
+  s->device = c0.device;
+  s->vi = vi;
+  s->vf = vf;
+  s->sf = sf;
+  s->var = var;
+  s->ctx.assign(n, nullptr);
+  s->view.resize(n);
+  for (int i = 0; i < n; ++i) {
+    const int rc = tg_ctx_create(&cfgs[i], &s->ctx[i]);
+    if (rc) {
+      char msg[512];
+      tg_last_error(nullptr, msg, sizeof(msg));
+      free_ensemble(s);
+      return efail(nullptr, rc, "ensemble instance %d: %s", i, msg);
+    }
+    tg::ctx_view(s->ctx[i], &s->view[i]);
+  }
+  auto fail_free = [&](int rc) {
+    std::string m = s->err;
+    free_ensemble(s);
+    return efail(nullptr, rc, "%s", m.c_str());
+  };
+  if (cudaSetDevice(s->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    s->err = "ensemble: stream creation failed";
+    return fail_free(TG_ERR_CUDA);
+  }
+  std::vector<MixedParams> params(n);
+  std::vector<Clock*> clocks(n);
+  std::vector<int32_t> nn(n);
+  for (int i = 0; i < n; ++i) {
+    params[i] = *s->view[i].mp;
+    clocks[i] = s->view[i].clock;
+    nn[i] = s->view[i].N;
+  }
+  if (cudaMalloc((void**)&s->d_params, sizeof(MixedParams) * n) != cudaSuccess ||
+      cudaMalloc((void**)&s->d_args, sizeof(MixedArgs) * 10 * (size_t)n) != cudaSuccess ||
+      cudaMalloc((void**)&s->d_clocks, sizeof(Clock*) * n) != cudaSuccess ||
+      cudaMalloc((void**)&s->d_nnodes, sizeof(int32_t) * n) != cudaSuccess ||
+      cudaMalloc((void**)&s->d_gather, sizeof(Clock) * n) != cudaSuccess) {
+    s->err = "ensemble: device allocation failed";
+    return fail_free(TG_ERR_CUDA);
+  }
+  cudaMemcpy(s->d_params, params.data(), sizeof(MixedParams) * n, cudaMemcpyHostToDevice);
+  cudaMemcpy(s->d_clocks, clocks.data(), sizeof(Clock*) * n, cudaMemcpyHostToDevice);
+  cudaMemcpy(s->d_nnodes, nn.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice);
+  s->h_clock.resize(n);
+  int rc = build_args(s);
+  if (!rc) rc = build_schedule(s);
+  if (rc) return fail_free(rc);
+  *out = s;
+  return TG_OK;
+}
+
+int tg_ensemble_destroy(tg_ensemble* ens) {
+  free_ensemble(ens);
+  return TG_OK;
+}
+
+int tg_ensemble_size(const tg_ensemble* ens) { return ens ? ens->n : 0; }
+
+int tg_ensemble_context(tg_ensemble* ens, int32_t i, tg_ctx** ctx) {
+  if (!ens || !ctx || i < 0 || i >= ens->n) return TG_ERR_INVALID_ARGUMENT;
+  // the context reads its state from the buffer the ensemble left it in
+  *ctx = ens->ctx[i];
+  return TG_OK;
+}
+
+int tg_ensemble_threads_per_block(const tg_ensemble* ens) { return ens ? ens->var->nt : 0; }
+
+int tg_ensemble_last_error(const tg_ensemble* ens, char* buf, size_t len) {
+  if (!buf || len == 0) return TG_ERR_INVALID_ARGUMENT;
+  if (!ens) return tg_last_error(nullptr, buf, len);
+  snprintf(buf, len, "%s", ens->err.c_str());
+  return TG_OK;
+}
+
+int tg_ensemble_step(tg_ensemble* s, int64_t max_steps, double cfl, double t_end, double* t,
+                     int64_t* steps) {
+  if (!s || !t || max_steps < 0 || !(cfl > 0)) return TG_ERR_INVALID_ARGUMENT;
+  ENS_TRY(s, cudaSetDevice(s->device));
+  for (int i = 0; i < s->n; ++i) {
+    tg::ctx_view(s->ctx[i], &s->view[i]);
+    if (!s->view[i].uploaded) return efail(s, TG_ERR_STATE, "instance %d: no state uploaded", i);
+  }
+  int rc = align_buffers(s);
+  if (rc) return rc;
+  for (int i = 0; i < s->n; ++i) {
+    rc = tg::ctx_clock_prepare(s->ctx[i], t[i], t_end, cfl);
+    if (rc) {
+      char msg[512];
+      tg_last_error(s->ctx[i], msg, sizeof(msg));
+      return efail(s, rc, "instance %d: %s", i, msg);
+    }
+  }
+  for (int p = 0; p < 2; ++p)
+    if (!s->graph[p] && (rc = capture(s, p))) return rc;
+  const unsigned gb = (unsigned)((s->n + 63) / 64);
+  auto read_clocks = [&]() -> int {
+    ens_clock_gather_kernel<<<gb, 64, 0, s->stream>>>(s->d_clocks, s->n, s->d_gather);
+    ENS_TRY(s, cudaMemcpyAsync(s->h_clock.data(), s->d_gather, sizeof(Clock) * s->n,
+                               cudaMemcpyDeviceToHost, s->stream));
+    ENS_TRY(s, cudaStreamSynchronize(s->stream));
+    return TG_OK;
+  };
+  if ((rc = read_clocks())) return rc;
+  std::vector<int64_t> steps0(s->n);
+  for (int i = 0; i < s->n; ++i) steps0[i] = s->h_clock[i].steps;
+  int64_t launched = 0;
+  const int64_t poll = 64;
+  while (launched < max_steps) {
+    const int64_t chunk = std::min(poll, max_steps - launched);
+    for (int64_t k = 0; k < chunk; ++k) {
+      ENS_TRY(s, cudaGraphLaunch(s->graph[s->cur], s->stream));
+      s->cur ^= 1;
+    }
+    launched += chunk;
+    if ((rc = read_clocks())) return rc;
+    bool all = true;
+    for (int i = 0; i < s->n; ++i) all = all && s->h_clock[i].finished;
+    if (all) break;
+  }
+  for (int i = 0; i < s->n; ++i) {
+    tg::ctx_set_cur(s->ctx[i], s->cur);
+    t[i] = s->h_clock[i].t;
+    if (steps) steps[i] = s->h_clock[i].steps - steps0[i];
+  }
+  for (int i = 0; i < s->n; ++i)
+    if (s->h_clock[i].nan_dt) return efail(s, TG_ERR_NUMERICAL, "instance %d: time step size `dt` is NaN", i);
+  return TG_OK;
+}
+
+// Time one stage of every instance for each block size the kernel is built
+// for and keep the fastest.  The timed launches read the current states and
+// write only buffers that are dead between steps (the other state buffer and
+// the 2N register), with their own clock copies, status word and no speed
+// reduction, so the solution is not changed.
+int tg_ensemble_autotune(tg_ensemble* s, int32_t iters, int32_t* threads_per_block,
+                         double* ms_per_stage) {
+  if (!s || iters <= 0) return TG_ERR_INVALID_ARGUMENT;
+  ENS_TRY(s, cudaSetDevice(s->device));
+  int rc = align_buffers(s);
+  if (rc) return rc;
+  Clock* d_clk = nullptr;
+  int32_t* d_st = nullptr;
+  MixedArgs* d_a = nullptr;
+  std::vector<MixedArgs> a(s->n);
+  ENS_TRY(s, cudaMalloc((void**)&d_clk, sizeof(Clock) * s->n));
+  ENS_TRY(s, cudaMemset(d_clk, 0, sizeof(Clock) * s->n));
+  ENS_TRY(s, cudaMalloc((void**)&d_st, sizeof(int32_t)));
+  ENS_TRY(s, cudaMalloc((void**)&d_a, sizeof(MixedArgs) * s->n));
+  for (int i = 0; i < s->n; ++i) {
+    const CtxView& v = s->view[i];
+    MixedArgs& A = a[i];
+    A = MixedArgs{};
+    A.u_in = (const float2*)v.u[s->cur];
+    A.u_out = (float2*)v.u[s->cur ^ 1];
+    A.u_tmp = (float*)v.utmp;
+    A.clock = d_clk + i;  // zeroed: dt = 0, not skipped
+    A.status = d_st;
+    A.a = CK_A[1];
+    A.b = CK_B[1];
+    A.c = CK_C[1];
+    A.mode = MODE_STAGE;
+    A.zero_tmp = 0;
+    A.stage = 1;
+  }
+  cudaMemcpy(d_a, a.data(), sizeof(MixedArgs) * s->n, cudaMemcpyHostToDevice);
+  const Variant* keep = s->var;
+  const Variant* best = nullptr;
+  float best_ms = 0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (const Variant& v : variants()) {
+    if (v.vi != keep->vi || v.vf != keep->vf || v.sf != keep->sf) continue;
+    s->var = &v;
+    if ((rc = build_schedule(s))) break;
+    for (int w = 0; w < 3 && !rc; ++w) rc = launch_stage(s, d_a);
+    cudaEventRecord(e0, s->stream);
+    for (int k = 0; k < iters && !rc; ++k) rc = launch_stage(s, d_a);
+    cudaEventRecord(e1, s->stream);
+    if (rc) break;
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      rc = efail(s, TG_ERR_CUDA, "autotune: stage launch failed");
+      break;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms /= iters;
+    if (!best || ms < best_ms) {
+      best = &v;
+      best_ms = ms;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d_clk);
+  cudaFree(d_st);
+  cudaFree(d_a);
+  s->var = best && !rc ? best : keep;
+  const int rc2 = build_schedule(s);
+  if (rc) return rc;
+  if (rc2) return rc2;
+  if (threads_per_block) *threads_per_block = s->var->nt;
+  if (ms_per_stage) *ms_per_stage = best_ms;
+  return TG_OK;
+}
+
+}  // extern "C"

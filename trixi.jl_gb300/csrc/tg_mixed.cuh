@@ -617,9 +617,14 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
   }
 }
 
+// The work of one block: EPB elements (block index blk) of one mesh.  It is
+// the body of mixed_element_kernel and of the ensemble kernel, which runs it
+// on work items of many meshes (tg_ensemble.cu).  Every thread of the block
+// calls it with the same arguments, blockDim.x == NT, and smem_raw holds
+// MixedKernel::smem_bytes() bytes.
 template <int D, int N, int VI, int VF, int SF, int EPB>
-__global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D, N, VI, EPB>::MINB)
-    mixed_element_kernel(const MixedParams P, const MixedArgs A) {
+__device__ __forceinline__ void mixed_element_block(const MixedParams& P, const MixedArgs& A,
+                                                    int64_t blk, unsigned char* smem_raw) {
   using K = MixedKernel<D, N, VI, EPB>;
   using Lay = NodeLayout<D, N, EPB>;
   using Dv = Dev<D>;
@@ -627,7 +632,6 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
   constexpr int CHUNK = K::CHUNK, NFLD = K::NFLD, FACE = K::FACE;
   constexpr int PP = D + 1;
 
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* s_u = reinterpret_cast<float2*>(smem_raw);
   float2* s_fu = s_u + CHUNK;                               // neighbour traces
   float* s_tmp = reinterpret_cast<float*>(s_fu + FACE);
@@ -643,7 +647,7 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
   float* s_iw = s_mat + N * N;
 
   const int tid = threadIdx.x;
-  const int64_t e0 = (int64_t)blockIdx.x * EPB;
+  const int64_t e0 = blk * EPB;
   const int nel = (int)min((int64_t)EPB, P.nelements - e0);
   const size_t gofs = (size_t)e0 * NN * NV;
   const int nval = nel * NN * NV;
@@ -851,6 +855,13 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
     const float sp = P.inv_jac[e0 + tid] * sum;
     if (sp == sp) atomicMax(A.speed_bits, (unsigned long long)__double_as_longlong((double)sp));
   }
+}
+
+template <int D, int N, int VI, int VF, int SF, int EPB>
+__global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D, N, VI, EPB>::MINB)
+    mixed_element_kernel(const MixedParams P, const MixedArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  mixed_element_block<D, N, VI, VF, SF, EPB>(P, A, blockIdx.x, smem_raw);
 }
 
 }  // namespace tg

@@ -37,3 +37,4 @@ from .solvers import (DGSEM, IndicatorHennemannGassner, VolumeIntegralFluxDiffer
 from .time_integration import (AliveCallback, AnalysisCallback, CallbackSet,  # noqa: F401
                                CarpenterKennedy2N54, StepsizeCallback, SummaryCallback,
                                ode_default_options, solve)
+from .ensemble import Ensemble  # noqa: F401

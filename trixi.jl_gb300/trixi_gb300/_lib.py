@@ -32,7 +32,9 @@ EXPORTS = ("tg_api_version", "tg_ctx_create", "tg_ctx_destroy", "tg_last_error",
            "tg_mlp_create", "tg_mlp_destroy", "tg_mlp_nparams", "tg_mlp_get_params",
            "tg_mlp_set_params", "tg_mlp_harvest", "tg_mlp_dataset", "tg_mlp_train",
            "tg_mlp_gradient", "tg_mlp_predict", "tg_ctx_set_learned_indicator", "tg_mlp_last",
-           "tg_entropy_timederivative")
+           "tg_entropy_timederivative", "tg_ensemble_create", "tg_ensemble_destroy",
+           "tg_ensemble_size", "tg_ensemble_context", "tg_ensemble_step", "tg_ensemble_autotune",
+           "tg_ensemble_threads_per_block", "tg_ensemble_last_error")
 
 
 class TrixiGB300Error(RuntimeError):
@@ -124,6 +126,14 @@ def load(path: str | None = None):
         "tg_ctx_set_learned_indicator": ([vp, vp, ctypes.c_float], ctypes.c_int),
         "tg_mlp_last": ([vp, vp, vp, vp, vp], ctypes.c_int),
         "tg_entropy_timederivative": ([vp, d, pd], ctypes.c_int),
+        "tg_ensemble_create": ([P(tg_config), i32, i32, P(vp)], ctypes.c_int),
+        "tg_ensemble_destroy": ([vp], ctypes.c_int),
+        "tg_ensemble_size": ([vp], ctypes.c_int),
+        "tg_ensemble_context": ([vp, i32, P(vp)], ctypes.c_int),
+        "tg_ensemble_step": ([vp, i64, d, d, pd, P(i64)], ctypes.c_int),
+        "tg_ensemble_autotune": ([vp, i32, P(i32), pd], ctypes.c_int),
+        "tg_ensemble_threads_per_block": ([vp], ctypes.c_int),
+        "tg_ensemble_last_error": ([vp, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

@@ -41,67 +41,79 @@ def _ptr_of(x):
     raise TypeError(f"cannot take the address of {type(x)}")
 
 
+def make_config(semi, precision="fp64", device=0, elements_per_block=0):
+    """tg_config of a semidiscretization, and the arrays it points into (they
+    must stay alive while the config is in use)."""
+    dg, eq = semi.solver, semi.equations
+    vi = dg.volume_integral
+    b = dg.basis
+    # keep every array alive while the config points at it
+    keep = []
+
+    def arr(a, dtype=np.float64):
+        a = np.ascontiguousarray(a, dtype=dtype)
+        keep.append(a)
+        return a
+
+    nb, orient = semi.neighbor_ids, semi.orientations
+    cfg = _lib.tg_config()
+    cfg.ndims = eq.ndims
+    cfg.polydeg = b.polydeg
+    cfg.nelements = semi.nelements
+    cfg.ninterfaces = nb.shape[0]
+    cfg.gamma = eq.gamma
+    cfg.volume_integral = vi.code
+    if isinstance(vi, VolumeIntegralShockCapturingHG):
+        ind = vi.indicator
+        cfg.volume_flux = vi.volume_flux_dg.code
+        cfg.volume_flux_fv = vi.volume_flux_fv.code
+        cfg.alpha_max, cfg.alpha_min = ind.alpha_max, ind.alpha_min
+        cfg.alpha_smooth = int(ind.alpha_smooth)
+    else:
+        cfg.volume_flux = getattr(vi, "volume_flux", None).code if hasattr(vi, "volume_flux") else 0
+        cfg.volume_flux_fv = dg.surface_flux.code
+    cfg.surface_flux = dg.surface_flux.code
+    cfg.source_terms = semi.source_terms.code if semi.source_terms is not None else 0
+    cfg.precision = {"fp64": _lib.TG_PRECISION_FP64, "mixed": _lib.TG_PRECISION_MIXED}[precision]
+    cfg.device = device
+    # Julia column-major matrices: pass the transpose's C buffer
+    cfg.nodes = _dptr(arr(b.nodes))
+    cfg.weights = _dptr(arr(b.weights))
+    cfg.inverse_weights = _dptr(arr(b.inverse_weights))
+    cfg.derivative_hat = _dptr(arr(np.asfortranarray(b.derivative_hat).ravel(order="F")))
+    cfg.derivative_split = _dptr(arr(np.asfortranarray(b.derivative_split).ravel(order="F")))
+    cfg.inverse_vandermonde_legendre = _dptr(
+        arr(np.asfortranarray(b.inverse_vandermonde_legendre).ravel(order="F")))
+    cfg.neighbor_ids = arr(nb, np.int64).ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    cfg.orientations = arr(orient, np.int64).ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    cfg.inverse_jacobian = _dptr(arr(semi.inverse_jacobian))
+    cfg.node_coordinates = _dptr(arr(semi.node_coordinates))
+    cfg.elements_per_block = int(elements_per_block)
+    return cfg, keep
+
+
 class DeviceContext:
     """One tg_ctx: device-resident state, stage buffers and step graphs."""
 
-    def __init__(self, semi, precision="fp64", device=0, elements_per_block=0):
+    def __init__(self, semi, precision="fp64", device=0, elements_per_block=0, _handle=None):
         lib = _lib.load()
         self.lib = lib
         self.semi = semi
-        dg, eq = semi.solver, semi.equations
-        vi = dg.volume_integral
-        b = dg.basis
-        # keep every array alive while the config points at it
-        self._keep = []
-
-        def arr(a, dtype=np.float64):
-            a = np.ascontiguousarray(a, dtype=dtype)
-            self._keep.append(a)
-            return a
-
-        nb, orient = semi.neighbor_ids, semi.orientations
-        cfg = _lib.tg_config()
-        cfg.ndims = eq.ndims
-        cfg.polydeg = b.polydeg
-        cfg.nelements = semi.nelements
-        cfg.ninterfaces = nb.shape[0]
-        cfg.gamma = eq.gamma
-        cfg.volume_integral = vi.code
-        if isinstance(vi, VolumeIntegralShockCapturingHG):
-            ind = vi.indicator
-            cfg.volume_flux = vi.volume_flux_dg.code
-            cfg.volume_flux_fv = vi.volume_flux_fv.code
-            cfg.alpha_max, cfg.alpha_min = ind.alpha_max, ind.alpha_min
-            cfg.alpha_smooth = int(ind.alpha_smooth)
+        self._owned = _handle is None
+        if _handle is None:
+            cfg, self._keep = make_config(semi, precision, device, elements_per_block)
+            h = ctypes.c_void_p()
+            _lib.check(lib.tg_ctx_create(ctypes.byref(cfg), ctypes.byref(h)))
         else:
-            cfg.volume_flux = getattr(vi, "volume_flux", None).code if hasattr(vi, "volume_flux") else 0
-            cfg.volume_flux_fv = dg.surface_flux.code
-        cfg.surface_flux = dg.surface_flux.code
-        cfg.source_terms = semi.source_terms.code if semi.source_terms is not None else 0
-        cfg.precision = {"fp64": _lib.TG_PRECISION_FP64, "mixed": _lib.TG_PRECISION_MIXED}[precision]
-        cfg.device = device
-        # Julia column-major matrices: pass the transpose's C buffer
-        cfg.nodes = _dptr(arr(b.nodes))
-        cfg.weights = _dptr(arr(b.weights))
-        cfg.inverse_weights = _dptr(arr(b.inverse_weights))
-        cfg.derivative_hat = _dptr(arr(np.asfortranarray(b.derivative_hat).ravel(order="F")))
-        cfg.derivative_split = _dptr(arr(np.asfortranarray(b.derivative_split).ravel(order="F")))
-        cfg.inverse_vandermonde_legendre = _dptr(
-            arr(np.asfortranarray(b.inverse_vandermonde_legendre).ravel(order="F")))
-        cfg.neighbor_ids = arr(nb, np.int64).ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
-        cfg.orientations = arr(orient, np.int64).ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
-        cfg.inverse_jacobian = _dptr(arr(semi.inverse_jacobian))
-        cfg.node_coordinates = _dptr(arr(semi.node_coordinates))
-        cfg.elements_per_block = int(elements_per_block)
-        h = ctypes.c_void_p()
-        _lib.check(lib.tg_ctx_create(ctypes.byref(cfg), ctypes.byref(h)))
+            h = ctypes.c_void_p(_handle)
         self.h = h
         self.precision = precision
         self.t = None
 
     def close(self):
         if getattr(self, "h", None):
-            self.lib.tg_ctx_destroy(self.h)
+            if self._owned:
+                self.lib.tg_ctx_destroy(self.h)
             self.h = None
 
     def __del__(self):
