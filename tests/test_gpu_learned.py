@@ -99,3 +99,23 @@ def test_learned_indicator_deployed_with_hg_fallback(trained):
     rho_hg, rho_ml = res["hg"][..., 0], res["ml"][..., 0]
     assert np.sqrt(np.mean((rho_ml - rho_hg) ** 2)) < 1e-3 * np.sqrt(np.mean(rho_hg ** 2))
     ShockIndicatorMLP.undeploy(semi_ml)
+
+
+def test_deployed_predictions_equal_the_inference_kernel(trained):
+    # the one-pass 2D deployment kernel evaluates the same network as predict()
+    net = trained[0]
+    semi, _ = build(KHI, precision="mixed")
+    ctx = semi.device_context
+    ctx.upload(semi.compute_coefficients(0.0))
+    net.deploy(semi, band=0.01)
+    ctx.step(40, 1.0, 10.0, 0.0)
+    ctx.alpha()  # evaluates the indicator on the current state
+    pred, hg, flag, _ = net.last(semi.nelements)
+    n0 = net.count
+    net.harvest(semi)
+    x, y = net.dataset()
+    x = x[n0:]
+    np.testing.assert_array_equal(net.predict(x), pred)
+    sqrt_thr = np.sqrt(0.5 * 10 ** (-1.8 * 4 ** 0.25))
+    np.testing.assert_array_equal(flag == 1, np.abs(pred - sqrt_thr) < 0.01)
+    ShockIndicatorMLP.undeploy(semi)

@@ -94,15 +94,16 @@ struct FeatParams {
   float alpha_min, alpha_max, hg_threshold, hg_parameter_s;
 };
 
+// Modes of rho*p of element e (normalised to unit energy when `normalise`),
+// the HG energy indicator max(f1, f2) and positivity of rho*p at the nodes.
 template <int D, int N, typename TS>
-__global__ void features_kernel(const FeatParams P, const TS* __restrict__ u,
-                                float* __restrict__ feat, float* __restrict__ target,
-                                float* __restrict__ alpha_hg, int32_t* __restrict__ pos_flag) {
+__device__ __forceinline__ void element_modes(const FeatParams& P, const TS* __restrict__ u,
+                                              int64_t e, float* modes, float& energy,
+                                              bool& positive) {
   constexpr int NV = D + 2, NN = Pow<N, D>::value;
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= P.E) return;
   float a[NN], b[NN];
-  bool positive = true;
+  positive = true;
+#pragma unroll
   for (int q = 0; q < NN; ++q) {
     float uu[NV];
 #pragma unroll
@@ -142,14 +143,34 @@ __global__ void features_kernel(const FeatParams P, const TS* __restrict__ u,
   }
   const float f1 = tot != 0.0f ? (tot - clip1) / tot : 0.0f;
   const float f2 = clip1 != 0.0f ? (clip1 - clip2) / clip1 : 0.0f;
-  const float energy = fmaxf(f1, f2);
-  float al = 1.0f / (1.0f + expf(-P.hg_parameter_s / P.hg_threshold * (energy - P.hg_threshold)));
-  if (al < P.alpha_min) al = 0.0f;
-  if (al > 1.0f - P.alpha_min) al = 1.0f;
-  alpha_hg[e] = fminf(P.alpha_max, al);
+  energy = fmaxf(f1, f2);
   const float inv = tot > 0.0f ? rsqrtf(tot) : 0.0f;
 #pragma unroll
-  for (int q = 0; q < NN; ++q) feat[(size_t)e * NN + q] = in[q] * inv;
+  for (int q = 0; q < NN; ++q) modes[q] = in[q] * inv;
+}
+
+// HG logistic of an energy indicator, clipped (indicators_2d.jl:92-100)
+__device__ __forceinline__ float hg_logistic(float energy, float thr, float s_par, float alpha_min,
+                                             float alpha_max) {
+  float al = 1.0f / (1.0f + expf(-s_par / thr * (energy - thr)));
+  if (al < alpha_min) al = 0.0f;
+  if (al > 1.0f - alpha_min) al = 1.0f;
+  return fminf(alpha_max, al);
+}
+
+template <int D, int N, typename TS>
+__global__ void features_kernel(const FeatParams P, const TS* __restrict__ u,
+                                float* __restrict__ feat, float* __restrict__ target,
+                                float* __restrict__ alpha_hg, int32_t* __restrict__ pos_flag) {
+  constexpr int NN = Pow<N, D>::value;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.E) return;
+  float m[NN], energy;
+  bool positive;
+  element_modes<D, N, TS>(P, u, e, m, energy, positive);
+  alpha_hg[e] = hg_logistic(energy, P.hg_threshold, P.hg_parameter_s, P.alpha_min, P.alpha_max);
+#pragma unroll
+  for (int q = 0; q < NN; ++q) feat[(size_t)e * NN + q] = m[q];
   if (target) target[e] = sqrtf(fmaxf(energy, 0.0f));
   pos_flag[e] = positive ? 0 : 2;
 }
@@ -210,6 +231,67 @@ __global__ void learned_alpha_kernel(const float* __restrict__ pred, const float
   if (f == 1) atomicAdd(&stats[1], 1ull);
   if (f == 2) atomicAdd(&stats[2], 1ull);
   if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&stats[0], (unsigned long long)E);
+}
+
+// Deployment path of the 2D networks (H = 64): modes, HG fallback value,
+// network and blending factor of each element in one pass, one thread per
+// element and nothing but alpha (and the per-element report) written.  A
+// block stages the weights once in shared memory as FP32 copies of the BF16
+// values, keeps the first hidden layer in registers and walks element tiles;
+// products and sums are the FP32 operations of mlp_infer_kernel in the same
+// order, so the predictions are the same bits.
+struct AlphaParams {
+  float sqrt_thr, band, thr, s_par, alpha_min, alpha_max;
+};
+
+template <int N, typename TS, typename R>
+__global__ void __launch_bounds__(128) learned_alpha2d_kernel(
+    const FeatParams P, const TS* __restrict__ u, const __nv_bfloat16* __restrict__ w,
+    const AlphaParams A, R* __restrict__ alpha_raw, float* __restrict__ pred_out,
+    float* __restrict__ hg_out, int32_t* __restrict__ flag_out,
+    unsigned long long* __restrict__ stats) {
+  constexpr int NM = N * N, H = 64;
+  const MlpLayout L{NM, H};
+  extern __shared__ float sw[];
+  for (int k = threadIdx.x; k < L.count(); k += blockDim.x) sw[k] = __bfloat162float(w[k]);
+  __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[0], (unsigned long long)P.E);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < P.E;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    float xv[NM], energy;
+    bool positive;
+    element_modes<2, N, TS>(P, u, e, xv, energy, positive);
+    float h1[H];
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+      float z = sw[L.b1() + i];
+#pragma unroll
+      for (int k = 0; k < NM; ++k) z = fmaf(sw[L.w1() + i * NM + k], xv[k], z);
+      h1[i] = fmaxf(z, 0.0f);
+    }
+    float out = sw[L.b3()];
+#pragma unroll 1
+    for (int i = 0; i < H; ++i) {
+      float z = sw[L.b2() + i];
+#pragma unroll
+      for (int j = 0; j < H; ++j) z = fmaf(sw[L.w2() + i * H + j], h1[j], z);
+      out = fmaf(sw[L.w3() + i], fmaxf(z, 0.0f), out);
+    }
+    const float hg = hg_logistic(energy, A.thr, A.s_par, 0.0f, 1.0f);
+    int f = positive ? 0 : 2;
+    if (f == 0 && !(fabsf(out - A.sqrt_thr) >= A.band)) f = 1;  // also catches NaN
+    const float ep = fmaxf(out, 0.0f);
+    float a = f != 0 ? hg : 1.0f / (1.0f + expf(-A.s_par / A.thr * (ep * ep - A.thr)));
+    if (a < A.alpha_min) a = 0.0f;
+    if (a > 1.0f - A.alpha_min) a = 1.0f;
+    a = fminf(A.alpha_max, a);
+    alpha_raw[e] = (R)a;
+    pred_out[e] = out;
+    hg_out[e] = hg;
+    flag_out[e] = f;
+    if (f == 1) atomicAdd(&stats[1], 1ull);
+    if (f == 2) atomicAdd(&stats[2], 1ull);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -426,6 +508,51 @@ static int launch_infer(tg_mlp* m, const float* x, int64_t M, float* pred, cudaS
 }
 
 namespace tg {
+// One-pass deployment of the 2D networks (learned_alpha2d_kernel).
+static int fused_alpha2d(tg_mlp* m, tg_ctx* c, void* alpha_raw, bool fp64, float alpha_min,
+                         float alpha_max) {
+  const void* state;
+  int ff, D, N;
+  int64_t E;
+  double gamma;
+  const double* vinv;
+  void* stream;
+  int rc = ctx_state_view(c, &state, &ff, &D, &N, &E, &gamma, &vinv, &stream);
+  if (rc) return rc;
+  if (D != m->D || N != m->N) return mfail(m, TG_ERR_INVALID_ARGUMENT, "network/context shape mismatch");
+  if (E > m->ecap) return mfail(m, TG_ERR_STATE, "context larger than prepared");
+  FeatParams P{};
+  P.E = E;
+  P.gamma = gamma;
+  for (int k = 0; k < N * N; ++k) P.Vinv[k] = (float)vinv[k];
+  AlphaParams A{};
+  A.thr = (float)(0.5 * std::pow(10.0, -1.8 * std::pow((double)N, 0.25)));
+  A.s_par = (float)std::log((1 - 0.0001) / 0.0001);
+  A.sqrt_thr = (float)m->sqrt_threshold;
+  A.band = m->band;
+  A.alpha_min = alpha_min;
+  A.alpha_max = alpha_max;
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned nb = (unsigned)std::min<int64_t>((E + 127) / 128, 152 * 8);
+  const size_t smem = sizeof(float) * MlpLayout{m->NM, m->H}.count();
+#define FUSED(NN)                                                                              \
+  if (N == NN) {                                                                               \
+    if (ff)                                                                                    \
+      learned_alpha2d_kernel<NN, float2, float><<<nb, 128, smem, s>>>(                         \
+          P, (const float2*)state, m->d_wb, A, (float*)alpha_raw, m->d_pred, m->d_hg,          \
+          m->d_flag, m->d_stats);                                                              \
+    else                                                                                       \
+      learned_alpha2d_kernel<NN, double, double><<<nb, 128, smem, s>>>(                        \
+          P, (const double*)state, m->d_wb, A, (double*)alpha_raw, m->d_pred, m->d_hg,         \
+          m->d_flag, m->d_stats);                                                              \
+  }
+  FUSED(3) else FUSED(4) else FUSED(5) else return mfail(m, TG_ERR_UNSUPPORTED, "polydeg");
+#undef FUSED
+  (void)fp64;
+  MCUDA(m, cudaGetLastError());
+  return TG_OK;
+}
+
 // Called by the context before every stage when the learned indicator is on:
 // writes the blending factors (unsmoothed) into alpha_raw (R = float or double).
 int mlp_alpha(tg_mlp* m, tg_ctx* c, void* alpha_raw, bool fp64, float alpha_min,
@@ -433,6 +560,7 @@ int mlp_alpha(tg_mlp* m, tg_ctx* c, void* alpha_raw, bool fp64, float alpha_min,
   cudaStream_t s;
   int64_t E;
   if (m->ecap == 0) return mfail(m, TG_ERR_STATE, "learned indicator not prepared for this context");
+  if (m->D == 2 && m->H == 64) return fused_alpha2d(m, c, alpha_raw, fp64, alpha_min, alpha_max);
   int rc = launch_features(m, c, m->d_feat, nullptr, m->d_hg, m->d_flag, &s, &E);
   if (rc) return rc;
   if (E > m->ecap) return mfail(m, TG_ERR_STATE, "context larger than prepared");

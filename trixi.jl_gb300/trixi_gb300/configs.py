@@ -1,0 +1,366 @@
+"""Runs of the benchmark configurations on the GB300 path, FP64 beside mixed.
+
+    python -m trixi_gb300.configs --only c1,c3 --out results.json
+
+  c1   2D isentropic vortex, 16^2 elements, polydeg 3, weak form, LLF, CFL 1, t = 20
+       (examples/tree_2d_dgsem/elixir_euler_vortex.jl with p = 1): L2/Linf against
+       the exact solution (the vortex is back at its start at t = 20).
+  c3   2D Kelvin-Helmholtz instability, 256^2, polydeg 3, HG shock capturing on
+       rho*p (alpha_max 0.002, alpha_min 1e-4), flux_ranocha / LLF, CFL 1.3,
+       t = 3 (elixir_euler_kelvin_helmholtz_instability.jl): density error of
+       FP64 and mixed against a 512^2 run, sampled on a uniform grid.
+  c4   learned indicator: pairs harvested every 10 steps from the c3 run and a
+       Gaussian blast (128^2), trained on the GPU, deployed at 512^2 with HG as
+       fallback; alpha MAE, fallbacks, positivity and the L2 density
+       difference to the plain-HG run, throughput against FP64 + HG.
+  c5a  64 uneven vortices (8^2..128^2, polydeg 2..4, eps ~ U[1, 5], seed
+       20261204) in one ensemble to t = 20, against FP64 instance by instance.
+  c5b  3D Taylor-Green vortex, Ma 0.1, polydeg 3, flux_ranocha volume flux,
+       naive LLF, CFL 1.4 (elixir_euler_taylor_green_vortex.jl): kinetic
+       energy history of mixed against FP64 (32^3 to t = 20; 64^3 mixed to
+       t = 20 and FP64 to t = 2).
+
+The 3D manufactured solution at 32^3 is the headline case of bench.py.
+Throughput is DOF-updates per second per RK stage (ndofs x 5 stages x steps /
+seconds), with the device synchronised around each timed call.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import time
+
+import numpy as np
+
+import trixi_gb300 as T
+from .learned import ShockIndicatorMLP
+
+
+# ---------------------------------------------------------------------------
+# helpers
+def solve_timed(semi, t_end, cfl, max_steps=10 ** 9, u0=None):
+    c = semi.device_context
+    c.upload(semi.compute_coefficients(0.0) if u0 is None else u0)
+    c.synchronize()
+    t0 = time.perf_counter()
+    t, n = c.step(max_steps, cfl, t_end, 0.0)
+    c.synchronize()
+    secs = time.perf_counter() - t0
+    return c.download(), t, n, secs
+
+
+def rate(ndofs, steps, secs):
+    return float(ndofs) * 5 * steps / secs if secs > 0 else float("nan")
+
+
+def lagrange(nodes, x):
+    """Lagrange basis of `nodes` at points x: (len(x), n)."""
+    n = len(nodes)
+    out = np.ones((len(x), n))
+    for i in range(n):
+        for k in range(n):
+            if k != i:
+                out[:, i] *= (x - nodes[k]) / (nodes[i] - nodes[k])
+    return out
+
+
+def sample2d(semi, u, npts, var=0, chunk=1 << 17):
+    """Values of variable `var` of a 2D DG solution at the centres of an
+    npts x npts grid over the domain (row-major in y)."""
+    xc = semi.node_coordinates  # (E, j, i, 2)
+    lo = xc.reshape(-1, 2).min(axis=0)
+    hi = xc.reshape(-1, 2).max(axis=0)
+    cen = xc.mean(axis=(1, 2))
+    dx = (hi - lo) / np.round((hi - lo) / (xc[0, 0, -1, 0] - xc[0, 0, 0, 0]))
+    nel = np.round((hi - lo) / dx).astype(int)
+    ij = np.floor((cen - lo) / dx).astype(int)
+    lookup = np.empty((nel[1], nel[0]), dtype=np.int64)
+    lookup[ij[:, 1], ij[:, 0]] = np.arange(len(cen))
+    nodes = np.asarray(semi.solver.basis.nodes)
+    g = lo[None, :] + (np.arange(npts)[:, None] + 0.5) * (hi - lo)[None, :] / npts
+    X, Y = np.meshgrid(g[:, 0], g[:, 1])
+    P = np.stack([X.ravel(), Y.ravel()], axis=1)
+    out = np.empty(len(P))
+    for s in range(0, len(P), chunk):
+        p = P[s:s + chunk]
+        k = np.clip(np.floor((p - lo) / dx).astype(int), 0, nel - 1)
+        e = lookup[k[:, 1], k[:, 0]]
+        loc = 2 * (p - (lo + k * dx)) / dx - 1
+        lx, ly = lagrange(nodes, loc[:, 0]), lagrange(nodes, loc[:, 1])
+        out[s:s + chunk] = np.einsum("mji,mi,mj->m", u[e, :, :, var], lx, ly)
+    return out
+
+
+def vortex_semi(level, polydeg, eps, precision, surface_flux=None):
+    eq = T.CompressibleEulerEquations2D(1.4)
+    solver = T.DGSEM(polydeg=polydeg, surface_flux=surface_flux or T.flux_lax_friedrichs,
+                     volume_integral=T.VolumeIntegralWeakForm())
+    mesh = T.TreeMesh((-10.0, -10.0), (10.0, 10.0), initial_refinement_level=level)
+    ic = T.initial_condition_isentropic_vortex(1.0, eps)
+    return T.SemidiscretizationHyperbolic(mesh, eq, ic, solver, precision=precision)
+
+
+def khi_semi(level, precision):
+    eq = T.CompressibleEulerEquations2D(1.4)
+    basis = T.LobattoLegendreBasis(3)
+    ind = T.IndicatorHennemannGassner(eq, basis, alpha_max=0.002, alpha_min=0.0001,
+                                      alpha_smooth=True, variable=T.density_pressure)
+    vi = T.VolumeIntegralShockCapturingHG(ind, volume_flux_dg=T.flux_ranocha,
+                                          volume_flux_fv=T.flux_lax_friedrichs)
+    solver = T.DGSEM(basis, T.flux_lax_friedrichs, vi)
+    mesh = T.TreeMesh((-1.0, -1.0), (1.0, 1.0), initial_refinement_level=level)
+    return T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_kelvin_helmholtz_instability,
+                                          solver, precision=precision)
+
+
+def blast_semi(level, precision):
+    eq = T.CompressibleEulerEquations2D(1.4)
+    basis = T.LobattoLegendreBasis(3)
+    ind = T.IndicatorHennemannGassner(eq, basis, alpha_max=0.5, alpha_min=0.001,
+                                      alpha_smooth=True, variable=T.density_pressure)
+    vi = T.VolumeIntegralShockCapturingHG(ind, volume_flux_dg=T.flux_ranocha,
+                                          volume_flux_fv=T.flux_lax_friedrichs)
+    solver = T.DGSEM(basis, T.flux_lax_friedrichs, vi)
+    mesh = T.TreeMesh((-1.5, -1.5), (1.5, 1.5), initial_refinement_level=level)
+    ic = T.initial_condition_gaussian_blast(1e-5, 1.0, 0.25)
+    return T.SemidiscretizationHyperbolic(mesh, eq, ic, solver, precision=precision)
+
+
+def tgv_semi(level, precision):
+    eq = T.CompressibleEulerEquations3D(1.4)
+    solver = T.DGSEM(polydeg=3, surface_flux=T.FluxLaxFriedrichs(T.max_abs_speed_naive),
+                     volume_integral=T.VolumeIntegralFluxDifferencing(T.flux_ranocha))
+    mesh = T.TreeMesh((-math.pi,) * 3, (math.pi,) * 3, initial_refinement_level=level)
+    return T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_taylor_green_vortex(0.1),
+                                          solver, precision=precision)
+
+
+# ---------------------------------------------------------------------------
+def c1():
+    out = {}
+    for prec in ("fp64", "mixed"):
+        semi = vortex_semi(4, 3, 5.0, prec)
+        u, t, n, secs = solve_timed(semi, 20.0, 1.0)
+        l2, linf = T.calc_error_norms(u, t, semi)
+        out[prec] = dict(l2=l2.tolist(), linf=linf.tolist(), t=t, steps=n, secs=secs,
+                         rate=rate(semi.ndofs, n, secs))
+    out["l2_rho_ratio"] = out["mixed"]["l2"][0] / out["fp64"]["l2"][0]
+    out["linf_rho_ratio"] = out["mixed"]["linf"][0] / out["fp64"]["linf"][0]
+    out["speedup"] = out["mixed"]["rate"] / out["fp64"]["rate"]
+    return out
+
+
+def c3(npts=1024):
+    out = {}
+    sol = {}
+    for prec, level in (("fp64", 8), ("mixed", 8), ("mixed_512", 9)):
+        semi = khi_semi(level, "mixed" if prec == "mixed_512" else prec)
+        u, t, n, secs = solve_timed(semi, 3.0, 1.3)
+        sol[prec] = sample2d(semi, u, npts)
+        out[prec] = dict(t=t, steps=n, secs=secs, rate=rate(semi.ndofs, n, secs))
+        del semi
+    truth = sol["mixed_512"]
+
+    def rms(a):
+        return float(np.sqrt(np.mean(a * a)))
+
+    for prec in ("fp64", "mixed"):
+        out[prec]["l2_rho_vs_512"] = rms(sol[prec] - truth)
+        out[prec]["linf_rho_vs_512"] = float(np.max(np.abs(sol[prec] - truth)))
+    out["l2_rho_ratio"] = out["mixed"]["l2_rho_vs_512"] / out["fp64"]["l2_rho_vs_512"]
+    out["l2_rho_mixed_vs_fp64"] = rms(sol["mixed"] - sol["fp64"])
+    out["speedup"] = out["mixed"]["rate"] / out["fp64"]["rate"]
+    out["sample_grid"] = npts
+    return out
+
+
+def _clip_alpha(a, alpha_min, alpha_max):
+    a = np.where(a < alpha_min, 0.0, a)
+    a = np.where(a > 1 - alpha_min, 1.0, a)
+    return np.minimum(alpha_max, a)
+
+
+def c4(harvest_every=10, train_steps=4000, deploy_level=9, fp64_steps=200):
+    """Learned indicator: harvest, train, deploy against HG."""
+    out = {}
+    net = ShockIndicatorMLP(2, 3, seed=3)
+    t_start = time.perf_counter()
+    for name, semi, t_end, stride in (("khi_256", khi_semi(8, "mixed"), 3.0, 32),
+                                      ("blast_128", blast_semi(7, "mixed"), 0.3, 4)):
+        c = semi.device_context
+        c.upload(semi.compute_coefficients(0.0))
+        t, steps, k = 0.0, 0, 0
+        cfl = 1.3 if name.startswith("khi") else 1.0
+        while True:
+            t, n = c.step(harvest_every, cfl, t_end, t)
+            steps += n
+            net.harvest(semi, stride=stride, phase=k % stride)
+            k += 1
+            if n < harvest_every or t >= t_end:
+                break
+        out[f"harvest_{name}"] = dict(t=t, steps=steps, pairs_total=net.count, stride=stride)
+        del semi
+    out["harvest_secs"] = time.perf_counter() - t_start
+    t0 = time.perf_counter()
+    first = net.train(50, batch=4096, lr=2e-3)
+    last = net.train(train_steps, batch=4096, lr=2e-3)
+    out["train"] = dict(pairs=net.count, steps=train_steps + 50, loss_first=first, loss_last=last,
+                        secs=time.perf_counter() - t0)
+    x, y = net.dataset()
+    held = np.arange(len(y)) % 10 == 0
+    pred = net.predict(x[held])
+    out["train"]["heldout_mae_sqrtE"] = float(np.mean(np.abs(pred - y[held])))
+    out["train"]["heldout_mae_const"] = float(np.mean(np.abs(np.median(y[~held]) - y[held])))
+    del x, y
+
+    # deployment at 512^2: mixed + learned vs mixed + HG (same states), FP64 + HG throughput
+    thr = 0.5 * 10 ** (-1.8 * 4 ** 0.25)
+    s_par = math.log((1 - 0.0001) / 0.0001)
+    res = {}
+    mae = []
+    for name in ("hg", "learned"):
+        semi = khi_semi(deploy_level, "mixed")
+        c = semi.device_context
+        c.upload(semi.compute_coefficients(0.0))
+        if name == "learned":
+            net.deploy(semi, band=0.01)
+        c.synchronize()
+        t, steps, secs = 0.0, 0, 0.0
+        for t_stop in (0.5, 1.0, 1.5, 2.0, 2.5, 3.0):
+            t0 = time.perf_counter()
+            t, n = c.step(10 ** 9, 1.3, t_stop, t)
+            c.synchronize()
+            secs += time.perf_counter() - t0
+            steps += n
+            if name == "learned":
+                p, hg, flag, counts = net.last(semi.nelements)
+                a_net = _clip_alpha(1 / (1 + np.exp(-s_par / thr * (np.maximum(p, 0) ** 2 - thr))),
+                                    0.0001, 0.002)
+                a_hg = _clip_alpha(hg, 0.0001, 0.002)
+                a_used = np.where(flag != 0, a_hg, a_net)
+                mae.append(dict(t=t, mae_used=float(np.mean(np.abs(a_used - a_hg))),
+                                mae_network=float(np.mean(np.abs(a_net - a_hg))),
+                                fallback_fraction=float(np.mean(flag != 0)),
+                                active_hg=float(np.mean(a_hg > 0))))
+        res[name] = c.download()
+        out[f"deploy_{name}"] = dict(t=t, steps=steps, secs=secs, rate=rate(semi.ndofs, steps, secs),
+                                     status=c.status())
+        if name == "learned":
+            _, _, _, counts = net.last(semi.nelements)
+            out["deploy_learned"]["evaluated"] = int(counts[0])
+            out["deploy_learned"]["band_fallbacks"] = int(counts[1])
+            out["deploy_learned"]["positivity_fallbacks"] = int(counts[2])
+            ShockIndicatorMLP.undeploy(semi)
+        del semi
+    out["alpha_mae"] = mae
+    rho_hg, rho_ml = res["hg"][..., 0], res["learned"][..., 0]
+    out["l2_rho_learned_vs_hg"] = float(np.sqrt(np.mean((rho_ml - rho_hg) ** 2)))
+    out["l2_rho_learned_vs_hg_rel"] = out["l2_rho_learned_vs_hg"] / float(np.sqrt(np.mean(rho_hg ** 2)))
+    semi = khi_semi(deploy_level, "fp64")
+    _, t, n, secs = solve_timed(semi, 10.0, 1.3, max_steps=fp64_steps)
+    out["fp64_hg"] = dict(steps=n, secs=secs, rate=rate(semi.ndofs, n, secs))
+    out["speedup_learned_vs_fp64"] = out["deploy_learned"]["rate"] / out["fp64_hg"]["rate"]
+    out["speedup_hg_mixed_vs_fp64"] = out["deploy_hg"]["rate"] / out["fp64_hg"]["rate"]
+    return out
+
+
+def c5a(n=64, seed=20261204, t_end=20.0):
+    rng = np.random.default_rng(seed)
+    specs = [(int(rng.integers(3, 8)), int(rng.integers(2, 5)), float(rng.uniform(1.0, 5.0)))
+             for _ in range(n)]
+    out = dict(specs=specs)
+    semis = [vortex_semi(lv, p, eps, "mixed") for lv, p, eps in specs]
+    ens = T.Ensemble(semis)
+    ens.upload_initial()
+    tpb, ms = ens.autotune(iters=20)
+    out["autotune"] = dict(threads_per_block=tpb, ms_per_stage=ms)
+    t0 = time.perf_counter()
+    t, steps = ens.step(10 ** 9, 1.0, t_end)
+    secs = time.perf_counter() - t0
+    dof_updates = sum(s.ndofs * 5 * int(k) for s, k in zip(semis, steps))
+    out["ensemble"] = dict(secs=secs, rate=dof_updates / secs, steps=steps.tolist(),
+                           ndofs=sum(s.ndofs for s in semis))
+    l2m = [T.calc_error_norms(ens.download(i), t[i], s)[0][0] for i, s in enumerate(semis)]
+    ens.close()
+    del ens
+    # one context at a time: mixed and FP64
+    for prec in ("mixed", "fp64"):
+        secs, upd, l2 = 0.0, 0, []
+        for lv, p, eps in specs:
+            semi = vortex_semi(lv, p, eps, prec)
+            u, tt, k, s = solve_timed(semi, t_end, 1.0)
+            secs += s
+            upd += semi.ndofs * 5 * k
+            l2.append(T.calc_error_norms(u, tt, semi)[0][0])
+            del semi
+        out[f"sequential_{prec}"] = dict(secs=secs, rate=upd / secs)
+        if prec == "fp64":
+            l2f = l2
+    ratio = np.asarray(l2m) / np.asarray(l2f)
+    out["l2_rho_mixed"] = [float(v) for v in l2m]
+    out["l2_rho_fp64"] = [float(v) for v in l2f]
+    out["l2_rho_ratio_max"] = float(ratio.max())
+    out["l2_rho_ratio_median"] = float(np.median(ratio))
+    out["speedup_vs_fp64"] = out["ensemble"]["rate"] / out["sequential_fp64"]["rate"]
+    out["speedup_vs_sequential_mixed"] = out["ensemble"]["rate"] / out["sequential_mixed"]["rate"]
+    return out
+
+
+def _ke_history(semi, t_end, dt_out, cfl=1.4):
+    c = semi.device_context
+    c.upload(semi.compute_coefficients(0.0))
+    hist = [(0.0, float(c.integrals()[-1]))]
+    t, steps, secs = 0.0, 0, 0.0
+    while t < t_end:
+        t0 = time.perf_counter()
+        t, n = c.step(10 ** 9, cfl, min(t_end, t + dt_out), t)
+        c.synchronize()
+        secs += time.perf_counter() - t0
+        steps += n
+        hist.append((t, float(c.integrals()[-1])))
+    return hist, steps, secs
+
+
+def c5b(levels=((5, 20.0, 20.0), (6, 20.0, 2.0)), dt_out=0.25):
+    """levels: (refinement level, mixed t_end, FP64 t_end)."""
+    out = {}
+    for level, t_mixed, t_fp64 in levels:
+        r = {}
+        for prec, t_end in (("mixed", t_mixed), ("fp64", t_fp64)):
+            semi = tgv_semi(level, prec)
+            hist, steps, secs = _ke_history(semi, t_end, dt_out)
+            r[prec] = dict(ke=hist, steps=steps, secs=secs, rate=rate(semi.ndofs, steps, secs))
+            del semi
+        km = {round(t, 9): k for t, k in r["mixed"]["ke"]}
+        diffs = [abs(km[round(t, 9)] - k) / k for t, k in r["fp64"]["ke"] if round(t, 9) in km]
+        r["ke_rel_diff_max"] = float(max(diffs))
+        r["ke_rel_diff_final_common"] = float(diffs[-1])
+        r["speedup"] = r["mixed"]["rate"] / r["fp64"]["rate"]
+        out[f"{2 ** level}^3"] = r
+    return out
+
+
+RUNS = dict(c1=c1, c3=c3, c4=c4, c5a=c5a, c5b=c5b)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--only", default=",".join(RUNS), help="comma-separated subset of " + ",".join(RUNS))
+    ap.add_argument("--out", default=None, help="write the results as JSON here")
+    args = ap.parse_args(argv)
+    results = {}
+    for name in args.only.split(","):
+        t0 = time.perf_counter()
+        results[name] = RUNS[name]()
+        results[name]["wall_secs"] = time.perf_counter() - t0
+        brief = {k: v for k, v in results[name].items() if not isinstance(v, (list, dict))}
+        print(name, json.dumps(brief), flush=True)
+        if args.out:
+            with open(args.out, "w") as f:
+                json.dump(results, f, indent=1)
+    return results
+
+
+if __name__ == "__main__":
+    main()
