@@ -303,6 +303,11 @@ int tg_ensemble_last_error(const tg_ensemble* ens, char* buf, size_t len);
 /* Elements per CUDA block in use (set by tg_config.elements_per_block or the
  * library default for the (ndims, polydeg, precision) combination). */
 int tg_elements_per_block(const tg_ctx* ctx, int32_t* epb);
+/* Autotuner: times one 2N stage (iters launches each) for every elements-per-
+ * block value the element kernel is built with for this (ndims, polydeg) on
+ * the uploaded state, without changing the solution, and keeps the fastest
+ * for the following stages (best_epb, ms_per_stage may be NULL). */
+int tg_ctx_autotune(tg_ctx* ctx, int32_t iters, int32_t* best_epb, double* ms_per_stage);
 
 #ifdef __cplusplus
 }

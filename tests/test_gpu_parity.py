@@ -250,3 +250,21 @@ def test_entropy_conservative_scheme_produces_no_entropy(ndims, precision, tol):
     ds_llf = semi_llf.device_context.entropy_timederivative(0.0)
     assert ds_llf < 0
     assert abs(ds) <= tol * abs(ds_llf), (ds, ds_llf)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_autotune_keeps_state_and_steps_like_a_fixed_choice(precision):
+    c = RHS_CASES[6]  # 3D, polydeg 3: kernels built for 2, 4 and 8 elements per block
+    semi, _ = build(c, precision=precision)
+    ctx = semi.device_context
+    ctx.upload(perturbed_state(semi, seed=41))
+    before = ctx.download()
+    epb, ms = ctx.autotune(iters=3)
+    assert epb in (2, 4, 8) and ms > 0 and ctx.elements_per_block() == epb
+    np.testing.assert_array_equal(ctx.download(), before)
+    ctx.step(3, 0.6, 10.0, 0.0)
+    ref, _ = build(c, precision=precision, elements_per_block=epb)
+    rctx = ref.device_context
+    rctx.upload(perturbed_state(ref, seed=41))
+    rctx.step(3, 0.6, 10.0, 0.0)
+    np.testing.assert_array_equal(ctx.download(), rctx.download())

@@ -212,7 +212,7 @@ __global__ void clock_config_kernel(Clock* c, double t_end, double cfl) {
   c->finalstep = 0;
 }
 
-__global__ void clock_begin_kernel(Clock* c) { clock_begin(c); }
+__global__ void clock_begin_kernel(Clock* c) { clock_begin_warp(c); }
 
 __global__ void clock_end_kernel(Clock* c, int n) { clock_end(c, n); }
 
@@ -880,6 +880,81 @@ int tg_ndofs(const tg_ctx* ctx, int64_t* ndofs, int64_t* nvalues) {
   return TG_OK;
 }
 
+// Autotuner: times one stage for every elements-per-block value the element
+// kernel is built with for this (D, N) and keeps the fastest.  The timed
+// launches read the current state and write only what is dead between steps
+// (the other state buffer and the 2N register), with a scratch clock (dt = 0)
+// and status word and no wave-speed reduction, so the solution is unchanged.
+int tg_ctx_autotune(tg_ctx* c, int32_t iters, int32_t* best_epb, double* ms_per_stage) {
+  if (!c || iters <= 0) return TG_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return fail(c, TG_ERR_STATE, "no state uploaded");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  const bool mixed = !c->fp64;
+  std::vector<int> cand;
+  for (int e : {mixed ? default_epb_mixed(c->D, c->N) : default_epb(c->D, c->N), 2, 4, 8, 16, 32})
+    if (std::find(cand.begin(), cand.end(), e) == cand.end() &&
+        (mixed ? supported_epb_mixed(c->D, c->N, e) : supported_epb(c->D, c->N, e)))
+      cand.push_back(e);
+  Clock* d_clk = nullptr;
+  int32_t* d_st = nullptr;
+  CUDA_TRY(c, cudaMalloc((void**)&d_clk, sizeof(Clock)));
+  if (cudaMalloc((void**)&d_st, sizeof(int32_t)) != cudaSuccess) {
+    cudaFree(d_clk);
+    return fail(c, TG_ERR_CUDA, "autotune: allocation failed");
+  }
+  cudaMemsetAsync(d_clk, 0, sizeof(Clock), c->stream);
+  cudaMemsetAsync(d_st, 0, sizeof(int32_t), c->stream);
+  Clock* keep_clock = c->d_clock;
+  int32_t* keep_status = c->d_status;
+  const int keep_epb = c->epb;
+  int rc = indicator(c, c->d_u[c->cur]);  // blending factors of the current state (HG)
+  c->d_clock = d_clk;
+  c->d_status = d_st;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int best = keep_epb;
+  float best_ms = 0;
+  for (size_t k = 0; k < cand.size() && rc == TG_OK; ++k) {
+    c->epb = cand[k];
+    for (int w = 0; w < 2 && rc == TG_OK; ++w)
+      rc = launch_kernel(c, MODE_STAGE, c->d_u[c->cur], c->d_u[c->cur ^ 1], nullptr, 0.0, 1, false);
+    cudaEventRecord(e0, c->stream);
+    for (int it = 0; it < iters && rc == TG_OK; ++it)
+      rc = launch_kernel(c, MODE_STAGE, c->d_u[c->cur], c->d_u[c->cur ^ 1], nullptr, 0.0, 1, false);
+    cudaEventRecord(e1, c->stream);
+    if (rc != TG_OK) break;
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      rc = fail(c, TG_ERR_CUDA, "autotune: stage launch failed");
+      break;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms /= iters;
+    if (k == 0 || ms < best_ms) {
+      best = cand[k];
+      best_ms = ms;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamSynchronize(c->stream);
+  c->d_clock = keep_clock;
+  c->d_status = keep_status;
+  cudaFree(d_clk);
+  cudaFree(d_st);
+  c->epb = rc == TG_OK ? best : keep_epb;
+  for (int p = 0; p < 2; ++p)
+    if (c->graph[p]) {
+      cudaGraphExecDestroy(c->graph[p]);
+      c->graph[p] = nullptr;
+    }
+  if (rc) return rc;
+  if (best_epb) *best_epb = best;
+  if (ms_per_stage) *ms_per_stage = best_ms;
+  return TG_OK;
+}
+
 int tg_elements_per_block(const tg_ctx* ctx, int32_t* epb) {
   if (!ctx || !epb) return TG_ERR_INVALID_ARGUMENT;
   *epb = ctx->epb;
@@ -1047,7 +1122,7 @@ static int capture_step_graph(tg_ctx* c, int parity) {
   c->cur = parity;
   cudaGraph_t g = nullptr;
   CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
-  clock_begin_kernel<<<1, 1, 0, c->stream>>>(c->d_clock);
+  clock_begin_kernel<<<1, 32, 0, c->stream>>>(c->d_clock);
   int rc = TG_OK;
   for (int s = 0; s < 5 && rc == TG_OK; ++s) rc = enqueue_stage(c, s, s == 4);
   if (rc == TG_OK) clock_end_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, c->N);

@@ -28,44 +28,49 @@ static __device__ const double CK_C_DEV[5] = {0.0, 1432997174477.0 / 95750804417
                                               2006345519317.0 / 3224310063776.0,
                                               2802321613138.0 / 2924317926251.0};
 
-// sin/cos(pi t_s) of the five stage times as float-float pairs, for the mixed
-// kernels' source phase
+// sin/cos(pi t_s) of stage s as float-float pairs, for the mixed kernels'
+// source phase
+static __device__ __forceinline__ void stage_phase(Clock* c, int s) {
+  double sn, cs;
+  sincospi(c->t + CK_C_DEV[s] * c->dt, &sn, &cs);
+  c->sin_t[s] = (float)sn;
+  c->cos_t[s] = (float)cs;
+  c->sin_tl[s] = (float)(sn - (double)c->sin_t[s]);
+  c->cos_tl[s] = (float)(cs - (double)c->cos_t[s]);
+}
+
 static __device__ __forceinline__ void stage_phases(Clock* c) {
-  for (int s = 0; s < 5; ++s) {
-    double sn, cs;
-    sincospi(c->t + CK_C_DEV[s] * c->dt, &sn, &cs);
-    c->sin_t[s] = (float)sn;
-    c->cos_t[s] = (float)cs;
-    c->sin_tl[s] = (float)(sn - (double)c->sin_t[s]);
-    c->cos_tl[s] = (float)(cs - (double)c->cos_t[s]);
-  }
+  for (int s = 0; s < 5; ++s) stage_phase(c, s);
 }
 
 // step! prologue: NaN check and limit_dt! (methods_2N.jl:131-140,
-// time_integration.jl:46-55), then reset of the CFL reduction.
-static __device__ __forceinline__ void clock_begin(Clock* c) {
-  c->speed_bits = 1ull;  // nextfloat(0.0), where max_dt starts (stepsize_dg2d.jl:12)
-  if (c->finished) {
-    c->skip = 1;
-    return;
+// time_integration.jl:46-55) and reset of the CFL reduction by lane 0 of a
+// warp, then the five stage phases by lanes 0..4 (FP64 sincospi in parallel).
+static __device__ __forceinline__ void clock_begin_warp(Clock* c) {
+  const int lane = threadIdx.x & 31;
+  if (lane == 0) {
+    c->speed_bits = 1ull;  // nextfloat(0.0), where max_dt starts (stepsize_dg2d.jl:12)
+    if (c->finished) {
+      c->skip = 1;
+    } else if (isnan(c->dt)) {
+      c->nan_dt = 1;
+      c->finished = 1;
+      c->skip = 1;
+    } else {
+      c->skip = 0;
+      const double tn = c->t + c->dt;
+      const double te = c->t_end;
+      // Julia isapprox: exact equality, or finite operands within rtol = sqrt(eps)
+      const bool approx = tn == te || (isfinite(tn) && isfinite(te) &&
+                                       fabs(tn - te) <= 1.4901161193847656e-08 * fmax(fabs(tn), fabs(te)));
+      if (tn > te || approx) {
+        c->dt = te - c->t;
+        c->finalstep = 1;
+      }
+    }
   }
-  if (isnan(c->dt)) {
-    c->nan_dt = 1;
-    c->finished = 1;
-    c->skip = 1;
-    return;
-  }
-  c->skip = 0;
-  const double tn = c->t + c->dt;
-  const double te = c->t_end;
-  // Julia isapprox: exact equality, or finite operands within rtol = sqrt(eps)
-  const bool approx = tn == te || (isfinite(tn) && isfinite(te) &&
-                                   fabs(tn - te) <= 1.4901161193847656e-08 * fmax(fabs(tn), fabs(te)));
-  if (tn > te || approx) {
-    c->dt = te - c->t;
-    c->finalstep = 1;
-  }
-  stage_phases(c);
+  __syncwarp();
+  if (lane < 5 && !c->skip) stage_phase(c, lane);
 }
 
 // step! epilogue: t += dt, then StepsizeCallback: dt = cfl * max_dt(u_new)

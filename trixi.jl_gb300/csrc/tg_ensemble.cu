@@ -83,9 +83,9 @@ __global__ void __launch_bounds__(NT, 480 / NT) ensemble_stage_kernel(const Mixe
   }
 }
 
+// one warp per instance
 __global__ void ens_clock_begin_kernel(Clock* const* clocks, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) clock_begin(clocks[i]);
+  if ((int)blockIdx.x < n) clock_begin_warp(clocks[blockIdx.x]);
 }
 
 __global__ void ens_clock_end_kernel(Clock* const* clocks, const int32_t* nnodes, int n) {
@@ -240,7 +240,7 @@ int capture(tg_ensemble* s, int p) {
   cudaGraph_t g = nullptr;
   ENS_TRY(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeRelaxed));
   const unsigned cb = (unsigned)((s->n + 63) / 64);
-  ens_clock_begin_kernel<<<cb, 64, 0, s->stream>>>(s->d_clocks, s->n);
+  ens_clock_begin_kernel<<<(unsigned)s->n, 32, 0, s->stream>>>(s->d_clocks, s->n);
   int rc = TG_OK;
   for (int st = 0; st < 5 && rc == TG_OK; ++st)
     rc = launch_stage(s, s->d_args + ((size_t)p * 5 + st) * s->n);

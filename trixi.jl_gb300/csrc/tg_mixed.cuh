@@ -167,6 +167,13 @@ struct Dev {
     n.dq = (R.rq + drho - R.q * dp) / n.w[P];
   }
 
+  // Conservative deviation of a node from its float-float state (as make_node).
+  static __host__ __device__ __forceinline__ void node_du(const float2* x, const RefState<D>& R,
+                                                  float* du) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) du[v] = ((x[v].x - R.hi[v]) + x[v].y) + R.r[v];
+  }
+
   // Full primitives from deviations (nodes stored as dw + dq only).
   static __host__ __device__ __forceinline__ void complete(const RefState<D>& R, Node<D>& n) {
     n.w[0] = R.rho + n.dw[0];
@@ -367,6 +374,10 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
@@ -408,16 +419,16 @@ struct MixedKernel {
   static constexpr int L = D * NF;           // lines per element
   static constexpr int NT = EPB * L;         // threads per block
   static constexpr int SP = NodeLayout<D, N, EPB>::FS;  // field stride of node arrays
-  static constexpr int NFLD = 2 * NV + 1;    // dw[NV], dq, du[NV]
+  static constexpr int NFLD = NV + 1;        // dw[NV], dq
   static constexpr int CHUNK = EPB * NN * NV;
   static constexpr int FACE = EPB * 2 * D * NF * NV;  // neighbour traces (float2)
   static constexpr int REFW = (sizeof(RefState<D>) + 3) / 4;
-  static constexpr int MINB = NT <= 128 ? 4 : (NT <= 256 ? 3 : 1);  // resident blocks per SM
+  static constexpr int MINB = NT <= 192 ? 4 : (NT <= 256 ? 3 : 1);  // resident blocks per SM
 
-  static constexpr int ALIGN4 = (4 - (CHUNK % 4)) % 4;  // keeps node fields 16-byte aligned
+  static constexpr int PADF = (CHUNK + FACE) & 1;  // keeps node fields 16-byte aligned
 
   static constexpr size_t smem_bytes() {
-    return sizeof(float2) * (CHUNK + FACE) + sizeof(float) * (CHUNK + ALIGN4)  // state, traces, u_tmp
+    return sizeof(float2) * (CHUNK + FACE + PADF)               // state, traces
            + sizeof(float) * (NFLD * SP + D * NV * SP               // node fields, partial du
                               + EPB * REFW + EPB * 8 + 8            // references, per element
                               + EPB * D                             // speed maxima
@@ -473,7 +484,7 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
   const bool vec4 = Lay::PADDED && dd == 0;  // x-line: 4 contiguous, aligned nodes
   Node<D> nd[N];
   {
-    constexpr int NLOAD = NEED_DU ? 2 * NV + 1 : NV + 1;
+    constexpr int NLOAD = NV + 1;
 #pragma unroll
     for (int f = 0; f < NLOAD; ++f) {
       float x[N];
@@ -496,16 +507,16 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
       for (int a = 0; a < N; ++a) {
         if (f < NV)
           nd[a].dw[f] = x[a];
-        else if (f == NV)
-          nd[a].dq = x[a];
         else
-          nd[a].du[f - NV - 1] = x[a];
+          nd[a].dq = x[a];
       }
     }
 #pragma unroll
     for (int a = 0; a < N; ++a) {
       Dv::complete(R, nd[a]);
       Dv::orient(nd[a], dd);
+      // conservative deviations (jumps of Lax-Friedrichs fluxes) from the staged state
+      if (NEED_DU) Dv::node_du(s_u + ((size_t)slot * NN + lb + a * S) * NV, R, nd[a].du);
     }
   }
   float acc[N][NV];
@@ -586,11 +597,7 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
     Dv::make_node(hi, lo, R, eos, nn_);
     Dv::orient(nn_, dd);
     Node<D>& own = side ? nd[N - 1] : nd[0];
-    if (!NEED_DU) {
-      const int idx = Lay::pos(slot, lb + (side ? (N - 1) * S : 0));
-#pragma unroll
-      for (int v = 0; v < NV; ++v) own.du[v] = s_nd[(NV + 1 + v) * SP + idx];
-    }
+    if (!NEED_DU) Dv::node_du(s_u + ((size_t)slot * NN + lb + (side ? (N - 1) * S : 0)) * NV, R, own.du);
     float F[NV];
     if (side) {
       Dv::template flux2<SF>(P.surface_flux, R, own, nn_, dd, vro, eos, F);
@@ -634,13 +641,12 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
 
   float2* s_u = reinterpret_cast<float2*>(smem_raw);
   float2* s_fu = s_u + CHUNK;                               // neighbour traces
-  float* s_tmp = reinterpret_cast<float*>(s_fu + FACE);
-  float* s_nd = s_tmp + CHUNK + K::ALIGN4;
+  float* s_nd = reinterpret_cast<float*>(s_fu + FACE + K::PADF);
   float* s_part = s_nd + NFLD * SP;
   RefState<D>* s_ref = reinterpret_cast<RefState<D>*>(s_part + D * NV * SP);
   // [EPB][8]: alpha, then sin/cos (hi, hi, lo, lo) of pi (x_first - t)
   float* s_elem = reinterpret_cast<float*>(s_ref + EPB);
-  // b dt, a, sin/cos(pi t) (hi, hi, lo, lo), b dt lo, a lo
+  // b dt, a, (unused: 2..5), b dt lo, a lo
   float* s_scal = s_elem + EPB * 8;
   unsigned int* s_smax = reinterpret_cast<unsigned int*>(s_scal + 8);
   float* s_mat = reinterpret_cast<float*>(s_smax + EPB * D);
@@ -658,13 +664,18 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
     return;
   }
 
-  // ---- asynchronous staging of every global input of the block -----------------
-  for (int k = tid; k < nval; k += NT) cp_async8(s_u + k, A.u_in + gofs + k);
-  const bool load_tmp = A.mode == MODE_STAGE && !A.zero_tmp;
-  if (load_tmp)
-    for (int k = tid; k < nval; k += NT) cp_async4(s_tmp + k, A.u_tmp + gofs + k);
+  // ---- asynchronous staging of the block's state (16-byte copies where the
+  //      chunk is 16-byte aligned) and of the face traces of neighbours in
+  //      other blocks -------------------------------------------------------------
+  if ((gofs & 1) == 0) {
+    const float4* src = reinterpret_cast<const float4*>(A.u_in + gofs);
+    float4* dst = reinterpret_cast<float4*>(s_u);
+    for (int k = tid; k < nval / 2; k += NT) cp_async16(dst + k, src + k);
+    if ((nval & 1) && tid == 0) cp_async8(s_u + nval - 1, A.u_in + gofs + nval - 1);
+  } else {
+    for (int k = tid; k < nval; k += NT) cp_async8(s_u + k, A.u_in + gofs + k);
+  }
   for (int k = tid; k < nel * 2 * D * NF; k += NT) {
-    // face traces of neighbours in other blocks
     const int sl = k / (2 * D * NF);
     const int rem = k - sl * (2 * D * NF);
     const int dir = rem / NF;
@@ -677,8 +688,6 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
 #pragma unroll
     for (int v = 0; v < NV; ++v) cp_async8(s_fu + k * NV + v, g + v);
   }
-  if (!load_tmp && A.mode == MODE_STAGE)
-    for (int k = tid; k < nval; k += NT) s_tmp[k] = 0.0f;
   for (int k = tid; k < N * N; k += NT) s_mat[k] = VI == VI_WEAK ? P.Dhat[k] : P.Dsplit[k];
   if (tid < N) s_iw[tid] = P.inv_weights[tid];
   if (tid < EPB * D) s_smax[tid] = 0u;
@@ -691,18 +700,10 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
     s_scal[6] = (float)(bdt - (double)bh);
     s_scal[1] = ah;
     s_scal[7] = (float)(A.a - (double)ah);
-    if (A.mode == MODE_RHS) {
-      s_scal[2] = A.sin_t;
-      s_scal[3] = A.cos_t;
-      s_scal[4] = A.sin_tl;
-      s_scal[5] = A.cos_tl;
-    } else {
-      s_scal[2] = A.clock->sin_t[A.stage];
-      s_scal[3] = A.clock->cos_t[A.stage];
-      s_scal[4] = A.clock->sin_tl[A.stage];
-      s_scal[5] = A.clock->cos_tl[A.stage];
-    }
   }
+  // ---- per element, while the copies are in flight: blending factor,
+  //      reference state (from global loads of two corner nodes) and the
+  //      element part of the source phase ------------------------------------------
   if (tid < nel) {
     const int64_t e = e0 + tid;
     if (VI == VI_HG) {
@@ -714,25 +715,25 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
       s_elem[tid * 8 + 0] = a;
       if (A.alpha_out) A.alpha_out[e] = a;
     }
-  }
-  cp_async_wait_all();
-  __syncthreads();
-
-  // ---- per element: reference state and source phase ------------------------------
-  if (tid < nel) {
     // reference = mean of two opposite corner nodes: the element centre for a
     // linear state, which makes the deviations (and their FP32 rounding) about
     // three times smaller in rms than those from a corner
+    const float2* ue = A.u_in + (size_t)e * NN * NV;
     float hi[NV];
 #pragma unroll
-    for (int v = 0; v < NV; ++v)
-      hi[v] = 0.5f * (s_u[tid * NN * NV + v].x + s_u[(tid * NN + NN - 1) * NV + v].x);
+    for (int v = 0; v < NV; ++v) hi[v] = 0.5f * (ue[v].x + ue[(NN - 1) * NV + v].x);
     Dv::make_ref(hi, P.eos, s_ref[tid]);
     if (P.source == SRC_CONVERGENCE_TEST) {
       // sin/cos of pi (x_first - t) in float-float by the angle-difference
       // formula: sin(a - b) = sa cb - ca sb, cos(a - b) = ca cb + sa sb
-      const float4 a = P.sc0[e0 + tid];
-      const float st = s_scal[2], ct = s_scal[3], stl = s_scal[4], ctl = s_scal[5];
+      float st, ct, stl, ctl;
+      if (A.mode == MODE_RHS) {
+        st = A.sin_t, ct = A.cos_t, stl = A.sin_tl, ctl = A.cos_tl;
+      } else {
+        st = A.clock->sin_t[A.stage], ct = A.clock->cos_t[A.stage];
+        stl = A.clock->sin_tl[A.stage], ctl = A.clock->cos_tl[A.stage];
+      }
+      const float4 a = P.sc0[e];
       const float2 sn = ff_dot2(a.x, a.z, ct, ctl, -a.y, -a.w, st, stl);
       const float2 cs = ff_dot2(a.y, a.w, ct, ctl, a.x, a.z, st, stl);
       float* el = s_elem + tid * 8;
@@ -742,6 +743,7 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
       el[4] = cs.y;
     }
   }
+  cp_async_wait_all();
   __syncthreads();
 
   // ---- node deviations -----------------------------------------------------------
@@ -758,10 +760,7 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
     Dv::make_node(hi, lo, s_ref[sl], P.eos, nd);
     const int ps = Lay::pos(sl, n - sl * NN);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      s_nd[v * SP + ps] = nd.dw[v];
-      s_nd[(NV + 1 + v) * SP + ps] = nd.du[v];
-    }
+    for (int v = 0; v < NV; ++v) s_nd[v * SP + ps] = nd.dw[v];
     s_nd[NV * SP + ps] = nd.dq;
   }
   __syncthreads();
@@ -777,16 +776,34 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
                                         VI == VI_HG ? s_elem[sl * 8] : 0.0f, sl, line, dd,
                                         e0 + sl, e0, nel);
   }
+  // 2N register of this thread's node-phase nodes (zero at the first stage),
+  // loaded before the barrier so that its latency overlaps the wait
+  constexpr int NPT = (EPB * NN + NT - 1) / NT;  // nodes per thread in the node phase
+  const bool stage = A.mode == MODE_STAGE;
+  float ut_pre[NPT][NV];
+#pragma unroll
+  for (int k = 0; k < NPT; ++k) {
+    const int n = tid + k * NT;
+    const bool ld = stage && !A.zero_tmp && n < nel * NN;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) ut_pre[k][v] = ld ? A.u_tmp[gofs + (size_t)n * NV + v] : 0.0f;
+  }
   __syncthreads();
 
-  // ---- nodes: sum of directions, Jacobian, sources, 2N update ---------------------
+  // ---- nodes: sum of directions, Jacobian, sources, 2N update, written
+  //      straight to HBM ---------------------------------------------------------------
   const float bdt = s_scal[0], bdt_lo = s_scal[6];
   const float a_s = s_scal[1], a_lo = s_scal[7];
   bool bad = false;
-  for (int n = tid; n < nel * NN; n += NT) {
+#pragma unroll
+  for (int k = 0; k < NPT; ++k) {
+    const int n = tid + k * NT;
+    if (n >= nel * NN) continue;
     const int sl = n / NN;
     const int node = n - sl * NN;
     const int64_t e = e0 + sl;
+    const size_t g = gofs + (size_t)n * NV;
+    const float* ut_old = ut_pre[k];
     const float jfac = -P.inv_jac[e];
     const int ps = Lay::pos(sl, node);
     float du[NV];
@@ -810,19 +827,18 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
 #pragma unroll
       for (int v = 0; v < NV; ++v) du[v] += src[v];
     }
-    if (A.mode == MODE_RHS) {
+    if (!stage) {
 #pragma unroll
-      for (int v = 0; v < NV; ++v) s_tmp[n * NV + v] = du[v];
+      for (int v = 0; v < NV; ++v) A.du_out[g + v] = (double)du[v];
       continue;
     }
     float hi[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      const int k = n * NV + v;
-      const float ut = fmaf(-a_lo, s_tmp[k], fmaf(-a_s, s_tmp[k], du[v]));
-      s_tmp[k] = ut;
-      const float2 un = ff_add(s_u[k], fmaf(ut, bdt_lo, ut * bdt));
-      s_u[k] = un;
+      const float ut = fmaf(-a_lo, ut_old[v], fmaf(-a_s, ut_old[v], du[v]));
+      A.u_tmp[g + v] = ut;
+      const float2 un = ff_add(s_u[n * NV + v], fmaf(ut, bdt_lo, ut * bdt));
+      A.u_out[g + v] = un;
       hi[v] = un.x;
       bad |= !(un.x == un.x);
     }
@@ -839,21 +855,15 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
     }
   }
   if (bad) atomicOr(A.status, 1);
-  __syncthreads();
-  if (A.mode == MODE_RHS) {
-    for (int k = tid; k < nval; k += NT) A.du_out[gofs + k] = (double)s_tmp[k];
-    return;
-  }
-  for (int k = tid; k < nval; k += NT) {
-    A.u_out[gofs + k] = s_u[k];
-    A.u_tmp[gofs + k] = s_tmp[k];
-  }
-  if (A.speed_bits && tid < nel) {
-    float sum = 0;
+  if (stage && A.speed_bits) {
+    __syncthreads();
+    if (tid < nel) {
+      float sum = 0;
 #pragma unroll
-    for (int d = 0; d < D; ++d) sum += __uint_as_float(s_smax[tid * D + d]);
-    const float sp = P.inv_jac[e0 + tid] * sum;
-    if (sp == sp) atomicMax(A.speed_bits, (unsigned long long)__double_as_longlong((double)sp));
+      for (int d = 0; d < D; ++d) sum += __uint_as_float(s_smax[tid * D + d]);
+      const float sp = P.inv_jac[e0 + tid] * sum;
+      if (sp == sp) atomicMax(A.speed_bits, (unsigned long long)__double_as_longlong((double)sp));
+    }
   }
 }
 

@@ -34,7 +34,7 @@ EXPORTS = ("tg_api_version", "tg_ctx_create", "tg_ctx_destroy", "tg_last_error",
            "tg_mlp_gradient", "tg_mlp_predict", "tg_ctx_set_learned_indicator", "tg_mlp_last",
            "tg_entropy_timederivative", "tg_ensemble_create", "tg_ensemble_destroy",
            "tg_ensemble_size", "tg_ensemble_context", "tg_ensemble_step", "tg_ensemble_autotune",
-           "tg_ensemble_threads_per_block", "tg_ensemble_last_error")
+           "tg_ensemble_threads_per_block", "tg_ensemble_last_error", "tg_ctx_autotune")
 
 
 class TrixiGB300Error(RuntimeError):
@@ -134,6 +134,7 @@ def load(path: str | None = None):
         "tg_ensemble_autotune": ([vp, i32, P(i32), pd], ctypes.c_int),
         "tg_ensemble_threads_per_block": ([vp], ctypes.c_int),
         "tg_ensemble_last_error": ([vp, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
+        "tg_ctx_autotune": ([vp, i32, P(i32), pd], ctypes.c_int),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(lib, name)

@@ -193,6 +193,14 @@ class DeviceContext:
     def synchronize(self):
         self._check(self.lib.tg_synchronize(self.h))
 
+    def autotune(self, iters=20):
+        """Time every elements-per-block value of the element kernel on the
+        uploaded state (unchanged) and keep the fastest; returns (epb, ms per stage)."""
+        epb = ctypes.c_int32()
+        ms = ctypes.c_double()
+        self._check(self.lib.tg_ctx_autotune(self.h, int(iters), ctypes.byref(epb), ctypes.byref(ms)))
+        return epb.value, ms.value
+
     def stream(self) -> int:
         """cudaStream_t of the context (for torch.cuda.ExternalStream)."""
         p = ctypes.c_void_p()
