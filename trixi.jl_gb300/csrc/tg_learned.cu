@@ -28,6 +28,7 @@
 #include <cmath>
 #include <cstdio>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/trixi_gb300.h"
@@ -94,6 +95,17 @@ struct FeatParams {
   float alpha_min, alpha_max, hg_threshold, hg_parameter_s;
 };
 
+// One 16-byte read-only load kept whole even where only some lanes of it are
+// used (the hi halves of a float-float pair): split into 4-byte loads it
+// would touch every 32-byte sector twice.
+__device__ __forceinline__ float4 ldg_v4(const void* p) {
+  float4 r;
+  asm("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
+      : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+      : "l"(p));
+  return r;
+}
+
 // Modes of rho*p of element e (normalised to unit energy when `normalise`),
 // the HG energy indicator max(f1, f2) and positivity of rho*p at the nodes.
 template <int D, int N, typename TS>
@@ -106,8 +118,20 @@ __device__ __forceinline__ void element_modes(const FeatParams& P, const TS* __r
 #pragma unroll
   for (int q = 0; q < NN; ++q) {
     float uu[NV];
+    if constexpr (std::is_same<TS, float2>::value && NV % 2 == 0) {
+      // float-float state: two values per 16-byte load (the element's values
+      // are contiguous and 16-byte aligned when NV is even)
+      const float4* p4 = reinterpret_cast<const float4*>(u + ((size_t)e * NN + q) * NV);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) uu[v] = (float)state_value(u[((size_t)e * NN + q) * NV + v]);
+      for (int v = 0; v < NV; v += 2) {
+        const float4 x = ldg_v4(p4 + v / 2);
+        uu[v] = state_value(make_float2(x.x, x.y));
+        uu[v + 1] = state_value(make_float2(x.z, x.w));
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) uu[v] = (float)state_value(u[((size_t)e * NN + q) * NV + v]);
+    }
     a[q] = Euler<D, float>::density_pressure(uu, (float)P.gamma);
     positive &= a[q] > 0.0f;
   }
@@ -245,7 +269,7 @@ struct AlphaParams {
 };
 
 template <int N, typename TS, typename R>
-__global__ void __launch_bounds__(128) learned_alpha2d_kernel(
+__global__ void __launch_bounds__(128, 4) learned_alpha2d_kernel(
     const FeatParams P, const TS* __restrict__ u, const __nv_bfloat16* __restrict__ w,
     const AlphaParams A, R* __restrict__ alpha_raw, float* __restrict__ pred_out,
     float* __restrict__ hg_out, int32_t* __restrict__ flag_out,
@@ -269,13 +293,21 @@ __global__ void __launch_bounds__(128) learned_alpha2d_kernel(
       for (int k = 0; k < NM; ++k) z = fmaf(sw[L.w1() + i * NM + k], xv[k], z);
       h1[i] = fmaxf(z, 0.0f);
     }
+    // layer 2, eight neurons at a time: independent FMA chains, each in the
+    // same order (j ascending) as a one-neuron loop
+    constexpr int G = 8;
     float out = sw[L.b3()];
 #pragma unroll 1
-    for (int i = 0; i < H; ++i) {
-      float z = sw[L.b2() + i];
+    for (int i = 0; i < H; i += G) {
+      float z[G];
 #pragma unroll
-      for (int j = 0; j < H; ++j) z = fmaf(sw[L.w2() + i * H + j], h1[j], z);
-      out = fmaf(sw[L.w3() + i], fmaxf(z, 0.0f), out);
+      for (int r = 0; r < G; ++r) z[r] = sw[L.b2() + i + r];
+#pragma unroll
+      for (int j = 0; j < H; ++j)
+#pragma unroll
+        for (int r = 0; r < G; ++r) z[r] = fmaf(sw[L.w2() + (i + r) * H + j], h1[j], z[r]);
+#pragma unroll
+      for (int r = 0; r < G; ++r) out = fmaf(sw[L.w3() + i + r], fmaxf(z[r], 0.0f), out);
     }
     const float hg = hg_logistic(energy, A.thr, A.s_par, 0.0f, 1.0f);
     int f = positive ? 0 : 2;
