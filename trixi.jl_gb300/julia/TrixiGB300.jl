@@ -93,24 +93,30 @@ end
 Builds a device context from a `SemidiscretizationHyperbolic` on a periodic
 `TreeMesh` with `DGSEM` (precision 0 = FP64, 1 = mixed FP32/float-float).
 """
-function create_context(semi; precision = 0, device = 0)
+# tg_config of a semidiscretization; the pointers stay valid while `semi` is
+# preserved (GC.@preserve) by the caller.
+function config(semi, precision, device)
     (; mesh, equations, solver, cache, source_terms) = semi
     b = solver.basis
     vi, vf, sf_fv, amax, amin, asmooth = volume_codes(solver.volume_integral,
                                                       solver.surface_integral.surface_flux)
     sf = flux_code(solver.surface_integral.surface_flux)
-    GC.@preserve b cache begin
-        cfg = TgConfig(ndims(mesh), Trixi.polydeg(solver), nelements(solver, cache),
-                       ninterfaces(solver, cache), equations.gamma, vi, vf, sf,
-                       vi == TG_VOLUME_SHOCK_CAPTURING_HG ? sf_fv : sf, amax, amin, asmooth,
-                       source_code(source_terms), precision, device,
-                       pointer(b.nodes), pointer(b.weights), pointer(b.inverse_weights),
-                       pointer(b.derivative_hat), pointer(b.derivative_split),
-                       pointer(b.inverse_vandermonde_legendre),
-                       pointer(cache.interfaces.neighbor_ids),
-                       pointer(cache.interfaces.orientations),
-                       pointer(cache.elements.inverse_jacobian),
-                       pointer(cache.elements.node_coordinates), 0)
+    return TgConfig(ndims(mesh), Trixi.polydeg(solver), nelements(solver, cache),
+                    ninterfaces(solver, cache), equations.gamma, vi, vf, sf,
+                    vi == TG_VOLUME_SHOCK_CAPTURING_HG ? sf_fv : sf, amax, amin, asmooth,
+                    source_code(source_terms), precision, device,
+                    pointer(b.nodes), pointer(b.weights), pointer(b.inverse_weights),
+                    pointer(b.derivative_hat), pointer(b.derivative_split),
+                    pointer(b.inverse_vandermonde_legendre),
+                    pointer(cache.interfaces.neighbor_ids),
+                    pointer(cache.interfaces.orientations),
+                    pointer(cache.elements.inverse_jacobian),
+                    pointer(cache.elements.node_coordinates), 0)
+end
+
+function create_context(semi; precision = 0, device = 0)
+    GC.@preserve semi begin
+        cfg = config(semi, precision, device)
         out = Ref{Ptr{Cvoid}}(C_NULL)
         check(ccall((:tg_ctx_create, lib), Cint, (Ref{TgConfig}, Ref{Ptr{Cvoid}}), cfg, out))
     end
@@ -155,6 +161,94 @@ function max_dt(ctx::GB300Context)
     check(ccall((:tg_max_dt, lib), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ref{Cdouble}),
                 ctx.ptr, C_NULL, dt), ctx.ptr)
     return dt[]
+end
+
+"""
+    entropy_timederivative(ctx, t)
+
+`analyze(entropy_timederivative, du, u, t, ...)` of the device state
+(analysis_dg2d.jl:460-472): the normalised integral of cons2entropy(u) . rhs(u).
+"""
+function entropy_timederivative(ctx::GB300Context, t)
+    out = Ref{Cdouble}(0)
+    check(ccall((:tg_entropy_timederivative, lib), Cint, (Ptr{Cvoid}, Cdouble, Ref{Cdouble}),
+                ctx.ptr, t, out), ctx.ptr)
+    return out[]
+end
+
+"""
+    autotune!(ctx; iters = 20)
+
+Times every elements-per-block choice of the element kernel on the uploaded
+state (which it leaves unchanged) and keeps the fastest; returns it and the
+time per stage in ms.
+"""
+function autotune!(ctx::GB300Context; iters = 20)
+    epb = Ref{Int32}(0)
+    ms = Ref{Cdouble}(0)
+    check(ccall((:tg_ctx_autotune, lib), Cint, (Ptr{Cvoid}, Int32, Ref{Int32}, Ref{Cdouble}),
+                ctx.ptr, iters, epb, ms), ctx.ptr)
+    return epb[], ms[]
+end
+
+# ---- batched ensembles: many 2D semidiscretizations stepped together -------------
+mutable struct GB300Ensemble
+    ptr::Ptr{Cvoid}
+end
+
+function ensemble_error(ens::Ptr{Cvoid})
+    buf = Vector{UInt8}(undef, 1024)
+    ccall((:tg_ensemble_last_error, lib), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Csize_t), ens, buf,
+          length(buf))
+    return unsafe_string(pointer(buf))
+end
+
+"""
+    create_ensemble(semis; threads_per_block = 0, device = 0)
+
+One persistent launch per 2N stage and one CUDA graph per step for all of
+`semis` (2D, polydeg 2..4, mixed precision, one solver type).
+"""
+function create_ensemble(semis; threads_per_block = 0, device = 0)
+    GC.@preserve semis begin
+        cfgs = [config(semi, 1, device) for semi in semis]
+        out = Ref{Ptr{Cvoid}}(C_NULL)
+        rc = ccall((:tg_ensemble_create, lib), Cint, (Ptr{TgConfig}, Int32, Int32, Ref{Ptr{Cvoid}}),
+                   cfgs, length(cfgs), threads_per_block, out)
+        rc == 0 || error(ensemble_error(C_NULL))
+    end
+    ens = GB300Ensemble(out[])
+    finalizer(e -> ccall((:tg_ensemble_destroy, lib), Cint, (Ptr{Cvoid},), e.ptr), ens)
+    return ens
+end
+
+"""
+    instance(ens, i)
+
+Context of instance i (1-based), owned by the ensemble: `upload!`,
+`download!` and the analysis calls work on it.
+"""
+function instance(ens::GB300Ensemble, i)
+    p = Ref{Ptr{Cvoid}}(C_NULL)
+    rc = ccall((:tg_ensemble_context, lib), Cint, (Ptr{Cvoid}, Int32, Ref{Ptr{Cvoid}}), ens.ptr,
+               i - 1, p)
+    rc == 0 || error(ensemble_error(ens.ptr))
+    return GB300Context(p[])  # no finalizer: the ensemble owns it
+end
+
+"""
+    step_to!(ens, t, t_end, cfl; max_steps)
+
+Every instance from its own `t[i]` with its own StepsizeCallback(cfl) step
+size; updates `t` and returns the step counts.
+"""
+function step_to!(ens::GB300Ensemble, t::Vector{Float64}, t_end, cfl; max_steps = typemax(Int64))
+    steps = zeros(Int64, length(t))
+    rc = ccall((:tg_ensemble_step, lib), Cint,
+               (Ptr{Cvoid}, Int64, Cdouble, Cdouble, Ptr{Cdouble}, Ptr{Int64}),
+               ens.ptr, max_steps, cfl, t_end, t, steps)
+    rc == 0 || error(ensemble_error(ens.ptr))
+    return steps
 end
 
 end # module

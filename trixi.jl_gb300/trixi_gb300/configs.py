@@ -307,9 +307,12 @@ def c5a(n=64, seed=20261204, t_end=20.0):
     return out
 
 
-def _ke_history(semi, t_end, dt_out, cfl=1.4):
+def _ke_history(semi, t_end, dt_out, cfl=1.4, perturb=0.0):
     c = semi.device_context
-    c.upload(semi.compute_coefficients(0.0))
+    u0 = semi.compute_coefficients(0.0)
+    if perturb:
+        u0 = u0 * (1.0 + perturb * np.random.default_rng(1).uniform(-1, 1, size=u0.shape))
+    c.upload(u0)
     hist = [(0.0, float(c.integrals()[-1]))]
     t, steps, secs = 0.0, 0, 0.0
     while t < t_end:
@@ -322,20 +325,33 @@ def _ke_history(semi, t_end, dt_out, cfl=1.4):
     return hist, steps, secs
 
 
-def c5b(levels=((5, 20.0, 20.0), (6, 20.0, 2.0)), dt_out=0.25):
-    """levels: (refinement level, mixed t_end, FP64 t_end)."""
+def c5b(levels=((5, 20.0, 20.0), (6, 20.0, 2.0)), dt_out=0.25, control_level=5):
+    """levels: (refinement level, mixed t_end, FP64 t_end).  At control_level
+    an FP64 run from the initial state perturbed by 1e-13 (relative) shows how
+    far two FP64 runs drift apart through the turbulent phase alone."""
     out = {}
     for level, t_mixed, t_fp64 in levels:
         r = {}
-        for prec, t_end in (("mixed", t_mixed), ("fp64", t_fp64)):
-            semi = tgv_semi(level, prec)
-            hist, steps, secs = _ke_history(semi, t_end, dt_out)
-            r[prec] = dict(ke=hist, steps=steps, secs=secs, rate=rate(semi.ndofs, steps, secs))
+        runs = [("mixed", t_mixed, 0.0), ("fp64", t_fp64, 0.0)]
+        if level == control_level:
+            runs.append(("fp64_perturbed", t_fp64, 1e-13))
+        for name, t_end, eps in runs:
+            semi = tgv_semi(level, "mixed" if name == "mixed" else "fp64")
+            hist, steps, secs = _ke_history(semi, t_end, dt_out, perturb=eps)
+            r[name] = dict(ke=hist, steps=steps, secs=secs, rate=rate(semi.ndofs, steps, secs))
             del semi
-        km = {round(t, 9): k for t, k in r["mixed"]["ke"]}
-        diffs = [abs(km[round(t, 9)] - k) / k for t, k in r["fp64"]["ke"] if round(t, 9) in km]
+
+        def rel_diffs(a, b):
+            ka = {round(t, 9): k for t, k in r[a]["ke"]}
+            return [abs(ka[round(t, 9)] - k) / k for t, k in r[b]["ke"] if round(t, 9) in ka]
+
+        diffs = rel_diffs("mixed", "fp64")
         r["ke_rel_diff_max"] = float(max(diffs))
         r["ke_rel_diff_final_common"] = float(diffs[-1])
+        if "fp64_perturbed" in r:
+            ctrl = rel_diffs("fp64_perturbed", "fp64")
+            r["control_ke_rel_diff_max"] = float(max(ctrl))
+            r["control_ke_rel_diff_final"] = float(ctrl[-1])
         r["speedup"] = r["mixed"]["rate"] / r["fp64"]["rate"]
         out[f"{2 ** level}^3"] = r
     return out
