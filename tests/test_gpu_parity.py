@@ -268,3 +268,25 @@ def test_autotune_keeps_state_and_steps_like_a_fixed_choice(precision):
     rctx.upload(perturbed_state(ref, seed=41))
     rctx.step(3, 0.6, 10.0, 0.0)
     np.testing.assert_array_equal(ctx.download(), rctx.download())
+
+
+def test_mixed_pinned_and_pageable_transfers_agree():
+    # page-locked buffers are converted in place by the device (no staging
+    # copy); the result must be the same bits as through pageable memory
+    torch = pytest.importorskip("torch")
+    c = RHS_CASES[6]
+    semi, _ = build(c, precision="mixed")
+    ctx = semi.device_context
+    u = perturbed_state(semi, seed=43)
+    ctx.upload(u)
+    ref = ctx.download()
+    ctx.step(2, 0.6, 10.0, 0.0)
+    ref_stepped = ctx.download()
+    pin_in = torch.from_numpy(np.ascontiguousarray(u).reshape(-1)).pin_memory()
+    pin_out = torch.empty_like(pin_in).pin_memory()
+    ctx.upload(pin_in.data_ptr())
+    ctx.download(pin_out.data_ptr())
+    np.testing.assert_array_equal(pin_out.numpy().reshape(ref.shape), ref)
+    ctx.step(2, 0.6, 10.0, 0.0)
+    ctx.download(pin_out.data_ptr())
+    np.testing.assert_array_equal(pin_out.numpy().reshape(ref.shape), ref_stepped)

@@ -176,6 +176,43 @@ __global__ void max_speed_kernel(const TS* __restrict__ u, const double* __restr
   if (bad) atomicOr(status, 2);
 }
 
+// The same reduction for a mixed context in the FP32 arithmetic its stage
+// kernel uses for the wave speed of the updated state (hi parts, FP32
+// primitives and sound speed, FP32 inverse Jacobian), so that the first dt
+// after an upload is computed like every later one.
+template <int D>
+__global__ void max_speed_ff_kernel(const float2* __restrict__ u, const float* __restrict__ inv_jac,
+                                    int64_t E, int NN, float gamma,
+                                    unsigned long long* __restrict__ speed_bits,
+                                    int32_t* __restrict__ status) {
+  constexpr int NV = D + 2;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  float ml[D];
+  for (int d = 0; d < D; ++d) ml[d] = 0.0f;
+  bool bad = false;
+  for (int q = 0; q < NN; ++q) {
+    const float2* p = u + ((size_t)e * NN + q) * NV;
+    float hi[NV], w[NV];
+    for (int v = 0; v < NV; ++v) hi[v] = p[v].x;
+    Euler<D, float>::cons2prim(hi, w, gamma);
+    const float cs = sqrtf(gamma * w[NV - 1] / w[0]);
+    bad |= !(w[0] > 0.0f) || !(w[NV - 1] > 0.0f);
+    for (int d = 0; d < D; ++d) {
+      const float lam = fabsf(w[1 + d]) + cs;
+      if (lam == lam) ml[d] = fmaxf(ml[d], lam);
+    }
+  }
+  float sum = 0;
+  for (int d = 0; d < D; ++d) sum += ml[d];
+  const float sp = inv_jac[e] * sum;
+  if (sp == sp)
+    atomicMax(speed_bits, (unsigned long long)__double_as_longlong((double)sp));
+  else
+    bad = true;
+  if (bad) atomicOr(status, 2);
+}
+
 __global__ void speed_reset_kernel(unsigned long long* speed_bits) {
   // nextfloat(0.0): max_dt starts its reduction there (stepsize_dg2d.jl:12)
   *speed_bits = 1ull;
@@ -532,16 +569,26 @@ static int enqueue_stage(tg_ctx* c, int stage, bool reduce_speed) {
   return TG_OK;
 }
 
-// CFL reduction of an FP64 state (Trixi layout).
-static int reduce_speed(tg_ctx* c, const double* u, unsigned long long* dst) {
+// CFL reduction of a state: FP64 values, or (ff) the float-float state of a
+// mixed context in that context's FP32 wave-speed arithmetic.
+static int reduce_speed(tg_ctx* c, const void* u, bool ff, unsigned long long* dst) {
   speed_reset_kernel<<<1, 1, 0, c->stream>>>(dst);
-  const int64_t nb = (c->E + 127) / 128;
-  if (c->D == 2)
-    max_speed_kernel<2, double><<<(unsigned)nb, 128, 0, c->stream>>>(u, c->d_invj, c->E, c->NN,
-                                                                     c->P.gamma, dst, c->d_status);
-  else
-    max_speed_kernel<3, double><<<(unsigned)nb, 128, 0, c->stream>>>(u, c->d_invj, c->E, c->NN,
-                                                                     c->P.gamma, dst, c->d_status);
+  const unsigned nb = (unsigned)((c->E + 127) / 128);
+  if (c->D == 2) {
+    if (ff)
+      max_speed_ff_kernel<2><<<nb, 128, 0, c->stream>>>((const float2*)u, c->d_invj_f, c->E, c->NN,
+                                                       (float)c->P.gamma, dst, c->d_status);
+    else
+      max_speed_kernel<2, double><<<nb, 128, 0, c->stream>>>((const double*)u, c->d_invj, c->E,
+                                                            c->NN, c->P.gamma, dst, c->d_status);
+  } else {
+    if (ff)
+      max_speed_ff_kernel<3><<<nb, 128, 0, c->stream>>>((const float2*)u, c->d_invj_f, c->E, c->NN,
+                                                       (float)c->P.gamma, dst, c->d_status);
+    else
+      max_speed_kernel<3, double><<<nb, 128, 0, c->stream>>>((const double*)u, c->d_invj, c->E,
+                                                            c->NN, c->P.gamma, dst, c->d_status);
+  }
   CUDA_TRY(c, cudaGetLastError());
   return TG_OK;
 }
@@ -961,12 +1008,29 @@ int tg_elements_per_block(const tg_ctx* ctx, int32_t* epb) {
   return TG_OK;
 }
 
+// Device address of page-locked host memory (cudaHostAlloc / cudaHostRegister),
+// or null for pageable memory.  The mixed path's conversion kernels read and
+// write such buffers directly (over NVLink-C2C on GB300) instead of staging
+// them through a device copy first.
+static const void* pinned_device_ptr(const void* host) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();  // pageable memory unknown to CUDA: not an error here
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int tg_upload_state(tg_ctx* c, const double* u_host) {
   if (!c || !u_host) return TG_ERR_INVALID_ARGUMENT;
   CUDA_TRY(c, cudaSetDevice(c->device));
   const size_t vb = sizeof(double) * c->nvalues;
+  const void* pinned = c->fp64 ? nullptr : pinned_device_ptr(u_host);
   if (c->fp64) {
     CUDA_TRY(c, cudaMemcpyAsync(c->d_u[c->cur], u_host, vb, cudaMemcpyHostToDevice, c->stream));
+  } else if (pinned) {
+    int rc = import_state(c, (const double*)pinned, c->d_u[c->cur]);
+    if (rc) return rc;
   } else {
     int rc = ensure(c, (void**)&c->d_stage64, vb);
     if (rc) return rc;
@@ -983,6 +1047,15 @@ int tg_upload_state(tg_ctx* c, const double* u_host) {
 int tg_download_state(tg_ctx* c, double* u_host) {
   if (!c || !u_host) return TG_ERR_INVALID_ARGUMENT;
   CUDA_TRY(c, cudaSetDevice(c->device));
+  if (!c->fp64) {
+    if (void* pinned = const_cast<void*>(pinned_device_ptr(u_host))) {
+      from_ff_kernel<<<conv_blocks(c->nvalues), 256, 0, c->stream>>>(
+          (const float2*)c->d_u[c->cur], (double*)pinned, c->nvalues);
+      CUDA_TRY(c, cudaGetLastError());
+      CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+      return TG_OK;
+    }
+  }
   int rc;
   const double* src = export_state(c, &rc);
   if (rc) return rc;
@@ -1034,10 +1107,9 @@ int tg_rhs_host(tg_ctx* c, double* du_host, const double* u_host, double t) {
 int tg_max_dt(tg_ctx* c, const double* u_dev, double* dt) {
   if (!c || !dt) return TG_ERR_INVALID_ARGUMENT;
   CUDA_TRY(c, cudaSetDevice(c->device));
-  int rc = TG_OK;
-  const double* u = u_dev ? u_dev : export_state(c, &rc);
-  if (rc) return rc;
-  rc = reduce_speed(c, u, c->d_speed);
+  // a caller's FP64 state, or the context state as it is stored
+  int rc = reduce_speed(c, u_dev ? (const void*)u_dev : c->d_u[c->cur], !u_dev && !c->fp64,
+                        c->d_speed);
   if (rc) return rc;
   unsigned long long bits = 0;
   CUDA_TRY(c, cudaMemcpyAsync(&bits, c->d_speed, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
@@ -1074,13 +1146,10 @@ int tg_set_time(tg_ctx* c, double t) {
 
 extern "C++" {
 namespace tg {
-int ctx_clock_prepare(tg_ctx* c, double t0, double t_end, double cfl) {
+int ctx_clock_prepare(tg_ctx* c, double t0, double t_end, double cfl, bool sync) {
   if (!c->clock_valid) {
     // initialize!(StepsizeCallback): dt = cfl * max_dt(u0)
-    int rc = TG_OK;
-    const double* u64 = export_state(c, &rc);
-    if (rc) return rc;
-    rc = reduce_speed(c, u64, &c->d_clock->speed_bits);
+    int rc = reduce_speed(c, c->d_u[c->cur], !c->fp64, &c->d_clock->speed_bits);
     if (rc) return rc;
     clock_init_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, t0, t_end, cfl, c->N);
     CUDA_TRY(c, cudaGetLastError());
@@ -1089,7 +1158,7 @@ int ctx_clock_prepare(tg_ctx* c, double t0, double t_end, double cfl) {
     clock_config_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, t_end, cfl);
     CUDA_TRY(c, cudaGetLastError());
   }
-  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (sync) CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return TG_OK;
 }
 
@@ -1149,7 +1218,7 @@ int tg_step(tg_ctx* c, int64_t max_steps, double cfl, double t_end, double* t_in
       int rc = capture_step_graph(c, p);
       if (rc) return rc;
     }
-  int rc = tg::ctx_clock_prepare(c, *t_inout, t_end, cfl);
+  int rc = tg::ctx_clock_prepare(c, *t_inout, t_end, cfl, false);  // the clock read below orders it
   if (rc) return rc;
   Clock h{};
   CUDA_TRY(c, cudaMemcpyAsync(&h, c->d_clock, sizeof(Clock), cudaMemcpyDeviceToHost, c->stream));

@@ -62,24 +62,28 @@ __global__ void __launch_bounds__(NT, 480 / NT) ensemble_stage_kernel(const Mixe
   __shared__ __align__(16) MixedParams sP;
   __shared__ __align__(16) MixedArgs sA;
   static_assert(sizeof(MixedParams) % 4 == 0 && sizeof(MixedArgs) % 4 == 0, "word copies");
+  int staged = -1;  // instance whose parameters are in shared memory
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const EnsItem w = items[it];
-    {
+    // items are grouped by instance, so a block's consecutive items mostly
+    // share it: stage parameters and arguments only when it changes
+    if (w.inst != staged) {
       const int* src = reinterpret_cast<const int*>(params + w.inst);
       int* dst = reinterpret_cast<int*>(&sP);
       for (int k = threadIdx.x; k < (int)(sizeof(MixedParams) / 4); k += NT) dst[k] = src[k];
       const int* srca = reinterpret_cast<const int*>(args + w.inst);
       int* dsta = reinterpret_cast<int*>(&sA);
       for (int k = threadIdx.x; k < (int)(sizeof(MixedArgs) / 4); k += NT) dsta[k] = srca[k];
+      staged = w.inst;
+      __syncthreads();
     }
-    __syncthreads();
     switch (w.n) {
       case 3: mixed_element_block<2, 3, VI, VF, SF, NT / 6>(sP, sA, w.blk, smem_raw); break;
       case 4: mixed_element_block<2, 4, VI, VF, SF, NT / 8>(sP, sA, w.blk, smem_raw); break;
       case 5: mixed_element_block<2, 5, VI, VF, SF, NT / 10>(sP, sA, w.blk, smem_raw); break;
       default: break;
     }
-    __syncthreads();  // shared memory is reused by the next item
+    __syncthreads();  // shared memory (and sP, sA) is reused by the next item
   }
 }
 
@@ -411,7 +415,7 @@ int tg_ensemble_step(tg_ensemble* s, int64_t max_steps, double cfl, double t_end
   int rc = align_buffers(s);
   if (rc) return rc;
   for (int i = 0; i < s->n; ++i) {
-    rc = tg::ctx_clock_prepare(s->ctx[i], t[i], t_end, cfl);
+    rc = tg::ctx_clock_prepare(s->ctx[i], t[i], t_end, cfl, true);
     if (rc) {
       char msg[512];
       tg_last_error(s->ctx[i], msg, sizeof(msg));

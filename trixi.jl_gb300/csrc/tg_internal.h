@@ -25,8 +25,9 @@ struct CtxView {
 int ctx_view(tg_ctx* c, CtxView* v);
 void ctx_set_cur(tg_ctx* c, int cur);
 // initialize!(StepsizeCallback) on the first call (dt = cfl * max_dt(u) at
-// t0), otherwise a new t_end and cfl; returns after the clock is set.
-int ctx_clock_prepare(tg_ctx* c, double t0, double t_end, double cfl);
+// t0), otherwise a new t_end and cfl, on the context's stream; with `sync`
+// it returns after the clock is set.
+int ctx_clock_prepare(tg_ctx* c, double t0, double t_end, double cfl, bool sync);
 // message for tg_last_error(NULL, ...) of the calling thread
 void set_thread_error(const char* msg);
 
