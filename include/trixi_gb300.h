@@ -90,6 +90,32 @@ typedef enum tg_precision {
   TG_PRECISION_MIXED = 1
 } tg_precision;
 
+/* Boundary conditions of a non-periodic TreeMesh, per direction:
+ * BoundaryConditionDirichlet(initial_condition) (src/equations/equations.jl:
+ * 159-182) and boundary_condition_slip_wall (compressible_euler_2d.jl:322-393,
+ * 3d.jl:315-416). */
+typedef enum tg_boundary {
+  TG_BOUNDARY_PERIODIC = 0,
+  TG_BOUNDARY_DIRICHLET = 1,
+  TG_BOUNDARY_SLIP_WALL = 2
+} tg_boundary;
+
+/* Initial conditions a Dirichlet boundary can take its values from, with
+ * their free constants (boundary_value_params): convergence_test,
+ * weak_blast_wave, constant (compressible_euler_{2,3}d.jl);
+ * isentropic_vortex {p_inf, amplitude}, kelvin_helmholtz,
+ * taylor_green_vortex {Ma} (the elixirs of that name); gaussian_blast
+ * {p_background, energy, width}. */
+typedef enum tg_initial_condition {
+  TG_IC_CONSTANT = 0,
+  TG_IC_CONVERGENCE_TEST = 1,
+  TG_IC_ISENTROPIC_VORTEX = 2,
+  TG_IC_WEAK_BLAST_WAVE = 3,
+  TG_IC_KELVIN_HELMHOLTZ = 4,
+  TG_IC_TAYLOR_GREEN = 5,
+  TG_IC_GAUSSIAN_BLAST = 6
+} tg_initial_condition;
+
 typedef struct tg_config {
   int32_t ndims;            /* 2 or 3 */
   int32_t polydeg;          /* 1..7 (LobattoLegendreBasis) */
@@ -121,6 +147,16 @@ typedef struct tg_config {
   const double* node_coordinates;  /* [ndims, n^ndims, nelements]; may be NULL
                                       when source_terms == TG_SOURCE_NONE */
   int32_t elements_per_block;      /* 0 = library default */
+  /* Non-periodic meshes (TreeMesh periodicity = false): the boundary
+   * condition of each direction (-x, +x, -y, +y[, -z, +z]), applied on the
+   * element faces that no interface covers; all TG_BOUNDARY_PERIODIC (0)
+   * for periodic meshes.  Dirichlet faces take the values of
+   * boundary_value_function (tg_initial_condition) with its free constants
+   * boundary_value_params at the boundary node and the stage time; they need
+   * node_coordinates. */
+  int32_t boundary_conditions[6];
+  int32_t boundary_value_function;
+  double boundary_value_params[4];
 } tg_config;
 
 typedef struct tg_ctx tg_ctx;

@@ -23,6 +23,7 @@ _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 VI_WEAK, VI_FLUXDIFF, VI_SHOCKCAPTURING_HG = 0, 1, 2
 FLUX_CENTRAL, FLUX_RANOCHA, FLUX_SHIMA_ETAL, FLUX_LAX_FRIEDRICHS, FLUX_LAX_FRIEDRICHS_NAIVE = range(5)
 SRC_NONE, SRC_CONVERGENCE_TEST = 0, 1
+BC_PERIODIC, BC_DIRICHLET, BC_SLIP_WALL = 0, 1, 2
 (IC_CONSTANT, IC_CONVERGENCE_TEST, IC_ISENTROPIC_VORTEX, IC_WEAK_BLAST_WAVE,
  IC_KELVIN_HELMHOLTZ, IC_TAYLOR_GREEN, IC_GAUSSIAN_BLAST) = range(7)
 
@@ -68,6 +69,8 @@ def _load():
     lib.orc_integrals.argtypes = [vp, P(d), P(d)]
     lib.orc_entropy_timederivative.restype = d
     lib.orc_entropy_timederivative.argtypes = [vp, P(d), d]
+    lib.orc_set_boundaries.restype = i
+    lib.orc_set_boundaries.argtypes = [vp, P(i), i, P(d)]
     _lib = lib
     return lib
 
@@ -197,6 +200,22 @@ def _entropy_timederivative(self, u, t=0.0):
 
 
 Oracle.entropy_timederivative = _entropy_timederivative
+
+
+def _set_boundaries(self, bc, ic=0, params=None):
+    """periodicity = false: boundary condition per direction (-x, +x, -y, ...),
+    BC_DIRICHLET with the values of initial condition `ic`, or BC_SLIP_WALL."""
+    codes = np.ascontiguousarray(bc, dtype=np.int32)
+    assert codes.size == 2 * self.ndims
+    par = np.zeros(8)
+    if params is not None:
+        par[:len(params)] = params
+    if self.lib.orc_set_boundaries(self.h, _p(codes, ctypes.c_int), int(ic), _p(par)) != 0:
+        raise ValueError("oracle: invalid boundary condition")
+    self.ninterfaces = self.lib.orc_ninterfaces(self.h)
+
+
+Oracle.set_boundaries = _set_boundaries
 
 
 def set_threads(n: int) -> None:

@@ -39,6 +39,7 @@ enum Flux {
   FLUX_LAX_FRIEDRICHS_NAIVE = 4,  // FluxLaxFriedrichs(max_abs_speed_naive)
 };
 enum Source { SRC_NONE = 0, SRC_CONVERGENCE_TEST = 1 };
+enum Boundary { BC_PERIODIC = 0, BC_DIRICHLET = 1, BC_SLIP_WALL = 2 };
 enum InitialCondition {
   IC_CONSTANT = 0,
   IC_CONVERGENCE_TEST = 1,
@@ -573,7 +574,9 @@ static void initial_condition(const Eq& eq, int ic, const double* par, const dou
 }
 
 // ---------------------------------------------------------------------------
-// Mesh: uniformly refined periodic TreeMesh
+// Mesh: uniformly refined TreeMesh, periodic or not (periodicity = false:
+// faces at the domain edges have no neighbour and become boundaries,
+// containers_2d.jl:355-421, 475-532)
 //   src/meshes/tree_mesh.jl:128-185, abstract_tree.jl:122-130, 206-248, 668-674,
 //   src/solvers/dgsem_tree/containers_2d.jl:85-127, 228-284 (3d: 87, 229)
 // ---------------------------------------------------------------------------
@@ -615,7 +618,7 @@ static void refine_dfs(Mesh& m, int level, int maxlevel, const double* c, double
 }
 
 static Mesh make_mesh(int D, int level, const double* xmin, const double* xmax,
-                      const Basis& b) {
+                      const Basis& b, bool periodic = true) {
   Mesh m;
   m.D = D;
   m.level = level;
@@ -659,11 +662,15 @@ static Mesh make_mesh(int D, int level, const double* xmin, const double* xmax,
     for (int dir = 0; dir < 2 * D; ++dir) {
       int c[3] = {m.cart[3 * e], m.cart[3 * e + 1], m.cart[3 * e + 2]};
       const int d = dir / 2;
-      c[d] = (c[d] + (dir % 2 ? 1 : m.M - 1)) % m.M;
+      const int cn = c[d] + (dir % 2 ? 1 : -1);
+      if (!periodic && (cn < 0 || cn >= m.M)) continue;  // boundary face
+      c[d] = (cn + m.M) % m.M;
       m.nbr[e * 2 * D + dir] = c2e[lin(c[0], c[1], c[2])];
     }
-    // init_interfaces!: per element in order, positive directions only
+    // init_interfaces!: per element in order, positive directions only, where
+    // a neighbour exists
     for (int d = 0; d < D; ++d) {
+      if (m.nbr[e * 2 * D + 2 * d + 1] < 0) continue;
       m.if_left.push_back(e);
       m.if_right.push_back(m.nbr[e * 2 * D + 2 * d + 1]);
       m.if_orient.push_back(d);
@@ -687,6 +694,12 @@ struct Solver {
   double alpha_max = 0.5, alpha_min = 0.001;
   bool alpha_smooth = true;
   int source = SRC_NONE;
+  // boundary conditions per direction (0:-x, 1:+x, 2:-y, ...) of a
+  // non-periodic mesh, and the initial condition that Dirichlet faces use
+  bool periodic = true;
+  int bc[6] = {0, 0, 0, 0, 0, 0};
+  int bc_ic = 0;
+  double bc_par[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   std::vector<double> alpha, alpha_tmp, sfv;  // sfv: [NV, n^(D-1), 2D, E]
   int64_t ndofs() const { return (int64_t)nn * m.nelem; }
 };
@@ -843,7 +856,42 @@ static void fv_volume(const Solver& s, double* du, const double* u, int64_t e, d
   }
 }
 
-// rhs_hyperbolic!, dg_2d.jl:113-186 (periodic, conforming: no boundaries/mortars)
+// Boundary flux of one face node: BoundaryConditionDirichlet (equations.jl:164-182,
+// u_inner left of the face on + faces) or boundary_condition_slip_wall on a
+// TreeMesh (compressible_euler_2d.jl:322-393, 3d.jl:315-416): p* from the 1D
+// pressure Riemann problem on the outward normal velocity, flux p* in the
+// normal momentum and zero elsewhere.
+static void boundary_flux(const Solver& s, int bc, const double* ui, int o, int side,
+                          const double* x, double t, double* F) {
+  const Eq& eq = s.eq;
+  if (bc == BC_DIRICHLET) {
+    double ub[5];
+    initial_condition(eq, s.bc_ic, s.bc_par, x, t, ub);
+    if (side)
+      two_point_flux(eq, s.sflux, ui, ub, o, F);
+    else
+      two_point_flux(eq, s.sflux, ub, ui, o, F);
+    return;
+  }
+  double w[5];
+  cons2prim(eq, ui, w);
+  const double rho = w[0], p = w[eq.NV - 1], g = eq.gamma;
+  const double vn = side ? w[1 + o] : -w[1 + o];
+  double p_star;
+  if (vn <= 0) {
+    const double c = std::sqrt(g * p / rho);
+    const double base = 1 + 0.5 * (g - 1) * vn / c;
+    p_star = base >= 0 ? p * std::pow(base, 2 * g * eq.inv_gamma_minus_one) : 0.0;
+  } else {
+    const double A = 2 / ((g + 1) * rho);
+    const double B = p * (g - 1) / (g + 1);
+    p_star = p + 0.5 * vn / A * (vn + std::sqrt(vn * vn + 4 * A * (p + B)));
+  }
+  for (int v = 0; v < eq.NV; ++v) F[v] = 0.0;
+  F[1 + o] = p_star;
+}
+
+// rhs_hyperbolic!, dg_2d.jl:113-186 (conforming: no mortars)
 static void rhs(Solver& s, double* du, const double* u, double t) {
   const int n = s.b.n, D = s.eq.D, NV = s.eq.NV, nn = s.nn;
   const int64_t E = s.m.nelem;
@@ -893,6 +941,25 @@ static void rhs(Solver& s, double* du, const double* u, double t) {
         s.sfv[sidx(r, 2 * o, fn, v)] = F[v];
       }
     }
+  }
+  // prolong2boundaries! + calc_boundary_flux!, dg_2d.jl:680-717, 795-860
+  if (!s.periodic) {
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < E; ++e)
+      for (int dir = 0; dir < 2 * D; ++dir) {
+        if (s.m.nbr[e * 2 * D + dir] >= 0) continue;
+        const int o = dir / 2, side = dir % 2;
+        int stride = 1;
+        for (int q = 0; q < o; ++q) stride *= n;
+        for (int fn = 0; fn < nf; ++fn) {
+          const int lo = fn % stride, hi = fn / stride;
+          const int node = lo + hi * stride * n + (side ? (n - 1) * stride : 0);
+          double F[5];
+          boundary_flux(s, s.bc[dir], &u[uidx(s, e, node, 0)], o, side,
+                        &s.m.node_coords[((size_t)e * nn + node) * D], t, F);
+          for (int v = 0; v < NV; ++v) s.sfv[sidx(e, dir, fn, v)] = F[v];
+        }
+      }
   }
   // calc_surface_integral!, dg_2d.jl:1245-1287; apply_jacobian!, dg_2d.jl:1345-1363;
   // calc_sources!, dg_2d.jl:1366-1386
@@ -1008,6 +1075,26 @@ void* orc_create(int ndims, int polydeg, int level, const double* xmin, const do
 }
 
 void orc_destroy(void* h) { delete (Solver*)h; }
+
+// periodicity = false with boundary conditions per direction (BC_DIRICHLET
+// takes the values of initial condition `ic` with `params`, BC_SLIP_WALL);
+// rebuilds the interfaces.  Returns 0, or -1 for an invalid code.
+int orc_set_boundaries(void* h, const int* bc, int ic, const double* params) {
+  Solver& s = *(Solver*)h;
+  for (int dir = 0; dir < 2 * s.eq.D; ++dir)
+    if (bc[dir] != BC_DIRICHLET && bc[dir] != BC_SLIP_WALL) return -1;
+  double xmin[3], xmax[3];
+  for (int d = 0; d < s.eq.D; ++d) {
+    xmin[d] = s.m.xmin[d];
+    xmax[d] = s.m.xmin[d] + s.m.length0;
+  }
+  s.m = make_mesh(s.eq.D, s.m.level, xmin, xmax, s.b, false);
+  s.periodic = false;
+  for (int dir = 0; dir < 2 * s.eq.D; ++dir) s.bc[dir] = bc[dir];
+  s.bc_ic = ic;
+  for (int k = 0; k < 8; ++k) s.bc_par[k] = params ? params[k] : 0.0;
+  return 0;
+}
 
 void orc_set_threads(int n) {
 #ifdef _OPENMP

@@ -16,11 +16,15 @@ def oracle_from_case(O, c, **over):
     fl = dict(central=O.FLUX_CENTRAL, ranocha=O.FLUX_RANOCHA, shima_etal=O.FLUX_SHIMA_ETAL,
               llf=O.FLUX_LAX_FRIEDRICHS, llf_naive=O.FLUX_LAX_FRIEDRICHS_NAIVE)
     src = O.SRC_CONVERGENCE_TEST if c.get("source") == "convergence_test" else O.SRC_NONE
-    return O.Oracle(c["ndims"], c["polydeg"], c["level"], c["xmin"], c["xmax"],
-                    volume_integral=vi, volume_flux=fl[c["volume_flux"]],
-                    surface_flux=fl[c["surface_flux"]],
-                    alpha_max=c.get("alpha_max", 0.5), alpha_min=c.get("alpha_min", 0.001),
-                    alpha_smooth=c.get("alpha_smooth", True), source=src)
+    orc = O.Oracle(c["ndims"], c["polydeg"], c["level"], c["xmin"], c["xmax"],
+                   volume_integral=vi, volume_flux=fl[c["volume_flux"]],
+                   surface_flux=fl[c["surface_flux"]],
+                   alpha_max=c.get("alpha_max", 0.5), alpha_min=c.get("alpha_min", 0.001),
+                   alpha_smooth=c.get("alpha_smooth", True), source=src)
+    if c.get("boundary"):
+        code = dict(dirichlet=O.BC_DIRICHLET, slip_wall=O.BC_SLIP_WALL)[c["boundary"]]
+        orc.set_boundaries([code] * (2 * c["ndims"]), ic_id(O, c["ic"]), c.get("ic_params"))
+    return orc
 
 
 def ic_id(O, name):

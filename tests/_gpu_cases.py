@@ -42,11 +42,15 @@ def build(c, precision="fp64", elements_per_block=0):
         vi = T.VolumeIntegralShockCapturingHG(ind, volume_flux_dg=vflux, volume_flux_fv=sflux)
         ovi = O.VI_SHOCKCAPTURING_HG
     solver = T.DGSEM(basis, sflux, vi)
-    mesh = T.TreeMesh(c["xmin"], c["xmax"], initial_refinement_level=c["level"])
+    boundary = c.get("boundary")
+    mesh = T.TreeMesh(c["xmin"], c["xmax"], initial_refinement_level=c["level"],
+                      periodicity=boundary is None)
     src = T.source_terms_convergence_test if c.get("source") == "convergence_test" else None
     ic = IC[c["ic"]][0](c.get("ic_params"))
+    bcs = {None: T.boundary_condition_periodic, "slip_wall": T.boundary_condition_slip_wall,
+           "dirichlet": T.BoundaryConditionDirichlet(ic)}[boundary]
     semi = T.SemidiscretizationHyperbolic(mesh, eq, ic, solver, source_terms=src,
-                                          precision=precision,
+                                          boundary_conditions=bcs, precision=precision,
                                           elements_per_block=elements_per_block)
     orc = O.Oracle(D, c["polydeg"], c["level"], c["xmin"], c["xmax"], volume_integral=ovi,
                    volume_flux=FLUX[c.get("volume_flux", "central")][1],
@@ -54,6 +58,9 @@ def build(c, precision="fp64", elements_per_block=0):
                    alpha_max=c.get("alpha_max", 0.5), alpha_min=c.get("alpha_min", 0.001),
                    alpha_smooth=c.get("alpha_smooth", True),
                    source=O.SRC_CONVERGENCE_TEST if src is not None else O.SRC_NONE)
+    if boundary is not None:
+        code = dict(dirichlet=O.BC_DIRICHLET, slip_wall=O.BC_SLIP_WALL)[boundary]
+        orc.set_boundaries([code] * (2 * D), IC[c["ic"]][1], c.get("ic_params"))
     return semi, orc
 
 

@@ -32,6 +32,20 @@ CASES = {
         ndims=2, polydeg=3, level=5, xmin=[-2.0, -2.0], xmax=[2.0, 2.0],
         ic="weak_blast_wave", source="none", vi="fluxdiff",
         volume_flux="ranocha", surface_flux="ranocha", cfl=1.0, tspan=[0.0, 0.4]),
+    "TreeMesh2D Euler: elixir_euler_source_terms_nonperiodic.jl": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_source_terms_nonperiodic.jl",
+        ndims=2, polydeg=3, level=4, xmin=[0.0, 0.0], xmax=[2.0, 2.0],
+        ic="convergence_test", source="convergence_test", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=1.0, tspan=[0.0, 2.0],
+        boundary="dirichlet"),
+    "TreeMesh2D Euler: elixir_euler_ec.jl with boundary_condition_slip_wall": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_ec.jl",
+        ndims=2, polydeg=3, level=5, xmin=[-2.0, -2.0], xmax=[2.0, 2.0],
+        ic="weak_blast_wave", source="none", vi="fluxdiff",
+        volume_flux="ranocha", surface_flux="ranocha", cfl=0.3, tspan=[0.0, 0.1],
+        boundary="slip_wall"),
     "TreeMesh2D Euler: elixir_euler_shockcapturing.jl": dict(
         file="test/test_tree_2d_euler.jl",
         elixir="examples/tree_2d_dgsem/elixir_euler_shockcapturing.jl",

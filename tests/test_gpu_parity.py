@@ -183,7 +183,8 @@ def test_gpu_free_stream_golden_one_step():
 
 
 @pytest.mark.parametrize("name", ["TreeMesh3D Euler: elixir_euler_source_terms.jl",
-                                  "TreeMesh2D Euler: elixir_euler_source_terms.jl"])
+                                  "TreeMesh2D Euler: elixir_euler_source_terms.jl",
+                                  "TreeMesh2D Euler: elixir_euler_source_terms_nonperiodic.jl"])
 def test_mixed_precision_error_within_1p1x_of_fp64(name):
     c = dict(GOLDENS[name])
     errs = {}
@@ -290,3 +291,54 @@ def test_mixed_pinned_and_pageable_transfers_agree():
     ctx.step(2, 0.6, 10.0, 0.0)
     ctx.download(pin_out.data_ptr())
     np.testing.assert_array_equal(pin_out.numpy().reshape(ref.shape), ref_stepped)
+
+
+
+BOUNDARY_CASES = [
+    dict(ndims=2, polydeg=3, level=3, xmin=[0, 0], xmax=[2, 2], vi="weak", surface_flux="llf_naive",
+         ic="convergence_test", source="convergence_test", boundary="dirichlet"),
+    dict(ndims=2, polydeg=3, level=3, xmin=[-2, -2], xmax=[2, 2], vi="fluxdiff",
+         volume_flux="ranocha", surface_flux="ranocha", ic="weak_blast_wave", boundary="slip_wall"),
+    dict(ndims=2, polydeg=3, level=3, xmin=[-2, -2], xmax=[2, 2], vi="hg", volume_flux="ranocha",
+         surface_flux="llf", ic="weak_blast_wave", boundary="slip_wall"),
+    dict(ndims=2, polydeg=3, level=3, xmin=[-2, -2], xmax=[2, 2], vi="fluxdiff",
+         volume_flux="ranocha", surface_flux="llf", ic="weak_blast_wave", boundary="dirichlet"),
+    dict(ndims=3, polydeg=3, level=2, xmin=[0] * 3, xmax=[2] * 3, vi="fluxdiff",
+         volume_flux="ranocha", surface_flux="llf", ic="convergence_test",
+         source="convergence_test", boundary="dirichlet"),
+    dict(ndims=3, polydeg=2, level=2, xmin=[-2] * 3, xmax=[2] * 3, vi="fluxdiff",
+         volume_flux="ranocha", surface_flux="llf_naive", ic="weak_blast_wave", boundary="slip_wall"),
+]
+
+
+def _bid(c):
+    return f"{c['ndims']}d-p{c['polydeg']}-{c['vi']}-{c['surface_flux']}-{c['boundary']}"
+
+
+@pytest.mark.parametrize("c", BOUNDARY_CASES, ids=_bid)
+def test_nonperiodic_rhs_fp64_matches_oracle(c):
+    semi, orc = build(c)
+    u = perturbed_state(semi, seed=47)
+    np.testing.assert_array_less(rel_err(semi.device_context.rhs_host(u, 0.41), orc.rhs(u, 0.41)), 1e-12)
+
+
+@pytest.mark.parametrize("c", BOUNDARY_CASES, ids=_bid)
+def test_nonperiodic_rhs_mixed_close_to_oracle(c):
+    semi, orc = build(c, precision="mixed")
+    u = perturbed_state(semi, seed=47)
+    assert rel_err(semi.device_context.rhs_host(u, 0.41), orc.rhs(u, 0.41)) < 2e-4
+
+
+@pytest.mark.parametrize("c", BOUNDARY_CASES[:2], ids=_bid)
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_nonperiodic_steps_match_oracle(c, precision):
+    semi, orc = build(c, precision=precision)
+    u0 = semi.compute_coefficients(0.0)
+    ctx = semi.device_context
+    ctx.upload(u0)
+    t, n = ctx.step(6, 0.5, 10.0, 0.0)
+    ref, t_ref, n_ref = orc.solve(u0, 0.0, 10.0, 0.5, max_steps=6)
+    assert n == n_ref == 6
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    assert abs(t - t_ref) <= tol * t_ref
+    assert rel_err(ctx.download(), ref) < tol

@@ -89,3 +89,34 @@ def test_error_norms_match_oracle():
     ol2, olinf = orc.error_norms(u, 0.25, O.IC_CONVERGENCE_TEST)
     np.testing.assert_allclose(l2, ol2, rtol=1e-12)
     np.testing.assert_allclose(linf, olinf, rtol=1e-12)
+
+
+@pytest.mark.parametrize("ndims,level", [(2, 2), (3, 1)])
+def test_nonperiodic_treemesh_interfaces_match_oracle(ndims, level):
+    # periodicity = false: faces at the domain edge have no interface
+    xmin, xmax = [0.0] * ndims, [2.0] * ndims
+    mesh = T.TreeMesh(xmin, xmax, initial_refinement_level=level, periodicity=False)
+    eq = T.CompressibleEulerEquations2D(1.4) if ndims == 2 else T.CompressibleEulerEquations3D(1.4)
+    semi = T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_convergence_test,
+                                          T.DGSEM(polydeg=3),
+                                          boundary_conditions=T.boundary_condition_slip_wall)
+    orc = O.Oracle(ndims, 3, level, xmin, xmax)
+    orc.set_boundaries([O.BC_SLIP_WALL] * (2 * ndims))
+    m = orc.mesh()
+    np.testing.assert_array_equal(semi.neighbor_ids, m["neighbor_ids"])
+    np.testing.assert_array_equal(semi.orientations, m["orientations"])
+    M = 1 << level
+    assert len(semi.neighbor_ids) == ndims * (M - 1) * M ** (ndims - 1)
+
+
+def test_boundary_conditions_must_match_periodicity():
+    eq = T.CompressibleEulerEquations2D(1.4)
+    with pytest.raises(ValueError):
+        T.SemidiscretizationHyperbolic(T.TreeMesh((0, 0), (1, 1), initial_refinement_level=1),
+                                       eq, T.initial_condition_convergence_test, T.DGSEM(polydeg=3),
+                                       boundary_conditions=T.boundary_condition_slip_wall)
+    with pytest.raises(ValueError):
+        T.SemidiscretizationHyperbolic(
+            T.TreeMesh((0, 0), (1, 1), initial_refinement_level=1, periodicity=(True, False)),
+            eq, T.initial_condition_convergence_test, T.DGSEM(polydeg=3),
+            boundary_conditions=T.boundary_condition_slip_wall)

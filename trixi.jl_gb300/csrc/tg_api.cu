@@ -344,6 +344,53 @@ __global__ void sum_rows_kernel(const double* __restrict__ partial, int64_t E, i
   }
 }
 
+// Boundary pre-pass of a mixed context (calc_boundary_flux!, dg_2d.jl:795-860,
+// evaluated for the stage's input state): for every node of every boundary
+// face, in FP64, the Dirichlet state (the initial condition at the node and
+// the stage time t + c dt) or the slip-wall flux, stored as float-float pairs
+// for the stage kernel, which reads them like a neighbour's trace.
+template <int D>
+__global__ void boundary_ghost_kernel(const DgParams P, const float2* __restrict__ u,
+                                      const int32_t* __restrict__ bface, int64_t B, int N,
+                                      const Clock* clock, double c_s, double t_rhs, int mode,
+                                      float2* __restrict__ ghost) {
+  constexpr int NV = D + 2;
+  const int NF = D == 2 ? N : N * N;
+  const int NN = NF * N;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= B * NF) return;
+  const int64_t b = k / NF;
+  const int fn = (int)(k - b * NF);
+  const int64_t e = bface[2 * b];
+  const int dir = bface[2 * b + 1];
+  const int d = dir >> 1, side = dir & 1;
+  const int S = d == 0 ? 1 : (d == 1 ? N : N * N);
+  const int node = (fn % S) + (fn / S) * S * N + (side ? (N - 1) * S : 0);
+  double out[NV];
+  if (P.bc[dir] == BC_SLIP_WALL) {
+    const float2* p = u + ((size_t)e * NN + node) * NV;
+    double ui[NV], w[NV];
+    for (int v = 0; v < NV; ++v) ui[v] = (double)p[v].x + (double)p[v].y;
+    Euler<D, double>::cons2prim(ui, w, P.gamma);
+    const double vn = side ? w[1 + d] : -w[1 + d];  // outward normal velocity
+    const double ps = slip_wall_pressure<double>(w[0], vn, w[NV - 1], P.gamma, P.inv_gamma_minus_one);
+    for (int v = 0; v < NV; ++v) out[v] = 0.0;
+    out[1 + d] = ps;
+  } else {
+    double x[D];
+    for (int q = 0; q < D; ++q) {
+      const int Sq = q == 0 ? 1 : (q == 1 ? N : N * N);
+      x[q] = P.xline[((size_t)e * D + q) * N + (node / Sq) % N];
+    }
+    const double t = mode == MODE_RHS ? t_rhs : clock->t + c_s * clock->dt;
+    boundary_value<D>(P.bc_ic, P.bc_par, x, t, P.gamma, out);
+  }
+  for (int v = 0; v < NV; ++v) {
+    const float hi = (float)out[v];
+    ghost[k * NV + v] = make_float2(hi, (float)(out[v] - (double)hi));
+  }
+}
+
 // apply_smoothing! as a gather (indicators_2d.jl:104-136): alpha_e =
 // max(raw_e, 0.5 * raw_n for every face neighbour n).
 template <typename R>
@@ -353,7 +400,10 @@ __global__ void smooth_alpha_kernel(const R* __restrict__ raw, const int32_t* __
   if (e >= E) return;
   R a = raw[e];
   if (smooth)
-    for (int f = 0; f < nfaces; ++f) a = fmax(a, R(0.5) * raw[nbr[e * nfaces + f]]);
+    for (int f = 0; f < nfaces; ++f) {
+      const int32_t nb = nbr[e * nfaces + f];  // interfaces only
+      if (nb >= 0) a = fmax(a, R(0.5) * raw[nb]);
+    }
   out[e] = (double)a;
 }
 
@@ -385,6 +435,9 @@ struct tg_ctx {
   float* d_xline_f = nullptr;
   float4* d_sc0 = nullptr;            // mixed source phase of each element's first node
   float4* d_scn = nullptr;            // and of the node offsets (one table)
+  int64_t nbound = 0;                 // boundary faces (non-periodic meshes)
+  int32_t* d_bface = nullptr;         // [nbound][2]: element, direction
+  float2* d_ghost = nullptr;          // mixed: [nbound][NF][NV] boundary pre-pass output
   double* d_weights = nullptr;
   double* d_partial = nullptr;
   double* d_sums = nullptr;
@@ -436,7 +489,7 @@ static void free_ctx(tg_ctx* c) {
     if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
   void* ptrs[] = {c->d_u[0], c->d_u[1], c->d_utmp, c->d_du, c->d_uscratch, c->d_stage64,
                   c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_nbr, c->d_invj, c->d_xline,
-                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_weights, c->d_partial, c->d_sums, c->d_clock,
+                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_weights, c->d_partial, c->d_sums, c->d_clock,
                   c->d_status, c->d_speed};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -549,6 +602,20 @@ static int launch_kernel(tg_ctx* c, int mode, const void* u_in, void* u_out, dou
       A.cos_tl = (float)(cs - (double)A.cos_t);
     }
     A.speed_bits = reduce ? &c->d_clock->speed_bits : nullptr;
+    if (c->nbound > 0) {
+      // boundary pre-pass for this stage's input state
+      const int64_t nk = c->nbound * (c->NN / c->N);
+      const unsigned nb = (unsigned)((nk + 127) / 128);
+      const double cs = mode == MODE_STAGE ? CK_C[stage] : 0.0;
+      if (c->D == 2)
+        boundary_ghost_kernel<2><<<nb, 128, 0, c->stream>>>(c->P, (const float2*)u_in, c->d_bface,
+                                                            c->nbound, c->N, c->d_clock, cs, t_rhs,
+                                                            mode, c->d_ghost);
+      else
+        boundary_ghost_kernel<3><<<nb, 128, 0, c->stream>>>(c->P, (const float2*)u_in, c->d_bface,
+                                                            c->nbound, c->N, c->d_clock, cs, t_rhs,
+                                                            mode, c->d_ghost);
+    }
     rc = launch_mixed(c->D, c->N, c->vi, c->epb, c->MP, A, c->stream);
   }
   if (rc != 0) {
@@ -704,12 +771,40 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     a = (int32_t)r;
     b = (int32_t)l;
   }
+  // faces without interface are boundaries of a non-periodic mesh and need a
+  // boundary condition for their direction
+  bool has_dirichlet = false;
+  for (int dir = 0; dir < nf; ++dir) {
+    const int bc = cfg->boundary_conditions[dir];
+    if (bc < TG_BOUNDARY_PERIODIC || bc > TG_BOUNDARY_SLIP_WALL) {
+      delete c;
+      return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "boundary condition %d of direction %d", bc, dir);
+    }
+    has_dirichlet |= bc == TG_BOUNDARY_DIRICHLET;
+  }
   for (size_t k = 0; k < nbr.size(); ++k)
-    if (nbr[k] < 0) {
+    if (nbr[k] < 0 && cfg->boundary_conditions[k % nf] == TG_BOUNDARY_PERIODIC) {
       delete c;
       return fail(nullptr, TG_ERR_UNSUPPORTED,
-                  "element face without interface: only periodic conforming meshes");
+                  "element face without interface and without a boundary condition for "
+                  "direction %d (conforming meshes only: no mortars)", (int)(k % nf));
     }
+  if (has_dirichlet && (!cfg->node_coordinates || cfg->boundary_value_function < TG_IC_CONSTANT ||
+                        cfg->boundary_value_function > TG_IC_GAUSSIAN_BLAST)) {
+    delete c;
+    return fail(nullptr, TG_ERR_INVALID_ARGUMENT,
+                "Dirichlet boundaries need node coordinates and a valid boundary_value_function");
+  }
+  // boundary faces: numbered in element order, nbr = -1 - number
+  std::vector<int32_t> bface;
+  for (size_t k = 0; k < nbr.size(); ++k)
+    if (nbr[k] < 0) {
+      const int32_t b = (int32_t)(bface.size() / 2);
+      bface.push_back((int32_t)(k / nf));
+      bface.push_back((int32_t)(k % nf));
+      nbr[k] = -1 - b;
+    }
+  c->nbound = (int64_t)bface.size() / 2;
 
   // ---- node coordinates along each axis (tensor-product TreeMesh elements) ----
   std::vector<double> xline;
@@ -756,6 +851,9 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   P.surface_flux = cfg->surface_flux;
   P.fv_flux = cfg->volume_flux_fv;
   P.source = cfg->source_terms;
+  for (int dir = 0; dir < 6; ++dir) P.bc[dir] = dir < nf ? cfg->boundary_conditions[dir] : 0;
+  P.bc_ic = cfg->boundary_value_function;
+  for (int k = 0; k < 4; ++k) P.bc_par[k] = cfg->boundary_value_params[k];
   P.alpha_max = cfg->alpha_max;
   P.alpha_min = cfg->alpha_min;
   P.alpha_smooth = cfg->alpha_smooth;
@@ -790,6 +888,10 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   ALLOC(c->d_u[1], vb);
   ALLOC(c->d_utmp, rsize(c) * (size_t)c->nvalues);
   ALLOC(c->d_nbr, sizeof(int32_t) * nbr.size());
+  if (c->nbound > 0) {
+    ALLOC(c->d_bface, sizeof(int32_t) * bface.size());
+    if (!c->fp64) ALLOC(c->d_ghost, sizeof(float2) * (size_t)c->nbound * (c->NN / N) * c->NV);
+  }
   ALLOC(c->d_invj, sizeof(double) * c->E);
   ALLOC(c->d_weights, sizeof(double) * N);
   ALLOC(c->d_clock, sizeof(Clock));
@@ -862,6 +964,8 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     }
   }
   cudaMemcpy(c->d_nbr, nbr.data(), sizeof(int32_t) * nbr.size(), cudaMemcpyHostToDevice);
+  if (c->nbound > 0)
+    cudaMemcpy(c->d_bface, bface.data(), sizeof(int32_t) * bface.size(), cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_invj, cfg->inverse_jacobian, sizeof(double) * c->E, cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_weights, c->weights.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
   if (!xline.empty())
@@ -908,6 +1012,12 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   M.xline = c->d_xline_f;
   M.sc0 = c->d_sc0;
   M.scn = c->d_scn;
+  M.has_wall = 0;
+  for (int dir = 0; dir < 6; ++dir) {
+    M.bc[dir] = P.bc[dir];
+    M.has_wall |= P.bc[dir] == BC_SLIP_WALL;
+  }
+  M.ghost = c->d_ghost;
   *out = c;
   return TG_OK;
 }

@@ -52,9 +52,13 @@ struct DgParams {
   int32_t volume_flux, surface_flux, fv_flux, source;
   double alpha_max, alpha_min, alpha_atol, hg_threshold, hg_parameter_s;
   int32_t alpha_smooth;
-  const int32_t* nbr;     // [E][2D] neighbour across face (-x,+x,-y,+y,-z,+z)
+  const int32_t* nbr;     // [E][2D] neighbour across face (-x,+x,-y,+y,-z,+z), -1: boundary
   const double* inv_jac;  // [E]
   const double* xline;    // [E][D][N] node coordinates along each axis, or null
+  // boundary conditions of the faces with nbr < 0 (non-periodic meshes)
+  int32_t bc[6];          // per direction, BoundaryKind
+  int32_t bc_ic;          // Dirichlet values: InitialConditionKind
+  double bc_par[4];       // and its free constants
 };
 
 // Device-resident clock of the time loop (one per context).
@@ -149,6 +153,42 @@ struct ElementKernel {
   }
 };
 
+// Flux through face node `node` of element e on a face without neighbour
+// (prolong2boundaries! + calc_boundary_flux!, dg_2d.jl:680-717, 795-860):
+// BoundaryConditionDirichlet with the initial condition's values at the node
+// and the stage time (u_inner left of + faces), or boundary_condition_slip_wall.
+template <int D, int N, typename R>
+__device__ inline void boundary_face_flux(const DgParams& P, const StageArgs& A, int64_t e,
+                                          int node, int d, int side, const R* uo, R gamma,
+                                          R igm1, R* F) {
+  using Eu = Euler<D, R>;
+  constexpr int NV = D + 2;
+  R wo[NV];
+  Eu::cons2prim(uo, wo, gamma);
+  if (P.bc[2 * d + side] == BC_SLIP_WALL) {
+    const R vn = side ? wo[1 + d] : -wo[1 + d];  // outward normal velocity
+    const R ps = slip_wall_pressure<R>(wo[0], vn, wo[NV - 1], gamma, igm1);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) F[v] = R(0);
+    F[1 + d] = ps;
+    return;
+  }
+  double x[D];
+#pragma unroll
+  for (int q = 0; q < D; ++q) x[q] = P.xline[((size_t)e * D + q) * N + axis_index<N>(node, q)];
+  const double t = A.mode == MODE_RHS ? A.t_rhs : A.clock->t + A.c * A.clock->dt;
+  double ubd[NV];
+  boundary_value<D>(P.bc_ic, P.bc_par, x, t, P.gamma, ubd);
+  R ub[NV], wb[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) ub[v] = (R)ubd[v];
+  Eu::cons2prim(ub, wb, gamma);
+  if (side)
+    Eu::two_point(P.surface_flux, uo, wo, ub, wb, d, gamma, igm1, F);
+  else
+    Eu::two_point(P.surface_flux, ub, wb, uo, wo, d, gamma, igm1, F);
+}
+
 template <int D, int N, typename R, typename RT, int VI, int EPB>
 __global__ void __launch_bounds__(EPB * Pow<N, D>::value)
     dg_element_kernel(const DgParams P, const StageArgs A) {
@@ -204,7 +244,10 @@ __global__ void __launch_bounds__(EPB * Pow<N, D>::value)
     R a = raw[e];
     if (P.alpha_smooth) {
 #pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) a = fmax(a, R(0.5) * raw[P.nbr[e * 2 * D + dir]]);
+      for (int dir = 0; dir < 2 * D; ++dir) {
+        const int32_t nb = P.nbr[e * 2 * D + dir];  // interfaces only
+        if (nb >= 0) a = fmax(a, R(0.5) * raw[nb]);
+      }
     }
     s_alpha[slot] = a;
     if (A.alpha_out) reinterpret_cast<R*>(A.alpha_out)[e] = a;
@@ -240,6 +283,12 @@ __global__ void __launch_bounds__(EPB * Pow<N, D>::value)
     R uo[NV], un[NV], ul[NV], ur[NV], wl[NV], wr[NV], F[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) uo[v] = s_c[v * SP + sl * NN + own];
+    if (nb < 0) {
+      boundary_face_flux<D, N, R>(P, A, e0 + sl, own, d, side, uo, gamma, igm1, F);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) s_face[((sl * 2 * D + dir) * NF + fn) * NV + v] = F[v];
+      continue;
+    }
     const int64_t nbs = nb - e0;
     if (nbs >= 0 && nbs < nel) {
 #pragma unroll

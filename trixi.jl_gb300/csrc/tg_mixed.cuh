@@ -63,6 +63,13 @@ struct MixedParams {
   // conforming mesh have one size)
   const float4* sc0;        // [E]
   const float4* scn;        // [NN]
+  // Non-periodic meshes: a face without neighbour has nbr = -1 - b, b its
+  // boundary-face index; ghost[b][face node][v] holds, for the current stage,
+  // the Dirichlet state (float-float) or, on slip walls (bc), the wall flux
+  // (float-float), written by a pre-pass from the stage's input state.
+  int32_t bc[6];            // per direction, BoundaryKind
+  int32_t has_wall;         // any bc == BC_SLIP_WALL
+  const float2* ghost;      // [B][NF][NV]
 };
 
 struct MixedArgs {
@@ -172,6 +179,21 @@ struct Dev {
                                                   float* du) {
 #pragma unroll
     for (int v = 0; v < NV; ++v) du[v] = ((x[v].x - R.hi[v]) + x[v].y) + R.r[v];
+  }
+
+  // A boundary flux given as float-float values (the slip-wall flux of the
+  // pre-pass) as a deviation from the reference state's physical flux along o.
+  static __device__ __forceinline__ void wall_flux(const RefState<D>& R, const float2* fw, int o,
+                                                   float vro, const EosF& eos, float* f) {
+    const float m = R.rho * vro;
+    float v2 = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) v2 += R.v[d] * R.v[d];
+    f[0] = (fw[0].x - m) + fw[0].y;
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+      f[1 + d] = (fw[1 + d].x - ((d == o) ? fmaf(m, R.v[d], R.p) : m * R.v[d])) + fw[1 + d].y;
+    f[P] = (fw[P].x - ((R.p * eos.igm1 + 0.5f * R.rho * v2) + R.p) * vro) + fw[P].y;
   }
 
   // Full primitives from deviations (nodes stored as dw + dq only).
@@ -580,31 +602,43 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
   for (int side = 0; side < 2; ++side) {
     const int dir = 2 * dd + side;
     const int64_t nb = P.nbr[e * 2 * D + dir];
-    const int64_t nbs = nb - e0;
-    const float2* src;
-    if (nbs >= 0 && nbs < nel)
-      src = s_u + ((int)nbs * NN + lb + (side ? 0 : (N - 1) * S)) * NV;
-    else
-      src = s_fu + ((slot * 2 * D + dir) * NF + line) * NV;
-    float hi[NV], lo[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      const float2 x = src[v];
-      hi[v] = x.x;
-      lo[v] = x.y;
-    }
-    Node<D> nn_;
-    Dv::make_node(hi, lo, R, eos, nn_);
-    Dv::orient(nn_, dd);
+    const int own_node = lb + (side ? (N - 1) * S : 0);
     Node<D>& own = side ? nd[N - 1] : nd[0];
-    if (!NEED_DU) Dv::node_du(s_u + ((size_t)slot * NN + lb + (side ? (N - 1) * S : 0)) * NV, R, own.du);
+    if (!NEED_DU) Dv::node_du(s_u + ((size_t)slot * NN + own_node) * NV, R, own.du);
+    // neighbour trace: in this block, or staged (other blocks, and the ghost
+    // trace of a boundary face)
+    const int64_t nbs = nb - e0;
+    const float2* src = (nb >= 0 && nbs < nel && nbs >= 0)
+                            ? s_u + ((int)nbs * NN + lb + (side ? 0 : (N - 1) * S)) * NV
+                            : s_fu + ((slot * 2 * D + dir) * NF + line) * NV;
     float F[NV];
+    // slip walls are compiled into the run-time flux kernels only: contexts
+    // with a wall use those (the flux-specialised instances keep registers
+    // for the periodic hot path)
+    bool wall = false;
+    if constexpr (SF < 0) wall = nb < 0 && P.bc[dir] == BC_SLIP_WALL;
+    if (wall) {
+      Dv::wall_flux(R, src, dd, vro, eos, F);
+    } else {
+      float hi[NV], lo[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const float2 x = src[v];
+        hi[v] = x.x;
+        lo[v] = x.y;
+      }
+      Node<D> nn_;
+      Dv::make_node(hi, lo, R, eos, nn_);
+      Dv::orient(nn_, dd);
+      if (side)
+        Dv::template flux2<SF>(P.surface_flux, R, own, nn_, dd, vro, eos, F);
+      else
+        Dv::template flux2<SF>(P.surface_flux, R, nn_, own, dd, vro, eos, F);
+    }
     if (side) {
-      Dv::template flux2<SF>(P.surface_flux, R, own, nn_, dd, vro, eos, F);
 #pragma unroll
       for (int v = 0; v < NV; ++v) acc[N - 1][v] = fmaf(F[v], factor, acc[N - 1][v]);
     } else {
-      Dv::template flux2<SF>(P.surface_flux, R, nn_, own, dd, vro, eos, F);
 #pragma unroll
       for (int v = 0; v < NV; ++v) acc[0][v] = fmaf(-F[v], factor, acc[0][v]);
     }
@@ -681,10 +715,11 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
     const int dir = rem / NF;
     const int fn = rem - dir * NF;
     const int64_t nb = P.nbr[(e0 + sl) * 2 * D + dir];
-    if (nb >= e0 && nb < e0 + nel) continue;
+    if (nb >= e0 && nb < e0 + nel) continue;  // in this block
     const int dd = dir >> 1;
     const int nnode = line_base<N>(fn, dd) + ((dir & 1) ? 0 : (N - 1) * axis_stride<N>(dd));
-    const float2* g = A.u_in + ((size_t)nb * NN + nnode) * NV;
+    const float2* g = nb >= 0 ? A.u_in + ((size_t)nb * NN + nnode) * NV
+                              : P.ghost + ((size_t)(-1 - nb) * NF + fn) * NV;  // boundary face
 #pragma unroll
     for (int v = 0; v < NV; ++v) cp_async8(s_fu + k * NV + v, g + v);
   }
@@ -710,7 +745,10 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
       float a = A.alpha_raw[e];
       if (P.alpha_smooth) {
 #pragma unroll
-        for (int dir = 0; dir < 2 * D; ++dir) a = fmaxf(a, 0.5f * A.alpha_raw[P.nbr[e * 2 * D + dir]]);
+        for (int dir = 0; dir < 2 * D; ++dir) {
+          const int32_t nb = P.nbr[e * 2 * D + dir];  // interfaces only
+          if (nb >= 0) a = fmaxf(a, 0.5f * A.alpha_raw[nb]);
+        }
       }
       s_elem[tid * 8 + 0] = a;
       if (A.alpha_out) A.alpha_out[e] = a;

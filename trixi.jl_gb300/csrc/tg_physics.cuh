@@ -21,6 +21,18 @@ enum FluxKind {
   FLUX_LLF_NAIVE = 4
 };
 enum SourceKind { SRC_NONE = 0, SRC_CONVERGENCE_TEST = 1 };
+// boundary conditions of a non-periodic TreeMesh, per direction
+enum BoundaryKind { BC_PERIODIC = 0, BC_DIRICHLET = 1, BC_SLIP_WALL = 2 };
+// initial conditions a Dirichlet boundary can take its values from
+enum InitialConditionKind {
+  IC_CONSTANT = 0,
+  IC_CONVERGENCE_TEST = 1,
+  IC_ISENTROPIC_VORTEX = 2,
+  IC_WEAK_BLAST_WAVE = 3,
+  IC_KELVIN_HELMHOLTZ = 4,
+  IC_TAYLOR_GREEN = 5,
+  IC_GAUSSIAN_BLAST = 6
+};
 
 template <typename R>
 struct Real;
@@ -238,5 +250,124 @@ struct Euler {
     return (gamma - R(1)) * (u[0] * u[P] - R(0.5) * m2);
   }
 };
+
+// ---------------------------------------------------------------------------
+// Boundary values and boundary fluxes of a non-periodic TreeMesh (FP64)
+// ---------------------------------------------------------------------------
+
+// Conservative state of an initial condition at x, t: the value a
+// BoundaryConditionDirichlet(initial_condition) imposes (equations.jl:164-182).
+// par: the free constants of the configurable conditions (see each case).
+template <int D>
+__host__ __device__ inline void boundary_value(int ic, const double* par, const double* x, double t,
+                                               double gamma, double* u) {
+  constexpr int NV = D + 2, P = D + 1;
+  const double igm1 = 1.0 / (gamma - 1.0);
+  double w[NV];
+  switch (ic) {
+    case IC_CONSTANT:  // compressible_euler_2d.jl:71-78, 3d.jl:71-79
+      u[0] = 1.0;
+      u[1] = 0.1;
+      u[2] = -0.2;
+      if (D == 3) u[3] = 0.7;
+      u[P] = 10.0;
+      return;
+    case IC_CONVERGENCE_TEST: {  // compressible_euler_2d.jl:87-104, 3d.jl:93-110
+      double s = x[0];
+      for (int d = 1; d < D; ++d) s += x[d];
+      const double ini = 2.0 + 0.1 * sin(3.141592653589793 * (s - t));
+      for (int v = 0; v < P; ++v) u[v] = ini;
+      u[P] = ini * ini;
+      return;
+    }
+    case IC_ISENTROPIC_VORTEX: {  // elixir_euler_vortex.jl:18-52; par = {p_inf, amplitude}
+      const double p0 = par[0], amp = par[1];
+      const double c0 = -x[1], c1 = x[0];
+      const double du = amp / (2.0 * 3.141592653589793) * exp(0.5 * (1.0 - (c0 * c0 + c1 * c1)));
+      const double dtemp = -(gamma - 1.0) / (2.0 * gamma * p0) * du * du;
+      w[0] = pow(1.0 + dtemp, igm1);
+      w[1] = 1.0 + du * c0;
+      w[2] = 1.0 + du * c1;
+      w[P] = p0 * pow(1.0 + dtemp, gamma * igm1);
+      break;
+    }
+    case IC_WEAK_BLAST_WAVE: {  // compressible_euler_2d.jl:245-264, 3d.jl:241-263
+      double r2 = 0;
+      for (int d = 0; d < D; ++d) r2 += x[d] * x[d];
+      const double r = sqrt(r2);
+      const bool out = r > 0.5;
+      const double phi = atan2(x[1], x[0]);
+      w[0] = out ? 1.0 : 1.1691;
+      w[P] = out ? 1.0 : 1.245;
+      if (D == 2) {
+        w[1] = out ? 0.0 : 0.1882 * cos(phi);
+        w[2] = out ? 0.0 : 0.1882 * sin(phi);
+      } else {
+        const double theta = r == 0.0 ? 0.0 : acos(x[D - 1] / r);
+        w[1] = out ? 0.0 : 0.1882 * cos(phi) * sin(theta);
+        w[2] = out ? 0.0 : 0.1882 * sin(phi) * sin(theta);
+        w[D] = out ? 0.0 : 0.1882 * cos(theta);
+      }
+      break;
+    }
+    case IC_KELVIN_HELMHOLTZ: {  // elixir_euler_kelvin_helmholtz_instability.jl:18-31
+      const double B = tanh(15.0 * x[1] + 7.5) - tanh(15.0 * x[1] - 7.5);
+      w[0] = 0.5 + 0.75 * B;
+      w[1] = 0.5 * (B - 1.0);
+      w[2] = 0.1 * sinpi(2.0 * x[0]);
+      for (int d = 3; d <= D; ++d) w[d] = 0.0;
+      w[P] = 1.0;
+      break;
+    }
+    case IC_TAYLOR_GREEN: {  // elixir_euler_taylor_green_vortex.jl:14-30; par = {Ma}
+      const double Ms = par[0];
+      w[0] = 1.0;
+      w[1] = sin(x[0]) * cos(x[1]) * cos(x[D - 1]);
+      w[2] = -cos(x[0]) * sin(x[1]) * cos(x[D - 1]);
+      if (D == 3) w[3] = 0.0;
+      w[P] = (1.0 / Ms) * (1.0 / Ms) / gamma +
+             1.0 / 16.0 * (cos(2 * x[0]) * cos(2 * x[D - 1]) + 2 * cos(2 * x[1]) + 2 * cos(2 * x[0]) +
+                           cos(2 * x[1]) * cos(2 * x[D - 1]));
+      break;
+    }
+    case IC_GAUSSIAN_BLAST: {  // energy deposit; par = {p_bg, E, width}
+      const double pbg = par[0], E = par[1], wd = par[2];
+      double r2 = 0;
+      for (int d = 0; d < D; ++d) r2 += x[d] * x[d];
+      const double area = 3.141592653589793 * wd * wd;
+      const double norm = D == 2 ? area : area * sqrt(area);
+      w[0] = 1.0;
+      for (int d = 1; d <= D; ++d) w[d] = 0.0;
+      w[P] = pbg + (gamma - 1.0) * E * exp(-r2 / (wd * wd)) / norm;
+      break;
+    }
+    default:
+      for (int v = 0; v < NV; ++v) u[v] = NAN;
+      return;
+  }
+  double ke = 0;
+  u[0] = w[0];
+  for (int d = 0; d < D; ++d) {
+    u[1 + d] = w[0] * w[1 + d];
+    ke += u[1 + d] * w[1 + d];
+  }
+  u[P] = w[P] * igm1 + 0.5 * ke;
+}
+
+// Pressure of boundary_condition_slip_wall (compressible_euler_2d.jl:322-371,
+// 3d.jl:315-373): the 1D pressure Riemann problem of density rho, pressure p
+// and outward normal velocity vn; the wall flux is this pressure in the
+// normal momentum and zero elsewhere.
+template <typename R>
+__host__ __device__ inline R slip_wall_pressure(R rho, R vn, R p, R gamma, R igm1) {
+  if (vn <= R(0)) {
+    const R c = Real<R>::sqrt(gamma * p / rho);
+    const R base = R(1) + R(0.5) * (gamma - R(1)) * vn / c;
+    return base >= R(0) ? p * pow(base, R(2) * gamma * igm1) : R(0);
+  }
+  const R A = R(2) / ((gamma + R(1)) * rho);
+  const R B = p * (gamma - R(1)) / (gamma + R(1));
+  return p + R(0.5) * vn / A * (vn + Real<R>::sqrt(vn * vn + R(4) * A * (p + B)));
+}
 
 }  // namespace tg

@@ -42,6 +42,9 @@ struct TgConfig
     inverse_jacobian::Ptr{Float64}
     node_coordinates::Ptr{Float64}
     elements_per_block::Int32
+    boundary_conditions::NTuple{6, Int32}  # per direction: 0 periodic, 1 Dirichlet, 2 slip wall
+    boundary_value_function::Int32         # tg_initial_condition of Dirichlet faces
+    boundary_value_params::NTuple{4, Float64}
 end
 
 const TG_VOLUME_WEAK_FORM, TG_VOLUME_FLUX_DIFFERENCING, TG_VOLUME_SHOCK_CAPTURING_HG = 0, 1, 2
@@ -111,7 +114,29 @@ function config(semi, precision, device)
                     pointer(cache.interfaces.neighbor_ids),
                     pointer(cache.interfaces.orientations),
                     pointer(cache.elements.inverse_jacobian),
-                    pointer(cache.elements.node_coordinates), 0)
+                    pointer(cache.elements.node_coordinates), 0,
+                    boundary_codes(semi.boundary_conditions, ndims(mesh)),
+                    boundary_value_code(semi.boundary_conditions)...)
+end
+
+# boundary_conditions of the semidiscretization (digested: one per direction
+# for non-periodic meshes) as tg_boundary codes
+bc_code(::Trixi.BoundaryConditionPeriodic) = Int32(0)
+bc_code(::Trixi.BoundaryConditionDirichlet) = Int32(1)
+bc_code(::typeof(Trixi.boundary_condition_slip_wall)) = Int32(2)
+boundary_codes(bcs::Trixi.BoundaryConditionPeriodic, nd) = ntuple(_ -> Int32(0), 6)
+boundary_codes(bcs::NamedTuple, nd) = ntuple(k -> k <= 2nd ? bc_code(bcs[k]) : Int32(0), 6)
+
+# Dirichlet values: the initial conditions the device evaluates
+ic_code(::typeof(Trixi.initial_condition_constant)) = Int32(0)
+ic_code(::typeof(Trixi.initial_condition_convergence_test)) = Int32(1)
+ic_code(::typeof(Trixi.initial_condition_weak_blast_wave)) = Int32(3)
+function boundary_value_code(bcs)
+    for bc in (bcs isa NamedTuple ? values(bcs) : (bcs,))
+        bc isa Trixi.BoundaryConditionDirichlet &&
+            return ic_code(bc.boundary_value_function), (0.0, 0.0, 0.0, 0.0)
+    end
+    return Int32(0), (0.0, 0.0, 0.0, 0.0)
 end
 
 function create_context(semi; precision = 0, device = 0)

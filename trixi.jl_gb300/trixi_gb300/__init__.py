@@ -30,8 +30,9 @@ from .equations import (CompressibleEulerEquations2D, CompressibleEulerEquations
                         max_abs_speed, max_abs_speed_naive, prim2cons,
                         source_terms_convergence_test)
 from .mesh import TreeMesh  # noqa: F401
-from .semidiscretization import (DeviceContext, ODEProblem, SemidiscretizationHyperbolic,  # noqa: F401
-                                 boundary_condition_periodic, semidiscretize)
+from .semidiscretization import (BoundaryConditionDirichlet, DeviceContext, ODEProblem,  # noqa: F401
+                                 SemidiscretizationHyperbolic, boundary_condition_periodic,
+                                 boundary_condition_slip_wall, semidiscretize)
 from .solvers import (DGSEM, IndicatorHennemannGassner, VolumeIntegralFluxDifferencing,  # noqa: F401
                       VolumeIntegralShockCapturingHG, VolumeIntegralWeakForm)
 from .time_integration import (AliveCallback, AnalysisCallback, CallbackSet,  # noqa: F401

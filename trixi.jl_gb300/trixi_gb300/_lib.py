@@ -22,6 +22,7 @@ TG_VOLUME_WEAK_FORM, TG_VOLUME_FLUX_DIFFERENCING, TG_VOLUME_SHOCK_CAPTURING_HG =
  TG_FLUX_LAX_FRIEDRICHS_NAIVE) = range(5)
 TG_SOURCE_NONE, TG_SOURCE_CONVERGENCE_TEST = 0, 1
 TG_PRECISION_FP64, TG_PRECISION_MIXED = 0, 1
+TG_BOUNDARY_PERIODIC, TG_BOUNDARY_DIRICHLET, TG_BOUNDARY_SLIP_WALL = 0, 1, 2
 
 # Every symbol declared in include/trixi_gb300.h.
 EXPORTS = ("tg_api_version", "tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ndofs",
@@ -71,6 +72,9 @@ class tg_config(ctypes.Structure):
         ("inverse_jacobian", ctypes.POINTER(ctypes.c_double)),
         ("node_coordinates", ctypes.POINTER(ctypes.c_double)),
         ("elements_per_block", ctypes.c_int32),
+        ("boundary_conditions", ctypes.c_int32 * 6),
+        ("boundary_value_function", ctypes.c_int32),
+        ("boundary_value_params", ctypes.c_double * 4),
     ]
 
 

@@ -1,4 +1,4 @@
-"""Uniformly refined, periodic TreeMesh (host setup).
+"""Uniformly refined TreeMesh (host setup), periodic or not per dimension.
 
 Element order is Trixi's: cells are created depth-first with children in
 _child_signs order (x fastest, then y, then z; abstract_tree.jl:122-130,
@@ -26,7 +26,8 @@ def _morton_cells(ndims: int, level: int):
 
 class TreeMesh:
     """TreeMesh(coordinates_min, coordinates_max; initial_refinement_level, periodicity),
-    tree_mesh.jl:128-185 (uniform, periodic only)."""
+    tree_mesh.jl:128-185 (uniform).  periodicity: a bool for all dimensions or one
+    per dimension; faces at a non-periodic domain edge are boundaries."""
 
     def __init__(self, coordinates_min, coordinates_max, initial_refinement_level: int,
                  periodicity=True, n_cells_max=None):
@@ -34,8 +35,12 @@ class TreeMesh:
         cmax = tuple(float(x) for x in coordinates_max)
         if len(cmin) != len(cmax) or len(cmin) not in (2, 3):
             raise ValueError("TreeMesh needs 2 or 3 coordinates")
-        if periodicity is not True and not (isinstance(periodicity, (tuple, list)) and all(periodicity)):
-            raise NotImplementedError("only fully periodic TreeMesh is supported on the GPU path")
+        if isinstance(periodicity, (tuple, list)):
+            if len(periodicity) != len(cmin):
+                raise ValueError("periodicity needs one entry per dimension")
+            self.periodicity = tuple(bool(p) for p in periodicity)
+        else:
+            self.periodicity = (bool(periodicity),) * len(cmin)
         if initial_refinement_level < 0:
             raise ValueError("initial_refinement_level must be non-negative")
         length = cmax[0] - cmin[0]
@@ -72,7 +77,9 @@ class TreeMesh:
         return self.length_level_0 / (1 << self.initial_refinement_level)
 
     def interfaces(self):
-        """neighbor_ids [I, 2] (1-based, (left, right)) and orientations [I] (1-based)."""
+        """neighbor_ids [I, 2] (1-based, (left, right)) and orientations [I] (1-based),
+        per element in order and positive directions only where a neighbour
+        exists (init_interfaces!, containers_2d.jl:228-284)."""
         D, M, E = self.ndims, self.cells_per_dim, self.nelements
         lin = np.zeros(E, dtype=np.int64)
         mult = 1
@@ -83,8 +90,11 @@ class TreeMesh:
         c2e[lin] = np.arange(E)
         nb = np.zeros((E, D, 2), dtype=np.int64)
         orient = np.zeros((E, D), dtype=np.int64)
+        exists = np.ones((E, D), dtype=bool)
         for d in range(D):
             c = self.cartesian.copy()
+            if not self.periodicity[d]:
+                exists[:, d] = c[:, d] + 1 < M
             c[:, d] = (c[:, d] + 1) % M
             l2 = np.zeros(E, dtype=np.int64)
             mult = 1
@@ -94,8 +104,10 @@ class TreeMesh:
             nb[:, d, 0] = np.arange(E) + 1
             nb[:, d, 1] = c2e[l2] + 1
             orient[:, d] = d + 1
-        return nb.reshape(E * D, 2), orient.reshape(E * D)
+        keep = exists.reshape(E * D)
+        return nb.reshape(E * D, 2)[keep], orient.reshape(E * D)[keep]
 
     def __repr__(self):
+        per = "periodic" if all(self.periodicity) else f"periodicity {self.periodicity}"
         return (f"TreeMesh{{{self.ndims}}} with {self.nelements} elements "
-                f"(level {self.initial_refinement_level}, periodic)")
+                f"(level {self.initial_refinement_level}, {per})")

@@ -19,11 +19,65 @@ from .solvers import DGSEM, VolumeIntegralShockCapturingHG
 
 
 class BoundaryConditionPeriodic:
+    code = _lib.TG_BOUNDARY_PERIODIC
+
     def __repr__(self):
         return "boundary_condition_periodic"
 
 
 boundary_condition_periodic = BoundaryConditionPeriodic()
+
+
+class BoundaryConditionDirichlet:
+    """BoundaryConditionDirichlet(boundary_value_function), equations.jl:159-182: the
+    values of an initial condition at the boundary node and time.  On the GPU
+    path the function is one of the package's initial conditions."""
+    code = _lib.TG_BOUNDARY_DIRICHLET
+
+    def __init__(self, boundary_value_function):
+        self.boundary_value_function = boundary_value_function
+
+    def __repr__(self):
+        return f"BoundaryConditionDirichlet({getattr(self.boundary_value_function, '__name__', '?')})"
+
+
+class BoundaryConditionSlipWall:
+    code = _lib.TG_BOUNDARY_SLIP_WALL
+
+    def __repr__(self):
+        return "boundary_condition_slip_wall"
+
+
+# compressible_euler_2d.jl:322-393, 3d.jl:315-416
+boundary_condition_slip_wall = BoundaryConditionSlipWall()
+
+# initial conditions the device can evaluate for Dirichlet boundaries
+_IC_CODES = {"initial_condition_constant": 0, "initial_condition_convergence_test": 1,
+             "initial_condition_isentropic_vortex": 2, "initial_condition_weak_blast_wave": 3,
+             "initial_condition_kelvin_helmholtz_instability": 4,
+             "initial_condition_taylor_green_vortex": 5, "initial_condition_gaussian_blast": 6}
+
+
+def _digest_boundary_conditions(bcs, mesh):
+    """One boundary condition per direction (-x, +x, -y, +y[, -z, +z]) from a single
+    condition, a tuple of 2D conditions or a dict with keys x_neg, x_pos, ...
+    (digest_boundary_conditions, semidiscretization_hyperbolic.jl)."""
+    D = mesh.ndims
+    names = ["x_neg", "x_pos", "y_neg", "y_pos", "z_neg", "z_pos"][:2 * D]
+    if isinstance(bcs, dict):
+        per_dir = [bcs[k] for k in names]
+    elif isinstance(bcs, (tuple, list)):
+        if len(bcs) != 2 * D:
+            raise ValueError(f"need {2 * D} boundary conditions")
+        per_dir = list(bcs)
+    else:
+        per_dir = [bcs] * (2 * D)
+    for k, bc in enumerate(per_dir):
+        periodic_dir = mesh.periodicity[k // 2]
+        if periodic_dir != isinstance(bc, BoundaryConditionPeriodic):
+            raise ValueError(f"boundary condition {bc!r} of direction {names[k]} does not match "
+                             f"the mesh periodicity {mesh.periodicity}")
+    return per_dir
 
 
 def _dptr(a):
@@ -89,6 +143,22 @@ def make_config(semi, precision="fp64", device=0, elements_per_block=0):
     cfg.inverse_jacobian = _dptr(arr(semi.inverse_jacobian))
     cfg.node_coordinates = _dptr(arr(semi.node_coordinates))
     cfg.elements_per_block = int(elements_per_block)
+    funcs = set()
+    for k, bc in enumerate(getattr(semi, "boundary_conditions", [])):
+        cfg.boundary_conditions[k] = bc.code
+        if isinstance(bc, BoundaryConditionDirichlet):
+            funcs.add(bc.boundary_value_function)
+    if len(funcs) > 1:
+        raise NotImplementedError("Dirichlet boundaries with different functions")
+    if funcs:
+        f = funcs.pop()
+        name = getattr(f, "__name__", None)
+        if name not in _IC_CODES:
+            raise NotImplementedError(f"Dirichlet values from {name!r}: only the package's "
+                                      "initial conditions run on the device")
+        cfg.boundary_value_function = _IC_CODES[name]
+        for k, v in enumerate(getattr(f, "params", ())):
+            cfg.boundary_value_params[k] = v
     return cfg, keep
 
 
@@ -222,8 +292,7 @@ class SemidiscretizationHyperbolic:
                  precision="fp64", device=0, elements_per_block=0):
         if mesh.ndims != equations.ndims:
             raise ValueError("mesh and equations have different dimensions")
-        if not isinstance(boundary_conditions, BoundaryConditionPeriodic):
-            raise NotImplementedError("only periodic boundary conditions are on the GPU path")
+        self.boundary_conditions = _digest_boundary_conditions(boundary_conditions, mesh)
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self.mesh, self.equations, self.solver = mesh, equations, solver
