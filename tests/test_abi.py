@@ -40,6 +40,6 @@ def test_invalid_config_is_rejected_without_gpu():
     rc = lib.tg_ctx_create(ctypes.byref(cfg), ctypes.byref(h))
     assert rc == -2 and not h.value
     assert "ndims" in _lib.last_error()
-    cfg.ndims, cfg.polydeg, cfg.nelements, cfg.ninterfaces = 2, 3, 4, 7
+    cfg.ndims, cfg.polydeg, cfg.nelements, cfg.ninterfaces = 2, 3, 4, 9
     assert lib.tg_ctx_create(ctypes.byref(cfg), ctypes.byref(h)) == -2
-    assert "periodic" in _lib.last_error()
+    assert "interfaces" in _lib.last_error()

@@ -713,10 +713,9 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   if (default_epb(D, N) == 0)
     return fail(nullptr, TG_ERR_UNSUPPORTED, "polydeg %d is not compiled for %dD", cfg->polydeg, D);
   if (cfg->nelements <= 0) return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "nelements must be > 0");
-  if (cfg->ninterfaces != (int64_t)D * cfg->nelements)
+  if (cfg->ninterfaces < 0 || cfg->ninterfaces > (int64_t)D * cfg->nelements)
     return fail(nullptr, TG_ERR_UNSUPPORTED,
-                "ninterfaces != ndims * nelements: only periodic conforming TreeMesh "
-                "(no boundaries, no mortars) is supported");
+                "more interfaces than element faces: conforming TreeMesh only (no mortars)");
   if (cfg->volume_integral < 0 || cfg->volume_integral > 2)
     return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "unknown volume integral %d", cfg->volume_integral);
   const int fl[3] = {cfg->volume_flux, cfg->surface_flux, cfg->volume_flux_fv};
