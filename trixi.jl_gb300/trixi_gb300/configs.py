@@ -266,9 +266,7 @@ def c4(harvest_every=10, train_steps=4000, deploy_level=9, fp64_steps=200):
 
 
 def c5a(n=64, seed=20261204, t_end=20.0):
-    rng = np.random.default_rng(seed)
-    specs = [(int(rng.integers(3, 8)), int(rng.integers(2, 5)), float(rng.uniform(1.0, 5.0)))
-             for _ in range(n)]
+    specs = c5a_specs(n, seed)
     out = dict(specs=specs)
     semis = [vortex_semi(lv, p, eps, "mixed") for lv, p, eps in specs]
     ens = T.Ensemble(semis)
@@ -357,18 +355,48 @@ def c5b(levels=((5, 20.0, 20.0), (6, 20.0, 2.0)), dt_out=0.25, control_level=5):
     return out
 
 
+def c5a_specs(n=64, seed=20261204):
+    rng = np.random.default_rng(seed)
+    return [(int(rng.integers(3, 8)), int(rng.integers(2, 5)), float(rng.uniform(1.0, 5.0)))
+            for _ in range(n)]
+
+
+# Short runs of single kernels (for profiling a handful of launches).
+def learned_steps(steps=4):
+    """KHI 256^2, mixed precision, a 16-64-64-1 network with its initial weights
+    deployed as the shock indicator, `steps` steps."""
+    semi = khi_semi(8, "mixed")
+    net = ShockIndicatorMLP(2, 3, seed=3)
+    c = semi.device_context
+    c.upload(semi.compute_coefficients(0.0))
+    net.deploy(semi, band=0.01)
+    t, n = c.step(steps, 1.3, 10.0, 0.0)
+    c.synchronize()
+    return dict(steps=n, t=t, status=c.status())
+
+
+def ensemble_steps(steps=3):
+    """The 64-vortex ensemble of c5a, `steps` steps."""
+    ens = T.Ensemble([vortex_semi(lv, p, eps, "mixed") for lv, p, eps in c5a_specs()])
+    ens.upload_initial()
+    t, n = ens.step(steps, 1.0, 20.0)
+    return dict(steps=n.tolist())
+
+
 RUNS = dict(c1=c1, c3=c3, c4=c4, c5a=c5a, c5b=c5b)
+SHORT_RUNS = dict(learned_steps=learned_steps, ensemble_steps=ensemble_steps)
 
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("--only", default=",".join(RUNS), help="comma-separated subset of " + ",".join(RUNS))
+    ap.add_argument("--only", default=",".join(RUNS),
+                    help="comma-separated subset of " + ",".join(list(RUNS) + list(SHORT_RUNS)))
     ap.add_argument("--out", default=None, help="write the results as JSON here")
     args = ap.parse_args(argv)
     results = {}
     for name in args.only.split(","):
         t0 = time.perf_counter()
-        results[name] = RUNS[name]()
+        results[name] = {**RUNS, **SHORT_RUNS}[name]()
         results[name]["wall_secs"] = time.perf_counter() - t0
         brief = {k: v for k, v in results[name].items() if not isinstance(v, (list, dict))}
         print(name, json.dumps(brief), flush=True)
