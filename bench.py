@@ -112,6 +112,25 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
+def max_over_ranks(value: float, world: int) -> float:
+    """The largest of every rank's `value` (timings: the slowest replica sets the
+    whole-job time).  NCCL reduces on the device, gloo on the host."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(ndofs: int, ms_per_step: float, world: int) -> float:
+    """DOF-updates/s per RK stage of all replicas: each of `world` ranks advances
+    its own copy of the workload (ndofs per field, 5 stages per step)."""
+    return world * ndofs * 5 / (ms_per_step * 1e-3)
+
+
 def gpu_arm(args, rank: int, world: int):
     import torch
 
@@ -151,14 +170,10 @@ def gpu_arm(args, rank: int, world: int):
         clocks = sampler.stop() if sampler else None
         if world > 1:
             torch.distributed.barrier()
-        tot = sum(times)
-        if world > 1:
-            tt = torch.tensor([tot], dtype=torch.float64, device="cuda")
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            tot = float(tt.item())
+        tot = max_over_ranks(sum(times), world)
         ms_step = tot / steps
         results[prec] = dict(ms_per_step=ms_step, steps=steps,
-                             value=world * semi.ndofs * 5 / (ms_step * 1e-3), clocks=clocks)
+                             value=whole_job_rate(semi.ndofs, ms_step, world), clocks=clocks)
         if ctx.status() != 0:
             raise RuntimeError(f"{prec}: device status word flagged a non-physical state")
 
@@ -223,7 +238,8 @@ def gpu_arm(args, rank: int, world: int):
                 et.append(e0.elapsed_time(e1))
         ms = statistics.mean(et)
         nbytes = semi.nvalues * 8
-        e2e = {"value": world * semi.ndofs * 5 / (ms * 1e-3), "unit": "DOF-updates/s",
+        e2e = {"value": whole_job_rate(semi.ndofs, max_over_ranks(ms, world), world),
+               "unit": "DOF-updates/s",
                "ms_per_step": ms, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
 
     # ---- accuracy at t_end (untimed): L2 density error of both paths ----
