@@ -119,3 +119,28 @@ def test_deployed_predictions_equal_the_inference_kernel(trained):
     sqrt_thr = np.sqrt(0.5 * 10 ** (-1.8 * 4 ** 0.25))
     np.testing.assert_array_equal(flag == 1, np.abs(pred - sqrt_thr) < 0.01)
     ShockIndicatorMLP.undeploy(semi)
+
+
+def test_3d_deployment_uses_the_network_and_the_hg_fallback():
+    # 3D networks (64-128-128-1) deploy through the features / inference /
+    # alpha kernels: the per-element predictions are the network's on the
+    # current state, and elements in the band around sqrt(T) take HG
+    case = dict(ndims=3, polydeg=3, level=2, xmin=[-2.0] * 3, xmax=[2.0] * 3, vi="hg",
+                volume_flux="ranocha", surface_flux="llf", ic="weak_blast_wave",
+                alpha_max=0.5, alpha_min=0.001)
+    net = ShockIndicatorMLP(3, 3, seed=21)
+    semi, _ = build(case, precision="mixed")
+    ctx = semi.device_context
+    ctx.upload(semi.compute_coefficients(0.0))
+    net.deploy(semi, band=0.05)
+    t, n = ctx.step(3, 0.5, 10.0, 0.0)
+    assert n == 3 and ctx.status() == 0
+    ctx.alpha()
+    pred, hg, flag, counts = net.last(semi.nelements)
+    n0 = net.count
+    net.harvest(semi)
+    x, _ = net.dataset()
+    np.testing.assert_allclose(net.predict(x[n0:]), pred, rtol=1e-6, atol=1e-7)
+    sqrt_thr = np.sqrt(0.5 * 10 ** (-1.8 * 4 ** 0.25))
+    np.testing.assert_array_equal(flag == 1, np.abs(pred - sqrt_thr) < 0.05)
+    ShockIndicatorMLP.undeploy(semi)
