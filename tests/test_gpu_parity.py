@@ -342,3 +342,26 @@ def test_nonperiodic_steps_match_oracle(c, precision):
     tol = 1e-12 if precision == "fp64" else 1e-5
     assert abs(t - t_ref) <= tol * t_ref
     assert rel_err(ctx.download(), ref) < tol
+
+
+# the edges of the compiled polynomial degrees (2D polydeg 1..5, 3D 1..4)
+EDGE_CASES = [
+    dict(ndims=2, polydeg=1, level=3, xmin=[0, 0], xmax=[2, 2], vi="weak", surface_flux="llf",
+         ic="convergence_test", source="convergence_test"),
+    dict(ndims=2, polydeg=5, level=2, xmin=[-1, -1], xmax=[1, 1], vi="fluxdiff",
+         volume_flux="ranocha", surface_flux="llf", ic="kelvin_helmholtz"),
+    dict(ndims=2, polydeg=5, level=3, xmin=[-2, -2], xmax=[2, 2], vi="hg", volume_flux="shima_etal",
+         surface_flux="llf_naive", ic="weak_blast_wave"),
+    dict(ndims=3, polydeg=1, level=2, xmin=[0] * 3, xmax=[2] * 3, vi="fluxdiff",
+         volume_flux="ranocha", surface_flux="llf", ic="convergence_test", source="convergence_test"),
+    dict(ndims=3, polydeg=4, level=1, xmin=[0] * 3, xmax=[2] * 3, vi="weak", surface_flux="llf",
+         ic="convergence_test", source="convergence_test"),
+]
+
+
+@pytest.mark.parametrize("c", EDGE_CASES, ids=[_id(c) for c in EDGE_CASES])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 2e-4)])
+def test_rhs_edge_polydeg_matches_oracle(c, precision, tol):
+    semi, orc = build(c, precision=precision)
+    u = perturbed_state(semi, seed=53)
+    assert rel_err(semi.device_context.rhs_host(u, 0.29), orc.rhs(u, 0.29)) < tol
