@@ -25,7 +25,8 @@ FLUX_CENTRAL, FLUX_RANOCHA, FLUX_SHIMA_ETAL, FLUX_LAX_FRIEDRICHS, FLUX_LAX_FRIED
 SRC_NONE, SRC_CONVERGENCE_TEST = 0, 1
 BC_PERIODIC, BC_DIRICHLET, BC_SLIP_WALL = 0, 1, 2
 (IC_CONSTANT, IC_CONVERGENCE_TEST, IC_ISENTROPIC_VORTEX, IC_WEAK_BLAST_WAVE,
- IC_KELVIN_HELMHOLTZ, IC_TAYLOR_GREEN, IC_GAUSSIAN_BLAST) = range(7)
+ IC_KELVIN_HELMHOLTZ, IC_TAYLOR_GREEN, IC_GAUSSIAN_BLAST,
+ IC_ISENTROPIC_VORTEX_ADVECTED) = range(8)
 
 _lib = None
 
@@ -71,6 +72,12 @@ def _load():
     lib.orc_entropy_timederivative.argtypes = [vp, P(d), d]
     lib.orc_set_boundaries.restype = i
     lib.orc_set_boundaries.argtypes = [vp, P(i), i, P(d)]
+    lib.orc_set_refinement.restype = i
+    lib.orc_set_refinement.argtypes = [vp, i, P(i), P(d)]
+    lib.orc_nmortars.restype = i64
+    lib.orc_nmortars.argtypes = [vp]
+    lib.orc_get_mortars.argtypes = [vp, P(i64), P(i64), P(i64)]
+    lib.orc_get_mortar_matrices.argtypes = [vp, P(d)]
     _lib = lib
     return lib
 
@@ -216,6 +223,57 @@ def _set_boundaries(self, bc, ic=0, params=None):
 
 
 Oracle.set_boundaries = _set_boundaries
+
+
+def _set_refinement(self, patches):
+    """Refinement patches after the initial refinement (TreeMesh
+    refinement_patches): dicts with type "box" (coordinates_min,
+    coordinates_max) or "sphere" (center, radius)."""
+    kinds = np.zeros(max(1, len(patches)), dtype=np.int32)
+    par = np.zeros(7 * max(1, len(patches)))
+    for k, p in enumerate(patches):
+        if p["type"] == "box":
+            kinds[k] = 0
+            par[7 * k:7 * k + self.ndims] = p["coordinates_min"]
+            par[7 * k + 3:7 * k + 3 + self.ndims] = p["coordinates_max"]
+        elif p["type"] == "sphere":
+            kinds[k] = 1
+            par[7 * k:7 * k + self.ndims] = p["center"]
+            par[7 * k + 6] = p["radius"]
+        else:
+            raise ValueError(f"unknown refinement patch type {p['type']!r}")
+    if self.lib.orc_set_refinement(self.h, len(patches), _p(kinds, ctypes.c_int), _p(par)) != 0:
+        raise ValueError("oracle: invalid refinement patch")
+    self.nelements = self.lib.orc_nelements(self.h)
+    self.ninterfaces = self.lib.orc_ninterfaces(self.h)
+    self.nmortars = self.lib.orc_nmortars(self.h)
+    self.ndofs = self.lib.orc_ndofs(self.h)
+
+
+def _mortars(self):
+    """cache.mortars: neighbor_ids [M, 2^(ndims-1) + 1] (1-based, large last),
+    large_sides [M] (1 or 2), orientations [M] (1-based)."""
+    M = self.lib.orc_nmortars(self.h)
+    ids = np.zeros((M, (1 << (self.ndims - 1)) + 1), dtype=np.int64)
+    ls = np.zeros(M, dtype=np.int64)
+    orient = np.zeros(M, dtype=np.int64)
+    if M:
+        self.lib.orc_get_mortars(self.h, _p(ids, ctypes.c_int64), _p(ls, ctypes.c_int64),
+                                 _p(orient, ctypes.c_int64))
+    return ids, ls, orient
+
+
+def _mortar_matrices(self):
+    """forward_upper, forward_lower, reverse_upper, reverse_lower as (n, n) arrays."""
+    n = self.n
+    out = np.zeros(4 * n * n)
+    self.lib.orc_get_mortar_matrices(self.h, _p(out))
+    return [out[k * n * n:(k + 1) * n * n].reshape(n, n).copy() for k in range(4)]
+
+
+Oracle.set_refinement = _set_refinement
+Oracle.mortars = _mortars
+Oracle.mortar_matrices = _mortar_matrices
 
 
 def set_threads(n: int) -> None:

@@ -22,7 +22,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <unordered_map>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -48,6 +51,7 @@ enum InitialCondition {
   IC_KELVIN_HELMHOLTZ = 4,
   IC_TAYLOR_GREEN = 5,
   IC_GAUSSIAN_BLAST = 6,
+  IC_ISENTROPIC_VORTEX_ADVECTED = 7,
 };
 
 // ---------------------------------------------------------------------------
@@ -206,6 +210,103 @@ static std::vector<double> invert(std::vector<double> A, int n) {
   return B;
 }
 
+// legendre_polynomial_and_derivative, basis_lobatto_legendre.jl:677-706
+// (normalised by sqrt(N + 1/2))
+static void legendre_and_derivative(int N, double x, double& poly, double& deriv) {
+  if (N == 0) {
+    poly = 1;
+    deriv = 0;
+  } else if (N == 1) {
+    poly = x;
+    deriv = 1;
+  } else {
+    double p2 = 1, p1 = x, d2 = 0, d1 = 1;
+    poly = deriv = 0;
+    for (int i = 2; i <= N; ++i) {
+      poly = ((2 * i - 1) * x * p1 - (i - 1) * p2) / i;
+      deriv = d2 + (2 * i - 1) * p1;
+      p2 = p1;
+      p1 = poly;
+      d2 = d1;
+      d1 = deriv;
+    }
+  }
+  poly *= std::sqrt(N + 0.5);
+  deriv *= std::sqrt(N + 0.5);
+}
+
+// gauss_nodes_weights, basis_gauss_legendre.jl:149-205 (Kopriva alg. 23):
+// Newton iteration from -cos(pi (2i+1)/(2N+2)), symmetric completion.
+static void gauss_nodes_weights(int n_nodes, std::vector<double>& nodes,
+                                std::vector<double>& weights) {
+  nodes.assign(n_nodes, 1.0);
+  weights.assign(n_nodes, 0.0);
+  const int N = n_nodes - 1;
+  if (N == 0) {
+    nodes[0] = 0;
+    weights[0] = 2;
+    return;
+  }
+  if (N == 1) {
+    nodes[0] = -std::sqrt(1.0 / 3);
+    nodes[1] = -nodes[0];
+    weights[0] = weights[1] = 1;
+    return;
+  }
+  const double tol = 2 * 2.220446049250313e-16;
+  for (int i = 0; i <= (N + 1) / 2 - 1; ++i) {
+    double x = -std::cos(M_PI * (2 * i + 1) / (2.0 * N + 2));
+    for (int k = 0; k <= 20; ++k) {
+      double p, dp;
+      legendre_and_derivative(N + 1, x, p, dp);
+      const double dx = -p / dp;
+      x += dx;
+      if (std::fabs(dx) < tol * std::fabs(x)) break;
+    }
+    double p, dp;
+    legendre_and_derivative(N + 1, x, p, dp);
+    nodes[i] = x;
+    weights[i] = (2 * N + 3) / ((1 - x * x) * dp * dp);
+    nodes[N - i] = -x;
+    weights[N - i] = weights[i];
+  }
+  if (n_nodes % 2 == 1) {
+    double p, dp;
+    legendre_and_derivative(N + 1, 0.0, p, dp);
+    nodes[N / 2] = 0;
+    weights[N / 2] = (2 * N + 3) / (dp * dp);
+  }
+}
+
+// lagrange_interpolating_polynomials, basis_lobatto_legendre.jl:533-557
+static std::vector<double> lagrange_polys(double x, const std::vector<double>& nodes,
+                                          const std::vector<double>& wbary) {
+  const int n = (int)nodes.size();
+  std::vector<double> p(n, 0.0);
+  const double ex = std::nextafter(std::fabs(x), INFINITY) - std::fabs(x);  // eps(x)
+  for (int i = 0; i < n; ++i)
+    if (x == nodes[i] || std::fabs(x - nodes[i]) <= ex * std::max(std::fabs(x), std::fabs(nodes[i]))) {
+      p[i] = 1;
+      return p;
+    }
+  double total = 0;
+  for (int i = 0; i < n; ++i) {
+    p[i] = wbary[i] / (x - nodes[i]);
+    total += p[i];
+  }
+  for (int i = 0; i < n; ++i) p[i] /= total;
+  return p;
+}
+
+static std::vector<double> matmul(const std::vector<double>& A, const std::vector<double>& B,
+                                  int n) {
+  std::vector<double> C(n * n, 0.0);
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j) C[i * n + j] += A[i * n + k] * B[k * n + j];
+  return C;
+}
+
 struct Basis {
   int n = 0;
   std::vector<double> nodes, weights, inv_weights;
@@ -214,7 +315,39 @@ struct Basis {
   // basis_lobatto_legendre.jl:274-290)
   int na = 0;
   std::vector<double> anodes, aweights, avand;  // avand: na x n
+  // MortarL2(basis), basis_lobatto_legendre.jl:159-205: forward (interpolation
+  // to the lower/upper half) and reverse (Gauss-quadrature L2 projection back)
+  std::vector<double> fwd[2], rev[2];  // [0]: lower, [1]: upper; n x n
 };
+
+// calc_forward_{upper,lower}, calc_reverse_{upper,lower}(::Val{:gauss}),
+// l2projection.jl:26-115
+static void make_mortar(Basis& b) {
+  const int n = b.n;
+  std::vector<double> wb = barycentric_weights(b.nodes);
+  for (int h = 0; h < 2; ++h) {
+    const double shift = h ? 1.0 : -1.0;
+    b.fwd[h].assign(n * n, 0.0);
+    for (int j = 0; j < n; ++j) {
+      std::vector<double> p = lagrange_polys(0.5 * (b.nodes[j] + shift), b.nodes, wb);
+      for (int i = 0; i < n; ++i) b.fwd[h][j * n + i] = p[i];
+    }
+  }
+  std::vector<double> gn, gw;
+  gauss_nodes_weights(n, gn, gw);
+  std::vector<double> gwb = barycentric_weights(gn);
+  std::vector<double> g2l = interpolation_matrix(gn, b.nodes);
+  std::vector<double> l2g = interpolation_matrix(b.nodes, gn);
+  for (int h = 0; h < 2; ++h) {
+    const double shift = h ? 1.0 : -1.0;
+    std::vector<double> op(n * n, 0.0);
+    for (int j = 0; j < n; ++j) {
+      std::vector<double> p = lagrange_polys(0.5 * (gn[j] + shift), gn, gwb);
+      for (int i = 0; i < n; ++i) op[i * n + j] = 0.5 * p[i] * gw[j] / gw[i];
+    }
+    b.rev[h] = matmul(matmul(g2l, op, n), l2g, n);
+  }
+}
 
 // LobattoLegendreBasis(RealT, polydeg), basis_lobatto_legendre.jl:54-85
 static Basis make_basis(int polydeg) {
@@ -253,6 +386,7 @@ static Basis make_basis(int polydeg) {
   b.na = 2 * polydeg + 1;
   lgl_nodes_weights(b.na, b.anodes, b.aweights);
   b.avand = interpolation_matrix(b.nodes, b.anodes);
+  make_mortar(b);
   return b;
 }
 
@@ -504,6 +638,30 @@ static void initial_condition(const Eq& eq, int ic, const double* par, const dou
       prim2cons(eq, prim, u);
       return;
     }
+    case IC_ISENTROPIC_VORTEX_ADVECTED: {
+      // examples/tree_2d_dgsem/elixir_euler_vortex_mortar.jl:18-64: the vortex
+      // of elixir_euler_vortex.jl advected with the base flow (1, 1) and
+      // wrapped to the nearest periodic image on [-10, 10]^2;
+      // par = {p_inf, amplitude}
+      const double p0 = par ? par[0] : 25.0;
+      const double amp = par ? par[1] : 5.0;
+      double rho = 1, v1 = 1, v2 = 1, p = p0;
+      const double rt = p / rho;
+      double c0 = x[0] - v1 * t, c1 = x[1] - v2 * t;
+      c0 = c0 - 20.0 * std::nearbyint(c0 / 20.0);  // round-half-even, as Julia's round
+      c1 = c1 - 20.0 * std::nearbyint(c1 / 20.0);
+      const double cent0 = -c1, cent1 = c0;
+      const double r2 = cent0 * cent0 + cent1 * cent1;
+      const double du = amp / (2 * M_PI) * std::exp(0.5 * (1 - r2));
+      const double dtemp = -(eq.gamma - 1) / (2 * eq.gamma * rt) * du * du;
+      rho = rho * std::pow(1 + dtemp, 1 / (eq.gamma - 1));
+      v1 = v1 + du * cent0;
+      v2 = v2 + du * cent1;
+      p = p * std::pow(1 + dtemp, eq.gamma / (eq.gamma - 1));
+      prim[0] = rho; prim[1] = v1; prim[2] = v2; prim[3] = p;
+      prim2cons(eq, prim, u);
+      return;
+    }
     case IC_WEAK_BLAST_WAVE: {
       // initial_condition_weak_blast_wave, compressible_euler_2d.jl:245-264, 3d.jl:241-263
       if (eq.D == 2) {
@@ -574,109 +732,270 @@ static void initial_condition(const Eq& eq, int ic, const double* par, const dou
 }
 
 // ---------------------------------------------------------------------------
-// Mesh: uniformly refined TreeMesh, periodic or not (periodicity = false:
-// faces at the domain edges have no neighbour and become boundaries,
-// containers_2d.jl:355-421, 475-532)
-//   src/meshes/tree_mesh.jl:128-185, abstract_tree.jl:122-130, 206-248, 668-674,
-//   src/solvers/dgsem_tree/containers_2d.jl:85-127, 228-284 (3d: 87, 229)
+// Mesh: TreeMesh with an initial uniform refinement and optional refinement
+// patches, periodic or not (periodicity = false: faces at the domain edge are
+// boundaries).
+//   tree_mesh.jl:128-215 (TreeMesh, initialize!),
+//   abstract_tree.jl:35-47 (has_neighbor, has_coarse_neighbor), 122-130
+//   (_child_signs), 317-402 (refine_unbalanced!, refine!), 405-447
+//   (refine_box!, refine_sphere!), 453-489 (rebalance!), 668-674
+//   (child_coordinates);
+//   containers_2d.jl:85-127 (elements), 193-284 (interfaces), 660-810
+//   (mortars); containers_3d.jl:87, 229, 652-790.
+// Cells live in a map keyed by (level, integer position); a same-level
+// neighbour exists iff that key is present (periodic wrap from the root),
+// which is what Trixi's neighbour links record.  Leaves are enumerated in
+// depth-first order with children in _child_signs order, the order in which
+// Trixi stores its cells (children are inserted right behind the parent).
 // ---------------------------------------------------------------------------
 
+struct Patch {
+  int kind;       // 0: box (a = coordinates_min, b = coordinates_max); 1: sphere (a = center, r)
+  double a[3], b[3], r;
+};
+
+struct Tree {
+  struct Cell {
+    int level;
+    int64_t ix[3];
+    double c[3];
+    int64_t child0;  // index of the first child, -1 for a leaf
+  };
+  int D = 2;
+  bool periodic = true;
+  double length0 = 0;
+  std::vector<Cell> cells;
+  std::unordered_map<uint64_t, int64_t> index;
+
+  static uint64_t key(int level, const int64_t* ix) {
+    return ((uint64_t)level << 60) | (uint64_t)ix[0] | ((uint64_t)ix[1] << 20) |
+           ((uint64_t)ix[2] << 40);
+  }
+  int64_t find(int level, const int64_t* ix) const {
+    auto it = index.find(key(level, ix));
+    return it == index.end() ? -1 : it->second;
+  }
+  int64_t add(int level, const int64_t* ix, const double* c) {
+    Cell cl;
+    cl.level = level;
+    for (int d = 0; d < 3; ++d) {
+      cl.ix[d] = ix[d];
+      cl.c[d] = c[d];
+    }
+    cl.child0 = -1;
+    cells.push_back(cl);
+    index[key(level, ix)] = (int64_t)cells.size() - 1;
+    return (int64_t)cells.size() - 1;
+  }
+  double length(int level) const { return length0 / (double)(1LL << level); }
+  // same-level neighbour in direction dir (0:-x, 1:+x, 2:-y, ...), -1 if none
+  int64_t neighbour(int64_t cell, int dir) const {
+    const Cell& c = cells[cell];
+    int64_t ix[3] = {c.ix[0], c.ix[1], c.ix[2]};
+    const int d = dir / 2;
+    const int64_t M = 1LL << c.level;
+    ix[d] += (dir & 1) ? 1 : -1;
+    if (ix[d] < 0 || ix[d] >= M) {
+      if (!periodic) return -1;
+      ix[d] = (ix[d] + M) % M;
+    }
+    return find(c.level, ix);
+  }
+  int64_t parent(int64_t cell) const {
+    const Cell& c = cells[cell];
+    if (c.level == 0) return -1;
+    int64_t ix[3] = {c.ix[0] >> 1, c.ix[1] >> 1, c.ix[2] >> 1};
+    return find(c.level - 1, ix);
+  }
+  bool leaf(int64_t cell) const { return cells[cell].child0 < 0; }
+  // init_child! with child_coordinates: centre + sign * (parent length / 2) / 2
+  void refine_cell(int64_t cell) {
+    const int nch = 1 << D;
+    const double child_len = length(cells[cell].level) / 2;
+    int64_t first = -1;
+    for (int ch = 0; ch < nch; ++ch) {
+      const Cell p = cells[cell];
+      int64_t ix[3] = {0, 0, 0};
+      double c[3] = {0, 0, 0};
+      for (int d = 0; d < D; ++d) {
+        const int bit = (ch >> d) & 1;
+        ix[d] = 2 * p.ix[d] + bit;
+        c[d] = p.c[d] + (bit ? 1.0 : -1.0) * child_len / 2;
+      }
+      const int64_t id = add(p.level + 1, ix, c);
+      if (ch == 0) first = id;
+    }
+    cells[cell].child0 = first;
+  }
+  int64_t child(int64_t cell, int ch) const { return cells[cell].child0 + ch; }
+  void refine_unbalanced(std::vector<int64_t> ids) {
+    std::sort(ids.begin(), ids.end());
+    ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+    for (int64_t id : ids) refine_cell(id);
+  }
+  // refine!(t, cell_ids): refine, then rebalance! until the 2:1 rule holds
+  // across faces (Cartesian neighbours only)
+  void refine(const std::vector<int64_t>& ids) {
+    std::vector<int64_t> refined(ids);
+    refine_unbalanced(refined);
+    while (!refined.empty()) {
+      std::vector<int64_t> to_refine;
+      for (int64_t cell : refined)
+        for (int dir = 0; dir < 2 * D; ++dir) {
+          if (neighbour(cell, dir) >= 0) continue;
+          const int64_t p = parent(cell);
+          if (p < 0) continue;
+          const int64_t pn = neighbour(p, dir);
+          if (pn < 0) continue;
+          to_refine.push_back(pn);
+        }
+      std::sort(to_refine.begin(), to_refine.end());
+      to_refine.erase(std::unique(to_refine.begin(), to_refine.end()), to_refine.end());
+      refine_unbalanced(to_refine);
+      refined.swap(to_refine);
+    }
+  }
+  void leaves(int64_t cell, std::vector<int64_t>& out) const {
+    if (leaf(cell)) {
+      out.push_back(cell);
+      return;
+    }
+    for (int ch = 0; ch < (1 << D); ++ch) leaves(child(cell, ch), out);
+  }
+  std::vector<int64_t> leaves() const {
+    std::vector<int64_t> out;
+    leaves(0, out);
+    return out;
+  }
+};
+
 struct Mesh {
-  int D = 2, level = 0, M = 1;  // M cells per direction
-  int64_t nelem = 0, nif = 0;
-  std::vector<int> cart;        // [3, E] Cartesian cell index
-  std::vector<double> center;   // [D, E]
+  int D = 2, level = 0;
+  int64_t nelem = 0, nif = 0, nmortar = 0;
+  std::vector<int> elevel;               // [E] tree level
+  std::vector<double> center;            // [D, E]
   std::vector<double> inverse_jacobian;  // [E]
   std::vector<double> node_coords;       // [D, n^D, E]
   std::vector<int64_t> if_left, if_right;  // 0-based
   std::vector<int> if_orient;               // 0-based orientation
-  std::vector<int64_t> nbr;  // [E, 2D]: neighbour across face (0:-x,1:+x,2:-y,...)
+  // mortars: [2^(D-1) small elements (lower(_left), ...), large], 0-based;
+  // large side 0 = large element on the negative side (Trixi large_sides 1)
+  std::vector<int64_t> mo_ids;
+  std::vector<int> mo_large_side, mo_orient;
+  // [E, 2D] across face (0:-x,1:+x,2:-y,...): a conforming neighbour (>= 0),
+  // -1 for a domain boundary, -2 - m for a face of mortar m
+  std::vector<int64_t> nbr;
   double length0 = 0;
   double xmin[3] = {0, 0, 0};
+  std::vector<Patch> patches;
 };
 
-static void refine_dfs(Mesh& m, int level, int maxlevel, const double* c, double len,
-                       const int* ci) {
-  if (level >= maxlevel) {
-    for (int d = 0; d < m.D; ++d) m.center.push_back(c[d]);
-    for (int d = 0; d < 3; ++d) m.cart.push_back(ci[d]);
-    return;
-  }
-  const int nchild = 1 << m.D;
-  for (int child = 0; child < nchild; ++child) {
-    double cc[3];
-    int cci[3] = {0, 0, 0};
-    const double child_len = len / 2;
-    for (int d = 0; d < m.D; ++d) {
-      const int bit = (child >> d) & 1;  // _child_signs: x fastest
-      const double sign = bit ? 1.0 : -1.0;
-      cc[d] = c[d] + sign * child_len / 2;
-      cci[d] = 2 * ci[d] + bit;
-    }
-    refine_dfs(m, level + 1, maxlevel, cc, child_len, cci);
-  }
-}
-
-static Mesh make_mesh(int D, int level, const double* xmin, const double* xmax,
-                      const Basis& b, bool periodic = true) {
+static Mesh make_mesh(int D, int level, const double* xmin, const double* xmax, const Basis& b,
+                      bool periodic = true, const std::vector<Patch>& patches = {}) {
   Mesh m;
   m.D = D;
   m.level = level;
-  m.M = 1 << level;
-  double c0[3];
+  m.patches = patches;
+  Tree t;
+  t.D = D;
+  t.periodic = periodic;
+  double c0[3] = {0, 0, 0};
   for (int d = 0; d < D; ++d) {
     c0[d] = (xmin[d] + xmax[d]) / 2;
     m.xmin[d] = xmin[d];
   }
-  m.length0 = xmax[0] - xmin[0];
-  int ci0[3] = {0, 0, 0};
-  refine_dfs(m, 0, level, c0, m.length0, ci0);
-  m.nelem = (int64_t)m.center.size() / D;
+  m.length0 = t.length0 = xmax[0] - xmin[0];
+  const int64_t root_ix[3] = {0, 0, 0};
+  t.add(0, root_ix, c0);
+  // refine_uniformly!: refine! of all leaves, level by level
+  for (int l = 0; l < level; ++l) t.refine(t.leaves());
+  // refinement patches (each one refine! of the leaves inside)
+  for (const Patch& p : patches) {
+    std::vector<int64_t> sel;
+    for (int64_t cell : t.leaves()) {
+      const double* c = t.cells[cell].c;
+      bool in = true;
+      if (p.kind == 0) {
+        for (int d = 0; d < D; ++d) in = in && p.a[d] < c[d] && p.b[d] > c[d];
+      } else {
+        double r2 = 0;
+        for (int d = 0; d < D; ++d) r2 += (c[d] - p.a[d]) * (c[d] - p.a[d]);
+        in = r2 < p.r * p.r;
+      }
+      if (in) sel.push_back(cell);
+    }
+    if (!sel.empty()) t.refine(sel);
+  }
+  const std::vector<int64_t> leaves = t.leaves();
+  m.nelem = (int64_t)leaves.size();
+  std::unordered_map<int64_t, int64_t> c2e;
+  for (int64_t e = 0; e < m.nelem; ++e) c2e[leaves[e]] = e;
   const int n = b.n;
   int nn = 1;
   for (int d = 0; d < D; ++d) nn *= n;
-  // reference_length = integrate(one, nodes, basis): sum of weights
+  // init_elements!: reference_length = integrate(one, basis), node coordinates
   double reference_length = 0;
   for (int i = 0; i < n; ++i) reference_length += 1.0 * b.weights[i];
   const double reference_offset = (b.nodes[0] + b.nodes[n - 1]) / 2;
-  const double dx = m.length0 / (double)(1 << level);
-  const double jac = dx / reference_length;
-  m.inverse_jacobian.assign(m.nelem, 1.0 / jac);
+  m.elevel.resize(m.nelem);
+  m.center.resize((size_t)D * m.nelem);
+  m.inverse_jacobian.resize(m.nelem);
   m.node_coords.resize((size_t)D * nn * m.nelem);
-  for (int64_t e = 0; e < m.nelem; ++e)
+  for (int64_t e = 0; e < m.nelem; ++e) {
+    const Tree::Cell& c = t.cells[leaves[e]];
+    m.elevel[e] = c.level;
+    const double jac = t.length(c.level) / reference_length;
+    m.inverse_jacobian[e] = 1.0 / jac;
+    for (int d = 0; d < D; ++d) m.center[e * D + d] = c.c[d];
     for (int node = 0; node < nn; ++node) {
       int idx[3] = {node % n, (node / n) % n, node / (n * n)};
       for (int d = 0; d < D; ++d)
-        m.node_coords[((size_t)e * nn + node) * D + d] =
-            m.center[e * D + d] + jac * (b.nodes[idx[d]] - reference_offset);
-    }
-  // cartesian -> element map
-  std::vector<int64_t> c2e((size_t)1 << (D * level));
-  auto lin = [&](int i, int j, int k) -> size_t {
-    return (size_t)i + (size_t)m.M * ((size_t)j + (size_t)m.M * (size_t)k);
-  };
-  for (int64_t e = 0; e < m.nelem; ++e)
-    c2e[lin(m.cart[3 * e], m.cart[3 * e + 1], m.cart[3 * e + 2])] = e;
-  m.nbr.assign((size_t)m.nelem * 2 * D, -1);
-  for (int64_t e = 0; e < m.nelem; ++e) {
-    for (int dir = 0; dir < 2 * D; ++dir) {
-      int c[3] = {m.cart[3 * e], m.cart[3 * e + 1], m.cart[3 * e + 2]};
-      const int d = dir / 2;
-      const int cn = c[d] + (dir % 2 ? 1 : -1);
-      if (!periodic && (cn < 0 || cn >= m.M)) continue;  // boundary face
-      c[d] = (cn + m.M) % m.M;
-      m.nbr[e * 2 * D + dir] = c2e[lin(c[0], c[1], c[2])];
-    }
-    // init_interfaces!: per element in order, positive directions only, where
-    // a neighbour exists
-    for (int d = 0; d < D; ++d) {
-      if (m.nbr[e * 2 * D + 2 * d + 1] < 0) continue;
-      m.if_left.push_back(e);
-      m.if_right.push_back(m.nbr[e * 2 * D + 2 * d + 1]);
-      m.if_orient.push_back(d);
+        m.node_coords[((size_t)e * nn + node) * D + d] = c.c[d] + jac * (b.nodes[idx[d]] - reference_offset);
     }
   }
+  m.nbr.assign((size_t)m.nelem * 2 * D, -1);
+  // init_interfaces!: per element, positive directions, same-level leaf neighbour
+  for (int64_t e = 0; e < m.nelem; ++e)
+    for (int d = 0; d < D; ++d) {
+      const int64_t nc = t.neighbour(leaves[e], 2 * d + 1);
+      if (nc < 0 || !t.leaf(nc)) continue;
+      const int64_t r = c2e[nc];
+      m.if_left.push_back(e);
+      m.if_right.push_back(r);
+      m.if_orient.push_back(d);
+      m.nbr[e * 2 * D + 2 * d + 1] = r;
+      m.nbr[r * 2 * D + 2 * d] = e;
+    }
   m.nif = (int64_t)m.if_left.size();
+  // init_mortars!: per element (the large one), all directions, neighbour
+  // refined; the small elements are the neighbour's children facing it, in
+  // child order
+  const int ns = 1 << (D - 1);
+  for (int64_t e = 0; e < m.nelem; ++e)
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      const int64_t nc = t.neighbour(leaves[e], dir);
+      if (nc < 0 || t.leaf(nc)) continue;
+      const int d = dir / 2;
+      const int want = (dir & 1) ? 0 : 1;  // children on the side facing e
+      const int64_t k = (int64_t)m.mo_large_side.size();
+      for (int ch = 0; ch < (1 << D); ++ch) {
+        if (((ch >> d) & 1) != want) continue;
+        const int64_t sc = t.child(nc, ch);
+        if (!t.leaf(sc)) {
+          std::fprintf(stderr, "oracle: unbalanced tree at a mortar\n");
+          std::abort();
+        }
+        const int64_t se = c2e[sc];
+        m.mo_ids.push_back(se);
+        m.nbr[se * 2 * D + (dir ^ 1)] = -2 - k;
+      }
+      m.mo_ids.push_back(e);
+      m.nbr[e * 2 * D + dir] = -2 - k;
+      m.mo_large_side.push_back((dir & 1) ? 0 : 1);
+      m.mo_orient.push_back(d);
+    }
+  m.nmortar = (int64_t)m.mo_large_side.size();
+  (void)ns;
   return m;
 }
 
@@ -762,6 +1081,16 @@ static void calc_alpha(Solver& s, const double* u) {
       const int64_t l = s.m.if_left[f], r = s.m.if_right[f];
       s.alpha[l] = std::max({s.alpha_tmp[l], 0.5 * s.alpha_tmp[r], s.alpha[l]});
       s.alpha[r] = std::max({s.alpha_tmp[r], 0.5 * s.alpha_tmp[l], s.alpha[r]});
+    }
+    // L2 mortars: each small element with the large one (indicators_3d.jl:140-162)
+    const int ns = 1 << (D - 1);
+    for (int64_t k = 0; k < s.m.nmortar; ++k) {
+      const int64_t* ids = &s.m.mo_ids[(size_t)k * (ns + 1)];
+      const int64_t large = ids[ns];
+      for (int q = 0; q < ns; ++q)
+        s.alpha[ids[q]] = std::max({s.alpha_tmp[ids[q]], 0.5 * s.alpha_tmp[large], s.alpha[ids[q]]});
+      for (int q = 0; q < ns; ++q)
+        s.alpha[large] = std::max({s.alpha_tmp[large], 0.5 * s.alpha_tmp[ids[q]], s.alpha[large]});
     }
   }
 }
@@ -891,7 +1220,7 @@ static void boundary_flux(const Solver& s, int bc, const double* ui, int o, int 
   F[1 + o] = p_star;
 }
 
-// rhs_hyperbolic!, dg_2d.jl:113-186 (conforming: no mortars)
+// rhs_hyperbolic!, dg_2d.jl:113-186
 static void rhs(Solver& s, double* du, const double* u, double t) {
   const int n = s.b.n, D = s.eq.D, NV = s.eq.NV, nn = s.nn;
   const int64_t E = s.m.nelem;
@@ -942,12 +1271,85 @@ static void rhs(Solver& s, double* du, const double* u, double t) {
       }
     }
   }
+  // prolong2mortars! + calc_mortar_flux! + mortar_fluxes_to_elements!,
+  // dg_2d.jl:899-1243, dg_3d.jl:770-1335: the large element's trace is
+  // interpolated to each half (quarter) face, the surface flux is taken there
+  // against the small element's trace, copied to the small element, and
+  // L2-projected back to the large face.
+  const int ns = 1 << (D - 1);
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < s.m.nmortar; ++k) {
+    const int o = s.m.mo_orient[k], ls = s.m.mo_large_side[k];
+    const int64_t* ids = &s.m.mo_ids[(size_t)k * (ns + 1)];
+    const int64_t large = ids[ns];
+    const int dir_large = ls == 0 ? 2 * o + 1 : 2 * o;  // large face towards the small ones
+    const int dir_small = dir_large ^ 1;
+    int stride = 1;
+    for (int q = 0; q < o; ++q) stride *= n;
+    auto face_node = [&](int fn, int dir) {
+      const int lo = fn % stride, hi = fn / stride;
+      return lo + hi * stride * n + ((dir & 1) ? (n - 1) * stride : 0);
+    };
+    std::vector<double> ul((size_t)nf * NV), up((size_t)nf * NV), fs((size_t)ns * nf * NV);
+    for (int fn = 0; fn < nf; ++fn)
+      for (int v = 0; v < NV; ++v) ul[fn * NV + v] = u[uidx(s, large, face_node(fn, dir_large), v)];
+    for (int q = 0; q < ns; ++q) {
+      // u_lower / u_upper (2D) and u_{lower,upper}_{left,right} (3D): the
+      // first face axis picks left/right, the second lower/upper
+      const double* F1 = s.b.fwd[q & 1].data();
+      const double* F2 = s.b.fwd[(q >> 1) & 1].data();
+      for (int fn = 0; fn < nf; ++fn) {
+        const int i = fn % n, j = fn / n;
+        for (int v = 0; v < NV; ++v) {
+          double r = 0;
+          if (D == 2) {
+            for (int a = 0; a < n; ++a) r += F1[i * n + a] * ul[a * NV + v];
+          } else {
+            for (int bb = 0; bb < n; ++bb)
+              for (int a = 0; a < n; ++a) r += F1[i * n + a] * F2[j * n + bb] * ul[(a + bb * n) * NV + v];
+          }
+          up[fn * NV + v] = r;
+        }
+      }
+      const int64_t small = ids[q];
+      for (int fn = 0; fn < nf; ++fn) {
+        const double* us = &u[uidx(s, small, face_node(fn, dir_small), 0)];
+        double F[5];
+        if (ls == 0)
+          two_point_flux(s.eq, s.sflux, &up[fn * NV], us, o, F);
+        else
+          two_point_flux(s.eq, s.sflux, us, &up[fn * NV], o, F);
+        for (int v = 0; v < NV; ++v) {
+          fs[((size_t)q * nf + fn) * NV + v] = F[v];
+          s.sfv[sidx(small, dir_small, fn, v)] = F[v];
+        }
+      }
+    }
+    for (int fn = 0; fn < nf; ++fn) {
+      const int i = fn % n, j = fn / n;
+      for (int v = 0; v < NV; ++v) {
+        double r = 0;
+        for (int q = 0; q < ns; ++q) {
+          const double* R1 = s.b.rev[q & 1].data();
+          const double* R2 = s.b.rev[(q >> 1) & 1].data();
+          const double* f = &fs[(size_t)q * nf * NV];
+          if (D == 2) {
+            for (int a = 0; a < n; ++a) r += R1[i * n + a] * f[a * NV + v];
+          } else {
+            for (int bb = 0; bb < n; ++bb)
+              for (int a = 0; a < n; ++a) r += R1[i * n + a] * R2[j * n + bb] * f[(a + bb * n) * NV + v];
+          }
+        }
+        s.sfv[sidx(large, dir_large, fn, v)] = r;
+      }
+    }
+  }
   // prolong2boundaries! + calc_boundary_flux!, dg_2d.jl:680-717, 795-860
   if (!s.periodic) {
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < E; ++e)
       for (int dir = 0; dir < 2 * D; ++dir) {
-        if (s.m.nbr[e * 2 * D + dir] >= 0) continue;
+        if (s.m.nbr[e * 2 * D + dir] != -1) continue;
         const int o = dir / 2, side = dir % 2;
         int stride = 1;
         for (int q = 0; q < o; ++q) stride *= n;
@@ -1088,12 +1490,66 @@ int orc_set_boundaries(void* h, const int* bc, int ic, const double* params) {
     xmin[d] = s.m.xmin[d];
     xmax[d] = s.m.xmin[d] + s.m.length0;
   }
-  s.m = make_mesh(s.eq.D, s.m.level, xmin, xmax, s.b, false);
+  s.m = make_mesh(s.eq.D, s.m.level, xmin, xmax, s.b, false, s.m.patches);
   s.periodic = false;
   for (int dir = 0; dir < 2 * s.eq.D; ++dir) s.bc[dir] = bc[dir];
   s.bc_ic = ic;
   for (int k = 0; k < 8; ++k) s.bc_par[k] = params ? params[k] : 0.0;
   return 0;
+}
+
+// Refinement patches applied after the initial refinement, in order
+// (tree_mesh.jl:186-215): kinds[p] 0 = box, 1 = sphere; params[7 p ...] =
+// coordinates_min[3], coordinates_max[3] (box) or center[3], -, -, -, radius
+// (sphere).  Keeps the periodicity and the boundary conditions.  Returns 0,
+// or -1 for an invalid patch.
+int orc_set_refinement(void* h, int npatches, const int* kinds, const double* params) {
+  Solver& s = *(Solver*)h;
+  std::vector<Patch> patches;
+  for (int k = 0; k < npatches; ++k) {
+    if (kinds[k] != 0 && kinds[k] != 1) return -1;
+    Patch p;
+    p.kind = kinds[k];
+    for (int d = 0; d < 3; ++d) {
+      p.a[d] = params[7 * k + d];
+      p.b[d] = params[7 * k + 3 + d];
+    }
+    p.r = params[7 * k + 6];
+    patches.push_back(p);
+  }
+  double xmin[3], xmax[3];
+  for (int d = 0; d < s.eq.D; ++d) {
+    xmin[d] = s.m.xmin[d];
+    xmax[d] = s.m.xmin[d] + s.m.length0;
+  }
+  s.m = make_mesh(s.eq.D, s.m.level, xmin, xmax, s.b, s.periodic, patches);
+  return 0;
+}
+
+int64_t orc_nmortars(void* h) { return ((Solver*)h)->m.nmortar; }
+
+// cache.mortars: neighbor_ids [2^(D-1) + 1, nmortars] (1-based; small ones
+// first, the large one last), large_sides (1: large element on the negative
+// side), orientations (1-based)
+void orc_get_mortars(void* h, int64_t* neighbor_ids, int64_t* large_sides, int64_t* orientations) {
+  const Solver& s = *(Solver*)h;
+  const int ns1 = (1 << (s.eq.D - 1)) + 1;
+  for (int64_t k = 0; k < s.m.nmortar; ++k) {
+    for (int q = 0; q < ns1; ++q) neighbor_ids[k * ns1 + q] = s.m.mo_ids[k * ns1 + q] + 1;
+    large_sides[k] = s.m.mo_large_side[k] + 1;
+    orientations[k] = s.m.mo_orient[k] + 1;
+  }
+}
+
+// dg.mortar (LobattoLegendreMortarL2): forward_upper, forward_lower,
+// reverse_upper, reverse_lower, each n x n row-major
+void orc_get_mortar_matrices(void* h, double* out) {
+  const Solver& s = *(Solver*)h;
+  const size_t nn = (size_t)s.b.n * s.b.n;
+  std::memcpy(out, s.b.fwd[1].data(), sizeof(double) * nn);
+  std::memcpy(out + nn, s.b.fwd[0].data(), sizeof(double) * nn);
+  std::memcpy(out + 2 * nn, s.b.rev[1].data(), sizeof(double) * nn);
+  std::memcpy(out + 3 * nn, s.b.rev[0].data(), sizeof(double) * nn);
 }
 
 void orc_set_threads(int n) {

@@ -91,6 +91,32 @@ CASES = {
         xmax=[3.141592653589793] * 3, ic="taylor_green", ic_params=[0.1], source="none",
         vi="fluxdiff", volume_flux="ranocha", surface_flux="llf_naive", cfl=1.4,
         tspan=[0.0, 10.0]),
+    "TreeMesh2D Euler: elixir_euler_vortex_mortar_split.jl": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_vortex_mortar_split.jl",
+        ndims=2, polydeg=3, level=4, xmin=[-10.0, -10.0], xmax=[10.0, 10.0],
+        refinement_patches=[dict(type="box", coordinates_min=[0.0, -10.0],
+                                 coordinates_max=[10.0, 10.0])],
+        ic="isentropic_vortex", ic_params=[25.0, 5.0], source="none",
+        vi="fluxdiff", volume_flux="shima_etal", surface_flux="llf_naive", cfl=1.4,
+        tspan=[0.0, 1.0]),
+    "TreeMesh2D Euler: elixir_euler_vortex_mortar_shockcapturing.jl": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_vortex_mortar_shockcapturing.jl",
+        ndims=2, polydeg=3, level=4, xmin=[-10.0, -10.0], xmax=[10.0, 10.0],
+        refinement_patches=[dict(type="box", coordinates_min=[0.0, -10.0],
+                                 coordinates_max=[10.0, 10.0])],
+        ic="isentropic_vortex", ic_params=[25.0, 5.0], source="none",
+        vi="hg", volume_flux="shima_etal", surface_flux="llf_naive", alpha_max=0.5,
+        alpha_min=0.001, alpha_smooth=True, cfl=0.7, tspan=[0.0, 1.0]),
+    "TreeMesh3D Euler: elixir_euler_mortar.jl": dict(
+        file="test/test_tree_3d_euler.jl",
+        elixir="examples/tree_3d_dgsem/elixir_euler_mortar.jl",
+        ndims=3, polydeg=3, level=2, xmin=[0.0] * 3, xmax=[2.0] * 3,
+        refinement_patches=[dict(type="box", coordinates_min=[0.5] * 3,
+                                 coordinates_max=[1.5] * 3)],
+        ic="convergence_test", source="convergence_test", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=0.6, tspan=[0.0, 1.0]),
     "TreeMesh3D Euler: elixir_euler_ec.jl": dict(
         file="test/test_tree_3d_euler.jl",
         elixir="examples/tree_3d_dgsem/elixir_euler_ec.jl",
