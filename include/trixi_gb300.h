@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define TG_API_VERSION 1
+#define TG_API_VERSION 2
 
 typedef enum tg_status_code {
   TG_OK = 0,
@@ -157,6 +157,24 @@ typedef struct tg_config {
   int32_t boundary_conditions[6];
   int32_t boundary_value_function;
   double boundary_value_params[4];
+  /* Non-conforming meshes (TreeMesh with refinement patches): the L2 mortars
+   * of cache.mortars (containers_2d.jl:604-810, containers_3d.jl:591-790) and
+   * the projections of dg.mortar (LobattoLegendreMortarL2,
+   * basis_lobatto_legendre.jl:159-205).  nmortars = 0 (pointers may be NULL)
+   * on conforming meshes.  The face of a large element towards its
+   * 2^(ndims-1) small neighbours, and their faces towards it, take the
+   * fluxes of prolong2mortars! / calc_mortar_flux! /
+   * mortar_fluxes_to_elements! (dg_2d.jl:899-1243, dg_3d.jl:770-1335). */
+  int64_t nmortars;
+  const int64_t* mortar_neighbor_ids;  /* [2^(ndims-1) + 1, nmortars], 1-based:
+                                          the small elements, then the large one */
+  const int64_t* mortar_large_sides;   /* [nmortars]: 1 = large element on the
+                                          negative side, 2 = positive side */
+  const int64_t* mortar_orientations;  /* [nmortars], 1..ndims */
+  const double* mortar_forward_upper;  /* n x n, column-major (as the basis) */
+  const double* mortar_forward_lower;
+  const double* mortar_reverse_upper;
+  const double* mortar_reverse_lower;
 } tg_config;
 
 typedef struct tg_ctx tg_ctx;

@@ -44,7 +44,8 @@ def build(c, precision="fp64", elements_per_block=0):
     solver = T.DGSEM(basis, sflux, vi)
     boundary = c.get("boundary")
     mesh = T.TreeMesh(c["xmin"], c["xmax"], initial_refinement_level=c["level"],
-                      periodicity=boundary is None)
+                      periodicity=boundary is None,
+                      refinement_patches=c.get("refinement_patches", ()))
     src = T.source_terms_convergence_test if c.get("source") == "convergence_test" else None
     ic = IC[c["ic"]][0](c.get("ic_params"))
     bcs = {None: T.boundary_condition_periodic, "slip_wall": T.boundary_condition_slip_wall,
@@ -58,6 +59,8 @@ def build(c, precision="fp64", elements_per_block=0):
                    alpha_max=c.get("alpha_max", 0.5), alpha_min=c.get("alpha_min", 0.001),
                    alpha_smooth=c.get("alpha_smooth", True),
                    source=O.SRC_CONVERGENCE_TEST if src is not None else O.SRC_NONE)
+    if c.get("refinement_patches"):
+        orc.set_refinement(c["refinement_patches"])
     if boundary is not None:
         code = dict(dirichlet=O.BC_DIRICHLET, slip_wall=O.BC_SLIP_WALL)[boundary]
         orc.set_boundaries([code] * (2 * D), IC[c["ic"]][1], c.get("ic_params"))

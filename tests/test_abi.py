@@ -27,7 +27,7 @@ def test_library_exports_every_declared_symbol():
     lib = ctypes.CDLL(_lib.LIB_PATH)
     for name in declared_symbols():
         assert hasattr(lib, name), name
-    assert _lib.load().tg_api_version() == 1
+    assert _lib.load().tg_api_version() == 2
 
 
 def test_invalid_config_is_rejected_without_gpu():
@@ -41,5 +41,7 @@ def test_invalid_config_is_rejected_without_gpu():
     assert rc == -2 and not h.value
     assert "ndims" in _lib.last_error()
     cfg.ndims, cfg.polydeg, cfg.nelements, cfg.ninterfaces = 2, 3, 4, 9
-    assert lib.tg_ctx_create(ctypes.byref(cfg), ctypes.byref(h)) == -2
+    assert lib.tg_ctx_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.TG_ERR_INVALID_ARGUMENT
     assert "interfaces" in _lib.last_error()
+    cfg.ninterfaces, cfg.nmortars = 8, -1
+    assert lib.tg_ctx_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.TG_ERR_INVALID_ARGUMENT

@@ -1,0 +1,164 @@
+"""Non-conforming TreeMesh meshes (refinement patches, L2 mortars) on the GPU.
+
+The mortar pre-pass (prolong2mortars! + calc_mortar_flux! +
+mortar_fluxes_to_elements!, dg_2d.jl:899-1243, dg_3d.jl:770-1335) and the
+element kernels that consume its fluxes must give the oracle's rhs! to 1e-12
+(FP64) on meshes with one and two levels of refinement, in 2D and 3D, for the
+weak form, flux differencing and HG shock capturing (whose smoothing reaches
+across mortars, indicators_2d.jl:104-136); the mixed path stays within its
+FP32 tolerance.  Trixi's three mortar regression goldens are reproduced.
+"""
+import numpy as np
+import pytest
+
+from _cases import load_goldens
+from _gpu_cases import build, perturbed_state, rel_err
+import trixi_gb300 as T
+
+pytestmark = pytest.mark.gpu
+
+
+def box(lo, hi):
+    return dict(type="box", coordinates_min=lo, coordinates_max=hi)
+
+
+def sphere(c, r):
+    return dict(type="sphere", center=c, radius=r)
+
+
+MORTAR_CASES = [
+    dict(ndims=2, polydeg=3, level=3, xmin=[0, 0], xmax=[2, 2], vi="weak", surface_flux="llf",
+         ic="convergence_test", source="convergence_test",
+         refinement_patches=[box([0.5, 0.5], [1.5, 1.5])]),
+    dict(ndims=2, polydeg=3, level=3, xmin=[-2, -2], xmax=[2, 2], vi="fluxdiff",
+         volume_flux="ranocha", surface_flux="llf_naive", ic="weak_blast_wave",
+         refinement_patches=[sphere([0.1, -0.2], 1.2), sphere([0.1, -0.2], 0.6)]),
+    dict(ndims=2, polydeg=4, level=3, xmin=[-2, -2], xmax=[2, 2], vi="hg",
+         volume_flux="shima_etal", surface_flux="llf_naive", ic="weak_blast_wave",
+         refinement_patches=[box([-1.0, -1.0], [0.5, 2.0])]),
+    dict(ndims=2, polydeg=2, level=3, xmin=[-1, -1], xmax=[1, 1], vi="hg", volume_flux="ranocha",
+         surface_flux="llf", ic="kelvin_helmholtz", alpha_max=0.002, alpha_min=0.0001,
+         refinement_patches=[box([-1.5, -0.6], [1.5, 0.6])]),
+    dict(ndims=2, polydeg=3, level=4, xmin=[-10, -10], xmax=[10, 10], vi="weak",
+         surface_flux="ranocha", ic="isentropic_vortex", ic_params=[25.0, 5.0],
+         refinement_patches=[box([0.0, -10.0], [10.0, 10.0])]),
+    dict(ndims=3, polydeg=3, level=2, xmin=[0] * 3, xmax=[2] * 3, vi="weak", surface_flux="llf_naive",
+         ic="convergence_test", source="convergence_test",
+         refinement_patches=[box([0.5] * 3, [1.5] * 3)]),
+    dict(ndims=3, polydeg=3, level=2, xmin=[-2] * 3, xmax=[2] * 3, vi="fluxdiff",
+         volume_flux="ranocha", surface_flux="llf", ic="weak_blast_wave",
+         refinement_patches=[sphere([0.2, 0.0, -0.1], 1.3)]),
+    dict(ndims=3, polydeg=2, level=2, xmin=[-2] * 3, xmax=[2] * 3, vi="hg", volume_flux="shima_etal",
+         surface_flux="llf_naive", ic="weak_blast_wave",
+         refinement_patches=[box([-1.0, -1.0, -3.0], [1.0, 1.0, 0.0])]),
+    dict(ndims=3, polydeg=4, level=1, xmin=[0] * 3, xmax=[2] * 3, vi="fluxdiff",
+         volume_flux="central", surface_flux="llf", ic="convergence_test",
+         source="convergence_test", refinement_patches=[box([0.0] * 3, [1.0] * 3)]),
+]
+
+
+def _id(c):
+    return (f"{c['ndims']}d-p{c['polydeg']}-{c['vi']}-{c.get('volume_flux', '')}-"
+            f"{c['surface_flux']}-{c['ic']}")
+
+
+def _has_mortars(semi):
+    return semi.mortar_neighbor_ids.shape[0] > 0
+
+
+@pytest.mark.parametrize("c", MORTAR_CASES, ids=[_id(c) for c in MORTAR_CASES])
+def test_mortar_rhs_fp64_matches_oracle(c):
+    semi, orc = build(c)
+    assert _has_mortars(semi) and semi.nelements == orc.nelements
+    u = perturbed_state(semi, seed=11)
+    du_gpu = semi.device_context.rhs_host(u, 0.29)
+    du_orc = orc.rhs(u, 0.29)
+    assert rel_err(du_gpu, du_orc) < 1e-12
+
+
+@pytest.mark.parametrize("c", MORTAR_CASES, ids=[_id(c) for c in MORTAR_CASES])
+def test_mortar_rhs_mixed_close_to_oracle(c):
+    semi, orc = build(c, precision="mixed")
+    u = perturbed_state(semi, seed=11)
+    du_gpu = semi.device_context.rhs_host(u, 0.29)
+    du_orc = orc.rhs(u, 0.29)
+    assert rel_err(du_gpu, du_orc) < 2e-4
+
+
+@pytest.mark.parametrize("c", [c for c in MORTAR_CASES if c["vi"] == "hg"], ids=lambda c: _id(c))
+def test_mortar_hg_alpha_matches_oracle(c):
+    semi, orc = build(c)
+    u = perturbed_state(semi, seed=5, amp=0.05)
+    ctx = semi.device_context
+    ctx.upload(u)
+    a_gpu = ctx.alpha()
+    a_orc = orc.alpha(u)
+    assert np.max(np.abs(a_gpu - a_orc)) < 1e-12
+    assert np.any(a_orc > 0)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("mixed", 1e-6)])
+@pytest.mark.parametrize("c", [MORTAR_CASES[1], MORTAR_CASES[3], MORTAR_CASES[6]],
+                         ids=lambda c: _id(c))
+def test_mortar_conservation(c, precision, tol):
+    # the reverse projection of the mortar fluxes is conservative: the domain
+    # sum of w J du vanishes (periodic, no sources)
+    semi, _ = build(c, precision=precision)
+    u = perturbed_state(semi, seed=7)
+    du = semi.device_context.rhs_host(u, 0.0)
+    b = semi.solver.basis
+    D = semi.equations.ndims
+    W = np.einsum("j,i->ji", b.weights, b.weights) if D == 2 else \
+        np.einsum("k,j,i->kji", b.weights, b.weights, b.weights)
+    J = (1.0 / semi.inverse_jacobian) ** D
+    nv = du.shape[-1]
+    wj = (J[:, None] * W.reshape(1, -1)).reshape(-1, 1)
+    tot = np.sum(du.reshape(-1, nv) * wj, axis=0)
+    scale = np.sum(np.abs(du.reshape(-1, nv)) * wj, axis=0)
+    assert np.all(np.abs(tot) <= tol * scale)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("ndims", [2, 3])
+def test_mortar_free_stream(ndims, precision):
+    c = dict(ndims=ndims, polydeg=3, level=2, xmin=[-1] * ndims, xmax=[1] * ndims,
+             vi="fluxdiff", volume_flux="ranocha", surface_flux="llf", ic="constant",
+             refinement_patches=[box([-1.0] * ndims, [0.0] * ndims)])
+    semi, _ = build(c, precision=precision)
+    assert _has_mortars(semi)
+    du = semi.device_context.rhs_host(semi.compute_coefficients(0.0), 0.0)
+    assert np.max(np.abs(du)) < (1e-12 if precision == "fp64" else 1e-4)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("c", [MORTAR_CASES[0], MORTAR_CASES[2], MORTAR_CASES[5]],
+                         ids=lambda c: _id(c))
+def test_mortar_steps_match_oracle(c, precision):
+    semi, orc = build(c, precision=precision)
+    u0 = semi.compute_coefficients(0.0)
+    ctx = semi.device_context
+    ctx.upload(u0)
+    t, n = ctx.step(6, 0.8, 100.0, 0.0)
+    u_orc, t_orc, n_orc = orc.solve(u0, 0.0, 100.0, 0.8, max_steps=6)
+    assert n == n_orc == 6
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    assert abs(t - t_orc) <= tol * t_orc
+    assert rel_err(ctx.download(), u_orc) < tol
+
+
+GOLDENS = load_goldens()
+MORTAR_GOLDENS = sorted(k for k in GOLDENS if GOLDENS[k].get("refinement_patches"))
+
+
+@pytest.mark.parametrize("name", MORTAR_GOLDENS)
+def test_mixed_mortar_goldens_within_1p1x_of_fp64(name):
+    c = dict(GOLDENS[name])
+    errs = {}
+    for prec in ("fp64", "mixed"):
+        semi, _ = build(c, precision=prec)
+        ana = T.AnalysisCallback(semi)
+        T.solve(T.semidiscretize(semi, c["tspan"]), T.CarpenterKennedy2N54(), dt=1.0,
+                callback=T.CallbackSet(T.StepsizeCallback(cfl=c["cfl"]), ana))
+        errs[prec] = ana.l2
+    np.testing.assert_allclose(errs["fp64"], c["l2"], rtol=1e-8)
+    assert errs["mixed"][0] <= 1.1 * errs["fp64"][0]

@@ -120,3 +120,102 @@ def test_boundary_conditions_must_match_periodicity():
             T.TreeMesh((0, 0), (1, 1), initial_refinement_level=1, periodicity=(True, False)),
             eq, T.initial_condition_convergence_test, T.DGSEM(polydeg=3),
             boundary_conditions=T.boundary_condition_slip_wall)
+
+
+@pytest.mark.parametrize("polydeg", [1, 2, 3, 4, 5, 7])
+def test_mortar_matrices_match_oracle(polydeg):
+    m = T.MortarL2(T.LobattoLegendreBasis(polydeg))
+    orc = O.Oracle(2, polydeg, 1, [0, 0], [1, 1])
+    for mine, ref in zip((m.forward_upper, m.forward_lower, m.reverse_upper, m.reverse_lower),
+                         orc.mortar_matrices()):
+        np.testing.assert_allclose(mine, ref, rtol=0, atol=1e-14)
+    # interpolation reproduces constants; the two reverse projections of a
+    # constant flux add up to it
+    for F in (m.forward_upper, m.forward_lower):
+        np.testing.assert_allclose(F.sum(axis=1), 1.0, atol=1e-14)
+    np.testing.assert_allclose((m.reverse_upper + m.reverse_lower).sum(axis=1), 1.0, atol=1e-14)
+
+
+PATCH_CASES = [
+    (2, 4, [-10.0] * 2, [10.0] * 2, [dict(type="box", coordinates_min=(0.0, -10.0),
+                                          coordinates_max=(10.0, 10.0))]),
+    (2, 3, [-32.0] * 2, [32.0] * 2, [dict(type="box", coordinates_min=(-40.0, -5.0),
+                                          coordinates_max=(40.0, 5.0))] * 2),
+    (2, 3, [-1.0] * 2, [1.0] * 2, [dict(type="sphere", center=(0.1, 0.2), radius=0.5),
+                                   dict(type="sphere", center=(0.1, 0.2), radius=0.2)]),
+    (3, 2, [0.0] * 3, [2.0] * 3, [dict(type="box", coordinates_min=(0.5,) * 3,
+                                       coordinates_max=(1.5,) * 3)]),
+    (3, 2, [-1.0] * 3, [1.0] * 3, [dict(type="sphere", center=(0.3, 0.0, 0.0), radius=0.4)] * 3),
+]
+
+
+@pytest.mark.parametrize("ndims,level,xmin,xmax,patches", PATCH_CASES)
+def test_refined_treemesh_matches_oracle(ndims, level, xmin, xmax, patches):
+    # refine_box!/refine_sphere! with 2:1 rebalancing, leaf order, interfaces,
+    # mortars and per-element geometry (abstract_tree.jl, containers_{2,3}d.jl)
+    mesh = T.TreeMesh(xmin, xmax, initial_refinement_level=level, refinement_patches=patches)
+    eq = T.CompressibleEulerEquations2D(1.4) if ndims == 2 else T.CompressibleEulerEquations3D(1.4)
+    semi = T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_convergence_test,
+                                          T.DGSEM(polydeg=3))
+    orc = O.Oracle(ndims, 3, level, xmin, xmax)
+    orc.set_refinement(patches)
+    om = orc.mesh()
+    assert semi.nelements == orc.nelements and not mesh.is_uniform
+    np.testing.assert_array_equal(semi.neighbor_ids, om["neighbor_ids"])
+    np.testing.assert_array_equal(semi.orientations, om["orientations"])
+    ids, ls, orient = orc.mortars()
+    assert ids.shape[0] > 0
+    np.testing.assert_array_equal(semi.mortar_neighbor_ids, ids)
+    np.testing.assert_array_equal(semi.mortar_large_sides, ls)
+    np.testing.assert_array_equal(semi.mortar_orientations, orient)
+    np.testing.assert_allclose(semi.inverse_jacobian, om["inverse_jacobian"], rtol=1e-15)
+    np.testing.assert_allclose(semi.node_coordinates, om["node_coordinates"], rtol=0, atol=1e-13)
+    # every element face is covered exactly once by an interface side, a mortar side
+    # or (periodic mesh) nothing else
+    E, D = semi.nelements, ndims
+    cover = np.zeros((E, 2 * D), dtype=int)
+    for (l, r), o in zip(semi.neighbor_ids, semi.orientations):
+        cover[l - 1, 2 * (o - 1) + 1] += 1
+        cover[r - 1, 2 * (o - 1)] += 1
+    ns = 1 << (D - 1)
+    for row, side, o in zip(ids, ls, orient):
+        dl = 2 * (o - 1) + (1 if side == 1 else 0)
+        for q in range(ns):
+            cover[row[q] - 1, dl ^ 1] += 1
+        cover[row[ns] - 1, dl] += 1
+    assert np.all(cover == 1)
+
+
+def test_refined_mesh_config_carries_mortars():
+    from trixi_gb300.semidiscretization import make_config
+    patches = [dict(type="box", coordinates_min=(0.5,) * 3, coordinates_max=(1.5,) * 3)]
+    mesh = T.TreeMesh([0.0] * 3, [2.0] * 3, initial_refinement_level=2, refinement_patches=patches)
+    semi = T.SemidiscretizationHyperbolic(mesh, T.CompressibleEulerEquations3D(1.4),
+                                          T.initial_condition_convergence_test, T.DGSEM(polydeg=3),
+                                          source_terms=T.source_terms_convergence_test)
+    cfg, keep = make_config(semi)
+    assert cfg.nmortars == 24 and cfg.ninterfaces == 300 and cfg.nelements == 120
+    ids = np.ctypeslib.as_array(cfg.mortar_neighbor_ids, shape=(24 * 5,))
+    np.testing.assert_array_equal(ids.reshape(24, 5), semi.mortar_neighbor_ids)
+    n = 4
+    fu = np.ctypeslib.as_array(cfg.mortar_forward_upper, shape=(n * n,)).reshape(n, n, order="F")
+    np.testing.assert_array_equal(fu, semi.solver.mortar.forward_upper)
+    # uniform meshes pass no mortars
+    semi_u = T.SemidiscretizationHyperbolic(T.TreeMesh([0.0] * 2, [2.0] * 2, 2),
+                                            T.CompressibleEulerEquations2D(1.4),
+                                            T.initial_condition_convergence_test, T.DGSEM(polydeg=3))
+    cfg_u, _ = make_config(semi_u)
+    assert cfg_u.nmortars == 0
+
+
+def test_refinement_patch_validation():
+    with pytest.raises(ValueError):
+        T.TreeMesh([0.0] * 2, [1.0] * 2, 2, refinement_patches=[dict(type="cone")])
+    with pytest.raises(ValueError):
+        T.TreeMesh([0.0] * 2, [1.0] * 2, 2,
+                   refinement_patches=[dict(type="box", coordinates_min=(0.5, 0.5),
+                                            coordinates_max=(0.2, 0.9))])
+    m = T.TreeMesh([0.0] * 2, [1.0] * 2, 2,
+                   refinement_patches=[dict(type="box", coordinates_min=(5.0, 5.0),
+                                            coordinates_max=(6.0, 6.0))])
+    assert m.nelements == 16 and m.is_uniform and m.element_length() == 0.25

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/trixi_gb300.h"
@@ -391,19 +392,145 @@ __global__ void boundary_ghost_kernel(const DgParams P, const float2* __restrict
   }
 }
 
+// Mortar pre-pass (prolong2mortars! + calc_mortar_flux! +
+// mortar_fluxes_to_elements!, dg_2d.jl:899-1243, dg_3d.jl:770-1335) for the
+// stage's input state, in FP64, one block per mortar: the large element's
+// trace is interpolated to each half (2D) or quarter (3D) face with
+// forward_{lower,upper} (one matrix per face axis), the surface flux is taken
+// there against the small element's trace, and the small faces' fluxes are
+// projected back onto the large face with reverse_{lower,upper}.  mtab per
+// mortar: the 2^(D-1) small elements (first face axis fastest), the large
+// one, large side (0: large element on the negative side), orientation.
+// The flux of mortar face slot m (2^(D-1) + 1) + q (q: small element q, then
+// the large one) goes to out64 (FP64 contexts) or, as float-float, to
+// outff at slot + ff_offset (mixed contexts, after the boundary faces).
+template <int D, typename S>
+__global__ void __launch_bounds__(128)
+    mortar_flux_kernel(const DgParams P, const S* __restrict__ u, const int32_t* __restrict__ mtab,
+                       const double* __restrict__ mmat, int64_t M, int N, int64_t ff_offset,
+                       double* __restrict__ out64, float2* __restrict__ outff) {
+  constexpr int NV = D + 2, NS = 1 << (D - 1);
+  constexpr int MAXF = D == 2 ? MAXN : MAXN * MAXN;
+  __shared__ double s_mat[4 * MAXN * MAXN];  // forward lower, upper; reverse lower, upper
+  __shared__ double s_ul[MAXF * NV];         // large element's trace
+  __shared__ double s_f[NS * MAXF * NV];     // fluxes on the small faces
+  const int64_t m = blockIdx.x;
+  if (m >= M) return;
+  const int tid = threadIdx.x;
+  const int NF = D == 2 ? N : N * N, NN = NF * N, NM = N * N;
+  for (int k = tid; k < 4 * NM; k += blockDim.x) s_mat[k] = mmat[k];
+  const int32_t* t = mtab + m * (NS + 3);
+  const int ls = t[NS + 1], o = t[NS + 2];
+  const int dir_large = ls == 0 ? 2 * o + 1 : 2 * o;  // large face towards the small ones
+  const int dir_small = dir_large ^ 1;
+  const int Sd = o == 0 ? 1 : (o == 1 ? N : N * N);
+  auto face_node = [&](int fn, int dir) {
+    return (fn % Sd) + (fn / Sd) * Sd * N + ((dir & 1) ? (N - 1) * Sd : 0);
+  };
+  auto load = [&](int64_t e, int node, double* x) {
+    const S* p = u + ((size_t)e * NN + node) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      if constexpr (std::is_same<S, double>::value)
+        x[v] = p[v];
+      else
+        x[v] = (double)p[v].x + (double)p[v].y;  // float-float pair
+    }
+  };
+  auto store = [&](int64_t slot, int fn, const double* f) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const size_t k = ((size_t)slot * NF + fn) * NV + v;
+      if (out64) {
+        out64[k] = f[v];
+      } else {
+        const float hi = (float)f[v];
+        outff[(size_t)ff_offset * NF * NV + k] = make_float2(hi, (float)(f[v] - (double)hi));
+      }
+    }
+  };
+  for (int fn = tid; fn < NF; fn += blockDim.x) {
+    double x[NV];
+    load(t[NS], face_node(fn, dir_large), x);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) s_ul[fn * NV + v] = x[v];
+  }
+  __syncthreads();
+  const double gamma = P.gamma, igm1 = P.inv_gamma_minus_one;
+  using Eu = Euler<D, double>;
+  for (int it = tid; it < NS * NF; it += blockDim.x) {
+    const int q = it / NF, fn = it - q * NF;
+    const int i = fn % N, j = fn / N;
+    const double* F1 = s_mat + (q & 1) * NM;
+    const double* F2 = s_mat + ((q >> 1) & 1) * NM;
+    double up[NV], us[NV], wp[NV], ws[NV], F[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) up[v] = 0.0;
+    if (D == 2) {
+      for (int a = 0; a < N; ++a) {
+        const double c = F1[i * N + a];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) up[v] += c * s_ul[a * NV + v];
+      }
+    } else {
+      for (int b = 0; b < N; ++b)
+        for (int a = 0; a < N; ++a) {
+          const double c = F1[i * N + a] * F2[j * N + b];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) up[v] += c * s_ul[(a + b * N) * NV + v];
+        }
+    }
+    load(t[q], face_node(fn, dir_small), us);
+    Eu::cons2prim(up, wp, gamma);
+    Eu::cons2prim(us, ws, gamma);
+    if (ls == 0)
+      Eu::two_point(P.surface_flux, up, wp, us, ws, o, gamma, igm1, F);
+    else
+      Eu::two_point(P.surface_flux, us, ws, up, wp, o, gamma, igm1, F);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) s_f[it * NV + v] = F[v];
+    store(m * (NS + 1) + q, fn, F);
+  }
+  __syncthreads();
+  for (int fn = tid; fn < NF; fn += blockDim.x) {
+    const int i = fn % N, j = fn / N;
+    double r[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) r[v] = 0.0;
+    for (int q = 0; q < NS; ++q) {
+      const double* R1 = s_mat + (2 + (q & 1)) * NM;
+      const double* R2 = s_mat + (2 + ((q >> 1) & 1)) * NM;
+      const double* f = s_f + (size_t)q * NF * NV;
+      if (D == 2) {
+        for (int a = 0; a < N; ++a) {
+          const double c = R1[i * N + a];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) r[v] += c * f[a * NV + v];
+        }
+      } else {
+        for (int b = 0; b < N; ++b)
+          for (int a = 0; a < N; ++a) {
+            const double c = R1[i * N + a] * R2[j * N + b];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) r[v] += c * f[(a + b * N) * NV + v];
+          }
+      }
+    }
+    store(m * (NS + 1) + NS, fn, r);
+  }
+}
+
 // apply_smoothing! as a gather (indicators_2d.jl:104-136): alpha_e =
-// max(raw_e, 0.5 * raw_n for every face neighbour n).
+// max(raw_e, 0.5 * raw_n for every element n across a face or a mortar).
 template <typename R>
 __global__ void smooth_alpha_kernel(const R* __restrict__ raw, const int32_t* __restrict__ nbr,
-                                    int64_t E, int nfaces, int smooth, double* __restrict__ out) {
+                                    int64_t E, int nfaces, int smooth, int32_t nbc,
+                                    const int32_t* __restrict__ mnbr, double* __restrict__ out) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
   R a = raw[e];
   if (smooth)
-    for (int f = 0; f < nfaces; ++f) {
-      const int32_t nb = nbr[e * nfaces + f];  // interfaces only
-      if (nb >= 0) a = fmax(a, R(0.5) * raw[nb]);
-    }
+    for (int f = 0; f < nfaces; ++f) a = smooth_over_face<R>(a, nbr[e * nfaces + f], raw, nbc, mnbr);
   out[e] = (double)a;
 }
 
@@ -437,7 +564,14 @@ struct tg_ctx {
   float4* d_scn = nullptr;            // and of the node offsets (one table)
   int64_t nbound = 0;                 // boundary faces (non-periodic meshes)
   int32_t* d_bface = nullptr;         // [nbound][2]: element, direction
-  float2* d_ghost = nullptr;          // mixed: [nbound][NF][NV] boundary pre-pass output
+  float2* d_ghost = nullptr;          // mixed: [nbound + nmface][NF][NV] pre-pass output
+  int64_t nmortar = 0;                // L2 mortars
+  int64_t nmface = 0;                 // mortar face slots (2^(D-1) + 1 per mortar)
+  int32_t* d_mtab = nullptr;          // [nmortar][2^(D-1) + 3]: elements, large side, orientation
+  int32_t* d_mnbr = nullptr;          // [nmface][4]: elements across each mortar face
+  double* d_mmat = nullptr;           // forward lower/upper, reverse lower/upper (row-major)
+  double* d_mflux = nullptr;          // fp64: [nmface][NF][NV] mortar pre-pass output
+  int8_t* d_scls = nullptr;           // mixed: size class of each element (source tables)
   double* d_weights = nullptr;
   double* d_partial = nullptr;
   double* d_sums = nullptr;
@@ -489,7 +623,7 @@ static void free_ctx(tg_ctx* c) {
     if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
   void* ptrs[] = {c->d_u[0], c->d_u[1], c->d_utmp, c->d_du, c->d_uscratch, c->d_stage64,
                   c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_nbr, c->d_invj, c->d_xline,
-                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_weights, c->d_partial, c->d_sums, c->d_clock,
+                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mflux, c->d_scls, c->d_weights, c->d_partial, c->d_sums, c->d_clock,
                   c->d_status, c->d_speed};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -554,10 +688,33 @@ static int indicator(tg_ctx* c, const void* u) {
   return TG_OK;
 }
 
+// Mortar pre-pass for the state u_in (context representation).
+static void launch_mortars(tg_ctx* c, const void* u_in) {
+  const unsigned nb = (unsigned)c->nmortar;
+  if (c->fp64) {
+    if (c->D == 2)
+      mortar_flux_kernel<2, double><<<nb, 128, 0, c->stream>>>(
+          c->P, (const double*)u_in, c->d_mtab, c->d_mmat, c->nmortar, c->N, 0, c->d_mflux, nullptr);
+    else
+      mortar_flux_kernel<3, double><<<nb, 128, 0, c->stream>>>(
+          c->P, (const double*)u_in, c->d_mtab, c->d_mmat, c->nmortar, c->N, 0, c->d_mflux, nullptr);
+  } else {
+    if (c->D == 2)
+      mortar_flux_kernel<2, float2><<<nb, 128, 0, c->stream>>>(
+          c->P, (const float2*)u_in, c->d_mtab, c->d_mmat, c->nmortar, c->N, c->nbound, nullptr,
+          c->d_ghost);
+    else
+      mortar_flux_kernel<3, float2><<<nb, 128, 0, c->stream>>>(
+          c->P, (const float2*)u_in, c->d_mtab, c->d_mmat, c->nmortar, c->N, c->nbound, nullptr,
+          c->d_ghost);
+  }
+}
+
 // One element-kernel launch.  u_in is in the context representation.
 static int launch_kernel(tg_ctx* c, int mode, const void* u_in, void* u_out, double* du_out,
                          double t_rhs, int stage, bool reduce) {
   int rc;
+  if (c->nmortar > 0) launch_mortars(c, u_in);
   if (c->fp64) {
     StageArgs A{};
     A.alpha_raw = c->d_alpha_raw;
@@ -714,8 +871,7 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     return fail(nullptr, TG_ERR_UNSUPPORTED, "polydeg %d is not compiled for %dD", cfg->polydeg, D);
   if (cfg->nelements <= 0) return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "nelements must be > 0");
   if (cfg->ninterfaces < 0 || cfg->ninterfaces > (int64_t)D * cfg->nelements)
-    return fail(nullptr, TG_ERR_UNSUPPORTED,
-                "more interfaces than element faces: conforming TreeMesh only (no mortars)");
+    return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "more interfaces than element faces");
   if (cfg->volume_integral < 0 || cfg->volume_integral > 2)
     return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "unknown volume integral %d", cfg->volume_integral);
   const int fl[3] = {cfg->volume_flux, cfg->surface_flux, cfg->volume_flux_fv};
@@ -770,8 +926,54 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     a = (int32_t)r;
     b = (int32_t)l;
   }
-  // faces without interface are boundaries of a non-periodic mesh and need a
-  // boundary condition for their direction
+  // ---- L2 mortars: mark their element faces (-2); their slots are numbered
+  //      after the boundary faces below ----
+  const int ns = 1 << (D - 1);
+  const int64_t nm = cfg->nmortars;
+  if (nm < 0 || (nm > 0 && (!cfg->mortar_neighbor_ids || !cfg->mortar_large_sides ||
+                            !cfg->mortar_orientations || !cfg->mortar_forward_upper ||
+                            !cfg->mortar_forward_lower || !cfg->mortar_reverse_upper ||
+                            !cfg->mortar_reverse_lower))) {
+    delete c;
+    return fail(nullptr, TG_ERR_INVALID_ARGUMENT,
+                "mortars need neighbor_ids, large_sides, orientations and the mortar matrices");
+  }
+  std::vector<int32_t> mtab((size_t)nm * (ns + 3)), mnbr((size_t)nm * (ns + 1) * 4, -1);
+  std::vector<int64_t> mface((size_t)nm * (ns + 1));  // element face (e * 2D + dir) of each slot
+  for (int64_t m = 0; m < nm; ++m) {
+    const int64_t o = cfg->mortar_orientations[m] - 1, ls = cfg->mortar_large_sides[m];
+    if (o < 0 || o >= D || (ls != 1 && ls != 2)) {
+      delete c;
+      return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "mortar %lld: invalid orientation or large side",
+                  (long long)m);
+    }
+    const int dir_large = ls == 1 ? (int)(2 * o + 1) : (int)(2 * o);
+    int64_t ids[5];
+    for (int q = 0; q <= ns; ++q) {
+      ids[q] = cfg->mortar_neighbor_ids[m * (ns + 1) + q] - 1;
+      if (ids[q] < 0 || ids[q] >= c->E) {
+        delete c;
+        return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "mortar %lld: element out of range",
+                    (long long)m);
+      }
+      const int64_t face = ids[q] * nf + (q < ns ? (dir_large ^ 1) : dir_large);
+      if (nbr[face] != -1) {
+        delete c;
+        return fail(nullptr, TG_ERR_UNSUPPORTED, "element face used by an interface and a mortar");
+      }
+      nbr[face] = -2;
+      mface[m * (ns + 1) + q] = face;
+      mtab[m * (ns + 3) + q] = (int32_t)ids[q];
+    }
+    mtab[m * (ns + 3) + ns + 1] = ls == 1 ? 0 : 1;
+    mtab[m * (ns + 3) + ns + 2] = (int32_t)o;
+    for (int q = 0; q < ns; ++q) {
+      mnbr[(m * (ns + 1) + q) * 4] = (int32_t)ids[ns];
+      mnbr[(m * (ns + 1) + ns) * 4 + q] = (int32_t)ids[q];
+    }
+  }
+  // faces without interface or mortar are boundaries of a non-periodic mesh
+  // and need a boundary condition for their direction
   bool has_dirichlet = false;
   for (int dir = 0; dir < nf; ++dir) {
     const int bc = cfg->boundary_conditions[dir];
@@ -782,11 +984,11 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     has_dirichlet |= bc == TG_BOUNDARY_DIRICHLET;
   }
   for (size_t k = 0; k < nbr.size(); ++k)
-    if (nbr[k] < 0 && cfg->boundary_conditions[k % nf] == TG_BOUNDARY_PERIODIC) {
+    if (nbr[k] == -1 && cfg->boundary_conditions[k % nf] == TG_BOUNDARY_PERIODIC) {
       delete c;
       return fail(nullptr, TG_ERR_UNSUPPORTED,
-                  "element face without interface and without a boundary condition for "
-                  "direction %d (conforming meshes only: no mortars)", (int)(k % nf));
+                  "element face without interface, mortar or boundary condition (direction %d)",
+                  (int)(k % nf));
     }
   if (has_dirichlet && (!cfg->node_coordinates || cfg->boundary_value_function < TG_IC_CONSTANT ||
                         cfg->boundary_value_function > TG_IC_GAUSSIAN_BLAST)) {
@@ -797,13 +999,16 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   // boundary faces: numbered in element order, nbr = -1 - number
   std::vector<int32_t> bface;
   for (size_t k = 0; k < nbr.size(); ++k)
-    if (nbr[k] < 0) {
+    if (nbr[k] == -1) {
       const int32_t b = (int32_t)(bface.size() / 2);
       bface.push_back((int32_t)(k / nf));
       bface.push_back((int32_t)(k % nf));
       nbr[k] = -1 - b;
     }
   c->nbound = (int64_t)bface.size() / 2;
+  c->nmortar = nm;
+  c->nmface = nm * (ns + 1);
+  for (int64_t sl = 0; sl < c->nmface; ++sl) nbr[mface[sl]] = (int32_t)(-1 - (c->nbound + sl));
 
   // ---- node coordinates along each axis (tensor-product TreeMesh elements) ----
   std::vector<double> xline;
@@ -887,9 +1092,22 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   ALLOC(c->d_u[1], vb);
   ALLOC(c->d_utmp, rsize(c) * (size_t)c->nvalues);
   ALLOC(c->d_nbr, sizeof(int32_t) * nbr.size());
-  if (c->nbound > 0) {
-    ALLOC(c->d_bface, sizeof(int32_t) * bface.size());
-    if (!c->fp64) ALLOC(c->d_ghost, sizeof(float2) * (size_t)c->nbound * (c->NN / N) * c->NV);
+  if (c->nbound > 0) ALLOC(c->d_bface, sizeof(int32_t) * bface.size());
+  if (!c->fp64 && c->nbound + c->nmface > 0)
+    ALLOC(c->d_ghost, sizeof(float2) * (size_t)(c->nbound + c->nmface) * (c->NN / N) * c->NV);
+  std::vector<double> mmat;
+  if (nm > 0) {
+    ALLOC(c->d_mtab, sizeof(int32_t) * mtab.size());
+    ALLOC(c->d_mnbr, sizeof(int32_t) * mnbr.size());
+    ALLOC(c->d_mmat, sizeof(double) * 4 * N * N);
+    if (c->fp64) ALLOC(c->d_mflux, sizeof(double) * (size_t)c->nmface * (c->NN / N) * c->NV);
+    // row-major copies of the column-major n x n mortar matrices
+    const double* src[4] = {cfg->mortar_forward_lower, cfg->mortar_forward_upper,
+                            cfg->mortar_reverse_lower, cfg->mortar_reverse_upper};
+    mmat.resize((size_t)4 * N * N);
+    for (int k = 0; k < 4; ++k)
+      for (int a = 0; a < N; ++a)
+        for (int b = 0; b < N; ++b) mmat[(size_t)k * N * N + a * N + b] = src[k][a + b * N];
   }
   ALLOC(c->d_invj, sizeof(double) * c->E);
   ALLOC(c->d_weights, sizeof(double) * N);
@@ -904,6 +1122,7 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   }
   std::vector<float> invj_f, xline_f;
   std::vector<float4> sc0, scn;
+  std::vector<int8_t> scls;
   if (!c->fp64) {
     invj_f.resize(c->E);
     for (int64_t k = 0; k < c->E; ++k) invj_f[k] = (float)cfg->inverse_jacobian[k];
@@ -914,39 +1133,58 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
       if (c->P.source == SRC_CONVERGENCE_TEST) {
         // source phase pi (sum_d x_d - t) of the mixed path, split into the
         // first node of each element (FP64 -> float-float sin/cos) and the
-        // node offsets from it, which are the same for every element of a
-        // conforming mesh (checked)
+        // node offsets from it, which are the same for all elements of one
+        // size (one table per size class; checked)
         auto ffsc = [](double ph) {
           const double sn = std::sin(M_PI * ph), cs = std::cos(M_PI * ph);
           const float sh = (float)sn, ch = (float)cs;
           return make_float4(sh, ch, (float)(sn - (double)sh), (float)(cs - (double)ch));
         };
         sc0.resize(c->E);
+        scls.resize(c->E);
+        std::vector<double> cls_invj;   // inverse Jacobian of each size class
+        std::vector<int64_t> cls_elem;  // its first element
         for (int64_t e2 = 0; e2 < c->E; ++e2) {
+          size_t k = 0;
+          while (k < cls_invj.size() && cls_invj[k] != cfg->inverse_jacobian[e2]) ++k;
+          if (k == cls_invj.size()) {
+            if (k == 64) {
+              free_ctx(c);
+              return fail(nullptr, TG_ERR_UNSUPPORTED,
+                          "mixed precision source terms: more than 64 element sizes");
+            }
+            cls_invj.push_back(cfg->inverse_jacobian[e2]);
+            cls_elem.push_back(e2);
+          }
+          scls[e2] = (int8_t)k;
           double ph = 0;
           for (int d = 0; d < D; ++d) {
             const double* xl = &xline[((size_t)e2 * D + d) * N];
-            const double* x1 = &xline[(size_t)d * N];
+            const double* x1 = &xline[((size_t)cls_elem[k] * D + d) * N];
             ph += xl[0];
             for (int i = 0; i < N; ++i)
               if (std::fabs((xl[i] - xl[0]) - (x1[i] - x1[0])) > 1e-12 * std::fabs(x1[N - 1] - x1[0])) {
                 free_ctx(c);
                 return fail(nullptr, TG_ERR_UNSUPPORTED,
-                            "mixed precision source terms need elements of one size");
+                            "mixed precision source terms need tensor-product elements of "
+                            "regular node spacing");
               }
           }
           sc0[e2] = ffsc(ph);
         }
         int NN = 1;
         for (int d = 0; d < D; ++d) NN *= N;
-        scn.resize(NN);
-        for (int q = 0; q < NN; ++q) {
-          double ph = 0;
-          for (int d = 0, r = q; d < D; ++d, r /= N) ph += xline[(size_t)d * N + r % N] - xline[(size_t)d * N];
-          scn[q] = ffsc(ph);
-        }
+        scn.resize(cls_elem.size() * NN);
+        for (size_t k = 0; k < cls_elem.size(); ++k)
+          for (int q = 0; q < NN; ++q) {
+            const double* x1 = &xline[(size_t)cls_elem[k] * D * N];
+            double ph = 0;
+            for (int d = 0, r = q; d < D; ++d, r /= N) ph += x1[(size_t)d * N + r % N] - x1[(size_t)d * N];
+            scn[k * NN + q] = ffsc(ph);
+          }
         ALLOC(c->d_sc0, sizeof(float4) * sc0.size());
         ALLOC(c->d_scn, sizeof(float4) * scn.size());
+        ALLOC(c->d_scls, sizeof(int8_t) * scls.size());
       }
     }
   }
@@ -959,12 +1197,18 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
       if (!sc0.empty()) {
         cudaMemcpy(c->d_sc0, sc0.data(), sizeof(float4) * sc0.size(), cudaMemcpyHostToDevice);
         cudaMemcpy(c->d_scn, scn.data(), sizeof(float4) * scn.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(c->d_scls, scls.data(), sizeof(int8_t) * scls.size(), cudaMemcpyHostToDevice);
       }
     }
   }
   cudaMemcpy(c->d_nbr, nbr.data(), sizeof(int32_t) * nbr.size(), cudaMemcpyHostToDevice);
   if (c->nbound > 0)
     cudaMemcpy(c->d_bface, bface.data(), sizeof(int32_t) * bface.size(), cudaMemcpyHostToDevice);
+  if (nm > 0) {
+    cudaMemcpy(c->d_mtab, mtab.data(), sizeof(int32_t) * mtab.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(c->d_mnbr, mnbr.data(), sizeof(int32_t) * mnbr.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(c->d_mmat, mmat.data(), sizeof(double) * mmat.size(), cudaMemcpyHostToDevice);
+  }
   cudaMemcpy(c->d_invj, cfg->inverse_jacobian, sizeof(double) * c->E, cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_weights, c->weights.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
   if (!xline.empty())
@@ -980,6 +1224,9 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   P.nbr = c->d_nbr;
   P.inv_jac = c->d_invj;
   P.xline = c->d_xline;
+  P.nbc = (int32_t)c->nbound;
+  P.mflux = c->d_mflux;
+  P.mnbr = c->d_mnbr;
   // single-precision copy of the parameters for the mixed path
   MixedParams& M = c->MP;
   M.nelements = P.nelements;
@@ -1011,12 +1258,15 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   M.xline = c->d_xline_f;
   M.sc0 = c->d_sc0;
   M.scn = c->d_scn;
-  M.has_wall = 0;
+  M.scls = c->d_scls;
+  M.has_direct = c->nmortar > 0;
   for (int dir = 0; dir < 6; ++dir) {
     M.bc[dir] = P.bc[dir];
-    M.has_wall |= P.bc[dir] == BC_SLIP_WALL;
+    M.has_direct |= P.bc[dir] == BC_SLIP_WALL;
   }
+  M.nbc = (int32_t)c->nbound;
   M.ghost = c->d_ghost;
+  M.mnbr = c->d_mnbr;
   *out = c;
   return TG_OK;
 }
@@ -1432,10 +1682,12 @@ int tg_alpha(tg_ctx* c, const double* u_dev, double* alpha_host) {
   const int64_t nb = (c->E + 127) / 128;
   if (c->fp64)
     smooth_alpha_kernel<double><<<(unsigned)nb, 128, 0, c->stream>>>(
-        (const double*)c->d_alpha_raw, c->d_nbr, c->E, 2 * c->D, c->P.alpha_smooth, c->d_alpha);
+        (const double*)c->d_alpha_raw, c->d_nbr, c->E, 2 * c->D, c->P.alpha_smooth, c->P.nbc,
+        c->d_mnbr, c->d_alpha);
   else
     smooth_alpha_kernel<float><<<(unsigned)nb, 128, 0, c->stream>>>(
-        (const float*)c->d_alpha_raw, c->d_nbr, c->E, 2 * c->D, c->P.alpha_smooth, c->d_alpha);
+        (const float*)c->d_alpha_raw, c->d_nbr, c->E, 2 * c->D, c->P.alpha_smooth, c->P.nbc,
+        c->d_mnbr, c->d_alpha);
   CUDA_TRY(c, cudaGetLastError());
   CUDA_TRY(c, cudaMemcpyAsync(alpha_host, c->d_alpha, sizeof(double) * c->E, cudaMemcpyDeviceToHost,
                               c->stream));

@@ -52,14 +52,38 @@ struct DgParams {
   int32_t volume_flux, surface_flux, fv_flux, source;
   double alpha_max, alpha_min, alpha_atol, hg_threshold, hg_parameter_s;
   int32_t alpha_smooth;
-  const int32_t* nbr;     // [E][2D] neighbour across face (-x,+x,-y,+y,-z,+z), -1: boundary
+  // [E][2D] neighbour across face (-x,+x,-y,+y,-z,+z); a face without a
+  // conforming neighbour has nbr = -1 - b: b < nbc a boundary face, else
+  // mortar face slot b - nbc
+  const int32_t* nbr;
   const double* inv_jac;  // [E]
   const double* xline;    // [E][D][N] node coordinates along each axis, or null
   // boundary conditions of the faces with nbr < 0 (non-periodic meshes)
   int32_t bc[6];          // per direction, BoundaryKind
   int32_t bc_ic;          // Dirichlet values: InitialConditionKind
   double bc_par[4];       // and its free constants
+  // L2 mortars: fluxes of the mortar faces from the mortar pre-pass
+  int32_t nbc;            // boundary faces (nbr = -1 - b with b < nbc)
+  const double* mflux;    // [mortar face slot][NF][NV]
+  const int32_t* mnbr;    // [mortar face slot][4]: elements across it (-1: none)
 };
+
+// max(a, 0.5 raw[n]) over the elements n across face `dir` of e: the
+// conforming neighbour, or the elements on the other side of a mortar
+// (apply_smoothing!, indicators_2d.jl:104-136, indicators_3d.jl:125-166).
+template <typename R>
+__device__ __forceinline__ R smooth_over_face(R a, int32_t nb, const R* raw, int32_t nbc,
+                                              const int32_t* mnbr) {
+  if (nb >= 0) return fmax(a, R(0.5) * raw[nb]);
+  const int32_t b = -1 - nb - nbc;
+  if (b < 0) return a;  // domain boundary
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int32_t m = mnbr[4 * b + q];
+    if (m >= 0) a = fmax(a, R(0.5) * raw[m]);
+  }
+  return a;
+}
 
 // Device-resident clock of the time loop (one per context).
 struct Clock {
@@ -244,10 +268,8 @@ __global__ void __launch_bounds__(EPB * Pow<N, D>::value)
     R a = raw[e];
     if (P.alpha_smooth) {
 #pragma unroll
-      for (int dir = 0; dir < 2 * D; ++dir) {
-        const int32_t nb = P.nbr[e * 2 * D + dir];  // interfaces only
-        if (nb >= 0) a = fmax(a, R(0.5) * raw[nb]);
-      }
+      for (int dir = 0; dir < 2 * D; ++dir)
+        a = smooth_over_face<R>(a, P.nbr[e * 2 * D + dir], raw, P.nbc, P.mnbr);
     }
     s_alpha[slot] = a;
     if (A.alpha_out) reinterpret_cast<R*>(A.alpha_out)[e] = a;
@@ -283,6 +305,13 @@ __global__ void __launch_bounds__(EPB * Pow<N, D>::value)
     R uo[NV], un[NV], ul[NV], ur[NV], wl[NV], wr[NV], F[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) uo[v] = s_c[v * SP + sl * NN + own];
+    if (nb < 0 && -1 - nb >= P.nbc) {
+      // mortar face: flux from the mortar pre-pass
+      const double* mf = P.mflux + ((size_t)(-1 - nb - P.nbc) * NF + fn) * NV;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) s_face[((sl * 2 * D + dir) * NF + fn) * NV + v] = (R)mf[v];
+      continue;
+    }
     if (nb < 0) {
       boundary_face_flux<D, N, R>(P, A, e0 + sl, own, d, side, uo, gamma, igm1, F);
 #pragma unroll

@@ -24,11 +24,11 @@ static int launch_mixed_one(const MixedParams& P, const MixedArgs& A, cudaStream
 }
 
 // Flux-specialised instances for polydeg 3 (flux_ranocha volume flux with the
-// two Lax-Friedrichs surface fluxes, no slip wall); every other choice
-// dispatches at run time.
+// two Lax-Friedrichs surface fluxes, no slip wall or mortar); every other
+// choice dispatches at run time.
 template <int D, int VI, int EPB>
 static int launch_mixed_n4(const MixedParams& P, const MixedArgs& A, cudaStream_t s) {
-  const bool ranocha = (VI == VI_WEAK || P.volume_flux == FLUX_RANOCHA) && !P.has_wall;
+  const bool ranocha = (VI == VI_WEAK || P.volume_flux == FLUX_RANOCHA) && !P.has_direct;
   if (ranocha && P.surface_flux == FLUX_LLF)
     return launch_mixed_one<D, 4, VI, VI == VI_WEAK ? -1 : FLUX_RANOCHA, FLUX_LLF, EPB>(P, A, s);
   if (ranocha && P.surface_flux == FLUX_LLF_NAIVE)

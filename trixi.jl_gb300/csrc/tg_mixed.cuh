@@ -59,17 +59,21 @@ struct MixedParams {
   const float* xline;       // [E][D][N] or null (unused by the stage kernel)
   // source phase pi (sum_d x_d - t) as float-float sin/cos parts
   // (sin_hi, cos_hi, sin_lo, cos_lo): of the first node of each element, and
-  // of each node's offset from the first node (one table: all elements of a
-  // conforming mesh have one size)
+  // of each node's offset from the first node (one table per element size)
   const float4* sc0;        // [E]
-  const float4* scn;        // [NN]
-  // Non-periodic meshes: a face without neighbour has nbr = -1 - b, b its
-  // boundary-face index; ghost[b][face node][v] holds, for the current stage,
-  // the Dirichlet state (float-float) or, on slip walls (bc), the wall flux
-  // (float-float), written by a pre-pass from the stage's input state.
+  const float4* scn;        // [size class][NN]
+  const int8_t* scls;       // [E] size class of each element
+  // Faces without a conforming neighbour have nbr = -1 - b.  b < nbc: a
+  // boundary face of a non-periodic mesh; ghost[b][face node][v] holds, for
+  // the current stage, the Dirichlet state (float-float) or, on slip walls
+  // (bc), the wall flux (float-float), written by a pre-pass from the stage's
+  // input state.  b >= nbc: a mortar face; ghost[b] holds its flux from the
+  // mortar pre-pass, and mnbr[b - nbc] the elements across it.
   int32_t bc[6];            // per direction, BoundaryKind
-  int32_t has_wall;         // any bc == BC_SLIP_WALL
+  int32_t has_direct;       // any face whose flux is given (slip wall, mortar)
+  int32_t nbc;
   const float2* ghost;      // [B][NF][NV]
+  const int32_t* mnbr;      // [mortar face slot][4]
 };
 
 struct MixedArgs {
@@ -612,11 +616,11 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
                             ? s_u + ((int)nbs * NN + lb + (side ? 0 : (N - 1) * S)) * NV
                             : s_fu + ((slot * 2 * D + dir) * NF + line) * NV;
     float F[NV];
-    // slip walls are compiled into the run-time flux kernels only: contexts
-    // with a wall use those (the flux-specialised instances keep registers
-    // for the periodic hot path)
+    // faces with a given flux (slip walls, mortars) are compiled into the
+    // run-time flux kernels only: contexts with such faces use those (the
+    // flux-specialised instances keep registers for the conforming hot path)
     bool wall = false;
-    if constexpr (SF < 0) wall = nb < 0 && P.bc[dir] == BC_SLIP_WALL;
+    if constexpr (SF < 0) wall = nb < 0 && (-1 - nb >= P.nbc || P.bc[dir] == BC_SLIP_WALL);
     if (wall) {
       Dv::wall_flux(R, src, dd, vro, eos, F);
     } else {
@@ -745,10 +749,8 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
       float a = A.alpha_raw[e];
       if (P.alpha_smooth) {
 #pragma unroll
-        for (int dir = 0; dir < 2 * D; ++dir) {
-          const int32_t nb = P.nbr[e * 2 * D + dir];  // interfaces only
-          if (nb >= 0) a = fmaxf(a, 0.5f * A.alpha_raw[nb]);
-        }
+        for (int dir = 0; dir < 2 * D; ++dir)
+          a = smooth_over_face<float>(a, P.nbr[e * 2 * D + dir], A.alpha_raw, P.nbc, P.mnbr);
       }
       s_elem[tid * 8 + 0] = a;
       if (A.alpha_out) A.alpha_out[e] = a;
@@ -779,6 +781,7 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
       el[2] = cs.x;
       el[3] = sn.y;
       el[4] = cs.y;
+      el[5] = (float)P.scls[e];
     }
   }
   cp_async_wait_all();
@@ -856,8 +859,8 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
       // phase of this node: element part + node offset, each float-float, so
       // that the only rounding is the final one (which varies with t instead
       // of repeating the same pattern every stage)
-      const float4 o = P.scn[node];
       const float* el = s_elem + sl * 8;
+      const float4 o = P.scn[(int)el[5] * NN + node];
       const float2 sn = ff_dot2(el[1], el[3], o.y, o.w, el[2], el[4], o.x, o.z);
       const float2 cs = ff_dot2(el[2], el[4], o.y, o.w, -el[1], -el[3], o.x, o.z);
       float src[NV];

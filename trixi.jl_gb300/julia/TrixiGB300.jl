@@ -45,6 +45,14 @@ struct TgConfig
     boundary_conditions::NTuple{6, Int32}  # per direction: 0 periodic, 1 Dirichlet, 2 slip wall
     boundary_value_function::Int32         # tg_initial_condition of Dirichlet faces
     boundary_value_params::NTuple{4, Float64}
+    nmortars::Int64                        # cache.mortars (L2 mortars)
+    mortar_neighbor_ids::Ptr{Int64}
+    mortar_large_sides::Ptr{Int64}
+    mortar_orientations::Ptr{Int64}
+    mortar_forward_upper::Ptr{Float64}     # dg.mortar
+    mortar_forward_lower::Ptr{Float64}
+    mortar_reverse_upper::Ptr{Float64}
+    mortar_reverse_lower::Ptr{Float64}
 end
 
 const TG_VOLUME_WEAK_FORM, TG_VOLUME_FLUX_DIFFERENCING, TG_VOLUME_SHOCK_CAPTURING_HG = 0, 1, 2
@@ -116,7 +124,20 @@ function config(semi, precision, device)
                     pointer(cache.elements.inverse_jacobian),
                     pointer(cache.elements.node_coordinates), 0,
                     boundary_codes(semi.boundary_conditions, ndims(mesh)),
-                    boundary_value_code(semi.boundary_conditions)...)
+                    boundary_value_code(semi.boundary_conditions)...,
+                    mortar_fields(solver, cache)...)
+end
+
+# cache.mortars / dg.mortar of a TreeMesh with L2 mortars (none: zero and NULL)
+function mortar_fields(solver, cache)
+    m = solver.mortar
+    nm = hasproperty(cache, :mortars) ? Trixi.nmortars(cache.mortars) : 0
+    nm == 0 && return (Int64(0), Ptr{Int64}(C_NULL), Ptr{Int64}(C_NULL), Ptr{Int64}(C_NULL),
+                       Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL),
+                       Ptr{Float64}(C_NULL))
+    return (Int64(nm), pointer(cache.mortars.neighbor_ids), pointer(cache.mortars.large_sides),
+            pointer(cache.mortars.orientations), pointer(m.forward_upper),
+            pointer(m.forward_lower), pointer(m.reverse_upper), pointer(m.reverse_lower))
 end
 
 # boundary_conditions of the semidiscretization (digested: one per direction

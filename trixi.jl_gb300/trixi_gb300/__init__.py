@@ -19,7 +19,7 @@ the host side: mesh/basis setup, the C-ABI binding and the driver loop.
 """
 from ._lib import TrixiGB300Error, load as load_library  # noqa: F401
 from .analysis import calc_error_norms  # noqa: F401
-from .basis import LobattoLegendreAnalyzer, LobattoLegendreBasis  # noqa: F401
+from .basis import LobattoLegendreAnalyzer, LobattoLegendreBasis, MortarL2  # noqa: F401
 from .equations import (CompressibleEulerEquations2D, CompressibleEulerEquations3D,  # noqa: F401
                         FluxLaxFriedrichs, cons2prim, density_pressure, flux_central,
                         flux_lax_friedrichs, flux_ranocha, flux_shima_etal,

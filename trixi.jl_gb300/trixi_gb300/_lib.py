@@ -13,6 +13,8 @@ PKG_ROOT = os.path.dirname(_HERE)
 LIB_PATH = os.path.join(PKG_ROOT, "_build", "libtrixi_gb300.so")
 
 TG_OK = 0
+(TG_ERR_INVALID_ARGUMENT, TG_ERR_UNSUPPORTED, TG_ERR_CUDA, TG_ERR_NUMERICAL,
+ TG_ERR_STATE) = -1, -2, -3, -4, -5
 STATUS_NAMES = {-1: "invalid argument", -2: "unsupported", -3: "CUDA error",
                 -4: "numerical failure", -5: "invalid call order"}
 
@@ -75,6 +77,14 @@ class tg_config(ctypes.Structure):
         ("boundary_conditions", ctypes.c_int32 * 6),
         ("boundary_value_function", ctypes.c_int32),
         ("boundary_value_params", ctypes.c_double * 4),
+        ("nmortars", ctypes.c_int64),
+        ("mortar_neighbor_ids", ctypes.POINTER(ctypes.c_int64)),
+        ("mortar_large_sides", ctypes.POINTER(ctypes.c_int64)),
+        ("mortar_orientations", ctypes.POINTER(ctypes.c_int64)),
+        ("mortar_forward_upper", ctypes.POINTER(ctypes.c_double)),
+        ("mortar_forward_lower", ctypes.POINTER(ctypes.c_double)),
+        ("mortar_reverse_upper", ctypes.POINTER(ctypes.c_double)),
+        ("mortar_reverse_lower", ctypes.POINTER(ctypes.c_double)),
     ]
 
 

@@ -102,6 +102,98 @@ def _legendre_normalised(N: int, x: float) -> float:
     return p * math.sqrt(N + 0.5)
 
 
+def _legendre_and_derivative(N: int, x: float):
+    """legendre_polynomial_and_derivative, basis_lobatto_legendre.jl:677-706."""
+    if N == 0:
+        p, dp = 1.0, 0.0
+    elif N == 1:
+        p, dp = x, 1.0
+    else:
+        p2, p1, d2, d1 = 1.0, x, 0.0, 1.0
+        p = dp = 0.0
+        for i in range(2, N + 1):
+            p = ((2 * i - 1) * x * p1 - (i - 1) * p2) / i
+            dp = d2 + (2 * i - 1) * p1
+            p2, p1, d2, d1 = p1, p, d1, dp
+    return p * math.sqrt(N + 0.5), dp * math.sqrt(N + 0.5)
+
+
+def gauss_nodes_weights(n_nodes: int):
+    """Legendre-Gauss nodes and weights, basis_gauss_legendre.jl:149-205
+    (Newton iteration on P_{N+1} from -cos(pi (2i+1) / (2N+2)))."""
+    nodes = np.ones(n_nodes)
+    weights = np.zeros(n_nodes)
+    N = n_nodes - 1
+    if N == 0:
+        return np.zeros(1), np.full(1, 2.0)
+    if N == 1:
+        x = math.sqrt(1.0 / 3)
+        return np.array([-x, x]), np.ones(2)
+    tol = 2 * _EPS
+    for i in range((N + 1) // 2):
+        x = -math.cos(math.pi * (2 * i + 1) / (2 * N + 2))
+        for _ in range(21):
+            p, dp = _legendre_and_derivative(N + 1, x)
+            dx = -p / dp
+            x += dx
+            if abs(dx) < tol * abs(x):
+                break
+        _, dp = _legendre_and_derivative(N + 1, x)
+        nodes[i], nodes[N - i] = x, -x
+        weights[i] = weights[N - i] = (2 * N + 3) / ((1 - x * x) * dp * dp)
+    if n_nodes % 2 == 1:
+        _, dp = _legendre_and_derivative(N + 1, 0.0)
+        nodes[N // 2] = 0.0
+        weights[N // 2] = (2 * N + 3) / (dp * dp)
+    return nodes, weights
+
+
+def lagrange_interpolating_polynomials(x: float, nodes, wbary):
+    """basis_lobatto_legendre.jl:533-557."""
+    p = np.zeros(len(nodes))
+    ex = float(np.spacing(abs(x)))
+    for i, xi in enumerate(nodes):
+        if x == xi or abs(x - xi) <= ex * max(abs(x), abs(xi)):
+            p[i] = 1.0
+            return p
+    p = wbary / (x - np.asarray(nodes))
+    return p / p.sum()
+
+
+class MortarL2:
+    """LobattoLegendreMortarL2 = MortarL2(basis), basis_lobatto_legendre.jl:159-205
+    with l2projection.jl:26-115: forward_{upper,lower} interpolate a face trace
+    to the upper/lower half of the face, reverse_{upper,lower} project fluxes on
+    the halves back with a Gauss-quadrature L2 projection."""
+
+    def __init__(self, basis):
+        n = basis.nnodes()
+        nodes = basis.nodes
+        wb = barycentric_weights(nodes)
+        fwd = []
+        for shift in (1.0, -1.0):
+            F = np.zeros((n, n))
+            for j in range(n):
+                F[j, :] = lagrange_interpolating_polynomials(0.5 * (nodes[j] + shift), nodes, wb)
+            fwd.append(F)
+        self.forward_upper, self.forward_lower = fwd
+        gn, gw = gauss_nodes_weights(n)
+        gwb = barycentric_weights(gn)
+        g2l = polynomial_interpolation_matrix(gn, nodes)
+        l2g = polynomial_interpolation_matrix(nodes, gn)
+        rev = []
+        for shift in (1.0, -1.0):
+            op = np.zeros((n, n))
+            for j in range(n):
+                p = lagrange_interpolating_polynomials(0.5 * (gn[j] + shift), gn, gwb)
+                op[:, j] = 0.5 * p * gw[j] / gw
+            rev.append(g2l @ op @ l2g)
+        self.reverse_upper, self.reverse_lower = rev
+
+    def __repr__(self):
+        return f"LobattoLegendreMortarL2{{Float64}}(polydeg={self.forward_upper.shape[0] - 1})"
+
+
 class LobattoLegendreBasis:
     """LobattoLegendreBasis(polydeg), basis_lobatto_legendre.jl:54-85."""
 

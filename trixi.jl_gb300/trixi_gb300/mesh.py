@@ -1,11 +1,14 @@
-"""Uniformly refined TreeMesh (host setup), periodic or not per dimension.
+"""TreeMesh (host setup): a uniform initial refinement plus optional
+refinement patches, periodic or not per dimension.
 
 Element order is Trixi's: cells are created depth-first with children in
 _child_signs order (x fastest, then y, then z; abstract_tree.jl:122-130,
 206-248), and elements are the leaf cells in cell-id order
 (abstract_tree.jl:154-174).  For a uniform refinement that is the Morton
 (Z-order) curve with x as the lowest bit.  Interfaces are created per element
-in the positive directions only (containers_2d.jl:228-284).
+in the positive directions only (containers_2d.jl:228-284); L2 mortars per
+large element in every direction towards a refined neighbour
+(containers_2d.jl:660-810, containers_3d.jl:652-790).
 """
 from __future__ import annotations
 
@@ -24,13 +27,123 @@ def _morton_cells(ndims: int, level: int):
     return cart
 
 
+class _Tree:
+    """The refinement tree of a TreeMesh (abstract_tree.jl): cells keyed by
+    (level, integer position); a same-level neighbour exists iff its key is
+    present (periodic wrap per dimension), as Trixi's neighbour links record."""
+
+    def __init__(self, ndims, periodicity, length0, center0):
+        self.D = ndims
+        self.periodicity = periodicity
+        self.length0 = length0
+        self.level, self.ix, self.center, self.child0 = [], [], [], []
+        self.index = {}
+        self._add(0, (0,) * ndims, tuple(center0))
+
+    def _add(self, level, ix, c):
+        self.index[(level, ix)] = len(self.level)
+        self.level.append(level)
+        self.ix.append(ix)
+        self.center.append(c)
+        self.child0.append(-1)
+
+    def length(self, level):
+        return self.length0 / (1 << level)
+
+    def is_leaf(self, cell):
+        return self.child0[cell] < 0
+
+    def neighbour(self, cell, direction):
+        """Same-level neighbour across face `direction` (0: -x, 1: +x, ...) or -1."""
+        lev, ix = self.level[cell], list(self.ix[cell])
+        d = direction // 2
+        M = 1 << lev
+        ix[d] += 1 if direction & 1 else -1
+        if not 0 <= ix[d] < M:
+            if not self.periodicity[d]:
+                return -1
+            ix[d] %= M
+        return self.index.get((lev, tuple(ix)), -1)
+
+    def parent(self, cell):
+        lev = self.level[cell]
+        if lev == 0:
+            return -1
+        return self.index[(lev - 1, tuple(i >> 1 for i in self.ix[cell]))]
+
+    def _refine_cell(self, cell):
+        # init_child! / child_coordinates (abstract_tree.jl:668-674)
+        lev, ix, c = self.level[cell], self.ix[cell], self.center[cell]
+        child_len = self.length(lev) / 2
+        self.child0[cell] = len(self.level)
+        for ch in range(1 << self.D):
+            bits = [(ch >> d) & 1 for d in range(self.D)]
+            self._add(lev + 1, tuple(2 * i + b for i, b in zip(ix, bits)),
+                      tuple(cc + (1.0 if b else -1.0) * child_len / 2 for cc, b in zip(c, bits)))
+
+    def refine(self, cells):
+        """refine!(t, cell_ids): refine the given leaves, then rebalance! until no
+        two face neighbours differ by more than one level (abstract_tree.jl:367-402,
+        453-489)."""
+        refined = sorted(set(cells))
+        for c in refined:
+            self._refine_cell(c)
+        while refined:
+            marks = set()
+            for cell in refined:
+                for direction in range(2 * self.D):
+                    if self.neighbour(cell, direction) >= 0:
+                        continue
+                    p = self.parent(cell)
+                    if p < 0:
+                        continue
+                    pn = self.neighbour(p, direction)
+                    if pn >= 0:
+                        marks.add(pn)
+            refined = sorted(marks)
+            for c in refined:
+                self._refine_cell(c)
+
+    def leaves(self):
+        """Leaf cells depth-first with children in _child_signs order."""
+        out, stack = [], [0]
+        nch = 1 << self.D
+        while stack:
+            cell = stack.pop()
+            if self.child0[cell] < 0:
+                out.append(cell)
+            else:
+                stack.extend(range(self.child0[cell] + nch - 1, self.child0[cell] - 1, -1))
+        return out
+
+
+def _patch(p, ndims):
+    """A refinement patch as in tree_mesh.jl:194-203: (type = "box",
+    coordinates_min, coordinates_max) or (type = "sphere", center, radius)."""
+    get = p.get if isinstance(p, dict) else (lambda k, default=None: getattr(p, k, default))
+    kind = get("type")
+    if kind == "box":
+        lo = tuple(float(x) for x in get("coordinates_min"))
+        hi = tuple(float(x) for x in get("coordinates_max"))
+        if len(lo) != ndims or len(hi) != ndims or any(a >= b for a, b in zip(lo, hi)):
+            raise ValueError("a box patch needs coordinates_min < coordinates_max per dimension")
+        return ("box", lo, hi)
+    if kind == "sphere":
+        c = tuple(float(x) for x in get("center"))
+        r = float(get("radius"))
+        if len(c) != ndims or r < 0:
+            raise ValueError("a sphere patch needs a center per dimension and a radius >= 0")
+        return ("sphere", c, r)
+    raise ValueError(f"unknown refinement patch type {kind!r}")
+
+
 class TreeMesh:
     """TreeMesh(coordinates_min, coordinates_max; initial_refinement_level, periodicity),
     tree_mesh.jl:128-185 (uniform).  periodicity: a bool for all dimensions or one
     per dimension; faces at a non-periodic domain edge are boundaries."""
 
     def __init__(self, coordinates_min, coordinates_max, initial_refinement_level: int,
-                 periodicity=True, n_cells_max=None):
+                 periodicity=True, n_cells_max=None, refinement_patches=()):
         cmin = tuple(float(x) for x in coordinates_min)
         cmax = tuple(float(x) for x in coordinates_max)
         if len(cmin) != len(cmax) or len(cmin) not in (2, 3):
@@ -53,15 +166,53 @@ class TreeMesh:
         self.length_level_0 = length
         self.center_level_0 = tuple((a + b) / 2 for a, b in zip(cmin, cmax))
         self.cells_per_dim = 1 << initial_refinement_level
-        self.cartesian = _morton_cells(self.ndims, initial_refinement_level)
+        self.refinement_patches = tuple(_patch(p, self.ndims) for p in refinement_patches)
+        self._tree = None
+        if self.refinement_patches:
+            self._build_tree()
+        else:
+            self.cartesian = _morton_cells(self.ndims, initial_refinement_level)
+
+    def _build_tree(self):
+        """initialize!(mesh, initial_refinement_level, refinement_patches),
+        tree_mesh.jl:186-215: uniform refinement, then each patch refines the
+        leaves whose centre lies strictly inside it (refine_box!, refine_sphere!,
+        abstract_tree.jl:405-447)."""
+        t = _Tree(self.ndims, self.periodicity, self.length_level_0, self.center_level_0)
+        for _ in range(self.initial_refinement_level):
+            t.refine(t.leaves())
+        for kind, a, b in self.refinement_patches:
+            sel = []
+            for cell in t.leaves():
+                c = t.center[cell]
+                if kind == "box":
+                    inside = all(lo < x < hi for x, lo, hi in zip(c, a, b))
+                else:
+                    inside = sum((x - y) ** 2 for x, y in zip(c, a)) < b * b
+                if inside:
+                    sel.append(cell)
+            if sel:
+                t.refine(sel)
+        self._tree = t
+        self._leaves = t.leaves()
 
     @property
     def nelements(self) -> int:
+        if self._tree is not None:
+            return len(self._leaves)
         return self.cartesian.shape[0]
+
+    @property
+    def is_uniform(self) -> bool:
+        if self._tree is None:
+            return True
+        return len({self._tree.level[c] for c in self._leaves}) == 1
 
     def cell_centers(self):
         """Cell midpoints, computed like child_coordinates (abstract_tree.jl:668-674):
         each level adds sign * (parent_length / 2) / 2 to the parent centre."""
+        if self._tree is not None:
+            return np.array([self._tree.center[c] for c in self._leaves], dtype=np.float64)
         L = self.initial_refinement_level
         centers = np.tile(np.array(self.center_level_0), (self.nelements, 1))
         length = self.length_level_0
@@ -74,12 +225,28 @@ class TreeMesh:
         return centers
 
     def element_length(self) -> float:
-        return self.length_level_0 / (1 << self.initial_refinement_level)
+        """Edge length of the elements of a uniform mesh."""
+        if not self.is_uniform:
+            raise ValueError("the elements of this mesh have different sizes")
+        return float(self.element_lengths()[0])
+
+    def element_lengths(self):
+        """length_at_cell of every element (length_level_0 / 2^level)."""
+        if self._tree is not None:
+            return np.array([self._tree.length(self._tree.level[c]) for c in self._leaves])
+        return np.full(self.nelements, self.length_level_0 / (1 << self.initial_refinement_level))
+
+    def element_levels(self):
+        if self._tree is not None:
+            return np.array([self._tree.level[c] for c in self._leaves], dtype=np.int64)
+        return np.full(self.nelements, self.initial_refinement_level, dtype=np.int64)
 
     def interfaces(self):
         """neighbor_ids [I, 2] (1-based, (left, right)) and orientations [I] (1-based),
         per element in order and positive directions only where a neighbour
         exists (init_interfaces!, containers_2d.jl:228-284)."""
+        if self._tree is not None:
+            return self._tree_interfaces()
         D, M, E = self.ndims, self.cells_per_dim, self.nelements
         lin = np.zeros(E, dtype=np.int64)
         mult = 1
@@ -106,6 +273,48 @@ class TreeMesh:
             orient[:, d] = d + 1
         keep = exists.reshape(E * D)
         return nb.reshape(E * D, 2)[keep], orient.reshape(E * D)[keep]
+
+    def _tree_interfaces(self):
+        t, D = self._tree, self.ndims
+        c2e = {c: e for e, c in enumerate(self._leaves)}
+        nb, orient = [], []
+        for e, cell in enumerate(self._leaves):
+            for d in range(D):
+                n = t.neighbour(cell, 2 * d + 1)
+                if n >= 0 and t.is_leaf(n):
+                    nb.append((e + 1, c2e[n] + 1))
+                    orient.append(d + 1)
+        return (np.array(nb, dtype=np.int64).reshape(-1, 2),
+                np.array(orient, dtype=np.int64))
+
+    def mortars(self):
+        """cache.mortars of L2 mortars (init_mortars!, containers_2d.jl:707-810,
+        containers_3d.jl:652-790): neighbor_ids [M, 2^(ndims-1) + 1] (1-based; the
+        small elements facing the large one in child order, then the large one),
+        large_sides [M] (1: large element on the negative side), orientations [M]."""
+        D = self.ndims
+        ns = 1 << (D - 1)
+        if self._tree is None:
+            return (np.zeros((0, ns + 1), dtype=np.int64), np.zeros(0, dtype=np.int64),
+                    np.zeros(0, dtype=np.int64))
+        t = self._tree
+        c2e = {c: e for e, c in enumerate(self._leaves)}
+        ids, ls, orient = [], [], []
+        for e, cell in enumerate(self._leaves):
+            for direction in range(2 * D):
+                n = t.neighbour(cell, direction)
+                if n < 0 or t.is_leaf(n):
+                    continue
+                d = direction // 2
+                want = 0 if direction & 1 else 1
+                small = [t.child0[n] + ch for ch in range(1 << D) if (ch >> d) & 1 == want]
+                if not all(t.is_leaf(c) for c in small):
+                    raise RuntimeError("refinement tree is not 2:1 balanced")
+                ids.append([c2e[c] + 1 for c in small] + [e + 1])
+                ls.append(1 if direction & 1 else 2)
+                orient.append(d + 1)
+        return (np.array(ids, dtype=np.int64).reshape(-1, ns + 1),
+                np.array(ls, dtype=np.int64), np.array(orient, dtype=np.int64))
 
     def __repr__(self):
         per = "periodic" if all(self.periodicity) else f"periodicity {self.periodicity}"

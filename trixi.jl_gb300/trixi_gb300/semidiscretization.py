@@ -143,6 +143,17 @@ def make_config(semi, precision="fp64", device=0, elements_per_block=0):
     cfg.inverse_jacobian = _dptr(arr(semi.inverse_jacobian))
     cfg.node_coordinates = _dptr(arr(semi.node_coordinates))
     cfg.elements_per_block = int(elements_per_block)
+    mids = getattr(semi, "mortar_neighbor_ids", None)
+    if mids is not None and len(mids):
+        i64p = ctypes.POINTER(ctypes.c_int64)
+        cfg.nmortars = mids.shape[0]
+        cfg.mortar_neighbor_ids = arr(mids, np.int64).ctypes.data_as(i64p)
+        cfg.mortar_large_sides = arr(semi.mortar_large_sides, np.int64).ctypes.data_as(i64p)
+        cfg.mortar_orientations = arr(semi.mortar_orientations, np.int64).ctypes.data_as(i64p)
+        m = dg.mortar
+        for name in ("forward_upper", "forward_lower", "reverse_upper", "reverse_lower"):
+            setattr(cfg, "mortar_" + name,
+                    _dptr(arr(np.asfortranarray(getattr(m, name)).ravel(order="F"))))
     funcs = set()
     for k, bc in enumerate(getattr(semi, "boundary_conditions", [])):
         cfg.boundary_conditions[k] = bc.code
@@ -312,20 +323,22 @@ class SemidiscretizationHyperbolic:
         for w in b.weights:
             reference_length += 1.0 * w
         reference_offset = (b.nodes[0] + b.nodes[-1]) / 2
-        dx = mesh.element_length()
-        jac = dx / reference_length
-        self.inverse_jacobian = np.full(self.nelements, 1.0 / jac)
+        jac = mesh.element_lengths() / reference_length  # per element
+        self.inverse_jacobian = 1.0 / jac
         centers = mesh.cell_centers()
         X = np.empty((self.nelements,) + (n,) * D + (D,))
-        rel = jac * (b.nodes - reference_offset)
+        rel = b.nodes - reference_offset
+        jb = jac.reshape((-1,) + (1,) * D)
         for d in range(D):
             # axis of node index along d in the (e, k, j, i) array order
             ax = D - d
             shape = [1] * (D + 1)
             shape[ax] = n
-            X[..., d] = centers[:, d].reshape((-1,) + (1,) * D) + rel.reshape(shape)
+            X[..., d] = centers[:, d].reshape((-1,) + (1,) * D) + jb * rel.reshape(shape)
         self.node_coordinates = X
         self.neighbor_ids, self.orientations = mesh.interfaces()
+        (self.mortar_neighbor_ids, self.mortar_large_sides,
+         self.mortar_orientations) = mesh.mortars()
         self._ctx = None
 
     @property

@@ -3,7 +3,7 @@ src/solvers/dgsem/indicators.jl."""
 from __future__ import annotations
 
 from . import _lib
-from .basis import LobattoLegendreBasis
+from .basis import LobattoLegendreBasis, MortarL2
 from .equations import density_pressure, flux_central, flux_lax_friedrichs
 
 
@@ -67,6 +67,7 @@ class DGSEM:
         elif isinstance(basis, int):
             basis = LobattoLegendreBasis(basis)
         self.basis = basis
+        self.mortar = MortarL2(basis)  # dg.mortar (dgsem.jl:25-35)
         self.surface_flux = surface_flux
         self.volume_integral = volume_integral if volume_integral is not None else VolumeIntegralWeakForm()
 
