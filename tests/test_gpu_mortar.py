@@ -130,10 +130,16 @@ def test_mortar_free_stream(ndims, precision):
     assert np.max(np.abs(du)) < (1e-12 if precision == "fp64" else 1e-4)
 
 
+# mixed tolerances: smooth solutions 1e-5; on the weak blast wave the FP32
+# wave speed moves dt by ~1e-5 relative and the discontinuous state then
+# differs by ~1e-4 in the momentum (small maximum) -- on the conforming mesh
+# of the same case by 1.6e-4, so this is the mixed path's shock behaviour,
+# not the mortars'
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("c", [MORTAR_CASES[0], MORTAR_CASES[2], MORTAR_CASES[5]],
-                         ids=lambda c: _id(c))
-def test_mortar_steps_match_oracle(c, precision):
+@pytest.mark.parametrize("c,tol_mixed", [(MORTAR_CASES[0], 1e-5), (MORTAR_CASES[2], 5e-4),
+                                         (MORTAR_CASES[5], 1e-5)],
+                         ids=lambda x: _id(x) if isinstance(x, dict) else str(x))
+def test_mortar_steps_match_oracle(c, tol_mixed, precision):
     semi, orc = build(c, precision=precision)
     u0 = semi.compute_coefficients(0.0)
     ctx = semi.device_context
@@ -141,8 +147,8 @@ def test_mortar_steps_match_oracle(c, precision):
     t, n = ctx.step(6, 0.8, 100.0, 0.0)
     u_orc, t_orc, n_orc = orc.solve(u0, 0.0, 100.0, 0.8, max_steps=6)
     assert n == n_orc == 6
-    tol = 1e-12 if precision == "fp64" else 1e-5
-    assert abs(t - t_orc) <= tol * t_orc
+    tol = 1e-12 if precision == "fp64" else tol_mixed
+    assert abs(t - t_orc) <= min(tol, 1e-4) * t_orc
     assert rel_err(ctx.download(), u_orc) < tol
 
 
