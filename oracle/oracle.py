@@ -26,7 +26,7 @@ SRC_NONE, SRC_CONVERGENCE_TEST = 0, 1
 BC_PERIODIC, BC_DIRICHLET, BC_SLIP_WALL = 0, 1, 2
 (IC_CONSTANT, IC_CONVERGENCE_TEST, IC_ISENTROPIC_VORTEX, IC_WEAK_BLAST_WAVE,
  IC_KELVIN_HELMHOLTZ, IC_TAYLOR_GREEN, IC_GAUSSIAN_BLAST,
- IC_ISENTROPIC_VORTEX_ADVECTED) = range(8)
+ IC_ISENTROPIC_VORTEX_ADVECTED, IC_BLAST_WAVE) = range(9)
 
 _lib = None
 
@@ -78,6 +78,13 @@ def _load():
     lib.orc_nmortars.argtypes = [vp]
     lib.orc_get_mortars.argtypes = [vp, P(i64), P(i64), P(i64)]
     lib.orc_get_mortar_matrices.argtypes = [vp, P(d)]
+    lib.orc_set_amr.argtypes = [vp, P(i), P(d)]
+    lib.orc_adapt.restype = i
+    lib.orc_adapt.argtypes = [vp, P(d), i, i]
+    lib.orc_get_state.argtypes = [vp, P(d)]
+    lib.orc_element_levels.argtypes = [vp, P(i)]
+    lib.orc_solve_amr.restype = i
+    lib.orc_solve_amr.argtypes = [vp, i, P(d), d, d, d, i64, P(d), P(i64)]
     _lib = lib
     return lib
 
@@ -271,6 +278,61 @@ def _mortar_matrices(self):
     return [out[k * n * n:(k + 1) * n * n].reshape(n, n).copy() for k in range(4)]
 
 
+def _refresh(self):
+    self.nelements = self.lib.orc_nelements(self.h)
+    self.ninterfaces = self.lib.orc_ninterfaces(self.h)
+    self.nmortars = self.lib.orc_nmortars(self.h)
+    self.ndofs = self.lib.orc_ndofs(self.h)
+
+
+def _set_amr(self, interval=5, adapt_initial_condition=True,
+             adapt_initial_condition_only_refine=True, alpha_max=0.5, alpha_min=0.001,
+             alpha_smooth=True, base_level=1, med_level=None, med_threshold=0.0,
+             max_level=None, max_threshold=1.0):
+    """AMRCallback(semi, ControllerThreeLevel(semi, IndicatorHennemannGassner(...)))."""
+    med_level = base_level if med_level is None else med_level
+    max_level = base_level if max_level is None else max_level
+    ints = np.array([interval, adapt_initial_condition, adapt_initial_condition_only_refine,
+                     alpha_smooth, base_level, med_level, max_level], dtype=np.int32)
+    dbls = np.array([alpha_max, alpha_min, med_threshold, max_threshold], dtype=np.float64)
+    self.lib.orc_set_amr(self.h, _p(ints, ctypes.c_int), _p(dbls))
+
+
+def _adapt(self, u, only_refine=False, only_coarsen=False):
+    """One AMR pass; returns (changed, new state)."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    changed = bool(self.lib.orc_adapt(self.h, _p(u), int(only_refine), int(only_coarsen)))
+    self.refresh()
+    out = np.zeros(self.shape)
+    self.lib.orc_get_state(self.h, _p(out))
+    return changed, out
+
+
+def _element_levels(self):
+    out = np.zeros(self.nelements, dtype=np.int32)
+    self.lib.orc_element_levels(self.h, _p(out, ctypes.c_int))
+    return out
+
+
+def _solve_amr(self, ic, params, t0, t_end, cfl, max_steps=10**9):
+    par = None if params is None else np.ascontiguousarray(params, dtype=np.float64)
+    t_out = ctypes.c_double(0)
+    nsteps = ctypes.c_int64(0)
+    rc = self.lib.orc_solve_amr(self.h, ic, None if par is None else _p(par), t0, t_end, cfl,
+                                max_steps, ctypes.byref(t_out), ctypes.byref(nsteps))
+    self.refresh()
+    if rc != 0:
+        raise FloatingPointError("oracle: time step size is NaN")
+    out = np.zeros(self.shape)
+    self.lib.orc_get_state(self.h, _p(out))
+    return out, t_out.value, nsteps.value
+
+
+Oracle.refresh = _refresh
+Oracle.set_amr = _set_amr
+Oracle.adapt = _adapt
+Oracle.element_levels = _element_levels
+Oracle.solve_amr = _solve_amr
 Oracle.set_refinement = _set_refinement
 Oracle.mortars = _mortars
 Oracle.mortar_matrices = _mortar_matrices

@@ -52,6 +52,7 @@ enum InitialCondition {
   IC_TAYLOR_GREEN = 5,
   IC_GAUSSIAN_BLAST = 6,
   IC_ISENTROPIC_VORTEX_ADVECTED = 7,
+  IC_BLAST_WAVE = 8,
 };
 
 // ---------------------------------------------------------------------------
@@ -662,6 +663,21 @@ static void initial_condition(const Eq& eq, int ic, const double* par, const dou
       prim2cons(eq, prim, u);
       return;
     }
+    case IC_BLAST_WAVE: {
+      // the medium blast wave of examples/tree_2d_dgsem/elixir_euler_blast_wave_amr.jl:18-34
+      // (Hennemann & Gassner 2020, sec. 6.3): the weak blast wave's inner state
+      // in a background at p = 1e-3
+      const double r = std::sqrt(x[0] * x[0] + x[1] * x[1]);
+      const double phi = std::atan2(x[1], x[0]);
+      const double sp = std::sin(phi), cp = std::cos(phi);
+      const bool out = r > 0.5;
+      prim[0] = out ? 1.0 : 1.1691;
+      prim[1] = out ? 0.0 : 0.1882 * cp;
+      prim[2] = out ? 0.0 : 0.1882 * sp;
+      prim[3] = out ? 1.0e-3 : 1.245;
+      prim2cons(eq, prim, u);
+      return;
+    }
     case IC_WEAK_BLAST_WAVE: {
       // initial_condition_weak_blast_wave, compressible_euler_2d.jl:245-264, 3d.jl:241-263
       if (eq.D == 2) {
@@ -855,6 +871,40 @@ struct Tree {
       refined.swap(to_refine);
     }
   }
+  // coarsen!(t, cell_ids), abstract_tree.jl:516-618: parents (all children
+  // leaves) from the highest level down; a parent is kept when a child has a
+  // same-level neighbour with children across a face that is not shared with
+  // a sibling (the 2:1 rule).  Returns the parents that were coarsened.
+  std::vector<int64_t> coarsen(std::vector<int64_t> ids) {
+    std::stable_sort(ids.begin(), ids.end(),
+                     [&](int64_t a, int64_t b) { return cells[a].level < cells[b].level; });
+    std::vector<int64_t> done;
+    while (!ids.empty()) {
+      const int64_t cell = ids.back();
+      ids.pop_back();
+      bool skip = false;
+      for (int ch = 0; ch < (1 << D) && !skip; ++ch) {
+        const int64_t c = child(cell, ch);
+        for (int dir = 0; dir < 2 * D; ++dir) {
+          const int bit = (ch >> (dir / 2)) & 1;
+          if (bit != (dir & 1)) continue;  // the neighbour there is a sibling
+          const int64_t nb = neighbour(c, dir);
+          if (nb >= 0 && !leaf(nb)) {
+            skip = true;
+            break;
+          }
+        }
+      }
+      if (skip) continue;
+      for (int ch = 0; ch < (1 << D); ++ch) {
+        const Cell& c = cells[child(cell, ch)];
+        index.erase(key(c.level, c.ix));
+      }
+      cells[cell].child0 = -1;
+      done.push_back(cell);
+    }
+    return done;
+  }
   void leaves(int64_t cell, std::vector<int64_t>& out) const {
     if (leaf(cell)) {
       out.push_back(cell);
@@ -888,23 +938,20 @@ struct Mesh {
   double length0 = 0;
   double xmin[3] = {0, 0, 0};
   std::vector<Patch> patches;
+  Tree tree;
+  std::vector<int64_t> leaf_cells;  // [E] tree cell of each element
 };
+
+static Mesh mesh_from_tree(const Tree& t, int level, const double* xmin, const Basis& b);
 
 static Mesh make_mesh(int D, int level, const double* xmin, const double* xmax, const Basis& b,
                       bool periodic = true, const std::vector<Patch>& patches = {}) {
-  Mesh m;
-  m.D = D;
-  m.level = level;
-  m.patches = patches;
   Tree t;
   t.D = D;
   t.periodic = periodic;
   double c0[3] = {0, 0, 0};
-  for (int d = 0; d < D; ++d) {
-    c0[d] = (xmin[d] + xmax[d]) / 2;
-    m.xmin[d] = xmin[d];
-  }
-  m.length0 = t.length0 = xmax[0] - xmin[0];
+  for (int d = 0; d < D; ++d) c0[d] = (xmin[d] + xmax[d]) / 2;
+  t.length0 = xmax[0] - xmin[0];
   const int64_t root_ix[3] = {0, 0, 0};
   t.add(0, root_ix, c0);
   // refine_uniformly!: refine! of all leaves, level by level
@@ -926,7 +973,23 @@ static Mesh make_mesh(int D, int level, const double* xmin, const double* xmax, 
     }
     if (!sel.empty()) t.refine(sel);
   }
+  Mesh out = mesh_from_tree(t, level, xmin, b);
+  out.patches = patches;
+  return out;
+}
+
+// The elements, interfaces and mortars of the leaves of a tree
+// (init_elements!, init_interfaces!, init_mortars!).
+static Mesh mesh_from_tree(const Tree& t, int level, const double* xmin, const Basis& b) {
+  Mesh m;
+  const int D = t.D;
+  m.D = D;
+  m.level = level;
+  m.tree = t;
+  for (int d = 0; d < D; ++d) m.xmin[d] = xmin[d];
+  m.length0 = t.length0;
   const std::vector<int64_t> leaves = t.leaves();
+  m.leaf_cells = leaves;
   m.nelem = (int64_t)leaves.size();
   std::unordered_map<int64_t, int64_t> c2e;
   for (int64_t e = 0; e < m.nelem; ++e) c2e[leaves[e]] = e;
@@ -1003,6 +1066,16 @@ static Mesh make_mesh(int D, int level, const double* xmin, const double* xmax, 
 // Solver
 // ---------------------------------------------------------------------------
 
+// AMRCallback + ControllerThreeLevel settings (callbacks_step/amr.jl)
+struct AmrParams {
+  double alpha_max = 0.5, alpha_min = 0.001;
+  bool alpha_smooth = true;
+  int base_level = 1, med_level = 1, max_level = 1;
+  double med_threshold = 0.0, max_threshold = 1.0;
+  int interval = 5;
+  bool adapt_initial = true, initial_only_refine = true;
+};
+
 struct Solver {
   Eq eq;
   Basis b;
@@ -1020,6 +1093,8 @@ struct Solver {
   int bc_ic = 0;
   double bc_par[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   std::vector<double> alpha, alpha_tmp, sfv;  // sfv: [NV, n^(D-1), 2D, E]
+  AmrParams amr;
+  std::vector<double> u_state;  // state of the AMR entry points
   int64_t ndofs() const { return (int64_t)nn * m.nelem; }
 };
 
@@ -1028,12 +1103,22 @@ static inline size_t uidx(const Solver& s, int64_t e, int node, int v) {
 }
 
 // HG indicator: indicators.jl:114-148 + indicators_2d.jl:30-101, indicators_3d.jl:39-123
+static void hg_alpha(const Solver& s, const double* u, double alpha_max, double alpha_min,
+                     bool alpha_smooth, std::vector<double>& alpha);
+
 static void calc_alpha(Solver& s, const double* u) {
+  hg_alpha(s, u, s.alpha_max, s.alpha_min, s.alpha_smooth, s.alpha);
+}
+
+// The HG indicator with the given parameters (IndicatorHennemannGassner, also
+// as the AMR indicator of ControllerThreeLevel).
+static void hg_alpha(const Solver& s, const double* u, double alpha_max, double alpha_min,
+                     bool alpha_smooth, std::vector<double>& alpha) {
   const int n = s.b.n, D = s.eq.D, nn = s.nn;
   const double threshold = 0.5 * std::pow(10.0, -1.8 * std::pow((double)n, 0.25));
   const double o_0001 = 0.0001;
   const double parameter_s = std::log((1 - o_0001) / o_0001);
-  s.alpha.assign(s.m.nelem, 0.0);
+  alpha.assign(s.m.nelem, 0.0);
 #pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < s.m.nelem; ++e) {
     double ind[512], t1[512], t2[512];
@@ -1070,17 +1155,17 @@ static void calc_alpha(Solver& s, const double* u) {
     double f2 = e_clip1 != 0 ? (e_clip1 - e_clip2) / e_clip1 : 0.0;
     const double energy = std::max(f1, f2);
     double a = 1 / (1 + std::exp(-parameter_s / threshold * (energy - threshold)));
-    if (a < s.alpha_min) a = 0;
-    if (a > 1 - s.alpha_min) a = 1;
-    s.alpha[e] = std::min(s.alpha_max, a);
+    if (a < alpha_min) a = 0;
+    if (a > 1 - alpha_min) a = 1;
+    alpha[e] = std::min(alpha_max, a);
   }
-  if (s.alpha_smooth) {
+  if (alpha_smooth) {
     // apply_smoothing!, indicators_2d.jl:104-136
-    s.alpha_tmp = s.alpha;
+    const std::vector<double> alpha_tmp = alpha;
     for (int64_t f = 0; f < s.m.nif; ++f) {
       const int64_t l = s.m.if_left[f], r = s.m.if_right[f];
-      s.alpha[l] = std::max({s.alpha_tmp[l], 0.5 * s.alpha_tmp[r], s.alpha[l]});
-      s.alpha[r] = std::max({s.alpha_tmp[r], 0.5 * s.alpha_tmp[l], s.alpha[r]});
+      alpha[l] = std::max({alpha_tmp[l], 0.5 * alpha_tmp[r], alpha[l]});
+      alpha[r] = std::max({alpha_tmp[r], 0.5 * alpha_tmp[l], alpha[r]});
     }
     // L2 mortars: each small element with the large one (indicators_3d.jl:140-162)
     const int ns = 1 << (D - 1);
@@ -1088,9 +1173,9 @@ static void calc_alpha(Solver& s, const double* u) {
       const int64_t* ids = &s.m.mo_ids[(size_t)k * (ns + 1)];
       const int64_t large = ids[ns];
       for (int q = 0; q < ns; ++q)
-        s.alpha[ids[q]] = std::max({s.alpha_tmp[ids[q]], 0.5 * s.alpha_tmp[large], s.alpha[ids[q]]});
+        alpha[ids[q]] = std::max({alpha_tmp[ids[q]], 0.5 * alpha_tmp[large], alpha[ids[q]]});
       for (int q = 0; q < ns; ++q)
-        s.alpha[large] = std::max({s.alpha_tmp[large], 0.5 * s.alpha_tmp[ids[q]], s.alpha[large]});
+        alpha[large] = std::max({alpha_tmp[large], 0.5 * alpha_tmp[ids[q]], alpha[large]});
     }
   }
 }
@@ -1438,6 +1523,120 @@ static void rk_update(int64_t ndof, double* u, double* u_tmp, const double* du, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// AMR: AMRCallback on a TreeMesh (callbacks_step/amr.jl:143-197, 244-392)
+// with ControllerThreeLevel (amr.jl:984-1168) on the HG indicator, and the
+// solution transfer of amr_dg2d.jl:85-485 / amr_dg3d.jl (LobattoLegendre
+// AdaptorL2: the mortar matrices).
+// ---------------------------------------------------------------------------
+
+
+// ControllerThreeLevel: +1 refine, -1 coarsen, 0 keep
+static std::vector<int> amr_controller(const Solver& s, const double* u, const AmrParams& ap) {
+  std::vector<double> alpha;
+  hg_alpha(s, u, ap.alpha_max, ap.alpha_min, ap.alpha_smooth, alpha);
+  std::vector<int> lambda(s.m.nelem, 0);
+  for (int64_t e = 0; e < s.m.nelem; ++e) {
+    const int cur = s.m.elevel[e];
+    int target = cur;
+    if (alpha[e] > ap.max_threshold)
+      target = ap.max_level;
+    else if (alpha[e] > ap.med_threshold) {
+      if (ap.med_level > 0) target = ap.med_level;
+    } else
+      target = ap.base_level;
+    lambda[e] = cur < target ? 1 : (cur > target ? -1 : 0);
+  }
+  return lambda;
+}
+
+// One AMR pass on the state u (resized in place): refine! (with rebalancing),
+// then coarsen! of the parents whose children are all marked; refined
+// elements get the tensor-product interpolation of their parent
+// (refine_element!), coarsened ones the sum of the L2 projections of their
+// children (coarsen_elements!).  Returns whether the mesh changed.
+static bool amr_adapt(Solver& s, std::vector<double>& u, const AmrParams& ap, bool only_refine,
+                      bool only_coarsen) {
+  const int D = s.eq.D, NV = s.eq.NV, n = s.b.n, nn = s.nn, nch = 1 << D;
+  const std::vector<int> lambda = amr_controller(s, u.data(), ap);
+  Tree& t = s.m.tree;
+  const std::vector<int64_t> old_leaves = s.m.leaf_cells;
+  std::unordered_map<int64_t, int64_t> old_elem;
+  for (int64_t e = 0; e < (int64_t)old_leaves.size(); ++e) old_elem[old_leaves[e]] = e;
+  std::vector<int64_t> to_refine, to_coarsen;
+  for (int64_t e = 0; e < (int64_t)lambda.size(); ++e) {
+    if (lambda[e] > 0) to_refine.push_back(old_leaves[e]);
+    if (lambda[e] < 0) to_coarsen.push_back(old_leaves[e]);
+  }
+  bool changed = false;
+  std::unordered_map<int64_t, int64_t> former_child0;  // first child of each coarsened parent
+  if (!only_coarsen && !to_refine.empty()) {
+    t.refine(to_refine);
+    changed = true;
+  }
+  if (!only_refine && !to_coarsen.empty()) {
+    std::unordered_map<int64_t, int> count;
+    std::vector<int64_t> parents;
+    for (int64_t cell : to_coarsen) {
+      if (t.cells[cell].level == 0 || !t.leaf(cell)) continue;
+      const int64_t p = t.parent(cell);
+      if (++count[p] == nch) parents.push_back(p);
+    }
+    std::sort(parents.begin(), parents.end());  // cell order does not change the result
+    for (int64_t p : parents) former_child0[p] = t.cells[p].child0;
+    if (!t.coarsen(parents).empty()) changed = true;
+  }
+  if (!changed) return false;
+  Mesh nm = mesh_from_tree(t, s.m.level, s.m.xmin, s.b);
+  nm.patches = s.m.patches;
+  std::vector<double> un((size_t)nm.nelem * nn * NV, 0.0);
+  const std::vector<double>* F[2] = {&s.b.fwd[0], &s.b.fwd[1]};
+  const std::vector<double>* R[2] = {&s.b.rev[0], &s.b.rev[1]};
+  for (int64_t e = 0; e < nm.nelem; ++e) {
+    const int64_t cell = nm.leaf_cells[e];
+    double* dst = &un[(size_t)e * nn * NV];
+    auto it = old_elem.find(cell);
+    if (it != old_elem.end()) {
+      std::memcpy(dst, &u[(size_t)it->second * nn * NV], sizeof(double) * nn * NV);
+      continue;
+    }
+    const int64_t p = t.parent(cell);
+    auto ip = p >= 0 ? old_elem.find(p) : old_elem.end();
+    if (ip != old_elem.end()) {
+      // child q of a refined element: forward_{lower,upper} per axis
+      const int q = (int)(cell - t.cells[p].child0);
+      const double* src = &u[(size_t)ip->second * nn * NV];
+      for (int node = 0; node < nn; ++node) {
+        const int i[3] = {node % n, (node / n) % n, node / (n * n)};
+        for (int sn = 0; sn < nn; ++sn) {
+          const int k[3] = {sn % n, (sn / n) % n, sn / (n * n)};
+          double w = 1;
+          for (int d = 0; d < D; ++d) w *= (*F[(q >> d) & 1])[i[d] * n + k[d]];
+          for (int v = 0; v < NV; ++v) dst[node * NV + v] += w * src[sn * NV + v];
+        }
+      }
+      continue;
+    }
+    // a coarsened parent: sum over its children of reverse_{lower,upper} per axis
+    for (int q = 0; q < nch; ++q) {
+      const int64_t c = former_child0.at(cell) + q;
+      const double* src = &u[(size_t)old_elem.at(c) * nn * NV];
+      for (int node = 0; node < nn; ++node) {
+        const int i[3] = {node % n, (node / n) % n, node / (n * n)};
+        for (int sn = 0; sn < nn; ++sn) {
+          const int k[3] = {sn % n, (sn / n) % n, sn / (n * n)};
+          double w = 1;
+          for (int d = 0; d < D; ++d) w *= (*R[(q >> d) & 1])[i[d] * n + k[d]];
+          for (int v = 0; v < NV; ++v) dst[node * NV + v] += w * src[sn * NV + v];
+        }
+      }
+    }
+  }
+  s.m = std::move(nm);
+  u.swap(un);
+  return true;
+}
+
 // Julia isapprox(a, b) with default rtol = sqrt(eps)
 static bool isapprox(double a, double b) {
   return a == b || (std::isfinite(a) && std::isfinite(b) &&
@@ -1664,6 +1863,102 @@ int orc_solve(void* h, double* u, double t0, double t_end, double cfl, int64_t m
     iter += 1;
     t += dt;
     dt = cfl * max_dt(s, u);
+  }
+  *t_out = t;
+  *nsteps_out = iter;
+  return 0;
+}
+
+// AMR settings of the solver (AMRCallback + ControllerThreeLevel with an HG
+// indicator); ints: interval, adapt_initial_condition,
+// adapt_initial_condition_only_refine, alpha_smooth, base_level, med_level,
+// max_level; doubles: alpha_max, alpha_min, med_threshold, max_threshold.
+void orc_set_amr(void* h, const int* ints, const double* dbls) {
+  Solver& s = *(Solver*)h;
+  AmrParams& a = s.amr;
+  a.interval = ints[0];
+  a.adapt_initial = ints[1] != 0;
+  a.initial_only_refine = ints[2] != 0;
+  a.alpha_smooth = ints[3] != 0;
+  a.base_level = ints[4];
+  a.med_level = ints[5];
+  a.max_level = ints[6];
+  a.alpha_max = dbls[0];
+  a.alpha_min = dbls[1];
+  a.med_threshold = dbls[2];
+  a.max_threshold = dbls[3];
+}
+
+// One AMR pass on u (nelements(h) elements); the adapted state is kept in
+// the solver (orc_get_state).  Returns 1 if the mesh changed.
+int orc_adapt(void* h, const double* u, int only_refine, int only_coarsen) {
+  Solver& s = *(Solver*)h;
+  s.u_state.assign(u, u + (size_t)s.ndofs() * s.eq.NV);
+  return amr_adapt(s, s.u_state, s.amr, only_refine != 0, only_coarsen != 0) ? 1 : 0;
+}
+
+void orc_get_state(void* h, double* u) {
+  const Solver& s = *(Solver*)h;
+  std::memcpy(u, s.u_state.data(), sizeof(double) * s.u_state.size());
+}
+
+void orc_element_levels(void* h, int* levels) {
+  const Solver& s = *(Solver*)h;
+  for (int64_t e = 0; e < s.m.nelem; ++e) levels[e] = s.m.elevel[e];
+}
+
+// solve() with the AMR callback: initial-condition adaptation (repeated with
+// a fresh initial condition while the mesh changes, at most
+// max(10, max_level) passes, amr.jl:143-181), then AMR after every
+// `interval` accepted steps unless the final time is reached; the step size
+// is recomputed from the adapted state (StepsizeCallback after AMRCallback).
+// The final state stays in the solver (orc_get_state).
+int orc_solve_amr(void* h, int ic, const double* params, double t0, double t_end, double cfl,
+                  int64_t max_steps, double* t_out, int64_t* nsteps_out) {
+  Solver& s = *(Solver*)h;
+  const AmrParams& ap = s.amr;
+  auto fresh = [&]() {
+    s.u_state.assign((size_t)s.ndofs() * s.eq.NV, 0.0);
+    orc_initial_condition(h, ic, params, t0, s.u_state.data());
+  };
+  fresh();
+  if (ap.adapt_initial) {
+    bool changed = amr_adapt(s, s.u_state, ap, ap.initial_only_refine, false);
+    int iterations = 1;
+    while (changed) {
+      fresh();
+      changed = amr_adapt(s, s.u_state, ap, ap.initial_only_refine, false);
+      if (++iterations > std::max(10, ap.max_level)) break;
+    }
+    fresh();
+  }
+  double t = t0;
+  std::vector<double> du, u_tmp;
+  double dt = cfl * max_dt(s, s.u_state.data());
+  int64_t iter = 0;
+  bool finalstep = false;
+  while (!finalstep && iter < max_steps) {
+    if (std::isnan(dt)) {
+      *t_out = t;
+      *nsteps_out = iter;
+      return -1;
+    }
+    if (t + dt > t_end || isapprox(t + dt, t_end)) {
+      dt = t_end - t;
+      finalstep = true;
+    }
+    const int64_t ndof = s.ndofs() * s.eq.NV;
+    du.assign(ndof, 0.0);
+    u_tmp.assign(ndof, 0.0);
+    for (int stage = 0; stage < 5; ++stage) {
+      rhs(s, du.data(), s.u_state.data(), t + dt * CK_C[stage]);
+      rk_update(ndof, s.u_state.data(), u_tmp.data(), du.data(), CK_A[stage], CK_B[stage] * dt);
+    }
+    iter += 1;
+    t += dt;
+    if (ap.interval > 0 && iter % ap.interval == 0 && !finalstep)
+      amr_adapt(s, s.u_state, ap, false, false);
+    dt = cfl * max_dt(s, s.u_state.data());
   }
   *t_out = t;
   *nsteps_out = iter;

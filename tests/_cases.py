@@ -23,6 +23,8 @@ def oracle_from_case(O, c, **over):
                    alpha_smooth=c.get("alpha_smooth", True), source=src)
     if c.get("refinement_patches"):
         orc.set_refinement(c["refinement_patches"])
+    if c.get("amr"):
+        orc.set_amr(**c["amr"])
     if c.get("boundary"):
         code = dict(dirichlet=O.BC_DIRICHLET, slip_wall=O.BC_SLIP_WALL)[c["boundary"]]
         orc.set_boundaries([code] * (2 * c["ndims"]), ic_id(O, c["ic"]), c.get("ic_params"))
@@ -34,4 +36,5 @@ def ic_id(O, name):
                 isentropic_vortex=O.IC_ISENTROPIC_VORTEX, weak_blast_wave=O.IC_WEAK_BLAST_WAVE,
                 kelvin_helmholtz=O.IC_KELVIN_HELMHOLTZ, taylor_green=O.IC_TAYLOR_GREEN,
                 gaussian_blast=O.IC_GAUSSIAN_BLAST,
-                isentropic_vortex_advected=O.IC_ISENTROPIC_VORTEX_ADVECTED)[name]
+                isentropic_vortex_advected=O.IC_ISENTROPIC_VORTEX_ADVECTED,
+                blast_wave=O.IC_BLAST_WAVE)[name]

@@ -109,6 +109,16 @@ CASES = {
         ic="isentropic_vortex", ic_params=[25.0, 5.0], source="none",
         vi="hg", volume_flux="shima_etal", surface_flux="llf_naive", alpha_max=0.5,
         alpha_min=0.001, alpha_smooth=True, cfl=0.7, tspan=[0.0, 1.0]),
+    "TreeMesh2D Euler: elixir_euler_blast_wave_amr.jl": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_blast_wave_amr.jl",
+        ndims=2, polydeg=3, level=6, xmin=[-2.0, -2.0], xmax=[2.0, 2.0],
+        ic="blast_wave", source="none", vi="hg", volume_flux="ranocha",
+        surface_flux="llf_naive", alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
+        cfl=0.9, tspan=[0.0, 12.5],
+        amr=dict(interval=5, adapt_initial_condition=True,
+                 adapt_initial_condition_only_refine=True, alpha_max=0.5, alpha_min=0.001,
+                 alpha_smooth=True, base_level=4, max_level=6, max_threshold=0.01)),
     "TreeMesh3D Euler: elixir_euler_mortar.jl": dict(
         file="test/test_tree_3d_euler.jl",
         elixir="examples/tree_3d_dgsem/elixir_euler_mortar.jl",

@@ -20,9 +20,12 @@ def test_oracle_reproduces_trixi_golden(oracle_mod, name):
     orc = oracle_from_case(O, c)
     ic = ic_id(O, c["ic"])
     par = c.get("ic_params")
-    u0 = orc.initial_condition(ic, par, c["tspan"][0])
-    u, t, nsteps = orc.solve(u0, c["tspan"][0], c["tspan"][1], c["cfl"],
-                             max_steps=c.get("maxiters", 10**9))
+    if c.get("amr"):
+        u, t, nsteps = orc.solve_amr(ic, par, c["tspan"][0], c["tspan"][1], c["cfl"])
+    else:
+        u0 = orc.initial_condition(ic, par, c["tspan"][0])
+        u, t, nsteps = orc.solve(u0, c["tspan"][0], c["tspan"][1], c["cfl"],
+                                 max_steps=c.get("maxiters", 10**9))
     l2, linf = orc.error_norms(u, t, ic, par)
     if "maxiters" in c:
         # free-stream preservation: goldens are round-off (~1e-16); compare absolutely
