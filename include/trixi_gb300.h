@@ -252,6 +252,32 @@ int tg_entropy_timederivative(tg_ctx* ctx, double t, double* out);
  * Only for TG_VOLUME_SHOCK_CAPTURING_HG contexts. */
 int tg_alpha(tg_ctx* ctx, const double* u_dev, double* alpha_host);
 
+/* AMR (AMRCallback on a TreeMesh, src/callbacks_step/amr.jl:244-392).
+ *
+ * tg_amr_indicator: IndicatorHennemannGassner of the context state with the
+ * given parameters (variable density_pressure; indicators.jl:114-148 and
+ * apply_smoothing!), always evaluated in FP64 -- the element values
+ * ControllerThreeLevel compares with its thresholds (amr.jl:1116-1168).
+ * Synchronous; alpha_host has nelements entries.
+ *
+ * tg_adapt_state: the solution transfer of refine!/coarsen!
+ * (amr_dg2d.jl:85-485, amr_dg3d.jl) from the state of `src` (the mesh before
+ * adaptation) into `dst` (a context built for the adapted mesh), on the
+ * device.  Per new element e: kind[e] = 0 copies element source_element[e];
+ * kind[e] = 1 + q makes it child q (child order of the tree, x fastest) of
+ * the refined element source_element[e] by tensor-product interpolation with
+ * forward_{lower,upper}; kind[e] = -1 makes it the parent of the coarsened
+ * elements source_element[e] .. + 2^ndims - 1 by the sum of their
+ * reverse_{lower,upper} L2 projections.  The matrices are those of the
+ * LobattoLegendreAdaptorL2 (= the mortar matrices), n x n column-major.
+ * Both contexts must share device, ndims, polydeg and precision.
+ * Synchronous; dst then holds an uploaded state. */
+int tg_amr_indicator(tg_ctx* ctx, double alpha_max, double alpha_min, int32_t alpha_smooth,
+                     double* alpha_host);
+int tg_adapt_state(tg_ctx* dst, tg_ctx* src, const int64_t* source_element, const int8_t* kind,
+                   const double* forward_upper, const double* forward_lower,
+                   const double* reverse_upper, const double* reverse_lower);
+
 /* Sticky device status word (bit 0: NaN in the state, bit 1: non-positive
  * density or pressure seen by the CFL reduction).  Reading clears it. */
 int tg_status(tg_ctx* ctx, int32_t* flags);

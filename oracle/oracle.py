@@ -82,6 +82,9 @@ def _load():
     lib.orc_adapt.restype = i
     lib.orc_adapt.argtypes = [vp, P(d), i, i]
     lib.orc_get_state.argtypes = [vp, P(d)]
+    lib.orc_adapt_with.restype = i
+    lib.orc_adapt_with.argtypes = [vp, P(d), P(i), i, i]
+    lib.orc_amr_lambda.argtypes = [vp, P(d), P(i)]
     lib.orc_element_levels.argtypes = [vp, P(i)]
     lib.orc_solve_amr.restype = i
     lib.orc_solve_amr.argtypes = [vp, i, P(d), d, d, d, i64, P(d), P(i64)]
@@ -306,6 +309,29 @@ def _adapt(self, u, only_refine=False, only_coarsen=False):
     out = np.zeros(self.shape)
     self.lib.orc_get_state(self.h, _p(out))
     return changed, out
+
+
+def _adapt_with(self, u, controller_value, only_refine=False, only_coarsen=False):
+    """One AMR pass with given controller values; returns (changed, new state)."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    lam = np.ascontiguousarray(controller_value, dtype=np.int32)
+    changed = bool(self.lib.orc_adapt_with(self.h, _p(u), _p(lam, ctypes.c_int),
+                                           int(only_refine), int(only_coarsen)))
+    self.refresh()
+    out = np.zeros(self.shape)
+    self.lib.orc_get_state(self.h, _p(out))
+    return changed, out
+
+
+def _amr_lambda(self, u):
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    out = np.zeros(self.nelements, dtype=np.int32)
+    self.lib.orc_amr_lambda(self.h, _p(u), _p(out, ctypes.c_int))
+    return out
+
+
+Oracle.adapt_with = _adapt_with
+Oracle.amr_lambda = _amr_lambda
 
 
 def _element_levels(self):

@@ -1555,10 +1555,18 @@ static std::vector<int> amr_controller(const Solver& s, const double* u, const A
 // elements get the tensor-product interpolation of their parent
 // (refine_element!), coarsened ones the sum of the L2 projections of their
 // children (coarsen_elements!).  Returns whether the mesh changed.
+static bool amr_adapt_with(Solver& s, std::vector<double>& u, const std::vector<int>& lambda,
+                           bool only_refine, bool only_coarsen);
+
 static bool amr_adapt(Solver& s, std::vector<double>& u, const AmrParams& ap, bool only_refine,
                       bool only_coarsen) {
+  return amr_adapt_with(s, u, amr_controller(s, u.data(), ap), only_refine, only_coarsen);
+}
+
+// The AMR pass for given controller values (+1 refine, -1 coarsen, 0 keep).
+static bool amr_adapt_with(Solver& s, std::vector<double>& u, const std::vector<int>& lambda,
+                           bool only_refine, bool only_coarsen) {
   const int D = s.eq.D, NV = s.eq.NV, n = s.b.n, nn = s.nn, nch = 1 << D;
-  const std::vector<int> lambda = amr_controller(s, u.data(), ap);
   Tree& t = s.m.tree;
   const std::vector<int64_t> old_leaves = s.m.leaf_cells;
   std::unordered_map<int64_t, int64_t> old_elem;
@@ -1897,6 +1905,21 @@ int orc_adapt(void* h, const double* u, int only_refine, int only_coarsen) {
   return amr_adapt(s, s.u_state, s.amr, only_refine != 0, only_coarsen != 0) ? 1 : 0;
 }
 
+// The same pass with controller values given per element.
+int orc_adapt_with(void* h, const double* u, const int* lambda, int only_refine, int only_coarsen) {
+  Solver& s = *(Solver*)h;
+  s.u_state.assign(u, u + (size_t)s.ndofs() * s.eq.NV);
+  std::vector<int> lam(lambda, lambda + s.m.nelem);
+  return amr_adapt_with(s, s.u_state, lam, only_refine != 0, only_coarsen != 0) ? 1 : 0;
+}
+
+// ControllerThreeLevel's values for u with the AMR settings of the solver.
+void orc_amr_lambda(void* h, const double* u, int* lambda) {
+  const Solver& s = *(Solver*)h;
+  const std::vector<int> lam = amr_controller(s, u, s.amr);
+  std::memcpy(lambda, lam.data(), sizeof(int) * lam.size());
+}
+
 void orc_get_state(void* h, double* u) {
   const Solver& s = *(Solver*)h;
   std::memcpy(u, s.u_state.data(), sizeof(double) * s.u_state.size());
@@ -1930,7 +1953,6 @@ int orc_solve_amr(void* h, int ic, const double* params, double t0, double t_end
       changed = amr_adapt(s, s.u_state, ap, ap.initial_only_refine, false);
       if (++iterations > std::max(10, ap.max_level)) break;
     }
-    fresh();
   }
   double t = t0;
   std::vector<double> du, u_tmp;

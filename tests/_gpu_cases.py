@@ -18,6 +18,7 @@ IC = {"convergence_test": (lambda p: T.initial_condition_convergence_test, O.IC_
       "taylor_green": (lambda p: T.initial_condition_taylor_green_vortex(*(p or [0.1])),
                        O.IC_TAYLOR_GREEN),
       "constant": (lambda p: T.initial_condition_constant, O.IC_CONSTANT),
+      "blast_wave": (lambda p: T.initial_condition_blast_wave, O.IC_BLAST_WAVE),
       "gaussian_blast": (lambda p: T.initial_condition_gaussian_blast(*(p or [1e-5, 1.0, 0.25])),
                          O.IC_GAUSSIAN_BLAST)}
 
@@ -61,10 +62,27 @@ def build(c, precision="fp64", elements_per_block=0):
                    source=O.SRC_CONVERGENCE_TEST if src is not None else O.SRC_NONE)
     if c.get("refinement_patches"):
         orc.set_refinement(c["refinement_patches"])
+    if c.get("amr"):
+        orc.set_amr(**c["amr"])
     if boundary is not None:
         code = dict(dirichlet=O.BC_DIRICHLET, slip_wall=O.BC_SLIP_WALL)[boundary]
         orc.set_boundaries([code] * (2 * D), IC[c["ic"]][1], c.get("ic_params"))
     return semi, orc
+
+
+def amr_callback(semi, c):
+    """AMRCallback + ControllerThreeLevel(IndicatorHennemannGassner) from a case's amr dict."""
+    a = dict(c["amr"])
+    ind = T.IndicatorHennemannGassner(semi, alpha_max=a.pop("alpha_max", 0.5),
+                                      alpha_min=a.pop("alpha_min", 0.001),
+                                      alpha_smooth=a.pop("alpha_smooth", True),
+                                      variable=T.density_pressure)
+    ctrl = T.ControllerThreeLevel(semi, ind, base_level=a.pop("base_level", 1),
+                                  med_level=a.pop("med_level", None),
+                                  med_threshold=a.pop("med_threshold", 0.0),
+                                  max_level=a.pop("max_level", None),
+                                  max_threshold=a.pop("max_threshold", 1.0))
+    return T.AMRCallback(semi, ctrl, **a)
 
 
 def perturbed_state(semi, seed=0, amp=1e-2):

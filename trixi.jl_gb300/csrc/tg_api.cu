@@ -520,6 +520,72 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// Solution transfer of AMR (refine_element! / coarsen_elements!,
+// amr_dg2d.jl:224-294, 429-485; amr_dg3d.jl): one thread per node of the
+// adapted mesh.  mats: forward lower, upper, reverse lower, upper
+// (row-major, M[a * N + b] = M[a, b]); the matrix along axis d of child q is
+// the upper one when bit d of q is set.  Interpolated and projected values
+// are formed in FP64 (float-float states: from hi + lo).
+struct AdaptMats {
+  double m[4][MAXN * MAXN];
+};
+
+template <int D, typename S>
+__global__ void adapt_state_kernel(const S* __restrict__ uo, S* __restrict__ un,
+                                   const int64_t* __restrict__ source, const int8_t* __restrict__ kind,
+                                   int64_t E, int N, const AdaptMats M) {
+  constexpr int NV = D + 2;
+  const int NN = D == 2 ? N * N : N * N * N;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= E * NN) return;
+  const int64_t e = k / NN;
+  const int node = (int)(k - e * NN);
+  const int kd = kind[e];
+  const int64_t s0 = source[e];
+  if (kd == 0) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) un[k * NV + v] = uo[(s0 * NN + node) * NV + v];
+    return;
+  }
+  const int i[3] = {node % N, (node / N) % N, node / (N * N)};
+  double acc[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) acc[v] = 0.0;
+  const int nsrc = kd > 0 ? 1 : (1 << D);
+  for (int q = 0; q < nsrc; ++q) {
+    const int child = kd > 0 ? kd - 1 : q;
+    const int64_t se = kd > 0 ? s0 : s0 + q;
+    const double* Md[3];
+#pragma unroll
+    for (int d = 0; d < D; ++d) Md[d] = M.m[(kd > 0 ? 0 : 2) + ((child >> d) & 1)];
+    for (int sn = 0; sn < NN; ++sn) {
+      const int kk[3] = {sn % N, (sn / N) % N, sn / (N * N)};
+      double w = 1.0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) w *= Md[d][i[d] * N + kk[d]];
+      const S* p = uo + (se * NN + sn) * NV;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double x;
+        if constexpr (std::is_same<S, double>::value)
+          x = p[v];
+        else
+          x = (double)p[v].x + (double)p[v].y;
+        acc[v] += w * x;
+      }
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    if constexpr (std::is_same<S, double>::value) {
+      un[k * NV + v] = acc[v];
+    } else {
+      const float hi = (float)acc[v];
+      un[k * NV + v] = make_float2(hi, (float)(acc[v] - (double)hi));
+    }
+  }
+}
+
 // apply_smoothing! as a gather (indicators_2d.jl:104-136): alpha_e =
 // max(raw_e, 0.5 * raw_n for every element n across a face or a mortar).
 template <typename R>
@@ -572,6 +638,10 @@ struct tg_ctx {
   double* d_mmat = nullptr;           // forward lower/upper, reverse lower/upper (row-major)
   double* d_mflux = nullptr;          // fp64: [nmface][NF][NV] mortar pre-pass output
   int8_t* d_scls = nullptr;           // mixed: size class of each element (source tables)
+  double* d_amr_raw = nullptr;        // AMR indicator (unsmoothed, smoothed)
+  double* d_amr_alpha = nullptr;
+  int64_t* d_amap = nullptr;          // AMR transfer map of the last tg_adapt_state
+  int8_t* d_akind = nullptr;
   double* d_weights = nullptr;
   double* d_partial = nullptr;
   double* d_sums = nullptr;
@@ -623,7 +693,7 @@ static void free_ctx(tg_ctx* c) {
     if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
   void* ptrs[] = {c->d_u[0], c->d_u[1], c->d_utmp, c->d_du, c->d_uscratch, c->d_stage64,
                   c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_nbr, c->d_invj, c->d_xline,
-                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mflux, c->d_scls, c->d_weights, c->d_partial, c->d_sums, c->d_clock,
+                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mflux, c->d_scls, c->d_amr_raw, c->d_amr_alpha, c->d_amap, c->d_akind, c->d_weights, c->d_partial, c->d_sums, c->d_clock,
                   c->d_status, c->d_speed};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1659,6 +1729,98 @@ int tg_entropy_timederivative(tg_ctx* c, double t, double* out) {
   CUDA_TRY(c, cudaMemcpyAsync(h, c->d_sums, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   *out = h[0] / h[1];
+  return TG_OK;
+}
+
+int tg_amr_indicator(tg_ctx* c, double alpha_max, double alpha_min, int32_t alpha_smooth,
+                     double* alpha_host) {
+  if (!c || !alpha_host) return TG_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return fail(c, TG_ERR_STATE, "no state uploaded");
+  if (!(alpha_max >= 0 && alpha_min >= 0)) return fail(c, TG_ERR_INVALID_ARGUMENT, "alpha bounds");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  int rc = ensure(c, (void**)&c->d_amr_raw, sizeof(double) * c->E);
+  if (!rc) rc = ensure(c, (void**)&c->d_amr_alpha, sizeof(double) * c->E);
+  if (rc) return rc;
+  const double* u = export_state(c, &rc);
+  if (!u) return rc;
+  DgParams P = c->P;
+  P.alpha_max = alpha_max;
+  P.alpha_min = alpha_min;
+  rc = launch_indicator(c->D, c->N, true, P, u, c->d_amr_raw, c->stream);
+  if (rc != 0) return fail(c, TG_ERR_CUDA, "indicator kernel launch failed (%d)", rc);
+  smooth_alpha_kernel<double><<<(unsigned)((c->E + 127) / 128), 128, 0, c->stream>>>(
+      c->d_amr_raw, c->d_nbr, c->E, 2 * c->D, alpha_smooth, c->P.nbc, c->d_mnbr, c->d_amr_alpha);
+  CUDA_TRY(c, cudaGetLastError());
+  CUDA_TRY(c, cudaMemcpyAsync(alpha_host, c->d_amr_alpha, sizeof(double) * c->E,
+                              cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return TG_OK;
+}
+
+int tg_adapt_state(tg_ctx* dst, tg_ctx* src, const int64_t* source_element, const int8_t* kind,
+                   const double* forward_upper, const double* forward_lower,
+                   const double* reverse_upper, const double* reverse_lower) {
+  if (!dst || !src || !source_element || !kind || !forward_upper || !forward_lower ||
+      !reverse_upper || !reverse_lower)
+    return TG_ERR_INVALID_ARGUMENT;
+  if (dst == src || dst->device != src->device || dst->D != src->D || dst->N != src->N ||
+      dst->fp64 != src->fp64)
+    return fail(dst, TG_ERR_INVALID_ARGUMENT,
+                "adapt_state: contexts differ in device, ndims, polydeg or precision");
+  if (!src->uploaded) return fail(dst, TG_ERR_STATE, "adapt_state: the source has no state");
+  const int nch = 1 << dst->D, N = dst->N;
+  for (int64_t e = 0; e < dst->E; ++e) {
+    const int k = kind[e];
+    const int64_t last = source_element[e] + (k < 0 ? nch - 1 : 0);
+    if (k < -1 || k > nch || source_element[e] < 0 || last >= src->E)
+      return fail(dst, TG_ERR_INVALID_ARGUMENT, "adapt_state: element %lld maps outside the source",
+                  (long long)e);
+  }
+  AdaptMats M{};
+  const double* in[4] = {forward_lower, forward_upper, reverse_lower, reverse_upper};
+  for (int q = 0; q < 4; ++q)
+    for (int a = 0; a < N; ++a)
+      for (int b = 0; b < N; ++b) M.m[q][a * N + b] = in[q][a + b * N];
+  CUDA_TRY(dst, cudaSetDevice(dst->device));
+  CUDA_TRY(dst, cudaStreamSynchronize(src->stream));  // the source state is final
+  if (dst->d_amap) {
+    cudaFree(dst->d_amap);
+    dst->d_amap = nullptr;
+  }
+  if (dst->d_akind) {
+    cudaFree(dst->d_akind);
+    dst->d_akind = nullptr;
+  }
+  int rc = ensure(dst, (void**)&dst->d_amap, sizeof(int64_t) * dst->E);
+  if (!rc) rc = ensure(dst, (void**)&dst->d_akind, sizeof(int8_t) * dst->E);
+  if (rc) return rc;
+  CUDA_TRY(dst, cudaMemcpyAsync(dst->d_amap, source_element, sizeof(int64_t) * dst->E,
+                                cudaMemcpyHostToDevice, dst->stream));
+  CUDA_TRY(dst, cudaMemcpyAsync(dst->d_akind, kind, sizeof(int8_t) * dst->E, cudaMemcpyHostToDevice,
+                                dst->stream));
+  const int64_t nt = dst->E * dst->NN;
+  const unsigned nb = (unsigned)((nt + 127) / 128);
+  void* out = dst->d_u[dst->cur];
+  const void* uo = src->d_u[src->cur];
+  if (dst->fp64) {
+    if (dst->D == 2)
+      adapt_state_kernel<2, double><<<nb, 128, 0, dst->stream>>>((const double*)uo, (double*)out,
+                                                                 dst->d_amap, dst->d_akind, dst->E, N, M);
+    else
+      adapt_state_kernel<3, double><<<nb, 128, 0, dst->stream>>>((const double*)uo, (double*)out,
+                                                                 dst->d_amap, dst->d_akind, dst->E, N, M);
+  } else {
+    if (dst->D == 2)
+      adapt_state_kernel<2, float2><<<nb, 128, 0, dst->stream>>>((const float2*)uo, (float2*)out,
+                                                                 dst->d_amap, dst->d_akind, dst->E, N, M);
+    else
+      adapt_state_kernel<3, float2><<<nb, 128, 0, dst->stream>>>((const float2*)uo, (float2*)out,
+                                                                 dst->d_amap, dst->d_akind, dst->E, N, M);
+  }
+  CUDA_TRY(dst, cudaGetLastError());
+  CUDA_TRY(dst, cudaStreamSynchronize(dst->stream));
+  dst->uploaded = true;
+  dst->clock_valid = false;
   return TG_OK;
 }
 

@@ -20,7 +20,8 @@ the host side: mesh/basis setup, the C-ABI binding and the driver loop.
 from ._lib import TrixiGB300Error, load as load_library  # noqa: F401
 from .analysis import calc_error_norms  # noqa: F401
 from .basis import LobattoLegendreAnalyzer, LobattoLegendreBasis, MortarL2  # noqa: F401
-from .equations import (CompressibleEulerEquations2D, CompressibleEulerEquations3D,  # noqa: F401
+from .equations import (initial_condition_blast_wave,  # noqa: F401
+                        CompressibleEulerEquations2D, CompressibleEulerEquations3D,  # noqa: F401
                         FluxLaxFriedrichs, cons2prim, density_pressure, flux_central,
                         flux_lax_friedrichs, flux_ranocha, flux_shima_etal,
                         initial_condition_constant, initial_condition_convergence_test,
@@ -39,3 +40,4 @@ from .time_integration import (AliveCallback, AnalysisCallback, CallbackSet,  # 
                                CarpenterKennedy2N54, StepsizeCallback, SummaryCallback,
                                ode_default_options, solve)
 from .ensemble import Ensemble  # noqa: F401
+from .amr import AMRCallback, ControllerThreeLevel  # noqa: F401

@@ -37,7 +37,8 @@ EXPORTS = ("tg_api_version", "tg_ctx_create", "tg_ctx_destroy", "tg_last_error",
            "tg_mlp_gradient", "tg_mlp_predict", "tg_ctx_set_learned_indicator", "tg_mlp_last",
            "tg_entropy_timederivative", "tg_ensemble_create", "tg_ensemble_destroy",
            "tg_ensemble_size", "tg_ensemble_context", "tg_ensemble_step", "tg_ensemble_autotune",
-           "tg_ensemble_threads_per_block", "tg_ensemble_last_error", "tg_ctx_autotune")
+           "tg_ensemble_threads_per_block", "tg_ensemble_last_error", "tg_ctx_autotune",
+           "tg_amr_indicator", "tg_adapt_state")
 
 
 class TrixiGB300Error(RuntimeError):
@@ -121,6 +122,9 @@ def load(path: str | None = None):
         "tg_set_time": ([vp, d], ctypes.c_int),
         "tg_integrals": ([vp, pd], ctypes.c_int),
         "tg_alpha": ([vp, vp, pd], ctypes.c_int),
+        "tg_amr_indicator": ([vp, ctypes.c_double, ctypes.c_double, i32, pd], ctypes.c_int),
+        "tg_adapt_state": ([vp, vp, P(ctypes.c_int64), P(ctypes.c_int8), pd, pd, pd, pd],
+                           ctypes.c_int),
         "tg_status": ([vp, P(i32)], ctypes.c_int),
         "tg_synchronize": ([vp], ctypes.c_int),
         "tg_elements_per_block": ([vp, P(i32)], ctypes.c_int),

@@ -146,6 +146,23 @@ def initial_condition_convergence_test(x, t, equations):
     return u
 
 
+def initial_condition_blast_wave(x, t, equations):
+    """The medium blast wave of examples/tree_2d_dgsem/elixir_euler_blast_wave_amr.jl:18-34
+    (Hennemann & Gassner 2020, sec. 6.3): the weak blast wave's inner state in a
+    background at p = 1e-3."""
+    if equations.ndims != 2:
+        raise NotImplementedError("initial_condition_blast_wave is the 2D elixir's")
+    r = np.sqrt(x[..., 0] ** 2 + x[..., 1] ** 2)
+    phi = np.arctan2(x[..., 1], x[..., 0])
+    out = r > 0.5
+    prim = np.empty(x.shape[:-1] + (4,))
+    prim[..., 0] = np.where(out, 1.0, 1.1691)
+    prim[..., 1] = np.where(out, 0.0, 0.1882 * np.cos(phi))
+    prim[..., 2] = np.where(out, 0.0, 0.1882 * np.sin(phi))
+    prim[..., 3] = np.where(out, 1.0e-3, 1.245)
+    return prim2cons(prim, equations)
+
+
 def initial_condition_weak_blast_wave(x, t, equations):
     """compressible_euler_2d.jl:245-264, 3d.jl:241-263."""
     D = equations.ndims

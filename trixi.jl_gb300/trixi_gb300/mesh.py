@@ -104,6 +104,38 @@ class _Tree:
             for c in refined:
                 self._refine_cell(c)
 
+    def coarsen(self, parents):
+        """coarsen!(t, cell_ids), abstract_tree.jl:516-618: parents whose children
+        are all leaves, highest level first; a parent is kept when one of its
+        children has a same-level neighbour with children across a face that is
+        not shared with a sibling (the 2:1 rule).  Returns {parent: first child}
+        of the coarsened parents."""
+        order = sorted(parents, key=lambda c: self.level[c])  # stable, as Julia's sort
+        done = {}
+        nch = 1 << self.D
+        while order:
+            cell = order.pop()
+            first = self.child0[cell]
+            skip = False
+            for ch in range(nch):
+                c = first + ch
+                for direction in range(2 * self.D):
+                    if (ch >> (direction // 2)) & 1 != direction & 1:
+                        continue  # the neighbour across this face is a sibling
+                    nb = self.neighbour(c, direction)
+                    if nb >= 0 and not self.is_leaf(nb):
+                        skip = True
+                        break
+                if skip:
+                    break
+            if skip:
+                continue
+            for ch in range(nch):
+                del self.index[(self.level[first + ch], self.ix[first + ch])]
+            self.child0[cell] = -1
+            done[cell] = first
+        return done
+
     def leaves(self):
         """Leaf cells depth-first with children in _child_signs order."""
         out, stack = [], [0]
@@ -201,6 +233,62 @@ class TreeMesh:
         if self._tree is not None:
             return len(self._leaves)
         return self.cartesian.shape[0]
+
+    def _ensure_tree(self):
+        if self._tree is None:
+            self._build_tree()
+            del self.cartesian
+
+    def adapt(self, controller_value, only_refine=False, only_coarsen=False):
+        """One AMR pass on the tree (amr.jl:244-392): refine! the leaves with
+        controller_value > 0 (with rebalancing), then coarsen! the parents whose
+        children all have controller_value < 0.  Returns (changed,
+        source_element, kind) for the elements of the adapted mesh: kind 0 copies
+        element source_element, 1 + q is child q of the refined element
+        source_element, -1 the parent of the coarsened elements source_element ..
+        source_element + 2^ndims - 1 (the layout tg_adapt_state takes)."""
+        self._ensure_tree()
+        t = self._tree
+        lam = np.asarray(controller_value)
+        if lam.shape != (len(self._leaves),):
+            raise ValueError("one controller value per element")
+        old_leaves = self._leaves
+        old_elem = {c: e for e, c in enumerate(old_leaves)}
+        to_refine = [old_leaves[e] for e in np.flatnonzero(lam > 0)]
+        to_coarsen = [old_leaves[e] for e in np.flatnonzero(lam < 0)]
+        changed = False
+        former = {}
+        if not only_coarsen and to_refine:
+            t.refine(to_refine)
+            changed = True
+        if not only_refine and to_coarsen:
+            count = {}
+            parents = []
+            nch = 1 << self.ndims
+            for cell in to_coarsen:
+                if t.level[cell] == 0 or not t.is_leaf(cell):
+                    continue
+                p = t.parent(cell)
+                count[p] = count.get(p, 0) + 1
+                if count[p] == nch:
+                    parents.append(p)
+            former = t.coarsen(sorted(parents))
+            changed = changed or bool(former)
+        if not changed:
+            return False, None, None
+        self._leaves = t.leaves()
+        E = len(self._leaves)
+        src = np.zeros(E, dtype=np.int64)
+        kind = np.zeros(E, dtype=np.int8)
+        for e, cell in enumerate(self._leaves):
+            if cell in old_elem:
+                src[e] = old_elem[cell]
+            elif cell in former:
+                src[e], kind[e] = old_elem[former[cell]], -1
+            else:
+                p = t.parent(cell)
+                src[e], kind[e] = old_elem[p], 1 + (cell - t.child0[p])
+        return True, src, kind
 
     @property
     def is_uniform(self) -> bool:

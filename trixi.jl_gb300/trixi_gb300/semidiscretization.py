@@ -206,6 +206,27 @@ class DeviceContext:
     def _check(self, rc):
         _lib.check(rc, self.h)
 
+    # -- AMR ----------------------------------------------------------------
+    def amr_indicator(self, alpha_max, alpha_min, alpha_smooth):
+        """The smoothed HG indicator of the state with these parameters, in FP64
+        (tg_amr_indicator)."""
+        out = np.zeros(self.semi.nelements)
+        self._check(self.lib.tg_amr_indicator(self.h, float(alpha_max), float(alpha_min),
+                                              int(bool(alpha_smooth)), _dptr(out)))
+        return out
+
+    def adapt_from(self, src, source_element, kind):
+        """This context's state from `src`'s by the AMR transfer map
+        (tg_adapt_state) with the solver's L2 adaptor matrices."""
+        m = self.semi.solver.mortar
+        mats = [np.ascontiguousarray(np.asfortranarray(getattr(m, k)).ravel(order="F"))
+                for k in ("forward_upper", "forward_lower", "reverse_upper", "reverse_lower")]
+        src_e = np.ascontiguousarray(source_element, dtype=np.int64)
+        kd = np.ascontiguousarray(kind, dtype=np.int8)
+        self._check(self.lib.tg_adapt_state(
+            self.h, src.h, src_e.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+            kd.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)), *[_dptr(x) for x in mats]))
+
     # -- state --------------------------------------------------------------
     def upload(self, u):
         if isinstance(u, np.ndarray):
@@ -311,6 +332,12 @@ class SemidiscretizationHyperbolic:
         self.source_terms = source_terms
         self.precision = precision
         self.device, self.elements_per_block = device, elements_per_block
+        self._ctx = None
+        self._setup_containers()
+
+    def _setup_containers(self):
+        """Element geometry, interfaces and mortars of the current mesh."""
+        mesh, equations, solver = self.mesh, self.equations, self.solver
         D, n = equations.ndims, solver.nnodes()
         self.nelements = mesh.nelements
         self.nnodes_per_element = n ** D
@@ -339,7 +366,23 @@ class SemidiscretizationHyperbolic:
         self.neighbor_ids, self.orientations = mesh.interfaces()
         (self.mortar_neighbor_ids, self.mortar_large_sides,
          self.mortar_orientations) = mesh.mortars()
+
+    def adapt(self, controller_value, only_refine=False, only_coarsen=False):
+        """One AMR pass (amr.jl:244-392): adapts the mesh, rebuilds the
+        containers and a device context for them, and transfers the state of the
+        current context on the device (tg_adapt_state).  Returns whether the
+        mesh changed."""
+        changed, src, kind = self.mesh.adapt(controller_value, only_refine, only_coarsen)
+        if not changed:
+            return False
+        old = self._ctx
+        self._setup_containers()
         self._ctx = None
+        if old is not None:
+            new = self.device_context
+            new.adapt_from(old, src, kind)
+            old.close()
+        return True
 
     @property
     def device_context(self) -> DeviceContext:

@@ -30,10 +30,13 @@ class IndicatorHennemannGassner:
     """IndicatorHennemannGassner(equations, basis; alpha_max, alpha_min, alpha_smooth,
     variable), indicators.jl:50-72.  Only variable = density_pressure is on the GPU path."""
 
-    def __init__(self, equations, basis, alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
+    def __init__(self, equations, basis=None, alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
                  variable=density_pressure):
         if variable is not density_pressure:
             raise NotImplementedError("IndicatorHennemannGassner: only variable=density_pressure")
+        if basis is None and hasattr(equations, "solver"):
+            # IndicatorHennemannGassner(semi; ...), indicators.jl:74-83
+            equations, basis = equations.equations, equations.solver.basis
         self.equations, self.basis = equations, basis
         self.alpha_max, self.alpha_min = float(alpha_max), float(alpha_min)
         self.alpha_smooth = bool(alpha_smooth)

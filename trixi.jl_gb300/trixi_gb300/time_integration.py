@@ -12,6 +12,7 @@ import time
 import numpy as np
 
 from .analysis import calc_error_norms
+from .amr import AMRCallback
 
 
 class CarpenterKennedy2N54:
@@ -92,8 +93,25 @@ def solve(ode, alg, dt=None, callback=None, save_everystep=False, maxiters=10**1
     ctx.upload(ode.u0)
     t0, t_end = ode.tspan
     stepsize = cbs.find(StepsizeCallback)
+    amr = cbs.find(AMRCallback)
     tic = time.perf_counter()
-    if stepsize is not None:
+    if amr is not None:
+        if stepsize is None:
+            raise NotImplementedError("AMR on the GPU path needs a StepsizeCallback")
+        # AMRCallback before StepsizeCallback: the initial mesh is adapted
+        # first, and after every `interval` accepted steps the mesh is adapted
+        # and the next step size computed from the adapted state
+        amr.initialize(semi, t0)
+        t, nsteps = t0, 0
+        chunk = amr.interval if amr.interval > 0 else maxiters
+        while nsteps < maxiters:
+            t, n = semi.device_context.step(min(chunk, maxiters - nsteps), stepsize.cfl, t_end, t)
+            nsteps += n
+            if t >= t_end or n < chunk or amr.interval == 0:
+                break
+            amr(semi)
+        ctx = semi.device_context
+    elif stepsize is not None:
         t, nsteps = ctx.step(maxiters, stepsize.cfl, t_end, t0)
     else:
         if dt is None:
