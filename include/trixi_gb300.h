@@ -252,6 +252,39 @@ int tg_entropy_timederivative(tg_ctx* ctx, double t, double* out);
  * Only for TG_VOLUME_SHOCK_CAPTURING_HG contexts. */
 int tg_alpha(tg_ctx* ctx, const double* u_dev, double* alpha_host);
 
+/* Refinement tree of a TreeMesh on the host (no GPU needed): Trixi's
+ * TreeMesh(coordinates_min, coordinates_max; initial_refinement_level,
+ * periodicity, refinement_patches) (tree_mesh.jl:128-215) with refine!
+ * (2:1 rebalancing), coarsen! and the mesh containers of its leaves
+ * (abstract_tree.jl:317-618, containers_{2,3}d.jl), for meshes with
+ * refinement patches or AMR.  Elements are the leaves in Trixi's order.
+ *   tg_tree_refine_patch: type 0 = box (a = coordinates_min, b =
+ *     coordinates_max), 1 = sphere (a = center, radius).
+ *   tg_tree_elements: level and cell centre ([nelements][ndims]) per element.
+ *   tg_tree_interfaces / tg_tree_mortars: cache.interfaces and
+ *     cache.mortars (1-based; layouts as in tg_config), sized by
+ *     tg_tree_counts.
+ *   tg_tree_adapt: the refine-then-coarsen pass of AMR (amr.jl:244-392) for
+ *     controller values per element (+1 refine, -1 coarsen, 0 keep);
+ *     changed = 0 when the mesh stayed the same.  tg_tree_transfer_map then
+ *     gives the source_element / kind arrays tg_adapt_state takes.
+ * Errors are read with tg_last_error(NULL, ...). */
+typedef struct tg_tree tg_tree;
+int tg_tree_create(int32_t ndims, int32_t initial_refinement_level, const double* coordinates_min,
+                   const double* coordinates_max, const int32_t* periodicity, tg_tree** out);
+int tg_tree_destroy(tg_tree* tree);
+int tg_tree_refine_patch(tg_tree* tree, int32_t type, const double* a, const double* b,
+                         double radius);
+int tg_tree_nelements(const tg_tree* tree, int64_t* nelements);
+int tg_tree_elements(const tg_tree* tree, int32_t* levels, double* centers);
+int tg_tree_counts(tg_tree* tree, int64_t* ninterfaces, int64_t* nmortars);
+int tg_tree_interfaces(tg_tree* tree, int64_t* neighbor_ids, int64_t* orientations);
+int tg_tree_mortars(tg_tree* tree, int64_t* neighbor_ids, int64_t* large_sides,
+                    int64_t* orientations);
+int tg_tree_adapt(tg_tree* tree, const int8_t* controller_value, int32_t only_refine,
+                  int32_t only_coarsen, int32_t* changed);
+int tg_tree_transfer_map(const tg_tree* tree, int64_t* source_element, int8_t* kind);
+
 /* AMR (AMRCallback on a TreeMesh, src/callbacks_step/amr.jl:244-392).
  *
  * tg_amr_indicator: IndicatorHennemannGassner of the context state with the

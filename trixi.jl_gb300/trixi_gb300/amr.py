@@ -10,6 +10,8 @@ tree lives on the host.
 """
 from __future__ import annotations
 
+import time
+
 import numpy as np
 
 from .solvers import IndicatorHennemannGassner
@@ -59,11 +61,16 @@ class AMRCallback:
         self.adapt_initial_condition = bool(adapt_initial_condition)
         self.adapt_initial_condition_only_refine = bool(adapt_initial_condition_only_refine)
         self.passes = 0
+        self.seconds = dict(indicator=0.0, adapt=0.0)  # wall time of the passes
 
     def __call__(self, semi, only_refine=False, only_coarsen=False):
         """One AMR pass on the device state of semi; returns whether the mesh changed."""
+        tic = time.perf_counter()
         lam = self.controller(semi)
+        toc = time.perf_counter()
         changed = semi.adapt(lam, only_refine=only_refine, only_coarsen=only_coarsen)
+        self.seconds["indicator"] += toc - tic
+        self.seconds["adapt"] += time.perf_counter() - toc
         self.passes += 1
         return changed
 

@@ -19,6 +19,12 @@
        naive LLF, CFL 1.4 (elixir_euler_taylor_green_vortex.jl): kinetic
        energy history of mixed against FP64 (32^3 to t = 20; 64^3 mixed to
        t = 20 and FP64 to t = 2).
+  c6   AMR: the medium blast wave of elixir_euler_blast_wave_amr.jl at initial
+       level 8 (ControllerThreeLevel on HG, base 6, max 8, interval 5) to
+       t = 0.5, FP64 and mixed: time stepping vs in AMR passes; and the elixir's
+       own size (level 6, base 4, t = 1) in FP64.
+  c7   mortars: 3D MMS 32^3 with the central box refined once, against the
+       uniform 32^3 mesh, FP64 and mixed.
 
 The 3D manufactured solution at 32^3 is the headline case of bench.py.
 Throughput is DOF-updates per second per RK stage (ndofs x 5 stages x steps /
@@ -383,7 +389,98 @@ def ensemble_steps(steps=3):
     return dict(steps=n.tolist())
 
 
-RUNS = dict(c1=c1, c3=c3, c4=c4, c5a=c5a, c5b=c5b)
+# ---------------------------------------------------------------------------
+# c6: AMR (elixir_euler_blast_wave_amr.jl scaled up)
+def amr_blast_semi(level, precision):
+    eq = T.CompressibleEulerEquations2D(1.4)
+    basis = T.LobattoLegendreBasis(3)
+    llf = T.FluxLaxFriedrichs(T.max_abs_speed_naive)
+    ind = T.IndicatorHennemannGassner(eq, basis, alpha_max=0.5, alpha_min=0.001,
+                                      alpha_smooth=True, variable=T.density_pressure)
+    vi = T.VolumeIntegralShockCapturingHG(ind, volume_flux_dg=T.flux_ranocha, volume_flux_fv=llf)
+    mesh = T.TreeMesh((-2.0, -2.0), (2.0, 2.0), initial_refinement_level=level)
+    return T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_blast_wave,
+                                          T.DGSEM(basis, llf, vi), precision=precision)
+
+
+def amr_run(level, base_level, max_level, t_end, precision, cfl=0.9, interval=5):
+    """solve() with AMRCallback, stepping and AMR passes timed apart."""
+    semi = amr_blast_semi(level, precision)
+    ind = T.IndicatorHennemannGassner(semi, alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
+                                      variable=T.density_pressure)
+    ctrl = T.ControllerThreeLevel(semi, ind, base_level=base_level, max_level=max_level,
+                                  max_threshold=0.01)
+    amr = T.AMRCallback(semi, ctrl, interval=interval, adapt_initial_condition=True,
+                        adapt_initial_condition_only_refine=True)
+    wall0 = time.perf_counter()
+    semi.device_context.upload(semi.compute_coefficients(0.0))
+    amr.initialize(semi, 0.0)
+    t, steps, dof_updates, step_secs, elements = 0.0, 0, 0, 0.0, []
+    while True:
+        c = semi.device_context
+        c.synchronize()
+        tic = time.perf_counter()
+        t, n = c.step(interval, cfl, t_end, t)
+        c.synchronize()
+        step_secs += time.perf_counter() - tic
+        steps += n
+        dof_updates += semi.ndofs * 5 * n
+        elements.append(semi.nelements)
+        if t >= t_end or n < interval:
+            break
+        amr(semi)
+    wall = time.perf_counter() - wall0
+    u = semi.device_context.download()
+    l2, linf = T.calc_error_norms(u, t, semi)
+    return dict(t=t, steps=steps, passes=amr.passes, wall_secs=wall, step_secs=step_secs,
+                amr_indicator_secs=amr.seconds["indicator"], amr_adapt_secs=amr.seconds["adapt"],
+                rate_while_stepping=dof_updates / step_secs, rate_overall=dof_updates / wall,
+                elements_min=int(min(elements)), elements_max=int(max(elements)),
+                elements_final=int(semi.nelements), l2=l2.tolist(), linf=linf.tolist())
+
+
+def c6(level=8, base_level=6, max_level=8, t_end=0.5):
+    """AMR blast wave at 8x the elixir's resolution (initial level 8, base 6, max 8)
+    in FP64 and mixed precision: time in steps and in AMR passes, DOF-updates/s."""
+    out = {}
+    for prec in ("fp64", "mixed"):
+        out[prec] = amr_run(level, base_level, max_level, t_end, prec)
+    out["elixir_size_fp64"] = amr_run(6, 4, 6, 1.0, "fp64")
+    out["l2_rho_mixed_over_fp64"] = out["mixed"]["l2"][0] / out["fp64"]["l2"][0]
+    return out
+
+
+# ---------------------------------------------------------------------------
+# c7: throughput on a mesh with mortars
+def c7(steps=40):
+    """3D MMS (polydeg 3, flux_ranocha, LLF, CFL 0.6) on 32^3 elements and on the
+    same mesh with the central box (0.5, 1.5)^3 refined once (61,440 elements,
+    4,096 mortars... counted below), FP64 and mixed: DOF-updates/s per stage."""
+    out = {}
+    for prec in ("mixed", "fp64"):
+        for name, patches in (("uniform", ()),
+                              ("refined", (dict(type="box", coordinates_min=(0.5,) * 3,
+                                                coordinates_max=(1.5,) * 3),))):
+            eq = T.CompressibleEulerEquations3D(1.4)
+            solver = T.DGSEM(polydeg=3, surface_flux=T.flux_lax_friedrichs,
+                             volume_integral=T.VolumeIntegralFluxDifferencing(T.flux_ranocha))
+            mesh = T.TreeMesh((0.0,) * 3, (2.0,) * 3, initial_refinement_level=5,
+                              refinement_patches=patches)
+            semi = T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_convergence_test,
+                                                  solver, source_terms=T.source_terms_convergence_test,
+                                                  precision=prec)
+            solve_timed(semi, 10.0, 0.6, max_steps=3)  # warm-up (graphs, caches)
+            _, t, n, secs = solve_timed(semi, 10.0, 0.6, max_steps=steps)
+            out[f"{prec}_{name}"] = dict(elements=semi.nelements,
+                                         mortars=int(semi.mortar_neighbor_ids.shape[0]),
+                                         steps=n, secs=secs, rate=rate(semi.ndofs, n, secs))
+    for prec in ("mixed", "fp64"):
+        out[f"{prec}_refined_over_uniform_rate"] = (out[f"{prec}_refined"]["rate"] /
+                                                    out[f"{prec}_uniform"]["rate"])
+    return out
+
+
+RUNS = dict(c1=c1, c3=c3, c4=c4, c5a=c5a, c5b=c5b, c6=c6, c7=c7)
 SHORT_RUNS = dict(learned_steps=learned_steps, ensemble_steps=ensemble_steps)
 
 

@@ -12,6 +12,8 @@ large element in every direction towards a refined neighbour
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 
 
@@ -27,126 +29,87 @@ def _morton_cells(ndims: int, level: int):
     return cart
 
 
-class _Tree:
-    """The refinement tree of a TreeMesh (abstract_tree.jl): cells keyed by
-    (level, integer position); a same-level neighbour exists iff its key is
-    present (periodic wrap per dimension), as Trixi's neighbour links record."""
+class _NativeTree:
+    """The refinement tree of a TreeMesh, held by the library (tg_tree_*: Trixi's
+    refine!/coarsen! rules and the containers of the leaves, in C++)."""
 
-    def __init__(self, ndims, periodicity, length0, center0):
-        self.D = ndims
-        self.periodicity = periodicity
-        self.length0 = length0
-        self.level, self.ix, self.center, self.child0 = [], [], [], []
-        self.index = {}
-        self._add(0, (0,) * ndims, tuple(center0))
+    def __init__(self, ndims, level, cmin, cmax, periodicity):
+        from . import _lib
+        self._lib = _lib
+        self.lib = _lib.load()
+        self.ndims = ndims
+        h = ctypes.c_void_p()
+        lo = np.ascontiguousarray(cmin, dtype=np.float64)
+        hi = np.ascontiguousarray(cmax, dtype=np.float64)
+        per = np.ascontiguousarray([int(p) for p in periodicity] + [1] * (3 - ndims), dtype=np.int32)
+        _lib.check(self.lib.tg_tree_create(ndims, level, _dp(lo), _dp(hi),
+                                           per.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                           ctypes.byref(h)))
+        self.h = h
 
-    def _add(self, level, ix, c):
-        self.index[(level, ix)] = len(self.level)
-        self.level.append(level)
-        self.ix.append(ix)
-        self.center.append(c)
-        self.child0.append(-1)
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.tg_tree_destroy(self.h)
+            self.h = None
 
-    def length(self, level):
-        return self.length0 / (1 << level)
+    def refine_patch(self, kind, a, b):
+        pa = np.zeros(3)
+        pa[:self.ndims] = a
+        if kind == "box":
+            pb = np.zeros(3)
+            pb[:self.ndims] = b
+            self._lib.check(self.lib.tg_tree_refine_patch(self.h, 0, _dp(pa), _dp(pb), 0.0))
+        else:
+            self._lib.check(self.lib.tg_tree_refine_patch(self.h, 1, _dp(pa), None, float(b)))
 
-    def is_leaf(self, cell):
-        return self.child0[cell] < 0
+    def nelements(self):
+        n = ctypes.c_int64()
+        self._lib.check(self.lib.tg_tree_nelements(self.h, ctypes.byref(n)))
+        return n.value
 
-    def neighbour(self, cell, direction):
-        """Same-level neighbour across face `direction` (0: -x, 1: +x, ...) or -1."""
-        lev, ix = self.level[cell], list(self.ix[cell])
-        d = direction // 2
-        M = 1 << lev
-        ix[d] += 1 if direction & 1 else -1
-        if not 0 <= ix[d] < M:
-            if not self.periodicity[d]:
-                return -1
-            ix[d] %= M
-        return self.index.get((lev, tuple(ix)), -1)
+    def elements(self):
+        E = self.nelements()
+        lev = np.zeros(E, dtype=np.int32)
+        ctr = np.zeros((E, self.ndims))
+        self._lib.check(self.lib.tg_tree_elements(
+            self.h, lev.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _dp(ctr)))
+        return lev.astype(np.int64), ctr
 
-    def parent(self, cell):
-        lev = self.level[cell]
-        if lev == 0:
-            return -1
-        return self.index[(lev - 1, tuple(i >> 1 for i in self.ix[cell]))]
+    def containers(self):
+        ni, nm = ctypes.c_int64(), ctypes.c_int64()
+        self._lib.check(self.lib.tg_tree_counts(self.h, ctypes.byref(ni), ctypes.byref(nm)))
+        ns = 1 << (self.ndims - 1)
+        nb = np.zeros((ni.value, 2), dtype=np.int64)
+        orient = np.zeros(ni.value, dtype=np.int64)
+        mids = np.zeros((nm.value, ns + 1), dtype=np.int64)
+        ls = np.zeros(nm.value, dtype=np.int64)
+        mor = np.zeros(nm.value, dtype=np.int64)
+        self._lib.check(self.lib.tg_tree_interfaces(self.h, _ip(nb), _ip(orient)))
+        self._lib.check(self.lib.tg_tree_mortars(self.h, _ip(mids), _ip(ls), _ip(mor)))
+        return (nb, orient), (mids, ls, mor)
 
-    def _refine_cell(self, cell):
-        # init_child! / child_coordinates (abstract_tree.jl:668-674)
-        lev, ix, c = self.level[cell], self.ix[cell], self.center[cell]
-        child_len = self.length(lev) / 2
-        self.child0[cell] = len(self.level)
-        for ch in range(1 << self.D):
-            bits = [(ch >> d) & 1 for d in range(self.D)]
-            self._add(lev + 1, tuple(2 * i + b for i, b in zip(ix, bits)),
-                      tuple(cc + (1.0 if b else -1.0) * child_len / 2 for cc, b in zip(c, bits)))
+    def adapt(self, controller_value, only_refine, only_coarsen):
+        lam = np.ascontiguousarray(controller_value, dtype=np.int8)
+        changed = ctypes.c_int32()
+        self._lib.check(self.lib.tg_tree_adapt(self.h, lam.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)),
+                                               int(only_refine), int(only_coarsen),
+                                               ctypes.byref(changed)))
+        if not changed.value:
+            return False, None, None
+        E = self.nelements()
+        src = np.zeros(E, dtype=np.int64)
+        kind = np.zeros(E, dtype=np.int8)
+        self._lib.check(self.lib.tg_tree_transfer_map(
+            self.h, _ip(src), kind.ctypes.data_as(ctypes.POINTER(ctypes.c_int8))))
+        return True, src, kind
 
-    def refine(self, cells):
-        """refine!(t, cell_ids): refine the given leaves, then rebalance! until no
-        two face neighbours differ by more than one level (abstract_tree.jl:367-402,
-        453-489)."""
-        refined = sorted(set(cells))
-        for c in refined:
-            self._refine_cell(c)
-        while refined:
-            marks = set()
-            for cell in refined:
-                for direction in range(2 * self.D):
-                    if self.neighbour(cell, direction) >= 0:
-                        continue
-                    p = self.parent(cell)
-                    if p < 0:
-                        continue
-                    pn = self.neighbour(p, direction)
-                    if pn >= 0:
-                        marks.add(pn)
-            refined = sorted(marks)
-            for c in refined:
-                self._refine_cell(c)
 
-    def coarsen(self, parents):
-        """coarsen!(t, cell_ids), abstract_tree.jl:516-618: parents whose children
-        are all leaves, highest level first; a parent is kept when one of its
-        children has a same-level neighbour with children across a face that is
-        not shared with a sibling (the 2:1 rule).  Returns {parent: first child}
-        of the coarsened parents."""
-        order = sorted(parents, key=lambda c: self.level[c])  # stable, as Julia's sort
-        done = {}
-        nch = 1 << self.D
-        while order:
-            cell = order.pop()
-            first = self.child0[cell]
-            skip = False
-            for ch in range(nch):
-                c = first + ch
-                for direction in range(2 * self.D):
-                    if (ch >> (direction // 2)) & 1 != direction & 1:
-                        continue  # the neighbour across this face is a sibling
-                    nb = self.neighbour(c, direction)
-                    if nb >= 0 and not self.is_leaf(nb):
-                        skip = True
-                        break
-                if skip:
-                    break
-            if skip:
-                continue
-            for ch in range(nch):
-                del self.index[(self.level[first + ch], self.ix[first + ch])]
-            self.child0[cell] = -1
-            done[cell] = first
-        return done
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
-    def leaves(self):
-        """Leaf cells depth-first with children in _child_signs order."""
-        out, stack = [], [0]
-        nch = 1 << self.D
-        while stack:
-            cell = stack.pop()
-            if self.child0[cell] < 0:
-                out.append(cell)
-            else:
-                stack.extend(range(self.child0[cell] + nch - 1, self.child0[cell] - 1, -1))
-        return out
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
 
 
 def _patch(p, ndims):
@@ -209,29 +172,22 @@ class TreeMesh:
         """initialize!(mesh, initial_refinement_level, refinement_patches),
         tree_mesh.jl:186-215: uniform refinement, then each patch refines the
         leaves whose centre lies strictly inside it (refine_box!, refine_sphere!,
-        abstract_tree.jl:405-447)."""
-        t = _Tree(self.ndims, self.periodicity, self.length_level_0, self.center_level_0)
-        for _ in range(self.initial_refinement_level):
-            t.refine(t.leaves())
+        abstract_tree.jl:405-447); the tree is the library's (tg_tree_*)."""
+        t = _NativeTree(self.ndims, self.initial_refinement_level, self.coordinates_min,
+                        self.coordinates_max, self.periodicity)
         for kind, a, b in self.refinement_patches:
-            sel = []
-            for cell in t.leaves():
-                c = t.center[cell]
-                if kind == "box":
-                    inside = all(lo < x < hi for x, lo, hi in zip(c, a, b))
-                else:
-                    inside = sum((x - y) ** 2 for x, y in zip(c, a)) < b * b
-                if inside:
-                    sel.append(cell)
-            if sel:
-                t.refine(sel)
+            t.refine_patch(kind, a, b)
         self._tree = t
-        self._leaves = t.leaves()
+        self._refresh()
+
+    def _refresh(self):
+        self._levels, self._centers = self._tree.elements()
+        self._interfaces, self._mortars = self._tree.containers()
 
     @property
     def nelements(self) -> int:
         if self._tree is not None:
-            return len(self._leaves)
+            return len(self._levels)
         return self.cartesian.shape[0]
 
     def _ensure_tree(self):
@@ -240,7 +196,7 @@ class TreeMesh:
             del self.cartesian
 
     def adapt(self, controller_value, only_refine=False, only_coarsen=False):
-        """One AMR pass on the tree (amr.jl:244-392): refine! the leaves with
+        """One AMR pass on the tree (amr.jl:244-392): refine! the elements with
         controller_value > 0 (with rebalancing), then coarsen! the parents whose
         children all have controller_value < 0.  Returns (changed,
         source_element, kind) for the elements of the adapted mesh: kind 0 copies
@@ -248,59 +204,25 @@ class TreeMesh:
         source_element, -1 the parent of the coarsened elements source_element ..
         source_element + 2^ndims - 1 (the layout tg_adapt_state takes)."""
         self._ensure_tree()
-        t = self._tree
         lam = np.asarray(controller_value)
-        if lam.shape != (len(self._leaves),):
+        if lam.shape != (self.nelements,):
             raise ValueError("one controller value per element")
-        old_leaves = self._leaves
-        old_elem = {c: e for e, c in enumerate(old_leaves)}
-        to_refine = [old_leaves[e] for e in np.flatnonzero(lam > 0)]
-        to_coarsen = [old_leaves[e] for e in np.flatnonzero(lam < 0)]
-        changed = False
-        former = {}
-        if not only_coarsen and to_refine:
-            t.refine(to_refine)
-            changed = True
-        if not only_refine and to_coarsen:
-            count = {}
-            parents = []
-            nch = 1 << self.ndims
-            for cell in to_coarsen:
-                if t.level[cell] == 0 or not t.is_leaf(cell):
-                    continue
-                p = t.parent(cell)
-                count[p] = count.get(p, 0) + 1
-                if count[p] == nch:
-                    parents.append(p)
-            former = t.coarsen(sorted(parents))
-            changed = changed or bool(former)
-        if not changed:
-            return False, None, None
-        self._leaves = t.leaves()
-        E = len(self._leaves)
-        src = np.zeros(E, dtype=np.int64)
-        kind = np.zeros(E, dtype=np.int8)
-        for e, cell in enumerate(self._leaves):
-            if cell in old_elem:
-                src[e] = old_elem[cell]
-            elif cell in former:
-                src[e], kind[e] = old_elem[former[cell]], -1
-            else:
-                p = t.parent(cell)
-                src[e], kind[e] = old_elem[p], 1 + (cell - t.child0[p])
-        return True, src, kind
+        changed, src, kind = self._tree.adapt(lam, only_refine, only_coarsen)
+        if changed:
+            self._refresh()
+        return changed, src, kind
 
     @property
     def is_uniform(self) -> bool:
         if self._tree is None:
             return True
-        return len({self._tree.level[c] for c in self._leaves}) == 1
+        return bool(np.all(self._levels == self._levels[0]))
 
     def cell_centers(self):
         """Cell midpoints, computed like child_coordinates (abstract_tree.jl:668-674):
         each level adds sign * (parent_length / 2) / 2 to the parent centre."""
         if self._tree is not None:
-            return np.array([self._tree.center[c] for c in self._leaves], dtype=np.float64)
+            return self._centers.copy()
         L = self.initial_refinement_level
         centers = np.tile(np.array(self.center_level_0), (self.nelements, 1))
         length = self.length_level_0
@@ -321,12 +243,12 @@ class TreeMesh:
     def element_lengths(self):
         """length_at_cell of every element (length_level_0 / 2^level)."""
         if self._tree is not None:
-            return np.array([self._tree.length(self._tree.level[c]) for c in self._leaves])
+            return self.length_level_0 / np.power(2.0, self._levels)
         return np.full(self.nelements, self.length_level_0 / (1 << self.initial_refinement_level))
 
     def element_levels(self):
         if self._tree is not None:
-            return np.array([self._tree.level[c] for c in self._leaves], dtype=np.int64)
+            return self._levels.copy()
         return np.full(self.nelements, self.initial_refinement_level, dtype=np.int64)
 
     def interfaces(self):
@@ -363,46 +285,20 @@ class TreeMesh:
         return nb.reshape(E * D, 2)[keep], orient.reshape(E * D)[keep]
 
     def _tree_interfaces(self):
-        t, D = self._tree, self.ndims
-        c2e = {c: e for e, c in enumerate(self._leaves)}
-        nb, orient = [], []
-        for e, cell in enumerate(self._leaves):
-            for d in range(D):
-                n = t.neighbour(cell, 2 * d + 1)
-                if n >= 0 and t.is_leaf(n):
-                    nb.append((e + 1, c2e[n] + 1))
-                    orient.append(d + 1)
-        return (np.array(nb, dtype=np.int64).reshape(-1, 2),
-                np.array(orient, dtype=np.int64))
+        nb, orient = self._interfaces
+        return nb.copy(), orient.copy()
 
     def mortars(self):
         """cache.mortars of L2 mortars (init_mortars!, containers_2d.jl:707-810,
         containers_3d.jl:652-790): neighbor_ids [M, 2^(ndims-1) + 1] (1-based; the
         small elements facing the large one in child order, then the large one),
         large_sides [M] (1: large element on the negative side), orientations [M]."""
-        D = self.ndims
-        ns = 1 << (D - 1)
+        ns = 1 << (self.ndims - 1)
         if self._tree is None:
             return (np.zeros((0, ns + 1), dtype=np.int64), np.zeros(0, dtype=np.int64),
                     np.zeros(0, dtype=np.int64))
-        t = self._tree
-        c2e = {c: e for e, c in enumerate(self._leaves)}
-        ids, ls, orient = [], [], []
-        for e, cell in enumerate(self._leaves):
-            for direction in range(2 * D):
-                n = t.neighbour(cell, direction)
-                if n < 0 or t.is_leaf(n):
-                    continue
-                d = direction // 2
-                want = 0 if direction & 1 else 1
-                small = [t.child0[n] + ch for ch in range(1 << D) if (ch >> d) & 1 == want]
-                if not all(t.is_leaf(c) for c in small):
-                    raise RuntimeError("refinement tree is not 2:1 balanced")
-                ids.append([c2e[c] + 1 for c in small] + [e + 1])
-                ls.append(1 if direction & 1 else 2)
-                orient.append(d + 1)
-        return (np.array(ids, dtype=np.int64).reshape(-1, ns + 1),
-                np.array(ls, dtype=np.int64), np.array(orient, dtype=np.int64))
+        ids, ls, orient = self._mortars
+        return ids.copy(), ls.copy(), orient.copy()
 
     def __repr__(self):
         per = "periodic" if all(self.periodicity) else f"periodicity {self.periodicity}"
