@@ -5,10 +5,10 @@
 
 namespace tg {
 
-template <int D, int N, int VI, int VF, int SF, int EPB>
+template <int D, int N, int VI, int VF, int SF, int EPB, bool DIRECT = false>
 static int launch_mixed_one(const MixedParams& P, const MixedArgs& A, cudaStream_t s) {
   using K = MixedKernel<D, N, VI, EPB>;
-  auto kern = mixed_element_kernel<D, N, VI, VF, SF, EPB>;
+  auto kern = mixed_element_kernel<D, N, VI, VF, SF, EPB, DIRECT>;
   static bool configured = false;
   const size_t smem = K::smem_bytes();
   if (!configured) {
@@ -24,16 +24,27 @@ static int launch_mixed_one(const MixedParams& P, const MixedArgs& A, cudaStream
 }
 
 // Flux-specialised instances for polydeg 3 (flux_ranocha volume flux with the
-// two Lax-Friedrichs surface fluxes, no slip wall or mortar); every other
-// choice dispatches at run time.
-template <int D, int VI, int EPB>
+// two Lax-Friedrichs surface fluxes); every other choice dispatches at run
+// time.  Meshes with faces of a given flux (slip walls, mortars) take the
+// DIRECT instances, built for the default elements per block (DEF) only; other
+// block sizes run those meshes through the run-time flux kernel.
+template <int D, int VI, int EPB, bool DEF>
 static int launch_mixed_n4(const MixedParams& P, const MixedArgs& A, cudaStream_t s) {
-  const bool ranocha = (VI == VI_WEAK || P.volume_flux == FLUX_RANOCHA) && !P.has_direct;
-  if (ranocha && P.surface_flux == FLUX_LLF)
-    return launch_mixed_one<D, 4, VI, VI == VI_WEAK ? -1 : FLUX_RANOCHA, FLUX_LLF, EPB>(P, A, s);
-  if (ranocha && P.surface_flux == FLUX_LLF_NAIVE)
-    return launch_mixed_one<D, 4, VI, VI == VI_WEAK ? -1 : FLUX_RANOCHA, FLUX_LLF_NAIVE, EPB>(P, A,
-                                                                                              s);
+  constexpr int VF = VI == VI_WEAK ? -1 : FLUX_RANOCHA;
+  const bool ranocha = VI == VI_WEAK || P.volume_flux == FLUX_RANOCHA;
+  if (ranocha && !P.has_direct) {
+    if (P.surface_flux == FLUX_LLF) return launch_mixed_one<D, 4, VI, VF, FLUX_LLF, EPB>(P, A, s);
+    if (P.surface_flux == FLUX_LLF_NAIVE)
+      return launch_mixed_one<D, 4, VI, VF, FLUX_LLF_NAIVE, EPB>(P, A, s);
+  }
+  if constexpr (DEF) {
+    if (ranocha && P.has_direct) {
+      if (P.surface_flux == FLUX_LLF)
+        return launch_mixed_one<D, 4, VI, VF, FLUX_LLF, EPB, true>(P, A, s);
+      if (P.surface_flux == FLUX_LLF_NAIVE)
+        return launch_mixed_one<D, 4, VI, VF, FLUX_LLF_NAIVE, EPB, true>(P, A, s);
+    }
+  }
   return launch_mixed_one<D, 4, VI, -1, -1, EPB>(P, A, s);
 }
 
@@ -48,9 +59,9 @@ int TG_CAT(launch_mixed_, TG_SUFFIX)(int N, int epb, const MixedParams& P, const
     case 2: return launch_mixed_one<2, 2, TG_VI, -1, -1, 32>(P, A, s);
     case 3: return launch_mixed_one<2, 3, TG_VI, -1, -1, 32>(P, A, s);
     case 4:
-      if (epb == 8) return launch_mixed_n4<2, TG_VI, 8>(P, A, s);
-      if (epb == 32) return launch_mixed_n4<2, TG_VI, 32>(P, A, s);
-      return launch_mixed_n4<2, TG_VI, 16>(P, A, s);
+      if (epb == 8) return launch_mixed_n4<2, TG_VI, 8, false>(P, A, s);
+      if (epb == 32) return launch_mixed_n4<2, TG_VI, 32, false>(P, A, s);
+      return launch_mixed_n4<2, TG_VI, 16, true>(P, A, s);
     case 5: return launch_mixed_one<2, 5, TG_VI, -1, -1, 16>(P, A, s);
     case 6: return launch_mixed_one<2, 6, TG_VI, -1, -1, 16>(P, A, s);
   }
@@ -59,9 +70,9 @@ int TG_CAT(launch_mixed_, TG_SUFFIX)(int N, int epb, const MixedParams& P, const
     case 2: return launch_mixed_one<3, 2, TG_VI, -1, -1, 16>(P, A, s);
     case 3: return launch_mixed_one<3, 3, TG_VI, -1, -1, 8>(P, A, s);
     case 4:
-      if (epb == 2) return launch_mixed_n4<3, TG_VI, 2>(P, A, s);
-      if (epb == 8) return launch_mixed_n4<3, TG_VI, 8>(P, A, s);
-      return launch_mixed_n4<3, TG_VI, 4>(P, A, s);
+      if (epb == 2) return launch_mixed_n4<3, TG_VI, 2, false>(P, A, s);
+      if (epb == 8) return launch_mixed_n4<3, TG_VI, 8, false>(P, A, s);
+      return launch_mixed_n4<3, TG_VI, 4, true>(P, A, s);
     case 5: return launch_mixed_one<3, 5, TG_VI, -1, -1, 2>(P, A, s);
   }
 #endif

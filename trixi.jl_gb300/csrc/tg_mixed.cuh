@@ -491,7 +491,7 @@ struct SourceMMS {
   }
 };
 
-template <int D, int N, int VI, int VF, int SF, int EPB>
+template <int D, int N, int VI, int VF, int SF, int EPB, bool DIRECT = false>
 __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<D>& R,
                                            const float2* s_u, const float2* s_fu,
                                            const float* s_nd, float* s_part, const float* s_mat,
@@ -617,10 +617,12 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
                             : s_fu + ((slot * 2 * D + dir) * NF + line) * NV;
     float F[NV];
     // faces with a given flux (slip walls, mortars) are compiled into the
-    // run-time flux kernels only: contexts with such faces use those (the
-    // flux-specialised instances keep registers for the conforming hot path)
+    // run-time flux kernels and the DIRECT instances only: contexts with such
+    // faces use those (the other flux-specialised instances keep registers
+    // for the conforming hot path)
     bool wall = false;
-    if constexpr (SF < 0) wall = nb < 0 && (-1 - nb >= P.nbc || P.bc[dir] == BC_SLIP_WALL);
+    if constexpr (SF < 0 || DIRECT)
+      wall = nb < 0 && (-1 - nb >= P.nbc || P.bc[dir] == BC_SLIP_WALL);
     if (wall) {
       Dv::wall_flux(R, src, dd, vro, eos, F);
     } else {
@@ -667,7 +669,7 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
 // on work items of many meshes (tg_ensemble.cu).  Every thread of the block
 // calls it with the same arguments, blockDim.x == NT, and smem_raw holds
 // MixedKernel::smem_bytes() bytes.
-template <int D, int N, int VI, int VF, int SF, int EPB>
+template <int D, int N, int VI, int VF, int SF, int EPB, bool DIRECT = false>
 __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const MixedArgs& A,
                                                     int64_t blk, unsigned char* smem_raw) {
   using K = MixedKernel<D, N, VI, EPB>;
@@ -813,7 +815,7 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
     const int sl = r / NF;
     const int line = r - sl * NF;
     if (sl < nel)
-      mixed_line<D, N, VI, VF, SF, EPB>(P, s_ref[sl], s_u, s_fu, s_nd, s_part, s_mat, s_iw,
+      mixed_line<D, N, VI, VF, SF, EPB, DIRECT>(P, s_ref[sl], s_u, s_fu, s_nd, s_part, s_mat, s_iw,
                                         VI == VI_HG ? s_elem[sl * 8] : 0.0f, sl, line, dd,
                                         e0 + sl, e0, nel);
   }
@@ -908,11 +910,11 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
   }
 }
 
-template <int D, int N, int VI, int VF, int SF, int EPB>
+template <int D, int N, int VI, int VF, int SF, int EPB, bool DIRECT = false>
 __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D, N, VI, EPB>::MINB)
     mixed_element_kernel(const MixedParams P, const MixedArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  mixed_element_block<D, N, VI, VF, SF, EPB>(P, A, blockIdx.x, smem_raw);
+  mixed_element_block<D, N, VI, VF, SF, EPB, DIRECT>(P, A, blockIdx.x, smem_raw);
 }
 
 }  // namespace tg

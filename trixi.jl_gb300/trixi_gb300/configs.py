@@ -480,8 +480,25 @@ def c7(steps=40):
     return out
 
 
+def mortar_steps(steps=4):
+    """c7's refined mesh (3D MMS 32^3 with the central box refined once, 61,440
+    elements, 1,536 mortars), mixed precision, `steps` steps."""
+    eq = T.CompressibleEulerEquations3D(1.4)
+    solver = T.DGSEM(polydeg=3, surface_flux=T.flux_lax_friedrichs,
+                     volume_integral=T.VolumeIntegralFluxDifferencing(T.flux_ranocha))
+    mesh = T.TreeMesh((0.0,) * 3, (2.0,) * 3, initial_refinement_level=5,
+                      refinement_patches=(dict(type="box", coordinates_min=(0.5,) * 3,
+                                               coordinates_max=(1.5,) * 3),))
+    semi = T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_convergence_test, solver,
+                                          source_terms=T.source_terms_convergence_test,
+                                          precision="mixed")
+    _, t, n, secs = solve_timed(semi, 10.0, 0.6, max_steps=steps)
+    return dict(steps=n, t=t)
+
+
 RUNS = dict(c1=c1, c3=c3, c4=c4, c5a=c5a, c5b=c5b, c6=c6, c7=c7)
-SHORT_RUNS = dict(learned_steps=learned_steps, ensemble_steps=ensemble_steps)
+SHORT_RUNS = dict(learned_steps=learned_steps, ensemble_steps=ensemble_steps,
+                  mortar_steps=mortar_steps)
 
 
 def main(argv=None):
