@@ -520,6 +520,140 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// Mortar pre-pass of a mixed context: the same fluxes as mortar_flux_kernel
+// with the two linear projections in FP32 on deviations.  The large trace is
+// split into a float-float reference (its first face node) and FP32
+// deviations; forward_{lower,upper} act on the deviations only, which is exact
+// to FP32 rounding of the deviations because every row sums to one.  The
+// surface flux is taken in FP64 on reference + projected deviation, and the
+// small faces' fluxes go back through reverse_{lower,upper} as deviations
+// from the flux at the first small node (the reverse rows of all small faces
+// together sum to one).  mat32: the four matrices in FP32, row-major.
+template <int D>
+__global__ void __launch_bounds__(128)
+    mortar_flux_ff_kernel(const DgParams P, const float2* __restrict__ u,
+                          const int32_t* __restrict__ mtab, const float* __restrict__ mat32,
+                          int64_t M, int N, int64_t ff_offset, float2* __restrict__ outff) {
+  constexpr int NV = D + 2, NS = 1 << (D - 1);
+  constexpr int MAXF = D == 2 ? MAXN : MAXN * MAXN;
+  __shared__ float s_mat[4 * MAXN * MAXN];
+  __shared__ float s_dl[MAXF * NV];        // large trace - reference
+  __shared__ float s_df[NS * MAXF * NV];   // small-face fluxes - first flux
+  __shared__ double s_ref[NV], s_fref[NV];
+  const int64_t m = blockIdx.x;
+  if (m >= M) return;
+  const int tid = threadIdx.x;
+  const int NF = D == 2 ? N : N * N, NN = NF * N, NM = N * N;
+  for (int k = tid; k < 4 * NM; k += blockDim.x) s_mat[k] = mat32[k];
+  const int32_t* t = mtab + m * (NS + 3);
+  const int ls = t[NS + 1], o = t[NS + 2];
+  const int dir_large = ls == 0 ? 2 * o + 1 : 2 * o;
+  const int dir_small = dir_large ^ 1;
+  const int Sd = o == 0 ? 1 : (o == 1 ? N : N * N);
+  auto face_node = [&](int fn, int dir) {
+    return (fn % Sd) + (fn / Sd) * Sd * N + ((dir & 1) ? (N - 1) * Sd : 0);
+  };
+  const float2* ul = u + (size_t)t[NS] * NN * NV;
+  const float2* ur0 = ul + (size_t)face_node(0, dir_large) * NV;  // reference node
+  if (tid < NV) s_ref[tid] = (double)ur0[tid].x + (double)ur0[tid].y;
+  for (int fn = tid; fn < NF; fn += blockDim.x) {
+    const float2* p = ul + (size_t)face_node(fn, dir_large) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) s_dl[fn * NV + v] = (p[v].x - ur0[v].x) + (p[v].y - ur0[v].y);
+  }
+  __syncthreads();
+  const double gamma = P.gamma, igm1 = P.inv_gamma_minus_one;
+  using Eu = Euler<D, double>;
+  double F[NV];
+  for (int it = tid; it < NS * NF; it += blockDim.x) {
+    const int q = it / NF, fn = it - q * NF;
+    const int i = fn % N, j = fn / N;
+    const float* F1 = s_mat + (q & 1) * NM;
+    const float* F2 = s_mat + ((q >> 1) & 1) * NM;
+    float dp[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) dp[v] = 0.f;
+    if (D == 2) {
+      for (int a = 0; a < N; ++a) {
+        const float c = F1[i * N + a];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) dp[v] = fmaf(c, s_dl[a * NV + v], dp[v]);
+      }
+    } else {
+      for (int b = 0; b < N; ++b)
+        for (int a = 0; a < N; ++a) {
+          const float c = F1[i * N + a] * F2[j * N + b];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) dp[v] = fmaf(c, s_dl[(a + b * N) * NV + v], dp[v]);
+        }
+    }
+    double up[NV], us[NV], wp[NV], ws[NV];
+    const float2* ps = u + ((size_t)t[q] * NN + face_node(fn, dir_small)) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      up[v] = s_ref[v] + (double)dp[v];
+      us[v] = (double)ps[v].x + (double)ps[v].y;
+    }
+    Eu::cons2prim(up, wp, gamma);
+    Eu::cons2prim(us, ws, gamma);
+    if (ls == 0)
+      Eu::two_point(P.surface_flux, up, wp, us, ws, o, gamma, igm1, F);
+    else
+      Eu::two_point(P.surface_flux, us, ws, up, wp, o, gamma, igm1, F);
+    const size_t slot = (size_t)(ff_offset + m * (NS + 1) + q);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const float hi = (float)F[v];
+      outff[(slot * NF + fn) * NV + v] = make_float2(hi, (float)(F[v] - (double)hi));
+    }
+    if (it == 0) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) s_fref[v] = F[v];
+    }
+  }
+  __syncthreads();
+  for (int it = tid; it < NS * NF; it += blockDim.x) {
+    const size_t slot = (size_t)(ff_offset + m * (NS + 1) + it / NF);
+    const float2* f = outff + (slot * NF + (it % NF)) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      s_df[it * NV + v] = (float)(((double)f[v].x - s_fref[v]) + (double)f[v].y);
+  }
+  __syncthreads();
+  for (int fn = tid; fn < NF; fn += blockDim.x) {
+    const int i = fn % N, j = fn / N;
+    float r[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) r[v] = 0.f;
+    for (int q = 0; q < NS; ++q) {
+      const float* R1 = s_mat + (2 + (q & 1)) * NM;
+      const float* R2 = s_mat + (2 + ((q >> 1) & 1)) * NM;
+      const float* f = s_df + (size_t)q * NF * NV;
+      if (D == 2) {
+        for (int a = 0; a < N; ++a) {
+          const float c = R1[i * N + a];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) r[v] = fmaf(c, f[a * NV + v], r[v]);
+        }
+      } else {
+        for (int b = 0; b < N; ++b)
+          for (int a = 0; a < N; ++a) {
+            const float c = R1[i * N + a] * R2[j * N + b];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) r[v] = fmaf(c, f[(a + b * N) * NV + v], r[v]);
+          }
+      }
+    }
+    const size_t slot = (size_t)(ff_offset + m * (NS + 1) + NS);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const double x = s_fref[v] + (double)r[v];
+      const float hi = (float)x;
+      outff[(slot * NF + fn) * NV + v] = make_float2(hi, (float)(x - (double)hi));
+    }
+  }
+}
+
 // Solution transfer of AMR (refine_element! / coarsen_elements!,
 // amr_dg2d.jl:224-294, 429-485; amr_dg3d.jl): one thread per node of the
 // adapted mesh.  mats: forward lower, upper, reverse lower, upper
@@ -636,6 +770,7 @@ struct tg_ctx {
   int32_t* d_mtab = nullptr;          // [nmortar][2^(D-1) + 3]: elements, large side, orientation
   int32_t* d_mnbr = nullptr;          // [nmface][4]: elements across each mortar face
   double* d_mmat = nullptr;           // forward lower/upper, reverse lower/upper (row-major)
+  float* d_mmat32 = nullptr;          // the same in FP32 (mixed pre-pass)
   double* d_mflux = nullptr;          // fp64: [nmface][NF][NV] mortar pre-pass output
   int8_t* d_scls = nullptr;           // mixed: size class of each element (source tables)
   double* d_amr_raw = nullptr;        // AMR indicator (unsmoothed, smoothed)
@@ -693,7 +828,7 @@ static void free_ctx(tg_ctx* c) {
     if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
   void* ptrs[] = {c->d_u[0], c->d_u[1], c->d_utmp, c->d_du, c->d_uscratch, c->d_stage64,
                   c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_nbr, c->d_invj, c->d_xline,
-                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mflux, c->d_scls, c->d_amr_raw, c->d_amr_alpha, c->d_amap, c->d_akind, c->d_weights, c->d_partial, c->d_sums, c->d_clock,
+                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mmat32, c->d_mflux, c->d_scls, c->d_amr_raw, c->d_amr_alpha, c->d_amap, c->d_akind, c->d_weights, c->d_partial, c->d_sums, c->d_clock,
                   c->d_status, c->d_speed};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -770,13 +905,13 @@ static void launch_mortars(tg_ctx* c, const void* u_in) {
           c->P, (const double*)u_in, c->d_mtab, c->d_mmat, c->nmortar, c->N, 0, c->d_mflux, nullptr);
   } else {
     if (c->D == 2)
-      mortar_flux_kernel<2, float2><<<nb, 128, 0, c->stream>>>(
-          c->P, (const float2*)u_in, c->d_mtab, c->d_mmat, c->nmortar, c->N, c->nbound, nullptr,
-          c->d_ghost);
+      mortar_flux_ff_kernel<2><<<nb, 128, 0, c->stream>>>(c->P, (const float2*)u_in, c->d_mtab,
+                                                          c->d_mmat32, c->nmortar, c->N, c->nbound,
+                                                          c->d_ghost);
     else
-      mortar_flux_kernel<3, float2><<<nb, 128, 0, c->stream>>>(
-          c->P, (const float2*)u_in, c->d_mtab, c->d_mmat, c->nmortar, c->N, c->nbound, nullptr,
-          c->d_ghost);
+      mortar_flux_ff_kernel<3><<<nb, 128, 0, c->stream>>>(c->P, (const float2*)u_in, c->d_mtab,
+                                                          c->d_mmat32, c->nmortar, c->N, c->nbound,
+                                                          c->d_ghost);
   }
 }
 
@@ -1170,6 +1305,7 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     ALLOC(c->d_mtab, sizeof(int32_t) * mtab.size());
     ALLOC(c->d_mnbr, sizeof(int32_t) * mnbr.size());
     ALLOC(c->d_mmat, sizeof(double) * 4 * N * N);
+    if (!c->fp64) ALLOC(c->d_mmat32, sizeof(float) * 4 * N * N);
     if (c->fp64) ALLOC(c->d_mflux, sizeof(double) * (size_t)c->nmface * (c->NN / N) * c->NV);
     // row-major copies of the column-major n x n mortar matrices
     const double* src[4] = {cfg->mortar_forward_lower, cfg->mortar_forward_upper,
@@ -1278,6 +1414,10 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     cudaMemcpy(c->d_mtab, mtab.data(), sizeof(int32_t) * mtab.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(c->d_mnbr, mnbr.data(), sizeof(int32_t) * mnbr.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(c->d_mmat, mmat.data(), sizeof(double) * mmat.size(), cudaMemcpyHostToDevice);
+    if (!c->fp64) {
+      std::vector<float> m32(mmat.begin(), mmat.end());
+      cudaMemcpy(c->d_mmat32, m32.data(), sizeof(float) * m32.size(), cudaMemcpyHostToDevice);
+    }
   }
   cudaMemcpy(c->d_invj, cfg->inverse_jacobian, sizeof(double) * c->E, cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_weights, c->weights.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
