@@ -119,6 +119,16 @@ CASES = {
         amr=dict(interval=5, adapt_initial_condition=True,
                  adapt_initial_condition_only_refine=True, alpha_max=0.5, alpha_min=0.001,
                  alpha_smooth=True, base_level=4, max_level=6, max_threshold=0.01)),
+    "TreeMesh3D Euler: elixir_euler_shockcapturing_amr.jl": dict(
+        file="test/test_tree_3d_euler.jl",
+        elixir="examples/tree_3d_dgsem/elixir_euler_shockcapturing_amr.jl",
+        ndims=3, polydeg=3, level=3, xmin=[-2.0] * 3, xmax=[2.0] * 3,
+        ic="weak_blast_wave", source="none", vi="hg", volume_flux="ranocha",
+        surface_flux="ranocha", alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
+        cfl=1.3, tspan=[0.0, 0.4],
+        amr=dict(interval=1, adapt_initial_condition=True,
+                 adapt_initial_condition_only_refine=True, alpha_max=0.5, alpha_min=0.001,
+                 alpha_smooth=False, base_level=2, max_level=4, max_threshold=0.0003)),
     "TreeMesh3D Euler: elixir_euler_mortar.jl": dict(
         file="test/test_tree_3d_euler.jl",
         elixir="examples/tree_3d_dgsem/elixir_euler_mortar.jl",

@@ -16,7 +16,7 @@ import trixi_gb300 as T
 pytestmark = pytest.mark.gpu
 
 GOLDENS = load_goldens()
-AMR_GOLDEN = "TreeMesh2D Euler: elixir_euler_blast_wave_amr.jl"
+AMR_GOLDENS = sorted(k for k in GOLDENS if GOLDENS[k].get("amr"))
 
 
 def _case(ndims, level, patches=()):
@@ -72,33 +72,40 @@ def test_adapt_state_matches_oracle(ndims, level, precision):
     assert err < (1e-12 if precision == "fp64" else 2e-4)
 
 
-def _amr_run(precision):
-    c = dict(GOLDENS[AMR_GOLDEN])
+def _amr_run(name, precision):
+    c = dict(GOLDENS[name])
     semi, _ = build(c, precision=precision)
     cb_amr = amr_callback(semi, c)
     ana = T.AnalysisCallback(semi)
-    sol = T.solve(T.semidiscretize(semi, (0.0, 1.0)), T.CarpenterKennedy2N54(), dt=1.0,
+    sol = T.solve(T.semidiscretize(semi, tuple(c["tspan"])), T.CarpenterKennedy2N54(), dt=1.0,
+                  maxiters=c.get("maxiters", 10 ** 12),
                   callback=T.CallbackSet(ana, cb_amr, T.StepsizeCallback(cfl=c["cfl"])))
     return semi, sol, ana, cb_amr
 
 
-def test_gpu_fp64_reproduces_blast_wave_amr_golden():
-    c = GOLDENS[AMR_GOLDEN]
-    semi, sol, ana, cb = _amr_run("fp64")
-    assert sol.t[-1] == pytest.approx(1.0, rel=1e-14)
+@pytest.mark.parametrize("name", AMR_GOLDENS)
+def test_gpu_fp64_reproduces_amr_goldens(name):
+    c = GOLDENS[name]
+    semi, sol, ana, cb = _amr_run(name, "fp64")
     np.testing.assert_allclose(ana.l2, c["l2"], rtol=1e-8)
     np.testing.assert_allclose(ana.linf, c["linf"], rtol=1e-7)
     # the same adaptive history as the oracle: steps, passes and final mesh
     from _cases import oracle_from_case
     orc = oracle_from_case(O, c)
-    _, t, n = orc.solve_amr(ic_id(O, c["ic"]), None, 0.0, 1.0, c["cfl"])
-    # one pass on the initial condition, then one after every 5 steps but the last
-    assert sol.nsteps == n and cb.passes == 1 + (n - 1) // 5
+    _, t, n = orc.solve_amr(ic_id(O, c["ic"]), c.get("ic_params"), c["tspan"][0],
+                            c["tspan"][1], c["cfl"], max_steps=c.get("maxiters", 10 ** 9))
+    assert sol.nsteps == n and sol.t[-1] == pytest.approx(t, rel=1e-14)
+    k = c["amr"]["interval"]
+    # one pass on the initial condition, then one after every `interval` steps
+    # unless the final time was reached
+    finished = t >= c["tspan"][1]
+    assert cb.passes == 1 + (n - 1) // k + (0 if finished or n % k else 1)
     np.testing.assert_array_equal(semi.mesh.element_levels(), orc.element_levels())
 
 
-def test_mixed_blast_wave_amr_within_1p1x_of_fp64():
-    _, _, ana64, _ = _amr_run("fp64")
-    semi, _, ana, _ = _amr_run("mixed")
+@pytest.mark.parametrize("name", AMR_GOLDENS)
+def test_mixed_amr_goldens_within_1p1x_of_fp64(name):
+    _, _, ana64, _ = _amr_run(name, "fp64")
+    semi, _, ana, _ = _amr_run(name, "mixed")
     assert ana.l2[0] <= 1.1 * ana64.l2[0]
     assert semi.nelements > 0

@@ -21,18 +21,22 @@ def test_oracle_reproduces_trixi_golden(oracle_mod, name):
     ic = ic_id(O, c["ic"])
     par = c.get("ic_params")
     if c.get("amr"):
-        u, t, nsteps = orc.solve_amr(ic, par, c["tspan"][0], c["tspan"][1], c["cfl"])
+        u, t, nsteps = orc.solve_amr(ic, par, c["tspan"][0], c["tspan"][1], c["cfl"],
+                                     max_steps=c.get("maxiters", 10**9))
     else:
         u0 = orc.initial_condition(ic, par, c["tspan"][0])
         u, t, nsteps = orc.solve(u0, c["tspan"][0], c["tspan"][1], c["cfl"],
                                  max_steps=c.get("maxiters", 10**9))
     l2, linf = orc.error_norms(u, t, ic, par)
-    if "maxiters" in c:
+    if "maxiters" in c and not c.get("amr"):
         # free-stream preservation: goldens are round-off (~1e-16); compare absolutely
         assert np.all(l2 < 1e-14) and np.all(linf < 1e-13)
         assert np.allclose(l2, c["l2"], atol=5e-15, rtol=0)
         return
-    assert t == pytest.approx(c["tspan"][1], rel=1e-14)
+    if "maxiters" in c:
+        assert nsteps == c["maxiters"]
+    else:
+        assert t == pytest.approx(c["tspan"][1], rel=1e-14)
     np.testing.assert_allclose(l2, c["l2"], rtol=1e-9, atol=0)
     np.testing.assert_allclose(linf, c["linf"], rtol=1e-8, atol=0)
 
