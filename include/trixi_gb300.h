@@ -288,8 +288,8 @@ int tg_tree_transfer_map(const tg_tree* tree, int64_t* source_element, int8_t* k
 /* AMR (AMRCallback on a TreeMesh, src/callbacks_step/amr.jl:244-392).
  *
  * tg_amr_indicator: IndicatorHennemannGassner of the context state with the
- * given parameters (variable density_pressure; indicators.jl:114-148 and
- * apply_smoothing!), always evaluated in FP64 -- the element values
+ * given parameters and indicator variable (tg_indicator_variable;
+ * indicators.jl:114-148 and apply_smoothing!), always evaluated in FP64 -- the element values
  * ControllerThreeLevel compares with its thresholds (amr.jl:1116-1168).
  * Synchronous; alpha_host has nelements entries.
  *
@@ -305,8 +305,12 @@ int tg_tree_transfer_map(const tg_tree* tree, int64_t* source_element, int8_t* k
  * LobattoLegendreAdaptorL2 (= the mortar matrices), n x n column-major.
  * Both contexts must share device, ndims, polydeg and precision.
  * Synchronous; dst then holds an uploaded state. */
+typedef enum tg_indicator_variable {
+  TG_INDICATOR_DENSITY_PRESSURE = 0, /* density_pressure (compressible_euler_2d.jl:2205) */
+  TG_INDICATOR_DENSITY = 1           /* density */
+} tg_indicator_variable;
 int tg_amr_indicator(tg_ctx* ctx, double alpha_max, double alpha_min, int32_t alpha_smooth,
-                     double* alpha_host);
+                     int32_t variable, double* alpha_host);
 int tg_adapt_state(tg_ctx* dst, tg_ctx* src, const int64_t* source_element, const int8_t* kind,
                    const double* forward_upper, const double* forward_lower,
                    const double* reverse_upper, const double* reverse_lower);

@@ -1072,6 +1072,7 @@ struct AmrParams {
   bool alpha_smooth = true;
   int base_level = 1, med_level = 1, max_level = 1;
   double med_threshold = 0.0, max_threshold = 1.0;
+  int variable = 0;  // 0 density_pressure, 1 density
   int interval = 5;
   bool adapt_initial = true, initial_only_refine = true;
 };
@@ -1104,16 +1105,17 @@ static inline size_t uidx(const Solver& s, int64_t e, int node, int v) {
 
 // HG indicator: indicators.jl:114-148 + indicators_2d.jl:30-101, indicators_3d.jl:39-123
 static void hg_alpha(const Solver& s, const double* u, double alpha_max, double alpha_min,
-                     bool alpha_smooth, std::vector<double>& alpha);
+                     bool alpha_smooth, std::vector<double>& alpha, int variable = 0);
 
 static void calc_alpha(Solver& s, const double* u) {
   hg_alpha(s, u, s.alpha_max, s.alpha_min, s.alpha_smooth, s.alpha);
 }
 
 // The HG indicator with the given parameters (IndicatorHennemannGassner, also
-// as the AMR indicator of ControllerThreeLevel).
+// as the AMR indicator of ControllerThreeLevel); variable 0 density_pressure,
+// 1 density.
 static void hg_alpha(const Solver& s, const double* u, double alpha_max, double alpha_min,
-                     bool alpha_smooth, std::vector<double>& alpha) {
+                     bool alpha_smooth, std::vector<double>& alpha, int variable) {
   const int n = s.b.n, D = s.eq.D, nn = s.nn;
   const double threshold = 0.5 * std::pow(10.0, -1.8 * std::pow((double)n, 0.25));
   const double o_0001 = 0.0001;
@@ -1122,7 +1124,8 @@ static void hg_alpha(const Solver& s, const double* u, double alpha_max, double 
 #pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < s.m.nelem; ++e) {
     double ind[512], t1[512], t2[512];
-    for (int node = 0; node < nn; ++node) ind[node] = density_pressure(s.eq, &u[uidx(s, e, node, 0)]);
+    for (int node = 0; node < nn; ++node)
+      ind[node] = variable == 1 ? u[uidx(s, e, node, 0)] : density_pressure(s.eq, &u[uidx(s, e, node, 0)]);
     const double* V = s.b.Vinv.data();
     // multiply_scalar_dimensionwise!, interpolation.jl:207-234, 348-385
     double* in = ind;
@@ -1534,7 +1537,7 @@ static void rk_update(int64_t ndof, double* u, double* u_tmp, const double* du, 
 // ControllerThreeLevel: +1 refine, -1 coarsen, 0 keep
 static std::vector<int> amr_controller(const Solver& s, const double* u, const AmrParams& ap) {
   std::vector<double> alpha;
-  hg_alpha(s, u, ap.alpha_max, ap.alpha_min, ap.alpha_smooth, alpha);
+  hg_alpha(s, u, ap.alpha_max, ap.alpha_min, ap.alpha_smooth, alpha, ap.variable);
   std::vector<int> lambda(s.m.nelem, 0);
   for (int64_t e = 0; e < s.m.nelem; ++e) {
     const int cur = s.m.elevel[e];
@@ -1880,7 +1883,8 @@ int orc_solve(void* h, double* u, double t0, double t_end, double cfl, int64_t m
 // AMR settings of the solver (AMRCallback + ControllerThreeLevel with an HG
 // indicator); ints: interval, adapt_initial_condition,
 // adapt_initial_condition_only_refine, alpha_smooth, base_level, med_level,
-// max_level; doubles: alpha_max, alpha_min, med_threshold, max_threshold.
+// max_level, indicator variable (0 density_pressure, 1 density); doubles:
+// alpha_max, alpha_min, med_threshold, max_threshold.
 void orc_set_amr(void* h, const int* ints, const double* dbls) {
   Solver& s = *(Solver*)h;
   AmrParams& a = s.amr;
@@ -1891,6 +1895,7 @@ void orc_set_amr(void* h, const int* ints, const double* dbls) {
   a.base_level = ints[4];
   a.med_level = ints[5];
   a.max_level = ints[6];
+  a.variable = ints[7];
   a.alpha_max = dbls[0];
   a.alpha_min = dbls[1];
   a.med_threshold = dbls[2];

@@ -76,7 +76,9 @@ def amr_callback(semi, c):
     ind = T.IndicatorHennemannGassner(semi, alpha_max=a.pop("alpha_max", 0.5),
                                       alpha_min=a.pop("alpha_min", 0.001),
                                       alpha_smooth=a.pop("alpha_smooth", True),
-                                      variable=T.density_pressure)
+                                      variable={"density_pressure": T.density_pressure,
+                                                "density": T.density}[
+                                          a.pop("variable", "density_pressure")])
     ctrl = T.ControllerThreeLevel(semi, ind, base_level=a.pop("base_level", 1),
                                   med_level=a.pop("med_level", None),
                                   med_threshold=a.pop("med_threshold", 0.0),

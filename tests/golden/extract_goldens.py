@@ -129,6 +129,17 @@ CASES = {
         amr=dict(interval=1, adapt_initial_condition=True,
                  adapt_initial_condition_only_refine=True, alpha_max=0.5, alpha_min=0.001,
                  alpha_smooth=False, base_level=2, max_level=4, max_threshold=0.0003)),
+    "TreeMesh2D Euler: elixir_euler_kelvin_helmholtz_instability_amr.jl": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_kelvin_helmholtz_instability_amr.jl",
+        ndims=2, polydeg=3, level=5, xmin=[-1.0, -1.0], xmax=[1.0, 1.0],
+        ic="kelvin_helmholtz", source="none", vi="hg", volume_flux="ranocha",
+        surface_flux="llf_naive", alpha_max=0.002, alpha_min=0.0001, alpha_smooth=True,
+        cfl=1.3, tspan=[0.0, 3.0],
+        amr=dict(interval=1, adapt_initial_condition=True,
+                 adapt_initial_condition_only_refine=True, alpha_max=1.0, alpha_min=0.0001,
+                 alpha_smooth=False, variable="density", base_level=4, med_level=0,
+                 med_threshold=0.0003, max_level=6, max_threshold=0.003)),
     "TreeMesh3D Euler: elixir_euler_mortar.jl": dict(
         file="test/test_tree_3d_euler.jl",
         elixir="examples/tree_3d_dgsem/elixir_euler_mortar.jl",

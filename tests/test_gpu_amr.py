@@ -42,6 +42,16 @@ def test_amr_indicator_matches_oracle(ndims, precision, tol):
         a_orc = o2.alpha(u)
         assert np.any(a_orc > 0)
         assert np.max(np.abs(a_gpu - a_orc)) < tol
+    # the indicator on density (the KHI AMR elixir's): against the oracle's controller
+    o3 = O.Oracle(ndims, 3, 4 if ndims == 2 else 2, [-2.0] * ndims, [2.0] * ndims)
+    o3.set_refinement([patch])
+    o3.set_amr(alpha_max=1.0, alpha_min=0.0001, alpha_smooth=False, variable="density",
+               base_level=1, med_level=0, med_threshold=0.0003, max_level=6, max_threshold=0.003)
+    ind = T.IndicatorHennemannGassner(semi, alpha_max=1.0, alpha_min=0.0001, alpha_smooth=False,
+                                      variable=T.density)
+    ctrl = T.ControllerThreeLevel(semi, ind, base_level=1, med_level=0, med_threshold=0.0003,
+                                  max_level=6, max_threshold=0.003)
+    np.testing.assert_array_equal(ctrl(semi), o3.amr_lambda(u))
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])

@@ -1873,8 +1873,10 @@ int tg_entropy_timederivative(tg_ctx* c, double t, double* out) {
 }
 
 int tg_amr_indicator(tg_ctx* c, double alpha_max, double alpha_min, int32_t alpha_smooth,
-                     double* alpha_host) {
+                     int32_t variable, double* alpha_host) {
   if (!c || !alpha_host) return TG_ERR_INVALID_ARGUMENT;
+  if (variable != TG_INDICATOR_DENSITY_PRESSURE && variable != TG_INDICATOR_DENSITY)
+    return fail(c, TG_ERR_INVALID_ARGUMENT, "unknown indicator variable %d", variable);
   if (!c->uploaded) return fail(c, TG_ERR_STATE, "no state uploaded");
   if (!(alpha_max >= 0 && alpha_min >= 0)) return fail(c, TG_ERR_INVALID_ARGUMENT, "alpha bounds");
   CUDA_TRY(c, cudaSetDevice(c->device));
@@ -1886,6 +1888,7 @@ int tg_amr_indicator(tg_ctx* c, double alpha_max, double alpha_min, int32_t alph
   DgParams P = c->P;
   P.alpha_max = alpha_max;
   P.alpha_min = alpha_min;
+  P.hg_variable = variable;
   rc = launch_indicator(c->D, c->N, true, P, u, c->d_amr_raw, c->stream);
   if (rc != 0) return fail(c, TG_ERR_CUDA, "indicator kernel launch failed (%d)", rc);
   smooth_alpha_kernel<double><<<(unsigned)((c->E + 127) / 128), 128, 0, c->stream>>>(

@@ -52,6 +52,7 @@ struct DgParams {
   int32_t volume_flux, surface_flux, fv_flux, source;
   double alpha_max, alpha_min, alpha_atol, hg_threshold, hg_parameter_s;
   int32_t alpha_smooth;
+  int32_t hg_variable;    // indicator variable: 0 density_pressure, 1 density
   // [E][2D] neighbour across face (-x,+x,-y,+y,-z,+z); a face without a
   // conforming neighbour has nbr = -1 - b: b < nbc a boundary face, else
   // mortar face slot b - nbc
@@ -583,7 +584,7 @@ __global__ void __launch_bounds__(EPB * Pow<N, D>::value)
     const TS* p = u + ((size_t)e * NN + node) * NV;
 #pragma unroll
     for (int v = 0; v < NV; ++v) uu[v] = (R)state_value(p[v]);
-    s_a[tid] = Euler<D, R>::density_pressure(uu, (R)P.gamma);
+    s_a[tid] = P.hg_variable == 1 ? uu[0] : Euler<D, R>::density_pressure(uu, (R)P.gamma);
   }
   __syncthreads();
   // multiply_scalar_dimensionwise!: x, then y, then z

@@ -54,6 +54,7 @@ struct MixedParams {
   int32_t volume_flux, surface_flux, fv_flux, source;
   float alpha_max, alpha_min, alpha_atol, hg_threshold, hg_parameter_s;
   int32_t alpha_smooth;
+  int32_t hg_variable;      // indicator variable: 0 density_pressure, 1 density
   const int32_t* nbr;       // [E][2D]
   const float* inv_jac;     // [E]
   const float* xline;       // [E][D][N] or null (unused by the stage kernel)

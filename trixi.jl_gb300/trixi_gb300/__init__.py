@@ -22,7 +22,7 @@ from .analysis import calc_error_norms  # noqa: F401
 from .basis import LobattoLegendreAnalyzer, LobattoLegendreBasis, MortarL2  # noqa: F401
 from .equations import (initial_condition_blast_wave,  # noqa: F401
                         CompressibleEulerEquations2D, CompressibleEulerEquations3D,  # noqa: F401
-                        FluxLaxFriedrichs, cons2prim, density_pressure, flux_central,
+                        FluxLaxFriedrichs, cons2prim, density, density_pressure, flux_central,
                         flux_lax_friedrichs, flux_ranocha, flux_shima_etal,
                         initial_condition_constant, initial_condition_convergence_test,
                         initial_condition_gaussian_blast, initial_condition_isentropic_vortex,

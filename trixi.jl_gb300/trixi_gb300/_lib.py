@@ -124,7 +124,7 @@ def load(path: str | None = None):
         "tg_set_time": ([vp, d], ctypes.c_int),
         "tg_integrals": ([vp, pd], ctypes.c_int),
         "tg_alpha": ([vp, vp, pd], ctypes.c_int),
-        "tg_amr_indicator": ([vp, ctypes.c_double, ctypes.c_double, i32, pd], ctypes.c_int),
+        "tg_amr_indicator": ([vp, ctypes.c_double, ctypes.c_double, i32, i32, pd], ctypes.c_int),
         "tg_tree_create": ([i32, i32, pd, pd, P(i32), P(vp)], ctypes.c_int),
         "tg_tree_destroy": ([vp], ctypes.c_int),
         "tg_tree_refine_patch": ([vp, i32, pd, pd, d], ctypes.c_int),

@@ -14,6 +14,7 @@ import time
 
 import numpy as np
 
+from .equations import density
 from .solvers import IndicatorHennemannGassner
 
 
@@ -36,7 +37,9 @@ class ControllerThreeLevel:
 
     def indicator_values(self, semi):
         ind = self.indicator
-        return semi.device_context.amr_indicator(ind.alpha_max, ind.alpha_min, ind.alpha_smooth)
+        variable = 1 if ind.variable is density else 0
+        return semi.device_context.amr_indicator(ind.alpha_max, ind.alpha_min, ind.alpha_smooth,
+                                                 variable)
 
     def __call__(self, semi):
         alpha = self.indicator_values(semi)

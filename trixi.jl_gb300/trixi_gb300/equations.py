@@ -272,6 +272,11 @@ def initial_condition_gaussian_blast(p_background=1e-5, energy=1.0, width=0.25):
     return ic
 
 
+def density(u, equations):
+    """density, compressible_euler_2d.jl (the first conserved variable)."""
+    return u[..., 0]
+
+
 def density_pressure(u, equations):
     """density_pressure, compressible_euler_2d.jl:2205-2210."""
     D = equations.ndims

@@ -207,12 +207,12 @@ class DeviceContext:
         _lib.check(rc, self.h)
 
     # -- AMR ----------------------------------------------------------------
-    def amr_indicator(self, alpha_max, alpha_min, alpha_smooth):
-        """The smoothed HG indicator of the state with these parameters, in FP64
-        (tg_amr_indicator)."""
+    def amr_indicator(self, alpha_max, alpha_min, alpha_smooth, variable=0):
+        """The HG indicator of the state with these parameters (variable 0:
+        density_pressure, 1: density), in FP64 (tg_amr_indicator)."""
         out = np.zeros(self.semi.nelements)
         self._check(self.lib.tg_amr_indicator(self.h, float(alpha_max), float(alpha_min),
-                                              int(bool(alpha_smooth)), _dptr(out)))
+                                              int(bool(alpha_smooth)), int(variable), _dptr(out)))
         return out
 
     def adapt_from(self, src, source_element, kind):

@@ -4,7 +4,7 @@ from __future__ import annotations
 
 from . import _lib
 from .basis import LobattoLegendreBasis, MortarL2
-from .equations import density_pressure, flux_central, flux_lax_friedrichs
+from .equations import density, density_pressure, flux_central, flux_lax_friedrichs
 
 
 class VolumeIntegralWeakForm:
@@ -32,8 +32,8 @@ class IndicatorHennemannGassner:
 
     def __init__(self, equations, basis=None, alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
                  variable=density_pressure):
-        if variable is not density_pressure:
-            raise NotImplementedError("IndicatorHennemannGassner: only variable=density_pressure")
+        if variable is not density_pressure and variable is not density:
+            raise NotImplementedError("IndicatorHennemannGassner: variable density_pressure or density")
         if basis is None and hasattr(equations, "solver"):
             # IndicatorHennemannGassner(semi; ...), indicators.jl:74-83
             equations, basis = equations.equations, equations.solver.basis
@@ -48,6 +48,8 @@ class VolumeIntegralShockCapturingHG:
     code = _lib.TG_VOLUME_SHOCK_CAPTURING_HG
 
     def __init__(self, indicator, volume_flux_dg=flux_central, volume_flux_fv=flux_lax_friedrichs):
+        if indicator.variable is not density_pressure:
+            raise NotImplementedError("shock capturing: the indicator variable is density_pressure")
         self.indicator = indicator
         self.volume_flux_dg = volume_flux_dg
         self.volume_flux_fv = volume_flux_fv
