@@ -311,6 +311,9 @@ typedef enum tg_indicator_variable {
 } tg_indicator_variable;
 int tg_amr_indicator(tg_ctx* ctx, double alpha_max, double alpha_min, int32_t alpha_smooth,
                      int32_t variable, double* alpha_host);
+/* IndicatorMax(semi; variable) (indicators_3d.jl:239-259): the maximum of
+ * the variable over the nodes of each element, FP64.  Synchronous. */
+int tg_amr_indicator_max(tg_ctx* ctx, int32_t variable, double* out_host);
 int tg_adapt_state(tg_ctx* dst, tg_ctx* src, const int64_t* source_element, const int8_t* kind,
                    const double* forward_upper, const double* forward_lower,
                    const double* reverse_upper, const double* reverse_lower);

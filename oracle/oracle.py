@@ -26,7 +26,7 @@ SRC_NONE, SRC_CONVERGENCE_TEST = 0, 1
 BC_PERIODIC, BC_DIRICHLET, BC_SLIP_WALL = 0, 1, 2
 (IC_CONSTANT, IC_CONVERGENCE_TEST, IC_ISENTROPIC_VORTEX, IC_WEAK_BLAST_WAVE,
  IC_KELVIN_HELMHOLTZ, IC_TAYLOR_GREEN, IC_GAUSSIAN_BLAST,
- IC_ISENTROPIC_VORTEX_ADVECTED, IC_BLAST_WAVE) = range(9)
+ IC_ISENTROPIC_VORTEX_ADVECTED, IC_BLAST_WAVE, IC_DENSITY_PULSE) = range(10)
 
 _lib = None
 
@@ -291,13 +291,15 @@ def _refresh(self):
 def _set_amr(self, interval=5, adapt_initial_condition=True,
              adapt_initial_condition_only_refine=True, alpha_max=0.5, alpha_min=0.001,
              alpha_smooth=True, base_level=1, med_level=None, med_threshold=0.0,
-             max_level=None, max_threshold=1.0, variable="density_pressure"):
+             max_level=None, max_threshold=1.0, variable="density_pressure",
+             indicator="hennemann_gassner"):
     """AMRCallback(semi, ControllerThreeLevel(semi, IndicatorHennemannGassner(...)))."""
     med_level = base_level if med_level is None else med_level
     max_level = base_level if max_level is None else max_level
     ints = np.array([interval, adapt_initial_condition, adapt_initial_condition_only_refine,
                      alpha_smooth, base_level, med_level, max_level,
-                     {"density_pressure": 0, "density": 1}[variable]], dtype=np.int32)
+                     {"density_pressure": 0, "density": 1}[variable],
+                     {"hennemann_gassner": 0, "max": 1}[indicator]], dtype=np.int32)
     dbls = np.array([alpha_max, alpha_min, med_threshold, max_threshold], dtype=np.float64)
     self.lib.orc_set_amr(self.h, _p(ints, ctypes.c_int), _p(dbls))
 

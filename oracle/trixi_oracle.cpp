@@ -53,6 +53,7 @@ enum InitialCondition {
   IC_GAUSSIAN_BLAST = 6,
   IC_ISENTROPIC_VORTEX_ADVECTED = 7,
   IC_BLAST_WAVE = 8,
+  IC_DENSITY_PULSE = 9,
 };
 
 // ---------------------------------------------------------------------------
@@ -663,6 +664,16 @@ static void initial_condition(const Eq& eq, int ic, const double* par, const dou
       prim2cons(eq, prim, u);
       return;
     }
+    case IC_DENSITY_PULSE: {
+      // examples/tree_3d_dgsem/elixir_euler_amr.jl:9-25 (3D; conservative state given directly)
+      const double rho = 1 + std::exp(-(x[0] * x[0] + x[1] * x[1] + x[2] * x[2])) / 2;
+      u[0] = rho;
+      u[1] = rho;
+      u[2] = rho;
+      u[3] = rho;
+      u[4] = 1 / (eq.gamma - 1) + 1.0 / 2 * rho * 3;
+      return;
+    }
     case IC_BLAST_WAVE: {
       // the medium blast wave of examples/tree_2d_dgsem/elixir_euler_blast_wave_amr.jl:18-34
       // (Hennemann & Gassner 2020, sec. 6.3): the weak blast wave's inner state
@@ -1072,7 +1083,8 @@ struct AmrParams {
   bool alpha_smooth = true;
   int base_level = 1, med_level = 1, max_level = 1;
   double med_threshold = 0.0, max_threshold = 1.0;
-  int variable = 0;  // 0 density_pressure, 1 density
+  int variable = 0;   // 0 density_pressure, 1 density
+  int indicator = 0;  // 0 IndicatorHennemannGassner, 1 IndicatorMax
   int interval = 5;
   bool adapt_initial = true, initial_only_refine = true;
 };
@@ -1537,7 +1549,17 @@ static void rk_update(int64_t ndof, double* u, double* u_tmp, const double* du, 
 // ControllerThreeLevel: +1 refine, -1 coarsen, 0 keep
 static std::vector<int> amr_controller(const Solver& s, const double* u, const AmrParams& ap) {
   std::vector<double> alpha;
-  hg_alpha(s, u, ap.alpha_max, ap.alpha_min, ap.alpha_smooth, alpha, ap.variable);
+  if (ap.indicator == 1) {
+    // IndicatorMax, indicators_3d.jl:239-259
+    alpha.assign(s.m.nelem, -INFINITY);
+    for (int64_t e = 0; e < s.m.nelem; ++e)
+      for (int node = 0; node < s.nn; ++node) {
+        const double* un = &u[uidx(s, e, node, 0)];
+        alpha[e] = std::max(alpha[e], ap.variable == 1 ? un[0] : density_pressure(s.eq, un));
+      }
+  } else {
+    hg_alpha(s, u, ap.alpha_max, ap.alpha_min, ap.alpha_smooth, alpha, ap.variable);
+  }
   std::vector<int> lambda(s.m.nelem, 0);
   for (int64_t e = 0; e < s.m.nelem; ++e) {
     const int cur = s.m.elevel[e];
@@ -1883,7 +1905,8 @@ int orc_solve(void* h, double* u, double t0, double t_end, double cfl, int64_t m
 // AMR settings of the solver (AMRCallback + ControllerThreeLevel with an HG
 // indicator); ints: interval, adapt_initial_condition,
 // adapt_initial_condition_only_refine, alpha_smooth, base_level, med_level,
-// max_level, indicator variable (0 density_pressure, 1 density); doubles:
+// max_level, indicator variable (0 density_pressure, 1 density), indicator
+// (0 IndicatorHennemannGassner, 1 IndicatorMax); doubles:
 // alpha_max, alpha_min, med_threshold, max_threshold.
 void orc_set_amr(void* h, const int* ints, const double* dbls) {
   Solver& s = *(Solver*)h;
@@ -1896,6 +1919,7 @@ void orc_set_amr(void* h, const int* ints, const double* dbls) {
   a.med_level = ints[5];
   a.max_level = ints[6];
   a.variable = ints[7];
+  a.indicator = ints[8];
   a.alpha_max = dbls[0];
   a.alpha_min = dbls[1];
   a.med_threshold = dbls[2];

@@ -37,4 +37,4 @@ def ic_id(O, name):
                 kelvin_helmholtz=O.IC_KELVIN_HELMHOLTZ, taylor_green=O.IC_TAYLOR_GREEN,
                 gaussian_blast=O.IC_GAUSSIAN_BLAST,
                 isentropic_vortex_advected=O.IC_ISENTROPIC_VORTEX_ADVECTED,
-                blast_wave=O.IC_BLAST_WAVE)[name]
+                blast_wave=O.IC_BLAST_WAVE, density_pulse=O.IC_DENSITY_PULSE)[name]

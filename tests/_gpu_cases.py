@@ -19,6 +19,7 @@ IC = {"convergence_test": (lambda p: T.initial_condition_convergence_test, O.IC_
                        O.IC_TAYLOR_GREEN),
       "constant": (lambda p: T.initial_condition_constant, O.IC_CONSTANT),
       "blast_wave": (lambda p: T.initial_condition_blast_wave, O.IC_BLAST_WAVE),
+      "density_pulse": (lambda p: T.initial_condition_density_pulse, O.IC_DENSITY_PULSE),
       "gaussian_blast": (lambda p: T.initial_condition_gaussian_blast(*(p or [1e-5, 1.0, 0.25])),
                          O.IC_GAUSSIAN_BLAST)}
 
@@ -73,7 +74,12 @@ def build(c, precision="fp64", elements_per_block=0):
 def amr_callback(semi, c):
     """AMRCallback + ControllerThreeLevel(IndicatorHennemannGassner) from a case's amr dict."""
     a = dict(c["amr"])
-    ind = T.IndicatorHennemannGassner(semi, alpha_max=a.pop("alpha_max", 0.5),
+    variables = {"density_pressure": T.density_pressure, "density": T.density}
+    if a.pop("indicator", "hennemann_gassner") == "max":
+        ind = T.IndicatorMax(semi, variable=variables[a.pop("variable", "density")])
+    else:
+        ind = None
+    ind = ind or T.IndicatorHennemannGassner(semi, alpha_max=a.pop("alpha_max", 0.5),
                                       alpha_min=a.pop("alpha_min", 0.001),
                                       alpha_smooth=a.pop("alpha_smooth", True),
                                       variable={"density_pressure": T.density_pressure,

@@ -140,6 +140,15 @@ CASES = {
                  adapt_initial_condition_only_refine=True, alpha_max=1.0, alpha_min=0.0001,
                  alpha_smooth=False, variable="density", base_level=4, med_level=0,
                  med_threshold=0.0003, max_level=6, max_threshold=0.003)),
+    "TreeMesh3D Euler: elixir_euler_amr.jl": dict(
+        file="test/test_tree_3d_euler.jl",
+        elixir="examples/tree_3d_dgsem/elixir_euler_amr.jl",
+        ndims=3, polydeg=3, level=4, xmin=[-5.0] * 3, xmax=[5.0] * 3,
+        ic="density_pulse", source="none", vi="weak", volume_flux="central",
+        surface_flux="llf_naive", cfl=0.9, tspan=[0.0, 10.0],
+        amr=dict(interval=5, adapt_initial_condition=True,
+                 adapt_initial_condition_only_refine=True, indicator="max", variable="density",
+                 base_level=4, med_level=5, med_threshold=1.05, max_level=6, max_threshold=1.3)),
     "TreeMesh3D Euler: elixir_euler_mortar.jl": dict(
         file="test/test_tree_3d_euler.jl",
         elixir="examples/tree_3d_dgsem/elixir_euler_mortar.jl",

@@ -120,3 +120,18 @@ def test_mixed_amr_goldens_within_1p1x_of_fp64(name):
     semi, _, ana, _ = _amr_run(name, "mixed")
     assert ana.l2[0] <= 1.1 * ana64.l2[0]
     assert semi.nelements > 0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_indicator_max_matches_host(precision):
+    # IndicatorMax(semi; variable) (indicators_3d.jl:239-259) on the device
+    c = dict(ndims=3, polydeg=3, level=2, xmin=[-5.0] * 3, xmax=[5.0] * 3, vi="weak",
+             surface_flux="llf_naive", ic="density_pulse")
+    semi, _ = build(c, precision=precision)
+    u = semi.compute_coefficients(0.0)
+    ctx = semi.device_context
+    ctx.upload(u)
+    rho_max = u[..., 0].reshape(semi.nelements, -1).max(axis=1)
+    np.testing.assert_allclose(ctx.amr_indicator_max(1), rho_max, rtol=1e-15, atol=0)
+    dp = T.density_pressure(u, semi.equations).reshape(semi.nelements, -1).max(axis=1)
+    np.testing.assert_allclose(ctx.amr_indicator_max(0), dp, rtol=1e-13, atol=0)

@@ -654,6 +654,34 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// IndicatorMax (indicators_2d.jl / indicators_3d.jl:239-259): the maximum of
+// the indicator variable over the nodes of each element, one warp per
+// element, FP64 (float-float states read as hi + lo).
+template <int D, typename S>
+__global__ void indicator_max_kernel(const S* __restrict__ u, int64_t E, int NN, int variable,
+                                     double gamma, double* __restrict__ out) {
+  constexpr int NV = D + 2;
+  const int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (e >= E) return;
+  double m = -INFINITY;
+  for (int n = lane; n < NN; n += 32) {
+    double x[NV];
+    const S* p = u + ((size_t)e * NN + n) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      if constexpr (std::is_same<S, double>::value)
+        x[v] = p[v];
+      else
+        x[v] = (double)p[v].x + (double)p[v].y;
+    }
+    m = fmax(m, variable == 1 ? x[0] : Euler<D, double>::density_pressure(x, gamma));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) out[e] = m;
+}
+
 // Solution transfer of AMR (refine_element! / coarsen_elements!,
 // amr_dg2d.jl:224-294, 429-485; amr_dg3d.jl): one thread per node of the
 // adapted mesh.  mats: forward lower, upper, reverse lower, upper
@@ -1895,6 +1923,38 @@ int tg_amr_indicator(tg_ctx* c, double alpha_max, double alpha_min, int32_t alph
       c->d_amr_raw, c->d_nbr, c->E, 2 * c->D, alpha_smooth, c->P.nbc, c->d_mnbr, c->d_amr_alpha);
   CUDA_TRY(c, cudaGetLastError());
   CUDA_TRY(c, cudaMemcpyAsync(alpha_host, c->d_amr_alpha, sizeof(double) * c->E,
+                              cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return TG_OK;
+}
+
+int tg_amr_indicator_max(tg_ctx* c, int32_t variable, double* out_host) {
+  if (!c || !out_host) return TG_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return fail(c, TG_ERR_STATE, "no state uploaded");
+  if (variable != TG_INDICATOR_DENSITY_PRESSURE && variable != TG_INDICATOR_DENSITY)
+    return fail(c, TG_ERR_INVALID_ARGUMENT, "unknown indicator variable %d", variable);
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  int rc = ensure(c, (void**)&c->d_amr_alpha, sizeof(double) * c->E);
+  if (rc) return rc;
+  const unsigned nb = (unsigned)((c->E * 32 + 127) / 128);
+  const void* u = c->d_u[c->cur];
+  if (c->fp64) {
+    if (c->D == 2)
+      indicator_max_kernel<2, double><<<nb, 128, 0, c->stream>>>((const double*)u, c->E, c->NN,
+                                                                 variable, c->P.gamma, c->d_amr_alpha);
+    else
+      indicator_max_kernel<3, double><<<nb, 128, 0, c->stream>>>((const double*)u, c->E, c->NN,
+                                                                 variable, c->P.gamma, c->d_amr_alpha);
+  } else {
+    if (c->D == 2)
+      indicator_max_kernel<2, float2><<<nb, 128, 0, c->stream>>>((const float2*)u, c->E, c->NN,
+                                                                 variable, c->P.gamma, c->d_amr_alpha);
+    else
+      indicator_max_kernel<3, float2><<<nb, 128, 0, c->stream>>>((const float2*)u, c->E, c->NN,
+                                                                 variable, c->P.gamma, c->d_amr_alpha);
+  }
+  CUDA_TRY(c, cudaGetLastError());
+  CUDA_TRY(c, cudaMemcpyAsync(out_host, c->d_amr_alpha, sizeof(double) * c->E,
                               cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return TG_OK;

@@ -20,7 +20,8 @@ the host side: mesh/basis setup, the C-ABI binding and the driver loop.
 from ._lib import TrixiGB300Error, load as load_library  # noqa: F401
 from .analysis import calc_error_norms  # noqa: F401
 from .basis import LobattoLegendreAnalyzer, LobattoLegendreBasis, MortarL2  # noqa: F401
-from .equations import (initial_condition_blast_wave,  # noqa: F401
+from .equations import (initial_condition_density_pulse,  # noqa: F401
+                        initial_condition_blast_wave,  # noqa: F401
                         CompressibleEulerEquations2D, CompressibleEulerEquations3D,  # noqa: F401
                         FluxLaxFriedrichs, cons2prim, density, density_pressure, flux_central,
                         flux_lax_friedrichs, flux_ranocha, flux_shima_etal,
@@ -34,7 +35,7 @@ from .mesh import TreeMesh  # noqa: F401
 from .semidiscretization import (BoundaryConditionDirichlet, DeviceContext, ODEProblem,  # noqa: F401
                                  SemidiscretizationHyperbolic, boundary_condition_periodic,
                                  boundary_condition_slip_wall, semidiscretize)
-from .solvers import (DGSEM, IndicatorHennemannGassner, VolumeIntegralFluxDifferencing,  # noqa: F401
+from .solvers import (DGSEM, IndicatorHennemannGassner, IndicatorMax, VolumeIntegralFluxDifferencing,  # noqa: F401
                       VolumeIntegralShockCapturingHG, VolumeIntegralWeakForm)
 from .time_integration import (AliveCallback, AnalysisCallback, CallbackSet,  # noqa: F401
                                CarpenterKennedy2N54, StepsizeCallback, SummaryCallback,

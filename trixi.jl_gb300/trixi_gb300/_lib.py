@@ -38,7 +38,7 @@ EXPORTS = ("tg_api_version", "tg_ctx_create", "tg_ctx_destroy", "tg_last_error",
            "tg_entropy_timederivative", "tg_ensemble_create", "tg_ensemble_destroy",
            "tg_ensemble_size", "tg_ensemble_context", "tg_ensemble_step", "tg_ensemble_autotune",
            "tg_ensemble_threads_per_block", "tg_ensemble_last_error", "tg_ctx_autotune",
-           "tg_amr_indicator", "tg_adapt_state", "tg_tree_create", "tg_tree_destroy",
+           "tg_amr_indicator", "tg_amr_indicator_max", "tg_adapt_state", "tg_tree_create", "tg_tree_destroy",
            "tg_tree_refine_patch", "tg_tree_nelements", "tg_tree_elements", "tg_tree_counts",
            "tg_tree_interfaces", "tg_tree_mortars", "tg_tree_adapt", "tg_tree_transfer_map")
 
@@ -125,6 +125,7 @@ def load(path: str | None = None):
         "tg_integrals": ([vp, pd], ctypes.c_int),
         "tg_alpha": ([vp, vp, pd], ctypes.c_int),
         "tg_amr_indicator": ([vp, ctypes.c_double, ctypes.c_double, i32, i32, pd], ctypes.c_int),
+        "tg_amr_indicator_max": ([vp, i32, pd], ctypes.c_int),
         "tg_tree_create": ([i32, i32, pd, pd, P(i32), P(vp)], ctypes.c_int),
         "tg_tree_destroy": ([vp], ctypes.c_int),
         "tg_tree_refine_patch": ([vp, i32, pd, pd, d], ctypes.c_int),

@@ -15,7 +15,7 @@ import time
 import numpy as np
 
 from .equations import density
-from .solvers import IndicatorHennemannGassner
+from .solvers import IndicatorHennemannGassner, IndicatorMax
 
 
 class ControllerThreeLevel:
@@ -26,8 +26,9 @@ class ControllerThreeLevel:
 
     def __init__(self, semi, indicator, base_level=1, med_level=None, med_threshold=0.0,
                  max_level=None, max_threshold=1.0):
-        if not isinstance(indicator, IndicatorHennemannGassner):
-            raise NotImplementedError("ControllerThreeLevel: the HG indicator is on the GPU path")
+        if not isinstance(indicator, (IndicatorHennemannGassner, IndicatorMax)):
+            raise NotImplementedError("ControllerThreeLevel: IndicatorHennemannGassner or "
+                                      "IndicatorMax on the GPU path")
         self.indicator = indicator
         self.base_level = int(base_level)
         self.med_level = self.base_level if med_level is None else int(med_level)
@@ -38,6 +39,8 @@ class ControllerThreeLevel:
     def indicator_values(self, semi):
         ind = self.indicator
         variable = 1 if ind.variable is density else 0
+        if isinstance(ind, IndicatorMax):
+            return semi.device_context.amr_indicator_max(variable)
         return semi.device_context.amr_indicator(ind.alpha_max, ind.alpha_min, ind.alpha_smooth,
                                                  variable)
 

@@ -146,6 +146,22 @@ def initial_condition_convergence_test(x, t, equations):
     return u
 
 
+def initial_condition_density_pulse(x, t, equations):
+    """examples/tree_3d_dgsem/elixir_euler_amr.jl:9-25: a Gaussian density pulse
+    at rest pressure 1 moving with velocity (1, 1, 1)."""
+    if equations.ndims != 3:
+        raise NotImplementedError("initial_condition_density_pulse is the 3D elixir's")
+    g = equations.gamma
+    rho = 1 + np.exp(-(x[..., 0] ** 2 + x[..., 1] ** 2 + x[..., 2] ** 2)) / 2
+    u = np.empty(x.shape[:-1] + (5,))
+    u[..., 0] = rho
+    u[..., 1] = rho
+    u[..., 2] = rho
+    u[..., 3] = rho
+    u[..., 4] = 1 / (g - 1) + 1 / 2 * rho * 3
+    return u
+
+
 def initial_condition_blast_wave(x, t, equations):
     """The medium blast wave of examples/tree_2d_dgsem/elixir_euler_blast_wave_amr.jl:18-34
     (Hennemann & Gassner 2020, sec. 6.3): the weak blast wave's inner state in a

@@ -215,6 +215,13 @@ class DeviceContext:
                                               int(bool(alpha_smooth)), int(variable), _dptr(out)))
         return out
 
+    def amr_indicator_max(self, variable=1):
+        """IndicatorMax: the maximum of the variable (1: density, 0:
+        density_pressure) over each element's nodes, in FP64."""
+        out = np.zeros(self.semi.nelements)
+        self._check(self.lib.tg_amr_indicator_max(self.h, int(variable), _dptr(out)))
+        return out
+
     def adapt_from(self, src, source_element, kind):
         """This context's state from `src`'s by the AMR transfer map
         (tg_adapt_state) with the solver's L2 adaptor matrices."""

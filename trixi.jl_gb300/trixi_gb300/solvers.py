@@ -43,6 +43,17 @@ class IndicatorHennemannGassner:
         self.variable = variable
 
 
+class IndicatorMax:
+    """IndicatorMax(semi; variable), indicators.jl: the maximum of `variable`
+    (density or density_pressure on the GPU path) over the nodes of each element;
+    an AMR indicator (indicators_3d.jl:239-259)."""
+
+    def __init__(self, semi, variable=density):
+        if variable is not density and variable is not density_pressure:
+            raise NotImplementedError("IndicatorMax: variable density or density_pressure")
+        self.variable = variable
+
+
 class VolumeIntegralShockCapturingHG:
     """VolumeIntegralShockCapturingHG(indicator; volume_flux_dg, volume_flux_fv), dg.jl:208-221."""
     code = _lib.TG_VOLUME_SHOCK_CAPTURING_HG
