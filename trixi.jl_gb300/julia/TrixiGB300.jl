@@ -297,4 +297,46 @@ function step_to!(ens::GB300Ensemble, t::Vector{Float64}, t_end, cfl; max_steps 
     return steps
 end
 
+"""
+    amr_indicator(ctx, indicator)
+
+The values ControllerThreeLevel compares with its thresholds, computed on the
+device in FP64: `IndicatorHennemannGassner` (its alpha_max, alpha_min,
+alpha_smooth; variable density_pressure or density) or `IndicatorMax`.
+"""
+function amr_indicator(ctx::GB300Context, ind::IndicatorHennemannGassner, nelements)
+    out = zeros(Float64, nelements)
+    variable = ind.variable === Trixi.density ? Int32(1) : Int32(0)
+    check(ccall((:tg_amr_indicator, lib), Cint,
+                (Ptr{Cvoid}, Cdouble, Cdouble, Int32, Int32, Ptr{Float64}),
+                ctx.ptr, ind.alpha_max, ind.alpha_min, Int32(ind.alpha_smooth), variable, out),
+          ctx.ptr)
+    return out
+end
+function amr_indicator(ctx::GB300Context, ind::Trixi.IndicatorMax, nelements)
+    out = zeros(Float64, nelements)
+    variable = ind.variable === Trixi.density_pressure ? Int32(0) : Int32(1)
+    check(ccall((:tg_amr_indicator_max, lib), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}),
+                ctx.ptr, variable, out), ctx.ptr)
+    return out
+end
+
+"""
+    adapt_state!(new_ctx, old_ctx, source_element, kind, adaptor)
+
+The solution transfer of refine!/coarsen! (amr_dg2d.jl) on the device, from
+the context of the mesh before adaptation into the context of the adapted
+mesh.  `source_element` (0-based) and `kind` (0 copy, 1 + child, -1 coarsen)
+describe each new element; `adaptor` is the solver's LobattoLegendreAdaptorL2.
+"""
+function adapt_state!(new::GB300Context, old::GB300Context, source_element::Vector{Int64},
+                      kind::Vector{Int8}, a)
+    check(ccall((:tg_adapt_state, lib), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Int64}, Ptr{Int8}, Ptr{Float64}, Ptr{Float64},
+                 Ptr{Float64}, Ptr{Float64}),
+                new.ptr, old.ptr, source_element, kind, a.forward_upper, a.forward_lower,
+                a.reverse_upper, a.reverse_lower), new.ptr)
+    return new
+end
+
 end # module
