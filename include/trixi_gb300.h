@@ -66,13 +66,16 @@ typedef enum tg_volume_integral {
 /* two-point fluxes: flux_central (numerical_fluxes.jl:17-25), flux_ranocha
  * (compressible_euler_2d.jl:686-722), flux_shima_etal (:466-495),
  * FluxLaxFriedrichs(max_abs_speed) = flux_lax_friedrichs and
- * FluxLaxFriedrichs(max_abs_speed_naive) (numerical_fluxes.jl:222-253) */
+ * FluxLaxFriedrichs(max_abs_speed_naive) (numerical_fluxes.jl:222-253),
+ * flux_hllc (compressible_euler_2d.jl:1720-1816; surface and FV subcell flux
+ * only, not a flux-differencing volume flux) */
 typedef enum tg_flux {
   TG_FLUX_CENTRAL = 0,
   TG_FLUX_RANOCHA = 1,
   TG_FLUX_SHIMA_ETAL = 2,
   TG_FLUX_LAX_FRIEDRICHS = 3,
-  TG_FLUX_LAX_FRIEDRICHS_NAIVE = 4
+  TG_FLUX_LAX_FRIEDRICHS_NAIVE = 4,
+  TG_FLUX_HLLC = 5
 } tg_flux;
 
 /* source_terms_convergence_test, compressible_euler_2d.jl:116-145, 3d.jl:127-150 */

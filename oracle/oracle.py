@@ -21,7 +21,8 @@ _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 
 # enums mirrored from trixi_oracle.cpp
 VI_WEAK, VI_FLUXDIFF, VI_SHOCKCAPTURING_HG = 0, 1, 2
-FLUX_CENTRAL, FLUX_RANOCHA, FLUX_SHIMA_ETAL, FLUX_LAX_FRIEDRICHS, FLUX_LAX_FRIEDRICHS_NAIVE = range(5)
+(FLUX_CENTRAL, FLUX_RANOCHA, FLUX_SHIMA_ETAL, FLUX_LAX_FRIEDRICHS, FLUX_LAX_FRIEDRICHS_NAIVE,
+ FLUX_HLLC) = range(6)
 SRC_NONE, SRC_CONVERGENCE_TEST = 0, 1
 BC_PERIODIC, BC_DIRICHLET, BC_SLIP_WALL = 0, 1, 2
 (IC_CONSTANT, IC_CONVERGENCE_TEST, IC_ISENTROPIC_VORTEX, IC_WEAK_BLAST_WAVE,

@@ -40,6 +40,7 @@ enum Flux {
   FLUX_SHIMA_ETAL = 2,
   FLUX_LAX_FRIEDRICHS = 3,        // FluxLaxFriedrichs(max_abs_speed)
   FLUX_LAX_FRIEDRICHS_NAIVE = 4,  // FluxLaxFriedrichs(max_abs_speed_naive)
+  FLUX_HLLC = 5,                  // flux_hllc
 };
 enum Source { SRC_NONE = 0, SRC_CONVERGENCE_TEST = 1 };
 enum Boundary { BC_PERIODIC = 0, BC_DIRICHLET = 1, BC_SLIP_WALL = 2 };
@@ -521,6 +522,66 @@ static inline void flux_llf(const Eq& eq, const double* ul, const double* ur, in
   for (int v = 0; v < eq.NV; ++v) f[v] = f[v] + (-0.5 * lam * (ur[v] - ul[v]));
 }
 
+// flux_hllc, compressible_euler_2d.jl:1720-1816, 3d.jl:1423-1541 (Toro's HLLC
+// with Roe-average and Einfeldt-type bounds on the signal speeds)
+static inline void flux_hllc(const Eq& eq, const double* ul, const double* ur, int o, double* F) {
+  const int D = eq.D, NV = eq.NV;
+  const double g = eq.gamma;
+  double vl[3] = {0, 0, 0}, vr[3] = {0, 0, 0}, v2l = 0, v2r = 0;
+  for (int d = 0; d < D; ++d) {
+    vl[d] = ul[1 + d] / ul[0];
+    vr[d] = ur[1 + d] / ur[0];
+    v2l += vl[d] * vl[d];
+    v2r += vr[d] * vr[d];
+  }
+  const double rl = ul[0], rr = ur[0];
+  const double el = ul[NV - 1] / rl, er = ur[NV - 1] / rr;
+  const double pl = (g - 1) * (ul[NV - 1] - 0.5 * rl * v2l);
+  const double pr = (g - 1) * (ur[NV - 1] - 0.5 * rr * v2r);
+  const double cl = std::sqrt(g * pl / rl), cr = std::sqrt(g * pr / rr);
+  double fl[5], fr[5];
+  flux_phys(eq, ul, o, fl);
+  flux_phys(eq, ur, o, fr);
+  const double sl = std::sqrt(rl), sr = std::sqrt(rr), ss = sl + sr;
+  const double vel_L = vl[o], vel_R = vr[o];
+  const double vel_roe = (sl * vel_L + sr * vel_R) / ss;
+  double vroe2 = 0;
+  for (int d = 0; d < D; ++d) {
+    const double vroe = sl * vl[d] + sr * vr[d];
+    vroe2 += vroe * vroe;
+  }
+  const double vel_roe_mag = vroe2 / (ss * ss);
+  const double Hl = (ul[NV - 1] + pl) / rl, Hr = (ur[NV - 1] + pr) / rr;
+  const double H_roe = (sl * Hl + sr * Hr) / ss;
+  const double c_roe = std::sqrt((g - 1) * (H_roe - 0.5 * vel_roe_mag));
+  const double Ssl = std::min(vel_L - cl, vel_roe - c_roe);
+  const double Ssr = std::max(vel_R + cr, vel_roe + c_roe);
+  const double sMu_L = Ssl - vel_L, sMu_R = Ssr - vel_R;
+  if (Ssl >= 0) {
+    for (int v = 0; v < NV; ++v) F[v] = fl[v];
+    return;
+  }
+  if (Ssr <= 0) {
+    for (int v = 0; v < NV; ++v) F[v] = fr[v];
+    return;
+  }
+  const double SStar =
+      (pr - pl + rl * vel_L * sMu_L - rr * vel_R * sMu_R) / (rl * sMu_L - rr * sMu_R);
+  const bool left = Ssl <= 0 && 0 <= SStar;
+  const double* u = left ? ul : ur;
+  const double* f = left ? fl : fr;
+  const double* vv = left ? vl : vr;
+  const double S = left ? Ssl : Ssr, sMu = left ? sMu_L : sMu_R, rho = left ? rl : rr;
+  const double vel = left ? vel_L : vel_R, e = left ? el : er, p = left ? pl : pr;
+  const double densStar = rho * sMu / (S - SStar);
+  const double enerStar = e + (SStar - vel) * (SStar + p / (rho * sMu));
+  double UStar[5];
+  UStar[0] = densStar;
+  for (int d = 0; d < D; ++d) UStar[1 + d] = densStar * (d == o ? SStar : vv[d]);
+  UStar[NV - 1] = densStar * enerStar;
+  for (int v = 0; v < NV; ++v) F[v] = f[v] + S * (UStar[v] - u[v]);
+}
+
 static inline void two_point_flux(const Eq& eq, int kind, const double* ul, const double* ur,
                                   int o, double* f) {
   switch (kind) {
@@ -529,6 +590,7 @@ static inline void two_point_flux(const Eq& eq, int kind, const double* ul, cons
     case FLUX_SHIMA_ETAL: flux_shima(eq, ul, ur, o, f); break;
     case FLUX_LAX_FRIEDRICHS: flux_llf(eq, ul, ur, o, false, f); break;
     case FLUX_LAX_FRIEDRICHS_NAIVE: flux_llf(eq, ul, ur, o, true, f); break;
+    case FLUX_HLLC: flux_hllc(eq, ul, ur, o, f); break;
     default: for (int v = 0; v < eq.NV; ++v) f[v] = NAN;
   }
 }

@@ -14,7 +14,8 @@ def oracle_from_case(O, c, **over):
     c = dict(c, **over)
     vi = dict(weak=O.VI_WEAK, fluxdiff=O.VI_FLUXDIFF, hg=O.VI_SHOCKCAPTURING_HG)[c["vi"]]
     fl = dict(central=O.FLUX_CENTRAL, ranocha=O.FLUX_RANOCHA, shima_etal=O.FLUX_SHIMA_ETAL,
-              llf=O.FLUX_LAX_FRIEDRICHS, llf_naive=O.FLUX_LAX_FRIEDRICHS_NAIVE)
+              llf=O.FLUX_LAX_FRIEDRICHS, llf_naive=O.FLUX_LAX_FRIEDRICHS_NAIVE,
+              hllc=O.FLUX_HLLC)
     src = O.SRC_CONVERGENCE_TEST if c.get("source") == "convergence_test" else O.SRC_NONE
     orc = O.Oracle(c["ndims"], c["polydeg"], c["level"], c["xmin"], c["xmax"],
                    volume_integral=vi, volume_flux=fl[c["volume_flux"]],

@@ -8,7 +8,8 @@ from oracle import oracle as O
 FLUX = {"central": (T.flux_central, O.FLUX_CENTRAL), "ranocha": (T.flux_ranocha, O.FLUX_RANOCHA),
         "shima_etal": (T.flux_shima_etal, O.FLUX_SHIMA_ETAL),
         "llf": (T.flux_lax_friedrichs, O.FLUX_LAX_FRIEDRICHS),
-        "llf_naive": (T.FluxLaxFriedrichs(T.max_abs_speed_naive), O.FLUX_LAX_FRIEDRICHS_NAIVE)}
+        "llf_naive": (T.FluxLaxFriedrichs(T.max_abs_speed_naive), O.FLUX_LAX_FRIEDRICHS_NAIVE),
+        "hllc": (T.flux_hllc, O.FLUX_HLLC)}
 IC = {"convergence_test": (lambda p: T.initial_condition_convergence_test, O.IC_CONVERGENCE_TEST),
       "weak_blast_wave": (lambda p: T.initial_condition_weak_blast_wave, O.IC_WEAK_BLAST_WAVE),
       "kelvin_helmholtz": (lambda p: T.initial_condition_kelvin_helmholtz_instability,
@@ -20,6 +21,9 @@ IC = {"convergence_test": (lambda p: T.initial_condition_convergence_test, O.IC_
       "constant": (lambda p: T.initial_condition_constant, O.IC_CONSTANT),
       "blast_wave": (lambda p: T.initial_condition_blast_wave, O.IC_BLAST_WAVE),
       "density_pulse": (lambda p: T.initial_condition_density_pulse, O.IC_DENSITY_PULSE),
+      "isentropic_vortex_advected": (
+          lambda p: T.initial_condition_isentropic_vortex_advected(*(p or [25.0, 5.0])),
+          O.IC_ISENTROPIC_VORTEX_ADVECTED),
       "gaussian_blast": (lambda p: T.initial_condition_gaussian_blast(*(p or [1e-5, 1.0, 0.25])),
                          O.IC_GAUSSIAN_BLAST)}
 

@@ -18,7 +18,7 @@ import re
 import sys
 
 # Elixir settings transcribed from examples/tree_{2,3}d_dgsem/*.jl.
-# vi: weak | fluxdiff | hg ; fluxes: central | ranocha | shima_etal | llf | llf_naive
+# vi: weak | fluxdiff | hg ; fluxes: central | ranocha | shima_etal | llf | llf_naive | hllc
 CASES = {
     "TreeMesh2D Euler: elixir_euler_source_terms.jl": dict(
         file="test/test_tree_2d_euler.jl",
@@ -100,6 +100,14 @@ CASES = {
         ic="isentropic_vortex", ic_params=[25.0, 5.0], source="none",
         vi="fluxdiff", volume_flux="shima_etal", surface_flux="llf_naive", cfl=1.4,
         tspan=[0.0, 1.0]),
+    "TreeMesh2D Euler: elixir_euler_vortex_mortar.jl": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_vortex_mortar.jl",
+        ndims=2, polydeg=3, level=4, xmin=[-10.0, -10.0], xmax=[10.0, 10.0],
+        refinement_patches=[dict(type="box", coordinates_min=[0.0, -10.0],
+                                 coordinates_max=[10.0, 10.0])],
+        ic="isentropic_vortex_advected", ic_params=[25.0, 5.0], source="none",
+        vi="weak", volume_flux="central", surface_flux="hllc", cfl=1.4, tspan=[0.0, 1.0]),
     "TreeMesh2D Euler: elixir_euler_vortex_mortar_shockcapturing.jl": dict(
         file="test/test_tree_2d_euler.jl",
         elixir="examples/tree_2d_dgsem/elixir_euler_vortex_mortar_shockcapturing.jl",

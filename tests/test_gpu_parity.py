@@ -366,3 +366,40 @@ def test_rhs_edge_polydeg_matches_oracle(c, precision, tol):
     semi, orc = build(c, precision=precision)
     u = perturbed_state(semi, seed=53)
     assert rel_err(semi.device_context.rhs_host(u, 0.29), orc.rhs(u, 0.29)) < tol
+
+
+# flux_hllc (compressible_euler_{2,3}d.jl) as surface flux and as the FV
+# subcell flux of HG shock capturing
+HLLC_CASES = [
+    dict(ndims=2, polydeg=3, level=3, xmin=[-10, -10], xmax=[10, 10], vi="weak",
+         surface_flux="hllc", ic="isentropic_vortex_advected", ic_params=[25.0, 5.0]),
+    dict(ndims=3, polydeg=3, level=2, xmin=[0] * 3, xmax=[2] * 3, vi="weak", surface_flux="hllc",
+         ic="convergence_test", source="convergence_test"),
+    dict(ndims=2, polydeg=3, level=4, xmin=[-2, -2], xmax=[2, 2], vi="hg", volume_flux="ranocha",
+         surface_flux="hllc", ic="weak_blast_wave"),
+    dict(ndims=3, polydeg=3, level=2, xmin=[-2] * 3, xmax=[2] * 3, vi="fluxdiff",
+         volume_flux="ranocha", surface_flux="hllc", ic="weak_blast_wave"),
+    dict(ndims=2, polydeg=3, level=3, xmin=[-10, -10], xmax=[10, 10], vi="weak",
+         surface_flux="hllc", ic="isentropic_vortex_advected", ic_params=[25.0, 5.0],
+         refinement_patches=[dict(type="box", coordinates_min=[0.0, -10.0],
+                                  coordinates_max=[10.0, 10.0])]),
+]
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 2e-4)])
+@pytest.mark.parametrize("c", HLLC_CASES, ids=[_id(c) + ("-mortar" if c.get("refinement_patches") else "")
+                                              for c in HLLC_CASES])
+def test_rhs_hllc_matches_oracle(c, precision, tol):
+    semi, orc = build(c, precision=precision)
+    u = perturbed_state(semi, seed=13, amp=0.05)
+    du_gpu = semi.device_context.rhs_host(u, 0.41)
+    du_orc = orc.rhs(u, 0.41)
+    assert rel_err(du_gpu, du_orc) < tol
+
+
+def test_hllc_is_not_a_volume_flux():
+    c = dict(ndims=2, polydeg=3, level=2, xmin=[-1, -1], xmax=[1, 1], vi="fluxdiff",
+             volume_flux="hllc", surface_flux="llf", ic="weak_blast_wave")
+    semi, _ = build(c)
+    with pytest.raises(T.TrixiGB300Error):
+        semi.device_context

@@ -59,7 +59,8 @@ def test_treemesh_morton_order_2d():
     (2, "weak_blast_wave", O.IC_WEAK_BLAST_WAVE), (3, "weak_blast_wave", O.IC_WEAK_BLAST_WAVE),
     (2, "khi", O.IC_KELVIN_HELMHOLTZ), (2, "vortex", O.IC_ISENTROPIC_VORTEX),
     (3, "tgv", O.IC_TAYLOR_GREEN), (2, "constant", O.IC_CONSTANT), (3, "constant", O.IC_CONSTANT),
-    (2, "gauss", O.IC_GAUSSIAN_BLAST)])
+    (2, "gauss", O.IC_GAUSSIAN_BLAST), (2, "blast", O.IC_BLAST_WAVE),
+    (3, "pulse", O.IC_DENSITY_PULSE), (2, "vortex_advected", O.IC_ISENTROPIC_VORTEX_ADVECTED)])
 def test_initial_conditions_match_oracle(ndims, ic, oic):
     funcs = dict(convergence_test=(T.initial_condition_convergence_test, None),
                  weak_blast_wave=(T.initial_condition_weak_blast_wave, None),
@@ -67,14 +68,19 @@ def test_initial_conditions_match_oracle(ndims, ic, oic):
                  vortex=(T.initial_condition_isentropic_vortex(1.0, 5.0), [1.0, 5.0]),
                  tgv=(T.initial_condition_taylor_green_vortex(0.1), [0.1]),
                  constant=(T.initial_condition_constant, None),
-                 gauss=(T.initial_condition_gaussian_blast(1e-5, 1.0, 0.25), [1e-5, 1.0, 0.25]))
+                 gauss=(T.initial_condition_gaussian_blast(1e-5, 1.0, 0.25), [1e-5, 1.0, 0.25]),
+                 blast=(T.initial_condition_blast_wave, None),
+                 pulse=(T.initial_condition_density_pulse, None),
+                 vortex_advected=(T.initial_condition_isentropic_vortex_advected(25.0, 5.0),
+                                  [25.0, 5.0]))
     f, par = funcs[ic]
     xmin, xmax = [-1.5] * ndims, [1.5] * ndims
     eq = T.CompressibleEulerEquations2D(1.4) if ndims == 2 else T.CompressibleEulerEquations3D(1.4)
     semi = T.SemidiscretizationHyperbolic(T.TreeMesh(xmin, xmax, initial_refinement_level=2), eq, f,
                                           T.DGSEM(polydeg=3))
     orc = O.Oracle(ndims, 3, 2, xmin, xmax)
-    np.testing.assert_allclose(semi.compute_coefficients(0.3), orc.initial_condition(oic, par, 0.3),
+    t = 13.7 if ic == "vortex_advected" else 0.3  # the advected vortex wraps around
+    np.testing.assert_allclose(semi.compute_coefficients(t), orc.initial_condition(oic, par, t),
                                rtol=1e-13, atol=1e-13)
 
 

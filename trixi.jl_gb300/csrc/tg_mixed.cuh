@@ -344,6 +344,67 @@ struct Dev {
   }
 
   // KIND >= 0 selects the flux at compile time; KIND < 0 dispatches on `kind`.
+  // flux_hllc(a, b) - f(w_ref) (compressible_euler_2d.jl:1720-1816, 3d.jl:1423-1541).
+  // Signal speeds from the full primitives (they only weight the terms).  The
+  // outer branches are physical-flux deviations; the star-state correction is
+  // written in terms of SStar - v of the upwind side, which comes from the
+  // pressure and velocity deviations without cancellation:
+  //   SStar - v_L = (p_R - p_L + rho_R sMu_R (v_L - v_R)) / den,
+  //   SStar - v_R = (p_R - p_L + rho_L sMu_L (v_L - v_R)) / den,
+  //   den = rho_L sMu_L - rho_R sMu_R,
+  // and rho* - rho = rho (SStar - v) / (S - SStar), so every correction term is
+  // proportional to SStar - v.
+  static __host__ __device__ __forceinline__ void dhllc(const RefState<D>& R, const Node<D>& a,
+                                                const Node<D>& b, int o, float vro,
+                                                const EosF& eos, float* f) {
+    const float g = eos.gamma;
+    const float rl = a.w[0], rr = b.w[0], pl = a.w[P], pr = b.w[P];
+    const float cl = sqrtf(g * pl / rl), cr = sqrtf(g * pr / rr);
+    const float sl = sqrtf(rl), sr = sqrtf(rr), iss = 1.0f / (sl + sr);
+    const float vel_L = a.vo, vel_R = b.vo;
+    const float vel_roe = (sl * vel_L + sr * vel_R) * iss;
+    float vroe2 = 0, kl = 0, kr = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const float vroe = sl * a.w[1 + d] + sr * b.w[1 + d];
+      vroe2 += vroe * vroe;
+      kl += a.w[1 + d] * a.w[1 + d];
+      kr += b.w[1 + d] * b.w[1 + d];
+    }
+    const float El = pl * eos.igm1 + 0.5f * rl * kl, Er = pr * eos.igm1 + 0.5f * rr * kr;
+    const float H_roe = (sl * ((El + pl) / rl) + sr * ((Er + pr) / rr)) * iss;
+    const float c_roe = sqrtf(eos.pressure(H_roe - 0.5f * vroe2 * iss * iss));
+    const float Ssl = fminf(vel_L - cl, vel_roe - c_roe);
+    const float Ssr = fmaxf(vel_R + cr, vel_roe + c_roe);
+    if (Ssl >= 0.0f) {
+      dflux(R, a, o, vro, eos, f);
+      return;
+    }
+    if (Ssr <= 0.0f) {
+      dflux(R, b, o, vro, eos, f);
+      return;
+    }
+    const float sMu_L = Ssl - vel_L, sMu_R = Ssr - vel_R;
+    const float iden = 1.0f / (rl * sMu_L - rr * sMu_R);
+    const float dv = a.dvo - b.dvo;     // v_L - v_R
+    const float dp = b.dw[P] - a.dw[P];  // p_R - p_L
+    const float ds_L = (dp + rr * sMu_R * dv) * iden;
+    const float SStar = vel_L + ds_L;
+    const bool left = SStar >= 0.0f;
+    const Node<D>& X = left ? a : b;
+    const float S = left ? Ssl : Ssr, sMu = left ? sMu_L : sMu_R;
+    const float ds = left ? ds_L : (dp + rl * sMu_L * dv) * iden;
+    const float rho = X.w[0], vel = X.vo;
+    const float dr = rho * ds / (S - SStar);  // rho* - rho
+    const float rs = rho + dr;
+    const float e = (left ? El : Er) / rho;
+    dflux(R, X, o, vro, eos, f);
+    f[0] += S * dr;
+#pragma unroll
+    for (int d = 0; d < D; ++d) f[1 + d] += S * ((d == o) ? fmaf(rs, ds, vel * dr) : X.w[1 + d] * dr);
+    f[P] += S * (e * dr + rs * ds * (SStar + X.w[P] / (rho * sMu)));
+  }
+
   template <int KIND>
   static __host__ __device__ __forceinline__ void flux2(int kind, const RefState<D>& R,
                                                          const Node<D>& a, const Node<D>& b, int o,
@@ -353,6 +414,7 @@ struct Dev {
     else if constexpr (KIND == FLUX_LLF) dllf(R, a, b, o, vro, false, eos, f);
     else if constexpr (KIND == FLUX_LLF_NAIVE) dllf(R, a, b, o, vro, true, eos, f);
     else if constexpr (KIND == FLUX_CENTRAL) dcentral(R, a, b, o, vro, eos, f);
+    else if constexpr (KIND == FLUX_HLLC) dhllc(R, a, b, o, vro, eos, f);
     else two_point(kind, R, a, b, o, vro, eos, f);
   }
 
@@ -364,6 +426,7 @@ struct Dev {
       case FLUX_SHIMA_ETAL: dshima(R, a, b, o, vro, eos, f); break;
       case FLUX_LLF: dllf(R, a, b, o, vro, false, eos, f); break;
       case FLUX_LLF_NAIVE: dllf(R, a, b, o, vro, true, eos, f); break;
+      case FLUX_HLLC: dhllc(R, a, b, o, vro, eos, f); break;
       default: dcentral(R, a, b, o, vro, eos, f); break;
     }
   }

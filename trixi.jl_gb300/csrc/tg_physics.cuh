@@ -18,7 +18,8 @@ enum FluxKind {
   FLUX_RANOCHA = 1,
   FLUX_SHIMA_ETAL = 2,
   FLUX_LLF = 3,
-  FLUX_LLF_NAIVE = 4
+  FLUX_LLF_NAIVE = 4,
+  FLUX_HLLC = 5
 };
 enum SourceKind { SRC_NONE = 0, SRC_CONVERGENCE_TEST = 1 };
 // boundary conditions of a non-periodic TreeMesh, per direction
@@ -204,6 +205,50 @@ struct Euler {
     for (int v = 0; v < NV; ++v) f[v] = f[v] + (R(-0.5) * lam * (ur[v] - ul[v]));
   }
 
+  // flux_hllc, compressible_euler_2d.jl:1720-1816, 3d.jl:1423-1541: Toro's HLLC
+  // with signal speeds bounded by the Roe average
+  static __host__ __device__ __forceinline__ void flux_hllc(const R* ul, const R* wl, const R* ur,
+                                                    const R* wr, int o, R gamma, R* F) {
+    const R rl = wl[0], rr = wr[0], pl = wl[P], pr = wr[P];
+    const R cl = Real<R>::sqrt(gamma * pl / rl), cr = Real<R>::sqrt(gamma * pr / rr);
+    const R sl = Real<R>::sqrt(rl), sr = Real<R>::sqrt(rr), ss = sl + sr;
+    const R vel_L = pick(wl + 1, o), vel_R = pick(wr + 1, o);
+    const R vel_roe = (sl * vel_L + sr * vel_R) / ss;
+    R vroe2 = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const R vroe = sl * wl[1 + d] + sr * wr[1 + d];
+      vroe2 += vroe * vroe;
+    }
+    const R Hl = (ul[P] + pl) / rl, Hr = (ur[P] + pr) / rr;
+    const R H_roe = (sl * Hl + sr * Hr) / ss;
+    const R c_roe = Real<R>::sqrt((gamma - R(1)) * (H_roe - R(0.5) * (vroe2 / (ss * ss))));
+    const R Ssl = fmin(vel_L - cl, vel_roe - c_roe);
+    const R Ssr = fmax(vel_R + cr, vel_roe + c_roe);
+    if (Ssl >= R(0)) {
+      flux(ul, wl, o, F);
+      return;
+    }
+    if (Ssr <= R(0)) {
+      flux(ur, wr, o, F);
+      return;
+    }
+    const R sMu_L = Ssl - vel_L, sMu_R = Ssr - vel_R;
+    const R SStar = (pr - pl + rl * vel_L * sMu_L - rr * vel_R * sMu_R) / (rl * sMu_L - rr * sMu_R);
+    const bool left = SStar >= R(0);
+    const R* u = left ? ul : ur;
+    const R* w = left ? wl : wr;
+    const R S = left ? Ssl : Ssr, sMu = left ? sMu_L : sMu_R;
+    const R rho = w[0], vel = left ? vel_L : vel_R, p = w[P];
+    flux(u, w, o, F);
+    const R densStar = rho * sMu / (S - SStar);
+    const R enerStar = u[P] / rho + (SStar - vel) * (SStar + p / (rho * sMu));
+    F[0] += S * (densStar - u[0]);
+#pragma unroll
+    for (int d = 0; d < D; ++d) F[1 + d] += S * (densStar * (d == o ? SStar : w[1 + d]) - u[1 + d]);
+    F[P] += S * (densStar * enerStar - u[P]);
+  }
+
   static __host__ __device__ __forceinline__ void two_point(int kind, const R* ul, const R* wl,
                                                     const R* ur, const R* wr, int o, R gamma,
                                                     R inv_gm1, R* f) {
@@ -212,6 +257,7 @@ struct Euler {
       case FLUX_SHIMA_ETAL: flux_shima(wl, wr, o, inv_gm1, f); break;
       case FLUX_LLF: flux_llf(ul, wl, ur, wr, o, false, gamma, f); break;
       case FLUX_LLF_NAIVE: flux_llf(ul, wl, ur, wr, o, true, gamma, f); break;
+      case FLUX_HLLC: flux_hllc(ul, wl, ur, wr, o, gamma, f); break;
       default: flux_central(ul, wl, ur, wr, o, f); break;
     }
   }

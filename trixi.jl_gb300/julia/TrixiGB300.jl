@@ -57,11 +57,12 @@ end
 
 const TG_VOLUME_WEAK_FORM, TG_VOLUME_FLUX_DIFFERENCING, TG_VOLUME_SHOCK_CAPTURING_HG = 0, 1, 2
 const TG_FLUX_CENTRAL, TG_FLUX_RANOCHA, TG_FLUX_SHIMA_ETAL = 0, 1, 2
-const TG_FLUX_LAX_FRIEDRICHS, TG_FLUX_LAX_FRIEDRICHS_NAIVE = 3, 4
+const TG_FLUX_LAX_FRIEDRICHS, TG_FLUX_LAX_FRIEDRICHS_NAIVE, TG_FLUX_HLLC = 3, 4, 5
 
 flux_code(::typeof(Trixi.flux_central)) = TG_FLUX_CENTRAL
 flux_code(::typeof(Trixi.flux_ranocha)) = TG_FLUX_RANOCHA
 flux_code(::typeof(Trixi.flux_shima_etal)) = TG_FLUX_SHIMA_ETAL
+flux_code(::typeof(Trixi.flux_hllc)) = TG_FLUX_HLLC
 function flux_code(f::Trixi.FluxLaxFriedrichs)
     f.dissipation.max_abs_speed === Trixi.max_abs_speed_naive ?
     TG_FLUX_LAX_FRIEDRICHS_NAIVE : TG_FLUX_LAX_FRIEDRICHS

@@ -48,6 +48,8 @@ class _Flux:
 flux_central = _Flux("flux_central", _lib.TG_FLUX_CENTRAL)
 flux_ranocha = _Flux("flux_ranocha", _lib.TG_FLUX_RANOCHA)
 flux_shima_etal = _Flux("flux_shima_etal", _lib.TG_FLUX_SHIMA_ETAL)
+# flux_hllc, compressible_euler_2d.jl:1720-1816 (a surface flux)
+flux_hllc = _Flux("flux_hllc", _lib.TG_FLUX_HLLC)
 
 
 class _MaxAbsSpeed:
@@ -144,6 +146,35 @@ def initial_condition_convergence_test(x, t, equations):
         u[..., v] = ini
     u[..., -1] = ini * ini
     return u
+
+
+def initial_condition_isentropic_vortex_advected(p_inf=25.0, amplitude=5.0):
+    """examples/tree_2d_dgsem/elixir_euler_vortex_mortar.jl:18-64: the vortex of
+    initial_condition_isentropic_vortex advected with the base flow (1, 1) and
+    wrapped to the nearest periodic image on [-10, 10]^2 (exact at every t)."""
+
+    def ic(x, t, equations):
+        g = equations.gamma
+        rho0, p0 = 1.0, float(p_inf)
+        rt = p0 / rho0
+        c0 = x[..., 0] - t
+        c1 = x[..., 1] - t
+        c0 = c0 - 20.0 * np.round(c0 / 20.0)  # round half to even, as Julia's round
+        c1 = c1 - 20.0 * np.round(c1 / 20.0)
+        a0, a1 = -c1, c0
+        r2 = a0 * a0 + a1 * a1
+        du = amplitude / (2 * math.pi) * np.exp(0.5 * (1 - r2))
+        dtemp = -(g - 1) / (2 * g * rt) * du * du
+        prim = np.empty(x.shape[:-1] + (4,))
+        prim[..., 0] = rho0 * (1 + dtemp) ** (1 / (g - 1))
+        prim[..., 1] = 1.0 + du * a0
+        prim[..., 2] = 1.0 + du * a1
+        prim[..., 3] = p0 * (1 + dtemp) ** (g / (g - 1))
+        return prim2cons(prim, equations)
+
+    ic.__name__ = "initial_condition_isentropic_vortex_advected"
+    ic.params = (float(p_inf), float(amplitude))
+    return ic
 
 
 def initial_condition_density_pulse(x, t, equations):
