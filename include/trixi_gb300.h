@@ -67,15 +67,19 @@ typedef enum tg_volume_integral {
  * (compressible_euler_2d.jl:686-722), flux_shima_etal (:466-495),
  * FluxLaxFriedrichs(max_abs_speed) = flux_lax_friedrichs and
  * FluxLaxFriedrichs(max_abs_speed_naive) (numerical_fluxes.jl:222-253),
- * flux_hllc (compressible_euler_2d.jl:1720-1816; surface and FV subcell flux
- * only, not a flux-differencing volume flux) */
+ * flux_hllc (compressible_euler_2d.jl:1720-1816), flux_chandrashekar
+ * (compressible_euler_2d.jl, 3d.jl:640-692), flux_hlle = FluxHLL(
+ * min_max_speed_einfeldt) (numerical_fluxes.jl:422-457; HLLC and HLLE are
+ * surface and FV subcell fluxes only, not flux-differencing volume fluxes) */
 typedef enum tg_flux {
   TG_FLUX_CENTRAL = 0,
   TG_FLUX_RANOCHA = 1,
   TG_FLUX_SHIMA_ETAL = 2,
   TG_FLUX_LAX_FRIEDRICHS = 3,
   TG_FLUX_LAX_FRIEDRICHS_NAIVE = 4,
-  TG_FLUX_HLLC = 5
+  TG_FLUX_HLLC = 5,
+  TG_FLUX_CHANDRASHEKAR = 6,
+  TG_FLUX_HLLE = 7
 } tg_flux;
 
 /* source_terms_convergence_test, compressible_euler_2d.jl:116-145, 3d.jl:127-150 */

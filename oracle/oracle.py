@@ -22,12 +22,12 @@ _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 # enums mirrored from trixi_oracle.cpp
 VI_WEAK, VI_FLUXDIFF, VI_SHOCKCAPTURING_HG = 0, 1, 2
 (FLUX_CENTRAL, FLUX_RANOCHA, FLUX_SHIMA_ETAL, FLUX_LAX_FRIEDRICHS, FLUX_LAX_FRIEDRICHS_NAIVE,
- FLUX_HLLC) = range(6)
+ FLUX_HLLC, FLUX_CHANDRASHEKAR, FLUX_HLLE) = range(8)
 SRC_NONE, SRC_CONVERGENCE_TEST = 0, 1
 BC_PERIODIC, BC_DIRICHLET, BC_SLIP_WALL = 0, 1, 2
 (IC_CONSTANT, IC_CONVERGENCE_TEST, IC_ISENTROPIC_VORTEX, IC_WEAK_BLAST_WAVE,
  IC_KELVIN_HELMHOLTZ, IC_TAYLOR_GREEN, IC_GAUSSIAN_BLAST,
- IC_ISENTROPIC_VORTEX_ADVECTED, IC_BLAST_WAVE, IC_DENSITY_PULSE) = range(10)
+ IC_ISENTROPIC_VORTEX_ADVECTED, IC_BLAST_WAVE, IC_DENSITY_PULSE, IC_SEDOV_BLAST_WAVE) = range(11)
 
 _lib = None
 

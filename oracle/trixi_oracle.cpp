@@ -41,6 +41,8 @@ enum Flux {
   FLUX_LAX_FRIEDRICHS = 3,        // FluxLaxFriedrichs(max_abs_speed)
   FLUX_LAX_FRIEDRICHS_NAIVE = 4,  // FluxLaxFriedrichs(max_abs_speed_naive)
   FLUX_HLLC = 5,                  // flux_hllc
+  FLUX_CHANDRASHEKAR = 6,         // flux_chandrashekar
+  FLUX_HLLE = 7,                  // flux_hlle = FluxHLL(min_max_speed_einfeldt)
 };
 enum Source { SRC_NONE = 0, SRC_CONVERGENCE_TEST = 1 };
 enum Boundary { BC_PERIODIC = 0, BC_DIRICHLET = 1, BC_SLIP_WALL = 2 };
@@ -55,6 +57,7 @@ enum InitialCondition {
   IC_ISENTROPIC_VORTEX_ADVECTED = 7,
   IC_BLAST_WAVE = 8,
   IC_DENSITY_PULSE = 9,
+  IC_SEDOV_BLAST_WAVE = 10,
 };
 
 // ---------------------------------------------------------------------------
@@ -467,6 +470,73 @@ static inline void flux_ranocha(const Eq& eq, const double* ul, const double* ur
          0.5 * (pl[P] * pr[1 + o] + pr[P] * pl[1 + o]);
 }
 
+// flux_chandrashekar, compressible_euler_2d.jl (orientation method), 3d.jl:640-692
+static inline void flux_chandrashekar(const Eq& eq, const double* ul, const double* ur, int o,
+                                      double* f) {
+  double pl[5], pr[5];
+  cons2prim(eq, ul, pl);
+  cons2prim(eq, ur, pr);
+  const int P = eq.NV - 1;
+  const double beta_ll = 0.5 * pl[0] / pl[P], beta_rr = 0.5 * pr[0] / pr[P];
+  double kin_ll = 0, kin_rr = 0, vavg[3] = {0, 0, 0};
+  for (int d = 0; d < eq.D; ++d) {
+    kin_ll += pl[1 + d] * pl[1 + d];
+    kin_rr += pr[1 + d] * pr[1 + d];
+    vavg[d] = 0.5 * (pl[1 + d] + pr[1 + d]);
+  }
+  kin_ll *= 0.5;
+  kin_rr *= 0.5;
+  const double rho_avg = 0.5 * (pl[0] + pr[0]);
+  const double rho_mean = ln_mean(pl[0], pr[0]);
+  const double beta_mean = ln_mean(beta_ll, beta_rr);
+  const double beta_avg = 0.5 * (beta_ll + beta_rr);
+  const double p_mean = 0.5 * rho_avg / beta_avg;
+  const double velocity_square_avg = kin_ll + kin_rr;
+  const double f1 = rho_mean * vavg[o];
+  f[0] = f1;
+  for (int d = 0; d < eq.D; ++d) f[1 + d] = f1 * vavg[d];
+  f[1 + o] += p_mean;
+  double e = f1 * 0.5 * (1 / (eq.gamma - 1) / beta_mean - velocity_square_avg);
+  for (int d = 0; d < eq.D; ++d) e += f[1 + d] * vavg[d];
+  f[P] = e;
+}
+
+// flux_hlle = FluxHLL(min_max_speed_einfeldt): numerical_fluxes.jl:422-457,
+// min_max_speed_einfeldt compressible_euler_2d.jl:1925-1963 (3d analogue)
+static inline void flux_hlle(const Eq& eq, const double* ul, const double* ur, int o, double* F) {
+  double pl[5], pr[5];
+  cons2prim(eq, ul, pl);
+  cons2prim(eq, ur, pr);
+  const int P = eq.NV - 1;
+  const double g = eq.gamma;
+  const double Hl = (ul[P] + pl[P]) / pl[0], Hr = (ur[P] + pr[P]) / pr[0];
+  const double cl = std::sqrt(g * pl[P] / pl[0]), cr = std::sqrt(g * pr[P] / pr[0]);
+  const double sl = std::sqrt(pl[0]), sr = std::sqrt(pr[0]);
+  const double inv = 1 / (sl + sr);
+  double vroe[3] = {0, 0, 0}, vroe2 = 0;
+  for (int d = 0; d < eq.D; ++d) {
+    vroe[d] = (sl * pl[1 + d] + sr * pr[1 + d]) * inv;
+    vroe2 += vroe[d] * vroe[d];
+  }
+  const double H_roe = (sl * Hl + sr * Hr) * inv;
+  const double c_roe = std::sqrt((g - 1) * (H_roe - 0.5 * vroe2));
+  const double beta = std::sqrt(0.5 * (g - 1) / g);
+  const double lmin = std::min({vroe[o] - c_roe, pl[1 + o] - beta * cl, 0.0});
+  const double lmax = std::max({vroe[o] + c_roe, pr[1 + o] + beta * cr, 0.0});
+  double fl[5], fr[5];
+  flux_phys(eq, ul, o, fl);
+  flux_phys(eq, ur, o, fr);
+  if (lmin >= 0 && lmax >= 0) {
+    for (int v = 0; v < eq.NV; ++v) F[v] = fl[v];
+  } else if (lmax <= 0 && lmin <= 0) {
+    for (int v = 0; v < eq.NV; ++v) F[v] = fr[v];
+  } else {
+    const double id = 1 / (lmax - lmin);
+    const double fac_ll = lmax * id, fac_rr = lmin * id, fac_diss = lmin * lmax * id;
+    for (int v = 0; v < eq.NV; ++v) F[v] = fac_ll * fl[v] - fac_rr * fr[v] + fac_diss * (ur[v] - ul[v]);
+  }
+}
+
 // flux_shima_etal, compressible_euler_2d.jl:466-495, 3d analogue
 static inline void flux_shima(const Eq& eq, const double* ul, const double* ur, int o,
                               double* f) {
@@ -591,6 +661,8 @@ static inline void two_point_flux(const Eq& eq, int kind, const double* ul, cons
     case FLUX_LAX_FRIEDRICHS: flux_llf(eq, ul, ur, o, false, f); break;
     case FLUX_LAX_FRIEDRICHS_NAIVE: flux_llf(eq, ul, ur, o, true, f); break;
     case FLUX_HLLC: flux_hllc(eq, ul, ur, o, f); break;
+    case FLUX_CHANDRASHEKAR: flux_chandrashekar(eq, ul, ur, o, f); break;
+    case FLUX_HLLE: flux_hlle(eq, ul, ur, o, f); break;
     default: for (int v = 0; v < eq.NV; ++v) f[v] = NAN;
   }
 }
@@ -723,6 +795,19 @@ static void initial_condition(const Eq& eq, int ic, const double* par, const dou
       v2 = v2 + du * cent1;
       p = p * std::pow(1 + dtemp, eq.gamma / (eq.gamma - 1));
       prim[0] = rho; prim[1] = v1; prim[2] = v2; prim[3] = p;
+      prim2cons(eq, prim, u);
+      return;
+    }
+    case IC_SEDOV_BLAST_WAVE: {
+      // examples/tree_2d_dgsem/elixir_euler_sedov_blast_wave.jl:11-32 (2D)
+      const double r = std::sqrt(x[0] * x[0] + x[1] * x[1]);
+      const double r0 = 0.21875;
+      const double E = 1;
+      const double p_inner = 3 * (eq.gamma - 1) * E / (3 * M_PI * r0 * r0);
+      prim[0] = 1;
+      prim[1] = 0;
+      prim[2] = 0;
+      prim[3] = r > r0 ? 1.0e-5 : p_inner;
       prim2cons(eq, prim, u);
       return;
     }

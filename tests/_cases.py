@@ -15,7 +15,7 @@ def oracle_from_case(O, c, **over):
     vi = dict(weak=O.VI_WEAK, fluxdiff=O.VI_FLUXDIFF, hg=O.VI_SHOCKCAPTURING_HG)[c["vi"]]
     fl = dict(central=O.FLUX_CENTRAL, ranocha=O.FLUX_RANOCHA, shima_etal=O.FLUX_SHIMA_ETAL,
               llf=O.FLUX_LAX_FRIEDRICHS, llf_naive=O.FLUX_LAX_FRIEDRICHS_NAIVE,
-              hllc=O.FLUX_HLLC)
+              hllc=O.FLUX_HLLC, chandrashekar=O.FLUX_CHANDRASHEKAR, hlle=O.FLUX_HLLE)
     src = O.SRC_CONVERGENCE_TEST if c.get("source") == "convergence_test" else O.SRC_NONE
     orc = O.Oracle(c["ndims"], c["polydeg"], c["level"], c["xmin"], c["xmax"],
                    volume_integral=vi, volume_flux=fl[c["volume_flux"]],
@@ -38,4 +38,5 @@ def ic_id(O, name):
                 kelvin_helmholtz=O.IC_KELVIN_HELMHOLTZ, taylor_green=O.IC_TAYLOR_GREEN,
                 gaussian_blast=O.IC_GAUSSIAN_BLAST,
                 isentropic_vortex_advected=O.IC_ISENTROPIC_VORTEX_ADVECTED,
-                blast_wave=O.IC_BLAST_WAVE, density_pulse=O.IC_DENSITY_PULSE)[name]
+                blast_wave=O.IC_BLAST_WAVE, density_pulse=O.IC_DENSITY_PULSE,
+                sedov_blast_wave=O.IC_SEDOV_BLAST_WAVE)[name]

@@ -9,7 +9,9 @@ FLUX = {"central": (T.flux_central, O.FLUX_CENTRAL), "ranocha": (T.flux_ranocha,
         "shima_etal": (T.flux_shima_etal, O.FLUX_SHIMA_ETAL),
         "llf": (T.flux_lax_friedrichs, O.FLUX_LAX_FRIEDRICHS),
         "llf_naive": (T.FluxLaxFriedrichs(T.max_abs_speed_naive), O.FLUX_LAX_FRIEDRICHS_NAIVE),
-        "hllc": (T.flux_hllc, O.FLUX_HLLC)}
+        "hllc": (T.flux_hllc, O.FLUX_HLLC),
+        "chandrashekar": (T.flux_chandrashekar, O.FLUX_CHANDRASHEKAR),
+        "hlle": (T.flux_hlle, O.FLUX_HLLE)}
 IC = {"convergence_test": (lambda p: T.initial_condition_convergence_test, O.IC_CONVERGENCE_TEST),
       "weak_blast_wave": (lambda p: T.initial_condition_weak_blast_wave, O.IC_WEAK_BLAST_WAVE),
       "kelvin_helmholtz": (lambda p: T.initial_condition_kelvin_helmholtz_instability,
@@ -21,6 +23,7 @@ IC = {"convergence_test": (lambda p: T.initial_condition_convergence_test, O.IC_
       "constant": (lambda p: T.initial_condition_constant, O.IC_CONSTANT),
       "blast_wave": (lambda p: T.initial_condition_blast_wave, O.IC_BLAST_WAVE),
       "density_pulse": (lambda p: T.initial_condition_density_pulse, O.IC_DENSITY_PULSE),
+      "sedov_blast_wave": (lambda p: T.initial_condition_sedov_blast_wave, O.IC_SEDOV_BLAST_WAVE),
       "isentropic_vortex_advected": (
           lambda p: T.initial_condition_isentropic_vortex_advected(*(p or [25.0, 5.0])),
           O.IC_ISENTROPIC_VORTEX_ADVECTED),

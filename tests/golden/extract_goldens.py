@@ -18,7 +18,7 @@ import re
 import sys
 
 # Elixir settings transcribed from examples/tree_{2,3}d_dgsem/*.jl.
-# vi: weak | fluxdiff | hg ; fluxes: central | ranocha | shima_etal | llf | llf_naive | hllc
+# vi: weak | fluxdiff | hg ; fluxes: central | ranocha | shima_etal | llf | llf_naive | hllc | chandrashekar | hlle
 CASES = {
     "TreeMesh2D Euler: elixir_euler_source_terms.jl": dict(
         file="test/test_tree_2d_euler.jl",
@@ -157,6 +157,23 @@ CASES = {
         amr=dict(interval=5, adapt_initial_condition=True,
                  adapt_initial_condition_only_refine=True, indicator="max", variable="density",
                  base_level=4, med_level=5, med_threshold=1.05, max_level=6, max_threshold=1.3)),
+    "TreeMesh2D Euler: elixir_euler_sedov_blast_wave.jl": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_sedov_blast_wave.jl",
+        ndims=2, polydeg=3, level=6, xmin=[-2.0, -2.0], xmax=[2.0, 2.0],
+        ic="sedov_blast_wave", source="none", vi="hg", volume_flux="chandrashekar",
+        surface_flux="llf_naive", alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
+        cfl=0.8, tspan=[0.0, 12.5],
+        amr=dict(interval=5, adapt_initial_condition=True,
+                 adapt_initial_condition_only_refine=True, alpha_max=0.5, alpha_min=0.001,
+                 alpha_smooth=True, base_level=4, max_level=6, max_threshold=0.01)),
+    "TreeMesh2D Euler: elixir_euler_sedov_blast_wave.jl (HLLE)": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_sedov_blast_wave.jl",
+        ndims=2, polydeg=3, level=6, xmin=[-2.0, -2.0], xmax=[2.0, 2.0],
+        ic="sedov_blast_wave", source="none", vi="hg", volume_flux="chandrashekar",
+        surface_flux="hlle", alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
+        cfl=0.8, tspan=[0.0, 12.5]),
     "TreeMesh3D Euler: elixir_euler_mortar.jl": dict(
         file="test/test_tree_3d_euler.jl",
         elixir="examples/tree_3d_dgsem/elixir_euler_mortar.jl",

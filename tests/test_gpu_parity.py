@@ -368,9 +368,9 @@ def test_rhs_edge_polydeg_matches_oracle(c, precision, tol):
     assert rel_err(semi.device_context.rhs_host(u, 0.29), orc.rhs(u, 0.29)) < tol
 
 
-# flux_hllc (compressible_euler_{2,3}d.jl) as surface flux and as the FV
-# subcell flux of HG shock capturing
-HLLC_CASES = [
+# flux_hllc, flux_hlle (surface and FV subcell fluxes) and flux_chandrashekar
+# (volume and surface flux), compressible_euler_{2,3}d.jl
+MORE_FLUX_CASES = [
     dict(ndims=2, polydeg=3, level=3, xmin=[-10, -10], xmax=[10, 10], vi="weak",
          surface_flux="hllc", ic="isentropic_vortex_advected", ic_params=[25.0, 5.0]),
     dict(ndims=3, polydeg=3, level=2, xmin=[0] * 3, xmax=[2] * 3, vi="weak", surface_flux="hllc",
@@ -383,13 +383,25 @@ HLLC_CASES = [
          surface_flux="hllc", ic="isentropic_vortex_advected", ic_params=[25.0, 5.0],
          refinement_patches=[dict(type="box", coordinates_min=[0.0, -10.0],
                                   coordinates_max=[10.0, 10.0])]),
+    # flux_chandrashekar volume flux, flux_hlle surface / FV flux
+    dict(ndims=2, polydeg=3, level=3, xmin=[-1, -1], xmax=[1, 1], vi="fluxdiff",
+         volume_flux="chandrashekar", surface_flux="hlle", ic="kelvin_helmholtz"),
+    dict(ndims=3, polydeg=3, level=2, xmin=[0] * 3, xmax=[2] * 3, vi="fluxdiff",
+         volume_flux="chandrashekar", surface_flux="chandrashekar", ic="convergence_test",
+         source="convergence_test"),
+    dict(ndims=2, polydeg=3, level=4, xmin=[-2, -2], xmax=[2, 2], vi="hg",
+         volume_flux="chandrashekar", surface_flux="hlle", ic="weak_blast_wave"),
+    dict(ndims=3, polydeg=2, level=2, xmin=[-2] * 3, xmax=[2] * 3, vi="weak", surface_flux="hlle",
+         ic="weak_blast_wave", refinement_patches=[dict(type="box", coordinates_min=[-1.0] * 3,
+                                                        coordinates_max=[1.0] * 3)]),
 ]
 
 
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 2e-4)])
-@pytest.mark.parametrize("c", HLLC_CASES, ids=[_id(c) + ("-mortar" if c.get("refinement_patches") else "")
-                                              for c in HLLC_CASES])
-def test_rhs_hllc_matches_oracle(c, precision, tol):
+@pytest.mark.parametrize("c", MORE_FLUX_CASES,
+                         ids=[_id(c) + ("-mortar" if c.get("refinement_patches") else "")
+                              for c in MORE_FLUX_CASES])
+def test_rhs_more_fluxes_match_oracle(c, precision, tol):
     semi, orc = build(c, precision=precision)
     u = perturbed_state(semi, seed=13, amp=0.05)
     du_gpu = semi.device_context.rhs_host(u, 0.41)

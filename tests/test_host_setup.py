@@ -60,7 +60,8 @@ def test_treemesh_morton_order_2d():
     (2, "khi", O.IC_KELVIN_HELMHOLTZ), (2, "vortex", O.IC_ISENTROPIC_VORTEX),
     (3, "tgv", O.IC_TAYLOR_GREEN), (2, "constant", O.IC_CONSTANT), (3, "constant", O.IC_CONSTANT),
     (2, "gauss", O.IC_GAUSSIAN_BLAST), (2, "blast", O.IC_BLAST_WAVE),
-    (3, "pulse", O.IC_DENSITY_PULSE), (2, "vortex_advected", O.IC_ISENTROPIC_VORTEX_ADVECTED)])
+    (3, "pulse", O.IC_DENSITY_PULSE), (2, "vortex_advected", O.IC_ISENTROPIC_VORTEX_ADVECTED),
+    (2, "sedov", O.IC_SEDOV_BLAST_WAVE)])
 def test_initial_conditions_match_oracle(ndims, ic, oic):
     funcs = dict(convergence_test=(T.initial_condition_convergence_test, None),
                  weak_blast_wave=(T.initial_condition_weak_blast_wave, None),
@@ -71,6 +72,7 @@ def test_initial_conditions_match_oracle(ndims, ic, oic):
                  gauss=(T.initial_condition_gaussian_blast(1e-5, 1.0, 0.25), [1e-5, 1.0, 0.25]),
                  blast=(T.initial_condition_blast_wave, None),
                  pulse=(T.initial_condition_density_pulse, None),
+                 sedov=(T.initial_condition_sedov_blast_wave, None),
                  vortex_advected=(T.initial_condition_isentropic_vortex_advected(25.0, 5.0),
                                   [25.0, 5.0]))
     f, par = funcs[ic]

@@ -1109,10 +1109,12 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "unknown volume integral %d", cfg->volume_integral);
   const int fl[3] = {cfg->volume_flux, cfg->surface_flux, cfg->volume_flux_fv};
   for (int k = 0; k < 3; ++k)
-    if (fl[k] < 0 || fl[k] > 5) return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "unknown flux %d", fl[k]);
-  if (cfg->volume_flux == TG_FLUX_HLLC && cfg->volume_integral != TG_VOLUME_WEAK_FORM)
+    if (fl[k] < 0 || fl[k] > 7) return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "unknown flux %d", fl[k]);
+  if ((cfg->volume_flux == TG_FLUX_HLLC || cfg->volume_flux == TG_FLUX_HLLE) &&
+      cfg->volume_integral != TG_VOLUME_WEAK_FORM)
     return fail(nullptr, TG_ERR_UNSUPPORTED,
-                "flux_hllc is a surface flux: not a two-point volume flux for flux differencing");
+                "flux_hllc / flux_hlle are surface fluxes: not two-point volume fluxes for flux "
+                "differencing");
   if (cfg->source_terms != TG_SOURCE_NONE && cfg->source_terms != TG_SOURCE_CONVERGENCE_TEST)
     return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "unknown source terms %d", cfg->source_terms);
   if (cfg->precision != TG_PRECISION_FP64 && cfg->precision != TG_PRECISION_MIXED)

@@ -344,6 +344,85 @@ struct Dev {
   }
 
   // KIND >= 0 selects the flux at compile time; KIND < 0 dispatches on `kind`.
+  // flux_chandrashekar(a, b) - f(w_ref).  With beta = q / 2 (q = rho / p) its
+  // energy flux is f1 (igm1 / q_ln + v_a . v_b / 2) + p_mean v_avg,o: the
+  // enthalpy term of flux_ranocha, with p_mean = rho_avg / q_avg in place of the
+  // arithmetic mean pressure, so p_mean - p_ref = (rq_ref + drho_avg -
+  // p_ref dq_avg) / q_avg in deviations.
+  static __host__ __device__ __forceinline__ void dchandrashekar(const RefState<D>& R,
+                                                         const Node<D>& a, const Node<D>& b,
+                                                         int o, float vro, const EosF& eos,
+                                                         float* f) {
+    const float igm1 = eos.igm1;
+    const float drho_ln = dev_ln_mean(R.rho, a.dw[0], b.dw[0], a.w[0], b.w[0]);
+    const float dq_ln = dev_ln_mean(R.q, a.dq, b.dq, R.q + a.dq, R.q + b.dq);
+    const float q_ln = R.q + dq_ln;
+    const float dq_avg = 0.5f * (a.dq + b.dq);
+    const float dp_mean = (R.rq + 0.5f * (a.dw[0] + b.dw[0]) - R.p * dq_avg) / (R.q + dq_avg);
+    float dvavg[D], vavg[D];
+    float dvsq = 0, vsq = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      dvavg[d] = 0.5f * (a.dw[1 + d] + b.dw[1 + d]);
+      vavg[d] = R.v[d] + dvavg[d];
+      dvsq += R.v[d] * (a.dw[1 + d] + b.dw[1 + d]) + a.dw[1 + d] * b.dw[1 + d];
+      vsq += a.w[1 + d] * b.w[1 + d];
+    }
+    dvsq *= 0.5f;
+    const float F1r = R.rho * vro;
+    const float dvavgo = 0.5f * (a.dvo + b.dvo);
+    const float d1 = R.rho * dvavgo + drho_ln * (vro + dvavgo);
+    f[0] = d1;
+#pragma unroll
+    for (int d = 0; d < D; ++d) f[1 + d] = d1 * vavg[d] + F1r * dvavg[d] + ((d == o) ? dp_mean : 0.0f);
+    const float H = 0.5f * vsq + igm1 / q_ln;
+    const float dH = dvsq + igm1 * (R.rq - R.p * dq_ln) / (R.rho * q_ln);
+    f[P] = d1 * H + F1r * dH + (R.p * dvavgo + dp_mean * (vro + dvavgo));
+  }
+
+  // flux_hlle(a, b) - f(w_ref): FluxHLL with min_max_speed_einfeldt
+  // (numerical_fluxes.jl:422-457, compressible_euler_2d.jl:1925-1963).  The
+  // HLL combination is linear in the two physical fluxes, so it is exact in
+  // their deviations and in the conservative deviations b.du - a.du.
+  static __host__ __device__ __forceinline__ void dhlle(const RefState<D>& R, const Node<D>& a,
+                                                const Node<D>& b, int o, float vro,
+                                                const EosF& eos, float* f) {
+    const float g = eos.gamma;
+    const float rl = a.w[0], rr = b.w[0], pl = a.w[P], pr = b.w[P];
+    const float cl = sqrtf(g * pl / rl), cr = sqrtf(g * pr / rr);
+    const float sl = sqrtf(rl), sr = sqrtf(rr), iss = 1.0f / (sl + sr);
+    float vroe2 = 0, kl = 0, kr = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const float vr = (sl * a.w[1 + d] + sr * b.w[1 + d]) * iss;
+      vroe2 += vr * vr;
+      kl += a.w[1 + d] * a.w[1 + d];
+      kr += b.w[1 + d] * b.w[1 + d];
+    }
+    const float vroe_o = (sl * a.vo + sr * b.vo) * iss;
+    const float Hl = (pl * eos.gigm1 + 0.5f * rl * kl) / rl;
+    const float Hr = (pr * eos.gigm1 + 0.5f * rr * kr) / rr;
+    const float c_roe = sqrtf(eos.pressure((sl * Hl + sr * Hr) * iss - 0.5f * vroe2));
+    const float beta = sqrtf(0.5f * eos.gm1 / g);
+    const float lmin = fminf(fminf(vroe_o - c_roe, a.vo - beta * cl), 0.0f);
+    const float lmax = fmaxf(fmaxf(vroe_o + c_roe, b.vo + beta * cr), 0.0f);
+    if (lmin >= 0.0f && lmax >= 0.0f) {
+      dflux(R, a, o, vro, eos, f);
+      return;
+    }
+    if (lmax <= 0.0f && lmin <= 0.0f) {
+      dflux(R, b, o, vro, eos, f);
+      return;
+    }
+    float fb[NV];
+    dflux(R, a, o, vro, eos, f);
+    dflux(R, b, o, vro, eos, fb);
+    const float id = 1.0f / (lmax - lmin);
+    const float ca = lmax * id, cb = lmin * id, cd = lmin * lmax * id;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) f[v] = ca * f[v] - cb * fb[v] + cd * (b.du[v] - a.du[v]);
+  }
+
   // flux_hllc(a, b) - f(w_ref) (compressible_euler_2d.jl:1720-1816, 3d.jl:1423-1541).
   // Signal speeds from the full primitives (they only weight the terms).  The
   // outer branches are physical-flux deviations; the star-state correction is
@@ -415,6 +494,8 @@ struct Dev {
     else if constexpr (KIND == FLUX_LLF_NAIVE) dllf(R, a, b, o, vro, true, eos, f);
     else if constexpr (KIND == FLUX_CENTRAL) dcentral(R, a, b, o, vro, eos, f);
     else if constexpr (KIND == FLUX_HLLC) dhllc(R, a, b, o, vro, eos, f);
+    else if constexpr (KIND == FLUX_CHANDRASHEKAR) dchandrashekar(R, a, b, o, vro, eos, f);
+    else if constexpr (KIND == FLUX_HLLE) dhlle(R, a, b, o, vro, eos, f);
     else two_point(kind, R, a, b, o, vro, eos, f);
   }
 
@@ -427,6 +508,8 @@ struct Dev {
       case FLUX_LLF: dllf(R, a, b, o, vro, false, eos, f); break;
       case FLUX_LLF_NAIVE: dllf(R, a, b, o, vro, true, eos, f); break;
       case FLUX_HLLC: dhllc(R, a, b, o, vro, eos, f); break;
+      case FLUX_CHANDRASHEKAR: dchandrashekar(R, a, b, o, vro, eos, f); break;
+      case FLUX_HLLE: dhlle(R, a, b, o, vro, eos, f); break;
       default: dcentral(R, a, b, o, vro, eos, f); break;
     }
   }

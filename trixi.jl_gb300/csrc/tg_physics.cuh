@@ -19,7 +19,9 @@ enum FluxKind {
   FLUX_SHIMA_ETAL = 2,
   FLUX_LLF = 3,
   FLUX_LLF_NAIVE = 4,
-  FLUX_HLLC = 5
+  FLUX_HLLC = 5,
+  FLUX_CHANDRASHEKAR = 6,
+  FLUX_HLLE = 7
 };
 enum SourceKind { SRC_NONE = 0, SRC_CONVERGENCE_TEST = 1 };
 // boundary conditions of a non-periodic TreeMesh, per direction
@@ -159,6 +161,74 @@ struct Euler {
            R(0.5) * (wl[P] * pick(wr + 1, o) + wr[P] * pick(wl + 1, o));
   }
 
+  // flux_chandrashekar, compressible_euler_2d.jl (orientation method), 3d.jl:640-692
+  static __host__ __device__ __forceinline__ void flux_chandrashekar(const R* wl, const R* wr, int o,
+                                                             R inv_gm1, R* f) {
+    const R beta_ll = R(0.5) * wl[0] / wl[P], beta_rr = R(0.5) * wr[0] / wr[P];
+    R kin = 0, vavg[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      kin += wl[1 + d] * wl[1 + d] + wr[1 + d] * wr[1 + d];
+      vavg[d] = R(0.5) * (wl[1 + d] + wr[1 + d]);
+    }
+    const R rho_mean = ln_mean(wl[0], wr[0]);
+    const R beta_mean = ln_mean(beta_ll, beta_rr);
+    const R p_mean = R(0.5) * (R(0.5) * (wl[0] + wr[0])) / (R(0.5) * (beta_ll + beta_rr));
+    const R f1 = rho_mean * pick(vavg, o);
+    f[0] = f1;
+    R e = f1 * R(0.5) * (inv_gm1 / beta_mean - R(0.5) * kin);
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      f[1 + d] = (d == o) ? f1 * vavg[d] + p_mean : f1 * vavg[d];
+      e += f[1 + d] * vavg[d];
+    }
+    f[P] = e;
+  }
+
+  // flux_hlle = FluxHLL(min_max_speed_einfeldt): numerical_fluxes.jl:422-457,
+  // compressible_euler_2d.jl:1925-1963 (3d analogue)
+  static __host__ __device__ __forceinline__ void flux_hlle(const R* ul, const R* wl, const R* ur,
+                                                    const R* wr, int o, R gamma, R* F) {
+    R lmin, lmax;
+    einfeldt(ul, wl, ur, wr, o, gamma, lmin, lmax);
+    if (lmin >= R(0) && lmax >= R(0)) {
+      flux(ul, wl, o, F);
+      return;
+    }
+    if (lmax <= R(0) && lmin <= R(0)) {
+      flux(ur, wr, o, F);
+      return;
+    }
+    R fl[NV], fr[NV];
+    flux(ul, wl, o, fl);
+    flux(ur, wr, o, fr);
+    const R id = R(1) / (lmax - lmin);
+    const R a = lmax * id, b = lmin * id, c = lmin * lmax * id;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) F[v] = a * fl[v] - b * fr[v] + c * (ur[v] - ul[v]);
+  }
+
+  // min_max_speed_einfeldt, compressible_euler_2d.jl:1925-1963
+  static __host__ __device__ __forceinline__ void einfeldt(const R* ul, const R* wl, const R* ur,
+                                                   const R* wr, int o, R gamma, R& lmin, R& lmax) {
+    const R Hl = (ul[P] + wl[P]) / wl[0], Hr = (ur[P] + wr[P]) / wr[0];
+    const R cl = Real<R>::sqrt(gamma * wl[P] / wl[0]), cr = Real<R>::sqrt(gamma * wr[P] / wr[0]);
+    const R sl = Real<R>::sqrt(wl[0]), sr = Real<R>::sqrt(wr[0]);
+    const R inv = R(1) / (sl + sr);
+    R vroe2 = 0, vroe_o = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const R vr = (sl * wl[1 + d] + sr * wr[1 + d]) * inv;
+      vroe2 += vr * vr;
+      if (d == o) vroe_o = vr;
+    }
+    const R H_roe = (sl * Hl + sr * Hr) * inv;
+    const R c_roe = Real<R>::sqrt((gamma - R(1)) * (H_roe - R(0.5) * vroe2));
+    const R beta = Real<R>::sqrt(R(0.5) * (gamma - R(1)) / gamma);
+    lmin = fmin(fmin(vroe_o - c_roe, pick(wl + 1, o) - beta * cl), R(0));
+    lmax = fmax(fmax(vroe_o + c_roe, pick(wr + 1, o) + beta * cr), R(0));
+  }
+
   // flux_shima_etal, compressible_euler_2d.jl:466-495
   static __host__ __device__ __forceinline__ void flux_shima(const R* wl, const R* wr, int o, R inv_gm1,
                                                      R* f) {
@@ -258,6 +328,8 @@ struct Euler {
       case FLUX_LLF: flux_llf(ul, wl, ur, wr, o, false, gamma, f); break;
       case FLUX_LLF_NAIVE: flux_llf(ul, wl, ur, wr, o, true, gamma, f); break;
       case FLUX_HLLC: flux_hllc(ul, wl, ur, wr, o, gamma, f); break;
+      case FLUX_CHANDRASHEKAR: flux_chandrashekar(wl, wr, o, inv_gm1, f); break;
+      case FLUX_HLLE: flux_hlle(ul, wl, ur, wr, o, gamma, f); break;
       default: flux_central(ul, wl, ur, wr, o, f); break;
     }
   }

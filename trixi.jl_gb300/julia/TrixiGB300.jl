@@ -58,11 +58,15 @@ end
 const TG_VOLUME_WEAK_FORM, TG_VOLUME_FLUX_DIFFERENCING, TG_VOLUME_SHOCK_CAPTURING_HG = 0, 1, 2
 const TG_FLUX_CENTRAL, TG_FLUX_RANOCHA, TG_FLUX_SHIMA_ETAL = 0, 1, 2
 const TG_FLUX_LAX_FRIEDRICHS, TG_FLUX_LAX_FRIEDRICHS_NAIVE, TG_FLUX_HLLC = 3, 4, 5
+const TG_FLUX_CHANDRASHEKAR, TG_FLUX_HLLE = 6, 7
 
 flux_code(::typeof(Trixi.flux_central)) = TG_FLUX_CENTRAL
 flux_code(::typeof(Trixi.flux_ranocha)) = TG_FLUX_RANOCHA
 flux_code(::typeof(Trixi.flux_shima_etal)) = TG_FLUX_SHIMA_ETAL
 flux_code(::typeof(Trixi.flux_hllc)) = TG_FLUX_HLLC
+flux_code(::typeof(Trixi.flux_chandrashekar)) = TG_FLUX_CHANDRASHEKAR
+flux_code(f::Trixi.FluxHLL) = f.min_max_speed === Trixi.min_max_speed_einfeldt ? TG_FLUX_HLLE :
+                              error("FluxHLL: only min_max_speed_einfeldt (flux_hlle) is on the GPU path")
 function flux_code(f::Trixi.FluxLaxFriedrichs)
     f.dissipation.max_abs_speed === Trixi.max_abs_speed_naive ?
     TG_FLUX_LAX_FRIEDRICHS_NAIVE : TG_FLUX_LAX_FRIEDRICHS

@@ -21,7 +21,7 @@ STATUS_NAMES = {-1: "invalid argument", -2: "unsupported", -3: "CUDA error",
 # enums (trixi_gb300.h)
 TG_VOLUME_WEAK_FORM, TG_VOLUME_FLUX_DIFFERENCING, TG_VOLUME_SHOCK_CAPTURING_HG = 0, 1, 2
 (TG_FLUX_CENTRAL, TG_FLUX_RANOCHA, TG_FLUX_SHIMA_ETAL, TG_FLUX_LAX_FRIEDRICHS,
- TG_FLUX_LAX_FRIEDRICHS_NAIVE, TG_FLUX_HLLC) = range(6)
+ TG_FLUX_LAX_FRIEDRICHS_NAIVE, TG_FLUX_HLLC, TG_FLUX_CHANDRASHEKAR, TG_FLUX_HLLE) = range(8)
 TG_SOURCE_NONE, TG_SOURCE_CONVERGENCE_TEST = 0, 1
 TG_PRECISION_FP64, TG_PRECISION_MIXED = 0, 1
 TG_BOUNDARY_PERIODIC, TG_BOUNDARY_DIRICHLET, TG_BOUNDARY_SLIP_WALL = 0, 1, 2

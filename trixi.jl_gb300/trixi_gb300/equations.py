@@ -50,6 +50,10 @@ flux_ranocha = _Flux("flux_ranocha", _lib.TG_FLUX_RANOCHA)
 flux_shima_etal = _Flux("flux_shima_etal", _lib.TG_FLUX_SHIMA_ETAL)
 # flux_hllc, compressible_euler_2d.jl:1720-1816 (a surface flux)
 flux_hllc = _Flux("flux_hllc", _lib.TG_FLUX_HLLC)
+# flux_chandrashekar, compressible_euler_2d.jl, 3d.jl:640-692
+flux_chandrashekar = _Flux("flux_chandrashekar", _lib.TG_FLUX_CHANDRASHEKAR)
+# flux_hlle = FluxHLL(min_max_speed_einfeldt), numerical_fluxes.jl:422-457 (a surface flux)
+flux_hlle = _Flux("flux_hlle", _lib.TG_FLUX_HLLE)
 
 
 class _MaxAbsSpeed:
@@ -175,6 +179,20 @@ def initial_condition_isentropic_vortex_advected(p_inf=25.0, amplitude=5.0):
     ic.__name__ = "initial_condition_isentropic_vortex_advected"
     ic.params = (float(p_inf), float(amplitude))
     return ic
+
+
+def initial_condition_sedov_blast_wave(x, t, equations):
+    """examples/tree_2d_dgsem/elixir_euler_sedov_blast_wave.jl:11-32: energy 1 in a
+    disc of radius 0.21875 at rest in a background at p = 1e-5."""
+    if equations.ndims != 2:
+        raise NotImplementedError("initial_condition_sedov_blast_wave is the 2D elixir's")
+    r = np.sqrt(x[..., 0] ** 2 + x[..., 1] ** 2)
+    r0, E = 0.21875, 1.0
+    p_inner = 3 * (equations.gamma - 1) * E / (3 * math.pi * r0 ** 2)
+    prim = np.zeros(x.shape[:-1] + (4,))
+    prim[..., 0] = 1.0
+    prim[..., 3] = np.where(r > r0, 1.0e-5, p_inner)
+    return prim2cons(prim, equations)
 
 
 def initial_condition_density_pulse(x, t, equations):
