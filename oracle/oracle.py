@@ -27,7 +27,8 @@ SRC_NONE, SRC_CONVERGENCE_TEST = 0, 1
 BC_PERIODIC, BC_DIRICHLET, BC_SLIP_WALL = 0, 1, 2
 (IC_CONSTANT, IC_CONVERGENCE_TEST, IC_ISENTROPIC_VORTEX, IC_WEAK_BLAST_WAVE,
  IC_KELVIN_HELMHOLTZ, IC_TAYLOR_GREEN, IC_GAUSSIAN_BLAST,
- IC_ISENTROPIC_VORTEX_ADVECTED, IC_BLAST_WAVE, IC_DENSITY_PULSE, IC_SEDOV_BLAST_WAVE) = range(11)
+ IC_ISENTROPIC_VORTEX_ADVECTED, IC_BLAST_WAVE, IC_DENSITY_PULSE, IC_SEDOV_BLAST_WAVE,
+ IC_DENSITY_WAVE) = range(12)
 
 _lib = None
 

@@ -58,6 +58,7 @@ enum InitialCondition {
   IC_BLAST_WAVE = 8,
   IC_DENSITY_PULSE = 9,
   IC_SEDOV_BLAST_WAVE = 10,
+  IC_DENSITY_WAVE = 11,
 };
 
 // ---------------------------------------------------------------------------
@@ -796,6 +797,16 @@ static void initial_condition(const Eq& eq, int ic, const double* par, const dou
       p = p * std::pow(1 + dtemp, eq.gamma / (eq.gamma - 1));
       prim[0] = rho; prim[1] = v1; prim[2] = v2; prim[3] = p;
       prim2cons(eq, prim, u);
+      return;
+    }
+    case IC_DENSITY_WAVE: {
+      // initial_condition_density_wave, compressible_euler_2d.jl:161-171 (2D)
+      const double v1 = 0.1, v2 = 0.2;
+      const double rho = 1 + 0.98 * sinpi(2 * (x[0] + x[1] - t * (v1 + v2)));
+      u[0] = rho;
+      u[1] = rho * v1;
+      u[2] = rho * v2;
+      u[3] = 20 / (eq.gamma - 1) + 0.5 * rho * (v1 * v1 + v2 * v2);
       return;
     }
     case IC_SEDOV_BLAST_WAVE: {

@@ -39,4 +39,4 @@ def ic_id(O, name):
                 gaussian_blast=O.IC_GAUSSIAN_BLAST,
                 isentropic_vortex_advected=O.IC_ISENTROPIC_VORTEX_ADVECTED,
                 blast_wave=O.IC_BLAST_WAVE, density_pulse=O.IC_DENSITY_PULSE,
-                sedov_blast_wave=O.IC_SEDOV_BLAST_WAVE)[name]
+                sedov_blast_wave=O.IC_SEDOV_BLAST_WAVE, density_wave=O.IC_DENSITY_WAVE)[name]

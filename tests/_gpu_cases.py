@@ -24,6 +24,7 @@ IC = {"convergence_test": (lambda p: T.initial_condition_convergence_test, O.IC_
       "blast_wave": (lambda p: T.initial_condition_blast_wave, O.IC_BLAST_WAVE),
       "density_pulse": (lambda p: T.initial_condition_density_pulse, O.IC_DENSITY_PULSE),
       "sedov_blast_wave": (lambda p: T.initial_condition_sedov_blast_wave, O.IC_SEDOV_BLAST_WAVE),
+      "density_wave": (lambda p: T.initial_condition_density_wave, O.IC_DENSITY_WAVE),
       "isentropic_vortex_advected": (
           lambda p: T.initial_condition_isentropic_vortex_advected(*(p or [25.0, 5.0])),
           O.IC_ISENTROPIC_VORTEX_ADVECTED),

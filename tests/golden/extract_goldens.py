@@ -174,6 +174,63 @@ CASES = {
         ic="sedov_blast_wave", source="none", vi="hg", volume_flux="chandrashekar",
         surface_flux="hlle", alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
         cfl=0.8, tspan=[0.0, 12.5]),
+    "TreeMesh2D Euler: elixir_euler_blast_wave.jl": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_blast_wave.jl",
+        ndims=2, polydeg=3, level=6, xmin=[-2.0, -2.0], xmax=[2.0, 2.0],
+        ic="blast_wave", source="none", vi="hg", volume_flux="ranocha",
+        surface_flux="llf_naive", alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
+        cfl=0.9, tspan=[0.0, 12.5]),
+    "TreeMesh2D Euler: elixir_euler_vortex_shockcapturing.jl": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_vortex_shockcapturing.jl",
+        ndims=2, polydeg=3, level=4, xmin=[-10.0, -10.0], xmax=[10.0, 10.0],
+        ic="isentropic_vortex", ic_params=[25.0, 5.0], source="none", vi="hg",
+        volume_flux="shima_etal", surface_flux="llf_naive", alpha_max=0.5, alpha_min=0.001,
+        alpha_smooth=True, cfl=0.7, tspan=[0.0, 1.0]),
+    "TreeMesh2D Euler: elixir_euler_density_wave.jl": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_density_wave.jl",
+        ndims=2, polydeg=5, level=2, xmin=[-1.0, -1.0], xmax=[1.0, 1.0],
+        ic="density_wave", source="none", vi="weak", volume_flux="central",
+        surface_flux="central", cfl=1.6, tspan=[0.0, 2.0]),
+    "TreeMesh2D Euler: elixir_euler_ec.jl with flux_chandrashekar": dict(
+        file="test/test_tree_2d_euler.jl",
+        elixir="examples/tree_2d_dgsem/elixir_euler_ec.jl",
+        ndims=2, polydeg=3, level=5, xmin=[-2.0, -2.0], xmax=[2.0, 2.0],
+        ic="weak_blast_wave", source="none", vi="fluxdiff", volume_flux="chandrashekar",
+        surface_flux="chandrashekar", cfl=1.0, tspan=[0.0, 0.4]),
+    "TreeMesh3D Euler: elixir_euler_ec.jl with flux_chandrashekar": dict(
+        file="test/test_tree_3d_euler.jl",
+        elixir="examples/tree_3d_dgsem/elixir_euler_ec.jl",
+        ndims=3, polydeg=3, level=3, xmin=[-2.0] * 3, xmax=[2.0] * 3,
+        ic="weak_blast_wave", source="none", vi="fluxdiff", volume_flux="chandrashekar",
+        surface_flux="chandrashekar", cfl=1.3, tspan=[0.0, 0.4]),
+    "TreeMesh3D Euler: elixir_euler_ec.jl with flux_shima_etal": dict(
+        file="test/test_tree_3d_euler.jl",
+        elixir="examples/tree_3d_dgsem/elixir_euler_ec.jl",
+        ndims=3, polydeg=3, level=3, xmin=[-2.0] * 3, xmax=[2.0] * 3,
+        ic="weak_blast_wave", source="none", vi="fluxdiff", volume_flux="shima_etal",
+        surface_flux="shima_etal", cfl=1.3, tspan=[0.0, 0.4]),
+    "TreeMesh3D Euler: elixir_euler_ec.jl with initial_condition=initial_condition_constant": dict(
+        file="test/test_tree_3d_euler.jl",
+        elixir="examples/tree_3d_dgsem/elixir_euler_ec.jl",
+        ndims=3, polydeg=3, level=3, xmin=[-2.0] * 3, xmax=[2.0] * 3,
+        ic="constant", source="none", vi="fluxdiff", volume_flux="ranocha",
+        surface_flux="ranocha", cfl=1.3, tspan=[0.0, 0.4]),
+    "TreeMesh3D Euler: elixir_euler_shockcapturing.jl": dict(
+        file="test/test_tree_3d_euler.jl",
+        elixir="examples/tree_3d_dgsem/elixir_euler_shockcapturing.jl",
+        ndims=3, polydeg=3, level=3, xmin=[-2.0] * 3, xmax=[2.0] * 3,
+        ic="weak_blast_wave", source="none", vi="hg", volume_flux="ranocha",
+        surface_flux="ranocha", alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
+        cfl=1.4, tspan=[0.0, 0.4]),
+    "TreeMesh3D Euler: elixir_euler_density_pulse.jl": dict(
+        file="test/test_tree_3d_euler.jl",
+        elixir="examples/tree_3d_dgsem/elixir_euler_density_pulse.jl",
+        ndims=3, polydeg=3, level=3, xmin=[-2.0] * 3, xmax=[2.0] * 3,
+        ic="density_pulse", source="none", vi="fluxdiff", volume_flux="ranocha",
+        surface_flux="ranocha", cfl=1.1, tspan=[0.0, 0.4]),
     "TreeMesh3D Euler: elixir_euler_mortar.jl": dict(
         file="test/test_tree_3d_euler.jl",
         elixir="examples/tree_3d_dgsem/elixir_euler_mortar.jl",

@@ -155,32 +155,40 @@ def test_rk_stage_matches_oracle():
 
 
 GOLDENS = load_goldens()
-GOLDEN_NAMES = sorted(k for k in GOLDENS if "maxiters" not in GOLDENS[k]
-                      and "amr" not in GOLDENS[k])  # AMR goldens: test_gpu_amr.py
+# AMR goldens: test_gpu_amr.py; constant initial conditions (free stream): below
+GOLDEN_NAMES = sorted(k for k in GOLDENS if "amr" not in GOLDENS[k]
+                      and GOLDENS[k]["ic"] != "constant")
+FREE_STREAM_GOLDENS = sorted(k for k in GOLDENS if GOLDENS[k]["ic"] == "constant")
+
+
+def _golden_run(c):
+    semi, _ = build(c)
+    ode = T.semidiscretize(semi, c["tspan"])
+    ana = T.AnalysisCallback(semi)
+    sol = T.solve(ode, T.CarpenterKennedy2N54(williamson_condition=False), dt=1.0,
+                  maxiters=c.get("maxiters", 10 ** 12),
+                  callback=T.CallbackSet(T.StepsizeCallback(cfl=c["cfl"]), ana))
+    return sol, ana
 
 
 @pytest.mark.parametrize("name", GOLDEN_NAMES)
 def test_gpu_fp64_reproduces_trixi_goldens(name):
     c = dict(GOLDENS[name])
-    semi, _ = build(c)
-    ode = T.semidiscretize(semi, c["tspan"])
-    ana = T.AnalysisCallback(semi)
-    sol = T.solve(ode, T.CarpenterKennedy2N54(williamson_condition=False), dt=1.0,
-                  callback=T.CallbackSet(T.StepsizeCallback(cfl=c["cfl"]), ana))
-    assert sol.t[-1] == pytest.approx(c["tspan"][1], rel=1e-14)
+    sol, ana = _golden_run(c)
+    if "maxiters" in c:
+        assert sol.nsteps == c["maxiters"]
+    else:
+        assert sol.t[-1] == pytest.approx(c["tspan"][1], rel=1e-14)
     np.testing.assert_allclose(ana.l2, c["l2"], rtol=1e-8)
     np.testing.assert_allclose(ana.linf, c["linf"], rtol=1e-7)
 
 
-def test_gpu_free_stream_golden_one_step():
-    name = "TreeMesh2D Euler: elixir_euler_vortex.jl one step with initial_condition_constant"
-    c = dict(GOLDENS[name])
-    semi, _ = build(c)
-    ode = T.semidiscretize(semi, c["tspan"])
-    ana = T.AnalysisCallback(semi)
-    T.solve(ode, T.CarpenterKennedy2N54(), dt=1.0, maxiters=1,
-            callback=T.CallbackSet(T.StepsizeCallback(cfl=c["cfl"]), ana))
+@pytest.mark.parametrize("name", FREE_STREAM_GOLDENS)
+def test_gpu_free_stream_goldens(name):
+    # the goldens are round-off (~1e-16): compare absolutely
+    _, ana = _golden_run(dict(GOLDENS[name]))
     assert np.all(ana.l2 < 1e-14) and np.all(ana.linf < 1e-13)
+    assert np.allclose(ana.l2, GOLDENS[name]["l2"], atol=5e-15, rtol=0)
 
 
 @pytest.mark.parametrize("name", ["TreeMesh3D Euler: elixir_euler_source_terms.jl",

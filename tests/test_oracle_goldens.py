@@ -28,7 +28,7 @@ def test_oracle_reproduces_trixi_golden(oracle_mod, name):
         u, t, nsteps = orc.solve(u0, c["tspan"][0], c["tspan"][1], c["cfl"],
                                  max_steps=c.get("maxiters", 10**9))
     l2, linf = orc.error_norms(u, t, ic, par)
-    if "maxiters" in c and not c.get("amr"):
+    if c["ic"] == "constant":
         # free-stream preservation: goldens are round-off (~1e-16); compare absolutely
         assert np.all(l2 < 1e-14) and np.all(linf < 1e-13)
         assert np.allclose(l2, c["l2"], atol=5e-15, rtol=0)

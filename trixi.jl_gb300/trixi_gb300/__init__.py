@@ -20,7 +20,8 @@ the host side: mesh/basis setup, the C-ABI binding and the driver loop.
 from ._lib import TrixiGB300Error, load as load_library  # noqa: F401
 from .analysis import calc_error_norms  # noqa: F401
 from .basis import LobattoLegendreAnalyzer, LobattoLegendreBasis, MortarL2  # noqa: F401
-from .equations import (flux_chandrashekar, flux_hlle, initial_condition_sedov_blast_wave,  # noqa: F401
+from .equations import (initial_condition_density_wave,  # noqa: F401
+                        flux_chandrashekar, flux_hlle, initial_condition_sedov_blast_wave,  # noqa: F401
                         flux_hllc, initial_condition_isentropic_vortex_advected,  # noqa: F401
                         initial_condition_density_pulse,  # noqa: F401
                         initial_condition_blast_wave,  # noqa: F401

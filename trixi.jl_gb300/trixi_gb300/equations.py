@@ -181,6 +181,22 @@ def initial_condition_isentropic_vortex_advected(p_inf=25.0, amplitude=5.0):
     return ic
 
 
+def initial_condition_density_wave(x, t, equations):
+    """initial_condition_density_wave, compressible_euler_2d.jl:161-171: a density
+    sine wave advected with velocity (0.1, 0.2) at pressure 20 (exact at every t)."""
+    if equations.ndims != 2:
+        raise NotImplementedError("initial_condition_density_wave is 2D")
+    v1, v2 = 0.1, 0.2
+    a = 2 * (x[..., 0] + x[..., 1] - t * (v1 + v2))
+    rho = 1 + 0.98 * _sinpi(a)
+    u = np.empty(x.shape[:-1] + (4,))
+    u[..., 0] = rho
+    u[..., 1] = rho * v1
+    u[..., 2] = rho * v2
+    u[..., 3] = 20 / (equations.gamma - 1) + 0.5 * rho * (v1 ** 2 + v2 ** 2)
+    return u
+
+
 def initial_condition_sedov_blast_wave(x, t, equations):
     """examples/tree_2d_dgsem/elixir_euler_sedov_blast_wave.jl:11-32: energy 1 in a
     disc of radius 0.21875 at rest in a background at p = 1e-5."""
