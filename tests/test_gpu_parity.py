@@ -191,9 +191,14 @@ def test_gpu_free_stream_goldens(name):
     assert np.allclose(ana.l2, GOLDENS[name]["l2"], atol=5e-15, rtol=0)
 
 
+# every golden with a smooth exact solution (errors against it measure accuracy)
 @pytest.mark.parametrize("name", ["TreeMesh3D Euler: elixir_euler_source_terms.jl",
+                                  "TreeMesh3D Euler: elixir_euler_source_terms.jl with split_form",
                                   "TreeMesh2D Euler: elixir_euler_source_terms.jl",
-                                  "TreeMesh2D Euler: elixir_euler_source_terms_nonperiodic.jl"])
+                                  "TreeMesh2D Euler: elixir_euler_source_terms_nonperiodic.jl",
+                                  "TreeMesh2D Euler: elixir_euler_density_wave.jl",
+                                  "TreeMesh3D Euler: elixir_euler_density_pulse.jl",
+                                  "TreeMesh2D Euler: elixir_euler_vortex.jl"])
 def test_mixed_precision_error_within_1p1x_of_fp64(name):
     c = dict(GOLDENS[name])
     errs = {}
