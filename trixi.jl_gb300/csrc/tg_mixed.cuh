@@ -568,11 +568,7 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // global reads of a block (state chunk, u_tmp chunk and the neighbour traces
 // of faces between blocks) are issued up front as cp.async copies.
 // Position of node n of block slot `slot` inside one SoA field of the node
-// arrays.  For 3D polydeg 3 (the production case) the slot stride is 80
-// (= 16 mod 32) with 4 words of padding after every 16 nodes: then the 32
-// lanes of a warp (2 elements x 16 lines of one direction) hit 32 distinct
-// banks for y- and z-lines, and an x-line's 4 nodes stay contiguous and
-// 16-byte aligned so it reads each field with one 128-bit load.
+// arrays (for 3D polydeg 3, the production case, see pos()).
 template <int D, int N, int EPB>
 struct NodeLayout {
   static constexpr int NN = Pow<N, D>::value;
@@ -580,7 +576,15 @@ struct NodeLayout {
   static constexpr int SS = PADDED ? 80 : NN;
   static constexpr int FS = PADDED ? EPB * 80 : EPB * NN + 1;  // field stride
   static __host__ __device__ __forceinline__ int pos(int slot, int n) {
-    return PADDED ? slot * SS + n + 4 * (n >> 4) : slot * SS + n;
+    // 3D, N = 4: an XOR swizzle of bits 2-3 of the node index by bits 4-5
+    // (a permutation of each element's 64 nodes) with an 80-float element
+    // stride.  A warp holds 16 lines of one direction of two elements: with it
+    // the node-field reads and partial-sum writes of x-lines (float4), y- and
+    // z-lines (scalar) and the node phase (32 consecutive nodes) each take one
+    // shared-memory wavefront, and the 4 nodes of an x-line stay contiguous
+    // and 16-byte aligned.
+    return PADDED ? slot * SS + (n ^ (((n >> 4) & 1) << 2) ^ (((n >> 5) & 1) << 3))
+                  : slot * SS + n;
   }
 };
 
