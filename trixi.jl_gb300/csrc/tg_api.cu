@@ -520,30 +520,35 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-// Mortar pre-pass of a mixed context: the same fluxes as mortar_flux_kernel
-// with the two linear projections in FP32 on deviations.  The large trace is
-// split into a float-float reference (its first face node) and FP32
-// deviations; forward_{lower,upper} act on the deviations only, which is exact
-// to FP32 rounding of the deviations because every row sums to one.  The
-// surface flux is taken in FP64 on reference + projected deviation, and the
-// small faces' fluxes go back through reverse_{lower,upper} as deviations
-// from the flux at the first small node (the reverse rows of all small faces
-// together sum to one).  mat32: the four matrices in FP32, row-major.
+// Mortar pre-pass of a mixed context: the fluxes of mortar_flux_kernel in the
+// mixed kernel's deviation form.  The large element's first face node is the
+// reference (Dev::make_ref on its hi part); every other state is a deviation
+// from it: the large trace's in FP32, forward_{lower,upper} acting on those
+// deviations (exact to their FP32 rounding, every row sums to one), and the
+// small traces through Dev::make_node.  The surface flux is the element
+// kernel's (Dev::two_point, F - f(w_ref)); f(w_ref) is added back in FP64 and
+// reverse_{lower,upper} project the deviations F - f(w_ref) (the reverse
+// rows of all small faces together sum to one).  mat32: the four matrices in
+// FP32, row-major.
 template <int D>
 __global__ void __launch_bounds__(128)
-    mortar_flux_ff_kernel(const DgParams P, const float2* __restrict__ u,
+    mortar_flux_ff_kernel(const MixedParams P, const float2* __restrict__ u,
                           const int32_t* __restrict__ mtab, const float* __restrict__ mat32,
                           int64_t M, int N, int64_t ff_offset, float2* __restrict__ outff) {
-  constexpr int NV = D + 2, NS = 1 << (D - 1);
+  constexpr int NV = D + 2, NS = 1 << (D - 1), PP = D + 1;
   constexpr int MAXF = D == 2 ? MAXN : MAXN * MAXN;
+  using Dv = Dev<D>;
   __shared__ float s_mat[4 * MAXN * MAXN];
-  __shared__ float s_dl[MAXF * NV];        // large trace - reference
-  __shared__ float s_df[NS * MAXF * NV];   // small-face fluxes - first flux
-  __shared__ double s_ref[NV], s_fref[NV];
+  __shared__ float s_dl[MAXF * NV];        // large trace - reference (FP32)
+  __shared__ float s_df[NS * MAXF * NV];   // F - f(w_ref) on the small faces
+  __shared__ RefState<D> s_R;
+  __shared__ float s_lo[NV];               // low part of the reference node
+  __shared__ double s_fref[NV];            // f(w_ref) along the mortar's orientation
   const int64_t m = blockIdx.x;
   if (m >= M) return;
   const int tid = threadIdx.x;
   const int NF = D == 2 ? N : N * N, NN = NF * N, NM = N * N;
+  const EosF& eos = P.eos;
   for (int k = tid; k < 4 * NM; k += blockDim.x) s_mat[k] = mat32[k];
   const int32_t* t = mtab + m * (NS + 3);
   const int ls = t[NS + 1], o = t[NS + 2];
@@ -555,69 +560,85 @@ __global__ void __launch_bounds__(128)
   };
   const float2* ul = u + (size_t)t[NS] * NN * NV;
   const float2* ur0 = ul + (size_t)face_node(0, dir_large) * NV;  // reference node
-  if (tid < NV) s_ref[tid] = (double)ur0[tid].x + (double)ur0[tid].y;
-  for (int fn = tid; fn < NF; fn += blockDim.x) {
-    const float2* p = ul + (size_t)face_node(fn, dir_large) * NV;
+  if (tid == 0) {
+    float hi[NV];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) s_dl[fn * NV + v] = (p[v].x - ur0[v].x) + (p[v].y - ur0[v].y);
+    for (int v = 0; v < NV; ++v) {
+      hi[v] = ur0[v].x;
+      s_lo[v] = ur0[v].y;
+    }
+    RefState<D> R;
+    Dv::make_ref(hi, eos, R);
+    s_R = R;
+    // the physical flux of the reference primitives, with the EOS constants
+    // of the deviation functions
+    const double rho = R.rho, p = R.p, vo = R.v[o];
+    double v2 = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) v2 += (double)R.v[d] * (double)R.v[d];
+    s_fref[0] = rho * vo;
+#pragma unroll
+    for (int d = 0; d < D; ++d) s_fref[1 + d] = rho * vo * (double)R.v[d] + (d == o ? p : 0.0);
+    s_fref[PP] = (p * (double)eos.igm1 + 0.5 * rho * v2 + p) * vo;
+  }
+  for (int fn = tid; fn < NF; fn += blockDim.x) {
+    const float2* q = ul + (size_t)face_node(fn, dir_large) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) s_dl[fn * NV + v] = (q[v].x - ur0[v].x) + (q[v].y - ur0[v].y);
   }
   __syncthreads();
-  const double gamma = P.gamma, igm1 = P.inv_gamma_minus_one;
-  using Eu = Euler<D, double>;
-  double F[NV];
+  const RefState<D>& R = s_R;
+  const float vro = Dv::pick(R.v, o);
   for (int it = tid; it < NS * NF; it += blockDim.x) {
     const int q = it / NF, fn = it - q * NF;
     const int i = fn % N, j = fn / N;
     const float* F1 = s_mat + (q & 1) * NM;
     const float* F2 = s_mat + ((q >> 1) & 1) * NM;
-    float dp[NV];
+    float hp[NV], lp[NV];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) dp[v] = 0.f;
+    for (int v = 0; v < NV; ++v) {
+      hp[v] = R.hi[v];
+      lp[v] = s_lo[v];
+    }
     if (D == 2) {
       for (int a = 0; a < N; ++a) {
         const float c = F1[i * N + a];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) dp[v] = fmaf(c, s_dl[a * NV + v], dp[v]);
+        for (int v = 0; v < NV; ++v) lp[v] = fmaf(c, s_dl[a * NV + v], lp[v]);
       }
     } else {
       for (int b = 0; b < N; ++b)
         for (int a = 0; a < N; ++a) {
           const float c = F1[i * N + a] * F2[j * N + b];
 #pragma unroll
-          for (int v = 0; v < NV; ++v) dp[v] = fmaf(c, s_dl[(a + b * N) * NV + v], dp[v]);
+          for (int v = 0; v < NV; ++v) lp[v] = fmaf(c, s_dl[(a + b * N) * NV + v], lp[v]);
         }
     }
-    double up[NV], us[NV], wp[NV], ws[NV];
     const float2* ps = u + ((size_t)t[q] * NN + face_node(fn, dir_small)) * NV;
+    float hs[NV], lo_s[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      up[v] = s_ref[v] + (double)dp[v];
-      us[v] = (double)ps[v].x + (double)ps[v].y;
+      hs[v] = ps[v].x;
+      lo_s[v] = ps[v].y;
     }
-    Eu::cons2prim(up, wp, gamma);
-    Eu::cons2prim(us, ws, gamma);
+    Node<D> np, ns;
+    Dv::make_node(hp, lp, R, eos, np);
+    Dv::make_node(hs, lo_s, R, eos, ns);
+    Dv::orient(np, o);
+    Dv::orient(ns, o);
+    float F[NV];
     if (ls == 0)
-      Eu::two_point(P.surface_flux, up, wp, us, ws, o, gamma, igm1, F);
+      Dv::two_point(P.surface_flux, R, np, ns, o, vro, eos, F);
     else
-      Eu::two_point(P.surface_flux, us, ws, up, wp, o, gamma, igm1, F);
+      Dv::two_point(P.surface_flux, R, ns, np, o, vro, eos, F);
     const size_t slot = (size_t)(ff_offset + m * (NS + 1) + q);
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      const float hi = (float)F[v];
-      outff[(slot * NF + fn) * NV + v] = make_float2(hi, (float)(F[v] - (double)hi));
+      s_df[it * NV + v] = F[v];
+      const double x = s_fref[v] + (double)F[v];
+      const float hi = (float)x;
+      outff[(slot * NF + fn) * NV + v] = make_float2(hi, (float)(x - (double)hi));
     }
-    if (it == 0) {
-#pragma unroll
-      for (int v = 0; v < NV; ++v) s_fref[v] = F[v];
-    }
-  }
-  __syncthreads();
-  for (int it = tid; it < NS * NF; it += blockDim.x) {
-    const size_t slot = (size_t)(ff_offset + m * (NS + 1) + it / NF);
-    const float2* f = outff + (slot * NF + (it % NF)) * NV;
-#pragma unroll
-    for (int v = 0; v < NV; ++v)
-      s_df[it * NV + v] = (float)(((double)f[v].x - s_fref[v]) + (double)f[v].y);
   }
   __syncthreads();
   for (int fn = tid; fn < NF; fn += blockDim.x) {
@@ -933,11 +954,11 @@ static void launch_mortars(tg_ctx* c, const void* u_in) {
           c->P, (const double*)u_in, c->d_mtab, c->d_mmat, c->nmortar, c->N, 0, c->d_mflux, nullptr);
   } else {
     if (c->D == 2)
-      mortar_flux_ff_kernel<2><<<nb, 128, 0, c->stream>>>(c->P, (const float2*)u_in, c->d_mtab,
+      mortar_flux_ff_kernel<2><<<nb, 128, 0, c->stream>>>(c->MP, (const float2*)u_in, c->d_mtab,
                                                           c->d_mmat32, c->nmortar, c->N, c->nbound,
                                                           c->d_ghost);
     else
-      mortar_flux_ff_kernel<3><<<nb, 128, 0, c->stream>>>(c->P, (const float2*)u_in, c->d_mtab,
+      mortar_flux_ff_kernel<3><<<nb, 128, 0, c->stream>>>(c->MP, (const float2*)u_in, c->d_mtab,
                                                           c->d_mmat32, c->nmortar, c->N, c->nbound,
                                                           c->d_ghost);
   }
