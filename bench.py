@@ -238,9 +238,31 @@ def gpu_arm(args, rank: int, world: int):
                 et.append(e0.elapsed_time(e1))
         ms = statistics.mean(et)
         nbytes = semi.nvalues * 8
+        # the host link's own speed for these buffers (DMA copies of the same pinned
+        # arrays): the conversion kernels read and write pinned memory directly and
+        # run at this rate, so bytes / rate per direction is the e2e transfer floor
+        dev_buf = torch.empty(u_host.numel(), dtype=torch.float64, device="cuda")
+        link = {}
+        for name, dst, src in (("h2d", dev_buf, u_host), ("d2h", out_host, dev_buf)):
+            times = []
+            for r in range(4):
+                with torch.cuda.stream(stream):
+                    a0 = torch.cuda.Event(enable_timing=True)
+                    a1 = torch.cuda.Event(enable_timing=True)
+                    a0.record(stream)
+                    dst.copy_(src, non_blocking=True)
+                    a1.record(stream)
+                a1.synchronize()
+                if r:
+                    times.append(a0.elapsed_time(a1))
+            link[name] = nbytes / (statistics.mean(times) * 1e-3) / 1e9
+        del dev_buf
         e2e = {"value": whole_job_rate(semi.ndofs, max_over_ranks(ms, world), world),
                "unit": "DOF-updates/s",
-               "ms_per_step": ms, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
+               "ms_per_step": ms, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "host_link_gbs": {k: round(v, 1) for k, v in link.items()},
+               "transfer_floor_ms": nbytes / (link["h2d"] * 1e9) * 1e3 +
+                                    nbytes / (link["d2h"] * 1e9) * 1e3}
 
     # ---- accuracy at t_end (untimed): L2 density error of both paths ----
     acc = None
