@@ -113,3 +113,38 @@ def test_controller_three_level_matches_oracle():
     lam = ctrl(semi)
     np.testing.assert_array_equal(lam, orc.amr_lambda(u))
     assert set(np.unique(lam)) == {-1, 1}
+
+
+def test_native_tree_rejects_invalid_input():
+    from trixi_gb300 import _lib
+    lib = _lib.load()
+    import ctypes
+    h = ctypes.c_void_p()
+    lo = (ctypes.c_double * 3)(0, 0, 0)
+    hi = (ctypes.c_double * 3)(1, 1, 1)
+    assert lib.tg_tree_create(4, 2, lo, hi, None, ctypes.byref(h)) == _lib.TG_ERR_INVALID_ARGUMENT
+    assert "ndims" in _lib.last_error()
+    assert lib.tg_tree_create(2, 2, hi, lo, None, ctypes.byref(h)) == _lib.TG_ERR_INVALID_ARGUMENT
+    assert lib.tg_tree_create(2, 2, lo, hi, None, ctypes.byref(h)) == _lib.TG_OK
+    assert lib.tg_tree_refine_patch(h, 7, lo, hi, 0.0) == _lib.TG_ERR_INVALID_ARGUMENT
+    n = ctypes.c_int64()
+    assert lib.tg_tree_nelements(h, ctypes.byref(n)) == _lib.TG_OK and n.value == 16
+    # no transfer map before an adaptation changed the mesh
+    src = (ctypes.c_int64 * 16)()
+    kind = (ctypes.c_int8 * 16)()
+    assert lib.tg_tree_transfer_map(h, src, kind) == _lib.TG_ERR_INVALID_ARGUMENT
+    lib.tg_tree_destroy(h)
+
+
+def test_refinement_stops_at_the_maximum_level():
+    # sphere patches shrinking with the cell size refine the cells around one
+    # point level by level (2:1 balanced); the tree stops at level 15, and the
+    # mesh constructor raises beyond it
+    def patches(levels):
+        return [dict(type="sphere", center=(0.01, 0.02), radius=0.75 * 2.0 / 2 ** k) for k in levels]
+    mesh = T.TreeMesh((-1.0, -1.0), (1.0, 1.0), initial_refinement_level=2,
+                      refinement_patches=patches(range(2, 15)))
+    assert mesh.element_levels().max() == 15 and mesh.nelements < 2000
+    with pytest.raises(T.TrixiGB300Error):
+        T.TreeMesh((-1.0, -1.0), (1.0, 1.0), initial_refinement_level=2,
+                   refinement_patches=patches(range(2, 16)))

@@ -109,13 +109,15 @@ struct tg_tree {
     }
     child0[c] = first;
   }
+  // All or nothing: no cell is refined when one is at the maximum level
+  // (rebalance! only marks cells coarser than the ones that triggered it, so a
+  // refine! that passes this check for its own cells cannot fail later).
   bool refine_unbalanced(std::vector<int64_t>& ids) {
     std::sort(ids.begin(), ids.end());
     ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
-    for (int64_t c : ids) {
+    for (int64_t c : ids)
       if (level[c] >= kMaxLevel) return false;
-      refine_cell(c);
-    }
+    for (int64_t c : ids) refine_cell(c);
     return true;
   }
   // refine!(t, cell_ids): the leaves given, then rebalance! until no two face
