@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define TG_API_VERSION 2
+#define TG_API_VERSION 3
 
 typedef enum tg_status_code {
   TG_OK = 0,
@@ -96,6 +96,13 @@ typedef enum tg_precision {
   TG_PRECISION_FP64 = 0,
   TG_PRECISION_MIXED = 1
 } tg_precision;
+
+/* Mesh of a context: TreeMesh (Cartesian elements, per-element Jacobian) or a
+ * curvilinear 2D StructuredMesh / P4estMesh brick (per-node metric terms). */
+typedef enum tg_mesh_type {
+  TG_MESH_TREE = 0,
+  TG_MESH_CURVED = 1
+} tg_mesh_type;
 
 /* Boundary conditions of a non-periodic TreeMesh, per direction:
  * BoundaryConditionDirichlet(initial_condition) (src/equations/equations.jl:
@@ -182,6 +189,20 @@ typedef struct tg_config {
   const double* mortar_forward_lower;
   const double* mortar_reverse_upper;
   const double* mortar_reverse_lower;
+  /* Curvilinear meshes (mesh_type = TG_MESH_CURVED, 2D): StructuredMesh, and
+   * P4estMesh built from a brick of trees with a uniform refinement level
+   * (src/meshes/structured_mesh.jl, p4est_mesh.jl:189-244, connectivity
+   * :1149-1240).  Every face is conforming and both elements of an interface
+   * index its nodes in the same direction (no flipped faces); neighbor_ids /
+   * orientations list each interface once as (element on the negative side,
+   * element on the positive side, reference direction 1 or 2).
+   * contravariant_vectors is cache.elements.contravariant_vectors
+   * ([2, 2, n, n, nelements], Ja^i_x / Ja^i_y, containers_2d.jl:107-134) and
+   * inverse_jacobian then points to the per-node
+   * cache.elements.inverse_jacobian ([n, n, nelements], :136-152).
+   * node_coordinates is [2, n, n, nelements].  Periodic meshes only. */
+  int32_t mesh_type;                   /* tg_mesh_type; 0 = TreeMesh */
+  const double* contravariant_vectors;
 } tg_config;
 
 typedef struct tg_ctx tg_ctx;

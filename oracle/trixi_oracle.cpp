@@ -2310,3 +2310,447 @@ double orc_entropy_timederivative(void* h, const double* u, double t) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Curvilinear 2D meshes: StructuredMesh and P4estMesh built from a brick of
+// trees (src/meshes/structured_mesh.jl, p4est_mesh.jl:189-244) with DGSEM on
+// the mapped elements (src/solvers/dgsem_structured/*_2d.jl,
+// dgsem_p4est/dg_2d.jl).  The caller gives the element node coordinates and
+// the neighbours of every element (periodic bricks: all four exist); the
+// metric terms are computed here.
+// ---------------------------------------------------------------------------
+
+namespace orc {
+
+// flux(u, normal_direction), compressible_euler_2d.jl:436-448
+static inline void flux_n(const Eq& eq, const double* u, const double* n, double* f) {
+  double w[4];
+  cons2prim(eq, u, w);
+  const double vn = w[1] * n[0] + w[2] * n[1];
+  const double rvn = w[0] * vn;
+  f[0] = rvn;
+  f[1] = rvn * w[1] + w[3] * n[0];
+  f[2] = rvn * w[2] + w[3] * n[1];
+  f[3] = (u[3] + w[3]) * vn;
+}
+
+// flux_ranocha(u_ll, u_rr, normal_direction), compressible_euler_2d.jl:724-753
+static inline void flux_ranocha_n(const Eq& eq, const double* ul, const double* ur,
+                                  const double* n, double* f) {
+  double a[4], b[4];
+  cons2prim(eq, ul, a);
+  cons2prim(eq, ur, b);
+  const double vna = a[1] * n[0] + a[2] * n[1];
+  const double vnb = b[1] * n[0] + b[2] * n[1];
+  const double rho_mean = ln_mean(a[0], b[0]);
+  const double inv_rho_p_mean = a[3] * b[3] * inv_ln_mean(a[0] * b[3], b[0] * a[3]);
+  const double v1 = 0.5 * (a[1] + b[1]), v2 = 0.5 * (a[2] + b[2]);
+  const double p_avg = 0.5 * (a[3] + b[3]);
+  const double vsq = 0.5 * (a[1] * b[1] + a[2] * b[2]);
+  const double f1 = rho_mean * 0.5 * (vna + vnb);
+  f[0] = f1;
+  f[1] = std::fma(f1, v1, p_avg * n[0]);
+  f[2] = std::fma(f1, v2, p_avg * n[1]);
+  f[3] = f1 * (vsq + inv_rho_p_mean * eq.inv_gamma_minus_one) +
+         0.5 * (a[3] * vnb + b[3] * vna);
+}
+
+// flux_shima_etal(u_ll, u_rr, normal_direction), compressible_euler_2d.jl:497-526
+static inline void flux_shima_n(const Eq& eq, const double* ul, const double* ur,
+                                const double* n, double* f) {
+  double a[4], b[4];
+  cons2prim(eq, ul, a);
+  cons2prim(eq, ur, b);
+  const double vna = a[1] * n[0] + a[2] * n[1];
+  const double vnb = b[1] * n[0] + b[2] * n[1];
+  const double rho_avg = 0.5 * (a[0] + b[0]);
+  const double v1 = 0.5 * (a[1] + b[1]), v2 = 0.5 * (a[2] + b[2]);
+  const double vn_avg = 0.5 * (vna + vnb);
+  const double p_avg = 0.5 * (a[3] + b[3]);
+  const double vsq = 0.5 * (a[1] * b[1] + a[2] * b[2]);
+  const double f1 = rho_avg * vn_avg;
+  f[0] = f1;
+  f[1] = std::fma(f1, v1, p_avg * n[0]);
+  f[2] = std::fma(f1, v2, p_avg * n[1]);
+  f[3] = f1 * vsq + p_avg * vn_avg * eq.inv_gamma_minus_one + 0.5 * (a[3] * vnb + b[3] * vna);
+}
+
+// flux_chandrashekar(u_ll, u_rr, normal_direction), compressible_euler_2d.jl:639-670
+static inline void flux_chandrashekar_n(const Eq& eq, const double* ul, const double* ur,
+                                        const double* n, double* f) {
+  double a[4], b[4];
+  cons2prim(eq, ul, a);
+  cons2prim(eq, ur, b);
+  const double vna = a[1] * n[0] + a[2] * n[1];
+  const double vnb = b[1] * n[0] + b[2] * n[1];
+  const double beta_a = 0.5 * a[0] / a[3], beta_b = 0.5 * b[0] / b[3];
+  const double kin_a = 0.5 * (a[1] * a[1] + a[2] * a[2]);
+  const double kin_b = 0.5 * (b[1] * b[1] + b[2] * b[2]);
+  const double rho_avg = 0.5 * (a[0] + b[0]);
+  const double rho_mean = ln_mean(a[0], b[0]);
+  const double beta_mean = ln_mean(beta_a, beta_b);
+  const double beta_avg = 0.5 * (beta_a + beta_b);
+  const double v1 = 0.5 * (a[1] + b[1]), v2 = 0.5 * (a[2] + b[2]);
+  const double p_mean = 0.5 * rho_avg / beta_avg;
+  const double vsq_avg = kin_a + kin_b;
+  const double f1 = rho_mean * 0.5 * (vna + vnb);
+  f[0] = f1;
+  f[1] = std::fma(f1, v1, p_mean * n[0]);
+  f[2] = std::fma(f1, v2, p_mean * n[1]);
+  f[3] = f1 * 0.5 * (1 / (eq.gamma - 1) / beta_mean - vsq_avg) + f[1] * v1 + f[2] * v2;
+}
+
+// max_abs_speed(_naive)(u_ll, u_rr, normal_direction), compressible_euler_2d.jl:1443-1509
+static inline double max_abs_speed_n(const Eq& eq, const double* ul, const double* ur,
+                                     const double* n, bool naive) {
+  double a[4], b[4];
+  cons2prim(eq, ul, a);
+  cons2prim(eq, ur, b);
+  const double va = a[1] * n[0] + a[2] * n[1];
+  const double vb = b[1] * n[0] + b[2] * n[1];
+  const double ca = std::sqrt(eq.gamma * a[3] / a[0]);
+  const double cb = std::sqrt(eq.gamma * b[3] / b[0]);
+  const double nn = std::sqrt(n[0] * n[0] + n[1] * n[1]);
+  if (naive) return std::max(std::fabs(va), std::fabs(vb)) + std::max(ca, cb) * nn;
+  return std::max(std::fabs(va) + ca * nn, std::fabs(vb) + cb * nn);
+}
+
+// Two-point fluxes along a normal direction (volume and surface)
+static inline void two_point_flux_n(const Eq& eq, int kind, const double* ul, const double* ur,
+                                    const double* n, double* f) {
+  switch (kind) {
+    case FLUX_CENTRAL:
+    case FLUX_LAX_FRIEDRICHS:
+    case FLUX_LAX_FRIEDRICHS_NAIVE: {
+      // flux_central, numerical_fluxes.jl:17-25, plus DissipationLocalLaxFriedrichs
+      double fl[4], fr[4];
+      flux_n(eq, ul, n, fl);
+      flux_n(eq, ur, n, fr);
+      for (int v = 0; v < 4; ++v) f[v] = 0.5 * (fl[v] + fr[v]);
+      if (kind != FLUX_CENTRAL) {
+        const double lam = max_abs_speed_n(eq, ul, ur, n, kind == FLUX_LAX_FRIEDRICHS_NAIVE);
+        for (int v = 0; v < 4; ++v) f[v] = f[v] + (-0.5 * lam * (ur[v] - ul[v]));
+      }
+      return;
+    }
+    case FLUX_RANOCHA: flux_ranocha_n(eq, ul, ur, n, f); return;
+    case FLUX_SHIMA_ETAL: flux_shima_n(eq, ul, ur, n, f); return;
+    case FLUX_CHANDRASHEKAR: flux_chandrashekar_n(eq, ul, ur, n, f); return;
+    default: for (int v = 0; v < 4; ++v) f[v] = NAN;
+  }
+}
+
+struct Curved {
+  Eq eq;
+  Basis b;
+  int n = 0, nn = 0;
+  int64_t E = 0;
+  int vi = VI_WEAK, vf = FLUX_CENTRAL, sf = FLUX_LAX_FRIEDRICHS, source = SRC_NONE;
+  std::vector<double> x;     // [E][nn][2] node coordinates, node = i + n j
+  std::vector<int64_t> nbr;  // [E][4]: neighbours across -x, +x, -y, +y
+  std::vector<double> Ja;    // [E][nn][4]: Ja^1 (x, y), Ja^2 (x, y)
+  std::vector<double> invJ;  // [E][nn]
+  size_t ui(int64_t e, int node) const { return ((size_t)e * nn + node) * 4; }
+};
+
+// calc_jacobian_matrix!, calc_contravariant_vectors!, calc_inverse_jacobian!
+// (dgsem_structured/containers_2d.jl:61-152)
+static void curved_metric(Curved& c) {
+  const int n = c.n, nn = c.nn;
+  const std::vector<double>& Dm = c.b.D;
+  c.Ja.assign((size_t)c.E * nn * 4, 0.0);
+  c.invJ.assign((size_t)c.E * nn, 0.0);
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < c.E; ++e) {
+    const double* X = &c.x[(size_t)e * nn * 2];
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        double J[2][2];  // J[xy][dir]
+        for (int xy = 0; xy < 2; ++xy) {
+          double r1 = 0, r2 = 0;
+          for (int k = 0; k < n; ++k) {
+            r1 += Dm[i * n + k] * X[(k + n * j) * 2 + xy];
+            r2 += Dm[j * n + k] * X[(i + n * k) * 2 + xy];
+          }
+          J[xy][0] = r1;
+          J[xy][1] = r2;
+        }
+        double* a = &c.Ja[((size_t)e * nn + i + n * j) * 4];
+        a[0] = J[1][1];
+        a[1] = -J[0][1];
+        a[2] = -J[1][0];
+        a[3] = J[0][0];
+        c.invJ[(size_t)e * nn + i + n * j] = 1.0 / (J[0][0] * J[1][1] - J[0][1] * J[1][0]);
+      }
+  }
+}
+
+// rhs! of a curvilinear 2D mesh: volume integral (weak_form_kernel! /
+// flux_differencing_kernel!, dgsem_structured/dg_2d.jl:34-139), interface
+// fluxes with the normal of the element on the + side (dg_2d.jl:551-606),
+// surface integral (dgsem_tree/dg_2d.jl:1245-1287), apply_jacobian! per node
+// (dgsem_structured/dg_2d.jl:751-771) and sources (dg_2d.jl:1366-1386).
+static void curved_rhs(const Curved& c, double* du, const double* u, double t) {
+  const int n = c.n, nn = c.nn;
+  const Basis& b = c.b;
+  const Eq& eq = c.eq;
+  std::vector<double> sfv((size_t)c.E * 4 * n * 4);  // [E][dir][l][v]
+  // interface fluxes: for each element, the faces towards its -x and -y neighbours
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < c.E; ++e) {
+    for (int o = 0; o < 2; ++o) {
+      const int64_t left = c.nbr[e * 4 + 2 * o];
+      if (left < 0) continue;
+      for (int l = 0; l < n; ++l) {
+        const int nr = o == 0 ? n * l : l;                        // (1, l) / (l, 1) of e
+        const int nl = o == 0 ? (n - 1) + n * l : l + n * (n - 1);  // (N, l) / (l, N) of left
+        const double sj = c.invJ[(size_t)e * nn + nr] >= 0 ? 1.0 : -1.0;
+        const double* a = &c.Ja[((size_t)e * nn + nr) * 4 + 2 * o];
+        const double nd[2] = {sj * a[0], sj * a[1]};
+        double F[4];
+        two_point_flux_n(eq, c.sf, &u[c.ui(left, nl)], &u[c.ui(e, nr)], nd, F);
+        for (int v = 0; v < 4; ++v) {
+          F[v] *= sj;
+          sfv[(((size_t)e * 4 + 2 * o) * n + l) * 4 + v] = F[v];
+          sfv[(((size_t)left * 4 + 2 * o + 1) * n + l) * 4 + v] = F[v];
+        }
+      }
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < c.E; ++e) {
+    double* de = du + (size_t)e * nn * 4;
+    const double* ue = u + (size_t)e * nn * 4;
+    const double* Ja = &c.Ja[(size_t)e * nn * 4];
+    for (int k = 0; k < nn * 4; ++k) de[k] = 0;
+    if (c.vi == VI_WEAK) {
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          const int q = i + n * j;
+          double f1[5] = {}, f2[5] = {};
+          flux_phys(eq, ue + q * 4, 0, f1);
+          flux_phys(eq, ue + q * 4, 1, f2);
+          const double* a = Ja + q * 4;
+          double cf1[4], cf2[4];
+          for (int v = 0; v < 4; ++v) {
+            cf1[v] = std::fma(a[0], f1[v], a[1] * f2[v]);
+            cf2[v] = std::fma(a[2], f1[v], a[3] * f2[v]);
+          }
+          for (int ii = 0; ii < n; ++ii)
+            for (int v = 0; v < 4; ++v)
+              de[(ii + n * j) * 4 + v] = std::fma(b.Dhat[ii * n + i], cf1[v], de[(ii + n * j) * 4 + v]);
+          for (int jj = 0; jj < n; ++jj)
+            for (int v = 0; v < 4; ++v)
+              de[(i + n * jj) * 4 + v] = std::fma(b.Dhat[jj * n + j], cf2[v], de[(i + n * jj) * 4 + v]);
+        }
+    } else {
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          const int q = i + n * j;
+          for (int ii = i + 1; ii < n; ++ii) {
+            const int r = ii + n * j;
+            const double avg[2] = {0.5 * (Ja[q * 4] + Ja[r * 4]), 0.5 * (Ja[q * 4 + 1] + Ja[r * 4 + 1])};
+            double F[4];
+            two_point_flux_n(eq, c.vf, ue + q * 4, ue + r * 4, avg, F);
+            for (int v = 0; v < 4; ++v) {
+              de[q * 4 + v] = std::fma(b.Dsplit[i * n + ii], F[v], de[q * 4 + v]);
+              de[r * 4 + v] = std::fma(b.Dsplit[ii * n + i], F[v], de[r * 4 + v]);
+            }
+          }
+          for (int jj = j + 1; jj < n; ++jj) {
+            const int r = i + n * jj;
+            const double avg[2] = {0.5 * (Ja[q * 4 + 2] + Ja[r * 4 + 2]),
+                                   0.5 * (Ja[q * 4 + 3] + Ja[r * 4 + 3])};
+            double F[4];
+            two_point_flux_n(eq, c.vf, ue + q * 4, ue + r * 4, avg, F);
+            for (int v = 0; v < 4; ++v) {
+              de[q * 4 + v] = std::fma(b.Dsplit[j * n + jj], F[v], de[q * 4 + v]);
+              de[r * 4 + v] = std::fma(b.Dsplit[jj * n + j], F[v], de[r * 4 + v]);
+            }
+          }
+        }
+    }
+    // surface integral
+    const double factor = b.inv_weights[0];
+    const double* sf = &sfv[(size_t)e * 4 * n * 4];
+    for (int l = 0; l < n; ++l)
+      for (int v = 0; v < 4; ++v) {
+        double& a0 = de[(n * l) * 4 + v];
+        a0 = a0 - sf[(0 * n + l) * 4 + v] * factor;
+        double& a1 = de[((n - 1) + n * l) * 4 + v];
+        a1 = a1 + sf[(1 * n + l) * 4 + v] * factor;
+        double& a2 = de[l * 4 + v];
+        a2 = a2 - sf[(2 * n + l) * 4 + v] * factor;
+        double& a3 = de[(l + n * (n - 1)) * 4 + v];
+        a3 = a3 + sf[(3 * n + l) * 4 + v] * factor;
+      }
+    for (int q = 0; q < nn; ++q) {
+      const double fac = -c.invJ[(size_t)e * nn + q];
+      for (int v = 0; v < 4; ++v) de[q * 4 + v] *= fac;
+      if (c.source == SRC_CONVERGENCE_TEST) {
+        double s[5];
+        source_convergence(eq, &c.x[((size_t)e * nn + q) * 2], t, s);
+        for (int v = 0; v < 4; ++v) de[q * 4 + v] += s[v];
+      }
+    }
+  }
+}
+
+// max_dt of a curvilinear 2D mesh (stepsize_dg2d.jl:114-157)
+static double curved_max_dt(const Curved& c, const double* u) {
+  double mss = 4.9406564584124654e-324;  // nextfloat(0.0)
+  for (int64_t e = 0; e < c.E; ++e) {
+    double m1 = 0, m2 = 0;
+    for (int q = 0; q < c.nn; ++q) {
+      double lam[2];
+      max_abs_speeds(c.eq, &u[c.ui(e, q)], lam);
+      const double* a = &c.Ja[((size_t)e * c.nn + q) * 4];
+      const double l1 = std::fabs(a[0] * lam[0] + a[1] * lam[1]);
+      const double l2 = std::fabs(a[2] * lam[0] + a[3] * lam[1]);
+      const double ij = std::fabs(c.invJ[(size_t)e * c.nn + q]);
+      m1 = std::max(m1, l1 * ij);
+      m2 = std::max(m2, l2 * ij);
+    }
+    mss = std::max(mss, m1 + m2);
+  }
+  return 2 / (c.n * mss);
+}
+
+// calc_error_norms of a curvilinear 2D mesh (analysis_dg2d.jl:141-197)
+static void curved_errors(const Curved& c, const double* u, double t, int ic, const double* par,
+                          double* l2, double* linf) {
+  const Basis& b = c.b;
+  const int n = c.n, na = b.na;
+  for (int v = 0; v < 4; ++v) l2[v] = linf[v] = 0;
+  double vol = 0;
+  std::vector<double> tmp((size_t)na * n * 4), ua((size_t)na * na * 4), xt((size_t)na * n * 2),
+      xa((size_t)na * na * 2), jt((size_t)na * n), ja((size_t)na * na);
+  for (int64_t e = 0; e < c.E; ++e) {
+    // interpolate along i, then along j (multiply_dimensionwise!)
+    for (int j = 0; j < n; ++j)
+      for (int a = 0; a < na; ++a) {
+        double s4[4] = {0, 0, 0, 0}, s2[2] = {0, 0}, s1 = 0;
+        for (int i = 0; i < n; ++i) {
+          const double w = b.avand[a * n + i];
+          const int q = i + n * j;
+          for (int v = 0; v < 4; ++v) s4[v] += w * u[c.ui(e, q) + v];
+          for (int d = 0; d < 2; ++d) s2[d] += w * c.x[((size_t)e * c.nn + q) * 2 + d];
+          s1 += w * (1.0 / c.invJ[(size_t)e * c.nn + q]);
+        }
+        for (int v = 0; v < 4; ++v) tmp[(a + na * j) * 4 + v] = s4[v];
+        for (int d = 0; d < 2; ++d) xt[(a + na * j) * 2 + d] = s2[d];
+        jt[a + na * j] = s1;
+      }
+    for (int bb = 0; bb < na; ++bb)
+      for (int a = 0; a < na; ++a) {
+        double s4[4] = {0, 0, 0, 0}, s2[2] = {0, 0}, s1 = 0;
+        for (int j = 0; j < n; ++j) {
+          const double w = b.avand[bb * n + j];
+          for (int v = 0; v < 4; ++v) s4[v] += w * tmp[(a + na * j) * 4 + v];
+          for (int d = 0; d < 2; ++d) s2[d] += w * xt[(a + na * j) * 2 + d];
+          s1 += w * jt[a + na * j];
+        }
+        double ue[4];
+        initial_condition(c.eq, ic, par, s2, t, ue);
+        const double wj = b.aweights[a] * b.aweights[bb] * std::fabs(s1);
+        for (int v = 0; v < 4; ++v) {
+          const double d = ue[v] - s4[v];
+          l2[v] += d * d * wj;
+          linf[v] = std::max(linf[v], std::fabs(d));
+        }
+        vol += wj;
+      }
+  }
+  for (int v = 0; v < 4; ++v) l2[v] = std::sqrt(l2[v] / vol);
+}
+
+}  // namespace orc
+
+extern "C" {
+
+// Curvilinear 2D solver on element node coordinates x[E][n][n][2] (i fastest)
+// and neighbours nbr[E][4] (0-based, -x, +x, -y, +y).
+void* orc_curved_create(int polydeg, int64_t nelements, const double* x, const int64_t* nbr,
+                        double gamma, int volume_integral, int volume_flux, int surface_flux,
+                        int source) {
+  Curved* c = new Curved();
+  c->eq.D = 2;
+  c->eq.NV = 4;
+  c->eq.gamma = gamma;
+  c->eq.inv_gamma_minus_one = 1 / (gamma - 1);
+  c->b = make_basis(polydeg);
+  c->n = polydeg + 1;
+  c->nn = c->n * c->n;
+  c->E = nelements;
+  c->vi = volume_integral;
+  c->vf = volume_flux;
+  c->sf = surface_flux;
+  c->source = source;
+  c->x.assign(x, x + (size_t)nelements * c->nn * 2);
+  c->nbr.assign(nbr, nbr + (size_t)nelements * 4);
+  curved_metric(*c);
+  return c;
+}
+
+void orc_curved_destroy(void* h) { delete (Curved*)h; }
+
+// contravariant_vectors [E][n][n][2 (dir)][2 (xy)], inverse_jacobian [E][n][n]
+void orc_curved_metric(void* h, double* contravariant, double* inverse_jacobian) {
+  Curved& c = *(Curved*)h;
+  std::copy(c.Ja.begin(), c.Ja.end(), contravariant);
+  std::copy(c.invJ.begin(), c.invJ.end(), inverse_jacobian);
+}
+
+void orc_curved_initial_condition(void* h, int ic, const double* params, double t, double* u) {
+  Curved& c = *(Curved*)h;
+  for (int64_t e = 0; e < c.E; ++e)
+    for (int q = 0; q < c.nn; ++q)
+      initial_condition(c.eq, ic, params, &c.x[((size_t)e * c.nn + q) * 2], t, &u[c.ui(e, q)]);
+}
+
+void orc_curved_rhs(void* h, double* du, const double* u, double t) {
+  curved_rhs(*(Curved*)h, du, u, t);
+}
+
+double orc_curved_max_dt(void* h, const double* u) { return curved_max_dt(*(Curved*)h, u); }
+
+// SimpleIntegrator2N + StepsizeCallback(cfl), as orc_solve
+int orc_curved_solve(void* h, double* u, double t0, double t_end, double cfl, int64_t max_steps,
+                     double* t_out, int64_t* nsteps_out) {
+  Curved& c = *(Curved*)h;
+  const int64_t ndof = c.E * c.nn * 4;
+  std::vector<double> du(ndof), u_tmp(ndof);
+  double t = t0;
+  double dt = cfl * curved_max_dt(c, u);
+  int64_t iter = 0;
+  bool finalstep = false;
+  while (!finalstep && iter < max_steps) {
+    if (std::isnan(dt)) {
+      *t_out = t;
+      *nsteps_out = iter;
+      return -1;
+    }
+    if (t + dt > t_end || isapprox(t + dt, t_end)) {
+      dt = t_end - t;
+      finalstep = true;
+    }
+    std::fill(u_tmp.begin(), u_tmp.end(), 0.0);
+    for (int stage = 0; stage < 5; ++stage) {
+      curved_rhs(c, du.data(), u, t + dt * CK_C[stage]);
+      rk_update(ndof, u, u_tmp.data(), du.data(), CK_A[stage], CK_B[stage] * dt);
+    }
+    iter += 1;
+    t += dt;
+    dt = cfl * curved_max_dt(c, u);
+  }
+  *t_out = t;
+  *nsteps_out = iter;
+  return 0;
+}
+
+void orc_curved_errors(void* h, const double* u, double t, int ic, const double* params,
+                       double* l2, double* linf) {
+  curved_errors(*(Curved*)h, u, t, ic, params, l2, linf);
+}
+
+}  // extern "C"

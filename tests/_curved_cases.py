@@ -1,0 +1,75 @@
+"""Curvilinear 2D golden cases: meshes and mappings of the elixirs named in
+tests/golden/curved_goldens.json, restated from
+examples/structured_2d_dgsem/elixir_euler_{source_terms,source_terms_parallelogram,
+source_terms_waving_flag,free_stream,ec}.jl and
+examples/p4est_2d_dgsem/elixir_euler_source_terms.jl."""
+import json
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def load_curved_goldens():
+    with open(os.path.join(HERE, "golden", "curved_goldens.json"), encoding="utf-8") as f:
+        return json.load(f)
+
+
+def _warped_square_0_3(xi_, eta_):
+    # elixir_euler_free_stream.jl / elixir_euler_ec.jl: a warped [0, 3]^2
+    xi = 1.5 * xi_ + 1.5
+    eta = 1.5 * eta_ + 1.5
+    y = eta + 3 / 8 * (np.cos(1.5 * np.pi * (2 * xi - 3) / 3) *
+                       np.cos(0.5 * np.pi * (2 * eta - 3) / 3))
+    x = xi + 3 / 8 * (np.cos(0.5 * np.pi * (2 * xi - 3) / 3) *
+                      np.cos(2 * np.pi * (2 * y - 3) / 3))
+    return x, y
+
+
+def _parallelogram(xi, eta):
+    # elixir_euler_source_terms_parallelogram.jl
+    return xi + eta, eta
+
+
+WAVING_FLAG_FACES = (
+    # elixir_euler_source_terms_waving_flag.jl
+    lambda s: (-1.0, s - 1.0),
+    lambda s: (1.0, s + 1.0),
+    lambda s: (s, -1.0 + np.sin(0.5 * np.pi * s)),
+    lambda s: (s, 1.0 + np.sin(0.5 * np.pi * s)),
+)
+
+
+def mapping_kwargs(name):
+    if name == "square_0_2":
+        return dict(coordinates_min=(0.0, 0.0), coordinates_max=(2.0, 2.0))
+    if name == "parallelogram":
+        return dict(mapping=_parallelogram)
+    if name == "waving_flag":
+        return dict(faces=WAVING_FLAG_FACES)
+    if name == "warped_square_0_3":
+        return dict(mapping=_warped_square_0_3)
+    raise KeyError(name)
+
+
+def curved_mesh(c, cells=None):
+    """The mesh of a case (optionally with another number of cells per direction)."""
+    from trixi_gb300.curved_mesh import P4estMesh, StructuredMesh
+    kw = mapping_kwargs(c["mapping"])
+    if c["mesh"] == "structured":
+        return StructuredMesh(tuple(cells or c["cells"]), **kw)
+    return P4estMesh(tuple(cells or c["trees"]), polydeg=c["polydeg"],
+                     initial_refinement_level=c.get("level", 0), **kw)
+
+
+def curved_oracle(O, c, mesh):
+    from trixi_gb300.basis import LobattoLegendreBasis
+    vi = dict(weak=O.VI_WEAK, fluxdiff=O.VI_FLUXDIFF)[c["vi"]]
+    fl = dict(central=O.FLUX_CENTRAL, ranocha=O.FLUX_RANOCHA, shima_etal=O.FLUX_SHIMA_ETAL,
+              llf=O.FLUX_LAX_FRIEDRICHS, llf_naive=O.FLUX_LAX_FRIEDRICHS_NAIVE,
+              chandrashekar=O.FLUX_CHANDRASHEKAR)
+    src = O.SRC_CONVERGENCE_TEST if c.get("source") == "convergence_test" else O.SRC_NONE
+    X = mesh.node_coordinates(LobattoLegendreBasis(c["polydeg"]))
+    return O.CurvedOracle(c["polydeg"], X, mesh.neighbors(), 1.4, vi, fl[c["volume_flux"]],
+                          fl[c["surface_flux"]], src)

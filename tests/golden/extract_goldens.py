@@ -1,4 +1,5 @@
-"""Extract the L2/Linf goldens of Trixi.jl's TreeMesh Euler regression tests.
+"""Extract the L2/Linf goldens of Trixi.jl's TreeMesh, StructuredMesh and P4estMesh
+Euler regression tests.
 
 Run once in a checkout that has the Trixi.jl sources (read as text, nothing is
 executed):
@@ -247,6 +248,56 @@ CASES = {
         surface_flux="ranocha", cfl=1.3, tspan=[0.0, 0.4]),
 }
 
+# Curvilinear 2D meshes (examples/structured_2d_dgsem, examples/p4est_2d_dgsem).
+# mesh: structured (cells) | p4est (trees, level); mapping: the elixir's
+# mapping or faces by name (restated in tests/_curved_cases.py).
+CURVED_CASES = {
+    "StructuredMesh2D: elixir_euler_source_terms.jl": dict(
+        file="test/test_structured_2d.jl",
+        elixir="examples/structured_2d_dgsem/elixir_euler_source_terms.jl",
+        mesh="structured", cells=[16, 16], mapping="square_0_2", polydeg=3,
+        ic="convergence_test", source="convergence_test", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=1.0, tspan=[0.0, 2.0]),
+    "StructuredMesh2D: elixir_euler_source_terms_parallelogram.jl": dict(
+        file="test/test_structured_2d.jl",
+        elixir="examples/structured_2d_dgsem/elixir_euler_source_terms_parallelogram.jl",
+        mesh="structured", cells=[16, 16], mapping="parallelogram", polydeg=3,
+        ic="convergence_test", source="convergence_test", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=0.5, tspan=[0.0, 2.0]),
+    "StructuredMesh2D: elixir_euler_source_terms_waving_flag.jl": dict(
+        file="test/test_structured_2d.jl",
+        elixir="examples/structured_2d_dgsem/elixir_euler_source_terms_waving_flag.jl",
+        mesh="structured", cells=[16, 16], mapping="waving_flag", polydeg=3,
+        ic="convergence_test", source="convergence_test", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=0.8, tspan=[0.0, 2.0]),
+    "StructuredMesh2D: elixir_euler_free_stream.jl": dict(
+        file="test/test_structured_2d.jl",
+        elixir="examples/structured_2d_dgsem/elixir_euler_free_stream.jl",
+        mesh="structured", cells=[16, 16], mapping="warped_square_0_3", polydeg=3,
+        ic="constant", source="none", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=2.0, tspan=[0.0, 2.0]),
+    "StructuredMesh2D: elixir_euler_ec.jl": dict(
+        file="test/test_structured_2d.jl",
+        elixir="examples/structured_2d_dgsem/elixir_euler_ec.jl",
+        mesh="structured", cells=[16, 16], mapping="warped_square_0_3", polydeg=4,
+        ic="weak_blast_wave", source="none", vi="fluxdiff",
+        volume_flux="ranocha", surface_flux="ranocha", cfl=1.0, tspan=[0.0, 2.0]),
+    "CUDA 2D: elixir_euler_source_terms.jl native": dict(
+        file="test/test_cuda_2d.jl",
+        elixir="examples/p4est_2d_dgsem/elixir_euler_source_terms.jl",
+        mesh="p4est", trees=[16, 16], level=0, mapping="square_0_2", polydeg=3,
+        ic="convergence_test", source="convergence_test", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=1.0, tspan=[0.0, 2.0]),
+    # the reference's own Float32 run on a GPU (storage_type = CuArray)
+    "CUDA 2D: elixir_euler_source_terms.jl Float32 / CUDA": dict(
+        file="test/test_cuda_2d.jl",
+        elixir="examples/p4est_2d_dgsem/elixir_euler_source_terms.jl",
+        mesh="p4est", trees=[16, 16], level=0, mapping="square_0_2", polydeg=3,
+        ic="convergence_test", source="convergence_test", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=1.0, tspan=[0.0, 2.0],
+        float32=True),
+}
+
 _NUM = r"[-+]?\d+(?:\.\d*)?(?:[eE][-+]?\d+)?"
 
 
@@ -261,7 +312,7 @@ def _testitem_body(text: str, name: str) -> tuple[str, int]:
 
 
 def _vector(body: str, key: str) -> list[float]:
-    m = re.search(key + r"\s*=\s*\[([^\]]*)\]", body)
+    m = re.search(r"\b" + key + r"\s*=\s*(?:Float32)?\[([^\]]*)\]", body)
     if not m:
         raise KeyError(key)
     return [float(x) for x in re.findall(_NUM, m.group(1))]
@@ -287,6 +338,25 @@ def main(root: str) -> None:
     with open(dst, "w", encoding="utf-8") as f:
         json.dump(out, f, indent=1, sort_keys=True)
     print(f"wrote {len(out)} goldens to {dst}")
+    curved = {}
+    for name, case in CURVED_CASES.items():
+        text = open(os.path.join(root, case["file"]), encoding="utf-8").read()
+        body, line = _testitem_body(text, name)
+        entry = dict(case)
+        entry["source_line"] = f"{case['file']}:{line}"
+        entry["l2"] = _vector(body, "l2")
+        entry["linf"] = _vector(body, "linf")
+        m = re.search(r"tspan\s*=\s*\((" + _NUM + r")f?0?,\s*(" + _NUM + r")\)", body)
+        if m:
+            entry["tspan"] = [float(m.group(1)), float(m.group(2))]
+        m = re.search(r"atol\s*=\s*(" + _NUM + r")", body)
+        if m:
+            entry["atol"] = float(m.group(1))
+        curved[name] = entry
+    dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "curved_goldens.json")
+    with open(dst, "w", encoding="utf-8") as f:
+        json.dump(curved, f, indent=1, sort_keys=True)
+    print(f"wrote {len(curved)} curvilinear goldens to {dst}")
 
 
 if __name__ == "__main__":

@@ -27,7 +27,7 @@ def test_library_exports_every_declared_symbol():
     lib = ctypes.CDLL(_lib.LIB_PATH)
     for name in declared_symbols():
         assert hasattr(lib, name), name
-    assert _lib.load().tg_api_version() == 2
+    assert _lib.load().tg_api_version() == 3
 
 
 def test_invalid_config_is_rejected_without_gpu():

@@ -1,0 +1,97 @@
+"""Curvilinear 2D meshes on the CPU: the oracle against the goldens of Trixi.jl's
+StructuredMesh and P4estMesh Euler tests, and the host mesh setup against the
+oracle's metric terms."""
+import numpy as np
+import pytest
+
+from _curved_cases import curved_mesh, curved_oracle, load_curved_goldens
+
+GOLDENS = load_curved_goldens()
+FP64_GOLDENS = sorted(k for k, v in GOLDENS.items() if not v.get("float32"))
+
+
+def _ic(O, name):
+    return dict(constant=O.IC_CONSTANT, convergence_test=O.IC_CONVERGENCE_TEST,
+                weak_blast_wave=O.IC_WEAK_BLAST_WAVE)[name]
+
+
+@pytest.mark.parametrize("name", FP64_GOLDENS)
+def test_curved_oracle_reproduces_trixi_golden(oracle_mod, name):
+    O = oracle_mod
+    c = GOLDENS[name]
+    orc = curved_oracle(O, c, curved_mesh(c))
+    ic = _ic(O, c["ic"])
+    u0 = orc.initial_condition(ic, c["tspan"][0])
+    u, t, _ = orc.solve(u0, c["tspan"][0], c["tspan"][1], c["cfl"])
+    assert t == pytest.approx(c["tspan"][1], rel=1e-14)
+    l2, linf = orc.error_norms(u, t, ic)
+    if c["ic"] == "constant":
+        # free-stream preservation on a warped mesh: round-off goldens, compared
+        # with the test's own absolute tolerance
+        np.testing.assert_allclose(l2, c["l2"], rtol=0, atol=c.get("atol", 7e-13))
+        np.testing.assert_allclose(linf, c["linf"], rtol=0, atol=c.get("atol", 7e-13))
+        return
+    np.testing.assert_allclose(l2, c["l2"], rtol=1e-8, atol=0)
+    np.testing.assert_allclose(linf, c["linf"], rtol=1e-7, atol=0)
+
+
+def test_host_metric_terms_match_oracle(oracle_mod):
+    from trixi_gb300.basis import LobattoLegendreBasis
+    from trixi_gb300.curved_mesh import metric_terms
+    c = GOLDENS["StructuredMesh2D: elixir_euler_ec.jl"]
+    mesh = curved_mesh(c, cells=(8, 6))
+    b = LobattoLegendreBasis(c["polydeg"])
+    X = mesh.node_coordinates(b)
+    orc = curved_oracle(oracle_mod, c, mesh)
+    Ja, ij = orc.metric()
+    Ja2, ij2 = metric_terms(X, b)
+    np.testing.assert_allclose(Ja2, Ja, rtol=0, atol=1e-13)
+    np.testing.assert_allclose(ij2, ij, rtol=1e-13)
+
+
+def test_p4est_refined_trees_cover_the_structured_mesh():
+    # a 4x4 brick refined twice and a 16x16 StructuredMesh of the same mapping
+    # hold the same elements (the mapping is affine, so interpolation is exact)
+    from trixi_gb300.basis import LobattoLegendreBasis
+    from trixi_gb300.curved_mesh import P4estMesh, StructuredMesh
+    b = LobattoLegendreBasis(3)
+    kw = dict(coordinates_min=(0.0, 0.0), coordinates_max=(2.0, 2.0))
+    s = StructuredMesh((16, 16), **kw).node_coordinates(b)
+    p4 = P4estMesh((4, 4), polydeg=3, initial_refinement_level=2, **kw)
+    p = p4.node_coordinates(b)
+    key = lambda X: np.lexsort((np.round(X[:, 0, 0, 0], 9), np.round(X[:, 0, 0, 1], 9)))
+    np.testing.assert_allclose(p[key(p)], s[key(s)], rtol=0, atol=1e-14)
+    # Morton order inside the first tree: (0,0), (1,0), (0,1), (1,1), ...
+    np.testing.assert_array_equal(p4.cells[:4], [[0, 0], [1, 0], [0, 1], [1, 1]])
+
+
+def test_p4est_curved_interpolation_converges():
+    # element nodes interpolated from the tree nodes approach the mapping as the
+    # mesh polydeg grows (calc_node_coordinates!, dgsem_p4est/containers_2d.jl:41-89)
+    from trixi_gb300.basis import LobattoLegendreBasis
+    from trixi_gb300.curved_mesh import P4estMesh
+    from _curved_cases import _warped_square_0_3
+    b = LobattoLegendreBasis(3)
+    errs = []
+    for pd in (3, 5, 7):
+        m = P4estMesh((2, 2), polydeg=pd, mapping=_warped_square_0_3, initial_refinement_level=2)
+        b2 = LobattoLegendreBasis(max(pd, 3))
+        X = m.node_coordinates(b2)
+        mx, my = m.grid
+        xi = -1 + (m.cells[:, 0, None, None] + 0.5 * (b2.nodes[None, None, :] + 1)) * 2 / mx
+        eta = -1 + (m.cells[:, 1, None, None] + 0.5 * (b2.nodes[None, :, None] + 1)) * 2 / my
+        xe, ye = _warped_square_0_3(*np.broadcast_arrays(xi, eta))
+        errs.append(max(np.abs(X[..., 0] - xe).max(), np.abs(X[..., 1] - ye).max()))
+    assert errs[0] > errs[1] > errs[2]
+    assert errs[2] < errs[0] / 5
+
+
+def test_curved_mesh_rejects_unsupported():
+    from trixi_gb300.curved_mesh import P4estMesh, StructuredMesh
+    with pytest.raises(NotImplementedError):
+        StructuredMesh((4, 4), (0.0, 0.0), (1.0, 1.0), periodicity=False)
+    with pytest.raises(ValueError):
+        P4estMesh((2, 2), polydeg=3)
+    with pytest.raises(ValueError):
+        P4estMesh((2, 2), polydeg=3, coordinates_min=(0.0, 0.0), coordinates_max=(1.0, 1.0),
+                  initial_refinement_level=-1)

@@ -24,6 +24,7 @@ TG_VOLUME_WEAK_FORM, TG_VOLUME_FLUX_DIFFERENCING, TG_VOLUME_SHOCK_CAPTURING_HG =
  TG_FLUX_LAX_FRIEDRICHS_NAIVE, TG_FLUX_HLLC, TG_FLUX_CHANDRASHEKAR, TG_FLUX_HLLE) = range(8)
 TG_SOURCE_NONE, TG_SOURCE_CONVERGENCE_TEST = 0, 1
 TG_PRECISION_FP64, TG_PRECISION_MIXED = 0, 1
+TG_MESH_TREE, TG_MESH_CURVED = 0, 1
 TG_BOUNDARY_PERIODIC, TG_BOUNDARY_DIRICHLET, TG_BOUNDARY_SLIP_WALL = 0, 1, 2
 
 # Every symbol declared in include/trixi_gb300.h.
@@ -88,6 +89,8 @@ class tg_config(ctypes.Structure):
         ("mortar_forward_lower", ctypes.POINTER(ctypes.c_double)),
         ("mortar_reverse_upper", ctypes.POINTER(ctypes.c_double)),
         ("mortar_reverse_lower", ctypes.POINTER(ctypes.c_double)),
+        ("mesh_type", ctypes.c_int32),
+        ("contravariant_vectors", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
