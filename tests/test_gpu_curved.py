@@ -1,0 +1,173 @@
+"""Curvilinear 2D meshes (StructuredMesh, P4estMesh bricks) on the GPU against the
+oracle and the goldens of Trixi.jl's StructuredMesh / P4estMesh Euler tests."""
+import numpy as np
+import pytest
+
+import trixi_gb300 as T
+from _curved_cases import curved_mesh, curved_oracle, load_curved_goldens
+from _gpu_cases import FLUX, perturbed_state, rel_err
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+GOLDENS = load_curved_goldens()
+FP64_GOLDENS = sorted(k for k, v in GOLDENS.items() if not v.get("float32"))
+
+
+def build(c, precision="fp64", cells=None):
+    eq = T.CompressibleEulerEquations2D(1.4)
+    basis = T.LobattoLegendreBasis(c["polydeg"])
+    sflux = FLUX[c["surface_flux"]][0]
+    if c["vi"] == "weak":
+        vi = T.VolumeIntegralWeakForm()
+    else:
+        vi = T.VolumeIntegralFluxDifferencing(FLUX[c["volume_flux"]][0])
+    solver = T.DGSEM(basis, sflux, vi)
+    mesh = curved_mesh(c, cells)
+    ic = {"convergence_test": T.initial_condition_convergence_test,
+          "weak_blast_wave": T.initial_condition_weak_blast_wave,
+          "constant": T.initial_condition_constant}[c["ic"]]
+    src = T.source_terms_convergence_test if c.get("source") == "convergence_test" else None
+    semi = T.SemidiscretizationHyperbolic(mesh, eq, ic, solver, source_terms=src,
+                                          precision=precision)
+    return semi, curved_oracle(O, c, mesh)
+
+
+def _case(name, **over):
+    return dict(GOLDENS[name], **over)
+
+
+PAR = "StructuredMesh2D: elixir_euler_source_terms_parallelogram.jl"
+FLAG = "StructuredMesh2D: elixir_euler_source_terms_waving_flag.jl"
+EC = "StructuredMesh2D: elixir_euler_ec.jl"
+P4 = "CUDA 2D: elixir_euler_source_terms.jl native"
+RHS_CASES = [
+    _case(PAR),
+    _case(FLAG),
+    _case(EC),                                               # FD ranocha / ranocha, N = 5
+    _case(EC, polydeg=3, volume_flux="shima_etal", surface_flux="llf"),
+    _case(EC, polydeg=2, volume_flux="chandrashekar", surface_flux="llf_naive"),
+    _case(EC, polydeg=3, volume_flux="central", surface_flux="central"),
+    _case(FLAG, vi="fluxdiff", volume_flux="ranocha", surface_flux="llf"),
+    _case(P4, mesh="p4est", trees=[6, 4], level=1, mapping="warped_square_0_3"),
+]
+
+
+def _id(c):
+    return f"{c['mesh']}-{c['mapping']}-{c['vi']}-{c['volume_flux']}-{c['surface_flux']}-p{c['polydeg']}"
+
+
+@pytest.mark.parametrize("c", RHS_CASES, ids=_id)
+def test_curved_rhs_fp64_matches_oracle(c):
+    semi, orc = build(c, cells=(12, 10) if c["mesh"] == "structured" else None)
+    u = perturbed_state(semi, seed=5)
+    np.testing.assert_array_less(rel_err(semi.device_context.rhs_host(u, 0.37), orc.rhs(u, 0.37)),
+                                 1e-12)
+
+
+@pytest.mark.parametrize("c", RHS_CASES, ids=_id)
+def test_curved_rhs_mixed_close_to_oracle(c):
+    # float-float state, FP32 deviation fluxes: the perturbed state's node
+    # deviations are ~1e-2 of the state, FP32 rounds them to ~1e-9 relative and
+    # the derivative operator amplifies that by |D| ~ N^2
+    semi, orc = build(c, precision="mixed", cells=(12, 10) if c["mesh"] == "structured" else None)
+    u = perturbed_state(semi, seed=5)
+    assert rel_err(semi.device_context.rhs_host(u, 0.37), orc.rhs(u, 0.37)) < 2e-4
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_curved_max_dt_and_integrals(precision):
+    c = _case(FLAG)
+    semi, orc = build(c, precision, cells=(12, 10))
+    u = perturbed_state(semi, seed=2)
+    ctx = semi.device_context
+    ctx.upload(u)
+    tol = 1e-13 if precision == "fp64" else 1e-6
+    assert ctx.max_dt() == pytest.approx(orc.max_dt(u), rel=tol)
+    tot = ctx.integrals()
+    w = semi.solver.basis.weights
+    J = 1.0 / semi.inverse_jacobian
+    ref = np.einsum("j,i,eji,ejiv->v", w, w, J, u)
+    np.testing.assert_allclose(tot[:4], ref, rtol=1e-12 if precision == "fp64" else 1e-12)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_curved_time_steps_match_oracle(precision):
+    c = _case(FLAG)
+    semi, orc = build(c, precision, cells=(12, 10))
+    u0 = semi.compute_coefficients(0.0)
+    ctx = semi.device_context
+    ctx.upload(u0)
+    t, n = ctx.step(8, c["cfl"], 10.0, 0.0)
+    u_orc, t_orc, n_orc = orc.solve(u0, 0.0, 10.0, c["cfl"], max_steps=8)
+    assert n == n_orc == 8
+    assert t == pytest.approx(t_orc, rel=1e-12 if precision == "fp64" else 1e-6)
+    tol = 1e-12 if precision == "fp64" else 1e-7
+    assert rel_err(ctx.download(), u_orc) < tol
+
+
+def _golden_run(c, precision="fp64"):
+    semi, _ = build(c, precision)
+    ode = T.semidiscretize(semi, c["tspan"])
+    ana = T.AnalysisCallback(semi)
+    sol = T.solve(ode, T.CarpenterKennedy2N54(williamson_condition=False), dt=1.0,
+                  callback=T.CallbackSet(T.StepsizeCallback(cfl=c["cfl"]), ana))
+    return sol, ana
+
+
+@pytest.mark.parametrize("name", FP64_GOLDENS)
+def test_curved_gpu_fp64_reproduces_trixi_goldens(name):
+    c = dict(GOLDENS[name])
+    sol, ana = _golden_run(c)
+    assert sol.t[-1] == pytest.approx(c["tspan"][1], rel=1e-14)
+    if c["ic"] == "constant":
+        atol = c.get("atol", 7e-13)
+        np.testing.assert_allclose(ana.l2, c["l2"], rtol=0, atol=atol)
+        np.testing.assert_allclose(ana.linf, c["linf"], rtol=0, atol=atol)
+        return
+    np.testing.assert_allclose(ana.l2, c["l2"], rtol=1e-8)
+    np.testing.assert_allclose(ana.linf, c["linf"], rtol=1e-7)
+
+
+@pytest.mark.parametrize("name", [PAR, FLAG, P4, "StructuredMesh2D: elixir_euler_source_terms.jl"])
+def test_curved_mixed_error_within_1p1x_of_fp64_golden(name):
+    c = dict(GOLDENS[name])
+    _, ana = _golden_run(c, "mixed")
+    assert np.all(ana.l2 <= 1.1 * np.asarray(c["l2"]))
+    assert np.all(ana.l2 >= 0.9 * np.asarray(c["l2"]))
+
+
+def test_curved_mixed_free_stream():
+    # the deviation form carries no reference flux: a free stream on the warped
+    # mesh stays constant to round-off in mixed precision too
+    c = dict(GOLDENS["StructuredMesh2D: elixir_euler_free_stream.jl"])
+    _, ana = _golden_run(c, "mixed")
+    assert np.all(ana.l2 < 1e-11) and np.all(ana.linf < 1e-10)
+
+
+def test_curved_mixed_beats_reference_float32_gpu_run():
+    # the reference's own Float32 run of this P4estMesh elixir on a GPU
+    # (test_cuda_2d.jl) against the mixed path: float-float state and deviation
+    # fluxes keep the FP64 discretization error
+    c32 = GOLDENS["CUDA 2D: elixir_euler_source_terms.jl Float32 / CUDA"]
+    c64 = GOLDENS[P4]
+    _, ana = _golden_run(dict(c64), "mixed")
+    assert np.all(ana.l2 < np.asarray(c32["l2"]))
+    np.testing.assert_allclose(ana.l2, c64["l2"], rtol=1e-3)
+
+
+def test_curved_unsupported_options_fail_loudly():
+    c = _case(EC)
+    eq = T.CompressibleEulerEquations2D(1.4)
+    basis = T.LobattoLegendreBasis(3)
+    ind = T.IndicatorHennemannGassner(eq, basis, alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
+                                      variable=T.density_pressure)
+    vi = T.VolumeIntegralShockCapturingHG(ind, volume_flux_dg=T.flux_ranocha,
+                                          volume_flux_fv=T.flux_lax_friedrichs)
+    with pytest.raises(NotImplementedError):
+        T.SemidiscretizationHyperbolic(curved_mesh(c, (4, 4)), eq, T.initial_condition_constant,
+                                       T.DGSEM(basis, T.flux_lax_friedrichs, vi))
+    semi = T.SemidiscretizationHyperbolic(curved_mesh(c, (4, 4)), eq, T.initial_condition_constant,
+                                          T.DGSEM(basis, T.flux_hllc))
+    with pytest.raises(T.TrixiGB300Error):
+        semi.device_context

@@ -21,6 +21,7 @@
 #include "../../include/trixi_gb300.h"
 #include "tg_clock.cuh"
 #include "tg_internal.h"
+#include "tg_curved.cuh"
 #include "tg_mixed.cuh"
 
 namespace tg {
@@ -827,6 +828,14 @@ struct tg_ctx {
   int64_t* d_amap = nullptr;          // AMR transfer map of the last tg_adapt_state
   int8_t* d_akind = nullptr;
   double* d_weights = nullptr;
+  // curvilinear meshes (mesh_type TG_MESH_CURVED)
+  bool curved = false;
+  tg::CurvedParams CP{};
+  double* d_cmet = nullptr;           // [E][NN][5]: Ja^1, Ja^2, inverse Jacobian
+  float4* d_cja32 = nullptr;          // mixed: [E][NN] Ja^1, Ja^2
+  float* d_cinvj32 = nullptr;         // mixed: [E][NN] inverse Jacobian
+  double* d_cxy = nullptr;            // fp64 sources: [E][NN][2] node coordinates
+  float4* d_csc = nullptr;            // mixed sources: [E][NN] sin/cos(pi (x + y))
   double* d_partial = nullptr;
   double* d_sums = nullptr;
   Clock* d_clock = nullptr;
@@ -877,7 +886,7 @@ static void free_ctx(tg_ctx* c) {
     if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
   void* ptrs[] = {c->d_u[0], c->d_u[1], c->d_utmp, c->d_du, c->d_uscratch, c->d_stage64,
                   c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_nbr, c->d_invj, c->d_xline,
-                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mmat32, c->d_mflux, c->d_scls, c->d_amr_raw, c->d_amr_alpha, c->d_amap, c->d_akind, c->d_weights, c->d_partial, c->d_sums, c->d_clock,
+                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mmat32, c->d_mflux, c->d_scls, c->d_amr_raw, c->d_amr_alpha, c->d_amap, c->d_akind, c->d_weights, c->d_cmet, c->d_cja32, c->d_cinvj32, c->d_cxy, c->d_csc, c->d_partial, c->d_sums, c->d_clock,
                   c->d_status, c->d_speed};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -969,6 +978,42 @@ static int launch_kernel(tg_ctx* c, int mode, const void* u_in, void* u_out, dou
                          double t_rhs, int stage, bool reduce) {
   int rc;
   if (c->nmortar > 0) launch_mortars(c, u_in);
+  if (c->curved) {
+    StageArgs A{};
+    MixedArgs M{};
+    A.status = M.status = c->d_status;
+    A.clock = M.clock = c->d_clock;
+    A.mode = M.mode = mode;
+    A.u_in = (const double*)u_in;
+    A.u_out = (double*)u_out;
+    M.u_in = (const float2*)u_in;
+    M.u_out = (float2*)u_out;
+    A.du_out = M.du_out = du_out;
+    A.u_tmp = c->d_utmp;
+    M.u_tmp = (float*)c->d_utmp;
+    A.t_rhs = M.t_rhs = t_rhs;
+    if (mode == MODE_STAGE) {
+      A.a = M.a = CK_A[stage];
+      A.b = M.b = CK_B[stage];
+      A.c = M.c = CK_C[stage];
+      A.zero_tmp = M.zero_tmp = stage == 0;
+      M.stage = stage;
+    } else {
+      const double sn = std::sin(M_PI * t_rhs), cs = std::cos(M_PI * t_rhs);
+      M.sin_t = (float)sn;
+      M.cos_t = (float)cs;
+      M.sin_tl = (float)(sn - (double)M.sin_t);
+      M.cos_tl = (float)(cs - (double)M.cos_t);
+    }
+    A.speed_bits = M.speed_bits = reduce ? &c->d_clock->speed_bits : nullptr;
+    rc = tg::launch_curved(c->CP, c->fp64 ? &A : nullptr, c->fp64 ? nullptr : &M, c->stream);
+    if (rc != 0) {
+      cudaError_t e = cudaGetLastError();
+      return fail(c, TG_ERR_CUDA, "curvilinear kernel launch failed (%d): %s", rc,
+                  cudaGetErrorString(e));
+    }
+    return TG_OK;
+  }
   if (c->fp64) {
     StageArgs A{};
     A.alpha_raw = c->d_alpha_raw;
@@ -1051,6 +1096,11 @@ static int enqueue_stage(tg_ctx* c, int stage, bool reduce_speed) {
 // mixed context in that context's FP32 wave-speed arithmetic.
 static int reduce_speed(tg_ctx* c, const void* u, bool ff, unsigned long long* dst) {
   speed_reset_kernel<<<1, 1, 0, c->stream>>>(dst);
+  if (c->curved) {
+    if (tg::launch_curved_speed(c->CP, u, ff, dst, c->d_status, c->stream) != 0)
+      return fail(c, TG_ERR_CUDA, "curvilinear wave-speed launch failed");
+    return TG_OK;
+  }
   const unsigned nb = (unsigned)((c->E + 127) / 128);
   if (c->D == 2) {
     if (ff)
@@ -1068,6 +1118,83 @@ static int reduce_speed(tg_ctx* c, const void* u, bool ff, unsigned long long* d
                                                             c->NN, c->P.gamma, dst, c->d_status);
   }
   CUDA_TRY(c, cudaGetLastError());
+  return TG_OK;
+}
+
+// Metric terms and source tables of a curvilinear context, and its kernel
+// parameters (after the generic setup of tg_ctx_create).
+static int curved_setup(tg_ctx* c, const tg_config* cfg) {
+  const int N = c->N, NN = c->NN;
+  const int64_t E = c->E;
+  const size_t nq = (size_t)E * NN;
+  std::vector<double> met(nq * 5);
+  for (size_t k = 0; k < nq; ++k) {
+    for (int m = 0; m < 4; ++m) met[k * 5 + m] = cfg->contravariant_vectors[k * 4 + m];
+    met[k * 5 + 4] = cfg->inverse_jacobian[k];
+  }
+  CUDA_TRY(nullptr, cudaMalloc((void**)&c->d_cmet, sizeof(double) * met.size()));
+  CUDA_TRY(nullptr, cudaMemcpy(c->d_cmet, met.data(), sizeof(double) * met.size(),
+                               cudaMemcpyHostToDevice));
+  const bool src = c->P.source == SRC_CONVERGENCE_TEST;
+  if (!c->fp64) {
+    std::vector<float4> ja(nq);
+    std::vector<float> ij(nq);
+    for (size_t k = 0; k < nq; ++k) {
+      const double* m = &met[k * 5];
+      ja[k] = make_float4((float)m[0], (float)m[1], (float)m[2], (float)m[3]);
+      ij[k] = (float)m[4];
+    }
+    CUDA_TRY(nullptr, cudaMalloc((void**)&c->d_cja32, sizeof(float4) * nq));
+    CUDA_TRY(nullptr, cudaMalloc((void**)&c->d_cinvj32, sizeof(float) * nq));
+    CUDA_TRY(nullptr, cudaMemcpy(c->d_cja32, ja.data(), sizeof(float4) * nq,
+                                 cudaMemcpyHostToDevice));
+    CUDA_TRY(nullptr, cudaMemcpy(c->d_cinvj32, ij.data(), sizeof(float) * nq,
+                                 cudaMemcpyHostToDevice));
+    if (src) {
+      // sin/cos(pi (x + y)) per node as float-float pairs; the stage kernel
+      // combines them with sin/cos(pi t) by the angle-difference formula
+      std::vector<float4> sc(nq);
+      for (size_t k = 0; k < nq; ++k) {
+        const double ph = cfg->node_coordinates[k * 2] + cfg->node_coordinates[k * 2 + 1];
+        const double sn = std::sin(M_PI * ph), cs = std::cos(M_PI * ph);
+        const float sh = (float)sn, ch = (float)cs;
+        sc[k] = make_float4(sh, ch, (float)(sn - (double)sh), (float)(cs - (double)ch));
+      }
+      CUDA_TRY(nullptr, cudaMalloc((void**)&c->d_csc, sizeof(float4) * nq));
+      CUDA_TRY(nullptr, cudaMemcpy(c->d_csc, sc.data(), sizeof(float4) * nq,
+                                   cudaMemcpyHostToDevice));
+    }
+  } else if (src) {
+    CUDA_TRY(nullptr, cudaMalloc((void**)&c->d_cxy, sizeof(double) * nq * 2));
+    CUDA_TRY(nullptr, cudaMemcpy(c->d_cxy, cfg->node_coordinates, sizeof(double) * nq * 2,
+                                 cudaMemcpyHostToDevice));
+  }
+  tg::CurvedParams& C = c->CP;
+  C.nelements = E;
+  C.N = N;
+  C.vi = c->vi;
+  C.volume_flux = c->P.volume_flux;
+  C.surface_flux = c->P.surface_flux;
+  C.source = c->P.source;
+  C.gamma = c->P.gamma;
+  C.inv_gamma_minus_one = c->P.inv_gamma_minus_one;
+  C.eos = c->MP.eos;
+  for (int k = 0; k < MAXN * MAXN; ++k) {
+    C.Dhat[k] = c->P.Dhat[k];
+    C.Dsplit[k] = c->P.Dsplit[k];
+    C.Dhat32[k] = (float)c->P.Dhat[k];
+    C.Dsplit32[k] = (float)c->P.Dsplit[k];
+  }
+  for (int k = 0; k < MAXN; ++k) {
+    C.inv_weights[k] = c->P.inv_weights[k];
+    C.inv_weights32[k] = (float)c->P.inv_weights[k];
+  }
+  C.nbr = c->d_nbr;
+  C.met = c->d_cmet;
+  C.ja32 = c->d_cja32;
+  C.invj32 = c->d_cinvj32;
+  C.xy = c->d_cxy;
+  C.sc = c->d_csc;
   return TG_OK;
 }
 
@@ -1147,9 +1274,44 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   if (cfg->source_terms != TG_SOURCE_NONE && !cfg->node_coordinates)
     return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "source terms need node_coordinates");
   const bool mixed = cfg->precision == TG_PRECISION_MIXED;
-  int epb = cfg->elements_per_block > 0 ? cfg->elements_per_block
-                                        : (mixed ? default_epb_mixed(D, N) : default_epb(D, N));
-  if (mixed ? !supported_epb_mixed(D, N, epb) : !supported_epb(D, N, epb))
+  if (cfg->mesh_type != TG_MESH_TREE && cfg->mesh_type != TG_MESH_CURVED)
+    return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "unknown mesh type %d", cfg->mesh_type);
+  const bool curved = cfg->mesh_type == TG_MESH_CURVED;
+  if (curved) {
+    // StructuredMesh / P4estMesh bricks: the curvilinear kernels of tg_curved.cu
+    if (D != 2) return fail(nullptr, TG_ERR_UNSUPPORTED, "curvilinear meshes are 2D only");
+    if (tg::curved_epb(N) == 0)
+      return fail(nullptr, TG_ERR_UNSUPPORTED, "curvilinear meshes: polydeg %d is not compiled",
+                  cfg->polydeg);
+    if (cfg->volume_integral == TG_VOLUME_SHOCK_CAPTURING_HG)
+      return fail(nullptr, TG_ERR_UNSUPPORTED,
+                  "curvilinear meshes: weak form or flux differencing only");
+    const int vf = cfg->volume_flux, sf = cfg->surface_flux;
+    if (cfg->volume_integral == TG_VOLUME_FLUX_DIFFERENCING &&
+        vf != TG_FLUX_CENTRAL && vf != TG_FLUX_RANOCHA && vf != TG_FLUX_SHIMA_ETAL &&
+        vf != TG_FLUX_CHANDRASHEKAR)
+      return fail(nullptr, TG_ERR_UNSUPPORTED,
+                  "curvilinear meshes: volume flux must be central, ranocha, shima_etal or "
+                  "chandrashekar");
+    if (sf == TG_FLUX_HLLC || sf == TG_FLUX_HLLE)
+      return fail(nullptr, TG_ERR_UNSUPPORTED, "curvilinear meshes: flux_hllc / flux_hlle");
+    if (cfg->nmortars != 0)
+      return fail(nullptr, TG_ERR_UNSUPPORTED, "curvilinear meshes: no mortars");
+    if (!cfg->contravariant_vectors)
+      return fail(nullptr, TG_ERR_INVALID_ARGUMENT,
+                  "curvilinear meshes need contravariant_vectors");
+    const int64_t nn = (int64_t)N * N;
+    for (int64_t k = 0; k < cfg->nelements * nn; ++k)
+      if (!(cfg->inverse_jacobian[k] > 0.0))
+        return fail(nullptr, TG_ERR_UNSUPPORTED,
+                    "curvilinear meshes: the mapping must preserve orientation (inverse Jacobian "
+                    "> 0 at every node)");
+  }
+  int epb = curved ? tg::curved_epb(N)
+                   : (cfg->elements_per_block > 0
+                          ? cfg->elements_per_block
+                          : (mixed ? default_epb_mixed(D, N) : default_epb(D, N)));
+  if (!curved && (mixed ? !supported_epb_mixed(D, N, epb) : !supported_epb(D, N, epb)))
     return fail(nullptr, TG_ERR_UNSUPPORTED, "elements_per_block %d not compiled for %dD N=%d", epb,
                 D, N);
 
@@ -1165,6 +1327,7 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   c->fp64 = cfg->precision == TG_PRECISION_FP64;
   c->epb = epb;
   c->device = cfg->device;
+  c->curved = curved;
 
   // ---- face-neighbour table from the interface container ----
   const int nf = 2 * D;
@@ -1243,7 +1406,7 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     has_dirichlet |= bc == TG_BOUNDARY_DIRICHLET;
   }
   for (size_t k = 0; k < nbr.size(); ++k)
-    if (nbr[k] == -1 && cfg->boundary_conditions[k % nf] == TG_BOUNDARY_PERIODIC) {
+    if (nbr[k] == -1 && (curved || cfg->boundary_conditions[k % nf] == TG_BOUNDARY_PERIODIC)) {
       delete c;
       return fail(nullptr, TG_ERR_UNSUPPORTED,
                   "element face without interface, mortar or boundary condition (direction %d)",
@@ -1271,7 +1434,7 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
 
   // ---- node coordinates along each axis (tensor-product TreeMesh elements) ----
   std::vector<double> xline;
-  if (cfg->node_coordinates) {
+  if (cfg->node_coordinates && !curved) {
     xline.resize((size_t)c->E * D * N);
     const double* X = cfg->node_coordinates;
     for (int64_t e = 0; e < c->E; ++e)
@@ -1531,6 +1694,13 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   M.nbc = (int32_t)c->nbound;
   M.ghost = c->d_ghost;
   M.mnbr = c->d_mnbr;
+  if (curved) {
+    int rc = curved_setup(c, cfg);
+    if (rc != TG_OK) {
+      free_ctx(c);
+      return rc;
+    }
+  }
   *out = c;
   return TG_OK;
 }
@@ -1556,6 +1726,8 @@ int tg_ndofs(const tg_ctx* ctx, int64_t* ndofs, int64_t* nvalues) {
 // (the other state buffer and the 2N register), with a scratch clock (dt = 0)
 // and status word and no wave-speed reduction, so the solution is unchanged.
 int tg_ctx_autotune(tg_ctx* c, int32_t iters, int32_t* best_epb, double* ms_per_stage) {
+  if (c && c->curved)
+    return fail(c, TG_ERR_UNSUPPORTED, "not available for curvilinear meshes");
   if (!c || iters <= 0) return TG_ERR_INVALID_ARGUMENT;
   if (!c->uploaded) return fail(c, TG_ERR_STATE, "no state uploaded");
   CUDA_TRY(c, cudaSetDevice(c->device));
@@ -1874,7 +2046,11 @@ int tg_integrals(tg_ctx* c, double* out) {
   const int K = c->NV + 2;
   if (!c->d_partial) CUDA_TRY(c, cudaMalloc((void**)&c->d_partial, sizeof(double) * K * c->E));
   const int64_t nb = (c->E + 127) / 128;
-  if (c->fp64) {
+  if (c->curved) {
+    if (tg::launch_curved_integrals(c->CP, c->d_u[c->cur], !c->fp64, c->d_weights, c->d_partial,
+                                    c->stream) != 0)
+      return fail(c, TG_ERR_CUDA, "curvilinear integrals launch failed");
+  } else if (c->fp64) {
     const double* u = (const double*)c->d_u[c->cur];
     if (c->D == 2)
       element_integrals_kernel<2, double><<<(unsigned)nb, 128, 0, c->stream>>>(
@@ -1899,6 +2075,8 @@ int tg_integrals(tg_ctx* c, double* out) {
 }
 
 int tg_entropy_timederivative(tg_ctx* c, double t, double* out) {
+  if (c && c->curved)
+    return fail(c, TG_ERR_UNSUPPORTED, "not available for curvilinear meshes");
   if (!c || !out) return TG_ERR_INVALID_ARGUMENT;
   CUDA_TRY(c, cudaSetDevice(c->device));
   const size_t vb = sizeof(double) * c->nvalues;
@@ -1928,6 +2106,8 @@ int tg_entropy_timederivative(tg_ctx* c, double t, double* out) {
 
 int tg_amr_indicator(tg_ctx* c, double alpha_max, double alpha_min, int32_t alpha_smooth,
                      int32_t variable, double* alpha_host) {
+  if (c && c->curved)
+    return fail(c, TG_ERR_UNSUPPORTED, "not available for curvilinear meshes");
   if (!c || !alpha_host) return TG_ERR_INVALID_ARGUMENT;
   if (variable != TG_INDICATOR_DENSITY_PRESSURE && variable != TG_INDICATOR_DENSITY)
     return fail(c, TG_ERR_INVALID_ARGUMENT, "unknown indicator variable %d", variable);
@@ -1955,6 +2135,8 @@ int tg_amr_indicator(tg_ctx* c, double alpha_max, double alpha_min, int32_t alph
 }
 
 int tg_amr_indicator_max(tg_ctx* c, int32_t variable, double* out_host) {
+  if (c && c->curved)
+    return fail(c, TG_ERR_UNSUPPORTED, "not available for curvilinear meshes");
   if (!c || !out_host) return TG_ERR_INVALID_ARGUMENT;
   if (!c->uploaded) return fail(c, TG_ERR_STATE, "no state uploaded");
   if (variable != TG_INDICATOR_DENSITY_PRESSURE && variable != TG_INDICATOR_DENSITY)
@@ -1989,6 +2171,8 @@ int tg_amr_indicator_max(tg_ctx* c, int32_t variable, double* out_host) {
 int tg_adapt_state(tg_ctx* dst, tg_ctx* src, const int64_t* source_element, const int8_t* kind,
                    const double* forward_upper, const double* forward_lower,
                    const double* reverse_upper, const double* reverse_lower) {
+  if ((dst && dst->curved) || (src && src->curved))
+    return fail(dst, TG_ERR_UNSUPPORTED, "not available for curvilinear meshes");
   if (!dst || !src || !source_element || !kind || !forward_upper || !forward_lower ||
       !reverse_upper || !reverse_lower)
     return TG_ERR_INVALID_ARGUMENT;

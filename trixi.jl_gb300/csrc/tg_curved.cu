@@ -1,0 +1,801 @@
+// Curvilinear 2D stage kernels (declarations and references in tg_curved.cuh).
+//
+// Layout as in the TreeMesh kernels: one block owns EPB consecutive elements
+// and stages their state in shared memory; one thread owns one (direction,
+// line) of an element, evaluates the N(N-1)/2 two-point fluxes of its line
+// once each (or the weak-form fluxes) and the two face fluxes at its ends,
+// accumulating the line's node contributions in registers; a node phase sums
+// the two directions, applies the per-node inverse Jacobian and the sources
+// and performs the 2N stage update.  Each interface flux is evaluated by both
+// elements, along their own contravariant vector of the shared face (equal up
+// to the rounding of the node coordinates the metric was built from), with
+// the element on the negative side as the left state.
+//
+// The mixed kernel evaluates the fluxes in deviation form relative to a
+// per-element reference state as the TreeMesh mixed kernel does.  The
+// two-point fluxes are linear in the normal direction n, so the deviation of
+// a flux along n is n_x times its deviation along x plus n_y times its
+// deviation along y; the reference flux f(w_e) . n drops out because the
+// metric terms satisfy the discrete metric identities (the scheme preserves
+// free streams), which is the curvilinear form of the cancellation used on
+// Cartesian elements.  The Lax-Friedrichs dissipation takes its speed from
+// the normal velocity and |n|.
+#include <cuda_runtime.h>
+
+#include "tg_curved.cuh"
+
+namespace tg {
+
+int curved_epb(int N) { return N == 3 || N == 4 ? 16 : (N == 5 ? 8 : 0); }
+
+// ---------------------------------------------------------------------------
+// FP64 fluxes along a normal direction, compressible_euler_2d.jl
+// ---------------------------------------------------------------------------
+struct FluxN {
+  using Eu = Euler<2, double>;
+
+  // flux(u, normal_direction), :436-448
+  static __device__ __forceinline__ void phys(const double* u, const double* w, double n0, double n1,
+                                              double* f) {
+    const double vn = w[1] * n0 + w[2] * n1;
+    const double rvn = w[0] * vn;
+    f[0] = rvn;
+    f[1] = fma(rvn, w[1], w[3] * n0);
+    f[2] = fma(rvn, w[2], w[3] * n1);
+    f[3] = (u[3] + w[3]) * vn;
+  }
+
+  // flux_ranocha(u_ll, u_rr, normal_direction), :724-753
+  static __device__ __forceinline__ void ranocha(const double* a, const double* b, double n0,
+                                                 double n1, double igm1, double* f) {
+    const double vna = a[1] * n0 + a[2] * n1, vnb = b[1] * n0 + b[2] * n1;
+    const double rho_mean = ln_mean(a[0], b[0]);
+    const double irpm = a[3] * b[3] * inv_ln_mean(a[0] * b[3], b[0] * a[3]);
+    const double v1 = 0.5 * (a[1] + b[1]), v2 = 0.5 * (a[2] + b[2]);
+    const double p_avg = 0.5 * (a[3] + b[3]);
+    const double vsq = 0.5 * (a[1] * b[1] + a[2] * b[2]);
+    const double f1 = rho_mean * 0.5 * (vna + vnb);
+    f[0] = f1;
+    f[1] = fma(f1, v1, p_avg * n0);
+    f[2] = fma(f1, v2, p_avg * n1);
+    f[3] = f1 * (vsq + irpm * igm1) + 0.5 * (a[3] * vnb + b[3] * vna);
+  }
+
+  // flux_shima_etal(u_ll, u_rr, normal_direction), :497-526
+  static __device__ __forceinline__ void shima(const double* a, const double* b, double n0,
+                                               double n1, double igm1, double* f) {
+    const double vna = a[1] * n0 + a[2] * n1, vnb = b[1] * n0 + b[2] * n1;
+    const double rho_avg = 0.5 * (a[0] + b[0]);
+    const double v1 = 0.5 * (a[1] + b[1]), v2 = 0.5 * (a[2] + b[2]);
+    const double vn_avg = 0.5 * (vna + vnb);
+    const double p_avg = 0.5 * (a[3] + b[3]);
+    const double vsq = 0.5 * (a[1] * b[1] + a[2] * b[2]);
+    const double f1 = rho_avg * vn_avg;
+    f[0] = f1;
+    f[1] = fma(f1, v1, p_avg * n0);
+    f[2] = fma(f1, v2, p_avg * n1);
+    f[3] = f1 * vsq + p_avg * vn_avg * igm1 + 0.5 * (a[3] * vnb + b[3] * vna);
+  }
+
+  // flux_chandrashekar(u_ll, u_rr, normal_direction), :639-670
+  static __device__ __forceinline__ void chandrashekar(const double* a, const double* b, double n0,
+                                                       double n1, double gamma, double* f) {
+    const double vna = a[1] * n0 + a[2] * n1, vnb = b[1] * n0 + b[2] * n1;
+    const double beta_a = 0.5 * a[0] / a[3], beta_b = 0.5 * b[0] / b[3];
+    const double kin_a = 0.5 * (a[1] * a[1] + a[2] * a[2]);
+    const double kin_b = 0.5 * (b[1] * b[1] + b[2] * b[2]);
+    const double rho_avg = 0.5 * (a[0] + b[0]);
+    const double rho_mean = ln_mean(a[0], b[0]);
+    const double beta_mean = ln_mean(beta_a, beta_b);
+    const double beta_avg = 0.5 * (beta_a + beta_b);
+    const double v1 = 0.5 * (a[1] + b[1]), v2 = 0.5 * (a[2] + b[2]);
+    const double p_mean = 0.5 * rho_avg / beta_avg;
+    const double f1 = rho_mean * 0.5 * (vna + vnb);
+    f[0] = f1;
+    f[1] = fma(f1, v1, p_mean * n0);
+    f[2] = fma(f1, v2, p_mean * n1);
+    f[3] = f1 * 0.5 * (1 / (gamma - 1) / beta_mean - (kin_a + kin_b)) + f[1] * v1 + f[2] * v2;
+  }
+
+  // two-point flux of kind k between states (u, w) a and b along (n0, n1):
+  // central (+ local Lax-Friedrichs dissipation, max_abs_speed(_naive) along
+  // the normal, :1443-1509, numerical_fluxes.jl:17-45, 166-253), ranocha,
+  // shima_etal, chandrashekar
+  static __device__ __forceinline__ void two_point(int k, const double* ua, const double* wa,
+                                                   const double* ub, const double* wb, double n0,
+                                                   double n1, double gamma, double igm1,
+                                                   double* f) {
+    switch (k) {
+      case FLUX_RANOCHA: ranocha(wa, wb, n0, n1, igm1, f); return;
+      case FLUX_SHIMA_ETAL: shima(wa, wb, n0, n1, igm1, f); return;
+      case FLUX_CHANDRASHEKAR: chandrashekar(wa, wb, n0, n1, gamma, f); return;
+      default: break;
+    }
+    double fa[4], fb[4];
+    phys(ua, wa, n0, n1, fa);
+    phys(ub, wb, n0, n1, fb);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) f[v] = 0.5 * (fa[v] + fb[v]);
+    if (k == FLUX_LLF || k == FLUX_LLF_NAIVE) {
+      const double va = wa[1] * n0 + wa[2] * n1, vb = wb[1] * n0 + wb[2] * n1;
+      const double ca = sqrt(gamma * wa[3] / wa[0]), cb = sqrt(gamma * wb[3] / wb[0]);
+      const double nn = sqrt(n0 * n0 + n1 * n1);
+      const double lam = k == FLUX_LLF_NAIVE ? fmax(fabs(va), fabs(vb)) + fmax(ca, cb) * nn
+                                             : fmax(fabs(va) + ca * nn, fabs(vb) + cb * nn);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) f[v] = f[v] + (-0.5 * lam * (ub[v] - ua[v]));
+    }
+  }
+};
+
+template <int N>
+__device__ __forceinline__ int cline_node(int line, int dd, int a) {
+  // node a of line `line` in direction dd (node index q = i + N j)
+  return dd == 0 ? a + N * line : line + N * a;
+}
+
+// Node of the neighbour across face dir of an element that meets face node fn.
+template <int N>
+__device__ __forceinline__ int cface_partner(int dir, int fn) {
+  switch (dir) {
+    case 0: return (N - 1) + N * fn;  // -x: neighbour's +x face
+    case 1: return N * fn;            // +x: neighbour's -x face
+    case 2: return fn + N * (N - 1);  // -y: neighbour's +y face
+    default: return fn;               // +y: neighbour's -y face
+  }
+}
+
+}  // namespace tg
+
+namespace tg {
+
+template <int N, int EPB>
+struct CurvedK {
+  static constexpr int NN = N * N, NV = 4, NT = EPB * 2 * N;
+  static constexpr int CHUNK = EPB * NN * NV;  // state values of a block
+  static constexpr int FACE = EPB * 4 * N * NV;
+  static constexpr int SP = EPB * NN;          // field stride of the partial sums
+};
+
+// ---------------------------------------------------------------------------
+// FP64 stage kernel
+// ---------------------------------------------------------------------------
+template <int N, int VI, int EPB>
+__global__ void __launch_bounds__(CurvedK<N, EPB>::NT)
+    curved_kernel_f64(const CurvedParams P, const StageArgs A) {
+  using K = CurvedK<N, EPB>;
+  using Eu = Euler<2, double>;
+  constexpr int NN = K::NN, NV = 4, NT = K::NT, SP = K::SP, CHUNK = K::CHUNK;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* s_u = reinterpret_cast<double*>(smem_raw);
+  double* s_fu = s_u + CHUNK;
+  double* s_part = s_fu + K::FACE;                       // [2][NV][SP]
+  unsigned long long* s_smax = reinterpret_cast<unsigned long long*>(s_part + 2 * NV * SP);
+
+  const int tid = threadIdx.x;
+  const int64_t e0 = (int64_t)blockIdx.x * EPB;
+  const int nel = (int)min((int64_t)EPB, P.nelements - e0);
+  const size_t gofs = (size_t)e0 * NN * NV;
+  const int nval = nel * NN * NV;
+  const double gamma = P.gamma, igm1 = P.inv_gamma_minus_one;
+
+  if (A.mode == MODE_STAGE && A.clock->skip) {
+    for (int k = tid; k < nval; k += NT) A.u_out[gofs + k] = A.u_in[gofs + k];
+    return;
+  }
+  for (int k = tid; k < nval; k += NT) s_u[k] = __ldg(A.u_in + gofs + k);
+  for (int k = tid; k < nel * 4 * N; k += NT) {
+    const int sl = k / (4 * N);
+    const int dir = (k / N) & 3;
+    const int fn = k % N;
+    const int32_t nb = P.nbr[(e0 + sl) * 4 + dir];
+    if (nb >= e0 && nb < e0 + nel) continue;  // read from s_u below
+    const double* g = A.u_in + ((size_t)nb * NN + cface_partner<N>(dir, fn)) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) s_fu[k * NV + v] = __ldg(g + v);
+  }
+  if (tid < 2 * EPB) s_smax[tid] = 0ull;
+  __syncthreads();
+
+  // ---- lines ---------------------------------------------------------------------
+  {
+    const int dd = tid / (EPB * N);
+    const int r = tid - dd * (EPB * N);
+    const int sl = r / N;
+    const int line = r - sl * N;
+    if (sl < nel) {
+      const int64_t e = e0 + sl;
+      double uu[N][NV], ww[N][NV], ja[N][2];
+#pragma unroll
+      for (int a = 0; a < N; ++a) {
+        const int q = cline_node<N>(line, dd, a);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) uu[a][v] = s_u[(sl * NN + q) * NV + v];
+        Eu::cons2prim(uu[a], ww[a], gamma);
+        const double* m = P.met + ((size_t)e * NN + q) * 5 + 2 * dd;
+        ja[a][0] = m[0];
+        ja[a][1] = m[1];
+      }
+      double acc[N][NV];
+#pragma unroll
+      for (int a = 0; a < N; ++a)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc[a][v] = 0.0;
+      if (VI == VI_WEAK) {
+#pragma unroll
+        for (int a = 0; a < N; ++a) {
+          double f[NV];
+          FluxN::phys(uu[a], ww[a], ja[a][0], ja[a][1], f);
+#pragma unroll
+          for (int ii = 0; ii < N; ++ii) {
+            const double c = P.Dhat[ii * N + a];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[ii][v] = fma(c, f[v], acc[ii][v]);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int a = 0; a < N; ++a)
+#pragma unroll
+          for (int b = a + 1; b < N; ++b) {
+            double F[NV];
+            FluxN::two_point(P.volume_flux, uu[a], ww[a], uu[b], ww[b], 0.5 * (ja[a][0] + ja[b][0]),
+                             0.5 * (ja[a][1] + ja[b][1]), gamma, igm1, F);
+            const double cab = P.Dsplit[a * N + b], cba = P.Dsplit[b * N + a];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+              acc[a][v] = fma(cab, F[v], acc[a][v]);
+              acc[b][v] = fma(cba, F[v], acc[b][v]);
+            }
+          }
+      }
+      // faces -dd (node 0) and +dd (node N-1), along this element's
+      // contravariant vector, negative-side element as the left state
+      const double factor = P.inv_weights[0];
+#pragma unroll
+      for (int side = 0; side < 2; ++side) {
+        const int dir = 2 * dd + side;
+        const int32_t nb = P.nbr[e * 4 + dir];
+        const int own = side ? N - 1 : 0;
+        const double* src = (nb >= e0 && nb < e0 + nel)
+                                ? s_u + (((int)(nb - e0)) * NN + cface_partner<N>(dir, line)) * NV
+                                : s_fu + ((sl * 4 + dir) * N + line) * NV;
+        double un[NV], wn[NV], F[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) un[v] = src[v];
+        Eu::cons2prim(un, wn, gamma);
+        if (side)
+          FluxN::two_point(P.surface_flux, uu[own], ww[own], un, wn, ja[own][0], ja[own][1], gamma,
+                           igm1, F);
+        else
+          FluxN::two_point(P.surface_flux, un, wn, uu[own], ww[own], ja[own][0], ja[own][1], gamma,
+                           igm1, F);
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          acc[own][v] = side ? acc[own][v] + F[v] * factor : acc[own][v] - F[v] * factor;
+      }
+#pragma unroll
+      for (int a = 0; a < N; ++a) {
+        const int q = cline_node<N>(line, dd, a);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) s_part[(dd * NV + v) * SP + sl * NN + q] = acc[a][v];
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- nodes -----------------------------------------------------------------------
+  const bool stage = A.mode == MODE_STAGE;
+  const double bdt = stage ? A.b * A.clock->dt : 0.0;
+  bool bad = false;
+  for (int n = tid; n < nel * NN; n += NT) {
+    const int sl = n / NN;
+    const int q = n - sl * NN;
+    const int64_t e = e0 + sl;
+    const double* m = P.met + ((size_t)e * NN + q) * 5;
+    const double jfac = -m[4];
+    double du[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) du[v] = (s_part[v * SP + n] + s_part[(NV + v) * SP + n]) * jfac;
+    if (P.source == SRC_CONVERGENCE_TEST) {
+      double x[2], s[NV];
+      x[0] = P.xy[((size_t)e * NN + q) * 2];
+      x[1] = P.xy[((size_t)e * NN + q) * 2 + 1];
+      const double tt = stage ? A.clock->t + A.c * A.clock->dt : A.t_rhs;
+      Eu::source_convergence(x, tt, gamma, s);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) du[v] += s[v];
+    }
+    const size_t g = gofs + (size_t)n * NV;
+    if (!stage) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) A.du_out[g + v] = du[v];
+      continue;
+    }
+    double* ut = reinterpret_cast<double*>(A.u_tmp) + g;
+    double un[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const double t0 = A.zero_tmp ? 0.0 : ut[v];
+      const double t1 = du[v] - t0 * A.a;
+      ut[v] = t1;
+      un[v] = s_u[n * NV + v] + t1 * bdt;
+      A.u_out[g + v] = un[v];
+      bad |= !(un[v] == un[v]);
+    }
+    if (A.speed_bits) {
+      double w[NV];
+      Eu::cons2prim(un, w, gamma);
+      const double cs = sqrt(gamma * w[3] / w[0]);
+      bad |= !(w[0] > 0.0) || !(w[3] > 0.0);
+      const double l1 = fabs(w[1]) + cs, l2 = fabs(w[2]) + cs;
+      const double ij = fabs(m[4]);
+      const double s1 = fabs(m[0] * l1 + m[1] * l2) * ij;
+      const double s2 = fabs(m[2] * l1 + m[3] * l2) * ij;
+      if (s1 == s1) atomicMax(&s_smax[2 * sl], (unsigned long long)__double_as_longlong(s1));
+      if (s2 == s2) atomicMax(&s_smax[2 * sl + 1], (unsigned long long)__double_as_longlong(s2));
+    }
+  }
+  if (bad) atomicOr(A.status, 1);
+  if (stage && A.speed_bits) {
+    __syncthreads();
+    if (tid < nel) {
+      const double sp = __longlong_as_double((long long)s_smax[2 * tid]) +
+                        __longlong_as_double((long long)s_smax[2 * tid + 1]);
+      if (sp == sp) atomicMax(A.speed_bits, (unsigned long long)__double_as_longlong(sp));
+    }
+  }
+}
+
+}  // namespace tg
+
+namespace tg {
+
+// ---------------------------------------------------------------------------
+// Mixed-precision stage kernel (float-float state, FP32 deviation fluxes)
+// ---------------------------------------------------------------------------
+
+// Deviation of the two-point flux of kind KIND (or `kind` at run time) along
+// the normal (n0, n1): n0 times its deviation along x plus n1 times its
+// deviation along y (the fluxes are linear in the normal direction).
+template <int KIND>
+__device__ __forceinline__ void dev_flux_n(int kind, const RefState<2>& R, const Node<2>& a,
+                                           const Node<2>& b, float n0, float n1, const EosF& eos,
+                                           float* F) {
+  using Dv = Dev<2>;
+  Node<2> ax = a, bx = b, ay = a, by = b;
+  Dv::orient(ax, 0);
+  Dv::orient(bx, 0);
+  Dv::orient(ay, 1);
+  Dv::orient(by, 1);
+  float fx[4], fy[4];
+  Dv::template flux2<KIND>(kind, R, ax, bx, 0, R.v[0], eos, fx);
+  Dv::template flux2<KIND>(kind, R, ay, by, 1, R.v[1], eos, fy);
+#pragma unroll
+  for (int v = 0; v < 4; ++v) F[v] = fmaf(n1, fy[v], n0 * fx[v]);
+}
+
+// Surface flux deviation along n: the linear fluxes as above; the
+// Lax-Friedrichs fluxes as the central flux plus the dissipation
+// -lambda/2 (u_b - u_a) with lambda from the normal velocities and |n|.
+__device__ __forceinline__ void dev_surface_n(int kind, const RefState<2>& R, const Node<2>& a,
+                                              const Node<2>& b, float n0, float n1,
+                                              const EosF& eos, float* F) {
+  if (kind != FLUX_LLF && kind != FLUX_LLF_NAIVE) {
+    dev_flux_n<-1>(kind, R, a, b, n0, n1, eos, F);
+    return;
+  }
+  dev_flux_n<FLUX_CENTRAL>(FLUX_CENTRAL, R, a, b, n0, n1, eos, F);
+  const float va = a.w[1] * n0 + a.w[2] * n1, vb = b.w[1] * n0 + b.w[2] * n1;
+  const float ca = sqrtf(eos.gamma * a.w[3] / a.w[0]), cb = sqrtf(eos.gamma * b.w[3] / b.w[0]);
+  const float nn = sqrtf(n0 * n0 + n1 * n1);
+  const float lam = kind == FLUX_LLF_NAIVE ? fmaxf(fabsf(va), fabsf(vb)) + fmaxf(ca, cb) * nn
+                                           : fmaxf(fabsf(va) + ca * nn, fabsf(vb) + cb * nn);
+#pragma unroll
+  for (int v = 0; v < 4; ++v) F[v] = F[v] + (-0.5f * lam * (b.du[v] - a.du[v]));
+}
+
+template <int N, int VI, int EPB>
+__global__ void __launch_bounds__(CurvedK<N, EPB>::NT)
+    curved_kernel_mixed(const CurvedParams P, const MixedArgs A) {
+  using K = CurvedK<N, EPB>;
+  using Dv = Dev<2>;
+  constexpr int NN = K::NN, NV = 4, NT = K::NT, SP = K::SP, CHUNK = K::CHUNK;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* s_u = reinterpret_cast<float2*>(smem_raw);
+  float2* s_fu = s_u + CHUNK;
+  float* s_nd = reinterpret_cast<float*>(s_fu + K::FACE);  // [NV + 1][SP]: dw, dq
+  float* s_part = s_nd + (NV + 1) * SP;                     // [2][NV][SP]
+  RefState<2>* s_ref = reinterpret_cast<RefState<2>*>(s_part + 2 * NV * SP);
+  float* s_scal = reinterpret_cast<float*>(s_ref + EPB);    // b dt, a (hi, lo)
+  unsigned int* s_smax = reinterpret_cast<unsigned int*>(s_scal + 4);
+
+  const int tid = threadIdx.x;
+  const int64_t e0 = (int64_t)blockIdx.x * EPB;
+  const int nel = (int)min((int64_t)EPB, P.nelements - e0);
+  const size_t gofs = (size_t)e0 * NN * NV;
+  const int nval = nel * NN * NV;
+  const EosF& eos = P.eos;
+  const bool stage = A.mode == MODE_STAGE;
+
+  if (stage && A.clock->skip) {
+    for (int k = tid; k < nval; k += NT) A.u_out[gofs + k] = A.u_in[gofs + k];
+    return;
+  }
+  {
+    // gofs is even (NN * NV is), so the chunk is 16-byte aligned; nval is even
+    const float4* src = reinterpret_cast<const float4*>(A.u_in + gofs);
+    float4* dst = reinterpret_cast<float4*>(s_u);
+    for (int k = tid; k < nval / 2; k += NT) cp_async16(dst + k, src + k);
+  }
+  for (int k = tid; k < nel * 4 * N; k += NT) {
+    const int sl = k / (4 * N);
+    const int dir = (k / N) & 3;
+    const int fn = k % N;
+    const int32_t nb = P.nbr[(e0 + sl) * 4 + dir];
+    if (nb >= e0 && nb < e0 + nel) continue;
+    const float2* g = A.u_in + ((size_t)nb * NN + cface_partner<N>(dir, fn)) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) cp_async8(s_fu + k * NV + v, g + v);
+  }
+  if (tid < 2 * EPB) s_smax[tid] = 0u;
+  if (tid == 0) {
+    const double bdt = stage ? A.b * A.clock->dt : 0.0;
+    const float bh = (float)bdt, ah = (float)A.a;
+    s_scal[0] = bh;
+    s_scal[1] = (float)(bdt - (double)bh);
+    s_scal[2] = ah;
+    s_scal[3] = (float)(A.a - (double)ah);
+  }
+  if (tid < nel) {
+    // reference state: mean hi of two opposite corner nodes
+    const float2* ue = A.u_in + (size_t)(e0 + tid) * NN * NV;
+    float hi[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) hi[v] = 0.5f * (ue[v].x + ue[(NN - 1) * NV + v].x);
+    Dv::make_ref(hi, eos, s_ref[tid]);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+
+  for (int n = tid; n < nel * NN; n += NT) {
+    const int sl = n / NN;
+    float hi[NV], lo[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const float2 x = s_u[n * NV + v];
+      hi[v] = x.x;
+      lo[v] = x.y;
+    }
+    Node<2> nd;
+    Dv::make_node(hi, lo, s_ref[sl], eos, nd);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) s_nd[v * SP + n] = nd.dw[v];
+    s_nd[NV * SP + n] = nd.dq;
+  }
+  __syncthreads();
+
+  // ---- lines ---------------------------------------------------------------------
+  {
+    const int dd = tid / (EPB * N);
+    const int r = tid - dd * (EPB * N);
+    const int sl = r / N;
+    const int line = r - sl * N;
+    if (sl < nel) {
+      const int64_t e = e0 + sl;
+      const RefState<2>& R = s_ref[sl];
+      Node<2> nd[N];
+      float ja[N][2];
+#pragma unroll
+      for (int a = 0; a < N; ++a) {
+        const int q = cline_node<N>(line, dd, a);
+        const int n = sl * NN + q;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) nd[a].dw[v] = s_nd[v * SP + n];
+        nd[a].dq = s_nd[NV * SP + n];
+        Dv::complete(R, nd[a]);
+        const float4 j = P.ja32[(size_t)e * NN + q];
+        ja[a][0] = dd ? j.z : j.x;
+        ja[a][1] = dd ? j.w : j.y;
+      }
+      float acc[N][NV];
+#pragma unroll
+      for (int a = 0; a < N; ++a)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc[a][v] = 0.0f;
+      if (VI == VI_WEAK) {
+#pragma unroll
+        for (int a = 0; a < N; ++a) {
+          Node<2> ax = nd[a], ay = nd[a];
+          Dv::orient(ax, 0);
+          Dv::orient(ay, 1);
+          float fx[NV], fy[NV];
+          Dv::dflux(R, ax, 0, R.v[0], eos, fx);
+          Dv::dflux(R, ay, 1, R.v[1], eos, fy);
+#pragma unroll
+          for (int ii = 0; ii < N; ++ii) {
+            const float c = P.Dhat32[ii * N + a];
+#pragma unroll
+            for (int v = 0; v < NV; ++v)
+              acc[ii][v] = fmaf(c, fmaf(ja[a][1], fy[v], ja[a][0] * fx[v]), acc[ii][v]);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int a = 0; a < N; ++a)
+#pragma unroll
+          for (int b = a + 1; b < N; ++b) {
+            float F[NV];
+            dev_flux_n<-1>(P.volume_flux, R, nd[a], nd[b], 0.5f * (ja[a][0] + ja[b][0]),
+                           0.5f * (ja[a][1] + ja[b][1]), eos, F);
+            const float cab = P.Dsplit32[a * N + b], cba = P.Dsplit32[b * N + a];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+              acc[a][v] = fmaf(cab, F[v], acc[a][v]);
+              acc[b][v] = fmaf(cba, F[v], acc[b][v]);
+            }
+          }
+      }
+      const float factor = P.inv_weights32[0];
+#pragma unroll
+      for (int side = 0; side < 2; ++side) {
+        const int dir = 2 * dd + side;
+        const int32_t nb = P.nbr[e * 4 + dir];
+        const int own = side ? N - 1 : 0;
+        Dv::node_du(s_u + ((size_t)sl * NN + cline_node<N>(line, dd, own)) * NV, R, nd[own].du);
+        const float2* src = (nb >= e0 && nb < e0 + nel)
+                                ? s_u + (((int)(nb - e0)) * NN + cface_partner<N>(dir, line)) * NV
+                                : s_fu + ((sl * 4 + dir) * N + line) * NV;
+        float hi[NV], lo[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          hi[v] = src[v].x;
+          lo[v] = src[v].y;
+        }
+        Node<2> other;
+        Dv::make_node(hi, lo, R, eos, other);
+        float F[NV];
+        if (side)
+          dev_surface_n(P.surface_flux, R, nd[own], other, ja[own][0], ja[own][1], eos, F);
+        else
+          dev_surface_n(P.surface_flux, R, other, nd[own], ja[own][0], ja[own][1], eos, F);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc[own][v] = fmaf(side ? F[v] : -F[v], factor, acc[own][v]);
+      }
+#pragma unroll
+      for (int a = 0; a < N; ++a) {
+        const int q = cline_node<N>(line, dd, a);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) s_part[(dd * NV + v) * SP + sl * NN + q] = acc[a][v];
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- nodes -----------------------------------------------------------------------
+  const float bdt = s_scal[0], bdt_lo = s_scal[1], a_s = s_scal[2], a_lo = s_scal[3];
+  float st = 0, ct = 0, stl = 0, ctl = 0;
+  if (P.source == SRC_CONVERGENCE_TEST) {
+    if (stage) {
+      st = A.clock->sin_t[A.stage];
+      ct = A.clock->cos_t[A.stage];
+      stl = A.clock->sin_tl[A.stage];
+      ctl = A.clock->cos_tl[A.stage];
+    } else {
+      st = A.sin_t, ct = A.cos_t, stl = A.sin_tl, ctl = A.cos_tl;
+    }
+  }
+  bool bad = false;
+  for (int n = tid; n < nel * NN; n += NT) {
+    const int sl = n / NN;
+    const int q = n - sl * NN;
+    const int64_t e = e0 + sl;
+    const size_t gq = (size_t)e * NN + q;
+    const float jfac = -P.invj32[gq];
+    float du[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) du[v] = (s_part[v * SP + n] + s_part[(NV + v) * SP + n]) * jfac;
+    if (P.source == SRC_CONVERGENCE_TEST) {
+      // sin/cos(pi (x + y - t)) by the angle-difference formula in float-float
+      const float4 o = P.sc[gq];
+      const float2 sn = ff_dot2(o.x, o.z, ct, ctl, -o.y, -o.w, st, stl);
+      const float2 cs = ff_dot2(o.y, o.w, ct, ctl, o.x, o.z, st, stl);
+      float s[NV];
+      SourceMMS<2>::eval(sn.x, cs.x, eos, s);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) du[v] += s[v];
+    }
+    const size_t g = gofs + (size_t)n * NV;
+    if (!stage) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) A.du_out[g + v] = (double)du[v];
+      continue;
+    }
+    float hi[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const float old = A.zero_tmp ? 0.0f : A.u_tmp[g + v];
+      const float ut = fmaf(-a_lo, old, fmaf(-a_s, old, du[v]));
+      A.u_tmp[g + v] = ut;
+      const float2 un = ff_add(s_u[n * NV + v], fmaf(ut, bdt_lo, ut * bdt));
+      A.u_out[g + v] = un;
+      hi[v] = un.x;
+      bad |= !(un.x == un.x);
+    }
+    if (A.speed_bits) {
+      float w[NV];
+      Euler<2, float>::cons2prim(hi, w, eos.gamma);
+      const float cs = sqrtf(eos.gamma * w[3] / w[0]);
+      bad |= !(w[0] > 0.0f) || !(w[3] > 0.0f);
+      const float l1 = fabsf(w[1]) + cs, l2 = fabsf(w[2]) + cs;
+      const float4 j = P.ja32[gq];
+      const float ij = fabsf(P.invj32[gq]);
+      const float s1 = fabsf(j.x * l1 + j.y * l2) * ij;
+      const float s2 = fabsf(j.z * l1 + j.w * l2) * ij;
+      if (s1 == s1) atomicMax(&s_smax[2 * sl], __float_as_uint(s1));
+      if (s2 == s2) atomicMax(&s_smax[2 * sl + 1], __float_as_uint(s2));
+    }
+  }
+  if (bad) atomicOr(A.status, 1);
+  if (stage && A.speed_bits) {
+    __syncthreads();
+    if (tid < nel) {
+      const float sp = __uint_as_float(s_smax[2 * tid]) + __uint_as_float(s_smax[2 * tid + 1]);
+      if (sp == sp) atomicMax(A.speed_bits, (unsigned long long)__double_as_longlong((double)sp));
+    }
+  }
+}
+
+}  // namespace tg
+
+namespace tg {
+
+__device__ __forceinline__ double cstate(double x) { return x; }
+__device__ __forceinline__ double cstate(float2 x) { return (double)x.x + (double)x.y; }
+
+// max_dt of a curvilinear mesh (stepsize_dg2d.jl:114-157), one thread per
+// element: FP64 for an FP64 state, the stage kernel's FP32 arithmetic on the
+// hi parts for a float-float state.
+template <typename TS>
+__global__ void curved_speed_kernel(const CurvedParams P, const TS* __restrict__ u, int NN,
+                                    unsigned long long* __restrict__ speed_bits,
+                                    int32_t* __restrict__ status) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.nelements) return;
+  constexpr bool FF = !std::is_same<TS, double>::value;
+  double m1 = 0, m2 = 0;
+  bool bad = false;
+  for (int q = 0; q < NN; ++q) {
+    const size_t gq = (size_t)e * NN + q;
+    const TS* p = u + gq * 4;
+    double s1, s2;
+    if constexpr (FF) {
+      float hi[4], w[4];
+      for (int v = 0; v < 4; ++v) hi[v] = reinterpret_cast<const float2*>(p)[v].x;
+      Euler<2, float>::cons2prim(hi, w, P.eos.gamma);
+      const float cs = sqrtf(P.eos.gamma * w[3] / w[0]);
+      bad |= !(w[0] > 0.0f) || !(w[3] > 0.0f);
+      const float l1 = fabsf(w[1]) + cs, l2 = fabsf(w[2]) + cs;
+      const float4 j = P.ja32[gq];
+      const float ij = fabsf(P.invj32[gq]);
+      s1 = (double)(fabsf(j.x * l1 + j.y * l2) * ij);
+      s2 = (double)(fabsf(j.z * l1 + j.w * l2) * ij);
+    } else {
+      double uu[4], w[4];
+      for (int v = 0; v < 4; ++v) uu[v] = cstate(p[v]);
+      Euler<2, double>::cons2prim(uu, w, P.gamma);
+      const double cs = sqrt(P.gamma * w[3] / w[0]);
+      bad |= !(w[0] > 0) || !(w[3] > 0);
+      const double l1 = fabs(w[1]) + cs, l2 = fabs(w[2]) + cs;
+      const double* m = P.met + gq * 5;
+      s1 = fabs(m[0] * l1 + m[1] * l2) * fabs(m[4]);
+      s2 = fabs(m[2] * l1 + m[3] * l2) * fabs(m[4]);
+    }
+    m1 = fmax(m1, s1);
+    m2 = fmax(m2, s2);
+  }
+  const double sp = m1 + m2;
+  if (sp == sp)
+    atomicMax(speed_bits, (unsigned long long)__double_as_longlong(sp));
+  else
+    bad = true;
+  if (bad) atomicOr(status, 2);
+}
+
+// Per-element FP64 integrals with the per-node Jacobian |J| = 1/|invJ|
+// (integrate_via_indices, analysis_dg2d.jl:313-336): conserved totals,
+// mathematical entropy and kinetic energy, as element_integrals_kernel.
+template <typename TS>
+__global__ void curved_integrals_kernel(const CurvedParams P, const TS* __restrict__ u,
+                                        const double* __restrict__ weights, int N,
+                                        double* __restrict__ partial) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.nelements) return;
+  const int NN = N * N;
+  const double g = P.gamma;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int q = 0; q < NN; ++q) {
+    const size_t gq = (size_t)e * NN + q;
+    const double w = weights[q % N] * weights[q / N] / fabs(P.met[gq * 5 + 4]);
+    double p[4];
+    for (int v = 0; v < 4; ++v) p[v] = cstate(u[gq * 4 + v]);
+    const double m2 = p[1] * p[1] + p[2] * p[2];
+    for (int v = 0; v < 4; ++v) acc[v] += w * p[v];
+    const double pr = (g - 1) * (p[3] - 0.5 * m2 / p[0]);
+    const double s = log(pr) - g * log(p[0]);
+    acc[4] += w * (-s * p[0] / (g - 1));
+    acc[5] += w * (m2 / (2 * p[0]));
+  }
+  for (int k = 0; k < 6; ++k) partial[(size_t)e * 6 + k] = acc[k];
+}
+
+template <int N, int VI>
+static int launch_curved_n(const CurvedParams& P, const StageArgs* A64, const MixedArgs* A32,
+                           cudaStream_t stream) {
+  constexpr int EPB = N == 5 ? 8 : 16;
+  using K = CurvedK<N, EPB>;
+  const unsigned nb = (unsigned)((P.nelements + EPB - 1) / EPB);
+  if (A64) {
+    const size_t smem = sizeof(double) * (K::CHUNK + K::FACE + 2 * 4 * K::SP) +
+                        sizeof(unsigned long long) * 2 * EPB;
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(curved_kernel_f64<N, VI, EPB>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      attr = true;
+    }
+    curved_kernel_f64<N, VI, EPB><<<nb, K::NT, smem, stream>>>(P, *A64);
+  } else {
+    const size_t smem = sizeof(float2) * (K::CHUNK + K::FACE) +
+                        sizeof(float) * ((4 + 1) * K::SP + 2 * 4 * K::SP) +
+                        sizeof(RefState<2>) * EPB + sizeof(float) * 4 +
+                        sizeof(unsigned int) * 2 * EPB;
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(curved_kernel_mixed<N, VI, EPB>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      attr = true;
+    }
+    curved_kernel_mixed<N, VI, EPB><<<nb, K::NT, smem, stream>>>(P, *A32);
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_curved(const CurvedParams& P, const StageArgs* A64, const MixedArgs* A32,
+                  cudaStream_t stream) {
+  if ((A64 == nullptr) == (A32 == nullptr)) return -2;
+  const bool weak = P.vi == VI_WEAK;
+  switch (P.N) {
+    case 3: return weak ? launch_curved_n<3, VI_WEAK>(P, A64, A32, stream)
+                        : launch_curved_n<3, VI_FD>(P, A64, A32, stream);
+    case 4: return weak ? launch_curved_n<4, VI_WEAK>(P, A64, A32, stream)
+                        : launch_curved_n<4, VI_FD>(P, A64, A32, stream);
+    case 5: return weak ? launch_curved_n<5, VI_WEAK>(P, A64, A32, stream)
+                        : launch_curved_n<5, VI_FD>(P, A64, A32, stream);
+    default: return -3;
+  }
+}
+
+int launch_curved_speed(const CurvedParams& P, const void* u, bool ff, unsigned long long* dst,
+                        int32_t* status, cudaStream_t stream) {
+  const unsigned nb = (unsigned)((P.nelements + 127) / 128);
+  if (ff)
+    curved_speed_kernel<float2><<<nb, 128, 0, stream>>>(P, (const float2*)u, P.N * P.N, dst, status);
+  else
+    curved_speed_kernel<double><<<nb, 128, 0, stream>>>(P, (const double*)u, P.N * P.N, dst, status);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_curved_integrals(const CurvedParams& P, const void* u, bool ff, const double* weights,
+                            double* partial, cudaStream_t stream) {
+  const unsigned nb = (unsigned)((P.nelements + 127) / 128);
+  if (ff)
+    curved_integrals_kernel<float2><<<nb, 128, 0, stream>>>(P, (const float2*)u, weights, P.N,
+                                                            partial);
+  else
+    curved_integrals_kernel<double><<<nb, 128, 0, stream>>>(P, (const double*)u, weights, P.N,
+                                                            partial);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace tg

@@ -1,0 +1,55 @@
+// Fused DGSEM stage kernels of curvilinear 2D meshes (StructuredMesh and
+// P4estMesh bricks), FP64 and mixed precision, for sm_103a.
+//
+// The element work follows dgsem_structured/dg_2d.jl: volume integrals with
+// contravariant fluxes (weak_form_kernel! :34-75 with Ja^i . f, and
+// flux_differencing_kernel! :77-139 with the two-point flux along the averaged
+// contravariant vector), interface fluxes along the contravariant vector of
+// the element face (calc_interface_flux!, :551-606; dgsem_p4est/dg_2d.jl:263-
+// 434), the surface integral of dgsem_tree/dg_2d.jl:1245-1287, apply_jacobian!
+// with the per-node inverse Jacobian (dgsem_structured/dg_2d.jl:751-771) and
+// sources at the node coordinates.  The CFL reduction is the curvilinear
+// max_dt (stepsize_dg2d.jl:114-157).
+#pragma once
+
+#include "tg_mixed.cuh"
+
+namespace tg {
+
+struct CurvedParams {
+  int64_t nelements;
+  int32_t N;                // nodes per direction
+  int32_t vi;               // VI_WEAK or VI_FD
+  int32_t volume_flux, surface_flux, source;
+  double gamma, inv_gamma_minus_one;
+  EosF eos;
+  // n x n matrices row-major with the actual n: M[a * n + b] = M[a, b]
+  double Dhat[MAXN * MAXN], Dsplit[MAXN * MAXN], inv_weights[MAXN];
+  float Dhat32[MAXN * MAXN], Dsplit32[MAXN * MAXN], inv_weights32[MAXN];
+  const int32_t* nbr;       // [E][4]: element across -x, +x, -y, +y
+  const double* met;        // [E][NN][5]: Ja^1_x, Ja^1_y, Ja^2_x, Ja^2_y, inverse Jacobian
+  const float4* ja32;       // [E][NN]: Ja^1_x, Ja^1_y, Ja^2_x, Ja^2_y
+  const float* invj32;      // [E][NN]
+  const double* xy;         // [E][NN][2] node coordinates (FP64 sources)
+  const float4* sc;         // [E][NN] sin/cos(pi (x + y)): (sin hi, cos hi, sin lo, cos lo)
+};
+
+// Elements per block of the curvilinear kernels (0: polydeg not compiled).
+int curved_epb(int N);
+
+// One stage (or rhs) launch; exactly one of A64 (FP64 context) and A32
+// (mixed context) is non-null.
+int launch_curved(const CurvedParams& P, const StageArgs* A64, const MixedArgs* A32,
+                  cudaStream_t stream);
+
+// max_dt reduction of a state (FP64 values, or the float-float state of a
+// mixed context in that context's FP32 arithmetic) into dst (double bits).
+int launch_curved_speed(const CurvedParams& P, const void* u, bool ff, unsigned long long* dst,
+                        int32_t* status, cudaStream_t stream);
+
+// Per-element FP64 integrals (conserved totals, entropy, kinetic energy) with
+// the per-node Jacobian, as element_integrals_kernel.
+int launch_curved_integrals(const CurvedParams& P, const void* u, bool ff, const double* weights,
+                            double* partial, cudaStream_t stream);
+
+}  // namespace tg

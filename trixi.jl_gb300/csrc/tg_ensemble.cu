@@ -315,8 +315,9 @@ int tg_ensemble_create(const tg_config* cfgs, int32_t n, int32_t threads_per_blo
     for (int dir = 0; dir < 2 * c.ndims; ++dir)
       if (c.boundary_conditions[dir] != TG_BOUNDARY_PERIODIC)
         return efail(nullptr, TG_ERR_UNSUPPORTED, "ensemble instance %d: periodic meshes only", i);
-    if (c.nmortars != 0)
-      return efail(nullptr, TG_ERR_UNSUPPORTED, "ensemble instance %d: conforming meshes only", i);
+    if (c.nmortars != 0 || c.mesh_type != TG_MESH_TREE)
+      return efail(nullptr, TG_ERR_UNSUPPORTED,
+                   "ensemble instance %d: conforming TreeMeshes only", i);
     if (c.volume_integral != c0.volume_integral || c.volume_flux != c0.volume_flux ||
         c.surface_flux != c0.surface_flux || c.device != c0.device)
       return efail(nullptr, TG_ERR_UNSUPPORTED,

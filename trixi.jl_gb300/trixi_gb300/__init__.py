@@ -35,6 +35,7 @@ from .equations import (initial_condition_density_wave,  # noqa: F401
                         max_abs_speed, max_abs_speed_naive, prim2cons,
                         source_terms_convergence_test)
 from .mesh import TreeMesh  # noqa: F401
+from .curved_mesh import P4estMesh, StructuredMesh  # noqa: F401
 from .semidiscretization import (BoundaryConditionDirichlet, DeviceContext, ODEProblem,  # noqa: F401
                                  SemidiscretizationHyperbolic, boundary_condition_periodic,
                                  boundary_condition_slip_wall, semidiscretize)

@@ -26,7 +26,8 @@ def calc_error_norms(u, t, semi, analyzer: LobattoLegendreAnalyzer | None = None
         W = np.einsum("j,i->ji", w, w)
     else:
         W = np.einsum("k,j,i->kji", w, w, w)
-    vol = semi.mesh.length_level_0 ** D
+    curved = getattr(semi, "curved", False)
+    vol = 0.0 if curved else semi.mesh.length_level_0 ** D
     for s in range(0, E, chunk):
         ue = u[s:s + chunk]
         xe = X[s:s + chunk]
@@ -38,9 +39,17 @@ def calc_error_norms(u, t, semi, analyzer: LobattoLegendreAnalyzer | None = None
             xa = np.einsum("ak,bj,ci,ekjid->eabcd", V, V, V, xe, optimize=True)
         ue_exact = exact(xa, t, eq)
         diff = ue_exact - ua
-        vj = (1.0 / semi.inverse_jacobian[s:s + chunk]) ** D
-        wshape = (-1,) + (1,) * D + (1,)
-        l2 += np.sum(diff ** 2 * W[None, ..., None] * vj.reshape(wshape),
-                     axis=tuple(range(D + 1)))
+        if curved:
+            # |J| interpolated to the analyzer nodes (analysis_dg2d.jl:141-197)
+            ja = np.abs(np.einsum("aj,bi,eji->eab", V, V, 1.0 / semi.inverse_jacobian[s:s + chunk],
+                                  optimize=True))
+            wj = W[None] * ja
+            l2 += np.sum(diff ** 2 * wj[..., None], axis=(0, 1, 2))
+            vol += wj.sum()
+        else:
+            vj = (1.0 / semi.inverse_jacobian[s:s + chunk]) ** D
+            wshape = (-1,) + (1,) * D + (1,)
+            l2 += np.sum(diff ** 2 * W[None, ..., None] * vj.reshape(wshape),
+                         axis=tuple(range(D + 1)))
         linf = np.maximum(linf, np.max(np.abs(diff), axis=tuple(range(D + 1))))
     return np.sqrt(l2 / vol), linf

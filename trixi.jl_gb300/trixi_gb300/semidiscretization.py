@@ -141,6 +141,9 @@ def make_config(semi, precision="fp64", device=0, elements_per_block=0):
     cfg.neighbor_ids = arr(nb, np.int64).ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
     cfg.orientations = arr(orient, np.int64).ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
     cfg.inverse_jacobian = _dptr(arr(semi.inverse_jacobian))
+    if getattr(semi, "curved", False):
+        cfg.mesh_type = _lib.TG_MESH_CURVED
+        cfg.contravariant_vectors = _dptr(arr(semi.contravariant_vectors))
     cfg.node_coordinates = _dptr(arr(semi.node_coordinates))
     cfg.elements_per_block = int(elements_per_block)
     mids = getattr(semi, "mortar_neighbor_ids", None)
@@ -351,6 +354,20 @@ class SemidiscretizationHyperbolic:
         self.ndofs = self.nelements * self.nnodes_per_element
         self.nvalues = self.ndofs * equations.nvariables
         self.u_shape = (self.nelements,) + (n,) * D + (equations.nvariables,)
+        self.curved = bool(getattr(mesh, "curved", False))
+        if self.curved:
+            # StructuredMesh / P4estMesh brick: per-node metric terms
+            # (dgsem_structured/containers_2d.jl:9-35, dgsem_p4est/containers_2d.jl:9-27)
+            from .curved_mesh import metric_terms
+            if isinstance(solver.volume_integral, VolumeIntegralShockCapturingHG):
+                raise NotImplementedError("curvilinear meshes: weak form or flux differencing only")
+            self.node_coordinates = mesh.node_coordinates(solver.basis)
+            self.contravariant_vectors, self.inverse_jacobian = metric_terms(
+                self.node_coordinates, solver.basis)
+            self.neighbor_ids, self.orientations = mesh.interfaces()
+            (self.mortar_neighbor_ids, self.mortar_large_sides,
+             self.mortar_orientations) = mesh.mortars()
+            return
         # init_elements!, containers_2d.jl:85-127
         b = solver.basis
         reference_length = 0.0
