@@ -279,6 +279,168 @@ def gpu_arm(args, rank: int, world: int):
         e2e, acc, semis["mixed"]
 
 
+# ---------------------------------------------------------------------------
+# Curvilinear 2D workload (--workload curved2d): StructuredMesh of the waving
+# flag (examples/structured_2d_dgsem/elixir_euler_source_terms_waving_flag.jl)
+# at 512^2 elements, polydeg 3, weak form, LLF (max_abs_speed_naive),
+# source_terms_convergence_test, CFL 0.8.
+CURVED_CELLS, CURVED_CFL, CURVED_T_END = 512, 0.8, 0.25
+CURVED_WORKLOAD = ("2D Euler MMS on the waving-flag StructuredMesh (transfinite map), 512^2 "
+                   "elements, polydeg 3, weak form, LLF naive, CK2N54 CFL 0.8")
+
+
+def _waving_flag_faces():
+    return (lambda s: (-1.0, s - 1.0), lambda s: (1.0, s + 1.0),
+            lambda s: (s, -1.0 + np.sin(0.5 * np.pi * s)),
+            lambda s: (s, 1.0 + np.sin(0.5 * np.pi * s)))
+
+
+def make_curved_semi(precision: str, cells: int = CURVED_CELLS):
+    import trixi_gb300 as T
+    eq = T.CompressibleEulerEquations2D(1.4)
+    solver = T.DGSEM(polydeg=3, surface_flux=T.FluxLaxFriedrichs(T.max_abs_speed_naive))
+    mesh = T.StructuredMesh((cells, cells), faces=_waving_flag_faces())
+    return T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_convergence_test, solver,
+                                          source_terms=T.source_terms_convergence_test,
+                                          precision=precision)
+
+
+def curved_cpu_rate(threads: int, nsteps: int, max_seconds: float):
+    """Oracle (CPU FP64 restatement of Trixi's curvilinear rhs! + 2N54) on the
+    curved workload's mesh: DOF-updates/s per RK stage."""
+    from oracle import oracle as O
+    O.set_threads(threads)
+    semi = make_curved_semi("fp64")
+    orc = O.CurvedOracle(3, semi.node_coordinates, semi.mesh.neighbors(), 1.4, O.VI_WEAK,
+                         O.FLUX_CENTRAL, O.FLUX_LAX_FRIEDRICHS_NAIVE, O.SRC_CONVERGENCE_TEST)
+    u = orc.initial_condition(O.IC_CONVERGENCE_TEST, 0.0)
+    t0 = time.perf_counter()
+    done = 0
+    while done < nsteps:
+        u, _t, k = orc.solve(u, 0.0, 10.0, CURVED_CFL, max_steps=1)
+        done += k
+        if time.perf_counter() - t0 > max_seconds:
+            break
+    el = time.perf_counter() - t0
+    return semi.ndofs * 5 * done / el, done, el
+
+
+def curved_arm(args):
+    import torch
+
+    import trixi_gb300 as T
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    res, semis = {}, {}
+    clocks = None
+    for prec in ("mixed", "fp64"):
+        semi = make_curved_semi(prec)
+        semis[prec] = semi
+        ctx = semi.device_context
+        stream = torch.cuda.ExternalStream(ctx.stream())
+        ctx.upload(semi.compute_coefficients(0.0))
+        steps = args.steps if prec == "mixed" else max(3, min(args.steps, args.fp64_steps))
+        t, _ = ctx.step(args.warmup, CURVED_CFL, math.inf, 0.0)
+        ctx.synchronize()
+        sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) if prec == "mixed" else None
+        with torch.cuda.stream(stream):
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+        t, n = ctx.step(steps, CURVED_CFL, math.inf, t)
+        with torch.cuda.stream(stream):
+            ev1.record(stream)
+        ev1.synchronize()
+        ms = ev0.elapsed_time(ev1) / steps
+        if sampler:
+            clocks = sampler.stop()
+        res[prec] = dict(ms_per_step=ms, steps=n, value=whole_job_rate(semi.ndofs, ms, 1))
+        if ctx.status() != 0:
+            raise RuntimeError(f"{prec}: device status word flagged a non-physical state")
+    # roofline of the mixed curvilinear stage kernel, single stages after an L2 flush
+    semi = semis["mixed"]
+    ctx = semi.device_context
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    ctx.upload(semi.compute_coefficients(0.0))
+    dt = CURVED_CFL * ctx.max_dt()
+    for s in range(5):
+        ctx.rk_stage(s, 0.0, dt)
+    st = []
+    for rep in range(max(10, args.steps)):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        ctx.rk_stage(rep % 5, 0.0, dt)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        st.append(e0.elapsed_time(e1))
+    stage_ms = statistics.mean(st)
+    # per node and stage: u (4 float-float) read + write, u_tmp (4 FP32) read +
+    # write, contravariant vectors (float4) + inverse Jacobian (FP32) + source
+    # phase (float4) read
+    alg_bytes = semi.ndofs * (4 * 8 * 2 + 4 * 4 * 2 + 16 + 4 + 16)
+    achieved = alg_bytes / (stage_ms * 1e-3) / 1e9
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        peaks = {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    acc = None
+    if not args.no_accuracy:
+        acc = {}
+        for prec, sp in semis.items():
+            c = sp.device_context
+            c.upload(sp.compute_coefficients(0.0))
+            tt, n = c.step(10 ** 7, CURVED_CFL, CURVED_T_END, 0.0)
+            l2, linf = T.calc_error_norms(c.download(), tt, sp)
+            acc[prec] = {"l2_rho": float(l2[0]), "linf_rho": float(linf[0]), "t": tt, "steps": n}
+        # at the elixir's own size and t_end (16^2, t = 2), where the scheme's
+        # error (~3e-5) is far above the mixed path's FP32 rounding floor
+        # (~1e-9 relative at t = 0.25 on 512^2, where FP64's error is ~2e-11)
+        for prec in ("mixed", "fp64"):
+            sp = make_curved_semi(prec, 16)
+            c = sp.device_context
+            c.upload(sp.compute_coefficients(0.0))
+            tt, n = c.step(10 ** 7, CURVED_CFL, 2.0, 0.0)
+            l2, linf = T.calc_error_norms(c.download(), tt, sp)
+            acc[prec + "_16x16_t2"] = {"l2_rho": float(l2[0]), "linf_rho": float(linf[0]),
+                                       "t": tt, "steps": n}
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, done, el = curved_cpu_rate(threads, 2, 20.0)
+        cpu = {"value": rate, "unit": "DOF-updates/s", "cores": threads, "kind": "port",
+               "sample": f"{done} CK2N54 steps of the full 512^2 curved mesh, FP64, {threads} "
+                         f"threads (C++ restatement of Trixi's curvilinear rhs!, not Trixi)"}
+    line = {
+        "metric": METRIC, "value": res["mixed"]["value"], "unit": "DOF-updates/s", "n_gpus": 1,
+        "steps": res["mixed"]["steps"], "warmup": args.warmup,
+        "ms_per_step": res["mixed"]["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (analytic manufactured solution)",
+        "config": {"workload": CURVED_WORKLOAD, "ndofs_per_field": semi.ndofs,
+                   "precision": "mixed", "parallelism": "single GPU",
+                   "l2_policy": "inputs larger than L2 (2 x 134 MB state + 67 MB u_tmp per step); "
+                                "stage-kernel roofline timed after a 256 MB L2 flush"},
+        "fp64": {"value": res["fp64"]["value"], "ms_per_step": res["fp64"]["ms_per_step"],
+                 "steps": res["fp64"]["steps"], "dtype": "f64"},
+        "mixed_over_fp64": res["mixed"]["value"] / res["fp64"]["value"],
+        "accuracy": acc,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "curved_kernel_mixed<4,weak>", "stage_ms": stage_ms,
+                     "algorithmic_bytes": alg_bytes,
+                     "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
+        "cpu_baseline": cpu, "e2e": None, "clocks": clocks,
+        "gpu_launches": 7 * res["mixed"]["steps"],
+    }
+    print(json.dumps(line))
+
+
 def cpu_oracle_rate(threads: int, nsteps: int, max_seconds: float):
     """Oracle (CPU FP64 restatement of Trixi's rhs! + 2N54) DOF-updates/s per RK stage."""
     from oracle import oracle as O
@@ -333,6 +495,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="mms3d", choices=["mms3d", "curved2d"],
+                    help="mms3d: the headline TreeMesh case; curved2d: the curvilinear "
+                         "StructuredMesh case (single GPU, gb300 arm)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
@@ -344,6 +509,10 @@ def main():
             "nccl" if args.impl == "gb300" else "gloo")
     if args.impl == "reference":
         reference_arm(args, rank, world)
+        return
+    if args.workload == "curved2d":
+        if rank == 0:
+            curved_arm(args)
         return
     results, roof, e2e, acc, semi = gpu_arm(args, rank, world)
     if rank != 0:

@@ -25,6 +25,9 @@
        own size (level 6, base 4, t = 1) in FP64.
   c7   mortars: 3D MMS 32^3 with the central box refined once, against the
        uniform 32^3 mesh, FP64 and mixed.
+  c8   curvilinear meshes: the waving-flag StructuredMesh MMS (weak form) and a
+       warped P4estMesh weak blast wave (flux differencing) at 512^2, FP64 and
+       mixed.
 
 The 3D manufactured solution at 32^3 is the headline case of bench.py.
 Throughput is DOF-updates per second per RK stage (ndofs x 5 stages x steps /
@@ -480,6 +483,63 @@ def c7(steps=40):
     return out
 
 
+def _waving_flag_faces():
+    # examples/structured_2d_dgsem/elixir_euler_source_terms_waving_flag.jl
+    return (lambda s: (-1.0, s - 1.0), lambda s: (1.0, s + 1.0),
+            lambda s: (s, -1.0 + np.sin(0.5 * np.pi * s)),
+            lambda s: (s, 1.0 + np.sin(0.5 * np.pi * s)))
+
+
+def _warped_square(xi_, eta_):
+    # examples/structured_2d_dgsem/elixir_euler_free_stream.jl / elixir_euler_ec.jl
+    xi = 1.5 * xi_ + 1.5
+    eta = 1.5 * eta_ + 1.5
+    y = eta + 3 / 8 * (np.cos(1.5 * np.pi * (2 * xi - 3) / 3) * np.cos(0.5 * np.pi * (2 * eta - 3) / 3))
+    x = xi + 3 / 8 * (np.cos(0.5 * np.pi * (2 * xi - 3) / 3) * np.cos(2 * np.pi * (2 * y - 3) / 3))
+    return x, y
+
+
+def c8(cells=512, steps=30, t_end=0.25):
+    """Curvilinear 2D meshes: (a) the waving-flag StructuredMesh MMS at cells^2,
+    polydeg 3, weak form, naive LLF, CFL 0.8 (L2 density error at t_end of both
+    paths); (b) the weak blast wave on the warped square as a P4estMesh of
+    16 x 16 trees refined to cells^2, polydeg 3, flux_ranocha volume and surface
+    flux, CFL 1.0.  DOF-updates/s per stage, FP64 and mixed."""
+    out = {}
+    eq = T.CompressibleEulerEquations2D(1.4)
+    level = int(round(math.log2(cells // 16)))
+    for name in ("flag_weak", "p4est_fd_ranocha"):
+        for prec in ("mixed", "fp64"):
+            if name == "flag_weak":
+                solver = T.DGSEM(polydeg=3, surface_flux=T.FluxLaxFriedrichs(T.max_abs_speed_naive))
+                mesh = T.StructuredMesh((cells, cells), faces=_waving_flag_faces())
+                semi = T.SemidiscretizationHyperbolic(
+                    mesh, eq, T.initial_condition_convergence_test, solver,
+                    source_terms=T.source_terms_convergence_test, precision=prec)
+                cfl = 0.8
+            else:
+                solver = T.DGSEM(polydeg=3, surface_flux=T.flux_ranocha,
+                                 volume_integral=T.VolumeIntegralFluxDifferencing(T.flux_ranocha))
+                mesh = T.P4estMesh((16, 16), polydeg=3, mapping=_warped_square,
+                                   initial_refinement_level=level)
+                semi = T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_weak_blast_wave,
+                                                      solver, precision=prec)
+                cfl = 1.0
+            solve_timed(semi, 10.0, cfl, max_steps=3)  # warm-up
+            n_steps = steps if prec == "mixed" else max(3, steps // 3)
+            _, t, n, secs = solve_timed(semi, 10.0, cfl, max_steps=n_steps)
+            r = dict(elements=semi.nelements, steps=n, secs=secs, rate=rate(semi.ndofs, n, secs))
+            if name == "flag_weak":
+                u, tt, _, _ = solve_timed(semi, t_end, cfl)
+                l2, linf = T.calc_error_norms(u, tt, semi)
+                r.update(l2_rho=float(l2[0]), linf_rho=float(linf[0]), t=tt)
+            out[f"{name}_{prec}"] = r
+        out[f"{name}_speedup"] = out[f"{name}_mixed"]["rate"] / out[f"{name}_fp64"]["rate"]
+    out["flag_l2_rho_mixed_over_fp64"] = (out["flag_weak_mixed"]["l2_rho"] /
+                                          out["flag_weak_fp64"]["l2_rho"])
+    return out
+
+
 def mortar_steps(steps=4):
     """c7's refined mesh (3D MMS 32^3 with the central box refined once, 61,440
     elements, 1,536 mortars), mixed precision, `steps` steps."""
@@ -496,7 +556,7 @@ def mortar_steps(steps=4):
     return dict(steps=n, t=t)
 
 
-RUNS = dict(c1=c1, c3=c3, c4=c4, c5a=c5a, c5b=c5b, c6=c6, c7=c7)
+RUNS = dict(c1=c1, c3=c3, c4=c4, c5a=c5a, c5b=c5b, c6=c6, c7=c7, c8=c8)
 SHORT_RUNS = dict(learned_steps=learned_steps, ensemble_steps=ensemble_steps,
                   mortar_steps=mortar_steps)
 

@@ -263,12 +263,13 @@ class P4estMesh(_CurvedBrick2D):
             pts = 2 * (ql * 0.5 * (basis.nodes + 1) + k * ql) - 1
             mats[k] = polynomial_interpolation_matrix(self.nodes, pts)
         per_tree = 1 << (2 * L)
-        for e0 in range(0, self.nelements, per_tree):
-            T = self.tree_node_coordinates[self._tree[e0]]
-            for q in range(per_tree):
-                m1 = mats[int(self._quad[q, 0])]
-                m2 = mats[int(self._quad[q, 1])]
-                out[e0 + q] = np.einsum("ia,jb,bac->jic", m1, m2, T, optimize=True)
+        ntrees = self.nelements // per_tree
+        view = out.reshape((ntrees, per_tree) + out.shape[1:])
+        T = self.tree_node_coordinates
+        for q in range(per_tree):
+            m1 = mats[int(self._quad[q, 0])]
+            m2 = mats[int(self._quad[q, 1])]
+            view[:, q] = np.einsum("ia,jb,tbac->tjic", m1, m2, T, optimize=True)
         return out
 
     def __repr__(self):
