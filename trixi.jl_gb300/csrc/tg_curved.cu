@@ -404,7 +404,13 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* s_u = reinterpret_cast<float2*>(smem_raw);
   float2* s_fu = s_u + CHUNK;
-  float* s_nd = reinterpret_cast<float*>(s_fu + K::FACE);  // [NV + 1][SP]: dw, dq
+  // per-node metric, source phase, inverse Jacobian and 2N register of the
+  // block, staged with the state so that no phase waits on global loads
+  float4* s_ja = reinterpret_cast<float4*>(s_fu + K::FACE);  // [SP]
+  float4* s_sc = s_ja + SP;                                   // [SP]
+  float* s_ut = reinterpret_cast<float*>(s_sc + SP);          // [SP][NV]
+  float* s_ij = s_ut + SP * NV;                               // [SP]
+  float* s_nd = s_ij + SP;                                    // [NV + 1][SP]: dw, dq
   float* s_part = s_nd + (NV + 1) * SP;                     // [2][NV][SP]
   RefState<2>* s_ref = reinterpret_cast<RefState<2>*>(s_part + 2 * NV * SP);
   float* s_scal = reinterpret_cast<float*>(s_ref + EPB);    // b dt, a (hi, lo)
@@ -437,6 +443,23 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT)
     const float2* g = A.u_in + ((size_t)nb * NN + cface_partner<N>(dir, fn)) * NV;
 #pragma unroll
     for (int v = 0; v < NV; ++v) cp_async8(s_fu + k * NV + v, g + v);
+  }
+  {
+    // metric (one float4 per node) and inverse Jacobian; u_tmp rows are
+    // 16-byte aligned (NV = 4 floats per node)
+    const int nn = nel * NN;
+    const float4* ja = P.ja32 + (size_t)e0 * NN;
+    for (int k = tid; k < nn; k += NT) cp_async16(s_ja + k, ja + k);
+    const float* ij = P.invj32 + (size_t)e0 * NN;
+    for (int k = tid; k < nn; k += NT) cp_async4(s_ij + k, ij + k);
+    if (P.source == SRC_CONVERGENCE_TEST) {
+      const float4* sc = P.sc + (size_t)e0 * NN;
+      for (int k = tid; k < nn; k += NT) cp_async16(s_sc + k, sc + k);
+    }
+    if (stage && !A.zero_tmp) {
+      const float4* ut = reinterpret_cast<const float4*>(A.u_tmp + gofs);
+      for (int k = tid; k < nval / 4; k += NT) cp_async16(reinterpret_cast<float4*>(s_ut) + k, ut + k);
+    }
   }
   if (tid < 2 * EPB) s_smax[tid] = 0u;
   if (tid == 0) {
@@ -494,7 +517,7 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT)
         for (int v = 0; v < NV; ++v) nd[a].dw[v] = s_nd[v * SP + n];
         nd[a].dq = s_nd[NV * SP + n];
         Dv::complete(R, nd[a]);
-        const float4 j = P.ja32[(size_t)e * NN + q];
+        const float4 j = s_ja[n];
         ja[a][0] = dd ? j.z : j.x;
         ja[a][1] = dd ? j.w : j.y;
       }
@@ -588,16 +611,13 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT)
   bool bad = false;
   for (int n = tid; n < nel * NN; n += NT) {
     const int sl = n / NN;
-    const int q = n - sl * NN;
-    const int64_t e = e0 + sl;
-    const size_t gq = (size_t)e * NN + q;
-    const float jfac = -P.invj32[gq];
+    const float jfac = -s_ij[n];
     float du[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) du[v] = (s_part[v * SP + n] + s_part[(NV + v) * SP + n]) * jfac;
     if (P.source == SRC_CONVERGENCE_TEST) {
       // sin/cos(pi (x + y - t)) by the angle-difference formula in float-float
-      const float4 o = P.sc[gq];
+      const float4 o = s_sc[n];
       const float2 sn = ff_dot2(o.x, o.z, ct, ctl, -o.y, -o.w, st, stl);
       const float2 cs = ff_dot2(o.y, o.w, ct, ctl, o.x, o.z, st, stl);
       float s[NV];
@@ -614,7 +634,7 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT)
     float hi[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      const float old = A.zero_tmp ? 0.0f : A.u_tmp[g + v];
+      const float old = A.zero_tmp ? 0.0f : s_ut[n * NV + v];
       const float ut = fmaf(-a_lo, old, fmaf(-a_s, old, du[v]));
       A.u_tmp[g + v] = ut;
       const float2 un = ff_add(s_u[n * NV + v], fmaf(ut, bdt_lo, ut * bdt));
@@ -628,8 +648,8 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT)
       const float cs = sqrtf(eos.gamma * w[3] / w[0]);
       bad |= !(w[0] > 0.0f) || !(w[3] > 0.0f);
       const float l1 = fabsf(w[1]) + cs, l2 = fabsf(w[2]) + cs;
-      const float4 j = P.ja32[gq];
-      const float ij = fabsf(P.invj32[gq]);
+      const float4 j = s_ja[n];
+      const float ij = fabsf(s_ij[n]);
       const float s1 = fabsf(j.x * l1 + j.y * l2) * ij;
       const float s2 = fabsf(j.z * l1 + j.w * l2) * ij;
       if (s1 == s1) atomicMax(&s_smax[2 * sl], __float_as_uint(s1));
@@ -746,7 +766,8 @@ static int launch_curved_n(const CurvedParams& P, const StageArgs* A64, const Mi
     }
     curved_kernel_f64<N, VI, EPB><<<nb, K::NT, smem, stream>>>(P, *A64);
   } else {
-    const size_t smem = sizeof(float2) * (K::CHUNK + K::FACE) +
+    const size_t smem = sizeof(float2) * (K::CHUNK + K::FACE) + sizeof(float4) * 2 * K::SP +
+                        sizeof(float) * (4 * K::SP + K::SP) +
                         sizeof(float) * ((4 + 1) * K::SP + 2 * 4 * K::SP) +
                         sizeof(RefState<2>) * EPB + sizeof(float) * 4 +
                         sizeof(unsigned int) * 2 * EPB;

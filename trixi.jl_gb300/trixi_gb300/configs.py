@@ -556,9 +556,22 @@ def mortar_steps(steps=4):
     return dict(steps=n, t=t)
 
 
+def curved_steps(steps=3, cells=512):
+    """c8's waving-flag StructuredMesh MMS (cells^2, polydeg 3, weak form, naive
+    LLF, CFL 0.8), mixed precision, `steps` steps."""
+    eq = T.CompressibleEulerEquations2D(1.4)
+    solver = T.DGSEM(polydeg=3, surface_flux=T.FluxLaxFriedrichs(T.max_abs_speed_naive))
+    mesh = T.StructuredMesh((cells, cells), faces=_waving_flag_faces())
+    semi = T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_convergence_test, solver,
+                                          source_terms=T.source_terms_convergence_test,
+                                          precision="mixed")
+    _, t, n, secs = solve_timed(semi, 10.0, 0.8, max_steps=steps)
+    return dict(steps=n, t=t)
+
+
 RUNS = dict(c1=c1, c3=c3, c4=c4, c5a=c5a, c5b=c5b, c6=c6, c7=c7, c8=c8)
 SHORT_RUNS = dict(learned_steps=learned_steps, ensemble_steps=ensemble_steps,
-                  mortar_steps=mortar_steps)
+                  mortar_steps=mortar_steps, curved_steps=curved_steps)
 
 
 def main(argv=None):
