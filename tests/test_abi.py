@@ -45,3 +45,27 @@ def test_invalid_config_is_rejected_without_gpu():
     assert "interfaces" in _lib.last_error()
     cfg.ninterfaces, cfg.nmortars = 8, -1
     assert lib.tg_ctx_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.TG_ERR_INVALID_ARGUMENT
+
+
+def test_config_struct_layout_matches_header(tmp_path):
+    # the ctypes mirror of tg_config (trixi_gb300/_lib.py) against the C header,
+    # field by field: offsetof from a C program compiled against include/
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc") or shutil.which("cc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    fields = [f[0] for f in _lib.tg_config._fields_]
+    src = tmp_path / "layout.c"
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "trixi_gb300.h"',
+             'int main(void) {', '  printf("size %zu\\n", sizeof(tg_config));']
+    lines += [f'  printf("{f} %zu\\n", offsetof(tg_config, {f}));' for f in fields]
+    lines += ['  return 0;', '}']
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([gcc, "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    out = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                       check=True).stdout.splitlines())
+    assert int(out["size"]) == ctypes.sizeof(_lib.tg_config)
+    for f in fields:
+        assert int(out[f]) == getattr(_lib.tg_config, f).offset, f

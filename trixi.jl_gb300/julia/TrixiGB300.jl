@@ -53,6 +53,8 @@ struct TgConfig
     mortar_forward_lower::Ptr{Float64}
     mortar_reverse_upper::Ptr{Float64}
     mortar_reverse_lower::Ptr{Float64}
+    mesh_type::Int32                        # 0 TreeMesh, 1 curvilinear 2D brick
+    contravariant_vectors::Ptr{Float64}     # [2, 2, n, n, E] (curvilinear)
 end
 
 const TG_VOLUME_WEAK_FORM, TG_VOLUME_FLUX_DIFFERENCING, TG_VOLUME_SHOCK_CAPTURING_HG = 0, 1, 2
@@ -113,6 +115,8 @@ Builds a device context from a `SemidiscretizationHyperbolic` on a periodic
 # preserved (GC.@preserve) by the caller.
 function config(semi, precision, device)
     (; mesh, equations, solver, cache, source_terms) = semi
+    mesh isa Union{Trixi.StructuredMesh{2}, Trixi.P4estMesh{2}} &&
+        return curved_config(semi, precision, device)
     b = solver.basis
     vi, vf, sf_fv, amax, amin, asmooth = volume_codes(solver.volume_integral,
                                                       solver.surface_integral.surface_flux)
@@ -130,7 +134,55 @@ function config(semi, precision, device)
                     pointer(cache.elements.node_coordinates), 0,
                     boundary_codes(semi.boundary_conditions, ndims(mesh)),
                     boundary_value_code(semi.boundary_conditions)...,
-                    mortar_fields(solver, cache)...)
+                    mortar_fields(solver, cache)...,
+                    Int32(0), Ptr{Float64}(C_NULL))
+end
+
+# Interfaces of a curvilinear brick as (element on the negative side, element on
+# the positive side) pairs and directions, 1-based like Trixi's arrays.  The
+# arrays are kept in `CURVED_KEEP` while the config is in use.
+const CURVED_KEEP = IdDict{Any, Any}()
+curved_interfaces(mesh::Trixi.StructuredMesh{2}, cache) =
+    # left_neighbors[dir, element]: the element across the face at -dir
+    (vec([cache.elements.left_neighbors[d, e] for d in 1:2, e in 1:size(cache.elements.left_neighbors, 2)]),
+     vec([e for d in 1:2, e in 1:size(cache.elements.left_neighbors, 2)]),
+     vec([d for d in 1:2, e in 1:size(cache.elements.left_neighbors, 2)]))
+function curved_interfaces(mesh::Trixi.P4estMesh{2}, cache)
+    # primary side at :end of its face coordinate = negative side of the interface
+    ids, ni = cache.interfaces.neighbor_ids, cache.interfaces.node_indices
+    neg, pos, dir = Int[], Int[], Int[]
+    for i in axes(ids, 2)
+        d = Trixi.indices2direction(ni[1, i])      # 1..4: -x, +x, -y, +y of the primary
+        push!(neg, iseven(d) ? ids[1, i] : ids[2, i])
+        push!(pos, iseven(d) ? ids[2, i] : ids[1, i])
+        push!(dir, (d + 1) >> 1)
+    end
+    return neg, pos, dir
+end
+
+function curved_config(semi, precision, device)
+    (; mesh, equations, solver, cache, source_terms) = semi
+    b = solver.basis
+    neg, pos, dir = curved_interfaces(mesh, cache)
+    nb = permutedims(hcat(neg, pos))           # [2, I], column-major as Trixi's
+    ori = Vector{Int}(dir)
+    CURVED_KEEP[semi] = (nb, ori)
+    vi, vf, sf_fv, amax, amin, asmooth = volume_codes(solver.volume_integral,
+                                                      solver.surface_integral.surface_flux)
+    sf = flux_code(solver.surface_integral.surface_flux)
+    return TgConfig(2, Trixi.polydeg(solver), nelements(solver, cache), length(ori),
+                    equations.gamma, vi, vf, sf, sf, amax, amin, asmooth,
+                    source_code(source_terms), precision, device,
+                    pointer(b.nodes), pointer(b.weights), pointer(b.inverse_weights),
+                    pointer(b.derivative_hat), pointer(b.derivative_split),
+                    pointer(b.inverse_vandermonde_legendre), pointer(nb), pointer(ori),
+                    pointer(cache.elements.inverse_jacobian),      # [n, n, E]
+                    pointer(cache.elements.node_coordinates), 0,
+                    ntuple(_ -> Int32(0), 6), Int32(0), (0.0, 0.0, 0.0, 0.0),
+                    Int64(0), Ptr{Int64}(C_NULL), Ptr{Int64}(C_NULL), Ptr{Int64}(C_NULL),
+                    Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL),
+                    Ptr{Float64}(C_NULL),
+                    Int32(1), pointer(cache.elements.contravariant_vectors))
 end
 
 # cache.mortars / dg.mortar of a TreeMesh with L2 mortars (none: zero and NULL)
