@@ -148,18 +148,23 @@ __global__ void from_ff_kernel(const float2* __restrict__ in, double* __restrict
 }
 
 // max_dt's reduction (stepsize_dg2d.jl:8-30): max_e invJ_e * sum_d max_nodes lambda_d.
+// max_dt reductions (stepsize_dg{2,3}d.jl): one warp per element, lanes over
+// its nodes (consecutive lanes read consecutive nodes), a warp max per
+// direction, then lane 0 adds the directions and updates the global maximum.
 template <int D, typename TS>
-__global__ void max_speed_kernel(const TS* __restrict__ u, const double* __restrict__ inv_jac,
-                                 int64_t E, int NN, double gamma,
-                                 unsigned long long* __restrict__ speed_bits,
-                                 int32_t* __restrict__ status) {
+__global__ void __launch_bounds__(128) max_speed_kernel(const TS* __restrict__ u,
+                                                        const double* __restrict__ inv_jac,
+                                                        int64_t E, int NN, double gamma,
+                                                        unsigned long long* __restrict__ speed_bits,
+                                                        int32_t* __restrict__ status) {
   constexpr int NV = D + 2;
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (e >= E) return;
   double ml[D];
   for (int d = 0; d < D; ++d) ml[d] = 0;
   bool bad = false;
-  for (int q = 0; q < NN; ++q) {
+  for (int q = lane; q < NN; q += 32) {
     const TS* p = u + ((size_t)e * NN + q) * NV;
     double uu[NV], w[NV];
     for (int v = 0; v < NV; ++v) uu[v] = state_f64(p[v]);
@@ -168,13 +173,17 @@ __global__ void max_speed_kernel(const TS* __restrict__ u, const double* __restr
     bad |= !(w[0] > 0) || !(w[NV - 1] > 0);
     for (int d = 0; d < D; ++d) ml[d] = fmax(ml[d], fabs(w[1 + d]) + c);
   }
-  double sum = ml[0];
-  for (int d = 1; d < D; ++d) sum += ml[d];
-  const double sp = inv_jac[e] * sum;
-  if (sp == sp)
-    atomicMax(speed_bits, (unsigned long long)__double_as_longlong(sp));
-  else
-    bad = true;
+  for (int d = 0; d < D; ++d)
+    for (int o = 16; o > 0; o >>= 1) ml[d] = fmax(ml[d], __shfl_xor_sync(0xffffffffu, ml[d], o));
+  if (lane == 0) {
+    double sum = ml[0];
+    for (int d = 1; d < D; ++d) sum += ml[d];
+    const double sp = inv_jac[e] * sum;
+    if (sp == sp)
+      atomicMax(speed_bits, (unsigned long long)__double_as_longlong(sp));
+    else
+      bad = true;
+  }
   if (bad) atomicOr(status, 2);
 }
 
@@ -183,17 +192,19 @@ __global__ void max_speed_kernel(const TS* __restrict__ u, const double* __restr
 // primitives and sound speed, FP32 inverse Jacobian), so that the first dt
 // after an upload is computed like every later one.
 template <int D>
-__global__ void max_speed_ff_kernel(const float2* __restrict__ u, const float* __restrict__ inv_jac,
-                                    int64_t E, int NN, float gamma,
-                                    unsigned long long* __restrict__ speed_bits,
-                                    int32_t* __restrict__ status) {
+__global__ void __launch_bounds__(128) max_speed_ff_kernel(const float2* __restrict__ u,
+                                                           const float* __restrict__ inv_jac,
+                                                           int64_t E, int NN, float gamma,
+                                                           unsigned long long* __restrict__ speed_bits,
+                                                           int32_t* __restrict__ status) {
   constexpr int NV = D + 2;
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (e >= E) return;
   float ml[D];
   for (int d = 0; d < D; ++d) ml[d] = 0.0f;
   bool bad = false;
-  for (int q = 0; q < NN; ++q) {
+  for (int q = lane; q < NN; q += 32) {
     const float2* p = u + ((size_t)e * NN + q) * NV;
     float hi[NV], w[NV];
     for (int v = 0; v < NV; ++v) hi[v] = p[v].x;
@@ -205,13 +216,17 @@ __global__ void max_speed_ff_kernel(const float2* __restrict__ u, const float* _
       if (lam == lam) ml[d] = fmaxf(ml[d], lam);
     }
   }
-  float sum = 0;
-  for (int d = 0; d < D; ++d) sum += ml[d];
-  const float sp = inv_jac[e] * sum;
-  if (sp == sp)
-    atomicMax(speed_bits, (unsigned long long)__double_as_longlong((double)sp));
-  else
-    bad = true;
+  for (int d = 0; d < D; ++d)
+    for (int o = 16; o > 0; o >>= 1) ml[d] = fmaxf(ml[d], __shfl_xor_sync(0xffffffffu, ml[d], o));
+  if (lane == 0) {
+    float sum = 0;
+    for (int d = 0; d < D; ++d) sum += ml[d];
+    const float sp = inv_jac[e] * sum;
+    if (sp == sp)
+      atomicMax(speed_bits, (unsigned long long)__double_as_longlong((double)sp));
+    else
+      bad = true;
+  }
   if (bad) atomicOr(status, 2);
 }
 
@@ -1101,7 +1116,7 @@ static int reduce_speed(tg_ctx* c, const void* u, bool ff, unsigned long long* d
       return fail(c, TG_ERR_CUDA, "curvilinear wave-speed launch failed");
     return TG_OK;
   }
-  const unsigned nb = (unsigned)((c->E + 127) / 128);
+  const unsigned nb = (unsigned)((c->E + 3) / 4);  // one warp per element
   if (c->D == 2) {
     if (ff)
       max_speed_ff_kernel<2><<<nb, 128, 0, c->stream>>>((const float2*)u, c->d_invj_f, c->E, c->NN,

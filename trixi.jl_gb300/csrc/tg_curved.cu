@@ -674,19 +674,26 @@ __device__ __forceinline__ double cstate(double x) { return x; }
 __device__ __forceinline__ double cstate(float2 x) { return (double)x.x + (double)x.y; }
 
 // max_dt of a curvilinear mesh (stepsize_dg2d.jl:114-157), one thread per
-// element: FP64 for an FP64 state, the stage kernel's FP32 arithmetic on the
-// hi parts for a float-float state.
+// node (consecutive threads read consecutive nodes): FP64 for an FP64 state,
+// the stage kernel's FP32 arithmetic on the hi parts for a float-float state.
+// A block holds EB = 128 / NN elements; per-element maxima meet in shared
+// memory (positive doubles order like their bit patterns).
 template <typename TS>
-__global__ void curved_speed_kernel(const CurvedParams P, const TS* __restrict__ u, int NN,
-                                    unsigned long long* __restrict__ speed_bits,
-                                    int32_t* __restrict__ status) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= P.nelements) return;
+__global__ void __launch_bounds__(128) curved_speed_kernel(const CurvedParams P,
+                                                           const TS* __restrict__ u, int NN,
+                                                           unsigned long long* __restrict__ speed_bits,
+                                                           int32_t* __restrict__ status) {
+  __shared__ unsigned long long s_m[2 * 128];
   constexpr bool FF = !std::is_same<TS, double>::value;
-  double m1 = 0, m2 = 0;
+  const int EB = 128 / NN;
+  const int tid = threadIdx.x;
+  const int sl = tid / NN;
+  const int64_t e = (int64_t)blockIdx.x * EB + sl;
+  if (tid < 2 * EB) s_m[tid] = 0ull;
+  __syncthreads();
   bool bad = false;
-  for (int q = 0; q < NN; ++q) {
-    const size_t gq = (size_t)e * NN + q;
+  if (sl < EB && e < P.nelements) {
+    const size_t gq = (size_t)e * NN + (tid - sl * NN);
     const TS* p = u + gq * 4;
     double s1, s2;
     if constexpr (FF) {
@@ -711,14 +718,19 @@ __global__ void curved_speed_kernel(const CurvedParams P, const TS* __restrict__
       s1 = fabs(m[0] * l1 + m[1] * l2) * fabs(m[4]);
       s2 = fabs(m[2] * l1 + m[3] * l2) * fabs(m[4]);
     }
-    m1 = fmax(m1, s1);
-    m2 = fmax(m2, s2);
+    if (s1 == s1 && s2 == s2) {
+      atomicMax(&s_m[2 * sl], (unsigned long long)__double_as_longlong(s1));
+      atomicMax(&s_m[2 * sl + 1], (unsigned long long)__double_as_longlong(s2));
+    } else {
+      bad = true;
+    }
   }
-  const double sp = m1 + m2;
-  if (sp == sp)
+  __syncthreads();
+  if (tid < EB && (int64_t)blockIdx.x * EB + tid < P.nelements) {
+    const double sp = __longlong_as_double((long long)s_m[2 * tid]) +
+                      __longlong_as_double((long long)s_m[2 * tid + 1]);
     atomicMax(speed_bits, (unsigned long long)__double_as_longlong(sp));
-  else
-    bad = true;
+  }
   if (bad) atomicOr(status, 2);
 }
 
@@ -799,7 +811,8 @@ int launch_curved(const CurvedParams& P, const StageArgs* A64, const MixedArgs* 
 
 int launch_curved_speed(const CurvedParams& P, const void* u, bool ff, unsigned long long* dst,
                         int32_t* status, cudaStream_t stream) {
-  const unsigned nb = (unsigned)((P.nelements + 127) / 128);
+  const int eb = 128 / (P.N * P.N);  // elements per block (N <= 5: at least 5)
+  const unsigned nb = (unsigned)((P.nelements + eb - 1) / eb);
   if (ff)
     curved_speed_kernel<float2><<<nb, 128, 0, stream>>>(P, (const float2*)u, P.N * P.N, dst, status);
   else
