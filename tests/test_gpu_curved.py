@@ -171,3 +171,13 @@ def test_curved_unsupported_options_fail_loudly():
                                           T.DGSEM(basis, T.flux_hllc))
     with pytest.raises(T.TrixiGB300Error):
         semi.device_context
+
+
+def test_curved_mixed_ec_golden():
+    # flux_ranocha as volume and surface flux (the one-pass deviation form along
+    # the normal) on the warped mesh, polydeg 4: the mixed run stays on the
+    # golden of the FP64 elixir
+    c = dict(GOLDENS[EC])
+    _, ana = _golden_run(c, "mixed")
+    np.testing.assert_allclose(ana.l2, c["l2"], rtol=1e-4)
+    np.testing.assert_allclose(ana.linf, c["linf"], rtol=1e-3)
