@@ -155,6 +155,9 @@ struct CurvedK {
   static constexpr int CHUNK = EPB * NN * NV;  // state values of a block
   static constexpr int FACE = EPB * 4 * N * NV;
   static constexpr int SP = EPB * NN;          // field stride of the partial sums
+  // resident blocks per SM asked of the mixed kernel: for N <= 4 five blocks
+  // fit its shared memory (44 KB at N = 4) and 96 registers per thread
+  static constexpr int MINB_MIXED = N <= 4 ? 5 : 1;
 };
 
 // ---------------------------------------------------------------------------
@@ -440,7 +443,7 @@ __device__ __forceinline__ void dev_surface_n(int kind, const RefState<2>& R, co
 }
 
 template <int N, int VI, int EPB>
-__global__ void __launch_bounds__(CurvedK<N, EPB>::NT)
+__global__ void __launch_bounds__(CurvedK<N, EPB>::NT, CurvedK<N, EPB>::MINB_MIXED)
     curved_kernel_mixed(const CurvedParams P, const MixedArgs A) {
   using K = CurvedK<N, EPB>;
   using Dv = Dev<2>;
