@@ -95,3 +95,23 @@ def test_curved_mesh_rejects_unsupported():
     with pytest.raises(ValueError):
         P4estMesh((2, 2), polydeg=3, coordinates_min=(0.0, 0.0), coordinates_max=(1.0, 1.0),
                   initial_refinement_level=-1)
+
+
+@pytest.mark.parametrize("level", [0, 2])
+def test_p4est_warped_free_stream_rhs_vanishes(oracle_mod, level):
+    # free-stream preservation on a refined, warped P4estMesh: the element nodes
+    # are interpolated from the tree nodes, and the cross-product metric of the
+    # interpolant satisfies the discrete metric identities, so rhs(constant) = 0
+    # to round-off for the split form with flux_ranocha as well as the weak form
+    O = oracle_mod
+    from trixi_gb300.basis import LobattoLegendreBasis
+    from trixi_gb300.curved_mesh import P4estMesh
+    from _curved_cases import _warped_square_0_3
+    m = P4estMesh((6, 4), polydeg=3, mapping=_warped_square_0_3, initial_refinement_level=level)
+    X = m.node_coordinates(LobattoLegendreBasis(3))
+    for vi, vf, sf in ((O.VI_WEAK, O.FLUX_CENTRAL, O.FLUX_LAX_FRIEDRICHS),
+                       (O.VI_FLUXDIFF, O.FLUX_RANOCHA, O.FLUX_RANOCHA)):
+        orc = O.CurvedOracle(3, X, m.neighbors(), 1.4, vi, vf, sf, O.SRC_NONE)
+        u = orc.initial_condition(O.IC_CONSTANT)
+        du = orc.rhs(u)
+        assert np.max(np.abs(du)) < 1e-13 * np.max(np.abs(u)) * np.max(np.abs(orc.metric()[1]))
