@@ -93,6 +93,7 @@ def _load():
     lib.orc_curved_create.restype = vp
     lib.orc_curved_create.argtypes = [i, i64, P(d), P(i64), d, i, i, i, i]
     lib.orc_curved_destroy.argtypes = [vp]
+    lib.orc_curved_set_dirichlet.argtypes = [vp, i, P(d)]
     lib.orc_curved_metric.argtypes = [vp, P(d), P(d)]
     lib.orc_curved_initial_condition.argtypes = [vp, i, P(d), d, P(d)]
     lib.orc_curved_rhs.argtypes = [vp, P(d), P(d), d]
@@ -411,6 +412,14 @@ class CurvedOracle:
     @property
     def shape(self):
         return (self.E, self.n, self.n, 4)
+
+    def set_dirichlet(self, ic, params=None):
+        """BoundaryConditionDirichlet(initial condition ic) on every face without a
+        neighbour (nbr < 0)."""
+        par = np.zeros(8)
+        if params is not None:
+            par[:len(params)] = params
+        _lib.orc_curved_set_dirichlet(self.h, ic, _p(par))
 
     def metric(self):
         Ja = np.empty((self.E, self.n, self.n, 2, 2))

@@ -2450,6 +2450,10 @@ struct Curved {
   std::vector<int64_t> nbr;  // [E][4]: neighbours across -x, +x, -y, +y
   std::vector<double> Ja;    // [E][nn][4]: Ja^1 (x, y), Ja^2 (x, y)
   std::vector<double> invJ;  // [E][nn]
+  // faces without a neighbour (nbr < 0): BoundaryConditionDirichlet of an
+  // initial condition (bc_ic, bc_par)
+  int bc_ic = -1;
+  double bc_par[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   size_t ui(int64_t e, int node) const { return ((size_t)e * nn + node) * 4; }
 };
 
@@ -2514,6 +2518,32 @@ static void curved_rhs(const Curved& c, double* du, const double* u, double t) {
           sfv[(((size_t)e * 4 + 2 * o) * n + l) * 4 + v] = F[v];
           sfv[(((size_t)left * 4 + 2 * o + 1) * n + l) * 4 + v] = F[v];
         }
+      }
+    }
+  }
+  // Dirichlet boundary faces (calc_boundary_flux!, dgsem_structured/dg_2d.jl:680-750,
+  // dg.jl:124-163; BoundaryConditionDirichlet, equations.jl:183-211): the flux
+  // along the element's own contravariant vector, the boundary value on the
+  // outer side
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < c.E; ++e) {
+    for (int dir = 0; dir < 4; ++dir) {
+      if (c.nbr[e * 4 + dir] >= 0) continue;
+      const int o = dir >> 1;
+      for (int l = 0; l < n; ++l) {
+        const int q = o == 0 ? ((dir & 1) ? (n - 1) + n * l : n * l)
+                             : ((dir & 1) ? l + n * (n - 1) : l);
+        const double sj = c.invJ[(size_t)e * nn + q] >= 0 ? 1.0 : -1.0;
+        const double* a = &c.Ja[((size_t)e * nn + q) * 4 + 2 * o];
+        const double nd[2] = {sj * a[0], sj * a[1]};
+        double ub[5];
+        initial_condition(c.eq, c.bc_ic, c.bc_par, &c.x[((size_t)e * nn + q) * 2], t, ub);
+        double F[4];
+        if (dir & 1)
+          two_point_flux_n(eq, c.sf, &u[c.ui(e, q)], ub, nd, F);
+        else
+          two_point_flux_n(eq, c.sf, ub, &u[c.ui(e, q)], nd, F);
+        for (int v = 0; v < 4; ++v) sfv[(((size_t)e * 4 + dir) * n + l) * 4 + v] = sj * F[v];
       }
     }
   }
@@ -2693,6 +2723,14 @@ void* orc_curved_create(int polydeg, int64_t nelements, const double* x, const i
 }
 
 void orc_curved_destroy(void* h) { delete (Curved*)h; }
+
+// Dirichlet values (an initial condition and its parameters) of the faces
+// without a neighbour
+void orc_curved_set_dirichlet(void* h, int ic, const double* params) {
+  Curved& c = *(Curved*)h;
+  c.bc_ic = ic;
+  for (int k = 0; k < 8; ++k) c.bc_par[k] = params ? params[k] : 0.0;
+}
 
 // contravariant_vectors [E][n][n][2 (dir)][2 (xy)], inverse_jacobian [E][n][n]
 void orc_curved_metric(void* h, double* contravariant, double* inverse_jacobian) {

@@ -57,6 +57,7 @@ def curved_mesh(c, cells=None):
     """The mesh of a case (optionally with another number of cells per direction)."""
     from trixi_gb300.curved_mesh import P4estMesh, StructuredMesh
     kw = mapping_kwargs(c["mapping"])
+    kw["periodicity"] = c.get("boundary") is None
     if c["mesh"] == "structured":
         return StructuredMesh(tuple(cells or c["cells"]), **kw)
     return P4estMesh(tuple(cells or c["trees"]), polydeg=c["polydeg"],
@@ -71,5 +72,10 @@ def curved_oracle(O, c, mesh):
               chandrashekar=O.FLUX_CHANDRASHEKAR)
     src = O.SRC_CONVERGENCE_TEST if c.get("source") == "convergence_test" else O.SRC_NONE
     X = mesh.node_coordinates(LobattoLegendreBasis(c["polydeg"]))
-    return O.CurvedOracle(c["polydeg"], X, mesh.neighbors(), 1.4, vi, fl[c["volume_flux"]],
-                          fl[c["surface_flux"]], src)
+    orc = O.CurvedOracle(c["polydeg"], X, mesh.neighbors(), 1.4, vi, fl[c["volume_flux"]],
+                         fl[c["surface_flux"]], src)
+    if c.get("boundary") == "dirichlet":
+        orc.set_dirichlet(dict(convergence_test=O.IC_CONVERGENCE_TEST,
+                               weak_blast_wave=O.IC_WEAK_BLAST_WAVE,
+                               constant=O.IC_CONSTANT)[c["ic"]])
+    return orc

@@ -270,6 +270,13 @@ CURVED_CASES = {
         mesh="structured", cells=[16, 16], mapping="waving_flag", polydeg=3,
         ic="convergence_test", source="convergence_test", vi="weak",
         volume_flux="central", surface_flux="llf_naive", cfl=0.8, tspan=[0.0, 2.0]),
+    "StructuredMesh2D: elixir_euler_source_terms_nonperiodic.jl": dict(
+        file="test/test_structured_2d.jl",
+        elixir="examples/structured_2d_dgsem/elixir_euler_source_terms_nonperiodic.jl",
+        mesh="structured", cells=[16, 16], mapping="square_0_2", polydeg=3,
+        ic="convergence_test", source="convergence_test", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=1.0, tspan=[0.0, 2.0],
+        boundary="dirichlet"),
     "StructuredMesh2D: elixir_euler_free_stream.jl": dict(
         file="test/test_structured_2d.jl",
         elixir="examples/structured_2d_dgsem/elixir_euler_free_stream.jl",

@@ -18,7 +18,8 @@ interpolated from the tree nodes (dgsem_p4est/containers_2d.jl:29-89).
 Both give the element node coordinates, the metric terms
 (calc_jacobian_matrix!, calc_contravariant_vectors!, calc_inverse_jacobian!,
 dgsem_structured/containers_2d.jl:61-152) and the interfaces of a brick whose
-faces are all conforming and aligned.  Only periodic bricks are supported.
+faces are all conforming and aligned.  Edges of the brick are periodic or
+(per dimension) boundaries.
 """
 from __future__ import annotations
 
@@ -102,7 +103,7 @@ def _periodicity(periodicity):
 
 
 class _CurvedBrick2D:
-    """A periodic brick of elements on a uniform grid of mx x my cells with a
+    """A brick of elements on a uniform grid of mx x my cells with a
     mapping; subclasses fix the element order and the node coordinates."""
     ndims = 2
     curved = True
@@ -117,7 +118,8 @@ class _CurvedBrick2D:
         self._c2e = c2e
 
     def neighbors(self):
-        """[E, 4] (0-based) elements across the -x, +x, -y and +y faces."""
+        """[E, 4] (0-based) elements across the -x, +x, -y and +y faces; -1 on a
+        face at a non-periodic edge of the brick."""
         mx, my = self.grid
         cx, cy = self.cells[:, 0], self.cells[:, 1]
         out = np.empty((self.nelements, 4), dtype=np.int64)
@@ -125,6 +127,12 @@ class _CurvedBrick2D:
         out[:, 1] = self._c2e[(cx + 1) % mx + mx * cy]
         out[:, 2] = self._c2e[cx + mx * ((cy - 1) % my)]
         out[:, 3] = self._c2e[cx + mx * ((cy + 1) % my)]
+        if not self.periodicity[0]:
+            out[cx == 0, 0] = -1
+            out[cx == mx - 1, 1] = -1
+        if not self.periodicity[1]:
+            out[cy == 0, 2] = -1
+            out[cy == my - 1, 3] = -1
         return out
 
     def interfaces(self):
@@ -139,7 +147,8 @@ class _CurvedBrick2D:
             ids[:, d, 0] = np.arange(E) + 1
             ids[:, d, 1] = nb[:, 2 * d + 1] + 1
             ori[:, d] = d + 1
-        return ids.reshape(2 * E, 2), ori.reshape(2 * E)
+        keep = (nb[:, 1::2] >= 0).reshape(2 * E)
+        return ids.reshape(2 * E, 2)[keep], ori.reshape(2 * E)[keep]
 
     def mortars(self):
         z = np.zeros((0, 3), dtype=np.int64)
@@ -181,8 +190,6 @@ class StructuredMesh(_CurvedBrick2D):
         if len(cells_per_dimension) != 2:
             raise NotImplementedError("curvilinear meshes are 2D only")
         self.periodicity = _periodicity(periodicity)
-        if not all(self.periodicity):
-            raise NotImplementedError("curvilinear meshes: periodic boundaries only")
         self.cells_per_dimension = (nx, ny)
         self.grid = (nx, ny)
         cx, cy = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
@@ -216,8 +223,6 @@ class P4estMesh(_CurvedBrick2D):
             raise NotImplementedError("curvilinear meshes are 2D only")
         self.mapping = _resolve_mapping(mapping, faces, coordinates_min, coordinates_max)
         self.periodicity = _periodicity(periodicity)
-        if not all(self.periodicity):
-            raise NotImplementedError("curvilinear meshes: periodic boundaries only")
         tx, ty = (int(t) for t in trees_per_dimension)
         L = int(initial_refinement_level)
         if L < 0 or L > 15:
