@@ -200,7 +200,8 @@ typedef struct tg_config {
    * ([2, 2, n, n, nelements], Ja^i_x / Ja^i_y, containers_2d.jl:107-134) and
    * inverse_jacobian then points to the per-node
    * cache.elements.inverse_jacobian ([n, n, nelements], :136-152).
-   * node_coordinates is [2, n, n, nelements].  Periodic meshes only. */
+   * node_coordinates is [2, n, n, nelements].  Edges of the brick are periodic
+ * or take TG_BOUNDARY_DIRICHLET (slip walls are not built for these meshes). */
   int32_t mesh_type;                   /* tg_mesh_type; 0 = TreeMesh */
   const double* contravariant_vectors;
 } tg_config;

@@ -28,8 +28,10 @@ def build(c, precision="fp64", cells=None):
           "weak_blast_wave": T.initial_condition_weak_blast_wave,
           "constant": T.initial_condition_constant}[c["ic"]]
     src = T.source_terms_convergence_test if c.get("source") == "convergence_test" else None
+    bcs = (T.BoundaryConditionDirichlet(ic) if c.get("boundary") == "dirichlet"
+           else T.boundary_condition_periodic)
     semi = T.SemidiscretizationHyperbolic(mesh, eq, ic, solver, source_terms=src,
-                                          precision=precision)
+                                          boundary_conditions=bcs, precision=precision)
     return semi, curved_oracle(O, c, mesh)
 
 
@@ -50,11 +52,15 @@ RHS_CASES = [
     _case(EC, polydeg=3, volume_flux="central", surface_flux="central"),
     _case(FLAG, vi="fluxdiff", volume_flux="ranocha", surface_flux="llf"),
     _case(P4, mesh="p4est", trees=[6, 4], level=1, mapping="warped_square_0_3"),
+    # Dirichlet faces on a curved boundary
+    _case(FLAG, boundary="dirichlet"),
+    _case(FLAG, boundary="dirichlet", vi="fluxdiff", volume_flux="ranocha", surface_flux="llf"),
 ]
 
 
 def _id(c):
-    return f"{c['mesh']}-{c['mapping']}-{c['vi']}-{c['volume_flux']}-{c['surface_flux']}-p{c['polydeg']}"
+    return (f"{c['mesh']}-{c['mapping']}-{c['vi']}-{c['volume_flux']}-{c['surface_flux']}"
+            f"-p{c['polydeg']}" + ("-dirichlet" if c.get("boundary") else ""))
 
 
 @pytest.mark.parametrize("c", RHS_CASES, ids=_id)
@@ -129,7 +135,8 @@ def test_curved_gpu_fp64_reproduces_trixi_goldens(name):
     np.testing.assert_allclose(ana.linf, c["linf"], rtol=1e-7)
 
 
-@pytest.mark.parametrize("name", [PAR, FLAG, P4, "StructuredMesh2D: elixir_euler_source_terms.jl"])
+@pytest.mark.parametrize("name", [PAR, FLAG, P4, "StructuredMesh2D: elixir_euler_source_terms.jl",
+                                  "StructuredMesh2D: elixir_euler_source_terms_nonperiodic.jl"])
 def test_curved_mixed_error_within_1p1x_of_fp64_golden(name):
     c = dict(GOLDENS[name])
     _, ana = _golden_run(c, "mixed")
@@ -169,6 +176,13 @@ def test_curved_unsupported_options_fail_loudly():
                                        T.DGSEM(basis, T.flux_lax_friedrichs, vi))
     semi = T.SemidiscretizationHyperbolic(curved_mesh(c, (4, 4)), eq, T.initial_condition_constant,
                                           T.DGSEM(basis, T.flux_hllc))
+    with pytest.raises(T.TrixiGB300Error):
+        semi.device_context
+    # slip walls are not built for curvilinear meshes
+    semi = T.SemidiscretizationHyperbolic(curved_mesh(dict(c, boundary="dirichlet"), (4, 4)), eq,
+                                          T.initial_condition_constant,
+                                          T.DGSEM(basis, T.flux_lax_friedrichs),
+                                          boundary_conditions=T.boundary_condition_slip_wall)
     with pytest.raises(T.TrixiGB300Error):
         semi.device_context
 

@@ -1021,6 +1021,11 @@ static int launch_kernel(tg_ctx* c, int mode, const void* u_in, void* u_out, dou
       M.cos_tl = (float)(cs - (double)M.cos_t);
     }
     A.speed_bits = M.speed_bits = reduce ? &c->d_clock->speed_bits : nullptr;
+    if (!c->fp64 && c->nbound > 0 &&
+        tg::launch_curved_ghost(c->CP, c->nbound, c->d_clock,
+                                mode == MODE_STAGE ? CK_C[stage] : 0.0, t_rhs, mode, c->d_ghost,
+                                c->stream) != 0)
+      return fail(c, TG_ERR_CUDA, "curvilinear boundary pre-pass launch failed");
     rc = tg::launch_curved(c->CP, c->fp64 ? &A : nullptr, c->fp64 ? nullptr : &M, c->stream);
     if (rc != 0) {
       cudaError_t e = cudaGetLastError();
@@ -1179,7 +1184,9 @@ static int curved_setup(tg_ctx* c, const tg_config* cfg) {
       CUDA_TRY(nullptr, cudaMemcpy(c->d_csc, sc.data(), sizeof(float4) * nq,
                                    cudaMemcpyHostToDevice));
     }
-  } else if (src) {
+  }
+  if ((src && c->fp64) || c->nbound > 0) {
+    // FP64 node coordinates: sources of FP64 contexts, Dirichlet boundary values
     CUDA_TRY(nullptr, cudaMalloc((void**)&c->d_cxy, sizeof(double) * nq * 2));
     CUDA_TRY(nullptr, cudaMemcpy(c->d_cxy, cfg->node_coordinates, sizeof(double) * nq * 2,
                                  cudaMemcpyHostToDevice));
@@ -1210,6 +1217,10 @@ static int curved_setup(tg_ctx* c, const tg_config* cfg) {
   C.invj32 = c->d_cinvj32;
   C.xy = c->d_cxy;
   C.sc = c->d_csc;
+  C.bc_ic = c->P.bc_ic;
+  for (int k = 0; k < 4; ++k) C.bc_par[k] = c->P.bc_par[k];
+  C.bface = c->d_bface;
+  C.ghost = c->d_ghost;
   return TG_OK;
 }
 
@@ -1420,8 +1431,15 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     }
     has_dirichlet |= bc == TG_BOUNDARY_DIRICHLET;
   }
+  if (curved)
+    for (int dir = 0; dir < nf; ++dir)
+      if (cfg->boundary_conditions[dir] == TG_BOUNDARY_SLIP_WALL) {
+        delete c;
+        return fail(nullptr, TG_ERR_UNSUPPORTED,
+                    "curvilinear meshes: periodic or Dirichlet boundaries only");
+      }
   for (size_t k = 0; k < nbr.size(); ++k)
-    if (nbr[k] == -1 && (curved || cfg->boundary_conditions[k % nf] == TG_BOUNDARY_PERIODIC)) {
+    if (nbr[k] == -1 && cfg->boundary_conditions[k % nf] == TG_BOUNDARY_PERIODIC) {
       delete c;
       return fail(nullptr, TG_ERR_UNSUPPORTED,
                   "element face without interface, mortar or boundary condition (direction %d)",

@@ -145,6 +145,17 @@ __device__ __forceinline__ int cface_partner(int dir, int fn) {
   }
 }
 
+// Node of this element at face dir that meets face node fn.
+template <int N>
+__device__ __forceinline__ int cface_own(int dir, int fn) {
+  switch (dir) {
+    case 0: return N * fn;
+    case 1: return (N - 1) + N * fn;
+    case 2: return fn;
+    default: return fn + N * (N - 1);
+  }
+}
+
 }  // namespace tg
 
 namespace tg {
@@ -193,6 +204,16 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT)
     const int fn = k % N;
     const int32_t nb = P.nbr[(e0 + sl) * 4 + dir];
     if (nb >= e0 && nb < e0 + nel) continue;  // read from s_u below
+    if (nb < 0) {
+      // Dirichlet boundary face: the boundary value at this face node
+      const double* x = P.xy + ((size_t)(e0 + sl) * NN + cface_own<N>(dir, fn)) * 2;
+      const double tt = A.mode == MODE_STAGE ? A.clock->t + A.c * A.clock->dt : A.t_rhs;
+      double xv[2] = {x[0], x[1]}, ub[NV];
+      boundary_value<2>(P.bc_ic, P.bc_par, xv, tt, gamma, ub);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) s_fu[k * NV + v] = ub[v];
+      continue;
+    }
     const double* g = A.u_in + ((size_t)nb * NN + cface_partner<N>(dir, fn)) * NV;
 #pragma unroll
     for (int v = 0; v < NV; ++v) s_fu[k * NV + v] = __ldg(g + v);
@@ -487,7 +508,8 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT, CurvedK<N, EPB>::MINB_MIX
     const int fn = k % N;
     const int32_t nb = P.nbr[(e0 + sl) * 4 + dir];
     if (nb >= e0 && nb < e0 + nel) continue;
-    const float2* g = A.u_in + ((size_t)nb * NN + cface_partner<N>(dir, fn)) * NV;
+    const float2* g = nb >= 0 ? A.u_in + ((size_t)nb * NN + cface_partner<N>(dir, fn)) * NV
+                              : P.ghost + ((size_t)(-1 - nb) * N + fn) * NV;  // boundary face
 #pragma unroll
     for (int v = 0; v < NV; ++v) cp_async8(s_fu + k * NV + v, g + v);
   }
@@ -857,6 +879,40 @@ int launch_curved(const CurvedParams& P, const StageArgs* A64, const MixedArgs* 
                         : launch_curved_n<5, VI_FD>(P, A64, A32, stream);
     default: return -3;
   }
+}
+
+__global__ void curved_ghost_kernel(const CurvedParams P, int64_t B, const Clock* clock, double c_s,
+                                    double t_rhs, int mode, float2* __restrict__ ghost) {
+  const int N = P.N, NN = N * N;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= B * N) return;
+  const int64_t b = k / N;
+  const int fn = (int)(k - b * N);
+  const int64_t e = P.bface[2 * b];
+  const int dir = P.bface[2 * b + 1];
+  int node;
+  switch (dir) {
+    case 0: node = N * fn; break;
+    case 1: node = (N - 1) + N * fn; break;
+    case 2: node = fn; break;
+    default: node = fn + N * (N - 1); break;
+  }
+  const double* x = P.xy + ((size_t)e * NN + node) * 2;
+  double xv[2] = {x[0], x[1]}, out[4];
+  const double t = mode == MODE_RHS ? t_rhs : clock->t + c_s * clock->dt;
+  boundary_value<2>(P.bc_ic, P.bc_par, xv, t, P.gamma, out);
+  for (int v = 0; v < 4; ++v) {
+    const float hi = (float)out[v];
+    ghost[k * 4 + v] = make_float2(hi, (float)(out[v] - (double)hi));
+  }
+}
+
+int launch_curved_ghost(const CurvedParams& P, int64_t B, const Clock* clock, double c_s,
+                        double t_rhs, int mode, float2* ghost, cudaStream_t stream) {
+  const int64_t nk = B * P.N;
+  curved_ghost_kernel<<<(unsigned)((nk + 127) / 128), 128, 0, stream>>>(P, B, clock, c_s, t_rhs,
+                                                                      mode, ghost);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 int launch_curved_speed(const CurvedParams& P, const void* u, bool ff, unsigned long long* dst,

@@ -32,6 +32,15 @@ struct CurvedParams {
   const float* invj32;      // [E][NN]
   const double* xy;         // [E][NN][2] node coordinates (FP64 sources)
   const float4* sc;         // [E][NN] sin/cos(pi (x + y)): (sin hi, cos hi, sin lo, cos lo)
+  // Faces at a non-periodic edge have nbr = -1 - b (b: boundary face number,
+  // bface[b] = element, direction) and take BoundaryConditionDirichlet of the
+  // initial condition bc_ic (dgsem_structured/dg_2d.jl:680-750, dg.jl:124-163):
+  // the FP64 kernel evaluates it at the face node (xy); the mixed kernel reads
+  // ghost[b][face node] (float-float), written by launch_curved_ghost.
+  int32_t bc_ic;
+  double bc_par[4];
+  const int32_t* bface;     // [B][2]
+  const float2* ghost;      // [B][N][4]
 };
 
 // Elements per block of the curvilinear kernels (0: polydeg not compiled).
@@ -41,6 +50,12 @@ int curved_epb(int N);
 // (mixed context) is non-null.
 int launch_curved(const CurvedParams& P, const StageArgs* A64, const MixedArgs* A32,
                   cudaStream_t stream);
+
+// Mixed contexts with boundary faces: the float-float Dirichlet states of the
+// B boundary faces for the stage with weight c_s (MODE_STAGE: t + c_s dt of
+// the clock) or at t_rhs (MODE_RHS), into ghost.
+int launch_curved_ghost(const CurvedParams& P, int64_t B, const Clock* clock, double c_s,
+                        double t_rhs, int mode, float2* ghost, cudaStream_t stream);
 
 // max_dt reduction of a state (FP64 values, or the float-float state of a
 // mixed context in that context's FP32 arithmetic) into dst (double bits).
