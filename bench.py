@@ -15,6 +15,7 @@ exact solution.  `e2e` drives the same steps through the C ABI with the state
 uploaded from and downloaded to pinned host memory every step.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+    python bench.py --workload curved2d    # the curvilinear StructuredMesh line (one GPU)
 
 `--impl reference` times the oracle (the CPU restatement of Trixi's FP64
 rhs! + 2N54 step) on all host cores instead.

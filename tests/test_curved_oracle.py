@@ -115,3 +115,33 @@ def test_p4est_warped_free_stream_rhs_vanishes(oracle_mod, level):
         u = orc.initial_condition(O.IC_CONSTANT)
         du = orc.rhs(u)
         assert np.max(np.abs(du)) < 1e-13 * np.max(np.abs(u)) * np.max(np.abs(orc.metric()[1]))
+
+
+def test_curved_config_carries_metric_and_boundaries():
+    # the tg_config of a curvilinear semidiscretization: mesh type, per-node
+    # inverse Jacobian and contravariant vectors, interfaces only where a
+    # neighbour exists, Dirichlet codes on the non-periodic edges
+    import trixi_gb300 as T
+    from trixi_gb300 import _lib
+    from trixi_gb300.semidiscretization import make_config
+    eq = T.CompressibleEulerEquations2D(1.4)
+    solver = T.DGSEM(polydeg=3, surface_flux=T.flux_lax_friedrichs)
+    for per, nif, codes in ((True, 2 * 12 * 10, [0, 0, 0, 0]),
+                            ((False, True), 11 * 10 + 12 * 10, [1, 1, 0, 0])):
+        mesh = T.StructuredMesh((12, 10), (0.0, 0.0), (1.0, 2.0), periodicity=per)
+        bcs = (T.boundary_condition_periodic if per is True else
+               dict(x_neg=T.BoundaryConditionDirichlet(T.initial_condition_convergence_test),
+                    x_pos=T.BoundaryConditionDirichlet(T.initial_condition_convergence_test),
+                    y_neg=T.boundary_condition_periodic, y_pos=T.boundary_condition_periodic))
+        semi = T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_convergence_test,
+                                              solver, boundary_conditions=bcs)
+        cfg, keep = make_config(semi, "mixed")
+        assert cfg.mesh_type == _lib.TG_MESH_CURVED
+        assert cfg.ninterfaces == nif
+        assert list(cfg.boundary_conditions)[:4] == codes
+        assert semi.inverse_jacobian.shape == (120, 4, 4)
+        assert semi.contravariant_vectors.shape == (120, 4, 4, 2, 2)
+        # affine map: Ja^1 = (dy/deta, 0) = (1/10 * 2 / 2, 0) per unit reference length
+        np.testing.assert_allclose(semi.contravariant_vectors[..., 0, 0], 2.0 / 10 / 2, rtol=1e-13)
+        np.testing.assert_allclose(semi.inverse_jacobian, 1.0 / ((1.0 / 12 / 2) * (2.0 / 10 / 2)),
+                                   rtol=1e-12)
