@@ -156,6 +156,22 @@ __device__ __forceinline__ int cface_own(int dir, int fn) {
   }
 }
 
+// Position of block node n (= slot * N^2 + node) in the mixed kernel's
+// per-node shared arrays.  For N = 4 the low and high halves of the node index
+// are XORed with bits 1-2 of the element slot: a warp holds the x-lines (or the
+// y-lines) of 8 elements, whose same-parity elements would otherwise fall on
+// the same 8 banks (4-way conflicts); with the permutation the 32 lanes of
+// every line-phase access and of the node phase hit 32 different banks.
+template <int N>
+__device__ __forceinline__ int cpos(int n) {
+  if constexpr (N == 4) {
+    const int g = (n >> 5) & 3;  // bits 1-2 of the slot n >> 4
+    return n ^ (g | (g << 2));
+  } else {
+    return n;
+  }
+}
+
 }  // namespace tg
 
 namespace tg {
@@ -561,9 +577,10 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT, CurvedK<N, EPB>::MINB_MIX
     }
     Node<2> nd;
     Dv::make_node(hi, lo, s_ref[sl], eos, nd);
+    const int pn = cpos<N>(n);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) s_nd[v * SP + n] = nd.dw[v];
-    s_nd[NV * SP + n] = nd.dq;
+    for (int v = 0; v < NV; ++v) s_nd[v * SP + pn] = nd.dw[v];
+    s_nd[NV * SP + pn] = nd.dq;
   }
   __syncthreads();
 
@@ -583,8 +600,8 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT, CurvedK<N, EPB>::MINB_MIX
         const int q = cline_node<N>(line, dd, a);
         const int n = sl * NN + q;
 #pragma unroll
-        for (int v = 0; v < NV; ++v) nd[a].dw[v] = s_nd[v * SP + n];
-        nd[a].dq = s_nd[NV * SP + n];
+        for (int v = 0; v < NV; ++v) nd[a].dw[v] = s_nd[v * SP + cpos<N>(n)];
+        nd[a].dq = s_nd[NV * SP + cpos<N>(n)];
         Dv::complete(R, nd[a]);
         const float4 j = s_ja[n];
         ja[a][0] = dd ? j.z : j.x;
@@ -661,7 +678,7 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT, CurvedK<N, EPB>::MINB_MIX
       for (int a = 0; a < N; ++a) {
         const int q = cline_node<N>(line, dd, a);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) s_part[(dd * NV + v) * SP + sl * NN + q] = acc[a][v];
+        for (int v = 0; v < NV; ++v) s_part[(dd * NV + v) * SP + cpos<N>(sl * NN + q)] = acc[a][v];
       }
     }
   }
@@ -686,7 +703,8 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT, CurvedK<N, EPB>::MINB_MIX
     const float jfac = -s_ij[n];
     float du[NV];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) du[v] = (s_part[v * SP + n] + s_part[(NV + v) * SP + n]) * jfac;
+    for (int v = 0; v < NV; ++v)
+      du[v] = (s_part[v * SP + cpos<N>(n)] + s_part[(NV + v) * SP + cpos<N>(n)]) * jfac;
     if (P.source == SRC_CONVERGENCE_TEST) {
       // sin/cos(pi (x + y - t)) by the angle-difference formula in float-float
       const float4 o = s_sc[n];
