@@ -102,6 +102,18 @@ def _load():
     lib.orc_curved_solve.restype = i
     lib.orc_curved_solve.argtypes = [vp, P(d), d, d, d, i64, P(d), P(i64)]
     lib.orc_curved_errors.argtypes = [vp, P(d), d, i, P(d), P(d), P(d)]
+    lib.orc_curved3_create.restype = vp
+    lib.orc_curved3_create.argtypes = [i, i64, P(d), P(i64), d, i, i, i, i]
+    lib.orc_curved3_destroy.argtypes = [vp]
+    lib.orc_curved3_set_dirichlet.argtypes = [vp, i, P(d)]
+    lib.orc_curved3_metric.argtypes = [vp, P(d), P(d)]
+    lib.orc_curved3_initial_condition.argtypes = [vp, i, P(d), d, P(d)]
+    lib.orc_curved3_rhs.argtypes = [vp, P(d), P(d), d]
+    lib.orc_curved3_max_dt.restype = d
+    lib.orc_curved3_max_dt.argtypes = [vp, P(d)]
+    lib.orc_curved3_solve.restype = i
+    lib.orc_curved3_solve.argtypes = [vp, P(d), d, d, d, i64, P(d), P(i64)]
+    lib.orc_curved3_errors.argtypes = [vp, P(d), d, i, P(d), P(d), P(d)]
     _lib = lib
     return lib
 
@@ -458,4 +470,75 @@ class CurvedOracle:
         par = np.ascontiguousarray(params if params is not None else np.zeros(8), dtype=np.float64)
         _lib.orc_curved_errors(self.h, _p(np.ascontiguousarray(u, dtype=np.float64)), t, ic,
                                _p(par), _p(l2), _p(linf))
+        return l2, linf
+
+
+class CurvedOracle3D:
+    """CPU restatement of DGSEM on a curvilinear 3D StructuredMesh: element node
+    coordinates x[E, n, n, n, 3] (i fastest) and neighbours nbr[E, 6] (0-based,
+    -x, +x, -y, +y, -z, +z; -1 on a Dirichlet face).  State layout [E, n, n, n, 5]."""
+
+    def __init__(self, polydeg, x, nbr, gamma=1.4, volume_integral=VI_WEAK,
+                 volume_flux=FLUX_CENTRAL, surface_flux=FLUX_LAX_FRIEDRICHS, source=SRC_NONE):
+        lib = _load()
+        self.x = np.ascontiguousarray(x, dtype=np.float64)
+        self.nbr = np.ascontiguousarray(nbr, dtype=np.int64)
+        self.n = polydeg + 1
+        self.E = self.x.shape[0]
+        self.h = lib.orc_curved3_create(polydeg, self.E, _p(self.x),
+                                        _p(self.nbr, ctypes.c_int64), gamma, volume_integral,
+                                        volume_flux, surface_flux, source)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_curved3_destroy(self.h)
+            self.h = None
+
+    @property
+    def shape(self):
+        return (self.E, self.n, self.n, self.n, 5)
+
+    def set_dirichlet(self, ic, params=None):
+        par = np.zeros(8)
+        if params is not None:
+            par[:len(params)] = params
+        _lib.orc_curved3_set_dirichlet(self.h, ic, _p(par))
+
+    def metric(self):
+        Ja = np.empty((self.E, self.n, self.n, self.n, 3, 3))
+        ij = np.empty((self.E, self.n, self.n, self.n))
+        _lib.orc_curved3_metric(self.h, _p(Ja), _p(ij))
+        return Ja, ij
+
+    def initial_condition(self, ic, t=0.0, params=None):
+        u = np.empty(self.shape)
+        par = np.ascontiguousarray(params if params is not None else np.zeros(8), dtype=np.float64)
+        _lib.orc_curved3_initial_condition(self.h, ic, _p(par), t, _p(u))
+        return u
+
+    def rhs(self, u, t=0.0):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        du = np.empty_like(u)
+        _lib.orc_curved3_rhs(self.h, _p(du), _p(u), t)
+        return du
+
+    def max_dt(self, u):
+        return _lib.orc_curved3_max_dt(self.h, _p(np.ascontiguousarray(u, dtype=np.float64)))
+
+    def solve(self, u, t0, t_end, cfl, max_steps=2 ** 62):
+        u = np.array(u, dtype=np.float64, copy=True)
+        t = ctypes.c_double()
+        k = ctypes.c_int64()
+        rc = _lib.orc_curved3_solve(self.h, _p(u), t0, t_end, cfl, max_steps, ctypes.byref(t),
+                                    ctypes.byref(k))
+        if rc != 0:
+            raise FloatingPointError("NaN time step")
+        return u, t.value, k.value
+
+    def error_norms(self, u, t, ic, params=None):
+        l2 = np.empty(5)
+        linf = np.empty(5)
+        par = np.ascontiguousarray(params if params is not None else np.zeros(8), dtype=np.float64)
+        _lib.orc_curved3_errors(self.h, _p(np.ascontiguousarray(u, dtype=np.float64)), t, ic,
+                                _p(par), _p(l2), _p(linf))
         return l2, linf

@@ -2792,3 +2792,447 @@ void orc_curved_errors(void* h, const double* u, double t, int ic, const double*
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Curvilinear 3D meshes (StructuredMesh{3}): the element node coordinates and
+// neighbours come from the caller; metric terms in the invariant curl form
+// (dgsem_structured/containers_3d.jl:67-286); rhs! of dgsem_structured/dg_3d.jl.
+// ---------------------------------------------------------------------------
+
+namespace orc {
+
+// flux(u, normal_direction) and the two-point fluxes along a normal,
+// compressible_euler_3d.jl (normal-direction methods)
+static inline void flux3_n(const Eq& eq, const double* u, const double* n, double* f) {
+  double w[5];
+  cons2prim(eq, u, w);
+  const double vn = w[1] * n[0] + w[2] * n[1] + w[3] * n[2];
+  const double rvn = w[0] * vn;
+  f[0] = rvn;
+  for (int d = 0; d < 3; ++d) f[1 + d] = std::fma(rvn, w[1 + d], w[4] * n[d]);
+  f[4] = (u[4] + w[4]) * vn;
+}
+
+static inline void two_point3_n(const Eq& eq, int kind, const double* ul, const double* ur,
+                                const double* n, double* f) {
+  double a[5], b[5];
+  cons2prim(eq, ul, a);
+  cons2prim(eq, ur, b);
+  const double vna = a[1] * n[0] + a[2] * n[1] + a[3] * n[2];
+  const double vnb = b[1] * n[0] + b[2] * n[1] + b[3] * n[2];
+  double vavg[3], vsq = 0;
+  for (int d = 0; d < 3; ++d) {
+    vavg[d] = 0.5 * (a[1 + d] + b[1 + d]);
+    vsq += a[1 + d] * b[1 + d];
+  }
+  vsq *= 0.5;
+  const double p_avg = 0.5 * (a[4] + b[4]);
+  switch (kind) {
+    case FLUX_RANOCHA: {
+      const double rho_mean = ln_mean(a[0], b[0]);
+      const double irpm = a[4] * b[4] * inv_ln_mean(a[0] * b[4], b[0] * a[4]);
+      const double f1 = rho_mean * 0.5 * (vna + vnb);
+      f[0] = f1;
+      for (int d = 0; d < 3; ++d) f[1 + d] = std::fma(f1, vavg[d], p_avg * n[d]);
+      f[4] = f1 * (vsq + irpm * eq.inv_gamma_minus_one) + 0.5 * (a[4] * vnb + b[4] * vna);
+      return;
+    }
+    case FLUX_SHIMA_ETAL: {
+      const double rho_avg = 0.5 * (a[0] + b[0]);
+      const double vn_avg = 0.5 * (vna + vnb);
+      const double f1 = rho_avg * vn_avg;
+      f[0] = f1;
+      for (int d = 0; d < 3; ++d) f[1 + d] = std::fma(f1, vavg[d], p_avg * n[d]);
+      f[4] = f1 * vsq + p_avg * vn_avg * eq.inv_gamma_minus_one + 0.5 * (a[4] * vnb + b[4] * vna);
+      return;
+    }
+    default: break;
+  }
+  double fl[5], fr[5];
+  flux3_n(eq, ul, n, fl);
+  flux3_n(eq, ur, n, fr);
+  for (int v = 0; v < 5; ++v) f[v] = 0.5 * (fl[v] + fr[v]);
+  if (kind == FLUX_LAX_FRIEDRICHS || kind == FLUX_LAX_FRIEDRICHS_NAIVE) {
+    // max_abs_speed(_naive)(u_ll, u_rr, normal_direction), compressible_euler_3d.jl
+    const double ca = std::sqrt(eq.gamma * a[4] / a[0]), cb = std::sqrt(eq.gamma * b[4] / b[0]);
+    const double nn = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    const double lam = kind == FLUX_LAX_FRIEDRICHS_NAIVE
+                           ? std::max(std::fabs(vna), std::fabs(vnb)) + std::max(ca, cb) * nn
+                           : std::max(std::fabs(vna) + ca * nn, std::fabs(vnb) + cb * nn);
+    for (int v = 0; v < 5; ++v) f[v] = f[v] + (-0.5 * lam * (ur[v] - ul[v]));
+  }
+}
+
+struct Curved3 {
+  Eq eq;
+  Basis b;
+  int n = 0, nn = 0;
+  int64_t E = 0;
+  int vi = VI_WEAK, vf = FLUX_CENTRAL, sf = FLUX_LAX_FRIEDRICHS, source = SRC_NONE;
+  std::vector<double> x;     // [E][nn][3], node = i + n j + n^2 k
+  std::vector<int64_t> nbr;  // [E][6]: -x, +x, -y, +y, -z, +z (< 0: Dirichlet face)
+  std::vector<double> Ja;    // [E][nn][9]: Ja^d_c at d * 3 + c
+  std::vector<double> invJ;  // [E][nn]
+  int bc_ic = -1;
+  double bc_par[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  size_t ui(int64_t e, int q) const { return ((size_t)e * nn + q) * 5; }
+  int node(int i, int j, int k) const { return i + n * (j + n * k); }
+};
+
+// calc_jacobian_matrix!, calc_contravariant_vectors! (curl form),
+// calc_inverse_jacobian! (containers_3d.jl:67-286)
+static void curved3_metric(Curved3& c) {
+  const int n = c.n, nn = c.nn;
+  const std::vector<double>& Dm = c.b.D;
+  c.Ja.assign((size_t)c.E * nn * 9, 0.0);
+  c.invJ.assign((size_t)c.E * nn, 0.0);
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < c.E; ++e) {
+    const double* X = &c.x[(size_t)e * nn * 3];
+    std::vector<double> J((size_t)nn * 9);  // J[q][c * 3 + d] = dX_c / dxi_d
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          const int q = c.node(i, j, k);
+          for (int cc = 0; cc < 3; ++cc) {
+            double r0 = 0, r1 = 0, r2 = 0;
+            for (int s = 0; s < n; ++s) {
+              r0 += Dm[i * n + s] * X[c.node(s, j, k) * 3 + cc];
+              r1 += Dm[j * n + s] * X[c.node(i, s, k) * 3 + cc];
+              r2 += Dm[k * n + s] * X[c.node(i, j, s) * 3 + cc];
+            }
+            J[q * 9 + cc * 3 + 0] = r0;
+            J[q * 9 + cc * 3 + 1] = r1;
+            J[q * 9 + cc * 3 + 2] = r2;
+          }
+        }
+    // (X_m dX_l/dxi_d - X_l dX_m/dxi_d) at node q
+    auto g = [&](int q, int m, int l, int d) {
+      return X[q * 3 + m] * J[q * 9 + l * 3 + d] - X[q * 3 + l] * J[q * 9 + m * 3 + d];
+    };
+    double* Ja = &c.Ja[(size_t)e * nn * 9];
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          const int q = c.node(i, j, k);
+          for (int cn = 0; cn < 3; ++cn) {
+            const int m = (cn + 1) % 3, l = (cn + 2) % 3;
+            double a1 = 0, a2 = 0, b1 = 0, b2 = 0, c1 = 0, c2 = 0;
+            for (int s = 0; s < n; ++s) {
+              a1 += 0.5 * Dm[j * n + s] * g(c.node(i, s, k), m, l, 2);  // (.)_zeta, d/deta
+              a2 += 0.5 * Dm[k * n + s] * g(c.node(i, j, s), m, l, 1);  // (.)_eta, d/dzeta
+              b1 += 0.5 * Dm[k * n + s] * g(c.node(i, j, s), m, l, 0);  // (.)_xi, d/dzeta
+              b2 += 0.5 * Dm[i * n + s] * g(c.node(s, j, k), m, l, 2);  // (.)_zeta, d/dxi
+              c1 += 0.5 * Dm[i * n + s] * g(c.node(s, j, k), m, l, 1);  // (.)_eta, d/dxi
+              c2 += 0.5 * Dm[j * n + s] * g(c.node(i, s, k), m, l, 0);  // (.)_xi, d/deta
+            }
+            Ja[q * 9 + 0 * 3 + cn] = a1 - a2;
+            Ja[q * 9 + 1 * 3 + cn] = b1 - b2;
+            Ja[q * 9 + 2 * 3 + cn] = c1 - c2;
+          }
+          const double* M = &J[q * 9];
+          const double det = M[0] * M[4] * M[8] + M[1] * M[5] * M[6] + M[2] * M[3] * M[7] -
+                             M[2] * M[4] * M[6] - M[1] * M[3] * M[8] - M[0] * M[5] * M[7];
+          c.invJ[(size_t)e * nn + q] = 1.0 / det;
+        }
+  }
+}
+
+}  // namespace orc
+
+namespace orc {
+
+// rhs! on a curvilinear 3D mesh (dgsem_structured/dg_3d.jl: weak form and flux
+// differencing with contravariant fluxes, interface fluxes along the + side
+// element's contravariant vector, Dirichlet faces, surface integral,
+// per-node Jacobian, sources)
+static void curved3_rhs(const Curved3& c, double* du, const double* u, double t) {
+  const int n = c.n, nn = c.nn, nf = n * n;
+  const Basis& b = c.b;
+  const Eq& eq = c.eq;
+  std::vector<double> sfv((size_t)c.E * 6 * nf * 5);  // [E][dir][face node][v]
+  // face node (a, b) of direction o at the - side (s = 0) or + side (s = n - 1)
+  auto fnode = [&](int o, int a, int bb, int s) {
+    return o == 0 ? c.node(s, a, bb) : (o == 1 ? c.node(a, s, bb) : c.node(a, bb, s));
+  };
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < c.E; ++e)
+    for (int o = 0; o < 3; ++o) {
+      const int64_t left = c.nbr[e * 6 + 2 * o];
+      if (left < 0) continue;
+      for (int bb = 0; bb < n; ++bb)
+        for (int a = 0; a < n; ++a) {
+          const int qr = fnode(o, a, bb, 0), ql = fnode(o, a, bb, n - 1);
+          const double sj = c.invJ[(size_t)e * nn + qr] >= 0 ? 1.0 : -1.0;
+          const double* J = &c.Ja[((size_t)e * nn + qr) * 9 + 3 * o];
+          const double nd[3] = {sj * J[0], sj * J[1], sj * J[2]};
+          double F[5];
+          two_point3_n(eq, c.sf, &u[c.ui(left, ql)], &u[c.ui(e, qr)], nd, F);
+          const int l = a + n * bb;
+          for (int v = 0; v < 5; ++v) {
+            sfv[(((size_t)e * 6 + 2 * o) * nf + l) * 5 + v] = sj * F[v];
+            sfv[(((size_t)left * 6 + 2 * o + 1) * nf + l) * 5 + v] = sj * F[v];
+          }
+        }
+    }
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < c.E; ++e)
+    for (int dir = 0; dir < 6; ++dir) {
+      if (c.nbr[e * 6 + dir] >= 0) continue;
+      const int o = dir >> 1;
+      for (int bb = 0; bb < n; ++bb)
+        for (int a = 0; a < n; ++a) {
+          const int q = fnode(o, a, bb, (dir & 1) ? n - 1 : 0);
+          const double sj = c.invJ[(size_t)e * nn + q] >= 0 ? 1.0 : -1.0;
+          const double* J = &c.Ja[((size_t)e * nn + q) * 9 + 3 * o];
+          const double nd[3] = {sj * J[0], sj * J[1], sj * J[2]};
+          double ub[5], F[5];
+          initial_condition(c.eq, c.bc_ic, c.bc_par, &c.x[((size_t)e * nn + q) * 3], t, ub);
+          if (dir & 1)
+            two_point3_n(eq, c.sf, &u[c.ui(e, q)], ub, nd, F);
+          else
+            two_point3_n(eq, c.sf, ub, &u[c.ui(e, q)], nd, F);
+          for (int v = 0; v < 5; ++v) sfv[(((size_t)e * 6 + dir) * nf + a + n * bb) * 5 + v] = sj * F[v];
+        }
+    }
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < c.E; ++e) {
+    double* de = du + (size_t)e * nn * 5;
+    const double* ue = u + (size_t)e * nn * 5;
+    const double* Ja = &c.Ja[(size_t)e * nn * 9];
+    for (int k = 0; k < nn * 5; ++k) de[k] = 0;
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          const int q = c.node(i, j, k);
+          const int idx[3] = {i, j, k};
+          if (c.vi == VI_WEAK) {
+            double f[3][5] = {};
+            for (int o = 0; o < 3; ++o) flux_phys(eq, ue + q * 5, o, f[o]);
+            for (int d = 0; d < 3; ++d) {
+              const double* a = Ja + q * 9 + 3 * d;
+              double cf[5];
+              for (int v = 0; v < 5; ++v)
+                cf[v] = std::fma(a[2], f[2][v], std::fma(a[1], f[1][v], a[0] * f[0][v]));
+              for (int s = 0; s < n; ++s) {
+                int id2[3] = {i, j, k};
+                id2[d] = s;
+                const int r = c.node(id2[0], id2[1], id2[2]);
+                for (int v = 0; v < 5; ++v)
+                  de[r * 5 + v] = std::fma(b.Dhat[s * n + idx[d]], cf[v], de[r * 5 + v]);
+              }
+            }
+          } else {
+            for (int d = 0; d < 3; ++d)
+              for (int s = idx[d] + 1; s < n; ++s) {
+                int id2[3] = {i, j, k};
+                id2[d] = s;
+                const int r = c.node(id2[0], id2[1], id2[2]);
+                const double* aq = Ja + q * 9 + 3 * d;
+                const double* ar = Ja + r * 9 + 3 * d;
+                const double avg[3] = {0.5 * (aq[0] + ar[0]), 0.5 * (aq[1] + ar[1]),
+                                       0.5 * (aq[2] + ar[2])};
+                double F[5];
+                two_point3_n(eq, c.vf, ue + q * 5, ue + r * 5, avg, F);
+                for (int v = 0; v < 5; ++v) {
+                  de[q * 5 + v] = std::fma(b.Dsplit[idx[d] * n + s], F[v], de[q * 5 + v]);
+                  de[r * 5 + v] = std::fma(b.Dsplit[s * n + idx[d]], F[v], de[r * 5 + v]);
+                }
+              }
+          }
+        }
+    const double factor = b.inv_weights[0];
+    const double* sf = &sfv[(size_t)e * 6 * nf * 5];
+    for (int o = 0; o < 3; ++o)
+      for (int bb = 0; bb < n; ++bb)
+        for (int a = 0; a < n; ++a) {
+          const int l = a + n * bb;
+          const int q0 = fnode(o, a, bb, 0), q1 = fnode(o, a, bb, n - 1);
+          for (int v = 0; v < 5; ++v) {
+            de[q0 * 5 + v] = de[q0 * 5 + v] - sf[((2 * o) * nf + l) * 5 + v] * factor;
+            de[q1 * 5 + v] = de[q1 * 5 + v] + sf[((2 * o + 1) * nf + l) * 5 + v] * factor;
+          }
+        }
+    for (int q = 0; q < nn; ++q) {
+      const double fac = -c.invJ[(size_t)e * nn + q];
+      for (int v = 0; v < 5; ++v) de[q * 5 + v] *= fac;
+      if (c.source == SRC_CONVERGENCE_TEST) {
+        double s[5] = {0, 0, 0, 0, 0};
+        source_convergence(eq, &c.x[((size_t)e * nn + q) * 3], t, s);
+        for (int v = 0; v < 5; ++v) de[q * 5 + v] += s[v];
+      }
+    }
+  }
+}
+
+// max_dt on a curvilinear 3D mesh (stepsize_dg3d.jl, curvilinear method)
+static double curved3_max_dt(const Curved3& c, const double* u) {
+  double mss = 4.9406564584124654e-324;
+  for (int64_t e = 0; e < c.E; ++e) {
+    double m[3] = {0, 0, 0};
+    for (int q = 0; q < c.nn; ++q) {
+      double lam[3];
+      max_abs_speeds(c.eq, &u[c.ui(e, q)], lam);
+      const double* a = &c.Ja[((size_t)e * c.nn + q) * 9];
+      const double ij = std::fabs(c.invJ[(size_t)e * c.nn + q]);
+      for (int d = 0; d < 3; ++d)
+        m[d] = std::max(m[d], std::fabs(a[3 * d] * lam[0] + a[3 * d + 1] * lam[1] +
+                                        a[3 * d + 2] * lam[2]) * ij);
+    }
+    mss = std::max(mss, m[0] + m[1] + m[2]);
+  }
+  return 2 / (c.n * mss);
+}
+
+// calc_error_norms on a curvilinear 3D mesh (analysis_dg3d.jl, curvilinear method)
+static void curved3_errors(const Curved3& c, const double* u, double t, int ic, const double* par,
+                           double* l2, double* linf) {
+  const Basis& b = c.b;
+  const int n = c.n, na = b.na, nn = c.nn;
+  for (int v = 0; v < 5; ++v) l2[v] = linf[v] = 0;
+  double vol = 0;
+  // fields per node: 5 state values, 3 coordinates, J
+  const int NFLD = 9;
+  std::vector<double> f0((size_t)nn * NFLD), f1((size_t)na * n * n * NFLD),
+      f2((size_t)na * na * n * NFLD), f3((size_t)na * na * na * NFLD);
+  for (int64_t e = 0; e < c.E; ++e) {
+    for (int q = 0; q < nn; ++q) {
+      for (int v = 0; v < 5; ++v) f0[q * NFLD + v] = u[c.ui(e, q) + v];
+      for (int d = 0; d < 3; ++d) f0[q * NFLD + 5 + d] = c.x[((size_t)e * nn + q) * 3 + d];
+      f0[q * NFLD + 8] = 1.0 / c.invJ[(size_t)e * nn + q];
+    }
+    // interpolate along i, j, k in turn (multiply_dimensionwise!)
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j)
+        for (int a = 0; a < na; ++a)
+          for (int f = 0; f < NFLD; ++f) {
+            double s = 0;
+            for (int i = 0; i < n; ++i) s += b.avand[a * n + i] * f0[(i + n * (j + n * k)) * NFLD + f];
+            f1[(a + na * (j + n * k)) * NFLD + f] = s;
+          }
+    for (int k = 0; k < n; ++k)
+      for (int bb = 0; bb < na; ++bb)
+        for (int a = 0; a < na; ++a)
+          for (int f = 0; f < NFLD; ++f) {
+            double s = 0;
+            for (int j = 0; j < n; ++j) s += b.avand[bb * n + j] * f1[(a + na * (j + n * k)) * NFLD + f];
+            f2[(a + na * (bb + na * k)) * NFLD + f] = s;
+          }
+    for (int cc = 0; cc < na; ++cc)
+      for (int bb = 0; bb < na; ++bb)
+        for (int a = 0; a < na; ++a) {
+          double* p = &f3[(a + na * (bb + na * cc)) * NFLD];
+          for (int f = 0; f < NFLD; ++f) {
+            double s = 0;
+            for (int k = 0; k < n; ++k) s += b.avand[cc * n + k] * f2[(a + na * (bb + na * k)) * NFLD + f];
+            p[f] = s;
+          }
+          double ue[5];
+          initial_condition(c.eq, ic, par, p + 5, t, ue);
+          const double wj = b.aweights[a] * b.aweights[bb] * b.aweights[cc] * std::fabs(p[8]);
+          for (int v = 0; v < 5; ++v) {
+            const double d = ue[v] - p[v];
+            l2[v] += d * d * wj;
+            linf[v] = std::max(linf[v], std::fabs(d));
+          }
+          vol += wj;
+        }
+  }
+  for (int v = 0; v < 5; ++v) l2[v] = std::sqrt(l2[v] / vol);
+}
+
+}  // namespace orc
+
+extern "C" {
+
+// Curvilinear 3D solver on element node coordinates x[E][n][n][n][3] (i
+// fastest) and neighbours nbr[E][6] (0-based; -1: Dirichlet face).
+void* orc_curved3_create(int polydeg, int64_t nelements, const double* x, const int64_t* nbr,
+                         double gamma, int volume_integral, int volume_flux, int surface_flux,
+                         int source) {
+  Curved3* c = new Curved3();
+  c->eq.D = 3;
+  c->eq.NV = 5;
+  c->eq.gamma = gamma;
+  c->eq.inv_gamma_minus_one = 1 / (gamma - 1);
+  c->b = make_basis(polydeg);
+  c->n = polydeg + 1;
+  c->nn = c->n * c->n * c->n;
+  c->E = nelements;
+  c->vi = volume_integral;
+  c->vf = volume_flux;
+  c->sf = surface_flux;
+  c->source = source;
+  c->x.assign(x, x + (size_t)nelements * c->nn * 3);
+  c->nbr.assign(nbr, nbr + (size_t)nelements * 6);
+  curved3_metric(*c);
+  return c;
+}
+
+void orc_curved3_destroy(void* h) { delete (Curved3*)h; }
+
+void orc_curved3_set_dirichlet(void* h, int ic, const double* params) {
+  Curved3& c = *(Curved3*)h;
+  c.bc_ic = ic;
+  for (int k = 0; k < 8; ++k) c.bc_par[k] = params ? params[k] : 0.0;
+}
+
+// contravariant_vectors [E][n][n][n][3 (dir)][3 (xyz)], inverse_jacobian [E][n][n][n]
+void orc_curved3_metric(void* h, double* contravariant, double* inverse_jacobian) {
+  Curved3& c = *(Curved3*)h;
+  std::copy(c.Ja.begin(), c.Ja.end(), contravariant);
+  std::copy(c.invJ.begin(), c.invJ.end(), inverse_jacobian);
+}
+
+void orc_curved3_initial_condition(void* h, int ic, const double* params, double t, double* u) {
+  Curved3& c = *(Curved3*)h;
+  for (int64_t e = 0; e < c.E; ++e)
+    for (int q = 0; q < c.nn; ++q)
+      initial_condition(c.eq, ic, params, &c.x[((size_t)e * c.nn + q) * 3], t, &u[c.ui(e, q)]);
+}
+
+void orc_curved3_rhs(void* h, double* du, const double* u, double t) {
+  curved3_rhs(*(Curved3*)h, du, u, t);
+}
+
+double orc_curved3_max_dt(void* h, const double* u) { return curved3_max_dt(*(Curved3*)h, u); }
+
+int orc_curved3_solve(void* h, double* u, double t0, double t_end, double cfl, int64_t max_steps,
+                      double* t_out, int64_t* nsteps_out) {
+  Curved3& c = *(Curved3*)h;
+  const int64_t ndof = c.E * c.nn * 5;
+  std::vector<double> du(ndof), u_tmp(ndof);
+  double t = t0;
+  double dt = cfl * curved3_max_dt(c, u);
+  int64_t iter = 0;
+  bool finalstep = false;
+  while (!finalstep && iter < max_steps) {
+    if (std::isnan(dt)) {
+      *t_out = t;
+      *nsteps_out = iter;
+      return -1;
+    }
+    if (t + dt > t_end || isapprox(t + dt, t_end)) {
+      dt = t_end - t;
+      finalstep = true;
+    }
+    std::fill(u_tmp.begin(), u_tmp.end(), 0.0);
+    for (int stage = 0; stage < 5; ++stage) {
+      curved3_rhs(c, du.data(), u, t + dt * CK_C[stage]);
+      rk_update(ndof, u, u_tmp.data(), du.data(), CK_A[stage], CK_B[stage] * dt);
+    }
+    iter += 1;
+    t += dt;
+    dt = cfl * curved3_max_dt(c, u);
+  }
+  *t_out = t;
+  *nsteps_out = iter;
+  return 0;
+}
+
+void orc_curved3_errors(void* h, const double* u, double t, int ic, const double* params,
+                        double* l2, double* linf) {
+  curved3_errors(*(Curved3*)h, u, t, ic, params, l2, linf);
+}
+
+}  // extern "C"

@@ -41,7 +41,42 @@ WAVING_FLAG_FACES = (
 )
 
 
+CUBE_0_2_FACES = (
+    # elixir_euler_source_terms.jl (structured_3d_dgsem): the faces of [0, 2]^3
+    lambda s, t: (0.0, s + 1.0, t + 1.0), lambda s, t: (2.0, s + 1.0, t + 1.0),
+    lambda s, t: (s + 1.0, 0.0, t + 1.0), lambda s, t: (s + 1.0, 2.0, t + 1.0),
+    lambda s, t: (s + 1.0, t + 1.0, 0.0), lambda s, t: (s + 1.0, t + 1.0, 2.0),
+)
+
+
+def _warp3(xi, eta, zeta, amp):
+    y = eta + amp * (np.cos(1.5 * np.pi * (2 * xi - 3) / 3) * np.cos(0.5 * np.pi * (2 * eta - 3) / 3) *
+                     np.cos(0.5 * np.pi * (2 * zeta - 3) / 3))
+    x = xi + amp * (np.cos(0.5 * np.pi * (2 * xi - 3) / 3) * np.cos(2 * np.pi * (2 * y - 3) / 3) *
+                    np.cos(0.5 * np.pi * (2 * zeta - 3) / 3))
+    z = zeta + amp * (np.cos(0.5 * np.pi * (2 * x - 3) / 3) * np.cos(np.pi * (2 * y - 3) / 3) *
+                      np.cos(0.5 * np.pi * (2 * zeta - 3) / 3))
+    return x, y, z
+
+
+def _warped_cube_0_3(xi_, eta_, zeta_):
+    # elixir_euler_free_stream.jl / elixir_euler_ec.jl (structured_3d_dgsem)
+    return _warp3(1.5 * xi_ + 1.5, 1.5 * eta_ + 1.5, 1.5 * zeta_ + 1.5, 3 / 8)
+
+
+def _warped_cube_nonperiodic(xi, eta, zeta):
+    # elixir_euler_source_terms_nonperiodic_curved.jl (structured_3d_dgsem)
+    x, y, z = _warp3(xi, eta, zeta, 1 / 6)
+    return x + 1, y + 1, z + 1
+
+
 def mapping_kwargs(name):
+    if name == "cube_0_2_faces":
+        return dict(faces=CUBE_0_2_FACES)
+    if name == "warped_cube_0_3":
+        return dict(mapping=_warped_cube_0_3)
+    if name == "warped_cube_nonperiodic":
+        return dict(mapping=_warped_cube_nonperiodic)
     if name == "square_0_2":
         return dict(coordinates_min=(0.0, 0.0), coordinates_max=(2.0, 2.0))
     if name == "parallelogram":
@@ -55,9 +90,11 @@ def mapping_kwargs(name):
 
 def curved_mesh(c, cells=None):
     """The mesh of a case (optionally with another number of cells per direction)."""
-    from trixi_gb300.curved_mesh import P4estMesh, StructuredMesh
+    from trixi_gb300.curved_mesh import P4estMesh, StructuredMesh, StructuredMesh3D
     kw = mapping_kwargs(c["mapping"])
     kw["periodicity"] = c.get("boundary") is None
+    if c.get("ndims", 2) == 3:
+        return StructuredMesh3D(tuple(cells or c["cells"]), **kw)
     if c["mesh"] == "structured":
         return StructuredMesh(tuple(cells or c["cells"]), **kw)
     return P4estMesh(tuple(cells or c["trees"]), polydeg=c["polydeg"],
@@ -72,8 +109,9 @@ def curved_oracle(O, c, mesh):
               chandrashekar=O.FLUX_CHANDRASHEKAR)
     src = O.SRC_CONVERGENCE_TEST if c.get("source") == "convergence_test" else O.SRC_NONE
     X = mesh.node_coordinates(LobattoLegendreBasis(c["polydeg"]))
-    orc = O.CurvedOracle(c["polydeg"], X, mesh.neighbors(), 1.4, vi, fl[c["volume_flux"]],
-                         fl[c["surface_flux"]], src)
+    cls = O.CurvedOracle3D if c.get("ndims", 2) == 3 else O.CurvedOracle
+    orc = cls(c["polydeg"], X, mesh.neighbors(), c.get("gamma", 1.4), vi, fl[c["volume_flux"]],
+              fl[c["surface_flux"]], src)
     if c.get("boundary") == "dirichlet":
         orc.set_dirichlet(dict(convergence_test=O.IC_CONVERGENCE_TEST,
                                weak_blast_wave=O.IC_WEAK_BLAST_WAVE,

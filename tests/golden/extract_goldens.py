@@ -289,6 +289,32 @@ CURVED_CASES = {
         mesh="structured", cells=[16, 16], mapping="warped_square_0_3", polydeg=4,
         ic="weak_blast_wave", source="none", vi="fluxdiff",
         volume_flux="ranocha", surface_flux="ranocha", cfl=1.0, tspan=[0.0, 2.0]),
+    # 3D (oracle only; the GPU path runs 2D curvilinear meshes)
+    "StructuredMesh3D: elixir_euler_source_terms.jl": dict(
+        file="test/test_structured_3d.jl",
+        elixir="examples/structured_3d_dgsem/elixir_euler_source_terms.jl",
+        mesh="structured", ndims=3, cells=[4, 4, 4], mapping="cube_0_2_faces", polydeg=3,
+        ic="convergence_test", source="convergence_test", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=0.6, tspan=[0.0, 5.0]),
+    "StructuredMesh3D: elixir_euler_free_stream.jl": dict(
+        file="test/test_structured_3d.jl",
+        elixir="examples/structured_3d_dgsem/elixir_euler_free_stream.jl",
+        mesh="structured", ndims=3, cells=[4, 4, 4], mapping="warped_cube_0_3", polydeg=3,
+        ic="constant", source="none", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=1.3, tspan=[0.0, 1.0]),
+    "StructuredMesh3D: elixir_euler_ec.jl": dict(
+        file="test/test_structured_3d.jl",
+        elixir="examples/structured_3d_dgsem/elixir_euler_ec.jl",
+        mesh="structured", ndims=3, cells=[4, 4, 4], mapping="warped_cube_0_3", polydeg=5,
+        gamma=5.0 / 3.0, ic="weak_blast_wave", source="none", vi="fluxdiff",
+        volume_flux="ranocha", surface_flux="ranocha", cfl=1.0, tspan=[0.0, 2.0]),
+    "StructuredMesh3D: elixir_euler_source_terms_nonperiodic_curved.jl": dict(
+        file="test/test_structured_3d.jl",
+        elixir="examples/structured_3d_dgsem/elixir_euler_source_terms_nonperiodic_curved.jl",
+        mesh="structured", ndims=3, cells=[4, 4, 4], mapping="warped_cube_nonperiodic", polydeg=3,
+        ic="convergence_test", source="convergence_test", vi="weak",
+        volume_flux="central", surface_flux="llf_naive", cfl=0.6, tspan=[0.0, 5.0],
+        boundary="dirichlet"),
     "CUDA 2D: elixir_euler_source_terms.jl native": dict(
         file="test/test_cuda_2d.jl",
         elixir="examples/p4est_2d_dgsem/elixir_euler_source_terms.jl",

@@ -66,6 +66,52 @@ def transfinite_mapping(faces):
     return mapping
 
 
+def transfinite_mapping_3d(faces):
+    """transfinite_mapping(faces) of six face functions (structured_mesh.jl:266-342):
+    faces[0..5] at xi = -1, xi = 1, eta = -1, eta = 1, zeta = -1, zeta = 1, each a
+    function of the two running coordinates returning (x, y, z)."""
+    f = faces
+
+    def fv(fun, s, t):
+        r = fun(s, t)
+        return [np.asarray(r[q], dtype=float) for q in range(3)]
+
+    def li(s, a, b):
+        return [_linear_interpolate(s, a[q], b[q]) for q in range(3)]
+
+    def add(a, b):
+        return [a[q] + b[q] for q in range(3)]
+
+    def mapping(x, y, z):
+        x, y, z = (np.asarray(v, dtype=float) for v in (x, y, z))
+        lin = add(add(li(x, fv(f[0], y, z), fv(f[1], y, z)), li(y, fv(f[2], x, z), fv(f[3], x, z))),
+                  li(z, fv(f[4], x, y), fv(f[5], x, y)))
+        # correction_term_3d
+        c_x = li(x, add(li(y, fv(f[2], -1, z), fv(f[3], -1, z)), li(z, fv(f[4], -1, y), fv(f[5], -1, y))),
+                 add(li(y, fv(f[2], 1, z), fv(f[3], 1, z)), li(z, fv(f[4], 1, y), fv(f[5], 1, y))))
+        c_y = li(y, add(li(x, fv(f[0], -1, z), fv(f[1], -1, z)), li(z, fv(f[4], x, -1), fv(f[5], x, -1))),
+                 add(li(x, fv(f[0], 1, z), fv(f[1], 1, z)), li(z, fv(f[4], x, 1), fv(f[5], x, 1))))
+        c_z = li(z, add(li(x, fv(f[0], y, -1), fv(f[1], y, -1)), li(y, fv(f[2], x, -1), fv(f[3], x, -1))),
+                 add(li(x, fv(f[0], y, 1), fv(f[1], y, 1)), li(y, fv(f[2], x, 1), fv(f[3], x, 1))))
+        corr = [0.5 * (c_x[q] + c_y[q] + c_z[q]) for q in range(3)]
+        # trilinear_mapping
+        corners = [fv(f[0], -1, -1), fv(f[1], -1, -1), fv(f[0], 1, -1), fv(f[1], 1, -1),
+                   fv(f[0], -1, 1), fv(f[1], -1, 1), fv(f[0], 1, 1), fv(f[1], 1, 1)]
+        sx, sy, sz = (1 - x, 1 + x), (1 - y, 1 + y), (1 - z, 1 + z)
+        tri = [0.125 * (corners[0][q] * sx[0] * sy[0] * sz[0] + corners[1][q] * sx[1] * sy[0] * sz[0] +
+                        corners[2][q] * sx[0] * sy[1] * sz[0] + corners[3][q] * sx[1] * sy[1] * sz[0] +
+                        corners[4][q] * sx[0] * sy[0] * sz[1] + corners[5][q] * sx[1] * sy[0] * sz[1] +
+                        corners[6][q] * sx[0] * sy[1] * sz[1] + corners[7][q] * sx[1] * sy[1] * sz[1])
+               for q in range(3)]
+        return tuple(lin[q] - corr[q] + tri[q] for q in range(3))
+    return mapping
+
+
+def _eval_mapping3(mapping, xi, eta, zeta):
+    r = mapping(xi, eta, zeta)
+    return tuple(np.array(np.broadcast_to(np.asarray(r[q], dtype=float), xi.shape)) for q in range(3))
+
+
 def _eval_mapping(mapping, xi, eta):
     """Evaluates a mapping on arrays of reference coordinates; a mapping that
     only takes scalars is applied point by point."""
@@ -210,6 +256,70 @@ class StructuredMesh(_CurvedBrick2D):
 
     def __repr__(self):
         return f"StructuredMesh{{2}}({self.grid[0]}x{self.grid[1]} cells)"
+
+
+class StructuredMesh3D:
+    """StructuredMesh with three cells_per_dimension (structured_mesh.jl): the
+    mapping of three reference coordinates, six faces (transfinite) or
+    coordinates_min/max.  Host setup of the element node coordinates
+    (containers_3d.jl:37-65, cells x fastest) and neighbours; the GPU path runs
+    2D curvilinear meshes only, the oracle also these."""
+    ndims = 3
+    curved = True
+
+    def __init__(self, cells_per_dimension, mapping=None, coordinates_max=None, *, faces=None,
+                 coordinates_min=None, periodicity=True):
+        if isinstance(mapping, (tuple, list)) and len(mapping) == 6 and callable(mapping[0]):
+            faces, mapping = tuple(mapping), None
+        elif isinstance(mapping, (tuple, list)) and coordinates_max is not None:
+            coordinates_min, mapping = tuple(mapping), None
+        if faces is not None:
+            self.mapping = transfinite_mapping_3d(faces)
+        elif coordinates_min is not None:
+            lo, hi = tuple(coordinates_min), tuple(coordinates_max)
+            self.mapping = lambda a, b, c: (_linear_interpolate(a, lo[0], hi[0]),
+                                            _linear_interpolate(b, lo[1], hi[1]),
+                                            _linear_interpolate(c, lo[2], hi[2]))
+        else:
+            self.mapping = mapping
+        self.grid = tuple(int(c) for c in cells_per_dimension)
+        self.periodicity = ((periodicity,) * 3 if isinstance(periodicity, bool)
+                            else tuple(bool(p) for p in periodicity))
+        nx, ny, nz = self.grid
+        self.nelements = nx * ny * nz
+        e = np.arange(self.nelements)
+        self.cells = np.stack([e % nx, (e // nx) % ny, e // (nx * ny)], axis=1)
+
+    def neighbors(self):
+        """[E, 6] (0-based) across -x, +x, -y, +y, -z, +z; -1 at a non-periodic edge."""
+        g = self.grid
+        out = np.empty((self.nelements, 6), dtype=np.int64)
+        for d in range(3):
+            for side, step in ((0, -1), (1, 1)):
+                c = self.cells.copy()
+                c[:, d] = (c[:, d] + step) % g[d]
+                out[:, 2 * d + side] = c[:, 0] + g[0] * (c[:, 1] + g[1] * c[:, 2])
+                if not self.periodicity[d]:
+                    edge = self.cells[:, d] == (0 if side == 0 else g[d] - 1)
+                    out[edge, 2 * d + side] = -1
+        return out
+
+    def node_coordinates(self, basis):
+        """calc_node_coordinates! (containers_3d.jl:37-65): [E, k, j, i, 3]."""
+        g = self.grid
+        nodes = basis.nodes
+        ref = []
+        for d in range(3):
+            dx = 2.0 / g[d]
+            ref.append(-1 + self.cells[:, d] * dx + dx / 2)
+        xi = ref[0][:, None, None, None] + (1.0 / g[0] * nodes)[None, None, None, :]
+        eta = ref[1][:, None, None, None] + (1.0 / g[1] * nodes)[None, None, :, None]
+        zeta = ref[2][:, None, None, None] + (1.0 / g[2] * nodes)[None, :, None, None]
+        xi, eta, zeta = (np.ascontiguousarray(a) for a in np.broadcast_arrays(xi, eta, zeta))
+        return np.stack(_eval_mapping3(self.mapping, xi, eta, zeta), axis=-1)
+
+    def __repr__(self):
+        return f"StructuredMesh{{3}}({self.grid[0]}x{self.grid[1]}x{self.grid[2]} cells)"
 
 
 class P4estMesh(_CurvedBrick2D):
