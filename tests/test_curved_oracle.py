@@ -156,3 +156,17 @@ def test_curved_config_carries_metric_and_boundaries():
         np.testing.assert_allclose(semi.contravariant_vectors[..., 0, 0], 2.0 / 10 / 2, rtol=1e-13)
         np.testing.assert_allclose(semi.inverse_jacobian, 1.0 / ((1.0 / 12 / 2) * (2.0 / 10 / 2)),
                                    rtol=1e-12)
+
+
+def test_host_metric_terms_3d_match_oracle(oracle_mod):
+    # numpy curl-form metric (the host side a 3D curvilinear context would
+    # pass) against the oracle's, on the warped cube
+    from trixi_gb300.basis import LobattoLegendreBasis
+    from trixi_gb300.curved_mesh import metric_terms_3d
+    c = GOLDENS["StructuredMesh3D: elixir_euler_free_stream.jl"]
+    mesh = curved_mesh(c, cells=(3, 2, 2))
+    X = mesh.node_coordinates(LobattoLegendreBasis(c["polydeg"]))
+    Ja, ij = curved_oracle(oracle_mod, c, mesh).metric()
+    Ja2, ij2 = metric_terms_3d(X, LobattoLegendreBasis(c["polydeg"]))
+    np.testing.assert_allclose(Ja2, Ja, rtol=0, atol=1e-13 * np.abs(Ja).max())
+    np.testing.assert_allclose(ij2, ij, rtol=1e-12)

@@ -222,6 +222,33 @@ def metric_terms(X, basis):
     return Ja, inv_j
 
 
+def metric_terms_3d(X, basis):
+    """Jacobian matrix, contravariant vectors in the invariant curl form and
+    inverse Jacobian per node (dgsem_structured/containers_3d.jl:67-286) of node
+    coordinates X[E, k, j, i, 3].  Returns contravariant [E, k, j, i, 3 (i), 3
+    (x, y, z)] and inverse_jacobian [E, k, j, i]."""
+    Dm = basis.derivative_matrix
+    # J[..., c, d] = dX_c / dxi_d (d: 0 xi along i, 1 eta along j, 2 zeta along k)
+    J = np.empty(X.shape[:4] + (3, 3))
+    J[..., 0] = np.einsum("is,ekjsc->ekjic", Dm, X)
+    J[..., 1] = np.einsum("js,eksic->ekjic", Dm, X)
+    J[..., 2] = np.einsum("ks,esjic->ekjic", Dm, X)
+    Ja = np.empty(X.shape[:4] + (3, 3))
+    d_xi = lambda G: np.einsum("is,ekjs->ekji", Dm, G)
+    d_eta = lambda G: np.einsum("js,eksi->ekji", Dm, G)
+    d_zeta = lambda G: np.einsum("ks,esji->ekji", Dm, G)
+    for n in range(3):
+        m, l = (n + 1) % 3, (n + 2) % 3
+        g = [X[..., m] * J[..., l, d] - X[..., l] * J[..., m, d] for d in range(3)]
+        Ja[..., 0, n] = 0.5 * d_eta(g[2]) - 0.5 * d_zeta(g[1])
+        Ja[..., 1, n] = 0.5 * d_zeta(g[0]) - 0.5 * d_xi(g[2])
+        Ja[..., 2, n] = 0.5 * d_xi(g[1]) - 0.5 * d_eta(g[0])
+    det = (J[..., 0, 0] * J[..., 1, 1] * J[..., 2, 2] + J[..., 0, 1] * J[..., 1, 2] * J[..., 2, 0] +
+           J[..., 0, 2] * J[..., 1, 0] * J[..., 2, 1] - J[..., 0, 2] * J[..., 1, 1] * J[..., 2, 0] -
+           J[..., 0, 1] * J[..., 1, 0] * J[..., 2, 2] - J[..., 0, 0] * J[..., 1, 2] * J[..., 2, 1])
+    return Ja, 1.0 / det
+
+
 class StructuredMesh(_CurvedBrick2D):
     """StructuredMesh(cells_per_dimension, mapping | faces | (cmin, cmax); periodicity)."""
 
