@@ -170,3 +170,12 @@ def test_host_metric_terms_3d_match_oracle(oracle_mod):
     Ja2, ij2 = metric_terms_3d(X, LobattoLegendreBasis(c["polydeg"]))
     np.testing.assert_allclose(Ja2, Ja, rtol=0, atol=1e-13 * np.abs(Ja).max())
     np.testing.assert_allclose(ij2, ij, rtol=1e-12)
+
+
+def test_amr_rejects_curvilinear_meshes():
+    import trixi_gb300 as T
+    semi = T.SemidiscretizationHyperbolic(
+        T.StructuredMesh((4, 4), (0.0, 0.0), (1.0, 1.0)), T.CompressibleEulerEquations2D(1.4),
+        T.initial_condition_constant, T.DGSEM(polydeg=3, surface_flux=T.flux_lax_friedrichs))
+    with pytest.raises(NotImplementedError):
+        T.AMRCallback(semi, None, interval=5)

@@ -62,6 +62,8 @@ class AMRCallback:
                  adapt_initial_condition_only_refine=True):
         if not (isinstance(interval, (int, np.integer)) and interval >= 0):
             raise ValueError("`interval` must be a non-negative integer")
+        if getattr(semi.mesh, "curved", False):
+            raise NotImplementedError("AMR runs on TreeMeshes; curvilinear meshes are not adapted")
         self.controller = controller
         self.interval = int(interval)
         self.adapt_initial_condition = bool(adapt_initial_condition)
