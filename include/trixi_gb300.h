@@ -189,7 +189,7 @@ typedef struct tg_config {
   const double* mortar_forward_lower;
   const double* mortar_reverse_upper;
   const double* mortar_reverse_lower;
-  /* Curvilinear meshes (mesh_type = TG_MESH_CURVED, 2D): StructuredMesh, and
+  /* Curvilinear meshes (mesh_type = TG_MESH_CURVED): 2D StructuredMesh, and
    * P4estMesh built from a brick of trees with a uniform refinement level
    * (src/meshes/structured_mesh.jl, p4est_mesh.jl:189-244, connectivity
    * :1149-1240).  Every face is conforming and both elements of an interface
@@ -201,7 +201,11 @@ typedef struct tg_config {
    * inverse_jacobian then points to the per-node
    * cache.elements.inverse_jacobian ([n, n, nelements], :136-152).
    * node_coordinates is [2, n, n, nelements].  Edges of the brick are periodic
- * or take TG_BOUNDARY_DIRICHLET (slip walls are not built for these meshes). */
+ * or take TG_BOUNDARY_DIRICHLET (slip walls are not built for these meshes).
+ * 3D StructuredMesh (FP64, weak form, polydeg 3; dgsem_structured/dg_3d.jl,
+ * containers_3d.jl:67-286): contravariant_vectors [3, 3, n, n, n, nelements]
+ * in the curl form, inverse_jacobian [n, n, n, nelements], node_coordinates
+ * [3, n, n, n, nelements], reference directions 1..3. */
   int32_t mesh_type;                   /* tg_mesh_type; 0 = TreeMesh */
   const double* contravariant_vectors;
 } tg_config;

@@ -17,7 +17,8 @@ FP64_GOLDENS = sorted(k for k, v in GOLDENS.items()
 
 
 def build(c, precision="fp64", cells=None):
-    eq = T.CompressibleEulerEquations2D(1.4)
+    eq = (T.CompressibleEulerEquations3D if c.get("ndims", 2) == 3
+          else T.CompressibleEulerEquations2D)(c.get("gamma", 1.4))
     basis = T.LobattoLegendreBasis(c["polydeg"])
     sflux = FLUX[c["surface_flux"]][0]
     if c["vi"] == "weak":
@@ -197,3 +198,65 @@ def test_curved_mixed_ec_golden():
     _, ana = _golden_run(c, "mixed")
     np.testing.assert_allclose(ana.l2, c["l2"], rtol=1e-4)
     np.testing.assert_allclose(ana.linf, c["linf"], rtol=1e-3)
+
+
+
+# ---- 3D curvilinear meshes (FP64) ----------------------------------------------
+FREE3 = "StructuredMesh3D: elixir_euler_free_stream.jl"
+EC3 = "StructuredMesh3D: elixir_euler_ec.jl"
+NONP3 = "StructuredMesh3D: elixir_euler_source_terms_nonperiodic_curved.jl"
+SRC3 = "StructuredMesh3D: elixir_euler_source_terms.jl"
+# the 3D path runs the weak form at polydeg 3 (the configuration of these goldens)
+GOLDENS_3D = sorted(k for k, v in GOLDENS.items()
+                    if v.get("ndims", 2) == 3 and v["vi"] == "weak" and v["polydeg"] == 3)
+RHS_CASES_3D = [
+    (_case(FREE3, ic="convergence_test", source="convergence_test"), (4, 4, 4)),
+    (_case(FREE3, ic="convergence_test", source="convergence_test", surface_flux="llf"), (4, 4, 4)),
+    (_case(NONP3), (3, 2, 2)),                                  # Dirichlet faces
+]
+
+
+@pytest.mark.parametrize("c,cells", RHS_CASES_3D, ids=lambda x: _id(x) if isinstance(x, dict) else "")
+def test_curved3_rhs_fp64_matches_oracle(c, cells):
+    # (the warped cube folds on meshes coarser than 4^3: cells keeps it valid)
+    semi, orc = build(c, cells=cells)
+    u = perturbed_state(semi, seed=7)
+    np.testing.assert_array_less(rel_err(semi.device_context.rhs_host(u, 0.29), orc.rhs(u, 0.29)),
+                                 1e-12)
+
+
+def test_curved3_max_dt_integrals_and_steps():
+    c = _case(NONP3)
+    semi, orc = build(c, cells=(3, 2, 2))
+    u0 = semi.compute_coefficients(0.0)
+    ctx = semi.device_context
+    ctx.upload(u0)
+    assert ctx.max_dt() == pytest.approx(orc.max_dt(u0), rel=1e-13)
+    w = semi.solver.basis.weights
+    ref = np.einsum("k,j,i,ekji,ekjiv->v", w, w, w, 1.0 / semi.inverse_jacobian, u0)
+    np.testing.assert_allclose(ctx.integrals()[:5], ref, rtol=1e-12)
+    t, n = ctx.step(5, c["cfl"], 10.0, 0.0)
+    u_orc, t_orc, n_orc = orc.solve(u0, 0.0, 10.0, c["cfl"], max_steps=5)
+    assert n == n_orc == 5 and t == pytest.approx(t_orc, rel=1e-12)
+    assert rel_err(ctx.download(), u_orc) < 1e-12
+
+
+@pytest.mark.parametrize("name", GOLDENS_3D)
+def test_curved3_gpu_fp64_reproduces_trixi_goldens(name):
+    c = dict(GOLDENS[name])
+    sol, ana = _golden_run(c)
+    assert sol.t[-1] == pytest.approx(c["tspan"][1], rel=1e-14)
+    if c["ic"] == "constant":
+        np.testing.assert_allclose(ana.l2, c["l2"], rtol=0, atol=7e-13)
+        return
+    np.testing.assert_allclose(ana.l2, c["l2"], rtol=1e-8)
+    np.testing.assert_allclose(ana.linf, c["linf"], rtol=1e-7)
+
+
+def test_curved3_mixed_and_flux_differencing_are_rejected():
+    semi, _ = build(_case(SRC3), precision="mixed", cells=(2, 2, 2))
+    with pytest.raises(T.TrixiGB300Error):
+        semi.device_context
+    semi, _ = build(_case(EC3), cells=(4, 4, 4))
+    with pytest.raises(T.TrixiGB300Error):
+        semi.device_context

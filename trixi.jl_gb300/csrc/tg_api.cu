@@ -1021,6 +1021,12 @@ static int launch_kernel(tg_ctx* c, int mode, const void* u_in, void* u_out, dou
       M.cos_tl = (float)(cs - (double)M.cos_t);
     }
     A.speed_bits = M.speed_bits = reduce ? &c->d_clock->speed_bits : nullptr;
+    if (c->D == 3) {
+      if (tg::launch_curved3(c->CP, A, c->stream) != 0)
+        return fail(c, TG_ERR_CUDA, "curvilinear 3D kernel launch failed: %s",
+                    cudaGetErrorString(cudaGetLastError()));
+      return TG_OK;
+    }
     if (!c->fp64 && c->nbound > 0 &&
         tg::launch_curved_ghost(c->CP, c->nbound, c->d_clock,
                                 mode == MODE_STAGE ? CK_C[stage] : 0.0, t_rhs, mode, c->d_ghost,
@@ -1117,8 +1123,10 @@ static int enqueue_stage(tg_ctx* c, int stage, bool reduce_speed) {
 static int reduce_speed(tg_ctx* c, const void* u, bool ff, unsigned long long* dst) {
   speed_reset_kernel<<<1, 1, 0, c->stream>>>(dst);
   if (c->curved) {
-    if (tg::launch_curved_speed(c->CP, u, ff, dst, c->d_status, c->stream) != 0)
-      return fail(c, TG_ERR_CUDA, "curvilinear wave-speed launch failed");
+    const int rc = c->D == 3 ? tg::launch_curved3_speed(c->CP, (const double*)u, dst, c->d_status,
+                                                        c->stream)
+                             : tg::launch_curved_speed(c->CP, u, ff, dst, c->d_status, c->stream);
+    if (rc != 0) return fail(c, TG_ERR_CUDA, "curvilinear wave-speed launch failed");
     return TG_OK;
   }
   const unsigned nb = (unsigned)((c->E + 3) / 4);  // one warp per element
@@ -1144,13 +1152,14 @@ static int reduce_speed(tg_ctx* c, const void* u, bool ff, unsigned long long* d
 // Metric terms and source tables of a curvilinear context, and its kernel
 // parameters (after the generic setup of tg_ctx_create).
 static int curved_setup(tg_ctx* c, const tg_config* cfg) {
-  const int N = c->N, NN = c->NN;
+  const int N = c->N, NN = c->NN, D = c->D;
   const int64_t E = c->E;
   const size_t nq = (size_t)E * NN;
-  std::vector<double> met(nq * 5);
+  const int MS = D * D + 1;  // metric values per node: Ja^d_c (d-major), inverse Jacobian
+  std::vector<double> met(nq * MS);
   for (size_t k = 0; k < nq; ++k) {
-    for (int m = 0; m < 4; ++m) met[k * 5 + m] = cfg->contravariant_vectors[k * 4 + m];
-    met[k * 5 + 4] = cfg->inverse_jacobian[k];
+    for (int m = 0; m < D * D; ++m) met[k * MS + m] = cfg->contravariant_vectors[k * D * D + m];
+    met[k * MS + D * D] = cfg->inverse_jacobian[k];
   }
   CUDA_TRY(nullptr, cudaMalloc((void**)&c->d_cmet, sizeof(double) * met.size()));
   CUDA_TRY(nullptr, cudaMemcpy(c->d_cmet, met.data(), sizeof(double) * met.size(),
@@ -1187,8 +1196,8 @@ static int curved_setup(tg_ctx* c, const tg_config* cfg) {
   }
   if ((src && c->fp64) || c->nbound > 0) {
     // FP64 node coordinates: sources of FP64 contexts, Dirichlet boundary values
-    CUDA_TRY(nullptr, cudaMalloc((void**)&c->d_cxy, sizeof(double) * nq * 2));
-    CUDA_TRY(nullptr, cudaMemcpy(c->d_cxy, cfg->node_coordinates, sizeof(double) * nq * 2,
+    CUDA_TRY(nullptr, cudaMalloc((void**)&c->d_cxy, sizeof(double) * nq * D));
+    CUDA_TRY(nullptr, cudaMemcpy(c->d_cxy, cfg->node_coordinates, sizeof(double) * nq * D,
                                  cudaMemcpyHostToDevice));
   }
   tg::CurvedParams& C = c->CP;
@@ -1274,7 +1283,8 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   const int D = cfg->ndims;
   if (D != 2 && D != 3) return fail(nullptr, TG_ERR_UNSUPPORTED, "ndims must be 2 or 3");
   const int N = cfg->polydeg + 1;
-  if (default_epb(D, N) == 0)
+  // (curvilinear meshes check their own kernels below)
+  if (cfg->mesh_type != TG_MESH_CURVED && default_epb(D, N) == 0)
     return fail(nullptr, TG_ERR_UNSUPPORTED, "polydeg %d is not compiled for %dD", cfg->polydeg, D);
   if (cfg->nelements <= 0) return fail(nullptr, TG_ERR_INVALID_ARGUMENT, "nelements must be > 0");
   if (cfg->ninterfaces < 0 || cfg->ninterfaces > (int64_t)D * cfg->nelements)
@@ -1305,8 +1315,15 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   const bool curved = cfg->mesh_type == TG_MESH_CURVED;
   if (curved) {
     // StructuredMesh / P4estMesh bricks: the curvilinear kernels of tg_curved.cu
-    if (D != 2) return fail(nullptr, TG_ERR_UNSUPPORTED, "curvilinear meshes are 2D only");
-    if (tg::curved_epb(N) == 0)
+    // (2D) and tg_curved3.cu (3D, FP64)
+    if (D == 3 && mixed)
+      return fail(nullptr, TG_ERR_UNSUPPORTED,
+                  "3D curvilinear meshes: FP64 only (the mixed path runs 2D curvilinear meshes)");
+    // 3D: tg_curved3.cu is built for the weak form at polydeg 3
+    if (D == 3 && (cfg->volume_integral != TG_VOLUME_WEAK_FORM || N != 4))
+      return fail(nullptr, TG_ERR_UNSUPPORTED,
+                  "3D curvilinear meshes: weak form at polydeg 3 only");
+    if (D == 2 ? tg::curved_epb(N) == 0 : !tg::curved3_supported(N))
       return fail(nullptr, TG_ERR_UNSUPPORTED, "curvilinear meshes: polydeg %d is not compiled",
                   cfg->polydeg);
     if (cfg->volume_integral == TG_VOLUME_SHOCK_CAPTURING_HG)
@@ -1326,7 +1343,7 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     if (!cfg->contravariant_vectors)
       return fail(nullptr, TG_ERR_INVALID_ARGUMENT,
                   "curvilinear meshes need contravariant_vectors");
-    const int64_t nn = (int64_t)N * N;
+    const int64_t nn = D == 2 ? (int64_t)N * N : (int64_t)N * N * N;
     for (int64_t k = 0; k < cfg->nelements * nn; ++k)
       if (!(cfg->inverse_jacobian[k] > 0.0))
         return fail(nullptr, TG_ERR_UNSUPPORTED,
@@ -2080,9 +2097,11 @@ int tg_integrals(tg_ctx* c, double* out) {
   if (!c->d_partial) CUDA_TRY(c, cudaMalloc((void**)&c->d_partial, sizeof(double) * K * c->E));
   const int64_t nb = (c->E + 127) / 128;
   if (c->curved) {
-    if (tg::launch_curved_integrals(c->CP, c->d_u[c->cur], !c->fp64, c->d_weights, c->d_partial,
-                                    c->stream) != 0)
-      return fail(c, TG_ERR_CUDA, "curvilinear integrals launch failed");
+    const int rc = c->D == 3 ? tg::launch_curved3_integrals(c->CP, (const double*)c->d_u[c->cur],
+                                                            c->d_weights, c->d_partial, c->stream)
+                             : tg::launch_curved_integrals(c->CP, c->d_u[c->cur], !c->fp64,
+                                                           c->d_weights, c->d_partial, c->stream);
+    if (rc != 0) return fail(c, TG_ERR_CUDA, "curvilinear integrals launch failed");
   } else if (c->fp64) {
     const double* u = (const double*)c->d_u[c->cur];
     if (c->D == 2)

@@ -67,4 +67,14 @@ int launch_curved_speed(const CurvedParams& P, const void* u, bool ff, unsigned 
 int launch_curved_integrals(const CurvedParams& P, const void* u, bool ff, const double* weights,
                             double* partial, cudaStream_t stream);
 
+// 3D curvilinear meshes (tg_curved3.cu), FP64 contexts only: P.met holds
+// [E][NN][10] (Ja^d_c at d * 3 + c, then the inverse Jacobian), P.xy [E][NN][3],
+// P.nbr [E][6].
+int curved3_supported(int N);
+int launch_curved3(const CurvedParams& P, const StageArgs& A, cudaStream_t stream);
+int launch_curved3_speed(const CurvedParams& P, const double* u, unsigned long long* dst,
+                         int32_t* status, cudaStream_t stream);
+int launch_curved3_integrals(const CurvedParams& P, const double* u, const double* weights,
+                             double* partial, cudaStream_t stream);
+
 }  // namespace tg

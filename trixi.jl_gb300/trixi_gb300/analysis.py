@@ -40,11 +40,15 @@ def calc_error_norms(u, t, semi, analyzer: LobattoLegendreAnalyzer | None = None
         ue_exact = exact(xa, t, eq)
         diff = ue_exact - ua
         if curved:
-            # |J| interpolated to the analyzer nodes (analysis_dg2d.jl:141-197)
-            ja = np.abs(np.einsum("aj,bi,eji->eab", V, V, 1.0 / semi.inverse_jacobian[s:s + chunk],
-                                  optimize=True))
+            # |J| interpolated to the analyzer nodes (analysis_dg2d.jl:141-197, 3D analogue)
+            if D == 2:
+                ja = np.abs(np.einsum("aj,bi,eji->eab", V, V,
+                                      1.0 / semi.inverse_jacobian[s:s + chunk], optimize=True))
+            else:
+                ja = np.abs(np.einsum("ak,bj,ci,ekji->eabc", V, V, V,
+                                      1.0 / semi.inverse_jacobian[s:s + chunk], optimize=True))
             wj = W[None] * ja
-            l2 += np.sum(diff ** 2 * wj[..., None], axis=(0, 1, 2))
+            l2 += np.sum(diff ** 2 * wj[..., None], axis=tuple(range(D + 1)))
             vol += wj.sum()
         else:
             vj = (1.0 / semi.inverse_jacobian[s:s + chunk]) ** D

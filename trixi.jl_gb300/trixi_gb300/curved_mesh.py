@@ -250,7 +250,13 @@ def metric_terms_3d(X, basis):
 
 
 class StructuredMesh(_CurvedBrick2D):
-    """StructuredMesh(cells_per_dimension, mapping | faces | (cmin, cmax); periodicity)."""
+    """StructuredMesh(cells_per_dimension, mapping | faces | (cmin, cmax); periodicity).
+    Three cells_per_dimension give a StructuredMesh3D."""
+
+    def __new__(cls, cells_per_dimension, *args, **kwargs):
+        if len(cells_per_dimension) == 3:
+            return StructuredMesh3D(cells_per_dimension, *args, **kwargs)
+        return super().__new__(cls)
 
     def __init__(self, cells_per_dimension, mapping=None, coordinates_max=None, *, faces=None,
                  coordinates_min=None, periodicity=True):
@@ -289,8 +295,8 @@ class StructuredMesh3D:
     """StructuredMesh with three cells_per_dimension (structured_mesh.jl): the
     mapping of three reference coordinates, six faces (transfinite) or
     coordinates_min/max.  Host setup of the element node coordinates
-    (containers_3d.jl:37-65, cells x fastest) and neighbours; the GPU path runs
-    2D curvilinear meshes only, the oracle also these."""
+    (containers_3d.jl:37-65, cells x fastest), neighbours and interfaces.  The
+    GPU path runs these in FP64."""
     ndims = 3
     curved = True
 
@@ -316,6 +322,29 @@ class StructuredMesh3D:
         self.nelements = nx * ny * nz
         e = np.arange(self.nelements)
         self.cells = np.stack([e % nx, (e // nx) % ny, e // (nx * ny)], axis=1)
+
+    def interfaces(self):
+        """neighbor_ids [I, 2] (1-based: element on the negative side, element on
+        the positive side) and orientations [I] (1..3), per element in order,
+        positive directions only."""
+        nb = self.neighbors()
+        E = self.nelements
+        ids = np.empty((E, 3, 2), dtype=np.int64)
+        ori = np.empty((E, 3), dtype=np.int64)
+        for d in range(3):
+            ids[:, d, 0] = np.arange(E) + 1
+            ids[:, d, 1] = nb[:, 2 * d + 1] + 1
+            ori[:, d] = d + 1
+        keep = (nb[:, 1::2] >= 0).reshape(3 * E)
+        return ids.reshape(3 * E, 2)[keep], ori.reshape(3 * E)[keep]
+
+    def mortars(self):
+        z = np.zeros((0, 5), dtype=np.int64)
+        return z, np.zeros(0, dtype=np.int64), np.zeros(0, dtype=np.int64)
+
+    @property
+    def is_uniform(self):
+        return True
 
     def neighbors(self):
         """[E, 6] (0-based) across -x, +x, -y, +y, -z, +z; -1 at a non-periodic edge."""

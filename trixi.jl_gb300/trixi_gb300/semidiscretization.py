@@ -358,12 +358,12 @@ class SemidiscretizationHyperbolic:
         if self.curved:
             # StructuredMesh / P4estMesh brick: per-node metric terms
             # (dgsem_structured/containers_2d.jl:9-35, dgsem_p4est/containers_2d.jl:9-27)
-            from .curved_mesh import metric_terms
+            from .curved_mesh import metric_terms, metric_terms_3d
             if isinstance(solver.volume_integral, VolumeIntegralShockCapturingHG):
                 raise NotImplementedError("curvilinear meshes: weak form or flux differencing only")
             self.node_coordinates = mesh.node_coordinates(solver.basis)
-            self.contravariant_vectors, self.inverse_jacobian = metric_terms(
-                self.node_coordinates, solver.basis)
+            self.contravariant_vectors, self.inverse_jacobian = (
+                metric_terms if D == 2 else metric_terms_3d)(self.node_coordinates, solver.basis)
             self.neighbor_ids, self.orientations = mesh.interfaces()
             (self.mortar_neighbor_ids, self.mortar_large_sides,
              self.mortar_orientations) = mesh.mortars()
