@@ -179,3 +179,21 @@ def test_amr_rejects_curvilinear_meshes():
         T.initial_condition_constant, T.DGSEM(polydeg=3, surface_flux=T.flux_lax_friedrichs))
     with pytest.raises(NotImplementedError):
         T.AMRCallback(semi, None, interval=5)
+
+
+def test_curved3_config_carries_metric_and_interfaces():
+    import trixi_gb300 as T
+    from trixi_gb300 import _lib
+    from trixi_gb300.semidiscretization import make_config
+    eq = T.CompressibleEulerEquations3D(1.4)
+    solver = T.DGSEM(polydeg=3, surface_flux=T.flux_lax_friedrichs)
+    mesh = T.StructuredMesh((3, 2, 2), (0.0, 0.0, 0.0), (3.0, 2.0, 1.0))
+    assert isinstance(mesh, T.curved_mesh.StructuredMesh3D)
+    semi = T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_convergence_test, solver)
+    cfg, keep = make_config(semi, "fp64")
+    assert cfg.mesh_type == _lib.TG_MESH_CURVED and cfg.ndims == 3
+    assert cfg.ninterfaces == 3 * 12
+    assert semi.contravariant_vectors.shape == (12, 4, 4, 4, 3, 3)
+    # affine box: Ja^1 = (dy/deta dz/dzeta, 0, 0) with cell sizes 1, 1, 0.5
+    np.testing.assert_allclose(semi.contravariant_vectors[..., 0, 0], 0.5 * 0.25, rtol=1e-13)
+    np.testing.assert_allclose(semi.inverse_jacobian, 1.0 / (0.5 * 0.5 * 0.25), rtol=1e-12)

@@ -115,7 +115,7 @@ Builds a device context from a `SemidiscretizationHyperbolic` on a periodic
 # preserved (GC.@preserve) by the caller.
 function config(semi, precision, device)
     (; mesh, equations, solver, cache, source_terms) = semi
-    mesh isa Union{Trixi.StructuredMesh{2}, Trixi.P4estMesh{2}} &&
+    mesh isa Union{Trixi.StructuredMesh{2}, Trixi.P4estMesh{2}, Trixi.StructuredMesh{3}} &&
         return curved_config(semi, precision, device)
     b = solver.basis
     vi, vf, sf_fv, amax, amin, asmooth = volume_codes(solver.volume_integral,
@@ -142,11 +142,18 @@ end
 # the positive side) pairs and directions, 1-based like Trixi's arrays.  The
 # arrays are kept in `CURVED_KEEP` while the config is in use.
 const CURVED_KEEP = IdDict{Any, Any}()
-curved_interfaces(mesh::Trixi.StructuredMesh{2}, cache) =
-    # left_neighbors[dir, element]: the element across the face at -dir
-    (vec([cache.elements.left_neighbors[d, e] for d in 1:2, e in 1:size(cache.elements.left_neighbors, 2)]),
-     vec([e for d in 1:2, e in 1:size(cache.elements.left_neighbors, 2)]),
-     vec([d for d in 1:2, e in 1:size(cache.elements.left_neighbors, 2)]))
+function curved_interfaces(mesh::Trixi.StructuredMesh{2}, cache)
+    ln = cache.elements.left_neighbors            # [2, E]: element across the face at -dir (0: boundary)
+    E = size(ln, 2)
+    keep = [(d, e) for e in 1:E for d in 1:2 if ln[d, e] > 0]
+    return [ln[d, e] for (d, e) in keep], [e for (d, e) in keep], [d for (d, e) in keep]
+end
+function curved_interfaces(mesh::Trixi.StructuredMesh{3}, cache)
+    ln = cache.elements.left_neighbors            # [3, E]: element across the face at -dir
+    E = size(ln, 2)
+    keep = [(d, e) for e in 1:E for d in 1:3 if ln[d, e] > 0]
+    return [ln[d, e] for (d, e) in keep], [e for (d, e) in keep], [d for (d, e) in keep]
+end
 function curved_interfaces(mesh::Trixi.P4estMesh{2}, cache)
     # primary side at :end of its face coordinate = negative side of the interface
     ids, ni = cache.interfaces.neighbor_ids, cache.interfaces.node_indices
@@ -170,15 +177,16 @@ function curved_config(semi, precision, device)
     vi, vf, sf_fv, amax, amin, asmooth = volume_codes(solver.volume_integral,
                                                       solver.surface_integral.surface_flux)
     sf = flux_code(solver.surface_integral.surface_flux)
-    return TgConfig(2, Trixi.polydeg(solver), nelements(solver, cache), length(ori),
+    return TgConfig(ndims(mesh), Trixi.polydeg(solver), nelements(solver, cache), length(ori),
                     equations.gamma, vi, vf, sf, sf, amax, amin, asmooth,
                     source_code(source_terms), precision, device,
                     pointer(b.nodes), pointer(b.weights), pointer(b.inverse_weights),
                     pointer(b.derivative_hat), pointer(b.derivative_split),
                     pointer(b.inverse_vandermonde_legendre), pointer(nb), pointer(ori),
-                    pointer(cache.elements.inverse_jacobian),      # [n, n, E]
+                    pointer(cache.elements.inverse_jacobian),      # [n, n(, n), E]
                     pointer(cache.elements.node_coordinates), 0,
-                    ntuple(_ -> Int32(0), 6), Int32(0), (0.0, 0.0, 0.0, 0.0),
+                    boundary_codes(semi.boundary_conditions, ndims(mesh)),
+                    boundary_value_code(semi.boundary_conditions)...,
                     Int64(0), Ptr{Int64}(C_NULL), Ptr{Int64}(C_NULL), Ptr{Int64}(C_NULL),
                     Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL),
                     Ptr{Float64}(C_NULL),
