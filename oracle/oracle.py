@@ -94,6 +94,7 @@ def _load():
     lib.orc_curved_create.argtypes = [i, i64, P(d), P(i64), d, i, i, i, i]
     lib.orc_curved_destroy.argtypes = [vp]
     lib.orc_curved_set_dirichlet.argtypes = [vp, i, P(d)]
+    lib.orc_curved_set_hg.argtypes = [vp, d, d, i, i]
     lib.orc_curved_metric.argtypes = [vp, P(d), P(d)]
     lib.orc_curved_initial_condition.argtypes = [vp, i, P(d), d, P(d)]
     lib.orc_curved_rhs.argtypes = [vp, P(d), P(d), d]
@@ -424,6 +425,11 @@ class CurvedOracle:
     @property
     def shape(self):
         return (self.E, self.n, self.n, 4)
+
+    def set_hg(self, alpha_max, alpha_min, alpha_smooth, fv_flux):
+        """IndicatorHennemannGassner(density_pressure) parameters and the FV flux of
+        a VI_SHOCKCAPTURING_HG solver."""
+        _lib.orc_curved_set_hg(self.h, alpha_max, alpha_min, int(alpha_smooth), fv_flux)
 
     def set_dirichlet(self, ic, params=None):
         """BoundaryConditionDirichlet(initial condition ic) on every face without a

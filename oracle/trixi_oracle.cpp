@@ -2454,8 +2454,95 @@ struct Curved {
   // initial condition (bc_ic, bc_par)
   int bc_ic = -1;
   double bc_par[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  // VolumeIntegralShockCapturingHG: indicator parameters, the FV flux and the
+  // subcell normal vectors [E][dir][N - 1][n][2] (calc_normalvectors_subcell_fv!)
+  double alpha_max = 0.5, alpha_min = 0.001;
+  bool alpha_smooth = true;
+  int fvflux = FLUX_LAX_FRIEDRICHS;
+  std::vector<double> snv;
   size_t ui(int64_t e, int node) const { return ((size_t)e * nn + node) * 4; }
 };
+
+// calc_normalvectors_subcell_fv! (dgsem_structured/containers_2d.jl:200-298):
+// the normal of the subcell interface between nodes i and i + 1 of a line is
+// Ja at the first node plus the partial sums of w_m D[m, :] Ja along the line,
+// which keeps the finite-volume subcells free-stream preserving.
+static void curved_subcell_normals(Curved& c) {
+  const int n = c.n, nn = c.nn;
+  const std::vector<double>& Dm = c.b.D;
+  const std::vector<double>& w = c.b.weights;
+  c.snv.assign((size_t)c.E * 2 * (n - 1) * n * 2, 0.0);
+  for (int64_t e = 0; e < c.E; ++e)
+    for (int dir = 0; dir < 2; ++dir)
+      for (int l = 0; l < n; ++l) {
+        // node a of line l in direction dir
+        auto q = [&](int a) { return dir == 0 ? a + n * l : l + n * a; };
+        double acc[2];
+        for (int xy = 0; xy < 2; ++xy) acc[xy] = c.Ja[((size_t)e * nn + q(0)) * 4 + 2 * dir + xy];
+        for (int i = 0; i < n - 1; ++i) {
+          for (int m = 0; m < n; ++m) {
+            const double wd = w[i] * Dm[i * n + m];
+            for (int xy = 0; xy < 2; ++xy)
+              acc[xy] += wd * c.Ja[((size_t)e * nn + q(m)) * 4 + 2 * dir + xy];
+          }
+          for (int xy = 0; xy < 2; ++xy)
+            c.snv[((((size_t)e * 2 + dir) * (n - 1) + i) * n + l) * 2 + xy] = acc[xy];
+        }
+      }
+}
+
+// IndicatorHennemannGassner on density_pressure (indicators.jl:114-148,
+// indicators_2d.jl:30-136) per element of a curvilinear mesh, smoothed over
+// the element neighbours
+static void curved_hg_alpha(const Curved& c, const double* u, std::vector<double>& alpha) {
+  const int n = c.n, nn = c.nn;
+  const double threshold = 0.5 * std::pow(10.0, -1.8 * std::pow((double)n, 0.25));
+  const double parameter_s = std::log((1 - 0.0001) / 0.0001);
+  alpha.assign(c.E, 0.0);
+  const double* V = c.b.Vinv.data();
+  for (int64_t e = 0; e < c.E; ++e) {
+    double ind[64], t1[64];
+    for (int q = 0; q < nn; ++q) ind[q] = density_pressure(c.eq, &u[c.ui(e, q)]);
+    double modal[64];
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        double r = 0;
+        for (int ii = 0; ii < n; ++ii) r += V[i * n + ii] * ind[ii + n * j];
+        t1[i + n * j] = r;
+      }
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        double r = 0;
+        for (int jj = 0; jj < n; ++jj) r += V[j * n + jj] * t1[i + n * jj];
+        modal[i + n * j] = r;
+      }
+    double e_clip2 = 0, e_clip1 = 0, e_tot = 0;
+    for (int q = 0; q < nn; ++q) {
+      const int mx = std::max(q % n, q / n);
+      const double m2 = modal[q] * modal[q];
+      if (mx <= n - 3) e_clip2 += m2;
+      if (mx <= n - 2) e_clip1 += m2;
+      e_tot += m2;
+    }
+    const double f1 = e_tot != 0 ? (e_tot - e_clip1) / e_tot : 0.0;
+    const double f2 = e_clip1 != 0 ? (e_clip1 - e_clip2) / e_clip1 : 0.0;
+    const double energy = std::max(f1, f2);
+    double a = 1 / (1 + std::exp(-parameter_s / threshold * (energy - threshold)));
+    if (a < c.alpha_min) a = 0;
+    if (a > 1 - c.alpha_min) a = 1;
+    alpha[e] = std::min(c.alpha_max, a);
+  }
+  if (c.alpha_smooth) {
+    const std::vector<double> tmp = alpha;
+    for (int64_t e = 0; e < c.E; ++e)
+      for (int o = 0; o < 2; ++o) {
+        const int64_t r = c.nbr[e * 4 + 2 * o + 1];  // interface (e, r) in direction o
+        if (r < 0) continue;
+        alpha[e] = std::max({tmp[e], 0.5 * tmp[r], alpha[e]});
+        alpha[r] = std::max({tmp[r], 0.5 * tmp[e], alpha[r]});
+      }
+  }
+}
 
 // calc_jacobian_matrix!, calc_contravariant_vectors!, calc_inverse_jacobian!
 // (dgsem_structured/containers_2d.jl:61-152)
@@ -2499,6 +2586,12 @@ static void curved_rhs(const Curved& c, double* du, const double* u, double t) {
   const Basis& b = c.b;
   const Eq& eq = c.eq;
   std::vector<double> sfv((size_t)c.E * 4 * n * 4);  // [E][dir][l][v]
+  // VolumeIntegralShockCapturingHG (calc_volume_integral.jl:231-272): the
+  // blending factor per element, FD weighted by 1 - alpha, FV by alpha
+  const bool hg = c.vi == VI_SHOCKCAPTURING_HG;
+  std::vector<double> alpha;
+  if (hg) curved_hg_alpha(c, u, alpha);
+  const double atol = std::max(100 * 2.220446049250313e-16, std::pow(2.220446049250313e-16, 0.75));
   // interface fluxes: for each element, the faces towards its -x and -y neighbours
 #pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < c.E; ++e) {
@@ -2574,6 +2667,9 @@ static void curved_rhs(const Curved& c, double* du, const double* u, double t) {
               de[(i + n * jj) * 4 + v] = std::fma(b.Dhat[jj * n + j], cf2[v], de[(i + n * jj) * 4 + v]);
         }
     } else {
+      const double ae = hg ? alpha[e] : 0.0;
+      const bool dg_only = !hg || std::fabs(ae) <= atol;
+      const double fdw = dg_only ? 1.0 : 1.0 - ae;
       for (int j = 0; j < n; ++j)
         for (int i = 0; i < n; ++i) {
           const int q = i + n * j;
@@ -2583,8 +2679,8 @@ static void curved_rhs(const Curved& c, double* du, const double* u, double t) {
             double F[4];
             two_point_flux_n(eq, c.vf, ue + q * 4, ue + r * 4, avg, F);
             for (int v = 0; v < 4; ++v) {
-              de[q * 4 + v] = std::fma(b.Dsplit[i * n + ii], F[v], de[q * 4 + v]);
-              de[r * 4 + v] = std::fma(b.Dsplit[ii * n + i], F[v], de[r * 4 + v]);
+              de[q * 4 + v] = std::fma(fdw * b.Dsplit[i * n + ii], F[v], de[q * 4 + v]);
+              de[r * 4 + v] = std::fma(fdw * b.Dsplit[ii * n + i], F[v], de[r * 4 + v]);
             }
           }
           for (int jj = j + 1; jj < n; ++jj) {
@@ -2594,11 +2690,28 @@ static void curved_rhs(const Curved& c, double* du, const double* u, double t) {
             double F[4];
             two_point_flux_n(eq, c.vf, ue + q * 4, ue + r * 4, avg, F);
             for (int v = 0; v < 4; ++v) {
-              de[q * 4 + v] = std::fma(b.Dsplit[j * n + jj], F[v], de[q * 4 + v]);
-              de[r * 4 + v] = std::fma(b.Dsplit[jj * n + j], F[v], de[r * 4 + v]);
+              de[q * 4 + v] = std::fma(fdw * b.Dsplit[j * n + jj], F[v], de[q * 4 + v]);
+              de[r * 4 + v] = std::fma(fdw * b.Dsplit[jj * n + j], F[v], de[r * 4 + v]);
             }
           }
         }
+      if (!dg_only) {
+        // fv_kernel! / calcflux_fv! (dgsem_structured/dg_2d.jl:304-345): subcell
+        // fluxes along the free-stream preserving subcell normals, zero at the
+        // element faces
+        for (int dir = 0; dir < 2; ++dir)
+          for (int l = 0; l < n; ++l) {
+            double fst[9][4] = {};
+            auto qn = [&](int a) { return dir == 0 ? a + n * l : l + n * a; };
+            for (int i = 1; i < n; ++i) {
+              const double* nv = &c.snv[((((size_t)e * 2 + dir) * (n - 1) + (i - 1)) * n + l) * 2];
+              two_point_flux_n(eq, c.fvflux, ue + qn(i - 1) * 4, ue + qn(i) * 4, nv, fst[i]);
+            }
+            for (int i = 0; i < n; ++i)
+              for (int v = 0; v < 4; ++v)
+                de[qn(i) * 4 + v] += ae * (b.inv_weights[i] * (fst[i + 1][v] - fst[i][v]));
+          }
+      }
     }
     // surface integral
     const double factor = b.inv_weights[0];
@@ -2723,6 +2836,17 @@ void* orc_curved_create(int polydeg, int64_t nelements, const double* x, const i
 }
 
 void orc_curved_destroy(void* h) { delete (Curved*)h; }
+
+// VolumeIntegralShockCapturingHG settings (the volume integral must be
+// VI_SHOCKCAPTURING_HG): indicator parameters and the FV subcell flux
+void orc_curved_set_hg(void* h, double alpha_max, double alpha_min, int alpha_smooth, int fvflux) {
+  Curved& c = *(Curved*)h;
+  c.alpha_max = alpha_max;
+  c.alpha_min = alpha_min;
+  c.alpha_smooth = alpha_smooth != 0;
+  c.fvflux = fvflux;
+  curved_subcell_normals(c);
+}
 
 // Dirichlet values (an initial condition and its parameters) of the faces
 // without a neighbour

@@ -70,7 +70,18 @@ def _warped_cube_nonperiodic(xi, eta, zeta):
     return x + 1, y + 1, z + 1
 
 
+def _sedov_warp(xi, eta):
+    # elixir_euler_sedov.jl (structured_2d_dgsem)
+    y = eta + 0.125 * (np.cos(1.5 * np.pi * xi) * np.cos(0.5 * np.pi * eta))
+    x = xi + 0.125 * (np.cos(0.5 * np.pi * xi) * np.cos(2 * np.pi * y))
+    return x, y
+
+
 def mapping_kwargs(name):
+    if name == "square_m1_1":
+        return dict(coordinates_min=(-1.0, -1.0), coordinates_max=(1.0, 1.0))
+    if name == "sedov_warp":
+        return dict(mapping=_sedov_warp)
     if name == "cube_0_2_faces":
         return dict(faces=CUBE_0_2_FACES)
     if name == "warped_cube_0_3":
@@ -103,7 +114,7 @@ def curved_mesh(c, cells=None):
 
 def curved_oracle(O, c, mesh):
     from trixi_gb300.basis import LobattoLegendreBasis
-    vi = dict(weak=O.VI_WEAK, fluxdiff=O.VI_FLUXDIFF)[c["vi"]]
+    vi = dict(weak=O.VI_WEAK, fluxdiff=O.VI_FLUXDIFF, hg=O.VI_SHOCKCAPTURING_HG)[c["vi"]]
     fl = dict(central=O.FLUX_CENTRAL, ranocha=O.FLUX_RANOCHA, shima_etal=O.FLUX_SHIMA_ETAL,
               llf=O.FLUX_LAX_FRIEDRICHS, llf_naive=O.FLUX_LAX_FRIEDRICHS_NAIVE,
               chandrashekar=O.FLUX_CHANDRASHEKAR)
@@ -112,6 +123,8 @@ def curved_oracle(O, c, mesh):
     cls = O.CurvedOracle3D if c.get("ndims", 2) == 3 else O.CurvedOracle
     orc = cls(c["polydeg"], X, mesh.neighbors(), c.get("gamma", 1.4), vi, fl[c["volume_flux"]],
               fl[c["surface_flux"]], src)
+    if c["vi"] == "hg":
+        orc.set_hg(c["alpha_max"], c["alpha_min"], c["alpha_smooth"], fl[c["volume_flux_fv"]])
     if c.get("boundary") == "dirichlet":
         orc.set_dirichlet(dict(convergence_test=O.IC_CONVERGENCE_TEST,
                                weak_blast_wave=O.IC_WEAK_BLAST_WAVE,

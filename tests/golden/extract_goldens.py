@@ -289,6 +289,28 @@ CURVED_CASES = {
         mesh="structured", cells=[16, 16], mapping="warped_square_0_3", polydeg=4,
         ic="weak_blast_wave", source="none", vi="fluxdiff",
         volume_flux="ranocha", surface_flux="ranocha", cfl=1.0, tspan=[0.0, 2.0]),
+    # shock capturing on curvilinear meshes (oracle)
+    "P4estMesh2D: elixir_euler_shockcapturing_ec.jl": dict(
+        file="test/test_p4est_2d.jl",
+        elixir="examples/p4est_2d_dgsem/elixir_euler_shockcapturing_ec.jl",
+        mesh="p4est", trees=[4, 4], level=2, mapping="square_m1_1", polydeg=4,
+        ic="weak_blast_wave", source="none", vi="hg", volume_flux="ranocha",
+        volume_flux_fv="ranocha", surface_flux="ranocha", alpha_max=1.0, alpha_min=0.001,
+        alpha_smooth=True, cfl=1.0, tspan=[0.0, 2.0]),
+    "P4estMesh2D: elixir_euler_shockcapturing_ec.jl (flux_chandrashekar)": dict(
+        file="test/test_p4est_2d.jl",
+        elixir="examples/p4est_2d_dgsem/elixir_euler_shockcapturing_ec.jl",
+        mesh="p4est", trees=[4, 4], level=2, mapping="square_m1_1", polydeg=4,
+        ic="weak_blast_wave", source="none", vi="hg", volume_flux="chandrashekar",
+        volume_flux_fv="ranocha", surface_flux="ranocha", alpha_max=1.0, alpha_min=0.001,
+        alpha_smooth=True, cfl=1.0, tspan=[0.0, 2.0]),
+    "StructuredMesh2D: elixir_euler_sedov.jl": dict(
+        file="test/test_structured_2d.jl",
+        elixir="examples/structured_2d_dgsem/elixir_euler_sedov.jl",
+        mesh="structured", cells=[16, 16], mapping="sedov_warp", polydeg=4,
+        ic="sedov_blast_wave", source="none", vi="hg", volume_flux="ranocha",
+        volume_flux_fv="llf_naive", surface_flux="llf_naive", alpha_max=1.0, alpha_min=0.001,
+        alpha_smooth=True, cfl=0.5, tspan=[0.0, 12.5]),
     # 3D (oracle only; the GPU path runs 2D curvilinear meshes)
     "StructuredMesh3D: elixir_euler_source_terms.jl": dict(
         file="test/test_structured_3d.jl",
