@@ -255,6 +255,16 @@ int tg_max_dt(tg_ctx* ctx, const double* u_dev, double* dt);
  * zeroes u_tmp first.  du never leaves the chip.  Asynchronous. */
 int tg_rk_stage(tg_ctx* ctx, int32_t stage, double t, double dt);
 
+/* The passes of one tg_rk_stage launched separately, so that each can be
+ * timed alone: parts = 1 sets the stage clock and runs the shock indicator
+ * of the current state (nothing else for contexts without HG shock
+ * capturing); parts = 2 runs the element kernel of the stage (with its
+ * mortar and boundary pre-passes) on the blending factors of the last
+ * indicator pass and advances the state; parts = 3 is tg_rk_stage.  Part 1
+ * must precede part 2 of the same stage.  No counterpart in the reference
+ * (its rhs! is one call); asynchronous. */
+int tg_rk_stage_part(tg_ctx* ctx, int32_t stage, double t, double dt, int32_t parts);
+
 /* Time stepping with Trixi's SimpleIntegrator2N + StepsizeCallback(cfl)
  * semantics: dt = cfl * max_dt(u) after every step (and before the first
  * one), clamped to reach t_end exactly (limit_dt!).  Steps are CUDA-graph

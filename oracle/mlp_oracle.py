@@ -4,7 +4,12 @@ Forward pass, mean-squared-error loss and its gradient for the network
 n_in -> H -> H -> 1 (ReLU) with the parameter layout of libtrixi_gb300
 (W1[H][n_in], b1[H], W2[H][H], b2[H], w3[H], b3), evaluated in float64 with
 the weights rounded to bfloat16 (round to nearest even) as the GPU kernels
-use them.  Used to check the GPU forward/backward kernels.
+use them; layer inputs and accumulation are exact.  With ``split_inputs``
+the inputs of the two hidden layers (the features and the first hidden
+layer's activations) are replaced by the sum of their BF16 hi and lo parts,
+hi = bf16(x), lo = bf16(x - hi) of the float32 value, which is what the
+tensor-core inference kernel feeds its MMAs.  Used to check the GPU
+forward/backward kernels.
 """
 import numpy as np
 
@@ -28,22 +33,33 @@ def unpack(w, n_in, H):
     return W1, b1, W2, b2, w3, b3
 
 
-def forward(w, x, n_in, H):
+def split_bf16(x):
+    """hi + lo with hi = bf16(x), lo = bf16(x - hi), of the float32 values of x."""
+    x32 = np.asarray(x, dtype=np.float32)
+    hi = to_bf16(x32)
+    lo = to_bf16((x32.astype(np.float64) - hi).astype(np.float32))
+    return hi + lo
+
+
+def forward(w, x, n_in, H, split_inputs=False):
+    """Network output and the layer inputs/activations (x as used, h1, h2)."""
     W1, b1, W2, b2, w3, b3 = unpack(w, n_in, H)
+    x = split_bf16(x) if split_inputs else np.asarray(x, dtype=np.float64)
     z1 = x @ W1.T + b1
     h1 = np.maximum(z1, 0)
+    if split_inputs:
+        h1 = split_bf16(h1)
     z2 = h1 @ W2.T + b2
     h2 = np.maximum(z2, 0)
-    return h2 @ w3 + b3, (h1, h2)
+    return h2 @ w3 + b3, (x, h1, h2)
 
 
 def loss_and_grad(w32, x, y, n_in, H):
     """MSE and its gradient with respect to the (bf16-rounded) parameters."""
     w = to_bf16(w32)
-    x = np.asarray(x, dtype=np.float64)
     y = np.asarray(y, dtype=np.float64)
     W1, b1, W2, b2, w3, b3 = unpack(w, n_in, H)
-    out, (h1, h2) = forward(w, x, n_in, H)
+    out, (xu, h1, h2) = forward(w, x, n_in, H)
     n = len(y)
     r = out - y
     loss = np.mean(r ** 2)
@@ -55,7 +71,7 @@ def loss_and_grad(w32, x, y, n_in, H):
     gb2 = dz2.sum(0)
     dh1 = dz2 @ W2
     dz1 = dh1 * (h1 > 0)
-    gW1 = dz1.T @ x
+    gW1 = dz1.T @ xu
     gb1 = dz1.sum(0)
     g = np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gw3, [gb3]])
     return loss, g

@@ -31,6 +31,25 @@ BC_PERIODIC, BC_DIRICHLET, BC_SLIP_WALL = 0, 1, 2
  IC_DENSITY_WAVE) = range(12)
 
 _lib = None
+_PORTABLE_FLAGS = "g++ -O3 -fopenmp (portable)"
+
+
+def select_build(kind: str = "portable") -> str:
+    """Chooses which build of the oracle the next load uses and returns its
+    compile flags: "portable" (the parity checker) or "native" (tuned for the
+    host CPU by oracle/build.sh; used only for timing the CPU baseline).  Has
+    no effect once a build is loaded."""
+    global _LIB_PATH
+    native = os.path.join(_HERE, "_build", "liboracle_native.so")
+    if _lib is None and kind == "native" and os.path.exists(native):
+        _LIB_PATH = native
+    if _LIB_PATH == native:
+        try:
+            with open(os.path.join(_HERE, "_build", "liboracle_native.flags")) as f:
+                return f.read().strip()
+        except OSError:
+            return "native"
+    return _PORTABLE_FLAGS
 
 
 def build() -> str:

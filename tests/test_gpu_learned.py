@@ -34,9 +34,14 @@ def test_mlp_gradient_matches_oracle(ndims):
     loss_ref, g_ref = MO.loss_and_grad(w, x.astype(np.float64), y.astype(np.float64), n_in, H)
     assert loss_gpu == pytest.approx(loss_ref, rel=1e-5)
     assert np.linalg.norm(g_gpu - g_ref) <= 1e-4 * np.linalg.norm(g_ref)
-    # predictions too
+    # predictions of the tensor-core kernel (BF16 MMAs on hi/lo splits of the
+    # FP32 layer inputs, FP32 accumulation) against the oracle of that
+    # evaluation, and against the exact network
+    p_gpu = net.predict(x)
+    p_split, _ = MO.forward(MO.to_bf16(w), x.astype(np.float64), n_in, H, split_inputs=True)
+    np.testing.assert_allclose(p_gpu, p_split, rtol=3e-5, atol=3e-6)
     p_ref, _ = MO.forward(MO.to_bf16(w), x.astype(np.float64), n_in, H)
-    np.testing.assert_allclose(net.predict(x), p_ref, rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(p_gpu, p_ref, rtol=1e-4, atol=1e-5)
 
 
 def _run_and_harvest(net, case, t_end, every=10, stride=1, precision="mixed"):
@@ -102,7 +107,7 @@ def test_learned_indicator_deployed_with_hg_fallback(trained):
 
 
 def test_deployed_predictions_equal_the_inference_kernel(trained):
-    # the one-pass 2D deployment kernel evaluates the same network as predict()
+    # deployment and predict() run the same tensor-core kernel: the same bits
     net = trained[0]
     semi, _ = build(KHI, precision="mixed")
     ctx = semi.device_context
@@ -140,7 +145,17 @@ def test_3d_deployment_uses_the_network_and_the_hg_fallback():
     n0 = net.count
     net.harvest(semi)
     x, _ = net.dataset()
-    np.testing.assert_allclose(net.predict(x[n0:]), pred, rtol=1e-6, atol=1e-7)
+    np.testing.assert_array_equal(net.predict(x[n0:]), pred)  # the same tensor-core kernel
     sqrt_thr = np.sqrt(0.5 * 10 ** (-1.8 * 4 ** 0.25))
     np.testing.assert_array_equal(flag == 1, np.abs(pred - sqrt_thr) < 0.05)
     ShockIndicatorMLP.undeploy(semi)
+
+
+def test_tensor_core_network_matches_the_oracle_on_the_training_set(trained):
+    # the trained network on its own harvested rows: the tcgen05 kernel against
+    # the FP64 oracle of the same evaluation (hi/lo BF16 layer inputs)
+    net, x, y = trained[:3]
+    rows = x[::7][:20000]
+    p_ref, _ = MO.forward(MO.to_bf16(net.params), rows.astype(np.float64), net.n_inputs,
+                          net.hidden, split_inputs=True)
+    np.testing.assert_allclose(net.predict(rows), p_ref, rtol=3e-5, atol=3e-6)

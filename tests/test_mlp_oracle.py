@@ -28,3 +28,20 @@ def test_bf16_rounding_is_nearest_even():
     assert r[0] == 1.0 and r[1] == 1.0  # tie to even
     assert r[2] == 1.0078125
     assert abs(r[3] - v[3]) <= abs(v[3]) * 2 ** -8
+
+
+def test_split_bf16_inputs_represent_float32_to_2_pow_minus_16():
+    # the tensor-core kernel feeds each FP32 layer input as BF16 hi + lo: the
+    # pair carries 16 significant bits, and the network it evaluates stays
+    # within that of the exact one
+    rng = np.random.default_rng(4)
+    v = rng.standard_normal(10000).astype(np.float32) * 10.0 ** rng.uniform(-4, 1, 10000)
+    assert np.max(np.abs(M.split_bf16(v) - v) / np.abs(v)) <= 2.0 ** -16
+    n_in, H = 16, 64
+    npar = H * n_in + 3 * H + H * H + 1
+    w = M.to_bf16(rng.standard_normal(npar).astype(np.float32) * 0.2)
+    x = rng.standard_normal((200, n_in))
+    x /= np.linalg.norm(x, axis=1, keepdims=True)
+    p_exact = M.forward(w, x, n_in, H)[0]
+    p_split = M.forward(w, x, n_in, H, split_inputs=True)[0]
+    assert np.max(np.abs(p_split - p_exact)) <= 2.0 ** -13 * np.max(np.abs(p_exact))

@@ -1249,6 +1249,8 @@ int ctx_state_view(tg_ctx* c, const void** state, int* is_ff, int* D, int* N, in
   return TG_OK;
 }
 
+int32_t* ctx_status_word(tg_ctx* c) { return c->d_status; }
+
 int ctx_set_alpha_source(tg_ctx* c, tg_mlp* m) {
   if (m && c->vi != VI_HG)
     return fail(c, TG_ERR_STATE, "the learned indicator replaces the HG indicator: "
@@ -1974,6 +1976,26 @@ int tg_rk_stage(tg_ctx* c, int32_t stage, double t, double dt) {
   CUDA_TRY(c, cudaGetLastError());
   c->clock_valid = false;
   return enqueue_stage(c, stage, false);
+}
+
+int tg_rk_stage_part(tg_ctx* c, int32_t stage, double t, double dt, int32_t parts) {
+  if (!c || stage < 0 || stage > 4 || parts < 1 || parts > 3) return TG_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return fail(c, TG_ERR_STATE, "no state uploaded");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  if (parts & 1) {
+    clock_set_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, t, dt);
+    CUDA_TRY(c, cudaGetLastError());
+    c->clock_valid = false;
+    int rc = indicator(c, c->d_u[c->cur]);
+    if (rc) return rc;
+  }
+  if (parts & 2) {
+    int rc = launch_kernel(c, MODE_STAGE, c->d_u[c->cur], c->d_u[c->cur ^ 1], nullptr, 0.0, stage,
+                           false);
+    if (rc) return rc;
+    c->cur ^= 1;
+  }
+  return TG_OK;
 }
 
 int tg_stream(tg_ctx* c, void** stream) {

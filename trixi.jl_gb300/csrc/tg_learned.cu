@@ -18,9 +18,14 @@
 //
 // Network: NM -> H -> H -> 1 with ReLU (2D polydeg 3: 16 -> 64 -> 64 -> 1,
 // 3D: 64 -> 128 -> 128 -> 1), weights stored in BF16 for the forward pass
-// with FP32 master copies, FP32 accumulation, trained with Adam on the MSE of
-// sqrt E by the fused forward+backward kernel below.  Layers this small
-// (K = 16..128) run on the CUDA cores.  Loss: mean squared error of sqrt(E).
+// with FP32 master copies, FP32 layer inputs and accumulation.  Inference and
+// deployment run the two hidden layers on the tensor cores (tcgen05 BF16
+// MMAs, FP32 accumulation in tensor memory), each FP32 layer input fed as a
+// BF16 pair hi + lo (two MMAs into one accumulator: a 16-bit significand; a
+// single BF16 rounding would erase the first layer's small-mode signal, which
+// rides on the O(1) mean mode); the output layer and everything per element
+// run on the CUDA cores.  Training (Adam on the mean squared error of sqrt E)
+// uses the fused forward+backward kernel below on the CUDA cores.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -33,6 +38,7 @@
 
 #include "../../include/trixi_gb300.h"
 #include "tg_dg.cuh"
+#include "tg_tcgen05.cuh"
 
 namespace tg {
 void set_thread_error(const char* msg);
@@ -58,12 +64,12 @@ struct tg_mlp {
   float band = 0.01f;                // half-width of the fallback zone around sqrt(T)
   double sqrt_threshold = 0.0;       // sqrt(T) of the HG indicator
   // deployment scratch
-  float* d_feat = nullptr;           // [E][NM] features of the current state
   float* d_pred = nullptr;           // [E] predicted sqrt(E)
   float* d_hg = nullptr;             // [E] HG alpha (unsmoothed)
   int32_t* d_flag = nullptr;         // [E] fallback reason (0 none, 1 band, 2 positivity)
   int64_t ecap = 0;
   unsigned long long* d_stats = nullptr;  // [3]: elements, band fallbacks, positivity fallbacks
+  int32_t* d_status = nullptr;       // tensor-core wait timeouts of tg_mlp_predict
   std::string err;
 };
 
@@ -82,6 +88,7 @@ struct MlpLayout {
 };
 
 __device__ __forceinline__ float wld(const __nv_bfloat16* w, int k) { return __bfloat162float(w[k]); }
+
 
 // ---------------------------------------------------------------------------
 // Features of every element: normalised modes, sqrt E target, HG alpha, and
@@ -200,129 +207,268 @@ __global__ void features_kernel(const FeatParams P, const TS* __restrict__ u,
 }
 
 // ---------------------------------------------------------------------------
-// Inference: one thread per element; hidden layer 1 in shared memory, weights
-// read as warp-uniform (broadcast) loads.
+// The network on the 5th-generation tensor cores (tcgen05), for deployment
+// (features computed from the state, blending factor out) and for predictions
+// of explicit rows.  A block of 128 threads walks tiles of 128 elements, one
+// thread per element, i.e. per row of the MMA operands and per TMEM lane:
+//   layer 1  D = X W1^T: X [128 x K1] (the n^d features, zero-padded to K1, a
+//            multiple of 16), W1 [H x K1]; FP32 accumulators in TMEM;
+//   layer 2  D = relu(D + b1) W2^T, in the same TMEM columns;
+//   output   b3 + sum_j w3_j relu(D_j + b2_j) in FP32 on the CUDA cores, from
+//            the thread's own TMEM lane.
+// The weights are BF16 (exact MMA operands).  Each FP32 layer input x is fed
+// as two BF16 operands, hi = bf16(x) and lo = bf16(x - hi), multiplied by the
+// same weights into the same accumulator: the products are exact and x is
+// represented to about 2^-17, so the tensor cores evaluate the FP32 network
+// the training kernel fits (a plain BF16 rounding of the inputs, 2^-9, would
+// erase the small high-mode part of the features next to the mean mode).
+// One thread issues the MMAs (M = 128, N = H, K = 16 per instruction) and
+// commits them to an mbarrier that every thread waits on; the operands are
+// written to shared memory by all threads in the K-major layout of
+// tg_tcgen05.cuh, the weights once per block.  The layer-2 operands overlay
+// the layer-1 ones (layer 1 has completed when they are written).  The same
+// code serves both entry points, so deployed predictions and tg_mlp_predict
+// agree bit for bit.
 // ---------------------------------------------------------------------------
-template <int NM, int H, int BT>
-__global__ void __launch_bounds__(BT) mlp_infer_kernel(const __nv_bfloat16* __restrict__ w,
-                                                       const float* __restrict__ x, int64_t M,
-                                                       float* __restrict__ pred) {
-  __shared__ float s_h1[H * BT];
-  const MlpLayout L{NM, H};
-  const int tid = threadIdx.x;
-  const int64_t s = (int64_t)blockIdx.x * BT + tid;
-  const bool act = s < M;
-  float xv[NM];
-#pragma unroll
-  for (int k = 0; k < NM; ++k) xv[k] = act ? x[s * NM + k] : 0.0f;
-  for (int i = 0; i < H; ++i) {
-    float z = wld(w, L.b1() + i);
-#pragma unroll
-    for (int k = 0; k < NM; ++k) z = fmaf(wld(w, L.w1() + i * NM + k), xv[k], z);
-    s_h1[i * BT + tid] = fmaxf(z, 0.0f);
-  }
-  float out = wld(w, L.b3());
-  for (int i = 0; i < H; ++i) {
-    float z = wld(w, L.b2() + i);
-    for (int j = 0; j < H; ++j) z = fmaf(wld(w, L.w2() + i * H + j), s_h1[j * BT + tid], z);
-    out = fmaf(wld(w, L.w3() + i), fmaxf(z, 0.0f), out);
-  }
-  if (act) pred[s] = out;
-}
-
-// Predicted sqrt(E) -> blending factor, with the HG fallback near the switch
-// and for non-positive rho*p; writes alpha_raw (R) for the stage kernels.
-template <typename R>
-__global__ void learned_alpha_kernel(const float* __restrict__ pred, const float* __restrict__ hg,
-                                     int32_t* __restrict__ flag, int64_t E, float sqrt_thr,
-                                     float band, float thr, float s_par, float alpha_min,
-                                     float alpha_max, R* __restrict__ alpha_raw,
-                                     unsigned long long* __restrict__ stats) {
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= E) return;
-  int f = flag[e];
-  const float p = pred[e];
-  if (f == 0 && !(fabsf(p - sqrt_thr) >= band)) f = 1;  // also catches NaN
-  // logistic of the HG indicator (fallback) or of the predicted one, then the
-  // clipping of indicators_2d.jl:92-100 with the context's constants
-  const float ep = fmaxf(p, 0.0f);
-  float a = f != 0 ? hg[e] : 1.0f / (1.0f + expf(-s_par / thr * (ep * ep - thr)));
-  if (a < alpha_min) a = 0.0f;
-  if (a > 1.0f - alpha_min) a = 1.0f;
-  a = fminf(alpha_max, a);
-  flag[e] = f;
-  alpha_raw[e] = (R)a;
-  if (f == 1) atomicAdd(&stats[1], 1ull);
-  if (f == 2) atomicAdd(&stats[2], 1ull);
-  if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&stats[0], (unsigned long long)E);
-}
-
-// Deployment path of the 2D networks (H = 64): modes, HG fallback value,
-// network and blending factor of each element in one pass, one thread per
-// element and nothing but alpha (and the per-element report) written.  A
-// block stages the weights once in shared memory as FP32 copies of the BF16
-// values, keeps the first hidden layer in registers and walks element tiles;
-// products and sums are the FP32 operations of mlp_infer_kernel in the same
-// order, so the predictions are the same bits.
 struct AlphaParams {
   float sqrt_thr, band, thr, s_par, alpha_min, alpha_max;
 };
 
-template <int N, typename TS, typename R>
-__global__ void __launch_bounds__(128, 4) learned_alpha2d_kernel(
-    const FeatParams P, const TS* __restrict__ u, const __nv_bfloat16* __restrict__ w,
-    const AlphaParams A, R* __restrict__ alpha_raw, float* __restrict__ pred_out,
-    float* __restrict__ hg_out, int32_t* __restrict__ flag_out,
-    unsigned long long* __restrict__ stats) {
-  constexpr int NM = N * N, H = 64;
+// Status bit set when a wait for the tensor core gave up (the block stops).
+constexpr int32_t STATUS_TC_TIMEOUT = 4;
+constexpr uint32_t TC_WAIT_POLLS = 1u << 22;
+
+template <int NM, int H>
+struct TcShape {
+  static constexpr int ROWS = 128;
+  static constexpr int K1 = (NM + 15) / 16 * 16;
+  static constexpr int OW1 = 0;
+  static constexpr int OW2 = OW1 + H * K1 * 2;
+  static constexpr int OA = OW2 + H * H * 2;            // operand area
+  static constexpr int A1 = ROWS * K1 * 2, A2 = ROWS * H * 2;  // bytes of one hi or lo operand
+  static constexpr int OA1H = OA, OA1L = OA + A1;       // layer 1: hi, lo
+  static constexpr int OA2H = OA, OA2L = OA + A2;       // layer 2: hi, lo (overlay layer 1)
+  static constexpr int OVEC = OA + 2 * (A1 > A2 ? A1 : A2);  // b1[H], b2[H], w3[H], b3 (FP32)
+  static constexpr int OBAR = OVEC + (3 * H + 2) * 4;   // mbarrier (8-byte aligned)
+  static constexpr int OSLOT = OBAR + 8;                // TMEM base address
+  static constexpr int SMEM = OSLOT + 8;
+  static constexpr int TCOLS = H;                       // layer 2 reuses layer 1's columns
+  static constexpr uint32_t IDESC = tc::idesc_bf16_f32(ROWS, H);
+  static_assert(OBAR % 8 == 0, "mbarrier alignment");
+  static_assert(H == 64 || H == 128, "TMEM columns: a power of two >= 32");
+};
+
+// 8 FP32 values as BF16 hi and lo parts (v = hi + lo + O(2^-17 |v|)).
+__device__ __forceinline__ void split8_bf16(const float* v, uint4& hi, uint4& lo) {
+  uint32_t h[4], l[4];
+#pragma unroll
+  for (int j = 0; j < 8; j += 2) {
+    const __nv_bfloat162 bh = __floats2bfloat162_rn(v[j], v[j + 1]);
+    const float2 fh = __bfloat1622float2(bh);
+    const __nv_bfloat162 bl = __floats2bfloat162_rn(v[j] - fh.x, v[j + 1] - fh.y);
+    h[j / 2] = *reinterpret_cast<const uint32_t*>(&bh);
+    l[j / 2] = *reinterpret_cast<const uint32_t*>(&bl);
+  }
+  hi = make_uint4(h[0], h[1], h[2], h[3]);
+  lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// Row r of the hi and lo K-major operands with K columns from FP32 values
+// (columns beyond `n` are zero): 16-byte stores of 8 values.
+template <int K>
+__device__ __forceinline__ void store_row_split(unsigned char* hi, unsigned char* lo, int r,
+                                                const float* v, int n) {
+#pragma unroll
+  for (int c = 0; c < K; c += 8) {
+    float x[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = c + j < n ? v[c + j] : 0.0f;
+    uint4 h, l;
+    split8_bf16(x, h, l);
+    const int o = tc::kmajor_offset(r, c, K);
+    *reinterpret_cast<uint4*>(hi + o) = h;
+    *reinterpret_cast<uint4*>(lo + o) = l;
+  }
+}
+
+// SRC 0: features of the elements of the state u (deployment: blending
+// factors with the HG fallback, per-element report); SRC 1: rows of x
+// ([nrows][NM], predictions only).
+template <int D, int N, int NM, int H, int SRC, typename TS, typename R>
+__global__ void __launch_bounds__(128) mlp_tc_kernel(
+    const FeatParams P, const TS* __restrict__ u, const float* __restrict__ x, int64_t nrows,
+    const __nv_bfloat16* __restrict__ w, const AlphaParams A, R* __restrict__ alpha_raw,
+    float* __restrict__ pred_out, float* __restrict__ hg_out, int32_t* __restrict__ flag_out,
+    unsigned long long* __restrict__ stats, int32_t* __restrict__ status) {
+  using S = TcShape<NM, H>;
+  constexpr int K1 = S::K1;
+  extern __shared__ __align__(128) unsigned char tc_smem[];
+  unsigned char* sm = tc_smem;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + S::OBAR);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(sm + S::OSLOT);
+  float* s_b1 = reinterpret_cast<float*>(sm + S::OVEC);
+  float* s_b2 = s_b1 + H;
+  float* s_w3 = s_b2 + H;  // s_w3[H] = b3
   const MlpLayout L{NM, H};
-  extern __shared__ float sw[];
-  for (int k = threadIdx.x; k < L.count(); k += blockDim.x) sw[k] = __bfloat162float(w[k]);
+
+  // weights into the K-major operand layouts (W1 zero-padded to K1 columns)
+  for (int k = tid; k < H * K1; k += S::ROWS) {
+    const int i = k / K1, j = k - i * K1;
+    *reinterpret_cast<__nv_bfloat16*>(sm + S::OW1 + tc::kmajor_offset(i, j, K1)) =
+        j < NM ? w[L.w1() + i * NM + j] : __float2bfloat16(0.0f);
+  }
+  for (int k = tid; k < H * H; k += S::ROWS) {
+    const int i = k / H, j = k - i * H;
+    *reinterpret_cast<__nv_bfloat16*>(sm + S::OW2 + tc::kmajor_offset(i, j, H)) = w[L.w2() + k];
+  }
+  for (int k = tid; k < H; k += S::ROWS) {
+    s_b1[k] = __bfloat162float(w[L.b1() + k]);
+    s_b2[k] = __bfloat162float(w[L.b2() + k]);
+    s_w3[k] = __bfloat162float(w[L.w3() + k]);
+  }
+  if (tid == 0) {
+    s_w3[H] = __bfloat162float(w[L.b3()]);
+    tc::mbar_init(bar, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(slot, S::TCOLS);
+    tc::tmem_relinquish();
+  }
+  tc::fence_proxy_async_smem();
+  tc::fence_before_sync();
   __syncthreads();
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[0], (unsigned long long)P.E);
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < P.E;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    float xv[NM], energy;
-    bool positive;
-    element_modes<2, N, TS>(P, u, e, xv, energy, positive);
-    float h1[H];
+  tc::fence_after_sync();
+  const uint32_t tmem = *slot;
+  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 lanes
+  const uint32_t a1h = tc::smem_u32(sm + S::OA1H), a1l = tc::smem_u32(sm + S::OA1L);
+  const uint32_t a2h = tc::smem_u32(sm + S::OA2H), a2l = tc::smem_u32(sm + S::OA2L);
+  const uint32_t w1 = tc::smem_u32(sm + S::OW1), w2 = tc::smem_u32(sm + S::OW2);
+  if (SRC == 0 && blockIdx.x == 0 && tid == 0) atomicAdd(&stats[0], (unsigned long long)P.E);
+
+  const int64_t total = SRC == 0 ? P.E : nrows;
+  const int64_t ntiles = (total + S::ROWS - 1) / S::ROWS;
+  uint32_t phase = 0;
+  bool failed = false;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t e = tile * S::ROWS + tid;
+    const bool act = e < total;
+    float xv[NM];
+    float energy = 0.0f;
+    bool positive = true;
+    if (act) {
+      if constexpr (SRC == 0) {
+        element_modes<D, N, TS>(P, u, e, xv, energy, positive);
+      } else {
 #pragma unroll
-    for (int i = 0; i < H; ++i) {
-      float z = sw[L.b1() + i];
+        for (int k = 0; k < NM; ++k) xv[k] = x[e * NM + k];
+      }
+    } else {
 #pragma unroll
-      for (int k = 0; k < NM; ++k) z = fmaf(sw[L.w1() + i * NM + k], xv[k], z);
-      h1[i] = fmaxf(z, 0.0f);
+      for (int k = 0; k < NM; ++k) xv[k] = 0.0f;
     }
-    // layer 2, eight neurons at a time: independent FMA chains, each in the
-    // same order (j ascending) as a one-neuron loop
-    constexpr int G = 8;
-    float out = sw[L.b3()];
-#pragma unroll 1
-    for (int i = 0; i < H; i += G) {
-      float z[G];
+    store_row_split<K1>(sm + S::OA1H, sm + S::OA1L, tid, xv, NM);
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
 #pragma unroll
-      for (int r = 0; r < G; ++r) z[r] = sw[L.b2() + i + r];
-#pragma unroll
-      for (int j = 0; j < H; ++j)
-#pragma unroll
-        for (int r = 0; r < G; ++r) z[r] = fmaf(sw[L.w2() + (i + r) * H + j], h1[j], z[r]);
-#pragma unroll
-      for (int r = 0; r < G; ++r) out = fmaf(sw[L.w3() + i + r], fmaxf(z[r], 0.0f), out);
+      for (int s = 0; s < K1 / 16; ++s) {
+        const uint64_t b = tc::smem_desc(w1 + s * 256, 128, K1 * 16);
+        tc::mma_bf16(tmem, tc::smem_desc(a1h + s * 256, 128, K1 * 16), b, S::IDESC, s > 0);
+        tc::mma_bf16(tmem, tc::smem_desc(a1l + s * 256, 128, K1 * 16), b, S::IDESC, 1);
+      }
+      tc::commit(bar);
     }
-    const float hg = hg_logistic(energy, A.thr, A.s_par, 0.0f, 1.0f);
-    int f = positive ? 0 : 2;
-    if (f == 0 && !(fabsf(out - A.sqrt_thr) >= A.band)) f = 1;  // also catches NaN
-    const float ep = fmaxf(out, 0.0f);
-    float a = f != 0 ? hg : 1.0f / (1.0f + expf(-A.s_par / A.thr * (ep * ep - A.thr)));
-    if (a < A.alpha_min) a = 0.0f;
-    if (a > 1.0f - A.alpha_min) a = 1.0f;
-    a = fminf(A.alpha_max, a);
-    alpha_raw[e] = (R)a;
-    pred_out[e] = out;
-    hg_out[e] = hg;
-    flag_out[e] = f;
-    if (f == 1) atomicAdd(&stats[1], 1ull);
-    if (f == 2) atomicAdd(&stats[2], 1ull);
+    if (__syncthreads_or(!tc::mbar_wait_bounded(bar, phase, TC_WAIT_POLLS))) {
+      failed = true;
+      break;
+    }
+    phase ^= 1;
+    tc::fence_after_sync();
+    // layer 1 epilogue: bias, ReLU -> row tid of the layer-2 operands (hi, lo)
+#pragma unroll
+    for (int c0 = 0; c0 < H; c0 += 32) {
+      float v[32];
+      tc::tmem_ld32(trow + c0, v);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + s_b1[c0 + j], 0.0f);
+#pragma unroll
+      for (int g = 0; g < 32; g += 8) {
+        uint4 h, l;
+        split8_bf16(v + g, h, l);
+        const int o = tc::kmajor_offset(tid, c0 + g, H);
+        *reinterpret_cast<uint4*>(sm + S::OA2H + o) = h;
+        *reinterpret_cast<uint4*>(sm + S::OA2L + o) = l;
+      }
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+#pragma unroll
+      for (int s = 0; s < H / 16; ++s) {
+        const uint64_t b = tc::smem_desc(w2 + s * 256, 128, H * 16);
+        tc::mma_bf16(tmem, tc::smem_desc(a2h + s * 256, 128, H * 16), b, S::IDESC, s > 0);
+        tc::mma_bf16(tmem, tc::smem_desc(a2l + s * 256, 128, H * 16), b, S::IDESC, 1);
+      }
+      tc::commit(bar);
+    }
+    if (__syncthreads_or(!tc::mbar_wait_bounded(bar, phase, TC_WAIT_POLLS))) {
+      failed = true;
+      break;
+    }
+    phase ^= 1;
+    tc::fence_after_sync();
+    // output layer from this thread's TMEM lane
+    float out = s_w3[H];
+#pragma unroll
+    for (int c0 = 0; c0 < H; c0 += 32) {
+      float v[32];
+      tc::tmem_ld32(trow + c0, v);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) out = fmaf(s_w3[c0 + j], fmaxf(v[j] + s_b2[c0 + j], 0.0f), out);
+    }
+    tc::fence_before_sync();  // the next tile's MMAs are issued after a barrier
+    if constexpr (SRC == 1) {
+      if (act) pred_out[e] = out;
+    } else {
+      // blending factor: the network's, or HG's near the switch and for
+      // non-positive rho*p; then the clipping of indicators_2d.jl:92-100
+      const float hg = hg_logistic(energy, A.thr, A.s_par, 0.0f, 1.0f);
+      int f = positive ? 0 : 2;
+      if (f == 0 && !(fabsf(out - A.sqrt_thr) >= A.band)) f = 1;  // also catches NaN
+      const float ep = fmaxf(out, 0.0f);
+      float al = f != 0 ? hg : 1.0f / (1.0f + expf(-A.s_par / A.thr * (ep * ep - A.thr)));
+      if (al < A.alpha_min) al = 0.0f;
+      if (al > 1.0f - A.alpha_min) al = 1.0f;
+      al = fminf(A.alpha_max, al);
+      const unsigned nb1 = __popc(__ballot_sync(0xffffffffu, act && f == 1));
+      const unsigned nb2 = __popc(__ballot_sync(0xffffffffu, act && f == 2));
+      if (lane == 0 && nb1) atomicAdd(&stats[1], (unsigned long long)nb1);
+      if (lane == 0 && nb2) atomicAdd(&stats[2], (unsigned long long)nb2);
+      if (act) {
+        alpha_raw[e] = (R)al;
+        pred_out[e] = out;
+        hg_out[e] = hg;
+        flag_out[e] = f;
+      }
+    }
+  }
+  if (failed) {
+    // a wait gave up: report it, wait (bounded) for the MMAs in flight, then
+    // free the tensor memory as on the normal path
+    if (tid == 0) atomicOr(status, STATUS_TC_TIMEOUT);
+    tc::mbar_wait_bounded(bar, phase, TC_WAIT_POLLS);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, S::TCOLS);
   }
 }
 
@@ -521,28 +667,66 @@ static int launch_features(tg_mlp* m, tg_ctx* c, float* feat, float* target, flo
   return TG_OK;
 }
 
-static int launch_infer(tg_mlp* m, const float* x, int64_t M, float* pred, cudaStream_t s) {
-  const unsigned nb = (unsigned)((M + 127) / 128);
-  if (m->NM == 16 && m->H == 64)
-    mlp_infer_kernel<16, 64, 128><<<nb, 128, 0, s>>>(m->d_wb, x, M, pred);
-  else if (m->NM == 9 && m->H == 64)
-    mlp_infer_kernel<9, 64, 128><<<nb, 128, 0, s>>>(m->d_wb, x, M, pred);
-  else if (m->NM == 25 && m->H == 64)
-    mlp_infer_kernel<25, 64, 128><<<nb, 128, 0, s>>>(m->d_wb, x, M, pred);
-  else if (m->NM == 27 && m->H == 128)
-    mlp_infer_kernel<27, 128, 64><<<nb * 2, 64, 0, s>>>(m->d_wb, x, M, pred);
-  else if (m->NM == 64 && m->H == 128)
-    mlp_infer_kernel<64, 128, 64><<<nb * 2, 64, 0, s>>>(m->d_wb, x, M, pred);
-  else
-    return mfail(m, TG_ERR_UNSUPPORTED, "network shape not compiled");
+// One launch of the tensor-core MLP kernel: a persistent grid of at most as
+// many 128-thread blocks as fit on the GPU at once (shared memory, registers
+// and tensor memory: 512 TMEM columns per SM).
+template <int D, int N, int NM, int H, int SRC, typename TS, typename R>
+static int launch_tc(tg_mlp* m, const FeatParams& P, const TS* u, const float* x, int64_t rows,
+                     const AlphaParams& A, R* alpha_raw, float* pred, int32_t* status,
+                     cudaStream_t s) {
+  using S = TcShape<NM, H>;
+  auto kern = mlp_tc_kernel<D, N, NM, H, SRC, TS, R>;
+  static int resident[64] = {0};  // blocks per SM, per device
+  int dev = 0;
+  MCUDA(m, cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return mfail(m, TG_ERR_UNSUPPORTED, "device index");
+  if (resident[dev] == 0) {
+    MCUDA(m, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM));
+    // without a carveout preference the occupancy query assumes a small
+    // shared-memory carveout and reports one block per SM
+    MCUDA(m, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  (int)cudaSharedmemCarveoutMaxShared));
+    int occ = 0;
+    MCUDA(m, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, S::ROWS, S::SMEM));
+    resident[dev] = std::max(1, std::min(occ, 512 / S::TCOLS));
+  }
+  int sms = 0;
+  MCUDA(m, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t ntiles = (rows + S::ROWS - 1) / S::ROWS;
+  if (ntiles == 0) return TG_OK;
+  const unsigned nb = (unsigned)std::min<int64_t>(ntiles, (int64_t)sms * resident[dev]);
+  kern<<<nb, S::ROWS, S::SMEM, s>>>(P, u, x, rows, m->d_wb, A, alpha_raw, pred, m->d_hg,
+                                    m->d_flag, m->d_stats, status);
   MCUDA(m, cudaGetLastError());
   return TG_OK;
 }
 
+// Predictions for rows x [M][NM] (device) into pred [M] (device).
+static int launch_predict(tg_mlp* m, const float* x, int64_t M, float* pred, cudaStream_t s) {
+  FeatParams P{};
+  AlphaParams A{};
+#define PRED(DD, NN, NMv, Hv)                                                              \
+  if (m->D == DD && m->N == NN)                                                            \
+    return launch_tc<DD, NN, NMv, Hv, 1, float, float>(m, P, nullptr, x, M, A, nullptr, pred, \
+                                                       m->d_status, s);
+  PRED(2, 3, 9, 64)
+  PRED(2, 4, 16, 64)
+  PRED(2, 5, 25, 64)
+  PRED(3, 3, 27, 128)
+  PRED(3, 4, 64, 128)
+#undef PRED
+  return mfail(m, TG_ERR_UNSUPPORTED, "network shape not compiled");
+}
+
 namespace tg {
-// One-pass deployment of the 2D networks (learned_alpha2d_kernel).
-static int fused_alpha2d(tg_mlp* m, tg_ctx* c, void* alpha_raw, bool fp64, float alpha_min,
-                         float alpha_max) {
+int32_t* ctx_status_word(tg_ctx* c);
+
+// Called by the context before every stage when the learned indicator is on:
+// writes the blending factors (unsmoothed) into alpha_raw (R = float for mixed
+// contexts, double for FP64 ones), one tensor-core kernel per stage.
+int mlp_alpha(tg_mlp* m, tg_ctx* c, void* alpha_raw, bool fp64, float alpha_min,
+              float alpha_max) {
+  if (m->ecap == 0) return mfail(m, TG_ERR_STATE, "learned indicator not prepared for this context");
   const void* state;
   int ff, D, N;
   int64_t E;
@@ -558,6 +742,7 @@ static int fused_alpha2d(tg_mlp* m, tg_ctx* c, void* alpha_raw, bool fp64, float
   P.gamma = gamma;
   for (int k = 0; k < N * N; ++k) P.Vinv[k] = (float)vinv[k];
   AlphaParams A{};
+  // HG constants of this polydeg (indicators.jl:128-131)
   A.thr = (float)(0.5 * std::pow(10.0, -1.8 * std::pow((double)N, 0.25)));
   A.s_par = (float)std::log((1 - 0.0001) / 0.0001);
   A.sqrt_thr = (float)m->sqrt_threshold;
@@ -565,55 +750,23 @@ static int fused_alpha2d(tg_mlp* m, tg_ctx* c, void* alpha_raw, bool fp64, float
   A.alpha_min = alpha_min;
   A.alpha_max = alpha_max;
   cudaStream_t s = (cudaStream_t)stream;
-  const unsigned nb = (unsigned)std::min<int64_t>((E + 127) / 128, 152 * 8);
-  const size_t smem = sizeof(float) * MlpLayout{m->NM, m->H}.count();
-#define FUSED(NN)                                                                              \
-  if (N == NN) {                                                                               \
-    if (ff)                                                                                    \
-      learned_alpha2d_kernel<NN, float2, float><<<nb, 128, smem, s>>>(                         \
-          P, (const float2*)state, m->d_wb, A, (float*)alpha_raw, m->d_pred, m->d_hg,          \
-          m->d_flag, m->d_stats);                                                              \
-    else                                                                                       \
-      learned_alpha2d_kernel<NN, double, double><<<nb, 128, smem, s>>>(                        \
-          P, (const double*)state, m->d_wb, A, (double*)alpha_raw, m->d_pred, m->d_hg,         \
-          m->d_flag, m->d_stats);                                                              \
+  int32_t* status = ctx_status_word(c);
+#define DEPLOY(DD, NN, NMv, Hv)                                                                 \
+  if (D == DD && N == NN) {                                                                     \
+    if (ff)                                                                                     \
+      return launch_tc<DD, NN, NMv, Hv, 0, float2, float>(                                      \
+          m, P, (const float2*)state, nullptr, E, A, (float*)alpha_raw, m->d_pred, status, s);  \
+    return launch_tc<DD, NN, NMv, Hv, 0, double, double>(                                       \
+        m, P, (const double*)state, nullptr, E, A, (double*)alpha_raw, m->d_pred, status, s);   \
   }
-  FUSED(3) else FUSED(4) else FUSED(5) else return mfail(m, TG_ERR_UNSUPPORTED, "polydeg");
-#undef FUSED
+  DEPLOY(2, 3, 9, 64)
+  DEPLOY(2, 4, 16, 64)
+  DEPLOY(2, 5, 25, 64)
+  DEPLOY(3, 3, 27, 128)
+  DEPLOY(3, 4, 64, 128)
+#undef DEPLOY
   (void)fp64;
-  MCUDA(m, cudaGetLastError());
-  return TG_OK;
-}
-
-// Called by the context before every stage when the learned indicator is on:
-// writes the blending factors (unsmoothed) into alpha_raw (R = float or double).
-int mlp_alpha(tg_mlp* m, tg_ctx* c, void* alpha_raw, bool fp64, float alpha_min,
-              float alpha_max) {
-  cudaStream_t s;
-  int64_t E;
-  if (m->ecap == 0) return mfail(m, TG_ERR_STATE, "learned indicator not prepared for this context");
-  if (m->D == 2 && m->H == 64) return fused_alpha2d(m, c, alpha_raw, fp64, alpha_min, alpha_max);
-  int rc = launch_features(m, c, m->d_feat, nullptr, m->d_hg, m->d_flag, &s, &E);
-  if (rc) return rc;
-  if (E > m->ecap) return mfail(m, TG_ERR_STATE, "context larger than prepared");
-  rc = launch_infer(m, m->d_feat, E, m->d_pred, s);
-  if (rc) return rc;
-  const float thr = (float)(0.5 * std::pow(10.0, -1.8 * std::pow((double)m->N, 0.25)));
-  const float spar = (float)std::log((1 - 0.0001) / 0.0001);
-  const unsigned nb = (unsigned)((E + 255) / 256);
-  // d_hg holds the unclipped HG logistic; the alpha kernel clips both paths
-  if (fp64)
-    learned_alpha_kernel<double><<<nb, 256, 0, s>>>(m->d_pred, m->d_hg, m->d_flag, E,
-                                                    (float)m->sqrt_threshold, m->band, thr, spar,
-                                                    alpha_min, alpha_max, (double*)alpha_raw,
-                                                    m->d_stats);
-  else
-    learned_alpha_kernel<float><<<nb, 256, 0, s>>>(m->d_pred, m->d_hg, m->d_flag, E,
-                                                   (float)m->sqrt_threshold, m->band, thr, spar,
-                                                   alpha_min, alpha_max, (float*)alpha_raw,
-                                                   m->d_stats);
-  MCUDA(m, cudaGetLastError());
-  return TG_OK;
+  return mfail(m, TG_ERR_UNSUPPORTED, "learned indicator: polydeg 2..4 only");
 }
 }  // namespace tg
 
@@ -658,6 +811,7 @@ int tg_mlp_create(int32_t ndims, int32_t polydeg, int32_t hidden, uint64_t seed,
   e = e ? e : cudaMalloc(&m->d_v, pb);
   e = e ? e : cudaMalloc(&m->d_loss, 2 * sizeof(float));
   e = e ? e : cudaMalloc(&m->d_stats, 3 * sizeof(unsigned long long));
+  e = e ? e : cudaMalloc(&m->d_status, sizeof(int32_t));
   if (e != cudaSuccess) {
     delete m;
     return mfail(nullptr, TG_ERR_CUDA, cudaGetErrorString(e));
@@ -677,7 +831,7 @@ int tg_mlp_create(int32_t ndims, int32_t polydeg, int32_t hidden, uint64_t seed,
 int tg_mlp_destroy(tg_mlp* m) {
   if (!m) return TG_ERR_INVALID_ARGUMENT;
   void* ptrs[] = {m->d_w, m->d_wb, m->d_g, m->d_m, m->d_v, m->d_x, m->d_y, m->d_loss,
-                  m->d_feat, m->d_pred, m->d_hg, m->d_flag, m->d_stats};
+                  m->d_pred, m->d_hg, m->d_flag, m->d_stats, m->d_status};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete m;
@@ -852,20 +1006,25 @@ int tg_mlp_gradient(tg_mlp* m, const float* x_host, const float* y_host, int32_t
   return TG_OK;
 }
 
-// Network predictions (sqrt E) for explicit rows x_host [n][NM].
+// Network predictions (sqrt E) for explicit rows x_host [n][NM], by the same
+// tensor-core kernel as the deployment.
 int tg_mlp_predict(tg_mlp* m, const float* x_host, int64_t n, float* pred_host) {
   if (!m || !x_host || !pred_host || n < 1) return TG_ERR_INVALID_ARGUMENT;
   float *x = nullptr, *p = nullptr;
   MCUDA(m, cudaMalloc(&x, sizeof(float) * n * m->NM));
-  MCUDA(m, cudaMalloc(&p, sizeof(float) * n));
-  cudaMemcpy(x, x_host, sizeof(float) * n * m->NM, cudaMemcpyHostToDevice);
-  int rc = launch_infer(m, x, n, p, 0);
-  cudaError_t e = cudaDeviceSynchronize();
+  cudaError_t e = cudaMalloc(&p, sizeof(float) * n);
+  if (e == cudaSuccess) e = cudaMemcpy(x, x_host, sizeof(float) * n * m->NM, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(m->d_status, 0, sizeof(int32_t));
+  int rc = e == cudaSuccess ? launch_predict(m, x, n, p, 0) : TG_OK;
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  int32_t st = 0;
+  if (rc == TG_OK && e == cudaSuccess) e = cudaMemcpy(&st, m->d_status, sizeof(st), cudaMemcpyDeviceToHost);
   if (rc == TG_OK && e == cudaSuccess) e = cudaMemcpy(pred_host, p, sizeof(float) * n, cudaMemcpyDeviceToHost);
   cudaFree(x);
   cudaFree(p);
   if (rc) return rc;
   if (e != cudaSuccess) return mfail(m, TG_ERR_CUDA, cudaGetErrorString(e));
+  if (st) return mfail(m, TG_ERR_CUDA, "tensor-core MLP: a wait for the tensor core timed out");
   return TG_OK;
 }
 
@@ -893,11 +1052,9 @@ int tg_ctx_set_learned_indicator(tg_ctx* c, tg_mlp* m, float band) {
     if (rc) return rc;
     if (D != m->D || N != m->N) return mfail(m, TG_ERR_INVALID_ARGUMENT, "network/context shape mismatch");
     if (E > m->ecap) {
-      cudaFree(m->d_feat);
       cudaFree(m->d_pred);
       cudaFree(m->d_hg);
       cudaFree(m->d_flag);
-      MCUDA(m, cudaMalloc(&m->d_feat, sizeof(float) * E * m->NM));
       MCUDA(m, cudaMalloc(&m->d_pred, sizeof(float) * E));
       MCUDA(m, cudaMalloc(&m->d_hg, sizeof(float) * E));
       MCUDA(m, cudaMalloc(&m->d_flag, sizeof(int32_t) * E));

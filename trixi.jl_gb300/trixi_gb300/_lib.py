@@ -30,7 +30,7 @@ TG_BOUNDARY_PERIODIC, TG_BOUNDARY_DIRICHLET, TG_BOUNDARY_SLIP_WALL = 0, 1, 2
 # Every symbol declared in include/trixi_gb300.h.
 EXPORTS = ("tg_api_version", "tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ndofs",
            "tg_upload_state", "tg_download_state", "tg_state_device_ptr", "tg_rhs",
-           "tg_rhs_host", "tg_max_dt", "tg_rk_stage", "tg_step", "tg_set_time",
+           "tg_rhs_host", "tg_max_dt", "tg_rk_stage", "tg_rk_stage_part", "tg_step", "tg_set_time",
            "tg_integrals", "tg_alpha", "tg_status", "tg_synchronize",
            "tg_elements_per_block", "tg_stream", "tg_integrals_noalloc",
            "tg_mlp_create", "tg_mlp_destroy", "tg_mlp_nparams", "tg_mlp_get_params",
@@ -123,6 +123,7 @@ def load(path: str | None = None):
         "tg_rhs_host": ([vp, vp, vp, d], ctypes.c_int),
         "tg_max_dt": ([vp, vp, pd], ctypes.c_int),
         "tg_rk_stage": ([vp, i32, d, d], ctypes.c_int),
+        "tg_rk_stage_part": ([vp, i32, d, d, i32], ctypes.c_int),
         "tg_step": ([vp, i64, d, d, pd, P(i64)], ctypes.c_int),
         "tg_set_time": ([vp, d], ctypes.c_int),
         "tg_integrals": ([vp, pd], ctypes.c_int),

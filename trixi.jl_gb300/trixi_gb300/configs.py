@@ -190,30 +190,37 @@ def _clip_alpha(a, alpha_min, alpha_max):
     return np.minimum(alpha_max, a)
 
 
-def c4(harvest_every=10, train_steps=4000, deploy_level=9, fp64_steps=200):
-    """Learned indicator: harvest, train, deploy against HG."""
+def harvest_and_train(net, every=10, khi_level=8, khi_t_end=3.0, khi_stride=16,
+                      blast_level=7, blast_t_end=0.3, blast_stride=4, train_steps=4000,
+                      batch=4096, lr=2e-3):
+    """Training set and training of the learned indicator: (modes, sqrt E) pairs of
+    every `*_stride`-th element, harvested every `every` steps from the KHI run
+    (256^2, t = 3, CFL 1.3) and the Gaussian blast (128^2, t = 0.3, CFL 1), both
+    mixed precision with the plain HG indicator; then `train_steps` Adam steps
+    on the GPU.  Returns the statistics of both phases."""
     out = {}
-    net = ShockIndicatorMLP(2, 3, seed=3)
     t_start = time.perf_counter()
-    for name, semi, t_end, stride in (("khi_256", khi_semi(8, "mixed"), 3.0, 32),
-                                      ("blast_128", blast_semi(7, "mixed"), 0.3, 4)):
+    for name, semi, t_end, stride in (
+            (f"khi_{2 ** khi_level}", khi_semi(khi_level, "mixed"), khi_t_end, khi_stride),
+            (f"blast_{2 ** blast_level}", blast_semi(blast_level, "mixed"), blast_t_end,
+             blast_stride)):
         c = semi.device_context
         c.upload(semi.compute_coefficients(0.0))
         t, steps, k = 0.0, 0, 0
         cfl = 1.3 if name.startswith("khi") else 1.0
         while True:
-            t, n = c.step(harvest_every, cfl, t_end, t)
+            t, n = c.step(every, cfl, t_end, t)
             steps += n
             net.harvest(semi, stride=stride, phase=k % stride)
             k += 1
-            if n < harvest_every or t >= t_end:
+            if n < every or t >= t_end:
                 break
         out[f"harvest_{name}"] = dict(t=t, steps=steps, pairs_total=net.count, stride=stride)
         del semi
     out["harvest_secs"] = time.perf_counter() - t_start
     t0 = time.perf_counter()
-    first = net.train(50, batch=4096, lr=2e-3)
-    last = net.train(train_steps, batch=4096, lr=2e-3)
+    first = net.train(50, batch=batch, lr=lr)
+    last = net.train(train_steps, batch=batch, lr=lr)
     out["train"] = dict(pairs=net.count, steps=train_steps + 50, loss_first=first, loss_last=last,
                         secs=time.perf_counter() - t0)
     x, y = net.dataset()
@@ -221,7 +228,13 @@ def c4(harvest_every=10, train_steps=4000, deploy_level=9, fp64_steps=200):
     pred = net.predict(x[held])
     out["train"]["heldout_mae_sqrtE"] = float(np.mean(np.abs(pred - y[held])))
     out["train"]["heldout_mae_const"] = float(np.mean(np.abs(np.median(y[~held]) - y[held])))
-    del x, y
+    return out
+
+
+def c4(harvest_every=10, train_steps=4000, deploy_level=9, fp64_steps=200):
+    """Learned indicator: harvest, train, deploy against HG."""
+    net = ShockIndicatorMLP(2, 3, seed=3)
+    out = harvest_and_train(net, every=harvest_every, train_steps=train_steps)
 
     # deployment at 512^2: mixed + learned vs mixed + HG (same states), FP64 + HG throughput
     thr = 0.5 * 10 ** (-1.8 * 4 ** 0.25)

@@ -274,6 +274,11 @@ class DeviceContext:
     def rk_stage(self, stage, t, dt):
         self._check(self.lib.tg_rk_stage(self.h, int(stage), float(t), float(dt)))
 
+    def rk_stage_part(self, stage, t, dt, parts):
+        """One pass of rk_stage (parts 1: clock + shock indicator, 2: element
+        kernel and state advance, 3: both), for timing the passes alone."""
+        self._check(self.lib.tg_rk_stage_part(self.h, int(stage), float(t), float(dt), int(parts)))
+
     def step(self, max_steps, cfl, t_end, t):
         tt = ctypes.c_double(t)
         n = ctypes.c_int64(0)
