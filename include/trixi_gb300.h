@@ -90,8 +90,11 @@ typedef enum tg_source {
 
 /* TG_PRECISION_FP64: every operation in FP64 (the reference's Float64 run).
  * TG_PRECISION_MIXED: fluxes, volume/surface integrals and the 2N register
- * u_tmp in FP32; the solution u and its stage accumulation, the time, the
- * step size and all integrals stay FP64. */
+ * u_tmp in FP32; the solution u is stored as float-float pairs (hi, lo), about
+ * 48 significant bits with FP32's exponent range, and its stage accumulation
+ * is a float-float addition (a deviation from FP64 storage: GB300's FP64 rate
+ * made even per-node FP64 conversions the bottleneck); the time, the step
+ * size and all integrals stay FP64.  States cross the ABI in FP64. */
 typedef enum tg_precision {
   TG_PRECISION_FP64 = 0,
   TG_PRECISION_MIXED = 1
@@ -265,6 +268,24 @@ int tg_rk_stage(tg_ctx* ctx, int32_t stage, double t, double dt);
  * (its rhs! is one call); asynchronous. */
 int tg_rk_stage_part(tg_ctx* ctx, int32_t stage, double t, double dt, int32_t parts);
 
+/* Device vectors for callers that keep the ODE state themselves: the Julia
+ * shim's GB300Array, through which OrdinaryDiffEq's integrator holds u and
+ * its stage registers (du, tmp) in device memory.  No counterpart in the
+ * reference, whose state vectors are Julia Arrays.
+ *   tg_vector_create: n FP64 values (zeroed), owned by the library until
+ *     tg_vector_destroy or tg_ctx_destroy;
+ *   tg_vector_copy: n values, kind 0 host -> device, 1 device -> host,
+ *     2 device -> device (host transfers are synchronous);
+ *   tg_lincomb: out = a x + b y elementwise (y == NULL: out = a x), out may
+ *     alias x or y, asynchronous on the context stream: the broadcasts of a
+ *     2N low-storage Runge-Kutta step (OrdinaryDiffEqLowStorageRK's
+ *     CarpenterKennedy2N54: tmp = A tmp + dt du; u = u + B tmp). */
+int tg_vector_create(tg_ctx* ctx, int64_t n, double** dev);
+int tg_vector_destroy(tg_ctx* ctx, double* dev);
+int tg_vector_copy(tg_ctx* ctx, void* dst, const void* src, int64_t n, int32_t kind);
+int tg_lincomb(tg_ctx* ctx, int64_t n, double* out, double a, const double* x, double b,
+               const double* y);
+
 /* Time stepping with Trixi's SimpleIntegrator2N + StepsizeCallback(cfl)
  * semantics: dt = cfl * max_dt(u) after every step (and before the first
  * one), clamped to reach t_end exactly (limit_dt!).  Steps are CUDA-graph
@@ -384,8 +405,11 @@ int tg_stream(tg_ctx* ctx, void** stream);
  * 4,194,304 (larger meshes are rejected with TG_ERR_INVALID_ARGUMENT and a
  * message for tg_last_error(NULL, ...)).  The first call on a device resolves
  * the array's device address; make that first call before any stream
- * capture.  All calls share the array, so calls that overlap on the GPU (for
- * example on two streams at once) race. */
+ * capture.  The address is resolved again when a later call runs under a
+ * different current context (after cudaDeviceReset, or with a non-primary
+ * context); that call too belongs outside a capture.  All calls share the
+ * array, so calls that overlap on the GPU (for example on two streams at
+ * once) race. */
 int tg_integrals_noalloc(int32_t ndims, int32_t polydeg, int64_t nelements, double gamma,
                          const double* weights, const double* u_dev,
                          const double* inverse_jacobian_dev, double* out_dev, void* stream);

@@ -159,3 +159,24 @@ def test_tensor_core_network_matches_the_oracle_on_the_training_set(trained):
     p_ref, _ = MO.forward(MO.to_bf16(net.params), rows.astype(np.float64), net.n_inputs,
                           net.hidden, split_inputs=True)
     np.testing.assert_allclose(net.predict(rows), p_ref, rtol=3e-5, atol=3e-6)
+
+
+def test_training_is_reproducible_bit_for_bit():
+    # gradient partial sums are reduced in a fixed order: two networks with the
+    # same seed, trained on the same harvested rows, end with the same weights
+    nets = [ShockIndicatorMLP(2, 3, seed=9) for _ in range(2)]
+    semi, _ = build(KHI, precision="mixed")
+    ctx = semi.device_context
+    ctx.upload(semi.compute_coefficients(0.0))
+    t = 0.0
+    for _ in range(5):
+        t, _n = ctx.step(20, 1.0, 3.0, t)
+        for net in nets:
+            net.harvest(semi, stride=3, phase=1)
+    losses = [net.train(200, batch=1000, lr=2e-3) for net in nets]
+    assert losses[0] == losses[1]
+    np.testing.assert_array_equal(nets[0].params, nets[1].params)
+    g0, l0 = nets[0].gradient(*nets[0].dataset())
+    g1, l1 = nets[0].gradient(*nets[0].dataset())
+    np.testing.assert_array_equal(g0, g1)
+    assert l0 == l1

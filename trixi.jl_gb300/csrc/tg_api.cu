@@ -785,18 +785,26 @@ __global__ void adapt_state_kernel(const S* __restrict__ uo, S* __restrict__ un,
   }
 }
 
+// out = a x + b y (y == nullptr: out = a x), elementwise; out may alias x or y.
+__global__ void lincomb_kernel(int64_t n, double* out, double a, const double* x, double b,
+                               const double* y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = y ? fma(b, y[i], a * x[i]) : a * x[i];
+}
+
 // apply_smoothing! as a gather (indicators_2d.jl:104-136): alpha_e =
 // max(raw_e, 0.5 * raw_n for every element n across a face or a mortar).
-template <typename R>
+template <typename R, typename O = double>
 __global__ void smooth_alpha_kernel(const R* __restrict__ raw, const int32_t* __restrict__ nbr,
                                     int64_t E, int nfaces, int smooth, int32_t nbc,
-                                    const int32_t* __restrict__ mnbr, double* __restrict__ out) {
+                                    const int32_t* __restrict__ mnbr, O* __restrict__ out) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
   R a = raw[e];
   if (smooth)
     for (int f = 0; f < nfaces; ++f) a = smooth_over_face<R>(a, nbr[e * nfaces + f], raw, nbc, mnbr);
-  out[e] = (double)a;
+  out[e] = (O)a;
 }
 
 }  // namespace tg
@@ -820,6 +828,7 @@ struct tg_ctx {
   float2* d_uff = nullptr;           // mixed: float-float copy of a tg_rhs input
   void* d_alpha_raw = nullptr;
   double* d_alpha = nullptr;
+  float* d_alpha_sm = nullptr;        // mixed 2D HG: smoothed blending factors (padded)
   int32_t* d_nbr = nullptr;
   double* d_invj = nullptr;
   double* d_xline = nullptr;
@@ -862,6 +871,7 @@ struct tg_ctx {
   tg_mlp* learned = nullptr;      // learned shock indicator (HG contexts), or null
   const void* view_state = nullptr;  // state the learned indicator reads next
   std::vector<double> weights;
+  std::vector<double*> vectors;      // tg_vector_create allocations (freed with the context)
   std::string err;
 };
 
@@ -893,6 +903,9 @@ static int fail(tg_ctx* c, int code, const char* fmt, ...) {
   } while (0)
 
 static size_t rsize(const tg_ctx* c) { return c->fp64 ? sizeof(double) : sizeof(float); }
+// Padding (elements) of per-element FP32 arrays that bulk copies read in
+// 16-byte groups past the last element.
+constexpr int64_t kElemPad = 64;
 
 static void free_ctx(tg_ctx* c) {
   if (!c) return;
@@ -900,11 +913,12 @@ static void free_ctx(tg_ctx* c) {
   for (int p = 0; p < 2; ++p)
     if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
   void* ptrs[] = {c->d_u[0], c->d_u[1], c->d_utmp, c->d_du, c->d_uscratch, c->d_stage64,
-                  c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_nbr, c->d_invj, c->d_xline,
+                  c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_alpha_sm, c->d_nbr, c->d_invj, c->d_xline,
                   c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mmat32, c->d_mflux, c->d_scls, c->d_amr_raw, c->d_amr_alpha, c->d_amap, c->d_akind, c->d_weights, c->d_cmet, c->d_cja32, c->d_cinvj32, c->d_cxy, c->d_csc, c->d_partial, c->d_sums, c->d_clock,
                   c->d_status, c->d_speed};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (double* p : c->vectors) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -945,7 +959,10 @@ static const double* export_state(tg_ctx* c, int* rc) {
   return c->d_stage64;
 }
 
-// HG indicator (unsmoothed) of a state in the context representation.
+// Blending factors of a state in the context representation: the HG (or
+// learned) indicator, unsmoothed, into d_alpha_raw; for mixed 2D contexts also
+// apply_smoothing! into d_alpha_sm, which the persistent 2D stage kernel
+// copies with the element block (the other kernels smooth inline).
 static int indicator(tg_ctx* c, const void* u) {
   if (c->vi != VI_HG) return TG_OK;
   int rc;
@@ -954,15 +971,24 @@ static int indicator(tg_ctx* c, const void* u) {
     rc = mlp_alpha(c->learned, c, c->d_alpha_raw, c->fp64, (float)c->P.alpha_min,
                    (float)c->P.alpha_max);
     c->view_state = nullptr;
-    return rc;
+    if (rc) return rc;
+  } else {
+    if (c->fp64)
+      rc = launch_indicator(c->D, c->N, true, c->P, (const double*)u, c->d_alpha_raw, c->stream);
+    else if (c->D == 2)
+      rc = launch_indicator_mixed_2(c->N, c->MP, (const float2*)u, (float*)c->d_alpha_raw,
+                                    c->stream);
+    else
+      rc = launch_indicator_mixed_3(c->N, c->MP, (const float2*)u, (float*)c->d_alpha_raw,
+                                    c->stream);
+    if (rc != 0) return fail(c, TG_ERR_CUDA, "indicator kernel launch failed (%d)", rc);
   }
-  if (c->fp64)
-    rc = launch_indicator(c->D, c->N, true, c->P, (const double*)u, c->d_alpha_raw, c->stream);
-  else if (c->D == 2)
-    rc = launch_indicator_mixed_2(c->N, c->MP, (const float2*)u, (float*)c->d_alpha_raw, c->stream);
-  else
-    rc = launch_indicator_mixed_3(c->N, c->MP, (const float2*)u, (float*)c->d_alpha_raw, c->stream);
-  if (rc != 0) return fail(c, TG_ERR_CUDA, "indicator kernel launch failed (%d)", rc);
+  if (!c->fp64 && c->D == 2 && !c->curved) {
+    smooth_alpha_kernel<float, float><<<(unsigned)((c->E + 255) / 256), 256, 0, c->stream>>>(
+        (const float*)c->d_alpha_raw, c->d_nbr, c->E, 2 * c->D, c->P.alpha_smooth, c->P.nbc,
+        c->d_mnbr, c->d_alpha_sm);
+    CUDA_TRY(c, cudaGetLastError());
+  }
   return TG_OK;
 }
 
@@ -1062,6 +1088,7 @@ static int launch_kernel(tg_ctx* c, int mode, const void* u_in, void* u_out, dou
   } else {
     MixedArgs A{};
     A.alpha_raw = (const float*)c->d_alpha_raw;
+    A.alpha_smoothed = c->d_alpha_sm;
     A.status = c->d_status;
     A.clock = c->d_clock;
     A.mode = mode;
@@ -1594,6 +1621,8 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   if (c->vi == VI_HG) {
     ALLOC(c->d_alpha_raw, rsize(c) * c->E);
     ALLOC(c->d_alpha, sizeof(double) * c->E);
+    // read in whole 16-byte groups by the bulk copies of the 2D stage kernel
+    if (!c->fp64) ALLOC(c->d_alpha_sm, sizeof(float) * (c->E + kElemPad));
   }
   std::vector<float> invj_f, xline_f;
   std::vector<float4> sc0, scn;
@@ -1602,7 +1631,7 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     invj_f.resize(c->E);
     for (int64_t k = 0; k < c->E; ++k) invj_f[k] = (float)cfg->inverse_jacobian[k];
     xline_f.assign(xline.begin(), xline.end());
-    ALLOC(c->d_invj_f, sizeof(float) * c->E);
+    ALLOC(c->d_invj_f, sizeof(float) * (c->E + kElemPad));  // padded as d_alpha_sm
     if (!xline_f.empty()) {
       ALLOC(c->d_xline_f, sizeof(float) * xline_f.size());
       if (c->P.source == SRC_CONVERGENCE_TEST) {
@@ -1665,6 +1694,7 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   }
 #undef ALLOC
   if (!c->fp64) {
+    cudaMemset(c->d_invj_f, 0, sizeof(float) * (c->E + kElemPad));
     cudaMemcpy(c->d_invj_f, invj_f.data(), sizeof(float) * c->E, cudaMemcpyHostToDevice);
     if (!xline_f.empty()) {
       cudaMemcpy(c->d_xline_f, xline_f.data(), sizeof(float) * xline_f.size(),
@@ -1995,6 +2025,50 @@ int tg_rk_stage_part(tg_ctx* c, int32_t stage, double t, double dt, int32_t part
     if (rc) return rc;
     c->cur ^= 1;
   }
+  return TG_OK;
+}
+
+int tg_vector_create(tg_ctx* c, int64_t n, double** dev) {
+  if (!c || !dev || n < 0) return TG_ERR_INVALID_ARGUMENT;
+  *dev = nullptr;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  double* p = nullptr;
+  CUDA_TRY(c, cudaMalloc(&p, sizeof(double) * (size_t)std::max<int64_t>(n, 1)));
+  CUDA_TRY(c, cudaMemsetAsync(p, 0, sizeof(double) * (size_t)n, c->stream));
+  c->vectors.push_back(p);
+  *dev = p;
+  return TG_OK;
+}
+
+int tg_vector_destroy(tg_ctx* c, double* dev) {
+  if (!c || !dev) return TG_ERR_INVALID_ARGUMENT;
+  auto it = std::find(c->vectors.begin(), c->vectors.end(), dev);
+  if (it == c->vectors.end())
+    return fail(c, TG_ERR_INVALID_ARGUMENT, "not a vector of this context");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // no launch still uses it
+  c->vectors.erase(it);
+  CUDA_TRY(c, cudaFree(dev));
+  return TG_OK;
+}
+
+int tg_vector_copy(tg_ctx* c, void* dst, const void* src, int64_t n, int32_t kind) {
+  if (!c || !dst || !src || n < 0 || kind < 0 || kind > 2) return TG_ERR_INVALID_ARGUMENT;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  const cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice
+                           : kind == 1 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  CUDA_TRY(c, cudaMemcpyAsync(dst, src, sizeof(double) * (size_t)n, k, c->stream));
+  if (kind != 2) CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return TG_OK;
+}
+
+int tg_lincomb(tg_ctx* c, int64_t n, double* out, double a, const double* x, double b,
+               const double* y) {
+  if (!c || !out || !x || n < 0) return TG_ERR_INVALID_ARGUMENT;
+  if (n == 0) return TG_OK;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  lincomb_kernel<<<conv_blocks(n), 256, 0, c->stream>>>(n, out, a, x, b, y);
+  CUDA_TRY(c, cudaGetLastError());
   return TG_OK;
 }
 

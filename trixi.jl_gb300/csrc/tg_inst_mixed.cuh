@@ -1,6 +1,8 @@
 // Explicit instantiation of the mixed-precision element kernels (tg_mixed.cuh)
 // for one (dimension, volume integral) pair; each tg_inst_*_mixed_*.cu unit
 // defines TG_D, TG_VI and TG_SUFFIX and includes this file.
+#include <algorithm>
+
 #include "tg_mixed.cuh"
 
 namespace tg {
@@ -8,6 +10,35 @@ namespace tg {
 template <int D, int N, int VI, int VF, int SF, int EPB, bool DIRECT = false>
 static int launch_mixed_one(const MixedParams& P, const MixedArgs& A, cudaStream_t s) {
   using K = MixedKernel<D, N, VI, EPB>;
+  const int64_t nblocks = (P.nelements + EPB - 1) / EPB;
+  if (nblocks <= 0) return 0;
+  if constexpr (D == 2) {
+    // 2D: the persistent, double-buffered kernel with bulk-copy staging, one
+    // block per resident slot (it needs the pre-smoothed blending factors)
+    if (VI != VI_HG || A.alpha_smoothed) {
+      using Q = MixedPipe<D, N, VI, EPB>;
+      auto kern = mixed_element_pipe_kernel<D, N, VI, VF, SF, EPB, DIRECT>;
+      static int resident[64] = {0};
+      static int sms[64] = {0};
+      int dev = 0;
+      if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+      if (resident[dev] == 0) {
+        int occ = 0;
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)Q::SMEM) != cudaSuccess ||
+            cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, K::NT, Q::SMEM) !=
+                cudaSuccess ||
+            cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+          return -1;
+        resident[dev] = occ > 0 ? occ : 1;
+      }
+      const int64_t grid = std::min<int64_t>(nblocks, (int64_t)sms[dev] * resident[dev]);
+      kern<<<(unsigned)grid, K::NT, Q::SMEM, s>>>(P, A);
+      return cudaGetLastError() == cudaSuccess ? 0 : -1;
+    }
+  }
   auto kern = mixed_element_kernel<D, N, VI, VF, SF, EPB, DIRECT>;
   static bool configured = false;
   const size_t smem = K::smem_bytes();
@@ -17,8 +48,6 @@ static int launch_mixed_one(const MixedParams& P, const MixedArgs& A, cudaStream
       return -1;
     configured = true;
   }
-  const int64_t nblocks = (P.nelements + EPB - 1) / EPB;
-  if (nblocks <= 0) return 0;
   kern<<<(unsigned)nblocks, K::NT, smem, s>>>(P, A);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

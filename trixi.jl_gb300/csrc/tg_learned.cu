@@ -60,6 +60,9 @@ struct tg_mlp {
   float* d_y = nullptr;              // dataset targets [cap]
   int64_t cap = 0, count = 0;
   float* d_loss = nullptr;           // [2]: loss sum, sample count
+  float* d_gpart = nullptr;          // [blocks][nparams] gradient partials of one step
+  float* d_lpart = nullptr;          // [blocks] squared-error partials of one step
+  int64_t part_blocks = 0;           // capacity of the partial buffers in blocks
   int64_t adam_t = 0;
   float band = 0.01f;                // half-width of the fallback zone around sqrt(T)
   double sqrt_threshold = 0.0;       // sqrt(T) of the HG indicator
@@ -113,35 +116,60 @@ __device__ __forceinline__ float4 ldg_v4(const void* p) {
   return r;
 }
 
-// Modes of rho*p of element e (normalised to unit energy when `normalise`),
-// the HG energy indicator max(f1, f2) and positivity of rho*p at the nodes.
-template <int D, int N, typename TS>
-__device__ __forceinline__ void element_modes(const FeatParams& P, const TS* __restrict__ u,
-                                              int64_t e, float* modes, float& energy,
-                                              bool& positive) {
-  constexpr int NV = D + 2, NN = Pow<N, D>::value;
-  float a[NN], b[NN];
+// rho*p at node `node` (global node index e * n^d + q) of the state, and
+// whether it is positive.
+template <int D, typename TS>
+__device__ __forceinline__ float node_rho_p(const FeatParams& P, const TS* __restrict__ u,
+                                            int64_t node) {
+  constexpr int NV = D + 2;
+  float uu[NV];
+  if constexpr (std::is_same<TS, float2>::value && NV % 2 == 0) {
+    // float-float state: two values per 16-byte load (a node's values are
+    // contiguous and 16-byte aligned when NV is even)
+    const float4* p4 = reinterpret_cast<const float4*>(u + (size_t)node * NV);
+#pragma unroll
+    for (int v = 0; v < NV; v += 2) {
+      const float4 x = ldg_v4(p4 + v / 2);
+      uu[v] = state_value(make_float2(x.x, x.y));
+      uu[v + 1] = state_value(make_float2(x.z, x.w));
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) uu[v] = (float)state_value(u[(size_t)node * NV + v]);
+  }
+  return Euler<D, float>::density_pressure(uu, (float)P.gamma);
+}
+
+// rho*p of node k of a 2D tile staged in shared memory (4 values per node, 32
+// bytes: float-float pairs or FP64), with node_rho_p's arithmetic.
+template <typename TS>
+__device__ __forceinline__ float staged_rho_p(const FeatParams& P, const float4* stg, int k) {
+  float uu[4];
+  if constexpr (std::is_same<TS, float2>::value) {
+    const float4 x0 = stg[2 * k], x1 = stg[2 * k + 1];
+    uu[0] = state_value(make_float2(x0.x, x0.y));
+    uu[1] = state_value(make_float2(x0.z, x0.w));
+    uu[2] = state_value(make_float2(x1.x, x1.y));
+    uu[3] = state_value(make_float2(x1.z, x1.w));
+  } else {
+    const double* d = reinterpret_cast<const double*>(stg) + 4 * k;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) uu[v] = (float)state_value(d[v]);
+  }
+  return Euler<2, float>::density_pressure(uu, (float)P.gamma);
+}
+
+// Modes of rho*p (a[NN], the nodal values; overwritten) normalised to unit
+// energy, the HG energy indicator max(f1, f2) and positivity of rho*p at the
+// nodes.
+template <int D, int N>
+__device__ __forceinline__ void modes_from_rho_p(const FeatParams& P, float* a, float* modes,
+                                                 float& energy, bool& positive) {
+  constexpr int NN = Pow<N, D>::value;
+  float b[NN];
   positive = true;
 #pragma unroll
-  for (int q = 0; q < NN; ++q) {
-    float uu[NV];
-    if constexpr (std::is_same<TS, float2>::value && NV % 2 == 0) {
-      // float-float state: two values per 16-byte load (the element's values
-      // are contiguous and 16-byte aligned when NV is even)
-      const float4* p4 = reinterpret_cast<const float4*>(u + ((size_t)e * NN + q) * NV);
-#pragma unroll
-      for (int v = 0; v < NV; v += 2) {
-        const float4 x = ldg_v4(p4 + v / 2);
-        uu[v] = state_value(make_float2(x.x, x.y));
-        uu[v + 1] = state_value(make_float2(x.z, x.w));
-      }
-    } else {
-#pragma unroll
-      for (int v = 0; v < NV; ++v) uu[v] = (float)state_value(u[((size_t)e * NN + q) * NV + v]);
-    }
-    a[q] = Euler<D, float>::density_pressure(uu, (float)P.gamma);
-    positive &= a[q] > 0.0f;
-  }
+  for (int q = 0; q < NN; ++q) positive &= a[q] > 0.0f;
   // multiply_scalar_dimensionwise!: x, then y, then z
   float* in = a;
   float* out = b;
@@ -178,6 +206,18 @@ __device__ __forceinline__ void element_modes(const FeatParams& P, const TS* __r
   const float inv = tot > 0.0f ? rsqrtf(tot) : 0.0f;
 #pragma unroll
   for (int q = 0; q < NN; ++q) modes[q] = in[q] * inv;
+}
+
+// Modes of rho*p of element e (one thread per element).
+template <int D, int N, typename TS>
+__device__ __forceinline__ void element_modes(const FeatParams& P, const TS* __restrict__ u,
+                                              int64_t e, float* modes, float& energy,
+                                              bool& positive) {
+  constexpr int NN = Pow<N, D>::value;
+  float a[NN];
+#pragma unroll
+  for (int q = 0; q < NN; ++q) a[q] = node_rho_p<D, TS>(P, u, e * NN + q);
+  modes_from_rho_p<D, N>(P, a, modes, energy, positive);
 }
 
 // HG logistic of an energy indicator, clipped (indicators_2d.jl:92-100)
@@ -249,8 +289,16 @@ struct TcShape {
   static constexpr int OA1H = OA, OA1L = OA + A1;       // layer 1: hi, lo
   static constexpr int OA2H = OA, OA2L = OA + A2;       // layer 2: hi, lo (overlay layer 1)
   static constexpr int OVEC = OA + 2 * (A1 > A2 ? A1 : A2);  // b1[H], b2[H], w3[H], b3 (FP32)
-  static constexpr int OBAR = OVEC + (3 * H + 2) * 4;   // mbarrier (8-byte aligned)
-  static constexpr int OSLOT = OBAR + 8;                // TMEM base address
+  // the deployment stages rho*p of the tile's nodes ([ROWS][NM + 1] floats)
+  // in the operand area before the layer-1 operands are written
+  static_assert(ROWS * (NM + 1) * 4 <= OVEC - OA, "rho*p staging fits the operand area");
+  static constexpr int OBAR = OVEC + (3 * H + 2) * 4;   // mbarriers: MMA, staging
+  static constexpr int OSLOT = OBAR + 16;               // TMEM base address
+  // 2D deployment: the tile's state (n^d nodes x 4 values, float-float or
+  // FP64: 32 bytes per node), staged by one bulk copy per tile
+  static constexpr int STAGE_BYTES = ROWS * NM * 32;
+  static constexpr int OSTG = (OSLOT + 8 + 127) / 128 * 128;
+  static constexpr int SMEM_STAGED = OSTG + STAGE_BYTES;
   static constexpr int SMEM = OSLOT + 8;
   static constexpr int TCOLS = H;                       // layer 2 reuses layer 1's columns
   static constexpr uint32_t IDESC = tc::idesc_bf16_f32(ROWS, H);
@@ -311,6 +359,21 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
   float* s_b2 = s_b1 + H;
   float* s_w3 = s_b2 + H;  // s_w3[H] = b3
   const MlpLayout L{NM, H};
+  // 2D deployment stages each tile's state with one bulk copy (contiguous in
+  // the element order), the next tile's issued as soon as this one's rho*p
+  // has been read
+  constexpr bool STAGED = SRC == 0 && D == 2;
+  uint64_t* sbar = bar + 1;
+  float4* s_stg = reinterpret_cast<float4*>(sm + S::OSTG);
+  const int64_t total = SRC == 0 ? P.E : nrows;
+  const int64_t ntiles = (total + S::ROWS - 1) / S::ROWS;
+  auto issue_tile = [&](int64_t t) {  // one thread
+    const int64_t rows = min((int64_t)S::ROWS, total - t * S::ROWS);
+    const uint32_t bytes = (uint32_t)(rows * NM * 32);
+    tc::mbar_arrive_expect_tx(sbar, bytes);
+    tc::bulk_g2s(s_stg, reinterpret_cast<const unsigned char*>(u) + (size_t)t * S::ROWS * NM * 32,
+                 bytes, sbar);
+  };
 
   // weights into the K-major operand layouts (W1 zero-padded to K1 columns)
   for (int k = tid; k < H * K1; k += S::ROWS) {
@@ -330,7 +393,9 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
   if (tid == 0) {
     s_w3[H] = __bfloat162float(w[L.b3()]);
     tc::mbar_init(bar, 1);
+    if (STAGED) tc::mbar_init(sbar, 1);
     tc::fence_mbar_init();
+    if (STAGED && blockIdx.x < ntiles) issue_tile(blockIdx.x);
   }
   if (warp == 0) {
     tc::tmem_alloc(slot, S::TCOLS);
@@ -347,26 +412,62 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
   const uint32_t w1 = tc::smem_u32(sm + S::OW1), w2 = tc::smem_u32(sm + S::OW2);
   if (SRC == 0 && blockIdx.x == 0 && tid == 0) atomicAdd(&stats[0], (unsigned long long)P.E);
 
-  const int64_t total = SRC == 0 ? P.E : nrows;
-  const int64_t ntiles = (total + S::ROWS - 1) / S::ROWS;
-  uint32_t phase = 0;
-  bool failed = false;
+  uint32_t phase = 0, sphase = 0;
+  bool failed = false, mma_in_flight = false, staging_in_flight = STAGED && blockIdx.x < ntiles;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int64_t e = tile * S::ROWS + tid;
     const bool act = e < total;
     float xv[NM];
     float energy = 0.0f;
     bool positive = true;
-    if (act) {
-      if constexpr (SRC == 0) {
-        element_modes<D, N, TS>(P, u, e, xv, energy, positive);
+    if constexpr (SRC == 0) {
+      // rho*p of the tile's nodes, one node per thread and pass, so that a
+      // warp's loads are consecutive nodes; staged in the (free) operand area
+      float* s_rp = reinterpret_cast<float*>(sm + S::OA);
+      const int64_t n0 = tile * S::ROWS * NM;
+      const int64_t nn = (min(total, (tile + 1) * S::ROWS) - tile * S::ROWS) * NM;
+      if constexpr (STAGED) {
+        if (__syncthreads_or(!tc::mbar_wait_bounded(sbar, sphase, TC_WAIT_POLLS))) {
+          failed = true;
+          break;
+        }
+        sphase ^= 1;
+        staging_in_flight = false;
+#pragma unroll 4
+        for (int j = 0; j < NM; ++j) {
+          const int k = j * S::ROWS + tid;
+          if (k < nn) s_rp[(k / NM) * (NM + 1) + k % NM] = staged_rho_p<TS>(P, s_stg, k);
+        }
+        __syncthreads();
+        // the staging buffer is free: the next tile's state lands meanwhile
+        if (tile + gridDim.x < ntiles) {
+          if (tid == 0) {
+            tc::fence_proxy_async_smem();  // the reads above before the copy's writes
+            issue_tile(tile + gridDim.x);
+          }
+          staging_in_flight = true;
+        }
+      } else {
+#pragma unroll 4
+        for (int j = 0; j < NM; ++j) {
+          const int k = j * S::ROWS + tid;
+          if (k < nn) s_rp[(k / NM) * (NM + 1) + k % NM] = node_rho_p<D, TS>(P, u, n0 + k);
+        }
+        __syncthreads();
+      }
+      if (act) {
+        float a[NM];
+#pragma unroll
+        for (int q = 0; q < NM; ++q) a[q] = s_rp[tid * (NM + 1) + q];
+        modes_from_rho_p<D, N>(P, a, xv, energy, positive);
       } else {
 #pragma unroll
-        for (int k = 0; k < NM; ++k) xv[k] = x[e * NM + k];
+        for (int k = 0; k < NM; ++k) xv[k] = 0.0f;
       }
+      __syncthreads();  // all rows read before the operand area is written
     } else {
 #pragma unroll
-      for (int k = 0; k < NM; ++k) xv[k] = 0.0f;
+      for (int k = 0; k < NM; ++k) xv[k] = act ? x[e * NM + k] : 0.0f;
     }
     store_row_split<K1>(sm + S::OA1H, sm + S::OA1L, tid, xv, NM);
     tc::fence_proxy_async_smem();
@@ -383,7 +484,7 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
       tc::commit(bar);
     }
     if (__syncthreads_or(!tc::mbar_wait_bounded(bar, phase, TC_WAIT_POLLS))) {
-      failed = true;
+      failed = mma_in_flight = true;
       break;
     }
     phase ^= 1;
@@ -418,7 +519,7 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
       tc::commit(bar);
     }
     if (__syncthreads_or(!tc::mbar_wait_bounded(bar, phase, TC_WAIT_POLLS))) {
-      failed = true;
+      failed = mma_in_flight = true;
       break;
     }
     phase ^= 1;
@@ -459,10 +560,11 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
     }
   }
   if (failed) {
-    // a wait gave up: report it, wait (bounded) for the MMAs in flight, then
-    // free the tensor memory as on the normal path
+    // a wait gave up: report it, wait (bounded) for the MMAs or the staging
+    // copy still in flight, then free the tensor memory as on the normal path
     if (tid == 0) atomicOr(status, STATUS_TC_TIMEOUT);
-    tc::mbar_wait_bounded(bar, phase, TC_WAIT_POLLS);
+    if (mma_in_flight) tc::mbar_wait_bounded(bar, phase, TC_WAIT_POLLS);
+    if (staging_in_flight) tc::mbar_wait_bounded(sbar, sphase, TC_WAIT_POLLS);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -474,8 +576,10 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
 
 // ---------------------------------------------------------------------------
 // Training: fused forward + backward over a tile of TS samples (one thread
-// per sample), weight gradients as tile-level contractions, accumulated into
-// the global gradient with atomics.  Loss: mean squared error.
+// per sample), weight gradients as tile-level contractions written as one
+// partial sum per block and tile squared error; reduce_partials_kernel sums
+// them in block order, so training is reproducible bit for bit.  Loss: mean
+// squared error.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t hash32(uint64_t x) {
   x ^= x >> 33;
@@ -494,6 +598,7 @@ __global__ void __launch_bounds__(TS) mlp_train_kernel(const __nv_bfloat16* __re
                                                        uint64_t seed, int batch, int holdout,
                                                        float* __restrict__ grad,
                                                        float* __restrict__ loss) {
+  // grad: [gridDim.x][nparams] partial sums, loss: [gridDim.x] squared errors
   extern __shared__ float sm[];
   float* sX = sm;             // [NM][TS]
   float* sH1 = sX + NM * TS;  // [H][TS]: h1, later dz1
@@ -528,19 +633,29 @@ __global__ void __launch_bounds__(TS) mlp_train_kernel(const __nv_bfloat16* __re
     out = fmaf(wld(w, L.w3() + i), h, out);
   }
   const float r = act ? out - Y[s] : 0.0f;
-  if (act) atomicAdd(&loss[0], r * r);
   sD[tid] = act ? 2.0f * r / (float)batch : 0.0f;
   __syncthreads();
+  if (tid == 0) {
+    // squared error of the tile, summed in a fixed order (from the residuals)
+    float l = 0;
+    for (int t = 0; t < TS; ++t) {
+      const float rt = sD[t] * (0.5f * (float)batch);
+      l = fmaf(rt, rt, l);
+    }
+    loss[blockIdx.x] = l;
+  }
+  // this block's gradient partial sums: grad[blockIdx.x][k]
+  grad += (size_t)blockIdx.x * L.count();
   // output layer gradients
   for (int i = tid; i < H; i += TS) {
     float g = 0;
     for (int t = 0; t < TS; ++t) g = fmaf(sD[t], sH2[i * TS + t], g);
-    atomicAdd(&grad[L.w3() + i], g);
+    grad[L.w3() + i] = g;
   }
   if (tid == 0) {
     float g = 0;
     for (int t = 0; t < TS; ++t) g += sD[t];
-    atomicAdd(&grad[L.b3()], g);
+    grad[L.b3()] = g;
   }
   __syncthreads();
   // dz2 = dout * w3 * [h2 > 0]   (in place of h2)
@@ -553,11 +668,11 @@ __global__ void __launch_bounds__(TS) mlp_train_kernel(const __nv_bfloat16* __re
   for (int i = tid; i < H; i += TS) {
     float gb = 0;
     for (int t = 0; t < TS; ++t) gb += sH2[i * TS + t];
-    atomicAdd(&grad[L.b2() + i], gb);
+    grad[L.b2() + i] = gb;
     for (int j = 0; j < H; ++j) {
       float g = 0;
       for (int t = 0; t < TS; ++t) g = fmaf(sH2[i * TS + t], sH1[j * TS + t], g);
-      atomicAdd(&grad[L.w2() + i * H + j], g);
+      grad[L.w2() + i * H + j] = g;
     }
   }
   __syncthreads();
@@ -578,14 +693,33 @@ __global__ void __launch_bounds__(TS) mlp_train_kernel(const __nv_bfloat16* __re
   for (int i = tid; i < H; i += TS) {
     float gb = 0;
     for (int t = 0; t < TS; ++t) gb += sH1[i * TS + t];
-    atomicAdd(&grad[L.b1() + i], gb);
+    grad[L.b1() + i] = gb;
     for (int k = 0; k < NM; ++k) {
       float g = 0;
       for (int t = 0; t < TS; ++t) g = fmaf(sH1[i * TS + t], sX[k * TS + t], g);
-      atomicAdd(&grad[L.w1() + i * NM + k], g);
+      grad[L.w1() + i * NM + k] = g;
     }
   }
-  if (tid == 0 && blockIdx.x == 0) atomicAdd(&loss[1], (float)batch);
+}
+
+// Sums of the per-block partials in block order (deterministic): the
+// gradient, and the tiles' squared errors added to loss[0] (with the sample
+// count in loss[1]).
+__global__ void reduce_partials_kernel(const float* __restrict__ part, int nblk, int64_t n,
+                                       float* __restrict__ grad, const float* __restrict__ lpart,
+                                       float* __restrict__ loss, int batch) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) {
+    float g = 0;
+    for (int b = 0; b < nblk; ++b) g += part[(size_t)b * n + k];
+    grad[k] = g;
+  }
+  if (k == 0) {
+    float l = 0;
+    for (int b = 0; b < nblk; ++b) l += lpart[b];
+    loss[0] += l;
+    loss[1] += (float)batch;
+  }
 }
 
 __global__ void adam_kernel(float* __restrict__ w, __nv_bfloat16* __restrict__ wb,
@@ -676,26 +810,35 @@ static int launch_tc(tg_mlp* m, const FeatParams& P, const TS* u, const float* x
                      cudaStream_t s) {
   using S = TcShape<NM, H>;
   auto kern = mlp_tc_kernel<D, N, NM, H, SRC, TS, R>;
+  constexpr int SMEM = (SRC == 0 && D == 2) ? S::SMEM_STAGED : S::SMEM;
   static int resident[64] = {0};  // blocks per SM, per device
   int dev = 0;
   MCUDA(m, cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return mfail(m, TG_ERR_UNSUPPORTED, "device index");
   if (resident[dev] == 0) {
-    MCUDA(m, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM));
-    // without a carveout preference the occupancy query assumes a small
-    // shared-memory carveout and reports one block per SM
+    MCUDA(m, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
     MCUDA(m, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                                   (int)cudaSharedmemCarveoutMaxShared));
-    int occ = 0;
-    MCUDA(m, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, S::ROWS, S::SMEM));
-    resident[dev] = std::max(1, std::min(occ, 512 / S::TCOLS));
+    // Blocks per SM from the kernel's own resources: registers, shared memory
+    // (plus the 1 KB the driver reserves per block) and tensor memory (512
+    // columns per SM).  The runtime's occupancy query reports one block per
+    // SM for this kernel, which would leave most of the GPU idle.
+    cudaFuncAttributes fa{};
+    MCUDA(m, cudaFuncGetAttributes(&fa, kern));
+    int smem_sm = 0, regs_sm = 0;
+    MCUDA(m, cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    MCUDA(m, cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
+    const int regs = (std::max(fa.numRegs, 1) + 7) / 8 * 8;  // allocated in units of 8
+    const int by_regs = regs_sm / (regs * S::ROWS);
+    const int by_smem = smem_sm / (SMEM + 1024);
+    resident[dev] = std::max(1, std::min({by_regs, by_smem, 512 / S::TCOLS, 2048 / S::ROWS}));
   }
   int sms = 0;
   MCUDA(m, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int64_t ntiles = (rows + S::ROWS - 1) / S::ROWS;
   if (ntiles == 0) return TG_OK;
   const unsigned nb = (unsigned)std::min<int64_t>(ntiles, (int64_t)sms * resident[dev]);
-  kern<<<nb, S::ROWS, S::SMEM, s>>>(P, u, x, rows, m->d_wb, A, alpha_raw, pred, m->d_hg,
+  kern<<<nb, S::ROWS, SMEM, s>>>(P, u, x, rows, m->d_wb, A, alpha_raw, pred, m->d_hg,
                                     m->d_flag, m->d_stats, status);
   MCUDA(m, cudaGetLastError());
   return TG_OK;
@@ -770,6 +913,46 @@ int mlp_alpha(tg_mlp* m, tg_ctx* c, void* alpha_raw, bool fp64, float alpha_min,
 }
 }  // namespace tg
 
+// Partial-sum buffers for `nblk` training blocks (grown on demand).
+static int ensure_partials(tg_mlp* m, int64_t nblk) {
+  if (nblk <= m->part_blocks) return TG_OK;
+  cudaFree(m->d_gpart);
+  cudaFree(m->d_lpart);
+  m->d_gpart = m->d_lpart = nullptr;
+  m->part_blocks = 0;
+  MCUDA(m, cudaMalloc(&m->d_gpart, sizeof(float) * nblk * m->nparams));
+  MCUDA(m, cudaMalloc(&m->d_lpart, sizeof(float) * nblk));
+  m->part_blocks = nblk;
+  return TG_OK;
+}
+
+// One forward + backward pass over `batch` rows (explicit indices `idx`, or
+// drawn from the training set by `seed`): gradient into d_g, squared error and
+// sample count added to d_loss.
+static int train_pass(tg_mlp* m, const float* X, const float* Y, int64_t M, const int64_t* idx,
+                      uint64_t seed, int batch, int holdout) {
+  constexpr int TS = 64;
+  const int nb = (batch + TS - 1) / TS;
+  int rc = ensure_partials(m, nb);
+  if (rc) return rc;
+  const size_t smem = sizeof(float) * (m->NM * TS + 2 * m->H * TS + TS);
+#define TRAIN(NMv, Hv)                                                                            \
+  if (m->NM == NMv && m->H == Hv) {                                                               \
+    MCUDA(m, cudaFuncSetAttribute(mlp_train_kernel<NMv, Hv, TS>,                                  \
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));       \
+    mlp_train_kernel<NMv, Hv, TS><<<nb, TS, smem>>>(m->d_wb, X, Y, M, idx, seed, batch, holdout,  \
+                                                    m->d_gpart, m->d_lpart);                       \
+  } else
+  TRAIN(16, 64) TRAIN(9, 64) TRAIN(25, 64) TRAIN(27, 128) TRAIN(64, 128) {
+    return mfail(m, TG_ERR_UNSUPPORTED, "network shape not compiled");
+  }
+#undef TRAIN
+  reduce_partials_kernel<<<(unsigned)((m->nparams + 255) / 256), 256>>>(
+      m->d_gpart, nb, m->nparams, m->d_g, m->d_lpart, m->d_loss, batch);
+  MCUDA(m, cudaGetLastError());
+  return TG_OK;
+}
+
 extern "C" {
 
 int tg_mlp_create(int32_t ndims, int32_t polydeg, int32_t hidden, uint64_t seed, tg_mlp** out) {
@@ -831,6 +1014,7 @@ int tg_mlp_create(int32_t ndims, int32_t polydeg, int32_t hidden, uint64_t seed,
 int tg_mlp_destroy(tg_mlp* m) {
   if (!m) return TG_ERR_INVALID_ARGUMENT;
   void* ptrs[] = {m->d_w, m->d_wb, m->d_g, m->d_m, m->d_v, m->d_x, m->d_y, m->d_loss,
+                  m->d_gpart, m->d_lpart,
                   m->d_pred, m->d_hg, m->d_flag, m->d_stats, m->d_status};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -924,32 +1108,11 @@ int tg_mlp_train(tg_mlp* m, int64_t steps, int32_t batch, float lr, int32_t hold
                  uint64_t seed, float* mean_loss) {
   if (!m || steps < 0 || batch < 1) return TG_ERR_INVALID_ARGUMENT;
   if (m->count < 2) return mfail(m, TG_ERR_STATE, "no training data harvested");
-  constexpr int TS = 64;
-  const int nb = (batch + TS - 1) / TS;
   MCUDA(m, cudaMemset(m->d_loss, 0, 2 * sizeof(float)));
-  const size_t smem = sizeof(float) * (m->NM * TS + 2 * m->H * TS + TS);
   for (int64_t it = 0; it < steps; ++it) {
     const uint64_t sd = seed * 1000003ull + (uint64_t)(m->adam_t + 1);
-    if (m->NM == 16 && m->H == 64) {
-      cudaFuncSetAttribute(mlp_train_kernel<16, 64, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      mlp_train_kernel<16, 64, TS><<<nb, TS, smem>>>(m->d_wb, m->d_x, m->d_y, m->count, nullptr, sd,
-                                                     batch, holdout, m->d_g, m->d_loss);
-    } else if (m->NM == 9 && m->H == 64) {
-      mlp_train_kernel<9, 64, TS><<<nb, TS, smem>>>(m->d_wb, m->d_x, m->d_y, m->count, nullptr, sd,
-                                                    batch, holdout, m->d_g, m->d_loss);
-    } else if (m->NM == 25 && m->H == 64) {
-      cudaFuncSetAttribute(mlp_train_kernel<25, 64, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      mlp_train_kernel<25, 64, TS><<<nb, TS, smem>>>(m->d_wb, m->d_x, m->d_y, m->count, nullptr, sd,
-                                                     batch, holdout, m->d_g, m->d_loss);
-    } else if (m->NM == 27 && m->H == 128) {
-      cudaFuncSetAttribute(mlp_train_kernel<27, 128, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      mlp_train_kernel<27, 128, TS><<<nb, TS, smem>>>(m->d_wb, m->d_x, m->d_y, m->count, nullptr, sd,
-                                                      batch, holdout, m->d_g, m->d_loss);
-    } else {
-      cudaFuncSetAttribute(mlp_train_kernel<64, 128, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      mlp_train_kernel<64, 128, TS><<<nb, TS, smem>>>(m->d_wb, m->d_x, m->d_y, m->count, nullptr, sd,
-                                                      batch, holdout, m->d_g, m->d_loss);
-    }
+    int rc = train_pass(m, m->d_x, m->d_y, m->count, nullptr, sd, batch, holdout);
+    if (rc) return rc;
     m->adam_t += 1;
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.0f - std::pow(b1, (float)m->adam_t), c2 = 1.0f - std::pow(b2, (float)m->adam_t);
@@ -979,20 +1142,14 @@ int tg_mlp_gradient(tg_mlp* m, const float* x_host, const float* y_host, int32_t
   cudaMemcpy(x, x_host, sizeof(float) * n * m->NM, cudaMemcpyHostToDevice);
   cudaMemcpy(y, y_host, sizeof(float) * n, cudaMemcpyHostToDevice);
   cudaMemcpy(idx, id.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice);
-  cudaMemset(m->d_g, 0, sizeof(float) * m->nparams);
   cudaMemset(m->d_loss, 0, 2 * sizeof(float));
-  constexpr int TS = 64;
-  const int nb = (n + TS - 1) / TS;
-  const size_t smem = sizeof(float) * (m->NM * TS + 2 * m->H * TS + TS);
-#define TRAIN(NMv, Hv)                                                                          \
-  if (m->NM == NMv && m->H == Hv) {                                                             \
-    cudaFuncSetAttribute(mlp_train_kernel<NMv, Hv, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                         (int)smem);                                                            \
-    mlp_train_kernel<NMv, Hv, TS><<<nb, TS, smem>>>(m->d_wb, x, y, n, idx, 0, n, 0, m->d_g,     \
-                                                    m->d_loss);                                  \
-  } else
-  TRAIN(16, 64) TRAIN(9, 64) TRAIN(25, 64) TRAIN(27, 128) TRAIN(64, 128) {}
-#undef TRAIN
+  const int rc = train_pass(m, x, y, n, idx, 0, n, 0);
+  if (rc) {
+    cudaFree(x);
+    cudaFree(y);
+    cudaFree(idx);
+    return rc;
+  }
   cudaError_t e = cudaDeviceSynchronize();
   if (e == cudaSuccess) e = cudaMemcpy(grad_host, m->d_g, sizeof(float) * m->nparams, cudaMemcpyDeviceToHost);
   float l[2];

@@ -27,6 +27,7 @@
 #pragma once
 
 #include "tg_dg.cuh"
+#include "tg_tcgen05.cuh"
 
 namespace tg {
 
@@ -83,6 +84,7 @@ struct MixedArgs {
   double* du_out;           // MODE_RHS (FP64 du, Trixi layout)
   float* u_tmp;             // MODE_STAGE
   const float* alpha_raw;   // VI_HG
+  const float* alpha_smoothed;  // VI_HG, persistent 2D kernel: alpha_raw after apply_smoothing!
   float* alpha_out;         // VI_HG (optional)
   const Clock* clock;
   unsigned long long* speed_bits;
@@ -555,6 +557,9 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
@@ -572,19 +577,30 @@ __device__ __forceinline__ void cp_async_wait_all() {
 template <int D, int N, int EPB>
 struct NodeLayout {
   static constexpr int NN = Pow<N, D>::value;
-  static constexpr bool PADDED = (D == 3 && N == 4);
-  static constexpr int SS = PADDED ? 80 : NN;
-  static constexpr int FS = PADDED ? EPB * 80 : EPB * NN + 1;  // field stride
+  // polydeg 3: swizzled layouts whose x-lines are 4 contiguous, 16-byte
+  // aligned nodes (read and written as float4)
+  static constexpr bool PADDED = N == 4;
+  static constexpr int SS = D == 3 && PADDED ? 80 : NN;
+  static constexpr int FS = PADDED ? EPB * SS : EPB * NN + 1;  // field stride
   static __host__ __device__ __forceinline__ int pos(int slot, int n) {
-    // 3D, N = 4: an XOR swizzle of bits 2-3 of the node index by bits 4-5
-    // (a permutation of each element's 64 nodes) with an 80-float element
-    // stride.  A warp holds 16 lines of one direction of two elements: with it
-    // the node-field reads and partial-sum writes of x-lines (float4), y- and
-    // z-lines (scalar) and the node phase (32 consecutive nodes) each take one
-    // shared-memory wavefront, and the 4 nodes of an x-line stay contiguous
-    // and 16-byte aligned.
-    return PADDED ? slot * SS + (n ^ (((n >> 4) & 1) << 2) ^ (((n >> 5) & 1) << 3))
-                  : slot * SS + n;
+    if constexpr (D == 3 && PADDED) {
+      // 3D: an XOR swizzle of bits 2-3 of the node index by bits 4-5 (a
+      // permutation of each element's 64 nodes) with an 80-float element
+      // stride.  A warp holds 16 lines of one direction of two elements: with
+      // it the node-field reads and partial-sum writes of x-lines (float4), y-
+      // and z-lines (scalar) and the node phase (32 consecutive nodes) each
+      // take one shared-memory wavefront.
+      return slot * SS + (n ^ (((n >> 4) & 1) << 2) ^ (((n >> 5) & 1) << 3));
+    } else if constexpr (PADDED) {
+      // 2D: the y index (bits 2-3 of the node) XORed with bits 1-2 of the
+      // element slot.  A warp holds the 4 lines of one direction of 8
+      // elements: x-lines read 8 x 4 distinct 16-byte groups, y-lines (node
+      // line + 4 a) land in 32 distinct banks, the node phase permutes within
+      // each element.
+      return slot * SS + (n ^ (((slot >> 1) & 3) << 2));
+    } else {
+      return slot * SS + n;
+    }
   }
 };
 
@@ -596,7 +612,9 @@ struct MixedKernel {
   static constexpr int L = D * NF;           // lines per element
   static constexpr int NT = EPB * L;         // threads per block
   static constexpr int SP = NodeLayout<D, N, EPB>::FS;  // field stride of node arrays
-  static constexpr int NFLD = NV + 1;        // dw[NV], dq
+  // node fields: dw[NV], dq and, for shock capturing (whose subcell and
+  // surface Lax-Friedrichs fluxes need them at every node), du[NV]
+  static constexpr int NFLD = NV + 1 + (VI == VI_HG ? NV : 0);
   static constexpr int CHUNK = EPB * NN * NV;
   static constexpr int FACE = EPB * 2 * D * NF * NV;  // neighbour traces (float2)
   static constexpr int REFW = (sizeof(RefState<D>) + 3) / 4;
@@ -609,7 +627,8 @@ struct MixedKernel {
            + sizeof(float) * (NFLD * SP + D * NV * SP               // node fields, partial du
                               + EPB * REFW + EPB * 8 + 8            // references, per element
                               + EPB * D                             // speed maxima
-                              + N * N + N + 4);                     // matrix, inverse weights
+                              + N * N + N + 4)                      // matrix, inverse weights
+           + 16;                                                    // staging mbarrier
   }
 };
 
@@ -647,7 +666,8 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
                                            const float2* s_u, const float2* s_fu,
                                            const float* s_nd, float* s_part, const float* s_mat,
                                            const float* s_iw, float alpha, int slot, int line,
-                                           int dd, int64_t e, int64_t e0, int nel) {
+                                           int dd, int64_t e, int64_t e0, int nel,
+                                           const int32_t* nbr_row) {
   using K = MixedKernel<D, N, VI, EPB>;
   using Lay = NodeLayout<D, N, EPB>;
   using Dv = Dev<D>;
@@ -656,12 +676,16 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
   const int S = axis_stride<N>(dd);
   const int lb = line_base<N>(line, dd);
   const float vro = Dv::pick(R.v, dd);
-  constexpr bool NEED_DU = VI == VI_HG || VF < 0 || VF == FLUX_LLF || VF == FLUX_LLF_NAIVE;
+  // conservative deviations at every node: for the Lax-Friedrichs jumps of the
+  // subcell fluxes and of a Lax-Friedrichs volume flux (the weak form's volume
+  // term is the physical flux: its face nodes get them below)
+  constexpr bool NEED_DU =
+      VI == VI_HG || (VI != VI_WEAK && (VF < 0 || VF == FLUX_LLF || VF == FLUX_LLF_NAIVE));
   // node a of the line sits at field position pos(slot, lb + a S)
   const bool vec4 = Lay::PADDED && dd == 0;  // x-line: 4 contiguous, aligned nodes
   Node<D> nd[N];
   {
-    constexpr int NLOAD = NV + 1;
+    constexpr int NLOAD = K::NFLD;  // dw, dq (and du for shock capturing)
 #pragma unroll
     for (int f = 0; f < NLOAD; ++f) {
       float x[N];
@@ -684,16 +708,20 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
       for (int a = 0; a < N; ++a) {
         if (f < NV)
           nd[a].dw[f] = x[a];
-        else
+        else if (f == NV)
           nd[a].dq = x[a];
+        else
+          nd[a].du[f - NV - 1] = x[a];
       }
     }
 #pragma unroll
     for (int a = 0; a < N; ++a) {
       Dv::complete(R, nd[a]);
       Dv::orient(nd[a], dd);
-      // conservative deviations (jumps of Lax-Friedrichs fluxes) from the staged state
-      if (NEED_DU) Dv::node_du(s_u + ((size_t)slot * NN + lb + a * S) * NV, R, nd[a].du);
+      // conservative deviations (jumps of Lax-Friedrichs fluxes) from the
+      // staged state where the node phase did not store them
+      if (NEED_DU && VI != VI_HG)
+        Dv::node_du(s_u + ((size_t)slot * NN + lb + a * S) * NV, R, nd[a].du);
     }
   }
   float acc[N][NV];
@@ -756,7 +784,7 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
 #pragma unroll
   for (int side = 0; side < 2; ++side) {
     const int dir = 2 * dd + side;
-    const int64_t nb = P.nbr[e * 2 * D + dir];
+    const int64_t nb = nbr_row[dir];
     const int own_node = lb + (side ? (N - 1) * S : 0);
     Node<D>& own = side ? nd[N - 1] : nd[0];
     if (!NEED_DU) Dv::node_du(s_u + ((size_t)slot * NN + own_node) * NV, R, own.du);
@@ -815,133 +843,86 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
   }
 }
 
-// The work of one block: EPB elements (block index blk) of one mesh.  It is
-// the body of mixed_element_kernel and of the ensemble kernel, which runs it
-// on work items of many meshes (tg_ensemble.cu).  Every thread of the block
-// calls it with the same arguments, blockDim.x == NT, and smem_raw holds
-// MixedKernel::smem_bytes() bytes.
-template <int D, int N, int VI, int VF, int SF, int EPB, bool DIRECT = false>
-__device__ __forceinline__ void mixed_element_block(const MixedParams& P, const MixedArgs& A,
-                                                    int64_t blk, unsigned char* smem_raw) {
+// Status bit of a stage kernel block whose (bounded) wait for its staged
+// inputs gave up; the block stops.
+constexpr int32_t STATUS_STAGING_TIMEOUT = 8;
+constexpr uint32_t STAGING_WAIT_POLLS = 1u << 22;
+
+// ---------------------------------------------------------------------------
+// Phases of one block's work (EPB elements of one mesh).  Every thread of the
+// block runs each phase; blockDim.x == MixedKernel::NT.
+// ---------------------------------------------------------------------------
+
+// Per element: blending factor (VI_HG: `alpha_pre` when a pre-pass smoothed
+// it, else alpha_raw smoothed here), the reference state (mean `hi` of two
+// opposite corner nodes, read from `chunk`, the block's state in global or
+// shared memory) and the element part of the source phase.
+template <int D, int N, int VI, int EPB>
+__device__ __forceinline__ void mixed_setup_elements(const MixedParams& P, const MixedArgs& A,
+                                                     int64_t e0, int nel, const float2* chunk,
+                                                     const float* alpha_pre, RefState<D>* s_ref,
+                                                     float* s_elem) {
   using K = MixedKernel<D, N, VI, EPB>;
-  using Lay = NodeLayout<D, N, EPB>;
   using Dv = Dev<D>;
-  constexpr int NV = K::NV, NN = K::NN, NF = K::NF, NT = K::NT, SP = K::SP;
-  constexpr int CHUNK = K::CHUNK, NFLD = K::NFLD, FACE = K::FACE;
-  constexpr int PP = D + 1;
-
-  float2* s_u = reinterpret_cast<float2*>(smem_raw);
-  float2* s_fu = s_u + CHUNK;                               // neighbour traces
-  float* s_nd = reinterpret_cast<float*>(s_fu + FACE + K::PADF);
-  float* s_part = s_nd + NFLD * SP;
-  RefState<D>* s_ref = reinterpret_cast<RefState<D>*>(s_part + D * NV * SP);
-  // [EPB][8]: alpha, then sin/cos (hi, hi, lo, lo) of pi (x_first - t)
-  float* s_elem = reinterpret_cast<float*>(s_ref + EPB);
-  // b dt, a, (unused: 2..5), b dt lo, a lo
-  float* s_scal = s_elem + EPB * 8;
-  unsigned int* s_smax = reinterpret_cast<unsigned int*>(s_scal + 8);
-  float* s_mat = reinterpret_cast<float*>(s_smax + EPB * D);
-  float* s_iw = s_mat + N * N;
-
+  constexpr int NV = K::NV, NN = K::NN;
   const int tid = threadIdx.x;
-  const int64_t e0 = blk * EPB;
-  const int nel = (int)min((int64_t)EPB, P.nelements - e0);
-  const size_t gofs = (size_t)e0 * NN * NV;
-  const int nval = nel * NN * NV;
-  const float gamma = P.gamma;
-
-  if (A.mode == MODE_STAGE && A.clock->skip) {
-    for (int k = tid; k < nval; k += NT) A.u_out[gofs + k] = A.u_in[gofs + k];
-    return;
-  }
-
-  // ---- asynchronous staging of the block's state (16-byte copies where the
-  //      chunk is 16-byte aligned) and of the face traces of neighbours in
-  //      other blocks -------------------------------------------------------------
-  if ((gofs & 1) == 0) {
-    const float4* src = reinterpret_cast<const float4*>(A.u_in + gofs);
-    float4* dst = reinterpret_cast<float4*>(s_u);
-    for (int k = tid; k < nval / 2; k += NT) cp_async16(dst + k, src + k);
-    if ((nval & 1) && tid == 0) cp_async8(s_u + nval - 1, A.u_in + gofs + nval - 1);
-  } else {
-    for (int k = tid; k < nval; k += NT) cp_async8(s_u + k, A.u_in + gofs + k);
-  }
-  for (int k = tid; k < nel * 2 * D * NF; k += NT) {
-    const int sl = k / (2 * D * NF);
-    const int rem = k - sl * (2 * D * NF);
-    const int dir = rem / NF;
-    const int fn = rem - dir * NF;
-    const int64_t nb = P.nbr[(e0 + sl) * 2 * D + dir];
-    if (nb >= e0 && nb < e0 + nel) continue;  // in this block
-    const int dd = dir >> 1;
-    const int nnode = line_base<N>(fn, dd) + ((dir & 1) ? 0 : (N - 1) * axis_stride<N>(dd));
-    const float2* g = nb >= 0 ? A.u_in + ((size_t)nb * NN + nnode) * NV
-                              : P.ghost + ((size_t)(-1 - nb) * NF + fn) * NV;  // boundary face
-#pragma unroll
-    for (int v = 0; v < NV; ++v) cp_async8(s_fu + k * NV + v, g + v);
-  }
-  for (int k = tid; k < N * N; k += NT) s_mat[k] = VI == VI_WEAK ? P.Dhat[k] : P.Dsplit[k];
-  if (tid < N) s_iw[tid] = P.inv_weights[tid];
-  if (tid < EPB * D) s_smax[tid] = 0u;
-  if (tid == 0) {
-    // b dt and a as float-float pairs: rounded once they would perturb the
-    // 2N weights by the same amount every step (a drift of the time axis)
-    const double bdt = A.mode == MODE_RHS ? 0.0 : A.b * A.clock->dt;
-    const float bh = (float)bdt, ah = (float)A.a;
-    s_scal[0] = bh;
-    s_scal[6] = (float)(bdt - (double)bh);
-    s_scal[1] = ah;
-    s_scal[7] = (float)(A.a - (double)ah);
-  }
-  // ---- per element, while the copies are in flight: blending factor,
-  //      reference state (from global loads of two corner nodes) and the
-  //      element part of the source phase ------------------------------------------
-  if (tid < nel) {
-    const int64_t e = e0 + tid;
-    if (VI == VI_HG) {
-      float a = A.alpha_raw[e];
+  if (tid >= nel) return;
+  const int64_t e = e0 + tid;
+  if (VI == VI_HG) {
+    float a;
+    if (alpha_pre) {
+      a = alpha_pre[tid];
+    } else {
+      a = A.alpha_raw[e];
       if (P.alpha_smooth) {
 #pragma unroll
         for (int dir = 0; dir < 2 * D; ++dir)
           a = smooth_over_face<float>(a, P.nbr[e * 2 * D + dir], A.alpha_raw, P.nbc, P.mnbr);
       }
-      s_elem[tid * 8 + 0] = a;
-      if (A.alpha_out) A.alpha_out[e] = a;
     }
-    // reference = mean of two opposite corner nodes: the element centre for a
-    // linear state, which makes the deviations (and their FP32 rounding) about
-    // three times smaller in rms than those from a corner
-    const float2* ue = A.u_in + (size_t)e * NN * NV;
-    float hi[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) hi[v] = 0.5f * (ue[v].x + ue[(NN - 1) * NV + v].x);
-    Dv::make_ref(hi, P.eos, s_ref[tid]);
-    if (P.source == SRC_CONVERGENCE_TEST) {
-      // sin/cos of pi (x_first - t) in float-float by the angle-difference
-      // formula: sin(a - b) = sa cb - ca sb, cos(a - b) = ca cb + sa sb
-      float st, ct, stl, ctl;
-      if (A.mode == MODE_RHS) {
-        st = A.sin_t, ct = A.cos_t, stl = A.sin_tl, ctl = A.cos_tl;
-      } else {
-        st = A.clock->sin_t[A.stage], ct = A.clock->cos_t[A.stage];
-        stl = A.clock->sin_tl[A.stage], ctl = A.clock->cos_tl[A.stage];
-      }
-      const float4 a = P.sc0[e];
-      const float2 sn = ff_dot2(a.x, a.z, ct, ctl, -a.y, -a.w, st, stl);
-      const float2 cs = ff_dot2(a.y, a.w, ct, ctl, a.x, a.z, st, stl);
-      float* el = s_elem + tid * 8;
-      el[1] = sn.x;
-      el[2] = cs.x;
-      el[3] = sn.y;
-      el[4] = cs.y;
-      el[5] = (float)P.scls[e];
-    }
+    s_elem[tid * 8 + 0] = a;
+    if (A.alpha_out) A.alpha_out[e] = a;
   }
-  cp_async_wait_all();
-  __syncthreads();
+  // reference = mean of two opposite corner nodes: the element centre for a
+  // linear state, which makes the deviations (and their FP32 rounding) about
+  // three times smaller in rms than those from a corner
+  const float2* ue = chunk + (size_t)tid * NN * NV;
+  float hi[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) hi[v] = 0.5f * (ue[v].x + ue[(NN - 1) * NV + v].x);
+  Dv::make_ref(hi, P.eos, s_ref[tid]);
+  if (P.source == SRC_CONVERGENCE_TEST) {
+    // sin/cos of pi (x_first - t) in float-float by the angle-difference
+    // formula: sin(a - b) = sa cb - ca sb, cos(a - b) = ca cb + sa sb
+    float st, ct, stl, ctl;
+    if (A.mode == MODE_RHS) {
+      st = A.sin_t, ct = A.cos_t, stl = A.sin_tl, ctl = A.cos_tl;
+    } else {
+      st = A.clock->sin_t[A.stage], ct = A.clock->cos_t[A.stage];
+      stl = A.clock->sin_tl[A.stage], ctl = A.clock->cos_tl[A.stage];
+    }
+    const float4 a = P.sc0[e];
+    const float2 sn = ff_dot2(a.x, a.z, ct, ctl, -a.y, -a.w, st, stl);
+    const float2 cs = ff_dot2(a.y, a.w, ct, ctl, a.x, a.z, st, stl);
+    float* el = s_elem + tid * 8;
+    el[1] = sn.x;
+    el[2] = cs.x;
+    el[3] = sn.y;
+    el[4] = cs.y;
+    el[5] = (float)P.scls[e];
+  }
+}
 
-  // ---- node deviations -----------------------------------------------------------
-  for (int n = tid; n < nel * NN; n += NT) {
+// Node deviations from the element's reference state -> s_nd (padded SoA).
+template <int D, int N, int VI, int EPB>
+__device__ __forceinline__ void mixed_node_deviations(const MixedParams& P, const float2* s_u,
+                                                      const RefState<D>* s_ref, float* s_nd,
+                                                      int nel) {
+  using K = MixedKernel<D, N, VI, EPB>;
+  using Lay = NodeLayout<D, N, EPB>;
+  using Dv = Dev<D>;
+  constexpr int NV = K::NV, NN = K::NN, NT = K::NT, SP = K::SP;
+  for (int n = threadIdx.x; n < nel * NN; n += NT) {
     const int sl = n / NN;
     float hi[NV], lo[NV];
 #pragma unroll
@@ -956,36 +937,58 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
 #pragma unroll
     for (int v = 0; v < NV; ++v) s_nd[v * SP + ps] = nd.dw[v];
     s_nd[NV * SP + ps] = nd.dq;
+    if (VI == VI_HG) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) s_nd[(NV + 1 + v) * SP + ps] = nd.du[v];
+    }
   }
-  __syncthreads();
+}
 
-  // ---- lines: volume + surface contributions -----------------------------------
-  {
-    const int dd = tid / (EPB * NF);
-    const int r = tid - dd * (EPB * NF);
-    const int sl = r / NF;
-    const int line = r - sl * NF;
-    if (sl < nel)
-      mixed_line<D, N, VI, VF, SF, EPB, DIRECT>(P, s_ref[sl], s_u, s_fu, s_nd, s_part, s_mat, s_iw,
-                                        VI == VI_HG ? s_elem[sl * 8] : 0.0f, sl, line, dd,
-                                        e0 + sl, e0, nel);
-  }
-  // 2N register of this thread's node-phase nodes (zero at the first stage),
-  // loaded before the barrier so that its latency overlaps the wait
-  constexpr int NPT = (EPB * NN + NT - 1) / NT;  // nodes per thread in the node phase
+// Lines: volume + surface contributions of this thread's line -> s_part.
+// nbr_rows: the face-neighbour rows of the block's elements ([nel][2D]).
+template <int D, int N, int VI, int VF, int SF, int EPB, bool DIRECT>
+__device__ __forceinline__ void mixed_lines(const MixedParams& P, const RefState<D>* s_ref,
+                                            const float2* s_u, const float2* s_fu,
+                                            const float* s_nd, float* s_part, const float* s_mat,
+                                            const float* s_iw, const float* s_elem,
+                                            const int32_t* nbr_rows, int64_t e0, int nel) {
+  using K = MixedKernel<D, N, VI, EPB>;
+  constexpr int NF = K::NF;
+  const int tid = threadIdx.x;
+  const int dd = tid / (EPB * NF);
+  const int r = tid - dd * (EPB * NF);
+  const int sl = r / NF;
+  const int line = r - sl * NF;
+  if (sl < nel)
+    mixed_line<D, N, VI, VF, SF, EPB, DIRECT>(P, s_ref[sl], s_u, s_fu, s_nd, s_part, s_mat, s_iw,
+                                              VI == VI_HG ? s_elem[sl * 8] : 0.0f, sl, line, dd,
+                                              e0 + sl, e0, nel, nbr_rows + sl * 2 * D);
+}
+
+// Nodes: sum of directions, Jacobian, sources, then either du (MODE_RHS) or
+// the 2N update written straight to HBM and the CFL wave-speed reduction of
+// the new state.  ut_old[k] holds the 2N register of this thread's k-th node
+// (zero at the first stage); inv_jac the inverse Jacobians of the block's
+// elements (global or shared memory).
+template <int D, int N, int VI, int EPB>
+__device__ __forceinline__ void mixed_node_update(const MixedParams& P, const MixedArgs& A,
+                                                  int64_t e0, int nel, const float2* s_u,
+                                                  const float* s_part, const float* s_elem,
+                                                  const float* s_scal, unsigned int* s_smax,
+                                                  const float* inv_jac,
+                                                  const float (&ut_pre)[(EPB * Pow<N, D>::value +
+                                                                         MixedKernel<D, N, VI, EPB>::NT - 1) /
+                                                                        MixedKernel<D, N, VI, EPB>::NT]
+                                                                       [D + 2]) {
+  using K = MixedKernel<D, N, VI, EPB>;
+  using Lay = NodeLayout<D, N, EPB>;
+  constexpr int NV = K::NV, NN = K::NN, NT = K::NT, SP = K::SP;
+  constexpr int PP = D + 1;
+  constexpr int NPT = (EPB * NN + NT - 1) / NT;
+  const int tid = threadIdx.x;
+  const size_t gofs = (size_t)e0 * NN * NV;
+  const float gamma = P.gamma;
   const bool stage = A.mode == MODE_STAGE;
-  float ut_pre[NPT][NV];
-#pragma unroll
-  for (int k = 0; k < NPT; ++k) {
-    const int n = tid + k * NT;
-    const bool ld = stage && !A.zero_tmp && n < nel * NN;
-#pragma unroll
-    for (int v = 0; v < NV; ++v) ut_pre[k][v] = ld ? A.u_tmp[gofs + (size_t)n * NV + v] : 0.0f;
-  }
-  __syncthreads();
-
-  // ---- nodes: sum of directions, Jacobian, sources, 2N update, written
-  //      straight to HBM ---------------------------------------------------------------
   const float bdt = s_scal[0], bdt_lo = s_scal[6];
   const float a_s = s_scal[1], a_lo = s_scal[7];
   bool bad = false;
@@ -995,10 +998,9 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
     if (n >= nel * NN) continue;
     const int sl = n / NN;
     const int node = n - sl * NN;
-    const int64_t e = e0 + sl;
     const size_t g = gofs + (size_t)n * NV;
     const float* ut_old = ut_pre[k];
-    const float jfac = -P.inv_jac[e];
+    const float jfac = -inv_jac[sl];
     const int ps = Lay::pos(sl, node);
     float du[NV];
 #pragma unroll
@@ -1055,9 +1057,141 @@ __device__ __forceinline__ void mixed_element_block(const MixedParams& P, const 
       float sum = 0;
 #pragma unroll
       for (int d = 0; d < D; ++d) sum += __uint_as_float(s_smax[tid * D + d]);
-      const float sp = P.inv_jac[e0 + tid] * sum;
+      const float sp = inv_jac[tid] * sum;
       if (sp == sp) atomicMax(A.speed_bits, (unsigned long long)__double_as_longlong((double)sp));
     }
+  }
+}
+
+// Per-kernel constants of a block: derivative matrix, inverse weights, the
+// 2N coefficients (b dt and a as float-float pairs: rounded once they would
+// perturb the 2N weights by the same amount every step, a drift of the time
+// axis) and the cleared speed maxima.
+template <int D, int N, int VI>
+__device__ __forceinline__ void mixed_block_constants(const MixedParams& P, const MixedArgs& A,
+                                                      int nthreads, float* s_mat, float* s_iw,
+                                                      float* s_scal) {
+  const int tid = threadIdx.x;
+  for (int k = tid; k < N * N; k += nthreads) s_mat[k] = VI == VI_WEAK ? P.Dhat[k] : P.Dsplit[k];
+  if (tid < N) s_iw[tid] = P.inv_weights[tid];
+  if (tid == 0) {
+    const double bdt = A.mode == MODE_RHS ? 0.0 : A.b * A.clock->dt;
+    const float bh = (float)bdt, ah = (float)A.a;
+    s_scal[0] = bh;
+    s_scal[6] = (float)(bdt - (double)bh);
+    s_scal[1] = ah;
+    s_scal[7] = (float)(A.a - (double)ah);
+  }
+}
+
+// The work of one block: EPB elements (block index blk) of one mesh.  It is
+// the body of mixed_element_kernel and of the ensemble kernel, which runs it
+// on work items of many meshes (tg_ensemble.cu).  Every thread of the block
+// calls it with the same arguments, blockDim.x == NT, and smem_raw holds
+// MixedKernel::smem_bytes() bytes.  All global reads of a block are issued up
+// front: the state chunk as one bulk (TMA) copy completed on an mbarrier, the
+// neighbour traces of faces between blocks as cp.async copies; each element's
+// reference state is built from direct loads of its two corner nodes while
+// the copies are in flight.
+template <int D, int N, int VI, int VF, int SF, int EPB, bool DIRECT = false>
+__device__ __forceinline__ void mixed_element_block(const MixedParams& P, const MixedArgs& A,
+                                                    int64_t blk, unsigned char* smem_raw) {
+  using K = MixedKernel<D, N, VI, EPB>;
+  constexpr int NV = K::NV, NN = K::NN, NF = K::NF, NT = K::NT, SP = K::SP;
+  constexpr int CHUNK = K::CHUNK, NFLD = K::NFLD, FACE = K::FACE;
+
+  float2* s_u = reinterpret_cast<float2*>(smem_raw);
+  float2* s_fu = s_u + CHUNK;                               // neighbour traces
+  float* s_nd = reinterpret_cast<float*>(s_fu + FACE + K::PADF);
+  float* s_part = s_nd + NFLD * SP;
+  RefState<D>* s_ref = reinterpret_cast<RefState<D>*>(s_part + D * NV * SP);
+  // [EPB][8]: alpha, then sin/cos (hi, hi, lo, lo) of pi (x_first - t)
+  float* s_elem = reinterpret_cast<float*>(s_ref + EPB);
+  // b dt, a, (unused: 2..5), b dt lo, a lo
+  float* s_scal = s_elem + EPB * 8;
+  unsigned int* s_smax = reinterpret_cast<unsigned int*>(s_scal + 8);
+  float* s_mat = reinterpret_cast<float*>(s_smax + EPB * D);
+  float* s_iw = s_mat + N * N;
+  uint64_t* s_bar = reinterpret_cast<uint64_t*>(
+      (reinterpret_cast<uintptr_t>(s_iw + N + 4) + 7) & ~static_cast<uintptr_t>(7));
+
+  const int tid = threadIdx.x;
+  const int64_t e0 = blk * EPB;
+  const int nel = (int)min((int64_t)EPB, P.nelements - e0);
+  const size_t gofs = (size_t)e0 * NN * NV;
+  const int nval = nel * NN * NV;
+
+  if (A.mode == MODE_STAGE && A.clock->skip) {
+    for (int k = tid; k < nval; k += NT) A.u_out[gofs + k] = A.u_in[gofs + k];
+    return;
+  }
+
+  // ---- asynchronous staging of the block's state (one bulk copy when the
+  //      chunk starts and ends on 16-byte boundaries, else 8-byte cp.async)
+  //      and of the face traces of neighbours in other blocks ---------------------
+  const bool bulk = (gofs & 1) == 0 && (nval & 1) == 0;
+  if (bulk && tid == 0) {
+    tc::mbar_init(s_bar, 1);
+    tc::fence_mbar_init();
+    tc::mbar_arrive_expect_tx(s_bar, (uint32_t)(sizeof(float2) * nval));
+    tc::bulk_g2s(s_u, A.u_in + gofs, (uint32_t)(sizeof(float2) * nval), s_bar);
+  }
+  if (!bulk)
+    for (int k = tid; k < nval; k += NT) cp_async8(s_u + k, A.u_in + gofs + k);
+  for (int k = tid; k < nel * 2 * D * NF; k += NT) {
+    const int sl = k / (2 * D * NF);
+    const int rem = k - sl * (2 * D * NF);
+    const int dir = rem / NF;
+    const int fn = rem - dir * NF;
+    const int64_t nb = P.nbr[(e0 + sl) * 2 * D + dir];
+    if (nb >= e0 && nb < e0 + nel) continue;  // in this block
+    const int dd = dir >> 1;
+    const int nnode = line_base<N>(fn, dd) + ((dir & 1) ? 0 : (N - 1) * axis_stride<N>(dd));
+    const float2* g = nb >= 0 ? A.u_in + ((size_t)nb * NN + nnode) * NV
+                              : P.ghost + ((size_t)(-1 - nb) * NF + fn) * NV;  // boundary face
+#pragma unroll
+    for (int v = 0; v < NV; ++v) cp_async8(s_fu + k * NV + v, g + v);
+  }
+  mixed_block_constants<D, N, VI>(P, A, NT, s_mat, s_iw, s_scal);
+  if (tid < EPB * D) s_smax[tid] = 0u;
+  // ---- per element, while the copies are in flight ---------------------------
+  mixed_setup_elements<D, N, VI, EPB>(P, A, e0, nel, A.u_in + gofs, nullptr, s_ref, s_elem);
+  cp_async_wait_all();
+  __syncthreads();  // also orders the mbarrier's initialisation before the waits
+  if (bulk && __syncthreads_or(!tc::mbar_wait_bounded(s_bar, 0u, STAGING_WAIT_POLLS))) {
+    // the bulk copy did not land in time: report it and leave the block
+    // (a second bounded wait for the copy still in flight first)
+    if (tid == 0) atomicOr(A.status, STATUS_STAGING_TIMEOUT);
+    tc::mbar_wait_bounded(s_bar, 0u, STAGING_WAIT_POLLS);
+    return;
+  }
+
+  mixed_node_deviations<D, N, VI, EPB>(P, s_u, s_ref, s_nd, nel);
+  __syncthreads();
+
+  mixed_lines<D, N, VI, VF, SF, EPB, DIRECT>(P, s_ref, s_u, s_fu, s_nd, s_part, s_mat, s_iw,
+                                             s_elem, P.nbr + e0 * 2 * D, e0, nel);
+  // 2N register of this thread's node-phase nodes (zero at the first stage),
+  // loaded before the barrier so that its latency overlaps the wait
+  constexpr int NPT = (EPB * NN + NT - 1) / NT;  // nodes per thread in the node phase
+  const bool stage = A.mode == MODE_STAGE;
+  float ut_pre[NPT][NV];
+#pragma unroll
+  for (int k = 0; k < NPT; ++k) {
+    const int n = tid + k * NT;
+    const bool ld = stage && !A.zero_tmp && n < nel * NN;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) ut_pre[k][v] = ld ? A.u_tmp[gofs + (size_t)n * NV + v] : 0.0f;
+  }
+  __syncthreads();
+
+  mixed_node_update<D, N, VI, EPB>(P, A, e0, nel, s_u, s_part, s_elem, s_scal, s_smax,
+                                   P.inv_jac + e0, ut_pre);
+  if (bulk) {
+    // the ensemble kernel calls this body again on the same shared memory:
+    // retire the mbarrier (its one phase has completed) before it is re-made
+    __syncthreads();
+    if (tid == 0) tc::mbar_inval(s_bar);
   }
 }
 
@@ -1066,6 +1200,222 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
     mixed_element_kernel(const MixedParams P, const MixedArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   mixed_element_block<D, N, VI, VF, SF, EPB, DIRECT>(P, A, blockIdx.x, smem_raw);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent, double-buffered form of the stage kernel (2D meshes).
+//
+// Each block walks element blocks blk = blockIdx.x, + gridDim.x, ...  The
+// inputs of the next element block are fetched while the current one
+// computes:
+//   - one thread issues bulk (TMA) copies of its state chunk, its 2N register
+//     chunk (after stage 0), its face-neighbour rows, its pre-smoothed blending
+//     factors and its inverse Jacobians into the other of two buffers, before
+//     the lines phase; they complete on that buffer's mbarrier;
+//   - after the lines phase (the last reader of the face traces), every thread
+//     issues cp.async copies of the next block's neighbour traces of faces to
+//     other blocks, addressed by the neighbour rows that have arrived by then;
+//     they land during the node phase.
+// The waits are bounded: a block that gives up sets STATUS_STAGING_TIMEOUT in
+// the status word, waits (bounded) for its copies in flight and stops.  The
+// arithmetic is that of mixed_element_block, phase by phase, so both give the
+// same bits.
+// ---------------------------------------------------------------------------
+template <int D, int N, int VI, int EPB>
+struct MixedPipe {
+  using K = MixedKernel<D, N, VI, EPB>;
+  static constexpr int NV = K::NV, NN = K::NN, NF = K::NF, NT = K::NT, SP = K::SP;
+  static __host__ __device__ constexpr size_t up(size_t x) { return (x + 15) / 16 * 16; }
+  // one buffer: state, u_tmp, neighbour rows, alpha, inverse Jacobian
+  static constexpr size_t B_U = 0;
+  static constexpr size_t B_UT = B_U + up(sizeof(float2) * K::CHUNK);
+  static constexpr size_t B_NBR = B_UT + up(sizeof(float) * K::CHUNK);
+  static constexpr size_t B_AL = B_NBR + up(sizeof(int32_t) * EPB * 2 * D);
+  static constexpr size_t B_IJ = B_AL + up(sizeof(float) * EPB);
+  static constexpr size_t BUF = B_IJ + up(sizeof(float) * EPB);
+  // single copies
+  static constexpr size_t O_FU = 2 * BUF;
+  static constexpr size_t O_ND = O_FU + up(sizeof(float2) * K::FACE);
+  static constexpr size_t O_PART = O_ND + up(sizeof(float) * K::NFLD * SP);
+  static constexpr size_t O_REF = O_PART + up(sizeof(float) * D * NV * SP);
+  static constexpr size_t O_ELEM = O_REF + up(sizeof(RefState<D>) * EPB);
+  static constexpr size_t O_SCAL = O_ELEM + up(sizeof(float) * EPB * 8);
+  static constexpr size_t O_SMAX = O_SCAL + up(sizeof(float) * 8);
+  static constexpr size_t O_MAT = O_SMAX + up(sizeof(unsigned) * EPB * D);
+  static constexpr size_t O_IW = O_MAT + up(sizeof(float) * N * N);
+  static constexpr size_t O_BAR = O_IW + up(sizeof(float) * N);
+  static constexpr size_t SMEM = O_BAR + 16;
+};
+
+// Bulk copies of element block blk's contiguous inputs into buffer `buf`
+// (thread 0).  2D sizes are multiples of 16 bytes for every polydeg; the
+// per-element float arrays are read in whole 16-byte groups (allocated with
+// padding).
+template <int D, int N, int VI, int EPB>
+__device__ __forceinline__ void mixed_pipe_issue(const MixedParams& P, const MixedArgs& A,
+                                                 int64_t blk, unsigned char* buf, uint64_t* mbar) {
+  using Q = MixedPipe<D, N, VI, EPB>;
+  constexpr int NN = Q::NN, NV = Q::NV;
+  const int64_t e0 = blk * EPB;
+  const int nel = (int)min((int64_t)EPB, P.nelements - e0);
+  const size_t gofs = (size_t)e0 * NN * NV;
+  const uint32_t b_u = (uint32_t)(sizeof(float2) * nel * NN * NV);
+  const bool need_ut = A.mode == MODE_STAGE && !A.zero_tmp;
+  const uint32_t b_ut = need_ut ? (uint32_t)(sizeof(float) * nel * NN * NV) : 0u;
+  const uint32_t b_nbr = (uint32_t)(sizeof(int32_t) * nel * 2 * D);
+  const uint32_t b_el = (uint32_t)Q::up(sizeof(float) * nel);
+  const uint32_t b_al = VI == VI_HG ? b_el : 0u;
+  tc::mbar_arrive_expect_tx(mbar, b_u + b_ut + b_nbr + b_al + b_el);
+  tc::bulk_g2s(buf + Q::B_U, A.u_in + gofs, b_u, mbar);
+  if (need_ut) tc::bulk_g2s(buf + Q::B_UT, A.u_tmp + gofs, b_ut, mbar);
+  tc::bulk_g2s(buf + Q::B_NBR, P.nbr + e0 * 2 * D, b_nbr, mbar);
+  if (VI == VI_HG) tc::bulk_g2s(buf + Q::B_AL, A.alpha_smoothed + e0, b_al, mbar);
+  tc::bulk_g2s(buf + Q::B_IJ, P.inv_jac + e0, b_el, mbar);
+}
+
+// cp.async copies of the neighbour traces of element block blk's faces to
+// other blocks (and of ghost traces) into `fu`, addressed by the block's
+// staged neighbour rows, then a commit.
+template <int D, int N, int VI, int EPB>
+__device__ __forceinline__ void mixed_pipe_faces(const MixedParams& P, const MixedArgs& A,
+                                                 int64_t blk, const int32_t* s_nbr, float2* fu) {
+  using Q = MixedPipe<D, N, VI, EPB>;
+  constexpr int NF = Q::NF, NT = Q::NT, NN = Q::NN, NV = Q::NV;
+  const int64_t e0 = blk * EPB;
+  const int nel = (int)min((int64_t)EPB, P.nelements - e0);
+  for (int k = threadIdx.x; k < nel * 2 * D * NF; k += NT) {
+    const int sl = k / (2 * D * NF);
+    const int rem = k - sl * (2 * D * NF);
+    const int dir = rem / NF;
+    const int fn = rem - dir * NF;
+    const int64_t nb = s_nbr[sl * 2 * D + dir];
+    if (nb >= e0 && nb < e0 + nel) continue;  // in the block
+    const int dd = dir >> 1;
+    const int nnode = line_base<N>(fn, dd) + ((dir & 1) ? 0 : (N - 1) * axis_stride<N>(dd));
+    const float2* g = nb >= 0 ? A.u_in + ((size_t)nb * NN + nnode) * NV
+                              : P.ghost + ((size_t)(-1 - nb) * NF + fn) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) cp_async8(fu + k * NV + v, g + v);
+  }
+  cp_async_commit();
+}
+
+template <int D, int N, int VI, int VF, int SF, int EPB, bool DIRECT = false>
+__global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D, N, VI, EPB>::MINB)
+    mixed_element_pipe_kernel(const MixedParams P, const MixedArgs A) {
+  using K = MixedKernel<D, N, VI, EPB>;
+  using Q = MixedPipe<D, N, VI, EPB>;
+  constexpr int NV = K::NV, NN = K::NN, NT = K::NT;
+  constexpr int NPT = (EPB * NN + NT - 1) / NT;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* s_fu = reinterpret_cast<float2*>(smem_raw + Q::O_FU);
+  float* s_nd = reinterpret_cast<float*>(smem_raw + Q::O_ND);
+  float* s_part = reinterpret_cast<float*>(smem_raw + Q::O_PART);
+  RefState<D>* s_ref = reinterpret_cast<RefState<D>*>(smem_raw + Q::O_REF);
+  float* s_elem = reinterpret_cast<float*>(smem_raw + Q::O_ELEM);
+  float* s_scal = reinterpret_cast<float*>(smem_raw + Q::O_SCAL);
+  unsigned int* s_smax = reinterpret_cast<unsigned int*>(smem_raw + Q::O_SMAX);
+  float* s_mat = reinterpret_cast<float*>(smem_raw + Q::O_MAT);
+  float* s_iw = reinterpret_cast<float*>(smem_raw + Q::O_IW);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + Q::O_BAR);
+
+  const int tid = threadIdx.x;
+  const int64_t nblocks = (P.nelements + EPB - 1) / EPB;
+  if (A.mode == MODE_STAGE && A.clock->skip) {
+    // past t_end: the state passes through unchanged (no copies issued)
+    for (int64_t blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
+      const int64_t e0 = blk * EPB;
+      const size_t gofs = (size_t)e0 * NN * NV;
+      const int nval = (int)min((int64_t)EPB, P.nelements - e0) * NN * NV;
+      for (int k = tid; k < nval; k += NT) A.u_out[gofs + k] = A.u_in[gofs + k];
+    }
+    return;
+  }
+  const bool need_ut = A.mode == MODE_STAGE && !A.zero_tmp;
+  if (tid == 0) {
+    tc::mbar_init(&mbar[0], 1);
+    tc::mbar_init(&mbar[1], 1);
+    tc::fence_mbar_init();
+  }
+  mixed_block_constants<D, N, VI>(P, A, NT, s_mat, s_iw, s_scal);
+  __syncthreads();
+
+  // prologue: the first element block's inputs
+  int64_t blk = blockIdx.x;
+  int failed_it = -1;
+  if (tid == 0) mixed_pipe_issue<D, N, VI, EPB>(P, A, blk, smem_raw, &mbar[0]);
+  if (__syncthreads_or(!tc::mbar_wait_bounded(&mbar[0], 0u, STAGING_WAIT_POLLS))) {
+    failed_it = 0;
+  } else {
+    mixed_pipe_faces<D, N, VI, EPB>(P, A, blk,
+                                    reinterpret_cast<const int32_t*>(smem_raw + Q::B_NBR), s_fu);
+  }
+  for (int it = 0; failed_it < 0 && blk < nblocks; ++it, blk += gridDim.x) {
+    const int b = it & 1;
+    unsigned char* cur = smem_raw + b * Q::BUF;
+    unsigned char* nxt_buf = smem_raw + (b ^ 1) * Q::BUF;
+    const int64_t nxt = blk + gridDim.x;
+    const int64_t e0 = blk * EPB;
+    const int nel = (int)min((int64_t)EPB, P.nelements - e0);
+    const float2* s_u = reinterpret_cast<const float2*>(cur + Q::B_U);
+    // ---- this block's bulk data: waited for at the end of the previous
+    //      iteration (or in the prologue), so this returns at once ------------------
+    if (__syncthreads_or(!tc::mbar_wait_bounded(&mbar[b], (uint32_t)((it >> 1) & 1),
+                                                 STAGING_WAIT_POLLS))) {
+      failed_it = it;
+      break;
+    }
+    if (tid < EPB * D) s_smax[tid] = 0u;
+    mixed_setup_elements<D, N, VI, EPB>(P, A, e0, nel, s_u,
+                                        VI == VI_HG ? reinterpret_cast<const float*>(cur + Q::B_AL)
+                                                    : nullptr,
+                                        s_ref, s_elem);
+    cp_async_wait_all();  // this thread's copies of this block's face traces
+    __syncthreads();
+
+    mixed_node_deviations<D, N, VI, EPB>(P, s_u, s_ref, s_nd, nel);
+    __syncthreads();
+
+    // ---- the next block's bulk inputs, into the other buffer (last read one
+    //      iteration ago, before two barriers) ------------------------------------
+    if (tid == 0 && nxt < nblocks) mixed_pipe_issue<D, N, VI, EPB>(P, A, nxt, nxt_buf, &mbar[b ^ 1]);
+
+    mixed_lines<D, N, VI, VF, SF, EPB, DIRECT>(
+        P, s_ref, s_u, s_fu, s_nd, s_part, s_mat, s_iw, s_elem,
+        reinterpret_cast<const int32_t*>(cur + Q::B_NBR), e0, nel);
+    __syncthreads();
+
+    // ---- the next block's face traces (the face buffer is free now) -------------
+    if (nxt < nblocks) {
+      if (__syncthreads_or(!tc::mbar_wait_bounded(&mbar[b ^ 1], (uint32_t)(((it + 1) >> 1) & 1),
+                                                   STAGING_WAIT_POLLS))) {
+        failed_it = it + 1;
+        break;
+      }
+      mixed_pipe_faces<D, N, VI, EPB>(P, A, nxt,
+                                      reinterpret_cast<const int32_t*>(nxt_buf + Q::B_NBR), s_fu);
+    }
+
+    const float* s_ut = reinterpret_cast<const float*>(cur + Q::B_UT);
+    float ut_pre[NPT][NV];
+#pragma unroll
+    for (int k = 0; k < NPT; ++k) {
+      const int n = tid + k * NT;
+      const bool ld = need_ut && n < nel * NN;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) ut_pre[k][v] = ld ? s_ut[n * NV + v] : 0.0f;
+    }
+    mixed_node_update<D, N, VI, EPB>(P, A, e0, nel, s_u, s_part, s_elem, s_scal, s_smax,
+                                     reinterpret_cast<const float*>(cur + Q::B_IJ), ut_pre);
+    __syncthreads();
+  }
+  if (failed_it >= 0) {
+    if (tid == 0) atomicOr(A.status, STATUS_STAGING_TIMEOUT);
+    cp_async_wait_all();
+    // the bulk copies that were waited for, if they are still landing
+    tc::mbar_wait_bounded(&mbar[failed_it & 1], (uint32_t)((failed_it >> 1) & 1),
+                          STAGING_WAIT_POLLS);
+  }
 }
 
 }  // namespace tg

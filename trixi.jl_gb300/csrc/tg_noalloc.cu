@@ -39,6 +39,26 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
 double* g_scratch[kMaxDevices] = {nullptr};
+void* g_scratch_ctx[kMaxDevices] = {nullptr};  // the context each address was resolved in
+
+// The calling thread's current driver context (CUcontext), through the
+// runtime's driver entry point so that the library needs no link to libcuda;
+// nullptr when it cannot be queried or no context is current yet.
+void* current_context() {
+  using Fn = int (*)(void**);
+  static Fn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return (Fn)p;
+  }();
+  void* ctx = nullptr;
+  if (fn && fn(&ctx) != 0) ctx = nullptr;
+  return ctx;
+}
 
 struct NoallocParams {
   int D, N, NV;
@@ -135,15 +155,18 @@ extern "C" int tg_integrals_noalloc(int32_t ndims, int32_t polydeg, int64_t nele
     return fail(TG_ERR_CUDA, "tg_integrals_noalloc: no current CUDA device");
   double* scratch;
   {
-    // First call on this device: resolve the device address of the static
-    // scratch array (its host-side name is only a stand-in).
+    // First call on this device (or in a context other than the one the
+    // address was resolved in, e.g. after cudaDeviceReset or under a
+    // non-primary context): resolve the device address of the static scratch
+    // array (its host-side name is only a stand-in).
     std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch[dev]) {
+    if (!g_scratch[dev] || g_scratch_ctx[dev] != current_context()) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_noalloc_partials);
       if (e != cudaSuccess || !p)
         return fail(TG_ERR_CUDA, "tg_integrals_noalloc: cudaGetSymbolAddress failed");
       g_scratch[dev] = (double*)p;
+      g_scratch_ctx[dev] = current_context();  // current now: the call above set it up
     }
     scratch = g_scratch[dev];
   }

@@ -1,9 +1,11 @@
-// Inline-PTX wrappers for the 5th-generation tensor cores of sm_100-family GPUs
-// (tcgen05: tensor memory, single-thread MMA issue, completion on an mbarrier).
-//
-// Only what the learned indicator's MLP kernels use: BF16 x BF16 -> FP32 MMAs
-// with both operands in shared memory in the K-major layout without swizzle,
-// accumulators in tensor memory (TMEM), read back with 32x32b loads.
+// Inline-PTX wrappers for the asynchronous units of sm_100-family GPUs:
+//   - the 5th-generation tensor cores (tcgen05): BF16 x BF16 -> FP32 MMAs with
+//     both operands in shared memory in the K-major layout without swizzle,
+//     accumulators in tensor memory (TMEM), read back with 32x32b loads (the
+//     learned indicator's MLP kernels);
+//   - bulk (TMA) copies from global to shared memory (the element kernels'
+//     staging);
+//   - the shared-memory mbarriers both complete on.
 //
 // K-major operand layout (no swizzle).  An R x K operand (rows = M for A, N
 // for B; K contiguous per row) is stored as 8 x 8 "core matrices" of 16-byte
@@ -97,6 +99,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count)
                : "memory");
 }
+__device__ __forceinline__ void mbar_inval(uint64_t* mbar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
 __device__ __forceinline__ void fence_mbar_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
@@ -119,6 +124,25 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mbar, uint32_t parit
   for (uint32_t k = 0; k < limit; ++k)
     if (mbar_try_wait(mbar, parity)) return true;
   return false;
+}
+
+// Expected transaction bytes of the current phase, plus this thread's arrival.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Bulk (TMA, untiled) copy global -> this CTA's shared memory, completed on
+// the mbarrier as transaction bytes.  Both addresses 16-byte aligned, bytes a
+// multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* smem_dst, const void* gmem_src, uint32_t bytes,
+                                         uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(smem_dst)),
+      "l"(gmem_src), "r"(bytes), "r"(smem_u32(mbar))
+      : "memory");
 }
 
 // 32 consecutive FP32 columns of this thread's TMEM lane (32x32b shape, x32),

@@ -196,8 +196,9 @@ def harvest_and_train(net, every=10, khi_level=8, khi_t_end=3.0, khi_stride=16,
     """Training set and training of the learned indicator: (modes, sqrt E) pairs of
     every `*_stride`-th element, harvested every `every` steps from the KHI run
     (256^2, t = 3, CFL 1.3) and the Gaussian blast (128^2, t = 0.3, CFL 1), both
-    mixed precision with the plain HG indicator; then `train_steps` Adam steps
-    on the GPU.  Returns the statistics of both phases."""
+    mixed precision with the plain HG indicator; then Adam on the GPU: 50 and
+    `train_steps` steps at `lr`, and `train_steps` / 4 at lr / 10 (training is
+    reproducible bit for bit).  Returns the statistics of both phases."""
     out = {}
     t_start = time.perf_counter()
     for name, semi, t_end, stride in (
@@ -220,9 +221,11 @@ def harvest_and_train(net, every=10, khi_level=8, khi_t_end=3.0, khi_stride=16,
     out["harvest_secs"] = time.perf_counter() - t_start
     t0 = time.perf_counter()
     first = net.train(50, batch=batch, lr=lr)
-    last = net.train(train_steps, batch=batch, lr=lr)
-    out["train"] = dict(pairs=net.count, steps=train_steps + 50, loss_first=first, loss_last=last,
-                        secs=time.perf_counter() - t0)
+    net.train(train_steps, batch=batch, lr=lr)
+    # a last quarter at a tenth of the rate settles the weights
+    last = net.train(train_steps // 4, batch=batch, lr=0.1 * lr)
+    out["train"] = dict(pairs=net.count, steps=50 + train_steps + train_steps // 4,
+                        loss_first=first, loss_last=last, secs=time.perf_counter() - t0)
     x, y = net.dataset()
     held = np.arange(len(y)) % 10 == 0
     pred = net.predict(x[held])
@@ -384,10 +387,10 @@ def c5a_specs(n=64, seed=20261204):
 
 
 # Short runs of single kernels (for profiling a handful of launches).
-def learned_steps(steps=4):
-    """KHI 256^2, mixed precision, a 16-64-64-1 network with its initial weights
-    deployed as the shock indicator, `steps` steps."""
-    semi = khi_semi(8, "mixed")
+def learned_steps(steps=4, level=9):
+    """KHI 512^2 (the bench mesh), mixed precision, a 16-64-64-1 network with its
+    initial weights deployed as the shock indicator, `steps` steps."""
+    semi = khi_semi(level, "mixed")
     net = ShockIndicatorMLP(2, 3, seed=3)
     c = semi.device_context
     c.upload(semi.compute_coefficients(0.0))
