@@ -89,6 +89,45 @@ def read_traffic(path):
         return None
 
 
+def read_profile(path, key):
+    try:
+        with open(path) as f:
+            return json.load(f).get(key)
+    except (OSError, ValueError):
+        return None
+
+
+def fma_peaks(dev):
+    """Measured FP32 and FP64 FMA rates of this GPU (library microbenchmark), with
+    the SM clock sampled meanwhile."""
+    import ctypes
+
+    from trixi_gb300 import _lib
+    lib = _lib.load()
+    sampler = ClockSampler(dev)
+    out = {}
+    for name, fp64 in (("fp32", 0), ("fp64", 1)):
+        best = 0.0
+        for _ in range(3):
+            v = ctypes.c_double()
+            _lib.check(lib.tg_fma_peak(fp64, ctypes.byref(v)))
+            best = max(best, v.value)
+        out[name + "_tflops"] = best / 1e12
+    out["clocks"] = sampler.stop()
+    return out
+
+
+def compute_record(flops_per_launch, ms, peaks):
+    """FP32 arithmetic rate of a kernel: flops per launch (from its committed ncu
+    capture: 2 FFMA + FADD + FMUL thread instructions) over the live event time."""
+    if not flops_per_launch or not peaks:
+        return None
+    achieved = flops_per_launch / (ms * 1e-3) / 1e12
+    return {"bound": "fp32", "achieved": achieved, "peak": peaks["fp32_tflops"],
+            "unit": "TFLOP/s", "frac": achieved / peaks["fp32_tflops"],
+            "flops_per_launch": flops_per_launch, "peak_source": "measured (tg_fma_peak)"}
+
+
 def make_semi(precision: str, epb: int = 0):
     import trixi_gb300 as T
     eq = T.CompressibleEulerEquations3D(1.4)
@@ -413,6 +452,10 @@ def khi_arm(args, rank: int, world: int):
                           "achieved": ind_bytes / (ind_ms * 1e-3) / 1e9}}
     roof["frac"] = roof["achieved"] / peak
     roof["indicator"]["frac"] = roof["indicator"]["achieved"] / peak
+    fpeaks = fma_peaks(dev) if rank == 0 else None
+    roof["compute"] = compute_record(read_profile(KHI_PROFILE_TRAFFIC, "fp32_flops_per_launch"),
+                                     el_ms, fpeaks)
+    roof["fma_peaks"] = fpeaks
 
     e2e = None if args.no_e2e else e2e_steps(ctx_ml, semi_ml, args.steps, args.warmup, KHI_CFL,
                                               world, flush)
@@ -856,8 +899,8 @@ def khi_line(args, rank, world):
         "cpu_baseline": cpu,
         "e2e": out["e2e"],
         "clocks": ml["clocks"],
-        # per step: clock prologue, 5 x (indicator + element kernel), clock epilogue
-        "gpu_launches": 12 * ml["steps"],
+        # per step: clock prologue, 5 x (indicator, smoothing, element kernel), clock epilogue
+        "gpu_launches": 17 * ml["steps"],
         "mms3d": mms,
     }
     print(json.dumps(line))

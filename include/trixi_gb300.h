@@ -392,6 +392,13 @@ int tg_synchronize(tg_ctx* ctx);
  * own work or timing events with the library's launches. */
 int tg_stream(tg_ctx* ctx, void** stream);
 
+/* FMA issue rate of the current device in FP32 (fp64 = 0) or FP64 (fp64 = 1),
+ * in flop/s (an FMA counts two): independent FMA chains on a full-occupancy
+ * grid, timed with CUDA events (a few milliseconds).  The compute-side
+ * denominator for the element kernels' arithmetic rate; no counterpart in the
+ * reference.  Synchronous. */
+int tg_fma_peak(int32_t fp64, double* flops_per_second);
+
 /* Allocation-free variant of tg_integrals, for callers that cannot allocate
  * device memory (a fixed-size memory pool, a runtime that owns all device
  * memory, work recorded while allocation is forbidden) and so cannot create a

@@ -4,13 +4,23 @@
 # The seam is rhs_hyperbolic!(backend, du, u, t, mesh, equations, ...)
 # (src/solvers/dgsem_tree/dg_2d.jl:113), selected by trixi_backend(u)
 # (src/auxiliary/containers.jl:278); the KernelAbstractions backend plugs in
-# at the same place (src/solvers/dgsem_p4est/dg_2d_gpu.jl:8).
+# at the same place (src/solvers/dgsem_p4est/dg_2d_gpu.jl:8).  The ODE state
+# is a GB300Array (device memory owned by the library), so that
+# `rhs_hyperbolic!(du_ode, u_ode, semi, t)`
+# (semidiscretization_hyperbolic.jl:578-597) finds the backend through
+# trixi_backend(u), and OrdinaryDiffEq's CarpenterKennedy2N54 drives it
+# unchanged: its broadcasts (tmp = A tmp + dt du; u = u + B tmp) lower to
+# the library's tg_lincomb.
 #
-# Not exercised in this repository's tests (no Julia toolchain here); the C ABI
-# it calls is tested from Python through the same entry points.
+# Julia is not installed where this repository is tested.  The calling
+# convention -- the tg_config built from Trixi's own arrays, library-owned
+# device vectors, tg_rhs on them, the 2N broadcasts through tg_lincomb -- is
+# exercised from C by tests/c/shim_driver.c (tests/test_gpu_shim_abi.py).
 module TrixiGB300
 
 using Trixi
+using Trixi: True, False
+using SciMLBase: ODEProblem
 
 const lib = joinpath(@__DIR__, "..", "_build", "libtrixi_gb300.so")
 
@@ -212,6 +222,13 @@ bc_code(::Trixi.BoundaryConditionDirichlet) = Int32(1)
 bc_code(::typeof(Trixi.boundary_condition_slip_wall)) = Int32(2)
 boundary_codes(bcs::Trixi.BoundaryConditionPeriodic, nd) = ntuple(_ -> Int32(0), 6)
 boundary_codes(bcs::NamedTuple, nd) = ntuple(k -> k <= 2nd ? bc_code(bcs[k]) : Int32(0), 6)
+# Non-periodic P4estMesh bricks carry their boundaries by name
+# (UnstructuredSortedBoundaryTypes); the library takes one condition per
+# direction of a TreeMesh or StructuredMesh only.
+boundary_codes(bcs, nd) =
+    error("TrixiGB300: boundary conditions of type $(typeof(bcs)) (for instance a " *
+          "non-periodic P4estMesh) are not on the GPU path; use a periodic P4estMesh or a " *
+          "StructuredMesh with one condition per direction")
 
 # Dirichlet values: the initial conditions the device evaluates
 ic_code(::typeof(Trixi.initial_condition_constant)) = Int32(0)
@@ -245,6 +262,156 @@ function rhs!(ctx::GB300Context, du, u, t)
     check(ccall((:tg_rhs, lib), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Cdouble),
                 ctx.ptr, pointer(du), pointer(u), t), ctx.ptr)
     return nothing
+end
+
+# ---- the ODE state in device memory ------------------------------------------------
+"""
+    GB300Array <: AbstractVector{Float64}
+
+A flat `u_ode` vector in Trixi's layout that lives in device memory owned by
+the library (tg_vector_create), tied to the context it is used with.  Scalar
+indexing is not supported; `copyto!` moves data to and from host `Vector`s,
+and broadcasts that are linear combinations of at most two GB300Arrays with
+scalar coefficients (what low-storage Runge-Kutta methods use) run on the
+device through tg_lincomb.
+"""
+mutable struct GB300Array <: AbstractVector{Float64}
+    ptr::Ptr{Float64}
+    len::Int
+    ctx::GB300Context
+    function GB300Array(ctx::GB300Context, len::Integer)
+        p = Ref{Ptr{Float64}}(C_NULL)
+        check(ccall((:tg_vector_create, lib), Cint, (Ptr{Cvoid}, Int64, Ref{Ptr{Float64}}),
+                    ctx.ptr, len, p), ctx.ptr)
+        a = new(p[], Int(len), ctx)
+        finalizer(a) do x
+            ctx.ptr == C_NULL ||
+                ccall((:tg_vector_destroy, lib), Cint, (Ptr{Cvoid}, Ptr{Float64}), ctx.ptr, x.ptr)
+        end
+        return a
+    end
+end
+
+Base.size(a::GB300Array) = (a.len,)
+Base.pointer(a::GB300Array) = a.ptr
+Base.IndexStyle(::Type{GB300Array}) = IndexLinear()
+Base.getindex(::GB300Array, ::Int) =
+    error("GB300Array: scalar indexing of device memory; copy it to a Vector first")
+Base.setindex!(::GB300Array, v, ::Int) =
+    error("GB300Array: scalar indexing of device memory; copy a Vector into it instead")
+Base.similar(a::GB300Array) = GB300Array(a.ctx, a.len)
+Base.similar(a::GB300Array, ::Type{Float64}) = similar(a)
+Base.similar(a::GB300Array, ::Type{Float64}, dims::Tuple{Int}) = GB300Array(a.ctx, dims[1])
+
+function vector_copy!(dst::Ptr, src::Ptr, n, kind, ctx)
+    check(ccall((:tg_vector_copy, lib), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Int64, Int32),
+                ctx.ptr, dst, src, n, kind), ctx.ptr)
+end
+function Base.copyto!(dst::GB300Array, src::Vector{Float64})
+    GC.@preserve src vector_copy!(dst.ptr, pointer(src), dst.len, 0, dst.ctx)
+    return dst
+end
+function Base.copyto!(dst::Vector{Float64}, src::GB300Array)
+    GC.@preserve dst vector_copy!(pointer(dst), src.ptr, src.len, 1, src.ctx)
+    return dst
+end
+function Base.copyto!(dst::GB300Array, src::GB300Array)
+    vector_copy!(dst.ptr, src.ptr, dst.len, 2, dst.ctx)
+    return dst
+end
+Base.Array(a::GB300Array) = copyto!(Vector{Float64}(undef, a.len), a)
+
+# broadcasts: sum of scalar multiples of at most two GB300Arrays
+Base.BroadcastStyle(::Type{GB300Array}) = Broadcast.ArrayStyle{GB300Array}()
+function Base.similar(bc::Broadcast.Broadcasted{Broadcast.ArrayStyle{GB300Array}},
+                      ::Type{Float64})
+    return similar(find_gb300(bc))
+end
+find_gb300(bc::Broadcast.Broadcasted) = find_gb300(bc.args)
+find_gb300(args::Tuple) = (a = find_gb300(first(args)); a === nothing ? find_gb300(Base.tail(args)) : a)
+find_gb300(::Tuple{}) = nothing
+find_gb300(a::GB300Array) = a
+find_gb300(x) = nothing
+
+# terms!(terms, expr, c): add c * expr to the list of (coefficient, array) terms
+terms!(t, a::GB300Array, c) = (push!(t, (c, a)); t)
+terms!(t, x::Number, c) = error("GB300Array broadcast: a scalar term is not a linear combination")
+function terms!(t, bc::Broadcast.Broadcasted, c)
+    f, args = bc.f, bc.args
+    if f === (+) && length(args) == 2
+        terms!(t, args[1], c); terms!(t, args[2], c)
+    elseif f === (-) && length(args) == 2
+        terms!(t, args[1], c); terms!(t, args[2], -c)
+    elseif f === (-) && length(args) == 1
+        terms!(t, args[1], -c)
+    elseif f === (*) && length(args) == 2 && args[1] isa Number
+        terms!(t, args[2], c * args[1])
+    elseif f === (*) && length(args) == 2 && args[2] isa Number
+        terms!(t, args[1], c * args[2])
+    elseif f === identity && length(args) == 1
+        terms!(t, args[1], c)
+    else
+        error("GB300Array broadcast: only linear combinations of device vectors run on the GPU")
+    end
+    return t
+end
+terms!(t, r::Base.RefValue, c) = terms!(t, r[], c)
+
+function Base.copyto!(dst::GB300Array,
+                      bc::Broadcast.Broadcasted{Broadcast.ArrayStyle{GB300Array}})
+    t = terms!(Tuple{Float64, GB300Array}[], bc, 1.0)
+    merged = Dict{Ptr{Float64}, Tuple{Float64, GB300Array}}()
+    for (c, a) in t
+        prev = get(merged, a.ptr, (0.0, a))
+        merged[a.ptr] = (prev[1] + c, a)
+    end
+    length(merged) <= 2 ||
+        error("GB300Array broadcast: at most two device vectors per linear combination")
+    (c1, x), rest = first(values(merged)), collect(values(merged))[2:end]
+    c2, y = isempty(rest) ? (0.0, nothing) : rest[1]
+    check(ccall((:tg_lincomb, lib), Cint,
+                (Ptr{Cvoid}, Int64, Ptr{Float64}, Cdouble, Ptr{Float64}, Cdouble, Ptr{Float64}),
+                dst.ctx.ptr, dst.len, dst.ptr, c1, x.ptr, c2,
+                y === nothing ? Ptr{Float64}(C_NULL) : y.ptr), dst.ctx.ptr)
+    return dst
+end
+
+# ---- the backend: Trixi dispatches rhs_hyperbolic! and max_dt on it ---------------
+Trixi.trixi_backend(::GB300Array) = GB300Backend()
+# the flat device vector is passed on as it is: the library reads Trixi's layout
+Trixi.wrap_array(u_ode::GB300Array, mesh, equations, dg::DGSEM, cache) = u_ode
+
+function Trixi.rhs_hyperbolic!(::GB300Backend, du::GB300Array, u::GB300Array, t,
+                               mesh::Union{TreeMesh, StructuredMesh, P4estMesh}, equations,
+                               boundary_conditions, source_terms, dg::DGSEM, cache)
+    rhs!(u.ctx, du, u, t)
+    return nothing
+end
+
+# StepsizeCallback: max_dt without the CFL factor, on the device
+function Trixi.max_dt(u::GB300Array, t, mesh::Union{TreeMesh, StructuredMesh, P4estMesh},
+                      constant_speed::False, equations, dg::DG, cache)
+    dt = Ref{Cdouble}(0)
+    check(ccall((:tg_max_dt, lib), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ref{Cdouble}),
+                u.ctx.ptr, u.ptr, dt), u.ctx.ptr)
+    return dt[]
+end
+
+"""
+    semidiscretize_gb300(semi, tspan; precision = 0, device = 0)
+
+`semidiscretize(semi, tspan)` with the state on the GB300: creates the
+device context of `semi` (kept alive with the returned problem's initial
+state), evaluates the initial condition on the host as Trixi does and uploads
+it into a GB300Array.  The ODEProblem's right-hand side is Trixi's own
+`rhs!`, which reaches the library through trixi_backend(u).
+"""
+function semidiscretize_gb300(semi::SemidiscretizationHyperbolic, tspan;
+                              precision = 0, device = 0)
+    ctx = create_context(semi; precision, device)
+    u0_host = Trixi.compute_coefficients(first(tspan), semi)
+    u0 = copyto!(GB300Array(ctx, length(u0_host)), u0_host)
+    return ODEProblem(Trixi.rhs!, u0, tspan, semi)
 end
 
 upload!(ctx::GB300Context, u::Vector{Float64}) =

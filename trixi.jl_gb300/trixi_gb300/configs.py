@@ -400,6 +400,23 @@ def learned_steps(steps=4, level=9):
     return dict(steps=n, t=t, status=c.status())
 
 
+def mms_steps(steps=3, level=5):
+    """3D manufactured solution at 32^3 (the mms3d bench mesh), flux differencing
+    with flux_ranocha, mixed precision, `steps` steps."""
+    eq = T.CompressibleEulerEquations3D(1.4)
+    solver = T.DGSEM(polydeg=3, surface_flux=T.flux_lax_friedrichs,
+                     volume_integral=T.VolumeIntegralFluxDifferencing(T.flux_ranocha))
+    mesh = T.TreeMesh((0.0,) * 3, (2.0,) * 3, initial_refinement_level=level)
+    semi = T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_convergence_test, solver,
+                                          source_terms=T.source_terms_convergence_test,
+                                          precision="mixed")
+    c = semi.device_context
+    c.upload(semi.compute_coefficients(0.0))
+    t, n = c.step(steps, 0.6, 10.0, 0.0)
+    c.synchronize()
+    return dict(steps=n, t=t, status=c.status())
+
+
 def ensemble_steps(steps=3):
     """The 64-vortex ensemble of c5a, `steps` steps."""
     ens = T.Ensemble([vortex_semi(lv, p, eps, "mixed") for lv, p, eps in c5a_specs()])
@@ -586,7 +603,7 @@ def curved_steps(steps=3, cells=512):
 
 
 RUNS = dict(c1=c1, c3=c3, c4=c4, c5a=c5a, c5b=c5b, c6=c6, c7=c7, c8=c8)
-SHORT_RUNS = dict(learned_steps=learned_steps, ensemble_steps=ensemble_steps,
+SHORT_RUNS = dict(learned_steps=learned_steps, mms_steps=mms_steps, ensemble_steps=ensemble_steps,
                   mortar_steps=mortar_steps, curved_steps=curved_steps)
 
 
