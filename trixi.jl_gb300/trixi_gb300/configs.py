@@ -228,9 +228,18 @@ def harvest_and_train(net, every=10, khi_level=8, khi_t_end=3.0, khi_stride=16,
                         loss_first=first, loss_last=last, secs=time.perf_counter() - t0)
     x, y = net.dataset()
     held = np.arange(len(y)) % 10 == 0
-    pred = net.predict(x[held])
-    out["train"]["heldout_mae_sqrtE"] = float(np.mean(np.abs(pred - y[held])))
-    out["train"]["heldout_mae_const"] = float(np.mean(np.abs(np.median(y[~held]) - y[held])))
+    pred = np.maximum(net.predict(x[held]), 0.0)  # as deployed: sqrt E >= 0
+    yh, yt = y[held], y[~held]
+    tr = out["train"]
+    # the objective (mean squared error of sqrt E) against the best constant, its mean
+    tr["heldout_rmse_sqrtE"] = float(np.sqrt(np.mean((pred - yh) ** 2)))
+    tr["heldout_rmse_const"] = float(np.sqrt(np.mean((np.mean(yt) - yh) ** 2)))
+    tr["heldout_mae_sqrtE"] = float(np.mean(np.abs(pred - yh)))
+    tr["heldout_mae_const"] = float(np.mean(np.abs(np.median(yt) - yh)))
+    # the decision that matters: alpha switched on (E above the HG threshold)
+    sqrt_thr = math.sqrt(0.5 * 10 ** (-1.8 * (net.polydeg + 1) ** 0.25))
+    tr["heldout_on_off_agreement"] = float(np.mean((pred > sqrt_thr) == (yh > sqrt_thr)))
+    tr["heldout_fraction_on"] = float(np.mean(yh > sqrt_thr))
     return out
 
 
