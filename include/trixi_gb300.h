@@ -305,6 +305,20 @@ int tg_set_time(tg_ctx* ctx, double t);
  * out[nvar] = total mathematical entropy, out[nvar+1] = kinetic energy. */
 int tg_integrals(tg_ctx* ctx, double* out);
 
+/* calc_error_norms(u, t, analyzer, semi, ...) (analysis_dg2d.jl:95-139,
+ * analysis_dg3d.jl:123-...) of u_dev (an FP64 device state in Trixi's layout;
+ * NULL: the context state) against the initial condition `ic`
+ * (tg_initial_condition, free constants `params[4]`, may be NULL) at time t,
+ * on the analyzer of Trixi's LobattoLegendreAnalyzer: its nanalyzer nodes'
+ * interpolation matrix (column-major [nanalyzer, polydeg + 1], as
+ * analyzer.vandermonde) and weights.  l2[nvar], linf[nvar] receive the L2
+ * error (normalised by the mesh volume) and the maximum error per conserved
+ * variable.  FP64 on the device, deterministic reduction; TreeMesh contexts
+ * created with node coordinates.  Synchronous. */
+int tg_error_norms(tg_ctx* ctx, const double* u_dev, double t, int32_t ic, const double* params,
+                   int32_t nanalyzer, const double* analyzer_vandermonde,
+                   const double* analyzer_weights, double* l2, double* linf);
+
 /* analyze(entropy_timederivative, du, u, t, ...) (analysis_dg2d.jl:460-472):
  * the volume-normalised integral of cons2entropy(u) . du with du = rhs(u, t)
  * of the context state, evaluated by the context's own rhs! (FP64 or mixed)

@@ -361,6 +361,126 @@ __global__ void sum_rows_kernel(const double* __restrict__ partial, int64_t E, i
   }
 }
 
+// calc_error_norms (analysis_dg2d.jl:95-139, analysis_dg3d.jl:123-...): per
+// element, the state and the node coordinates interpolated to the analyzer's
+// NA^D nodes dimension by dimension (multiply_dimensionwise!, x then y then z,
+// each sum in node order as the reference), the exact solution (a device
+// initial condition) there, and per variable the Jacobian-weighted sum of
+// squared differences and their maximum.  One block per element; the two
+// ping-pong buffers hold NC = NV + D values per node.
+struct ErrorNormArgs {
+  int N, NA, ic;
+  double par[4];
+  double t, gamma;
+  double avand[MAXN * (2 * MAXN - 1)];  // [NA][N], row-major
+  double aw[2 * MAXN - 1];
+};
+
+template <int D, typename TS>
+__global__ void __launch_bounds__(128) error_norms_kernel(const TS* __restrict__ u,
+                                                          const double* __restrict__ xline,
+                                                          const double* __restrict__ inv_jac,
+                                                          const ErrorNormArgs A,
+                                                          double* __restrict__ partial) {
+  constexpr int NV = D + 2, NC = NV + D;
+  extern __shared__ double esm[];
+  const int N = A.N, NA = A.NA;
+  int nn = N, nna = NA;
+  for (int d = 1; d < D; ++d) nn *= N, nna *= NA;
+  double* cur = esm;
+  double* nxt = esm + (size_t)nna * NC;
+  double* red = nxt + (size_t)nna * NC;  // [blockDim][2 NV]
+  const int64_t e = blockIdx.x;
+  for (int q = threadIdx.x; q < nn; q += blockDim.x) {
+    for (int v = 0; v < NV; ++v) cur[q * NC + v] = state_f64(u[((size_t)e * nn + q) * NV + v]);
+    const int idx[3] = {q % N, (q / N) % N, q / (N * N)};
+    for (int d = 0; d < D; ++d) cur[q * NC + NV + d] = xline[((size_t)e * D + d) * N + idx[d]];
+  }
+  __syncthreads();
+  int dims[3] = {N, N, N};
+  for (int d = 0; d < D; ++d) {
+    int so[3] = {dims[0], dims[1], dims[2]};
+    so[d] = NA;
+    int tot = 1;
+    for (int q = 0; q < D; ++q) tot *= so[q];
+    for (int o = threadIdx.x; o < tot; o += blockDim.x) {
+      const int ii[3] = {o % so[0], (o / so[0]) % so[1], o / (so[0] * so[1])};
+      for (int v = 0; v < NC; ++v) {
+        double r = 0;
+        for (int k = 0; k < N; ++k) {
+          int src[3] = {ii[0], ii[1], ii[2]};
+          src[d] = k;
+          const int si = src[0] + dims[0] * (src[1] + dims[1] * src[2]);
+          r += A.avand[ii[d] * N + k] * cur[si * NC + v];
+        }
+        nxt[o * NC + v] = r;
+      }
+    }
+    __syncthreads();
+    double* t = cur;
+    cur = nxt;
+    nxt = t;
+    dims[d] = NA;
+  }
+  double vj = 1.0 / inv_jac[e];
+  vj = D == 2 ? vj * vj : vj * vj * vj;
+  double loc[NV], mx[NV];
+  for (int v = 0; v < NV; ++v) loc[v] = mx[v] = 0.0;
+  for (int o = threadIdx.x; o < nna; o += blockDim.x) {
+    const int idx[3] = {o % NA, (o / NA) % NA, o / (NA * NA)};
+    double w = A.aw[idx[0]] * A.aw[idx[1]];
+    if (D == 3) w *= A.aw[idx[2]];
+    double ue[NV];
+    boundary_value<D>(A.ic, A.par, &cur[o * NC + NV], A.t, A.gamma, ue);
+    for (int v = 0; v < NV; ++v) {
+      const double diff = ue[v] - cur[o * NC + v];
+      loc[v] += diff * diff * (w * vj);
+      mx[v] = fmax(mx[v], fabs(diff));
+    }
+  }
+  for (int v = 0; v < NV; ++v) {
+    red[threadIdx.x * 2 * NV + v] = loc[v];
+    red[threadIdx.x * 2 * NV + NV + v] = mx[v];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {  // in thread order: deterministic
+    for (int v = 0; v < NV; ++v) {
+      double sum = 0, m = 0;
+      for (int k = 0; k < (int)blockDim.x; ++k) {
+        sum += red[k * 2 * NV + v];
+        m = fmax(m, red[k * 2 * NV + NV + v]);
+      }
+      partial[(size_t)e * 2 * NV + v] = sum;
+      partial[(size_t)e * 2 * NV + NV + v] = m;
+    }
+  }
+}
+
+// Column sums (k < K) and maxima (K <= k < 2K) of partial[E][2K], each
+// thread's share in element order and then a fixed tree: deterministic.
+__global__ void sum_max_rows_kernel(const double* __restrict__ partial, int64_t E, int K,
+                                    double* __restrict__ out) {
+  extern __shared__ double sh[];
+  for (int k = 0; k < 2 * K; ++k) {
+    const bool is_max = k >= K;
+    double s = 0;
+    for (int64_t e = threadIdx.x; e < E; e += blockDim.x) {
+      const double x = partial[(size_t)e * 2 * K + k];
+      s = is_max ? fmax(s, x) : s + x;
+    }
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w)
+        sh[threadIdx.x] = is_max ? fmax(sh[threadIdx.x], sh[threadIdx.x + w])
+                                 : sh[threadIdx.x] + sh[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[k] = sh[0];
+    __syncthreads();
+  }
+}
+
 // Boundary pre-pass of a mixed context (calc_boundary_flux!, dg_2d.jl:795-860,
 // evaluated for the stage's input state): for every node of every boundary
 // face, in FP64, the Dirichlet state (the initial condition at the node and
@@ -861,6 +981,8 @@ struct tg_ctx {
   double* d_cxy = nullptr;            // fp64 sources: [E][NN][2] node coordinates
   float4* d_csc = nullptr;            // mixed sources: [E][NN] sin/cos(pi (x + y))
   double* d_partial = nullptr;
+  double* d_enorm = nullptr;          // error norms: per-element sums and maxima [E][2 nvar]
+  double total_volume = 0.0;          // sum of the element volumes (TreeMesh: length_level_0^d)
   double* d_sums = nullptr;
   Clock* d_clock = nullptr;
   int32_t* d_status = nullptr;
@@ -914,7 +1036,7 @@ static void free_ctx(tg_ctx* c) {
     if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
   void* ptrs[] = {c->d_u[0], c->d_u[1], c->d_utmp, c->d_du, c->d_uscratch, c->d_stage64,
                   c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_alpha_sm, c->d_nbr, c->d_invj, c->d_xline,
-                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mmat32, c->d_mflux, c->d_scls, c->d_amr_raw, c->d_amr_alpha, c->d_amap, c->d_akind, c->d_weights, c->d_cmet, c->d_cja32, c->d_cinvj32, c->d_cxy, c->d_csc, c->d_partial, c->d_sums, c->d_clock,
+                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mmat32, c->d_mflux, c->d_scls, c->d_amr_raw, c->d_amr_alpha, c->d_amap, c->d_akind, c->d_weights, c->d_cmet, c->d_cja32, c->d_cinvj32, c->d_cxy, c->d_csc, c->d_partial, c->d_enorm, c->d_sums, c->d_clock,
                   c->d_status, c->d_speed};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1612,6 +1734,12 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
         for (int b = 0; b < N; ++b) mmat[(size_t)k * N * N + a * N + b] = src[k][a + b * N];
   }
   ALLOC(c->d_invj, sizeof(double) * c->E);
+  for (int64_t k = 0; k < c->E; ++k) {
+    // element volume (2 / inverse_jacobian)^d: the mesh volume analysis normalises by
+    double h = 2.0 / cfg->inverse_jacobian[k], v = h;
+    for (int d = 1; d < D; ++d) v *= h;
+    c->total_volume += v;
+  }
   ALLOC(c->d_weights, sizeof(double) * N);
   ALLOC(c->d_clock, sizeof(Clock));
   ALLOC(c->d_status, sizeof(int32_t));
@@ -2219,6 +2347,68 @@ int tg_integrals(tg_ctx* c, double* out) {
   CUDA_TRY(c, cudaGetLastError());
   CUDA_TRY(c, cudaMemcpyAsync(out, c->d_sums, sizeof(double) * K, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return TG_OK;
+}
+
+int tg_error_norms(tg_ctx* c, const double* u_dev, double t, int32_t ic, const double* params,
+                   int32_t nanalyzer, const double* analyzer_vandermonde,
+                   const double* analyzer_weights, double* l2, double* linf) {
+  if (!c || !analyzer_vandermonde || !analyzer_weights || !l2 || !linf)
+    return TG_ERR_INVALID_ARGUMENT;
+  if (ic < TG_IC_CONSTANT || ic > TG_IC_GAUSSIAN_BLAST)
+    return fail(c, TG_ERR_UNSUPPORTED, "error norms: the exact solution must be a device initial condition");
+  if (c->curved) return fail(c, TG_ERR_UNSUPPORTED, "error norms: TreeMesh contexts only");
+  if (!c->d_xline) return fail(c, TG_ERR_STATE, "error norms need the node coordinates in the config");
+  if (nanalyzer < 2 || nanalyzer > 2 * MAXN - 1)
+    return fail(c, TG_ERR_INVALID_ARGUMENT, "error norms: analyzer size out of range");
+  if (!u_dev && !c->uploaded) return fail(c, TG_ERR_STATE, "no state uploaded");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  ErrorNormArgs A{};
+  A.N = c->N;
+  A.NA = nanalyzer;
+  A.ic = ic;
+  for (int k = 0; k < 4; ++k) A.par[k] = params ? params[k] : 0.0;
+  A.t = t;
+  A.gamma = c->P.gamma;
+  for (int a = 0; a < nanalyzer; ++a) {
+    A.aw[a] = analyzer_weights[a];
+    for (int k = 0; k < c->N; ++k)  // column-major [nanalyzer, n] as Trixi's analyzer.vandermonde
+      A.avand[a * c->N + k] = analyzer_vandermonde[a + (size_t)k * nanalyzer];
+  }
+  const int NV = c->D + 2, NC = NV + c->D;
+  int nna = nanalyzer;
+  for (int d = 1; d < c->D; ++d) nna *= nanalyzer;
+  const size_t smem = sizeof(double) * ((size_t)2 * nna * NC + 128 * 2 * NV);
+  if (smem > 200 * 1024)
+    return fail(c, TG_ERR_UNSUPPORTED, "error norms: analyzer too large for shared memory");
+  int rc = ensure(c, (void**)&c->d_enorm, sizeof(double) * (size_t)c->E * 2 * NV);
+  if (rc) return rc;
+  const void* u = u_dev ? (const void*)u_dev : c->d_u[c->cur];
+  const bool ff = !u_dev && !c->fp64;
+#define ERRN(DD, TS)                                                                       \
+  {                                                                                        \
+    auto k = error_norms_kernel<DD, TS>;                                                    \
+    CUDA_TRY(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+    k<<<(unsigned)c->E, 128, smem, c->stream>>>((const TS*)u, c->d_xline, c->d_invj, A,      \
+                                                c->d_enorm);                                \
+  }
+  if (c->D == 2) {
+    if (ff) ERRN(2, float2) else ERRN(2, double)
+  } else {
+    if (ff) ERRN(3, float2) else ERRN(3, double)
+  }
+#undef ERRN
+  sum_max_rows_kernel<<<1, 256, 256 * sizeof(double), c->stream>>>(c->d_enorm, c->E, NV,
+                                                                    c->d_sums);
+  CUDA_TRY(c, cudaGetLastError());
+  double h[10];
+  CUDA_TRY(c, cudaMemcpyAsync(h, c->d_sums, sizeof(double) * 2 * NV, cudaMemcpyDeviceToHost,
+                              c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  for (int v = 0; v < NV; ++v) {
+    l2[v] = std::sqrt(h[v] / c->total_volume);
+    linf[v] = h[NV + v];
+  }
   return TG_OK;
 }
 

@@ -33,7 +33,7 @@ EXPORTS = ("tg_api_version", "tg_ctx_create", "tg_ctx_destroy", "tg_last_error",
            "tg_rhs_host", "tg_max_dt", "tg_rk_stage", "tg_rk_stage_part", "tg_step", "tg_set_time",
            "tg_integrals", "tg_alpha", "tg_status", "tg_synchronize",
            "tg_elements_per_block", "tg_stream", "tg_integrals_noalloc",
-           "tg_vector_create", "tg_vector_destroy", "tg_vector_copy", "tg_lincomb", "tg_fma_peak",
+           "tg_vector_create", "tg_vector_destroy", "tg_vector_copy", "tg_lincomb", "tg_fma_peak", "tg_error_norms",
            "tg_mlp_create", "tg_mlp_destroy", "tg_mlp_nparams", "tg_mlp_get_params",
            "tg_mlp_set_params", "tg_mlp_harvest", "tg_mlp_dataset", "tg_mlp_train",
            "tg_mlp_gradient", "tg_mlp_predict", "tg_ctx_set_learned_indicator", "tg_mlp_last",
@@ -152,6 +152,7 @@ def load(path: str | None = None):
         "tg_vector_copy": ([vp, vp, vp, i64, i32], ctypes.c_int),
         "tg_lincomb": ([vp, i64, vp, d, vp, d, vp], ctypes.c_int),
         "tg_fma_peak": ([i32, pd], ctypes.c_int),
+        "tg_error_norms": ([vp, vp, d, i32, pd, i32, pd, pd, pd, pd], ctypes.c_int),
         "tg_integrals_noalloc": ([i32, i32, i64, d, pd, vp, vp, vp, vp], ctypes.c_int),
         "tg_mlp_create": ([i32, i32, i32, ctypes.c_uint64, P(vp)], ctypes.c_int),
         "tg_mlp_destroy": ([vp], ctypes.c_int),

@@ -9,7 +9,11 @@ from .basis import LobattoLegendreAnalyzer
 def calc_error_norms(u, t, semi, analyzer: LobattoLegendreAnalyzer | None = None,
                      exact=None, chunk=4096):
     """L2 and Linf errors of the conservative variables against the initial
-    condition at time t (or `exact`), on the (2N+1)-node analyzer."""
+    condition at time t (or `exact`), on the (2N+1)-node analyzer.  u is None:
+    the device context's state, evaluated on the device (tg_error_norms, no
+    download); otherwise a host array, evaluated here in numpy."""
+    if u is None:
+        return semi.device_context.error_norms(t, exact=exact, analyzer=analyzer)
     if analyzer is None:
         analyzer = LobattoLegendreAnalyzer(semi.solver.basis)
     exact = exact or semi.initial_condition

@@ -291,6 +291,31 @@ class DeviceContext:
         self._check(self.lib.tg_integrals(self.h, _dptr(out)))
         return out
 
+    def error_norms(self, t, exact=None, u=None, analyzer=None):
+        """calc_error_norms on the device (tg_error_norms): L2 and Linf errors of
+        the context state (or of `u`, device buffer) against `exact` (default:
+        the semidiscretization's initial condition) at time t, on the
+        (2N+1)-node analyzer.  `exact` must be one of the package's initial
+        conditions (they run on the device)."""
+        from .basis import LobattoLegendreAnalyzer
+        f = exact or self.semi.initial_condition
+        name = getattr(f, "__name__", None)
+        if name not in _IC_CODES:
+            raise NotImplementedError(f"error norms on the device against {name!r}: only the "
+                                      "package's initial conditions run on the device")
+        an = analyzer or LobattoLegendreAnalyzer(self.semi.solver.basis)
+        vand = np.ascontiguousarray(np.asfortranarray(an.vandermonde).ravel(order="F"))
+        w = np.ascontiguousarray(an.weights, dtype=np.float64)
+        par = np.zeros(4)
+        for k, v in enumerate(getattr(f, "params", ())):
+            par[k] = v
+        nv = self.semi.equations.nvariables
+        l2, linf = np.zeros(nv), np.zeros(nv)
+        self._check(self.lib.tg_error_norms(self.h, None if u is None else _ptr_of(u), float(t),
+                                            _IC_CODES[name], _dptr(par), len(w), _dptr(vand),
+                                            _dptr(w), _dptr(l2), _dptr(linf)))
+        return l2, linf
+
     def entropy_timederivative(self, t=0.0) -> float:
         """Normalised integral of cons2entropy(u) . rhs(u, t) of the device state."""
         out = ctypes.c_double()
