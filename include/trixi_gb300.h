@@ -101,7 +101,7 @@ typedef enum tg_precision {
 } tg_precision;
 
 /* Mesh of a context: TreeMesh (Cartesian elements, per-element Jacobian) or a
- * curvilinear 2D StructuredMesh / P4estMesh brick (per-node metric terms). */
+ * curvilinear StructuredMesh / P4estMesh brick (per-node metric terms). */
 typedef enum tg_mesh_type {
   TG_MESH_TREE = 0,
   TG_MESH_CURVED = 1
@@ -205,7 +205,8 @@ typedef struct tg_config {
    * cache.elements.inverse_jacobian ([n, n, nelements], :136-152).
    * node_coordinates is [2, n, n, nelements].  Edges of the brick are periodic
  * or take TG_BOUNDARY_DIRICHLET (slip walls are not built for these meshes).
- * 3D StructuredMesh (FP64, weak form, polydeg 3; dgsem_structured/dg_3d.jl,
+ * 3D StructuredMesh (FP64, weak form or flux differencing, polydeg 3 or 5;
+ * dgsem_structured/dg_3d.jl,
  * containers_3d.jl:67-286): contravariant_vectors [3, 3, n, n, n, nelements]
  * in the curl form, inverse_jacobian [n, n, n, nelements], node_coordinates
  * [3, n, n, n, nelements], reference directions 1..3. */

@@ -114,6 +114,7 @@ def _load():
     lib.orc_curved_destroy.argtypes = [vp]
     lib.orc_curved_set_dirichlet.argtypes = [vp, i, P(d)]
     lib.orc_curved_set_hg.argtypes = [vp, d, d, i, i]
+    lib.orc_curved_alpha.argtypes = [vp, P(d), P(d)]
     lib.orc_curved_metric.argtypes = [vp, P(d), P(d)]
     lib.orc_curved_initial_condition.argtypes = [vp, i, P(d), d, P(d)]
     lib.orc_curved_rhs.argtypes = [vp, P(d), P(d), d]
@@ -449,6 +450,12 @@ class CurvedOracle:
         """IndicatorHennemannGassner(density_pressure) parameters and the FV flux of
         a VI_SHOCKCAPTURING_HG solver."""
         _lib.orc_curved_set_hg(self.h, alpha_max, alpha_min, int(alpha_smooth), fv_flux)
+
+    def alpha(self, u):
+        """Smoothed blending factors of state u (after set_hg)."""
+        a = np.empty(self.E)
+        _lib.orc_curved_alpha(self.h, _p(np.ascontiguousarray(u, dtype=np.float64)), _p(a))
+        return a
 
     def set_dirichlet(self, ic, params=None):
         """BoundaryConditionDirichlet(initial condition ic) on every face without a

@@ -2848,6 +2848,13 @@ void orc_curved_set_hg(void* h, double alpha_max, double alpha_min, int alpha_sm
   curved_subcell_normals(c);
 }
 
+// Smoothed blending factors of a state (VI_SHOCKCAPTURING_HG), alpha[E]
+void orc_curved_alpha(void* h, const double* u, double* alpha) {
+  std::vector<double> a;
+  curved_hg_alpha(*(const Curved*)h, u, a);
+  std::copy(a.begin(), a.end(), alpha);
+}
+
 // Dirichlet values (an initial condition and its parameters) of the faces
 // without a neighbour
 void orc_curved_set_dirichlet(void* h, int ic, const double* params) {
@@ -2968,6 +2975,23 @@ static inline void two_point3_n(const Eq& eq, int kind, const double* ul, const 
       f[0] = f1;
       for (int d = 0; d < 3; ++d) f[1 + d] = std::fma(f1, vavg[d], p_avg * n[d]);
       f[4] = f1 * vsq + p_avg * vn_avg * eq.inv_gamma_minus_one + 0.5 * (a[4] * vnb + b[4] * vna);
+      return;
+    }
+    case FLUX_CHANDRASHEKAR: {
+      // compressible_euler_3d.jl:693-729
+      const double beta_a = 0.5 * a[0] / a[4], beta_b = 0.5 * b[0] / b[4];
+      const double kin_a = 0.5 * (a[1] * a[1] + a[2] * a[2] + a[3] * a[3]);
+      const double kin_b = 0.5 * (b[1] * b[1] + b[2] * b[2] + b[3] * b[3]);
+      const double rho_avg = 0.5 * (a[0] + b[0]);
+      const double rho_mean = ln_mean(a[0], b[0]);
+      const double beta_mean = ln_mean(beta_a, beta_b);
+      const double beta_avg = 0.5 * (beta_a + beta_b);
+      const double p_mean = 0.5 * rho_avg / beta_avg;
+      const double f1 = rho_mean * 0.5 * (vna + vnb);
+      f[0] = f1;
+      for (int d = 0; d < 3; ++d) f[1 + d] = f1 * vavg[d] + p_mean * n[d];
+      f[4] = f1 * 0.5 * (1 / (eq.gamma - 1) / beta_mean - (kin_a + kin_b)) + f[1] * vavg[0] +
+             f[2] * vavg[1] + f[3] * vavg[2];
       return;
     }
     default: break;

@@ -11,9 +11,9 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 GOLDENS = load_curved_goldens()
-# the GPU path runs 2D curvilinear meshes (3D goldens pin the oracle only)
+# the 2D goldens (the 3D ones below), shock capturing included
 FP64_GOLDENS = sorted(k for k, v in GOLDENS.items()
-                      if not v.get("float32") and v.get("ndims", 2) == 2 and v["vi"] != "hg")
+                      if not v.get("float32") and v.get("ndims", 2) == 2)
 
 
 def build(c, precision="fp64", cells=None):
@@ -23,12 +23,19 @@ def build(c, precision="fp64", cells=None):
     sflux = FLUX[c["surface_flux"]][0]
     if c["vi"] == "weak":
         vi = T.VolumeIntegralWeakForm()
-    else:
+    elif c["vi"] == "fluxdiff":
         vi = T.VolumeIntegralFluxDifferencing(FLUX[c["volume_flux"]][0])
+    else:
+        ind = T.IndicatorHennemannGassner(eq, basis, alpha_max=c["alpha_max"],
+                                          alpha_min=c["alpha_min"], alpha_smooth=c["alpha_smooth"],
+                                          variable=T.density_pressure)
+        vi = T.VolumeIntegralShockCapturingHG(ind, volume_flux_dg=FLUX[c["volume_flux"]][0],
+                                              volume_flux_fv=FLUX[c["volume_flux_fv"]][0])
     solver = T.DGSEM(basis, sflux, vi)
     mesh = curved_mesh(c, cells)
     ic = {"convergence_test": T.initial_condition_convergence_test,
           "weak_blast_wave": T.initial_condition_weak_blast_wave,
+          "sedov_blast_wave": T.initial_condition_sedov_blast_wave,
           "constant": T.initial_condition_constant}[c["ic"]]
     src = T.source_terms_convergence_test if c.get("source") == "convergence_test" else None
     bcs = (T.BoundaryConditionDirichlet(ic) if c.get("boundary") == "dirichlet"
@@ -46,6 +53,11 @@ PAR = "StructuredMesh2D: elixir_euler_source_terms_parallelogram.jl"
 FLAG = "StructuredMesh2D: elixir_euler_source_terms_waving_flag.jl"
 EC = "StructuredMesh2D: elixir_euler_ec.jl"
 P4 = "CUDA 2D: elixir_euler_source_terms.jl native"
+P4SC = "P4estMesh2D: elixir_euler_shockcapturing_ec.jl"
+P4SC_CH = "P4estMesh2D: elixir_euler_shockcapturing_ec.jl (flux_chandrashekar)"
+SEDOV = "StructuredMesh2D: elixir_euler_sedov.jl"
+HG_FLAG = dict(vi="hg", volume_flux="ranocha", surface_flux="llf", volume_flux_fv="llf",
+               alpha_max=0.5, alpha_min=0.001, alpha_smooth=True)
 RHS_CASES = [
     _case(PAR),
     _case(FLAG),
@@ -58,12 +70,21 @@ RHS_CASES = [
     # Dirichlet faces on a curved boundary
     _case(FLAG, boundary="dirichlet"),
     _case(FLAG, boundary="dirichlet", vi="fluxdiff", volume_flux="ranocha", surface_flux="llf"),
+    # shock capturing: the P4estMesh EC elixirs (ranocha / chandrashekar, FV
+    # ranocha), Sedov on the warped square (FV llf_naive), a smooth state with
+    # Dirichlet faces and an unsmoothed indicator
+    _case(P4SC, trees=[4, 4], level=1),
+    _case(P4SC_CH, trees=[3, 4], level=1),
+    _case(SEDOV),
+    _case(SEDOV, polydeg=3, alpha_smooth=False, volume_flux="shima_etal"),
+    _case(FLAG, boundary="dirichlet", **HG_FLAG),
 ]
 
 
 def _id(c):
     return (f"{c['mesh']}-{c['mapping']}-{c['vi']}-{c['volume_flux']}-{c['surface_flux']}"
-            f"-p{c['polydeg']}" + ("-dirichlet" if c.get("boundary") else ""))
+            + (f"-fv_{c['volume_flux_fv']}" if c["vi"] == "hg" else "")
+            + f"-p{c['polydeg']}" + ("-dirichlet" if c.get("boundary") else ""))
 
 
 @pytest.mark.parametrize("c", RHS_CASES, ids=_id)
@@ -166,17 +187,52 @@ def test_curved_mixed_beats_reference_float32_gpu_run():
     np.testing.assert_allclose(ana.l2, c64["l2"], rtol=1e-3)
 
 
+HG_CASES = [c for c in RHS_CASES if c["vi"] == "hg"]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("c", HG_CASES, ids=_id)
+def test_curved_hg_alpha_matches_oracle(c, precision):
+    # IndicatorHennemannGassner on density_pressure with apply_smoothing! over
+    # the curvilinear face neighbours; mixed: FP32 indicator on the state's
+    # FP32 value (the logistic's slope turns its rounding into up to ~1e-3 of
+    # alpha_max near the threshold)
+    semi, orc = build(c, precision, cells=(12, 10) if c["mesh"] == "structured" else None)
+    u = perturbed_state(semi, seed=5)
+    ctx = semi.device_context
+    ctx.upload(u)
+    a_gpu, a_orc = ctx.alpha(), orc.alpha(u)
+    assert np.any(a_orc > 0)
+    tol = 1e-12 if precision == "fp64" else 1e-2 * c["alpha_max"]
+    assert np.max(np.abs(a_gpu - a_orc)) < tol
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_curved_hg_time_steps_match_oracle(precision):
+    c = _case(SEDOV)
+    semi, orc = build(c, precision, cells=(12, 10))
+    u0 = semi.compute_coefficients(0.0)
+    ctx = semi.device_context
+    ctx.upload(u0)
+    t, n = ctx.step(8, c["cfl"], 10.0, 0.0)
+    u_orc, t_orc, n_orc = orc.solve(u0, 0.0, 10.0, c["cfl"], max_steps=8)
+    assert n == n_orc == 8
+    assert t == pytest.approx(t_orc, rel=1e-12 if precision == "fp64" else 1e-5)
+    assert rel_err(ctx.download(), u_orc) < (1e-12 if precision == "fp64" else 1e-5)
+
+
+@pytest.mark.parametrize("name", [P4SC, SEDOV])
+def test_curved_hg_mixed_golden(name):
+    # shock capturing in mixed precision stays on the FP64 elixir's golden
+    c = dict(GOLDENS[name])
+    _, ana = _golden_run(c, "mixed")
+    np.testing.assert_allclose(ana.l2, c["l2"], rtol=1e-3)
+
+
 def test_curved_unsupported_options_fail_loudly():
     c = _case(EC)
     eq = T.CompressibleEulerEquations2D(1.4)
     basis = T.LobattoLegendreBasis(3)
-    ind = T.IndicatorHennemannGassner(eq, basis, alpha_max=0.5, alpha_min=0.001, alpha_smooth=True,
-                                      variable=T.density_pressure)
-    vi = T.VolumeIntegralShockCapturingHG(ind, volume_flux_dg=T.flux_ranocha,
-                                          volume_flux_fv=T.flux_lax_friedrichs)
-    with pytest.raises(NotImplementedError):
-        T.SemidiscretizationHyperbolic(curved_mesh(c, (4, 4)), eq, T.initial_condition_constant,
-                                       T.DGSEM(basis, T.flux_lax_friedrichs, vi))
     semi = T.SemidiscretizationHyperbolic(curved_mesh(c, (4, 4)), eq, T.initial_condition_constant,
                                           T.DGSEM(basis, T.flux_hllc))
     with pytest.raises(T.TrixiGB300Error):
@@ -206,13 +262,23 @@ FREE3 = "StructuredMesh3D: elixir_euler_free_stream.jl"
 EC3 = "StructuredMesh3D: elixir_euler_ec.jl"
 NONP3 = "StructuredMesh3D: elixir_euler_source_terms_nonperiodic_curved.jl"
 SRC3 = "StructuredMesh3D: elixir_euler_source_terms.jl"
-# the 3D path runs the weak form at polydeg 3 (the configuration of these goldens)
+# the 3D path runs the weak form and flux differencing at polydeg 3 and 5: every
+# StructuredMesh3D golden (EC3 is flux_ranocha flux differencing at polydeg 5)
 GOLDENS_3D = sorted(k for k, v in GOLDENS.items()
-                    if v.get("ndims", 2) == 3 and v["vi"] == "weak" and v["polydeg"] == 3)
+                    if v.get("ndims", 2) == 3 and v["vi"] in ("weak", "fluxdiff")
+                    and v["polydeg"] in (3, 5))
 RHS_CASES_3D = [
     (_case(FREE3, ic="convergence_test", source="convergence_test"), (4, 4, 4)),
     (_case(FREE3, ic="convergence_test", source="convergence_test", surface_flux="llf"), (4, 4, 4)),
     (_case(NONP3), (3, 2, 2)),                                  # Dirichlet faces
+    (_case(FREE3, polydeg=5, ic="convergence_test", source="convergence_test"), (4, 4, 4)),
+    # flux differencing: the EC elixir (ranocha / ranocha, polydeg 5, gamma 5/3)
+    # and each two-point volume flux at polydeg 3
+    (_case(EC3), (4, 4, 4)),
+    (_case(EC3, polydeg=3, volume_flux="shima_etal", surface_flux="llf"), (4, 4, 4)),
+    (_case(EC3, polydeg=3, volume_flux="chandrashekar", surface_flux="llf_naive"), (4, 4, 4)),
+    (_case(EC3, polydeg=3, volume_flux="central", surface_flux="central"), (4, 4, 4)),
+    (_case(NONP3, vi="fluxdiff", volume_flux="ranocha", surface_flux="llf"), (3, 2, 2)),
 ]
 
 
@@ -253,10 +319,24 @@ def test_curved3_gpu_fp64_reproduces_trixi_goldens(name):
     np.testing.assert_allclose(ana.linf, c["linf"], rtol=1e-7)
 
 
-def test_curved3_mixed_and_flux_differencing_are_rejected():
+def test_curved3_fd_steps_match_oracle():
+    # five CK2N54 steps of the EC elixir through the fused stage kernel, with
+    # the CFL reduction inside it
+    c = _case(EC3)
+    semi, orc = build(c, cells=(4, 4, 4))
+    u0 = semi.compute_coefficients(0.0)
+    ctx = semi.device_context
+    ctx.upload(u0)
+    t, n = ctx.step(5, c["cfl"], 10.0, 0.0)
+    u_orc, t_orc, n_orc = orc.solve(u0, 0.0, 10.0, c["cfl"], max_steps=5)
+    assert n == n_orc == 5 and t == pytest.approx(t_orc, rel=1e-12)
+    assert rel_err(ctx.download(), u_orc) < 1e-12
+
+
+def test_curved3_mixed_and_other_degrees_are_rejected():
     semi, _ = build(_case(SRC3), precision="mixed", cells=(2, 2, 2))
     with pytest.raises(T.TrixiGB300Error):
         semi.device_context
-    semi, _ = build(_case(EC3), cells=(4, 4, 4))
+    semi, _ = build(_case(EC3, polydeg=4), cells=(2, 2, 2))
     with pytest.raises(T.TrixiGB300Error):
         semi.device_context

@@ -976,6 +976,8 @@ struct tg_ctx {
   bool curved = false;
   tg::CurvedParams CP{};
   double* d_cmet = nullptr;           // [E][NN][5]: Ja^1, Ja^2, inverse Jacobian
+  double2* d_csnv = nullptr;          // HG: subcell normals [E][2][N][N - 1]
+  float2* d_csnv32 = nullptr;         // mixed HG: their FP32 copy
   float4* d_cja32 = nullptr;          // mixed: [E][NN] Ja^1, Ja^2
   float* d_cinvj32 = nullptr;         // mixed: [E][NN] inverse Jacobian
   double* d_cxy = nullptr;            // fp64 sources: [E][NN][2] node coordinates
@@ -1036,7 +1038,7 @@ static void free_ctx(tg_ctx* c) {
     if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
   void* ptrs[] = {c->d_u[0], c->d_u[1], c->d_utmp, c->d_du, c->d_uscratch, c->d_stage64,
                   c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_alpha_sm, c->d_nbr, c->d_invj, c->d_xline,
-                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mmat32, c->d_mflux, c->d_scls, c->d_amr_raw, c->d_amr_alpha, c->d_amap, c->d_akind, c->d_weights, c->d_cmet, c->d_cja32, c->d_cinvj32, c->d_cxy, c->d_csc, c->d_partial, c->d_enorm, c->d_sums, c->d_clock,
+                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mmat32, c->d_mflux, c->d_scls, c->d_amr_raw, c->d_amr_alpha, c->d_amap, c->d_akind, c->d_weights, c->d_cmet, c->d_csnv, c->d_csnv32, c->d_cja32, c->d_cinvj32, c->d_cxy, c->d_csc, c->d_partial, c->d_enorm, c->d_sums, c->d_clock,
                   c->d_status, c->d_speed};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1155,6 +1157,8 @@ static int launch_kernel(tg_ctx* c, int mode, const void* u_in, void* u_out, dou
     A.u_tmp = c->d_utmp;
     M.u_tmp = (float*)c->d_utmp;
     A.t_rhs = M.t_rhs = t_rhs;
+    A.alpha_raw = c->d_alpha_raw;
+    M.alpha_raw = (const float*)c->d_alpha_raw;
     if (mode == MODE_STAGE) {
       A.a = M.a = CK_A[stage];
       A.b = M.b = CK_B[stage];
@@ -1349,6 +1353,52 @@ static int curved_setup(tg_ctx* c, const tg_config* cfg) {
     CUDA_TRY(nullptr, cudaMemcpy(c->d_cxy, cfg->node_coordinates, sizeof(double) * nq * D,
                                  cudaMemcpyHostToDevice));
   }
+  if (c->vi == VI_HG) {
+    // calc_normalvectors_subcell_fv! (dgsem_structured/containers_2d.jl:200-298):
+    // the normal of the subcell interface between nodes i and i + 1 of a line
+    // is Ja at the line's first node plus the partial sums of w_m D[m, :] Ja
+    // along the line (D: polynomial_derivative_matrix by barycentric weights,
+    // Kopriva, Implementing Spectral Methods, algorithm 37)
+    const double* x = cfg->nodes;
+    std::vector<double> wb(N, 1.0), Dm((size_t)N * N, 0.0);
+    for (int j = 0; j < N; ++j)
+      for (int k = 0; k < N; ++k)
+        if (k != j) wb[j] /= x[j] - x[k];
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j)
+        if (j != i) {
+          Dm[i * N + j] = (wb[j] / wb[i]) / (x[i] - x[j]);
+          Dm[i * N + i] -= Dm[i * N + j];
+        }
+    const size_t nsv = (size_t)E * 2 * N * (N - 1);
+    std::vector<double2> snv(nsv);
+    for (int64_t e = 0; e < E; ++e)
+      for (int dd = 0; dd < 2; ++dd)
+        for (int l = 0; l < N; ++l) {
+          auto ja = [&](int a, int xy) {
+            const int q = dd == 0 ? a + N * l : l + N * a;
+            return met[((size_t)e * NN + q) * MS + 2 * dd + xy];
+          };
+          double acc[2] = {ja(0, 0), ja(0, 1)};
+          for (int i = 0; i < N - 1; ++i) {
+            for (int m = 0; m < N; ++m) {
+              const double wd = cfg->weights[i] * Dm[i * N + m];
+              for (int xy = 0; xy < 2; ++xy) acc[xy] += wd * ja(m, xy);
+            }
+            snv[(((size_t)e * 2 + dd) * N + l) * (N - 1) + i] = make_double2(acc[0], acc[1]);
+          }
+        }
+    CUDA_TRY(nullptr, cudaMalloc((void**)&c->d_csnv, sizeof(double2) * nsv));
+    CUDA_TRY(nullptr, cudaMemcpy(c->d_csnv, snv.data(), sizeof(double2) * nsv,
+                                 cudaMemcpyHostToDevice));
+    if (!c->fp64) {
+      std::vector<float2> snv32(nsv);
+      for (size_t k = 0; k < nsv; ++k) snv32[k] = make_float2((float)snv[k].x, (float)snv[k].y);
+      CUDA_TRY(nullptr, cudaMalloc((void**)&c->d_csnv32, sizeof(float2) * nsv));
+      CUDA_TRY(nullptr, cudaMemcpy(c->d_csnv32, snv32.data(), sizeof(float2) * nsv,
+                                   cudaMemcpyHostToDevice));
+    }
+  }
   tg::CurvedParams& C = c->CP;
   C.nelements = E;
   C.N = N;
@@ -1379,6 +1429,11 @@ static int curved_setup(tg_ctx* c, const tg_config* cfg) {
   for (int k = 0; k < 4; ++k) C.bc_par[k] = c->P.bc_par[k];
   C.bface = c->d_bface;
   C.ghost = c->d_ghost;
+  C.fv_flux = c->P.fv_flux;
+  C.alpha_smooth = c->P.alpha_smooth;
+  C.alpha_atol = c->P.alpha_atol;
+  C.snv = c->d_csnv;
+  C.snv32 = c->d_csnv32;
   return TG_OK;
 }
 
@@ -1470,18 +1525,18 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     if (D == 3 && mixed)
       return fail(nullptr, TG_ERR_UNSUPPORTED,
                   "3D curvilinear meshes: FP64 only (the mixed path runs 2D curvilinear meshes)");
-    // 3D: tg_curved3.cu is built for the weak form at polydeg 3
-    if (D == 3 && (cfg->volume_integral != TG_VOLUME_WEAK_FORM || N != 4))
-      return fail(nullptr, TG_ERR_UNSUPPORTED,
-                  "3D curvilinear meshes: weak form at polydeg 3 only");
+    // 3D: tg_curved3.cu is built for polydeg 3 and 5, weak form or flux differencing
     if (D == 2 ? tg::curved_epb(N) == 0 : !tg::curved3_supported(N))
       return fail(nullptr, TG_ERR_UNSUPPORTED, "curvilinear meshes: polydeg %d is not compiled",
                   cfg->polydeg);
-    if (cfg->volume_integral == TG_VOLUME_SHOCK_CAPTURING_HG)
+    const bool hg = cfg->volume_integral == TG_VOLUME_SHOCK_CAPTURING_HG;
+    if (hg && D == 3)
       return fail(nullptr, TG_ERR_UNSUPPORTED,
-                  "curvilinear meshes: weak form or flux differencing only");
+                  "3D curvilinear meshes: weak form or flux differencing only");
     const int vf = cfg->volume_flux, sf = cfg->surface_flux;
-    if (cfg->volume_integral == TG_VOLUME_FLUX_DIFFERENCING &&
+    if (hg && (cfg->volume_flux_fv == TG_FLUX_HLLC || cfg->volume_flux_fv == TG_FLUX_HLLE))
+      return fail(nullptr, TG_ERR_UNSUPPORTED, "curvilinear meshes: FV flux_hllc / flux_hlle");
+    if ((cfg->volume_integral == TG_VOLUME_FLUX_DIFFERENCING || hg) &&
         vf != TG_FLUX_CENTRAL && vf != TG_FLUX_RANOCHA && vf != TG_FLUX_SHIMA_ETAL &&
         vf != TG_FLUX_CHANDRASHEKAR)
       return fail(nullptr, TG_ERR_UNSUPPORTED,

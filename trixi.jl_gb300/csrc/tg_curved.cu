@@ -7,9 +7,11 @@
 // accumulating the line's node contributions in registers; a node phase sums
 // the two directions, applies the per-node inverse Jacobian and the sources
 // and performs the 2N stage update.  Each interface flux is evaluated by both
-// elements, along their own contravariant vector of the shared face (equal up
-// to the rounding of the node coordinates the metric was built from), with
-// the element on the negative side as the left state.
+// elements with the element on the negative side as the left state: the FP64
+// kernel along the contravariant vector of the element on the positive side
+// (as Trixi, so both elements evaluate the same flux), the mixed kernel along
+// its own element's vector of the shared face (equal up to the rounding of
+// the node coordinates the metric was built from).
 //
 // The mixed kernel evaluates the fluxes in deviation form relative to a
 // per-element reference state as the TreeMesh mixed kernel does.  The
@@ -201,6 +203,7 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT)
   double* s_fu = s_u + CHUNK;
   double* s_part = s_fu + K::FACE;                       // [2][NV][SP]
   unsigned long long* s_smax = reinterpret_cast<unsigned long long*>(s_part + 2 * NV * SP);
+  double* s_alpha = reinterpret_cast<double*>(s_smax + 2 * EPB);  // [EPB] (VI_HG)
 
   const int tid = threadIdx.x;
   const int64_t e0 = (int64_t)blockIdx.x * EPB;
@@ -235,6 +238,20 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT)
     for (int v = 0; v < NV; ++v) s_fu[k * NV + v] = __ldg(g + v);
   }
   if (tid < 2 * EPB) s_smax[tid] = 0ull;
+  if (VI == VI_HG && tid < nel) {
+    // apply_smoothing! as a gather (indicators_2d.jl:104-136)
+    const double* raw = static_cast<const double*>(A.alpha_raw);
+    const int64_t e = e0 + tid;
+    double a = raw[e];
+    if (P.alpha_smooth)
+#pragma unroll
+      for (int f = 0; f < 4; ++f) {
+        const int32_t nb = P.nbr[e * 4 + f];
+        if (nb >= 0) a = fmax(a, 0.5 * raw[nb]);
+      }
+    s_alpha[tid] = a;
+    if (A.alpha_out) static_cast<double*>(A.alpha_out)[e] = a;
+  }
   __syncthreads();
 
   // ---- lines ---------------------------------------------------------------------
@@ -289,6 +306,35 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT)
             }
           }
       }
+      if (VI == VI_HG) {
+        // VolumeIntegralShockCapturingHG (calc_volume_integral.jl:231-272):
+        // flux differencing weighted by 1 - alpha, the FV subcell fluxes of
+        // the line (fv_kernel!, calcflux_fv!, dgsem_structured/dg_2d.jl:
+        // 304-345) by alpha; the subcell fluxes at the element faces are zero
+        const double ae = s_alpha[sl];
+        if (!(fabs(ae) <= P.alpha_atol)) {
+#pragma unroll
+          for (int a = 0; a < N; ++a)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[a][v] *= 1.0 - ae;
+          const double2* nv = P.snv + (((size_t)e * 2 + dd) * N + line) * (N - 1);
+          double fl[NV] = {0.0, 0.0, 0.0, 0.0};  // subcell flux on the node's lower side
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            double fr[NV] = {0.0, 0.0, 0.0, 0.0};
+            if (i < N - 1) {
+              const double2 n = nv[i];
+              FluxN::two_point(P.fv_flux, uu[i], ww[i], uu[i + 1], ww[i + 1], n.x, n.y, gamma,
+                               igm1, fr);
+            }
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+              acc[i][v] += ae * (P.inv_weights[i] * (fr[v] - fl[v]));
+              fl[v] = fr[v];
+            }
+          }
+        }
+      }
       // faces -dd (node 0) and +dd (node N-1), along this element's
       // contravariant vector, negative-side element as the left state
       const double factor = P.inv_weights[0];
@@ -304,10 +350,19 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT)
 #pragma unroll
         for (int v = 0; v < NV; ++v) un[v] = src[v];
         Eu::cons2prim(un, wn, gamma);
-        if (side)
-          FluxN::two_point(P.surface_flux, uu[own], ww[own], un, wn, ja[own][0], ja[own][1], gamma,
-                           igm1, F);
-        else
+        if (side) {
+          // an interface takes the contravariant vector of the element on its
+          // positive side (calc_interface_flux!, dgsem_structured/dg_2d.jl:
+          // 551-606), so both elements evaluate the same flux; boundary faces
+          // take their own
+          double n0 = ja[own][0], n1 = ja[own][1];
+          if (nb >= 0) {
+            const double* m = P.met + ((size_t)nb * NN + cface_partner<N>(dir, line)) * 5 + 2 * dd;
+            n0 = m[0];
+            n1 = m[1];
+          }
+          FluxN::two_point(P.surface_flux, uu[own], ww[own], un, wn, n0, n1, gamma, igm1, F);
+        } else
           FluxN::two_point(P.surface_flux, un, wn, uu[own], ww[own], ja[own][0], ja[own][1], gamma,
                            igm1, F);
 #pragma unroll
@@ -499,6 +554,7 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT, CurvedK<N, EPB>::MINB_MIX
   RefState<2>* s_ref = reinterpret_cast<RefState<2>*>(s_part + 2 * NV * SP);
   float* s_scal = reinterpret_cast<float*>(s_ref + EPB);    // b dt, a (hi, lo)
   unsigned int* s_smax = reinterpret_cast<unsigned int*>(s_scal + 4);
+  float* s_alpha = reinterpret_cast<float*>(s_smax + 2 * EPB);  // [EPB] (VI_HG)
 
   const int tid = threadIdx.x;
   const int64_t e0 = (int64_t)blockIdx.x * EPB;
@@ -562,6 +618,19 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT, CurvedK<N, EPB>::MINB_MIX
 #pragma unroll
     for (int v = 0; v < NV; ++v) hi[v] = 0.5f * (ue[v].x + ue[(NN - 1) * NV + v].x);
     Dv::make_ref(hi, eos, s_ref[tid]);
+    if (VI == VI_HG) {
+      // apply_smoothing! as a gather (indicators_2d.jl:104-136)
+      const int64_t e = e0 + tid;
+      float a = A.alpha_raw[e];
+      if (P.alpha_smooth)
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+          const int32_t nb = P.nbr[e * 4 + f];
+          if (nb >= 0) a = fmaxf(a, 0.5f * A.alpha_raw[nb]);
+        }
+      s_alpha[tid] = a;
+      if (A.alpha_out) A.alpha_out[e] = a;
+    }
   }
   cp_async_wait_all();
   __syncthreads();
@@ -647,6 +716,37 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT, CurvedK<N, EPB>::MINB_MIX
               acc[b][v] = fmaf(cba, F[v], acc[b][v]);
             }
           }
+      }
+      if (VI == VI_HG) {
+        // the FP64 kernel's blend in deviation form: the subcell flux
+        // deviations F - f(w_ref) . n along the subcell normals, zero at the
+        // element faces.  The dropped reference terms of the FD, FV and
+        // surface parts cancel as for the unblended scheme: both volume
+        // integrals are free-stream preserving with the same surface fluxes
+        const float ae = s_alpha[sl];
+        if (!(fabsf(ae) <= (float)P.alpha_atol)) {
+#pragma unroll
+          for (int a = 0; a < N; ++a) {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[a][v] *= 1.0f - ae;
+            Dv::node_du(s_u + ((size_t)sl * NN + cline_node<N>(line, dd, a)) * NV, R, nd[a].du);
+          }
+          const float2* nv = P.snv32 + (((size_t)e * 2 + dd) * N + line) * (N - 1);
+          float fl[NV] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            float fr[NV] = {0.0f, 0.0f, 0.0f, 0.0f};
+            if (i < N - 1) {
+              const float2 n = nv[i];
+              dev_surface_n(P.fv_flux, R, nd[i], nd[i + 1], n.x, n.y, eos, fr);
+            }
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+              acc[i][v] = fmaf(ae, P.inv_weights32[i] * (fr[v] - fl[v]), acc[i][v]);
+              fl[v] = fr[v];
+            }
+          }
+        }
       }
       const float factor = P.inv_weights32[0];
 #pragma unroll
@@ -859,7 +959,7 @@ static int launch_curved_n(const CurvedParams& P, const StageArgs* A64, const Mi
   const unsigned nb = (unsigned)((P.nelements + EPB - 1) / EPB);
   if (A64) {
     const size_t smem = sizeof(double) * (K::CHUNK + K::FACE + 2 * 4 * K::SP) +
-                        sizeof(unsigned long long) * 2 * EPB;
+                        sizeof(unsigned long long) * 2 * EPB + sizeof(double) * EPB;
     static bool attr = false;
     if (!attr) {
       cudaFuncSetAttribute(curved_kernel_f64<N, VI, EPB>,
@@ -872,7 +972,7 @@ static int launch_curved_n(const CurvedParams& P, const StageArgs* A64, const Mi
                         sizeof(float) * (4 * K::SP + K::SP) +
                         sizeof(float) * ((4 + 1) * K::SP + 2 * 4 * K::SP) +
                         sizeof(RefState<2>) * EPB + sizeof(float) * 4 +
-                        sizeof(unsigned int) * 2 * EPB;
+                        sizeof(unsigned int) * 2 * EPB + sizeof(float) * EPB;
     static bool attr = false;
     if (!attr) {
       cudaFuncSetAttribute(curved_kernel_mixed<N, VI, EPB>,
@@ -887,16 +987,30 @@ static int launch_curved_n(const CurvedParams& P, const StageArgs* A64, const Mi
 int launch_curved(const CurvedParams& P, const StageArgs* A64, const MixedArgs* A32,
                   cudaStream_t stream) {
   if ((A64 == nullptr) == (A32 == nullptr)) return -2;
-  const bool weak = P.vi == VI_WEAK;
-  switch (P.N) {
-    case 3: return weak ? launch_curved_n<3, VI_WEAK>(P, A64, A32, stream)
-                        : launch_curved_n<3, VI_FD>(P, A64, A32, stream);
-    case 4: return weak ? launch_curved_n<4, VI_WEAK>(P, A64, A32, stream)
-                        : launch_curved_n<4, VI_FD>(P, A64, A32, stream);
-    case 5: return weak ? launch_curved_n<5, VI_WEAK>(P, A64, A32, stream)
-                        : launch_curved_n<5, VI_FD>(P, A64, A32, stream);
-    default: return -3;
+  switch (P.vi) {
+    case VI_WEAK:
+      switch (P.N) {
+        case 3: return launch_curved_n<3, VI_WEAK>(P, A64, A32, stream);
+        case 4: return launch_curved_n<4, VI_WEAK>(P, A64, A32, stream);
+        case 5: return launch_curved_n<5, VI_WEAK>(P, A64, A32, stream);
+      }
+      break;
+    case VI_FD:
+      switch (P.N) {
+        case 3: return launch_curved_n<3, VI_FD>(P, A64, A32, stream);
+        case 4: return launch_curved_n<4, VI_FD>(P, A64, A32, stream);
+        case 5: return launch_curved_n<5, VI_FD>(P, A64, A32, stream);
+      }
+      break;
+    case VI_HG:
+      switch (P.N) {
+        case 3: return launch_curved_n<3, VI_HG>(P, A64, A32, stream);
+        case 4: return launch_curved_n<4, VI_HG>(P, A64, A32, stream);
+        case 5: return launch_curved_n<5, VI_HG>(P, A64, A32, stream);
+      }
+      break;
   }
+  return -3;
 }
 
 __global__ void curved_ghost_kernel(const CurvedParams P, int64_t B, const Clock* clock, double c_s,

@@ -19,7 +19,7 @@ namespace tg {
 struct CurvedParams {
   int64_t nelements;
   int32_t N;                // nodes per direction
-  int32_t vi;               // VI_WEAK or VI_FD
+  int32_t vi;               // VI_WEAK, VI_FD or VI_HG (2D)
   int32_t volume_flux, surface_flux, source;
   double gamma, inv_gamma_minus_one;
   EosF eos;
@@ -41,6 +41,16 @@ struct CurvedParams {
   double bc_par[4];
   const int32_t* bface;     // [B][2]
   const float2* ghost;      // [B][N][4]
+  // VI_HG (VolumeIntegralShockCapturingHG, dgsem_structured/dg_2d.jl:304-345):
+  // the FV flux, apply_smoothing! of the raw indicator (the stage arguments'
+  // alpha_raw), the blending threshold (calc_volume_integral.jl:242-245) and
+  // the free-stream preserving subcell normals (containers_2d.jl:200-298):
+  // snv[e][d][l][i] = normal of the interface between nodes i and i + 1 of
+  // line l in direction d, i = 0 .. N - 2 (FP64 pairs; FP32 copy for mixed)
+  int32_t fv_flux, alpha_smooth;
+  double alpha_atol;
+  const double2* snv;       // [E][2][N][N - 1]
+  const float2* snv32;
 };
 
 // Elements per block of the curvilinear kernels (0: polydeg not compiled).

@@ -1,4 +1,5 @@
-// Curvilinear 3D stage kernel (StructuredMesh{3}), FP64 (weak form, polydeg 3).
+// Curvilinear 3D stage kernel (StructuredMesh{3}), FP64 (weak form and flux
+// differencing, polydeg 3 and 5).
 //
 // The 3D form of the FP64 kernel of tg_curved.cu: volume integrals with
 // contravariant fluxes along the three reference directions
@@ -268,9 +269,19 @@ __global__ void __launch_bounds__(Curved3K<N, EPB>::NT)
 #pragma unroll
         for (int v = 0; v < NV; ++v) un[v] = src[v];
         Eu::cons2prim(un, wn, gamma);
-        if (side)
-          FluxN3::two_point(P.surface_flux, uu[own], ww[own], un, wn, ja[own], gamma, igm1, F);
-        else
+        if (side) {
+          // an interface takes the contravariant vector of the element on its
+          // positive side (calc_interface_flux!, dgsem_structured/dg_3d.jl), so
+          // both elements evaluate the same flux; boundary faces take their own
+          double nrm[3] = {ja[own][0], ja[own][1], ja[own][2]};
+          if (nb >= 0) {
+            const double* m = P.met + ((size_t)nb * NN + face_partner3<N>(dir, line)) * MS + 3 * dd;
+            nrm[0] = m[0];
+            nrm[1] = m[1];
+            nrm[2] = m[2];
+          }
+          FluxN3::two_point(P.surface_flux, uu[own], ww[own], un, wn, nrm, gamma, igm1, F);
+        } else
           FluxN3::two_point(P.surface_flux, un, wn, uu[own], ww[own], ja[own], gamma, igm1, F);
 #pragma unroll
         for (int v = 0; v < NV; ++v)
@@ -430,15 +441,18 @@ int launch_curved3_n(const CurvedParams& P, const StageArgs& A, cudaStream_t str
 
 }  // namespace
 
-// Built for the weak form at polydeg 3 (N = 4), the configuration checked
-// against the oracle and the StructuredMesh3D goldens on the GPU; the kernel
-// template also holds the flux-differencing volume integral and other degrees
-// (EPB chosen per N above) for the next instantiations.
-int curved3_supported(int N) { return N == 4; }
+// Built for polydeg 3 and 5 (N = 4, 6: the degrees of Trixi's StructuredMesh3D
+// Euler elixirs), each with the weak form and flux differencing.
+int curved3_supported(int N) { return N == 4 || N == 6; }
 
 int launch_curved3(const CurvedParams& P, const StageArgs& A, cudaStream_t stream) {
-  if (P.N != 4 || P.vi != VI_WEAK) return -3;
-  return launch_curved3_n<4, VI_WEAK>(P, A, stream);
+  const bool fd = P.vi == VI_FD;
+  if (!fd && P.vi != VI_WEAK) return -3;
+  if (P.N == 4) return fd ? launch_curved3_n<4, VI_FD>(P, A, stream)
+                          : launch_curved3_n<4, VI_WEAK>(P, A, stream);
+  if (P.N == 6) return fd ? launch_curved3_n<6, VI_FD>(P, A, stream)
+                          : launch_curved3_n<6, VI_WEAK>(P, A, stream);
+  return -3;
 }
 
 int launch_curved3_speed(const CurvedParams& P, const double* u, unsigned long long* dst,
