@@ -1174,7 +1174,7 @@ static int launch_kernel(tg_ctx* c, int mode, const void* u_in, void* u_out, dou
     }
     A.speed_bits = M.speed_bits = reduce ? &c->d_clock->speed_bits : nullptr;
     if (c->D == 3) {
-      if (tg::launch_curved3(c->CP, A, c->stream) != 0)
+      if (tg::launch_curved3(c->CP, c->fp64 ? &A : nullptr, c->fp64 ? nullptr : &M, c->stream) != 0)
         return fail(c, TG_ERR_CUDA, "curvilinear 3D kernel launch failed: %s",
                     cudaGetErrorString(cudaGetLastError()));
       return TG_OK;
@@ -1276,8 +1276,7 @@ static int enqueue_stage(tg_ctx* c, int stage, bool reduce_speed) {
 static int reduce_speed(tg_ctx* c, const void* u, bool ff, unsigned long long* dst) {
   speed_reset_kernel<<<1, 1, 0, c->stream>>>(dst);
   if (c->curved) {
-    const int rc = c->D == 3 ? tg::launch_curved3_speed(c->CP, (const double*)u, dst, c->d_status,
-                                                        c->stream)
+    const int rc = c->D == 3 ? tg::launch_curved3_speed(c->CP, u, ff, dst, c->d_status, c->stream)
                              : tg::launch_curved_speed(c->CP, u, ff, dst, c->d_status, c->stream);
     if (rc != 0) return fail(c, TG_ERR_CUDA, "curvilinear wave-speed launch failed");
     return TG_OK;
@@ -1318,7 +1317,19 @@ static int curved_setup(tg_ctx* c, const tg_config* cfg) {
   CUDA_TRY(nullptr, cudaMemcpy(c->d_cmet, met.data(), sizeof(double) * met.size(),
                                cudaMemcpyHostToDevice));
   const bool src = c->P.source == SRC_CONVERGENCE_TEST;
-  if (!c->fp64) {
+  if (!c->fp64 && D == 3) {
+    // per node three float4 {Ja^d_x, Ja^d_y, Ja^d_z, (d = 0: inverse Jacobian)}
+    std::vector<float4> ja(nq * 3);
+    for (size_t k = 0; k < nq; ++k) {
+      const double* m = &met[k * MS];
+      for (int d = 0; d < 3; ++d)
+        ja[k * 3 + d] = make_float4((float)m[3 * d], (float)m[3 * d + 1], (float)m[3 * d + 2],
+                                    d == 0 ? (float)m[9] : 0.0f);
+    }
+    CUDA_TRY(nullptr, cudaMalloc((void**)&c->d_cja32, sizeof(float4) * nq * 3));
+    CUDA_TRY(nullptr, cudaMemcpy(c->d_cja32, ja.data(), sizeof(float4) * nq * 3,
+                                 cudaMemcpyHostToDevice));
+  } else if (!c->fp64) {
     std::vector<float4> ja(nq);
     std::vector<float> ij(nq);
     for (size_t k = 0; k < nq; ++k) {
@@ -1332,12 +1343,15 @@ static int curved_setup(tg_ctx* c, const tg_config* cfg) {
                                  cudaMemcpyHostToDevice));
     CUDA_TRY(nullptr, cudaMemcpy(c->d_cinvj32, ij.data(), sizeof(float) * nq,
                                  cudaMemcpyHostToDevice));
+  }
+  if (!c->fp64) {
     if (src) {
-      // sin/cos(pi (x + y)) per node as float-float pairs; the stage kernel
-      // combines them with sin/cos(pi t) by the angle-difference formula
+      // sin/cos(pi (x + y (+ z))) per node as float-float pairs; the stage
+      // kernel combines them with sin/cos(pi t) by the angle-difference formula
       std::vector<float4> sc(nq);
       for (size_t k = 0; k < nq; ++k) {
-        const double ph = cfg->node_coordinates[k * 2] + cfg->node_coordinates[k * 2 + 1];
+        double ph = 0.0;
+        for (int d = 0; d < D; ++d) ph += cfg->node_coordinates[k * D + d];
         const double sn = std::sin(M_PI * ph), cs = std::cos(M_PI * ph);
         const float sh = (float)sn, ch = (float)cs;
         sc[k] = make_float4(sh, ch, (float)(sn - (double)sh), (float)(cs - (double)ch));
@@ -1521,10 +1535,7 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   const bool curved = cfg->mesh_type == TG_MESH_CURVED;
   if (curved) {
     // StructuredMesh / P4estMesh bricks: the curvilinear kernels of tg_curved.cu
-    // (2D) and tg_curved3.cu (3D, FP64)
-    if (D == 3 && mixed)
-      return fail(nullptr, TG_ERR_UNSUPPORTED,
-                  "3D curvilinear meshes: FP64 only (the mixed path runs 2D curvilinear meshes)");
+    // (2D) and tg_curved3.cu (3D)
     // 3D: tg_curved3.cu is built for polydeg 3 and 5, weak form or flux differencing
     if (D == 2 ? tg::curved_epb(N) == 0 : !tg::curved3_supported(N))
       return fail(nullptr, TG_ERR_UNSUPPORTED, "curvilinear meshes: polydeg %d is not compiled",
@@ -2376,7 +2387,7 @@ int tg_integrals(tg_ctx* c, double* out) {
   if (!c->d_partial) CUDA_TRY(c, cudaMalloc((void**)&c->d_partial, sizeof(double) * K * c->E));
   const int64_t nb = (c->E + 127) / 128;
   if (c->curved) {
-    const int rc = c->D == 3 ? tg::launch_curved3_integrals(c->CP, (const double*)c->d_u[c->cur],
+    const int rc = c->D == 3 ? tg::launch_curved3_integrals(c->CP, c->d_u[c->cur], !c->fp64,
                                                             c->d_weights, c->d_partial, c->stream)
                              : tg::launch_curved_integrals(c->CP, c->d_u[c->cur], !c->fp64,
                                                            c->d_weights, c->d_partial, c->stream);

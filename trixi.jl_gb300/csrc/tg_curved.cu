@@ -450,90 +450,6 @@ namespace tg {
 // Mixed-precision stage kernel (float-float state, FP32 deviation fluxes)
 // ---------------------------------------------------------------------------
 
-// Deviation of the two-point flux of kind KIND (or `kind` at run time) along
-// the normal (n0, n1): n0 times its deviation along x plus n1 times its
-// deviation along y (the fluxes are linear in the normal direction).
-template <int KIND>
-__device__ __forceinline__ void dev_flux_n(int kind, const RefState<2>& R, const Node<2>& a,
-                                           const Node<2>& b, float n0, float n1, const EosF& eos,
-                                           float* F) {
-  using Dv = Dev<2>;
-  Node<2> ax = a, bx = b, ay = a, by = b;
-  Dv::orient(ax, 0);
-  Dv::orient(bx, 0);
-  Dv::orient(ay, 1);
-  Dv::orient(by, 1);
-  float fx[4], fy[4];
-  Dv::template flux2<KIND>(kind, R, ax, bx, 0, R.v[0], eos, fx);
-  Dv::template flux2<KIND>(kind, R, ay, by, 1, R.v[1], eos, fy);
-#pragma unroll
-  for (int v = 0; v < 4; ++v) F[v] = fmaf(n1, fy[v], n0 * fx[v]);
-}
-
-// flux_ranocha(a, b, n) - f(w_ref) . n in one pass (compressible_euler_2d.jl:
-// 724-753): Dev::dranocha with the axis replaced by the normal -- the
-// reference normal velocity v_ref . n, the nodes' normal-velocity deviations
-// dv . n and the pressure term dp_avg n -- so the two logarithmic means are
-// evaluated once instead of once per axis.  Algebraically equal to
-// dev_flux_n<FLUX_RANOCHA>.
-__device__ __forceinline__ void dev_ranocha_n(const RefState<2>& R, const Node<2>& a,
-                                              const Node<2>& b, float n0, float n1,
-                                              const EosF& eos, float* f) {
-  using Dv = Dev<2>;
-  const float igm1 = eos.igm1;
-  const float drho_ln = Dv::dev_ln_mean(R.rho, a.dw[0], b.dw[0], a.w[0], b.w[0]);
-  const float dq_ln = Dv::dev_ln_mean(R.q, a.dq, b.dq, R.q + a.dq, R.q + b.dq);
-  const float q_ln = R.q + dq_ln;
-  float dvavg[2], vavg[2];
-  float dvsq = 0;
-#pragma unroll
-  for (int d = 0; d < 2; ++d) {
-    dvavg[d] = 0.5f * (a.dw[1 + d] + b.dw[1 + d]);
-    vavg[d] = R.v[d] + dvavg[d];
-    dvsq += R.v[d] * (a.dw[1 + d] + b.dw[1 + d]) + a.dw[1 + d] * b.dw[1 + d];
-  }
-  dvsq *= 0.5f;
-  const float dpavg = 0.5f * (a.dw[3] + b.dw[3]);
-  const float vrn = fmaf(R.v[1], n1, R.v[0] * n0);
-  const float dvan = fmaf(a.dw[2], n1, a.dw[1] * n0), dvbn = fmaf(b.dw[2], n1, b.dw[1] * n0);
-  const float F1r = R.rho * vrn;
-  const float dvavgn = 0.5f * (dvan + dvbn);
-  const float d1 = R.rho * dvavgn + drho_ln * (vrn + dvavgn);
-  f[0] = d1;
-  f[1] = d1 * vavg[0] + F1r * dvavg[0] + dpavg * n0;
-  f[2] = d1 * vavg[1] + F1r * dvavg[1] + dpavg * n1;
-  const float vsq = a.w[1] * b.w[1] + a.w[2] * b.w[2];
-  const float H = 0.5f * vsq + igm1 / q_ln;
-  const float dH = dvsq + igm1 * (R.rq - R.p * dq_ln) / (R.rho * q_ln);
-  const float dpv = 0.5f * (R.p * (dvan + dvbn) + vrn * (a.dw[3] + b.dw[3]) + a.dw[3] * dvbn +
-                            b.dw[3] * dvan);
-  f[3] = d1 * H + F1r * dH + dpv;
-}
-
-// Surface flux deviation along n: the linear fluxes as above; the
-// Lax-Friedrichs fluxes as the central flux plus the dissipation
-// -lambda/2 (u_b - u_a) with lambda from the normal velocities and |n|.
-__device__ __forceinline__ void dev_surface_n(int kind, const RefState<2>& R, const Node<2>& a,
-                                              const Node<2>& b, float n0, float n1,
-                                              const EosF& eos, float* F) {
-  if (kind == FLUX_RANOCHA) {
-    dev_ranocha_n(R, a, b, n0, n1, eos, F);
-    return;
-  }
-  if (kind != FLUX_LLF && kind != FLUX_LLF_NAIVE) {
-    dev_flux_n<-1>(kind, R, a, b, n0, n1, eos, F);
-    return;
-  }
-  dev_flux_n<FLUX_CENTRAL>(FLUX_CENTRAL, R, a, b, n0, n1, eos, F);
-  const float va = a.w[1] * n0 + a.w[2] * n1, vb = b.w[1] * n0 + b.w[2] * n1;
-  const float ca = sqrtf(eos.gamma * a.w[3] / a.w[0]), cb = sqrtf(eos.gamma * b.w[3] / b.w[0]);
-  const float nn = sqrtf(n0 * n0 + n1 * n1);
-  const float lam = kind == FLUX_LLF_NAIVE ? fmaxf(fabsf(va), fabsf(vb)) + fmaxf(ca, cb) * nn
-                                           : fmaxf(fabsf(va) + ca * nn, fabsf(vb) + cb * nn);
-#pragma unroll
-  for (int v = 0; v < 4; ++v) F[v] = F[v] + (-0.5f * lam * (b.du[v] - a.du[v]));
-}
-
 template <int N, int VI, int EPB>
 __global__ void __launch_bounds__(CurvedK<N, EPB>::NT, CurvedK<N, EPB>::MINB_MIXED)
     curved_kernel_mixed(const CurvedParams P, const MixedArgs A) {
@@ -704,11 +620,11 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT, CurvedK<N, EPB>::MINB_MIX
 #pragma unroll
           for (int b = a + 1; b < N; ++b) {
             float F[NV];
-            const float n0 = 0.5f * (ja[a][0] + ja[b][0]), n1 = 0.5f * (ja[a][1] + ja[b][1]);
+            const float n[2] = {0.5f * (ja[a][0] + ja[b][0]), 0.5f * (ja[a][1] + ja[b][1])};
             if (P.volume_flux == FLUX_RANOCHA)
-              dev_ranocha_n(R, nd[a], nd[b], n0, n1, eos, F);
+              dev_ranocha_n<2>(R, nd[a], nd[b], n, eos, F);
             else
-              dev_flux_n<-1>(P.volume_flux, R, nd[a], nd[b], n0, n1, eos, F);
+              dev_flux_n<2, -1>(P.volume_flux, R, nd[a], nd[b], n, eos, F);
             const float cab = P.Dsplit32[a * N + b], cba = P.Dsplit32[b * N + a];
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
@@ -737,8 +653,9 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT, CurvedK<N, EPB>::MINB_MIX
           for (int i = 0; i < N; ++i) {
             float fr[NV] = {0.0f, 0.0f, 0.0f, 0.0f};
             if (i < N - 1) {
-              const float2 n = nv[i];
-              dev_surface_n(P.fv_flux, R, nd[i], nd[i + 1], n.x, n.y, eos, fr);
+              const float2 n2 = nv[i];
+              const float n[2] = {n2.x, n2.y};
+              dev_surface_n<2>(P.fv_flux, R, nd[i], nd[i + 1], n, eos, fr);
             }
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
@@ -768,9 +685,9 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT, CurvedK<N, EPB>::MINB_MIX
         Dv::make_node(hi, lo, R, eos, other);
         float F[NV];
         if (side)
-          dev_surface_n(P.surface_flux, R, nd[own], other, ja[own][0], ja[own][1], eos, F);
+          dev_surface_n<2>(P.surface_flux, R, nd[own], other, ja[own], eos, F);
         else
-          dev_surface_n(P.surface_flux, R, other, nd[own], ja[own][0], ja[own][1], eos, F);
+          dev_surface_n<2>(P.surface_flux, R, other, nd[own], ja[own], eos, F);
 #pragma unroll
         for (int v = 0; v < NV; ++v) acc[own][v] = fmaf(side ? F[v] : -F[v], factor, acc[own][v]);
       }

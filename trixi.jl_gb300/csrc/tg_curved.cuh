@@ -28,8 +28,8 @@ struct CurvedParams {
   float Dhat32[MAXN * MAXN], Dsplit32[MAXN * MAXN], inv_weights32[MAXN];
   const int32_t* nbr;       // [E][4]: element across -x, +x, -y, +y
   const double* met;        // [E][NN][5]: Ja^1_x, Ja^1_y, Ja^2_x, Ja^2_y, inverse Jacobian
-  const float4* ja32;       // [E][NN]: Ja^1_x, Ja^1_y, Ja^2_x, Ja^2_y
-  const float* invj32;      // [E][NN]
+  const float4* ja32;       // [E][NN]: Ja^1_x, Ja^1_y, Ja^2_x, Ja^2_y (3D: see below)
+  const float* invj32;      // [E][NN] (2D)
   const double* xy;         // [E][NN][2] node coordinates (FP64 sources)
   const float4* sc;         // [E][NN] sin/cos(pi (x + y)): (sin hi, cos hi, sin lo, cos lo)
   // Faces at a non-periodic edge have nbr = -1 - b (b: boundary face number,
@@ -52,6 +52,111 @@ struct CurvedParams {
   const double2* snv;       // [E][2][N][N - 1]
   const float2* snv32;
 };
+
+// ---------------------------------------------------------------------------
+// Flux deviations along a normal direction n (the mixed kernels): the
+// two-point flux between nodes a and b of the element with reference state R
+// minus the reference's physical flux f(w_ref) . n
+// ---------------------------------------------------------------------------
+
+// x . n with the products summed left to right
+template <int D>
+__device__ __forceinline__ float dot_n(const float* x, const float* n) {
+  float r = x[0] * n[0];
+#pragma unroll
+  for (int d = 1; d < D; ++d) r = fmaf(x[d], n[d], r);
+  return r;
+}
+
+// Flux of kind KIND (or `kind` at run time): the fluxes are linear in n, so
+// the deviation along n is the sum over d of n_d times the deviation along
+// axis d.
+template <int D, int KIND>
+__device__ __forceinline__ void dev_flux_n(int kind, const RefState<D>& R, const Node<D>& a,
+                                           const Node<D>& b, const float* n, const EosF& eos,
+                                           float* F) {
+  using Dv = Dev<D>;
+  constexpr int NV = D + 2;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    Node<D> ad = a, bd = b;
+    Dv::orient(ad, d);
+    Dv::orient(bd, d);
+    float fd[NV];
+    Dv::template flux2<KIND>(kind, R, ad, bd, d, R.v[d], eos, fd);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) F[v] = d == 0 ? n[0] * fd[v] : fmaf(n[d], fd[v], F[v]);
+  }
+}
+
+// flux_ranocha(a, b, n) - f(w_ref) . n in one pass (compressible_euler_2d.jl:
+// 724-753, compressible_euler_3d.jl normal-direction method): Dev::dranocha
+// with the axis replaced by the normal -- the reference normal velocity
+// v_ref . n, the nodes' normal-velocity deviations dv . n and the pressure
+// term dp_avg n -- so the two logarithmic means are evaluated once instead of
+// once per axis.  Algebraically equal to dev_flux_n<D, FLUX_RANOCHA>.
+template <int D>
+__device__ __forceinline__ void dev_ranocha_n(const RefState<D>& R, const Node<D>& a,
+                                              const Node<D>& b, const float* n, const EosF& eos,
+                                              float* f) {
+  using Dv = Dev<D>;
+  constexpr int P = D + 1;
+  const float igm1 = eos.igm1;
+  const float drho_ln = Dv::dev_ln_mean(R.rho, a.dw[0], b.dw[0], a.w[0], b.w[0]);
+  const float dq_ln = Dv::dev_ln_mean(R.q, a.dq, b.dq, R.q + a.dq, R.q + b.dq);
+  const float q_ln = R.q + dq_ln;
+  float dvavg[D], vavg[D];
+  float dvsq = 0, vsq = 0;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    dvavg[d] = 0.5f * (a.dw[1 + d] + b.dw[1 + d]);
+    vavg[d] = R.v[d] + dvavg[d];
+    dvsq += R.v[d] * (a.dw[1 + d] + b.dw[1 + d]) + a.dw[1 + d] * b.dw[1 + d];
+    vsq += a.w[1 + d] * b.w[1 + d];
+  }
+  dvsq *= 0.5f;
+  const float dpavg = 0.5f * (a.dw[P] + b.dw[P]);
+  const float vrn = dot_n<D>(R.v, n);
+  const float dvan = dot_n<D>(a.dw + 1, n), dvbn = dot_n<D>(b.dw + 1, n);
+  const float F1r = R.rho * vrn;
+  const float dvavgn = 0.5f * (dvan + dvbn);
+  const float d1 = R.rho * dvavgn + drho_ln * (vrn + dvavgn);
+  f[0] = d1;
+#pragma unroll
+  for (int d = 0; d < D; ++d) f[1 + d] = d1 * vavg[d] + F1r * dvavg[d] + dpavg * n[d];
+  const float H = 0.5f * vsq + igm1 / q_ln;
+  const float dH = dvsq + igm1 * (R.rq - R.p * dq_ln) / (R.rho * q_ln);
+  const float dpv = 0.5f * (R.p * (dvan + dvbn) + vrn * (a.dw[P] + b.dw[P]) + a.dw[P] * dvbn +
+                            b.dw[P] * dvan);
+  f[P] = d1 * H + F1r * dH + dpv;
+}
+
+// Surface (or FV subcell) flux deviation along n: the linear fluxes as above;
+// the Lax-Friedrichs fluxes as the central flux plus the dissipation
+// -lambda/2 (u_b - u_a) with lambda from the normal velocities and |n|
+// (max_abs_speed(_naive) along a normal).  Needs the nodes' du.
+template <int D>
+__device__ __forceinline__ void dev_surface_n(int kind, const RefState<D>& R, const Node<D>& a,
+                                              const Node<D>& b, const float* n, const EosF& eos,
+                                              float* F) {
+  constexpr int NV = D + 2, P = D + 1;
+  if (kind == FLUX_RANOCHA) {
+    dev_ranocha_n<D>(R, a, b, n, eos, F);
+    return;
+  }
+  if (kind != FLUX_LLF && kind != FLUX_LLF_NAIVE) {
+    dev_flux_n<D, -1>(kind, R, a, b, n, eos, F);
+    return;
+  }
+  dev_flux_n<D, FLUX_CENTRAL>(FLUX_CENTRAL, R, a, b, n, eos, F);
+  const float va = dot_n<D>(a.w + 1, n), vb = dot_n<D>(b.w + 1, n);
+  const float ca = sqrtf(eos.gamma * a.w[P] / a.w[0]), cb = sqrtf(eos.gamma * b.w[P] / b.w[0]);
+  const float nn = sqrtf(dot_n<D>(n, n));
+  const float lam = kind == FLUX_LLF_NAIVE ? fmaxf(fabsf(va), fabsf(vb)) + fmaxf(ca, cb) * nn
+                                           : fmaxf(fabsf(va) + ca * nn, fabsf(vb) + cb * nn);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) F[v] = F[v] + (-0.5f * lam * (b.du[v] - a.du[v]));
+}
 
 // Elements per block of the curvilinear kernels (0: polydeg not compiled).
 int curved_epb(int N);
@@ -77,14 +182,19 @@ int launch_curved_speed(const CurvedParams& P, const void* u, bool ff, unsigned 
 int launch_curved_integrals(const CurvedParams& P, const void* u, bool ff, const double* weights,
                             double* partial, cudaStream_t stream);
 
-// 3D curvilinear meshes (tg_curved3.cu), FP64 contexts only: P.met holds
-// [E][NN][10] (Ja^d_c at d * 3 + c, then the inverse Jacobian), P.xy [E][NN][3],
-// P.nbr [E][6].
+// 3D curvilinear meshes (tg_curved3.cu): P.met holds [E][NN][10] (Ja^d_c at
+// d * 3 + c, then the inverse Jacobian), P.xy [E][NN][3], P.nbr [E][6]; mixed
+// contexts also P.ja32 as [E][NN][3] float4 {Ja^d_x, Ja^d_y, Ja^d_z, (d = 0:
+// inverse Jacobian)} and, with MMS sources, P.sc with the phase x + y + z.
+// Exactly one of A64 (FP64 context) and A32 (mixed context) is non-null; u is
+// the context's state (float-float when ff), the speed and the integrals are
+// evaluated in FP64.
 int curved3_supported(int N);
-int launch_curved3(const CurvedParams& P, const StageArgs& A, cudaStream_t stream);
-int launch_curved3_speed(const CurvedParams& P, const double* u, unsigned long long* dst,
+int launch_curved3(const CurvedParams& P, const StageArgs* A64, const MixedArgs* A32,
+                   cudaStream_t stream);
+int launch_curved3_speed(const CurvedParams& P, const void* u, bool ff, unsigned long long* dst,
                          int32_t* status, cudaStream_t stream);
-int launch_curved3_integrals(const CurvedParams& P, const double* u, const double* weights,
+int launch_curved3_integrals(const CurvedParams& P, const void* u, bool ff, const double* weights,
                              double* partial, cudaStream_t stream);
 
 }  // namespace tg

@@ -1,5 +1,5 @@
-// Curvilinear 3D stage kernel (StructuredMesh{3}), FP64 (weak form and flux
-// differencing, polydeg 3 and 5).
+// Curvilinear 3D stage kernels (StructuredMesh{3}), FP64 and mixed precision
+// (weak form and flux differencing, polydeg 3 and 5).
 //
 // The 3D form of the FP64 kernel of tg_curved.cu: volume integrals with
 // contravariant fluxes along the three reference directions
@@ -362,6 +362,320 @@ __global__ void __launch_bounds__(Curved3K<N, EPB>::NT)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed-precision kernel: float-float state, FP32 flux deviations along the
+// contravariant vectors (the 2D mixed kernel's algebra, tg_curved.cu, with
+// three directions).  Per node the metric is three float4 {Ja^d_x, Ja^d_y,
+// Ja^d_z, (d = 0: inverse Jacobian)}; with MMS sources a float4 of
+// sin/cos(pi (x + y + z)) as float-float pairs.  Dirichlet faces take the
+// FP64 boundary value of the face node, split into a float-float pair, while
+// the block stages its neighbour traces.
+// ---------------------------------------------------------------------------
+template <int N, int EPB>
+struct Curved3M {
+  static constexpr int NF = N * N, NN = N * N * N, NV = 5, NT = EPB * 3 * NF;
+  static constexpr int CHUNK = EPB * NN * NV;     // float2 state values of a block
+  static constexpr int FACE = EPB * 6 * NF * NV;  // float2 neighbour / boundary traces
+  static constexpr int SP = EPB * NN;
+  static constexpr size_t smem() {
+    return sizeof(float2) * (CHUNK + FACE) + sizeof(float4) * 4 * SP +
+           sizeof(float) * (NV * SP + (NV + 1) * SP + 3 * NV * SP) + sizeof(RefState<3>) * EPB +
+           sizeof(float) * 4 + sizeof(unsigned int) * 3 * EPB;
+  }
+};
+
+template <int N, int VI, int EPB>
+__global__ void __launch_bounds__(Curved3M<N, EPB>::NT)
+    curved3_kernel_mixed(const CurvedParams P, const MixedArgs A) {
+  using K = Curved3M<N, EPB>;
+  using Dv = Dev<3>;
+  constexpr int NN = K::NN, NF = K::NF, NV = 5, NT = K::NT, SP = K::SP, CHUNK = K::CHUNK;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* s_u = reinterpret_cast<float2*>(smem_raw);
+  float2* s_fu = s_u + CHUNK;                                // [EPB][6][NF][NV]
+  float4* s_ja = reinterpret_cast<float4*>(s_fu + K::FACE);  // [SP][3]
+  float4* s_sc = s_ja + 3 * SP;                              // [SP]
+  float* s_ut = reinterpret_cast<float*>(s_sc + SP);         // [SP][NV]
+  float* s_nd = s_ut + SP * NV;                              // [NV + 1][SP]: dw, dq
+  float* s_part = s_nd + (NV + 1) * SP;                      // [3][NV][SP]
+  RefState<3>* s_ref = reinterpret_cast<RefState<3>*>(s_part + 3 * NV * SP);
+  float* s_scal = reinterpret_cast<float*>(s_ref + EPB);     // b dt, a (hi, lo)
+  unsigned int* s_smax = reinterpret_cast<unsigned int*>(s_scal + 4);
+
+  const int tid = threadIdx.x;
+  const int64_t e0 = (int64_t)blockIdx.x * EPB;
+  const int nel = (int)min((int64_t)EPB, P.nelements - e0);
+  const size_t gofs = (size_t)e0 * NN * NV;
+  const int nval = nel * NN * NV;
+  const EosF& eos = P.eos;
+  const bool stage = A.mode == MODE_STAGE;
+
+  if (stage && A.clock->skip) {
+    for (int k = tid; k < nval; k += NT) A.u_out[gofs + k] = A.u_in[gofs + k];
+    return;
+  }
+  {
+    // NN * NV is even for the compiled degrees: the chunk starts on a 16-byte
+    // boundary and holds an even number of values
+    const float4* src = reinterpret_cast<const float4*>(A.u_in + gofs);
+    float4* dst = reinterpret_cast<float4*>(s_u);
+    for (int k = tid; k < nval / 2; k += NT) cp_async16(dst + k, src + k);
+  }
+  for (int k = tid; k < nel * 6 * NF; k += NT) {
+    const int sl = k / (6 * NF);
+    const int rem = k - sl * (6 * NF);
+    const int dir = rem / NF;
+    const int fn = rem - dir * NF;
+    const int32_t nb = P.nbr[(e0 + sl) * 6 + dir];
+    if (nb >= e0 && nb < e0 + nel) continue;  // read from s_u below
+    if (nb < 0) {
+      const double* x = P.xy + ((size_t)(e0 + sl) * NN + face_own3<N>(dir, fn)) * 3;
+      const double tt = stage ? A.clock->t + A.c * A.clock->dt : A.t_rhs;
+      double xv[3] = {x[0], x[1], x[2]}, ub[NV];
+      boundary_value<3>(P.bc_ic, P.bc_par, xv, tt, P.gamma, ub);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const float hi = (float)ub[v];
+        s_fu[k * NV + v] = make_float2(hi, (float)(ub[v] - (double)hi));
+      }
+      continue;
+    }
+    const float2* g = A.u_in + ((size_t)nb * NN + face_partner3<N>(dir, fn)) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) cp_async8(s_fu + k * NV + v, g + v);
+  }
+  {
+    const int nn = nel * NN;
+    const float4* ja = P.ja32 + (size_t)e0 * NN * 3;
+    for (int k = tid; k < 3 * nn; k += NT) cp_async16(s_ja + k, ja + k);
+    if (P.source == SRC_CONVERGENCE_TEST) {
+      const float4* sc = P.sc + (size_t)e0 * NN;
+      for (int k = tid; k < nn; k += NT) cp_async16(s_sc + k, sc + k);
+    }
+    if (stage && !A.zero_tmp) {
+      // u_tmp rows of a block start on 16-byte boundaries (NN * NV * 4 bytes)
+      const float4* ut = reinterpret_cast<const float4*>(A.u_tmp + gofs);
+      for (int k = tid; k < nval / 4; k += NT)
+        cp_async16(reinterpret_cast<float4*>(s_ut) + k, ut + k);
+    }
+  }
+  if (tid < 3 * EPB) s_smax[tid] = 0u;
+  if (tid == 0) {
+    const double bdt = stage ? A.b * A.clock->dt : 0.0;
+    const float bh = (float)bdt, ah = (float)A.a;
+    s_scal[0] = bh;
+    s_scal[1] = (float)(bdt - (double)bh);
+    s_scal[2] = ah;
+    s_scal[3] = (float)(A.a - (double)ah);
+  }
+  if (tid < nel) {
+    // reference state: mean hi of two opposite corner nodes
+    const float2* ue = A.u_in + (size_t)(e0 + tid) * NN * NV;
+    float hi[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) hi[v] = 0.5f * (ue[v].x + ue[(NN - 1) * NV + v].x);
+    Dv::make_ref(hi, eos, s_ref[tid]);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+
+  for (int n = tid; n < nel * NN; n += NT) {
+    const int sl = n / NN;
+    float hi[NV], lo[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const float2 x = s_u[n * NV + v];
+      hi[v] = x.x;
+      lo[v] = x.y;
+    }
+    Node<3> nd;
+    Dv::make_node(hi, lo, s_ref[sl], eos, nd);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) s_nd[v * SP + n] = nd.dw[v];
+    s_nd[NV * SP + n] = nd.dq;
+  }
+  __syncthreads();
+
+  // ---- lines ---------------------------------------------------------------------
+  {
+    const int dd = tid / (EPB * NF);
+    const int r = tid - dd * (EPB * NF);
+    const int sl = r / NF;
+    const int line = r - sl * NF;
+    if (sl < nel) {
+      const int64_t e = e0 + sl;
+      const RefState<3>& R = s_ref[sl];
+      Node<3> nd[N];
+      float ja[N][3];
+#pragma unroll
+      for (int a = 0; a < N; ++a) {
+        const int n = sl * NN + line3<N>(line, dd, a);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) nd[a].dw[v] = s_nd[v * SP + n];
+        nd[a].dq = s_nd[NV * SP + n];
+        Dv::complete(R, nd[a]);
+        const float4 j = s_ja[n * 3 + dd];
+        ja[a][0] = j.x;
+        ja[a][1] = j.y;
+        ja[a][2] = j.z;
+      }
+      float acc[N][NV];
+#pragma unroll
+      for (int a = 0; a < N; ++a)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc[a][v] = 0.0f;
+      if (VI == VI_WEAK) {
+#pragma unroll
+        for (int a = 0; a < N; ++a) {
+          float cf[NV];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            Node<3> ad = nd[a];
+            Dv::orient(ad, d);
+            float fd[NV];
+            Dv::dflux(R, ad, d, R.v[d], eos, fd);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) cf[v] = d == 0 ? ja[a][0] * fd[v] : fmaf(ja[a][d], fd[v], cf[v]);
+          }
+#pragma unroll
+          for (int ii = 0; ii < N; ++ii) {
+            const float c = P.Dhat32[ii * N + a];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[ii][v] = fmaf(c, cf[v], acc[ii][v]);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int a = 0; a < N; ++a)
+#pragma unroll
+          for (int b = a + 1; b < N; ++b) {
+            float F[NV];
+            const float n[3] = {0.5f * (ja[a][0] + ja[b][0]), 0.5f * (ja[a][1] + ja[b][1]),
+                                0.5f * (ja[a][2] + ja[b][2])};
+            if (P.volume_flux == FLUX_RANOCHA)
+              dev_ranocha_n<3>(R, nd[a], nd[b], n, eos, F);
+            else
+              dev_flux_n<3, -1>(P.volume_flux, R, nd[a], nd[b], n, eos, F);
+            const float cab = P.Dsplit32[a * N + b], cba = P.Dsplit32[b * N + a];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+              acc[a][v] = fmaf(cab, F[v], acc[a][v]);
+              acc[b][v] = fmaf(cba, F[v], acc[b][v]);
+            }
+          }
+      }
+      const float factor = P.inv_weights32[0];
+#pragma unroll
+      for (int side = 0; side < 2; ++side) {
+        const int dir = 2 * dd + side;
+        const int32_t nb = P.nbr[e * 6 + dir];
+        const int own = side ? N - 1 : 0;
+        Dv::node_du(s_u + ((size_t)sl * NN + line3<N>(line, dd, own)) * NV, R, nd[own].du);
+        const float2* src = (nb >= e0 && nb < e0 + nel)
+                                ? s_u + (((int)(nb - e0)) * NN + face_partner3<N>(dir, line)) * NV
+                                : s_fu + ((sl * 6 + dir) * NF + line) * NV;
+        float hi[NV], lo[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          hi[v] = src[v].x;
+          lo[v] = src[v].y;
+        }
+        Node<3> other;
+        Dv::make_node(hi, lo, R, eos, other);
+        float F[NV];
+        if (side)
+          dev_surface_n<3>(P.surface_flux, R, nd[own], other, ja[own], eos, F);
+        else
+          dev_surface_n<3>(P.surface_flux, R, other, nd[own], ja[own], eos, F);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc[own][v] = fmaf(side ? F[v] : -F[v], factor, acc[own][v]);
+      }
+#pragma unroll
+      for (int a = 0; a < N; ++a) {
+        const int n = sl * NN + line3<N>(line, dd, a);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) s_part[(dd * NV + v) * SP + n] = acc[a][v];
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- nodes -----------------------------------------------------------------------
+  const float bdt = s_scal[0], bdt_lo = s_scal[1], a_s = s_scal[2], a_lo = s_scal[3];
+  float st = 0, ct = 0, stl = 0, ctl = 0;
+  if (P.source == SRC_CONVERGENCE_TEST) {
+    if (stage) {
+      st = A.clock->sin_t[A.stage];
+      ct = A.clock->cos_t[A.stage];
+      stl = A.clock->sin_tl[A.stage];
+      ctl = A.clock->cos_tl[A.stage];
+    } else {
+      st = A.sin_t, ct = A.cos_t, stl = A.sin_tl, ctl = A.cos_tl;
+    }
+  }
+  bool bad = false;
+  for (int n = tid; n < nel * NN; n += NT) {
+    const int sl = n / NN;
+    const float4 j0 = s_ja[n * 3], j1 = s_ja[n * 3 + 1], j2 = s_ja[n * 3 + 2];
+    const float jfac = -j0.w;
+    float du[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      du[v] = (s_part[v * SP + n] + s_part[(NV + v) * SP + n] + s_part[(2 * NV + v) * SP + n]) *
+              jfac;
+    if (P.source == SRC_CONVERGENCE_TEST) {
+      // sin/cos(pi (x + y + z - t)) by the angle-difference formula in float-float
+      const float4 o = s_sc[n];
+      const float2 sn = ff_dot2(o.x, o.z, ct, ctl, -o.y, -o.w, st, stl);
+      const float2 cs = ff_dot2(o.y, o.w, ct, ctl, o.x, o.z, st, stl);
+      float sv[NV];
+      SourceMMS<3>::eval(sn.x, cs.x, eos, sv);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) du[v] += sv[v];
+    }
+    const size_t g = gofs + (size_t)n * NV;
+    if (!stage) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) A.du_out[g + v] = (double)du[v];
+      continue;
+    }
+    float hi[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const float old = A.zero_tmp ? 0.0f : s_ut[n * NV + v];
+      const float ut = fmaf(-a_lo, old, fmaf(-a_s, old, du[v]));
+      A.u_tmp[g + v] = ut;
+      const float2 un = ff_add(s_u[n * NV + v], fmaf(ut, bdt_lo, ut * bdt));
+      A.u_out[g + v] = un;
+      hi[v] = un.x;
+      bad |= !(un.x == un.x);
+    }
+    if (A.speed_bits) {
+      float w[NV];
+      Euler<3, float>::cons2prim(hi, w, eos.gamma);
+      const float cs = sqrtf(eos.gamma * w[4] / w[0]);
+      bad |= !(w[0] > 0.0f) || !(w[4] > 0.0f);
+      const float l[3] = {fabsf(w[1]) + cs, fabsf(w[2]) + cs, fabsf(w[3]) + cs};
+      const float ij = fabsf(j0.w);
+      const float4 jd[3] = {j0, j1, j2};
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float sd = fabsf(jd[d].x * l[0] + jd[d].y * l[1] + jd[d].z * l[2]) * ij;
+        if (sd == sd) atomicMax(&s_smax[3 * sl + d], __float_as_uint(sd));
+      }
+    }
+  }
+  if (bad) atomicOr(A.status, 1);
+  if (stage && A.speed_bits) {
+    __syncthreads();
+    if (tid < nel) {
+      const float sp = __uint_as_float(s_smax[3 * tid]) + __uint_as_float(s_smax[3 * tid + 1]) +
+                       __uint_as_float(s_smax[3 * tid + 2]);
+      if (sp == sp) atomicMax(A.speed_bits, (unsigned long long)__double_as_longlong((double)sp));
+    }
+  }
+}
+
 }  // namespace
 
 }  // namespace tg
@@ -370,9 +684,14 @@ namespace tg {
 
 namespace {
 
-// curvilinear max_dt (stepsize_dg3d.jl), one warp per element
+__device__ __forceinline__ double state3(double x) { return x; }
+__device__ __forceinline__ double state3(float2 x) { return (double)x.x + (double)x.y; }
+
+// curvilinear max_dt (stepsize_dg3d.jl), one warp per element, in FP64 on an
+// FP64 or a float-float state
+template <typename TS>
 __global__ void __launch_bounds__(128) curved3_speed_kernel(const CurvedParams P,
-                                                            const double* __restrict__ u, int NN,
+                                                            const TS* __restrict__ u, int NN,
                                                             unsigned long long* __restrict__ speed_bits,
                                                             int32_t* __restrict__ status) {
   const int lane = threadIdx.x & 31;
@@ -383,7 +702,7 @@ __global__ void __launch_bounds__(128) curved3_speed_kernel(const CurvedParams P
   for (int q = lane; q < NN; q += 32) {
     const size_t gq = (size_t)e * NN + q;
     double uu[5], w[5];
-    for (int v = 0; v < 5; ++v) uu[v] = u[gq * 5 + v];
+    for (int v = 0; v < 5; ++v) uu[v] = state3(u[gq * 5 + v]);
     Euler<3, double>::cons2prim(uu, w, P.gamma);
     const double cs = sqrt(P.gamma * w[4] / w[0]);
     bad |= !(w[0] > 0) || !(w[4] > 0);
@@ -406,7 +725,8 @@ __global__ void __launch_bounds__(128) curved3_speed_kernel(const CurvedParams P
 }
 
 // per-element FP64 integrals with |J| per node, as element_integrals_kernel
-__global__ void curved3_integrals_kernel(const CurvedParams P, const double* __restrict__ u,
+template <typename TS>
+__global__ void curved3_integrals_kernel(const CurvedParams P, const TS* __restrict__ u,
                                          const double* __restrict__ weights, int N,
                                          double* __restrict__ partial) {
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -418,7 +738,8 @@ __global__ void curved3_integrals_kernel(const CurvedParams P, const double* __r
     const size_t gq = (size_t)e * NN + q;
     const double w = weights[q % N] * weights[(q / N) % N] * weights[q / (N * N)] /
                      fabs(P.met[gq * 10 + 9]);
-    const double* p = u + gq * 5;
+    double p[5];
+    for (int v = 0; v < 5; ++v) p[v] = state3(u[gq * 5 + v]);
     const double m2 = p[1] * p[1] + p[2] * p[2] + p[3] * p[3];
     for (int v = 0; v < 5; ++v) acc[v] += w * p[v];
     const double pr = (g - 1) * (p[4] - 0.5 * m2 / p[0]);
@@ -430,42 +751,67 @@ __global__ void curved3_integrals_kernel(const CurvedParams P, const double* __r
 }
 
 template <int N, int VI>
-int launch_curved3_n(const CurvedParams& P, const StageArgs& A, cudaStream_t stream) {
+int launch_curved3_n(const CurvedParams& P, const StageArgs* A64, const MixedArgs* A32,
+                     cudaStream_t stream) {
   constexpr int EPB = N == 3 ? 4 : (N == 4 ? 2 : 1);
-  using K = Curved3K<N, EPB>;
-  static_assert(K::smem() <= 48 * 1024, "curvilinear 3D block exceeds 48 KB of shared memory");
   const unsigned nb = (unsigned)((P.nelements + EPB - 1) / EPB);
-  curved3_kernel_f64<N, VI, EPB><<<nb, K::NT, K::smem(), stream>>>(P, A);
+  if (A64) {
+    using K = Curved3K<N, EPB>;
+    static_assert(K::smem() <= 48 * 1024, "curvilinear 3D block exceeds 48 KB of shared memory");
+    curved3_kernel_f64<N, VI, EPB><<<nb, K::NT, K::smem(), stream>>>(P, *A64);
+  } else {
+    using K = Curved3M<N, EPB>;
+    static_assert(K::smem() <= 227 * 1024, "curvilinear 3D block exceeds the shared memory");
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(curved3_kernel_mixed<N, VI, EPB>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::smem());
+      attr = true;
+    }
+    curved3_kernel_mixed<N, VI, EPB><<<nb, K::NT, K::smem(), stream>>>(P, *A32);
+  }
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 }  // namespace
 
 // Built for polydeg 3 and 5 (N = 4, 6: the degrees of Trixi's StructuredMesh3D
-// Euler elixirs), each with the weak form and flux differencing.
+// Euler elixirs), each with the weak form and flux differencing, FP64 and
+// mixed precision.
 int curved3_supported(int N) { return N == 4 || N == 6; }
 
-int launch_curved3(const CurvedParams& P, const StageArgs& A, cudaStream_t stream) {
+int launch_curved3(const CurvedParams& P, const StageArgs* A64, const MixedArgs* A32,
+                   cudaStream_t stream) {
+  if ((A64 == nullptr) == (A32 == nullptr)) return -2;
   const bool fd = P.vi == VI_FD;
   if (!fd && P.vi != VI_WEAK) return -3;
-  if (P.N == 4) return fd ? launch_curved3_n<4, VI_FD>(P, A, stream)
-                          : launch_curved3_n<4, VI_WEAK>(P, A, stream);
-  if (P.N == 6) return fd ? launch_curved3_n<6, VI_FD>(P, A, stream)
-                          : launch_curved3_n<6, VI_WEAK>(P, A, stream);
+  if (P.N == 4) return fd ? launch_curved3_n<4, VI_FD>(P, A64, A32, stream)
+                          : launch_curved3_n<4, VI_WEAK>(P, A64, A32, stream);
+  if (P.N == 6) return fd ? launch_curved3_n<6, VI_FD>(P, A64, A32, stream)
+                          : launch_curved3_n<6, VI_WEAK>(P, A64, A32, stream);
   return -3;
 }
 
-int launch_curved3_speed(const CurvedParams& P, const double* u, unsigned long long* dst,
+int launch_curved3_speed(const CurvedParams& P, const void* u, bool ff, unsigned long long* dst,
                          int32_t* status, cudaStream_t stream) {
   const unsigned nb = (unsigned)((P.nelements + 3) / 4);  // one warp per element
-  curved3_speed_kernel<<<nb, 128, 0, stream>>>(P, u, P.N * P.N * P.N, dst, status);
+  const int NN = P.N * P.N * P.N;
+  if (ff)
+    curved3_speed_kernel<float2><<<nb, 128, 0, stream>>>(P, (const float2*)u, NN, dst, status);
+  else
+    curved3_speed_kernel<double><<<nb, 128, 0, stream>>>(P, (const double*)u, NN, dst, status);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_curved3_integrals(const CurvedParams& P, const double* u, const double* weights,
+int launch_curved3_integrals(const CurvedParams& P, const void* u, bool ff, const double* weights,
                              double* partial, cudaStream_t stream) {
   const unsigned nb = (unsigned)((P.nelements + 127) / 128);
-  curved3_integrals_kernel<<<nb, 128, 0, stream>>>(P, u, weights, P.N, partial);
+  if (ff)
+    curved3_integrals_kernel<float2><<<nb, 128, 0, stream>>>(P, (const float2*)u, weights, P.N,
+                                                             partial);
+  else
+    curved3_integrals_kernel<double><<<nb, 128, 0, stream>>>(P, (const double*)u, weights, P.N,
+                                                             partial);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
