@@ -18,7 +18,7 @@
   c5b  3D Taylor-Green vortex, Ma 0.1, polydeg 3, flux_ranocha volume flux,
        naive LLF, CFL 1.4 (elixir_euler_taylor_green_vortex.jl): kinetic
        energy history of mixed against FP64 (32^3 to t = 20; 64^3 mixed to
-       t = 20 and FP64 to t = 2).
+       t = 20 and FP64 to t = 2); c5b_64: both to t = 20 at 64^3.
   c6   AMR: the medium blast wave of elixir_euler_blast_wave_amr.jl at initial
        level 8 (ControllerThreeLevel on HG, base 6, max 8, interval 5) to
        t = 0.5, FP64 and mixed: time stepping vs in AMR passes; and the elixir's
@@ -611,7 +611,12 @@ def curved_steps(steps=3, cells=512):
     return dict(steps=n, t=t)
 
 
-RUNS = dict(c1=c1, c3=c3, c4=c4, c5a=c5a, c5b=c5b, c6=c6, c7=c7, c8=c8)
+def c5b_64():
+    """C5b at its full size: 64^3, mixed and FP64 both to t = 20."""
+    return c5b(levels=((6, 20.0, 20.0),), control_level=None)
+
+
+RUNS = dict(c1=c1, c3=c3, c4=c4, c5a=c5a, c5b=c5b, c5b_64=c5b_64, c6=c6, c7=c7, c8=c8)
 SHORT_RUNS = dict(learned_steps=learned_steps, mms_steps=mms_steps, ensemble_steps=ensemble_steps,
                   mortar_steps=mortar_steps, curved_steps=curved_steps)
 
