@@ -42,6 +42,7 @@ TG_DECLM(3, weak) TG_DECLM(3, fd) TG_DECLM(3, hg)
 int launch_indicator_2d_f64_hg(int N, const DgParams& P, const double* u, void* a, cudaStream_t s);
 int launch_indicator_3d_f64_hg(int N, const DgParams& P, const double* u, void* a, cudaStream_t s);
 int launch_indicator_mixed_2(int N, const MixedParams& P, const float2* u, float* a, cudaStream_t s);
+int launch_hg_alpha_rp(int N, const MixedParams& P, const float* rp, float* alpha, cudaStream_t s);
 int launch_indicator_mixed_3(int N, const MixedParams& P, const float2* u, float* a, cudaStream_t s);
 
 int launch_element(int D, int N, bool fp64, int vi, int epb, const DgParams& P,
@@ -141,6 +142,19 @@ __global__ void to_ff_kernel(const double* __restrict__ in, float2* __restrict__
     out[k] = make_float2(hi, __double2float_rn(x - (double)hi));
   }
 }
+// rho*p of every node from the hi parts of a float-float state (nv values per
+// node), with the stage kernels' arithmetic
+__global__ void rho_p_ff_kernel(const float2* __restrict__ u, int64_t nnodes, int nv, float gamma,
+                                float* __restrict__ rp) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnodes;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    float hi[5];
+    for (int v = 0; v < nv; ++v) hi[v] = u[k * nv + v].x;
+    rp[k] = nv == 4 ? Euler<2, float>::density_pressure(hi, gamma)
+                    : Euler<3, float>::density_pressure(hi, gamma);
+  }
+}
+
 __global__ void from_ff_kernel(const float2* __restrict__ in, double* __restrict__ out, int64_t n) {
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * blockDim.x)
@@ -949,6 +963,10 @@ struct tg_ctx {
   void* d_alpha_raw = nullptr;
   double* d_alpha = nullptr;
   float* d_alpha_sm = nullptr;        // mixed 2D HG: smoothed blending factors (padded)
+  // mixed 2D HG: rho*p of every node of the state d_u[cur], written by the
+  // stage kernel that produced it (rp_valid), read by the next indicator
+  float* d_rp = nullptr;
+  bool rp_valid = false;
   int32_t* d_nbr = nullptr;
   double* d_invj = nullptr;
   double* d_xline = nullptr;
@@ -1037,7 +1055,7 @@ static void free_ctx(tg_ctx* c) {
   for (int p = 0; p < 2; ++p)
     if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
   void* ptrs[] = {c->d_u[0], c->d_u[1], c->d_utmp, c->d_du, c->d_uscratch, c->d_stage64,
-                  c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_alpha_sm, c->d_nbr, c->d_invj, c->d_xline,
+                  c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_alpha_sm, c->d_rp, c->d_nbr, c->d_invj, c->d_xline,
                   c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mmat32, c->d_mflux, c->d_scls, c->d_amr_raw, c->d_amr_alpha, c->d_amap, c->d_akind, c->d_weights, c->d_cmet, c->d_csnv, c->d_csnv32, c->d_cja32, c->d_cinvj32, c->d_cxy, c->d_csc, c->d_partial, c->d_enorm, c->d_sums, c->d_clock,
                   c->d_status, c->d_speed};
   for (void* p : ptrs)
@@ -1083,6 +1101,10 @@ static const double* export_state(tg_ctx* c, int* rc) {
   return c->d_stage64;
 }
 
+namespace tg {
+const float* ctx_state_rho_p(tg_ctx* c);
+}
+
 // Blending factors of a state in the context representation: the HG (or
 // learned) indicator, unsmoothed, into d_alpha_raw; for mixed 2D contexts also
 // apply_smoothing! into d_alpha_sm, which the persistent 2D stage kernel
@@ -1097,8 +1119,11 @@ static int indicator(tg_ctx* c, const void* u) {
     c->view_state = nullptr;
     if (rc) return rc;
   } else {
+    const float* rp = u == c->d_u[c->cur] ? tg::ctx_state_rho_p(c) : nullptr;
     if (c->fp64)
       rc = launch_indicator(c->D, c->N, true, c->P, (const double*)u, c->d_alpha_raw, c->stream);
+    else if (rp)
+      rc = launch_hg_alpha_rp(c->N, c->MP, rp, (float*)c->d_alpha_raw, c->stream);
     else if (c->D == 2)
       rc = launch_indicator_mixed_2(c->N, c->MP, (const float2*)u, (float*)c->d_alpha_raw,
                                     c->stream);
@@ -1140,7 +1165,7 @@ static void launch_mortars(tg_ctx* c, const void* u_in) {
 
 // One element-kernel launch.  u_in is in the context representation.
 static int launch_kernel(tg_ctx* c, int mode, const void* u_in, void* u_out, double* du_out,
-                         double t_rhs, int stage, bool reduce) {
+                         double t_rhs, int stage, bool reduce, bool write_rp = false) {
   int rc;
   if (c->nmortar > 0) launch_mortars(c, u_in);
   if (c->curved) {
@@ -1215,6 +1240,7 @@ static int launch_kernel(tg_ctx* c, int mode, const void* u_in, void* u_out, dou
     MixedArgs A{};
     A.alpha_raw = (const float*)c->d_alpha_raw;
     A.alpha_smoothed = c->d_alpha_sm;
+    A.rp_out = write_rp && mode == MODE_STAGE ? c->d_rp : nullptr;
     A.status = c->d_status;
     A.clock = c->d_clock;
     A.mode = mode;
@@ -1265,9 +1291,21 @@ static int enqueue_stage(tg_ctx* c, int stage, bool reduce_speed) {
   int rc = indicator(c, c->d_u[c->cur]);
   if (rc) return rc;
   rc = launch_kernel(c, MODE_STAGE, c->d_u[c->cur], c->d_u[c->cur ^ 1], nullptr, 0.0, stage,
-                     reduce_speed);
+                     reduce_speed, true);
   if (rc) return rc;
   c->cur ^= 1;
+  c->rp_valid = c->d_rp != nullptr;  // the kernel wrote rho*p of its output
+  return TG_OK;
+}
+
+// rho*p of the current state into d_rp (before a step graph whose first
+// indicator reads it, after the state was set from outside the stage kernels).
+static int refresh_rho_p(tg_ctx* c) {
+  if (!c->d_rp || c->rp_valid) return TG_OK;
+  rho_p_ff_kernel<<<conv_blocks(c->ndofs), 256, 0, c->stream>>>(
+      (const float2*)c->d_u[c->cur], c->ndofs, c->NV, c->MP.gamma, c->d_rp);
+  CUDA_TRY(c, cudaGetLastError());
+  c->rp_valid = true;
   return TG_OK;
 }
 
@@ -1468,6 +1506,15 @@ int ctx_state_view(tg_ctx* c, const void** state, int* is_ff, int* D, int* N, in
 }
 
 int32_t* ctx_status_word(tg_ctx* c) { return c->d_status; }
+
+// rho*p of the state the indicator is about to read, when the stage kernel
+// that produced that state wrote it (mixed 2D shock-capturing contexts), else
+// null
+const float* ctx_state_rho_p(tg_ctx* c) {
+  if (!c->d_rp || !c->rp_valid) return nullptr;
+  if (c->view_state && c->view_state != c->d_u[c->cur]) return nullptr;
+  return c->d_rp;
+}
 
 int ctx_set_alpha_source(tg_ctx* c, tg_mlp* m) {
   if (m && c->vi != VI_HG)
@@ -1817,6 +1864,7 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     ALLOC(c->d_alpha, sizeof(double) * c->E);
     // read in whole 16-byte groups by the bulk copies of the 2D stage kernel
     if (!c->fp64) ALLOC(c->d_alpha_sm, sizeof(float) * (c->E + kElemPad));
+    if (!c->fp64 && D == 2 && !curved) ALLOC(c->d_rp, sizeof(float) * c->ndofs);
   }
   std::vector<float> invj_f, xline_f;
   std::vector<float4> sc0, scn;
@@ -2112,6 +2160,7 @@ int tg_upload_state(tg_ctx* c, const double* u_host) {
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   c->uploaded = true;
   c->clock_valid = false;
+  c->rp_valid = false;
   return TG_OK;
 }
 
@@ -2139,6 +2188,7 @@ int tg_download_state(tg_ctx* c, double* u_host) {
 int tg_state_device_ptr(tg_ctx* c, double** u_dev) {
   if (!c || !u_dev) return TG_ERR_INVALID_ARGUMENT;
   *u_dev = (double*)c->d_u[c->cur];
+  c->rp_valid = false;  // the caller may write the state
   return TG_OK;
 }
 
@@ -2215,9 +2265,10 @@ int tg_rk_stage_part(tg_ctx* c, int32_t stage, double t, double dt, int32_t part
   }
   if (parts & 2) {
     int rc = launch_kernel(c, MODE_STAGE, c->d_u[c->cur], c->d_u[c->cur ^ 1], nullptr, 0.0, stage,
-                           false);
+                           false, true);
     if (rc) return rc;
     c->cur ^= 1;
+    c->rp_valid = c->d_rp != nullptr;
   }
   return TG_OK;
 }
@@ -2317,13 +2368,20 @@ int ctx_view(tg_ctx* c, CtxView* v) {
   return TG_OK;
 }
 
-void ctx_set_cur(tg_ctx* c, int cur) { c->cur = cur & 1; }
+void ctx_set_cur(tg_ctx* c, int cur) {
+  c->cur = cur & 1;
+  c->rp_valid = false;
+}
 }  // namespace tg
 }  // extern "C++"
 
 static int capture_step_graph(tg_ctx* c, int parity) {
   const int saved = c->cur;
+  const bool saved_rp = c->rp_valid;
   c->cur = parity;
+  // stage 0 reads rho*p of the step's input state: tg_step refreshes it
+  // before launching the graphs whenever the state was set from outside
+  c->rp_valid = c->d_rp != nullptr;
   cudaGraph_t g = nullptr;
   CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
   clock_begin_kernel<<<1, 32, 0, c->stream>>>(c->d_clock);
@@ -2332,6 +2390,7 @@ static int capture_step_graph(tg_ctx* c, int parity) {
   if (rc == TG_OK) clock_end_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, c->N);
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
   c->cur = saved;
+  c->rp_valid = saved_rp;
   if (rc != TG_OK) {
     if (g) cudaGraphDestroy(g);
     return rc;
@@ -2355,6 +2414,8 @@ int tg_step(tg_ctx* c, int64_t max_steps, double cfl, double t_end, double* t_in
     }
   int rc = tg::ctx_clock_prepare(c, *t_inout, t_end, cfl, false);  // the clock read below orders it
   if (rc) return rc;
+  rc = refresh_rho_p(c);
+  if (rc) return rc;
   Clock h{};
   CUDA_TRY(c, cudaMemcpyAsync(&h, c->d_clock, sizeof(Clock), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -2366,6 +2427,7 @@ int tg_step(tg_ctx* c, int64_t max_steps, double cfl, double t_end, double* t_in
     for (int64_t k = 0; k < chunk; ++k) {
       CUDA_TRY(c, cudaGraphLaunch(c->graph[c->cur], c->stream));
       c->cur ^= 1;
+      c->rp_valid = c->d_rp != nullptr;
     }
     launched += chunk;
     if (std::isfinite(t_end) || launched >= max_steps) {
@@ -2638,6 +2700,7 @@ int tg_adapt_state(tg_ctx* dst, tg_ctx* src, const int64_t* source_element, cons
   CUDA_TRY(dst, cudaStreamSynchronize(dst->stream));
   dst->uploaded = true;
   dst->clock_valid = false;
+  dst->rp_valid = false;
   return TG_OK;
 }
 

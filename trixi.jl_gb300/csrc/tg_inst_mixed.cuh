@@ -138,6 +138,74 @@ int TG_CAT(launch_indicator_mixed_, TG_D)(int N, const MixedParams& P, const flo
 #endif
   return -2;
 }
+
+#if TG_D == 2
+// IndicatorHennemannGassner from rho*p of the nodes ([E][N^2], the previous
+// stage kernel's output) instead of the state: hg_indicator_kernel's modal
+// transform (x, then y), energy and logistic in the same order, one thread per
+// element.
+template <int N>
+__global__ void __launch_bounds__(128) hg_alpha_rp_kernel(const MixedParams P,
+                                                          const float* __restrict__ rp,
+                                                          float* __restrict__ alpha_raw) {
+  constexpr int NN = N * N;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.nelements) return;
+  float a[NN], b[NN];
+#pragma unroll
+  for (int q = 0; q < NN; ++q) a[q] = __ldg(rp + e * NN + q);
+#pragma unroll
+  for (int j = 0; j < N; ++j)
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      float r = 0;
+#pragma unroll
+      for (int k = 0; k < N; ++k) r += P.Vinv[i * N + k] * a[k + N * j];
+      b[i + N * j] = r;
+    }
+#pragma unroll
+  for (int j = 0; j < N; ++j)
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      float r = 0;
+#pragma unroll
+      for (int k = 0; k < N; ++k) r += P.Vinv[j * N + k] * b[i + N * k];
+      a[i + N * j] = r;
+    }
+  float clip2 = 0, clip1 = 0, tot = 0;
+#pragma unroll
+  for (int q = 0; q < NN; ++q) {
+    const int mx = max(q % N, q / N);
+    const float m2 = a[q] * a[q];
+    if (mx <= N - 3) clip2 += m2;
+    if (mx <= N - 2) clip1 += m2;
+    tot += m2;
+  }
+  const float f1 = tot != 0.0f ? (tot - clip1) / tot : 0.0f;
+  const float f2 = clip1 != 0.0f ? (clip1 - clip2) / clip1 : 0.0f;
+  const float energy = fmaxf(f1, f2);
+  const float thr = P.hg_threshold;
+  float al = 1.0f / (1.0f + Real<float>::exp(-P.hg_parameter_s / thr * (energy - thr)));
+  if (al < P.alpha_min) al = 0;
+  if (al > 1.0f - P.alpha_min) al = 1;
+  alpha_raw[e] = fminf(P.alpha_max, al);
+}
+
+int launch_hg_alpha_rp(int N, const MixedParams& P, const float* rp, float* alpha,
+                       cudaStream_t s) {
+  const unsigned nb = (unsigned)((P.nelements + 127) / 128);
+  if (nb == 0) return 0;
+  switch (N) {
+    case 2: hg_alpha_rp_kernel<2><<<nb, 128, 0, s>>>(P, rp, alpha); break;
+    case 3: hg_alpha_rp_kernel<3><<<nb, 128, 0, s>>>(P, rp, alpha); break;
+    case 4: hg_alpha_rp_kernel<4><<<nb, 128, 0, s>>>(P, rp, alpha); break;
+    case 5: hg_alpha_rp_kernel<5><<<nb, 128, 0, s>>>(P, rp, alpha); break;
+    case 6: hg_alpha_rp_kernel<6><<<nb, 128, 0, s>>>(P, rp, alpha); break;
+    default: return -2;
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+#endif
 #endif
 
 }  // namespace tg

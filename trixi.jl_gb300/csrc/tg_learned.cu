@@ -299,6 +299,8 @@ struct TcShape {
   static constexpr int STAGE_BYTES = ROWS * NM * 32;
   static constexpr int OSTG = (OSLOT + 8 + 127) / 128 * 128;
   static constexpr int SMEM_STAGED = OSTG + STAGE_BYTES;
+  // deployment from rho*p rows (the stage kernel's output): NM floats per element
+  static constexpr int SMEM_RP = OSTG + ROWS * NM * 4;
   static constexpr int SMEM = OSLOT + 8;
   static constexpr int TCOLS = H;                       // layer 2 reuses layer 1's columns
   static constexpr uint32_t IDESC = tc::idesc_bf16_f32(ROWS, H);
@@ -341,7 +343,9 @@ __device__ __forceinline__ void store_row_split(unsigned char* hi, unsigned char
 
 // SRC 0: features of the elements of the state u (deployment: blending
 // factors with the HG fallback, per-element report); SRC 1: rows of x
-// ([nrows][NM], predictions only).
+// ([nrows][NM], predictions only); SRC 2: deployment as SRC 0 from x = rho*p
+// of the state's nodes ([E][NM], written by the previous stage kernel), the
+// same features without reading the state.
 template <int D, int N, int NM, int H, int SRC, typename TS, typename R>
 __global__ void __launch_bounds__(128) mlp_tc_kernel(
     const FeatParams P, const TS* __restrict__ u, const float* __restrict__ x, int64_t nrows,
@@ -362,17 +366,19 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
   // 2D deployment stages each tile's state with one bulk copy (contiguous in
   // the element order), the next tile's issued as soon as this one's rho*p
   // has been read
-  constexpr bool STAGED = SRC == 0 && D == 2;
+  constexpr bool STAGED = (SRC == 0 && D == 2) || SRC == 2;
+  constexpr int NODE_BYTES = SRC == 2 ? 4 : 32;  // staged bytes per node
   uint64_t* sbar = bar + 1;
   float4* s_stg = reinterpret_cast<float4*>(sm + S::OSTG);
-  const int64_t total = SRC == 0 ? P.E : nrows;
+  const int64_t total = SRC == 1 ? nrows : P.E;
   const int64_t ntiles = (total + S::ROWS - 1) / S::ROWS;
+  const unsigned char* stage_src =
+      SRC == 2 ? reinterpret_cast<const unsigned char*>(x) : reinterpret_cast<const unsigned char*>(u);
   auto issue_tile = [&](int64_t t) {  // one thread
     const int64_t rows = min((int64_t)S::ROWS, total - t * S::ROWS);
-    const uint32_t bytes = (uint32_t)(rows * NM * 32);
+    const uint32_t bytes = (uint32_t)(rows * NM * NODE_BYTES);
     tc::mbar_arrive_expect_tx(sbar, bytes);
-    tc::bulk_g2s(s_stg, reinterpret_cast<const unsigned char*>(u) + (size_t)t * S::ROWS * NM * 32,
-                 bytes, sbar);
+    tc::bulk_g2s(s_stg, stage_src + (size_t)t * S::ROWS * NM * NODE_BYTES, bytes, sbar);
   };
 
   // weights into the K-major operand layouts (W1 zero-padded to K1 columns)
@@ -410,7 +416,7 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
   const uint32_t a1h = tc::smem_u32(sm + S::OA1H), a1l = tc::smem_u32(sm + S::OA1L);
   const uint32_t a2h = tc::smem_u32(sm + S::OA2H), a2l = tc::smem_u32(sm + S::OA2L);
   const uint32_t w1 = tc::smem_u32(sm + S::OW1), w2 = tc::smem_u32(sm + S::OW2);
-  if (SRC == 0 && blockIdx.x == 0 && tid == 0) atomicAdd(&stats[0], (unsigned long long)P.E);
+  if (SRC != 1 && blockIdx.x == 0 && tid == 0) atomicAdd(&stats[0], (unsigned long long)P.E);
 
   uint32_t phase = 0, sphase = 0;
   bool failed = false, mma_in_flight = false, staging_in_flight = STAGED && blockIdx.x < ntiles;
@@ -420,7 +426,7 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
     float xv[NM];
     float energy = 0.0f;
     bool positive = true;
-    if constexpr (SRC == 0) {
+    if constexpr (SRC != 1) {
       // rho*p of the tile's nodes, one node per thread and pass, so that a
       // warp's loads are consecutive nodes; staged in the (free) operand area
       float* s_rp = reinterpret_cast<float*>(sm + S::OA);
@@ -436,7 +442,9 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
 #pragma unroll 4
         for (int j = 0; j < NM; ++j) {
           const int k = j * S::ROWS + tid;
-          if (k < nn) s_rp[(k / NM) * (NM + 1) + k % NM] = staged_rho_p<TS>(P, s_stg, k);
+          if (k < nn)
+            s_rp[(k / NM) * (NM + 1) + k % NM] =
+                SRC == 2 ? reinterpret_cast<const float*>(s_stg)[k] : staged_rho_p<TS>(P, s_stg, k);
         }
         __syncthreads();
         // the staging buffer is free: the next tile's state lands meanwhile
@@ -810,7 +818,7 @@ static int launch_tc(tg_mlp* m, const FeatParams& P, const TS* u, const float* x
                      cudaStream_t s) {
   using S = TcShape<NM, H>;
   auto kern = mlp_tc_kernel<D, N, NM, H, SRC, TS, R>;
-  constexpr int SMEM = (SRC == 0 && D == 2) ? S::SMEM_STAGED : S::SMEM;
+  constexpr int SMEM = SRC == 2 ? S::SMEM_RP : ((SRC == 0 && D == 2) ? S::SMEM_STAGED : S::SMEM);
   static int resident[64] = {0};  // blocks per SM, per device
   int dev = 0;
   MCUDA(m, cudaGetDevice(&dev));
@@ -863,6 +871,7 @@ static int launch_predict(tg_mlp* m, const float* x, int64_t M, float* pred, cud
 
 namespace tg {
 int32_t* ctx_status_word(tg_ctx* c);
+const float* ctx_state_rho_p(tg_ctx* c);
 
 // Called by the context before every stage when the learned indicator is on:
 // writes the blending factors (unsmoothed) into alpha_raw (R = float for mixed
@@ -894,8 +903,13 @@ int mlp_alpha(tg_mlp* m, tg_ctx* c, void* alpha_raw, bool fp64, float alpha_min,
   A.alpha_max = alpha_max;
   cudaStream_t s = (cudaStream_t)stream;
   int32_t* status = ctx_status_word(c);
+  // rho*p of the state from the previous stage kernel, when the context keeps it
+  const float* rp = ctx_state_rho_p(c);
 #define DEPLOY(DD, NN, NMv, Hv)                                                                 \
   if (D == DD && N == NN) {                                                                     \
+    if (ff && rp && DD == 2)                                                                    \
+      return launch_tc<DD, NN, NMv, Hv, 2, float2, float>(                                      \
+          m, P, nullptr, rp, E, A, (float*)alpha_raw, m->d_pred, status, s);                    \
     if (ff)                                                                                     \
       return launch_tc<DD, NN, NMv, Hv, 0, float2, float>(                                      \
           m, P, (const float2*)state, nullptr, E, A, (float*)alpha_raw, m->d_pred, status, s);  \

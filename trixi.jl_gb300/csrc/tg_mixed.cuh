@@ -86,6 +86,10 @@ struct MixedArgs {
   const float* alpha_raw;   // VI_HG
   const float* alpha_smoothed;  // VI_HG, persistent 2D kernel: alpha_raw after apply_smoothing!
   float* alpha_out;         // VI_HG (optional)
+  // MODE_STAGE (optional): rho*p of u_out per node (FP32 on the hi parts, as
+  // the indicators compute it), read by the next stage's indicator instead of
+  // the whole state
+  float* rp_out;
   const Clock* clock;
   unsigned long long* speed_bits;
   int32_t* status;
@@ -1038,6 +1042,7 @@ __device__ __forceinline__ void mixed_node_update(const MixedParams& P, const Mi
       hi[v] = un.x;
       bad |= !(un.x == un.x);
     }
+    if (A.rp_out) A.rp_out[g / NV] = Euler<D, float>::density_pressure(hi, gamma);
     if (A.speed_bits) {
       float w[NV];
       Euler<D, float>::cons2prim(hi, w, gamma);

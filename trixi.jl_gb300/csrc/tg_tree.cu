@@ -31,6 +31,63 @@ namespace {
 
 constexpr int kMaxLevel = 15;
 
+// Cell key -> cell id, open addressing with linear probing (capacity a power
+// of two, at most half full).  A key is re-pointed when a coarsened cell is
+// refined again; keys are never removed (dead cells are told apart by the
+// tree's alive flags and dropped when the tree is compacted).
+struct CellIndex {
+  static constexpr uint64_t kEmpty = ~0ull;  // no key: the level field is at most 15
+  std::vector<uint64_t> keys;
+  std::vector<int64_t> vals;
+  size_t count = 0;
+
+  static size_t hash(uint64_t k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    return (size_t)k;
+  }
+  void clear(size_t expected) {
+    size_t cap = 64;
+    while (cap < 2 * expected + 2) cap <<= 1;
+    keys.assign(cap, kEmpty);
+    vals.assign(cap, -1);
+    count = 0;
+  }
+  void put(uint64_t k, int64_t v) {
+    if (2 * (count + 1) > keys.size()) {
+      std::vector<uint64_t> ok;
+      std::vector<int64_t> ov;
+      ok.swap(keys);
+      ov.swap(vals);
+      clear(ok.size());
+      for (size_t i = 0; i < ok.size(); ++i)
+        if (ok[i] != kEmpty) put(ok[i], ov[i]);
+    }
+    const size_t mask = keys.size() - 1;
+    for (size_t i = hash(k) & mask;; i = (i + 1) & mask) {
+      if (keys[i] == k) {
+        vals[i] = v;
+        return;
+      }
+      if (keys[i] == kEmpty) {
+        keys[i] = k;
+        vals[i] = v;
+        ++count;
+        return;
+      }
+    }
+  }
+  int64_t get(uint64_t k) const {
+    if (keys.empty()) return -1;
+    const size_t mask = keys.size() - 1;
+    for (size_t i = hash(k) & mask;; i = (i + 1) & mask) {
+      if (keys[i] == k) return vals[i];
+      if (keys[i] == kEmpty) return -1;
+    }
+  }
+};
+
 }  // namespace
 
 struct tg_tree {
@@ -42,7 +99,9 @@ struct tg_tree {
   std::vector<int32_t> ix;      // [cell][3]
   std::vector<double> center;   // [cell][3]
   std::vector<int64_t> child0;  // first child, -1 for a leaf
-  std::unordered_map<uint64_t, int64_t> index;
+  std::vector<uint8_t> alive;   // 0: a child removed by coarsen!
+  int64_t nalive = 0;
+  CellIndex index;
   std::vector<int64_t> leaves;  // the elements, in order
   // transfer map of the last adaptation
   std::vector<int64_t> map_source;
@@ -59,8 +118,8 @@ struct tg_tree {
   double length(int lev) const { return length0 / (double)(1LL << lev); }
 
   int64_t find(int lev, const int32_t* p) const {
-    auto it = index.find(key(lev, p));
-    return it == index.end() ? -1 : it->second;
+    const int64_t id = index.get(key(lev, p));
+    return id >= 0 && alive[id] ? id : -1;
   }
   int64_t add(int lev, const int32_t* p, const double* c) {
     const int64_t id = ncells();
@@ -70,8 +129,51 @@ struct tg_tree {
       center.push_back(c[d]);
     }
     child0.push_back(-1);
-    index[key(lev, p)] = id;
+    alive.push_back(1);
+    ++nalive;
+    index.put(key(lev, p), id);
     return id;
+  }
+  // Drops the dead cells: the live ones renumbered breadth-first (children
+  // stay consecutive behind their first child), the index rebuilt.  The
+  // elements keep their order.
+  void compact() {
+    const int nch = 1 << D;
+    std::vector<int64_t> order{0}, newid(ncells(), -1);
+    order.reserve((size_t)nalive);
+    newid[0] = 0;
+    for (size_t i = 0; i < order.size(); ++i) {
+      const int64_t c = order[i];
+      if (child0[c] < 0) continue;
+      for (int ch = 0; ch < nch; ++ch) {
+        newid[child0[c] + ch] = (int64_t)order.size();
+        order.push_back(child0[c] + ch);
+      }
+    }
+    const size_t n = order.size();
+    std::vector<int8_t> lv(n);
+    std::vector<int32_t> p(3 * n);
+    std::vector<double> x(3 * n);
+    std::vector<int64_t> c0(n);
+    for (size_t i = 0; i < n; ++i) {
+      const int64_t c = order[i];
+      lv[i] = level[c];
+      for (int d = 0; d < 3; ++d) {
+        p[3 * i + d] = ix[3 * c + d];
+        x[3 * i + d] = center[3 * c + d];
+      }
+      c0[i] = child0[c] < 0 ? -1 : newid[child0[c]];
+    }
+    level.swap(lv);
+    ix.swap(p);
+    center.swap(x);
+    child0.swap(c0);
+    alive.assign(n, 1);
+    nalive = (int64_t)n;
+    index.clear(n);
+    for (size_t i = 0; i < n; ++i) index.put(key(level[i], &ix[3 * i]), (int64_t)i);
+    for (int64_t& c : leaves) c = newid[c];
+    containers_valid = false;
   }
   // same-level neighbour across face `dir` (0: -x, 1: +x, 2: -y, ...), or -1
   int64_t neighbour(int64_t c, int dir) const {
@@ -163,7 +265,8 @@ struct tg_tree {
           }
         }
       if (skip) continue;
-      for (int ch = 0; ch < (1 << D); ++ch) index.erase(key(level[first + ch], &ix[3 * (first + ch)]));
+      for (int ch = 0; ch < (1 << D); ++ch) alive[first + ch] = 0;
+      nalive -= 1 << D;
       child0[c] = -1;
       done.emplace_back(c, first);
     }
@@ -246,7 +349,7 @@ int tg_tree_create(int32_t ndims, int32_t initial_refinement_level, const double
     t->periodic[d] = periodicity ? periodicity[d] != 0 : true;
   }
   const int64_t expect = (int64_t)1 << (ndims * initial_refinement_level);
-  t->index.reserve((size_t)(expect * 1.5) + 16);
+  t->index.clear((size_t)(expect * 1.5) + 16);
   const int32_t root[3] = {0, 0, 0};
   t->add(0, root, c0);
   t->rebuild_leaves();
@@ -382,6 +485,9 @@ int tg_tree_adapt(tg_tree* t, const int8_t* controller_value, int32_t only_refin
       t->map_kind[e] = (int8_t)(1 + (c - t->child0[p]));
     }
   }
+  // the cells coarsened away stay in the arrays until they outnumber the live
+  // ones
+  if (t->ncells() > 2 * t->nalive) t->compact();
   *changed = 1;
   return TG_OK;
 }

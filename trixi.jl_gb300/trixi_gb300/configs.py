@@ -26,8 +26,9 @@
   c7   mortars: 3D MMS 32^3 with the central box refined once, against the
        uniform 32^3 mesh, FP64 and mixed.
   c8   curvilinear meshes: the waving-flag StructuredMesh MMS (weak form) and a
-       warped P4estMesh weak blast wave (flux differencing) at 512^2, FP64 and
-       mixed.
+       warped P4estMesh weak blast wave (flux differencing) at 512^2, the Sedov
+       blast with shock capturing on a warped StructuredMesh at 512^2 and the
+       3D warped-cube EC elixir at 32^3, FP64 and mixed.
 
 The 3D manufactured solution at 32^3 is the headline case of bench.py.
 Throughput is DOF-updates per second per RK stage (ndofs x 5 stages x steps /
@@ -541,7 +542,53 @@ def _warped_square(xi_, eta_):
     return x, y
 
 
-def c8(cells=512, steps=30, t_end=0.25):
+def _warped_cube(xi_, eta_, zeta_):
+    # examples/structured_3d_dgsem/elixir_euler_ec.jl / elixir_euler_free_stream.jl
+    xi, eta, zeta = 1.5 * xi_ + 1.5, 1.5 * eta_ + 1.5, 1.5 * zeta_ + 1.5
+    y = eta + 3 / 8 * (np.cos(1.5 * np.pi * (2 * xi - 3) / 3) * np.cos(0.5 * np.pi * (2 * eta - 3) / 3) *
+                       np.cos(0.5 * np.pi * (2 * zeta - 3) / 3))
+    x = xi + 3 / 8 * (np.cos(0.5 * np.pi * (2 * xi - 3) / 3) * np.cos(2 * np.pi * (2 * y - 3) / 3) *
+                      np.cos(0.5 * np.pi * (2 * zeta - 3) / 3))
+    z = zeta + 3 / 8 * (np.cos(0.5 * np.pi * (2 * x - 3) / 3) * np.cos(np.pi * (2 * y - 3) / 3) *
+                        np.cos(0.5 * np.pi * (2 * zeta - 3) / 3))
+    return x, y, z
+
+
+def _sedov_warp(xi, eta):
+    # examples/structured_2d_dgsem/elixir_euler_sedov.jl
+    y = eta + 0.125 * (np.cos(1.5 * np.pi * xi) * np.cos(0.5 * np.pi * eta))
+    x = xi + 0.125 * (np.cos(0.5 * np.pi * xi) * np.cos(2 * np.pi * y))
+    return x, y
+
+
+def curved3_semi(cells, precision):
+    """The EC elixir of the 3D StructuredMesh examples at cells^3, polydeg 3:
+    weak blast wave (gamma 5/3) on the warped cube, flux_ranocha volume and
+    surface flux."""
+    eq = T.CompressibleEulerEquations3D(5.0 / 3.0)
+    solver = T.DGSEM(polydeg=3, surface_flux=T.flux_ranocha,
+                     volume_integral=T.VolumeIntegralFluxDifferencing(T.flux_ranocha))
+    mesh = T.StructuredMesh((cells,) * 3, mapping=_warped_cube)
+    return T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_weak_blast_wave, solver,
+                                          precision=precision)
+
+
+def sedov_semi(cells, precision):
+    """The Sedov blast of the 2D StructuredMesh examples at cells^2, polydeg 3:
+    shock capturing (HG on rho*p, alpha_max 1, flux_ranocha / naive LLF FV)
+    on the warped square, naive LLF surface flux."""
+    eq = T.CompressibleEulerEquations2D(1.4)
+    basis = T.LobattoLegendreBasis(3)
+    llf = T.FluxLaxFriedrichs(T.max_abs_speed_naive)
+    ind = T.IndicatorHennemannGassner(eq, basis, alpha_max=1.0, alpha_min=0.001,
+                                      alpha_smooth=True, variable=T.density_pressure)
+    vi = T.VolumeIntegralShockCapturingHG(ind, volume_flux_dg=T.flux_ranocha, volume_flux_fv=llf)
+    mesh = T.StructuredMesh((cells, cells), mapping=_sedov_warp)
+    return T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_sedov_blast_wave,
+                                          T.DGSEM(basis, llf, vi), precision=precision)
+
+
+def c8(cells=512, steps=30, t_end=0.25, cells3=32):
     """Curvilinear 2D meshes: (a) the waving-flag StructuredMesh MMS at cells^2,
     polydeg 3, weak form, naive LLF, CFL 0.8 (L2 density error at t_end of both
     paths); (b) the weak blast wave on the warped square as a P4estMesh of
@@ -579,6 +626,19 @@ def c8(cells=512, steps=30, t_end=0.25):
         out[f"{name}_speedup"] = out[f"{name}_mixed"]["rate"] / out[f"{name}_fp64"]["rate"]
     out["flag_l2_rho_mixed_over_fp64"] = (out["flag_weak_mixed"]["l2_rho"] /
                                           out["flag_weak_fp64"]["l2_rho"])
+    # (c) 3D: the warped-cube EC elixir at cells3^3; (d) shock capturing: the
+    # Sedov blast on the warped square at cells^2
+    for name, make, cfl in (("cube3d_fd_ranocha", lambda p: curved3_semi(cells3, p), 1.0),
+                            ("sedov_hg", lambda p: sedov_semi(cells, p), 0.5)):
+        for prec in ("mixed", "fp64"):
+            semi = make(prec)
+            solve_timed(semi, 10.0, cfl, max_steps=3)  # warm-up
+            n_steps = steps if prec == "mixed" else max(3, steps // 3)
+            _, t, n, secs = solve_timed(semi, 10.0, cfl, max_steps=n_steps)
+            out[f"{name}_{prec}"] = dict(elements=semi.nelements, steps=n, secs=secs,
+                                         rate=rate(semi.ndofs, n, secs))
+            del semi
+        out[f"{name}_speedup"] = out[f"{name}_mixed"]["rate"] / out[f"{name}_fp64"]["rate"]
     return out
 
 
@@ -611,6 +671,14 @@ def curved_steps(steps=3, cells=512):
     return dict(steps=n, t=t)
 
 
+def curved3_steps(steps=3, cells=32):
+    """c8's 3D warped-cube EC case (cells^3, polydeg 3, flux_ranocha), mixed
+    precision, `steps` steps."""
+    semi = curved3_semi(cells, "mixed")
+    _, t, n, secs = solve_timed(semi, 10.0, 1.0, max_steps=steps)
+    return dict(steps=n, t=t)
+
+
 def c5b_64():
     """C5b at its full size: 64^3, mixed and FP64 both to t = 20."""
     return c5b(levels=((6, 20.0, 20.0),), control_level=None)
@@ -618,7 +686,8 @@ def c5b_64():
 
 RUNS = dict(c1=c1, c3=c3, c4=c4, c5a=c5a, c5b=c5b, c5b_64=c5b_64, c6=c6, c7=c7, c8=c8)
 SHORT_RUNS = dict(learned_steps=learned_steps, mms_steps=mms_steps, ensemble_steps=ensemble_steps,
-                  mortar_steps=mortar_steps, curved_steps=curved_steps)
+                  mortar_steps=mortar_steps, curved_steps=curved_steps,
+                  curved3_steps=curved3_steps)
 
 
 def main(argv=None):
