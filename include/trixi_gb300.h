@@ -238,7 +238,10 @@ int tg_upload_state(tg_ctx* ctx, const double* u_host);
 int tg_download_state(tg_ctx* ctx, double* u_host);
 
 /* Device pointer of the current solution buffer.  The solution ping-pongs
- * between two buffers during tg_rk_stage/tg_step: query again after them. */
+ * between two buffers during tg_rk_stage/tg_step: query again after them.
+ * The state may be written through it until then; the per-node indicator
+ * input that mixed 2D shock-capturing stage kernels keep for the next stage
+ * (rho*p of their output) is recomputed by the next tg_step or tg_rk_stage. */
 int tg_state_device_ptr(tg_ctx* ctx, double** u_dev);
 
 /* rhs_hyperbolic!(du, u, t): du and u are DEVICE pointers in Trixi's layout

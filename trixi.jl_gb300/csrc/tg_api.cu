@@ -1106,9 +1106,9 @@ const float* ctx_state_rho_p(tg_ctx* c);
 }
 
 // Blending factors of a state in the context representation: the HG (or
-// learned) indicator, unsmoothed, into d_alpha_raw; for mixed 2D contexts also
-// apply_smoothing! into d_alpha_sm, which the persistent 2D stage kernel
-// copies with the element block (the other kernels smooth inline).
+// learned) indicator, unsmoothed, into d_alpha_raw; for mixed TreeMesh
+// contexts also apply_smoothing! into d_alpha_sm, which the persistent stage
+// kernel copies with the element block (the other kernels smooth inline).
 static int indicator(tg_ctx* c, const void* u) {
   if (c->vi != VI_HG) return TG_OK;
   int rc;
@@ -1132,7 +1132,7 @@ static int indicator(tg_ctx* c, const void* u) {
                                     c->stream);
     if (rc != 0) return fail(c, TG_ERR_CUDA, "indicator kernel launch failed (%d)", rc);
   }
-  if (!c->fp64 && c->D == 2 && !c->curved) {
+  if (!c->fp64 && !c->curved) {
     smooth_alpha_kernel<float, float><<<(unsigned)((c->E + 255) / 256), 256, 0, c->stream>>>(
         (const float*)c->d_alpha_raw, c->d_nbr, c->E, 2 * c->D, c->P.alpha_smooth, c->P.nbc,
         c->d_mnbr, c->d_alpha_sm);
@@ -1827,7 +1827,8 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   ALLOC(c->d_u[0], vb);
   ALLOC(c->d_u[1], vb);
   ALLOC(c->d_utmp, rsize(c) * (size_t)c->nvalues);
-  ALLOC(c->d_nbr, sizeof(int32_t) * nbr.size());
+  // padded: the stage kernels' bulk copies read neighbour rows in 16-byte groups
+  ALLOC(c->d_nbr, sizeof(int32_t) * nbr.size() + 16);
   if (c->nbound > 0) ALLOC(c->d_bface, sizeof(int32_t) * bface.size());
   if (!c->fp64 && c->nbound + c->nmface > 0)
     ALLOC(c->d_ghost, sizeof(float2) * (size_t)(c->nbound + c->nmface) * (c->NN / N) * c->NV);
@@ -1949,6 +1950,7 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     }
   }
   cudaMemcpy(c->d_nbr, nbr.data(), sizeof(int32_t) * nbr.size(), cudaMemcpyHostToDevice);
+  cudaMemset(c->d_nbr + nbr.size(), 0, 16);
   if (c->nbound > 0)
     cudaMemcpy(c->d_bface, bface.data(), sizeof(int32_t) * bface.size(), cudaMemcpyHostToDevice);
   if (nm > 0) {

@@ -1253,9 +1253,10 @@ struct MixedPipe {
 };
 
 // Bulk copies of element block blk's contiguous inputs into buffer `buf`
-// (thread 0).  2D sizes are multiples of 16 bytes for every polydeg; the
-// per-element float arrays are read in whole 16-byte groups (allocated with
-// padding).
+// (thread 0).  The state and u_tmp chunks are multiples of 16 bytes for every
+// polydeg in 2D and for even N^3 in 3D; the neighbour rows (2D ints per
+// element) and the per-element float arrays are read in whole 16-byte groups
+// (allocated with padding), starting on 16-byte boundaries for EPB % 4 == 0.
 template <int D, int N, int VI, int EPB>
 __device__ __forceinline__ void mixed_pipe_issue(const MixedParams& P, const MixedArgs& A,
                                                  int64_t blk, unsigned char* buf, uint64_t* mbar) {
@@ -1267,7 +1268,10 @@ __device__ __forceinline__ void mixed_pipe_issue(const MixedParams& P, const Mix
   const uint32_t b_u = (uint32_t)(sizeof(float2) * nel * NN * NV);
   const bool need_ut = A.mode == MODE_STAGE && !A.zero_tmp;
   const uint32_t b_ut = need_ut ? (uint32_t)(sizeof(float) * nel * NN * NV) : 0u;
-  const uint32_t b_nbr = (uint32_t)(sizeof(int32_t) * nel * 2 * D);
+  // every source address below is 16-byte aligned: e0 is a multiple of EPB
+  static_assert(EPB % 4 == 0, "per-element float rows of a block start on 16-byte boundaries");
+  static_assert((Pow<N, D>::value * (D + 2)) % 2 == 0, "state chunks of whole 16-byte groups");
+  const uint32_t b_nbr = (uint32_t)Q::up(sizeof(int32_t) * nel * 2 * D);
   const uint32_t b_el = (uint32_t)Q::up(sizeof(float) * nel);
   const uint32_t b_al = VI == VI_HG ? b_el : 0u;
   tc::mbar_arrive_expect_tx(mbar, b_u + b_ut + b_nbr + b_al + b_el);

@@ -684,7 +684,26 @@ def c5b_64():
     return c5b(levels=((6, 20.0, 20.0),), control_level=None)
 
 
-RUNS = dict(c1=c1, c3=c3, c4=c4, c5a=c5a, c5b=c5b, c5b_64=c5b_64, c6=c6, c7=c7, c8=c8)
+def c5b_64_control(eps=1e-9, dt_out=0.25):
+    """How far two mixed runs at 64^3 drift apart through the turbulent phase when
+    one starts from the initial state perturbed by eps (relative): the growth of
+    a perturbation of the size of the mixed path's early difference to FP64."""
+    r = {}
+    for name, e in (("mixed", 0.0), ("mixed_perturbed", eps)):
+        semi = tgv_semi(6, "mixed")
+        hist, steps, secs = _ke_history(semi, 20.0, dt_out, perturb=e)
+        r[name] = dict(ke=hist, steps=steps, secs=secs)
+        del semi
+    ka = {round(t, 9): k for t, k in r["mixed_perturbed"]["ke"]}
+    diffs = [(t, abs(ka[round(t, 9)] - k) / k) for t, k in r["mixed"]["ke"] if round(t, 9) in ka]
+    r["ke_rel_diff"] = diffs
+    r["ke_rel_diff_max"] = float(max(d for _, d in diffs))
+    r["ke_rel_diff_final"] = float(diffs[-1][1])
+    return r
+
+
+RUNS = dict(c1=c1, c3=c3, c4=c4, c5a=c5a, c5b=c5b, c5b_64=c5b_64, c5b_64_control=c5b_64_control,
+            c6=c6, c7=c7, c8=c8)
 SHORT_RUNS = dict(learned_steps=learned_steps, mms_steps=mms_steps, ensemble_steps=ensemble_steps,
                   mortar_steps=mortar_steps, curved_steps=curved_steps,
                   curved3_steps=curved3_steps)
