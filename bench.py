@@ -262,9 +262,9 @@ def timed_stage_parts(ctx, cfl, reps, flush):
     return out
 
 
-def khi_semi(level, precision):
+def khi_semi(level, precision, epb=0):
     from trixi_gb300 import configs as C
-    return C.khi_semi(level, precision)
+    return C.khi_semi(level, precision, epb)
 
 
 def khi_rho_samples(semi, u, npts=KHI_SAMPLE):
@@ -362,8 +362,8 @@ def khi_arm(args, rank: int, world: int):
     train_secs = time.perf_counter() - setup_t0
 
     # ---- accuracy (untimed): t = 0 -> 0.5, learned and FP64 at 512^2, 1024^2 reference
-    semi_ml = khi_semi(KHI_LEVEL, "mixed")
-    semi_hg = khi_semi(KHI_LEVEL, "mixed")
+    semi_ml = khi_semi(KHI_LEVEL, "mixed", args.epb)
+    semi_hg = khi_semi(KHI_LEVEL, "mixed", args.epb)
     semi_64 = khi_semi(KHI_LEVEL, "fp64")
     u0 = semi_ml.compute_coefficients(0.0)
     ctx_ml, ctx_hg, ctx_64 = semi_ml.device_context, semi_hg.device_context, semi_64.device_context

@@ -111,7 +111,7 @@ def vortex_semi(level, polydeg, eps, precision, surface_flux=None):
     return T.SemidiscretizationHyperbolic(mesh, eq, ic, solver, precision=precision)
 
 
-def khi_semi(level, precision):
+def khi_semi(level, precision, elements_per_block=0):
     eq = T.CompressibleEulerEquations2D(1.4)
     basis = T.LobattoLegendreBasis(3)
     ind = T.IndicatorHennemannGassner(eq, basis, alpha_max=0.002, alpha_min=0.0001,
@@ -121,7 +121,8 @@ def khi_semi(level, precision):
     solver = T.DGSEM(basis, T.flux_lax_friedrichs, vi)
     mesh = T.TreeMesh((-1.0, -1.0), (1.0, 1.0), initial_refinement_level=level)
     return T.SemidiscretizationHyperbolic(mesh, eq, T.initial_condition_kelvin_helmholtz_instability,
-                                          solver, precision=precision)
+                                          solver, precision=precision,
+                                          elements_per_block=elements_per_block)
 
 
 def blast_semi(level, precision):
