@@ -237,6 +237,31 @@ int tg_ndofs(const tg_ctx* ctx, int64_t* ndofs, int64_t* nvalues);
 int tg_upload_state(tg_ctx* ctx, const double* u_host);
 int tg_download_state(tg_ctx* ctx, double* u_host);
 
+/* Host transfers that overlap the time stepping: the copies run on the
+ * context's two copy streams (one per direction, through two FP64 device
+ * staging slots each) while its own stream computes.  Host buffers are in
+ * Trixi's layout, should be page-locked (pageable memory works but does not
+ * overlap), and must stay valid until the transfer has completed.
+ *   tg_prefetch_state  starts copying u_host into staging slot 0 or 1 and
+ *                      returns at once (it waits, on the device, until the
+ *                      slot's previous contents were loaded);
+ *   tg_load_prefetched makes the slot's state the context's state, in the
+ *                      order of the calls that enqueue work on the context
+ *                      (a following tg_step uses it; the device waits for
+ *                      the copy, the host does not);
+ *   tg_fetch_state     enqueues the copy of the current state to u_host
+ *                      through staging slot 0 or 1 and returns at once;
+ *   tg_transfer_wait   blocks until the slot's prefetch copy (direction 0)
+ *                      or fetch (direction 1) has completed;
+ *   tg_transfer_join   makes the context stream wait for every transfer
+ *                      issued so far (work enqueued after it starts when
+ *                      they are done). */
+int tg_prefetch_state(tg_ctx* ctx, int32_t slot, const double* u_host);
+int tg_load_prefetched(tg_ctx* ctx, int32_t slot);
+int tg_fetch_state(tg_ctx* ctx, int32_t slot, double* u_host);
+int tg_transfer_wait(tg_ctx* ctx, int32_t slot, int32_t direction);
+int tg_transfer_join(tg_ctx* ctx);
+
 /* Device pointer of the current solution buffer.  The solution ping-pongs
  * between two buffers during tg_rk_stage/tg_step: query again after them.
  * The state may be written through it until then; the per-node indicator

@@ -967,6 +967,16 @@ struct tg_ctx {
   // stage kernel that produced it (rp_valid), read by the next indicator
   float* d_rp = nullptr;
   bool rp_valid = false;
+  // host transfers that overlap the stepping (tg_prefetch_state, tg_fetch_state):
+  // copy streams (0: host to device, 1: device to host), FP64 staging slots
+  // and the events that order them with the context stream
+  cudaStream_t xstream[2] = {nullptr, nullptr};
+  double* d_xin[2] = {nullptr, nullptr};
+  double* d_xout[2] = {nullptr, nullptr};
+  cudaEvent_t ev_in_copied[2] = {nullptr, nullptr}, ev_in_used[2] = {nullptr, nullptr};
+  cudaEvent_t ev_out_ready[2] = {nullptr, nullptr}, ev_out_done[2] = {nullptr, nullptr};
+  bool in_pending[2] = {false, false}, in_used_rec[2] = {false, false};
+  bool out_done_rec[2] = {false, false};
   int32_t* d_nbr = nullptr;
   double* d_invj = nullptr;
   double* d_xline = nullptr;
@@ -1058,8 +1068,17 @@ static void free_ctx(tg_ctx* c) {
                   c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_alpha_sm, c->d_rp, c->d_nbr, c->d_invj, c->d_xline,
                   c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mmat32, c->d_mflux, c->d_scls, c->d_amr_raw, c->d_amr_alpha, c->d_amap, c->d_akind, c->d_weights, c->d_cmet, c->d_csnv, c->d_csnv32, c->d_cja32, c->d_cinvj32, c->d_cxy, c->d_csc, c->d_partial, c->d_enorm, c->d_sums, c->d_clock,
                   c->d_status, c->d_speed};
+  for (int k = 0; k < 2; ++k)
+    if (c->xstream[k]) cudaStreamSynchronize(c->xstream[k]);
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (int k = 0; k < 2; ++k) {
+    if (c->d_xin[k]) cudaFree(c->d_xin[k]);
+    if (c->d_xout[k]) cudaFree(c->d_xout[k]);
+    for (cudaEvent_t ev : {c->ev_in_copied[k], c->ev_in_used[k], c->ev_out_ready[k], c->ev_out_done[k]})
+      if (ev) cudaEventDestroy(ev);
+    if (c->xstream[k]) cudaStreamDestroy(c->xstream[k]);
+  }
   for (double* p : c->vectors) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -2184,6 +2203,92 @@ int tg_download_state(tg_ctx* c, double* u_host) {
   CUDA_TRY(c, cudaMemcpyAsync(u_host, src, sizeof(double) * c->nvalues, cudaMemcpyDeviceToHost,
                               c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return TG_OK;
+}
+
+// ---- host transfers overlapping the stepping ---------------------------------
+static int xfer_setup(tg_ctx* c, int32_t slot, bool out) {
+  if (slot < 0 || slot > 1) return fail(c, TG_ERR_INVALID_ARGUMENT, "transfer slot must be 0 or 1");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  for (int k = 0; k < 2; ++k)
+    if (!c->xstream[k]) CUDA_TRY(c, cudaStreamCreateWithFlags(&c->xstream[k], cudaStreamNonBlocking));
+  for (cudaEvent_t* ev : {&c->ev_in_copied[slot], &c->ev_in_used[slot], &c->ev_out_ready[slot],
+                          &c->ev_out_done[slot]})
+    if (!*ev) CUDA_TRY(c, cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+  double** buf = out ? &c->d_xout[slot] : &c->d_xin[slot];
+  if (!*buf) CUDA_TRY(c, cudaMalloc((void**)buf, sizeof(double) * c->nvalues));
+  return TG_OK;
+}
+
+int tg_prefetch_state(tg_ctx* c, int32_t slot, const double* u_host) {
+  if (!c || !u_host) return TG_ERR_INVALID_ARGUMENT;
+  int rc = xfer_setup(c, slot, false);
+  if (rc) return rc;
+  // the slot's previous contents must have been loaded before they are replaced
+  if (c->in_used_rec[slot]) CUDA_TRY(c, cudaStreamWaitEvent(c->xstream[0], c->ev_in_used[slot], 0));
+  CUDA_TRY(c, cudaMemcpyAsync(c->d_xin[slot], u_host, sizeof(double) * c->nvalues,
+                              cudaMemcpyHostToDevice, c->xstream[0]));
+  CUDA_TRY(c, cudaEventRecord(c->ev_in_copied[slot], c->xstream[0]));
+  c->in_pending[slot] = true;
+  return TG_OK;
+}
+
+int tg_load_prefetched(tg_ctx* c, int32_t slot) {
+  if (!c) return TG_ERR_INVALID_ARGUMENT;
+  if (slot < 0 || slot > 1 || !c->in_pending[slot])
+    return fail(c, TG_ERR_STATE, "no state prefetched into slot %d", slot);
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_in_copied[slot], 0));
+  int rc = import_state(c, c->d_xin[slot], c->d_u[c->cur]);
+  if (rc) return rc;
+  CUDA_TRY(c, cudaEventRecord(c->ev_in_used[slot], c->stream));
+  c->in_used_rec[slot] = true;
+  c->in_pending[slot] = false;
+  c->uploaded = true;
+  c->clock_valid = false;
+  c->rp_valid = false;
+  return TG_OK;
+}
+
+int tg_fetch_state(tg_ctx* c, int32_t slot, double* u_host) {
+  if (!c || !u_host) return TG_ERR_INVALID_ARGUMENT;
+  int rc = xfer_setup(c, slot, true);
+  if (rc) return rc;
+  // the slot's previous copy to the host must have finished before it is reused
+  if (c->out_done_rec[slot]) CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_out_done[slot], 0));
+  if (c->fp64) {
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_xout[slot], c->d_u[c->cur], sizeof(double) * c->nvalues,
+                                cudaMemcpyDeviceToDevice, c->stream));
+  } else {
+    from_ff_kernel<<<conv_blocks(c->nvalues), 256, 0, c->stream>>>(
+        (const float2*)c->d_u[c->cur], c->d_xout[slot], c->nvalues);
+    CUDA_TRY(c, cudaGetLastError());
+  }
+  CUDA_TRY(c, cudaEventRecord(c->ev_out_ready[slot], c->stream));
+  CUDA_TRY(c, cudaStreamWaitEvent(c->xstream[1], c->ev_out_ready[slot], 0));
+  CUDA_TRY(c, cudaMemcpyAsync(u_host, c->d_xout[slot], sizeof(double) * c->nvalues,
+                              cudaMemcpyDeviceToHost, c->xstream[1]));
+  CUDA_TRY(c, cudaEventRecord(c->ev_out_done[slot], c->xstream[1]));
+  c->out_done_rec[slot] = true;
+  return TG_OK;
+}
+
+int tg_transfer_wait(tg_ctx* c, int32_t slot, int32_t direction) {
+  if (!c || slot < 0 || slot > 1 || direction < 0 || direction > 1) return TG_ERR_INVALID_ARGUMENT;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  const cudaEvent_t ev = direction == 0 ? c->ev_in_copied[slot] : c->ev_out_done[slot];
+  const bool rec = direction == 0 ? (c->in_pending[slot] || c->in_used_rec[slot]) : c->out_done_rec[slot];
+  if (ev && rec) CUDA_TRY(c, cudaEventSynchronize(ev));
+  return TG_OK;
+}
+
+int tg_transfer_join(tg_ctx* c) {
+  if (!c) return TG_ERR_INVALID_ARGUMENT;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  for (int k = 0; k < 2; ++k) {
+    if (c->out_done_rec[k]) CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_out_done[k], 0));
+    if (c->in_pending[k]) CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_in_copied[k], 0));
+  }
   return TG_OK;
 }
 

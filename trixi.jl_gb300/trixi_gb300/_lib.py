@@ -29,7 +29,8 @@ TG_BOUNDARY_PERIODIC, TG_BOUNDARY_DIRICHLET, TG_BOUNDARY_SLIP_WALL = 0, 1, 2
 
 # Every symbol declared in include/trixi_gb300.h.
 EXPORTS = ("tg_api_version", "tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ndofs",
-           "tg_upload_state", "tg_download_state", "tg_state_device_ptr", "tg_rhs",
+           "tg_upload_state", "tg_download_state", "tg_prefetch_state", "tg_load_prefetched",
+           "tg_fetch_state", "tg_transfer_wait", "tg_transfer_join", "tg_state_device_ptr", "tg_rhs",
            "tg_rhs_host", "tg_max_dt", "tg_rk_stage", "tg_rk_stage_part", "tg_step", "tg_set_time",
            "tg_integrals", "tg_alpha", "tg_status", "tg_synchronize",
            "tg_elements_per_block", "tg_stream", "tg_integrals_noalloc",
@@ -119,6 +120,11 @@ def load(path: str | None = None):
         "tg_ndofs": ([vp, P(i64), P(i64)], ctypes.c_int),
         "tg_upload_state": ([vp, vp], ctypes.c_int),
         "tg_download_state": ([vp, vp], ctypes.c_int),
+        "tg_prefetch_state": ([vp, ctypes.c_int32, vp], ctypes.c_int),
+        "tg_load_prefetched": ([vp, ctypes.c_int32], ctypes.c_int),
+        "tg_fetch_state": ([vp, ctypes.c_int32, vp], ctypes.c_int),
+        "tg_transfer_wait": ([vp, ctypes.c_int32, ctypes.c_int32], ctypes.c_int),
+        "tg_transfer_join": ([vp], ctypes.c_int),
         "tg_state_device_ptr": ([vp, P(vp)], ctypes.c_int),
         "tg_rhs": ([vp, vp, vp, d], ctypes.c_int),
         "tg_rhs_host": ([vp, vp, vp, d], ctypes.c_int),

@@ -250,6 +250,28 @@ class DeviceContext:
         self._check(self.lib.tg_download_state(self.h, _ptr_of(out)))
         return out
 
+    # -- transfers overlapping the stepping (page-locked host buffers: numpy
+    #    arrays that stay alive, or raw addresses) ------------------------------
+    def prefetch(self, slot, u_host):
+        """Start copying a host state into staging slot 0 or 1 (returns at once)."""
+        self._check(self.lib.tg_prefetch_state(self.h, int(slot), _ptr_of(u_host)))
+
+    def load_prefetched(self, slot):
+        """The prefetched state of `slot` becomes the context's state (in stream order)."""
+        self._check(self.lib.tg_load_prefetched(self.h, int(slot)))
+
+    def fetch(self, slot, u_host):
+        """Enqueue the copy of the current state to a host buffer (returns at once)."""
+        self._check(self.lib.tg_fetch_state(self.h, int(slot), _ptr_of(u_host)))
+
+    def transfer_wait(self, slot, direction):
+        """Block until slot's prefetch (direction 0) or fetch (direction 1) completed."""
+        self._check(self.lib.tg_transfer_wait(self.h, int(slot), int(direction)))
+
+    def transfer_join(self):
+        """The context stream waits for every transfer issued so far."""
+        self._check(self.lib.tg_transfer_join(self.h))
+
     def state_ptr(self) -> int:
         p = ctypes.c_void_p()
         self._check(self.lib.tg_state_device_ptr(self.h, ctypes.byref(p)))
