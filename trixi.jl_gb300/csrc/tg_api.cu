@@ -165,6 +165,30 @@ __global__ void from_ff_kernel(const float2* __restrict__ in, double* __restrict
 // max_dt reductions (stepsize_dg{2,3}d.jl): one warp per element, lanes over
 // its nodes (consecutive lanes read consecutive nodes), a warp max per
 // direction, then lane 0 adds the directions and updates the global maximum.
+// Block maximum of the lanes' speed bits (positive doubles order like their
+// bit patterns) into one atomicMax per block: the warps walk the elements with
+// a grid stride, so the whole reduction is one atomic per block instead of one
+// per element on a single address.
+__device__ __forceinline__ void block_speed_max(unsigned long long mine,
+                                                unsigned long long* __restrict__ speed_bits) {
+  __shared__ unsigned long long s_max[4];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long other = __shfl_xor_sync(0xffffffffu, mine, o);
+    mine = other > mine ? other : mine;
+  }
+  if (lane == 0) s_max[warp] = mine;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long m = s_max[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = s_max[w] > m ? s_max[w] : m;
+    if (m) atomicMax(speed_bits, m);
+  }
+}
+
+// max_dt's reduction (stepsize_dg2d.jl:8-30, stepsize_dg3d.jl): per element the
+// sum over directions of the node maxima of |v_d| + c, times the inverse
+// Jacobian; one warp per element at a time, 4 warps per block.
 template <int D, typename TS>
 __global__ void __launch_bounds__(128) max_speed_kernel(const TS* __restrict__ u,
                                                         const double* __restrict__ inv_jac,
@@ -173,32 +197,36 @@ __global__ void __launch_bounds__(128) max_speed_kernel(const TS* __restrict__ u
                                                         int32_t* __restrict__ status) {
   constexpr int NV = D + 2;
   const int lane = threadIdx.x & 31;
-  const int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (e >= E) return;
-  double ml[D];
-  for (int d = 0; d < D; ++d) ml[d] = 0;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  unsigned long long best = 0;
   bool bad = false;
-  for (int q = lane; q < NN; q += 32) {
-    const TS* p = u + ((size_t)e * NN + q) * NV;
-    double uu[NV], w[NV];
-    for (int v = 0; v < NV; ++v) uu[v] = state_f64(p[v]);
-    Euler<D, double>::cons2prim(uu, w, gamma);
-    const double c = sqrt(gamma * w[NV - 1] / w[0]);
-    bad |= !(w[0] > 0) || !(w[NV - 1] > 0);
-    for (int d = 0; d < D; ++d) ml[d] = fmax(ml[d], fabs(w[1 + d]) + c);
-  }
-  for (int d = 0; d < D; ++d)
-    for (int o = 16; o > 0; o >>= 1) ml[d] = fmax(ml[d], __shfl_xor_sync(0xffffffffu, ml[d], o));
-  if (lane == 0) {
+  for (int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); e < E;
+       e += nwarps) {
+    double ml[D];
+    for (int d = 0; d < D; ++d) ml[d] = 0;
+    for (int q = lane; q < NN; q += 32) {
+      const TS* p = u + ((size_t)e * NN + q) * NV;
+      double uu[NV], w[NV];
+      for (int v = 0; v < NV; ++v) uu[v] = state_f64(p[v]);
+      Euler<D, double>::cons2prim(uu, w, gamma);
+      const double c = sqrt(gamma * w[NV - 1] / w[0]);
+      bad |= !(w[0] > 0) || !(w[NV - 1] > 0);
+      for (int d = 0; d < D; ++d) ml[d] = fmax(ml[d], fabs(w[1 + d]) + c);
+    }
+    for (int d = 0; d < D; ++d)
+      for (int o = 16; o > 0; o >>= 1) ml[d] = fmax(ml[d], __shfl_xor_sync(0xffffffffu, ml[d], o));
     double sum = ml[0];
     for (int d = 1; d < D; ++d) sum += ml[d];
     const double sp = inv_jac[e] * sum;
-    if (sp == sp)
-      atomicMax(speed_bits, (unsigned long long)__double_as_longlong(sp));
-    else
+    if (sp == sp) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(sp);
+      best = b > best ? b : best;
+    } else if (lane == 0) {
       bad = true;
+    }
   }
   if (bad) atomicOr(status, 2);
+  block_speed_max(best, speed_bits);
 }
 
 // The same reduction for a mixed context in the FP32 arithmetic its stage
@@ -213,35 +241,39 @@ __global__ void __launch_bounds__(128) max_speed_ff_kernel(const float2* __restr
                                                            int32_t* __restrict__ status) {
   constexpr int NV = D + 2;
   const int lane = threadIdx.x & 31;
-  const int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (e >= E) return;
-  float ml[D];
-  for (int d = 0; d < D; ++d) ml[d] = 0.0f;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  unsigned long long best = 0;
   bool bad = false;
-  for (int q = lane; q < NN; q += 32) {
-    const float2* p = u + ((size_t)e * NN + q) * NV;
-    float hi[NV], w[NV];
-    for (int v = 0; v < NV; ++v) hi[v] = p[v].x;
-    Euler<D, float>::cons2prim(hi, w, gamma);
-    const float cs = sqrtf(gamma * w[NV - 1] / w[0]);
-    bad |= !(w[0] > 0.0f) || !(w[NV - 1] > 0.0f);
-    for (int d = 0; d < D; ++d) {
-      const float lam = fabsf(w[1 + d]) + cs;
-      if (lam == lam) ml[d] = fmaxf(ml[d], lam);
+  for (int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); e < E;
+       e += nwarps) {
+    float ml[D];
+    for (int d = 0; d < D; ++d) ml[d] = 0.0f;
+    for (int q = lane; q < NN; q += 32) {
+      const float2* p = u + ((size_t)e * NN + q) * NV;
+      float hi[NV], w[NV];
+      for (int v = 0; v < NV; ++v) hi[v] = p[v].x;
+      Euler<D, float>::cons2prim(hi, w, gamma);
+      const float cs = sqrtf(gamma * w[NV - 1] / w[0]);
+      bad |= !(w[0] > 0.0f) || !(w[NV - 1] > 0.0f);
+      for (int d = 0; d < D; ++d) {
+        const float lam = fabsf(w[1 + d]) + cs;
+        if (lam == lam) ml[d] = fmaxf(ml[d], lam);
+      }
     }
-  }
-  for (int d = 0; d < D; ++d)
-    for (int o = 16; o > 0; o >>= 1) ml[d] = fmaxf(ml[d], __shfl_xor_sync(0xffffffffu, ml[d], o));
-  if (lane == 0) {
+    for (int d = 0; d < D; ++d)
+      for (int o = 16; o > 0; o >>= 1) ml[d] = fmaxf(ml[d], __shfl_xor_sync(0xffffffffu, ml[d], o));
     float sum = 0;
     for (int d = 0; d < D; ++d) sum += ml[d];
     const float sp = inv_jac[e] * sum;
-    if (sp == sp)
-      atomicMax(speed_bits, (unsigned long long)__double_as_longlong((double)sp));
-    else
+    if (sp == sp) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong((double)sp);
+      best = b > best ? b : best;
+    } else if (lane == 0) {
       bad = true;
+    }
   }
   if (bad) atomicOr(status, 2);
+  block_speed_max(best, speed_bits);
 }
 
 __global__ void speed_reset_kernel(unsigned long long* speed_bits) {
@@ -1338,7 +1370,8 @@ static int reduce_speed(tg_ctx* c, const void* u, bool ff, unsigned long long* d
     if (rc != 0) return fail(c, TG_ERR_CUDA, "curvilinear wave-speed launch failed");
     return TG_OK;
   }
-  const unsigned nb = (unsigned)((c->E + 3) / 4);  // one warp per element
+  // warps stride over the elements: at most 16 blocks of 4 warps per SM
+  const unsigned nb = (unsigned)std::min<int64_t>((c->E + 3) / 4, 152 * 16);
   if (c->D == 2) {
     if (ff)
       max_speed_ff_kernel<2><<<nb, 128, 0, c->stream>>>((const float2*)u, c->d_invj_f, c->E, c->NN,

@@ -1057,13 +1057,27 @@ __device__ __forceinline__ void mixed_node_update(const MixedParams& P, const Mi
   }
   if (bad) atomicOr(A.status, 1);
   if (stage && A.speed_bits) {
+    // the block's largest element speed, one atomic per block: the first
+    // warp reduces the element speeds
     __syncthreads();
-    if (tid < nel) {
-      float sum = 0;
+    if (tid < 32) {
+      unsigned long long b = 0;
+      for (int k = tid; k < nel; k += 32) {
+        float sum = 0;
 #pragma unroll
-      for (int d = 0; d < D; ++d) sum += __uint_as_float(s_smax[tid * D + d]);
-      const float sp = inv_jac[tid] * sum;
-      if (sp == sp) atomicMax(A.speed_bits, (unsigned long long)__double_as_longlong((double)sp));
+        for (int d = 0; d < D; ++d) sum += __uint_as_float(s_smax[k * D + d]);
+        const float sp = inv_jac[k] * sum;
+        if (sp == sp) {
+          const unsigned long long x = (unsigned long long)__double_as_longlong((double)sp);
+          b = x > b ? x : b;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(0xffffffffu, b, o);
+        b = other > b ? other : b;
+      }
+      if (tid == 0 && b) atomicMax(A.speed_bits, b);
     }
   }
 }
