@@ -743,7 +743,9 @@ def curved_arm(args):
                      "algorithmic_bytes": alg_bytes,
                      "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
         "cpu_baseline": cpu, "e2e": None, "clocks": clocks,
-        "gpu_launches": 7 * res["mixed"]["steps"],
+        # per step: clock prologue, 5 element kernels, clock epilogue; per timed
+        # tg_step call: the clock set-up and two clock reads
+        "gpu_launches": 7 * res["mixed"]["steps"] + 3,
     }
     print(json.dumps(line))
 
@@ -872,8 +874,9 @@ def khi_line(args, rank, world):
         "cpu_baseline": cpu,
         "e2e": out["e2e"],
         "clocks": ml["clocks"],
-        # per step: clock prologue, 5 x (indicator, smoothing, element kernel), clock epilogue
-        "gpu_launches": 17 * ml["steps"],
+        # per step: clock prologue, 5 x (indicator, smoothing, element kernel), clock
+        # epilogue; per timed tg_step call: the clock set-up and two clock reads
+        "gpu_launches": 17 * ml["steps"] + 3,
         "mms3d": mms,
     }
     print(json.dumps(line))
@@ -916,7 +919,9 @@ def mms_line(args, rank, world):
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": mixed["clocks"],
-        "gpu_launches": 7 * mixed["steps"],
+        # per step: clock prologue, 5 element kernels, clock epilogue; per timed
+        # tg_step call: the clock set-up and two clock reads
+        "gpu_launches": 7 * mixed["steps"] + 3,
     }
     print(json.dumps(line))
 

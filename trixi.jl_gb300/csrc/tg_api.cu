@@ -1009,6 +1009,10 @@ struct tg_ctx {
   cudaEvent_t ev_out_ready[2] = {nullptr, nullptr}, ev_out_done[2] = {nullptr, nullptr};
   bool in_pending[2] = {false, false}, in_used_rec[2] = {false, false};
   bool out_done_rec[2] = {false, false};
+  // page-locked, device-mapped copy of the clock that tg_step polls: written by
+  // a kernel, so the poll does not queue behind copies on the copy engines
+  Clock* h_clock = nullptr;
+  Clock* h_clock_dev = nullptr;
   int32_t* d_nbr = nullptr;
   double* d_invj = nullptr;
   double* d_xline = nullptr;
@@ -1112,6 +1116,7 @@ static void free_ctx(tg_ctx* c) {
     if (c->xstream[k]) cudaStreamDestroy(c->xstream[k]);
   }
   for (double* p : c->vectors) cudaFree(p);
+  if (c->h_clock) cudaFreeHost(c->h_clock);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -2515,6 +2520,28 @@ void ctx_set_cur(tg_ctx* c, int cur) {
 }  // namespace tg
 }  // extern "C++"
 
+// The clock as the host sees it after everything enqueued so far: a kernel
+// writes it to mapped host memory (no copy engine), then the stream is
+// synchronised.
+__global__ void clock_publish_kernel(const Clock* __restrict__ src, Clock* __restrict__ dst) {
+  const int* s = reinterpret_cast<const int*>(src);
+  volatile int* d = reinterpret_cast<volatile int*>(dst);
+  for (int k = threadIdx.x; k < (int)(sizeof(Clock) / sizeof(int)); k += blockDim.x) d[k] = s[k];
+  __threadfence_system();
+}
+
+static int read_clock(tg_ctx* c, Clock* h) {
+  if (!c->h_clock) {
+    CUDA_TRY(c, cudaHostAlloc((void**)&c->h_clock, sizeof(Clock), cudaHostAllocMapped));
+    CUDA_TRY(c, cudaHostGetDevicePointer((void**)&c->h_clock_dev, c->h_clock, 0));
+  }
+  clock_publish_kernel<<<1, 32, 0, c->stream>>>(c->d_clock, c->h_clock_dev);
+  CUDA_TRY(c, cudaGetLastError());
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  std::memcpy(h, (const void*)c->h_clock, sizeof(Clock));
+  return TG_OK;
+}
+
 static int capture_step_graph(tg_ctx* c, int parity) {
   const int saved = c->cur;
   const bool saved_rp = c->rp_valid;
@@ -2557,8 +2584,8 @@ int tg_step(tg_ctx* c, int64_t max_steps, double cfl, double t_end, double* t_in
   rc = refresh_rho_p(c);
   if (rc) return rc;
   Clock h{};
-  CUDA_TRY(c, cudaMemcpyAsync(&h, c->d_clock, sizeof(Clock), cudaMemcpyDeviceToHost, c->stream));
-  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  rc = read_clock(c, &h);
+  if (rc) return rc;
   const int64_t steps0 = h.steps;
   int64_t launched = 0;
   const int64_t poll = 64;
@@ -2571,8 +2598,8 @@ int tg_step(tg_ctx* c, int64_t max_steps, double cfl, double t_end, double* t_in
     }
     launched += chunk;
     if (std::isfinite(t_end) || launched >= max_steps) {
-      CUDA_TRY(c, cudaMemcpyAsync(&h, c->d_clock, sizeof(Clock), cudaMemcpyDeviceToHost, c->stream));
-      CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+      rc = read_clock(c, &h);
+      if (rc) return rc;
       if (h.finished) break;
     }
   }
