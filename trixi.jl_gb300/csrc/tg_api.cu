@@ -1013,6 +1013,10 @@ struct tg_ctx {
   // a kernel, so the poll does not queue behind copies on the copy engines
   Clock* h_clock = nullptr;
   Clock* h_clock_dev = nullptr;
+  // the clock's step count as of the end of the last tg_step (or 0 after it
+  // was initialised), when nothing else has stepped the context since
+  int64_t host_steps = 0;
+  bool host_steps_valid = false;
   int32_t* d_nbr = nullptr;
   double* d_invj = nullptr;
   double* d_xline = nullptr;
@@ -2485,6 +2489,8 @@ int ctx_clock_prepare(tg_ctx* c, double t0, double t_end, double cfl, bool sync)
     clock_init_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, t0, t_end, cfl, c->N);
     CUDA_TRY(c, cudaGetLastError());
     c->clock_valid = true;
+    c->host_steps = 0;
+    c->host_steps_valid = true;
   } else {
     clock_config_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, t_end, cfl);
     CUDA_TRY(c, cudaGetLastError());
@@ -2516,6 +2522,7 @@ int ctx_view(tg_ctx* c, CtxView* v) {
 void ctx_set_cur(tg_ctx* c, int cur) {
   c->cur = cur & 1;
   c->rp_valid = false;
+  c->host_steps_valid = false;  // stepped by the ensemble
 }
 }  // namespace tg
 }  // extern "C++"
@@ -2584,9 +2591,15 @@ int tg_step(tg_ctx* c, int64_t max_steps, double cfl, double t_end, double* t_in
   rc = refresh_rho_p(c);
   if (rc) return rc;
   Clock h{};
-  rc = read_clock(c, &h);
-  if (rc) return rc;
-  const int64_t steps0 = h.steps;
+  // the step count before this call: known on the host unless something else
+  // stepped the context (then read, which waits for the stream)
+  if (!c->host_steps_valid) {
+    rc = read_clock(c, &h);
+    if (rc) return rc;
+    c->host_steps = h.steps;
+    c->host_steps_valid = true;
+  }
+  const int64_t steps0 = c->host_steps;
   int64_t launched = 0;
   const int64_t poll = 64;
   while (launched < max_steps) {
@@ -2603,7 +2616,12 @@ int tg_step(tg_ctx* c, int64_t max_steps, double cfl, double t_end, double* t_in
       if (h.finished) break;
     }
   }
+  if (launched == 0) {  // max_steps == 0: the clock as prepared
+    rc = read_clock(c, &h);
+    if (rc) return rc;
+  }
   *t_inout = h.t;
+  c->host_steps = h.steps;
   if (steps_taken) *steps_taken = h.steps - steps0;
   if (h.nan_dt) return fail(c, TG_ERR_NUMERICAL, "time step size `dt` is NaN");
   return TG_OK;
