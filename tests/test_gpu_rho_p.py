@@ -1,9 +1,9 @@
 """The indicator input kept on the device between stages: in mixed 2D
-shock-capturing contexts each stage kernel writes rho*p of its output state per
-node, and the next stage's indicator (HG or the learned network) reads those
-values instead of the whole state.  The blending factors so obtained equal the
-ones computed from the state itself, through a step, an upload and a state
-handed out for writing."""
+shock-capturing contexts each stage kernel (and an upload) writes rho*p of the
+new state per node, and the next stage's indicator (HG or the learned network)
+reads those values instead of the whole state.  The blending factors so
+obtained equal the ones computed from the state itself, through a step, an
+upload and a state handed out for writing."""
 import numpy as np
 import pytest
 
@@ -21,14 +21,19 @@ BLAST = dict(ndims=2, polydeg=3, level=5, xmin=[-1.5, -1.5], xmax=[1.5, 1.5], vi
 
 
 def _state_path_alpha(case, u, net=None):
-    """Blending factors of state u from a fresh context, whose indicator reads
-    the uploaded state (no stage kernel has run on it)."""
+    """Blending factors of state u from a fresh context, evaluated on an FP64
+    device copy of u (tg_alpha with a state argument: the indicator reads that
+    state, never the stored rho*p)."""
+    torch = pytest.importorskip("torch")
     semi, _ = build(case, precision="mixed")
     ctx = semi.device_context
     ctx.upload(u)
     if net is not None:
         net.deploy(semi, band=0.01)
-    return ctx.alpha()
+    u_dev = torch.from_numpy(np.ascontiguousarray(u).reshape(-1)).cuda()
+    a = ctx.alpha(u_dev)
+    torch.cuda.synchronize()
+    return a
 
 
 @pytest.mark.parametrize("case", [KHI, BLAST], ids=["khi", "blast"])

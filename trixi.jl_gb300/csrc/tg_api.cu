@@ -142,6 +142,24 @@ __global__ void to_ff_kernel(const double* __restrict__ in, float2* __restrict__
     out[k] = make_float2(hi, __double2float_rn(x - (double)hi));
   }
 }
+// to_ff_kernel for a 2D state (4 values per node) that also writes rho*p of
+// every node from the hi parts, with the stage kernels' arithmetic
+__global__ void to_ff_rp_kernel(const double* __restrict__ in, float2* __restrict__ out,
+                                int64_t nnodes, float gamma, float* __restrict__ rp) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnodes;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    float hi[4], lo[4];
+    for (int v = 0; v < 4; ++v) {  // 8-byte loads: `in` may be a caller's host buffer
+      const double x = in[4 * k + v];
+      hi[v] = __double2float_rn(x);
+      lo[v] = __double2float_rn(x - (double)hi[v]);
+    }
+    reinterpret_cast<float4*>(out)[2 * k] = make_float4(hi[0], lo[0], hi[1], lo[1]);
+    reinterpret_cast<float4*>(out)[2 * k + 1] = make_float4(hi[2], lo[2], hi[3], lo[3]);
+    rp[k] = Euler<2, float>::density_pressure(hi, gamma);
+  }
+}
+
 // rho*p of every node from the hi parts of a float-float state (nv values per
 // node), with the stage kernels' arithmetic
 __global__ void rho_p_ff_kernel(const float2* __restrict__ u, int64_t nnodes, int nv, float gamma,
@@ -1134,7 +1152,9 @@ static int ensure(tg_ctx* c, void** p, size_t bytes) {
   return TG_OK;
 }
 
-// FP64 state (Trixi layout) -> context representation in `dst`
+// FP64 state (Trixi layout) -> context representation in `dst`.  Into the
+// current state of a context that keeps the indicator input (mixed 2D shock
+// capturing), the same pass writes rho*p of every node (rp_valid).
 static int import_state(tg_ctx* c, const double* src, void* dst) {
   if (c->fp64) {
     if (src != dst)
@@ -1142,8 +1162,16 @@ static int import_state(tg_ctx* c, const double* src, void* dst) {
                                   c->stream));
     return TG_OK;
   }
+  if (c->d_rp && dst == c->d_u[c->cur] && c->NV == 4) {
+    to_ff_rp_kernel<<<conv_blocks(c->ndofs), 256, 0, c->stream>>>(src, (float2*)dst, c->ndofs,
+                                                                   c->MP.gamma, c->d_rp);
+    CUDA_TRY(c, cudaGetLastError());
+    c->rp_valid = true;
+    return TG_OK;
+  }
   to_ff_kernel<<<conv_blocks(c->nvalues), 256, 0, c->stream>>>(src, (float2*)dst, c->nvalues);
   CUDA_TRY(c, cudaGetLastError());
+  if (dst == c->d_u[c->cur]) c->rp_valid = false;
   return TG_OK;
 }
 
@@ -2223,7 +2251,7 @@ int tg_upload_state(tg_ctx* c, const double* u_host) {
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   c->uploaded = true;
   c->clock_valid = false;
-  c->rp_valid = false;
+  if (c->fp64) c->rp_valid = false;
   return TG_OK;
 }
 
@@ -2287,8 +2315,7 @@ int tg_load_prefetched(tg_ctx* c, int32_t slot) {
   c->in_used_rec[slot] = true;
   c->in_pending[slot] = false;
   c->uploaded = true;
-  c->clock_valid = false;
-  c->rp_valid = false;
+  c->clock_valid = false;  // (import_state keeps the indicator input valid)
   return TG_OK;
 }
 
