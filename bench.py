@@ -278,22 +278,25 @@ def e2e_steps(ctx, semi, steps, warmup, cfl, world, flush):
     page-locked host memory, the copies overlapping the stepping on the
     context's copy streams (tg_prefetch_state, tg_load_prefetched,
     tg_fetch_state: step k + 1's input arrives and step k's result leaves while
-    the device computes)."""
+    the device computes), the steps enqueued without waiting (tg_step_enqueue)
+    and the clock read once at the end (tg_clock_read)."""
     import torch
     stream = torch.cuda.ExternalStream(ctx.stream())
     u_host = torch.from_numpy(ctx.download().reshape(-1)).pin_memory()
     outs = [torch.empty_like(u_host).pin_memory() for _ in range(2)]
 
     def run(n):
-        t = 0.0
         ctx.prefetch(0, u_host.data_ptr())
         for k in range(n):
             ctx.load_prefetched(k % 2)
             if k + 1 < n:
                 ctx.prefetch((k + 1) % 2, u_host.data_ptr())
-            t, _n = ctx.step(1, cfl, math.inf, t)
+            ctx.step_enqueue(1, cfl, math.inf, 0.0)  # tg_step without the host wait
             ctx.fetch(k % 2, outs[k % 2].data_ptr())
         ctx.transfer_join()
+        t, steps, _ = ctx.clock_read()
+        if steps != 1:
+            raise RuntimeError(f"e2e: {steps} steps taken after the last load, 1 enqueued")
 
     run(max(warmup, 1))
     ctx.synchronize()

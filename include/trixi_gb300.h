@@ -326,6 +326,14 @@ int tg_lincomb(tg_ctx* ctx, int64_t n, double* out, double a, const double* x, d
 int tg_step(tg_ctx* ctx, int64_t max_steps, double cfl, double t_end, double* t_inout,
             int64_t* steps_taken);
 
+/* tg_step without waiting: enqueues nsteps step graphs (the same stepping,
+ * stopping at t_end on the device; t_start is used as tg_step uses *t_inout)
+ * and returns at once.  tg_clock_read then synchronises and reports the
+ * reached time, the step count since the clock was set up and whether t_end
+ * was reached (TG_ERR_NUMERICAL if dt became NaN). */
+int tg_step_enqueue(tg_ctx* ctx, int64_t nsteps, double cfl, double t_end, double t_start);
+int tg_clock_read(tg_ctx* ctx, double* t, int64_t* steps, int32_t* finished);
+
 /* Resets the device clock to t (next tg_step recomputes dt). */
 int tg_set_time(tg_ctx* ctx, double t);
 

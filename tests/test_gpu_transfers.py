@@ -26,11 +26,12 @@ def test_pipelined_transfers_match_synchronous(case, precision):
     semi, _ = build(case, precision=precision)
     ctx = semi.device_context
     inputs = [perturbed_state(semi, seed=s, amp=0.01) for s in (1, 2, 3, 4)]
-    ref = []
+    ref, ref_t = [], []
     for u in inputs:
         ctx.upload(u)
-        ctx.step(2, 0.5, 10.0, 0.0)
+        t, _ = ctx.step(2, 0.5, 10.0, 0.0)
         ref.append(ctx.download())
+        ref_t.append(t)
     hin = [torch.from_numpy(np.ascontiguousarray(u).reshape(-1)).pin_memory() for u in inputs]
     hout = [torch.empty_like(hin[0]).pin_memory() for _ in inputs]
     n = len(inputs)
@@ -39,10 +40,15 @@ def test_pipelined_transfers_match_synchronous(case, precision):
         ctx.load_prefetched(k % 2)
         if k + 1 < n:
             ctx.prefetch((k + 1) % 2, hin[k + 1].data_ptr())
-        ctx.step(2, 0.5, 10.0, 0.0)
+        if k % 2:
+            ctx.step(2, 0.5, 10.0, 0.0)
+        else:
+            ctx.step_enqueue(2, 0.5, 10.0, 0.0)  # no host wait
         ctx.fetch(k % 2, hout[k].data_ptr())  # slot reuse waits for its previous copy
     for slot in (0, 1):
         ctx.transfer_wait(slot, 1)
+    t, steps, finished = ctx.clock_read()
+    assert steps == 2 and not finished and t == ref_t[-1]
     for k in range(n):
         np.testing.assert_array_equal(hout[k].numpy().reshape(semi.u_shape), ref[k])
 

@@ -2654,6 +2654,43 @@ int tg_step(tg_ctx* c, int64_t max_steps, double cfl, double t_end, double* t_in
   return TG_OK;
 }
 
+int tg_step_enqueue(tg_ctx* c, int64_t nsteps, double cfl, double t_end, double t_start) {
+  if (!c || nsteps < 0 || !(cfl > 0)) return TG_ERR_INVALID_ARGUMENT;
+  if (!c->uploaded) return fail(c, TG_ERR_STATE, "no state uploaded");
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  for (int p = 0; p < 2; ++p)
+    if (!c->graph[p]) {
+      int rc = capture_step_graph(c, p);
+      if (rc) return rc;
+    }
+  int rc = tg::ctx_clock_prepare(c, t_start, t_end, cfl, false);
+  if (rc) return rc;
+  rc = refresh_rho_p(c);
+  if (rc) return rc;
+  for (int64_t k = 0; k < nsteps; ++k) {
+    CUDA_TRY(c, cudaGraphLaunch(c->graph[c->cur], c->stream));
+    c->cur ^= 1;
+    c->rp_valid = c->d_rp != nullptr;
+  }
+  c->host_steps_valid = false;  // known again at the next clock read
+  return TG_OK;
+}
+
+int tg_clock_read(tg_ctx* c, double* t, int64_t* steps, int32_t* finished) {
+  if (!c) return TG_ERR_INVALID_ARGUMENT;
+  CUDA_TRY(c, cudaSetDevice(c->device));
+  Clock h{};
+  int rc = read_clock(c, &h);
+  if (rc) return rc;
+  c->host_steps = h.steps;
+  c->host_steps_valid = c->clock_valid;
+  if (t) *t = h.t;
+  if (steps) *steps = h.steps;
+  if (finished) *finished = h.finished;
+  if (h.nan_dt) return fail(c, TG_ERR_NUMERICAL, "time step size `dt` is NaN");
+  return TG_OK;
+}
+
 int tg_integrals(tg_ctx* c, double* out) {
   if (!c || !out) return TG_ERR_INVALID_ARGUMENT;
   CUDA_TRY(c, cudaSetDevice(c->device));

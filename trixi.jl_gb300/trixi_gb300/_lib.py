@@ -31,7 +31,8 @@ TG_BOUNDARY_PERIODIC, TG_BOUNDARY_DIRICHLET, TG_BOUNDARY_SLIP_WALL = 0, 1, 2
 EXPORTS = ("tg_api_version", "tg_ctx_create", "tg_ctx_destroy", "tg_last_error", "tg_ndofs",
            "tg_upload_state", "tg_download_state", "tg_prefetch_state", "tg_load_prefetched",
            "tg_fetch_state", "tg_transfer_wait", "tg_transfer_join", "tg_state_device_ptr", "tg_rhs",
-           "tg_rhs_host", "tg_max_dt", "tg_rk_stage", "tg_rk_stage_part", "tg_step", "tg_set_time",
+           "tg_rhs_host", "tg_max_dt", "tg_rk_stage", "tg_rk_stage_part", "tg_step",
+           "tg_step_enqueue", "tg_clock_read", "tg_set_time",
            "tg_integrals", "tg_alpha", "tg_status", "tg_synchronize",
            "tg_elements_per_block", "tg_stream", "tg_integrals_noalloc",
            "tg_vector_create", "tg_vector_destroy", "tg_vector_copy", "tg_lincomb", "tg_fma_peak", "tg_error_norms",
@@ -132,6 +133,8 @@ def load(path: str | None = None):
         "tg_rk_stage": ([vp, i32, d, d], ctypes.c_int),
         "tg_rk_stage_part": ([vp, i32, d, d, i32], ctypes.c_int),
         "tg_step": ([vp, i64, d, d, pd, P(i64)], ctypes.c_int),
+        "tg_step_enqueue": ([vp, i64, d, d, d], ctypes.c_int),
+        "tg_clock_read": ([vp, pd, P(i64), P(ctypes.c_int32)], ctypes.c_int),
         "tg_set_time": ([vp, d], ctypes.c_int),
         "tg_integrals": ([vp, pd], ctypes.c_int),
         "tg_alpha": ([vp, vp, pd], ctypes.c_int),

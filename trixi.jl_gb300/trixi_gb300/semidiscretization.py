@@ -308,6 +308,20 @@ class DeviceContext:
                                      ctypes.byref(tt), ctypes.byref(n)))
         return tt.value, n.value
 
+    def step_enqueue(self, nsteps, cfl, t_end, t_start):
+        """tg_step without waiting: enqueue nsteps step graphs and return."""
+        self._check(self.lib.tg_step_enqueue(self.h, int(nsteps), float(cfl), float(t_end),
+                                             float(t_start)))
+
+    def clock_read(self):
+        """(t, steps since the clock was set up, reached t_end), after synchronising."""
+        t = ctypes.c_double()
+        n = ctypes.c_int64()
+        f = ctypes.c_int32()
+        self._check(self.lib.tg_clock_read(self.h, ctypes.byref(t), ctypes.byref(n),
+                                           ctypes.byref(f)))
+        return t.value, n.value, bool(f.value)
+
     def integrals(self):
         out = np.zeros(self.semi.equations.nvariables + 2)
         self._check(self.lib.tg_integrals(self.h, _dptr(out)))
