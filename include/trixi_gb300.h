@@ -1,9 +1,10 @@
 /*
  * trixi_gb300.h -- C ABI of the GB300 (sm_103a) DGSEM hot path.
  *
- * Drop-in device backend for Trixi.jl's TreeMesh DGSEM semidiscretization of
- * the compressible Euler equations (2D/3D, periodic, conforming meshes).  The
- * entry points replace, one for one, the pieces of the reference that a Julia
+ * Drop-in device backend for Trixi.jl's DGSEM semidiscretization of the
+ * compressible Euler equations (2D/3D; TreeMesh periodic or not, with L2
+ * mortars and AMR; curvilinear StructuredMesh / P4estMesh bricks).  The entry
+ * points replace, one for one, the pieces of the reference that a Julia
  * `ccall` shim hands to the device (paths relative to the Trixi.jl sources):
  *
  *   rhs_hyperbolic!(du_ode, u_ode, semi, t)
