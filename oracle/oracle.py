@@ -28,7 +28,7 @@ BC_PERIODIC, BC_DIRICHLET, BC_SLIP_WALL = 0, 1, 2
 (IC_CONSTANT, IC_CONVERGENCE_TEST, IC_ISENTROPIC_VORTEX, IC_WEAK_BLAST_WAVE,
  IC_KELVIN_HELMHOLTZ, IC_TAYLOR_GREEN, IC_GAUSSIAN_BLAST,
  IC_ISENTROPIC_VORTEX_ADVECTED, IC_BLAST_WAVE, IC_DENSITY_PULSE, IC_SEDOV_BLAST_WAVE,
- IC_DENSITY_WAVE) = range(12)
+ IC_DENSITY_WAVE, IC_MEDIUM_SEDOV_3D) = range(13)
 
 _lib = None
 _PORTABLE_FLAGS = "g++ -O3 -fopenmp (portable)"
@@ -123,6 +123,8 @@ def _load():
     lib.orc_curved_solve.restype = i
     lib.orc_curved_solve.argtypes = [vp, P(d), d, d, d, i64, P(d), P(i64)]
     lib.orc_curved_errors.argtypes = [vp, P(d), d, i, P(d), P(d), P(d)]
+    lib.orc_curved3_set_hg.argtypes = [vp, d, d, i, i]
+    lib.orc_curved3_alpha.argtypes = [vp, P(d), P(d)]
     lib.orc_curved3_create.restype = vp
     lib.orc_curved3_create.argtypes = [i, i64, P(d), P(i64), d, i, i, i, i]
     lib.orc_curved3_destroy.argtypes = [vp]
@@ -529,6 +531,17 @@ class CurvedOracle3D:
     @property
     def shape(self):
         return (self.E, self.n, self.n, self.n, 5)
+
+    def set_hg(self, alpha_max, alpha_min, alpha_smooth, fv_flux):
+        """IndicatorHennemannGassner(density_pressure) parameters and the FV flux of
+        a VI_SHOCKCAPTURING_HG solver."""
+        _lib.orc_curved3_set_hg(self.h, alpha_max, alpha_min, int(alpha_smooth), fv_flux)
+
+    def alpha(self, u):
+        """Smoothed blending factors of state u (after set_hg)."""
+        a = np.empty(self.E)
+        _lib.orc_curved3_alpha(self.h, _p(np.ascontiguousarray(u, dtype=np.float64)), _p(a))
+        return a
 
     def set_dirichlet(self, ic, params=None):
         par = np.zeros(8)

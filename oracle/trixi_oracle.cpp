@@ -59,6 +59,7 @@ enum InitialCondition {
   IC_DENSITY_PULSE = 9,
   IC_SEDOV_BLAST_WAVE = 10,
   IC_DENSITY_WAVE = 11,
+  IC_MEDIUM_SEDOV_3D = 12,
 };
 
 // ---------------------------------------------------------------------------
@@ -819,6 +820,21 @@ static void initial_condition(const Eq& eq, int ic, const double* par, const dou
       prim[1] = 0;
       prim[2] = 0;
       prim[3] = r > r0 ? 1.0e-5 : p_inner;
+      prim2cons(eq, prim, u);
+      return;
+    }
+    case IC_MEDIUM_SEDOV_3D: {
+      // initial_condition_medium_sedov_blast_wave of
+      // examples/structured_3d_dgsem/elixir_euler_sedov.jl (3D)
+      const double r = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+      const double r0 = 0.21875;
+      const double E = 1;
+      const double p_inner = 3 * (eq.gamma - 1) * E / (4 * M_PI * r0 * r0);
+      prim[0] = 1;
+      prim[1] = 0;
+      prim[2] = 0;
+      prim[3] = 0;
+      prim[4] = r > r0 ? 1.0e-3 : p_inner;
       prim2cons(eq, prim, u);
       return;
     }
@@ -3023,9 +3039,102 @@ struct Curved3 {
   std::vector<double> invJ;  // [E][nn]
   int bc_ic = -1;
   double bc_par[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  // VolumeIntegralShockCapturingHG: indicator parameters, the FV flux and the
+  // subcell normals [E][d][l][n - 1][3] (calc_normalvectors_subcell_fv!,
+  // containers_3d.jl:352-470): direction d, line l = the two other indices
+  // (lower one fastest), subcell interface between nodes i and i + 1
+  double alpha_max = 0.5, alpha_min = 0.001;
+  bool alpha_smooth = true;
+  int fvflux = FLUX_LAX_FRIEDRICHS;
+  std::vector<double> snv;
   size_t ui(int64_t e, int q) const { return ((size_t)e * nn + q) * 5; }
   int node(int i, int j, int k) const { return i + n * (j + n * k); }
+  // node a of line l = (l0, l1) in direction d
+  int line_node(int d, int l, int a) const {
+    const int l0 = l % n, l1 = l / n;
+    return d == 0 ? node(a, l0, l1) : (d == 1 ? node(l0, a, l1) : node(l0, l1, a));
+  }
 };
+
+// calc_normalvectors_subcell_fv! (3D): per direction, Ja^d at the line's first
+// node plus the partial sums of w_i D[i, :] Ja^d along the line
+static void curved3_subcell_normals(Curved3& c) {
+  const int n = c.n, nn = c.nn, nf = n * n;
+  const std::vector<double>& Dm = c.b.D;
+  const std::vector<double>& w = c.b.weights;
+  c.snv.assign((size_t)c.E * 3 * nf * (n - 1) * 3, 0.0);
+  for (int64_t e = 0; e < c.E; ++e)
+    for (int d = 0; d < 3; ++d)
+      for (int l = 0; l < nf; ++l) {
+        double acc[3];
+        for (int xyz = 0; xyz < 3; ++xyz)
+          acc[xyz] = c.Ja[((size_t)e * nn + c.line_node(d, l, 0)) * 9 + 3 * d + xyz];
+        for (int i = 0; i < n - 1; ++i) {
+          for (int m = 0; m < n; ++m) {
+            const double wd = w[i] * Dm[i * n + m];
+            for (int xyz = 0; xyz < 3; ++xyz)
+              acc[xyz] += wd * c.Ja[((size_t)e * nn + c.line_node(d, l, m)) * 9 + 3 * d + xyz];
+          }
+          for (int xyz = 0; xyz < 3; ++xyz)
+            c.snv[((((size_t)e * 3 + d) * nf + l) * (n - 1) + i) * 3 + xyz] = acc[xyz];
+        }
+      }
+}
+
+// IndicatorHennemannGassner on density_pressure (indicators.jl:114-148,
+// indicators_3d.jl:39-123) per element, smoothed over the face neighbours
+static void curved3_hg_alpha(const Curved3& c, const double* u, std::vector<double>& alpha) {
+  const int n = c.n, nn = c.nn;
+  const double threshold = 0.5 * std::pow(10.0, -1.8 * std::pow((double)n, 0.25));
+  const double parameter_s = std::log((1 - 0.0001) / 0.0001);
+  alpha.assign(c.E, 0.0);
+  const double* V = c.b.Vinv.data();
+  std::vector<double> a(nn), t(nn);
+  for (int64_t e = 0; e < c.E; ++e) {
+    for (int q = 0; q < nn; ++q) a[q] = density_pressure(c.eq, &u[c.ui(e, q)]);
+    // multiply_scalar_dimensionwise!: x, then y, then z
+    for (int d = 0; d < 3; ++d) {
+      for (int k = 0; k < n; ++k)
+        for (int j = 0; j < n; ++j)
+          for (int i = 0; i < n; ++i) {
+            const int idx[3] = {i, j, k};
+            double r = 0;
+            for (int s = 0; s < n; ++s) {
+              int id2[3] = {i, j, k};
+              id2[d] = s;
+              r += V[idx[d] * n + s] * a[c.node(id2[0], id2[1], id2[2])];
+            }
+            t[c.node(i, j, k)] = r;
+          }
+      std::swap(a, t);
+    }
+    double e_clip2 = 0, e_clip1 = 0, e_tot = 0;
+    for (int q = 0; q < nn; ++q) {
+      const int mx = std::max({q % n, (q / n) % n, q / (n * n)});
+      const double m2 = a[q] * a[q];
+      if (mx <= n - 3) e_clip2 += m2;
+      if (mx <= n - 2) e_clip1 += m2;
+      e_tot += m2;
+    }
+    const double f1 = e_tot != 0 ? (e_tot - e_clip1) / e_tot : 0.0;
+    const double f2 = e_clip1 != 0 ? (e_clip1 - e_clip2) / e_clip1 : 0.0;
+    const double energy = std::max(f1, f2);
+    double al = 1 / (1 + std::exp(-parameter_s / threshold * (energy - threshold)));
+    if (al < c.alpha_min) al = 0;
+    if (al > 1 - c.alpha_min) al = 1;
+    alpha[e] = std::min(c.alpha_max, al);
+  }
+  if (c.alpha_smooth) {
+    const std::vector<double> tmp = alpha;
+    for (int64_t e = 0; e < c.E; ++e)
+      for (int o = 0; o < 3; ++o) {
+        const int64_t r = c.nbr[e * 6 + 2 * o + 1];  // interface (e, r) in direction o
+        if (r < 0) continue;
+        alpha[e] = std::max({tmp[e], 0.5 * tmp[r], alpha[e]});
+        alpha[r] = std::max({tmp[r], 0.5 * tmp[e], alpha[r]});
+      }
+  }
+}
 
 // calc_jacobian_matrix!, calc_contravariant_vectors! (curl form),
 // calc_inverse_jacobian! (containers_3d.jl:67-286)
@@ -3099,6 +3208,11 @@ static void curved3_rhs(const Curved3& c, double* du, const double* u, double t)
   const Basis& b = c.b;
   const Eq& eq = c.eq;
   std::vector<double> sfv((size_t)c.E * 6 * nf * 5);  // [E][dir][face node][v]
+  // VolumeIntegralShockCapturingHG (calc_volume_integral.jl:231-272)
+  const bool hg = c.vi == VI_SHOCKCAPTURING_HG;
+  std::vector<double> alpha;
+  if (hg) curved3_hg_alpha(c, u, alpha);
+  const double atol = std::max(100 * 2.220446049250313e-16, std::pow(2.220446049250313e-16, 0.75));
   // face node (a, b) of direction o at the - side (s = 0) or + side (s = n - 1)
   auto fnode = [&](int o, int a, int bb, int s) {
     return o == 0 ? c.node(s, a, bb) : (o == 1 ? c.node(a, s, bb) : c.node(a, bb, s));
@@ -3149,6 +3263,9 @@ static void curved3_rhs(const Curved3& c, double* du, const double* u, double t)
     const double* ue = u + (size_t)e * nn * 5;
     const double* Ja = &c.Ja[(size_t)e * nn * 9];
     for (int k = 0; k < nn * 5; ++k) de[k] = 0;
+    const double ae = hg ? alpha[e] : 0.0;
+    const bool dg_only = !hg || std::fabs(ae) <= atol;
+    const double fdw = dg_only ? 1.0 : 1.0 - ae;
     for (int k = 0; k < n; ++k)
       for (int j = 0; j < n; ++j)
         for (int i = 0; i < n; ++i) {
@@ -3183,12 +3300,28 @@ static void curved3_rhs(const Curved3& c, double* du, const double* u, double t)
                 double F[5];
                 two_point3_n(eq, c.vf, ue + q * 5, ue + r * 5, avg, F);
                 for (int v = 0; v < 5; ++v) {
-                  de[q * 5 + v] = std::fma(b.Dsplit[idx[d] * n + s], F[v], de[q * 5 + v]);
-                  de[r * 5 + v] = std::fma(b.Dsplit[s * n + idx[d]], F[v], de[r * 5 + v]);
+                  de[q * 5 + v] = std::fma(fdw * b.Dsplit[idx[d] * n + s], F[v], de[q * 5 + v]);
+                  de[r * 5 + v] = std::fma(fdw * b.Dsplit[s * n + idx[d]], F[v], de[r * 5 + v]);
                 }
               }
           }
         }
+    if (!dg_only) {
+      // fv_kernel! / calcflux_fv! (dgsem_structured/dg_3d.jl): subcell fluxes
+      // along the subcell normals, zero at the element faces
+      for (int d = 0; d < 3; ++d)
+        for (int l = 0; l < nf; ++l) {
+          double fst[9][5] = {};
+          for (int i = 1; i < n; ++i) {
+            const double* nv = &c.snv[((((size_t)e * 3 + d) * nf + l) * (n - 1) + (i - 1)) * 3];
+            two_point3_n(eq, c.fvflux, ue + c.line_node(d, l, i - 1) * 5,
+                         ue + c.line_node(d, l, i) * 5, nv, fst[i]);
+          }
+          for (int i = 0; i < n; ++i)
+            for (int v = 0; v < 5; ++v)
+              de[c.line_node(d, l, i) * 5 + v] += ae * (b.inv_weights[i] * (fst[i + 1][v] - fst[i][v]));
+        }
+    }
     const double factor = b.inv_weights[0];
     const double* sf = &sfv[(size_t)e * 6 * nf * 5];
     for (int o = 0; o < 3; ++o)
@@ -3318,6 +3451,23 @@ void* orc_curved3_create(int polydeg, int64_t nelements, const double* x, const 
 }
 
 void orc_curved3_destroy(void* h) { delete (Curved3*)h; }
+
+// VolumeIntegralShockCapturingHG settings of a 3D curvilinear mesh
+void orc_curved3_set_hg(void* h, double alpha_max, double alpha_min, int alpha_smooth, int fvflux) {
+  Curved3& c = *(Curved3*)h;
+  c.alpha_max = alpha_max;
+  c.alpha_min = alpha_min;
+  c.alpha_smooth = alpha_smooth != 0;
+  c.fvflux = fvflux;
+  curved3_subcell_normals(c);
+}
+
+// Smoothed blending factors of a state, alpha[E]
+void orc_curved3_alpha(void* h, const double* u, double* alpha) {
+  std::vector<double> a;
+  curved3_hg_alpha(*(const Curved3*)h, u, a);
+  std::copy(a.begin(), a.end(), alpha);
+}
 
 void orc_curved3_set_dirichlet(void* h, int ic, const double* params) {
   Curved3& c = *(Curved3*)h;

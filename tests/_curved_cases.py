@@ -70,6 +70,15 @@ def _warped_cube_nonperiodic(xi, eta, zeta):
     return x + 1, y + 1, z + 1
 
 
+def _sedov_warp_3d(xi, eta, zeta):
+    # elixir_euler_sedov.jl (structured_3d_dgsem)
+    y = eta + 0.125 * (np.cos(1.5 * np.pi * xi) * np.cos(0.5 * np.pi * eta) *
+                       np.cos(0.5 * np.pi * zeta))
+    x = xi + 0.125 * (np.cos(0.5 * np.pi * xi) * np.cos(2 * np.pi * y) * np.cos(0.5 * np.pi * zeta))
+    z = zeta + 0.125 * (np.cos(0.5 * np.pi * x) * np.cos(np.pi * y) * np.cos(0.5 * np.pi * zeta))
+    return x, y, z
+
+
 def _sedov_warp(xi, eta):
     # elixir_euler_sedov.jl (structured_2d_dgsem)
     y = eta + 0.125 * (np.cos(1.5 * np.pi * xi) * np.cos(0.5 * np.pi * eta))
@@ -82,6 +91,8 @@ def mapping_kwargs(name):
         return dict(coordinates_min=(-1.0, -1.0), coordinates_max=(1.0, 1.0))
     if name == "sedov_warp":
         return dict(mapping=_sedov_warp)
+    if name == "sedov_warp_3d":
+        return dict(mapping=_sedov_warp_3d)
     if name == "cube_0_2_faces":
         return dict(faces=CUBE_0_2_FACES)
     if name == "warped_cube_0_3":

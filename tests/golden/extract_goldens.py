@@ -311,7 +311,14 @@ CURVED_CASES = {
         ic="sedov_blast_wave", source="none", vi="hg", volume_flux="ranocha",
         volume_flux_fv="llf_naive", surface_flux="llf_naive", alpha_max=1.0, alpha_min=0.001,
         alpha_smooth=True, cfl=0.5, tspan=[0.0, 12.5]),
-    # 3D (oracle only; the GPU path runs 2D curvilinear meshes)
+    # 3D
+    "StructuredMesh3D: elixir_euler_sedov.jl": dict(
+        file="test/test_structured_3d.jl",
+        elixir="examples/structured_3d_dgsem/elixir_euler_sedov.jl",
+        mesh="structured", ndims=3, cells=[4, 4, 4], mapping="sedov_warp_3d", polydeg=3,
+        ic="medium_sedov_3d", source="none", vi="hg", volume_flux="ranocha",
+        volume_flux_fv="llf_naive", surface_flux="llf_naive", alpha_max=1.0, alpha_min=0.001,
+        alpha_smooth=True, cfl=0.5, tspan=[0.0, 12.5]),
     "StructuredMesh3D: elixir_euler_source_terms.jl": dict(
         file="test/test_structured_3d.jl",
         elixir="examples/structured_3d_dgsem/elixir_euler_source_terms.jl",

@@ -23,7 +23,8 @@ def test_3d_host_metric_free_stream(oracle_mod):
 
 def _ic(O, name):
     return dict(constant=O.IC_CONSTANT, convergence_test=O.IC_CONVERGENCE_TEST,
-                weak_blast_wave=O.IC_WEAK_BLAST_WAVE, sedov_blast_wave=O.IC_SEDOV_BLAST_WAVE)[name]
+                weak_blast_wave=O.IC_WEAK_BLAST_WAVE, sedov_blast_wave=O.IC_SEDOV_BLAST_WAVE,
+                medium_sedov_3d=O.IC_MEDIUM_SEDOV_3D)[name]
 
 
 @pytest.mark.parametrize("name", FP64_GOLDENS)

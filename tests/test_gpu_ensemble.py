@@ -114,3 +114,23 @@ def test_ensemble_rejects_unsupported():
         T.Ensemble([vortex_semi(2, 3, 5.0), vortex_semi(2, 3, 5.0, surface_flux=T.flux_ranocha)])
     with pytest.raises(T.TrixiGB300Error):
         T.Ensemble([vortex_semi(2, 3, 5.0)], threads_per_block=128)
+
+
+def test_ensemble_mixed_error_within_1p1x_of_fp64():
+    # the 1.1x target on L2(rho) at t = 20 (the vortex is back at its start), for
+    # instances of the C5a kind up to 32^2 elements: there the FP64 error
+    # (1e-6 .. 1e-3) is far above the mixed path's rounding floor (~1e-8, see
+    # the design notes for the 128^2 polydeg-4 instances, where it is not)
+    specs = [(3, 2, 4.1), (4, 2, 2.3), (3, 3, 1.7), (4, 3, 3.6), (5, 3, 4.8), (4, 4, 2.9),
+             (5, 4, 1.2)]
+    semis = [vortex_semi(lv, p, eps) for lv, p, eps in specs]
+    ens = T.Ensemble(semis)
+    ens.upload_initial()
+    t, _ = ens.step(10 ** 7, 1.0, 20.0)
+    assert np.allclose(t, 20.0, rtol=1e-13)
+    for i, ((lv, p, eps), semi) in enumerate(zip(specs, semis)):
+        l2m = T.calc_error_norms(ens.download(i), 20.0, semi)[0][0]
+        ref = vortex_semi(lv, p, eps, precision="fp64")
+        u, tt, _ = solo_run(ref, 20.0, 10 ** 7)
+        l2f = T.calc_error_norms(u, tt, ref)[0][0]
+        assert l2m <= 1.1 * l2f, (lv, p, eps, l2m, l2f)
