@@ -36,6 +36,7 @@ def build(c, precision="fp64", cells=None):
     ic = {"convergence_test": T.initial_condition_convergence_test,
           "weak_blast_wave": T.initial_condition_weak_blast_wave,
           "sedov_blast_wave": T.initial_condition_sedov_blast_wave,
+          "medium_sedov_3d": T.initial_condition_medium_sedov_blast_wave,
           "constant": T.initial_condition_constant}[c["ic"]]
     src = T.source_terms_convergence_test if c.get("source") == "convergence_test" else None
     bcs = (T.BoundaryConditionDirichlet(ic) if c.get("boundary") == "dirichlet"
@@ -264,9 +265,9 @@ NONP3 = "StructuredMesh3D: elixir_euler_source_terms_nonperiodic_curved.jl"
 SRC3 = "StructuredMesh3D: elixir_euler_source_terms.jl"
 # the 3D path runs the weak form and flux differencing at polydeg 3 and 5: every
 # StructuredMesh3D golden (EC3 is flux_ranocha flux differencing at polydeg 5)
+SEDOV3 = "StructuredMesh3D: elixir_euler_sedov.jl"
 GOLDENS_3D = sorted(k for k, v in GOLDENS.items()
-                    if v.get("ndims", 2) == 3 and v["vi"] in ("weak", "fluxdiff")
-                    and v["polydeg"] in (3, 5))
+                    if v.get("ndims", 2) == 3 and v["polydeg"] in (3, 5))
 RHS_CASES_3D = [
     (_case(FREE3, ic="convergence_test", source="convergence_test"), (4, 4, 4)),
     (_case(FREE3, ic="convergence_test", source="convergence_test", surface_flux="llf"), (4, 4, 4)),
@@ -279,6 +280,11 @@ RHS_CASES_3D = [
     (_case(EC3, polydeg=3, volume_flux="chandrashekar", surface_flux="llf_naive"), (4, 4, 4)),
     (_case(EC3, polydeg=3, volume_flux="central", surface_flux="central"), (4, 4, 4)),
     (_case(NONP3, vi="fluxdiff", volume_flux="ranocha", surface_flux="llf"), (3, 2, 2)),
+    # shock capturing: the Sedov elixir (ranocha / naive LLF FV) and another
+    # flux set without smoothing
+    (_case(SEDOV3), (4, 4, 4)),
+    (_case(SEDOV3, volume_flux="shima_etal", surface_flux="llf", volume_flux_fv="llf",
+           alpha_smooth=False), (3, 4, 2)),
 ]
 
 
@@ -317,6 +323,30 @@ def test_curved3_gpu_fp64_reproduces_trixi_goldens(name):
         return
     np.testing.assert_allclose(ana.l2, c["l2"], rtol=1e-8)
     np.testing.assert_allclose(ana.linf, c["linf"], rtol=1e-7)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_curved3_hg_alpha_and_steps_match_oracle(precision):
+    c = _case(SEDOV3)
+    semi, orc = build(c, precision, cells=(4, 4, 4))
+    u0 = semi.compute_coefficients(0.0)
+    ctx = semi.device_context
+    ctx.upload(u0)
+    a_orc = orc.alpha(u0)
+    assert np.max(a_orc) > 0
+    tol = 1e-12 if precision == "fp64" else 1e-2 * c["alpha_max"]
+    assert np.max(np.abs(ctx.alpha() - a_orc)) < tol
+    t, n = ctx.step(5, c["cfl"], 10.0, 0.0)
+    u_orc, t_orc, n_orc = orc.solve(u0, 0.0, 10.0, c["cfl"], max_steps=5)
+    assert n == n_orc == 5
+    assert t == pytest.approx(t_orc, rel=1e-12 if precision == "fp64" else 1e-5)
+    assert rel_err(ctx.download(), u_orc) < (1e-12 if precision == "fp64" else 1e-5)
+
+
+def test_curved3_hg_mixed_golden():
+    c = dict(GOLDENS[SEDOV3])
+    _, ana = _golden_run(c, "mixed")
+    np.testing.assert_allclose(ana.l2, c["l2"], rtol=1e-3)
 
 
 def test_curved3_fd_steps_match_oracle():

@@ -1064,6 +1064,8 @@ struct tg_ctx {
   double* d_cmet = nullptr;           // [E][NN][5]: Ja^1, Ja^2, inverse Jacobian
   double2* d_csnv = nullptr;          // HG: subcell normals [E][2][N][N - 1]
   float2* d_csnv32 = nullptr;         // mixed HG: their FP32 copy
+  double* d_csnv3 = nullptr;          // 3D HG: [E][3][N^2][N - 1] triples
+  float4* d_csnv3_32 = nullptr;       // mixed 3D HG: (x, y, z, 0)
   float4* d_cja32 = nullptr;          // mixed: [E][NN] Ja^1, Ja^2
   float* d_cinvj32 = nullptr;         // mixed: [E][NN] inverse Jacobian
   double* d_cxy = nullptr;            // fp64 sources: [E][NN][2] node coordinates
@@ -1124,7 +1126,7 @@ static void free_ctx(tg_ctx* c) {
     if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
   void* ptrs[] = {c->d_u[0], c->d_u[1], c->d_utmp, c->d_du, c->d_uscratch, c->d_stage64,
                   c->d_uff, c->d_alpha_raw, c->d_alpha, c->d_alpha_sm, c->d_rp, c->d_nbr, c->d_invj, c->d_xline,
-                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mmat32, c->d_mflux, c->d_scls, c->d_amr_raw, c->d_amr_alpha, c->d_amap, c->d_akind, c->d_weights, c->d_cmet, c->d_csnv, c->d_csnv32, c->d_cja32, c->d_cinvj32, c->d_cxy, c->d_csc, c->d_partial, c->d_enorm, c->d_sums, c->d_clock,
+                  c->d_invj_f, c->d_xline_f, c->d_sc0, c->d_scn, c->d_bface, c->d_ghost, c->d_mtab, c->d_mnbr, c->d_mmat, c->d_mmat32, c->d_mflux, c->d_scls, c->d_amr_raw, c->d_amr_alpha, c->d_amap, c->d_akind, c->d_weights, c->d_cmet, c->d_csnv, c->d_csnv32, c->d_csnv3, c->d_csnv3_32, c->d_cja32, c->d_cinvj32, c->d_cxy, c->d_csc, c->d_partial, c->d_enorm, c->d_sums, c->d_clock,
                   c->d_status, c->d_speed};
   for (int k = 0; k < 2; ++k)
     if (c->xstream[k]) cudaStreamSynchronize(c->xstream[k]);
@@ -1494,7 +1496,56 @@ static int curved_setup(tg_ctx* c, const tg_config* cfg) {
     CUDA_TRY(nullptr, cudaMemcpy(c->d_cxy, cfg->node_coordinates, sizeof(double) * nq * D,
                                  cudaMemcpyHostToDevice));
   }
-  if (c->vi == VI_HG) {
+  if (c->vi == VI_HG && D == 3) {
+    // calc_normalvectors_subcell_fv! (dgsem_structured/containers_3d.jl:352-470):
+    // per direction d, Ja^d at the line's first node plus the partial sums of
+    // w_m D[m, :] Ja^d along the line (D by barycentric weights, as in 2D)
+    const double* x = cfg->nodes;
+    std::vector<double> wb(N, 1.0), Dm((size_t)N * N, 0.0);
+    for (int j = 0; j < N; ++j)
+      for (int k = 0; k < N; ++k)
+        if (k != j) wb[j] /= x[j] - x[k];
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j)
+        if (j != i) {
+          Dm[i * N + j] = (wb[j] / wb[i]) / (x[i] - x[j]);
+          Dm[i * N + i] -= Dm[i * N + j];
+        }
+    const int NF = N * N;
+    const size_t nsv = (size_t)E * 3 * NF * (N - 1);
+    std::vector<double> snv(nsv * 3);
+    for (int64_t e = 0; e < E; ++e)
+      for (int dd = 0; dd < 3; ++dd)
+        for (int l = 0; l < NF; ++l) {
+          const int l0 = l % N, l1 = l / N;
+          auto ja = [&](int a, int xyz) {
+            const int q = dd == 0 ? a + N * (l0 + N * l1)
+                                  : (dd == 1 ? l0 + N * (a + N * l1) : l0 + N * (l1 + N * a));
+            return met[((size_t)e * NN + q) * MS + 3 * dd + xyz];
+          };
+          double acc[3] = {ja(0, 0), ja(0, 1), ja(0, 2)};
+          for (int i = 0; i < N - 1; ++i) {
+            for (int m = 0; m < N; ++m) {
+              const double wd = cfg->weights[i] * Dm[i * N + m];
+              for (int xyz = 0; xyz < 3; ++xyz) acc[xyz] += wd * ja(m, xyz);
+            }
+            for (int xyz = 0; xyz < 3; ++xyz)
+              snv[((((size_t)e * 3 + dd) * NF + l) * (N - 1) + i) * 3 + xyz] = acc[xyz];
+          }
+        }
+    CUDA_TRY(nullptr, cudaMalloc((void**)&c->d_csnv3, sizeof(double) * snv.size()));
+    CUDA_TRY(nullptr, cudaMemcpy(c->d_csnv3, snv.data(), sizeof(double) * snv.size(),
+                                 cudaMemcpyHostToDevice));
+    if (!c->fp64) {
+      std::vector<float4> s32(nsv);
+      for (size_t k = 0; k < nsv; ++k)
+        s32[k] = make_float4((float)snv[3 * k], (float)snv[3 * k + 1], (float)snv[3 * k + 2], 0.0f);
+      CUDA_TRY(nullptr, cudaMalloc((void**)&c->d_csnv3_32, sizeof(float4) * nsv));
+      CUDA_TRY(nullptr, cudaMemcpy(c->d_csnv3_32, s32.data(), sizeof(float4) * nsv,
+                                   cudaMemcpyHostToDevice));
+    }
+  }
+  if (c->vi == VI_HG && D == 2) {
     // calc_normalvectors_subcell_fv! (dgsem_structured/containers_2d.jl:200-298):
     // the normal of the subcell interface between nodes i and i + 1 of a line
     // is Ja at the line's first node plus the partial sums of w_m D[m, :] Ja
@@ -1575,6 +1626,8 @@ static int curved_setup(tg_ctx* c, const tg_config* cfg) {
   C.alpha_atol = c->P.alpha_atol;
   C.snv = c->d_csnv;
   C.snv32 = c->d_csnv32;
+  C.snv3 = c->d_csnv3;
+  C.snv3_32 = c->d_csnv3_32;
   return TG_OK;
 }
 
@@ -1677,9 +1730,9 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
       return fail(nullptr, TG_ERR_UNSUPPORTED, "curvilinear meshes: polydeg %d is not compiled",
                   cfg->polydeg);
     const bool hg = cfg->volume_integral == TG_VOLUME_SHOCK_CAPTURING_HG;
-    if (hg && D == 3)
+    if (hg && D == 3 && N != 4)
       return fail(nullptr, TG_ERR_UNSUPPORTED,
-                  "3D curvilinear meshes: weak form or flux differencing only");
+                  "3D curvilinear meshes: shock capturing at polydeg 3 only");
     const int vf = cfg->volume_flux, sf = cfg->surface_flux;
     if (hg && (cfg->volume_flux_fv == TG_FLUX_HLLC || cfg->volume_flux_fv == TG_FLUX_HLLE))
       return fail(nullptr, TG_ERR_UNSUPPORTED, "curvilinear meshes: FV flux_hllc / flux_hlle");

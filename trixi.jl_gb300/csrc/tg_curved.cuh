@@ -51,6 +51,10 @@ struct CurvedParams {
   double alpha_atol;
   const double2* snv;       // [E][2][N][N - 1]
   const float2* snv32;
+  // 3D: the same per direction d and line l (the two other node indices,
+  // lower one fastest): [E][3][N^2][N - 1], FP64 triples and FP32 (x, y, z, 0)
+  const double* snv3;
+  const float4* snv3_32;
 };
 
 // ---------------------------------------------------------------------------

@@ -140,7 +140,8 @@ struct Curved3K {
   static constexpr int FACE = EPB * 6 * NF * NV;
   static constexpr int SP = EPB * NN;
   static constexpr size_t smem() {
-    return sizeof(double) * (CHUNK + FACE + 3 * NV * SP) + sizeof(unsigned long long) * 3 * EPB;
+    return sizeof(double) * (CHUNK + FACE + 3 * NV * SP) + sizeof(unsigned long long) * 3 * EPB +
+           sizeof(double) * EPB;  // blending factors (VI_HG)
   }
 };
 
@@ -165,6 +166,7 @@ __global__ void __launch_bounds__(Curved3K<N, EPB>::NT)
   double* s_fu = s_u + CHUNK;                 // [EPB][6][NF][NV] neighbour / boundary traces
   double* s_part = s_fu + K::FACE;            // [3][NV][SP]
   unsigned long long* s_smax = reinterpret_cast<unsigned long long*>(s_part + 3 * NV * SP);
+  double* s_alpha = reinterpret_cast<double*>(s_smax + 3 * EPB);  // [EPB] (VI_HG)
 
   const int tid = threadIdx.x;
   const int64_t e0 = (int64_t)blockIdx.x * EPB;
@@ -200,6 +202,20 @@ __global__ void __launch_bounds__(Curved3K<N, EPB>::NT)
     for (int v = 0; v < NV; ++v) s_fu[k * NV + v] = __ldg(g + v);
   }
   if (tid < 3 * EPB) s_smax[tid] = 0ull;
+  if (VI == VI_HG && tid < nel) {
+    // apply_smoothing! as a gather over the face neighbours
+    const double* raw = static_cast<const double*>(A.alpha_raw);
+    const int64_t e = e0 + tid;
+    double a = raw[e];
+    if (P.alpha_smooth)
+#pragma unroll
+      for (int f = 0; f < 6; ++f) {
+        const int32_t nb = P.nbr[e * 6 + f];
+        if (nb >= 0) a = fmax(a, 0.5 * raw[nb]);
+      }
+    s_alpha[tid] = a;
+    if (A.alpha_out) static_cast<double*>(A.alpha_out)[e] = a;
+  }
   __syncthreads();
 
   // ---- lines ---------------------------------------------------------------------
@@ -255,6 +271,33 @@ __global__ void __launch_bounds__(Curved3K<N, EPB>::NT)
               acc[b][v] = fma(cba, F[v], acc[b][v]);
             }
           }
+      }
+      if (VI == VI_HG) {
+        // (1 - alpha) flux differencing + alpha FV subcell fluxes along the
+        // subcell normals, zero at the element faces (calcflux_fv!,
+        // dgsem_structured/dg_3d.jl; calc_volume_integral.jl:231-272)
+        const double ae = s_alpha[sl];
+        if (!(fabs(ae) <= P.alpha_atol)) {
+#pragma unroll
+          for (int a = 0; a < N; ++a)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[a][v] *= 1.0 - ae;
+          const double* nv = P.snv3 + ((((size_t)e * 3 + dd) * NF + line) * (N - 1)) * 3;
+          double fl[NV] = {0.0, 0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            double fr[NV] = {0.0, 0.0, 0.0, 0.0, 0.0};
+            if (i < N - 1) {
+              const double n3[3] = {nv[3 * i], nv[3 * i + 1], nv[3 * i + 2]};
+              FluxN3::two_point(P.fv_flux, uu[i], ww[i], uu[i + 1], ww[i + 1], n3, gamma, igm1, fr);
+            }
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+              acc[i][v] += ae * (P.inv_weights[i] * (fr[v] - fl[v]));
+              fl[v] = fr[v];
+            }
+          }
+        }
       }
       const double factor = P.inv_weights[0];
 #pragma unroll
@@ -380,7 +423,7 @@ struct Curved3M {
   static constexpr size_t smem() {
     return sizeof(float2) * (CHUNK + FACE) + sizeof(float4) * 4 * SP +
            sizeof(float) * (NV * SP + (NV + 1) * SP + 3 * NV * SP) + sizeof(RefState<3>) * EPB +
-           sizeof(float) * 4 + sizeof(unsigned int) * 3 * EPB;
+           sizeof(float) * 4 + sizeof(unsigned int) * 3 * EPB + sizeof(float) * EPB;
   }
 };
 
@@ -401,6 +444,7 @@ __global__ void __launch_bounds__(Curved3M<N, EPB>::NT)
   RefState<3>* s_ref = reinterpret_cast<RefState<3>*>(s_part + 3 * NV * SP);
   float* s_scal = reinterpret_cast<float*>(s_ref + EPB);     // b dt, a (hi, lo)
   unsigned int* s_smax = reinterpret_cast<unsigned int*>(s_scal + 4);
+  float* s_alpha = reinterpret_cast<float*>(s_smax + 3 * EPB);  // [EPB] (VI_HG)
 
   const int tid = threadIdx.x;
   const int64_t e0 = (int64_t)blockIdx.x * EPB;
@@ -475,6 +519,19 @@ __global__ void __launch_bounds__(Curved3M<N, EPB>::NT)
 #pragma unroll
     for (int v = 0; v < NV; ++v) hi[v] = 0.5f * (ue[v].x + ue[(NN - 1) * NV + v].x);
     Dv::make_ref(hi, eos, s_ref[tid]);
+    if (VI == VI_HG) {
+      // apply_smoothing! as a gather over the face neighbours
+      const int64_t e = e0 + tid;
+      float a = A.alpha_raw[e];
+      if (P.alpha_smooth)
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+          const int32_t nb = P.nbr[e * 6 + f];
+          if (nb >= 0) a = fmaxf(a, 0.5f * A.alpha_raw[nb]);
+        }
+      s_alpha[tid] = a;
+      if (A.alpha_out) A.alpha_out[e] = a;
+    }
   }
   cp_async_wait_all();
   __syncthreads();
@@ -563,6 +620,34 @@ __global__ void __launch_bounds__(Curved3M<N, EPB>::NT)
               acc[b][v] = fmaf(cba, F[v], acc[b][v]);
             }
           }
+      }
+      if (VI == VI_HG) {
+        // the FP64 kernel's blend in deviation form (as in 2D, tg_curved.cu)
+        const float ae = s_alpha[sl];
+        if (!(fabsf(ae) <= (float)P.alpha_atol)) {
+#pragma unroll
+          for (int a = 0; a < N; ++a) {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[a][v] *= 1.0f - ae;
+            Dv::node_du(s_u + ((size_t)sl * NN + line3<N>(line, dd, a)) * NV, R, nd[a].du);
+          }
+          const float4* nv = P.snv3_32 + (((size_t)e * 3 + dd) * NF + line) * (N - 1);
+          float fl[NV] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            float fr[NV] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+            if (i < N - 1) {
+              const float4 n4 = nv[i];
+              const float n3[3] = {n4.x, n4.y, n4.z};
+              dev_surface_n<3>(P.fv_flux, R, nd[i], nd[i + 1], n3, eos, fr);
+            }
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+              acc[i][v] = fmaf(ae, P.inv_weights32[i] * (fr[v] - fl[v]), acc[i][v]);
+              fl[v] = fr[v];
+            }
+          }
+        }
       }
       const float factor = P.inv_weights32[0];
 #pragma unroll
@@ -780,13 +865,14 @@ int launch_curved3_n(const CurvedParams& P, const StageArgs* A64, const MixedArg
 }  // namespace
 
 // Built for polydeg 3 and 5 (N = 4, 6: the degrees of Trixi's StructuredMesh3D
-// Euler elixirs), each with the weak form and flux differencing, FP64 and
-// mixed precision.
+// Euler elixirs), each with the weak form and flux differencing, and shock
+// capturing at polydeg 3; FP64 and mixed precision.
 int curved3_supported(int N) { return N == 4 || N == 6; }
 
 int launch_curved3(const CurvedParams& P, const StageArgs* A64, const MixedArgs* A32,
                    cudaStream_t stream) {
   if ((A64 == nullptr) == (A32 == nullptr)) return -2;
+  if (P.vi == VI_HG) return P.N == 4 ? launch_curved3_n<4, VI_HG>(P, A64, A32, stream) : -3;
   const bool fd = P.vi == VI_FD;
   if (!fd && P.vi != VI_WEAK) return -3;
   if (P.N == 4) return fd ? launch_curved3_n<4, VI_FD>(P, A64, A32, stream)

@@ -22,6 +22,7 @@ from .analysis import calc_error_norms  # noqa: F401
 from .basis import LobattoLegendreAnalyzer, LobattoLegendreBasis, MortarL2  # noqa: F401
 from .equations import (initial_condition_density_wave,  # noqa: F401
                         flux_chandrashekar, flux_hlle, initial_condition_sedov_blast_wave,  # noqa: F401
+                        initial_condition_medium_sedov_blast_wave,  # noqa: F401
                         flux_hllc, initial_condition_isentropic_vortex_advected,  # noqa: F401
                         initial_condition_density_pulse,  # noqa: F401
                         initial_condition_blast_wave,  # noqa: F401

@@ -211,6 +211,21 @@ def initial_condition_sedov_blast_wave(x, t, equations):
     return prim2cons(prim, equations)
 
 
+def initial_condition_medium_sedov_blast_wave(x, t, equations):
+    """initial_condition_medium_sedov_blast_wave of
+    examples/structured_3d_dgsem/elixir_euler_sedov.jl: energy 1 in a ball of
+    radius 0.21875 at rest in a background at p = 1e-3."""
+    if equations.ndims != 3:
+        raise NotImplementedError("initial_condition_medium_sedov_blast_wave is the 3D elixir's")
+    r = np.sqrt(x[..., 0] ** 2 + x[..., 1] ** 2 + x[..., 2] ** 2)
+    r0, E = 0.21875, 1.0
+    p_inner = 3 * (equations.gamma - 1) * E / (4 * math.pi * r0 ** 2)
+    prim = np.zeros(x.shape[:-1] + (5,))
+    prim[..., 0] = 1.0
+    prim[..., 4] = np.where(r > r0, 1.0e-3, p_inner)
+    return prim2cons(prim, equations)
+
+
 def initial_condition_density_pulse(x, t, equations):
     """examples/tree_3d_dgsem/elixir_euler_amr.jl:9-25: a Gaussian density pulse
     at rest pressure 1 moving with velocity (1, 1, 1)."""

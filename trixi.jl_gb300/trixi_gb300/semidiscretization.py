@@ -425,8 +425,6 @@ class SemidiscretizationHyperbolic:
             # StructuredMesh / P4estMesh brick: per-node metric terms
             # (dgsem_structured/containers_2d.jl:9-35, dgsem_p4est/containers_2d.jl:9-27)
             from .curved_mesh import metric_terms, metric_terms_3d
-            if isinstance(solver.volume_integral, VolumeIntegralShockCapturingHG) and D == 3:
-                raise NotImplementedError("3D curvilinear meshes: weak form or flux differencing only")
             self.node_coordinates = mesh.node_coordinates(solver.basis)
             self.contravariant_vectors, self.inverse_jacobian = (
                 metric_terms if D == 2 else metric_terms_3d)(self.node_coordinates, solver.basis)
