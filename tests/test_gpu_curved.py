@@ -1,5 +1,6 @@
-"""Curvilinear 2D meshes (StructuredMesh, P4estMesh bricks) on the GPU against the
-oracle and the goldens of Trixi.jl's StructuredMesh / P4estMesh Euler tests."""
+"""Curvilinear meshes (2D StructuredMesh and P4estMesh bricks, 3D StructuredMesh) on
+the GPU against the oracle and the goldens of Trixi.jl's StructuredMesh / P4estMesh
+Euler tests."""
 import numpy as np
 import pytest
 
