@@ -14,6 +14,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -1035,6 +1036,9 @@ struct tg_ctx {
   // was initialised), when nothing else has stepped the context since
   int64_t host_steps = 0;
   bool host_steps_valid = false;
+  // buffers taken from the device's context pool (returned to it, in stream
+  // order, when the context is destroyed)
+  std::vector<void*> pool_ptrs;
   int32_t* d_nbr = nullptr;
   double* d_invj = nullptr;
   double* d_xline = nullptr;
@@ -1119,6 +1123,33 @@ static size_t rsize(const tg_ctx* c) { return c->fp64 ? sizeof(double) : sizeof(
 // 16-byte groups past the last element.
 constexpr int64_t kElemPad = 64;
 
+// Per-device memory pool for the buffers of contexts: an AMR pass destroys a
+// context and creates one for the adapted mesh, so their buffers come from a
+// pool that keeps freed memory (release threshold: never) instead of
+// cudaMalloc / cudaFree every time.
+static cudaMemPool_t context_pool(int device) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  if (device < 0 || device >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!pools[device]) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    cudaMemPool_t p = nullptr;
+    if (cudaMemPoolCreate(&p, &props) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    uint64_t keep = ~0ull;
+    cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    pools[device] = p;
+  }
+  return pools[device];
+}
+
 static void free_ctx(tg_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
@@ -1131,7 +1162,12 @@ static void free_ctx(tg_ctx* c) {
   for (int k = 0; k < 2; ++k)
     if (c->xstream[k]) cudaStreamSynchronize(c->xstream[k]);
   for (void* p : ptrs)
-    if (p) cudaFree(p);
+    if (p && std::find(c->pool_ptrs.begin(), c->pool_ptrs.end(), p) == c->pool_ptrs.end())
+      cudaFree(p);
+  // cudaFree waits for the whole device; the pool frees keep that guarantee
+  // (work on other streams that still reads a buffer ends before its reuse)
+  if (!c->pool_ptrs.empty()) cudaDeviceSynchronize();
+  for (void* p : c->pool_ptrs) cudaFreeAsync(p, c->stream);
   for (int k = 0; k < 2; ++k) {
     if (c->d_xin[k]) cudaFree(c->d_xin[k]);
     if (c->d_xout[k]) cudaFree(c->d_xout[k]);
@@ -1951,20 +1987,28 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     delete c;
     return fail(nullptr, TG_ERR_CUDA, "cudaSetDevice(%d): %s", cfg->device, cudaGetErrorString(e));
   }
-#define ALLOC(ptr, bytes)                                                                 \
-  do {                                                                                    \
-    e = cudaMalloc((void**)&(ptr), (bytes));                                              \
-    if (e != cudaSuccess) {                                                               \
-      free_ctx(c);                                                                        \
-      return fail(nullptr, TG_ERR_CUDA, "cudaMalloc(%zu): %s", (size_t)(bytes),          \
-                  cudaGetErrorString(e));                                                 \
-    }                                                                                     \
-  } while (0)
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     free_ctx(c);
     return fail(nullptr, TG_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
   }
+  // stream-ordered allocations from the device's context pool (cudaMalloc if
+  // the pool is unavailable); the stream is synchronised once they are made
+  cudaMemPool_t pool = context_pool(c->device);
+#define ALLOC(ptr, bytes)                                                                 \
+  do {                                                                                    \
+    if (pool) {                                                                           \
+      e = cudaMallocFromPoolAsync((void**)&(ptr), (bytes), pool, c->stream);              \
+      if (e == cudaSuccess) c->pool_ptrs.push_back((void*)(ptr));                         \
+    } else {                                                                              \
+      e = cudaMalloc((void**)&(ptr), (bytes));                                            \
+    }                                                                                     \
+    if (e != cudaSuccess) {                                                               \
+      free_ctx(c);                                                                        \
+      return fail(nullptr, TG_ERR_CUDA, "device allocation (%zu bytes): %s",              \
+                  (size_t)(bytes), cudaGetErrorString(e));                                \
+    }                                                                                     \
+  } while (0)
   const size_t vb = sizeof(double) * (size_t)c->nvalues;
   ALLOC(c->d_u[0], vb);
   ALLOC(c->d_u[1], vb);
@@ -2078,6 +2122,12 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     }
   }
 #undef ALLOC
+  // the pool allocations are complete before any other stream touches them
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    free_ctx(c);
+    return fail(nullptr, TG_ERR_CUDA, "context allocations: %s", cudaGetErrorString(e));
+  }
   if (!c->fp64) {
     cudaMemset(c->d_invj_f, 0, sizeof(float) * (c->E + kElemPad));
     cudaMemcpy(c->d_invj_f, invj_f.data(), sizeof(float) * c->E, cudaMemcpyHostToDevice);
