@@ -1125,8 +1125,9 @@ constexpr int64_t kElemPad = 64;
 
 // Per-device memory pool for the buffers of contexts: an AMR pass destroys a
 // context and creates one for the adapted mesh, so their buffers come from a
-// pool that keeps freed memory (release threshold: never) instead of
-// cudaMalloc / cudaFree every time.
+// pool that keeps up to 4 GiB of freed memory (its release threshold) instead
+// of cudaMalloc / cudaFree every time; freed memory above that goes back to
+// the device at the next synchronisation, for other allocators to use.
 static cudaMemPool_t context_pool(int device) {
   static std::mutex mu;
   static cudaMemPool_t pools[64] = {};
@@ -1143,7 +1144,7 @@ static cudaMemPool_t context_pool(int device) {
       cudaGetLastError();
       return nullptr;
     }
-    uint64_t keep = ~0ull;
+    uint64_t keep = 4ull << 30;
     cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
     pools[device] = p;
   }
