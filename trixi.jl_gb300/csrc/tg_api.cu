@@ -131,17 +131,61 @@ bool supported_epb(int D, int N, int epb) {
 // Small kernels: CFL reduction, clock, integrals, smoothing
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ double state_f64(double x) { return x; }
-__device__ __forceinline__ double state_f64(float2 x) { return (double)x.x + (double)x.y; }
+// FP64 <-> float-float conversions of the state (the mixed path's boundary).
+// The FP64 pipe of this GPU runs at 1/62 of the FP32 rate, and a conversion
+// between float and double is an FP64-pipe instruction, so the conversions of
+// a whole state were bound by that pipe, not by HBM.  They are done here with
+// integer operations on the IEEE-754 bit patterns where the values allow it,
+// with results identical to the conversion instructions, and with those
+// instructions for the rest (zeros, subnormals, infinities, NaN, extreme
+// exponents).
 
-// FP64 <-> float-float conversion of the state (mixed path boundary)
+// (double)f, exact: a normal float's exponent is rebiased (127 -> 1023) and its
+// 23-bit fraction shifted into the top of the 52-bit one.
+__device__ __forceinline__ double widen_f32(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xffu;
+  if (e - 1u < 254u)
+    return __longlong_as_double((long long)(((uint64_t)(b & 0x80000000u) << 32) |
+                                            ((uint64_t)(e + 896u) << 52) |
+                                            ((uint64_t)(b & 0x7fffffu) << 29)));
+  if ((b & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((uint64_t)b << 32));
+  return (double)f;  // subnormal, infinity, NaN
+}
+
+// hi = (float)x rounded to nearest even, lo = (float)(x - hi), as
+// __double2float_rn(x) and __double2float_rn(x - (double)hi).  For a binary
+// exponent E of x in [-74, 126], hi's fraction is x's top 23 fraction bits
+// rounded to nearest even on the 29 dropped bits r (a carry into the
+// exponent is the correct rounding); x - hi is exactly +-(r or r - 2^29) *
+// 2^(E-52), whose rounding to float is that integer's rounding to 24 bits
+// (__int2float_rn) times 2^(E-52), a normal float in this exponent range, so
+// the product is exact.
+__device__ __forceinline__ float2 split_f64(double x) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;  // biased exponent, 1023 + E
+  if (e - 949u <= 200u) {                           // E in [-74, 126]
+    const uint32_t keep = (uint32_t)(b >> 29) & 0x7fffffu;
+    const uint32_t rem = (uint32_t)b & 0x1fffffffu;
+    const uint32_t up = (rem > 0x10000000u || (rem == 0x10000000u && (keep & 1u))) ? 1u : 0u;
+    const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    const uint32_t hb = (sign | ((e - 896u) << 23) | keep) + up;
+    int32_t r = (int32_t)rem - (int32_t)(up << 29);  // |x| - |hi| in units of 2^(E-52)
+    if (sign) r = -r;                                 // x - hi (+0 when it vanishes)
+    const float scale = __uint_as_float((e - 949u + 1u) << 23);  // 2^(E-52), E-52 >= -126
+    return make_float2(__uint_as_float(hb), __fmul_rn(__int2float_rn(r), scale));
+  }
+  const float hi = __double2float_rn(x);
+  return make_float2(hi, __double2float_rn(x - (double)hi));
+}
+
+__device__ __forceinline__ double state_f64(double x) { return x; }
+__device__ __forceinline__ double state_f64(float2 x) { return widen_f32(x.x) + widen_f32(x.y); }
+
 __global__ void to_ff_kernel(const double* __restrict__ in, float2* __restrict__ out, int64_t n) {
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    const double x = in[k];
-    const float hi = __double2float_rn(x);
-    out[k] = make_float2(hi, __double2float_rn(x - (double)hi));
-  }
+       k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = split_f64(in[k]);
 }
 // to_ff_kernel for a 2D state (4 values per node) that also writes rho*p of
 // every node from the hi parts, with the stage kernels' arithmetic
@@ -151,14 +195,67 @@ __global__ void to_ff_rp_kernel(const double* __restrict__ in, float2* __restric
        k += (int64_t)gridDim.x * blockDim.x) {
     float hi[4], lo[4];
     for (int v = 0; v < 4; ++v) {  // 8-byte loads: `in` may be a caller's host buffer
-      const double x = in[4 * k + v];
-      hi[v] = __double2float_rn(x);
-      lo[v] = __double2float_rn(x - (double)hi[v]);
+      const float2 f = split_f64(in[4 * k + v]);
+      hi[v] = f.x;
+      lo[v] = f.y;
     }
     reinterpret_cast<float4*>(out)[2 * k] = make_float4(hi[0], lo[0], hi[1], lo[1]);
     reinterpret_cast<float4*>(out)[2 * k + 1] = make_float4(hi[2], lo[2], hi[3], lo[3]);
     rp[k] = Euler<2, float>::density_pressure(hi, gamma);
   }
+}
+
+template <int D>
+__device__ __forceinline__ bool node_speeds_ff(const float* hi, float gamma, float* ml);
+__device__ __forceinline__ void block_speed_max(unsigned long long mine,
+                                                unsigned long long* __restrict__ speed_bits);
+
+// to_ff_rp_kernel fused with the CFL reduction of the imported state (the
+// reduction max_speed_ff_kernel<2> makes, same arithmetic, same result): a
+// 2D element's NN nodes (NN a power of two <= 16) are NN consecutive threads,
+// which combine their speeds by shuffles within their lane group; the block
+// maximum goes to speed_bits by one atomicMax.  speed_bits must hold its
+// initial value (speed_reset_kernel) before the launch.
+template <int NN>
+__global__ void __launch_bounds__(256) to_ff_rp_speed_kernel(
+    const double* __restrict__ in, float2* __restrict__ out, int64_t nnodes, float gamma_rp,
+    float* __restrict__ rp, float gamma, const float* __restrict__ inv_jac,
+    unsigned long long* __restrict__ speed_bits, int32_t* __restrict__ status) {
+  static_assert(NN >= 1 && NN <= 16 && (NN & (NN - 1)) == 0, "lane groups of NN threads");
+  const int lane = threadIdx.x & 31;
+  const unsigned gmask = ((1u << NN) - 1u) << (lane & ~(NN - 1));
+  unsigned long long best = 0;
+  bool bad = false;
+  // the grid stride is a multiple of NN, so an element's threads stay together
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nnodes;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    float hi[4], lo[4];
+    for (int v = 0; v < 4; ++v) {  // 8-byte loads: `in` may be a caller's host buffer
+      const float2 f = split_f64(in[4 * k + v]);
+      hi[v] = f.x;
+      lo[v] = f.y;
+    }
+    reinterpret_cast<float4*>(out)[2 * k] = make_float4(hi[0], lo[0], hi[1], lo[1]);
+    reinterpret_cast<float4*>(out)[2 * k + 1] = make_float4(hi[2], lo[2], hi[3], lo[3]);
+    rp[k] = Euler<2, float>::density_pressure(hi, gamma_rp);
+    float ml[2];
+    bad |= node_speeds_ff<2>(hi, gamma, ml);
+    for (int d = 0; d < 2; ++d)
+      for (int o = NN / 2; o > 0; o >>= 1) ml[d] = fmaxf(ml[d], __shfl_xor_sync(gmask, ml[d], o));
+    if ((lane & (NN - 1)) == 0) {
+      float sum = 0;
+      for (int d = 0; d < 2; ++d) sum += ml[d];
+      const float sp = inv_jac[k / NN] * sum;
+      if (sp == sp) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong((double)sp);
+        best = b > best ? b : best;
+      } else {
+        bad = true;
+      }
+    }
+  }
+  if (bad) atomicOr(status, 2);
+  block_speed_max(best, speed_bits);
 }
 
 // rho*p of every node from the hi parts of a float-float state (nv values per
@@ -190,7 +287,7 @@ __global__ void from_ff_kernel(const float2* __restrict__ in, double* __restrict
 // per element on a single address.
 __device__ __forceinline__ void block_speed_max(unsigned long long mine,
                                                 unsigned long long* __restrict__ speed_bits) {
-  __shared__ unsigned long long s_max[4];
+  __shared__ unsigned long long s_max[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long other = __shfl_xor_sync(0xffffffffu, mine, o);
@@ -248,6 +345,22 @@ __global__ void __launch_bounds__(128) max_speed_kernel(const TS* __restrict__ u
   block_speed_max(best, speed_bits);
 }
 
+// Per-node wave speeds |v_d| + c of a mixed context's CFL reduction from the
+// hi parts of the state (FP32 primitives and sound speed); a NaN speed (a
+// non-positive density or pressure) counts as 0 and is flagged.
+template <int D>
+__device__ __forceinline__ bool node_speeds_ff(const float* hi, float gamma, float* ml) {
+  constexpr int NV = D + 2;
+  float w[NV];
+  Euler<D, float>::cons2prim(hi, w, gamma);
+  const float cs = sqrtf(gamma * w[NV - 1] / w[0]);
+  for (int d = 0; d < D; ++d) {
+    const float lam = fabsf(w[1 + d]) + cs;
+    ml[d] = lam == lam ? lam : 0.0f;
+  }
+  return !(w[0] > 0.0f) || !(w[NV - 1] > 0.0f);
+}
+
 // The same reduction for a mixed context in the FP32 arithmetic its stage
 // kernel uses for the wave speed of the updated state (hi parts, FP32
 // primitives and sound speed, FP32 inverse Jacobian), so that the first dt
@@ -269,15 +382,10 @@ __global__ void __launch_bounds__(128) max_speed_ff_kernel(const float2* __restr
     for (int d = 0; d < D; ++d) ml[d] = 0.0f;
     for (int q = lane; q < NN; q += 32) {
       const float2* p = u + ((size_t)e * NN + q) * NV;
-      float hi[NV], w[NV];
+      float hi[NV], lam[D];
       for (int v = 0; v < NV; ++v) hi[v] = p[v].x;
-      Euler<D, float>::cons2prim(hi, w, gamma);
-      const float cs = sqrtf(gamma * w[NV - 1] / w[0]);
-      bad |= !(w[0] > 0.0f) || !(w[NV - 1] > 0.0f);
-      for (int d = 0; d < D; ++d) {
-        const float lam = fabsf(w[1 + d]) + cs;
-        if (lam == lam) ml[d] = fmaxf(ml[d], lam);
-      }
+      bad |= node_speeds_ff<D>(hi, gamma, lam);
+      for (int d = 0; d < D; ++d) ml[d] = fmaxf(ml[d], lam[d]);
     }
     for (int d = 0; d < D; ++d)
       for (int o = 16; o > 0; o >>= 1) ml[d] = fmaxf(ml[d], __shfl_xor_sync(0xffffffffu, ml[d], o));
@@ -1018,6 +1126,10 @@ struct tg_ctx {
   // stage kernel that produced it (rp_valid), read by the next indicator
   float* d_rp = nullptr;
   bool rp_valid = false;
+  // the clock's speed_bits hold the CFL reduction of the current state, made
+  // when it was imported (to_ff_rp_speed_kernel); cleared by anything else
+  // that sets the state
+  bool speed_fresh = false;
   // host transfers that overlap the stepping (tg_prefetch_state, tg_fetch_state):
   // copy streams (0: host to device, 1: device to host), FP64 staging slots
   // and the events that order them with the context stream
@@ -1201,10 +1313,22 @@ static int import_state(tg_ctx* c, const double* src, void* dst) {
                                   c->stream));
     return TG_OK;
   }
+  c->speed_fresh = false;
   if (c->d_rp && dst == c->d_u[c->cur] && c->NV == 4) {
-    to_ff_rp_kernel<<<conv_blocks(c->ndofs), 256, 0, c->stream>>>(src, (float2*)dst, c->ndofs,
-                                                                   c->MP.gamma, c->d_rp);
-    CUDA_TRY(c, cudaGetLastError());
+    if (!c->curved && c->NN == 16) {
+      // the CFL reduction of the new state in the same pass (ctx_clock_prepare
+      // then skips its own)
+      speed_reset_kernel<<<1, 1, 0, c->stream>>>(&c->d_clock->speed_bits);
+      to_ff_rp_speed_kernel<16><<<conv_blocks(c->ndofs), 256, 0, c->stream>>>(
+          src, (float2*)dst, c->ndofs, c->MP.gamma, c->d_rp, (float)c->P.gamma, c->d_invj_f,
+          &c->d_clock->speed_bits, c->d_status);
+      CUDA_TRY(c, cudaGetLastError());
+      c->speed_fresh = true;
+    } else {
+      to_ff_rp_kernel<<<conv_blocks(c->ndofs), 256, 0, c->stream>>>(src, (float2*)dst, c->ndofs,
+                                                                     c->MP.gamma, c->d_rp);
+      CUDA_TRY(c, cudaGetLastError());
+    }
     c->rp_valid = true;
     return TG_OK;
   }
@@ -1294,6 +1418,7 @@ static void launch_mortars(tg_ctx* c, const void* u_in) {
 static int launch_kernel(tg_ctx* c, int mode, const void* u_in, void* u_out, double* du_out,
                          double t_rhs, int stage, bool reduce, bool write_rp = false) {
   int rc;
+  c->speed_fresh = false;
   if (c->nmortar > 0) launch_mortars(c, u_in);
   if (c->curved) {
     StageArgs A{};
@@ -2469,6 +2594,7 @@ int tg_state_device_ptr(tg_ctx* c, double** u_dev) {
   if (!c || !u_dev) return TG_ERR_INVALID_ARGUMENT;
   *u_dev = (double*)c->d_u[c->cur];
   c->rp_valid = false;  // the caller may write the state
+  c->speed_fresh = false;
   return TG_OK;
 }
 
@@ -2615,8 +2741,11 @@ namespace tg {
 int ctx_clock_prepare(tg_ctx* c, double t0, double t_end, double cfl, bool sync) {
   if (!c->clock_valid) {
     // initialize!(StepsizeCallback): dt = cfl * max_dt(u0)
-    int rc = reduce_speed(c, c->d_u[c->cur], !c->fp64, &c->d_clock->speed_bits);
-    if (rc) return rc;
+    if (!c->speed_fresh) {
+      int rc = reduce_speed(c, c->d_u[c->cur], !c->fp64, &c->d_clock->speed_bits);
+      if (rc) return rc;
+    }
+    c->speed_fresh = false;
     clock_init_kernel<<<1, 1, 0, c->stream>>>(c->d_clock, t0, t_end, cfl, c->N);
     CUDA_TRY(c, cudaGetLastError());
     c->clock_valid = true;
@@ -2653,6 +2782,7 @@ int ctx_view(tg_ctx* c, CtxView* v) {
 void ctx_set_cur(tg_ctx* c, int cur) {
   c->cur = cur & 1;
   c->rp_valid = false;
+  c->speed_fresh = false;
   c->host_steps_valid = false;  // stepped by the ensemble
 }
 }  // namespace tg
@@ -2682,7 +2812,7 @@ static int read_clock(tg_ctx* c, Clock* h) {
 
 static int capture_step_graph(tg_ctx* c, int parity) {
   const int saved = c->cur;
-  const bool saved_rp = c->rp_valid;
+  const bool saved_rp = c->rp_valid, saved_speed = c->speed_fresh;
   c->cur = parity;
   // stage 0 reads rho*p of the step's input state: tg_step refreshes it
   // before launching the graphs whenever the state was set from outside
@@ -2696,6 +2826,7 @@ static int capture_step_graph(tg_ctx* c, int parity) {
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
   c->cur = saved;
   c->rp_valid = saved_rp;
+  c->speed_fresh = saved_speed;  // (capture only records the launches)
   if (rc != TG_OK) {
     if (g) cudaGraphDestroy(g);
     return rc;
@@ -3054,6 +3185,7 @@ int tg_adapt_state(tg_ctx* dst, tg_ctx* src, const int64_t* source_element, cons
   dst->uploaded = true;
   dst->clock_valid = false;
   dst->rp_valid = false;
+  dst->speed_fresh = false;
   return TG_OK;
 }
 
