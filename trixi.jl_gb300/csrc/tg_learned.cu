@@ -53,6 +53,8 @@ struct tg_mlp {
   int64_t nparams = 0;
   float* d_w = nullptr;              // FP32 master parameters
   __nv_bfloat16* d_wb = nullptr;     // BF16 copy used by the kernels
+  unsigned char* d_wimg = nullptr;   // d_wb as mlp_tc_kernel's shared-memory image
+  size_t wimg_bytes = 0;
   float* d_g = nullptr;              // gradients
   float* d_m = nullptr;              // Adam first moments
   float* d_v = nullptr;              // Adam second moments
@@ -263,9 +265,10 @@ __global__ void features_kernel(const FeatParams P, const TS* __restrict__ u,
 // the training kernel fits (a plain BF16 rounding of the inputs, 2^-9, would
 // erase the small high-mode part of the features next to the mean mode).
 // One thread issues the MMAs (M = 128, N = H, K = 16 per instruction) and
-// commits them to an mbarrier that every thread waits on; the operands are
+// commits them to an mbarrier that every thread waits on; the layer inputs are
 // written to shared memory by all threads in the K-major layout of
-// tg_tcgen05.cuh, the weights once per block.  The layer-2 operands overlay
+// tg_tcgen05.cuh, and the weights arrive once per block, already in that
+// layout, by bulk copies of the weight image (mlp_weight_image_kernel).  The layer-2 operands overlay
 // the layer-1 ones (layer 1 has completed when they are written).  The same
 // code serves both entry points, so deployed predictions and tg_mlp_predict
 // agree bit for bit.
@@ -292,8 +295,14 @@ struct TcShape {
   // the deployment stages rho*p of the tile's nodes ([ROWS][NM + 1] floats)
   // in the operand area before the layer-1 operands are written
   static_assert(ROWS * (NM + 1) * 4 <= OVEC - OA, "rho*p staging fits the operand area");
-  static constexpr int OBAR = OVEC + (3 * H + 2) * 4;   // mbarriers: MMA, staging
-  static constexpr int OSLOT = OBAR + 16;               // TMEM base address
+  // the weight image (mlp_weight_image_kernel): W1 and W2 in their operand
+  // layouts (bytes [OW1, OA)), then the FP32 vectors padded to 16 bytes; two
+  // bulk copies per block
+  static constexpr int WIMG = OA - OW1;
+  static constexpr int VIMG = (3 * H + 4) * 4;
+  static_assert(WIMG % 16 == 0 && VIMG % 16 == 0 && OVEC % 16 == 0, "bulk copy sizes");
+  static constexpr int OBAR = OVEC + VIMG;              // mbarriers: MMA, staging, weights
+  static constexpr int OSLOT = OBAR + 24;               // TMEM base address
   // 2D deployment: the tile's state (n^d nodes x 4 values, float-float or
   // FP64: 32 bytes per node), staged by one bulk copy per tile
   static constexpr int STAGE_BYTES = ROWS * NM * 32;
@@ -349,7 +358,7 @@ __device__ __forceinline__ void store_row_split(unsigned char* hi, unsigned char
 template <int D, int N, int NM, int H, int SRC, typename TS, typename R>
 __global__ void __launch_bounds__(128) mlp_tc_kernel(
     const FeatParams P, const TS* __restrict__ u, const float* __restrict__ x, int64_t nrows,
-    const __nv_bfloat16* __restrict__ w, const AlphaParams A, R* __restrict__ alpha_raw,
+    const unsigned char* __restrict__ wimg, const AlphaParams A, R* __restrict__ alpha_raw,
     float* __restrict__ pred_out, float* __restrict__ hg_out, int32_t* __restrict__ flag_out,
     unsigned long long* __restrict__ stats, int32_t* __restrict__ status) {
   using S = TcShape<NM, H>;
@@ -362,13 +371,17 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
   float* s_b1 = reinterpret_cast<float*>(sm + S::OVEC);
   float* s_b2 = s_b1 + H;
   float* s_w3 = s_b2 + H;  // s_w3[H] = b3
-  const MlpLayout L{NM, H};
   // 2D deployment stages each tile's state with one bulk copy (contiguous in
   // the element order), the next tile's issued as soon as this one's rho*p
   // has been read
   constexpr bool STAGED = (SRC == 0 && D == 2) || SRC == 2;
   constexpr int NODE_BYTES = SRC == 2 ? 4 : 32;  // staged bytes per node
+  // rho*p rows of 16-byte multiples are read by each thread straight from the
+  // staging buffer (four-way bank conflicts, against a re-layout pass); up to
+  // 16 values, where the registers allow it
+  constexpr bool DIRECT_ROWS = SRC == 2 && NM % 4 == 0 && NM <= 16;
   uint64_t* sbar = bar + 1;
+  uint64_t* wbar = bar + 2;
   float4* s_stg = reinterpret_cast<float4*>(sm + S::OSTG);
   const int64_t total = SRC == 1 ? nrows : P.E;
   const int64_t ntiles = (total + S::ROWS - 1) / S::ROWS;
@@ -381,33 +394,21 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
     tc::bulk_g2s(s_stg, stage_src + (size_t)t * S::ROWS * NM * NODE_BYTES, bytes, sbar);
   };
 
-  // weights into the K-major operand layouts (W1 zero-padded to K1 columns)
-  for (int k = tid; k < H * K1; k += S::ROWS) {
-    const int i = k / K1, j = k - i * K1;
-    *reinterpret_cast<__nv_bfloat16*>(sm + S::OW1 + tc::kmajor_offset(i, j, K1)) =
-        j < NM ? w[L.w1() + i * NM + j] : __float2bfloat16(0.0f);
-  }
-  for (int k = tid; k < H * H; k += S::ROWS) {
-    const int i = k / H, j = k - i * H;
-    *reinterpret_cast<__nv_bfloat16*>(sm + S::OW2 + tc::kmajor_offset(i, j, H)) = w[L.w2() + k];
-  }
-  for (int k = tid; k < H; k += S::ROWS) {
-    s_b1[k] = __bfloat162float(w[L.b1() + k]);
-    s_b2[k] = __bfloat162float(w[L.b2() + k]);
-    s_w3[k] = __bfloat162float(w[L.w3() + k]);
-  }
+  // the first tile's staging and the weight image, by bulk copies
   if (tid == 0) {
-    s_w3[H] = __bfloat162float(w[L.b3()]);
     tc::mbar_init(bar, 1);
+    tc::mbar_init(wbar, 1);
     if (STAGED) tc::mbar_init(sbar, 1);
     tc::fence_mbar_init();
     if (STAGED && blockIdx.x < ntiles) issue_tile(blockIdx.x);
+    tc::mbar_arrive_expect_tx(wbar, S::WIMG + S::VIMG);
+    tc::bulk_g2s(sm + S::OW1, wimg, S::WIMG, wbar);
+    tc::bulk_g2s(sm + S::OVEC, wimg + S::WIMG, S::VIMG, wbar);
   }
   if (warp == 0) {
     tc::tmem_alloc(slot, S::TCOLS);
     tc::tmem_relinquish();
   }
-  tc::fence_proxy_async_smem();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -419,8 +420,10 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
   if (SRC != 1 && blockIdx.x == 0 && tid == 0) atomicAdd(&stats[0], (unsigned long long)P.E);
 
   uint32_t phase = 0, sphase = 0;
-  bool failed = false, mma_in_flight = false, staging_in_flight = STAGED && blockIdx.x < ntiles;
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  bool mma_in_flight = false, staging_in_flight = STAGED && blockIdx.x < ntiles;
+  bool failed = __syncthreads_or(!tc::mbar_wait_bounded(wbar, 0, TC_WAIT_POLLS));
+  const bool weights_late = failed;
+  for (int64_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
     const int64_t e = tile * S::ROWS + tid;
     const bool act = e < total;
     float xv[NM];
@@ -432,6 +435,7 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
       float* s_rp = reinterpret_cast<float*>(sm + S::OA);
       const int64_t n0 = tile * S::ROWS * NM;
       const int64_t nn = (min(total, (tile + 1) * S::ROWS) - tile * S::ROWS) * NM;
+      float a[NM];
       if constexpr (STAGED) {
         if (__syncthreads_or(!tc::mbar_wait_bounded(sbar, sphase, TC_WAIT_POLLS))) {
           failed = true;
@@ -439,12 +443,26 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
         }
         sphase ^= 1;
         staging_in_flight = false;
+        if constexpr (DIRECT_ROWS) {
+          if (act) {
+            const float4* row = s_stg + tid * (NM / 4);
+#pragma unroll
+            for (int q = 0; q < NM / 4; ++q) {
+              const float4 f = row[q];
+              a[4 * q] = f.x;
+              a[4 * q + 1] = f.y;
+              a[4 * q + 2] = f.z;
+              a[4 * q + 3] = f.w;
+            }
+          }
+        } else {
 #pragma unroll 4
-        for (int j = 0; j < NM; ++j) {
-          const int k = j * S::ROWS + tid;
-          if (k < nn)
-            s_rp[(k / NM) * (NM + 1) + k % NM] =
-                SRC == 2 ? reinterpret_cast<const float*>(s_stg)[k] : staged_rho_p<TS>(P, s_stg, k);
+          for (int j = 0; j < NM; ++j) {
+            const int k = j * S::ROWS + tid;
+            if (k < nn)
+              s_rp[(k / NM) * (NM + 1) + k % NM] =
+                  SRC == 2 ? reinterpret_cast<const float*>(s_stg)[k] : staged_rho_p<TS>(P, s_stg, k);
+          }
         }
         __syncthreads();
         // the staging buffer is free: the next tile's state lands meanwhile
@@ -464,9 +482,10 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
         __syncthreads();
       }
       if (act) {
-        float a[NM];
+        if constexpr (!DIRECT_ROWS) {
 #pragma unroll
-        for (int q = 0; q < NM; ++q) a[q] = s_rp[tid * (NM + 1) + q];
+          for (int q = 0; q < NM; ++q) a[q] = s_rp[tid * (NM + 1) + q];
+        }
         modes_from_rho_p<D, N>(P, a, xv, energy, positive);
       } else {
 #pragma unroll
@@ -503,7 +522,13 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
       float v[32];
       tc::tmem_ld32(trow + c0, v);
 #pragma unroll
-      for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + s_b1[c0 + j], 0.0f);
+      for (int j = 0; j < 32; j += 4) {
+        const float4 b = *reinterpret_cast<const float4*>(s_b1 + c0 + j);
+        v[j] = fmaxf(v[j] + b.x, 0.0f);
+        v[j + 1] = fmaxf(v[j + 1] + b.y, 0.0f);
+        v[j + 2] = fmaxf(v[j + 2] + b.z, 0.0f);
+        v[j + 3] = fmaxf(v[j + 3] + b.w, 0.0f);
+      }
 #pragma unroll
       for (int g = 0; g < 32; g += 8) {
         uint4 h, l;
@@ -539,7 +564,14 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
       float v[32];
       tc::tmem_ld32(trow + c0, v);
 #pragma unroll
-      for (int j = 0; j < 32; ++j) out = fmaf(s_w3[c0 + j], fmaxf(v[j] + s_b2[c0 + j], 0.0f), out);
+      for (int j = 0; j < 32; j += 4) {
+        const float4 b = *reinterpret_cast<const float4*>(s_b2 + c0 + j);
+        const float4 wv = *reinterpret_cast<const float4*>(s_w3 + c0 + j);
+        out = fmaf(wv.x, fmaxf(v[j] + b.x, 0.0f), out);
+        out = fmaf(wv.y, fmaxf(v[j + 1] + b.y, 0.0f), out);
+        out = fmaf(wv.z, fmaxf(v[j + 2] + b.z, 0.0f), out);
+        out = fmaf(wv.w, fmaxf(v[j + 3] + b.w, 0.0f), out);
+      }
     }
     tc::fence_before_sync();  // the next tile's MMAs are issued after a barrier
     if constexpr (SRC == 1) {
@@ -573,6 +605,7 @@ __global__ void __launch_bounds__(128) mlp_tc_kernel(
     if (tid == 0) atomicOr(status, STATUS_TC_TIMEOUT);
     if (mma_in_flight) tc::mbar_wait_bounded(bar, phase, TC_WAIT_POLLS);
     if (staging_in_flight) tc::mbar_wait_bounded(sbar, sphase, TC_WAIT_POLLS);
+    if (weights_late) tc::mbar_wait_bounded(wbar, 0, TC_WAIT_POLLS);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -752,6 +785,37 @@ __global__ void to_bf16_kernel(const float* __restrict__ w, __nv_bfloat16* __res
   if (k < n) wb[k] = __float2bfloat16(w[k]);
 }
 
+// The weight image that every block of mlp_tc_kernel copies into shared
+// memory: W1 [H][NM] zero-padded to K1 columns and W2 [H][H], BF16, in the
+// K-major operand layouts, then b1, b2, w3 and b3 as FP32, zero-padded to a
+// multiple of 16 bytes ((3H + 4) floats).
+__global__ void mlp_weight_image_kernel(const __nv_bfloat16* __restrict__ w, MlpLayout L, int K1,
+                                        unsigned char* __restrict__ img) {
+  const int NM = L.NM, H = L.H;
+  const int n1 = H * K1, n2 = H * H, nv = 3 * H + 4;
+  unsigned char* w2img = img + (size_t)H * K1 * 2;
+  float* vimg = reinterpret_cast<float*>(w2img + (size_t)H * H * 2);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n1 + n2 + nv;
+       k += gridDim.x * blockDim.x) {
+    if (k < n1) {
+      const int i = k / K1, j = k - i * K1;
+      *reinterpret_cast<__nv_bfloat16*>(img + tc::kmajor_offset(i, j, K1)) =
+          j < NM ? w[L.w1() + i * NM + j] : __float2bfloat16(0.0f);
+    } else if (k < n1 + n2) {
+      const int q = k - n1, i = q / H, j = q - i * H;
+      *reinterpret_cast<__nv_bfloat16*>(w2img + tc::kmajor_offset(i, j, H)) = w[L.w2() + q];
+    } else {
+      const int q = k - n1 - n2;
+      float v = 0.0f;
+      if (q < H) v = __bfloat162float(w[L.b1() + q]);
+      else if (q < 2 * H) v = __bfloat162float(w[L.b2() + q - H]);
+      else if (q < 3 * H) v = __bfloat162float(w[L.w3() + q - 2 * H]);
+      else if (q == 3 * H) v = __bfloat162float(w[L.b3()]);
+      vimg[q] = v;
+    }
+  }
+}
+
 }  // namespace tg
 
 using namespace tg;
@@ -846,7 +910,9 @@ static int launch_tc(tg_mlp* m, const FeatParams& P, const TS* u, const float* x
   const int64_t ntiles = (rows + S::ROWS - 1) / S::ROWS;
   if (ntiles == 0) return TG_OK;
   const unsigned nb = (unsigned)std::min<int64_t>(ntiles, (int64_t)sms * resident[dev]);
-  kern<<<nb, S::ROWS, SMEM, s>>>(P, u, x, rows, m->d_wb, A, alpha_raw, pred, m->d_hg,
+  if (m->wimg_bytes != (size_t)(S::WIMG + S::VIMG))
+    return mfail(m, TG_ERR_INVALID_ARGUMENT, "weight image of another network shape");
+  kern<<<nb, S::ROWS, SMEM, s>>>(P, u, x, rows, m->d_wimg, A, alpha_raw, pred, m->d_hg,
                                     m->d_flag, m->d_stats, status);
   MCUDA(m, cudaGetLastError());
   return TG_OK;
@@ -969,6 +1035,15 @@ static int train_pass(tg_mlp* m, const float* X, const float* Y, int64_t M, cons
 
 extern "C" {
 
+// Rebuilds the weight image from the BF16 weights (after every change of them),
+// on the legacy default stream like the weight updates themselves.
+static void refresh_weight_image(tg_mlp* m) {
+  const int K1 = (m->NM + 15) / 16 * 16;
+  const int n = m->H * K1 + m->H * m->H + 3 * m->H + 4;
+  mlp_weight_image_kernel<<<(unsigned)((n + 255) / 256), 256>>>(m->d_wb, MlpLayout{m->NM, m->H}, K1,
+                                                                m->d_wimg);
+}
+
 int tg_mlp_create(int32_t ndims, int32_t polydeg, int32_t hidden, uint64_t seed, tg_mlp** out) {
   if (!out) return mfail(nullptr, TG_ERR_INVALID_ARGUMENT, "null argument");
   *out = nullptr;
@@ -1003,6 +1078,11 @@ int tg_mlp_create(int32_t ndims, int32_t polydeg, int32_t hidden, uint64_t seed,
   cudaError_t e = cudaSuccess;
   e = e ? e : cudaMalloc(&m->d_w, pb);
   e = e ? e : cudaMalloc(&m->d_wb, sizeof(__nv_bfloat16) * m->nparams);
+  {
+    const int K1 = (NM + 15) / 16 * 16;
+    m->wimg_bytes = (size_t)H * K1 * 2 + (size_t)H * H * 2 + (size_t)(3 * H + 4) * 4;
+  }
+  e = e ? e : cudaMalloc(&m->d_wimg, m->wimg_bytes);
   e = e ? e : cudaMalloc(&m->d_g, pb);
   e = e ? e : cudaMalloc(&m->d_m, pb);
   e = e ? e : cudaMalloc(&m->d_v, pb);
@@ -1019,6 +1099,7 @@ int tg_mlp_create(int32_t ndims, int32_t polydeg, int32_t hidden, uint64_t seed,
   cudaMemset(m->d_v, 0, pb);
   cudaMemset(m->d_stats, 0, 3 * sizeof(unsigned long long));
   to_bf16_kernel<<<(unsigned)((m->nparams + 255) / 256), 256>>>(m->d_w, m->d_wb, m->nparams);
+  refresh_weight_image(m);
   e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return mfail(nullptr, TG_ERR_CUDA, cudaGetErrorString(e));
   *out = m;
@@ -1027,7 +1108,7 @@ int tg_mlp_create(int32_t ndims, int32_t polydeg, int32_t hidden, uint64_t seed,
 
 int tg_mlp_destroy(tg_mlp* m) {
   if (!m) return TG_ERR_INVALID_ARGUMENT;
-  void* ptrs[] = {m->d_w, m->d_wb, m->d_g, m->d_m, m->d_v, m->d_x, m->d_y, m->d_loss,
+  void* ptrs[] = {m->d_w, m->d_wb, m->d_wimg, m->d_g, m->d_m, m->d_v, m->d_x, m->d_y, m->d_loss,
                   m->d_gpart, m->d_lpart,
                   m->d_pred, m->d_hg, m->d_flag, m->d_stats, m->d_status};
   for (void* p : ptrs)
@@ -1052,6 +1133,7 @@ int tg_mlp_set_params(tg_mlp* m, const float* host) {
   if (!m || !host) return TG_ERR_INVALID_ARGUMENT;
   MCUDA(m, cudaMemcpy(m->d_w, host, sizeof(float) * m->nparams, cudaMemcpyHostToDevice));
   to_bf16_kernel<<<(unsigned)((m->nparams + 255) / 256), 256>>>(m->d_w, m->d_wb, m->nparams);
+  refresh_weight_image(m);
   MCUDA(m, cudaDeviceSynchronize());
   return TG_OK;
 }
@@ -1134,6 +1216,7 @@ int tg_mlp_train(tg_mlp* m, int64_t steps, int32_t batch, float lr, int32_t hold
                                                               m->d_v, m->nparams, lr, b1, b2, 1e-8f,
                                                               c1, c2);
   }
+  if (steps > 0) refresh_weight_image(m);
   float l[2] = {0, 0};
   MCUDA(m, cudaMemcpy(l, m->d_loss, sizeof(l), cudaMemcpyDeviceToHost));
   if (mean_loss) *mean_loss = l[1] > 0 ? l[0] / l[1] : 0.0f;
