@@ -59,14 +59,16 @@ static int launch_mixed_one(const MixedParams& P, const MixedArgs& A, cudaStream
 }
 
 // Flux-specialised instances for polydeg 3 (flux_ranocha volume flux with the
-// two Lax-Friedrichs surface fluxes); every other choice dispatches at run
-// time.  Meshes with faces of a given flux (slip walls, mortars) take the
-// DIRECT instances, built for the default elements per block (DEF) only; other
-// block sizes run those meshes through the run-time flux kernel.
+// two Lax-Friedrichs surface fluxes, and for shock capturing the surface flux
+// as the subcell flux too); every other choice dispatches at run time.
+// Meshes with faces of a given flux (slip walls, mortars) take the DIRECT
+// instances, built for the default elements per block (DEF) only; other block
+// sizes run those meshes through the run-time flux kernel.
 template <int D, int VI, int EPB, bool DEF>
 static int launch_mixed_n4(const MixedParams& P, const MixedArgs& A, cudaStream_t s) {
   constexpr int VF = VI == VI_WEAK ? -1 : FLUX_RANOCHA;
-  const bool ranocha = VI == VI_WEAK || P.volume_flux == FLUX_RANOCHA;
+  const bool ranocha = (VI == VI_WEAK || P.volume_flux == FLUX_RANOCHA) &&
+                       (VI != VI_HG || P.fv_flux == P.surface_flux);
   if (ranocha && !P.has_direct) {
     if (P.surface_flux == FLUX_LLF) return launch_mixed_one<D, 4, VI, VF, FLUX_LLF, EPB>(P, A, s);
     if (P.surface_flux == FLUX_LLF_NAIVE)

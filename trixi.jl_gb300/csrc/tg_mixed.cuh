@@ -771,7 +771,12 @@ __device__ __forceinline__ void mixed_line(const MixedParams& P, const RefState<
 #pragma unroll
       for (int a = 0; a + 1 < N; ++a) {
         float F[NV];
-        Dv::two_point(P.fv_flux, R, nd[a], nd[a + 1], dd, vro, eos, F);
+        // flux-specialised instances run only where the subcell flux is the
+        // surface flux (launch_mixed_n4); the others dispatch at run time
+        if constexpr (SF >= 0)
+          Dv::template flux2<SF>(SF, R, nd[a], nd[a + 1], dd, vro, eos, F);
+        else
+          Dv::two_point(P.fv_flux, R, nd[a], nd[a + 1], dd, vro, eos, F);
         const float ca = alpha * s_iw[a], cb = alpha * s_iw[a + 1];
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
