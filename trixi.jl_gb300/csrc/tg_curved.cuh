@@ -162,8 +162,129 @@ __device__ __forceinline__ void dev_surface_n(int kind, const RefState<D>& R, co
   for (int v = 0; v < NV; ++v) F[v] = F[v] + (-0.5f * lam * (b.du[v] - a.du[v]));
 }
 
+// dev_surface_n with the flux kind fixed at compile time (KIND >= 0; the
+// flux-specialised mixed kernels) or dispatched at run time (KIND < 0).
+template <int D, int KIND>
+__device__ __forceinline__ void dev_surface_k(int kind, const RefState<D>& R, const Node<D>& a,
+                                              const Node<D>& b, const float* n, const EosF& eos,
+                                              float* F) {
+  if constexpr (KIND < 0) {
+    dev_surface_n<D>(kind, R, a, b, n, eos, F);
+  } else if constexpr (KIND == FLUX_RANOCHA) {
+    dev_ranocha_n<D>(R, a, b, n, eos, F);
+  } else if constexpr (KIND == FLUX_LLF || KIND == FLUX_LLF_NAIVE) {
+    constexpr int NV = D + 2, P = D + 1;
+    dev_flux_n<D, FLUX_CENTRAL>(FLUX_CENTRAL, R, a, b, n, eos, F);
+    const float va = dot_n<D>(a.w + 1, n), vb = dot_n<D>(b.w + 1, n);
+    const float ca = sqrtf(eos.gamma * a.w[P] / a.w[0]), cb = sqrtf(eos.gamma * b.w[P] / b.w[0]);
+    const float nn = sqrtf(dot_n<D>(n, n));
+    const float lam = KIND == FLUX_LLF_NAIVE ? fmaxf(fabsf(va), fabsf(vb)) + fmaxf(ca, cb) * nn
+                                             : fmaxf(fabsf(va) + ca * nn, fabsf(vb) + cb * nn);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) F[v] = F[v] + (-0.5f * lam * (b.du[v] - a.du[v]));
+  } else {
+    dev_flux_n<D, KIND>(KIND, R, a, b, n, eos, F);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Node indexing and block shape of the 2D curvilinear kernels
+// ---------------------------------------------------------------------------
+template <int N>
+__device__ __forceinline__ int cline_node(int line, int dd, int a) {
+  // node a of line `line` in direction dd (node index q = i + N j)
+  return dd == 0 ? a + N * line : line + N * a;
+}
+
+// Node of the neighbour across face dir of an element that meets face node fn.
+template <int N>
+__device__ __forceinline__ int cface_partner(int dir, int fn) {
+  switch (dir) {
+    case 0: return (N - 1) + N * fn;  // -x: neighbour's +x face
+    case 1: return N * fn;            // +x: neighbour's -x face
+    case 2: return fn + N * (N - 1);  // -y: neighbour's +y face
+    default: return fn;               // +y: neighbour's -y face
+  }
+}
+
+// Node of this element at face dir that meets face node fn.
+template <int N>
+__device__ __forceinline__ int cface_own(int dir, int fn) {
+  switch (dir) {
+    case 0: return N * fn;
+    case 1: return (N - 1) + N * fn;
+    case 2: return fn;
+    default: return fn + N * (N - 1);
+  }
+}
+
+// Position of block node n (= slot * N^2 + node) in the mixed kernel's
+// per-node shared arrays.  For N = 4 the low and high halves of the node index
+// are XORed with bits 1-2 of the element slot: a warp holds the x-lines (or the
+// y-lines) of 8 elements, whose same-parity elements would otherwise fall on
+// the same 8 banks (4-way conflicts); with the permutation the 32 lanes of
+// every line-phase access and of the node phase hit 32 different banks.
+template <int N>
+__device__ __forceinline__ int cpos(int n) {
+  if constexpr (N == 4) {
+    const int g = (n >> 5) & 3;  // bits 1-2 of the slot n >> 4
+    return n ^ (g | (g << 2));
+  } else {
+    return n;
+  }
+}
+
+template <int N, int EPB>
+struct CurvedK {
+  static constexpr int NN = N * N, NV = 4, NT = EPB * 2 * N;
+  static constexpr int CHUNK = EPB * NN * NV;  // state values of a block
+  static constexpr int FACE = EPB * 4 * N * NV;
+  static constexpr int SP = EPB * NN;          // field stride of the partial sums
+  // resident blocks per SM asked of the mixed kernel: for N <= 4 five blocks
+  // fit its shared memory (44 KB at N = 4) and 96 registers per thread
+  static constexpr int MINB_MIXED = N <= 4 ? 5 : 1;
+};
+
 // Elements per block of the curvilinear kernels (0: polydeg not compiled).
 int curved_epb(int N);
+
+// The mixed-precision 2D stage kernels (tg_curved_mixed_2d.cu, compiled with
+// the FP32 flags of the mixed units).
+int launch_curved_mixed2(const CurvedParams& P, const MixedArgs& A, cudaStream_t stream);
+
+// ---------------------------------------------------------------------------
+// Node indexing of the 3D curvilinear kernels
+// ---------------------------------------------------------------------------
+// node a of line `line` (0 .. N^2 - 1) in direction dd, node q = i + N j + N^2 k
+template <int N>
+__device__ __forceinline__ int line3(int line, int dd, int a) {
+  if (dd == 0) return a + N * line;                           // line = j + N k
+  if (dd == 1) return (line % N) + N * a + N * N * (line / N);  // line = i + N k
+  return line + N * N * a;                                    // line = i + N j
+}
+
+// face node fn of face dir (fn runs over the two tangential indices, the
+// lower one fastest): this element's node there, and the neighbour's node
+template <int N>
+__device__ __forceinline__ int face_own3(int dir, int fn) {
+  switch (dir) {
+    case 0: return N * fn;
+    case 1: return (N - 1) + N * fn;
+    case 2: return (fn % N) + N * N * (fn / N);
+    case 3: return (fn % N) + N * (N - 1) + N * N * (fn / N);
+    case 4: return fn;
+    default: return fn + N * N * (N - 1);
+  }
+}
+
+template <int N>
+__device__ __forceinline__ int face_partner3(int dir, int fn) {
+  return face_own3<N>(dir ^ 1, fn);
+}
+
+// The mixed-precision 3D stage kernels (tg_curved_mixed_3d.cu, compiled with
+// the FP32 flags of the mixed units).
+int launch_curved_mixed3(const CurvedParams& P, const MixedArgs& A, cudaStream_t stream);
 
 // One stage (or rhs) launch; exactly one of A64 (FP64 context) and A32
 // (mixed context) is non-null.
