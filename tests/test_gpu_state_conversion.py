@@ -76,6 +76,13 @@ def test_upload_download_bitwise(case):
         ctx.fetch(seed % 2, out.data_ptr())
         ctx.transfer_wait(seed % 2, 1)
         _check(out.numpy(), x)
+        # page-locked buffers 8 bytes off a 16-byte boundary (the 8-byte kernels)
+        off = torch.zeros(x.size + 1, dtype=torch.float64).pin_memory()
+        off[1:] = torch.from_numpy(x)
+        ctx.upload(off.numpy()[1:].reshape(semi.u_shape))
+        off.zero_()
+        ctx.download(off.numpy()[1:].reshape(semi.u_shape))
+        _check(off.numpy()[1:], x)
     ctx.transfer_join()
     ctx.synchronize()
 
@@ -100,12 +107,18 @@ def test_upload_cfl_reduction_matches_separate_reduction(case):
     ctx.upload(u0)
     ctx.step(3, 1.0, 10.0, 0.0)
     u = ctx.download()
+    torch = pytest.importorskip("torch")
+    off = torch.zeros(u.size + 1, dtype=torch.float64).pin_memory()
+    off[1:] = torch.from_numpy(u.reshape(-1))
+    u_off = off.numpy()[1:].reshape(semi.u_shape)  # 8 bytes off a 16-byte boundary
     for cfl in (1.0, 0.37):
         ctx.upload(u)
         t_fused, _ = ctx.step(1, cfl, 10.0, 0.0)
+        ctx.upload(u_off)
+        t_fused8, _ = ctx.step(1, cfl, 10.0, 0.0)
         ctx.upload(u)
         ctx.state_ptr()
         t_sep, _ = ctx.step(1, cfl, 10.0, 0.0)
-        assert t_fused == t_sep and t_fused > 0
+        assert t_fused == t_sep and t_fused8 == t_sep and t_fused > 0
         ctx.upload(u)
         assert ctx.max_dt() * cfl == pytest.approx(t_fused, rel=1e-12)

@@ -187,6 +187,17 @@ __global__ void to_ff_kernel(const double* __restrict__ in, float2* __restrict__
        k += (int64_t)gridDim.x * blockDim.x)
     out[k] = split_f64(in[k]);
 }
+
+// The same with two values per thread and 16-byte loads and stores (n2 = n / 2
+// pairs; `in` 16-byte aligned): a warp reads and writes 512 contiguous bytes.
+__global__ void to_ff2_kernel(const double2* __restrict__ in, float4* __restrict__ out, int64_t n2) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n2;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const double2 x = in[k];
+    const float2 a = split_f64(x.x), b = split_f64(x.y);
+    out[k] = make_float4(a.x, a.y, b.x, b.y);
+  }
+}
 // to_ff_kernel for a 2D state (4 values per node) that also writes rho*p of
 // every node from the hi parts, with the stage kernels' arithmetic
 __global__ void to_ff_rp_kernel(const double* __restrict__ in, float2* __restrict__ out,
@@ -258,6 +269,57 @@ __global__ void __launch_bounds__(256) to_ff_rp_speed_kernel(
   block_speed_max(best, speed_bits);
 }
 
+// to_ff_rp_speed_kernel<16> with 16-byte loads and stores (`in` 16-byte
+// aligned): a thread converts two values of a node (lane pair: values 0-1 and
+// 2-3), the pair exchanges its hi parts by shuffles, and a warp covers one
+// element (16 nodes) per pass, so the element's speed reduction is a warp
+// reduction.  Same arithmetic, same results.
+__global__ void __launch_bounds__(256) to_ff_rp_speed_pair_kernel(
+    const double2* __restrict__ in, float4* __restrict__ out, int64_t nnodes, float gamma_rp,
+    float* __restrict__ rp, float gamma, const float* __restrict__ inv_jac,
+    unsigned long long* __restrict__ speed_bits, int32_t* __restrict__ status) {
+  const int lane = threadIdx.x & 31;
+  const int64_t npairs = 2 * nnodes;  // a multiple of 32: elements of 16 nodes
+  unsigned long long best = 0;
+  bool bad = false;
+  // blockDim and the grid stride are multiples of 32: a warp's 32 pairs are
+  // one element, and the loop condition is warp-uniform
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npairs;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const double2 x = in[p];
+    const float2 a = split_f64(x.x), b = split_f64(x.y);
+    out[p] = make_float4(a.x, a.y, b.x, b.y);
+    const float oa = __shfl_xor_sync(0xffffffffu, a.x, 1);
+    const float ob = __shfl_xor_sync(0xffffffffu, b.x, 1);
+    const bool first = (lane & 1) == 0;
+    float hi[4];
+    hi[0] = first ? a.x : oa;
+    hi[1] = first ? b.x : ob;
+    hi[2] = first ? oa : a.x;
+    hi[3] = first ? ob : b.x;
+    float ml[2] = {0.0f, 0.0f};
+    if (first) {
+      rp[p >> 1] = Euler<2, float>::density_pressure(hi, gamma_rp);
+      bad |= node_speeds_ff<2>(hi, gamma, ml);
+    }
+    for (int d = 0; d < 2; ++d)
+      for (int o = 16; o > 0; o >>= 1) ml[d] = fmaxf(ml[d], __shfl_xor_sync(0xffffffffu, ml[d], o));
+    if (lane == 0) {
+      float sum = 0;
+      for (int d = 0; d < 2; ++d) sum += ml[d];
+      const float sp = inv_jac[p >> 5] * sum;
+      if (sp == sp) {
+        const unsigned long long bits = (unsigned long long)__double_as_longlong((double)sp);
+        best = bits > best ? bits : best;
+      } else {
+        bad = true;
+      }
+    }
+  }
+  if (bad) atomicOr(status, 2);
+  block_speed_max(best, speed_bits);
+}
+
 // rho*p of every node from the hi parts of a float-float state (nv values per
 // node), with the stage kernels' arithmetic
 __global__ void rho_p_ff_kernel(const float2* __restrict__ u, int64_t nnodes, int nv, float gamma,
@@ -275,6 +337,16 @@ __global__ void from_ff_kernel(const float2* __restrict__ in, double* __restrict
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * blockDim.x)
     out[k] = state_f64(in[k]);
+}
+
+// The same with two values per thread and 16-byte loads and stores (`out`
+// 16-byte aligned).
+__global__ void from_ff2_kernel(const float4* __restrict__ in, double2* __restrict__ out, int64_t n2) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n2;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const float4 x = in[k];
+    out[k] = make_double2(state_f64(make_float2(x.x, x.y)), state_f64(make_float2(x.z, x.w)));
+  }
 }
 
 // max_dt's reduction (stepsize_dg2d.jl:8-30): max_e invJ_e * sum_d max_nodes lambda_d.
@@ -1319,9 +1391,14 @@ static int import_state(tg_ctx* c, const double* src, void* dst) {
       // the CFL reduction of the new state in the same pass (ctx_clock_prepare
       // then skips its own)
       speed_reset_kernel<<<1, 1, 0, c->stream>>>(&c->d_clock->speed_bits);
-      to_ff_rp_speed_kernel<16><<<conv_blocks(c->ndofs), 256, 0, c->stream>>>(
-          src, (float2*)dst, c->ndofs, c->MP.gamma, c->d_rp, (float)c->P.gamma, c->d_invj_f,
-          &c->d_clock->speed_bits, c->d_status);
+      if (((uintptr_t)src & 15) == 0)
+        to_ff_rp_speed_pair_kernel<<<conv_blocks(2 * c->ndofs), 256, 0, c->stream>>>(
+            (const double2*)src, (float4*)dst, c->ndofs, c->MP.gamma, c->d_rp,
+            (float)c->P.gamma, c->d_invj_f, &c->d_clock->speed_bits, c->d_status);
+      else
+        to_ff_rp_speed_kernel<16><<<conv_blocks(c->ndofs), 256, 0, c->stream>>>(
+            src, (float2*)dst, c->ndofs, c->MP.gamma, c->d_rp, (float)c->P.gamma, c->d_invj_f,
+            &c->d_clock->speed_bits, c->d_status);
       CUDA_TRY(c, cudaGetLastError());
       c->speed_fresh = true;
     } else {
@@ -1332,10 +1409,25 @@ static int import_state(tg_ctx* c, const double* src, void* dst) {
     c->rp_valid = true;
     return TG_OK;
   }
-  to_ff_kernel<<<conv_blocks(c->nvalues), 256, 0, c->stream>>>(src, (float2*)dst, c->nvalues);
+  if (((uintptr_t)src & 15) == 0 && c->nvalues % 2 == 0)
+    to_ff2_kernel<<<conv_blocks(c->nvalues / 2), 256, 0, c->stream>>>(
+        (const double2*)src, (float4*)dst, c->nvalues / 2);
+  else
+    to_ff_kernel<<<conv_blocks(c->nvalues), 256, 0, c->stream>>>(src, (float2*)dst, c->nvalues);
   CUDA_TRY(c, cudaGetLastError());
   if (dst == c->d_u[c->cur]) c->rp_valid = false;
   return TG_OK;
+}
+
+// Float-float state -> FP64 values in `out` (device or mapped host memory):
+// 16-byte accesses when `out` allows them.
+static void launch_from_ff(tg_ctx* c, const void* in, double* out) {
+  if (((uintptr_t)out & 15) == 0 && c->nvalues % 2 == 0)
+    from_ff2_kernel<<<conv_blocks(c->nvalues / 2), 256, 0, c->stream>>>(
+        (const float4*)in, (double2*)out, c->nvalues / 2);
+  else
+    from_ff_kernel<<<conv_blocks(c->nvalues), 256, 0, c->stream>>>((const float2*)in, out,
+                                                                    c->nvalues);
 }
 
 // Context state -> FP64 values (for mixed: into d_stage64); returns the FP64 pointer.
@@ -1343,8 +1435,7 @@ static const double* export_state(tg_ctx* c, int* rc) {
   *rc = TG_OK;
   if (c->fp64) return (const double*)c->d_u[c->cur];
   if ((*rc = ensure(c, (void**)&c->d_stage64, sizeof(double) * c->nvalues))) return nullptr;
-  from_ff_kernel<<<conv_blocks(c->nvalues), 256, 0, c->stream>>>((const float2*)c->d_u[c->cur],
-                                                                  c->d_stage64, c->nvalues);
+  launch_from_ff(c, c->d_u[c->cur], c->d_stage64);
   if (cudaGetLastError() != cudaSuccess) {
     *rc = fail(c, TG_ERR_CUDA, "state conversion launch failed");
     return nullptr;
@@ -2489,8 +2580,7 @@ int tg_download_state(tg_ctx* c, double* u_host) {
   CUDA_TRY(c, cudaSetDevice(c->device));
   if (!c->fp64) {
     if (void* pinned = const_cast<void*>(pinned_device_ptr(u_host))) {
-      from_ff_kernel<<<conv_blocks(c->nvalues), 256, 0, c->stream>>>(
-          (const float2*)c->d_u[c->cur], (double*)pinned, c->nvalues);
+      launch_from_ff(c, c->d_u[c->cur], (double*)pinned);
       CUDA_TRY(c, cudaGetLastError());
       CUDA_TRY(c, cudaStreamSynchronize(c->stream));
       return TG_OK;
@@ -2558,8 +2648,7 @@ int tg_fetch_state(tg_ctx* c, int32_t slot, double* u_host) {
     CUDA_TRY(c, cudaMemcpyAsync(c->d_xout[slot], c->d_u[c->cur], sizeof(double) * c->nvalues,
                                 cudaMemcpyDeviceToDevice, c->stream));
   } else {
-    from_ff_kernel<<<conv_blocks(c->nvalues), 256, 0, c->stream>>>(
-        (const float2*)c->d_u[c->cur], c->d_xout[slot], c->nvalues);
+    launch_from_ff(c, c->d_u[c->cur], c->d_xout[slot]);
     CUDA_TRY(c, cudaGetLastError());
   }
   CUDA_TRY(c, cudaEventRecord(c->ev_out_ready[slot], c->stream));
