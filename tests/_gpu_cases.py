@@ -49,7 +49,8 @@ def build(c, precision="fp64", elements_per_block=0):
                                           alpha_min=c.get("alpha_min", 0.001),
                                           alpha_smooth=c.get("alpha_smooth", True),
                                           variable=T.density_pressure)
-        vi = T.VolumeIntegralShockCapturingHG(ind, volume_flux_dg=vflux, volume_flux_fv=sflux)
+        fvflux = FLUX[c.get("fv_flux", c["surface_flux"])][0]
+        vi = T.VolumeIntegralShockCapturingHG(ind, volume_flux_dg=vflux, volume_flux_fv=fvflux)
         ovi = O.VI_SHOCKCAPTURING_HG
     solver = T.DGSEM(basis, sflux, vi)
     boundary = c.get("boundary")
@@ -68,6 +69,7 @@ def build(c, precision="fp64", elements_per_block=0):
                    surface_flux=FLUX[c["surface_flux"]][1],
                    alpha_max=c.get("alpha_max", 0.5), alpha_min=c.get("alpha_min", 0.001),
                    alpha_smooth=c.get("alpha_smooth", True),
+                   fv_flux=FLUX[c["fv_flux"]][1] if c.get("fv_flux") else None,
                    source=O.SRC_CONVERGENCE_TEST if src is not None else O.SRC_NONE)
     if c.get("refinement_patches"):
         orc.set_refinement(c["refinement_patches"])

@@ -80,6 +80,8 @@ RHS_CASES = [
     _case(SEDOV),
     _case(SEDOV, polydeg=3, alpha_smooth=False, volume_flux="shima_etal"),
     _case(FLAG, boundary="dirichlet", **HG_FLAG),
+    # a subcell flux other than the surface flux (the run-time flux instances)
+    _case(FLAG, boundary="dirichlet", **dict(HG_FLAG, volume_flux_fv="llf_naive")),
 ]
 
 
