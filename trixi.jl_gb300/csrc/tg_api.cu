@@ -2210,16 +2210,19 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
     return fail(nullptr, TG_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
   }
   // stream-ordered allocations from the device's context pool (cudaMalloc if
-  // the pool is unavailable); the stream is synchronised once they are made
+  // the pool is unavailable or refuses for another reason than memory, e.g.
+  // after a device reset); the stream is synchronised once they are made
   cudaMemPool_t pool = context_pool(c->device);
 #define ALLOC(ptr, bytes)                                                                 \
   do {                                                                                    \
+    e = cudaErrorNotSupported;                                                            \
     if (pool) {                                                                           \
       e = cudaMallocFromPoolAsync((void**)&(ptr), (bytes), pool, c->stream);              \
       if (e == cudaSuccess) c->pool_ptrs.push_back((void*)(ptr));                         \
-    } else {                                                                              \
-      e = cudaMalloc((void**)&(ptr), (bytes));                                            \
+      else if (e != cudaErrorMemoryAllocation) cudaGetLastError();                        \
     }                                                                                     \
+    if (e != cudaSuccess && e != cudaErrorMemoryAllocation)                               \
+      e = cudaMalloc((void**)&(ptr), (bytes)); /* no pool, or a pool that went away */    \
     if (e != cudaSuccess) {                                                               \
       free_ctx(c);                                                                        \
       return fail(nullptr, TG_ERR_CUDA, "device allocation (%zu bytes): %s",              \
