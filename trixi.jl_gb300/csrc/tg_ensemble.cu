@@ -49,12 +49,21 @@ struct EnsShape {
   }
 };
 
-// One 2N stage of every instance (at most 128 registers per thread, so that
-// 480 threads are resident per SM).  params[i] and args[i] are instance i's
+// Resident threads per SM asked of the register allocator: 480 (at most 128
+// registers per thread); 600 for the weak form with a fixed surface flux,
+// whose body fits 96 registers without spills (the latency-bound weak-form
+// items gain from the fifth block of 120 threads).
+template <int VI, int SF, int NT>
+struct EnsOcc {
+  static constexpr int THREADS = (VI == VI_WEAK && SF >= 0) ? 600 : 480;
+  static constexpr int MINB = THREADS / NT > 0 ? THREADS / NT : 1;
+};
+
+// One 2N stage of every instance.  params[i] and args[i] are instance i's
 // parameters and stage arguments; a block stages them in shared memory before
 // running a work item (they are read many times by every thread).
 template <int VI, int VF, int SF, int NT>
-__global__ void __launch_bounds__(NT, 480 / NT) ensemble_stage_kernel(const MixedParams* __restrict__ params,
+__global__ void __launch_bounds__(NT, EnsOcc<VI, SF, NT>::MINB) ensemble_stage_kernel(const MixedParams* __restrict__ params,
                                                             const MixedArgs* __restrict__ args,
                                                             const EnsItem* __restrict__ items,
                                                             int nitems) {
