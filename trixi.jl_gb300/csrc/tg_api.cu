@@ -1447,10 +1447,18 @@ namespace tg {
 const float* ctx_state_rho_p(tg_ctx* c);
 }
 
+// Mixed 2D TreeMesh contexts without mortars: the persistent stage kernel
+// applies apply_smoothing! to the raw factors itself (MixedArgs::alpha_gather),
+// so no smoothing pass runs between the indicator and the stage kernel.
+static bool alpha_gather_mode(const tg_ctx* c) {
+  return !c->fp64 && !c->curved && c->D == 2 && c->nmortar == 0;
+}
+
 // Blending factors of a state in the context representation: the HG (or
 // learned) indicator, unsmoothed, into d_alpha_raw; for mixed TreeMesh
-// contexts also apply_smoothing! into d_alpha_sm, which the persistent stage
-// kernel copies with the element block (the other kernels smooth inline).
+// contexts outside alpha_gather_mode also apply_smoothing! into d_alpha_sm,
+// which the persistent stage kernel copies with the element block (the other
+// kernels smooth inline).
 static int indicator(tg_ctx* c, const void* u) {
   if (c->vi != VI_HG) return TG_OK;
   int rc;
@@ -1474,7 +1482,7 @@ static int indicator(tg_ctx* c, const void* u) {
                                     c->stream);
     if (rc != 0) return fail(c, TG_ERR_CUDA, "indicator kernel launch failed (%d)", rc);
   }
-  if (!c->fp64 && !c->curved) {
+  if (!c->fp64 && !c->curved && !alpha_gather_mode(c)) {
     smooth_alpha_kernel<float, float><<<(unsigned)((c->E + 255) / 256), 256, 0, c->stream>>>(
         (const float*)c->d_alpha_raw, c->d_nbr, c->E, 2 * c->D, c->P.alpha_smooth, c->P.nbc,
         c->d_mnbr, c->d_alpha_sm);
@@ -1582,7 +1590,12 @@ static int launch_kernel(tg_ctx* c, int mode, const void* u_in, void* u_out, dou
   } else {
     MixedArgs A{};
     A.alpha_raw = (const float*)c->d_alpha_raw;
-    A.alpha_smoothed = c->d_alpha_sm;
+    if (alpha_gather_mode(c)) {
+      A.alpha_smoothed = (const float*)c->d_alpha_raw;
+      A.alpha_gather = c->P.alpha_smooth ? 1 : 0;
+    } else {
+      A.alpha_smoothed = c->d_alpha_sm;
+    }
     A.rp_out = write_rp && mode == MODE_STAGE ? c->d_rp : nullptr;
     A.status = c->d_status;
     A.clock = c->d_clock;
@@ -2267,7 +2280,7 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   ALLOC(c->d_sums, sizeof(double) * 16);
   if (!xline.empty()) ALLOC(c->d_xline, sizeof(double) * xline.size());
   if (c->vi == VI_HG) {
-    ALLOC(c->d_alpha_raw, rsize(c) * c->E);
+    ALLOC(c->d_alpha_raw, rsize(c) * (c->E + kElemPad));  // padded as d_alpha_sm
     ALLOC(c->d_alpha, sizeof(double) * c->E);
     // read in whole 16-byte groups by the bulk copies of the 2D stage kernel
     if (!c->fp64) ALLOC(c->d_alpha_sm, sizeof(float) * (c->E + kElemPad));

@@ -85,6 +85,10 @@ struct MixedArgs {
   float* u_tmp;             // MODE_STAGE
   const float* alpha_raw;   // VI_HG
   const float* alpha_smoothed;  // VI_HG, persistent 2D kernel: alpha_raw after apply_smoothing!
+  // VI_HG, persistent 2D kernel on a mesh without mortars: alpha_smoothed
+  // holds the raw factors and the kernel applies apply_smoothing! itself,
+  // from the face neighbours' raw factors gathered with the face traces
+  int32_t alpha_gather;
   float* alpha_out;         // VI_HG (optional)
   // MODE_STAGE (optional): rho*p of u_out per node (FP32 on the hi parts, as
   // the indicators compute it), read by the next stage's indicator instead of
@@ -863,14 +867,16 @@ constexpr uint32_t STAGING_WAIT_POLLS = 1u << 22;
 // ---------------------------------------------------------------------------
 
 // Per element: blending factor (VI_HG: `alpha_pre` when a pre-pass smoothed
-// it, else alpha_raw smoothed here), the reference state (mean `hi` of two
+// it, or raw with `alpha_nb` the raw factors across its faces, else alpha_raw
+// smoothed here from global memory), the reference state (mean `hi` of two
 // opposite corner nodes, read from `chunk`, the block's state in global or
 // shared memory) and the element part of the source phase.
 template <int D, int N, int VI, int EPB>
 __device__ __forceinline__ void mixed_setup_elements(const MixedParams& P, const MixedArgs& A,
                                                      int64_t e0, int nel, const float2* chunk,
                                                      const float* alpha_pre, RefState<D>* s_ref,
-                                                     float* s_elem) {
+                                                     float* s_elem,
+                                                     const float* alpha_nb = nullptr) {
   using K = MixedKernel<D, N, VI, EPB>;
   using Dv = Dev<D>;
   constexpr int NV = K::NV, NN = K::NN;
@@ -881,6 +887,12 @@ __device__ __forceinline__ void mixed_setup_elements(const MixedParams& P, const
     float a;
     if (alpha_pre) {
       a = alpha_pre[tid];
+      // alpha_nb: the raw factors across the element's faces, NaN at a domain
+      // boundary (fmax keeps `a` there), in smooth_over_face's order
+      if (alpha_nb) {
+#pragma unroll
+        for (int dir = 0; dir < 2 * D; ++dir) a = fmax(a, 0.5f * alpha_nb[tid * 2 * D + dir]);
+      }
     } else {
       a = A.alpha_raw[e];
       if (P.alpha_smooth) {
@@ -1267,7 +1279,8 @@ struct MixedPipe {
   static constexpr size_t O_SMAX = O_SCAL + up(sizeof(float) * 8);
   static constexpr size_t O_MAT = O_SMAX + up(sizeof(unsigned) * EPB * D);
   static constexpr size_t O_IW = O_MAT + up(sizeof(float) * N * N);
-  static constexpr size_t O_BAR = O_IW + up(sizeof(float) * N);
+  static constexpr size_t O_ANB = O_IW + up(sizeof(float) * N);  // neighbours' raw factors
+  static constexpr size_t O_BAR = O_ANB + up(sizeof(float) * EPB * 2 * D);
   static constexpr size_t SMEM = O_BAR + 16;
 };
 
@@ -1306,11 +1319,26 @@ __device__ __forceinline__ void mixed_pipe_issue(const MixedParams& P, const Mix
 // staged neighbour rows, then a commit.
 template <int D, int N, int VI, int EPB>
 __device__ __forceinline__ void mixed_pipe_faces(const MixedParams& P, const MixedArgs& A,
-                                                 int64_t blk, const int32_t* s_nbr, float2* fu) {
+                                                 int64_t blk, const int32_t* s_nbr, float2* fu,
+                                                 float* anb) {
   using Q = MixedPipe<D, N, VI, EPB>;
   constexpr int NF = Q::NF, NT = Q::NT, NN = Q::NN, NV = Q::NV;
   const int64_t e0 = blk * EPB;
   const int nel = (int)min((int64_t)EPB, P.nelements - e0);
+  if (VI == VI_HG && A.alpha_gather && (int)threadIdx.x < nel) {
+    // the raw blending factors across the faces of element threadIdx.x, by
+    // the thread that smooths its factor in the setup phase (which waits for
+    // its own copies only)
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int dir = 0; dir < 2 * D; ++dir) {
+      const int32_t nb = s_nbr[t * 2 * D + dir];
+      if (nb >= 0)
+        cp_async4(anb + t * 2 * D + dir, A.alpha_smoothed + nb);
+      else
+        anb[t * 2 * D + dir] = __int_as_float(0x7fffffff);  // domain boundary (no mortars here)
+    }
+  }
   for (int k = threadIdx.x; k < nel * 2 * D * NF; k += NT) {
     const int sl = k / (2 * D * NF);
     const int rem = k - sl * (2 * D * NF);
@@ -1345,6 +1373,7 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
   unsigned int* s_smax = reinterpret_cast<unsigned int*>(smem_raw + Q::O_SMAX);
   float* s_mat = reinterpret_cast<float*>(smem_raw + Q::O_MAT);
   float* s_iw = reinterpret_cast<float*>(smem_raw + Q::O_IW);
+  float* s_anb = reinterpret_cast<float*>(smem_raw + Q::O_ANB);
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + Q::O_BAR);
 
   const int tid = threadIdx.x;
@@ -1376,7 +1405,8 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
     failed_it = 0;
   } else {
     mixed_pipe_faces<D, N, VI, EPB>(P, A, blk,
-                                    reinterpret_cast<const int32_t*>(smem_raw + Q::B_NBR), s_fu);
+                                    reinterpret_cast<const int32_t*>(smem_raw + Q::B_NBR), s_fu,
+                                    s_anb);
   }
   for (int it = 0; failed_it < 0 && blk < nblocks; ++it, blk += gridDim.x) {
     const int b = it & 1;
@@ -1394,11 +1424,12 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
       break;
     }
     if (tid < EPB * D) s_smax[tid] = 0u;
+    cp_async_wait_all();  // this thread's copies of this block's face traces (and factors)
     mixed_setup_elements<D, N, VI, EPB>(P, A, e0, nel, s_u,
                                         VI == VI_HG ? reinterpret_cast<const float*>(cur + Q::B_AL)
                                                     : nullptr,
-                                        s_ref, s_elem);
-    cp_async_wait_all();  // this thread's copies of this block's face traces
+                                        s_ref, s_elem,
+                                        VI == VI_HG && A.alpha_gather ? s_anb : nullptr);
     __syncthreads();
 
     mixed_node_deviations<D, N, VI, EPB>(P, s_u, s_ref, s_nd, nel);
@@ -1421,7 +1452,8 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
         break;
       }
       mixed_pipe_faces<D, N, VI, EPB>(P, A, nxt,
-                                      reinterpret_cast<const int32_t*>(nxt_buf + Q::B_NBR), s_fu);
+                                      reinterpret_cast<const int32_t*>(nxt_buf + Q::B_NBR), s_fu,
+                                      s_anb);
     }
 
     const float* s_ut = reinterpret_cast<const float*>(cur + Q::B_UT);
