@@ -1455,10 +1455,10 @@ static bool alpha_gather_mode(const tg_ctx* c) {
 }
 
 // Blending factors of a state in the context representation: the HG (or
-// learned) indicator, unsmoothed, into d_alpha_raw; for mixed TreeMesh
-// contexts outside alpha_gather_mode also apply_smoothing! into d_alpha_sm,
-// which the persistent stage kernel copies with the element block (the other
-// kernels smooth inline).
+// learned) indicator, unsmoothed, into d_alpha_raw; for mixed 2D TreeMesh
+// contexts with mortars also apply_smoothing! into d_alpha_sm, which the
+// persistent stage kernel copies with the element block (the other kernels
+// smooth inline).
 static int indicator(tg_ctx* c, const void* u) {
   if (c->vi != VI_HG) return TG_OK;
   int rc;
@@ -1482,7 +1482,7 @@ static int indicator(tg_ctx* c, const void* u) {
                                     c->stream);
     if (rc != 0) return fail(c, TG_ERR_CUDA, "indicator kernel launch failed (%d)", rc);
   }
-  if (!c->fp64 && !c->curved && !alpha_gather_mode(c)) {
+  if (!c->fp64 && !c->curved && c->D == 2 && !alpha_gather_mode(c)) {
     smooth_alpha_kernel<float, float><<<(unsigned)((c->E + 255) / 256), 256, 0, c->stream>>>(
         (const float*)c->d_alpha_raw, c->d_nbr, c->E, 2 * c->D, c->P.alpha_smooth, c->P.nbc,
         c->d_mnbr, c->d_alpha_sm);
