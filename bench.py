@@ -836,8 +836,8 @@ def khi_line(args, rank, world):
                "roofline": {"achieved": roof["achieved"], "peak": roof["peak"],
                             "frac": roof["achieved"] / roof["peak"], "stage_ms": roof["stage_ms"],
                             "algorithmic_bytes": roof["alg_bytes"], "traffic": roof["traffic"],
-                            "kernel": "mixed_element_kernel<3,4,FD,flux_ranocha,"
-                                      "flux_lax_friedrichs>"}}
+                            "kernel": "mixed_element_pipe_kernel<3,4,FD,flux_ranocha,"
+                                      "flux_lax_friedrichs,EPB=2>"}}
     if rank != 0:
         return
     res = out["res"]
@@ -916,7 +916,7 @@ def mms_line(args, rank, world):
         "roofline": {"bound": "hbm", "achieved": roof["achieved"], "peak": roof["peak"],
                      "unit": "GB/s", "frac": roof["achieved"] / roof["peak"],
                      "traffic": roof["traffic"],
-                     "kernel": "mixed_element_kernel<3,4,FD,flux_ranocha,flux_lax_friedrichs>",
+                     "kernel": "mixed_element_pipe_kernel<3,4,FD,flux_ranocha,flux_lax_friedrichs,EPB=2>",
                      "stage_ms": roof["stage_ms"], "algorithmic_bytes": roof["alg_bytes"],
                      "peak_source": roof["peak_src"]},
         "cpu_baseline": cpu,

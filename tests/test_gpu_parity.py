@@ -455,3 +455,35 @@ def test_hllc_is_not_a_volume_flux():
     semi, _ = build(c)
     with pytest.raises(T.TrixiGB300Error):
         semi.device_context
+
+
+# 3D mixed contexts with 2 elements per block (the default at polydeg 3
+# without shock capturing or faces of a given flux) run the persistent kernel
+# (bulk copies of the next element block while the current one computes); its
+# phases are the per-block kernel's (4 elements per block), so both give the
+# same bits
+PERSISTENT_3D_CASES = [RHS_CASES[6], RHS_CASES[7], BOUNDARY_CASES[4]]
+
+
+@pytest.mark.parametrize("c", PERSISTENT_3D_CASES,
+                         ids=[_id(c) + ("-" + c["boundary"] if c.get("boundary") else "")
+                              for c in PERSISTENT_3D_CASES])
+def test_3d_persistent_kernel_equals_per_block_kernel(c):
+    u0 = None
+    out = {}
+    for epb in (2, 4):
+        semi, orc = build(c, precision="mixed", elements_per_block=epb)
+        ctx = semi.device_context
+        if u0 is None:
+            u0 = perturbed_state(semi, seed=29)
+        du = ctx.rhs_host(u0, 0.31)
+        ctx.upload(u0)
+        t, n = ctx.step(3, 0.6, 10.0, 0.0)
+        out[epb] = (du, ctx.download(), t)
+    assert ctx.elements_per_block() == 4
+    np.testing.assert_array_equal(out[2][0], out[4][0])
+    np.testing.assert_array_equal(out[2][1], out[4][1])
+    assert out[2][2] == out[4][2]
+    default, _ = build(c, precision="mixed")
+    assert default.device_context.elements_per_block() == 2
+    assert rel_err(out[2][0], orc.rhs(u0, 0.31)) < 2e-4

@@ -20,7 +20,11 @@ static int launch_mixed_one(const MixedParams& P, const MixedArgs& A, cudaStream
   // same kernel on the 3D MMS mesh at 32^3, 4 elements per block, took 0.195
   // ms per stage against the per-block kernel's 0.186: 3 resident blocks of
   // 68 KB against 4 of 53 KB.)
-  if constexpr (D == 2 && EPB % 4 == 0 && (Pow<N, D>::value * (D + 2)) % 2 == 0) {
+  // 3D: the same kernel with 2 elements (96 threads) per block, 6 blocks per
+  // SM, without shock capturing (whose 3D factors are smoothed inside the
+  // per-block kernel)
+  if constexpr ((Pow<N, D>::value * (D + 2)) % 2 == 0 &&
+                ((D == 2 && EPB % 4 == 0) || (D == 3 && EPB == 2 && VI != VI_HG))) {
     if (VI != VI_HG || A.alpha_smoothed) {
       using Q = MixedPipe<D, N, VI, EPB>;
       auto kern = mixed_element_pipe_kernel<D, N, VI, VF, SF, EPB, DIRECT>;

@@ -1282,6 +1282,13 @@ struct MixedPipe {
   static constexpr size_t O_ANB = O_IW + up(sizeof(float) * N);  // neighbours' raw factors
   static constexpr size_t O_BAR = O_ANB + up(sizeof(float) * EPB * 2 * D);
   static constexpr size_t SMEM = O_BAR + 16;
+  // the per-element float rows (blending factor, inverse Jacobian) of a block
+  // start on 16-byte boundaries only for EPB % 4 == 0; otherwise they are read
+  // with plain loads when the block starts
+  static constexpr bool ROWS_BULK = EPB % 4 == 0;
+  // resident blocks per SM asked of the register allocator: the 3D form runs
+  // small blocks (2 elements, 96 threads), six of them per SM
+  static constexpr int MINB = (D == 3 && EPB == 2) ? 6 : K::MINB;
 };
 
 // Bulk copies of element block blk's contiguous inputs into buffer `buf`
@@ -1300,18 +1307,22 @@ __device__ __forceinline__ void mixed_pipe_issue(const MixedParams& P, const Mix
   const uint32_t b_u = (uint32_t)(sizeof(float2) * nel * NN * NV);
   const bool need_ut = A.mode == MODE_STAGE && !A.zero_tmp;
   const uint32_t b_ut = need_ut ? (uint32_t)(sizeof(float) * nel * NN * NV) : 0u;
-  // every source address below is 16-byte aligned: e0 is a multiple of EPB
-  static_assert(EPB % 4 == 0, "per-element float rows of a block start on 16-byte boundaries");
+  // every source address below is 16-byte aligned: e0 is a multiple of EPB,
+  // the neighbour rows of EPB elements are whole 16-byte groups and the float
+  // rows are copied in bulk only where EPB % 4 == 0 (Q::ROWS_BULK)
   static_assert((Pow<N, D>::value * (D + 2)) % 2 == 0, "state chunks of whole 16-byte groups");
+  static_assert((EPB * 2 * D * sizeof(int32_t)) % 16 == 0, "neighbour rows of whole 16-byte groups");
   const uint32_t b_nbr = (uint32_t)Q::up(sizeof(int32_t) * nel * 2 * D);
-  const uint32_t b_el = (uint32_t)Q::up(sizeof(float) * nel);
+  const uint32_t b_el = Q::ROWS_BULK ? (uint32_t)Q::up(sizeof(float) * nel) : 0u;
   const uint32_t b_al = VI == VI_HG ? b_el : 0u;
   tc::mbar_arrive_expect_tx(mbar, b_u + b_ut + b_nbr + b_al + b_el);
   tc::bulk_g2s(buf + Q::B_U, A.u_in + gofs, b_u, mbar);
   if (need_ut) tc::bulk_g2s(buf + Q::B_UT, A.u_tmp + gofs, b_ut, mbar);
   tc::bulk_g2s(buf + Q::B_NBR, P.nbr + e0 * 2 * D, b_nbr, mbar);
-  if (VI == VI_HG) tc::bulk_g2s(buf + Q::B_AL, A.alpha_smoothed + e0, b_al, mbar);
-  tc::bulk_g2s(buf + Q::B_IJ, P.inv_jac + e0, b_el, mbar);
+  if constexpr (Q::ROWS_BULK) {
+    if (VI == VI_HG) tc::bulk_g2s(buf + Q::B_AL, A.alpha_smoothed + e0, b_al, mbar);
+    tc::bulk_g2s(buf + Q::B_IJ, P.inv_jac + e0, b_el, mbar);
+  }
 }
 
 // cp.async copies of the neighbour traces of element block blk's faces to
@@ -1357,7 +1368,7 @@ __device__ __forceinline__ void mixed_pipe_faces(const MixedParams& P, const Mix
 }
 
 template <int D, int N, int VI, int VF, int SF, int EPB, bool DIRECT = false>
-__global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D, N, VI, EPB>::MINB)
+__global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedPipe<D, N, VI, EPB>::MINB)
     mixed_element_pipe_kernel(const MixedParams P, const MixedArgs A) {
   using K = MixedKernel<D, N, VI, EPB>;
   using Q = MixedPipe<D, N, VI, EPB>;
@@ -1424,6 +1435,16 @@ __global__ void __launch_bounds__(MixedKernel<D, N, VI, EPB>::NT, MixedKernel<D,
       break;
     }
     if (tid < EPB * D) s_smax[tid] = 0u;
+    if constexpr (!Q::ROWS_BULK) {
+      // the per-element float rows, by the thread that sets its element up;
+      // the other threads read them after the barrier below.  The buffer is
+      // overwritten by bulk copies two blocks later: async-proxy ordering.
+      if (tid < nel) {
+        reinterpret_cast<float*>(cur + Q::B_IJ)[tid] = P.inv_jac[e0 + tid];
+        if (VI == VI_HG) reinterpret_cast<float*>(cur + Q::B_AL)[tid] = A.alpha_smoothed[e0 + tid];
+        tc::fence_proxy_async_smem();
+      }
+    }
     cp_async_wait_all();  // this thread's copies of this block's face traces (and factors)
     mixed_setup_elements<D, N, VI, EPB>(P, A, e0, nel, s_u,
                                         VI == VI_HG ? reinterpret_cast<const float*>(cur + Q::B_AL)
