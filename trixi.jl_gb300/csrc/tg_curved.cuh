@@ -245,7 +245,8 @@ struct CurvedK {
   static constexpr int MINB_MIXED = N <= 4 ? 5 : 1;
 };
 
-// Elements per block of the curvilinear kernels (0: polydeg not compiled).
+// Elements per block of the curvilinear kernels (0: polydeg not compiled);
+// the mixed 2D weak-form kernel at polydeg 3 runs 8 (tg_curved_mixed_2d.cu).
 int curved_epb(int N);
 
 // The mixed-precision 2D stage kernels (tg_curved_mixed_2d.cu, compiled with

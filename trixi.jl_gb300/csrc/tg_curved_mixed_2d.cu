@@ -347,7 +347,10 @@ __global__ void __launch_bounds__(CurvedK<N, EPB>::NT, CurvedK<N, EPB>::MINB_MIX
 
 template <int N, int VI, int VF, int SF>
 static int launch_mixed2_one(const CurvedParams& P, const MixedArgs& A, cudaStream_t stream) {
-  constexpr int EPB = N == 5 ? 8 : 16;
+  // elements per block: 8 for the polydeg-3 weak form (at 512^2 on the waving
+  // flag 0.194 ms per stage against 0.208 with 16; flux differencing and shock
+  // capturing were 3-4 % slower with 8); both give the same bits
+  constexpr int EPB = (N == 5 || (N == 4 && VI == VI_WEAK)) ? 8 : 16;
   using K = CurvedK<N, EPB>;
   const unsigned nb = (unsigned)((P.nelements + EPB - 1) / EPB);
   const size_t smem = sizeof(float2) * (K::CHUNK + K::FACE) + sizeof(float4) * 2 * K::SP +
