@@ -458,15 +458,24 @@ def test_hllc_is_not_a_volume_flux():
 
 
 # 3D mixed contexts with 2 elements per block (the default at polydeg 3
-# without shock capturing or faces of a given flux) run the persistent kernel
+# without shock capturing) run the persistent kernel
 # (bulk copies of the next element block while the current one computes); its
 # phases are the per-block kernel's (4 elements per block), so both give the
 # same bits
-PERSISTENT_3D_CASES = [RHS_CASES[6], RHS_CASES[7], BOUNDARY_CASES[4]]
+PERSISTENT_3D_CASES = [
+    RHS_CASES[6], RHS_CASES[7], BOUNDARY_CASES[4],
+    # faces of a given flux: slip walls, and mortars of a refined box
+    dict(ndims=3, polydeg=3, level=2, xmin=[-2] * 3, xmax=[2] * 3, vi="fluxdiff",
+         volume_flux="ranocha", surface_flux="llf", ic="weak_blast_wave", boundary="slip_wall"),
+    dict(ndims=3, polydeg=3, level=2, xmin=[0] * 3, xmax=[2] * 3, vi="fluxdiff",
+         volume_flux="ranocha", surface_flux="llf", ic="convergence_test", source="convergence_test",
+         refinement_patches=[dict(type="box", coordinates_min=[0.5] * 3, coordinates_max=[1.5] * 3)]),
+]
 
 
 @pytest.mark.parametrize("c", PERSISTENT_3D_CASES,
                          ids=[_id(c) + ("-" + c["boundary"] if c.get("boundary") else "")
+                              + ("-mortar" if c.get("refinement_patches") else "")
                               for c in PERSISTENT_3D_CASES])
 def test_3d_persistent_kernel_equals_per_block_kernel(c):
     u0 = None

@@ -2445,12 +2445,12 @@ int tg_ctx_create(const tg_config* cfg, tg_ctx** out) {
   M.nbc = (int32_t)c->nbound;
   M.ghost = c->d_ghost;
   M.mnbr = c->d_mnbr;
-  // 3D polydeg 3 without shock capturing and without faces of a given flux:
-  // the persistent kernel with 2 elements per block is the default (at 32^3
-  // on the MMS mesh 0.169 ms per stage against the per-block kernel's 0.188
-  // with 4 elements; both give the same bits)
+  // 3D polydeg 3 without shock capturing: the persistent kernel with 2
+  // elements per block is the default (at 32^3 on the MMS mesh 0.169 ms per
+  // stage against the per-block kernel's 0.188 with 4 elements; both give the
+  // same bits)
   if (!c->fp64 && !curved && c->D == 3 && c->N == 4 && cfg->elements_per_block <= 0 &&
-      c->vi != VI_HG && !M.has_direct)
+      c->vi != VI_HG)
     c->epb = 2;
   if (curved) {
     int rc = curved_setup(c, cfg);

@@ -111,7 +111,14 @@ int TG_CAT(launch_mixed_, TG_SUFFIX)(int N, int epb, const MixedParams& P, const
     case 2: return launch_mixed_one<3, 2, TG_VI, -1, -1, 16>(P, A, s);
     case 3: return launch_mixed_one<3, 3, TG_VI, -1, -1, 8>(P, A, s);
     case 4:
+      // 2 elements per block (the persistent kernel without shock capturing,
+      // the default) and 4 (shock capturing) both have the instances for
+      // faces of a given flux
+#if TG_VI != 2
+      if (epb == 2) return launch_mixed_n4<3, TG_VI, 2, true>(P, A, s);
+#else
       if (epb == 2) return launch_mixed_n4<3, TG_VI, 2, false>(P, A, s);
+#endif
       if (epb == 8) return launch_mixed_n4<3, TG_VI, 8, false>(P, A, s);
       return launch_mixed_n4<3, TG_VI, 4, true>(P, A, s);
     case 5: return launch_mixed_one<3, 5, TG_VI, -1, -1, 2>(P, A, s);
