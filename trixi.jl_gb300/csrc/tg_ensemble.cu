@@ -50,12 +50,13 @@ struct EnsShape {
 };
 
 // Resident threads per SM asked of the register allocator: 480 (at most 128
-// registers per thread); 600 for the weak form with a fixed surface flux,
-// whose body fits 96 registers without spills (the latency-bound weak-form
-// items gain from the fifth block of 120 threads).
+// registers per thread); 720 for the weak form with a fixed surface flux,
+// whose body fits 80 registers (12 bytes of spills): the latency-bound
+// weak-form items gain from more blocks (6 of 120 threads; shared memory
+// allows no seventh).
 template <int VI, int SF, int NT>
 struct EnsOcc {
-  static constexpr int THREADS = (VI == VI_WEAK && SF >= 0) ? 600 : 480;
+  static constexpr int THREADS = (VI == VI_WEAK && SF >= 0) ? 720 : 480;
   static constexpr int MINB = THREADS / NT > 0 ? THREADS / NT : 1;
 };
 
